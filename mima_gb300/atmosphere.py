@@ -1,0 +1,206 @@
+"""Seeded synthetic atmospheres in the form MiMA's ``run_rrtmg`` hands to RRTMG.
+
+The reference drives RRTMG from ``run_rrtmg`` (``src/atmos_param/rrtm_radiation/
+rrtm_radiation.f90:464-834``), which reshapes the GCM state to (column, layer)
+with layer 1 at the surface (``:649-664``), converts pressure to hPa, fixes the
+top interface (``:655-656``) and clamps ``h2o >= 2e-7``, ``100 <= T <= 370``
+(``:673-677``).  It passes *specific humidity* in the ``h2ovmr`` argument and the
+O3 *mass* mixing ratio in ``o3vmr`` (``rrtmg_lw_rad.nomcica.f90:775-778``).
+This generator produces exactly that form.
+
+Memory layout: every 2-D field is a C-contiguous ``(nlev, ncol)`` array, i.e. the
+Fortran ``(ncol, nlev)`` column-major layout with the column index fastest, which
+is what the C-ABI takes.  Columns are ordered longitude-fastest.
+
+Profile recipe (the published benchmark configurations name no dataset; these
+seeded profiles stand in for MiMA's state):
+
+* Gaussian grid: T42 128x64, T85 256x128, T170 512x256 (Gauss-Legendre latitudes).
+* Interfaces log-spaced in p from ps = 1000 hPa to the top (0.1 hPa for 40
+  layers, 0.01 hPa for 60); layer pressure = geometric mean of its interfaces.
+* Ts = 240 + 60 cos^2(lat) + N(0, sigma).
+* Constant lapse rate 6.5 K/km in hydrostatic form T = Ts (p/ps)^(R Gamma / g)
+  (R = 287.04, g = 9.80) down to a 200 K tropopause, isothermal above;
+  interface temperatures are linear in ln p between layers, Ts at the surface.
+* q = RH qsat(T, p) (Bolton 1980 saturation vapour pressure) below the
+  tropopause, RH = 0.7 or U(0.2, 0.95) per column; 3e-6 kg/kg at and above the
+  tropopause and as a lower bound everywhere.
+* O3 vmr = 8e-6 exp(-0.5 log10(p / 10 hPa)^2), passed as mass mixing ratio.
+* CO2 300 ppmv, every other gas zero; emissivity 1; all SW albedos 0.27.
+* cos(zenith): annual mean of the daily-mean value of ``astro.f90``
+  ((aa h + bb sin h)/pi), 365 declinations, obliquity 23.439 deg.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+AMDO = 0.603428  # dry air / ozone molecular weight ratio (rrtmg_lw_rad.nomcica.f90)
+R_DRY = 287.04
+GRAV = 9.80
+LAPSE = 6.5e-3
+T_TROP = 200.0
+
+
+@dataclass
+class Atmosphere:
+    """Inputs of ``rrtmg_lw`` / ``rrtmg_sw`` for ``ncol`` columns (see module doc)."""
+    ncol: int
+    nlay: int
+    play: np.ndarray      # (nlay, ncol) hPa
+    plev: np.ndarray      # (nlay+1, ncol) hPa
+    tlay: np.ndarray      # (nlay, ncol) K
+    tlev: np.ndarray      # (nlay+1, ncol) K
+    tsfc: np.ndarray      # (ncol,) K
+    h2o: np.ndarray       # (nlay, ncol) specific humidity kg/kg
+    o3: np.ndarray        # (nlay, ncol) O3 mass mixing ratio
+    co2: np.ndarray       # (nlay, ncol) vmr
+    ch4: np.ndarray
+    n2o: np.ndarray
+    o2: np.ndarray
+    cfc11: np.ndarray
+    cfc12: np.ndarray
+    cfc22: np.ndarray
+    ccl4: np.ndarray
+    emis: np.ndarray      # (16, ncol)
+    asdir: np.ndarray     # (ncol,)
+    asdif: np.ndarray
+    aldir: np.ndarray
+    aldif: np.ndarray
+    coszen: np.ndarray    # (ncol,)
+    scon: float = 1360.0
+    adjes: float = 1.0
+    dyofyr: int = 0
+    meta: dict = field(default_factory=dict)
+
+    def subset(self, idx) -> "Atmosphere":
+        idx = np.asarray(idx)
+        kw = {}
+        for k, v in self.__dict__.items():
+            if isinstance(v, np.ndarray):
+                kw[k] = np.ascontiguousarray(v[..., idx])
+            else:
+                kw[k] = v
+        kw["ncol"] = int(idx.size)
+        kw["meta"] = dict(self.meta, subset=True)
+        return Atmosphere(**kw)
+
+
+GRIDS = {"T42": (128, 64), "T85": (256, 128), "T170": (512, 256)}
+
+
+def gaussian_latitudes(nlat: int) -> np.ndarray:
+    x, _ = np.polynomial.legendre.leggauss(nlat)
+    return np.arcsin(x)[::-1]  # north to south, radians
+
+
+def annual_mean_coszen(lat: np.ndarray, obliquity_deg: float = 23.439) -> np.ndarray:
+    """Annual mean of the daily-mean cos(zenith) of astro.f90's daily formula."""
+    eps = np.deg2rad(obliquity_deg)
+    days = np.arange(365)
+    dec = np.arcsin(np.sin(eps) * np.sin(2.0 * np.pi * days / 365.0))
+    phi = lat[:, None]
+    d = dec[None, :]
+    aa = np.sin(phi) * np.sin(d)
+    bb = np.cos(phi) * np.cos(d)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        x = -np.tan(phi) * np.tan(d)
+    h = np.arccos(np.clip(x, -1.0, 1.0))
+    cosz = (aa * h + bb * np.sin(h)) / np.pi
+    return np.clip(cosz, 0.0, None).mean(axis=1)
+
+
+def qsat(T: np.ndarray, p_hpa: np.ndarray) -> np.ndarray:
+    es = 6.112 * np.exp(17.67 * (T - 273.15) / (T - 29.65))
+    es = np.minimum(es, 0.5 * p_hpa)
+    return 0.622 * es / (p_hpa - 0.378 * es)
+
+
+def make_columns(lat: np.ndarray, nlay: int, p_top: float, rng: np.random.Generator,
+                 ts_sigma: float, rh=0.7, ps: float = 1000.0) -> Atmosphere:
+    """Build columns at latitudes ``lat`` (radians, one per column)."""
+    ncol = lat.size
+    # Interfaces, surface first (RRTM order); layer = geometric mean.
+    plev1 = np.exp(np.linspace(np.log(ps), np.log(p_top), nlay + 1))
+    play1 = np.sqrt(plev1[:-1] * plev1[1:])
+    plev = np.repeat(plev1[:, None], ncol, axis=1)
+    play = np.repeat(play1[:, None], ncol, axis=1)
+
+    ts = 240.0 + 60.0 * np.cos(lat) ** 2 + ts_sigma * rng.standard_normal(ncol)
+    kappa = R_DRY * LAPSE / GRAV
+    tl = ts[None, :] * (play / ps) ** kappa
+    strat = tl <= T_TROP
+    tlay = np.maximum(tl, T_TROP)
+    lp_lay = np.log(play)
+    lp_lev = np.log(plev)
+    tlev = np.empty((nlay + 1, ncol))
+    tlev[0] = ts
+    w = (lp_lev[1:-1] - lp_lay[:-1]) / (lp_lay[1:] - lp_lay[:-1])
+    tlev[1:-1] = tlay[:-1] + w * (tlay[1:] - tlay[:-1])
+    tlev[-1] = tlay[-1]
+
+    if np.isscalar(rh):
+        rhc = np.full(ncol, float(rh))
+    else:
+        rhc = np.asarray(rh, dtype=np.float64)
+    q = rhc[None, :] * qsat(tlay, play)
+    q = np.where(strat, 3.0e-6, q)
+    q = np.maximum(q, 3.0e-6)
+
+    o3vmr = 8.0e-6 * np.exp(-0.5 * np.log10(play / 10.0) ** 2)
+    z = np.zeros((nlay, ncol))
+    return Atmosphere(
+        ncol=ncol, nlay=nlay, play=play, plev=plev, tlay=tlay, tlev=tlev, tsfc=ts,
+        h2o=q, o3=o3vmr / AMDO, co2=np.full((nlay, ncol), 300.0e-6), ch4=z.copy(),
+        n2o=z.copy(), o2=z.copy(), cfc11=z.copy(), cfc12=z.copy(), cfc22=z.copy(),
+        ccl4=z.copy(), emis=np.ones((16, ncol)), asdir=np.full(ncol, 0.27),
+        asdif=np.full(ncol, 0.27), aldir=np.full(ncol, 0.27), aldif=np.full(ncol, 0.27),
+        coszen=annual_mean_coszen(lat), scon=1360.0, adjes=1.0, dyofyr=0)
+
+
+def grid_atmosphere(grid: str, nlay: int, seed: int, ts_sigma: float = 2.0,
+                    rh_random: bool = False) -> Atmosphere:
+    """Full Gaussian grid (longitude fastest)."""
+    nlon, nlat = GRIDS[grid]
+    p_top = 0.1 if nlay <= 40 else 0.01
+    rng = np.random.default_rng(seed)
+    lat = np.repeat(gaussian_latitudes(nlat), nlon)
+    rh = rng.uniform(0.2, 0.95, size=lat.size) if rh_random else 0.7
+    atm = make_columns(lat, nlay, p_top, rng, ts_sigma, rh=rh)
+    atm.meta.update(grid=grid, nlon=nlon, nlat=nlat, seed=seed, ts_sigma=ts_sigma,
+                    rh_random=rh_random, p_top=p_top)
+    return atm
+
+
+# The five workload configurations (seed = 12345 + index).
+CONFIGS = {
+    0: dict(name="T42x40 FP64", grid="T42", nlay=40, ts_sigma=2.0, rh_random=False),
+    1: dict(name="T85x40 FP64 via C-ABI + CUDA graph", grid="T85", nlay=40, ts_sigma=2.0, rh_random=False),
+    2: dict(name="T170x60 FP32-split", grid="T170", nlay=60, ts_sigma=5.0, rh_random=True),
+    3: dict(name="T42x40 adjoint (256 columns)", grid="T42", nlay=40, ts_sigma=2.0, rh_random=False),
+    4: dict(name="1048576x60 stress (32 T170 members)", grid="T170", nlay=60, ts_sigma=3.0, rh_random=False),
+}
+
+
+def config_atmosphere(index: int, member: int = 0) -> Atmosphere:
+    c = CONFIGS[index]
+    seed = 12345 + index + 1000 * member
+    atm = grid_atmosphere(c["grid"], c["nlay"], seed, c["ts_sigma"], c["rh_random"])
+    if index == 3:
+        idx = np.random.default_rng(seed).choice(atm.ncol, size=256, replace=False)
+        atm = atm.subset(np.sort(idx))
+    atm.meta["config"] = index
+    return atm
+
+
+def small_atmosphere(ncol: int, nlay: int = 40, seed: int = 7, ts_sigma: float = 2.0,
+                     rh_random: bool = True) -> Atmosphere:
+    """Columns at random latitudes (tests)."""
+    rng = np.random.default_rng(seed)
+    lat = np.arcsin(rng.uniform(-1.0, 1.0, size=ncol))
+    p_top = 0.1 if nlay <= 40 else 0.01
+    rh = rng.uniform(0.2, 0.95, size=ncol) if rh_random else 0.7
+    atm = make_columns(lat, nlay, p_top, rng, ts_sigma, rh=rh)
+    atm.meta.update(seed=seed, small=True)
+    return atm

@@ -1,0 +1,142 @@
+"""ctypes front end of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use
+this module, as the checker.  It builds ``oracle/build/liboracle.so`` (the C++
+FP64 restatement of the reference's clear-sky RRTMG path, see the .cpp files
+for the file:line each function follows) with ``make`` when it is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "build" / "liboracle.so"
+
+_lib = None
+_blob = None
+
+_dp = C.POINTER(C.c_double)
+
+
+def build(force: bool = False) -> Path:
+    if force or not LIB.exists() or any(
+            p.stat().st_mtime > LIB.stat().st_mtime for p in HERE.glob("oracle_*")):
+        subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    return LIB
+
+
+def _p(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_dp)
+
+
+def load(blob_path, cpdair: float = 1004.64):
+    """Load the oracle with the given table blob (idempotent per blob)."""
+    global _lib, _blob
+    if _lib is None:
+        build()
+        _lib = C.CDLL(str(LIB))
+        _lib.orc_init.argtypes = [C.c_char_p, C.c_double]
+        _lib.orc_set_table_mode.argtypes = [C.c_int]
+        _lib.orc_table.argtypes = [C.c_char_p, C.c_char_p, _dp, C.c_int]
+        _lib.orc_max_threads.restype = C.c_int
+    key = (str(blob_path), cpdair)
+    if _blob != key:
+        rc = _lib.orc_init(str(blob_path).encode(), C.c_double(cpdair))
+        if rc != 0:
+            raise RuntimeError(f"oracle init failed ({rc}) for {blob_path}")
+        _blob = key
+    return _lib
+
+
+def set_table_mode(use_tables: bool) -> None:
+    _lib.orc_set_table_mode(1 if use_tables else 0)
+
+
+def max_threads() -> int:
+    return int(_lib.orc_max_threads())
+
+
+def _f(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def rrtmg_lw(atm, idrv: int = 0, tauaer=None, nthreads: int = 0):
+    """Clear-sky rrtmg_lw on ``atm``; returns dict of (nlev, ncol) arrays."""
+    n, L = atm.ncol, atm.nlay
+    out = {k: np.zeros((L + 1, n)) for k in ("uflx", "dflx", "uflxc", "dflxc", "duflx_dt", "duflxc_dt")}
+    out.update({k: np.zeros((L, n)) for k in ("hr", "hrc")})
+    args = [_f(atm.play), _f(atm.plev), _f(atm.tlay), _f(atm.tlev), _f(atm.tsfc), _f(atm.h2o),
+            _f(atm.o3), _f(atm.co2), _f(atm.ch4), _f(atm.n2o), _f(atm.o2), _f(atm.cfc11),
+            _f(atm.cfc12), _f(atm.cfc22), _f(atm.ccl4), _f(atm.emis),
+            None if tauaer is None else _f(tauaer)]
+    rc = _lib.orc_rrtmg_lw(C.c_int(n), C.c_int(L), C.c_int(0), C.c_int(idrv), *[_p(a) for a in args],
+                           _p(out["uflx"]), _p(out["dflx"]), _p(out["hr"]), _p(out["uflxc"]),
+                           _p(out["dflxc"]), _p(out["hrc"]), _p(out["duflx_dt"]), _p(out["duflxc_dt"]),
+                           C.c_int(nthreads))
+    if rc != 0:
+        raise RuntimeError(f"orc_rrtmg_lw failed ({rc})")
+    return out
+
+
+def rrtmg_sw(atm, iaer: int = 0, tauaer=None, ssaaer=None, asmaer=None, nthreads: int = 0):
+    n, L = atm.ncol, atm.nlay
+    out = {k: np.zeros((L + 1, n)) for k in ("swuflx", "swdflx", "swuflxc", "swdflxc")}
+    out.update({k: np.zeros((L, n)) for k in ("swhr", "swhrc")})
+    args = [_f(atm.play), _f(atm.plev), _f(atm.tlay), _f(atm.tlev), _f(atm.tsfc), _f(atm.h2o),
+            _f(atm.o3), _f(atm.co2), _f(atm.ch4), _f(atm.n2o), _f(atm.o2), _f(atm.asdir),
+            _f(atm.asdif), _f(atm.aldir), _f(atm.aldif), _f(atm.coszen)]
+    aer = [None if a is None else _f(a) for a in (tauaer, ssaaer, asmaer)]
+    rc = _lib.orc_rrtmg_sw(C.c_int(n), C.c_int(L), C.c_int(0), C.c_int(iaer), *[_p(a) for a in args],
+                           C.c_double(atm.adjes), C.c_int(atm.dyofyr), C.c_double(atm.scon),
+                           *[_p(a) for a in aer],
+                           _p(out["swuflx"]), _p(out["swdflx"]), _p(out["swhr"]), _p(out["swuflxc"]),
+                           _p(out["swdflxc"]), _p(out["swhrc"]), C.c_int(nthreads))
+    if rc != 0:
+        raise RuntimeError(f"orc_rrtmg_sw failed ({rc})")
+    return out
+
+
+def lw_optics(atm):
+    n, L = atm.ncol, atm.nlay
+    taug = np.zeros((140, L, n))
+    fracs = np.zeros((140, L, n))
+    laytrop = np.zeros(n, dtype=np.int32)
+    args = [_f(atm.play), _f(atm.plev), _f(atm.tlay), _f(atm.tlev), _f(atm.tsfc), _f(atm.h2o),
+            _f(atm.o3), _f(atm.co2), _f(atm.ch4), _f(atm.n2o), _f(atm.o2)]
+    rc = _lib.orc_lw_optics(C.c_int(n), C.c_int(L), *[_p(a) for a in args], _p(taug), _p(fracs),
+                            laytrop.ctypes.data_as(C.POINTER(C.c_int)))
+    if rc != 0:
+        raise RuntimeError("orc_lw_optics failed")
+    return taug, fracs, laytrop
+
+
+def sw_optics(atm):
+    n, L = atm.ncol, atm.nlay
+    taug = np.zeros((112, L, n))
+    taur = np.zeros((112, L, n))
+    sfz = np.zeros((112, n))
+    args = [_f(atm.play), _f(atm.plev), _f(atm.tlay), _f(atm.tlev), _f(atm.tsfc), _f(atm.h2o),
+            _f(atm.o3), _f(atm.co2), _f(atm.ch4), _f(atm.n2o), _f(atm.o2)]
+    rc = _lib.orc_sw_optics(C.c_int(n), C.c_int(L), *[_p(a) for a in args], _p(taug), _p(taur), _p(sfz))
+    if rc != 0:
+        raise RuntimeError("orc_sw_optics failed")
+    return taug, taur, sfz
+
+
+def table(key: str, name: str) -> np.ndarray:
+    buf = np.zeros(1 << 16)
+    n = _lib.orc_table(key.encode(), name.encode(), _p(buf), C.c_int(buf.size))
+    if n < 0:
+        raise KeyError((key, name))
+    if n > buf.size:
+        buf = np.zeros(n)
+        _lib.orc_table(key.encode(), name.encode(), _p(buf), C.c_int(n))
+    return buf[:n].copy()

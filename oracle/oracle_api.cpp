@@ -1,0 +1,200 @@
+// CPU oracle, C entry points -- TEST INFRASTRUCTURE ONLY.  Called (via
+// ctypes) by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg.
+// The argument lists follow rrtmg_lw (rrtmg_lw_rad.nomcica.f90:80-89) and
+// rrtmg_sw (rrtmg_sw_rad.nomcica.f90:78-88) for the clear-sky subset; arrays
+// are column-major with the column index fastest.  Columns run in parallel
+// with OpenMP (the reference loops over them serially, :453 / :500).
+#include <cstdio>
+#include <exception>
+
+#include "oracle_lw.hpp"
+#include "oracle_sw.hpp"
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+using namespace orc;
+
+static Blob g_blob;
+static int g_ready = 0;
+
+extern "C" {
+
+int orc_init(const char* blob_path, double cpdair) {
+  try {
+    g_blob = Blob();
+    g_blob.load(blob_path);
+    lw_init(g_blob, cpdair);
+    sw_init(g_blob, cpdair);
+    g_ready = 1;
+    return 0;
+  } catch (const std::exception& e) {
+    std::fprintf(stderr, "orc_init: %s\n", e.what());
+    return 1;
+  }
+}
+
+void orc_set_table_mode(int use_tables) { g_table_mode = use_tables ? 1 : 0; }
+
+int orc_max_threads() {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+int orc_rrtmg_lw(int ncol, int nlay, int icld, int idrv, const double* play, const double* plev,
+                 const double* tlay, const double* tlev, const double* tsfc, const double* h2ovmr,
+                 const double* o3vmr, const double* co2vmr, const double* ch4vmr, const double* n2ovmr,
+                 const double* o2vmr, const double* cfc11vmr, const double* cfc12vmr, const double* cfc22vmr,
+                 const double* ccl4vmr, const double* emis, const double* tauaer, double* uflx, double* dflx,
+                 double* hr, double* uflxc, double* dflxc, double* hrc, double* duflx_dt, double* duflxc_dt,
+                 int nthreads) {
+  if (!g_ready) return 2;
+  if (icld != 0) return 3;
+  LwInput in{ncol, nlay, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr,
+             cfc11vmr, cfc12vmr, cfc22vmr, ccl4vmr, emis, tauaer};
+#pragma omp parallel num_threads(nthreads > 0 ? nthreads : orc_max_threads())
+  {
+    LwColumn c;
+    LwOut o;
+#pragma omp for schedule(dynamic, 16)
+    for (int iplon = 0; iplon < ncol; ++iplon) {
+      lw_column(in, iplon, idrv, c, o);
+      for (int k = 0; k <= nlay; ++k) {
+        size_t ix = (size_t)iplon + (size_t)ncol * (size_t)k;
+        uflx[ix] = o.totu[k];
+        dflx[ix] = o.totd[k];
+        uflxc[ix] = o.totu[k];
+        dflxc[ix] = o.totd[k];
+        if (idrv == 1 && duflx_dt) {
+          duflx_dt[ix] = o.dtotu_dt[k];
+          if (duflxc_dt) duflxc_dt[ix] = o.dtotu_dt[k];
+        }
+      }
+      for (int k = 0; k < nlay; ++k) {
+        size_t ix = (size_t)iplon + (size_t)ncol * (size_t)k;
+        hr[ix] = o.htr[k];
+        hrc[ix] = o.htr[k];
+      }
+    }
+  }
+  return 0;
+}
+
+int orc_rrtmg_sw(int ncol, int nlay, int icld, int iaer, const double* play, const double* plev,
+                 const double* tlay, const double* tlev, const double* tsfc, const double* h2ovmr,
+                 const double* o3vmr, const double* co2vmr, const double* ch4vmr, const double* n2ovmr,
+                 const double* o2vmr, const double* asdir, const double* asdif, const double* aldir,
+                 const double* aldif, const double* coszen, double adjes, int dyofyr, double scon,
+                 const double* tauaer, const double* ssaaer, const double* asmaer, double* swuflx,
+                 double* swdflx, double* swhr, double* swuflxc, double* swdflxc, double* swhrc, int nthreads) {
+  if (!g_ready) return 2;
+  if (icld != 0) return 3;
+  if (iaer != 0 && iaer != 10) return 3;
+  SwInput in{ncol, nlay, iaer, dyofyr, adjes, scon, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr,
+             ch4vmr, n2ovmr, o2vmr, asdir, asdif, aldir, aldif, coszen, tauaer, ssaaer, asmaer};
+#pragma omp parallel num_threads(nthreads > 0 ? nthreads : orc_max_threads())
+  {
+    SwColumn c;
+    SwOut o;
+#pragma omp for schedule(dynamic, 16)
+    for (int iplon = 0; iplon < ncol; ++iplon) {
+      sw_column(in, iplon, c, o);
+      for (int k = 1; k <= nlay + 1; ++k) {
+        size_t ix = (size_t)iplon + (size_t)ncol * (size_t)(k - 1);
+        swuflx[ix] = o.fu[k];
+        swdflx[ix] = o.fd[k];
+        swuflxc[ix] = o.cu[k];
+        swdflxc[ix] = o.cd[k];
+      }
+      for (int k = 1; k <= nlay; ++k) {
+        size_t ix = (size_t)iplon + (size_t)ncol * (size_t)(k - 1);
+        swhr[ix] = o.hr[k];
+        swhrc[ix] = o.hrc[k];
+      }
+    }
+  }
+  return 0;
+}
+
+// Gas optics only (stage parity): taug/fracs (ncol, nlay, 140), laytrop (ncol).
+int orc_lw_optics(int ncol, int nlay, const double* play, const double* plev, const double* tlay,
+                  const double* tlev, const double* tsfc, const double* h2ovmr, const double* o3vmr,
+                  const double* co2vmr, const double* ch4vmr, const double* n2ovmr, const double* o2vmr,
+                  double* taug, double* fracs, int* laytrop) {
+  if (!g_ready) return 2;
+  LwInput in{ncol, nlay, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr,
+             nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+#pragma omp parallel
+  {
+    LwColumn c;
+#pragma omp for
+    for (int iplon = 0; iplon < ncol; ++iplon) {
+      lw_inatm(in, iplon, c);
+      lw_setcoef(c, 0);
+      lw_taumol(c);
+      laytrop[iplon] = c.laytrop;
+      for (int g = 1; g <= 140; ++g)
+        for (int k = 1; k <= nlay; ++k) {
+          size_t ix = (size_t)iplon + (size_t)ncol * ((size_t)(k - 1) + (size_t)nlay * (size_t)(g - 1));
+          taug[ix] = c.taug[g][k];
+          fracs[ix] = c.fracs[g][k];
+        }
+    }
+  }
+  return 0;
+}
+
+// Gas optics only: taug/taur (ncol, nlay, 112), sfluxzen (ncol, 112).
+int orc_sw_optics(int ncol, int nlay, const double* play, const double* plev, const double* tlay,
+                  const double* tlev, const double* tsfc, const double* h2ovmr, const double* o3vmr,
+                  const double* co2vmr, const double* ch4vmr, const double* n2ovmr, const double* o2vmr,
+                  double* taug, double* taur, double* sfluxzen) {
+  if (!g_ready) return 2;
+  SwInput in{ncol, nlay, 0, 0, 1.0, 1368.22, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr,
+             ch4vmr, n2ovmr, o2vmr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+#pragma omp parallel
+  {
+    SwColumn c;
+#pragma omp for
+    for (int iplon = 0; iplon < ncol; ++iplon) {
+      sw_inatm(in, iplon, c);
+      sw_setcoef(c);
+      sw_taumol(c);
+      for (int g = 1; g <= 112; ++g) {
+        sfluxzen[(size_t)iplon + (size_t)ncol * (size_t)(g - 1)] = c.sfluxzen[g];
+        for (int k = 1; k <= nlay; ++k) {
+          size_t ix = (size_t)iplon + (size_t)ncol * ((size_t)(k - 1) + (size_t)nlay * (size_t)(g - 1));
+          taug[ix] = c.taug[g][k];
+          taur[ix] = c.taur[g][k];
+        }
+      }
+    }
+  }
+  return 0;
+}
+
+// Reduced table access: key like "lw03" / "sw24", name like "ka", "fracrefa".
+// Returns the element count (copies at most n values), or -1.
+int orc_table(const char* key, const char* name, double* out, int n) {
+  if (!g_ready) return -1;
+  std::string k(key), nm(name);
+  const FArr* a = nullptr;
+  int b = std::atoi(k.c_str() + 2);
+  if (k.rfind("lw", 0) == 0 && b >= 1 && b <= 16) {
+    auto it = g_lw.t[b].find(nm);
+    if (it != g_lw.t[b].end()) a = &it->second;
+  } else if (k.rfind("sw", 0) == 0 && b >= 16 && b <= 29) {
+    auto it = g_sw.t[b].find(nm);
+    if (it != g_sw.t[b].end()) a = &it->second;
+  }
+  if (!a) return -1;
+  int m = (int)a->v.size();
+  for (int i = 0; i < m && i < n; ++i) out[i] = a->v[i];
+  return m;
+}
+
+}  // extern "C"

@@ -1,0 +1,79 @@
+// CPU oracle, longwave: data structures.  TEST INFRASTRUCTURE ONLY.
+#pragma once
+#include <map>
+#include <string>
+#include <vector>
+
+#include "oracle_tables.hpp"
+
+namespace orc {
+
+extern int g_table_mode;
+
+struct LwTables {
+  std::map<std::string, FArr> t[17];  // reduced per-band tables ("ka", "kb", "selfref", ...)
+  FArr pref, preflog, tref, chi_mls, totplnk, totplk16, totplnkderiv, totplk16deriv;
+  double delwave[17];
+  int ngc[17], ngs[17], nspa[17], nspb[17];
+  double tau_tbl[10001], exp_tbl[10001], tfn_tbl[10001];
+  double bpade, heatfac, fluxfac, oneminus, grav, avogad;
+};
+extern LwTables g_lw;
+
+// Arguments of rrtmg_lw (rrtmg_lw_rad.nomcica.f90:80-89), column-major with
+// the column index fastest; optional gases may be null (treated as zero).
+struct LwInput {
+  int ncol, nlay;
+  const double *play, *plev, *tlay, *tlev, *tsfc, *h2ovmr, *o3vmr, *co2vmr, *ch4vmr, *n2ovmr,
+      *o2vmr, *cfc11vmr, *cfc12vmr, *cfc22vmr, *ccl4vmr, *emis, *tauaer;
+};
+
+struct LwColumn {
+  int nlayers = 0, laytrop = 0;
+  double tbound = 0, pwvcm = 0;
+  std::vector<double> pavel, tavel, pz, tz, coldry, wbrodl;
+  std::vector<double> wkl[8], wx[5], taua[17];
+  double semiss[17], plankbnd[17], dplankbnd_dt[17];
+  std::vector<double> planklay[17], planklev[17];
+  std::vector<int> jp, jt, jt1, indself, indfor, indminor;
+  std::vector<double> colh2o, colco2, colo3, coln2o, colco, colch4, colo2, colbrd;
+  std::vector<double> fac00, fac01, fac10, fac11, selffac, selffrac, forfac, forfrac;
+  std::vector<double> minorfrac, scaleminor, scaleminorn2;
+  std::vector<double> rat_h2oco2, rat_h2oco2_1, rat_h2oo3, rat_h2oo3_1, rat_h2on2o, rat_h2on2o_1,
+      rat_h2och4, rat_h2och4_1, rat_n2oco2, rat_n2oco2_1, rat_o3co2, rat_o3co2_1;
+  std::vector<double> taug[141], fracs[141], taut[141];
+
+  void resize(int nl) {
+    auto r = [&](std::vector<double>& v) { v.assign(nl + 2, 0.0); };
+    auto ri = [&](std::vector<int>& v) { v.assign(nl + 2, 0); };
+    r(pavel); r(tavel); r(pz); r(tz); r(coldry); r(wbrodl);
+    for (auto& v : wkl) r(v);
+    for (auto& v : wx) r(v);
+    for (auto& v : taua) r(v);
+    for (auto& v : planklay) r(v);
+    for (auto& v : planklev) r(v);
+    ri(jp); ri(jt); ri(jt1); ri(indself); ri(indfor); ri(indminor);
+    r(colh2o); r(colco2); r(colo3); r(coln2o); r(colco); r(colch4); r(colo2); r(colbrd);
+    r(fac00); r(fac01); r(fac10); r(fac11); r(selffac); r(selffrac); r(forfac); r(forfrac);
+    r(minorfrac); r(scaleminor); r(scaleminorn2);
+    r(rat_h2oco2); r(rat_h2oco2_1); r(rat_h2oo3); r(rat_h2oo3_1); r(rat_h2on2o); r(rat_h2on2o_1);
+    r(rat_h2och4); r(rat_h2och4_1); r(rat_n2oco2); r(rat_n2oco2_1); r(rat_o3co2); r(rat_o3co2_1);
+    for (auto& v : taug) r(v);
+    for (auto& v : fracs) r(v);
+    for (auto& v : taut) r(v);
+    for (int b = 0; b < 17; ++b) semiss[b] = plankbnd[b] = dplankbnd_dt[b] = 0.0;
+  }
+};
+
+struct LwOut {
+  std::vector<double> totu, totd, htr, dtotu_dt;  // levels 0..nlay (htr: layers 0..nlay-1, top 0)
+};
+
+void lw_init(const Blob& blob, double cpdair);
+void lw_inatm(const LwInput& in, int iplon, LwColumn& c);
+void lw_setcoef(LwColumn& c, int idrv);
+void lw_taumol(LwColumn& c);
+void lw_rtrnmr(LwColumn& c, int idrv, LwOut& out);
+void lw_column(const LwInput& in, int iplon, int idrv, LwColumn& c, LwOut& out);
+
+}  // namespace orc

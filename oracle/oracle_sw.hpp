@@ -1,0 +1,74 @@
+// CPU oracle, shortwave: data structures.  TEST INFRASTRUCTURE ONLY.
+#pragma once
+#include <map>
+#include <string>
+#include <vector>
+
+#include "oracle_tables.hpp"
+
+namespace orc {
+
+extern int g_table_mode;
+
+struct SwTables {
+  std::map<std::string, FArr> t[30];  // reduced per-band tables, bands 16..29
+  FArr preflog, tref;
+  int ngc[30], ngs[30], nspa[30], nspb[30];
+  double exp_tbl[10001];
+  double bpade, heatfac, oneminus, grav, avogad, pi;
+};
+extern SwTables g_sw;
+
+// Arguments of rrtmg_sw (rrtmg_sw_rad.nomcica.f90:78-88); aerosol arrays are
+// (ncol, nlay, 14) and used when iaer = 10.
+struct SwInput {
+  int ncol, nlay, iaer, dyofyr;
+  double adjes, scon;
+  const double *play, *plev, *tlay, *tlev, *tsfc, *h2ovmr, *o3vmr, *co2vmr, *ch4vmr, *n2ovmr, *o2vmr;
+  const double *asdir, *asdif, *aldir, *aldif, *coszen;
+  const double *tauaer, *ssaaer, *asmaer;
+};
+
+struct SwColumn {
+  int nlayers = 0, laytrop = 0, laylow = 0;
+  double tbound = 0;
+  double adjflux[30];
+  std::vector<double> pavel, tavel, pz, tz, pdp, coldry;
+  std::vector<double> wkl[8], taua[15], ssaa[15], asma[15];
+  std::vector<int> jp, jt, jt1, indself, indfor;
+  std::vector<double> colh2o, colco2, colo3, coln2o, colch4, colo2, colmol;
+  std::vector<double> fac00, fac01, fac10, fac11, selffac, selffrac, forfac, forfrac;
+  std::vector<double> taug[113], taur[113];
+  double sfluxzen[113];
+
+  void resize(int nl) {
+    auto r = [&](std::vector<double>& v) { v.assign(nl + 2, 0.0); };
+    auto ri = [&](std::vector<int>& v) { v.assign(nl + 2, 0); };
+    r(pavel); r(tavel); r(pz); r(tz); r(pdp); r(coldry);
+    for (auto& v : wkl) r(v);
+    for (auto& v : taua) r(v);
+    for (auto& v : ssaa) r(v);
+    for (auto& v : asma) r(v);
+    ri(jp); ri(jt); ri(jt1); ri(indself); ri(indfor);
+    r(colh2o); r(colco2); r(colo3); r(coln2o); r(colch4); r(colo2); r(colmol);
+    r(fac00); r(fac01); r(fac10); r(fac11); r(selffac); r(selffrac); r(forfac); r(forfrac);
+    for (auto& v : taug) r(v);
+    for (auto& v : taur) r(v);
+    for (int g = 0; g < 113; ++g) sfluxzen[g] = 0.0;
+    for (int b = 0; b < 30; ++b) adjflux[b] = 0.0;
+  }
+};
+
+struct SwOut {
+  std::vector<double> fu, fd, cu, cd;  // levels 1..nlay+1 (surface first)
+  std::vector<double> hr, hrc;         // layers 1..nlay
+};
+
+void sw_init(const Blob& blob, double cpdair);
+void sw_inatm(const SwInput& in, int iplon, SwColumn& c);
+void sw_setcoef(SwColumn& c);
+void sw_taumol(SwColumn& c);
+void sw_spcvrt(SwColumn& c, double prmu0, const double* albdir, const double* albdif, SwOut& out);
+bool sw_column(const SwInput& in, int iplon, SwColumn& c, SwOut& out);
+
+}  // namespace orc

@@ -1,0 +1,150 @@
+/*
+ * rrtmg_gpu.h -- C-ABI of the GB300 (sm_103a) implementation of RRTMG clear-sky
+ * longwave and shortwave column radiation, the radiation hot path of MiMA.
+ *
+ * Drop-in boundary.  MiMA's radiation driver calls
+ *     rrtmg_lw(...)   src/atmos_param/rrtm_radiation/rrtmg_lw/gcm_model/src/rrtmg_lw_rad.nomcica.f90:80-89
+ *     rrtmg_sw(...)   src/atmos_param/rrtm_radiation/rrtmg_sw/gcm_model/src/rrtmg_sw_rad.nomcica.f90:78-88
+ *     rrtmg_lw_ini / rrtmg_sw_ini(cpdair)   rrtmg_lw_init.f90:28, rrtmg_sw_init.f90:28
+ * from run_rrtmg (src/atmos_param/rrtm_radiation/rrtm_radiation.f90:686-748).
+ * rrtmg_lw_c / rrtmg_sw_c below take the same arguments in the same order and
+ * with the same meaning, plus the handle and the two array extents the Fortran
+ * assumed-shape arrays carry implicitly.
+ *
+ * Conventions
+ *   - Arrays are Fortran column-major with the column index fastest:
+ *     (ncol,nlay), (ncol,nlay+1), (ncol), emis (ncol,16), tauaer (ncol,nlay,nbnd).
+ *     RRTM layer 1 is the surface layer; pressures in hPa.
+ *   - As in MiMA, the h2ovmr argument carries specific humidity (kg/kg) and
+ *     o3vmr the O3 mass mixing ratio; both are converted as in inatm
+ *     (rrtmg_lw_rad.nomcica.f90:775-778, rrtmg_sw_rad.nomcica.f90:1004-1007).
+ *   - Outputs are fully overwritten.  Heating rates are K/day.  The SW rate of
+ *     the top layer is 0 (MiMA's change, rrtmg_sw_rad.nomcica.f90:725-726);
+ *     the LW rate of the top layer is computed (rrtmg_lw_rtrnmr.f90:774-775
+ *     zeroes htr(nlayers), which lies above the last output layer).
+ *   - Optional gas arrays (ch4, n2o, o2, cfc*) and tauaer may be NULL (= 0).
+ *   - Cloud arguments are accepted for signature compatibility and must
+ *     describe clear sky: icld must be 0.  The reference coerces icld and
+ *     iaer silently (:437, :471-479); this library returns
+ *     RRTMG_ERR_UNSUPPORTED for any configuration it does not compute and never
+ *     falls back to a CPU path.
+ *   - Every entry point returns a status (0 = success).  A handle is not
+ *     thread-safe; use one handle per host thread.
+ */
+#ifndef RRTMG_GPU_H
+#define RRTMG_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct rrtmg_gpu_state* rrtmg_gpu_handle;
+
+enum rrtmg_gpu_status {
+  RRTMG_OK = 0,
+  RRTMG_ERR_ARG = 1,          /* bad dimension, null required pointer, bad handle */
+  RRTMG_ERR_UNSUPPORTED = 2,  /* icld != 0, iaer not in {0,10}, idrv not in {0,1} */
+  RRTMG_ERR_CUDA = 3,         /* CUDA runtime error (see rrtmg_gpu_last_error) */
+  RRTMG_ERR_TABLES = 4,       /* table blob missing, malformed or checksum mismatch */
+  RRTMG_ERR_INPUT = 5,        /* device-side validation flagged a non-finite or out-of-range input */
+  RRTMG_ERR_NOMEM = 6         /* device workspace allocation failed */
+};
+
+enum rrtmg_gpu_precision {
+  RRTMG_PREC_FP64 = 0,  /* FP64 everywhere; bit-level parity target vs the FP64 reference path */
+  RRTMG_PREC_SPLIT = 1  /* FP32 gas optics, transmittances and per-g recursions; FP64 g-point
+                           accumulation and heating-rate differencing */
+};
+
+/* Maximum number of layers (parrrtm.f90 / parrrsw.f90 mxlay). */
+#define RRTMG_GPU_MAX_LAYERS 203
+
+/* Replaces rrtmg_lw_ini(cpdair) + rrtmg_sw_ini(cpdair) (rrtmg_lw_init.f90:28-175,
+ * rrtmg_sw_init.f90:28-154): reads the unreduced coefficient tables from
+ * table_blob, performs the 256->140 / 224->112 g-point reduction, builds the
+ * transmittance tables and uploads everything to `device`. */
+int rrtmg_gpu_init(double cpdair, const char* table_blob, int device, rrtmg_gpu_handle* out);
+int rrtmg_gpu_finalize(rrtmg_gpu_handle h);
+
+/* Selects RRTMG_PREC_FP64 (default) or RRTMG_PREC_SPLIT for later calls. */
+int rrtmg_gpu_set_precision(rrtmg_gpu_handle h, int precision);
+
+const char* rrtmg_gpu_error_string(int status);
+/* Detail of the last failure on this handle ("" if none). */
+const char* rrtmg_gpu_last_error(rrtmg_gpu_handle h);
+/* Number of kernel launches issued by this handle since init. */
+long long rrtmg_gpu_launch_count(rrtmg_gpu_handle h);
+
+/* rrtmg_lw (rrtmg_lw_rad.nomcica.f90:80-89), host arrays.  tauaer (ncol,nlay,16)
+ * is always added to the gas optical depth (the reference forces iaer = 10,
+ * :442).  duflx_dt/duflxc_dt (ncol,nlay+1) are written when idrv = 1. */
+int rrtmg_lw_c(rrtmg_gpu_handle h, int ncol, int nlay, int icld, int idrv,
+               const double* play, const double* plev, const double* tlay, const double* tlev,
+               const double* tsfc, const double* h2ovmr, const double* o3vmr, const double* co2vmr,
+               const double* ch4vmr, const double* n2ovmr, const double* o2vmr,
+               const double* cfc11vmr, const double* cfc12vmr, const double* cfc22vmr,
+               const double* ccl4vmr, const double* emis, int inflglw, int iceflglw, int liqflglw,
+               const double* cldfr, const double* taucld, const double* cicewp, const double* cliqwp,
+               const double* reice, const double* reliq, const double* tauaer,
+               double* uflx, double* dflx, double* hr, double* uflxc, double* dflxc, double* hrc,
+               double* duflx_dt, double* duflxc_dt);
+
+/* rrtmg_sw (rrtmg_sw_rad.nomcica.f90:78-88), host arrays.  Columns with
+ * coszen < 1e-10 get zero fluxes and heating (MiMA's skip, :502-510).
+ * iaer = 10 uses tauaer/ssaaer/asmaer (ncol,nlay,14); ecaer is ignored. */
+int rrtmg_sw_c(rrtmg_gpu_handle h, int ncol, int nlay, int icld, int iaer,
+               const double* play, const double* plev, const double* tlay, const double* tlev,
+               const double* tsfc, const double* h2ovmr, const double* o3vmr, const double* co2vmr,
+               const double* ch4vmr, const double* n2ovmr, const double* o2vmr,
+               const double* asdir, const double* asdif, const double* aldir, const double* aldif,
+               const double* coszen, double adjes, int dyofyr, double scon,
+               int inflgsw, int iceflgsw, int liqflgsw, const double* cldfr, const double* taucld,
+               const double* ssacld, const double* asmcld, const double* fsfcld,
+               const double* cicewp, const double* cliqwp, const double* reice, const double* reliq,
+               const double* tauaer, const double* ssaaer, const double* asmaer, const double* ecaer,
+               double* swuflx, double* swdflx, double* swhr, double* swuflxc, double* swdflxc,
+               double* swhrc);
+
+/* Device-pointer variants: identical arguments, every array is a device
+ * pointer, work is enqueued on `stream` (a cudaStream_t, NULL = default) and
+ * the call returns without synchronising.  Input validation results are
+ * collected on the device; rrtmg_gpu_sync_status() waits for the stream and
+ * returns RRTMG_ERR_INPUT if any enqueued call saw invalid input.  After a
+ * first call with the same (ncol, nlay) the calls allocate nothing and may be
+ * captured in a CUDA graph. */
+int rrtmg_lw_dev(rrtmg_gpu_handle h, void* stream, int ncol, int nlay, int icld, int idrv,
+                 const double* play, const double* plev, const double* tlay, const double* tlev,
+                 const double* tsfc, const double* h2ovmr, const double* o3vmr, const double* co2vmr,
+                 const double* ch4vmr, const double* n2ovmr, const double* o2vmr,
+                 const double* cfc11vmr, const double* cfc12vmr, const double* cfc22vmr,
+                 const double* ccl4vmr, const double* emis, int inflglw, int iceflglw, int liqflglw,
+                 const double* cldfr, const double* taucld, const double* cicewp, const double* cliqwp,
+                 const double* reice, const double* reliq, const double* tauaer,
+                 double* uflx, double* dflx, double* hr, double* uflxc, double* dflxc, double* hrc,
+                 double* duflx_dt, double* duflxc_dt);
+
+int rrtmg_sw_dev(rrtmg_gpu_handle h, void* stream, int ncol, int nlay, int icld, int iaer,
+                 const double* play, const double* plev, const double* tlay, const double* tlev,
+                 const double* tsfc, const double* h2ovmr, const double* o3vmr, const double* co2vmr,
+                 const double* ch4vmr, const double* n2ovmr, const double* o2vmr,
+                 const double* asdir, const double* asdif, const double* aldir, const double* aldif,
+                 const double* coszen, double adjes, int dyofyr, double scon,
+                 int inflgsw, int iceflgsw, int liqflgsw, const double* cldfr, const double* taucld,
+                 const double* ssacld, const double* asmcld, const double* fsfcld,
+                 const double* cicewp, const double* cliqwp, const double* reice, const double* reliq,
+                 const double* tauaer, const double* ssaaer, const double* asmaer, const double* ecaer,
+                 double* swuflx, double* swdflx, double* swhr, double* swuflxc, double* swdflxc,
+                 double* swhrc);
+
+/* Reserves device workspace for calls of up to ncol columns and nlay layers,
+ * so that later device calls allocate nothing (e.g. before graph capture). */
+int rrtmg_gpu_reserve(rrtmg_gpu_handle h, int ncol, int nlay);
+
+/* Waits for `stream` and reports RRTMG_ERR_INPUT if an enqueued call flagged
+ * invalid input (the flag is then cleared). */
+int rrtmg_gpu_sync_status(rrtmg_gpu_handle h, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RRTMG_GPU_H */

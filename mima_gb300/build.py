@@ -1,0 +1,86 @@
+"""Builds the sm_103a shared library ``mima_gb300/lib/librrtmg_gpu.so`` in-tree.
+
+Every translation unit is compiled by nvcc in parallel with one
+``-gencode arch=compute_103a,code=sm_103a``; the FP64 kernels are compiled with
+``--fmad=false`` (separately rounded multiplies and adds, for bit-level
+reproducibility of the FP64 path), the FP32-split kernels with contraction.
+The library has a plain C ABI (include/rrtmg_gpu.h) and links the CUDA
+runtime statically, so it needs no torch at load time.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+CSRC = PKG / "csrc"
+LIBDIR = PKG / "lib"
+LIB = LIBDIR / "librrtmg_gpu.so"
+OBJDIR = LIBDIR / "obj"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+          f"-I{ROOT / 'include'}", f"-I{CSRC}", "--expt-relaxed-constexpr"]
+
+UNITS = {
+    "kernels_fp64.cu": ["--fmad=false"],
+    "kernels_split.cu": [],
+    "tables_host.cu": [],
+    "abi.cu": ["-Xcompiler", "-fvisibility=default"],
+}
+
+
+def nvcc() -> str:
+    exe = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not Path(exe).exists():
+        raise RuntimeError("nvcc not found: the CUDA toolkit is required to build librrtmg_gpu.so")
+    return exe
+
+
+def _stale(obj: Path, src: Path) -> bool:
+    if not obj.exists():
+        return True
+    deps = [src] + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + [ROOT / "include" / "rrtmg_gpu.h"]
+    t = obj.stat().st_mtime
+    return any(d.stat().st_mtime > t for d in deps)
+
+
+def build(force: bool = False, verbose: bool = False, extra=None) -> Path:
+    OBJDIR.mkdir(parents=True, exist_ok=True)
+    cc = nvcc()
+    procs = []
+    objs = []
+    for unit, flags in UNITS.items():
+        src = CSRC / unit
+        obj = OBJDIR / (unit + ".o")
+        objs.append(obj)
+        if force or _stale(obj, src):
+            cmd = [cc, *ARCH, *COMMON, *flags, *(extra or []), "-c", str(src), "-o", str(obj)]
+            if verbose:
+                print(" ".join(cmd), flush=True)
+            procs.append((unit, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
+    errors = []
+    for unit, p in procs:
+        out, _ = p.communicate()
+        if p.returncode != 0:
+            errors.append(f"--- {unit} ---\n{out}")
+        elif verbose and out.strip():
+            print(out)
+    if errors:
+        raise RuntimeError("nvcc failed:\n" + "\n".join(errors))
+    if force or procs or not LIB.exists():
+        tmp = LIB.with_suffix(".so.tmp")
+        cmd = [cc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
+        os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True))

@@ -1,0 +1,502 @@
+// C-ABI of the GB300 RRTMG path (declared in include/rrtmg_gpu.h).
+//
+// A handle owns: the device coefficient tables (FP64 and FP32 copies), one
+// internal stream for the host-pointer entry points, a device flag word for
+// input validation, and three device workspaces grown on demand: LW scratch,
+// SW scratch (kept separate so an LW and an SW call may run concurrently on
+// different streams) and staging buffers for the host-pointer entry points.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include <cmath>
+
+#include "common.cuh"
+#include "launch.h"
+#include "rrtmg_gpu.h"
+#include "tables_host.h"
+
+using namespace rrtmg;
+
+namespace {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace
+
+struct rrtmg_gpu_state {
+  int device = 0;
+  int precision = RRTMG_PREC_FP64;
+  cudaStream_t stream = nullptr;
+  HostTables host;
+  double *lw_tab64 = nullptr, *sw_tab64 = nullptr, *lw_exp64 = nullptr, *lw_tfn64 = nullptr, *sw_exp64 = nullptr;
+  double *totplnk = nullptr, *totplnkderiv = nullptr;
+  float *lw_tab32 = nullptr, *sw_tab32 = nullptr, *lw_exp32 = nullptr, *lw_tfn32 = nullptr, *sw_exp32 = nullptr;
+  unsigned* flags = nullptr;
+  DevBuf lw_ws, sw_ws, io;
+  long long launches = 0;
+  std::string err;
+};
+
+namespace {
+
+int fail(rrtmg_gpu_state* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+int cuda_fail(rrtmg_gpu_state* h, cudaError_t e, const char* where) {
+  return fail(h, RRTMG_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+template <class T>
+cudaError_t upload(T** dst, const std::vector<T>& src) {
+  cudaError_t e = cudaMalloc((void**)dst, src.size() * sizeof(T) + 16);
+  if (e != cudaSuccess) return e;
+  return cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+std::vector<float> to_f32(const std::vector<double>& v) {
+  std::vector<float> f(v.size());
+  for (size_t i = 0; i < v.size(); ++i) f[i] = (float)v[i];
+  return f;
+}
+
+size_t align256(size_t n) { return (n + 255) & ~(size_t)255; }
+
+// Grow a workspace; refuses while the stream is being captured.
+int ensure(rrtmg_gpu_state* h, DevBuf& b, size_t need, cudaStream_t s) {
+  if (b.bytes >= need) return RRTMG_OK;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (s != nullptr && cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone)
+    return fail(h, RRTMG_ERR_NOMEM, "workspace too small during stream capture; call rrtmg_gpu_reserve first");
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.bytes = 0;
+  cudaError_t e = cudaMalloc(&b.p, need);
+  if (e != cudaSuccess) {
+    b.p = nullptr;
+    return fail(h, RRTMG_ERR_NOMEM, std::string("device workspace allocation failed: ") + cudaGetErrorString(e));
+  }
+  b.bytes = need;
+  return RRTMG_OK;
+}
+
+struct Carver {
+  char* base;
+  size_t off = 0;
+  template <class T>
+  T* take(size_t n) {
+    T* p = (T*)(base ? base + off : nullptr);
+    off += align256(n * sizeof(T));
+    return p;
+  }
+};
+
+LwWork carve_lw(void* base, int ncol, int nlay, size_t* bytes) {
+  Carver c{(char*)base};
+  const size_t N = (size_t)ncol, L = (size_t)nlay;
+  LwWork w;
+  w.idx = c.take<uint32_t>(L * N);
+  w.f = c.take<double>((size_t)LF_N * L * N);
+  w.planklay = c.take<double>(16 * L * N);
+  w.planklev = c.take<double>(16 * (L + 1) * N);
+  w.plankbnd = c.take<double>(16 * N);
+  w.dplankbnd = c.take<double>(16 * N);
+  w.secdiff = c.take<double>(16 * N);
+  w.laytrop = c.take<int>(N);
+  w.bu = c.take<double>(16 * (L + 1) * N);
+  w.bd = c.take<double>(16 * (L + 1) * N);
+  w.bdu = c.take<double>(16 * (L + 1) * N);
+  if (bytes) *bytes = c.off;
+  return w;
+}
+
+SwWork carve_sw(void* base, int ncol, int nlay, size_t* bytes) {
+  Carver c{(char*)base};
+  const size_t N = (size_t)ncol, L = (size_t)nlay;
+  SwWork w;
+  w.idx = c.take<uint32_t>(L * N);
+  w.f = c.take<double>((size_t)SF_N * L * N);
+  w.laytrop = c.take<int>(N);
+  w.laysolfr = c.take<int>(14 * N);
+  w.su = c.take<double>(14 * (L + 1) * N);
+  w.sd = c.take<double>(14 * (L + 1) * N);
+  if (bytes) *bytes = c.off;
+  return w;
+}
+
+bool valid_handle(rrtmg_gpu_state* h) { return h != nullptr && h->lw_tab64 != nullptr; }
+
+int check_dims(rrtmg_gpu_state* h, int ncol, int nlay) {
+  if (ncol < 1) return fail(h, RRTMG_ERR_ARG, "ncol must be >= 1");
+  if (nlay < 2 || nlay > RRTMG_GPU_MAX_LAYERS) return fail(h, RRTMG_ERR_ARG, "nlay must be in [2, 203]");
+  if ((long long)ncol * (long long)(nlay + 1) * 16 > (1LL << 31) - 1)
+    return fail(h, RRTMG_ERR_ARG, "ncol * (nlay+1) too large for one call; split the columns");
+  return RRTMG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Enqueue one LW radiation call on stream s (all pointers on the device).
+// ---------------------------------------------------------------------------
+int lw_run(rrtmg_gpu_state* h, cudaStream_t s, int ncol, int nlay, int idrv, const LwIn& in, double* uflx,
+           double* dflx, double* hr, double* uflxc, double* dflxc, double* hrc, double* duflx_dt, double* duflxc_dt) {
+  size_t need;
+  carve_lw(nullptr, ncol, nlay, &need);
+  int rc = ensure(h, h->lw_ws, need, s);
+  if (rc) return rc;
+  LwWork w = carve_lw(h->lw_ws.p, ncol, nlay, nullptr);
+  launch_lw_prep(in, w, h->totplnk, h->totplnkderiv, ncol, nlay, idrv, h->flags, s);
+  LwPrep p{w.idx, w.f, w.planklay, w.planklev, w.plankbnd, w.dplankbnd, w.secdiff, w.laytrop};
+  const int nb = lw_gpoint_blocks(h->host.lw, ncol);
+  if (h->precision == RRTMG_PREC_SPLIT)
+    launch_lw_gpoint_split(p, in.emis, in.tauaer, h->lw_tab32, h->lw_exp32, h->lw_tfn32, w.bu, w.bd, w.bdu, ncol,
+                           nlay, idrv, nb, s);
+  else
+    launch_lw_gpoint_fp64(p, in.emis, in.tauaer, h->lw_tab64, h->lw_exp64, h->lw_tfn64, w.bu, w.bd, w.bdu, ncol, nlay,
+                          idrv, nb, s);
+  launch_lw_finalize(w.bu, w.bd, w.bdu, in.plev, ncol, nlay, idrv, uflx, dflx, hr, uflxc, dflxc, hrc, duflx_dt,
+                     duflxc_dt, s);
+  h->launches += 3;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(h, e, "LW kernel launch");
+  return RRTMG_OK;
+}
+
+int sw_run(rrtmg_gpu_state* h, cudaStream_t s, int ncol, int nlay, int iaer, double adjes, int dyofyr, double scon,
+           const SwIn& in, double* swuflx, double* swdflx, double* swhr, double* swuflxc, double* swdflxc,
+           double* swhrc) {
+  size_t need;
+  carve_sw(nullptr, ncol, nlay, &need);
+  int rc = ensure(h, h->sw_ws, need, s);
+  if (rc) return rc;
+  SwWork w = carve_sw(h->sw_ws.p, ncol, nlay, nullptr);
+  // Incident-flux scaling (inatm_sw, rrtmg_sw_rad.nomcica.f90:953-972): the
+  // GCM's Earth-Sun factor, or Iqbal's day-of-year formula, times scon/1368.22.
+  double adjflx = adjes;
+  if (dyofyr > 0) {
+    const double gamma = 2. * h->host.sw.pi * (dyofyr - 1) / 365.;
+    adjflx = 1.000110 + .034221 * std::cos(gamma) + .001289 * std::sin(gamma) + .000719 * std::cos(2. * gamma) +
+             .000077 * std::sin(2. * gamma);
+  }
+  const double adjflux = adjflx * (scon / 1.36822e+03);
+  launch_sw_prep(in, w, ncol, nlay, h->flags, s);
+  SwPrep p{w.idx, w.f, w.laytrop, w.laysolfr};
+  const int nb = sw_gpoint_blocks(h->host.sw, ncol);
+  if (h->precision == RRTMG_PREC_SPLIT)
+    launch_sw_gpoint_split(p, in, adjflux, iaer, h->sw_tab32, h->sw_tab64, h->sw_exp32, w.su, w.sd, ncol, nlay, nb, s);
+  else
+    launch_sw_gpoint_fp64(p, in, adjflux, iaer, h->sw_tab64, h->sw_exp64, w.su, w.sd, ncol, nlay, nb, s);
+  launch_sw_finalize(w.su, w.sd, in.plev, in.coszen, ncol, nlay, swuflx, swdflx, swhr, swuflxc, swdflxc, swhrc, s);
+  h->launches += 3;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(h, e, "SW kernel launch");
+  return RRTMG_OK;
+}
+
+int read_flags(rrtmg_gpu_state* h, cudaStream_t s) {
+  unsigned f = 0;
+  cudaError_t e = cudaMemcpyAsync(&f, h->flags, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(h, e, "synchronise");
+  if (f) {
+    cudaMemsetAsync(h->flags, 0, sizeof(unsigned), s);
+    cudaStreamSynchronize(s);
+    return fail(h, RRTMG_ERR_INPUT, "non-finite or out-of-range input (pressure <= 0, T <= 0, q outside [0,1), NaN/Inf)");
+  }
+  return RRTMG_OK;
+}
+
+// Staging of host arrays for the host-pointer entry points.
+struct Stage {
+  rrtmg_gpu_state* h;
+  cudaStream_t s;
+  Carver c;
+  cudaError_t err = cudaSuccess;
+  const double* in(const double* host, size_t n) {
+    if (!host) return nullptr;
+    double* d = c.take<double>(n);
+    if (d && err == cudaSuccess) err = cudaMemcpyAsync(d, host, n * sizeof(double), cudaMemcpyHostToDevice, s);
+    return d;
+  }
+  double* out(size_t n) { return c.take<double>(n); }
+};
+
+}  // namespace
+
+extern "C" {
+
+const char* rrtmg_gpu_error_string(int status) {
+  switch (status) {
+    case RRTMG_OK: return "success";
+    case RRTMG_ERR_ARG: return "invalid argument";
+    case RRTMG_ERR_UNSUPPORTED: return "unsupported configuration (only clear sky, iaer 0/10, idrv 0/1)";
+    case RRTMG_ERR_CUDA: return "CUDA error";
+    case RRTMG_ERR_TABLES: return "coefficient table blob missing or invalid";
+    case RRTMG_ERR_INPUT: return "invalid input values";
+    case RRTMG_ERR_NOMEM: return "device memory allocation failed";
+    default: return "unknown status";
+  }
+}
+
+const char* rrtmg_gpu_last_error(rrtmg_gpu_handle h) { return h ? h->err.c_str() : "null handle"; }
+
+long long rrtmg_gpu_launch_count(rrtmg_gpu_handle h) { return h ? h->launches : 0; }
+
+int rrtmg_gpu_init(double cpdair, const char* table_blob, int device, rrtmg_gpu_handle* out) {
+  if (!out) return RRTMG_ERR_ARG;
+  *out = nullptr;
+  if (!(cpdair > 0.0)) return RRTMG_ERR_ARG;
+  rrtmg_gpu_state* h = new (std::nothrow) rrtmg_gpu_state();
+  if (!h) return RRTMG_ERR_NOMEM;
+  std::string err = build_host_tables(table_blob, cpdair, h->host);
+  if (!err.empty()) {
+    std::fprintf(stderr, "rrtmg_gpu_init: %s\n", err.c_str());
+    delete h;
+    return RRTMG_ERR_TABLES;
+  }
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = upload(&h->lw_tab64, h->host.lw_tab);
+  if (e == cudaSuccess) e = upload(&h->sw_tab64, h->host.sw_tab);
+  if (e == cudaSuccess) e = upload(&h->lw_exp64, h->host.lw_exp);
+  if (e == cudaSuccess) e = upload(&h->lw_tfn64, h->host.lw_tfn);
+  if (e == cudaSuccess) e = upload(&h->sw_exp64, h->host.sw_exp);
+  if (e == cudaSuccess) e = upload(&h->totplnk, h->host.totplnk);
+  if (e == cudaSuccess) e = upload(&h->totplnkderiv, h->host.totplnkderiv);
+  if (e == cudaSuccess) e = upload(&h->lw_tab32, to_f32(h->host.lw_tab));
+  if (e == cudaSuccess) e = upload(&h->sw_tab32, to_f32(h->host.sw_tab));
+  if (e == cudaSuccess) e = upload(&h->lw_exp32, to_f32(h->host.lw_exp));
+  if (e == cudaSuccess) e = upload(&h->lw_tfn32, to_f32(h->host.lw_tfn));
+  if (e == cudaSuccess) e = upload(&h->sw_exp32, to_f32(h->host.sw_exp));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&h->flags, sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMemset(h->flags, 0, sizeof(unsigned));
+  if (e == cudaSuccess) e = upload_constants_fp64(h->host.lw, h->host.sw);
+  if (e == cudaSuccess) e = upload_constants_split(h->host.lw, h->host.sw);
+  if (e != cudaSuccess) {
+    std::fprintf(stderr, "rrtmg_gpu_init: %s\n", cudaGetErrorString(e));
+    h->device = device;
+    rrtmg_gpu_finalize(h);
+    return RRTMG_ERR_CUDA;
+  }
+  h->device = device;
+  *out = h;
+  return RRTMG_OK;
+}
+
+int rrtmg_gpu_finalize(rrtmg_gpu_handle h) {
+  if (!h) return RRTMG_ERR_ARG;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  void* ptrs[] = {h->lw_tab64, h->sw_tab64, h->lw_exp64, h->lw_tfn64, h->sw_exp64, h->totplnk, h->totplnkderiv,
+                  h->lw_tab32, h->sw_tab32, h->lw_exp32, h->lw_tfn32, h->sw_exp32, h->flags, h->lw_ws.p,
+                  h->sw_ws.p, h->io.p};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return RRTMG_OK;
+}
+
+int rrtmg_gpu_set_precision(rrtmg_gpu_handle h, int precision) {
+  if (!valid_handle(h)) return RRTMG_ERR_ARG;
+  if (precision != RRTMG_PREC_FP64 && precision != RRTMG_PREC_SPLIT)
+    return fail(h, RRTMG_ERR_ARG, "precision must be RRTMG_PREC_FP64 or RRTMG_PREC_SPLIT");
+  h->precision = precision;
+  return RRTMG_OK;
+}
+
+int rrtmg_gpu_reserve(rrtmg_gpu_handle h, int ncol, int nlay) {
+  if (!valid_handle(h)) return RRTMG_ERR_ARG;
+  int rc = check_dims(h, ncol, nlay);
+  if (rc) return rc;
+  cudaSetDevice(h->device);
+  size_t a, b;
+  carve_lw(nullptr, ncol, nlay, &a);
+  carve_sw(nullptr, ncol, nlay, &b);
+  rc = ensure(h, h->lw_ws, a, nullptr);
+  if (rc) return rc;
+  return ensure(h, h->sw_ws, b, nullptr);
+}
+
+int rrtmg_gpu_sync_status(rrtmg_gpu_handle h, void* stream) {
+  if (!valid_handle(h)) return RRTMG_ERR_ARG;
+  return read_flags(h, (cudaStream_t)stream);
+}
+
+int rrtmg_lw_dev(rrtmg_gpu_handle h, void* stream, int ncol, int nlay, int icld, int idrv, const double* play,
+                 const double* plev, const double* tlay, const double* tlev, const double* tsfc, const double* h2ovmr,
+                 const double* o3vmr, const double* co2vmr, const double* ch4vmr, const double* n2ovmr,
+                 const double* o2vmr, const double* cfc11vmr, const double* cfc12vmr, const double* cfc22vmr,
+                 const double* ccl4vmr, const double* emis, int inflglw, int iceflglw, int liqflglw,
+                 const double* cldfr, const double* taucld, const double* cicewp, const double* cliqwp,
+                 const double* reice, const double* reliq, const double* tauaer, double* uflx, double* dflx,
+                 double* hr, double* uflxc, double* dflxc, double* hrc, double* duflx_dt, double* duflxc_dt) {
+  (void)inflglw; (void)iceflglw; (void)liqflglw; (void)cldfr; (void)taucld; (void)cicewp; (void)cliqwp;
+  (void)reice; (void)reliq;
+  if (!valid_handle(h)) return RRTMG_ERR_ARG;
+  int rc = check_dims(h, ncol, nlay);
+  if (rc) return rc;
+  if (icld != 0) return fail(h, RRTMG_ERR_UNSUPPORTED, "only clear sky (icld = 0) is computed");
+  if (idrv != 0 && idrv != 1) return fail(h, RRTMG_ERR_UNSUPPORTED, "idrv must be 0 or 1");
+  if (!play || !plev || !tlay || !tlev || !tsfc || !h2ovmr || !o3vmr || !co2vmr || !uflx || !dflx || !hr ||
+      !uflxc || !dflxc || !hrc)
+    return fail(h, RRTMG_ERR_ARG, "a required array pointer is null");
+  if (idrv == 1 && !duflx_dt) return fail(h, RRTMG_ERR_ARG, "idrv = 1 needs duflx_dt");
+  cudaSetDevice(h->device);
+  LwIn in{play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr, cfc11vmr, cfc12vmr,
+          cfc22vmr, ccl4vmr, emis, tauaer};
+  return lw_run(h, (cudaStream_t)stream, ncol, nlay, idrv, in, uflx, dflx, hr, uflxc, dflxc, hrc, duflx_dt,
+                duflxc_dt);
+}
+
+int rrtmg_sw_dev(rrtmg_gpu_handle h, void* stream, int ncol, int nlay, int icld, int iaer, const double* play,
+                 const double* plev, const double* tlay, const double* tlev, const double* tsfc, const double* h2ovmr,
+                 const double* o3vmr, const double* co2vmr, const double* ch4vmr, const double* n2ovmr,
+                 const double* o2vmr, const double* asdir, const double* asdif, const double* aldir,
+                 const double* aldif, const double* coszen, double adjes, int dyofyr, double scon, int inflgsw,
+                 int iceflgsw, int liqflgsw, const double* cldfr, const double* taucld, const double* ssacld,
+                 const double* asmcld, const double* fsfcld, const double* cicewp, const double* cliqwp,
+                 const double* reice, const double* reliq, const double* tauaer, const double* ssaaer,
+                 const double* asmaer, const double* ecaer, double* swuflx, double* swdflx, double* swhr,
+                 double* swuflxc, double* swdflxc, double* swhrc) {
+  (void)inflgsw; (void)iceflgsw; (void)liqflgsw; (void)cldfr; (void)taucld; (void)ssacld; (void)asmcld;
+  (void)fsfcld; (void)cicewp; (void)cliqwp; (void)reice; (void)reliq; (void)ecaer;
+  if (!valid_handle(h)) return RRTMG_ERR_ARG;
+  int rc = check_dims(h, ncol, nlay);
+  if (rc) return rc;
+  if (icld != 0) return fail(h, RRTMG_ERR_UNSUPPORTED, "only clear sky (icld = 0) is computed");
+  if (iaer != 0 && iaer != 10) return fail(h, RRTMG_ERR_UNSUPPORTED, "iaer must be 0 or 10");
+  if (!play || !plev || !tlay || !tlev || !tsfc || !h2ovmr || !o3vmr || !co2vmr || !asdir || !asdif || !aldir ||
+      !aldif || !coszen || !swuflx || !swdflx || !swhr || !swuflxc || !swdflxc || !swhrc)
+    return fail(h, RRTMG_ERR_ARG, "a required array pointer is null");
+  if (iaer == 10 && (!tauaer || !ssaaer || !asmaer)) return fail(h, RRTMG_ERR_ARG, "iaer = 10 needs tauaer/ssaaer/asmaer");
+  if (!(scon > 0.0)) return fail(h, RRTMG_ERR_ARG, "scon must be positive");
+  cudaSetDevice(h->device);
+  SwIn in{play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr, asdir, asdif, aldir, aldif,
+          coszen, tauaer, ssaaer, asmaer};
+  return sw_run(h, (cudaStream_t)stream, ncol, nlay, iaer, adjes, dyofyr, scon, in, swuflx, swdflx, swhr, swuflxc,
+                swdflxc, swhrc);
+}
+
+int rrtmg_lw_c(rrtmg_gpu_handle h, int ncol, int nlay, int icld, int idrv, const double* play, const double* plev,
+               const double* tlay, const double* tlev, const double* tsfc, const double* h2ovmr, const double* o3vmr,
+               const double* co2vmr, const double* ch4vmr, const double* n2ovmr, const double* o2vmr,
+               const double* cfc11vmr, const double* cfc12vmr, const double* cfc22vmr, const double* ccl4vmr,
+               const double* emis, int inflglw, int iceflglw, int liqflglw, const double* cldfr, const double* taucld,
+               const double* cicewp, const double* cliqwp, const double* reice, const double* reliq,
+               const double* tauaer, double* uflx, double* dflx, double* hr, double* uflxc, double* dflxc,
+               double* hrc, double* duflx_dt, double* duflxc_dt) {
+  if (!valid_handle(h)) return RRTMG_ERR_ARG;
+  int rc = check_dims(h, ncol, nlay);
+  if (rc) return rc;
+  if (icld != 0) return fail(h, RRTMG_ERR_UNSUPPORTED, "only clear sky (icld = 0) is computed");
+  if (idrv != 0 && idrv != 1) return fail(h, RRTMG_ERR_UNSUPPORTED, "idrv must be 0 or 1");
+  if (!play || !plev || !tlay || !tlev || !tsfc || !h2ovmr || !o3vmr || !co2vmr || !uflx || !dflx || !hr ||
+      !uflxc || !dflxc || !hrc)
+    return fail(h, RRTMG_ERR_ARG, "a required array pointer is null");
+  if (idrv == 1 && !duflx_dt) return fail(h, RRTMG_ERR_ARG, "idrv = 1 needs duflx_dt");
+  cudaSetDevice(h->device);
+  const size_t N = ncol, L = nlay, Lv = nlay + 1;
+  // size the staging area
+  Stage probe{h, h->stream, Carver{nullptr}};
+  auto plan = [&](Stage& st, const double** dp, double** out) {
+    dp[0] = st.in(play, L * N); dp[1] = st.in(plev, Lv * N); dp[2] = st.in(tlay, L * N); dp[3] = st.in(tlev, Lv * N);
+    dp[4] = st.in(tsfc, N); dp[5] = st.in(h2ovmr, L * N); dp[6] = st.in(o3vmr, L * N); dp[7] = st.in(co2vmr, L * N);
+    dp[8] = st.in(ch4vmr, L * N); dp[9] = st.in(n2ovmr, L * N); dp[10] = st.in(o2vmr, L * N);
+    dp[11] = st.in(cfc11vmr, L * N); dp[12] = st.in(cfc12vmr, L * N); dp[13] = st.in(cfc22vmr, L * N);
+    dp[14] = st.in(ccl4vmr, L * N); dp[15] = st.in(emis, 16 * N); dp[16] = st.in(tauaer, 16 * L * N);
+    out[0] = st.out(Lv * N); out[1] = st.out(Lv * N); out[2] = st.out(L * N); out[3] = st.out(Lv * N);
+    out[4] = st.out(Lv * N); out[5] = st.out(L * N);
+    out[6] = idrv == 1 ? st.out(Lv * N) : nullptr;
+    out[7] = idrv == 1 ? st.out(Lv * N) : nullptr;
+  };
+  const double* dp[17];
+  double* dout[8];
+  plan(probe, dp, dout);
+  rc = ensure(h, h->io, probe.c.off, h->stream);
+  if (rc) return rc;
+  Stage st{h, h->stream, Carver{(char*)h->io.p}};
+  plan(st, dp, dout);
+  if (st.err != cudaSuccess) return cuda_fail(h, st.err, "copy LW inputs");
+  LwIn in{dp[0], dp[1], dp[2], dp[3], dp[4], dp[5], dp[6], dp[7], dp[8], dp[9], dp[10], dp[11], dp[12], dp[13],
+          dp[14], dp[15], dp[16]};
+  rc = lw_run(h, h->stream, ncol, nlay, idrv, in, dout[0], dout[1], dout[2], dout[3], dout[4], dout[5], dout[6],
+              dout[7]);
+  if (rc) return rc;
+  double* hosts[8] = {uflx, dflx, hr, uflxc, dflxc, hrc, duflx_dt, duflxc_dt};
+  const size_t sizes[8] = {Lv * N, Lv * N, L * N, Lv * N, Lv * N, L * N, Lv * N, Lv * N};
+  for (int k = 0; k < 8; ++k) {
+    if (!hosts[k] || !dout[k]) continue;
+    cudaError_t e = cudaMemcpyAsync(hosts[k], dout[k], sizes[k] * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "copy LW outputs");
+  }
+  return read_flags(h, h->stream);
+}
+
+int rrtmg_sw_c(rrtmg_gpu_handle h, int ncol, int nlay, int icld, int iaer, const double* play, const double* plev,
+               const double* tlay, const double* tlev, const double* tsfc, const double* h2ovmr, const double* o3vmr,
+               const double* co2vmr, const double* ch4vmr, const double* n2ovmr, const double* o2vmr,
+               const double* asdir, const double* asdif, const double* aldir, const double* aldif,
+               const double* coszen, double adjes, int dyofyr, double scon, int inflgsw, int iceflgsw,
+               int liqflgsw, const double* cldfr, const double* taucld, const double* ssacld, const double* asmcld,
+               const double* fsfcld, const double* cicewp, const double* cliqwp, const double* reice,
+               const double* reliq, const double* tauaer, const double* ssaaer, const double* asmaer,
+               const double* ecaer, double* swuflx, double* swdflx, double* swhr, double* swuflxc, double* swdflxc,
+               double* swhrc) {
+  (void)inflgsw; (void)iceflgsw; (void)liqflgsw; (void)cldfr; (void)taucld; (void)ssacld; (void)asmcld;
+  (void)fsfcld; (void)cicewp; (void)cliqwp; (void)reice; (void)reliq; (void)ecaer;
+  if (!valid_handle(h)) return RRTMG_ERR_ARG;
+  int rc = check_dims(h, ncol, nlay);
+  if (rc) return rc;
+  if (icld != 0) return fail(h, RRTMG_ERR_UNSUPPORTED, "only clear sky (icld = 0) is computed");
+  if (iaer != 0 && iaer != 10) return fail(h, RRTMG_ERR_UNSUPPORTED, "iaer must be 0 or 10");
+  if (!play || !plev || !tlay || !tlev || !tsfc || !h2ovmr || !o3vmr || !co2vmr || !asdir || !asdif || !aldir ||
+      !aldif || !coszen || !swuflx || !swdflx || !swhr || !swuflxc || !swdflxc || !swhrc)
+    return fail(h, RRTMG_ERR_ARG, "a required array pointer is null");
+  if (iaer == 10 && (!tauaer || !ssaaer || !asmaer)) return fail(h, RRTMG_ERR_ARG, "iaer = 10 needs tauaer/ssaaer/asmaer");
+  if (!(scon > 0.0)) return fail(h, RRTMG_ERR_ARG, "scon must be positive");
+  cudaSetDevice(h->device);
+  const size_t N = ncol, L = nlay, Lv = nlay + 1;
+  const bool aer = iaer == 10;
+  auto plan = [&](Stage& st, const double** dp, double** out) {
+    dp[0] = st.in(play, L * N); dp[1] = st.in(plev, Lv * N); dp[2] = st.in(tlay, L * N); dp[3] = st.in(tlev, Lv * N);
+    dp[4] = st.in(tsfc, N); dp[5] = st.in(h2ovmr, L * N); dp[6] = st.in(o3vmr, L * N); dp[7] = st.in(co2vmr, L * N);
+    dp[8] = st.in(ch4vmr, L * N); dp[9] = st.in(n2ovmr, L * N); dp[10] = st.in(o2vmr, L * N);
+    dp[11] = st.in(asdir, N); dp[12] = st.in(asdif, N); dp[13] = st.in(aldir, N); dp[14] = st.in(aldif, N);
+    dp[15] = st.in(coszen, N);
+    dp[16] = aer ? st.in(tauaer, 14 * L * N) : nullptr;
+    dp[17] = aer ? st.in(ssaaer, 14 * L * N) : nullptr;
+    dp[18] = aer ? st.in(asmaer, 14 * L * N) : nullptr;
+    for (int k = 0; k < 6; ++k) out[k] = st.out((k == 2 || k == 5) ? L * N : Lv * N);
+  };
+  const double* dp[19];
+  double* dout[6];
+  Stage probe{h, h->stream, Carver{nullptr}};
+  plan(probe, dp, dout);
+  rc = ensure(h, h->io, probe.c.off, h->stream);
+  if (rc) return rc;
+  Stage st{h, h->stream, Carver{(char*)h->io.p}};
+  plan(st, dp, dout);
+  if (st.err != cudaSuccess) return cuda_fail(h, st.err, "copy SW inputs");
+  SwIn in{dp[0], dp[1], dp[2], dp[3], dp[4], dp[5], dp[6], dp[7], dp[8], dp[9], dp[10], dp[11], dp[12], dp[13], dp[14],
+          dp[15], dp[16], dp[17], dp[18]};
+  rc = sw_run(h, h->stream, ncol, nlay, iaer, adjes, dyofyr, scon, in, dout[0], dout[1], dout[2], dout[3], dout[4],
+              dout[5]);
+  if (rc) return rc;
+  double* hosts[6] = {swuflx, swdflx, swhr, swuflxc, swdflxc, swhrc};
+  for (int k = 0; k < 6; ++k) {
+    const size_t n = (k == 2 || k == 5) ? L * N : Lv * N;
+    cudaError_t e = cudaMemcpyAsync(hosts[k], dout[k], n * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "copy SW outputs");
+  }
+  return read_flags(h, h->stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,137 @@
+// Shared definitions of the GB300 RRTMG column-radiation kernels.
+//
+// Data layout in HBM (all column-fastest so that a warp of consecutive
+// columns, or of the g-points of one column, touches contiguous memory):
+//   * inputs/outputs: the caller's Fortran (ncol, nlev) arrays as is;
+//   * per-layer gas state from the prep kernels: field-major SoA
+//     [field][layer][column];
+//   * coefficient tables: one buffer per precision, every reduced table
+//     stored with the g-point index fastest, [..non-g indices..][g], so the
+//     lanes that hold the g-points of one column read one contiguous run;
+//   * band partial fluxes: [band][level][column] (FP64), summed over bands
+//     in a fixed order by the finalize kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace rrtmg {
+
+constexpr int kMaxLay = 203;
+constexpr int kLwBands = 16;
+constexpr int kLwG = 140;
+constexpr int kSwBands = 14;
+constexpr int kSwG = 112;
+constexpr int kBlock = 128;  // threads per block in the g-point kernels
+constexpr int kNTbl = 10000;
+
+// Table roles (slots in BandDesc::off).  LW: key-species tables, continua,
+// Planck fractions, up to three lower / two upper minor-gas tables and two
+// cross-section tables.  SW: key species, continua, solar source, Rayleigh and
+// four band-specific extras.
+enum LwRole { LW_KA = 0, LW_KB, LW_SELF, LW_FOR, LW_FRA, LW_FRB, LW_MA1, LW_MA2, LW_MA3, LW_MB1, LW_MB2,
+              LW_X1, LW_X2, LW_NROLE };
+enum SwRole { SW_KA = 0, SW_KB, SW_SELF, SW_FOR, SW_SFLUX, SW_RAYL, SW_E1, SW_E2, SW_E3, SW_E4, SW_NROLE };
+
+struct BandDesc {
+  int ng;      // reduced g-points of the band
+  int ngpad;   // lanes per column: power of two >= ng
+  int goff;    // first g-point of the band in the 140 / 112 ordering
+  int nspa, nspb;
+  int off[16];     // element offset of each role's table, -1 if the band has none
+  int nrow[16];    // extent of the first non-g index of 2-/3-d tables (row stride helper)
+  double delwave;
+};
+
+// LW per-layer fields written by the prep kernel ([field][layer][column]).
+enum LwField {
+  LF_PAVEL = 0, LF_COLDRY, LF_COLH2O, LF_COLCO2, LF_COLO3, LF_COLN2O, LF_COLCO, LF_COLCH4, LF_COLO2,
+  LF_COLBRD, LF_FAC00, LF_FAC01, LF_FAC10, LF_FAC11, LF_SELFFAC, LF_SELFFRAC, LF_FORFAC, LF_FORFRAC,
+  LF_MINORFRAC, LF_SCALEMINOR, LF_SCALEMINORN2, LF_WX1, LF_WX2, LF_WX3, LF_WX4, LF_N
+};
+enum SwField {
+  SF_COLH2O = 0, SF_COLCO2, SF_COLO3, SF_COLCH4, SF_COLO2, SF_COLMOL, SF_FAC00, SF_FAC01, SF_FAC10,
+  SF_FAC11, SF_SELFFAC, SF_SELFFRAC, SF_FORFAC, SF_FORFRAC, SF_N
+};
+
+// Packed integer interpolation indices of one layer.
+__host__ __device__ inline uint32_t pack_idx(int jp, int jt, int jt1, int inds, int indf, int indm) {
+  return (uint32_t)jp | ((uint32_t)jt << 6) | ((uint32_t)jt1 << 9) | ((uint32_t)inds << 12) |
+         ((uint32_t)indf << 16) | ((uint32_t)indm << 18);
+}
+struct Idx {
+  int jp, jt, jt1, inds, indf, indm;
+};
+__host__ __device__ inline Idx unpack_idx(uint32_t v) {
+  Idx i;
+  i.jp = (int)(v & 63u);
+  i.jt = (int)((v >> 6) & 7u);
+  i.jt1 = (int)((v >> 9) & 7u);
+  i.inds = (int)((v >> 12) & 15u);
+  i.indf = (int)((v >> 16) & 3u);
+  i.indm = (int)((v >> 18) & 31u);
+  return i;
+}
+
+// Constants of the LW path (constant memory in every kernel translation unit).
+struct LwConst {
+  BandDesc band[kLwBands];
+  double chi[7 * 60];      // chi_mls(i, jp) at [(jp-1)*7 + (i-1)], jp = 1..59 (+ pad)
+  double preflog[60], tref[60];
+  // chi_mls ratios per reference level, identical to setcoef's per-layer
+  // divisions (rrtmg_lw_setcoef.f90:323-336, 370-374)
+  double r_h2oco2[61], r_h2oo3[61], r_h2on2o[61], r_h2och4[61], r_n2oco2[61], r_o3co2[61];
+  double refrat[kLwBands][4];  // band constants refrat_planck_a/b, refrat_m_a/b (or m_a3)
+  double heatfac, fluxfac, oneminus, bpade, grav, avogad;
+};
+
+struct SwConst {
+  BandDesc band[kSwBands];
+  double preflog[60], tref[60];
+  double heatfac, oneminus, bpade, grav, avogad, pi;
+};
+
+// Per-call view of the LW prep output.
+struct LwPrep {
+  const uint32_t* idx;     // [lay][col]
+  const double* f;         // [LF_N][lay][col]
+  const double* planklay;  // [band][lay][col]
+  const double* planklev;  // [band][lev 0..nlay][col]
+  const double* plankbnd;  // [band][col]
+  const double* dplankbnd; // [band][col]
+  const double* secdiff;   // [band][col]
+  const int* laytrop;      // [col]
+};
+
+struct SwPrep {
+  const uint32_t* idx;     // [lay][col]
+  const double* f;         // [SF_N][lay][col]
+  const int* laytrop;      // [col]
+  const int* laysolfr;     // [band][col], 0 = no solar-source layer
+};
+
+// ---------------------------------------------------------------------------
+// Device pointers of one call (inputs as passed by the caller) and of its
+// scratch workspace.
+// ---------------------------------------------------------------------------
+struct LwIn {
+  const double *play, *plev, *tlay, *tlev, *tsfc, *h2o, *o3, *co2, *ch4, *n2o, *o2, *cfc11, *cfc12, *cfc22, *ccl4,
+      *emis, *tauaer;
+};
+struct LwWork {
+  uint32_t* idx;
+  double *f, *planklay, *planklev, *plankbnd, *dplankbnd, *secdiff;
+  int* laytrop;
+  double *bu, *bd, *bdu;  // band partials [band][lev][col]
+};
+struct SwIn {
+  const double *play, *plev, *tlay, *tlev, *tsfc, *h2o, *o3, *co2, *ch4, *n2o, *o2, *asdir, *asdif, *aldir, *aldif,
+      *coszen, *tauaer, *ssaaer, *asmaer;
+};
+struct SwWork {
+  uint32_t* idx;
+  double* f;
+  int *laytrop, *laysolfr;
+  double *su, *sd;  // band partials [band][lev][col]
+};
+
+}  // namespace rrtmg

@@ -1,0 +1,824 @@
+// RRTMG clear-sky LW/SW column-radiation kernels for sm_103a.
+//
+// Work decomposition (per radiation call, LW and SW alike):
+//   1. prep    one thread per column: inatm + setcoef (FP64).  Writes the
+//              per-layer gas state SoA, Planck terms (LW) and solar-source
+//              layers (SW).
+//   2. gpoint  one thread per (column, g-point).  A warp holds the g-points
+//              of a single band for 32/ngpad columns (ngpad = next power of
+//              two >= the band's g count), so every warp runs one band's
+//              straight-line gas-optics code and its table loads for one
+//              column are contiguous.  Each thread evaluates taumol for its
+//              g-point layer by layer and runs that g-point's vertical
+//              recursions in registers/local memory; at every level the
+//              g-point contributions of a column are summed with warp
+//              shuffles (FP64) and one lane stores the band partial.
+//   3. finalize one thread per column: band partials summed in band order
+//              (FP64), flux outputs, heating-rate differencing (FP64).
+// The column kernels (prep, finalize) are FP64 in both paths and are defined
+// only in the translation unit that defines RRTMG_DEFINE_COLUMN_KERNELS.
+// Real = double gives the FP64 path; Real = float gives the FP32-split path
+// (gas optics, transmittances, recursions in FP32; g-point sums, band sums and
+// heating-rate differences in FP64).
+#pragma once
+#include <math.h>
+
+#include "sw_optics.cuh"
+
+namespace rrtmg {
+
+// Constant memory: one copy per translation unit, filled by upload_constants().
+static __constant__ LwConst c_lw;
+static __constant__ SwConst c_sw;
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+template <int W>
+__device__ __forceinline__ double seg_sum(double v) {
+#pragma unroll
+  for (int o = W / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ bool bad(double x) { return !isfinite(x); }
+
+#ifdef RRTMG_DEFINE_COLUMN_KERNELS
+// ---------------------------------------------------------------------------
+// LW prep: inatm (rrtmg_lw_rad.nomcica.f90:572-901) + setcoef
+// (rrtmg_lw_setcoef.f90:31-415) + secdiff (rrtmg_lw_rtrnmr.f90:271-279).
+// totplnk / totplnkderiv: device tables [(ind-1) + 181*(band-1)].
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) lw_prep_kernel(LwIn in, LwWork w, const double* __restrict__ totplnk,
+                                                      const double* __restrict__ totplnkderiv, int ncol, int nlay,
+                                                      int idrv, unsigned* __restrict__ flags) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncol) return;
+  const LwConst& C = c_lw;
+  const double amd = 28.9660, amw = 18.0160, amdw = 1.607793, amdo = 0.603428;
+  const double stpfac = 296. / 1013.;
+  const size_t N = (size_t)ncol;
+  const size_t fstride = (size_t)nlay * N;
+  auto A = [&](const double* p, int l) { return __ldg(p + (size_t)col + N * (size_t)(l - 1)); };
+  auto P = [&](int ind, int b) { return __ldg(totplnk + (ind - 1) + 181 * (b - 1)); };
+  auto PD = [&](int ind, int b) { return __ldg(totplnkderiv + (ind - 1) + 181 * (b - 1)); };
+  unsigned flag = 0;
+
+  const double tbound = __ldg(in.tsfc + col);
+  double pz_prev = A(in.plev, 1);
+  const double pz0 = pz_prev;
+  const double tz0 = A(in.tlev, 1);
+  if (bad(tbound) || bad(pz_prev) || bad(tz0) || tbound <= 0. || tz0 <= 0.) flag = 1;
+  const int indbound = clampi((int)(tbound - 159.), 1, 180);
+  const double tbndfrac = tbound - 159. - (double)indbound;
+  const int indlev0 = clampi((int)(tz0 - 159.), 1, 180);
+  const double t0frac = tz0 - 159. - (double)indlev0;
+  for (int b = 1; b <= 16; ++b) {
+    double semiss = in.emis ? __ldg(in.emis + col + N * (b - 1)) : 1.0;
+    double dbdtlev = P(indbound + 1, b) - P(indbound, b);
+    w.plankbnd[(b - 1) * N + col] = semiss * (P(indbound, b) + tbndfrac * dbdtlev);
+    dbdtlev = P(indlev0 + 1, b) - P(indlev0, b);
+    w.planklev[((size_t)(b - 1) * (nlay + 1)) * N + col] = P(indlev0, b) + t0frac * dbdtlev;
+    if (idrv == 1) {
+      dbdtlev = PD(indbound + 1, b) - PD(indbound, b);
+      w.dplankbnd[(b - 1) * N + col] = semiss * (PD(indbound, b) + tbndfrac * dbdtlev);
+    }
+  }
+
+  double amttl = 0.0, wvttl = 0.0;
+  int laytrop = 0;
+  for (int l = 1; l <= nlay; ++l) {
+    const double pavel = A(in.play, l), tavel = A(in.tlay, l);
+    const double pz_l = A(in.plev, l + 1), tz_l = A(in.tlev, l + 1);
+    const double h2o = A(in.h2o, l);
+    if (bad(pavel) || bad(tavel) || bad(pz_l) || bad(tz_l) || bad(h2o) || pavel <= 0. || tavel <= 0. ||
+        h2o < 0. || h2o >= 1. || pz_l < 0.)
+      flag = 1;
+    double wk1 = (h2o / (1. - h2o)) * amdw;
+    double wk2 = A(in.co2, l);
+    double wk3 = A(in.o3, l) * amdo;
+    double wk4 = in.n2o ? A(in.n2o, l) : 0.0;
+    double wk6 = in.ch4 ? A(in.ch4, l) : 0.0;
+    double wk7 = in.o2 ? A(in.o2, l) : 0.0;
+    double amm = (1. - wk1) * amd + wk1 * amw;
+    double coldry = (pz_prev - pz_l) * 1.e3 * C.avogad / (1.e2 * C.grav * amm * (1. + wk1));
+    double summol = 0.0;
+    summol = summol + wk2;
+    summol = summol + wk3;
+    summol = summol + wk4;
+    summol = summol + 0.0;
+    summol = summol + wk6;
+    summol = summol + wk7;
+    double wbrodl = coldry * (1. - summol);
+    wk1 = coldry * wk1;
+    wk2 = coldry * wk2;
+    wk3 = coldry * wk3;
+    wk4 = coldry * wk4;
+    double wk5 = coldry * 0.0;
+    wk6 = coldry * wk6;
+    wk7 = coldry * wk7;
+    amttl = amttl + coldry + wk1;
+    wvttl = wvttl + wk1;
+    double wx1 = in.ccl4 ? coldry * A(in.ccl4, l) * 1.e-20 : coldry * 0.0 * 1.e-20;
+    double wx2 = in.cfc11 ? coldry * A(in.cfc11, l) * 1.e-20 : coldry * 0.0 * 1.e-20;
+    double wx3 = in.cfc12 ? coldry * A(in.cfc12, l) * 1.e-20 : coldry * 0.0 * 1.e-20;
+    double wx4 = in.cfc22 ? coldry * A(in.cfc22, l) * 1.e-20 : coldry * 0.0 * 1.e-20;
+
+    // Planck functions of the layer and its upper interface
+    const int indlay = clampi((int)(tavel - 159.), 1, 180);
+    const double tlayfrac = tavel - 159. - (double)indlay;
+    const int indlev = clampi((int)(tz_l - 159.), 1, 180);
+    const double tlevfrac = tz_l - 159. - (double)indlev;
+    for (int b = 1; b <= 16; ++b) {
+      double dbdtlev = P(indlev + 1, b) - P(indlev, b);
+      double dbdtlay = P(indlay + 1, b) - P(indlay, b);
+      w.planklay[((size_t)(b - 1) * nlay + (l - 1)) * N + col] = P(indlay, b) + tlayfrac * dbdtlay;
+      w.planklev[((size_t)(b - 1) * (nlay + 1) + l) * N + col] = P(indlev, b) + tlevfrac * dbdtlev;
+    }
+
+    const double plog = log(pavel);
+    const int jp = clampi((int)(36. - 5 * (plog + 0.04)), 1, 58);
+    const int jp1 = jp + 1;
+    const double fp = 5. * (C.preflog[jp - 1] - plog);
+    const int jt = clampi((int)(3. + (tavel - C.tref[jp - 1]) / 15.), 1, 4);
+    const double ft = ((tavel - C.tref[jp - 1]) / 15.) - (double)(jt - 3);
+    const int jt1 = clampi((int)(3. + (tavel - C.tref[jp1 - 1]) / 15.), 1, 4);
+    const double ft1 = ((tavel - C.tref[jp1 - 1]) / 15.) - (double)(jt1 - 3);
+    const double water = wk1 / coldry;
+    const double scalefac = pavel * stpfac / tavel;
+    double forfac, forfrac, selffac, selffrac = 0.0, minorfrac, factor;
+    int indfor, indself = 1, indminor;
+    if (plog > 4.56) {
+      laytrop = laytrop + 1;
+      forfac = scalefac / (1. + water);
+      factor = (332.0 - tavel) / 36.0;
+      indfor = min(2, max(1, (int)factor));
+      forfrac = factor - (double)indfor;
+      selffac = water * forfac;
+      factor = (tavel - 188.0) / 7.2;
+      indself = min(9, max(1, (int)factor - 7));
+      selffrac = factor - (double)(indself + 7);
+    } else {
+      forfac = scalefac / (1. + water);
+      factor = (tavel - 188.0) / 36.0;
+      indfor = 3;
+      forfrac = factor - 1.0;
+      selffac = water * forfac;
+    }
+    const double scaleminor = pavel / tavel;
+    const double scaleminorn2 = (pavel / tavel) * (wbrodl / (coldry + wk1));
+    factor = (tavel - 180.8) / 7.2;
+    indminor = min(18, max(1, (int)factor));
+    minorfrac = factor - (double)indminor;
+
+    double colh2o = 1.e-20 * wk1, colco2 = 1.e-20 * wk2, colo3 = 1.e-20 * wk3, coln2o = 1.e-20 * wk4;
+    double colco = 1.e-20 * wk5, colch4 = 1.e-20 * wk6, colo2 = 1.e-20 * wk7;
+    if (colco2 == 0.) colco2 = 1.e-32 * coldry;
+    if (colo3 == 0.) colo3 = 1.e-32 * coldry;
+    if (coln2o == 0.) coln2o = 1.e-32 * coldry;
+    if (colco == 0.) colco = 1.e-32 * coldry;
+    if (colch4 == 0.) colch4 = 1.e-32 * coldry;
+    const double colbrd = 1.e-20 * wbrodl;
+    const double compfp = 1. - fp;
+    const size_t o = (size_t)(l - 1) * N + col;
+    double* f = w.f;
+    f[LF_PAVEL * fstride + o] = pavel;
+    f[LF_COLDRY * fstride + o] = coldry;
+    f[LF_COLH2O * fstride + o] = colh2o;
+    f[LF_COLCO2 * fstride + o] = colco2;
+    f[LF_COLO3 * fstride + o] = colo3;
+    f[LF_COLN2O * fstride + o] = coln2o;
+    f[LF_COLCO * fstride + o] = colco;
+    f[LF_COLCH4 * fstride + o] = colch4;
+    f[LF_COLO2 * fstride + o] = colo2;
+    f[LF_COLBRD * fstride + o] = colbrd;
+    f[LF_FAC10 * fstride + o] = compfp * ft;
+    f[LF_FAC00 * fstride + o] = compfp * (1. - ft);
+    f[LF_FAC11 * fstride + o] = fp * ft1;
+    f[LF_FAC01 * fstride + o] = fp * (1. - ft1);
+    f[LF_SELFFAC * fstride + o] = colh2o * selffac;
+    f[LF_SELFFRAC * fstride + o] = selffrac;
+    f[LF_FORFAC * fstride + o] = colh2o * forfac;
+    f[LF_FORFRAC * fstride + o] = forfrac;
+    f[LF_MINORFRAC * fstride + o] = minorfrac;
+    f[LF_SCALEMINOR * fstride + o] = scaleminor;
+    f[LF_SCALEMINORN2 * fstride + o] = scaleminorn2;
+    f[LF_WX1 * fstride + o] = wx1;
+    f[LF_WX2 * fstride + o] = wx2;
+    f[LF_WX3 * fstride + o] = wx3;
+    f[LF_WX4 * fstride + o] = wx4;
+    w.idx[o] = pack_idx(jp, jt, jt1, indself, indfor, indminor);
+    pz_prev = pz_l;
+  }
+  w.laytrop[col] = laytrop;
+  const double wvsh = (amw * wvttl) / (amd * amttl);
+  const double pwvcm = wvsh * (1.e3 * pz0) / (1.e2 * C.grav);
+  const double a0[16] = {1.66, 1.55, 1.58, 1.66, 1.54, 1.454, 1.89, 1.33, 1.668, 1.66, 1.66, 1.66, 1.66, 1.66, 1.66, 1.66};
+  const double a1[16] = {0.00, 0.25, 0.22, 0.00, 0.13, 0.446, -0.10, 0.40, -0.006, 0, 0, 0, 0, 0, 0, 0};
+  const double a2[16] = {0.00, -12.0, -11.7, 0.00, -0.72, -0.243, 0.19, -0.062, 0.414, 0, 0, 0, 0, 0, 0, 0};
+  for (int b = 1; b <= 16; ++b) {
+    double s;
+    if (b == 1 || b == 4 || b >= 10) {
+      s = 1.66;
+    } else {
+      s = a0[b - 1] + a1[b - 1] * exp(a2[b - 1] * pwvcm);
+      if (s > 1.80) s = 1.80;
+      if (s < 1.50) s = 1.50;
+    }
+    w.secdiff[(b - 1) * N + col] = s;
+  }
+  if (flag) atomicOr(flags, 1u);
+}
+
+#endif  // RRTMG_DEFINE_COLUMN_KERNELS
+
+// ---------------------------------------------------------------------------
+// LW g-point solver: taumol + rtrnmr clear-sky branch
+// (rrtmg_lw_rtrnmr.f90:505-616 downward, :628-713 upward) for one g-point.
+// ---------------------------------------------------------------------------
+template <int B, class R, int MAXL>
+__device__ __forceinline__ void lw_band(const LwPrep& p, const double* __restrict__ emis,
+                                        const double* __restrict__ tauaer, const R* __restrict__ tab,
+                                        const R* __restrict__ exptbl, const R* __restrict__ tfntbl,
+                                        double* __restrict__ bu, double* __restrict__ bd, double* __restrict__ bdu,
+                                        int ncol, int nlay, int idrv, int blk) {
+  const bool IDRV = idrv == 1;
+  constexpr int NG = lw_ng(B);
+  constexpr int W = pow2ceil(NG);
+  constexpr int CPB = kBlock / W;
+  const int lane_col = threadIdx.x / W, g = threadIdx.x % W;
+  const int col = blk * CPB + lane_col;
+  const bool valid = col < ncol;
+  const bool active = valid && g < NG;
+  const int c = valid ? col : ncol - 1;
+  const int gg = g < NG ? g : NG - 1;
+  const size_t N = (size_t)ncol;
+  const int lt = p.laytrop[c];
+  const R secdiff = (R)p.secdiff[(B - 1) * N + c];
+  const R bpade = (R)c_lw.bpade;
+  const R rec_6 = (R)0.166667;
+  const size_t fstride = (size_t)nlay * N;
+  R atrans[MAXL], bbugas[MAXL];
+  R radld = (R)0., fracs1 = (R)0.;
+  double* bdp = bd + (size_t)(B - 1) * (nlay + 1) * N + col;
+  double* bup = bu + (size_t)(B - 1) * (nlay + 1) * N + col;
+  for (int lev = nlay; lev >= 1; --lev) {
+    const size_t o = (size_t)(lev - 1) * N + c;
+    const Idx ix = unpack_idx(__ldg(p.idx + o));
+    LwLayerView<R> L{p.f, fstride, o};
+    R taug, fracs;
+    lw_gas<B, R>(c_lw, L, ix, lev <= lt, gg, tab, taug, fracs);
+    R taut = taug;
+    if (tauaer) taut = taug + (R)__ldg(tauaer + c + N * ((size_t)(lev - 1) + (size_t)nlay * (B - 1)));
+    const R plfrac = fracs;
+    const R blay = (R)__ldg(p.planklay + ((size_t)(B - 1) * nlay + (lev - 1)) * N + c);
+    const R dplankup = (R)__ldg(p.planklev + ((size_t)(B - 1) * (nlay + 1) + lev) * N + c) - blay;
+    const R dplankdn = (R)__ldg(p.planklev + ((size_t)(B - 1) * (nlay + 1) + lev - 1) * N + c) - blay;
+    R odepth = secdiff * taut;
+    if (odepth < (R)0.0) odepth = (R)0.0;
+    R atr, bbd, bbu;
+    if (odepth <= (R)0.06) {
+      atr = odepth - (R)0.5 * odepth * odepth;
+      odepth = rec_6 * odepth;
+      bbd = plfrac * (blay + dplankdn * odepth);
+      bbu = plfrac * (blay + dplankup * odepth);
+    } else {
+      const R tblind = odepth / (bpade + odepth);
+      const int itr = (int)((R)10000.0 * tblind + (R)0.5);
+      const R transc = __ldg(exptbl + itr);
+      atr = (R)1. - transc;
+      const R tausfac = __ldg(tfntbl + itr);
+      bbd = plfrac * (blay + tausfac * dplankdn);
+      bbu = plfrac * (blay + tausfac * dplankup);
+    }
+    atrans[lev - 1] = atr;
+    bbugas[lev - 1] = bbu;
+    radld = radld + (bbd - radld) * atr;
+    const double s = seg_sum<W>(active ? (double)radld : 0.0);
+    if (g == 0 && valid) bdp[(size_t)(lev - 1) * N] = s;
+    if (lev == 1) fracs1 = fracs;
+  }
+  const R semiss = emis ? (R)__ldg(emis + c + N * (B - 1)) : (R)1.0;
+  const R rad0 = fracs1 * (R)__ldg(p.plankbnd + (B - 1) * N + c);
+  const R reflect = (R)1. - semiss;
+  R radlu = rad0 + reflect * radld;
+  double s = seg_sum<W>(active ? (double)radlu : 0.0);
+  if (g == 0 && valid) bup[0] = s;
+  R dlu = (R)0.;
+  double* bdup = nullptr;
+  if (IDRV) {
+    bdup = bdu + (size_t)(B - 1) * (nlay + 1) * N + col;
+    dlu = fracs1 * (R)__ldg(p.dplankbnd + (B - 1) * N + c);
+    s = seg_sum<W>(active ? (double)dlu : 0.0);
+    if (g == 0 && valid) bdup[0] = s;
+  }
+  for (int lev = 1; lev <= nlay; ++lev) {
+    radlu = radlu + (bbugas[lev - 1] - radlu) * atrans[lev - 1];
+    s = seg_sum<W>(active ? (double)radlu : 0.0);
+    if (g == 0 && valid) bup[(size_t)lev * N] = s;
+    if (IDRV) {
+      dlu = dlu * ((R)1.0 - atrans[lev - 1]);
+      s = seg_sum<W>(active ? (double)dlu : 0.0);
+      if (g == 0 && valid) bdup[(size_t)lev * N] = s;
+    }
+  }
+}
+
+__host__ __device__ inline int lw_blocks_for_band(int ngpad, int ncol) {
+  const int cpb = kBlock / ngpad;
+  return (ncol + cpb - 1) / cpb;
+}
+
+template <class R, int MAXL>
+__global__ void __launch_bounds__(kBlock) lw_gpoint_kernel(LwPrep p, const double* __restrict__ emis,
+                                                           const double* __restrict__ tauaer,
+                                                           const R* __restrict__ tab, const R* __restrict__ exptbl,
+                                                           const R* __restrict__ tfntbl, double* bu, double* bd,
+                                                           double* bdu, int ncol, int nlay, int idrv) {
+  int blk = blockIdx.x, band = 0;
+  for (; band < kLwBands; ++band) {
+    const int nb = lw_blocks_for_band(c_lw.band[band].ngpad, ncol);
+    if (blk < nb) break;
+    blk -= nb;
+  }
+#define RRTMG_LW_CASE(b) \
+  case b - 1: lw_band<b, R, MAXL>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv, blk); break;
+  switch (band) {
+    RRTMG_LW_CASE(1) RRTMG_LW_CASE(2) RRTMG_LW_CASE(3) RRTMG_LW_CASE(4) RRTMG_LW_CASE(5) RRTMG_LW_CASE(6)
+    RRTMG_LW_CASE(7) RRTMG_LW_CASE(8) RRTMG_LW_CASE(9) RRTMG_LW_CASE(10) RRTMG_LW_CASE(11) RRTMG_LW_CASE(12)
+    RRTMG_LW_CASE(13) RRTMG_LW_CASE(14) RRTMG_LW_CASE(15) RRTMG_LW_CASE(16)
+    default: break;
+  }
+#undef RRTMG_LW_CASE
+}
+
+#ifdef RRTMG_DEFINE_COLUMN_KERNELS
+// ---------------------------------------------------------------------------
+// LW finalize: band sums (rrtmg_lw_rtrnmr.f90:720-746), fluxes and heating
+// (:752-776); clear-sky outputs equal the total ones in clear sky.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) lw_finalize_kernel(const double* __restrict__ bu, const double* __restrict__ bd,
+                                                          const double* __restrict__ bdu,
+                                                          const double* __restrict__ plev, int ncol, int nlay,
+                                                          int idrv, double* uflx, double* dflx, double* hr,
+                                                          double* uflxc, double* dflxc, double* hrc,
+                                                          double* duflx_dt, double* duflxc_dt) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncol) return;
+  const LwConst& C = c_lw;
+  const size_t N = (size_t)ncol;
+  const double wtdiff = 0.5;
+  double fnet_prev = 0.0, pz_prev = 0.0;
+  for (int lev = 0; lev <= nlay; ++lev) {
+    double tu = 0.0, td = 0.0, tdu = 0.0;
+    for (int b = 0; b < kLwBands; ++b) {
+      const size_t o = ((size_t)b * (nlay + 1) + lev) * N + col;
+      tu = tu + (__ldg(bu + o) * wtdiff) * C.band[b].delwave;
+      td = td + (__ldg(bd + o) * wtdiff) * C.band[b].delwave;
+      if (idrv == 1) tdu = tdu + (__ldg(bdu + o) * wtdiff) * C.band[b].delwave * C.fluxfac;
+    }
+    tu = tu * C.fluxfac;
+    td = td * C.fluxfac;
+    const size_t oo = (size_t)lev * N + col;
+    uflx[oo] = tu;
+    dflx[oo] = td;
+    uflxc[oo] = tu;
+    dflxc[oo] = td;
+    if (idrv == 1) {
+      if (duflx_dt) duflx_dt[oo] = tdu;
+      if (duflxc_dt) duflxc_dt[oo] = tdu;
+    }
+    const double fnet = tu - td;
+    const double pz = __ldg(plev + oo);
+    if (lev >= 1) {
+      const double h = C.heatfac * (fnet_prev - fnet) / (pz_prev - pz);
+      const size_t oh = (size_t)(lev - 1) * N + col;
+      hr[oh] = h;
+      hrc[oh] = h;
+    }
+    fnet_prev = fnet;
+    pz_prev = pz;
+  }
+}
+
+#endif  // RRTMG_DEFINE_COLUMN_KERNELS
+
+// ---------------------------------------------------------------------------
+// SW prep: inatm_sw (rrtmg_sw_rad.nomcica.f90:761-1101) + setcoef_sw
+// (rrtmg_sw_setcoef.f90:30-286) + the solar-source layer of every band
+// (laysolfr logic of taumol16..29).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int sw_layreffr(int b) {
+  switch (b) {
+    case 16: return 18; case 17: return 30; case 18: return 6; case 19: return 3; case 20: return 3;
+    case 21: return 8; case 22: return 2; case 23: return 6; case 24: return 1; case 25: return 2;
+    case 27: return 32; case 28: return 58; case 29: return 49; default: return 0;
+  }
+}
+// Bands whose solar source is taken in the upper-atmosphere loop.
+__host__ __device__ constexpr bool sw_upper_source(int b) { return b == 16 || b == 17 || b == 27 || b == 28 || b == 29; }
+
+#ifdef RRTMG_DEFINE_COLUMN_KERNELS
+__global__ void __launch_bounds__(128) sw_prep_kernel(SwIn in, SwWork w, int ncol, int nlay,
+                                                      unsigned* __restrict__ flags) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncol) return;
+  const SwConst& C = c_sw;
+  const double amd = 28.9660, amw = 18.0160, amdw = 1.607793, amdo = 0.603428;
+  const double stpfac = 296. / 1013.;
+  const size_t N = (size_t)ncol;
+  const size_t fstride = (size_t)nlay * N;
+  auto A = [&](const double* p, int l) { return __ldg(p + (size_t)col + N * (size_t)(l - 1)); };
+  unsigned flag = 0;
+  double pz_prev = A(in.plev, 1);
+  int laytrop = 0;
+  if (bad(__ldg(in.coszen + col))) flag = 1;
+  for (int l = 1; l <= nlay; ++l) {
+    const double pavel = A(in.play, l), tavel = A(in.tlay, l);
+    const double pz_l = A(in.plev, l + 1);
+    const double h2o = A(in.h2o, l);
+    if (bad(pavel) || bad(tavel) || bad(pz_l) || bad(h2o) || pavel <= 0. || tavel <= 0. || h2o < 0. || h2o >= 1. ||
+        pz_l < 0.)
+      flag = 1;
+    double wk1 = (h2o / (1. - h2o)) * amdw;
+    double wk2 = A(in.co2, l);
+    double wk3 = A(in.o3, l) * amdo;
+    double wk4 = in.n2o ? A(in.n2o, l) : 0.0;
+    double wk6 = in.ch4 ? A(in.ch4, l) : 0.0;
+    double wk7 = in.o2 ? A(in.o2, l) : 0.0;
+    double amm = (1. - wk1) * amd + wk1 * amw;
+    double coldry = (pz_prev - pz_l) * 1.e3 * C.avogad / (1.e2 * C.grav * amm * (1. + wk1));
+    wk1 = coldry * wk1;
+    wk2 = coldry * wk2;
+    wk3 = coldry * wk3;
+    wk4 = coldry * wk4;
+    wk6 = coldry * wk6;
+    wk7 = coldry * wk7;
+
+    const double plog = log(pavel);
+    const int jp = clampi((int)(36. - 5 * (plog + 0.04)), 1, 58);
+    const int jp1 = jp + 1;
+    const double fp = 5. * (C.preflog[jp - 1] - plog);
+    const int jt = clampi((int)(3. + (tavel - C.tref[jp - 1]) / 15.), 1, 4);
+    const double ft = ((tavel - C.tref[jp - 1]) / 15.) - (double)(jt - 3);
+    const int jt1 = clampi((int)(3. + (tavel - C.tref[jp1 - 1]) / 15.), 1, 4);
+    const double ft1 = ((tavel - C.tref[jp1 - 1]) / 15.) - (double)(jt1 - 3);
+    const double water = wk1 / coldry;
+    const double scalefac = pavel * stpfac / tavel;
+    double forfac, forfrac, selffac, selffrac, factor;
+    int indfor, indself;
+    const bool lower = plog > 4.56;
+    if (lower) {
+      laytrop = laytrop + 1;
+      forfac = scalefac / (1. + water);
+      factor = (332.0 - tavel) / 36.0;
+      indfor = min(2, max(1, (int)factor));
+      forfrac = factor - (double)indfor;
+      selffac = water * forfac;
+      factor = (tavel - 188.0) / 7.2;
+      indself = min(9, max(1, (int)factor - 7));
+      selffrac = factor - (double)(indself + 7);
+    } else {
+      forfac = scalefac / (1. + water);
+      factor = (tavel - 188.0) / 36.0;
+      indfor = 3;
+      forfrac = factor - 1.0;
+      selffac = 0.;
+      selffrac = 0.;
+      indself = 0;
+    }
+    double colh2o = 1.e-20 * wk1, colco2 = 1.e-20 * wk2, colo3 = 1.e-20 * wk3, coln2o = 1.e-20 * wk4;
+    double colch4 = 1.e-20 * wk6, colo2 = 1.e-20 * wk7;
+    const double colmol = 1.e-20 * coldry + colh2o;
+    if (colco2 == 0.) colco2 = 1.e-32 * coldry;
+    if (coln2o == 0.) coln2o = 1.e-32 * coldry;
+    if (colch4 == 0.) colch4 = 1.e-32 * coldry;
+    if (colo2 == 0.) colo2 = 1.e-32 * coldry;
+    const double compfp = 1. - fp;
+    const size_t o = (size_t)(l - 1) * N + col;
+    double* f = w.f;
+    f[SF_COLH2O * fstride + o] = colh2o;
+    f[SF_COLCO2 * fstride + o] = colco2;
+    f[SF_COLO3 * fstride + o] = colo3;
+    f[SF_COLCH4 * fstride + o] = colch4;
+    f[SF_COLO2 * fstride + o] = colo2;
+    f[SF_COLMOL * fstride + o] = colmol;
+    f[SF_FAC10 * fstride + o] = compfp * ft;
+    f[SF_FAC00 * fstride + o] = compfp * (1. - ft);
+    f[SF_FAC11 * fstride + o] = fp * ft1;
+    f[SF_FAC01 * fstride + o] = fp * (1. - ft1);
+    f[SF_SELFFAC * fstride + o] = selffac;
+    f[SF_SELFFRAC * fstride + o] = selffrac;
+    f[SF_FORFAC * fstride + o] = forfac;
+    f[SF_FORFRAC * fstride + o] = forfrac;
+    w.idx[o] = pack_idx(jp, jt, jt1, indself, indfor, 1);
+
+    pz_prev = pz_l;
+  }
+  w.laytrop[col] = laytrop;
+  // Solar-source layer of every band, as the taumol16..29 loops select it:
+  //   upper-loop bands (16, 17, 27, 28, 29): laysolfr = nlay, replaced by the
+  //     last lay in laytrop+1..nlay with jp(lay-1) < layreffr <= jp(lay);
+  //   lower-loop bands (18..25): laysolfr = laytrop, replaced by
+  //     min(lay+1, laytrop) for the last lay in 1..laytrop with
+  //     jp(lay) < layreffr <= jp(lay+1);
+  //   band 26: laytrop.
+  // jp(0) and jp(nlay+1) read as 0.  0 means "no source layer" (empty loop).
+  auto jpat = [&](int lay) -> int {
+    if (lay < 1 || lay > nlay) return 0;
+    return unpack_idx(w.idx[(size_t)(lay - 1) * N + col]).jp;
+  };
+  for (int bi = 0; bi < kSwBands; ++bi) {
+    const int b = bi + 16;
+    const int ref = sw_layreffr(b);
+    int ls;
+    if (b == 26) {
+      ls = laytrop;
+    } else if (sw_upper_source(b)) {
+      ls = (laytrop < nlay) ? nlay : 0;
+      for (int lay = laytrop + 1; lay <= nlay; ++lay)
+        if (jpat(lay - 1) < ref && jpat(lay) >= ref) ls = lay;
+    } else {
+      ls = laytrop;
+      for (int lay = 1; lay <= laytrop; ++lay)
+        if (jpat(lay) < ref && jpat(lay + 1) >= ref) ls = min(lay + 1, laytrop);
+    }
+    w.laysolfr[bi * N + col] = ls;
+  }
+  if (flag) atomicOr(flags, 1u);
+}
+
+#endif  // RRTMG_DEFINE_COLUMN_KERNELS
+
+// ---------------------------------------------------------------------------
+// SW g-point solver: taumol_sw, delta-scaling and reftra_sw, direct beam, the
+// two vrtqdr_sw sweeps, for one g-point (rrtmg_sw_spcvrt.f90:296-618,
+// rrtmg_sw_reftra.f90, rrtmg_sw_vrtqdr.f90).  In clear sky the reference's
+// "total" stream is bit-identical to its "clear" stream (cloud weights 0/1),
+// so one stream is computed and written to both outputs.
+// ---------------------------------------------------------------------------
+template <class R>
+__device__ __forceinline__ R sw_exp_tbl(R ze1, R bpade, const R* __restrict__ exptbl) {
+  if (ze1 <= (R)0.06) return (R)1. - ze1 + (R)0.5 * ze1 * ze1;
+  const R tblind = ze1 / (bpade + ze1);
+  const int itind = (int)((R)10000.0 * tblind + (R)0.5);
+  return __ldg(exptbl + itind);
+}
+
+// delta-Eddington layer reflectance/transmittance, kmodts = 2 (rrtmg_sw_reftra.f90:143-300)
+template <class R>
+__device__ __forceinline__ void reftra1(R zto1, R zw, R zg, R prmuz, R bpade, const R* __restrict__ exptbl, R& pref,
+                                        R& prefd, R& ptra, R& ptrad) {
+  const R eps = (R)1.e-08, zwcrit = (R)0.9999995;
+  const R zg3 = (R)3. * zg;
+  const R zgamma1 = ((R)8. - zw * ((R)5. + zg3)) * (R)0.25;
+  const R zgamma2 = (R)3. * (zw * ((R)1. - zg)) * (R)0.25;
+  const R zgamma3 = ((R)2. - zg3 * prmuz) * (R)0.25;
+  const R zgamma4 = (R)1. - zgamma3;
+  const R r = zg / ((R)1. - zg);
+  const R zwo = zw / ((R)1. - ((R)1. - zw) * (r * r));
+  if (zwo >= zwcrit) {
+    const R za = zgamma1 * prmuz;
+    const R za1 = za - zgamma3;
+    const R zgt = zgamma1 * zto1;
+    const R ze1 = fmin(zto1 / prmuz, (R)500.);
+    const R ze2 = sw_exp_tbl<R>(ze1, bpade, exptbl);
+    pref = (zgt - za1 * ((R)1. - ze2)) / ((R)1. + zgt);
+    ptra = (R)1. - pref;
+    prefd = zgt / ((R)1. + zgt);
+    ptrad = (R)1. - prefd;
+    if (ze2 == (R)1.0) {
+      pref = (R)0.0;
+      ptra = (R)1.0;
+      prefd = (R)0.0;
+      ptrad = (R)1.0;
+    }
+  } else {
+    const R za1 = zgamma1 * zgamma4 + zgamma2 * zgamma3;
+    const R za2 = zgamma1 * zgamma3 + zgamma2 * zgamma4;
+    const R zrk = sqrt(zgamma1 * zgamma1 - zgamma2 * zgamma2);
+    const R zrp = zrk * prmuz;
+    const R zrp1 = (R)1. + zrp;
+    const R zrm1 = (R)1. - zrp;
+    const R zrk2 = (R)2. * zrk;
+    const R zrpp = (R)1. - zrp * zrp;
+    const R zrkg = zrk + zgamma1;
+    const R zr1 = zrm1 * (za2 + zrk * zgamma3);
+    const R zr2 = zrp1 * (za2 - zrk * zgamma3);
+    const R zr3 = zrk2 * (zgamma3 - za2 * prmuz);
+    const R zr4 = zrpp * zrkg;
+    const R zr5 = zrpp * (zrk - zgamma1);
+    const R zt1 = zrp1 * (za1 + zrk * zgamma4);
+    const R zt2 = zrm1 * (za1 - zrk * zgamma4);
+    const R zt3 = zrk2 * (zgamma4 + za1 * prmuz);
+    const R zbeta = (zgamma1 - zrk) / zrkg;
+    const R ze1 = fmin(zrk * zto1, (R)500.);
+    const R ze2 = fmin(zto1 / prmuz, (R)500.);
+    const R zem1 = sw_exp_tbl<R>(ze1, bpade, exptbl);
+    const R zep1 = (R)1. / zem1;
+    const R zem2 = sw_exp_tbl<R>(ze2, bpade, exptbl);
+    const R zep2 = (R)1. / zem2;
+    const R zdenr = zr4 * zep1 + zr5 * zem1;
+    const R zt4 = zr4, zt5 = zr5;
+    const R zdent = zt4 * zep1 + zt5 * zem1;
+    if (zdenr >= -eps && zdenr <= eps) {
+      pref = eps;
+      ptra = zem2;
+    } else {
+      pref = zw * (zr1 * zep1 - zr2 * zem1 - zr3 * zem2) / zdenr;
+      ptra = zem2 - zem2 * zw * (zt1 * zep1 - zt2 * zem1 - zt3 * zep2) / zdent;
+    }
+    const R zemm = zem1 * zem1;
+    const R zdend = (R)1. / (((R)1. - zbeta * zemm) * zrkg);
+    prefd = zgamma2 * ((R)1. - zemm) * zdend;
+    ptrad = zrk2 * zem1 * zdend;
+  }
+}
+
+template <int B, class R, int MAXL>
+__device__ __forceinline__ void sw_band(const SwPrep& p, const SwIn& in, double adjflux, int iaer,
+                                        const R* __restrict__ tab, const double* __restrict__ tab64,
+                                        const R* __restrict__ exptbl, double* __restrict__ su,
+                                        double* __restrict__ sd, int ncol, int nlay, int blk) {
+  constexpr int NG = sw_ng(B);
+  constexpr int W = pow2ceil(NG);
+  constexpr int CPB = kBlock / W;
+  constexpr int ibm = B - 15;  // 1..14
+  const int lane_col = threadIdx.x / W, g = threadIdx.x % W;
+  const int col = blk * CPB + lane_col;
+  const bool valid = col < ncol;
+  const int c = valid ? col : ncol - 1;
+  const int gg = g < NG ? g : NG - 1;
+  const size_t N = (size_t)ncol;
+  const size_t fstride = (size_t)nlay * N;
+  const double coszen = __ldg(in.coszen + c);
+  const bool lit = coszen >= 1.e-10;
+  const bool active = valid && g < NG && lit;
+  const R prmu0 = lit ? (R)coszen : (R)1.0;
+  const R bpade = (R)c_sw.bpade;
+  const int lt = p.laytrop[c];
+  const int klev = nlay;
+
+  // Solar source and incident flux of this g-point.
+  double zincflx = 0.0;
+  {
+    const int ls = p.laysolfr[(size_t)(B - 16) * N + c];
+    if (ls >= 1) {
+      SwLayerView<double> L{p.f, fstride, (size_t)(ls - 1) * N + c};
+      const double sfz = sw_sfluxzen<B>(c_sw, L, ls <= lt, gg, tab64);
+      zincflx = adjflux * sfz * (lit ? coszen : 1.0);
+    }
+  }
+  const R albdir = (R)__ldg(((ibm >= 10 && ibm <= 13) ? in.asdir : in.aldir) + c);
+  const R albdif = (R)__ldg(((ibm >= 10 && ibm <= 13) ? in.asdif : in.aldif) + c);
+
+  // Layer arrays, top-down index jk = 1..klev (+ surface klev+1).
+  R pref[MAXL + 1], prefd[MAXL + 1], ptra[MAXL + 1], ptrad[MAXL + 1], pdbt[MAXL + 1];
+  R ptdbt[MAXL + 2], ztdn[MAXL + 2], prdnd[MAXL + 2];
+  ptdbt[1 - 1] = (R)1.0;
+  for (int jk = 1; jk <= klev; ++jk) {
+    const int ikl = klev + 1 - jk;
+    const size_t o = (size_t)(ikl - 1) * N + c;
+    const Idx ix = unpack_idx(__ldg(p.idx + o));
+    SwLayerView<R> L{p.f, fstride, o};
+    R taug, taur;
+    sw_gas<B, R>(c_sw, L, ix, ikl <= lt, gg, tab, taug, taur);
+    R taua = (R)0., omga = (R)1., asya = (R)0.;
+    if (iaer == 10) {
+      const size_t oa = c + N * ((size_t)(ikl - 1) + (size_t)nlay * (ibm - 1));
+      taua = (R)__ldg(in.tauaer + oa);
+      omga = (R)__ldg(in.ssaaer + oa);
+      asya = (R)__ldg(in.asmaer + oa);
+    }
+    R ztauc = taur + taug + taua;
+    R zomcc = taur * (R)1.0 + taua * omga;
+    R zgcc = asya * omga * taua / zomcc;
+    zomcc = zomcc / ztauc;
+    const R zf = zgcc * zgcc;
+    const R zwf = zomcc * zf;
+    ztauc = ((R)1.0 - zwf) * ztauc;
+    zomcc = (zomcc - zwf) / ((R)1.0 - zwf);
+    zgcc = (zgcc - zf) / ((R)1.0 - zf);
+    R rf, rfd, tr, trd;
+    reftra1<R>(ztauc, zomcc, zgcc, prmu0, bpade, exptbl, rf, rfd, tr, trd);
+    pref[jk - 1] = rf;
+    prefd[jk - 1] = rfd;
+    ptra[jk - 1] = tr;
+    ptrad[jk - 1] = trd;
+    const R zdbtmc = sw_exp_tbl<R>(ztauc / prmu0, bpade, exptbl);
+    pdbt[jk - 1] = zdbtmc;
+    ptdbt[jk] = zdbtmc * ptdbt[jk - 1];
+    // Downward adding sweep of vrtqdr_sw (:127-139), fused with the layer loop.
+    if (jk == 1) {
+      ztdn[0] = (R)1.;
+      prdnd[0] = (R)0.;
+      ztdn[1] = tr;
+      prdnd[1] = rfd;
+    } else {
+      const R zreflect = (R)1. / ((R)1. - rfd * prdnd[jk - 1]);
+      ztdn[jk] = ptdbt[jk - 1] * tr + (trd * ((ztdn[jk - 1] - ptdbt[jk - 1]) + ptdbt[jk - 1] * rf * prdnd[jk - 1])) * zreflect;
+      prdnd[jk] = rfd + trd * trd * prdnd[jk - 1] * zreflect;
+    }
+  }
+  // Upward sweep (vrtqdr_sw :104-124) from the surface, with the level fluxes
+  // (:141-149) as soon as each level's upward reflectances are known.
+  double* sup = su + (size_t)(B - 16) * (nlay + 1) * N + col;
+  double* sdp = sd + (size_t)(B - 16) * (nlay + 1) * N + col;
+  R prup = albdir, prupd = albdif;  // level klev+1 (surface)
+  for (int jk = klev + 1; jk >= 1; --jk) {
+    if (jk <= klev) {
+      const int k = jk - 1;
+      if (jk == klev) {
+        const R zreflect = (R)1. / ((R)1. - albdif * prefd[k]);
+        const R nup = pref[k] + (ptrad[k] * ((ptra[k] - pdbt[k]) * albdif + pdbt[k] * albdir)) * zreflect;
+        const R nupd = prefd[k] + ptrad[k] * ptrad[k] * albdif * zreflect;
+        prup = nup;
+        prupd = nupd;
+      } else {
+        const R zreflect = (R)1. / ((R)1. - prupd * prefd[k]);
+        const R nup = pref[k] + (ptrad[k] * ((ptra[k] - pdbt[k]) * prupd + pdbt[k] * prup)) * zreflect;
+        const R nupd = prefd[k] + ptrad[k] * ptrad[k] * prupd * zreflect;
+        prup = nup;
+        prupd = nupd;
+      }
+    }
+    const R tdbt = ptdbt[jk - 1], tdn = ztdn[jk - 1], rdnd = prdnd[jk - 1];
+    const R zreflect = (R)1. / ((R)1. - rdnd * prupd);
+    const R pfu = (tdbt * prup + (tdn - tdbt) * prupd) * zreflect;
+    const R pfd = tdbt + (tdn - tdbt + tdbt * prup * rdnd) * zreflect;
+    const double su_s = seg_sum<W>(active ? zincflx * (double)pfu : 0.0);
+    const double sd_s = seg_sum<W>(active ? zincflx * (double)pfd : 0.0);
+    // output level (surface first) ikl = klev + 2 - jk  ->  0-based klev + 1 - jk
+    if (g == 0 && valid) {
+      sup[(size_t)(klev + 1 - jk) * N] = su_s;
+      sdp[(size_t)(klev + 1 - jk) * N] = sd_s;
+    }
+  }
+}
+
+template <class R, int MAXL>
+__global__ void __launch_bounds__(kBlock) sw_gpoint_kernel(SwPrep p, SwIn in, double adjflux, int iaer,
+                                                           const R* __restrict__ tab, const double* __restrict__ tab64,
+                                                           const R* __restrict__ exptbl, double* su, double* sd,
+                                                           int ncol, int nlay) {
+  int blk = blockIdx.x, band = 0;
+  for (; band < kSwBands; ++band) {
+    const int nb = lw_blocks_for_band(c_sw.band[band].ngpad, ncol);
+    if (blk < nb) break;
+    blk -= nb;
+  }
+#define RRTMG_SW_CASE(b) \
+  case b - 16: sw_band<b, R, MAXL>(p, in, adjflux, iaer, tab, tab64, exptbl, su, sd, ncol, nlay, blk); break;
+  switch (band) {
+    RRTMG_SW_CASE(16) RRTMG_SW_CASE(17) RRTMG_SW_CASE(18) RRTMG_SW_CASE(19) RRTMG_SW_CASE(20) RRTMG_SW_CASE(21)
+    RRTMG_SW_CASE(22) RRTMG_SW_CASE(23) RRTMG_SW_CASE(24) RRTMG_SW_CASE(25) RRTMG_SW_CASE(26) RRTMG_SW_CASE(27)
+    RRTMG_SW_CASE(28) RRTMG_SW_CASE(29)
+    default: break;
+  }
+#undef RRTMG_SW_CASE
+}
+
+#ifdef RRTMG_DEFINE_COLUMN_KERNELS
+// SW finalize: band sums, outputs, heating (rrtmg_sw_rad.nomcica.f90:688-726);
+// dark columns (coszen < 1e-10) get zeros (:502-510).
+__global__ void __launch_bounds__(128) sw_finalize_kernel(const double* __restrict__ su, const double* __restrict__ sd,
+                                                          const double* __restrict__ plev,
+                                                          const double* __restrict__ coszen, int ncol, int nlay,
+                                                          double* swuflx, double* swdflx, double* swhr,
+                                                          double* swuflxc, double* swdflxc, double* swhrc) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncol) return;
+  const size_t N = (size_t)ncol;
+  const bool lit = __ldg(coszen + col) >= 1.e-10;
+  double nprev = 0.0;
+  for (int k = 0; k <= nlay; ++k) {
+    double fu = 0.0, fd = 0.0;
+    if (lit) {
+      for (int b = 0; b < kSwBands; ++b) {
+        const size_t o = ((size_t)b * (nlay + 1) + k) * N + col;
+        fu = fu + __ldg(su + o);
+        fd = fd + __ldg(sd + o);
+      }
+    }
+    const size_t oo = (size_t)k * N + col;
+    swuflx[oo] = fu;
+    swdflx[oo] = fd;
+    swuflxc[oo] = fu;
+    swdflxc[oo] = fd;
+    const double net = fd - fu;
+    if (k >= 1) {
+      const size_t oh = (size_t)(k - 1) * N + col;
+      double h = 0.0;
+      if (lit && k < nlay) {
+        const double zdpgcp = c_sw.heatfac / (__ldg(plev + (size_t)(k - 1) * N + col) - __ldg(plev + oo));
+        h = (net - nprev) * zdpgcp;
+      }
+      swhr[oh] = h;
+      swhrc[oh] = h;
+    }
+    nprev = net;
+  }
+}
+
+#endif  // RRTMG_DEFINE_COLUMN_KERNELS
+
+}  // namespace rrtmg

@@ -1,0 +1,68 @@
+// FP64 instantiation of the RRTMG kernels.  Built with --fmad=false: every
+// multiply and add is rounded separately, as written, so the FP64 path
+// reproduces a literal FP64 restatement of the reference bit for bit apart
+// from transcendental functions (log/exp) and the order of g-point sums.
+#define RRTMG_DEFINE_COLUMN_KERNELS
+#include "kernels.cuh"
+#include "launch.h"
+
+namespace rrtmg {
+
+cudaError_t upload_constants_fp64(const LwConst& lw, const SwConst& sw) {
+  cudaError_t e = cudaMemcpyToSymbol(c_lw, &lw, sizeof(LwConst));
+  if (e != cudaSuccess) return e;
+  return cudaMemcpyToSymbol(c_sw, &sw, sizeof(SwConst));
+}
+
+int lw_gpoint_blocks(const LwConst& c, int ncol) {
+  int n = 0;
+  for (int b = 0; b < kLwBands; ++b) n += lw_blocks_for_band(c.band[b].ngpad, ncol);
+  return n;
+}
+int sw_gpoint_blocks(const SwConst& c, int ncol) {
+  int n = 0;
+  for (int b = 0; b < kSwBands; ++b) n += lw_blocks_for_band(c.band[b].ngpad, ncol);
+  return n;
+}
+
+void launch_lw_prep(const LwIn& in, const LwWork& w, const double* totplnk, const double* totplnkderiv, int ncol,
+                    int nlay, int idrv, unsigned* flags, cudaStream_t s) {
+  lw_prep_kernel<<<(ncol + 127) / 128, 128, 0, s>>>(in, w, totplnk, totplnkderiv, ncol, nlay, idrv, flags);
+}
+
+void launch_lw_gpoint_fp64(const LwPrep& p, const double* emis, const double* tauaer, const double* tab,
+                           const double* exptbl, const double* tfntbl, double* bu, double* bd, double* bdu, int ncol,
+                           int nlay, int idrv, int nb, cudaStream_t s) {
+  if (maxl_for(nlay) == 64)
+    lw_gpoint_kernel<double, 64><<<nb, kBlock, 0, s>>>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv);
+  else
+    lw_gpoint_kernel<double, 208><<<nb, kBlock, 0, s>>>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv);
+}
+
+void launch_lw_finalize(const double* bu, const double* bd, const double* bdu, const double* plev, int ncol, int nlay,
+                        int idrv, double* uflx, double* dflx, double* hr, double* uflxc, double* dflxc, double* hrc,
+                        double* duflx_dt, double* duflxc_dt, cudaStream_t s) {
+  lw_finalize_kernel<<<(ncol + 127) / 128, 128, 0, s>>>(bu, bd, bdu, plev, ncol, nlay, idrv, uflx, dflx, hr, uflxc,
+                                                        dflxc, hrc, duflx_dt, duflxc_dt);
+}
+
+void launch_sw_prep(const SwIn& in, const SwWork& w, int ncol, int nlay, unsigned* flags, cudaStream_t s) {
+  sw_prep_kernel<<<(ncol + 127) / 128, 128, 0, s>>>(in, w, ncol, nlay, flags);
+}
+
+void launch_sw_gpoint_fp64(const SwPrep& p, const SwIn& in, double adjflux, int iaer, const double* tab,
+                           const double* exptbl, double* su, double* sd, int ncol, int nlay, int nb, cudaStream_t s) {
+  if (maxl_for(nlay) == 64)
+    sw_gpoint_kernel<double, 64><<<nb, kBlock, 0, s>>>(p, in, adjflux, iaer, tab, tab, exptbl, su, sd, ncol, nlay);
+  else
+    sw_gpoint_kernel<double, 208><<<nb, kBlock, 0, s>>>(p, in, adjflux, iaer, tab, tab, exptbl, su, sd, ncol, nlay);
+}
+
+void launch_sw_finalize(const double* su, const double* sd, const double* plev, const double* coszen, int ncol,
+                        int nlay, double* swuflx, double* swdflx, double* swhr, double* swuflxc, double* swdflxc,
+                        double* swhrc, cudaStream_t s) {
+  sw_finalize_kernel<<<(ncol + 127) / 128, 128, 0, s>>>(su, sd, plev, coszen, ncol, nlay, swuflx, swdflx, swhr,
+                                                        swuflxc, swdflxc, swhrc);
+}
+
+}  // namespace rrtmg

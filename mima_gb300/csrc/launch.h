@@ -1,0 +1,51 @@
+// Host-side launch wrappers of the kernel translation units (kernels_fp64.cu,
+// compiled without multiply-add contraction for bit-reproducible FP64, and
+// kernels_split.cu, the FP32-split path).  Each translation unit owns a copy
+// of the constant-memory tables and uploads it in upload_constants_*().
+#pragma once
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace rrtmg {
+
+struct LwIn;
+struct LwWork;
+struct SwIn;
+struct SwWork;
+
+// Choice of the compiled per-thread column depth (local-memory arrays).
+inline int maxl_for(int nlay) { return nlay <= 64 ? 64 : 208; }
+
+cudaError_t upload_constants_fp64(const LwConst& lw, const SwConst& sw);
+cudaError_t upload_constants_split(const LwConst& lw, const SwConst& sw);
+
+// FP64 translation unit: prep, FP64 g-point solvers, finalize.
+void launch_lw_prep(const LwIn& in, const LwWork& w, const double* totplnk, const double* totplnkderiv, int ncol,
+                    int nlay, int idrv, unsigned* flags, cudaStream_t s);
+void launch_lw_gpoint_fp64(const LwPrep& p, const double* emis, const double* tauaer, const double* tab,
+                           const double* exptbl, const double* tfntbl, double* bu, double* bd, double* bdu, int ncol,
+                           int nlay, int idrv, int nb, cudaStream_t s);
+void launch_lw_finalize(const double* bu, const double* bd, const double* bdu, const double* plev, int ncol, int nlay,
+                        int idrv, double* uflx, double* dflx, double* hr, double* uflxc, double* dflxc, double* hrc,
+                        double* duflx_dt, double* duflxc_dt, cudaStream_t s);
+void launch_sw_prep(const SwIn& in, const SwWork& w, int ncol, int nlay, unsigned* flags, cudaStream_t s);
+void launch_sw_gpoint_fp64(const SwPrep& p, const SwIn& in, double adjflux, int iaer, const double* tab,
+                           const double* exptbl, double* su, double* sd, int ncol, int nlay, int nb, cudaStream_t s);
+void launch_sw_finalize(const double* su, const double* sd, const double* plev, const double* coszen, int ncol,
+                        int nlay, double* swuflx, double* swdflx, double* swhr, double* swuflxc, double* swdflxc,
+                        double* swhrc, cudaStream_t s);
+
+// FP32-split translation unit.
+void launch_lw_gpoint_split(const LwPrep& p, const double* emis, const double* tauaer, const float* tab,
+                            const float* exptbl, const float* tfntbl, double* bu, double* bd, double* bdu, int ncol,
+                            int nlay, int idrv, int nb, cudaStream_t s);
+void launch_sw_gpoint_split(const SwPrep& p, const SwIn& in, double adjflux, int iaer, const float* tab,
+                            const double* tab64, const float* exptbl, double* su, double* sd, int ncol, int nlay,
+                            int nb, cudaStream_t s);
+
+// Number of blocks of the g-point grids (sum over bands of columns / (128 / ngpad)).
+int lw_gpoint_blocks(const LwConst& c, int ncol);
+int sw_gpoint_blocks(const SwConst& c, int ncol);
+
+}  // namespace rrtmg

@@ -1,0 +1,22 @@
+// Host-side construction of the device coefficient tables (replaces
+// rrtmg_lw_ini / rrtmg_sw_ini, rrtmg_lw_init.f90:28-175, rrtmg_sw_init.f90:28-154).
+#pragma once
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace rrtmg {
+
+struct HostTables {
+  std::vector<double> lw_tab, sw_tab;           // reduced band tables, g fastest
+  std::vector<double> lw_exp, lw_tfn, sw_exp;   // 0..10000 lookup tables
+  std::vector<double> totplnk, totplnkderiv;    // (181, 16) Fortran order
+  LwConst lw;
+  SwConst sw;
+};
+
+// Returns "" on success, else a message.
+std::string build_host_tables(const char* blob_path, double cpdair, HostTables& out);
+
+}  // namespace rrtmg

@@ -1,0 +1,244 @@
+"""Python mirror of MiMA's ``rrtmg_lw`` / ``rrtmg_sw`` calls over the C-ABI.
+
+The reference calls (``rrtmg_lw_rad.nomcica.f90:80-89``,
+``rrtmg_sw_rad.nomcica.f90:78-88``) become methods of :class:`RRTMG` with the
+same argument names and meaning; every array is passed straight to
+``librrtmg_gpu.so`` (include/rrtmg_gpu.h).  Host numpy arrays go through
+``rrtmg_lw_c`` / ``rrtmg_sw_c``; device arrays (anything exposing
+``data_ptr()``, e.g. torch CUDA tensors) through ``rrtmg_lw_dev`` /
+``rrtmg_sw_dev`` on a given stream.
+
+There is no CPU fallback: constructing :class:`RRTMG` raises if the shared
+library is missing or the GPU cannot be initialised.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+from . import tables
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "lib" / "librrtmg_gpu.so"
+
+RRTMG_OK = 0
+RRTMG_ERR_ARG = 1
+RRTMG_ERR_UNSUPPORTED = 2
+RRTMG_ERR_CUDA = 3
+RRTMG_ERR_TABLES = 4
+RRTMG_ERR_INPUT = 5
+RRTMG_ERR_NOMEM = 6
+PREC = {"fp64": 0, "split": 1}
+
+# Every symbol include/rrtmg_gpu.h declares.
+EXPORTED = ("rrtmg_gpu_init", "rrtmg_gpu_finalize", "rrtmg_gpu_set_precision", "rrtmg_gpu_error_string",
+            "rrtmg_gpu_last_error", "rrtmg_gpu_launch_count", "rrtmg_lw_c", "rrtmg_sw_c", "rrtmg_lw_dev",
+            "rrtmg_sw_dev", "rrtmg_gpu_reserve", "rrtmg_gpu_sync_status")
+
+_lib = None
+_dp = C.POINTER(C.c_double)
+
+
+class RRTMGError(RuntimeError):
+    def __init__(self, code: int, detail: str = ""):
+        self.code = code
+        msg = _lib.rrtmg_gpu_error_string(code).decode() if _lib else f"status {code}"
+        super().__init__(f"{msg} ({code}){': ' + detail if detail else ''}")
+
+
+def load_library(path: Path | str | None = None) -> C.CDLL:
+    """Load librrtmg_gpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = Path(path or os.environ.get("RRTMG_GPU_LIB", LIB_PATH))
+    if not p.exists():
+        raise RuntimeError(f"{p} not found; build it with `python -m mima_gb300.build` (no CPU fallback exists)")
+    lib = C.CDLL(str(p))
+    vp = C.c_void_p
+    lib.rrtmg_gpu_init.argtypes = [C.c_double, C.c_char_p, C.c_int, C.POINTER(vp)]
+    lib.rrtmg_gpu_finalize.argtypes = [vp]
+    lib.rrtmg_gpu_set_precision.argtypes = [vp, C.c_int]
+    lib.rrtmg_gpu_error_string.argtypes = [C.c_int]
+    lib.rrtmg_gpu_error_string.restype = C.c_char_p
+    lib.rrtmg_gpu_last_error.argtypes = [vp]
+    lib.rrtmg_gpu_last_error.restype = C.c_char_p
+    lib.rrtmg_gpu_launch_count.argtypes = [vp]
+    lib.rrtmg_gpu_launch_count.restype = C.c_longlong
+    lib.rrtmg_gpu_reserve.argtypes = [vp, C.c_int, C.c_int]
+    lib.rrtmg_gpu_sync_status.argtypes = [vp, vp]
+    _lib = lib
+    return lib
+
+
+def _host(a):
+    if a is None:
+        return None
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a
+
+
+def _hp(a):
+    return None if a is None else a.ctypes.data_as(_dp)
+
+
+def _dptr(t):
+    if t is None:
+        return None
+    return C.cast(C.c_void_p(int(t.data_ptr())), _dp)
+
+
+class RRTMG:
+    """One GPU handle: tables loaded once (rrtmg_lw_ini/rrtmg_sw_ini)."""
+
+    def __init__(self, blob=None, cpdair: float = 1004.64, device: int = 0, precision: str = "fp64"):
+        lib = load_library()
+        blob = Path(blob) if blob else tables.ensure_blob()
+        h = C.c_void_p()
+        rc = lib.rrtmg_gpu_init(C.c_double(cpdair), str(blob).encode(), C.c_int(device), C.byref(h))
+        if rc != RRTMG_OK:
+            raise RRTMGError(rc, f"rrtmg_gpu_init({blob})")
+        self._h = h
+        self.lib = lib
+        self.device = device
+        self.set_precision(precision)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.rrtmg_gpu_finalize(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_precision(self, precision: str) -> None:
+        rc = self.lib.rrtmg_gpu_set_precision(self._h, PREC[precision])
+        self._check(rc)
+        self.precision = precision
+
+    def launch_count(self) -> int:
+        return int(self.lib.rrtmg_gpu_launch_count(self._h))
+
+    def reserve(self, ncol: int, nlay: int) -> None:
+        self._check(self.lib.rrtmg_gpu_reserve(self._h, ncol, nlay))
+
+    def sync_status(self, stream=None) -> int:
+        return int(self.lib.rrtmg_gpu_sync_status(self._h, C.c_void_p(stream or 0)))
+
+    def _check(self, rc):
+        if rc != RRTMG_OK:
+            raise RRTMGError(rc, self.lib.rrtmg_gpu_last_error(self._h).decode())
+
+    # ---------------- host-array drop-ins ----------------
+    def rrtmg_lw(self, ncol, nlay, icld, idrv, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr,
+                 ch4vmr=None, n2ovmr=None, o2vmr=None, cfc11vmr=None, cfc12vmr=None, cfc22vmr=None,
+                 ccl4vmr=None, emis=None, tauaer=None, check=True):
+        """rrtmg_lw on host arrays; returns uflx, dflx, hr, uflxc, dflxc, hrc (+ duflx_dt, duflxc_dt)."""
+        L, N = nlay, ncol
+        ins = [_host(a) for a in (play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr,
+                                  cfc11vmr, cfc12vmr, cfc22vmr, ccl4vmr, emis)]
+        out = {k: np.empty((L + 1, N)) for k in ("uflx", "dflx", "uflxc", "dflxc")}
+        out.update({k: np.empty((L, N)) for k in ("hr", "hrc")})
+        if idrv == 1:
+            out["duflx_dt"] = np.empty((L + 1, N))
+            out["duflxc_dt"] = np.empty((L + 1, N))
+        ta = _host(tauaer)
+        rc = self.lib.rrtmg_lw_c(
+            self._h, C.c_int(N), C.c_int(L), C.c_int(icld), C.c_int(idrv), *[_hp(a) for a in ins],
+            C.c_int(0), C.c_int(0), C.c_int(0), None, None, None, None, None, None, _hp(ta),
+            _hp(out["uflx"]), _hp(out["dflx"]), _hp(out["hr"]), _hp(out["uflxc"]), _hp(out["dflxc"]),
+            _hp(out["hrc"]), _hp(out.get("duflx_dt")), _hp(out.get("duflxc_dt")))
+        out["status"] = rc
+        if check:
+            self._check(rc)
+        return out
+
+    def rrtmg_sw(self, ncol, nlay, icld, iaer, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr,
+                 n2ovmr, o2vmr, asdir, asdif, aldir, aldif, coszen, adjes, dyofyr, scon, tauaer=None,
+                 ssaaer=None, asmaer=None, check=True):
+        L, N = nlay, ncol
+        ins = [_host(a) for a in (play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr,
+                                  asdir, asdif, aldir, aldif, coszen)]
+        aer = [_host(a) for a in (tauaer, ssaaer, asmaer)]
+        out = {k: np.empty((L + 1, N)) for k in ("swuflx", "swdflx", "swuflxc", "swdflxc")}
+        out.update({k: np.empty((L, N)) for k in ("swhr", "swhrc")})
+        rc = self.lib.rrtmg_sw_c(
+            self._h, C.c_int(N), C.c_int(L), C.c_int(icld), C.c_int(iaer), *[_hp(a) for a in ins],
+            C.c_double(adjes), C.c_int(dyofyr), C.c_double(scon), C.c_int(0), C.c_int(0), C.c_int(0),
+            None, None, None, None, None, None, None, None, None, *[_hp(a) for a in aer], None,
+            _hp(out["swuflx"]), _hp(out["swdflx"]), _hp(out["swhr"]), _hp(out["swuflxc"]),
+            _hp(out["swdflxc"]), _hp(out["swhrc"]))
+        out["status"] = rc
+        if check:
+            self._check(rc)
+        return out
+
+    # Convenience: whole Atmosphere objects (mima_gb300.atmosphere)
+    def lw(self, atm, idrv=0, tauaer=None, check=True):
+        return self.rrtmg_lw(atm.ncol, atm.nlay, 0, idrv, atm.play, atm.plev, atm.tlay, atm.tlev, atm.tsfc,
+                             atm.h2o, atm.o3, atm.co2, atm.ch4, atm.n2o, atm.o2, atm.cfc11, atm.cfc12, atm.cfc22,
+                             atm.ccl4, atm.emis, tauaer, check=check)
+
+    def sw(self, atm, iaer=0, tauaer=None, ssaaer=None, asmaer=None, check=True):
+        return self.rrtmg_sw(atm.ncol, atm.nlay, 0, iaer, atm.play, atm.plev, atm.tlay, atm.tlev, atm.tsfc,
+                             atm.h2o, atm.o3, atm.co2, atm.ch4, atm.n2o, atm.o2, atm.asdir, atm.asdif,
+                             atm.aldir, atm.aldif, atm.coszen, atm.adjes, atm.dyofyr, atm.scon,
+                             tauaer, ssaaer, asmaer, check=check)
+
+    # ---------------- device-array entry points ----------------
+    def rrtmg_lw_dev(self, stream, ncol, nlay, icld, idrv, d, out, tauaer=None):
+        """``d``/``out``: dicts of CUDA tensors with the argument names of rrtmg_lw."""
+        g = lambda k: _dptr(d.get(k))
+        o = lambda k: _dptr(out.get(k))
+        rc = self.lib.rrtmg_lw_dev(
+            self._h, C.c_void_p(stream or 0), C.c_int(ncol), C.c_int(nlay), C.c_int(icld), C.c_int(idrv),
+            g("play"), g("plev"), g("tlay"), g("tlev"), g("tsfc"), g("h2ovmr"), g("o3vmr"), g("co2vmr"),
+            g("ch4vmr"), g("n2ovmr"), g("o2vmr"), g("cfc11vmr"), g("cfc12vmr"), g("cfc22vmr"), g("ccl4vmr"),
+            g("emis"), C.c_int(0), C.c_int(0), C.c_int(0), None, None, None, None, None, None, _dptr(tauaer),
+            o("uflx"), o("dflx"), o("hr"), o("uflxc"), o("dflxc"), o("hrc"), o("duflx_dt"), o("duflxc_dt"))
+        self._check(rc)
+
+    def rrtmg_sw_dev(self, stream, ncol, nlay, icld, iaer, d, out, adjes, dyofyr, scon):
+        g = lambda k: _dptr(d.get(k))
+        o = lambda k: _dptr(out.get(k))
+        rc = self.lib.rrtmg_sw_dev(
+            self._h, C.c_void_p(stream or 0), C.c_int(ncol), C.c_int(nlay), C.c_int(icld), C.c_int(iaer),
+            g("play"), g("plev"), g("tlay"), g("tlev"), g("tsfc"), g("h2ovmr"), g("o3vmr"), g("co2vmr"),
+            g("ch4vmr"), g("n2ovmr"), g("o2vmr"), g("asdir"), g("asdif"), g("aldir"), g("aldif"),
+            g("coszen"), C.c_double(adjes), C.c_int(dyofyr), C.c_double(scon), C.c_int(0), C.c_int(0),
+            C.c_int(0), None, None, None, None, None, None, None, None, None, g("tauaer"), g("ssaaer"),
+            g("asmaer"), None, o("swuflx"), o("swdflx"), o("swhr"), o("swuflxc"), o("swdflxc"), o("swhrc"))
+        self._check(rc)
+
+
+def atm_device_inputs(atm, device="cuda"):
+    """Copy an Atmosphere to CUDA tensors keyed by the rrtmg_lw/rrtmg_sw argument names."""
+    import torch
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(device)
+    return {
+        "play": t(atm.play), "plev": t(atm.plev), "tlay": t(atm.tlay), "tlev": t(atm.tlev),
+        "tsfc": t(atm.tsfc), "h2ovmr": t(atm.h2o), "o3vmr": t(atm.o3), "co2vmr": t(atm.co2),
+        "ch4vmr": t(atm.ch4), "n2ovmr": t(atm.n2o), "o2vmr": t(atm.o2), "cfc11vmr": t(atm.cfc11),
+        "cfc12vmr": t(atm.cfc12), "cfc22vmr": t(atm.cfc22), "ccl4vmr": t(atm.ccl4), "emis": t(atm.emis),
+        "asdir": t(atm.asdir), "asdif": t(atm.asdif), "aldir": t(atm.aldir), "aldif": t(atm.aldif),
+        "coszen": t(atm.coszen),
+    }
+
+
+def device_outputs(ncol, nlay, device="cuda", idrv=0):
+    import torch
+    e = lambda n: torch.empty((n, ncol), dtype=torch.float64, device=device)
+    lw = {"uflx": e(nlay + 1), "dflx": e(nlay + 1), "hr": e(nlay), "uflxc": e(nlay + 1), "dflxc": e(nlay + 1),
+          "hrc": e(nlay)}
+    if idrv == 1:
+        lw["duflx_dt"] = e(nlay + 1)
+        lw["duflxc_dt"] = e(nlay + 1)
+    sw = {"swuflx": e(nlay + 1), "swdflx": e(nlay + 1), "swhr": e(nlay), "swuflxc": e(nlay + 1),
+          "swdflxc": e(nlay + 1), "swhrc": e(nlay)}
+    return lw, sw

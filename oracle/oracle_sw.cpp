@@ -249,6 +249,12 @@ static inline double selfonly(const FArr& selfref, const SwColumn& c, int lay, i
   int inds = c.indself[lay];
   return c.selffac[lay] * (selfref(inds, ig) + c.selffrac[lay] * (selfref(inds + 1, ig) - selfref(inds, ig)));
 }
+// forref(indf,ig) + forfrac*(forref(indf+1,ig) - forref(indf,ig)); the upper
+// loops of taumol17/21 multiply it by colh2o*forfac (rrtmg_sw_taumol.f90:450-454, 858-862).
+static inline double forinterp(const FArr& forref, const SwColumn& c, int lay, int ig) {
+  int indf = c.indfor[lay];
+  return forref(indf, ig) + c.forfrac[lay] * (forref(indf + 1, ig) - forref(indf, ig));
+}
 static inline double foronly(const FArr& forref, const SwColumn& c, int lay, int ig) {
   int indf = c.indfor[lay];
   return c.forfac[lay] * (forref(indf, ig) + c.forfrac[lay] * (forref(indf + 1, ig) - forref(indf, ig)));
@@ -337,7 +343,7 @@ void sw_taumol(SwColumn& c) {
       int ind0 = ind_up(c, lay, T.nspb[17], e.js, false), ind1 = ind_up1(c, lay, T.nspb[17], e.js, false);
       double tauray = c.colmol[lay] * rayl;
       for (int ig = 1; ig <= T.ngc[17]; ++ig) {
-        taug[o + ig][lay] = major8(absb, c, lay, e, ind0, ind1, 5, ig) + c.colh2o[lay] * foronly(forref, c, lay, ig);
+        taug[o + ig][lay] = major8(absb, c, lay, e, ind0, ind1, 5, ig) + c.colh2o[lay] * c.forfac[lay] * forinterp(forref, c, lay, ig);
         if (lay == laysolfr) sfz[o + ig] = sfl_eta(sflux, ig, e);
         taur[o + ig][lay] = tauray;
       }
@@ -438,7 +444,7 @@ void sw_taumol(SwColumn& c) {
       int ind0 = ind_up(c, lay, T.nspb[21], e.js, false), ind1 = ind_up1(c, lay, T.nspb[21], e.js, false);
       double tauray = c.colmol[lay] * rayl;
       for (int ig = 1; ig <= T.ngc[21]; ++ig) {
-        taug[o + ig][lay] = major8(absb, c, lay, e, ind0, ind1, 5, ig) + c.colh2o[lay] * foronly(forref, c, lay, ig);
+        taug[o + ig][lay] = major8(absb, c, lay, e, ind0, ind1, 5, ig) + c.colh2o[lay] * c.forfac[lay] * forinterp(forref, c, lay, ig);
         taur[o + ig][lay] = tauray;
       }
     }

@@ -1,0 +1,116 @@
+"""Host-side checks that need no GPU: the C-ABI library loads and exports
+every symbol the public header declares, its host-only error paths, the
+synthetic atmosphere generator and column sharding (gloo, 2 ranks)."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from mima_gb300 import atmosphere as A
+from mima_gb300 import rrtmg as R
+from mima_gb300.shard import column_slice
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def header_symbols():
+    text = (ROOT / "include" / "rrtmg_gpu.h").read_text()
+    return sorted(set(re.findall(r"^(?:int|const char\*|long long)\s+(rrtmg_\w+)\(", text, re.M)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = R.load_library()
+    syms = header_symbols()
+    assert len(syms) == 12
+    assert set(syms) == set(R.EXPORTED)
+    for s in syms:
+        assert hasattr(lib, s), s
+
+
+def test_host_only_error_paths(tmp_path):
+    lib = R.load_library()
+    assert lib.rrtmg_gpu_error_string(0) == b"success"
+    assert b"table" in lib.rrtmg_gpu_error_string(R.RRTMG_ERR_TABLES)
+    h = C.c_void_p()
+    # a missing blob is reported before any CUDA call
+    rc = lib.rrtmg_gpu_init(C.c_double(1004.64), str(tmp_path / "nope.bin").encode(), 0, C.byref(h))
+    assert rc == R.RRTMG_ERR_TABLES and not h.value
+    bad = tmp_path / "bad.bin"
+    bad.write_bytes(b"RRTMGTB1" + b"\0" * 40)
+    assert lib.rrtmg_gpu_init(C.c_double(1004.64), str(bad).encode(), 0, C.byref(h)) == R.RRTMG_ERR_TABLES
+    assert lib.rrtmg_gpu_init(C.c_double(-1.0), b"x", 0, C.byref(h)) == R.RRTMG_ERR_ARG
+    assert lib.rrtmg_gpu_set_precision(None, 0) == R.RRTMG_ERR_ARG
+    assert lib.rrtmg_gpu_finalize(None) == R.RRTMG_ERR_ARG
+    assert lib.rrtmg_gpu_reserve(None, 10, 40) == R.RRTMG_ERR_ARG
+
+
+def test_generator_configurations():
+    atm = A.config_atmosphere(0)
+    assert atm.ncol == 128 * 64 and atm.nlay == 40
+    assert atm.play.shape == (40, 8192) and atm.plev.shape == (41, 8192)
+    assert np.all(np.diff(atm.plev, axis=0) < 0)  # surface first
+    assert np.isclose(atm.plev[-1, 0], 0.1) and np.isclose(atm.plev[0, 0], 1000.0)
+    assert np.all((atm.tlay >= 200.0) & (atm.tlay < 340.0))
+    assert np.all((atm.h2o >= 3e-6) & (atm.h2o < 0.05))
+    assert np.all((atm.coszen >= 0) & (atm.coszen < 0.5))
+    a3 = A.config_atmosphere(3)
+    assert a3.ncol == 256
+    a2 = A.grid_atmosphere("T170", 60, 12347, 5.0, True)
+    assert a2.ncol == 131072 and np.isclose(a2.plev[-1, 0], 0.01)
+    # reproducible
+    assert np.array_equal(A.config_atmosphere(0).tsfc, atm.tsfc)
+
+
+def test_column_slices_partition():
+    for n in (1, 7, 8192, 32768):
+        for w in (1, 2, 3, 8):
+            s = [column_slice(r, w, n) for r in range(w)]
+            cover = np.concatenate([np.arange(n)[x] for x in s])
+            assert np.array_equal(cover, np.arange(n))
+
+
+def _shard_worker(rank, world, port, q):
+    import os
+    import torch
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from mima_gb300 import tables
+    from oracle import oracle as orc
+    orc.load(tables.ensure_blob())
+    atm = A.small_atmosphere(64, 40, seed=12)
+    sl = column_slice(rank, world, atm.ncol)
+    part = orc.rrtmg_lw(atm.subset(np.arange(atm.ncol)[sl]), nthreads=1)["uflx"]
+    t = torch.from_numpy(np.ascontiguousarray(part.T))
+    sizes = [torch.zeros(1, dtype=torch.long) for _ in range(world)]
+    dist.all_gather(sizes, torch.tensor([t.shape[0]]))
+    out = [torch.zeros((int(s), t.shape[1]), dtype=t.dtype) for s in sizes]
+    dist.all_gather(out, t)
+    if rank == 0:
+        q.put(torch.cat(out).numpy().T.copy())
+    dist.destroy_process_group()
+
+
+def test_sharded_columns_gloo_world2():
+    import multiprocessing as mp
+    import socket
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    ps = [ctx.Process(target=_shard_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in ps:
+        p.start()
+    got = q.get(timeout=120)
+    for p in ps:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    from mima_gb300 import tables
+    from oracle import oracle as orc
+    orc.load(tables.ensure_blob())
+    full = orc.rrtmg_lw(A.small_atmosphere(64, 40, seed=12))["uflx"]
+    assert np.array_equal(got, full)

@@ -1,0 +1,189 @@
+"""GPU parity: the sm_103a path through the C-ABI against the CPU oracle.
+
+Tolerances (FP64 path): fluxes within 1e-10 relative (floor 1e-3 W/m2 for
+levels where the flux vanishes, e.g. LW downward flux at the top), heating
+rates within 1e-8 K/day absolute.  FP32-split path: heating rates within
+0.05 K/day, OLR and surface fluxes within 0.1 W/m2 of the FP64 oracle.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from mima_gb300 import atmosphere as A
+from mima_gb300 import rrtmg as R
+
+pytestmark = pytest.mark.gpu
+
+FLUX_TOL = 1e-10
+HR_TOL = 1e-8
+
+
+def check_lw(out, ref, idrv=0):
+    for k in ("uflx", "dflx", "uflxc", "dflxc"):
+        assert rel_err(out[k], ref[k], 1e-3) < FLUX_TOL, k
+    for k in ("hr", "hrc"):
+        assert np.max(np.abs(out[k] - ref[k])) < HR_TOL, k
+    if idrv == 1:
+        for k in ("duflx_dt", "duflxc_dt"):
+            assert rel_err(out[k], ref[k], 1e-6) < FLUX_TOL, k
+
+
+def check_sw(out, ref):
+    for k in ("swuflx", "swdflx", "swuflxc", "swdflxc"):
+        assert rel_err(out[k], ref[k], 1e-3) < FLUX_TOL, k
+    for k in ("swhr", "swhrc"):
+        assert np.max(np.abs(out[k] - ref[k])) < HR_TOL, k
+
+
+@pytest.mark.parametrize("nlay", [40, 60])
+def test_lw_fp64_matches_oracle(gpu, orc, nlay):
+    atm = A.small_atmosphere(1024, nlay, seed=11 + nlay)
+    gpu.set_precision("fp64")
+    check_lw(gpu.lw(atm), orc.rrtmg_lw(atm))
+
+
+@pytest.mark.parametrize("nlay", [40, 60])
+def test_sw_fp64_matches_oracle(gpu, orc, nlay):
+    atm = A.small_atmosphere(1024, nlay, seed=21 + nlay)
+    gpu.set_precision("fp64")
+    check_sw(gpu.sw(atm), orc.rrtmg_sw(atm))
+
+
+def test_t42_full_grid_fp64(gpu, orc):
+    """Configuration 0 of the benchmark set: T42 x 40 layers, 8192 columns."""
+    atm = A.config_atmosphere(0)
+    gpu.set_precision("fp64")
+    check_lw(gpu.lw(atm), orc.rrtmg_lw(atm))
+    check_sw(gpu.sw(atm), orc.rrtmg_sw(atm))
+
+
+def test_lw_idrv_surface_derivative(gpu, orc):
+    atm = A.small_atmosphere(256, 40, seed=5)
+    gpu.set_precision("fp64")
+    check_lw(gpu.lw(atm, idrv=1), orc.rrtmg_lw(atm, idrv=1), idrv=1)
+
+
+def test_trace_gases_emissivity_and_aerosol(gpu, orc):
+    """All optional gases non-zero, spectral emissivity < 1, LW and SW aerosols."""
+    rng = np.random.default_rng(9)
+    atm = A.small_atmosphere(512, 40, seed=9)
+    shp = atm.play.shape
+    atm.ch4 = np.full(shp, 1.8e-6)
+    atm.n2o = np.full(shp, 3.2e-7)
+    atm.o2 = np.full(shp, 0.209)
+    atm.cfc11 = np.full(shp, 2.5e-10)
+    atm.cfc12 = np.full(shp, 5.0e-10)
+    atm.cfc22 = np.full(shp, 1.5e-10)
+    atm.ccl4 = np.full(shp, 1.0e-10)
+    atm.co2 = rng.uniform(200e-6, 1500e-6, size=shp)  # exercises the CO2 column adjustments
+    atm.emis = rng.uniform(0.85, 1.0, size=(16, atm.ncol))
+    lw_aer = rng.uniform(0.0, 0.05, size=(16, atm.nlay, atm.ncol))
+    sw_tau = rng.uniform(0.0, 0.1, size=(14, atm.nlay, atm.ncol))
+    sw_ssa = rng.uniform(0.8, 1.0, size=(14, atm.nlay, atm.ncol))
+    sw_asm = rng.uniform(0.0, 0.8, size=(14, atm.nlay, atm.ncol))
+    gpu.set_precision("fp64")
+    check_lw(gpu.lw(atm, tauaer=lw_aer), orc.rrtmg_lw(atm, tauaer=lw_aer))
+    check_sw(gpu.sw(atm, iaer=10, tauaer=sw_tau, ssaaer=sw_ssa, asmaer=sw_asm),
+             orc.rrtmg_sw(atm, iaer=10, tauaer=sw_tau, ssaaer=sw_ssa, asmaer=sw_asm))
+
+
+def test_dark_columns_and_ragged_sizes(gpu, orc):
+    gpu.set_precision("fp64")
+    for n in (1, 3, 33, 127):
+        atm = A.small_atmosphere(n, 40, seed=100 + n)
+        atm.coszen[::2] = 0.0  # MiMA skips columns with coszen < 1e-10
+        sw = gpu.sw(atm)
+        ref = orc.rrtmg_sw(atm)
+        check_sw(sw, ref)
+        assert np.all(sw["swdflx"][:, ::2] == 0.0)
+        check_lw(gpu.lw(atm), orc.rrtmg_lw(atm))
+
+
+def test_extreme_temperatures(gpu, orc):
+    """Table-index clamps (Planck 1..180, jt 1..4) at MiMA's T limits 100..370 K."""
+    atm = A.small_atmosphere(64, 40, seed=77)
+    atm.tlay[:, :16] = 100.0
+    atm.tlev[:, :16] = 100.0
+    atm.tsfc[:16] = 100.0
+    atm.tlay[:, 16:32] = 370.0
+    atm.tlev[:, 16:32] = 370.0
+    atm.tsfc[16:32] = 370.0
+    gpu.set_precision("fp64")
+    check_lw(gpu.lw(atm), orc.rrtmg_lw(atm))
+    check_sw(gpu.sw(atm), orc.rrtmg_sw(atm))
+
+
+def test_split_precision_error_budget(gpu, orc):
+    """FP32-split vs the FP64 oracle on T170-like columns (60 layers, top 0.01 hPa)."""
+    atm = A.small_atmosphere(2048, 60, seed=31, ts_sigma=5.0, rh_random=True)
+    rlw, rsw = orc.rrtmg_lw(atm), orc.rrtmg_sw(atm)
+    gpu.set_precision("split")
+    try:
+        lw, sw = gpu.lw(atm), gpu.sw(atm)
+    finally:
+        gpu.set_precision("fp64")
+    hr = np.abs(lw["hr"] - rlw["hr"]) + 0.0
+    shr = np.abs(sw["swhr"] - rsw["swhr"])
+    assert hr.max() <= 0.05, hr.max()
+    assert shr.max() <= 0.05, shr.max()
+    assert np.abs(lw["uflx"][-1] - rlw["uflx"][-1]).max() <= 0.1  # OLR
+    for k in ("uflx", "dflx"):
+        assert np.abs(lw[k][0] - rlw[k][0]).max() <= 0.1
+    for k in ("swuflx", "swdflx"):
+        assert np.abs(sw[k][0] - rsw[k][0]).max() <= 0.1
+
+
+def test_device_api_matches_host_api_and_graph_capture(gpu):
+    import torch
+    atm = A.small_atmosphere(300, 40, seed=4)
+    gpu.set_precision("fp64")
+    hlw, hsw = gpu.lw(atm), gpu.sw(atm)
+    d = R.atm_device_inputs(atm)
+    olw, osw = R.device_outputs(atm.ncol, atm.nlay)
+    s = torch.cuda.Stream()
+    gpu.reserve(atm.ncol, atm.nlay)
+    with torch.cuda.stream(s):
+        gpu.rrtmg_lw_dev(s.cuda_stream, atm.ncol, atm.nlay, 0, 0, d, olw)
+        gpu.rrtmg_sw_dev(s.cuda_stream, atm.ncol, atm.nlay, 0, 0, d, osw, atm.adjes, atm.dyofyr, atm.scon)
+    s.synchronize()
+    for k in olw:
+        assert np.array_equal(olw[k].cpu().numpy(), hlw[k]), k
+    for k in osw:
+        assert np.array_equal(osw[k].cpu().numpy(), hsw[k]), k
+    # the same two calls captured once in a CUDA graph and replayed
+    for t in list(olw.values()) + list(osw.values()):
+        t.zero_()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        gpu.rrtmg_lw_dev(s.cuda_stream, atm.ncol, atm.nlay, 0, 0, d, olw)
+        gpu.rrtmg_sw_dev(s.cuda_stream, atm.ncol, atm.nlay, 0, 0, d, osw, atm.adjes, atm.dyofyr, atm.scon)
+    g.replay()
+    torch.cuda.synchronize()
+    for k in olw:
+        assert np.array_equal(olw[k].cpu().numpy(), hlw[k]), k
+    assert gpu.sync_status(s.cuda_stream) == 0
+
+
+def test_invalid_input_and_unsupported_configurations(gpu):
+    atm = A.small_atmosphere(8, 40, seed=1)
+    atm.tlay[5, 3] = np.nan
+    out = gpu.lw(atm, check=False)
+    assert out["status"] == R.RRTMG_ERR_INPUT
+    atm = A.small_atmosphere(8, 40, seed=1)
+    o = gpu.rrtmg_lw(atm.ncol, atm.nlay, 2, 0, atm.play, atm.plev, atm.tlay, atm.tlev, atm.tsfc, atm.h2o,
+                     atm.o3, atm.co2, check=False)
+    assert o["status"] == R.RRTMG_ERR_UNSUPPORTED
+    o = gpu.rrtmg_sw(atm.ncol, atm.nlay, 0, 6, atm.play, atm.plev, atm.tlay, atm.tlev, atm.tsfc, atm.h2o,
+                     atm.o3, atm.co2, None, None, None, atm.asdir, atm.asdif, atm.aldir, atm.aldif,
+                     atm.coszen, 1.0, 0, 1360.0, check=False)
+    assert o["status"] == R.RRTMG_ERR_UNSUPPORTED
+    # a valid call after the failures still works
+    assert gpu.lw(atm)["status"] == R.RRTMG_OK
+
+
+def test_launch_count_is_native(gpu):
+    atm = A.small_atmosphere(16, 40, seed=2)
+    before = gpu.launch_count()
+    gpu.lw(atm)
+    gpu.sw(atm)
+    assert gpu.launch_count() - before == 6

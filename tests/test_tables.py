@@ -1,0 +1,127 @@
+"""Coefficient tables: Fortran data parsing, blob format, synthetic LW data,
+and the g-point reduction restated in numpy against the oracle's C++ one."""
+import numpy as np
+import pytest
+
+from mima_gb300 import tables
+
+
+def test_blob_roundtrip_and_checksum(tmp_path):
+    t = {"a.x": (np.arange(12.0).reshape(3, 4, order="F"), (1, 13)),
+         "a.n": (np.array([1, 2, 3], dtype=np.int32), (1,))}
+    p = tmp_path / "b.bin"
+    tables.write_blob(p, t)
+    back = tables.read_blob(p)
+    assert np.array_equal(back["a.x"][0], t["a.x"][0]) and back["a.x"][1] == (1, 13)
+    assert back["a.n"][0].dtype == np.int32
+    raw = bytearray(p.read_bytes())
+    raw[100] ^= 1
+    p.write_bytes(bytes(raw))
+    data = bytes(raw)
+    assert tables.blob_checksum(data[:-8]) != int.from_bytes(data[-8:], "little")
+
+
+def test_blob_contents(blob):
+    d = tables.read_blob(blob)
+    # band structure of the 140 / 112 g-point models (parrrtm.f90, parrrsw.f90)
+    assert d["lw.ngc"][0].tolist() == [10, 12, 16, 14, 16, 8, 12, 8, 12, 6, 8, 8, 4, 2, 2, 2]
+    assert d["sw.ngc"][0].tolist() == [6, 12, 8, 8, 10, 10, 2, 10, 8, 6, 6, 8, 6, 12]
+    assert d["lw.ngn"][0].sum() == 256 and d["sw.ngn"][0].sum() == 224
+    # SW absorption data fully assigned, declared shapes (rrsw_kgNN)
+    assert d["sw17.kao"][0].shape == (9, 5, 13, 16)
+    assert d["sw17.kbo"][0].shape == (5, 5, 47, 16) and d["sw17.kbo"][1] == (1, 1, 13, 1)
+    assert d["sw24.raylao"][0].shape == (16, 9)
+    for k, (a, _) in d.items():
+        if a.dtype.kind == "f":
+            assert np.all(np.isfinite(a)), k
+    assert d["lw.totplnk"][0].shape == (181, 16)
+    assert d["lw.chi_mls"][0].shape == (7, 59)
+
+
+def test_synthetic_lw_planck_fractions_sum_to_one(blob):
+    d = tables.read_blob(blob)
+    for b in range(1, 17):
+        for nm in ("fracrefao", "fracrefbo"):
+            k = f"lw{b:02d}.{nm}"
+            if k in d:
+                s = d[k][0].sum(axis=0)
+                assert np.allclose(s, 1.0, atol=1e-12), k
+    assert int(d["meta.lw_synthetic_seed"][0][0]) == tables.DEFAULT_LW_SEED
+
+
+def _np_reduce(orig, gaxis, ngc, ngn, rw, weighted):
+    a = np.moveaxis(orig, gaxis, -1)
+    out = np.zeros(a.shape[:-1] + (ngc,))
+    src = 0
+    for igc in range(ngc):
+        acc = np.zeros(a.shape[:-1])
+        for _ in range(ngn[igc]):
+            acc = acc + (a[..., src] * rw[src] if weighted else a[..., src])
+            src += 1
+        out[..., igc] = acc
+    return np.moveaxis(out, -1, gaxis)
+
+
+def _rwgt(ngc, ngn, ngm, wt):
+    rw = np.zeros(len(ngc) * 16)
+    igcsm = 0
+    for b in range(len(ngc)):
+        if ngc[b] < 16:
+            wtsm = np.zeros(16)
+            ip = 0
+            for igc in range(ngc[b]):
+                s = 0.0
+                for _ in range(ngn[igcsm]):
+                    s = s + wt[ip]
+                    ip += 1
+                wtsm[igc] = s
+                igcsm += 1
+            for ig in range(16):
+                rw[b * 16 + ig] = wt[ig] / wtsm[ngm[b * 16 + ig] - 1]
+        else:
+            rw[b * 16:(b + 1) * 16] = 1.0
+            igcsm += 16
+    return rw
+
+
+@pytest.mark.parametrize("band,name,red", [(3, "kao", "ka"), (5, "fracrefao", "fracrefa"),
+                                           (13, "kao_mco", "ka_mco"), (1, "kbo", "kb")])
+def test_lw_reduction_numpy_vs_oracle(blob, orc, band, name, red):
+    d = tables.read_blob(blob)
+    ngc, ngn, ngm = d["lw.ngc"][0], d["lw.ngn"][0], d["lw.ngm"][0]
+    rw = _rwgt(ngc, ngn, ngm, d["lw.wt"][0])
+    goff = int(ngc[:band - 1].sum())
+    orig = d[f"lw{band:02d}.{name}"][0]
+    gaxis = 0 if name.startswith("fracref") else orig.ndim - 1
+    mine = _np_reduce(orig, gaxis, int(ngc[band - 1]), ngn[goff:], rw[(band - 1) * 16:], not name.startswith("fracref"))
+    theirs = orc.table(f"lw{band:02d}", red)
+    assert np.array_equal(mine.flatten(order="F"), theirs)
+
+
+@pytest.mark.parametrize("band,name,red", [(16, "kao", "ka"), (24, "raylao", "rayla"),
+                                           (17, "sfluxrefo", "sfluxref"), (29, "absco2o", "absco2")])
+def test_sw_reduction_numpy_vs_oracle(blob, orc, band, name, red):
+    d = tables.read_blob(blob)
+    ngc, ngn, ngm = d["sw.ngc"][0], d["sw.ngn"][0], d["sw.ngm"][0]
+    rw = _rwgt(ngc, ngn, ngm, d["sw.wt"][0])
+    ib = band - 16
+    goff = int(ngc[:ib].sum())
+    orig = d[f"sw{band}.{name}"][0]
+    plain = name.startswith("sfluxref")
+    gaxis = 0 if (plain or name == "raylao") else orig.ndim - 1
+    mine = _np_reduce(orig, gaxis, int(ngc[ib]), ngn[goff:], rw[ib * 16:], not plain)
+    assert np.array_equal(mine.flatten(order="F"), orc.table(f"sw{band}", red))
+
+
+def test_kurucz_solar_source_totals(orc):
+    """The reduced SW solar source sums to RRTMG's internal solar constant,
+    rrsw_scon = 1368.22 W/m2 (parrrsw.f90), at every eta of the mixed bands."""
+    total = 0.0
+    for b in range(16, 30):
+        sf = orc.table(f"sw{b}", "sfluxref")
+        ng = [6, 12, 8, 8, 10, 10, 2, 10, 8, 6, 6, 8, 6, 12][b - 16]
+        sf = sf.reshape(ng, -1, order="F")
+        col = sf[:, 0].sum()
+        assert np.allclose(sf.sum(axis=0), col, rtol=2e-3), b
+        total += col * (50.15 / 48.37 if b == 27 else 1.0)
+    assert abs(total - 1368.22) < 1.5, total

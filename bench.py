@@ -1,0 +1,331 @@
+"""Benchmark of the GB300 RRTMG clear-sky LW+SW radiation step.
+
+Workload: MiMA's radiation call on the T85 Gaussian grid (256 x 128 = 32768
+columns, 40 layers; seeded synthetic atmospheres, synthetic LW
+k-distribution, real AER SW tables).  One step = one LW + one SW call.
+
+Default arm: the sm_103a path through the C-ABI.
+  value       FP32-split columns/s with inputs resident in HBM, the LW+SW step
+              captured once in a CUDA graph and replayed (device entry points)
+  fp64        the same for the FP64 path (the ratio split/fp64 is the metric's
+              "FP32-split vs FP64")
+  e2e         FP32-split columns/s through the host-array entry points
+              (rrtmg_lw_c / rrtmg_sw_c) from pinned host memory: H2D copies,
+              kernels, D2H copies of all outputs in every step
+  error       FP32-split vs FP64 heating-rate / OLR / surface-flux differences
+              on the timed workload
+  cpu_baseline the FP64 CPU oracle (C++ restatement of the reference) on the
+              host cores, bounded sample
+--impl reference: the CPU restatement alone, all host threads, same workload.
+
+L2 (126 MB) is flushed before every timed step by writing a 256 MB buffer on
+the same stream, outside the CUDA-event interval of the step.
+Multi-GPU (torchrun): each rank runs its own T85 ensemble member (weak
+scaling, no collective on the data path); barrier + max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "RRTMG LW+SW columns/s at T85×40L: FP32-split vs FP64 on GB300 at ≤0.05 K/day"
+UNIT = "columns/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", type=int, default=1, help="workload configuration index (1 = T85x40)")
+    ap.add_argument("--cpu-sample", type=int, default=2048, help="columns per CPU baseline step")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return json.loads(p.read_text()), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def algorithmic_bytes(atm, lw_in, sw_in):
+    """Bytes one LW+SW step must move at minimum: every input array read once,
+    every output array written once (FP64)."""
+    n = atm.ncol
+    L = atm.nlay
+    nin = sum(v.numel() for v in lw_in.values()) + sum(v.numel() for k, v in sw_in.items() if k not in lw_in)
+    nout = n * (8 * (L + 1) + 4 * L)
+    return 8 * (nin + nout)
+
+
+def cpu_baseline(atm_full, sample, steps=1):
+    """FP64 oracle (C++ restatement of the reference) on the host cores."""
+    from mima_gb300 import tables
+    from oracle import oracle as orc
+    orc.load(tables.ensure_blob())
+    orc.set_table_mode(True)
+    idx = np.linspace(0, atm_full.ncol - 1, min(sample, atm_full.ncol)).astype(int)
+    sub = atm_full.subset(idx)
+    threads = orc.max_threads()
+    orc.rrtmg_lw(sub.subset(np.arange(min(64, sub.ncol))))  # warm
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        orc.rrtmg_lw(sub, nthreads=threads)
+        orc.rrtmg_sw(sub, nthreads=threads)
+        times.append(time.perf_counter() - t0)
+    return sub.ncol / float(np.median(times)), threads, sub.ncol, times
+
+
+def run_reference(args):
+    from mima_gb300 import atmosphere
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    atm = atmosphere.config_atmosphere(args.config)
+    warm = max(1, min(args.warmup, 3))
+    cpu_baseline(atm, min(args.cpu_sample, 256), steps=warm)
+    value, threads, nsample, times = cpu_baseline(atm, args.cpu_sample, steps=args.steps)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * float(np.median(times)),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded T85 atmospheres; synthetic LW k-distribution, AER SW tables)",
+        "config": {"workload": f"T85x40 LW+SW clear sky, {nsample}-column sample of {atm.ncol} per step"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{nsample} of {atm.ncol} T85 columns, LW+SW, FP64 lookup-table path"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "reference Fortran not buildable here (no Fortran compiler); C++ FP64 restatement timed",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def graph_step(torch, r, stream, atm, d, olw, osw, precision):
+    """Capture one LW+SW step (device entry points) in a CUDA graph."""
+    r.set_precision(precision)
+    call = lambda: (r.rrtmg_lw_dev(stream.cuda_stream, atm.ncol, atm.nlay, 0, 0, d, olw),
+                    r.rrtmg_sw_dev(stream.cuda_stream, atm.ncol, atm.nlay, 0, 0, d, osw, atm.adjes,
+                                   atm.dyofyr, atm.scon))
+    with torch.cuda.stream(stream):
+        call()  # first call outside capture (workspace already reserved)
+    stream.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=stream):
+        call()
+    return g
+
+
+def time_graph(torch, g, stream, flush, steps, warmup):
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            g.replay()
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for e0, e1 in evs:
+        with torch.cuda.stream(stream):
+            flush.add_(1.0)  # 256 MB write: evicts L2 between timed steps
+            e0.record(stream)
+            g.replay()
+            e1.record(stream)
+    torch.cuda.synchronize()
+    return [e0.elapsed_time(e1) for e0, e1 in evs]
+
+
+def run_ours(args):
+    import torch
+    from mima_gb300 import atmosphere, rrtmg
+    from mima_gb300.shard import env_rank_world
+
+    rank, world, local = env_rank_world()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    atm = atmosphere.config_atmosphere(args.config, member=rank)
+    r = rrtmg.RRTMG(device=local)
+    r.reserve(atm.ncol, atm.nlay)
+    d = rrtmg.atm_device_inputs(atm, dev)
+    lw_keys = ("play", "plev", "tlay", "tlev", "tsfc", "h2ovmr", "o3vmr", "co2vmr", "ch4vmr", "n2ovmr", "o2vmr",
+               "cfc11vmr", "cfc12vmr", "cfc22vmr", "ccl4vmr", "emis")
+    sw_keys = ("play", "plev", "tlay", "tlev", "tsfc", "h2ovmr", "o3vmr", "co2vmr", "ch4vmr", "n2ovmr", "o2vmr",
+               "asdir", "asdif", "aldir", "aldif", "coszen")
+    nbytes = algorithmic_bytes(atm, {k: d[k] for k in lw_keys}, {k: d[k] for k in sw_keys})
+    olw64, osw64 = rrtmg.device_outputs(atm.ncol, atm.nlay, dev)
+    olw32, osw32 = rrtmg.device_outputs(atm.ncol, atm.nlay, dev)
+    stream = torch.cuda.Stream(device=dev)
+    flush = torch.zeros(32 * 1024 * 1024, dtype=torch.float64, device=dev)
+    g64 = graph_step(torch, r, stream, atm, d, olw64, osw64, "fp64")
+    g32 = graph_step(torch, r, stream, atm, d, olw32, osw32, "split")
+
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = r.launch_count()
+    with ClockSampler(local) as clk:
+        t32 = time_graph(torch, g32, stream, flush, args.steps, args.warmup)
+        t64 = time_graph(torch, g64, stream, flush, max(3, args.steps // 4), min(args.warmup, 3))
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    # graph replays re-run the captured kernels: 6 launches of ours per step
+    launches = 6 * args.steps
+    ms32 = float(np.mean(t32))
+    ms64 = float(np.mean(t64))
+    if dist:
+        m = torch.tensor([ms32, ms64], device=dev)
+        dist.all_reduce(m, op=dist.ReduceOp.MAX)
+        ms32, ms64 = m.tolist()
+
+    # FP32-split error against FP64 on the timed workload
+    hr = (olw32["hr"] - olw64["hr"]).abs()
+    shr = (osw32["swhr"] - osw64["swhr"]).abs()
+    olr = (olw32["uflx"][-1] - olw64["uflx"][-1]).abs()
+    sfc = max(float((olw32[k][0] - olw64[k][0]).abs().max()) for k in ("uflx", "dflx"))
+    sfc = max(sfc, max(float((osw32[k][0] - osw64[k][0]).abs().max()) for k in ("swuflx", "swdflx")))
+    err = {"lw_hr_max_kday": float(hr.max()), "lw_hr_rms_kday": float(hr.pow(2).mean().sqrt()),
+           "sw_hr_max_kday": float(shr.max()), "sw_hr_rms_kday": float(shr.pow(2).mean().sqrt()),
+           "olr_max_wm2": float(olr.max()), "sfc_flux_max_wm2": sfc}
+
+    ncol_total = atm.ncol * world
+    value = ncol_total / (ms32 * 1e-3)
+    fp64_value = ncol_total / (ms64 * 1e-3)
+
+    # end to end through the host-array entry points, pinned host memory
+    e2e = None
+    if not args.no_e2e:
+        r.set_precision("split")
+        pin = {}
+        for k, v in d.items():
+            pin[k] = v.cpu().pin_memory()
+        hp = lambda k: pin[k].numpy()
+        h2d = sum(pin[k].numel() * 8 for k in set(lw_keys) | set(sw_keys))
+        d2h = 8 * atm.ncol * (8 * (atm.nlay + 1) + 4 * atm.nlay)
+        def host_step():
+            r.rrtmg_lw(atm.ncol, atm.nlay, 0, 0, *[hp(k) for k in lw_keys])
+            r.rrtmg_sw(atm.ncol, atm.nlay, 0, 0, *[hp(k) for k in sw_keys], atm.adjes, atm.dyofyr, atm.scon)
+        for _ in range(max(2, min(args.warmup, 3))):
+            host_step()
+        ts = []
+        for _ in range(max(3, args.steps // 4)):
+            t0 = time.perf_counter()
+            host_step()
+            ts.append(time.perf_counter() - t0)
+        e2e = {"value": atm.ncol * world / float(np.mean(ts)), "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "api": "rrtmg_lw_c + rrtmg_sw_c (host arrays), FP32-split"}
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+    cpu_value, threads, nsample, _ = cpu_baseline(atm, min(args.cpu_sample, 2048), steps=1)
+    peaks, src = measured_peaks()
+    achieved = nbytes / (ms32 * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64 (FP32-split)",
+        "data": "synthetic (seeded T85 atmospheres; synthetic LW k-distribution, AER SW tables)",
+        "config": {"workload": f"T85x40 (256x128 = {atm.ncol} columns, 40 layers) LW+SW clear sky per GPU",
+                   "per_gpu_columns": atm.ncol, "l2": "flushed (256 MB write) before every timed step",
+                   "graph": "LW+SW step captured in one CUDA graph", "parallelism": f"columns x{world}"},
+        "fp64": {"value": fp64_value, "unit": UNIT, "ms_per_step": ms64},
+        "split_over_fp64": fp64_value and value / fp64_value,
+        "error_vs_fp64": err,
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+                     "note": f"algorithmic bytes {nbytes} per step; peak {src}; the path is compute/latency bound"},
+        "cpu_baseline": {"value": cpu_value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{nsample} of {atm.ncol} T85 columns, LW+SW FP64 C++ restatement"},
+    }
+    if e2e:
+        line["e2e"] = e2e
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -261,6 +261,9 @@ __device__ __forceinline__ void lw_band(const LwPrep& p, const double* __restric
   R radld = (R)0., fracs1 = (R)0.;
   double* bdp = bd + (size_t)(B - 1) * (nlay + 1) * N + col;
   double* bup = bu + (size_t)(B - 1) * (nlay + 1) * N + col;
+  // No downward radiance enters at the top (drad(nlayers) stays 0,
+  // rrtmg_lw_rtrnmr.f90:290-300).
+  if (g == 0 && valid) bdp[(size_t)nlay * N] = 0.0;
   for (int lev = nlay; lev >= 1; --lev) {
     const size_t o = (size_t)(lev - 1) * N + c;
     const Idx ix = unpack_idx(__ldg(p.idx + o));
@@ -283,7 +286,8 @@ __device__ __forceinline__ void lw_band(const LwPrep& p, const double* __restric
       bbu = plfrac * (blay + dplankup * odepth);
     } else {
       const R tblind = odepth / (bpade + odepth);
-      const int itr = (int)((R)10000.0 * tblind + (R)0.5);
+      int itr = (int)((R)10000.0 * tblind + (R)0.5);
+      itr = itr < 0 ? 0 : (itr > kNTbl ? kNTbl : itr);  // in range for any odepth >= 0; guards NaN input
       const R transc = __ldg(exptbl + itr);
       atr = (R)1. - transc;
       const R tausfac = __ldg(tfntbl + itr);
@@ -560,7 +564,8 @@ template <class R>
 __device__ __forceinline__ R sw_exp_tbl(R ze1, R bpade, const R* __restrict__ exptbl) {
   if (ze1 <= (R)0.06) return (R)1. - ze1 + (R)0.5 * ze1 * ze1;
   const R tblind = ze1 / (bpade + ze1);
-  const int itind = (int)((R)10000.0 * tblind + (R)0.5);
+  int itind = (int)((R)10000.0 * tblind + (R)0.5);
+  itind = itind < 0 ? 0 : (itind > kNTbl ? kNTbl : itind);  // guards NaN / negative optical depths
   return __ldg(exptbl + itind);
 }
 
@@ -634,6 +639,90 @@ __device__ __forceinline__ void reftra1(R zto1, R zw, R zg, R prmuz, R bpade, co
   }
 }
 
+// exp(-x) from the SW table / series together with exp(-x) - 1, the latter
+// formed without cancellation (series: -x + x^2/2; table: tbl - 1).
+__device__ __forceinline__ void sw_exp_pair(float ze1, float bpade, const float* __restrict__ exptbl, float& e,
+                                            float& em1) {
+  if (ze1 <= 0.06f) {
+    em1 = -ze1 + 0.5f * ze1 * ze1;
+    e = 1.f - ze1 + 0.5f * ze1 * ze1;
+    return;
+  }
+  const float tblind = ze1 / (bpade + ze1);
+  int itind = (int)(10000.0f * tblind + 0.5f);
+  itind = itind < 0 ? 0 : (itind > kNTbl ? kNTbl : itind);
+  e = __ldg(exptbl + itind);
+  em1 = e - 1.f;
+}
+
+// FP32 delta-Eddington layer solution (same model as reftra1, kmodts = 2),
+// rearranged so that no O(1) terms cancel for optically thin or nearly
+// conservative layers, where FP32 would otherwise lose the layer absorptance:
+//   * the numerators zr1 e^{kt} - zr2 e^{-kt} - zr3 e^{-t/mu} (and the zt
+//     analogue) have zr1 - zr2 - zr3 = 0, so they are evaluated on the
+//     complements e - 1;
+//   * k = sqrt(g1^2 - g2^2) = sqrt(2 (1 - w) (g1 + g2)) since g1 - g2 = 2(1 - w);
+//   * (1 - beta e^{-2kt}) (k + g1) = 2k + (g1 - k)(1 - e^{-2kt});
+//   * zr4 e^{kt} + zr5 e^{-kt} = zrpp (k (e^{kt} + e^{-kt}) + g1 (e^{kt} - e^{-kt})).
+// Exponentials are the same table / series values as the reference uses.
+__device__ __forceinline__ void reftra_split(float zto1, float zw, float zg, float prmuz, float bpade,
+                                             const float* __restrict__ exptbl, float& pref, float& prefd,
+                                             float& ptra, float& ptrad) {
+  const float eps = 1.e-08f, zwcrit = 0.9999995f;
+  const float zg3 = 3.f * zg;
+  const float zgamma1 = (8.f - zw * (5.f + zg3)) * 0.25f;
+  const float zgamma2 = 3.f * (zw * (1.f - zg)) * 0.25f;
+  const float zgamma3 = (2.f - zg3 * prmuz) * 0.25f;
+  const float zgamma4 = 1.f - zgamma3;
+  const float r = zg / (1.f - zg);
+  const float zwo = zw / (1.f - (1.f - zw) * (r * r));
+  if (zwo >= zwcrit) {
+    const float za1 = zgamma1 * prmuz - zgamma3;
+    const float zgt = zgamma1 * zto1;
+    float ze2, m2;
+    sw_exp_pair(fminf(zto1 / prmuz, 500.f), bpade, exptbl, ze2, m2);
+    pref = (zgt + za1 * m2) / (1.f + zgt);
+    ptra = 1.f - pref;
+    prefd = zgt / (1.f + zgt);
+    ptrad = 1.f - prefd;
+    if (m2 == 0.f) {
+      pref = 0.f;
+      ptra = 1.f;
+      prefd = 0.f;
+      ptrad = 1.f;
+    }
+  } else {
+    const float za1 = zgamma1 * zgamma4 + zgamma2 * zgamma3;
+    const float za2 = zgamma1 * zgamma3 + zgamma2 * zgamma4;
+    const float zrk = sqrtf((2.f * (1.f - zw)) * (zgamma1 + zgamma2));
+    const float zrp = zrk * prmuz;
+    const float zrp1 = 1.f + zrp, zrm1 = 1.f - zrp, zrk2 = 2.f * zrk, zrpp = 1.f - zrp * zrp;
+    const float zr1 = zrm1 * (za2 + zrk * zgamma3);
+    const float zr2 = zrp1 * (za2 - zrk * zgamma3);
+    const float zr3 = zrk2 * (zgamma3 - za2 * prmuz);
+    const float zt1 = zrp1 * (za1 + zrk * zgamma4);
+    const float zt2 = zrm1 * (za1 - zrk * zgamma4);
+    const float zt3 = zrk2 * (zgamma4 + za1 * prmuz);
+    float zem1, m1, zem2, m2;
+    sw_exp_pair(fminf(zrk * zto1, 500.f), bpade, exptbl, zem1, m1);
+    sw_exp_pair(fminf(zto1 / prmuz, 500.f), bpade, exptbl, zem2, m2);
+    const float zep1 = 1.f / zem1, zep2 = 1.f / zem2;
+    const float p1 = -m1 * zep1, p2 = -m2 * zep2;  // e^{kt} - 1, e^{t/mu} - 1
+    const float zden = zrpp * (zrk * (zep1 + zem1) + zgamma1 * (p1 - m1));
+    if (zden >= -eps && zden <= eps) {
+      pref = eps;
+      ptra = zem2;
+    } else {
+      pref = zw * (zr1 * p1 - zr2 * m1 - zr3 * m2) / zden;
+      ptra = zem2 - zem2 * zw * (zt1 * p1 - zt2 * m1 - zt3 * p2) / zden;
+    }
+    const float omm = -m1 * (2.f + m1);  // 1 - e^{-2kt}
+    const float zdend = 1.f / (zrk2 + (zgamma1 - zrk) * omm);
+    prefd = zgamma2 * omm * zdend;
+    ptrad = zrk2 * zem1 * zdend;
+  }
+}
+
 template <int B, class R, int MAXL>
 __device__ __forceinline__ void sw_band(const SwPrep& p, const SwIn& in, double adjflux, int iaer,
                                         const R* __restrict__ tab, const double* __restrict__ tab64,
@@ -699,7 +788,10 @@ __device__ __forceinline__ void sw_band(const SwPrep& p, const SwIn& in, double 
     zomcc = (zomcc - zwf) / ((R)1.0 - zwf);
     zgcc = (zgcc - zf) / ((R)1.0 - zf);
     R rf, rfd, tr, trd;
-    reftra1<R>(ztauc, zomcc, zgcc, prmu0, bpade, exptbl, rf, rfd, tr, trd);
+    if constexpr (sizeof(R) == 4)
+      reftra_split(ztauc, zomcc, zgcc, prmu0, bpade, exptbl, rf, rfd, tr, trd);
+    else
+      reftra1<R>(ztauc, zomcc, zgcc, prmu0, bpade, exptbl, rf, rfd, tr, trd);
     pref[jk - 1] = rf;
     prefd[jk - 1] = rfd;
     ptra[jk - 1] = tr;

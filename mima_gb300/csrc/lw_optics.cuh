@@ -46,8 +46,13 @@ __device__ __forceinline__ EtaV<R> eta_mix(R a, R ratb, R b, R mult, R oneminus)
   if (e.specparm >= oneminus) e.specparm = oneminus;
   R specmult = mult * (e.specparm);
   int ip = (int)specmult;
-  e.js = 1 + ip;
   e.fs = specmult - (R)ip;  // mod(specmult, 1) for specmult >= 0
+  // For valid inputs 0 <= specparm <= oneminus, so 0 <= ip < mult; the clamp
+  // only keeps table reads in bounds for non-finite or negative inputs (which
+  // the prep kernels flag as invalid).
+  const int top = (int)mult - 1;
+  ip = ip < 0 ? 0 : (ip > top ? top : ip);
+  e.js = 1 + ip;
   return e;
 }
 

@@ -144,6 +144,33 @@ int rrtmg_gpu_reserve(rrtmg_gpu_handle h, int ncol, int nlay);
  * invalid input (the flag is then cleared). */
 int rrtmg_gpu_sync_status(rrtmg_gpu_handle h, void* stream);
 
+/* Size of the library's static LW device scratch (64 MiB), held by every GPU
+ * that loads the library until process exit.  At nlay = 40 a call needs about
+ * 34.7 KB per column, so up to about 1900 columns fit; at nlay = 60, about 1300. */
+#define RRTMG_GPU_STATIC_SCRATCH_BYTES (64u * 1024u * 1024u)
+
+/* No counterpart in the reference.  Same arguments and results as
+ * rrtmg_lw_dev, but the call allocates nothing: its scratch is the library's
+ * static device array of RRTMG_GPU_STATIC_SCRATCH_BYTES, not the handle's
+ * workspace (no cudaMalloc or cudaFree, no allocating library routine).
+ * A call whose (ncol, nlay) needs more scratch than that returns
+ * RRTMG_ERR_ARG with the byte counts in rrtmg_gpu_last_error().  The first call
+ * on a device looks up the array's device address (cudaGetSymbolAddress) with
+ * that device current; make that first call before any stream capture.  All
+ * calls on a device share the one array and it keeps the last call's
+ * contents, so calls that overlap on the GPU (different streams, or different
+ * handles on one device) race: order them on one stream or with events. */
+int rrtmg_lw_dev_static(rrtmg_gpu_handle h, void* stream, int ncol, int nlay, int icld, int idrv,
+                        const double* play, const double* plev, const double* tlay, const double* tlev,
+                        const double* tsfc, const double* h2ovmr, const double* o3vmr, const double* co2vmr,
+                        const double* ch4vmr, const double* n2ovmr, const double* o2vmr,
+                        const double* cfc11vmr, const double* cfc12vmr, const double* cfc22vmr,
+                        const double* ccl4vmr, const double* emis, int inflglw, int iceflglw, int liqflglw,
+                        const double* cldfr, const double* taucld, const double* cicewp, const double* cliqwp,
+                        const double* reice, const double* reliq, const double* tauaer,
+                        double* uflx, double* dflx, double* hr, double* uflxc, double* dflxc, double* hrc,
+                        double* duflx_dt, double* duflxc_dt);
+
 #ifdef __cplusplus
 }
 #endif

@@ -500,3 +500,100 @@ int rrtmg_sw_c(rrtmg_gpu_handle h, int ncol, int nlay, int icld, int iaer, const
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free LW device call (rrtmg_lw_dev_static).
+//
+// The LW scratch (per-layer optics, Planck terms, band partial fluxes) lives in
+// one file-scope device array of RRTMG_GPU_STATIC_SCRATCH_BYTES that every
+// device loading this library holds until process exit.  In host code
+// `g_lw_static_scratch` is only a stand-in for the symbol; its device address
+// is looked up once per device with cudaGetSymbolAddress, with that device
+// current, on the first call made on that device.  Every scratch word a call
+// reads is written earlier by the same call (prep writes all per-layer fields,
+// the g-point kernel writes every level of every band partial, including the
+// zero downward flux at the top), so no clearing is needed; the validation
+// flag word is the handle's.  All calls on a device share the array, so calls
+// that overlap on the GPU race.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+static __device__ __align__(256) unsigned char g_lw_static_scratch[RRTMG_GPU_STATIC_SCRATCH_BYTES];
+
+namespace {
+
+constexpr int kMaxStaticDevices = 64;
+std::mutex g_static_mu;
+void* g_static_ptr[kMaxStaticDevices] = {};
+
+// Device address of g_lw_static_scratch on `device` (current), looked up once.
+cudaError_t static_scratch(int device, void** out) {
+  std::lock_guard<std::mutex> lock(g_static_mu);
+  if (!g_static_ptr[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_lw_static_scratch);
+    if (e != cudaSuccess) return e;
+    g_static_ptr[device] = p;
+  }
+  *out = g_static_ptr[device];
+  return cudaSuccess;
+}
+
+}  // namespace
+
+extern "C" int rrtmg_lw_dev_static(rrtmg_gpu_handle h, void* stream, int ncol, int nlay, int icld, int idrv,
+                                   const double* play, const double* plev, const double* tlay, const double* tlev,
+                                   const double* tsfc, const double* h2ovmr, const double* o3vmr,
+                                   const double* co2vmr, const double* ch4vmr, const double* n2ovmr,
+                                   const double* o2vmr, const double* cfc11vmr, const double* cfc12vmr,
+                                   const double* cfc22vmr, const double* ccl4vmr, const double* emis, int inflglw,
+                                   int iceflglw, int liqflglw, const double* cldfr, const double* taucld,
+                                   const double* cicewp, const double* cliqwp, const double* reice,
+                                   const double* reliq, const double* tauaer, double* uflx, double* dflx,
+                                   double* hr, double* uflxc, double* dflxc, double* hrc, double* duflx_dt,
+                                   double* duflxc_dt) {
+  (void)inflglw; (void)iceflglw; (void)liqflglw; (void)cldfr; (void)taucld; (void)cicewp; (void)cliqwp;
+  (void)reice; (void)reliq;
+  if (!valid_handle(h)) return RRTMG_ERR_ARG;
+  int rc = check_dims(h, ncol, nlay);
+  if (rc) return rc;
+  if (icld != 0) return fail(h, RRTMG_ERR_UNSUPPORTED, "only clear sky (icld = 0) is computed");
+  if (idrv != 0 && idrv != 1) return fail(h, RRTMG_ERR_UNSUPPORTED, "idrv must be 0 or 1");
+  if (!play || !plev || !tlay || !tlev || !tsfc || !h2ovmr || !o3vmr || !co2vmr || !uflx || !dflx || !hr ||
+      !uflxc || !dflxc || !hrc)
+    return fail(h, RRTMG_ERR_ARG, "a required array pointer is null");
+  if (idrv == 1 && !duflx_dt) return fail(h, RRTMG_ERR_ARG, "idrv = 1 needs duflx_dt");
+  size_t need;
+  carve_lw(nullptr, ncol, nlay, &need);
+  if (need > (size_t)RRTMG_GPU_STATIC_SCRATCH_BYTES)
+    return fail(h, RRTMG_ERR_ARG,
+                "rrtmg_lw_dev_static: " + std::to_string(ncol) + " columns x " + std::to_string(nlay) +
+                    " layers need " + std::to_string(need) + " bytes of scratch, more than the static limit of " +
+                    std::to_string((size_t)RRTMG_GPU_STATIC_SCRATCH_BYTES) + " bytes; split the columns");
+  if (h->device < 0 || h->device >= kMaxStaticDevices)
+    return fail(h, RRTMG_ERR_ARG, "rrtmg_lw_dev_static: device ordinal out of range");
+  cudaError_t e = cudaSetDevice(h->device);
+  if (e != cudaSuccess) return cuda_fail(h, e, "rrtmg_lw_dev_static: set device");
+  void* base = nullptr;
+  e = static_scratch(h->device, &base);
+  if (e != cudaSuccess) return cuda_fail(h, e, "rrtmg_lw_dev_static: cudaGetSymbolAddress");
+  cudaStream_t s = (cudaStream_t)stream;
+  LwIn in{play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr, cfc11vmr, cfc12vmr,
+          cfc22vmr, ccl4vmr, emis, tauaer};
+  LwWork w = carve_lw(base, ncol, nlay, nullptr);
+  launch_lw_prep(in, w, h->totplnk, h->totplnkderiv, ncol, nlay, idrv, h->flags, s);
+  LwPrep p{w.idx, w.f, w.planklay, w.planklev, w.plankbnd, w.dplankbnd, w.secdiff, w.laytrop};
+  const int nb = lw_gpoint_blocks(h->host.lw, ncol);
+  if (h->precision == RRTMG_PREC_SPLIT)
+    launch_lw_gpoint_split(p, in.emis, in.tauaer, h->lw_tab32, h->lw_exp32, h->lw_tfn32, w.bu, w.bd, w.bdu, ncol,
+                           nlay, idrv, nb, s);
+  else
+    launch_lw_gpoint_fp64(p, in.emis, in.tauaer, h->lw_tab64, h->lw_exp64, h->lw_tfn64, w.bu, w.bd, w.bdu, ncol, nlay,
+                          idrv, nb, s);
+  launch_lw_finalize(w.bu, w.bd, w.bdu, in.plev, ncol, nlay, idrv, uflx, dflx, hr, uflxc, dflxc, hrc, duflx_dt,
+                     duflxc_dt, s);
+  h->launches += 3;
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(h, e, "rrtmg_lw_dev_static: kernel launch");
+  return RRTMG_OK;
+}

@@ -32,11 +32,12 @@ RRTMG_ERR_TABLES = 4
 RRTMG_ERR_INPUT = 5
 RRTMG_ERR_NOMEM = 6
 PREC = {"fp64": 0, "split": 1}
+STATIC_SCRATCH_BYTES = 64 * 1024 * 1024  # RRTMG_GPU_STATIC_SCRATCH_BYTES
 
 # Every symbol include/rrtmg_gpu.h declares.
 EXPORTED = ("rrtmg_gpu_init", "rrtmg_gpu_finalize", "rrtmg_gpu_set_precision", "rrtmg_gpu_error_string",
             "rrtmg_gpu_last_error", "rrtmg_gpu_launch_count", "rrtmg_lw_c", "rrtmg_sw_c", "rrtmg_lw_dev",
-            "rrtmg_sw_dev", "rrtmg_gpu_reserve", "rrtmg_gpu_sync_status")
+            "rrtmg_sw_dev", "rrtmg_gpu_reserve", "rrtmg_gpu_sync_status", "rrtmg_lw_dev_static")
 
 _lib = None
 _dp = C.POINTER(C.c_double)
@@ -197,6 +198,19 @@ class RRTMG:
         g = lambda k: _dptr(d.get(k))
         o = lambda k: _dptr(out.get(k))
         rc = self.lib.rrtmg_lw_dev(
+            self._h, C.c_void_p(stream or 0), C.c_int(ncol), C.c_int(nlay), C.c_int(icld), C.c_int(idrv),
+            g("play"), g("plev"), g("tlay"), g("tlev"), g("tsfc"), g("h2ovmr"), g("o3vmr"), g("co2vmr"),
+            g("ch4vmr"), g("n2ovmr"), g("o2vmr"), g("cfc11vmr"), g("cfc12vmr"), g("cfc22vmr"), g("ccl4vmr"),
+            g("emis"), C.c_int(0), C.c_int(0), C.c_int(0), None, None, None, None, None, None, _dptr(tauaer),
+            o("uflx"), o("dflx"), o("hr"), o("uflxc"), o("dflxc"), o("hrc"), o("duflx_dt"), o("duflxc_dt"))
+        self._check(rc)
+
+    def rrtmg_lw_dev_static(self, stream, ncol, nlay, icld, idrv, d, out, tauaer=None):
+        """As :meth:`rrtmg_lw_dev`, through the allocation-free entry point
+        (scratch in the library's static device array)."""
+        g = lambda k: _dptr(d.get(k))
+        o = lambda k: _dptr(out.get(k))
+        rc = self.lib.rrtmg_lw_dev_static(
             self._h, C.c_void_p(stream or 0), C.c_int(ncol), C.c_int(nlay), C.c_int(icld), C.c_int(idrv),
             g("play"), g("plev"), g("tlay"), g("tlev"), g("tsfc"), g("h2ovmr"), g("o3vmr"), g("co2vmr"),
             g("ch4vmr"), g("n2ovmr"), g("o2vmr"), g("cfc11vmr"), g("cfc12vmr"), g("cfc22vmr"), g("ccl4vmr"),

@@ -142,31 +142,59 @@ int check_dims(rrtmg_gpu_state* h, int ncol, int nlay) {
   return RRTMG_OK;
 }
 
+// The split path stores the per-layer fields as float in the same carving.
+template <class F>
+LwWorkT<F> work_as(const LwWork& w) {
+  return LwWorkT<F>{w.idx, (F*)w.f, (F*)w.planklay, (F*)w.planklev, (F*)w.plankbnd, (F*)w.dplankbnd, (F*)w.secdiff,
+                    w.laytrop, w.bu, w.bd, w.bdu};
+}
+template <class F>
+SwWorkT<F> work_as(const SwWork& w) {
+  return SwWorkT<F>{w.idx, (F*)w.f, w.laytrop, w.laysolfr, w.su, w.sd};
+}
+template <class F>
+LwPrepT<F> prep_of(const LwWorkT<F>& w) {
+  return LwPrepT<F>{w.idx, w.f, w.planklay, w.planklev, w.plankbnd, w.dplankbnd, w.secdiff, w.laytrop};
+}
+template <class F>
+SwPrepT<F> prep_of(const SwWorkT<F>& w) {
+  return SwPrepT<F>{w.idx, w.f, w.laytrop, w.laysolfr};
+}
+
 // ---------------------------------------------------------------------------
-// Enqueue one LW radiation call on stream s (all pointers on the device).
+// Enqueue one LW radiation call on stream s (all pointers on the device) with
+// its scratch carved from `base` (carve_lw bytes).
 // ---------------------------------------------------------------------------
-int lw_run(rrtmg_gpu_state* h, cudaStream_t s, int ncol, int nlay, int idrv, const LwIn& in, double* uflx,
-           double* dflx, double* hr, double* uflxc, double* dflxc, double* hrc, double* duflx_dt, double* duflxc_dt) {
-  size_t need;
-  carve_lw(nullptr, ncol, nlay, &need);
-  int rc = ensure(h, h->lw_ws, need, s);
-  if (rc) return rc;
-  LwWork w = carve_lw(h->lw_ws.p, ncol, nlay, nullptr);
-  launch_lw_prep(in, w, h->totplnk, h->totplnkderiv, ncol, nlay, idrv, h->flags, s);
-  LwPrep p{w.idx, w.f, w.planklay, w.planklev, w.plankbnd, w.dplankbnd, w.secdiff, w.laytrop};
+int lw_enqueue(rrtmg_gpu_state* h, cudaStream_t s, void* base, int ncol, int nlay, int idrv, const LwIn& in,
+               double* uflx, double* dflx, double* hr, double* uflxc, double* dflxc, double* hrc, double* duflx_dt,
+               double* duflxc_dt) {
+  LwWork w = carve_lw(base, ncol, nlay, nullptr);
   const int nb = lw_gpoint_blocks(h->host.lw, ncol);
-  if (h->precision == RRTMG_PREC_SPLIT)
-    launch_lw_gpoint_split(p, in.emis, in.tauaer, h->lw_tab32, h->lw_exp32, h->lw_tfn32, w.bu, w.bd, w.bdu, ncol,
-                           nlay, idrv, nb, s);
-  else
-    launch_lw_gpoint_fp64(p, in.emis, in.tauaer, h->lw_tab64, h->lw_exp64, h->lw_tfn64, w.bu, w.bd, w.bdu, ncol, nlay,
-                          idrv, nb, s);
+  if (h->precision == RRTMG_PREC_SPLIT) {
+    const LwWorkT<float> w32 = work_as<float>(w);
+    launch_lw_prep_split(in, w32, h->totplnk, h->totplnkderiv, ncol, nlay, idrv, h->flags, s);
+    launch_lw_gpoint_split(prep_of(w32), in.emis, in.tauaer, h->lw_tab32, h->lw_exp32, h->lw_tfn32, w.bu, w.bd,
+                           w.bdu, ncol, nlay, idrv, nb, s);
+  } else {
+    launch_lw_prep(in, w, h->totplnk, h->totplnkderiv, ncol, nlay, idrv, h->flags, s);
+    launch_lw_gpoint_fp64(prep_of(w), in.emis, in.tauaer, h->lw_tab64, h->lw_exp64, h->lw_tfn64, w.bu, w.bd, w.bdu,
+                          ncol, nlay, idrv, nb, s);
+  }
   launch_lw_finalize(w.bu, w.bd, w.bdu, in.plev, ncol, nlay, idrv, uflx, dflx, hr, uflxc, dflxc, hrc, duflx_dt,
                      duflxc_dt, s);
   h->launches += 3;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(h, e, "LW kernel launch");
   return RRTMG_OK;
+}
+
+int lw_run(rrtmg_gpu_state* h, cudaStream_t s, int ncol, int nlay, int idrv, const LwIn& in, double* uflx,
+           double* dflx, double* hr, double* uflxc, double* dflxc, double* hrc, double* duflx_dt, double* duflxc_dt) {
+  size_t need;
+  carve_lw(nullptr, ncol, nlay, &need);
+  int rc = ensure(h, h->lw_ws, need, s);
+  if (rc) return rc;
+  return lw_enqueue(h, s, h->lw_ws.p, ncol, nlay, idrv, in, uflx, dflx, hr, uflxc, dflxc, hrc, duflx_dt, duflxc_dt);
 }
 
 int sw_run(rrtmg_gpu_state* h, cudaStream_t s, int ncol, int nlay, int iaer, double adjes, int dyofyr, double scon,
@@ -186,13 +214,16 @@ int sw_run(rrtmg_gpu_state* h, cudaStream_t s, int ncol, int nlay, int iaer, dou
              .000077 * std::sin(2. * gamma);
   }
   const double adjflux = adjflx * (scon / 1.36822e+03);
-  launch_sw_prep(in, w, ncol, nlay, h->flags, s);
-  SwPrep p{w.idx, w.f, w.laytrop, w.laysolfr};
   const int nb = sw_gpoint_blocks(h->host.sw, ncol);
-  if (h->precision == RRTMG_PREC_SPLIT)
-    launch_sw_gpoint_split(p, in, adjflux, iaer, h->sw_tab32, h->sw_tab64, h->sw_exp32, w.su, w.sd, ncol, nlay, nb, s);
-  else
-    launch_sw_gpoint_fp64(p, in, adjflux, iaer, h->sw_tab64, h->sw_exp64, w.su, w.sd, ncol, nlay, nb, s);
+  if (h->precision == RRTMG_PREC_SPLIT) {
+    const SwWorkT<float> w32 = work_as<float>(w);
+    launch_sw_prep_split(in, w32, ncol, nlay, h->flags, s);
+    launch_sw_gpoint_split(prep_of(w32), in, adjflux, iaer, h->sw_tab32, h->sw_tab64, h->sw_exp32, w.su, w.sd, ncol,
+                           nlay, nb, s);
+  } else {
+    launch_sw_prep(in, w, ncol, nlay, h->flags, s);
+    launch_sw_gpoint_fp64(prep_of(w), in, adjflux, iaer, h->sw_tab64, h->sw_exp64, w.su, w.sd, ncol, nlay, nb, s);
+  }
   launch_sw_finalize(w.su, w.sd, in.plev, in.coszen, ncol, nlay, swuflx, swdflx, swhr, swuflxc, swdflxc, swhrc, s);
   h->launches += 3;
   cudaError_t e = cudaGetLastError();
@@ -577,23 +608,8 @@ extern "C" int rrtmg_lw_dev_static(rrtmg_gpu_handle h, void* stream, int ncol, i
   void* base = nullptr;
   e = static_scratch(h->device, &base);
   if (e != cudaSuccess) return cuda_fail(h, e, "rrtmg_lw_dev_static: cudaGetSymbolAddress");
-  cudaStream_t s = (cudaStream_t)stream;
   LwIn in{play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr, cfc11vmr, cfc12vmr,
           cfc22vmr, ccl4vmr, emis, tauaer};
-  LwWork w = carve_lw(base, ncol, nlay, nullptr);
-  launch_lw_prep(in, w, h->totplnk, h->totplnkderiv, ncol, nlay, idrv, h->flags, s);
-  LwPrep p{w.idx, w.f, w.planklay, w.planklev, w.plankbnd, w.dplankbnd, w.secdiff, w.laytrop};
-  const int nb = lw_gpoint_blocks(h->host.lw, ncol);
-  if (h->precision == RRTMG_PREC_SPLIT)
-    launch_lw_gpoint_split(p, in.emis, in.tauaer, h->lw_tab32, h->lw_exp32, h->lw_tfn32, w.bu, w.bd, w.bdu, ncol,
-                           nlay, idrv, nb, s);
-  else
-    launch_lw_gpoint_fp64(p, in.emis, in.tauaer, h->lw_tab64, h->lw_exp64, h->lw_tfn64, w.bu, w.bd, w.bdu, ncol, nlay,
-                          idrv, nb, s);
-  launch_lw_finalize(w.bu, w.bd, w.bdu, in.plev, ncol, nlay, idrv, uflx, dflx, hr, uflxc, dflxc, hrc, duflx_dt,
-                     duflxc_dt, s);
-  h->launches += 3;
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return cuda_fail(h, e, "rrtmg_lw_dev_static: kernel launch");
-  return RRTMG_OK;
+  return lw_enqueue(h, (cudaStream_t)stream, base, ncol, nlay, idrv, in, uflx, dflx, hr, uflxc, dflxc, hrc,
+                    duflx_dt, duflxc_dt);
 }

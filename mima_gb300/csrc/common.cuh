@@ -84,6 +84,15 @@ struct LwConst {
   double heatfac, fluxfac, oneminus, bpade, grav, avogad;
 };
 
+// FP32 copies of the LW constants the gas optics reads per layer, for the
+// FP32-split solvers (same member names as in LwConst).
+struct LwConstF {
+  float chi[7 * 60];
+  float r_h2oco2[61], r_h2oo3[61], r_h2on2o[61], r_h2och4[61], r_n2oco2[61], r_o3co2[61];
+  float refrat[kLwBands][4];
+  float oneminus;
+};
+
 struct SwConst {
   BandDesc band[kSwBands];
   double preflog[60], tref[60];
@@ -91,23 +100,30 @@ struct SwConst {
 };
 
 // Per-call view of the LW prep output.
-struct LwPrep {
-  const uint32_t* idx;     // [lay][col]
-  const double* f;         // [LF_N][lay][col]
-  const double* planklay;  // [band][lay][col]
-  const double* planklev;  // [band][lev 0..nlay][col]
-  const double* plankbnd;  // [band][col]
-  const double* dplankbnd; // [band][col]
-  const double* secdiff;   // [band][col]
-  const int* laytrop;      // [col]
+// Per-layer inputs of the g-point solvers, stored in the solver's arithmetic
+// type F (double for the FP64 path, float for the FP32-split path; the prep
+// kernels compute in FP64 either way and round on store).
+template <class F>
+struct LwPrepT {
+  const uint32_t* idx;  // [lay][col]
+  const F* f;           // [LF_N][lay][col]
+  const F* planklay;    // [band][lay][col]
+  const F* planklev;    // [band][lev 0..nlay][col]
+  const F* plankbnd;    // [band][col]
+  const F* dplankbnd;   // [band][col]
+  const F* secdiff;     // [band][col]
+  const int* laytrop;   // [col]
 };
+using LwPrep = LwPrepT<double>;
 
-struct SwPrep {
-  const uint32_t* idx;     // [lay][col]
-  const double* f;         // [SF_N][lay][col]
-  const int* laytrop;      // [col]
-  const int* laysolfr;     // [band][col], 0 = no solar-source layer
+template <class F>
+struct SwPrepT {
+  const uint32_t* idx;  // [lay][col]
+  const F* f;           // [SF_N][lay][col]
+  const int* laytrop;   // [col]
+  const int* laysolfr;  // [band][col], 0 = no solar-source layer
 };
+using SwPrep = SwPrepT<double>;
 
 // ---------------------------------------------------------------------------
 // Device pointers of one call (inputs as passed by the caller) and of its
@@ -117,21 +133,25 @@ struct LwIn {
   const double *play, *plev, *tlay, *tlev, *tsfc, *h2o, *o3, *co2, *ch4, *n2o, *o2, *cfc11, *cfc12, *cfc22, *ccl4,
       *emis, *tauaer;
 };
-struct LwWork {
+template <class F>
+struct LwWorkT {
   uint32_t* idx;
-  double *f, *planklay, *planklev, *plankbnd, *dplankbnd, *secdiff;
+  F *f, *planklay, *planklev, *plankbnd, *dplankbnd, *secdiff;
   int* laytrop;
   double *bu, *bd, *bdu;  // band partials [band][lev][col]
 };
+using LwWork = LwWorkT<double>;
 struct SwIn {
   const double *play, *plev, *tlay, *tlev, *tsfc, *h2o, *o3, *co2, *ch4, *n2o, *o2, *asdir, *asdif, *aldir, *aldif,
       *coszen, *tauaer, *ssaaer, *asmaer;
 };
-struct SwWork {
+template <class F>
+struct SwWorkT {
   uint32_t* idx;
-  double* f;
+  F* f;
   int *laytrop, *laysolfr;
   double *su, *sd;  // band partials [band][lev][col]
 };
+using SwWork = SwWorkT<double>;
 
 }  // namespace rrtmg

@@ -30,6 +30,16 @@ namespace rrtmg {
 // Constant memory: one copy per translation unit, filled by upload_constants().
 static __constant__ LwConst c_lw;
 static __constant__ SwConst c_sw;
+static __constant__ LwConstF c_lwf;  // uploaded by the FP32-split unit only
+
+// Per-layer LW constants in the solver's arithmetic type.
+template <class R>
+__device__ __forceinline__ const auto& lw_rconst() {
+  if constexpr (sizeof(R) == 4)
+    return c_lwf;
+  else
+    return c_lw;
+}
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
@@ -42,13 +52,64 @@ __device__ __forceinline__ double seg_sum(double v) {
 
 __device__ __forceinline__ bool bad(double x) { return !isfinite(x); }
 
+// FP64 g-point sums of the FP32-split solvers.  Each lane of a warp holds one
+// (column, g-point) value per level; NB value streams are staged in FP32 in
+// shared memory for up to W levels, then every lane forms one (column, level)
+// sum in FP64 -- NG conversions and NG adds (or multiply-adds with the
+// per-g weights `wt`, the SW incident fluxes) in g order -- and hands it to
+// the store.  Per lane and level that is about 2 NG / W FP64 operations,
+// against a conversion and log2(W) adds for a butterfly on every lane.
+// Rows are 33 floats wide so that the staging stores and the per-lane row
+// reads are free of bank conflicts.  All lanes of the warp must call put/next/
+// flush uniformly (the level loops are warp-uniform).
+constexpr int kRow = 33;
+template <int W, int NG, int NB, bool WEIGHTED>
+struct GSum {
+  float* buf;          // this warp's [NB][W][kRow]
+  const double* wt;    // this warp's [32] per-lane weights (WEIGHTED only)
+  int lane, n, first, dir;
+  int nb;              // streams in use (<= NB)
+  __device__ __forceinline__ void put(int b, float v) { buf[(b * W + n) * kRow + lane] = v; }
+  template <class Store>
+  __device__ __forceinline__ void flush(Store&& st) {
+    __syncwarp();
+    const int sl = lane % W, cs = lane / W;
+    if (sl < n) {
+#pragma unroll
+      for (int b = 0; b < NB; ++b) {
+        if (b >= nb) break;
+        const float* row = buf + (b * W + sl) * kRow + cs * W;
+        double acc = 0.0;
+#pragma unroll
+        for (int g = 0; g < NG; ++g) {
+          if constexpr (WEIGHTED)
+            acc = fma(wt[cs * W + g], (double)row[g], acc);
+          else
+            acc += (double)row[g];
+        }
+        st(b, first + dir * sl, cs, acc);
+      }
+    }
+    __syncwarp();
+    first += dir * n;
+    n = 0;
+  }
+  template <class Store>
+  __device__ __forceinline__ void next(Store&& st) {
+    if (++n == W) flush(st);
+  }
+};
+// Shared-memory floats of the staging buffers of one 128-thread block.
+constexpr int kGSumFloats = (kBlock / 32) * 2 * 16 * kRow;
+
 #ifdef RRTMG_DEFINE_COLUMN_KERNELS
 // ---------------------------------------------------------------------------
 // LW prep: inatm (rrtmg_lw_rad.nomcica.f90:572-901) + setcoef
 // (rrtmg_lw_setcoef.f90:31-415) + secdiff (rrtmg_lw_rtrnmr.f90:271-279).
 // totplnk / totplnkderiv: device tables [(ind-1) + 181*(band-1)].
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) lw_prep_kernel(LwIn in, LwWork w, const double* __restrict__ totplnk,
+template <class F>
+__global__ void __launch_bounds__(128) lw_prep_kernel(LwIn in, LwWorkT<F> w, const double* __restrict__ totplnk,
                                                       const double* __restrict__ totplnkderiv, int ncol, int nlay,
                                                       int idrv, unsigned* __restrict__ flags) {
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
@@ -180,7 +241,7 @@ __global__ void __launch_bounds__(128) lw_prep_kernel(LwIn in, LwWork w, const d
     const double colbrd = 1.e-20 * wbrodl;
     const double compfp = 1. - fp;
     const size_t o = (size_t)(l - 1) * N + col;
-    double* f = w.f;
+    F* f = w.f;
     f[LF_PAVEL * fstride + o] = pavel;
     f[LF_COLDRY * fstride + o] = coldry;
     f[LF_COLH2O * fstride + o] = colh2o;
@@ -236,12 +297,13 @@ __global__ void __launch_bounds__(128) lw_prep_kernel(LwIn in, LwWork w, const d
 // (rrtmg_lw_rtrnmr.f90:505-616 downward, :628-713 upward) for one g-point.
 // ---------------------------------------------------------------------------
 template <int B, class R, int MAXL>
-__device__ __forceinline__ void lw_band(const LwPrep& p, const double* __restrict__ emis,
+__device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __restrict__ emis,
                                         const double* __restrict__ tauaer, const R* __restrict__ tab,
                                         const R* __restrict__ exptbl, const R* __restrict__ tfntbl,
                                         double* __restrict__ bu, double* __restrict__ bd, double* __restrict__ bdu,
-                                        int ncol, int nlay, int idrv, int blk) {
+                                        int ncol, int nlay, int idrv, int blk, float* sbuf) {
   const bool IDRV = idrv == 1;
+  constexpr bool SPLIT = sizeof(R) == 4;
   constexpr int NG = lw_ng(B);
   constexpr int W = pow2ceil(NG);
   constexpr int CPB = kBlock / W;
@@ -253,7 +315,7 @@ __device__ __forceinline__ void lw_band(const LwPrep& p, const double* __restric
   const int gg = g < NG ? g : NG - 1;
   const size_t N = (size_t)ncol;
   const int lt = p.laytrop[c];
-  const R secdiff = (R)p.secdiff[(B - 1) * N + c];
+  const R secdiff = p.secdiff[(B - 1) * N + c];
   const R bpade = (R)c_lw.bpade;
   const R rec_6 = (R)0.166667;
   const size_t fstride = (size_t)nlay * N;
@@ -261,6 +323,25 @@ __device__ __forceinline__ void lw_band(const LwPrep& p, const double* __restric
   R radld = (R)0., fracs1 = (R)0.;
   double* bdp = bd + (size_t)(B - 1) * (nlay + 1) * N + col;
   double* bup = bu + (size_t)(B - 1) * (nlay + 1) * N + col;
+  double* bdup = IDRV ? bdu + (size_t)(B - 1) * (nlay + 1) * N + col : nullptr;
+  // Split path: FP64 band sums through the warp's staging buffers; the
+  // summing lane of column sub-index cs writes column wcol0 + cs.
+  const int wib = threadIdx.x >> 5;
+  const int wcol0 = blk * CPB + (wib * 32) / W;
+  GSum<W, NG, 2, false> gs{sbuf + (SPLIT ? wib * 2 * W * kRow : 0), nullptr, (int)(threadIdx.x & 31), 0, nlay - 1, -1,
+                           1};
+  auto store_dn = [&](int b, int lev, int cs, double v) {
+    const int cc = wcol0 + cs;
+    if (cc < ncol) bd[((size_t)(B - 1) * (nlay + 1) + lev) * N + cc] = v;
+  };
+  auto store_up = [&](int b, int lev, int cs, double v) {
+    const int cc = wcol0 + cs;
+    if (cc >= ncol) return;
+    if (b == 0)
+      bu[((size_t)(B - 1) * (nlay + 1) + lev) * N + cc] = v;
+    else if (IDRV)
+      bdu[((size_t)(B - 1) * (nlay + 1) + lev) * N + cc] = v;
+  };
   // No downward radiance enters at the top (drad(nlayers) stays 0,
   // rrtmg_lw_rtrnmr.f90:290-300).
   if (g == 0 && valid) bdp[(size_t)nlay * N] = 0.0;
@@ -269,13 +350,13 @@ __device__ __forceinline__ void lw_band(const LwPrep& p, const double* __restric
     const Idx ix = unpack_idx(__ldg(p.idx + o));
     LwLayerView<R> L{p.f, fstride, o};
     R taug, fracs;
-    lw_gas<B, R>(c_lw, L, ix, lev <= lt, gg, tab, taug, fracs);
+    lw_gas<B, R>(c_lw, lw_rconst<R>(), L, ix, lev <= lt, gg, tab, taug, fracs);
     R taut = taug;
     if (tauaer) taut = taug + (R)__ldg(tauaer + c + N * ((size_t)(lev - 1) + (size_t)nlay * (B - 1)));
     const R plfrac = fracs;
-    const R blay = (R)__ldg(p.planklay + ((size_t)(B - 1) * nlay + (lev - 1)) * N + c);
-    const R dplankup = (R)__ldg(p.planklev + ((size_t)(B - 1) * (nlay + 1) + lev) * N + c) - blay;
-    const R dplankdn = (R)__ldg(p.planklev + ((size_t)(B - 1) * (nlay + 1) + lev - 1) * N + c) - blay;
+    const R blay = __ldg(p.planklay + ((size_t)(B - 1) * nlay + (lev - 1)) * N + c);
+    const R dplankup = __ldg(p.planklev + ((size_t)(B - 1) * (nlay + 1) + lev) * N + c) - blay;
+    const R dplankdn = __ldg(p.planklev + ((size_t)(B - 1) * (nlay + 1) + lev - 1) * N + c) - blay;
     R odepth = secdiff * taut;
     if (odepth < (R)0.0) odepth = (R)0.0;
     R atr, bbd, bbu;
@@ -297,33 +378,57 @@ __device__ __forceinline__ void lw_band(const LwPrep& p, const double* __restric
     atrans[lev - 1] = atr;
     bbugas[lev - 1] = bbu;
     radld = radld + (bbd - radld) * atr;
-    const double s = seg_sum<W>(active ? (double)radld : 0.0);
-    if (g == 0 && valid) bdp[(size_t)(lev - 1) * N] = s;
+    if constexpr (SPLIT) {
+      gs.put(0, radld);
+      gs.next(store_dn);
+    } else {
+      const double s = seg_sum<W>(active ? (double)radld : 0.0);
+      if (g == 0 && valid) bdp[(size_t)(lev - 1) * N] = s;
+    }
     if (lev == 1) fracs1 = fracs;
   }
+  if constexpr (SPLIT) {
+    if (gs.n) gs.flush(store_dn);
+    gs.first = 0;
+    gs.dir = 1;
+    gs.nb = IDRV ? 2 : 1;
+  }
   const R semiss = emis ? (R)__ldg(emis + c + N * (B - 1)) : (R)1.0;
-  const R rad0 = fracs1 * (R)__ldg(p.plankbnd + (B - 1) * N + c);
+  const R rad0 = fracs1 * __ldg(p.plankbnd + (B - 1) * N + c);
   const R reflect = (R)1. - semiss;
   R radlu = rad0 + reflect * radld;
-  double s = seg_sum<W>(active ? (double)radlu : 0.0);
-  if (g == 0 && valid) bup[0] = s;
   R dlu = (R)0.;
-  double* bdup = nullptr;
-  if (IDRV) {
-    bdup = bdu + (size_t)(B - 1) * (nlay + 1) * N + col;
-    dlu = fracs1 * (R)__ldg(p.dplankbnd + (B - 1) * N + c);
-    s = seg_sum<W>(active ? (double)dlu : 0.0);
-    if (g == 0 && valid) bdup[0] = s;
+  if (IDRV) dlu = fracs1 * __ldg(p.dplankbnd + (B - 1) * N + c);
+  if constexpr (SPLIT) {
+    gs.put(0, radlu);
+    gs.put(1, dlu);
+    gs.next(store_up);
+  } else {
+    double s = seg_sum<W>(active ? (double)radlu : 0.0);
+    if (g == 0 && valid) bup[0] = s;
+    if (IDRV) {
+      s = seg_sum<W>(active ? (double)dlu : 0.0);
+      if (g == 0 && valid) bdup[0] = s;
+    }
   }
   for (int lev = 1; lev <= nlay; ++lev) {
     radlu = radlu + (bbugas[lev - 1] - radlu) * atrans[lev - 1];
-    s = seg_sum<W>(active ? (double)radlu : 0.0);
-    if (g == 0 && valid) bup[(size_t)lev * N] = s;
-    if (IDRV) {
-      dlu = dlu * ((R)1.0 - atrans[lev - 1]);
-      s = seg_sum<W>(active ? (double)dlu : 0.0);
-      if (g == 0 && valid) bdup[(size_t)lev * N] = s;
+    if (IDRV) dlu = dlu * ((R)1.0 - atrans[lev - 1]);
+    if constexpr (SPLIT) {
+      gs.put(0, radlu);
+      gs.put(1, dlu);
+      gs.next(store_up);
+    } else {
+      double s = seg_sum<W>(active ? (double)radlu : 0.0);
+      if (g == 0 && valid) bup[(size_t)lev * N] = s;
+      if (IDRV) {
+        s = seg_sum<W>(active ? (double)dlu : 0.0);
+        if (g == 0 && valid) bdup[(size_t)lev * N] = s;
+      }
     }
+  }
+  if constexpr (SPLIT) {
+    if (gs.n) gs.flush(store_up);
   }
 }
 
@@ -332,12 +437,26 @@ __host__ __device__ inline int lw_blocks_for_band(int ngpad, int ncol) {
   return (ncol + cpb - 1) / cpb;
 }
 
+// Minimum resident blocks per SM asked of the register allocator for the
+// FP32-split solvers.  They are latency-bound (table gathers, local-memory
+// column arrays), so occupancy pays even at the price of a few spills: on
+// GB300 at 32768 columns x 40 layers, 12/12 (40-42 registers) ran the LW+SW
+// split step in 11.1 ms against 19.0 ms at 1/1 (105 registers).  FP64
+// solvers: 1.
+#ifndef RRTMG_SPLIT_LW_MINB
+#define RRTMG_SPLIT_LW_MINB 12
+#endif
+#ifndef RRTMG_SPLIT_SW_MINB
+#define RRTMG_SPLIT_SW_MINB 12
+#endif
+
 template <class R, int MAXL>
-__global__ void __launch_bounds__(kBlock) lw_gpoint_kernel(LwPrep p, const double* __restrict__ emis,
+__global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_LW_MINB : 1) lw_gpoint_kernel(LwPrepT<R> p, const double* __restrict__ emis,
                                                            const double* __restrict__ tauaer,
                                                            const R* __restrict__ tab, const R* __restrict__ exptbl,
                                                            const R* __restrict__ tfntbl, double* bu, double* bd,
                                                            double* bdu, int ncol, int nlay, int idrv) {
+  __shared__ float sbuf[sizeof(R) == 4 ? kGSumFloats : 1];
   int blk = blockIdx.x, band = 0;
   for (; band < kLwBands; ++band) {
     const int nb = lw_blocks_for_band(c_lw.band[band].ngpad, ncol);
@@ -345,7 +464,7 @@ __global__ void __launch_bounds__(kBlock) lw_gpoint_kernel(LwPrep p, const doubl
     blk -= nb;
   }
 #define RRTMG_LW_CASE(b) \
-  case b - 1: lw_band<b, R, MAXL>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv, blk); break;
+  case b - 1: lw_band<b, R, MAXL>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv, blk, sbuf); break;
   switch (band) {
     RRTMG_LW_CASE(1) RRTMG_LW_CASE(2) RRTMG_LW_CASE(3) RRTMG_LW_CASE(4) RRTMG_LW_CASE(5) RRTMG_LW_CASE(6)
     RRTMG_LW_CASE(7) RRTMG_LW_CASE(8) RRTMG_LW_CASE(9) RRTMG_LW_CASE(10) RRTMG_LW_CASE(11) RRTMG_LW_CASE(12)
@@ -422,7 +541,8 @@ __device__ __forceinline__ int sw_layreffr(int b) {
 __host__ __device__ constexpr bool sw_upper_source(int b) { return b == 16 || b == 17 || b == 27 || b == 28 || b == 29; }
 
 #ifdef RRTMG_DEFINE_COLUMN_KERNELS
-__global__ void __launch_bounds__(128) sw_prep_kernel(SwIn in, SwWork w, int ncol, int nlay,
+template <class F>
+__global__ void __launch_bounds__(128) sw_prep_kernel(SwIn in, SwWorkT<F> w, int ncol, int nlay,
                                                       unsigned* __restrict__ flags) {
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= ncol) return;
@@ -499,7 +619,7 @@ __global__ void __launch_bounds__(128) sw_prep_kernel(SwIn in, SwWork w, int nco
     if (colo2 == 0.) colo2 = 1.e-32 * coldry;
     const double compfp = 1. - fp;
     const size_t o = (size_t)(l - 1) * N + col;
-    double* f = w.f;
+    F* f = w.f;
     f[SF_COLH2O * fstride + o] = colh2o;
     f[SF_COLCO2 * fstride + o] = colco2;
     f[SF_COLO3 * fstride + o] = colo3;
@@ -724,10 +844,12 @@ __device__ __forceinline__ void reftra_split(float zto1, float zw, float zg, flo
 }
 
 template <int B, class R, int MAXL>
-__device__ __forceinline__ void sw_band(const SwPrep& p, const SwIn& in, double adjflux, int iaer,
+__device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, double adjflux, int iaer,
                                         const R* __restrict__ tab, const double* __restrict__ tab64,
                                         const R* __restrict__ exptbl, double* __restrict__ su,
-                                        double* __restrict__ sd, int ncol, int nlay, int blk) {
+                                        double* __restrict__ sd, int ncol, int nlay, int blk, float* sbuf,
+                                        double* swt) {
+  constexpr bool SPLIT = sizeof(R) == 4;
   constexpr int NG = sw_ng(B);
   constexpr int W = pow2ceil(NG);
   constexpr int CPB = kBlock / W;
@@ -752,7 +874,7 @@ __device__ __forceinline__ void sw_band(const SwPrep& p, const SwIn& in, double 
   {
     const int ls = p.laysolfr[(size_t)(B - 16) * N + c];
     if (ls >= 1) {
-      SwLayerView<double> L{p.f, fstride, (size_t)(ls - 1) * N + c};
+      SwLayerView<double, R> L{p.f, fstride, (size_t)(ls - 1) * N + c};
       const double sfz = sw_sfluxzen<B>(c_sw, L, ls <= lt, gg, tab64);
       zincflx = adjflux * sfz * (lit ? coszen : 1.0);
     }
@@ -815,6 +937,17 @@ __device__ __forceinline__ void sw_band(const SwPrep& p, const SwIn& in, double 
   // (:141-149) as soon as each level's upward reflectances are known.
   double* sup = su + (size_t)(B - 16) * (nlay + 1) * N + col;
   double* sdp = sd + (size_t)(B - 16) * (nlay + 1) * N + col;
+  // Split path: FP64 incident-flux-weighted band sums through the warp's
+  // staging buffers (levels surface first); the summing lane of column
+  // sub-index cs writes column wcol0 + cs.
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int wcol0 = blk * CPB + (wib * 32) / W;
+  GSum<W, NG, 2, true> gs{sbuf + (SPLIT ? wib * 2 * W * kRow : 0), swt + (SPLIT ? wib * 32 : 0), lane, 0, 0, 1, 2};
+  if constexpr (SPLIT) swt[wib * 32 + lane] = active ? zincflx : 0.0;
+  auto store = [&](int b, int lev, int cs, double v) {
+    const int cc = wcol0 + cs;
+    if (cc < ncol) (b == 0 ? su : sd)[((size_t)(B - 16) * (nlay + 1) + lev) * N + cc] = v;
+  };
   R prup = albdir, prupd = albdif;  // level klev+1 (surface)
   for (int jk = klev + 1; jk >= 1; --jk) {
     if (jk <= klev) {
@@ -837,21 +970,32 @@ __device__ __forceinline__ void sw_band(const SwPrep& p, const SwIn& in, double 
     const R zreflect = (R)1. / ((R)1. - rdnd * prupd);
     const R pfu = (tdbt * prup + (tdn - tdbt) * prupd) * zreflect;
     const R pfd = tdbt + (tdn - tdbt + tdbt * prup * rdnd) * zreflect;
-    const double su_s = seg_sum<W>(active ? zincflx * (double)pfu : 0.0);
-    const double sd_s = seg_sum<W>(active ? zincflx * (double)pfd : 0.0);
     // output level (surface first) ikl = klev + 2 - jk  ->  0-based klev + 1 - jk
-    if (g == 0 && valid) {
-      sup[(size_t)(klev + 1 - jk) * N] = su_s;
-      sdp[(size_t)(klev + 1 - jk) * N] = sd_s;
+    if constexpr (SPLIT) {
+      gs.put(0, pfu);
+      gs.put(1, pfd);
+      gs.next(store);
+    } else {
+      const double su_s = seg_sum<W>(active ? zincflx * (double)pfu : 0.0);
+      const double sd_s = seg_sum<W>(active ? zincflx * (double)pfd : 0.0);
+      if (g == 0 && valid) {
+        sup[(size_t)(klev + 1 - jk) * N] = su_s;
+        sdp[(size_t)(klev + 1 - jk) * N] = sd_s;
+      }
     }
+  }
+  if constexpr (SPLIT) {
+    if (gs.n) gs.flush(store);
   }
 }
 
 template <class R, int MAXL>
-__global__ void __launch_bounds__(kBlock) sw_gpoint_kernel(SwPrep p, SwIn in, double adjflux, int iaer,
+__global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_SW_MINB : 1) sw_gpoint_kernel(SwPrepT<R> p, SwIn in, double adjflux, int iaer,
                                                            const R* __restrict__ tab, const double* __restrict__ tab64,
                                                            const R* __restrict__ exptbl, double* su, double* sd,
                                                            int ncol, int nlay) {
+  __shared__ float sbuf[sizeof(R) == 4 ? kGSumFloats : 1];
+  __shared__ double swt[sizeof(R) == 4 ? kBlock : 1];
   int blk = blockIdx.x, band = 0;
   for (; band < kSwBands; ++band) {
     const int nb = lw_blocks_for_band(c_sw.band[band].ngpad, ncol);
@@ -859,7 +1003,7 @@ __global__ void __launch_bounds__(kBlock) sw_gpoint_kernel(SwPrep p, SwIn in, do
     blk -= nb;
   }
 #define RRTMG_SW_CASE(b) \
-  case b - 16: sw_band<b, R, MAXL>(p, in, adjflux, iaer, tab, tab64, exptbl, su, sd, ncol, nlay, blk); break;
+  case b - 16: sw_band<b, R, MAXL>(p, in, adjflux, iaer, tab, tab64, exptbl, su, sd, ncol, nlay, blk, sbuf, swt); break;
   switch (band) {
     RRTMG_SW_CASE(16) RRTMG_SW_CASE(17) RRTMG_SW_CASE(18) RRTMG_SW_CASE(19) RRTMG_SW_CASE(20) RRTMG_SW_CASE(21)
     RRTMG_SW_CASE(22) RRTMG_SW_CASE(23) RRTMG_SW_CASE(24) RRTMG_SW_CASE(25) RRTMG_SW_CASE(26) RRTMG_SW_CASE(27)

@@ -27,7 +27,12 @@ int sw_gpoint_blocks(const SwConst& c, int ncol) {
 
 void launch_lw_prep(const LwIn& in, const LwWork& w, const double* totplnk, const double* totplnkderiv, int ncol,
                     int nlay, int idrv, unsigned* flags, cudaStream_t s) {
-  lw_prep_kernel<<<(ncol + 127) / 128, 128, 0, s>>>(in, w, totplnk, totplnkderiv, ncol, nlay, idrv, flags);
+  lw_prep_kernel<double><<<(ncol + 127) / 128, 128, 0, s>>>(in, w, totplnk, totplnkderiv, ncol, nlay, idrv, flags);
+}
+
+void launch_lw_prep_split(const LwIn& in, const LwWorkT<float>& w, const double* totplnk, const double* totplnkderiv,
+                          int ncol, int nlay, int idrv, unsigned* flags, cudaStream_t s) {
+  lw_prep_kernel<float><<<(ncol + 127) / 128, 128, 0, s>>>(in, w, totplnk, totplnkderiv, ncol, nlay, idrv, flags);
 }
 
 void launch_lw_gpoint_fp64(const LwPrep& p, const double* emis, const double* tauaer, const double* tab,
@@ -47,7 +52,12 @@ void launch_lw_finalize(const double* bu, const double* bd, const double* bdu, c
 }
 
 void launch_sw_prep(const SwIn& in, const SwWork& w, int ncol, int nlay, unsigned* flags, cudaStream_t s) {
-  sw_prep_kernel<<<(ncol + 127) / 128, 128, 0, s>>>(in, w, ncol, nlay, flags);
+  sw_prep_kernel<double><<<(ncol + 127) / 128, 128, 0, s>>>(in, w, ncol, nlay, flags);
+}
+
+void launch_sw_prep_split(const SwIn& in, const SwWorkT<float>& w, int ncol, int nlay, unsigned* flags,
+                          cudaStream_t s) {
+  sw_prep_kernel<float><<<(ncol + 127) / 128, 128, 0, s>>>(in, w, ncol, nlay, flags);
 }
 
 void launch_sw_gpoint_fp64(const SwPrep& p, const SwIn& in, double adjflux, int iaer, const double* tab,

@@ -9,10 +9,25 @@ namespace rrtmg {
 cudaError_t upload_constants_split(const LwConst& lw, const SwConst& sw) {
   cudaError_t e = cudaMemcpyToSymbol(c_lw, &lw, sizeof(LwConst));
   if (e != cudaSuccess) return e;
+  LwConstF f{};
+  for (int k = 0; k < 7 * 60; ++k) f.chi[k] = (float)lw.chi[k];
+  for (int j = 0; j < 61; ++j) {
+    f.r_h2oco2[j] = (float)lw.r_h2oco2[j];
+    f.r_h2oo3[j] = (float)lw.r_h2oo3[j];
+    f.r_h2on2o[j] = (float)lw.r_h2on2o[j];
+    f.r_h2och4[j] = (float)lw.r_h2och4[j];
+    f.r_n2oco2[j] = (float)lw.r_n2oco2[j];
+    f.r_o3co2[j] = (float)lw.r_o3co2[j];
+  }
+  for (int b = 0; b < kLwBands; ++b)
+    for (int k = 0; k < 4; ++k) f.refrat[b][k] = (float)lw.refrat[b][k];
+  f.oneminus = (float)lw.oneminus;
+  e = cudaMemcpyToSymbol(c_lwf, &f, sizeof(LwConstF));
+  if (e != cudaSuccess) return e;
   return cudaMemcpyToSymbol(c_sw, &sw, sizeof(SwConst));
 }
 
-void launch_lw_gpoint_split(const LwPrep& p, const double* emis, const double* tauaer, const float* tab,
+void launch_lw_gpoint_split(const LwPrepT<float>& p, const double* emis, const double* tauaer, const float* tab,
                             const float* exptbl, const float* tfntbl, double* bu, double* bd, double* bdu, int ncol,
                             int nlay, int idrv, int nb, cudaStream_t s) {
   if (maxl_for(nlay) == 64)
@@ -21,7 +36,7 @@ void launch_lw_gpoint_split(const LwPrep& p, const double* emis, const double* t
     lw_gpoint_kernel<float, 208><<<nb, kBlock, 0, s>>>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv);
 }
 
-void launch_sw_gpoint_split(const SwPrep& p, const SwIn& in, double adjflux, int iaer, const float* tab,
+void launch_sw_gpoint_split(const SwPrepT<float>& p, const SwIn& in, double adjflux, int iaer, const float* tab,
                             const double* tab64, const float* exptbl, double* su, double* sd, int ncol, int nlay,
                             int nb, cudaStream_t s) {
   if (maxl_for(nlay) == 64)

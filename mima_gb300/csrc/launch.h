@@ -9,11 +9,6 @@
 
 namespace rrtmg {
 
-struct LwIn;
-struct LwWork;
-struct SwIn;
-struct SwWork;
-
 // Choice of the compiled per-thread column depth (local-memory arrays).
 inline int maxl_for(int nlay) { return nlay <= 64 ? 64 : 208; }
 
@@ -30,6 +25,11 @@ void launch_lw_finalize(const double* bu, const double* bd, const double* bdu, c
                         int idrv, double* uflx, double* dflx, double* hr, double* uflxc, double* dflxc, double* hrc,
                         double* duflx_dt, double* duflxc_dt, cudaStream_t s);
 void launch_sw_prep(const SwIn& in, const SwWork& w, int ncol, int nlay, unsigned* flags, cudaStream_t s);
+// Prep for the FP32-split solvers: the same FP64 arithmetic, fields stored as float.
+void launch_lw_prep_split(const LwIn& in, const LwWorkT<float>& w, const double* totplnk, const double* totplnkderiv,
+                          int ncol, int nlay, int idrv, unsigned* flags, cudaStream_t s);
+void launch_sw_prep_split(const SwIn& in, const SwWorkT<float>& w, int ncol, int nlay, unsigned* flags,
+                          cudaStream_t s);
 void launch_sw_gpoint_fp64(const SwPrep& p, const SwIn& in, double adjflux, int iaer, const double* tab,
                            const double* exptbl, double* su, double* sd, int ncol, int nlay, int nb, cudaStream_t s);
 void launch_sw_finalize(const double* su, const double* sd, const double* plev, const double* coszen, int ncol,
@@ -37,10 +37,10 @@ void launch_sw_finalize(const double* su, const double* sd, const double* plev, 
                         double* swhrc, cudaStream_t s);
 
 // FP32-split translation unit.
-void launch_lw_gpoint_split(const LwPrep& p, const double* emis, const double* tauaer, const float* tab,
+void launch_lw_gpoint_split(const LwPrepT<float>& p, const double* emis, const double* tauaer, const float* tab,
                             const float* exptbl, const float* tfntbl, double* bu, double* bd, double* bdu, int ncol,
                             int nlay, int idrv, int nb, cudaStream_t s);
-void launch_sw_gpoint_split(const SwPrep& p, const SwIn& in, double adjflux, int iaer, const float* tab,
+void launch_sw_gpoint_split(const SwPrepT<float>& p, const SwIn& in, double adjflux, int iaer, const float* tab,
                             const double* tab64, const float* exptbl, double* su, double* sd, int ncol, int nlay,
                             int nb, cudaStream_t s);
 

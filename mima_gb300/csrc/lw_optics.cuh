@@ -12,6 +12,8 @@
 // The sum association of every expression follows the reference so that the
 // FP64 instantiation is bit-reproducible against a literal restatement.
 #pragma once
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace rrtmg {
@@ -26,10 +28,10 @@ __host__ __device__ constexpr int pow2ceil(int n) { return n <= 2 ? 2 : n <= 4 ?
 // Layer-state accessor: fields of one (layer, column) of the prep output.
 template <class R>
 struct LwLayerView {
-  const double* __restrict__ f;
-  size_t fstride;  // nlay * ncol
-  size_t o;        // (lay-1) * ncol + col
-  __device__ __forceinline__ R operator()(int fld) const { return (R)__ldg(f + (size_t)fld * fstride + o); }
+  const R* __restrict__ f;  // per-layer fields stored in the solver's type
+  size_t fstride;           // nlay * ncol
+  size_t o;                 // (lay-1) * ncol + col
+  __device__ __forceinline__ R operator()(int fld) const { return __ldg(f + (size_t)fld * fstride + o); }
 };
 
 template <class R>
@@ -134,14 +136,14 @@ __device__ __forceinline__ R minor_eta(const R* __restrict__ k, int nj, int jm, 
 }
 
 template <class R>
-__device__ __forceinline__ R adj_col(R col, R coldry, double chiref, R thresh, R base, double expo) {
+__device__ __forceinline__ R adj_col(R col, R coldry, R chiref, R thresh, R base, double expo) {
   // Empirical adjustment of a minor column that exceeds the reference
   // profile, e.g. rrtmg_lw_taumol.f90:528-535.
   R chi_x = col / (coldry);
-  R ratx = (R)1.e20 * chi_x / (R)chiref;
+  R ratx = (R)1.e20 * chi_x / chiref;
   if (ratx > thresh) {
     R adjfac = base + (R)pow((double)(ratx - base), expo);
-    return adjfac * (R)chiref * coldry * (R)1.e-20;
+    return adjfac * chiref * coldry * (R)1.e-20;
   }
   return col;
 }
@@ -152,9 +154,11 @@ struct LwBandCtx {
 };
 
 // taug / fracs of band B for g (0-based in band) at one layer.
-template <int B, class R>
-__device__ __forceinline__ void lw_gas(const LwConst& C, const LwLayerView<R>& L, const Idx& ix, bool lower, int g,
-                                       const R* __restrict__ tab, R& taug, R& fracs) {
+// C: band layout and FP64 constants; CR: the per-layer constants in type R
+// (C itself for FP64, its FP32 copy for the split path).
+template <int B, class R, class RC>
+__device__ __forceinline__ void lw_gas(const LwConst& C, const RC& CR, const LwLayerView<R>& L, const Idx& ix,
+                                       bool lower, int g, const R* __restrict__ tab, R& taug, R& fracs) {
   constexpr int NG = lw_ng(B);
   const BandDesc& bd = C.band[B - 1];
   const R* ka = tab + bd.off[LW_KA];
@@ -163,7 +167,8 @@ __device__ __forceinline__ void lw_gas(const LwConst& C, const LwLayerView<R>& L
   const R* forr = tab + bd.off[LW_FOR];
   const R* fra = tab + bd.off[LW_FRA];
   const R* frb = tab + bd.off[LW_FRB];
-  const R one_m = (R)C.oneminus;
+  using CT = std::remove_cv_t<std::remove_reference_t<decltype(CR.oneminus)>>;  // double or float
+  const R one_m = (R)CR.oneminus;
   const int jp = ix.jp;
   auto i_lo = [&](int js) { return ((jp - 1) * 5 + (ix.jt - 1)) * bd.nspa + js; };
   auto i_lo1 = [&](int js) { return (jp * 5 + (ix.jt1 - 1)) * bd.nspa + js; };
@@ -176,8 +181,8 @@ __device__ __forceinline__ void lw_gas(const LwConst& C, const LwLayerView<R>& L
   auto i4 = [&](const R* k, int i0, int i1) {
     return interp4<R, NG>(k, L(LF_FAC00), L(LF_FAC10), L(LF_FAC01), L(LF_FAC11), i0, i1, g);
   };
-  auto rat = [&](const double* r, int j) { return (R)r[j]; };
-  auto chi = [&](int i, int j) { return C.chi[(j - 1) * 7 + (i - 1)]; };
+  auto rat = [&](const auto* r, int j) { return (R)r[j]; };
+  auto chi = [&](int i, int j) { return (R)CR.chi[(j - 1) * 7 + (i - 1)]; };
 
   if constexpr (B == 1) {
     if (lower) {
@@ -217,16 +222,16 @@ __device__ __forceinline__ void lw_gas(const LwConst& C, const LwLayerView<R>& L
     // 15: n2o/co2 (minor n2).
     if (lower) {
       R a, b;
-      const double *r0, *r1;
-      if constexpr (B == 3 || B == 5) { a = L(LF_COLH2O); b = L(LF_COLCO2); r0 = C.r_h2oco2; }
-      else if constexpr (B == 7) { a = L(LF_COLH2O); b = L(LF_COLO3); r0 = C.r_h2oo3; }
-      else if constexpr (B == 9) { a = L(LF_COLH2O); b = L(LF_COLCH4); r0 = C.r_h2och4; }
-      else if constexpr (B == 13) { a = L(LF_COLH2O); b = L(LF_COLN2O); r0 = C.r_h2on2o; }
-      else { a = L(LF_COLN2O); b = L(LF_COLCO2); r0 = C.r_n2oco2; }
+      const CT *r0, *r1;
+      if constexpr (B == 3 || B == 5) { a = L(LF_COLH2O); b = L(LF_COLCO2); r0 = CR.r_h2oco2; }
+      else if constexpr (B == 7) { a = L(LF_COLH2O); b = L(LF_COLO3); r0 = CR.r_h2oo3; }
+      else if constexpr (B == 9) { a = L(LF_COLH2O); b = L(LF_COLCH4); r0 = CR.r_h2och4; }
+      else if constexpr (B == 13) { a = L(LF_COLH2O); b = L(LF_COLN2O); r0 = CR.r_h2on2o; }
+      else { a = L(LF_COLN2O); b = L(LF_COLCO2); r0 = CR.r_n2oco2; }
       r1 = r0;
       EtaV<R> e = eta_mix<R>(a, rat(r0, jp), b, (R)8., one_m);
       EtaV<R> e1 = eta_mix<R>(a, rat(r1, jp + 1), b, (R)8., one_m);
-      EtaV<R> em = eta_mix<R>(a, (R)C.refrat[B - 1][2], b, (R)8., one_m);
+      EtaV<R> em = eta_mix<R>(a, (R)CR.refrat[B - 1][2], b, (R)8., one_m);
       R extra, extra2 = (R)0;
       if constexpr (B == 3 || B == 9) {
         R adjcoln2o = adj_col<R>(L(LF_COLN2O), L(LF_COLDRY), chi(4, jp + 1), (R)1.5, (R)0.5, 0.65);
@@ -250,7 +255,7 @@ __device__ __forceinline__ void lw_gas(const LwConst& C, const LwLayerView<R>& L
         } else {
           adjcolco2 = L(LF_COLCO2);
         }
-        EtaV<R> emo = eta_mix<R>(a, (R)C.refrat[B - 1][3], b, (R)8., one_m);
+        EtaV<R> emo = eta_mix<R>(a, (R)CR.refrat[B - 1][3], b, (R)8., one_m);
         R absco2 = minor_eta<R, NG>(tab + bd.off[LW_MA1], 9, em.js, em.fs, ix.indm, L(LF_MINORFRAC), g);
         R absco = minor_eta<R, NG>(tab + bd.off[LW_MA2], 9, emo.js, emo.fs, ix.indm, L(LF_MINORFRAC), g);
         extra = adjcolco2 * absco2;
@@ -259,7 +264,7 @@ __device__ __forceinline__ void lw_gas(const LwConst& C, const LwLayerView<R>& L
         R scalen2 = L(LF_COLBRD) * L(LF_SCALEMINOR);
         extra = scalen2 * minor_eta<R, NG>(tab + bd.off[LW_MA1], 9, em.js, em.fs, ix.indm, L(LF_MINORFRAC), g);
       }
-      EtaV<R> ep = eta_mix<R>(a, (R)C.refrat[B - 1][0], b, (R)8., one_m);
+      EtaV<R> ep = eta_mix<R>(a, (R)CR.refrat[B - 1][0], b, (R)8., one_m);
       int ind0 = i_lo(e.js), ind1 = i_lo1(e1.js);
       W3<R> w0 = w3<R>(e.specparm, e.fs, L(LF_FAC00), L(LF_FAC10));
       W3<R> w1 = w3<R>(e1.specparm, e1.fs, L(LF_FAC01), L(LF_FAC11));
@@ -277,16 +282,16 @@ __device__ __forceinline__ void lw_gas(const LwConst& C, const LwLayerView<R>& L
     } else {
       if constexpr (B == 3 || B == 5) {
         R a = (B == 3) ? L(LF_COLH2O) : L(LF_COLO3);
-        const double* r0 = (B == 3) ? C.r_h2oco2 : C.r_o3co2;
+        const auto* r0 = (B == 3) ? CR.r_h2oco2 : CR.r_o3co2;
         R b = L(LF_COLCO2);
         EtaV<R> e = eta_mix<R>(a, rat(r0, jp), b, (R)4., one_m);
         EtaV<R> e1 = eta_mix<R>(a, rat(r0, jp + 1), b, (R)4., one_m);
-        EtaV<R> ep = eta_mix<R>(a, (R)C.refrat[B - 1][1], b, (R)4., one_m);
+        EtaV<R> ep = eta_mix<R>(a, (R)CR.refrat[B - 1][1], b, (R)4., one_m);
         int ind0 = i_up(e.js), ind1 = i_up1(e1.js);
         R maj = major5<R, NG>(kb, e.speccomb, e.fs, ind0, e1.speccomb, e1.fs, ind1, L(LF_FAC00), L(LF_FAC10),
                               L(LF_FAC01), L(LF_FAC11), g);
         if constexpr (B == 3) {
-          EtaV<R> em = eta_mix<R>(a, (R)C.refrat[B - 1][3], b, (R)4., one_m);
+          EtaV<R> em = eta_mix<R>(a, (R)CR.refrat[B - 1][3], b, (R)4., one_m);
           R adjcoln2o = adj_col<R>(L(LF_COLN2O), L(LF_COLDRY), chi(4, jp + 1), (R)1.5, (R)0.5, 0.65);
           R taufor = tfor();
           R absn2o = minor_eta<R, NG>(tab + bd.off[LW_MB1], 5, em.js, em.fs, ix.indm, L(LF_MINORFRAC), g);
@@ -322,10 +327,10 @@ __device__ __forceinline__ void lw_gas(const LwConst& C, const LwLayerView<R>& L
     if (lower) {
       R a = L(LF_COLH2O);
       R b = (B == 16) ? L(LF_COLCH4) : L(LF_COLCO2);
-      const double* r0 = (B == 16) ? C.r_h2och4 : C.r_h2oco2;
+      const auto* r0 = (B == 16) ? CR.r_h2och4 : CR.r_h2oco2;
       EtaV<R> e = eta_mix<R>(a, rat(r0, jp), b, (R)8., one_m);
       EtaV<R> e1 = eta_mix<R>(a, rat(r0, jp + 1), b, (R)8., one_m);
-      EtaV<R> ep = eta_mix<R>(a, (R)C.refrat[B - 1][0], b, (R)8., one_m);
+      EtaV<R> ep = eta_mix<R>(a, (R)CR.refrat[B - 1][0], b, (R)8., one_m);
       int ind0 = i_lo(e.js), ind1 = i_lo1(e1.js);
       W3<R> w0 = w3<R>(e.specparm, e.fs, L(LF_FAC00), L(LF_FAC10));
       W3<R> w1 = w3<R>(e1.specparm, e1.fs, L(LF_FAC01), L(LF_FAC11));
@@ -337,9 +342,9 @@ __device__ __forceinline__ void lw_gas(const LwConst& C, const LwLayerView<R>& L
     } else {
       if constexpr (B == 4) {
         R a = L(LF_COLO3), b = L(LF_COLCO2);
-        EtaV<R> e = eta_mix<R>(a, rat(C.r_o3co2, jp), b, (R)4., one_m);
-        EtaV<R> e1 = eta_mix<R>(a, rat(C.r_o3co2, jp + 1), b, (R)4., one_m);
-        EtaV<R> ep = eta_mix<R>(a, (R)C.refrat[B - 1][1], b, (R)4., one_m);
+        EtaV<R> e = eta_mix<R>(a, rat(CR.r_o3co2, jp), b, (R)4., one_m);
+        EtaV<R> e1 = eta_mix<R>(a, rat(CR.r_o3co2, jp + 1), b, (R)4., one_m);
+        EtaV<R> ep = eta_mix<R>(a, (R)CR.refrat[B - 1][1], b, (R)4., one_m);
         int ind0 = i_up(e.js), ind1 = i_up1(e1.js);
         R t = major5<R, NG>(kb, e.speccomb, e.fs, ind0, e1.speccomb, e1.fs, ind1, L(LF_FAC00), L(LF_FAC10),
                             L(LF_FAC01), L(LF_FAC11), g);

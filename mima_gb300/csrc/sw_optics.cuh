@@ -20,16 +20,17 @@ __host__ __device__ constexpr double sw_strrat(int b) {
        : b == 22 ? 0.022708 : b == 24 ? 0.124692 : b == 28 ? 6.67029e-07 : 0.0;
 }
 
-template <class R>
+// Per-layer fields stored as F (the solver's type), read as R.
+template <class R, class F = R>
 struct SwLayerView {
-  const double* __restrict__ f;
+  const F* __restrict__ f;
   size_t fstride, o;
   __device__ __forceinline__ R operator()(int fld) const { return (R)__ldg(f + (size_t)fld * fstride + o); }
 };
 
 // Eta of the band's key-species pair at one layer; mult 8 (lower) or 4 (upper).
-template <int B, class R>
-__device__ __forceinline__ EtaV<R> sw_band_eta(const SwLayerView<R>& L, R mult, R one_m) {
+template <int B, class R, class V>
+__device__ __forceinline__ EtaV<R> sw_band_eta(const V& L, R mult, R one_m) {
   constexpr double s = sw_strrat(B);
   if constexpr (B == 16 || B == 18) return eta_mix<R>(L(SF_COLH2O), (R)s, L(SF_COLCH4), mult, one_m);
   else if constexpr (B == 17 || B == 19 || B == 21) return eta_mix<R>(L(SF_COLH2O), (R)s, L(SF_COLCO2), mult, one_m);
@@ -50,8 +51,8 @@ __device__ __forceinline__ R sw_major8(const R* __restrict__ k, const EtaV<R>& e
                        fac001 * K(i1) + fac101 * K(i1 + 1) + fac011 * K(i1 + s) + fac111 * K(i1 + s + 1));
 }
 
-template <int B, class R>
-__device__ __forceinline__ void sw_gas(const SwConst& C, const SwLayerView<R>& L, const Idx& ix, bool lower, int g,
+template <int B, class R, class V>
+__device__ __forceinline__ void sw_gas(const SwConst& C, const V& L, const Idx& ix, bool lower, int g,
                                        const R* __restrict__ tab, R& taug, R& taur) {
   constexpr int NG = sw_ng(B);
   const BandDesc& bd = C.band[B - 16];
@@ -145,8 +146,8 @@ __device__ __forceinline__ void sw_gas(const SwConst& C, const SwLayerView<R>& L
 // Solar source of g-point g of band B, taken at the band's reference layer
 // (laysolfr, computed by the prep kernel exactly as the taumol loops do).
 // Bands whose sfluxref depends on eta interpolate it with that layer's eta.
-template <int B>
-__device__ __forceinline__ double sw_sfluxzen(const SwConst& C, const SwLayerView<double>& L, bool lower, int g,
+template <int B, class V>
+__device__ __forceinline__ double sw_sfluxzen(const SwConst& C, const V& L, bool lower, int g,
                                               const double* __restrict__ tab) {
   constexpr int NG = sw_ng(B);
   const BandDesc& bd = C.band[B - 16];

@@ -59,6 +59,12 @@ enum rrtmg_gpu_precision {
 /* Maximum number of layers (parrrtm.f90 / parrrsw.f90 mxlay). */
 #define RRTMG_GPU_MAX_LAYERS 203
 
+/* Transcendental evaluation of the solvers: the reference's lookup tables
+ * (exp_tbl / tfn_tbl, 10001 entries, the default) or the analytic functions
+ * they sample.  The analytic form is the smooth forward whose derivatives the
+ * adjoint entry points compute. */
+enum { RRTMG_TRANS_TABLE = 0, RRTMG_TRANS_ANALYTIC = 1 };
+
 /* Replaces rrtmg_lw_ini(cpdair) + rrtmg_sw_ini(cpdair) (rrtmg_lw_init.f90:28-175,
  * rrtmg_sw_init.f90:28-154): reads the unreduced coefficient tables from
  * table_blob, performs the 256->140 / 224->112 g-point reduction, builds the
@@ -136,6 +142,10 @@ int rrtmg_sw_dev(rrtmg_gpu_handle h, void* stream, int ncol, int nlay, int icld,
                  double* swuflx, double* swdflx, double* swhr, double* swuflxc, double* swdflxc,
                  double* swhrc);
 
+/* No counterpart in the reference (which always uses its tables).  Selects
+ * RRTMG_TRANS_TABLE or RRTMG_TRANS_ANALYTIC for later calls on the handle. */
+int rrtmg_gpu_set_transcendentals(rrtmg_gpu_handle h, int mode);
+
 /* Reserves device workspace for calls of up to ncol columns and nlay layers,
  * so that later device calls allocate nothing (e.g. before graph capture). */
 int rrtmg_gpu_reserve(rrtmg_gpu_handle h, int ncol, int nlay);
@@ -143,6 +153,49 @@ int rrtmg_gpu_reserve(rrtmg_gpu_handle h, int ncol, int nlay);
 /* Waits for `stream` and reports RRTMG_ERR_INPUT if an enqueued call flagged
  * invalid input (the flag is then cleared). */
 int rrtmg_gpu_sync_status(rrtmg_gpu_handle h, void* stream);
+
+/* Adjoint of the clear-sky LW + SW radiation: Jacobians of
+ *   rows (ny = 2*nlay + 3): LW heating rate of layers 1..nlay (K/day), OLR
+ *     (upward LW at the top level, W/m2), LW surface net flux (up - down),
+ *     SW heating rate of layers 1..nlay, SW surface net flux (down - up);
+ * with respect to
+ *   inputs (nx = 3*nlay + 2): tlay of layers 1..nlay, h2ovmr (specific
+ *     humidity) of layers 1..nlay, tlev of levels 0..nlay, tsfc.
+ * The differentiated forward is RRTMG_TRANS_ANALYTIC in FP64 (the reference's
+ * transmittance tables are piecewise constant in optical depth); no counterpart
+ * in the reference, which has only the LW surface-temperature derivative
+ * (idrv = 1, rrtmg_lw_rtrnmr.f90:628-745).  The reverse sweeps of rtrnmr and
+ * spcvrt run per g-point with the layer optics recomputed from checkpointed
+ * per-layer setcoef inputs.  Arguments are those of rrtmg_lw_dev and
+ * rrtmg_sw_dev (device arrays, clear sky; tauaer_lw (ncol,nlay,16) optional,
+ * SW aerosols when iaer = 10).
+ *   jac  (ncol, ny, nx), column index fastest: jac[(x*ny + r)*ncol + c].
+ * Workspace: about 16*(nlay+2)*(3*nlay+3)*8 bytes per column (661 KB at
+ * 40 layers); split large column counts into several calls. */
+int rrtmg_jacobian_dev(rrtmg_gpu_handle h, void* stream, int ncol, int nlay,
+                       const double* play, const double* plev, const double* tlay, const double* tlev,
+                       const double* tsfc, const double* h2ovmr, const double* o3vmr, const double* co2vmr,
+                       const double* ch4vmr, const double* n2ovmr, const double* o2vmr,
+                       const double* cfc11vmr, const double* cfc12vmr, const double* cfc22vmr,
+                       const double* ccl4vmr, const double* emis, const double* tauaer_lw,
+                       const double* asdir, const double* asdif, const double* aldir, const double* aldif,
+                       const double* coszen, double adjes, int dyofyr, double scon, int iaer,
+                       const double* tauaer_sw, const double* ssaaer, const double* asmaer, double* jac);
+
+/* Vector-Jacobian product (one reverse sweep per g-point): given cotangents
+ * cot (ncol, ny) of the rows above, writes grad (ncol, nx) = cot^T J per
+ * column: grad[x*ncol + c].  Same arguments as rrtmg_jacobian_dev otherwise;
+ * no counterpart in the reference. */
+int rrtmg_vjp_dev(rrtmg_gpu_handle h, void* stream, int ncol, int nlay,
+                  const double* play, const double* plev, const double* tlay, const double* tlev,
+                  const double* tsfc, const double* h2ovmr, const double* o3vmr, const double* co2vmr,
+                  const double* ch4vmr, const double* n2ovmr, const double* o2vmr,
+                  const double* cfc11vmr, const double* cfc12vmr, const double* cfc22vmr,
+                  const double* ccl4vmr, const double* emis, const double* tauaer_lw,
+                  const double* asdir, const double* asdif, const double* aldir, const double* aldif,
+                  const double* coszen, double adjes, int dyofyr, double scon, int iaer,
+                  const double* tauaer_sw, const double* ssaaer, const double* asmaer,
+                  const double* cot, double* grad);
 
 /* Size of the library's static LW device scratch (64 MiB), held by every GPU
  * that loads the library until process exit.  At nlay = 40 a call needs about

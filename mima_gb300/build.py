@@ -29,6 +29,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 UNITS = {
     "kernels_fp64.cu": ["--fmad=false"],
     "kernels_split.cu": [],
+    "adjoint.cu": [],
     "tables_host.cu": [],
     "abi.cu": ["-Xcompiler", "-fvisibility=default"],
 }

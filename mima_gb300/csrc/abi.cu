@@ -14,6 +14,7 @@
 
 #include <cmath>
 
+#include "adjoint.h"
 #include "common.cuh"
 #include "launch.h"
 #include "rrtmg_gpu.h"
@@ -33,13 +34,14 @@ struct DevBuf {
 struct rrtmg_gpu_state {
   int device = 0;
   int precision = RRTMG_PREC_FP64;
+  int analytic = 0;  // 1: exp/tfn evaluated instead of looked up
   cudaStream_t stream = nullptr;
   HostTables host;
   double *lw_tab64 = nullptr, *sw_tab64 = nullptr, *lw_exp64 = nullptr, *lw_tfn64 = nullptr, *sw_exp64 = nullptr;
   double *totplnk = nullptr, *totplnkderiv = nullptr;
   float *lw_tab32 = nullptr, *sw_tab32 = nullptr, *lw_exp32 = nullptr, *lw_tfn32 = nullptr, *sw_exp32 = nullptr;
   unsigned* flags = nullptr;
-  DevBuf lw_ws, sw_ws, io;
+  DevBuf lw_ws, sw_ws, io, adj_ws;
   long long launches = 0;
   std::string err;
 };
@@ -174,11 +176,11 @@ int lw_enqueue(rrtmg_gpu_state* h, cudaStream_t s, void* base, int ncol, int nla
     const LwWorkT<float> w32 = work_as<float>(w);
     launch_lw_prep_split(in, w32, h->totplnk, h->totplnkderiv, ncol, nlay, idrv, h->flags, s);
     launch_lw_gpoint_split(prep_of(w32), in.emis, in.tauaer, h->lw_tab32, h->lw_exp32, h->lw_tfn32, w.bu, w.bd,
-                           w.bdu, ncol, nlay, idrv, nb, s);
+                           w.bdu, ncol, nlay, idrv, nb, h->analytic, s);
   } else {
     launch_lw_prep(in, w, h->totplnk, h->totplnkderiv, ncol, nlay, idrv, h->flags, s);
     launch_lw_gpoint_fp64(prep_of(w), in.emis, in.tauaer, h->lw_tab64, h->lw_exp64, h->lw_tfn64, w.bu, w.bd, w.bdu,
-                          ncol, nlay, idrv, nb, s);
+                          ncol, nlay, idrv, nb, h->analytic, s);
   }
   launch_lw_finalize(w.bu, w.bd, w.bdu, in.plev, ncol, nlay, idrv, uflx, dflx, hr, uflxc, dflxc, hrc, duflx_dt,
                      duflxc_dt, s);
@@ -197,6 +199,18 @@ int lw_run(rrtmg_gpu_state* h, cudaStream_t s, int ncol, int nlay, int idrv, con
   return lw_enqueue(h, s, h->lw_ws.p, ncol, nlay, idrv, in, uflx, dflx, hr, uflxc, dflxc, hrc, duflx_dt, duflxc_dt);
 }
 
+// Incident-flux scaling (inatm_sw, rrtmg_sw_rad.nomcica.f90:953-972): the
+// GCM's Earth-Sun factor, or Iqbal's day-of-year formula, times scon/1368.22.
+double adjflux_of(const rrtmg_gpu_state* h, double adjes, int dyofyr, double scon) {
+  double adjflx = adjes;
+  if (dyofyr > 0) {
+    const double gamma = 2. * h->host.sw.pi * (dyofyr - 1) / 365.;
+    adjflx = 1.000110 + .034221 * std::cos(gamma) + .001289 * std::sin(gamma) + .000719 * std::cos(2. * gamma) +
+             .000077 * std::sin(2. * gamma);
+  }
+  return adjflx * (scon / 1.36822e+03);
+}
+
 int sw_run(rrtmg_gpu_state* h, cudaStream_t s, int ncol, int nlay, int iaer, double adjes, int dyofyr, double scon,
            const SwIn& in, double* swuflx, double* swdflx, double* swhr, double* swuflxc, double* swdflxc,
            double* swhrc) {
@@ -205,29 +219,77 @@ int sw_run(rrtmg_gpu_state* h, cudaStream_t s, int ncol, int nlay, int iaer, dou
   int rc = ensure(h, h->sw_ws, need, s);
   if (rc) return rc;
   SwWork w = carve_sw(h->sw_ws.p, ncol, nlay, nullptr);
-  // Incident-flux scaling (inatm_sw, rrtmg_sw_rad.nomcica.f90:953-972): the
-  // GCM's Earth-Sun factor, or Iqbal's day-of-year formula, times scon/1368.22.
-  double adjflx = adjes;
-  if (dyofyr > 0) {
-    const double gamma = 2. * h->host.sw.pi * (dyofyr - 1) / 365.;
-    adjflx = 1.000110 + .034221 * std::cos(gamma) + .001289 * std::sin(gamma) + .000719 * std::cos(2. * gamma) +
-             .000077 * std::sin(2. * gamma);
-  }
-  const double adjflux = adjflx * (scon / 1.36822e+03);
+  const double adjflux = adjflux_of(h, adjes, dyofyr, scon);
   const int nb = sw_gpoint_blocks(h->host.sw, ncol);
   if (h->precision == RRTMG_PREC_SPLIT) {
     const SwWorkT<float> w32 = work_as<float>(w);
     launch_sw_prep_split(in, w32, ncol, nlay, h->flags, s);
     launch_sw_gpoint_split(prep_of(w32), in, adjflux, iaer, h->sw_tab32, h->sw_tab64, h->sw_exp32, w.su, w.sd, ncol,
-                           nlay, nb, s);
+                           nlay, nb, h->analytic, s);
   } else {
     launch_sw_prep(in, w, ncol, nlay, h->flags, s);
-    launch_sw_gpoint_fp64(prep_of(w), in, adjflux, iaer, h->sw_tab64, h->sw_exp64, w.su, w.sd, ncol, nlay, nb, s);
+    launch_sw_gpoint_fp64(prep_of(w), in, adjflux, iaer, h->sw_tab64, h->sw_exp64, w.su, w.sd, ncol, nlay, nb,
+                          h->analytic, s);
   }
   launch_sw_finalize(w.su, w.sd, in.plev, in.coszen, ncol, nlay, swuflx, swdflx, swhr, swuflxc, swdflxc, swhrc, s);
   h->launches += 3;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(h, e, "SW kernel launch");
+  return RRTMG_OK;
+}
+
+// Adjoint workspace: dual prep fields and band partial gradients.
+void carve_adj(void* base, int ncol, int nlay, int nseed_lw, int nseed_sw, AdjLwWork* lw, AdjSwWork* sw,
+               size_t* bytes) {
+  Carver c{(char*)base};
+  const size_t N = (size_t)ncol, L = (size_t)nlay;
+  AdjLwWork a;
+  a.idx = c.take<uint32_t>(L * N);
+  a.laytrop = c.take<int>(N);
+  a.fv = c.take<double>((size_t)LF_N * L * N);
+  a.ft = c.take<double>((size_t)LF_N * L * N);
+  a.fq = c.take<double>((size_t)LF_N * L * N);
+  a.play_v = c.take<double>(16 * L * N);
+  a.play_t = c.take<double>(16 * L * N);
+  a.plev_v = c.take<double>(16 * (L + 1) * N);
+  a.plev_t = c.take<double>(16 * (L + 1) * N);
+  a.pbnd_v = c.take<double>(16 * N);
+  a.pbnd_t = c.take<double>(16 * N);
+  a.secdiff = c.take<double>(16 * N);
+  a.dsec = c.take<double>(16 * L * N);
+  a.part = c.take<double>((size_t)kLwBands * nseed_lw * adj_lw_entries(nlay) * N);
+  AdjSwWork b;
+  b.idx = c.take<uint32_t>(L * N);
+  b.laytrop = c.take<int>(N);
+  b.laysolfr = c.take<int>(14 * N);
+  b.fv = c.take<double>((size_t)SF_N * L * N);
+  b.ft = c.take<double>((size_t)SF_N * L * N);
+  b.fq = c.take<double>((size_t)SF_N * L * N);
+  b.part = c.take<double>((size_t)kSwBands * nseed_sw * adj_sw_entries(nlay) * N);
+  if (lw) *lw = a;
+  if (sw) *sw = b;
+  if (bytes) *bytes = c.off;
+}
+
+// Jacobians (cot == nullptr) or vector-Jacobian products of the analytic
+// FP64 forward, enqueued on s.
+int adj_run(rrtmg_gpu_state* h, cudaStream_t s, int ncol, int nlay, const LwIn& lin, const SwIn& sin, int iaer,
+            double adjflux, const double* cot, double* out) {
+  const int nseed_lw = cot ? 1 : nlay + 2, nseed_sw = cot ? 1 : nlay + 1;
+  size_t need;
+  carve_adj(nullptr, ncol, nlay, nseed_lw, nseed_sw, nullptr, nullptr, &need);
+  int rc = ensure(h, h->adj_ws, need, s);
+  if (rc) return rc;
+  AdjLwWork lw;
+  AdjSwWork sw;
+  carve_adj(h->adj_ws.p, ncol, nlay, nseed_lw, nseed_sw, &lw, &sw, nullptr);
+  launch_adj_lw(lin, lw, h->totplnk, h->lw_tab64, cot, nseed_lw, ncol, nlay, lw_gpoint_blocks(h->host.lw, ncol), s);
+  launch_adj_sw(sin, sw, adjflux, iaer, h->sw_tab64, cot, nseed_sw, ncol, nlay, sw_gpoint_blocks(h->host.sw, ncol),
+                s);
+  launch_adj_finalize(lw, sw, lin.plev, sin.coszen, nseed_lw, nseed_sw, ncol, nlay, out, cot != nullptr, s);
+  h->launches += 5;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(h, e, "adjoint kernel launch");
   return RRTMG_OK;
 }
 
@@ -310,6 +372,7 @@ int rrtmg_gpu_init(double cpdair, const char* table_blob, int device, rrtmg_gpu_
   if (e == cudaSuccess) e = cudaMemset(h->flags, 0, sizeof(unsigned));
   if (e == cudaSuccess) e = upload_constants_fp64(h->host.lw, h->host.sw);
   if (e == cudaSuccess) e = upload_constants_split(h->host.lw, h->host.sw);
+  if (e == cudaSuccess) e = upload_constants_adjoint(h->host.lw, h->host.sw);
   if (e != cudaSuccess) {
     std::fprintf(stderr, "rrtmg_gpu_init: %s\n", cudaGetErrorString(e));
     h->device = device;
@@ -327,7 +390,7 @@ int rrtmg_gpu_finalize(rrtmg_gpu_handle h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   void* ptrs[] = {h->lw_tab64, h->sw_tab64, h->lw_exp64, h->lw_tfn64, h->sw_exp64, h->totplnk, h->totplnkderiv,
                   h->lw_tab32, h->sw_tab32, h->lw_exp32, h->lw_tfn32, h->sw_exp32, h->flags, h->lw_ws.p,
-                  h->sw_ws.p, h->io.p};
+                  h->sw_ws.p, h->io.p, h->adj_ws.p};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -340,6 +403,14 @@ int rrtmg_gpu_set_precision(rrtmg_gpu_handle h, int precision) {
   if (precision != RRTMG_PREC_FP64 && precision != RRTMG_PREC_SPLIT)
     return fail(h, RRTMG_ERR_ARG, "precision must be RRTMG_PREC_FP64 or RRTMG_PREC_SPLIT");
   h->precision = precision;
+  return RRTMG_OK;
+}
+
+int rrtmg_gpu_set_transcendentals(rrtmg_gpu_handle h, int mode) {
+  if (!valid_handle(h)) return RRTMG_ERR_ARG;
+  if (mode != RRTMG_TRANS_TABLE && mode != RRTMG_TRANS_ANALYTIC)
+    return fail(h, RRTMG_ERR_ARG, "mode must be RRTMG_TRANS_TABLE or RRTMG_TRANS_ANALYTIC");
+  h->analytic = mode == RRTMG_TRANS_ANALYTIC;
   return RRTMG_OK;
 }
 
@@ -414,6 +485,62 @@ int rrtmg_sw_dev(rrtmg_gpu_handle h, void* stream, int ncol, int nlay, int icld,
           coszen, tauaer, ssaaer, asmaer};
   return sw_run(h, (cudaStream_t)stream, ncol, nlay, iaer, adjes, dyofyr, scon, in, swuflx, swdflx, swhr, swuflxc,
                 swdflxc, swhrc);
+}
+
+static int adjoint_entry(rrtmg_gpu_handle h, void* stream, int ncol, int nlay, const double* play,
+                         const double* plev, const double* tlay, const double* tlev, const double* tsfc,
+                         const double* h2ovmr, const double* o3vmr, const double* co2vmr, const double* ch4vmr,
+                         const double* n2ovmr, const double* o2vmr, const double* cfc11vmr,
+                         const double* cfc12vmr, const double* cfc22vmr, const double* ccl4vmr,
+                         const double* emis, const double* tauaer_lw, const double* asdir, const double* asdif,
+                         const double* aldir, const double* aldif, const double* coszen, double adjes, int dyofyr,
+                         double scon, int iaer, const double* tauaer_sw, const double* ssaaer,
+                         const double* asmaer, const double* cot, double* out) {
+  if (!valid_handle(h)) return RRTMG_ERR_ARG;
+  int rc = check_dims(h, ncol, nlay);
+  if (rc) return rc;
+  if (iaer != 0 && iaer != 10) return fail(h, RRTMG_ERR_UNSUPPORTED, "iaer must be 0 or 10");
+  if (!play || !plev || !tlay || !tlev || !tsfc || !h2ovmr || !o3vmr || !co2vmr || !asdir || !asdif || !aldir ||
+      !aldif || !coszen || !out)
+    return fail(h, RRTMG_ERR_ARG, "a required array pointer is null");
+  if (iaer == 10 && (!tauaer_sw || !ssaaer || !asmaer))
+    return fail(h, RRTMG_ERR_ARG, "iaer = 10 needs tauaer/ssaaer/asmaer");
+  if (!(scon > 0.0)) return fail(h, RRTMG_ERR_ARG, "scon must be positive");
+  if ((long long)kLwBands * (nlay + 2) * (3LL * nlay + 3) * ncol > (1LL << 40))
+    return fail(h, RRTMG_ERR_ARG, "too many columns for one Jacobian call; split the columns");
+  cudaSetDevice(h->device);
+  LwIn lin{play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr, cfc11vmr, cfc12vmr,
+           cfc22vmr, ccl4vmr, emis, tauaer_lw};
+  SwIn sin{play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr, asdir, asdif, aldir, aldif,
+           coszen, tauaer_sw, ssaaer, asmaer};
+  return adj_run(h, (cudaStream_t)stream, ncol, nlay, lin, sin, iaer, adjflux_of(h, adjes, dyofyr, scon), cot, out);
+}
+
+int rrtmg_jacobian_dev(rrtmg_gpu_handle h, void* stream, int ncol, int nlay, const double* play, const double* plev,
+                       const double* tlay, const double* tlev, const double* tsfc, const double* h2ovmr,
+                       const double* o3vmr, const double* co2vmr, const double* ch4vmr, const double* n2ovmr,
+                       const double* o2vmr, const double* cfc11vmr, const double* cfc12vmr, const double* cfc22vmr,
+                       const double* ccl4vmr, const double* emis, const double* tauaer_lw, const double* asdir,
+                       const double* asdif, const double* aldir, const double* aldif, const double* coszen,
+                       double adjes, int dyofyr, double scon, int iaer, const double* tauaer_sw,
+                       const double* ssaaer, const double* asmaer, double* jac) {
+  return adjoint_entry(h, stream, ncol, nlay, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr,
+                       o2vmr, cfc11vmr, cfc12vmr, cfc22vmr, ccl4vmr, emis, tauaer_lw, asdir, asdif, aldir, aldif,
+                       coszen, adjes, dyofyr, scon, iaer, tauaer_sw, ssaaer, asmaer, nullptr, jac);
+}
+
+int rrtmg_vjp_dev(rrtmg_gpu_handle h, void* stream, int ncol, int nlay, const double* play, const double* plev,
+                  const double* tlay, const double* tlev, const double* tsfc, const double* h2ovmr,
+                  const double* o3vmr, const double* co2vmr, const double* ch4vmr, const double* n2ovmr,
+                  const double* o2vmr, const double* cfc11vmr, const double* cfc12vmr, const double* cfc22vmr,
+                  const double* ccl4vmr, const double* emis, const double* tauaer_lw, const double* asdir,
+                  const double* asdif, const double* aldir, const double* aldif, const double* coszen,
+                  double adjes, int dyofyr, double scon, int iaer, const double* tauaer_sw, const double* ssaaer,
+                  const double* asmaer, const double* cot, double* grad) {
+  if (!cot) return fail(h, RRTMG_ERR_ARG, "rrtmg_vjp_dev needs cotangents");
+  return adjoint_entry(h, stream, ncol, nlay, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr,
+                       o2vmr, cfc11vmr, cfc12vmr, cfc22vmr, ccl4vmr, emis, tauaer_lw, asdir, asdif, aldir, aldif,
+                       coszen, adjes, dyofyr, scon, iaer, tauaer_sw, ssaaer, asmaer, cot, grad);
 }
 
 int rrtmg_lw_c(rrtmg_gpu_handle h, int ncol, int nlay, int icld, int idrv, const double* play, const double* plev,

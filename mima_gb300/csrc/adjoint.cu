@@ -1,0 +1,890 @@
+// Adjoint (reverse-mode) kernels of the clear-sky LW and SW paths: Jacobians
+// of the heating rates, OLR and surface net fluxes with respect to layer
+// temperature, specific humidity, level temperature and surface temperature,
+// or vector-Jacobian products with caller cotangents.
+//
+// The differentiated forward is the analytic-transcendental variant of the
+// FP64 path (exp / tau-transition function evaluated instead of looked up in
+// the 10001-entry tables, which are piecewise constant in the optical depth).
+// Per (column, g-point) thread:
+//   1. the layer optics are recomputed from checkpointed per-layer inputs (the
+//      setcoef fields with their d/dT and d/dq tangents, written once per
+//      column by the dual prep kernels below), through the same templated gas
+//      optics the forward runs, instantiated on dual numbers;
+//   2. the forward recursions (rtrnmr clear branch; spcvrt adding method)
+//      run once and keep their level states;
+//   3. for every cotangent seed the recursions are reversed (rtrnmr: two
+//      first-order sweeps; spcvrt: the reverse of the upward reflectance and
+//      of the downward transmission sweeps) and the layer gradients are
+//      contracted with the local tangents;
+//   4. gradients are summed over the band's g-points in FP64 (shared-memory
+//      staging, one (column, entry) sum per lane) into per-band partials,
+//      which a finalize kernel weights and sums over bands.
+#include <cuda_runtime.h>
+
+#include "adjoint.h"
+#include "dual.cuh"
+#include "kernels.cuh"
+#include "launch.h"
+
+namespace rrtmg {
+
+using D2 = Dual<double>;
+
+// ---------------------------------------------------------------------------
+// LW dual prep: inatm + setcoef (rrtmg_lw_rad.nomcica.f90:572-901,
+// rrtmg_lw_setcoef.f90:31-415) per layer with tangents d/dtlay and d/dq of the
+// same layer; Planck functions with their temperature slopes; secdiff
+// (rrtmg_lw_rtrnmr.f90:271-279) with d secdiff / d q of every layer through
+// the column water vapour pwvcm.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) adj_lw_prep_kernel(LwIn in, AdjLwWork w, const double* __restrict__ totplnk,
+                                                          int ncol, int nlay) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncol) return;
+  const LwConst& C = c_lw;
+  const double amd = 28.9660, amw = 18.0160, amdw = 1.607793, amdo = 0.603428;
+  const double stpfac = 296. / 1013.;
+  const size_t N = (size_t)ncol;
+  const size_t fstride = (size_t)nlay * N;
+  auto A = [&](const double* p, int l) { return __ldg(p + (size_t)col + N * (size_t)(l - 1)); };
+  auto P = [&](int ind, int b) { return __ldg(totplnk + (ind - 1) + 181 * (b - 1)); };
+
+  const double tbound = __ldg(in.tsfc + col);
+  double pz_prev = A(in.plev, 1);
+  const double pz0 = pz_prev;
+  const double tz0 = A(in.tlev, 1);
+  const int indbound = clampi((int)(tbound - 159.), 1, 180);
+  const double tbndfrac = tbound - 159. - (double)indbound;
+  const int indlev0 = clampi((int)(tz0 - 159.), 1, 180);
+  const double t0frac = tz0 - 159. - (double)indlev0;
+  for (int b = 1; b <= 16; ++b) {
+    const double semiss = in.emis ? __ldg(in.emis + col + N * (b - 1)) : 1.0;
+    double slope = P(indbound + 1, b) - P(indbound, b);
+    w.pbnd_v[(b - 1) * N + col] = semiss * (P(indbound, b) + tbndfrac * slope);
+    w.pbnd_t[(b - 1) * N + col] = semiss * slope;
+    slope = P(indlev0 + 1, b) - P(indlev0, b);
+    w.plev_v[((size_t)(b - 1) * (nlay + 1)) * N + col] = P(indlev0, b) + t0frac * slope;
+    w.plev_t[((size_t)(b - 1) * (nlay + 1)) * N + col] = slope;
+  }
+
+  double amttl = 0.0, wvttl = 0.0;
+  int laytrop = 0;
+  for (int l = 1; l <= nlay; ++l) {
+    const double pavel = A(in.play, l);
+    const D2 tavel(A(in.tlay, l), 1.0, 0.0);
+    const double pz_l = A(in.plev, l + 1), tz_l = A(in.tlev, l + 1);
+    const D2 h2o(A(in.h2o, l), 0.0, 1.0);
+    D2 wk1 = (h2o / (1. - h2o)) * amdw;
+    const double wk2 = A(in.co2, l);
+    const double wk3 = A(in.o3, l) * amdo;
+    const double wk4 = in.n2o ? A(in.n2o, l) : 0.0;
+    const double wk6 = in.ch4 ? A(in.ch4, l) : 0.0;
+    const double wk7 = in.o2 ? A(in.o2, l) : 0.0;
+    const D2 amm = (1. - wk1) * amd + wk1 * amw;
+    const D2 coldry = (pz_prev - pz_l) * 1.e3 * C.avogad / (1.e2 * C.grav * amm * (1. + wk1));
+    const double summol = wk2 + wk3 + wk4 + 0.0 + wk6 + wk7;
+    const D2 wbrodl = coldry * (1. - summol);
+    wk1 = coldry * wk1;
+    const D2 cwk2 = coldry * wk2, cwk3 = coldry * wk3, cwk4 = coldry * wk4, cwk6 = coldry * wk6,
+             cwk7 = coldry * wk7;
+    amttl = amttl + coldry.v + wk1.v;
+    wvttl = wvttl + wk1.v;
+    // d(wvttl)/dq_l and d(amttl)/dq_l, for d pwvcm / dq_l below
+    w.dsec[(size_t)(l - 1) * N + col] = wk1.q;
+    w.dsec[fstride + (size_t)(l - 1) * N + col] = coldry.q + wk1.q;
+    const D2 wx1 = in.ccl4 ? coldry * A(in.ccl4, l) * 1.e-20 : coldry * 0.0;
+    const D2 wx2 = in.cfc11 ? coldry * A(in.cfc11, l) * 1.e-20 : coldry * 0.0;
+    const D2 wx3 = in.cfc12 ? coldry * A(in.cfc12, l) * 1.e-20 : coldry * 0.0;
+    const D2 wx4 = in.cfc22 ? coldry * A(in.cfc22, l) * 1.e-20 : coldry * 0.0;
+
+    const int indlay = clampi((int)(tavel.v - 159.), 1, 180);
+    const double tlayfrac = tavel.v - 159. - (double)indlay;
+    const int indlev = clampi((int)(tz_l - 159.), 1, 180);
+    const double tlevfrac = tz_l - 159. - (double)indlev;
+    for (int b = 1; b <= 16; ++b) {
+      const double sl = P(indlay + 1, b) - P(indlay, b);
+      const double sv = P(indlev + 1, b) - P(indlev, b);
+      w.play_v[((size_t)(b - 1) * nlay + (l - 1)) * N + col] = P(indlay, b) + tlayfrac * sl;
+      w.play_t[((size_t)(b - 1) * nlay + (l - 1)) * N + col] = sl;
+      w.plev_v[((size_t)(b - 1) * (nlay + 1) + l) * N + col] = P(indlev, b) + tlevfrac * sv;
+      w.plev_t[((size_t)(b - 1) * (nlay + 1) + l) * N + col] = sv;
+    }
+
+    const double plog = log(pavel);
+    const int jp = clampi((int)(36. - 5 * (plog + 0.04)), 1, 58);
+    const int jp1 = jp + 1;
+    const double fp = 5. * (C.preflog[jp - 1] - plog);
+    const int jt = clampi((int)(3. + (tavel.v - C.tref[jp - 1]) / 15.), 1, 4);
+    const D2 ft = ((tavel - C.tref[jp - 1]) / 15.) - (double)(jt - 3);
+    const int jt1 = clampi((int)(3. + (tavel.v - C.tref[jp1 - 1]) / 15.), 1, 4);
+    const D2 ft1 = ((tavel - C.tref[jp1 - 1]) / 15.) - (double)(jt1 - 3);
+    const D2 water = wk1 / coldry;
+    const D2 scalefac = (pavel * stpfac) / tavel;
+    D2 forfac, forfrac, selffac, selffrac(0.0), minorfrac, factor;
+    int indfor, indself = 1, indminor;
+    if (plog > 4.56) {
+      laytrop = laytrop + 1;
+      forfac = scalefac / (1. + water);
+      factor = (332.0 - tavel) / 36.0;
+      indfor = min(2, max(1, (int)factor.v));
+      forfrac = factor - (double)indfor;
+      selffac = water * forfac;
+      factor = (tavel - 188.0) / 7.2;
+      indself = min(9, max(1, (int)factor.v - 7));
+      selffrac = factor - (double)(indself + 7);
+    } else {
+      forfac = scalefac / (1. + water);
+      factor = (tavel - 188.0) / 36.0;
+      indfor = 3;
+      forfrac = factor - 1.0;
+      selffac = water * forfac;
+    }
+    const D2 scaleminor = pavel / tavel;
+    const D2 scaleminorn2 = (pavel / tavel) * (wbrodl / (coldry + wk1));
+    factor = (tavel - 180.8) / 7.2;
+    indminor = min(18, max(1, (int)factor.v));
+    minorfrac = factor - (double)indminor;
+
+    const D2 colh2o = 1.e-20 * wk1;
+    D2 colco2 = 1.e-20 * cwk2, colo3 = 1.e-20 * cwk3, coln2o = 1.e-20 * cwk4;
+    D2 colco = coldry * 0.0, colch4 = 1.e-20 * cwk6;
+    const D2 colo2 = 1.e-20 * cwk7;
+    if (colco2.v == 0.) colco2 = 1.e-32 * coldry;
+    if (colo3.v == 0.) colo3 = 1.e-32 * coldry;
+    if (coln2o.v == 0.) coln2o = 1.e-32 * coldry;
+    if (colco.v == 0.) colco = 1.e-32 * coldry;
+    if (colch4.v == 0.) colch4 = 1.e-32 * coldry;
+    const D2 colbrd = 1.e-20 * wbrodl;
+    const double compfp = 1. - fp;
+    const size_t o = (size_t)(l - 1) * N + col;
+    auto put = [&](int fld, const D2& x) {
+      const size_t i = (size_t)fld * fstride + o;
+      w.fv[i] = x.v;
+      w.ft[i] = x.t;
+      w.fq[i] = x.q;
+    };
+    put(LF_PAVEL, D2(pavel));
+    put(LF_COLDRY, coldry);
+    put(LF_COLH2O, colh2o);
+    put(LF_COLCO2, colco2);
+    put(LF_COLO3, colo3);
+    put(LF_COLN2O, coln2o);
+    put(LF_COLCO, colco);
+    put(LF_COLCH4, colch4);
+    put(LF_COLO2, colo2);
+    put(LF_COLBRD, colbrd);
+    put(LF_FAC10, compfp * ft);
+    put(LF_FAC00, compfp * (1. - ft));
+    put(LF_FAC11, fp * ft1);
+    put(LF_FAC01, fp * (1. - ft1));
+    put(LF_SELFFAC, colh2o * selffac);
+    put(LF_SELFFRAC, selffrac);
+    put(LF_FORFAC, colh2o * forfac);
+    put(LF_FORFRAC, forfrac);
+    put(LF_MINORFRAC, minorfrac);
+    put(LF_SCALEMINOR, scaleminor);
+    put(LF_SCALEMINORN2, scaleminorn2);
+    put(LF_WX1, wx1);
+    put(LF_WX2, wx2);
+    put(LF_WX3, wx3);
+    put(LF_WX4, wx4);
+    w.idx[o] = pack_idx(jp, jt, jt1, indself, indfor, indminor);
+    pz_prev = pz_l;
+  }
+  w.laytrop[col] = laytrop;
+  // secdiff(pwvcm) and d secdiff / d q_l = secdiff'(pwvcm) pwvcm (dwv_l / wvttl - dam_l / amttl)
+  const double wvsh = (amw * wvttl) / (amd * amttl);
+  const double pwvcm = wvsh * (1.e3 * pz0) / (1.e2 * C.grav);
+  const double a0[16] = {1.66, 1.55, 1.58, 1.66, 1.54, 1.454, 1.89, 1.33, 1.668, 1.66, 1.66, 1.66, 1.66, 1.66, 1.66, 1.66};
+  const double a1[16] = {0.00, 0.25, 0.22, 0.00, 0.13, 0.446, -0.10, 0.40, -0.006, 0, 0, 0, 0, 0, 0, 0};
+  const double a2[16] = {0.00, -12.0, -11.7, 0.00, -0.72, -0.243, 0.19, -0.062, 0.414, 0, 0, 0, 0, 0, 0, 0};
+  double dsdp[16];
+  for (int b = 1; b <= 16; ++b) {
+    double s, d = 0.0;
+    if (b == 1 || b == 4 || b >= 10) {
+      s = 1.66;
+    } else {
+      const double e = exp(a2[b - 1] * pwvcm);
+      s = a0[b - 1] + a1[b - 1] * e;
+      d = a1[b - 1] * a2[b - 1] * e;
+      if (s > 1.80) { s = 1.80; d = 0.0; }
+      if (s < 1.50) { s = 1.50; d = 0.0; }
+    }
+    w.secdiff[(b - 1) * N + col] = s;
+    dsdp[b - 1] = d;
+  }
+  // dsec currently holds dwv_l (rows 0..nlay-1) and dam_l (rows nlay..2nlay-1)
+  // in its first two band planes; overwrite band by band from the top band
+  // down so that the two source planes are read before band 1 and 2 reuse them.
+  for (int l = 1; l <= nlay; ++l) {
+    const size_t o = (size_t)(l - 1) * N + col;
+    const double dp = pwvcm * (w.dsec[o] / wvttl - w.dsec[fstride + o] / amttl);
+    for (int b = 16; b >= 1; --b) w.dsec[(size_t)(b - 1) * fstride + o] = dsdp[b - 1] * dp;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 sums over the g-points of a band of per-lane FP64 gradient entries:
+// entries are staged in shared memory W at a time (rows padded to kRow), then
+// lane (cs, sl) sums entry sl of column sub-index cs over the band's NG lanes
+// in g order.  Warp-uniform calls only.
+// ---------------------------------------------------------------------------
+template <int W, int NG>
+struct GRed {
+  double* buf;  // this warp's [W][kRow]
+  int lane, n, first;
+  __device__ __forceinline__ void put(double v) { buf[n * kRow + lane] = v; }
+  template <class Store>
+  __device__ __forceinline__ void flush(Store&& st) {
+    __syncwarp();
+    const int sl = lane % W, cs = lane / W;
+    if (sl < n) {
+      const double* row = buf + sl * kRow + cs * W;
+      double acc = 0.0;
+#pragma unroll
+      for (int g = 0; g < NG; ++g) acc += row[g];
+      st(first + sl, cs, acc);
+    }
+    __syncwarp();
+    first += n;
+    n = 0;
+  }
+  template <class Store>
+  __device__ __forceinline__ void next(Store&& st) {
+    if (++n == W) flush(st);
+  }
+};
+constexpr int kRedDoubles = (kBlock / 32) * 16 * kRow;
+
+// Dual view of the checkpointed setcoef fields of one (layer, column).
+struct LwDualView {
+  const double *fv, *ft, *fq;
+  size_t fstride, o;
+  __device__ __forceinline__ D2 operator()(int fld) const {
+    const size_t i = (size_t)fld * fstride + o;
+    return D2(__ldg(fv + i), __ldg(ft + i), __ldg(fq + i));
+  }
+};
+
+// ---------------------------------------------------------------------------
+// LW reverse sweep of one g-point (rrtmg_lw_rtrnmr.f90:505-616 downward,
+// :628-713 upward, clear branch, analytic transcendentals).
+//   Recursions per g:  D_{l-1} = t_l D_l + sd_l,  U_l = t_l U_{l-1} + su_l,
+//   U_0 = fracs_1 * emis * B(tsfc) + (1 - emis) D_0,  t = 1 - atr,
+//   sd = atr * bbd, su = atr * bbu.
+//   Outputs per band (weight wtdiff * delwave * fluxfac applied at finalize):
+//   div_k = (U_{k-1} - U_k) - (D_{k-1} - D_k) for the heating of layer k,
+//   OLR = U_nlay, surface net = U_0 - D_0.
+//   Seed c: Phi = sum_k c_k div_k + c_olr U_nlay + c_sfc (U_0 - D_0).
+//   Adjoints: lamU_nlay = aU_nlay, lamU_m = aU_m + t_{m+1} lamU_{m+1};
+//             lamD_0 = aD_0 + (1 - emis) lamU_0, lamD_m = aD_m + t_m lamD_{m-1};
+//   dPhi/dt_l = lamU_l U_{l-1} + lamD_{l-1} D_l, dPhi/dsd_l = lamD_{l-1},
+//   dPhi/dsu_l = lamU_l, dPhi/drad0 = lamU_0, then the chain rule through the
+//   layer tangents (tlay, q, secdiff, tlev below / above).
+// ---------------------------------------------------------------------------
+template <int B, int MAXL>
+__device__ __forceinline__ void lw_adj_band(const LwIn& in, const AdjLwWork& w, const double* __restrict__ tab,
+                                            const double* __restrict__ cot, int nseed, int ncol, int nlay, int blk,
+                                            double* sred) {
+  constexpr int NG = lw_ng(B);
+  constexpr int W = pow2ceil(NG);
+  constexpr int CPB = kBlock / W;
+  const int lane_col = threadIdx.x / W, g = threadIdx.x % W;
+  const int col = blk * CPB + lane_col;
+  const bool valid = col < ncol;
+  const int c = valid ? col : ncol - 1;
+  const int gg = g < NG ? g : NG - 1;
+  const size_t N = (size_t)ncol;
+  const size_t fstride = (size_t)nlay * N;
+  const int lt = w.laytrop[c];
+  const double secdiff = w.secdiff[(B - 1) * N + c];
+  const double rec_6 = 0.166667;
+  const int E = 3 * nlay + 3;
+
+  // Layer state (index l-1) and level radiances.
+  double atr[MAXL], bbu[MAXL];
+  double tT[MAXL], dT[MAXL], uT[MAXL];  // d(t, sd, su)/dtlay
+  double tQ[MAXL], dQ[MAXL], uQ[MAXL];  // d(t, sd, su)/dq
+  double tS[MAXL], dS[MAXL], uS[MAXL];  // d(t, sd, su)/dsecdiff
+  double dLb[MAXL], uLt[MAXL];          // dsd/dtlev below, dsu/dtlev above
+  double Dl[MAXL + 1], Ul[MAXL + 1], lamU[MAXL + 1];
+
+  // 1. layer optics with tangents (recomputed from the checkpointed fields) and
+  //    the downward recursion
+  double radld = 0.0;
+  Dl[nlay] = 0.0;
+  D2 fr1;
+  for (int lev = nlay; lev >= 1; --lev) {
+    const int k = lev - 1;
+    const size_t o = (size_t)k * N + c;
+    const Idx ix = unpack_idx(__ldg(w.idx + o));
+    LwDualView L{w.fv, w.ft, w.fq, fstride, o};
+    D2 taug, fracs;
+    lw_gas<B, D2>(c_lw, c_lw, L, ix, lev <= lt, gg, tab, taug, fracs);
+    const double ta = in.tauaer ? __ldg(in.tauaer + c + N * ((size_t)k + (size_t)nlay * (B - 1))) : 0.0;
+    const double taut = taug.v + ta;
+    double od = secdiff * taut, odT = secdiff * taug.t, odQ = secdiff * taug.q, odS = taut;
+    if (od < 0.0) od = odT = odQ = odS = 0.0;
+    double a, a_d, tf, tf_d;
+    if (od <= 0.06) {
+      a = od - 0.5 * od * od;
+      a_d = 1.0 - od;
+      tf = rec_6 * od;
+      tf_d = rec_6;
+    } else {
+      const double e = exp(-od), om = 1.0 - e;
+      a = om;
+      a_d = e;
+      tf = 1.0 - 2.0 * ((1.0 / od) - (e / om));
+      tf_d = 2.0 / (od * od) - 2.0 * e / (om * om);
+    }
+    const double plf = fracs.v;
+    const size_t ol = ((size_t)(B - 1) * nlay + k) * N + c;
+    const double blay = __ldg(w.play_v + ol), blay_t = __ldg(w.play_t + ol);
+    const size_t ou = ((size_t)(B - 1) * (nlay + 1) + lev) * N + c, od_ = ou - N;
+    const double pup = __ldg(w.plev_v + ou), pup_t = __ldg(w.plev_t + ou);
+    const double pdn = __ldg(w.plev_v + od_), pdn_t = __ldg(w.plev_t + od_);
+    const double dpup = pup - blay, dpdn = pdn - blay;
+    const double bd = plf * (blay + tf * dpdn), bu = plf * (blay + tf * dpup);
+    atr[k] = a;
+    bbu[k] = bu;
+    auto tang = [&](double odx, double dplf, double dbl, double& ot, double& osd, double& osu) {
+      const double da = a_d * odx, dtf = tf_d * odx;
+      const double dbd = dplf * (blay + tf * dpdn) + plf * (dbl + dtf * dpdn - tf * dbl);
+      const double dbu = dplf * (blay + tf * dpup) + plf * (dbl + dtf * dpup - tf * dbl);
+      ot = -da;
+      osd = da * bd + a * dbd;
+      osu = da * bu + a * dbu;
+    };
+    tang(odT, fracs.t, blay_t, tT[k], dT[k], uT[k]);
+    tang(odQ, fracs.q, 0.0, tQ[k], dQ[k], uQ[k]);
+    tang(odS, 0.0, 0.0, tS[k], dS[k], uS[k]);
+    dLb[k] = a * plf * tf * pdn_t;
+    uLt[k] = a * plf * tf * pup_t;
+    radld = radld + (bd - radld) * a;
+    Dl[k] = radld;
+    if (lev == 1) fr1 = fracs;
+  }
+  // 2. upward recursion
+  const double pb = __ldg(w.pbnd_v + (B - 1) * N + c), pb_t = __ldg(w.pbnd_t + (B - 1) * N + c);
+  const double semiss = in.emis ? __ldg(in.emis + c + N * (B - 1)) : 1.0;
+  const double reflect = 1.0 - semiss;
+  Ul[0] = fr1.v * pb + reflect * Dl[0];
+  for (int l = 1; l <= nlay; ++l) Ul[l] = Ul[l - 1] + (bbu[l - 1] - Ul[l - 1]) * atr[l - 1];
+
+  // 3. reverse sweeps, one cotangent seed at a time
+  const int wib = threadIdx.x >> 5;
+  const int wcol0 = blk * CPB + (wib * 32) / W;
+  const double heatfac = c_lw.heatfac;
+  for (int s = 0; s < nseed; ++s) {
+    auto cdiv = [&](int kk) -> double {  // cotangent of div_kk (kk = 1..nlay), flux units
+      if (kk < 1 || kk > nlay) return 0.0;
+      const double hs = heatfac / (__ldg(in.plev + (size_t)(kk - 1) * N + c) - __ldg(in.plev + (size_t)kk * N + c));
+      if (cot) return __ldg(cot + (size_t)(kk - 1) * N + c) * hs;
+      return s == kk - 1 ? hs : 0.0;
+    };
+    const double colr = cot ? __ldg(cot + (size_t)nlay * N + c) : (s == nlay ? 1.0 : 0.0);
+    const double csfc = cot ? __ldg(cot + (size_t)(nlay + 1) * N + c) : (s == nlay + 1 ? 1.0 : 0.0);
+    auto aU = [&](int m) { return cdiv(m + 1) - cdiv(m) + (m == nlay ? colr : 0.0) + (m == 0 ? csfc : 0.0); };
+    auto aD = [&](int m) { return -cdiv(m + 1) + cdiv(m) - (m == 0 ? csfc : 0.0); };
+    lamU[nlay] = aU(nlay);
+    for (int m = nlay - 1; m >= 0; --m) lamU[m] = aU(m) + (1.0 - atr[m]) * lamU[m + 1];
+    GRed<W, NG> red{sred + wib * W * kRow, (int)(threadIdx.x & 31), 0, 0};
+    auto store = [&](int e, int cs, double v) {
+      const int cc = wcol0 + cs;
+      if (cc < ncol) w.part[(((size_t)(B - 1) * nseed + s) * E + e) * N + cc] = v;
+    };
+    double lamD = aD(0) + reflect * lamU[0];
+    double gS = 0.0, accLev = 0.0;
+    for (int l = 1; l <= nlay; ++l) {
+      const int k = l - 1;
+      const double gt = lamU[l] * Ul[l - 1] + lamD * Dl[l];
+      const double gsd = lamD, gsu = lamU[l];
+      double gT = gt * tT[k] + gsd * dT[k] + gsu * uT[k];
+      double gQ = gt * tQ[k] + gsd * dQ[k] + gsu * uQ[k];
+      if (l == 1) {
+        gT += lamU[0] * fr1.t * pb;
+        gQ += lamU[0] * fr1.q * pb;
+      }
+      gS += gt * tS[k] + gsd * dS[k] + gsu * uS[k];
+      const double gLev = accLev + gsd * dLb[k];
+      accLev = gsu * uLt[k];
+      red.put(gT);
+      red.next(store);
+      red.put(gQ);
+      red.next(store);
+      red.put(gLev);
+      red.next(store);
+      lamD = aD(l) + (1.0 - atr[k]) * lamD;
+    }
+    red.put(accLev);
+    red.next(store);
+    red.put(lamU[0] * fr1.v * pb_t);
+    red.next(store);
+    red.put(gS);
+    red.next(store);
+    if (red.n) red.flush(store);
+  }
+}
+
+template <int MAXL>
+__global__ void __launch_bounds__(kBlock) lw_adj_kernel(LwIn in, AdjLwWork w, const double* __restrict__ tab,
+                                                        const double* __restrict__ cot, int nseed, int ncol,
+                                                        int nlay) {
+  __shared__ double sred[kRedDoubles];
+  int blk = blockIdx.x, band = 0;
+  for (; band < kLwBands; ++band) {
+    const int nb = lw_blocks_for_band(c_lw.band[band].ngpad, ncol);
+    if (blk < nb) break;
+    blk -= nb;
+  }
+#define RRTMG_LW_ADJ_CASE(b) \
+  case b - 1: lw_adj_band<b, MAXL>(in, w, tab, cot, nseed, ncol, nlay, blk, sred); break;
+  switch (band) {
+    RRTMG_LW_ADJ_CASE(1) RRTMG_LW_ADJ_CASE(2) RRTMG_LW_ADJ_CASE(3) RRTMG_LW_ADJ_CASE(4) RRTMG_LW_ADJ_CASE(5)
+    RRTMG_LW_ADJ_CASE(6) RRTMG_LW_ADJ_CASE(7) RRTMG_LW_ADJ_CASE(8) RRTMG_LW_ADJ_CASE(9) RRTMG_LW_ADJ_CASE(10)
+    RRTMG_LW_ADJ_CASE(11) RRTMG_LW_ADJ_CASE(12) RRTMG_LW_ADJ_CASE(13) RRTMG_LW_ADJ_CASE(14) RRTMG_LW_ADJ_CASE(15)
+    RRTMG_LW_ADJ_CASE(16)
+    default: break;
+  }
+#undef RRTMG_LW_ADJ_CASE
+}
+
+// ---------------------------------------------------------------------------
+// SW dual prep: inatm_sw + setcoef_sw (rrtmg_sw_rad.nomcica.f90:761-1101,
+// rrtmg_sw_setcoef.f90:30-286) per layer with tangents d/dtlay and d/dq of the
+// same layer, and the solar-source layer of every band (as the forward prep).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) adj_sw_prep_kernel(SwIn in, AdjSwWork w, int ncol, int nlay) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncol) return;
+  const SwConst& C = c_sw;
+  const double amd = 28.9660, amw = 18.0160, amdw = 1.607793, amdo = 0.603428;
+  const double stpfac = 296. / 1013.;
+  const size_t N = (size_t)ncol;
+  const size_t fstride = (size_t)nlay * N;
+  auto A = [&](const double* p, int l) { return __ldg(p + (size_t)col + N * (size_t)(l - 1)); };
+  double pz_prev = A(in.plev, 1);
+  int laytrop = 0;
+  for (int l = 1; l <= nlay; ++l) {
+    const double pavel = A(in.play, l);
+    const D2 tavel(A(in.tlay, l), 1.0, 0.0);
+    const double pz_l = A(in.plev, l + 1);
+    const D2 h2o(A(in.h2o, l), 0.0, 1.0);
+    D2 wk1 = (h2o / (1. - h2o)) * amdw;
+    const double wk2 = A(in.co2, l);
+    const double wk3 = A(in.o3, l) * amdo;
+    const double wk4 = in.n2o ? A(in.n2o, l) : 0.0;
+    const double wk6 = in.ch4 ? A(in.ch4, l) : 0.0;
+    const double wk7 = in.o2 ? A(in.o2, l) : 0.0;
+    const D2 amm = (1. - wk1) * amd + wk1 * amw;
+    const D2 coldry = (pz_prev - pz_l) * 1.e3 * C.avogad / (1.e2 * C.grav * amm * (1. + wk1));
+    wk1 = coldry * wk1;
+    const D2 cwk2 = coldry * wk2, cwk3 = coldry * wk3, cwk4 = coldry * wk4, cwk6 = coldry * wk6,
+             cwk7 = coldry * wk7;
+    const double plog = log(pavel);
+    const int jp = clampi((int)(36. - 5 * (plog + 0.04)), 1, 58);
+    const int jp1 = jp + 1;
+    const double fp = 5. * (C.preflog[jp - 1] - plog);
+    const int jt = clampi((int)(3. + (tavel.v - C.tref[jp - 1]) / 15.), 1, 4);
+    const D2 ft = ((tavel - C.tref[jp - 1]) / 15.) - (double)(jt - 3);
+    const int jt1 = clampi((int)(3. + (tavel.v - C.tref[jp1 - 1]) / 15.), 1, 4);
+    const D2 ft1 = ((tavel - C.tref[jp1 - 1]) / 15.) - (double)(jt1 - 3);
+    const D2 water = wk1 / coldry;
+    const D2 scalefac = (pavel * stpfac) / tavel;
+    D2 forfac, forfrac, selffac(0.0), selffrac(0.0), factor;
+    int indfor, indself = 0;
+    if (plog > 4.56) {
+      laytrop = laytrop + 1;
+      forfac = scalefac / (1. + water);
+      factor = (332.0 - tavel) / 36.0;
+      indfor = min(2, max(1, (int)factor.v));
+      forfrac = factor - (double)indfor;
+      selffac = water * forfac;
+      factor = (tavel - 188.0) / 7.2;
+      indself = min(9, max(1, (int)factor.v - 7));
+      selffrac = factor - (double)(indself + 7);
+    } else {
+      forfac = scalefac / (1. + water);
+      factor = (tavel - 188.0) / 36.0;
+      indfor = 3;
+      forfrac = factor - 1.0;
+    }
+    const D2 colh2o = 1.e-20 * wk1;
+    D2 colco2 = 1.e-20 * cwk2, colch4 = 1.e-20 * cwk6, colo2 = 1.e-20 * cwk7, coln2o = 1.e-20 * cwk4;
+    const D2 colo3 = 1.e-20 * cwk3;
+    const D2 colmol = 1.e-20 * coldry + colh2o;
+    if (colco2.v == 0.) colco2 = 1.e-32 * coldry;
+    if (coln2o.v == 0.) coln2o = 1.e-32 * coldry;
+    if (colch4.v == 0.) colch4 = 1.e-32 * coldry;
+    if (colo2.v == 0.) colo2 = 1.e-32 * coldry;
+    const double compfp = 1. - fp;
+    const size_t o = (size_t)(l - 1) * N + col;
+    auto put = [&](int fld, const D2& x) {
+      const size_t i = (size_t)fld * fstride + o;
+      w.fv[i] = x.v;
+      w.ft[i] = x.t;
+      w.fq[i] = x.q;
+    };
+    put(SF_COLH2O, colh2o);
+    put(SF_COLCO2, colco2);
+    put(SF_COLO3, colo3);
+    put(SF_COLCH4, colch4);
+    put(SF_COLO2, colo2);
+    put(SF_COLMOL, colmol);
+    put(SF_FAC10, compfp * ft);
+    put(SF_FAC00, compfp * (1. - ft));
+    put(SF_FAC11, fp * ft1);
+    put(SF_FAC01, fp * (1. - ft1));
+    put(SF_SELFFAC, selffac);
+    put(SF_SELFFRAC, selffrac);
+    put(SF_FORFAC, forfac);
+    put(SF_FORFRAC, forfrac);
+    w.idx[o] = pack_idx(jp, jt, jt1, indself, indfor, 1);
+    pz_prev = pz_l;
+  }
+  w.laytrop[col] = laytrop;
+  auto jpat = [&](int lay) -> int {
+    if (lay < 1 || lay > nlay) return 0;
+    return unpack_idx(w.idx[(size_t)(lay - 1) * N + col]).jp;
+  };
+  for (int bi = 0; bi < kSwBands; ++bi) {
+    const int b = bi + 16;
+    const int ref = sw_layreffr(b);
+    int ls;
+    if (b == 26) {
+      ls = laytrop;
+    } else if (sw_upper_source(b)) {
+      ls = (laytrop < nlay) ? nlay : 0;
+      for (int lay = laytrop + 1; lay <= nlay; ++lay)
+        if (jpat(lay - 1) < ref && jpat(lay) >= ref) ls = lay;
+    } else {
+      ls = laytrop;
+      for (int lay = 1; lay <= laytrop; ++lay)
+        if (jpat(lay) < ref && jpat(lay + 1) >= ref) ls = min(lay + 1, laytrop);
+    }
+    w.laysolfr[bi * N + col] = ls;
+  }
+}
+
+struct SwDualView {
+  const double *fv, *ft, *fq;
+  size_t fstride, o;
+  __device__ __forceinline__ D2 operator()(int fld) const {
+    const size_t i = (size_t)fld * fstride + o;
+    return D2(__ldg(fv + i), __ldg(ft + i), __ldg(fq + i));
+  }
+};
+
+// ---------------------------------------------------------------------------
+// SW reverse sweep of one g-point (spcvrt_sw clear stream,
+// rrtmg_sw_spcvrt.f90:296-618, reftra_sw and vrtqdr_sw, analytic
+// transcendentals).  Top-down index j (0 = top of atmosphere, klev = surface):
+//   layer j: reflectance R, diffuse Rd, transmittance T, diffuse Td, direct Tx;
+//   downward:  tb_{j+1} = Tx_j tb_j,  z = 1 / (1 - Rd_j rn_j),
+//              tn_{j+1} = tb_j T_j + Td_j ((tn_j - tb_j) + tb_j R_j rn_j) z,
+//              rn_{j+1} = Rd_j + Td_j^2 rn_j z            (tb_0 = tn_0 = 1, rn_0 = 0);
+//   upward:    z = 1 / (1 - pd_{j+1} Rd_j),
+//              pu_j = R_j + Td_j ((T_j - Tx_j) pd_{j+1} + Tx_j pu_{j+1}) z,
+//              pd_j = Rd_j + Td_j^2 pd_{j+1} z           (pu, pd at the surface: albedos);
+//   fluxes:    z = 1 / (1 - rn pd),  fu = (tb pu + (tn - tb) pd) z,
+//              fd = tb + (tn - tb + tb pu rn) z,  net = zinc (fd - fu).
+// The reverse carries the adjoints of (pu, pd) downward from the top and of
+// (tb, tn, rn) upward from the surface, collecting d Phi / d(R, Rd, T, Td, Tx)
+// of every layer, then contracts them with the layer tangents.
+// ---------------------------------------------------------------------------
+template <int B, int MAXL>
+__device__ __forceinline__ void sw_adj_band(const SwIn& in, const AdjSwWork& w, double adjflux, int iaer,
+                                            const double* __restrict__ tab, const double* __restrict__ cot,
+                                            int nseed, int ncol, int nlay, int blk, double* sred) {
+  constexpr int NG = sw_ng(B);
+  constexpr int W = pow2ceil(NG);
+  constexpr int CPB = kBlock / W;
+  constexpr int ibm = B - 15;
+  const int lane_col = threadIdx.x / W, g = threadIdx.x % W;
+  const int col = blk * CPB + lane_col;
+  const bool valid = col < ncol;
+  const int c = valid ? col : ncol - 1;
+  const int gg = g < NG ? g : NG - 1;
+  const size_t N = (size_t)ncol;
+  const size_t fstride = (size_t)nlay * N;
+  const double coszen = __ldg(in.coszen + c);
+  const bool lit = coszen >= 1.e-10;
+  const double prmu0 = lit ? coszen : 1.0;
+  const double bpade = c_sw.bpade;
+  const int lt = w.laytrop[c];
+  const int klev = nlay;
+  const int E = 2 * nlay;
+
+  D2 zinc(0.0);
+  const int ls = w.laysolfr[(size_t)(B - 16) * N + c];
+  if (ls >= 1) {
+    SwDualView L{w.fv, w.ft, w.fq, fstride, (size_t)(ls - 1) * N + c};
+    const D2 sfz = sw_sfluxzen<B>(c_sw, L, ls <= lt, gg, tab);
+    zinc = (adjflux * sfz) * (lit ? coszen : 1.0);
+  }
+  const double albdir = __ldg(((ibm >= 10 && ibm <= 13) ? in.asdir : in.aldir) + c);
+  const double albdif = __ldg(((ibm >= 10 && ibm <= 13) ? in.asdif : in.aldif) + c);
+
+  // layer properties (value, d/dtlay, d/dq) and level states, top-down index
+  double Rv[MAXL], Rt[MAXL], Rq[MAXL], Dv[MAXL], Dt[MAXL], Dq[MAXL], Tv[MAXL], Tt[MAXL], Tq[MAXL];
+  double Sv[MAXL], St[MAXL], Sq[MAXL], Xv[MAXL], Xt[MAXL], Xq[MAXL];
+  double tb[MAXL + 1], tn[MAXL + 1], rn[MAXL + 1], pu[MAXL + 1], pd[MAXL + 1];
+  double gR[MAXL], gD[MAXL], gT[MAXL], gS[MAXL], gX[MAXL];
+  for (int j = 0; j < klev; ++j) {
+    const int ikl = klev - j;
+    const size_t o = (size_t)(ikl - 1) * N + c;
+    const Idx ix = unpack_idx(__ldg(w.idx + o));
+    SwDualView L{w.fv, w.ft, w.fq, fstride, o};
+    D2 taug, taur;
+    sw_gas<B, D2>(c_sw, L, ix, ikl <= lt, gg, tab, taug, taur);
+    double taua = 0., omga = 1., asya = 0.;
+    if (iaer == 10) {
+      const size_t oa = c + N * ((size_t)(ikl - 1) + (size_t)nlay * (ibm - 1));
+      taua = __ldg(in.tauaer + oa);
+      omga = __ldg(in.ssaaer + oa);
+      asya = __ldg(in.asmaer + oa);
+    }
+    D2 ztauc = taur + taug + taua;
+    D2 zomcc = taur * 1.0 + taua * omga;
+    D2 zgcc = (asya * omga * taua) / zomcc;
+    zomcc = zomcc / ztauc;
+    const D2 zf = zgcc * zgcc;
+    const D2 zwf = zomcc * zf;
+    ztauc = (1.0 - zwf) * ztauc;
+    zomcc = (zomcc - zwf) / (1.0 - zwf);
+    zgcc = (zgcc - zf) / (1.0 - zf);
+    D2 rf, rfd, tr, trd;
+    reftra1<D2, double>(ztauc, zomcc, zgcc, D2(prmu0), D2(bpade), (const double*)nullptr, true, rf, rfd, tr, trd);
+    const D2 tx = sw_exp_tbl<D2, double>(ztauc / prmu0, D2(bpade), (const double*)nullptr, true);
+    Rv[j] = rf.v; Rt[j] = rf.t; Rq[j] = rf.q;
+    Dv[j] = rfd.v; Dt[j] = rfd.t; Dq[j] = rfd.q;
+    Tv[j] = tr.v; Tt[j] = tr.t; Tq[j] = tr.q;
+    Sv[j] = trd.v; St[j] = trd.t; Sq[j] = trd.q;
+    Xv[j] = tx.v; Xt[j] = tx.t; Xq[j] = tx.q;
+  }
+  tb[0] = 1.0; tn[0] = 1.0; rn[0] = 0.0;
+  for (int j = 0; j < klev; ++j) {
+    tb[j + 1] = Xv[j] * tb[j];
+    const double z = 1.0 / (1.0 - Dv[j] * rn[j]);
+    tn[j + 1] = tb[j] * Tv[j] + Sv[j] * ((tn[j] - tb[j]) + tb[j] * Rv[j] * rn[j]) * z;
+    rn[j + 1] = Dv[j] + Sv[j] * Sv[j] * rn[j] * z;
+  }
+  pu[klev] = albdir; pd[klev] = albdif;
+  for (int j = klev - 1; j >= 0; --j) {
+    const double z = 1.0 / (1.0 - pd[j + 1] * Dv[j]);
+    pu[j] = Rv[j] + Sv[j] * ((Tv[j] - Xv[j]) * pd[j + 1] + Xv[j] * pu[j + 1]) * z;
+    pd[j] = Dv[j] + Sv[j] * Sv[j] * pd[j + 1] * z;
+  }
+
+  const int wib = threadIdx.x >> 5;
+  const int wcol0 = blk * CPB + (wib * 32) / W;
+  const double heatfac = c_sw.heatfac;
+  const double gate = lit ? 1.0 : 0.0;  // dark columns have zero SW outputs
+  for (int s = 0; s < nseed; ++s) {
+    // cotangent of net at bottom-up level m
+    auto cdiv = [&](int kk) -> double {  // layers 1..nlay-1 (the top layer's rate is 0)
+      if (kk < 1 || kk > nlay - 1) return 0.0;
+      const double hs = heatfac / (__ldg(in.plev + (size_t)(kk - 1) * N + c) - __ldg(in.plev + (size_t)kk * N + c));
+      if (cot) return __ldg(cot + (size_t)(nlay + 2 + kk - 1) * N + c) * hs;
+      return s == kk - 1 ? hs : 0.0;
+    };
+    const double csfc = cot ? __ldg(cot + (size_t)(2 * nlay + 2) * N + c) : (s == nlay ? 1.0 : 0.0);
+    auto anet = [&](int m) { return gate * (cdiv(m) - cdiv(m + 1) + (m == 0 ? csfc : 0.0)); };
+    // local cotangents of the level states at top-down level j from the fluxes there
+    auto local = [&](int j, double& ltb, double& ltn, double& lrn, double& lpu, double& lpd) {
+      const double a = zinc.v * anet(klev - j);
+      const double z = 1.0 / (1.0 - rn[j] * pd[j]);
+      const double Af = tb[j] * pu[j] + (tn[j] - tb[j]) * pd[j];
+      const double Bf = tn[j] - tb[j] + tb[j] * pu[j] * rn[j];
+      // fu = Af z (cotangent -a), fd = tb + Bf z (cotangent a)
+      ltb = -a * (pu[j] - pd[j]) * z + a * (1.0 + (-1.0 + pu[j] * rn[j]) * z);
+      ltn = -a * pd[j] * z + a * z;
+      lpu = -a * tb[j] * z + a * tb[j] * rn[j] * z;
+      lpd = -a * ((tn[j] - tb[j]) * z + Af * z * z * rn[j]) + a * Bf * z * z * rn[j];
+      lrn = -a * Af * z * z * pd[j] + a * (tb[j] * pu[j] * z + Bf * z * z * pd[j]);
+    };
+    double lzinc = 0.0;
+    for (int j = 0; j <= klev; ++j) {
+      const double z = 1.0 / (1.0 - rn[j] * pd[j]);
+      const double fu = (tb[j] * pu[j] + (tn[j] - tb[j]) * pd[j]) * z;
+      const double fd = tb[j] + (tn[j] - tb[j] + tb[j] * pu[j] * rn[j]) * z;
+      lzinc += anet(klev - j) * (fd - fu);
+    }
+    for (int j = 0; j < klev; ++j) gR[j] = gD[j] = gT[j] = gS[j] = gX[j] = 0.0;
+    // reverse of the upward sweep, carried from the top down
+    double Lu = 0.0, Ld = 0.0;
+    for (int j = 0; j < klev; ++j) {
+      double ltb, ltn, lrn, lpu, lpd;
+      local(j, ltb, ltn, lrn, lpu, lpd);
+      Lu += lpu;
+      Ld += lpd;
+      const double z = 1.0 / (1.0 - pd[j + 1] * Dv[j]);
+      const double Xx = (Tv[j] - Xv[j]) * pd[j + 1] + Xv[j] * pu[j + 1];
+      const double Td = Sv[j];
+      gR[j] += Lu;
+      gS[j] += Lu * Xx * z + Ld * 2.0 * Td * pd[j + 1] * z;
+      gT[j] += Lu * Td * pd[j + 1] * z;
+      gX[j] += Lu * Td * (pu[j + 1] - pd[j + 1]) * z;
+      gD[j] += Ld * (1.0 + Td * Td * pd[j + 1] * z * z * pd[j + 1]) + Lu * Td * Xx * z * z * pd[j + 1];
+      const double nLu = Lu * Td * Xv[j] * z;
+      const double nLd = Lu * (Td * (Tv[j] - Xv[j]) * z + Td * Xx * z * z * Dv[j]) +
+                         Ld * (Td * Td * z + Td * Td * pd[j + 1] * z * z * Dv[j]);
+      Lu = nLu;
+      Ld = nLd;
+    }
+    // reverse of the downward sweep, carried from the surface up
+    double Lb = 0.0, Ln = 0.0, Lr = 0.0;
+    for (int j = klev; j >= 1; --j) {
+      double ltb, ltn, lrn, lpu, lpd;
+      local(j, ltb, ltn, lrn, lpu, lpd);
+      Lb += ltb;
+      Ln += ltn;
+      Lr += lrn;
+      const int q = j - 1;
+      const double z = 1.0 / (1.0 - Dv[q] * rn[q]);
+      const double Y = (tn[q] - tb[q]) + tb[q] * Rv[q] * rn[q];
+      const double Td = Sv[q];
+      gX[q] += Lb * tb[q];
+      gT[q] += Ln * tb[q];
+      gS[q] += Ln * Y * z + Lr * 2.0 * Td * rn[q] * z;
+      gR[q] += Ln * Td * tb[q] * rn[q] * z;
+      gD[q] += Ln * Td * Y * z * z * rn[q] + Lr * (1.0 + Td * Td * rn[q] * z * z * rn[q]);
+      const double nLb = Lb * Xv[q] + Ln * (Tv[q] + Td * (-1.0 + Rv[q] * rn[q]) * z);
+      const double nLn = Ln * Td * z;
+      const double nLr = Ln * (Td * tb[q] * Rv[q] * z + Td * Y * z * z * Dv[q]) +
+                         Lr * (Td * Td * z + Td * Td * rn[q] * z * z * Dv[q]);
+      Lb = nLb;
+      Ln = nLn;
+      Lr = nLr;
+    }
+    GRed<W, NG> red{sred + wib * W * kRow, (int)(threadIdx.x & 31), 0, 0};
+    auto store = [&](int e, int cs, double v) {
+      const int cc = wcol0 + cs;
+      if (cc < ncol) w.part[(((size_t)(B - 16) * nseed + s) * E + e) * N + cc] = v;
+    };
+    for (int l = 1; l <= nlay; ++l) {
+      const int j = klev - l;
+      double gt = gR[j] * Rt[j] + gD[j] * Dt[j] + gT[j] * Tt[j] + gS[j] * St[j] + gX[j] * Xt[j];
+      double gq = gR[j] * Rq[j] + gD[j] * Dq[j] + gT[j] * Tq[j] + gS[j] * Sq[j] + gX[j] * Xq[j];
+      if (l == ls) {
+        gt += lzinc * zinc.t;
+        gq += lzinc * zinc.q;
+      }
+      red.put(gt);
+      red.next(store);
+      red.put(gq);
+      red.next(store);
+    }
+    if (red.n) red.flush(store);
+  }
+}
+
+template <int MAXL>
+__global__ void __launch_bounds__(kBlock) sw_adj_kernel(SwIn in, AdjSwWork w, double adjflux, int iaer,
+                                                        const double* __restrict__ tab,
+                                                        const double* __restrict__ cot, int nseed, int ncol,
+                                                        int nlay) {
+  __shared__ double sred[kRedDoubles];
+  int blk = blockIdx.x, band = 0;
+  for (; band < kSwBands; ++band) {
+    const int nb = lw_blocks_for_band(c_sw.band[band].ngpad, ncol);
+    if (blk < nb) break;
+    blk -= nb;
+  }
+#define RRTMG_SW_ADJ_CASE(b) \
+  case b - 16: sw_adj_band<b, MAXL>(in, w, adjflux, iaer, tab, cot, nseed, ncol, nlay, blk, sred); break;
+  switch (band) {
+    RRTMG_SW_ADJ_CASE(16) RRTMG_SW_ADJ_CASE(17) RRTMG_SW_ADJ_CASE(18) RRTMG_SW_ADJ_CASE(19) RRTMG_SW_ADJ_CASE(20)
+    RRTMG_SW_ADJ_CASE(21) RRTMG_SW_ADJ_CASE(22) RRTMG_SW_ADJ_CASE(23) RRTMG_SW_ADJ_CASE(24) RRTMG_SW_ADJ_CASE(25)
+    RRTMG_SW_ADJ_CASE(26) RRTMG_SW_ADJ_CASE(27) RRTMG_SW_ADJ_CASE(28) RRTMG_SW_ADJ_CASE(29)
+    default: break;
+  }
+#undef RRTMG_SW_ADJ_CASE
+}
+
+// ---------------------------------------------------------------------------
+// Band sums.  LW partials are weighted by wtdiff * delwave * fluxfac
+// (rrtmg_lw_rtrnmr.f90:720-746); the secdiff entry is chained to every
+// layer's q through d secdiff / d q.  SW partials are already in W/m2.
+// Jacobian: one thread per (column, output row); VJP: one per column.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) adj_finalize_kernel(AdjLwWork lw, AdjSwWork sw, const double* __restrict__ coszen,
+                                                           int nseed_lw, int nseed_sw, int ncol, int nlay,
+                                                           double* __restrict__ out, int vjp) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncol) return;
+  const int r = blockIdx.y;  // output row (Jacobian) or 0 (VJP)
+  const size_t N = (size_t)ncol;
+  const int L = nlay, ny = 2 * L + 3, nx = 3 * L + 2;
+  const int Elw = 3 * L + 3, Esw = 2 * L;
+  const double wtdiff = 0.5;
+  auto lwp = [&](int b, int s, int e) { return __ldg(lw.part + (((size_t)b * nseed_lw + s) * Elw + e) * N + col); };
+  auto swp = [&](int b, int s, int e) { return __ldg(sw.part + (((size_t)b * nseed_sw + s) * Esw + e) * N + col); };
+  auto wb = [&](int b) { return wtdiff * c_lw.band[b].delwave * c_lw.fluxfac; };
+  const bool do_lw = vjp || r < L + 2;
+  const bool do_sw = vjp || r >= L + 2;
+  const int slw = vjp ? 0 : r, ssw = vjp ? 0 : r - (L + 2);
+  for (int x = 0; x < nx; ++x) {
+    double v = 0.0;
+    if (do_lw) {
+      int e;
+      if (x < L) e = 3 * x;                          // tlay
+      else if (x < 2 * L) e = 3 * (x - L) + 1;       // q
+      else if (x < 3 * L) e = 3 * (x - 2 * L) + 2;   // tlev 0..nlay-1
+      else if (x == 3 * L) e = 3 * L;                // tlev nlay
+      else e = 3 * L + 1;                            // tsfc
+      for (int b = 0; b < kLwBands; ++b) {
+        double t = lwp(b, slw, e);
+        if (x >= L && x < 2 * L) t += lwp(b, slw, 3 * L + 2) * __ldg(lw.dsec + ((size_t)b * L + (x - L)) * N + col);
+        v += wb(b) * t;
+      }
+    }
+    if (do_sw && x < 2 * L) {
+      const int e = x < L ? 2 * x : 2 * (x - L) + 1;
+      for (int b = 0; b < kSwBands; ++b) v += swp(b, ssw, e);
+    }
+    if (vjp)
+      out[(size_t)x * N + col] = v;
+    else
+      out[((size_t)x * ny + r) * N + col] = v;
+  }
+  (void)coszen;
+}
+
+// ---------------------------------------------------------------------------
+// Host side.
+// ---------------------------------------------------------------------------
+cudaError_t upload_constants_adjoint(const LwConst& lw, const SwConst& sw) {
+  cudaError_t e = cudaMemcpyToSymbol(c_lw, &lw, sizeof(LwConst));
+  if (e != cudaSuccess) return e;
+  return cudaMemcpyToSymbol(c_sw, &sw, sizeof(SwConst));
+}
+
+void launch_adj_lw(const LwIn& in, const AdjLwWork& w, const double* totplnk, const double* tab,
+                   const double* cot, int nseed, int ncol, int nlay, int nb, cudaStream_t s) {
+  adj_lw_prep_kernel<<<(ncol + 127) / 128, 128, 0, s>>>(in, w, totplnk, ncol, nlay);
+  if (maxl_for(nlay) == 64)
+    lw_adj_kernel<64><<<nb, kBlock, 0, s>>>(in, w, tab, cot, nseed, ncol, nlay);
+  else
+    lw_adj_kernel<208><<<nb, kBlock, 0, s>>>(in, w, tab, cot, nseed, ncol, nlay);
+}
+
+void launch_adj_sw(const SwIn& in, const AdjSwWork& w, double adjflux, int iaer, const double* tab,
+                   const double* cot, int nseed, int ncol, int nlay, int nb, cudaStream_t s) {
+  adj_sw_prep_kernel<<<(ncol + 127) / 128, 128, 0, s>>>(in, w, ncol, nlay);
+  if (maxl_for(nlay) == 64)
+    sw_adj_kernel<64><<<nb, kBlock, 0, s>>>(in, w, adjflux, iaer, tab, cot, nseed, ncol, nlay);
+  else
+    sw_adj_kernel<208><<<nb, kBlock, 0, s>>>(in, w, adjflux, iaer, tab, cot, nseed, ncol, nlay);
+}
+
+void launch_adj_finalize(const AdjLwWork& lw, const AdjSwWork& sw, const double* plev, const double* coszen,
+                         int nseed_lw, int nseed_sw, int ncol, int nlay, double* out, bool vjp, cudaStream_t s) {
+  (void)plev;
+  dim3 grid((ncol + 127) / 128, vjp ? 1 : adj_ny(nlay));
+  adj_finalize_kernel<<<grid, 128, 0, s>>>(lw, sw, coszen, nseed_lw, nseed_sw, ncol, nlay, out, vjp ? 1 : 0);
+}
+
+}  // namespace rrtmg

@@ -301,7 +301,7 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
                                         const double* __restrict__ tauaer, const R* __restrict__ tab,
                                         const R* __restrict__ exptbl, const R* __restrict__ tfntbl,
                                         double* __restrict__ bu, double* __restrict__ bd, double* __restrict__ bdu,
-                                        int ncol, int nlay, int idrv, int blk, float* sbuf) {
+                                        int ncol, int nlay, int idrv, bool analytic, int blk, float* sbuf) {
   const bool IDRV = idrv == 1;
   constexpr bool SPLIT = sizeof(R) == 4;
   constexpr int NG = lw_ng(B);
@@ -365,6 +365,13 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
       odepth = rec_6 * odepth;
       bbd = plfrac * (blay + dplankdn * odepth);
       bbu = plfrac * (blay + dplankup * odepth);
+    } else if (analytic) {
+      // The functions the tables sample (rrtmg_lw_init.f90:115-122).
+      const R transc = exp(-odepth);
+      atr = (R)1. - transc;
+      const R tausfac = (R)1. - (R)2. * (((R)1. / odepth) - (transc / ((R)1. - transc)));
+      bbd = plfrac * (blay + tausfac * dplankdn);
+      bbu = plfrac * (blay + tausfac * dplankup);
     } else {
       const R tblind = odepth / (bpade + odepth);
       int itr = (int)((R)10000.0 * tblind + (R)0.5);
@@ -455,7 +462,8 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_LW_MINB :
                                                            const double* __restrict__ tauaer,
                                                            const R* __restrict__ tab, const R* __restrict__ exptbl,
                                                            const R* __restrict__ tfntbl, double* bu, double* bd,
-                                                           double* bdu, int ncol, int nlay, int idrv) {
+                                                           double* bdu, int ncol, int nlay, int idrv,
+                                                           int analytic) {
   __shared__ float sbuf[sizeof(R) == 4 ? kGSumFloats : 1];
   int blk = blockIdx.x, band = 0;
   for (; band < kLwBands; ++band) {
@@ -464,7 +472,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_LW_MINB :
     blk -= nb;
   }
 #define RRTMG_LW_CASE(b) \
-  case b - 1: lw_band<b, R, MAXL>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv, blk, sbuf); break;
+  case b - 1: lw_band<b, R, MAXL>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv, analytic != 0, blk, sbuf); break;
   switch (band) {
     RRTMG_LW_CASE(1) RRTMG_LW_CASE(2) RRTMG_LW_CASE(3) RRTMG_LW_CASE(4) RRTMG_LW_CASE(5) RRTMG_LW_CASE(6)
     RRTMG_LW_CASE(7) RRTMG_LW_CASE(8) RRTMG_LW_CASE(9) RRTMG_LW_CASE(10) RRTMG_LW_CASE(11) RRTMG_LW_CASE(12)
@@ -680,19 +688,20 @@ __global__ void __launch_bounds__(128) sw_prep_kernel(SwIn in, SwWorkT<F> w, int
 // "total" stream is bit-identical to its "clear" stream (cloud weights 0/1),
 // so one stream is computed and written to both outputs.
 // ---------------------------------------------------------------------------
-template <class R>
-__device__ __forceinline__ R sw_exp_tbl(R ze1, R bpade, const R* __restrict__ exptbl) {
+template <class R, class TT>
+__device__ __forceinline__ R sw_exp_tbl(R ze1, R bpade, const TT* __restrict__ exptbl, bool analytic) {
   if (ze1 <= (R)0.06) return (R)1. - ze1 + (R)0.5 * ze1 * ze1;
+  if (analytic) return exp(-ze1);
   const R tblind = ze1 / (bpade + ze1);
   int itind = (int)((R)10000.0 * tblind + (R)0.5);
   itind = itind < 0 ? 0 : (itind > kNTbl ? kNTbl : itind);  // guards NaN / negative optical depths
-  return __ldg(exptbl + itind);
+  return (R)__ldg(exptbl + itind);
 }
 
 // delta-Eddington layer reflectance/transmittance, kmodts = 2 (rrtmg_sw_reftra.f90:143-300)
-template <class R>
-__device__ __forceinline__ void reftra1(R zto1, R zw, R zg, R prmuz, R bpade, const R* __restrict__ exptbl, R& pref,
-                                        R& prefd, R& ptra, R& ptrad) {
+template <class R, class TT>
+__device__ __forceinline__ void reftra1(R zto1, R zw, R zg, R prmuz, R bpade, const TT* __restrict__ exptbl,
+                                        bool analytic, R& pref, R& prefd, R& ptra, R& ptrad) {
   const R eps = (R)1.e-08, zwcrit = (R)0.9999995;
   const R zg3 = (R)3. * zg;
   const R zgamma1 = ((R)8. - zw * ((R)5. + zg3)) * (R)0.25;
@@ -706,7 +715,7 @@ __device__ __forceinline__ void reftra1(R zto1, R zw, R zg, R prmuz, R bpade, co
     const R za1 = za - zgamma3;
     const R zgt = zgamma1 * zto1;
     const R ze1 = fmin(zto1 / prmuz, (R)500.);
-    const R ze2 = sw_exp_tbl<R>(ze1, bpade, exptbl);
+    const R ze2 = sw_exp_tbl<R, TT>(ze1, bpade, exptbl, analytic);
     pref = (zgt - za1 * ((R)1. - ze2)) / ((R)1. + zgt);
     ptra = (R)1. - pref;
     prefd = zgt / ((R)1. + zgt);
@@ -738,9 +747,9 @@ __device__ __forceinline__ void reftra1(R zto1, R zw, R zg, R prmuz, R bpade, co
     const R zbeta = (zgamma1 - zrk) / zrkg;
     const R ze1 = fmin(zrk * zto1, (R)500.);
     const R ze2 = fmin(zto1 / prmuz, (R)500.);
-    const R zem1 = sw_exp_tbl<R>(ze1, bpade, exptbl);
+    const R zem1 = sw_exp_tbl<R, TT>(ze1, bpade, exptbl, analytic);
     const R zep1 = (R)1. / zem1;
-    const R zem2 = sw_exp_tbl<R>(ze2, bpade, exptbl);
+    const R zem2 = sw_exp_tbl<R, TT>(ze2, bpade, exptbl, analytic);
     const R zep2 = (R)1. / zem2;
     const R zdenr = zr4 * zep1 + zr5 * zem1;
     const R zt4 = zr4, zt5 = zr5;
@@ -761,11 +770,16 @@ __device__ __forceinline__ void reftra1(R zto1, R zw, R zg, R prmuz, R bpade, co
 
 // exp(-x) from the SW table / series together with exp(-x) - 1, the latter
 // formed without cancellation (series: -x + x^2/2; table: tbl - 1).
-__device__ __forceinline__ void sw_exp_pair(float ze1, float bpade, const float* __restrict__ exptbl, float& e,
-                                            float& em1) {
+__device__ __forceinline__ void sw_exp_pair(float ze1, float bpade, const float* __restrict__ exptbl, bool analytic,
+                                            float& e, float& em1) {
   if (ze1 <= 0.06f) {
     em1 = -ze1 + 0.5f * ze1 * ze1;
     e = 1.f - ze1 + 0.5f * ze1 * ze1;
+    return;
+  }
+  if (analytic) {
+    e = expf(-ze1);
+    em1 = expm1f(-ze1);
     return;
   }
   const float tblind = ze1 / (bpade + ze1);
@@ -786,8 +800,8 @@ __device__ __forceinline__ void sw_exp_pair(float ze1, float bpade, const float*
 //   * zr4 e^{kt} + zr5 e^{-kt} = zrpp (k (e^{kt} + e^{-kt}) + g1 (e^{kt} - e^{-kt})).
 // Exponentials are the same table / series values as the reference uses.
 __device__ __forceinline__ void reftra_split(float zto1, float zw, float zg, float prmuz, float bpade,
-                                             const float* __restrict__ exptbl, float& pref, float& prefd,
-                                             float& ptra, float& ptrad) {
+                                             const float* __restrict__ exptbl, bool analytic, float& pref,
+                                             float& prefd, float& ptra, float& ptrad) {
   const float eps = 1.e-08f, zwcrit = 0.9999995f;
   const float zg3 = 3.f * zg;
   const float zgamma1 = (8.f - zw * (5.f + zg3)) * 0.25f;
@@ -800,7 +814,7 @@ __device__ __forceinline__ void reftra_split(float zto1, float zw, float zg, flo
     const float za1 = zgamma1 * prmuz - zgamma3;
     const float zgt = zgamma1 * zto1;
     float ze2, m2;
-    sw_exp_pair(fminf(zto1 / prmuz, 500.f), bpade, exptbl, ze2, m2);
+    sw_exp_pair(fminf(zto1 / prmuz, 500.f), bpade, exptbl, analytic, ze2, m2);
     pref = (zgt + za1 * m2) / (1.f + zgt);
     ptra = 1.f - pref;
     prefd = zgt / (1.f + zgt);
@@ -824,8 +838,8 @@ __device__ __forceinline__ void reftra_split(float zto1, float zw, float zg, flo
     const float zt2 = zrm1 * (za1 - zrk * zgamma4);
     const float zt3 = zrk2 * (zgamma4 + za1 * prmuz);
     float zem1, m1, zem2, m2;
-    sw_exp_pair(fminf(zrk * zto1, 500.f), bpade, exptbl, zem1, m1);
-    sw_exp_pair(fminf(zto1 / prmuz, 500.f), bpade, exptbl, zem2, m2);
+    sw_exp_pair(fminf(zrk * zto1, 500.f), bpade, exptbl, analytic, zem1, m1);
+    sw_exp_pair(fminf(zto1 / prmuz, 500.f), bpade, exptbl, analytic, zem2, m2);
     const float zep1 = 1.f / zem1, zep2 = 1.f / zem2;
     const float p1 = -m1 * zep1, p2 = -m2 * zep2;  // e^{kt} - 1, e^{t/mu} - 1
     const float zden = zrpp * (zrk * (zep1 + zem1) + zgamma1 * (p1 - m1));
@@ -847,7 +861,7 @@ template <int B, class R, int MAXL>
 __device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, double adjflux, int iaer,
                                         const R* __restrict__ tab, const double* __restrict__ tab64,
                                         const R* __restrict__ exptbl, double* __restrict__ su,
-                                        double* __restrict__ sd, int ncol, int nlay, int blk, float* sbuf,
+                                        double* __restrict__ sd, int ncol, int nlay, bool analytic, int blk, float* sbuf,
                                         double* swt) {
   constexpr bool SPLIT = sizeof(R) == 4;
   constexpr int NG = sw_ng(B);
@@ -911,14 +925,14 @@ __device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, dou
     zgcc = (zgcc - zf) / ((R)1.0 - zf);
     R rf, rfd, tr, trd;
     if constexpr (sizeof(R) == 4)
-      reftra_split(ztauc, zomcc, zgcc, prmu0, bpade, exptbl, rf, rfd, tr, trd);
+      reftra_split(ztauc, zomcc, zgcc, prmu0, bpade, exptbl, analytic, rf, rfd, tr, trd);
     else
-      reftra1<R>(ztauc, zomcc, zgcc, prmu0, bpade, exptbl, rf, rfd, tr, trd);
+      reftra1<R, R>(ztauc, zomcc, zgcc, prmu0, bpade, exptbl, analytic, rf, rfd, tr, trd);
     pref[jk - 1] = rf;
     prefd[jk - 1] = rfd;
     ptra[jk - 1] = tr;
     ptrad[jk - 1] = trd;
-    const R zdbtmc = sw_exp_tbl<R>(ztauc / prmu0, bpade, exptbl);
+    const R zdbtmc = sw_exp_tbl<R, R>(ztauc / prmu0, bpade, exptbl, analytic);
     pdbt[jk - 1] = zdbtmc;
     ptdbt[jk] = zdbtmc * ptdbt[jk - 1];
     // Downward adding sweep of vrtqdr_sw (:127-139), fused with the layer loop.
@@ -993,7 +1007,7 @@ template <class R, int MAXL>
 __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_SW_MINB : 1) sw_gpoint_kernel(SwPrepT<R> p, SwIn in, double adjflux, int iaer,
                                                            const R* __restrict__ tab, const double* __restrict__ tab64,
                                                            const R* __restrict__ exptbl, double* su, double* sd,
-                                                           int ncol, int nlay) {
+                                                           int ncol, int nlay, int analytic) {
   __shared__ float sbuf[sizeof(R) == 4 ? kGSumFloats : 1];
   __shared__ double swt[sizeof(R) == 4 ? kBlock : 1];
   int blk = blockIdx.x, band = 0;
@@ -1003,7 +1017,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_SW_MINB :
     blk -= nb;
   }
 #define RRTMG_SW_CASE(b) \
-  case b - 16: sw_band<b, R, MAXL>(p, in, adjflux, iaer, tab, tab64, exptbl, su, sd, ncol, nlay, blk, sbuf, swt); break;
+  case b - 16: sw_band<b, R, MAXL>(p, in, adjflux, iaer, tab, tab64, exptbl, su, sd, ncol, nlay, analytic != 0, blk, sbuf, swt); break;
   switch (band) {
     RRTMG_SW_CASE(16) RRTMG_SW_CASE(17) RRTMG_SW_CASE(18) RRTMG_SW_CASE(19) RRTMG_SW_CASE(20) RRTMG_SW_CASE(21)
     RRTMG_SW_CASE(22) RRTMG_SW_CASE(23) RRTMG_SW_CASE(24) RRTMG_SW_CASE(25) RRTMG_SW_CASE(26) RRTMG_SW_CASE(27)

@@ -37,11 +37,11 @@ void launch_lw_prep_split(const LwIn& in, const LwWorkT<float>& w, const double*
 
 void launch_lw_gpoint_fp64(const LwPrep& p, const double* emis, const double* tauaer, const double* tab,
                            const double* exptbl, const double* tfntbl, double* bu, double* bd, double* bdu, int ncol,
-                           int nlay, int idrv, int nb, cudaStream_t s) {
+                           int nlay, int idrv, int nb, int analytic, cudaStream_t s) {
   if (maxl_for(nlay) == 64)
-    lw_gpoint_kernel<double, 64><<<nb, kBlock, 0, s>>>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv);
+    lw_gpoint_kernel<double, 64><<<nb, kBlock, 0, s>>>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv, analytic);
   else
-    lw_gpoint_kernel<double, 208><<<nb, kBlock, 0, s>>>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv);
+    lw_gpoint_kernel<double, 208><<<nb, kBlock, 0, s>>>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv, analytic);
 }
 
 void launch_lw_finalize(const double* bu, const double* bd, const double* bdu, const double* plev, int ncol, int nlay,
@@ -61,11 +61,11 @@ void launch_sw_prep_split(const SwIn& in, const SwWorkT<float>& w, int ncol, int
 }
 
 void launch_sw_gpoint_fp64(const SwPrep& p, const SwIn& in, double adjflux, int iaer, const double* tab,
-                           const double* exptbl, double* su, double* sd, int ncol, int nlay, int nb, cudaStream_t s) {
+                           const double* exptbl, double* su, double* sd, int ncol, int nlay, int nb, int analytic, cudaStream_t s) {
   if (maxl_for(nlay) == 64)
-    sw_gpoint_kernel<double, 64><<<nb, kBlock, 0, s>>>(p, in, adjflux, iaer, tab, tab, exptbl, su, sd, ncol, nlay);
+    sw_gpoint_kernel<double, 64><<<nb, kBlock, 0, s>>>(p, in, adjflux, iaer, tab, tab, exptbl, su, sd, ncol, nlay, analytic);
   else
-    sw_gpoint_kernel<double, 208><<<nb, kBlock, 0, s>>>(p, in, adjflux, iaer, tab, tab, exptbl, su, sd, ncol, nlay);
+    sw_gpoint_kernel<double, 208><<<nb, kBlock, 0, s>>>(p, in, adjflux, iaer, tab, tab, exptbl, su, sd, ncol, nlay, analytic);
 }
 
 void launch_sw_finalize(const double* su, const double* sd, const double* plev, const double* coszen, int ncol,

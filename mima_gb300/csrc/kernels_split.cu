@@ -29,20 +29,20 @@ cudaError_t upload_constants_split(const LwConst& lw, const SwConst& sw) {
 
 void launch_lw_gpoint_split(const LwPrepT<float>& p, const double* emis, const double* tauaer, const float* tab,
                             const float* exptbl, const float* tfntbl, double* bu, double* bd, double* bdu, int ncol,
-                            int nlay, int idrv, int nb, cudaStream_t s) {
+                            int nlay, int idrv, int nb, int analytic, cudaStream_t s) {
   if (maxl_for(nlay) == 64)
-    lw_gpoint_kernel<float, 64><<<nb, kBlock, 0, s>>>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv);
+    lw_gpoint_kernel<float, 64><<<nb, kBlock, 0, s>>>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv, analytic);
   else
-    lw_gpoint_kernel<float, 208><<<nb, kBlock, 0, s>>>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv);
+    lw_gpoint_kernel<float, 208><<<nb, kBlock, 0, s>>>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv, analytic);
 }
 
 void launch_sw_gpoint_split(const SwPrepT<float>& p, const SwIn& in, double adjflux, int iaer, const float* tab,
                             const double* tab64, const float* exptbl, double* su, double* sd, int ncol, int nlay,
-                            int nb, cudaStream_t s) {
+                            int nb, int analytic, cudaStream_t s) {
   if (maxl_for(nlay) == 64)
-    sw_gpoint_kernel<float, 64><<<nb, kBlock, 0, s>>>(p, in, adjflux, iaer, tab, tab64, exptbl, su, sd, ncol, nlay);
+    sw_gpoint_kernel<float, 64><<<nb, kBlock, 0, s>>>(p, in, adjflux, iaer, tab, tab64, exptbl, su, sd, ncol, nlay, analytic);
   else
-    sw_gpoint_kernel<float, 208><<<nb, kBlock, 0, s>>>(p, in, adjflux, iaer, tab, tab64, exptbl, su, sd, ncol, nlay);
+    sw_gpoint_kernel<float, 208><<<nb, kBlock, 0, s>>>(p, in, adjflux, iaer, tab, tab64, exptbl, su, sd, ncol, nlay, analytic);
 }
 
 }  // namespace rrtmg

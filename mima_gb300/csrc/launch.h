@@ -20,7 +20,7 @@ void launch_lw_prep(const LwIn& in, const LwWork& w, const double* totplnk, cons
                     int nlay, int idrv, unsigned* flags, cudaStream_t s);
 void launch_lw_gpoint_fp64(const LwPrep& p, const double* emis, const double* tauaer, const double* tab,
                            const double* exptbl, const double* tfntbl, double* bu, double* bd, double* bdu, int ncol,
-                           int nlay, int idrv, int nb, cudaStream_t s);
+                           int nlay, int idrv, int nb, int analytic, cudaStream_t s);
 void launch_lw_finalize(const double* bu, const double* bd, const double* bdu, const double* plev, int ncol, int nlay,
                         int idrv, double* uflx, double* dflx, double* hr, double* uflxc, double* dflxc, double* hrc,
                         double* duflx_dt, double* duflxc_dt, cudaStream_t s);
@@ -31,7 +31,7 @@ void launch_lw_prep_split(const LwIn& in, const LwWorkT<float>& w, const double*
 void launch_sw_prep_split(const SwIn& in, const SwWorkT<float>& w, int ncol, int nlay, unsigned* flags,
                           cudaStream_t s);
 void launch_sw_gpoint_fp64(const SwPrep& p, const SwIn& in, double adjflux, int iaer, const double* tab,
-                           const double* exptbl, double* su, double* sd, int ncol, int nlay, int nb, cudaStream_t s);
+                           const double* exptbl, double* su, double* sd, int ncol, int nlay, int nb, int analytic, cudaStream_t s);
 void launch_sw_finalize(const double* su, const double* sd, const double* plev, const double* coszen, int ncol,
                         int nlay, double* swuflx, double* swdflx, double* swhr, double* swuflxc, double* swdflxc,
                         double* swhrc, cudaStream_t s);
@@ -39,10 +39,10 @@ void launch_sw_finalize(const double* su, const double* sd, const double* plev, 
 // FP32-split translation unit.
 void launch_lw_gpoint_split(const LwPrepT<float>& p, const double* emis, const double* tauaer, const float* tab,
                             const float* exptbl, const float* tfntbl, double* bu, double* bd, double* bdu, int ncol,
-                            int nlay, int idrv, int nb, cudaStream_t s);
+                            int nlay, int idrv, int nb, int analytic, cudaStream_t s);
 void launch_sw_gpoint_split(const SwPrepT<float>& p, const SwIn& in, double adjflux, int iaer, const float* tab,
                             const double* tab64, const float* exptbl, double* su, double* sd, int ncol, int nlay,
-                            int nb, cudaStream_t s);
+                            int nb, int analytic, cudaStream_t s);
 
 // Number of blocks of the g-point grids (sum over bands of columns / (128 / ngpad)).
 int lw_gpoint_blocks(const LwConst& c, int ncol);

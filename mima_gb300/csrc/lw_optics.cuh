@@ -15,6 +15,7 @@
 #include <type_traits>
 
 #include "common.cuh"
+#include "dual.cuh"
 
 namespace rrtmg {
 
@@ -90,8 +91,8 @@ __device__ __forceinline__ W3<R> w3(R specparm, R fs, R facA, R facB) {
 }
 
 // tab points at the band's key-species table (absa); rows are ind-1, g fastest.
-template <class R, int NG>
-__device__ __forceinline__ R major9(const R* __restrict__ ka, R specparm, R speccomb, int ind, int g,
+template <class R, int NG, class TT>
+__device__ __forceinline__ R major9(const TT* __restrict__ ka, R specparm, R speccomb, int ind, int g,
                                     const W3<R>& w) {
   auto K = [&](int i) { return __ldg(ka + (size_t)(i - 1) * NG + g); };
   if (specparm < (R)0.125)
@@ -103,15 +104,15 @@ __device__ __forceinline__ R major9(const R* __restrict__ ka, R specparm, R spec
   return speccomb * (w.a0 * K(ind) + w.a1 * K(ind + 1) + w.b0 * K(ind + 9) + w.b1 * K(ind + 10));
 }
 
-template <class R, int NG>
-__device__ __forceinline__ R interp4(const R* __restrict__ k, R f00, R f10, R f01, R f11, int i0, int i1, int g) {
+template <class R, int NG, class TT>
+__device__ __forceinline__ R interp4(const TT* __restrict__ k, R f00, R f10, R f01, R f11, int i0, int i1, int g) {
   auto K = [&](int i) { return __ldg(k + (size_t)(i - 1) * NG + g); };
   return f00 * K(i0) + f10 * K(i0 + 1) + f01 * K(i1) + f11 * K(i1 + 1);
 }
 
 // Upper-atmosphere 5-level eta form (two pressure levels summed).
-template <class R, int NG>
-__device__ __forceinline__ R major5(const R* __restrict__ kb, R sc, R fs, int i0, R sc1, R fs1, int i1, R f00,
+template <class R, int NG, class TT>
+__device__ __forceinline__ R major5(const TT* __restrict__ kb, R sc, R fs, int i0, R sc1, R fs1, int i1, R f00,
                                     R f10, R f01, R f11, int g) {
   auto K = [&](int i) { return __ldg(kb + (size_t)(i - 1) * NG + g); };
   R fac000 = ((R)1. - fs) * f00, fac010 = ((R)1. - fs) * f10, fac100 = fs * f00, fac110 = fs * f10;
@@ -121,18 +122,29 @@ __device__ __forceinline__ R major5(const R* __restrict__ kb, R sc, R fs, int i0
 }
 
 // k(row, g) + frac * (k(row+1, g) - k(row, g))
-template <class R, int NG>
-__device__ __forceinline__ R lin(const R* __restrict__ k, int row1, R frac, int g) {
-  R a = __ldg(k + (size_t)(row1 - 1) * NG + g), b = __ldg(k + (size_t)row1 * NG + g);
+template <class R, int NG, class TT>
+__device__ __forceinline__ R lin(const TT* __restrict__ k, int row1, R frac, int g) {
+  R a = (R)__ldg(k + (size_t)(row1 - 1) * NG + g), b = (R)__ldg(k + (size_t)row1 * NG + g);
   return a + frac * (b - a);
 }
 // Minor table k(j, indm, g) with nj rows in eta: eta- then T-interpolated.
-template <class R, int NG>
-__device__ __forceinline__ R minor_eta(const R* __restrict__ k, int nj, int jm, R fm, int indm, R minorfrac, int g) {
+template <class R, int NG, class TT>
+__device__ __forceinline__ R minor_eta(const TT* __restrict__ k, int nj, int jm, R fm, int indm, R minorfrac, int g) {
   auto K = [&](int j, int m) { return __ldg(k + ((size_t)(m - 1) * nj + (j - 1)) * NG + g); };
   R m1 = K(jm, indm) + fm * (K(jm + 1, indm) - K(jm, indm));
   R m2 = K(jm, indm + 1) + fm * (K(jm + 1, indm + 1) - K(jm, indm + 1));
   return m1 + minorfrac * (m2 - m1);
+}
+
+// x^e for the minor-gas column adjustments: the FP64/FP32 forms evaluate pow
+// in FP64 as written; the dual form carries the derivative.
+template <class R>
+__device__ __forceinline__ R rpow(R x, double e) {
+  return (R)pow((double)x, e);
+}
+template <class R>
+__device__ __forceinline__ Dual<R> rpow(Dual<R> x, double e) {
+  return pow(x, (R)e);
 }
 
 template <class R>
@@ -142,7 +154,7 @@ __device__ __forceinline__ R adj_col(R col, R coldry, R chiref, R thresh, R base
   R chi_x = col / (coldry);
   R ratx = (R)1.e20 * chi_x / chiref;
   if (ratx > thresh) {
-    R adjfac = base + (R)pow((double)(ratx - base), expo);
+    R adjfac = base + rpow(ratx - base, expo);
     return adjfac * chiref * coldry * (R)1.e-20;
   }
   return col;
@@ -156,17 +168,19 @@ struct LwBandCtx {
 // taug / fracs of band B for g (0-based in band) at one layer.
 // C: band layout and FP64 constants; CR: the per-layer constants in type R
 // (C itself for FP64, its FP32 copy for the split path).
-template <int B, class R, class RC>
-__device__ __forceinline__ void lw_gas(const LwConst& C, const RC& CR, const LwLayerView<R>& L, const Idx& ix,
-                                       bool lower, int g, const R* __restrict__ tab, R& taug, R& fracs) {
+// V: layer-field accessor returning R; TT: table element type (R itself, or
+// the value type of a dual R).
+template <int B, class R, class RC, class V, class TT>
+__device__ __forceinline__ void lw_gas(const LwConst& C, const RC& CR, const V& L, const Idx& ix, bool lower, int g,
+                                       const TT* __restrict__ tab, R& taug, R& fracs) {
   constexpr int NG = lw_ng(B);
   const BandDesc& bd = C.band[B - 1];
-  const R* ka = tab + bd.off[LW_KA];
-  const R* kb = tab + bd.off[LW_KB];
-  const R* self = tab + bd.off[LW_SELF];
-  const R* forr = tab + bd.off[LW_FOR];
-  const R* fra = tab + bd.off[LW_FRA];
-  const R* frb = tab + bd.off[LW_FRB];
+  const TT* ka = tab + bd.off[LW_KA];
+  const TT* kb = tab + bd.off[LW_KB];
+  const TT* self = tab + bd.off[LW_SELF];
+  const TT* forr = tab + bd.off[LW_FOR];
+  const TT* fra = tab + bd.off[LW_FRA];
+  const TT* frb = tab + bd.off[LW_FRB];
   using CT = std::remove_cv_t<std::remove_reference_t<decltype(CR.oneminus)>>;  // double or float
   const R one_m = (R)CR.oneminus;
   const int jp = ix.jp;
@@ -176,9 +190,9 @@ __device__ __forceinline__ void lw_gas(const LwConst& C, const RC& CR, const LwL
   auto i_up1 = [&](int js) { return ((jp - 12) * 5 + (ix.jt1 - 1)) * bd.nspb + js; };
   auto tself = [&]() { return L(LF_SELFFAC) * lin<R, NG>(self, ix.inds, L(LF_SELFFRAC), g); };
   auto tfor = [&]() { return L(LF_FORFAC) * lin<R, NG>(forr, ix.indf, L(LF_FORFRAC), g); };
-  auto fr1 = [&](const R* fr) { return __ldg(fr + g); };
-  auto fr_eta = [&](const R* fr, const EtaV<R>& e) { return lin<R, NG>(fr, e.js, e.fs, g); };
-  auto i4 = [&](const R* k, int i0, int i1) {
+  auto fr1 = [&](const TT* fr) { return (R)__ldg(fr + g); };
+  auto fr_eta = [&](const TT* fr, const EtaV<R>& e) { return lin<R, NG>(fr, e.js, e.fs, g); };
+  auto i4 = [&](const TT* k, int i0, int i1) {
     return interp4<R, NG>(k, L(LF_FAC00), L(LF_FAC10), L(LF_FAC01), L(LF_FAC11), i0, i1, g);
   };
   auto rat = [&](const auto* r, int j) { return (R)r[j]; };
@@ -250,7 +264,7 @@ __device__ __forceinline__ void lw_gas(const LwConst& C, const RC& CR, const LwL
         R ratco2 = (R)1.e20 * chi_co2 / (R)3.55e-4;
         R adjcolco2;
         if (ratco2 > (R)3.0) {
-          R adjfac = (R)2.0 + (R)pow((double)(ratco2 - (R)2.0), 0.68);
+          R adjfac = (R)2.0 + rpow(ratco2 - (R)2.0, 0.68);
           adjcolco2 = adjfac * (R)3.55e-4 * L(LF_COLDRY) * (R)1.e-20;
         } else {
           adjcolco2 = L(LF_COLCO2);

@@ -40,8 +40,8 @@ __device__ __forceinline__ EtaV<R> sw_band_eta(const V& L, R mult, R one_m) {
 }
 
 // speccomb * (8-term eta / T / p interpolation); stride 9 (lower) or 5 (upper).
-template <class R, int NG>
-__device__ __forceinline__ R sw_major8(const R* __restrict__ k, const EtaV<R>& e, R f00, R f10, R f01, R f11,
+template <class R, int NG, class TT>
+__device__ __forceinline__ R sw_major8(const TT* __restrict__ k, const EtaV<R>& e, R f00, R f10, R f01, R f11,
                                        int i0, int i1, int s, int g) {
   auto K = [&](int i) { return __ldg(k + (size_t)(i - 1) * NG + g); };
   R fs = e.fs;
@@ -51,31 +51,31 @@ __device__ __forceinline__ R sw_major8(const R* __restrict__ k, const EtaV<R>& e
                        fac001 * K(i1) + fac101 * K(i1 + 1) + fac011 * K(i1 + s) + fac111 * K(i1 + s + 1));
 }
 
-template <int B, class R, class V>
+template <int B, class R, class V, class TT>
 __device__ __forceinline__ void sw_gas(const SwConst& C, const V& L, const Idx& ix, bool lower, int g,
-                                       const R* __restrict__ tab, R& taug, R& taur) {
+                                       const TT* __restrict__ tab, R& taug, R& taur) {
   constexpr int NG = sw_ng(B);
   const BandDesc& bd = C.band[B - 16];
-  const R* ka = tab + bd.off[SW_KA];
-  const R* kb = tab + bd.off[SW_KB];
-  const R* self = tab + bd.off[SW_SELF];
-  const R* forr = tab + bd.off[SW_FOR];
-  const R* rayl = tab + bd.off[SW_RAYL];
+  const TT* ka = tab + bd.off[SW_KA];
+  const TT* kb = tab + bd.off[SW_KB];
+  const TT* self = tab + bd.off[SW_SELF];
+  const TT* forr = tab + bd.off[SW_FOR];
+  const TT* rayl = tab + bd.off[SW_RAYL];
   const R one_m = (R)C.oneminus;
   const int jp = ix.jp;
   auto i_lo = [&](int js) { return ((jp - 1) * 5 + (ix.jt - 1)) * bd.nspa + js; };
   auto i_lo1 = [&](int js) { return (jp * 5 + (ix.jt1 - 1)) * bd.nspa + js; };
   auto i_up = [&](int js) { return ((jp - 13) * 5 + (ix.jt - 1)) * bd.nspb + js; };
   auto i_up1 = [&](int js) { return ((jp - 12) * 5 + (ix.jt1 - 1)) * bd.nspb + js; };
-  auto i4 = [&](const R* k, int i0, int i1) {
+  auto i4 = [&](const TT* k, int i0, int i1) {
     return interp4<R, NG>(k, L(SF_FAC00), L(SF_FAC10), L(SF_FAC01), L(SF_FAC11), i0, i1, g);
   };
   auto selft = [&]() { return L(SF_SELFFAC) * lin<R, NG>(self, ix.inds, L(SF_SELFFRAC), g); };
   auto fort = [&]() { return L(SF_FORFAC) * lin<R, NG>(forr, ix.indf, L(SF_FORFRAC), g); };
-  auto m8 = [&](const R* k, const EtaV<R>& e, int i0, int i1, int s) {
+  auto m8 = [&](const TT* k, const EtaV<R>& e, int i0, int i1, int s) {
     return sw_major8<R, NG>(k, e, L(SF_FAC00), L(SF_FAC10), L(SF_FAC01), L(SF_FAC11), i0, i1, s, g);
   };
-  auto E = [&](int role) { return __ldg(tab + bd.off[role] + g); };
+  auto E = [&](int role) { return (R)__ldg(tab + bd.off[role] + g); };
   const R colmol = L(SF_COLMOL);
 
   if constexpr (B == 16 || B == 18 || B == 19 || B == 21 || B == 22 || B == 17) {
@@ -146,22 +146,24 @@ __device__ __forceinline__ void sw_gas(const SwConst& C, const V& L, const Idx& 
 // Solar source of g-point g of band B, taken at the band's reference layer
 // (laysolfr, computed by the prep kernel exactly as the taumol loops do).
 // Bands whose sfluxref depends on eta interpolate it with that layer's eta.
+// The result has the view's type (double, or a dual for the adjoint).
 template <int B, class V>
-__device__ __forceinline__ double sw_sfluxzen(const SwConst& C, const V& L, bool lower, int g,
-                                              const double* __restrict__ tab) {
+__device__ __forceinline__ auto sw_sfluxzen(const SwConst& C, const V& L, bool lower, int g,
+                                            const double* __restrict__ tab) {
+  using R = decltype(L(0));
   constexpr int NG = sw_ng(B);
   const BandDesc& bd = C.band[B - 16];
   const double* sf = tab + bd.off[SW_SFLUX];
   if constexpr (B == 17 || B == 28) {
-    EtaV<double> e = sw_band_eta<B, double>(L, 4., C.oneminus);
-    return lin<double, NG>(sf, e.js, e.fs, g);
+    EtaV<R> e = sw_band_eta<B, R>(L, (R)4., (R)C.oneminus);
+    return lin<R, NG>(sf, e.js, e.fs, g);
   } else if constexpr (B == 18 || B == 19 || B == 21 || B == 22 || B == 24) {
-    EtaV<double> e = sw_band_eta<B, double>(L, 8., C.oneminus);
-    return lin<double, NG>(sf, e.js, e.fs, g);
+    EtaV<R> e = sw_band_eta<B, R>(L, (R)8., (R)C.oneminus);
+    return lin<R, NG>(sf, e.js, e.fs, g);
   } else if constexpr (B == 27) {
-    return (50.15 / 48.37) * __ldg(sf + g);
+    return (R)((50.15 / 48.37) * __ldg(sf + g));
   } else {
-    return __ldg(sf + g);
+    return (R)__ldg(sf + g);
   }
 }
 

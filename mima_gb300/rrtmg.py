@@ -33,11 +33,13 @@ RRTMG_ERR_INPUT = 5
 RRTMG_ERR_NOMEM = 6
 PREC = {"fp64": 0, "split": 1}
 STATIC_SCRATCH_BYTES = 64 * 1024 * 1024  # RRTMG_GPU_STATIC_SCRATCH_BYTES
+TRANS = {"table": 0, "analytic": 1}
 
 # Every symbol include/rrtmg_gpu.h declares.
 EXPORTED = ("rrtmg_gpu_init", "rrtmg_gpu_finalize", "rrtmg_gpu_set_precision", "rrtmg_gpu_error_string",
             "rrtmg_gpu_last_error", "rrtmg_gpu_launch_count", "rrtmg_lw_c", "rrtmg_sw_c", "rrtmg_lw_dev",
-            "rrtmg_sw_dev", "rrtmg_gpu_reserve", "rrtmg_gpu_sync_status", "rrtmg_lw_dev_static")
+            "rrtmg_sw_dev", "rrtmg_gpu_reserve", "rrtmg_gpu_sync_status", "rrtmg_lw_dev_static",
+            "rrtmg_gpu_set_transcendentals", "rrtmg_jacobian_dev", "rrtmg_vjp_dev")
 
 _lib = None
 _dp = C.POINTER(C.c_double)
@@ -205,6 +207,53 @@ class RRTMG:
             o("uflx"), o("dflx"), o("hr"), o("uflxc"), o("dflxc"), o("hrc"), o("duflx_dt"), o("duflxc_dt"))
         self._check(rc)
 
+    def set_transcendentals(self, mode: str):
+        """"table" (the reference's lookup tables, default) or "analytic"."""
+        self._check(self.lib.rrtmg_gpu_set_transcendentals(self._h, TRANS[mode]))
+
+    def _adjoint(self, fn, stream, ncol, nlay, d, extra, adjes, dyofyr, scon, iaer=0, tauaer_lw=None,
+                 tauaer_sw=None, ssaaer=None, asmaer=None):
+        g = lambda k: _dptr(d.get(k))
+        rc = fn(self._h, C.c_void_p(stream or 0), C.c_int(ncol), C.c_int(nlay),
+                g("play"), g("plev"), g("tlay"), g("tlev"), g("tsfc"), g("h2ovmr"), g("o3vmr"), g("co2vmr"),
+                g("ch4vmr"), g("n2ovmr"), g("o2vmr"), g("cfc11vmr"), g("cfc12vmr"), g("cfc22vmr"), g("ccl4vmr"),
+                g("emis"), _dptr(tauaer_lw), g("asdir"), g("asdif"), g("aldir"), g("aldif"), g("coszen"),
+                C.c_double(adjes), C.c_int(dyofyr), C.c_double(scon), C.c_int(iaer), _dptr(tauaer_sw),
+                _dptr(ssaaer), _dptr(asmaer), *[_dptr(t) for t in extra])
+        self._check(rc)
+
+    def jacobian(self, atm):
+        """Host convenience: Jacobians (nx, ny, ncol) of ``atm`` (numpy)."""
+        import torch
+        nx, ny = adjoint_shape(atm.nlay)
+        d = atm_device_inputs(atm)
+        jac = torch.empty((nx, ny, atm.ncol), dtype=torch.float64, device="cuda")
+        s = torch.cuda.current_stream()
+        self.jacobian_dev(s.cuda_stream, atm.ncol, atm.nlay, d, jac, atm.adjes, atm.dyofyr, atm.scon)
+        s.synchronize()
+        return jac.cpu().numpy()
+
+    def vjp(self, atm, cot):
+        """Host convenience: cot (ny, ncol) -> grad (nx, ncol)."""
+        import torch
+        nx, ny = adjoint_shape(atm.nlay)
+        d = atm_device_inputs(atm)
+        c = torch.from_numpy(np.ascontiguousarray(cot, dtype=np.float64)).cuda()
+        grad = torch.empty((nx, atm.ncol), dtype=torch.float64, device="cuda")
+        s = torch.cuda.current_stream()
+        self.vjp_dev(s.cuda_stream, atm.ncol, atm.nlay, d, c, grad, atm.adjes, atm.dyofyr, atm.scon)
+        s.synchronize()
+        return grad.cpu().numpy()
+
+    def jacobian_dev(self, stream, ncol, nlay, d, jac, adjes, dyofyr, scon, **kw):
+        """Jacobians into ``jac`` (CUDA float64 tensor of shape (nx, ny, ncol),
+        nx = 3 nlay + 2 inputs, ny = 2 nlay + 3 rows; see include/rrtmg_gpu.h)."""
+        self._adjoint(self.lib.rrtmg_jacobian_dev, stream, ncol, nlay, d, [jac], adjes, dyofyr, scon, **kw)
+
+    def vjp_dev(self, stream, ncol, nlay, d, cot, grad, adjes, dyofyr, scon, **kw):
+        """grad (nx, ncol) = cot (ny, ncol) contracted with the Jacobian."""
+        self._adjoint(self.lib.rrtmg_vjp_dev, stream, ncol, nlay, d, [cot, grad], adjes, dyofyr, scon, **kw)
+
     def rrtmg_lw_dev_static(self, stream, ncol, nlay, icld, idrv, d, out, tauaer=None):
         """As :meth:`rrtmg_lw_dev`, through the allocation-free entry point
         (scratch in the library's static device array)."""
@@ -229,6 +278,19 @@ class RRTMG:
             C.c_int(0), None, None, None, None, None, None, None, None, None, g("tauaer"), g("ssaaer"),
             g("asmaer"), None, o("swuflx"), o("swdflx"), o("swhr"), o("swuflxc"), o("swdflxc"), o("swhrc"))
         self._check(rc)
+
+
+def adjoint_shape(nlay):
+    """(nx, ny) of the adjoint entry points: inputs tlay, q, tlev, tsfc; rows
+    LW heating, OLR, LW surface net, SW heating, SW surface net."""
+    return 3 * nlay + 2, 2 * nlay + 3
+
+
+def output_rows(lw, sw):
+    """The adjoint's output rows (ny, ncol) formed from forward outputs."""
+    L = lw["hr"].shape[0]
+    return np.concatenate([lw["hr"], lw["uflx"][L:L + 1], lw["uflx"][0:1] - lw["dflx"][0:1], sw["swhr"],
+                           sw["swdflx"][0:1] - sw["swuflx"][0:1]])
 
 
 def atm_device_inputs(atm, device="cuda"):

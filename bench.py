@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--config", type=int, default=1, help="workload configuration index (1 = T85x40)")
     ap.add_argument("--cpu-sample", type=int, default=2048, help="columns per CPU baseline step")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint cost measurement")
+    ap.add_argument("--members", type=int, default=32, help="stress configuration (4): ensemble members")
     return ap.parse_args()
 
 
@@ -109,6 +111,17 @@ class ClockSampler:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+def dominant_traffic(kernel, ncol):
+    """DRAM bytes per launch of the kernel from the committed ncu summary
+    (profiles/dram_traffic.json: bytes per column from one capture), scaled to
+    ncol columns; None when the kernel has no entry."""
+    p = ROOT / "profiles" / "dram_traffic.json"
+    if not p.exists():
+        return None
+    t = json.loads(p.read_text()).get(kernel)
+    return None if t is None else float(t["dram_bytes_per_column"]) * ncol
 
 
 def measured_peaks():
@@ -202,6 +215,198 @@ def time_graph(torch, g, stream, flush, steps, warmup):
     return [e0.elapsed_time(e1) for e0, e1 in evs]
 
 
+def workload_name(config, atm):
+    grid = {0: "T42", 1: "T85", 2: "T170", 3: "T42", 4: "T170"}[config]
+    return f"{grid}x{atm.nlay} ({atm.ncol} columns, {atm.nlay} layers) LW+SW clear sky per GPU"
+
+
+def kernel_bytes(name, ncol, nlay):
+    """Algorithmic bytes of one launch of an FP32-split g-point kernel: the
+    per-layer inputs it needs, read once in the float layout the prep kernel
+    writes, and the FP64 band partials it writes once."""
+    L = nlay
+    if name == "lw_gpoint":
+        rd = 4 * L + 4 * 25 * L + 4 * 16 * L + 4 * 16 * (L + 1) + 4 * 16 * 2 + 4 + 8 * 16
+        wr = 8 * 2 * 16 * (L + 1)
+    elif name == "sw_gpoint":
+        rd = 4 * L + 4 * 14 * L + 4 + 4 * 14 + 8 * 5
+        wr = 8 * 2 * 14 * (L + 1)
+    else:
+        return None
+    return ncol * (rd + wr)
+
+
+def dev_step(r, stream, atm, d, olw, osw):
+    r.rrtmg_lw_dev(stream.cuda_stream, atm.ncol, atm.nlay, 0, 0, d, olw)
+    r.rrtmg_sw_dev(stream.cuda_stream, atm.ncol, atm.nlay, 0, 0, d, osw, atm.adjes, atm.dyofyr, atm.scon)
+
+
+def profile_kernels(torch, r, stream, atm, d, olw, osw, precision, flush, n):
+    """Median CUDA-event duration of each kernel of the step, L2 flushed
+    before each of the LW and SW calls (non-graph launches)."""
+    r.set_precision(precision)
+    r.set_profiling(True)
+    runs = []
+    try:
+        for _ in range(n):
+            with torch.cuda.stream(stream):
+                flush.add_(1.0)
+                r.rrtmg_lw_dev(stream.cuda_stream, atm.ncol, atm.nlay, 0, 0, d, olw)
+                flush.add_(1.0)
+                r.rrtmg_sw_dev(stream.cuda_stream, atm.ncol, atm.nlay, 0, 0, d, osw, atm.adjes, atm.dyofyr,
+                               atm.scon)
+            runs.append(r.profile())
+    finally:
+        r.set_profiling(False)
+    return {k: float(np.median([x[k] for x in runs])) for k in runs[0]}
+
+
+def time_calls(torch, stream, flush, fn, steps, warmup):
+    """Mean CUDA-event time (ms) of fn() on stream, L2 flushed before each call."""
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            fn()
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for e0, e1 in evs:
+        with torch.cuda.stream(stream):
+            flush.add_(1.0)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+    torch.cuda.synchronize()
+    return float(np.mean([e0.elapsed_time(e1) for e0, e1 in evs]))
+
+
+def measure_adjoint(torch, rrtmg, atmosphere, r, stream, atm, d, olw, osw, flush, steps, warmup):
+    """Cost of the adjoint against the forward it differentiates (FP64,
+    analytic transcendentals): one vector-Jacobian product over the whole
+    workload, and full Jacobians of the 256-column adjoint configuration."""
+    dev = d["tlay"].device
+    nx, ny = rrtmg.adjoint_shape(atm.nlay)
+    cot = torch.randn(ny, atm.ncol, dtype=torch.float64, device=dev)
+    grad = torch.empty(nx, atm.ncol, dtype=torch.float64, device=dev)
+    r.set_precision("fp64")
+    r.set_transcendentals("analytic")
+    try:
+        fwd = lambda: dev_step(r, stream, atm, d, olw, osw)
+        vjp = lambda: r.vjp_dev(stream.cuda_stream, atm.ncol, atm.nlay, d, cot, grad, atm.adjes, atm.dyofyr,
+                                atm.scon)
+        ms_f = time_calls(torch, stream, flush, fwd, steps, warmup)
+        ms_v = time_calls(torch, stream, flush, vjp, steps, warmup)
+        a3 = atmosphere.config_atmosphere(3)
+        d3 = rrtmg.atm_device_inputs(a3, dev)
+        nx3, ny3 = rrtmg.adjoint_shape(a3.nlay)
+        jac = torch.empty(nx3, ny3, a3.ncol, dtype=torch.float64, device=dev)
+        o3lw, o3sw = rrtmg.device_outputs(a3.ncol, a3.nlay, dev)
+        jfn = lambda: r.jacobian_dev(stream.cuda_stream, a3.ncol, a3.nlay, d3, jac, a3.adjes, a3.dyofyr, a3.scon)
+        ms_j = time_calls(torch, stream, flush, jfn, steps, warmup)
+        ms_f3 = time_calls(torch, stream, flush, lambda: dev_step(r, stream, a3, d3, o3lw, o3sw), steps, warmup)
+    finally:
+        r.set_transcendentals("table")
+    return {"precision": "fp64 (analytic transcendentals)", "forward_ms": ms_f, "vjp_ms": ms_v,
+            "forward_plus_vjp_over_forward": (ms_f + ms_v) / ms_f,
+            "vjp_columns_per_s": atm.ncol / (ms_v * 1e-3),
+            "jacobian": {"workload": f"T42x40 adjoint configuration, {a3.ncol} columns", "ms": ms_j,
+                         "forward_ms": ms_f3, "rows": ny3, "inputs": nx3,
+                         "forward_plus_jacobian_over_forward": (ms_f3 + ms_j) / ms_f3}}
+
+
+def run_stress(args):
+    """1,048,576 x 60 stress configuration: a seeded ensemble of T170-like
+    members (131072 columns each, Ts noise 3 K), all resident in HBM; one
+    launch sequence runs the FP32-split forward of every member, a second one
+    the forward plus the FP64 adjoint (one vector-Jacobian product per member,
+    analytic transcendentals).  Reports columns/s of both, their cost ratio,
+    the peak device-memory footprint and the FP32-split error against FP64 on
+    a 4096-column subset."""
+    import torch
+    from mima_gb300 import atmosphere, rrtmg
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    free0, total = torch.cuda.mem_get_info()
+    r = rrtmg.RRTMG(device=0)
+    members = []
+    for m in range(args.members):
+        a = atmosphere.config_atmosphere(4, member=m)
+        members.append((a, rrtmg.atm_device_inputs(a, dev)))
+    a0 = members[0][0]
+    L, n = a0.nlay, a0.ncol
+    nx, ny = rrtmg.adjoint_shape(L)
+    olw, osw = rrtmg.device_outputs(n, L, dev)
+    cot = torch.randn(ny, n, dtype=torch.float64, device=dev)
+    grad = torch.empty(nx, n, dtype=torch.float64, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    r.reserve(n, L)
+
+    def forward(a, d):
+        r.set_precision("split")
+        r.set_transcendentals("table")
+        dev_step(r, stream, a, d, olw, osw)
+
+    def adjoint(a, d):
+        r.set_precision("fp64")
+        r.set_transcendentals("analytic")
+        r.vjp_dev(stream.cuda_stream, a.ncol, a.nlay, d, cot, grad, a.adjes, a.dyofyr, a.scon)
+
+    def sequence(with_adjoint):
+        for a, d in members:
+            forward(a, d)
+            if with_adjoint:
+                adjoint(a, d)
+
+    with torch.cuda.stream(stream):
+        forward(*members[0])
+        adjoint(*members[0])
+    torch.cuda.synchronize()
+    peak_used = total - torch.cuda.mem_get_info()[0]
+    times = {}
+    with ClockSampler(0) as clk:
+        for key, adj, reps in (("forward", False, 3), ("forward_adjoint", True, 1)):
+            ts = []
+            for it in range(1 + reps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                with torch.cuda.stream(stream):
+                    e0.record(stream)
+                    sequence(adj)
+                    e1.record(stream)
+                torch.cuda.synchronize()
+                if it >= 1:
+                    ts.append(e0.elapsed_time(e1))
+            times[key] = float(np.mean(ts))
+    r.set_transcendentals("table")
+    peak_used = max(peak_used, total - torch.cuda.mem_get_info()[0])
+    # FP32-split error against FP64 on a 4096-column subset of the first member
+    sub = a0.subset(np.linspace(0, n - 1, 4096).astype(int))
+    r.set_precision("fp64")
+    lw64, sw64 = r.lw(sub), r.sw(sub)
+    r.set_precision("split")
+    lw32, sw32 = r.lw(sub), r.sw(sub)
+    err = {"lw_hr_max_kday": float(np.abs(lw32["hr"] - lw64["hr"]).max()),
+           "sw_hr_max_kday": float(np.abs(sw32["swhr"] - sw64["swhr"]).max()),
+           "olr_max_wm2": float(np.abs(lw32["uflx"][-1] - lw64["uflx"][-1]).max()),
+           "sfc_flux_max_wm2": float(max(np.abs(lw32[k][0] - lw64[k][0]).max() for k in ("uflx", "dflx")))}
+    ncols = n * len(members)
+    line = {
+        "metric": METRIC, "value": ncols / (times["forward"] * 1e-3), "unit": UNIT, "n_gpus": 1,
+        "steps": 3, "warmup": 1, "ms_per_step": times["forward"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64 (FP32-split)",
+        "data": "synthetic (seeded T170-like ensemble; synthetic LW k-distribution, AER SW tables)",
+        "config": {"workload": f"stress: {len(members)} members x {n} columns x {L} layers = {ncols} columns",
+                   "l2": "inputs (GBs) far larger than L2"},
+        "stress": {"forward_columns_per_s": ncols / (times["forward"] * 1e-3),
+                   "forward_adjoint_columns_per_s": ncols / (times["forward_adjoint"] * 1e-3),
+                   "forward_adjoint_over_forward": times["forward_adjoint"] / times["forward"],
+                   "adjoint": "FP64 vector-Jacobian product per member (analytic transcendentals)",
+                   "peak_device_bytes": int(peak_used), "device_bytes_before": int(total - free0),
+                   "error_vs_fp64_4096_subset": err},
+        "gpu_launches": 6 * len(members) * 3,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_ours(args):
     import torch
     from mima_gb300 import atmosphere, rrtmg
@@ -263,6 +468,15 @@ def run_ours(args):
     value = ncol_total / (ms32 * 1e-3)
     fp64_value = ncol_total / (ms64 * 1e-3)
 
+    # per-kernel durations (CUDA events around each launch on the launching stream)
+    nprof = max(3, args.steps // 4)
+    kms32 = profile_kernels(torch, r, stream, atm, d, olw32, osw32, "split", flush, nprof)
+    kms64 = profile_kernels(torch, r, stream, atm, d, olw64, osw64, "fp64", flush, max(3, nprof // 2))
+    adjoint = None
+    if not args.no_adjoint:
+        adjoint = measure_adjoint(torch, rrtmg, atmosphere, r, stream, atm, d, olw64, osw64, flush,
+                                  max(3, args.steps // 4), min(args.warmup, 3))
+
     # end to end through the host-array entry points, pinned host memory
     e2e = None
     if not args.no_e2e:
@@ -292,13 +506,16 @@ def run_ours(args):
         return 0
     cpu_value, threads, nsample, _ = cpu_baseline(atm, min(args.cpu_sample, 2048), steps=1)
     peaks, src = measured_peaks()
-    achieved = nbytes / (ms32 * 1e-3) / 1e9
+    dom = max(("lw_gpoint", "sw_gpoint"), key=lambda k: kms32[k])
+    dom_bytes = kernel_bytes(dom, atm.ncol, atm.nlay)
+    achieved = dom_bytes / (kms32[dom] * 1e-3) / 1e9
+    traffic = dominant_traffic(dom, atm.ncol)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64 (FP32-split)",
-        "data": "synthetic (seeded T85 atmospheres; synthetic LW k-distribution, AER SW tables)",
-        "config": {"workload": f"T85x40 (256x128 = {atm.ncol} columns, 40 layers) LW+SW clear sky per GPU",
+        "data": "synthetic (seeded atmospheres of the configured grid; synthetic LW k-distribution, AER SW tables)",
+        "config": {"workload": workload_name(args.config, atm),
                    "per_gpu_columns": atm.ncol, "l2": "flushed (256 MB write) before every timed step",
                    "graph": "LW+SW step captured in one CUDA graph", "parallelism": f"columns x{world}"},
         "fp64": {"value": fp64_value, "unit": UNIT, "ms_per_step": ms64},
@@ -307,13 +524,18 @@ def run_ours(args):
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                     "frac": achieved / peaks["hbm_gbs"], "traffic": None,
-                     "note": f"algorithmic bytes {nbytes} per step; peak {src}; the path is compute/latency bound"},
+                     "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "kernel": f"{dom} (FP32-split)",
+                     "algorithmic_bytes_per_launch": dom_bytes, "kernel_ms": kms32[dom],
+                     "note": (f"peak {src}; the g-point solvers are latency/FP-pipe bound, not HBM bound: "
+                              f"step algorithmic bytes {nbytes}")},
+        "kernels_ms": {"split": kms32, "fp64": kms64},
         "cpu_baseline": {"value": cpu_value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{nsample} of {atm.ncol} T85 columns, LW+SW FP64 C++ restatement"},
+                         "sample": f"{nsample} of {atm.ncol} columns, LW+SW FP64 C++ restatement"},
     }
     if e2e:
         line["e2e"] = e2e
+    if adjoint:
+        line["adjoint"] = adjoint
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -324,6 +546,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.config == 4:
+        return run_stress(args)
     return run_ours(args)
 
 

@@ -142,6 +142,15 @@ int rrtmg_sw_dev(rrtmg_gpu_handle h, void* stream, int ncol, int nlay, int icld,
                  double* swuflx, double* swdflx, double* swhr, double* swuflxc, double* swdflxc,
                  double* swhrc);
 
+/* No counterpart in the reference.  Kernel timing: while enabled, the LW and
+ * SW calls record CUDA events around each of their three kernels (prep,
+ * g-point solver, finalize) on the call's stream (not while the stream is
+ * being captured).  rrtmg_gpu_profile waits for the events and writes the
+ * six durations of the last LW and SW call in ms: LW prep, LW g-point, LW
+ * finalize, SW prep, SW g-point, SW finalize. */
+int rrtmg_gpu_set_profiling(rrtmg_gpu_handle h, int on);
+int rrtmg_gpu_profile(rrtmg_gpu_handle h, float* ms);
+
 /* No counterpart in the reference (which always uses its tables).  Selects
  * RRTMG_TRANS_TABLE or RRTMG_TRANS_ANALYTIC for later calls on the handle. */
 int rrtmg_gpu_set_transcendentals(rrtmg_gpu_handle h, int mode);

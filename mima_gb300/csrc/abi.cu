@@ -44,6 +44,10 @@ struct rrtmg_gpu_state {
   DevBuf lw_ws, sw_ws, io, adj_ws;
   long long launches = 0;
   std::string err;
+  // Optional per-kernel timing: events around every launch of the last LW
+  // and SW call (prep, g-point, finalize), outside stream capture only.
+  bool profiling = false;
+  cudaEvent_t ev[2][4] = {};
 };
 
 namespace {
@@ -167,23 +171,36 @@ SwPrepT<F> prep_of(const SwWorkT<F>& w) {
 // Enqueue one LW radiation call on stream s (all pointers on the device) with
 // its scratch carved from `base` (carve_lw bytes).
 // ---------------------------------------------------------------------------
+// Records profiling event k of family fam (0 LW, 1 SW) on s when enabled.
+void mark(rrtmg_gpu_state* h, int fam, int k, cudaStream_t s) {
+  if (!h->profiling) return;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) return;
+  cudaEventRecord(h->ev[fam][k], s);
+}
+
 int lw_enqueue(rrtmg_gpu_state* h, cudaStream_t s, void* base, int ncol, int nlay, int idrv, const LwIn& in,
                double* uflx, double* dflx, double* hr, double* uflxc, double* dflxc, double* hrc, double* duflx_dt,
                double* duflxc_dt) {
   LwWork w = carve_lw(base, ncol, nlay, nullptr);
+  mark(h, 0, 0, s);
   const int nb = lw_gpoint_blocks(h->host.lw, ncol);
   if (h->precision == RRTMG_PREC_SPLIT) {
     const LwWorkT<float> w32 = work_as<float>(w);
     launch_lw_prep_split(in, w32, h->totplnk, h->totplnkderiv, ncol, nlay, idrv, h->flags, s);
+    mark(h, 0, 1, s);
     launch_lw_gpoint_split(prep_of(w32), in.emis, in.tauaer, h->lw_tab32, h->lw_exp32, h->lw_tfn32, w.bu, w.bd,
                            w.bdu, ncol, nlay, idrv, nb, h->analytic, s);
   } else {
     launch_lw_prep(in, w, h->totplnk, h->totplnkderiv, ncol, nlay, idrv, h->flags, s);
+    mark(h, 0, 1, s);
     launch_lw_gpoint_fp64(prep_of(w), in.emis, in.tauaer, h->lw_tab64, h->lw_exp64, h->lw_tfn64, w.bu, w.bd, w.bdu,
                           ncol, nlay, idrv, nb, h->analytic, s);
   }
+  mark(h, 0, 2, s);
   launch_lw_finalize(w.bu, w.bd, w.bdu, in.plev, ncol, nlay, idrv, uflx, dflx, hr, uflxc, dflxc, hrc, duflx_dt,
                      duflxc_dt, s);
+  mark(h, 0, 3, s);
   h->launches += 3;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(h, e, "LW kernel launch");
@@ -221,17 +238,22 @@ int sw_run(rrtmg_gpu_state* h, cudaStream_t s, int ncol, int nlay, int iaer, dou
   SwWork w = carve_sw(h->sw_ws.p, ncol, nlay, nullptr);
   const double adjflux = adjflux_of(h, adjes, dyofyr, scon);
   const int nb = sw_gpoint_blocks(h->host.sw, ncol);
+  mark(h, 1, 0, s);
   if (h->precision == RRTMG_PREC_SPLIT) {
     const SwWorkT<float> w32 = work_as<float>(w);
     launch_sw_prep_split(in, w32, ncol, nlay, h->flags, s);
+    mark(h, 1, 1, s);
     launch_sw_gpoint_split(prep_of(w32), in, adjflux, iaer, h->sw_tab32, h->sw_tab64, h->sw_exp32, w.su, w.sd, ncol,
                            nlay, nb, h->analytic, s);
   } else {
     launch_sw_prep(in, w, ncol, nlay, h->flags, s);
+    mark(h, 1, 1, s);
     launch_sw_gpoint_fp64(prep_of(w), in, adjflux, iaer, h->sw_tab64, h->sw_exp64, w.su, w.sd, ncol, nlay, nb,
                           h->analytic, s);
   }
+  mark(h, 1, 2, s);
   launch_sw_finalize(w.su, w.sd, in.plev, in.coszen, ncol, nlay, swuflx, swdflx, swhr, swuflxc, swdflxc, swhrc, s);
+  mark(h, 1, 3, s);
   h->launches += 3;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(h, e, "SW kernel launch");
@@ -394,6 +416,9 @@ int rrtmg_gpu_finalize(rrtmg_gpu_handle h) {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->stream) cudaStreamDestroy(h->stream);
+  for (auto& fam : h->ev)
+    for (auto& e : fam)
+      if (e) cudaEventDestroy(e);
   delete h;
   return RRTMG_OK;
 }
@@ -411,6 +436,32 @@ int rrtmg_gpu_set_transcendentals(rrtmg_gpu_handle h, int mode) {
   if (mode != RRTMG_TRANS_TABLE && mode != RRTMG_TRANS_ANALYTIC)
     return fail(h, RRTMG_ERR_ARG, "mode must be RRTMG_TRANS_TABLE or RRTMG_TRANS_ANALYTIC");
   h->analytic = mode == RRTMG_TRANS_ANALYTIC;
+  return RRTMG_OK;
+}
+
+int rrtmg_gpu_set_profiling(rrtmg_gpu_handle h, int on) {
+  if (!valid_handle(h)) return RRTMG_ERR_ARG;
+  cudaSetDevice(h->device);
+  if (on && !h->ev[0][0]) {
+    for (auto& fam : h->ev)
+      for (auto& e : fam) {
+        cudaError_t r = cudaEventCreate(&e);
+        if (r != cudaSuccess) return cuda_fail(h, r, "create profiling events");
+      }
+  }
+  h->profiling = on != 0;
+  return RRTMG_OK;
+}
+
+int rrtmg_gpu_profile(rrtmg_gpu_handle h, float* ms) {
+  if (!valid_handle(h) || !ms) return RRTMG_ERR_ARG;
+  if (!h->ev[0][0]) return fail(h, RRTMG_ERR_ARG, "profiling was never enabled on this handle");
+  for (int f = 0; f < 2; ++f)
+    for (int k = 0; k < 3; ++k) {
+      cudaError_t r = cudaEventSynchronize(h->ev[f][k + 1]);
+      if (r == cudaSuccess) r = cudaEventElapsedTime(&ms[3 * f + k], h->ev[f][k], h->ev[f][k + 1]);
+      if (r != cudaSuccess) return cuda_fail(h, r, "read profiling events");
+    }
   return RRTMG_OK;
 }
 

@@ -39,7 +39,9 @@ TRANS = {"table": 0, "analytic": 1}
 EXPORTED = ("rrtmg_gpu_init", "rrtmg_gpu_finalize", "rrtmg_gpu_set_precision", "rrtmg_gpu_error_string",
             "rrtmg_gpu_last_error", "rrtmg_gpu_launch_count", "rrtmg_lw_c", "rrtmg_sw_c", "rrtmg_lw_dev",
             "rrtmg_sw_dev", "rrtmg_gpu_reserve", "rrtmg_gpu_sync_status", "rrtmg_lw_dev_static",
-            "rrtmg_gpu_set_transcendentals", "rrtmg_jacobian_dev", "rrtmg_vjp_dev")
+            "rrtmg_gpu_set_transcendentals", "rrtmg_jacobian_dev", "rrtmg_vjp_dev", "rrtmg_gpu_set_profiling",
+            "rrtmg_gpu_profile")
+KERNELS = ("lw_prep", "lw_gpoint", "lw_finalize", "sw_prep", "sw_gpoint", "sw_finalize")
 
 _lib = None
 _dp = C.POINTER(C.c_double)
@@ -206,6 +208,15 @@ class RRTMG:
             g("emis"), C.c_int(0), C.c_int(0), C.c_int(0), None, None, None, None, None, None, _dptr(tauaer),
             o("uflx"), o("dflx"), o("hr"), o("uflxc"), o("dflxc"), o("hrc"), o("duflx_dt"), o("duflxc_dt"))
         self._check(rc)
+
+    def set_profiling(self, on: bool):
+        self._check(self.lib.rrtmg_gpu_set_profiling(self._h, int(bool(on))))
+
+    def profile(self) -> dict:
+        """Durations (ms) of the six kernels of the last profiled LW and SW call."""
+        ms = (C.c_float * 6)()
+        self._check(self.lib.rrtmg_gpu_profile(self._h, ms))
+        return dict(zip(KERNELS, [float(v) for v in ms]))
 
     def set_transcendentals(self, mode: str):
         """"table" (the reference's lookup tables, default) or "analytic"."""

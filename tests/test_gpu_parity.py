@@ -187,3 +187,20 @@ def test_launch_count_is_native(gpu):
     gpu.lw(atm)
     gpu.sw(atm)
     assert gpu.launch_count() - before == 6
+
+
+@pytest.mark.gpu
+def test_fp64_path_reproduces_golden_fixtures(gpu):
+    """The committed oracle regression fixtures (tests/golden) at the FP64 tolerance."""
+    from pathlib import Path
+    ref = np.load(Path(__file__).with_name("golden") / "oracle_regression.npz")
+    gpu.set_precision("fp64")
+    for name, (ncol, nlay, seed, sig, rh) in {"l40": (8, 40, 101, 2.0, False), "l60": (6, 60, 202, 5.0, True)}.items():
+        atm = A.small_atmosphere(ncol, nlay, seed=seed, ts_sigma=sig, rh_random=rh)
+        lw, sw = gpu.lw(atm, idrv=1), gpu.sw(atm)
+        for k in ("uflx", "dflx", "duflx_dt"):
+            assert rel_err(lw[k], ref[f"{name}_{k}"], 1e-6) <= FLUX_TOL, (name, k)
+        assert rel_err(lw["hr"], ref[f"{name}_hr"], 1e-3) <= HR_TOL, name
+        for k in ("swuflx", "swdflx"):
+            assert rel_err(sw[k], ref[f"{name}_{k}"], 1e-6) <= FLUX_TOL, (name, k)
+        assert rel_err(sw["swhr"], ref[f"{name}_swhr"], 1e-3) <= HR_TOL, name

@@ -113,3 +113,22 @@ def test_idrv_matches_finite_difference_of_surface_temperature(orc):
     # (rrtmg_lw_setcoef.f90:1287-1990), not the slope of the interpolated
     # totplnk, so the two agree to the tables' mutual consistency (~0.3%).
     assert np.allclose(d, fd, rtol=1e-2, atol=1e-4)
+
+
+def test_oracle_reproduces_golden_fixtures(orc):
+    """Regression fixtures of the oracle (tests/golden/make_golden.py)."""
+    import importlib.util
+    from pathlib import Path
+    from mima_gb300 import tables
+    g = Path(__file__).with_name("golden")
+    ref = np.load(g / "oracle_regression.npz")
+    blob = Path(tables.ensure_blob()).read_bytes()
+    assert int(ref["blob_checksum"][0]) == tables.blob_checksum(blob), "table blob differs from the fixtures'"
+    spec = importlib.util.spec_from_file_location("make_golden", g / "make_golden.py")
+    mk = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mk)
+    now = mk.compute()
+    for k in ref.files:
+        if k == "blob_checksum":
+            continue
+        np.testing.assert_allclose(now[k], ref[k], rtol=1e-11, atol=1e-12, err_msg=k)

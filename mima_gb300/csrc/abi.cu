@@ -120,6 +120,7 @@ LwWork carve_lw(void* base, int ncol, int nlay, size_t* bytes) {
   w.bu = c.take<double>(16 * (L + 1) * N);
   w.bd = c.take<double>(16 * (L + 1) * N);
   w.bdu = c.take<double>(16 * (L + 1) * N);
+  w.colsum = c.take<double>(2 * L * N);
   if (bytes) *bytes = c.off;
   return w;
 }
@@ -152,7 +153,7 @@ int check_dims(rrtmg_gpu_state* h, int ncol, int nlay) {
 template <class F>
 LwWorkT<F> work_as(const LwWork& w) {
   return LwWorkT<F>{w.idx, (F*)w.f, (F*)w.planklay, (F*)w.planklev, (F*)w.plankbnd, (F*)w.dplankbnd, (F*)w.secdiff,
-                    w.laytrop, w.bu, w.bd, w.bdu};
+                    w.laytrop, w.bu, w.bd, w.bdu, w.colsum};
 }
 template <class F>
 SwWorkT<F> work_as(const SwWork& w) {
@@ -201,7 +202,7 @@ int lw_enqueue(rrtmg_gpu_state* h, cudaStream_t s, void* base, int ncol, int nla
   launch_lw_finalize(w.bu, w.bd, w.bdu, in.plev, ncol, nlay, idrv, uflx, dflx, hr, uflxc, dflxc, hrc, duflx_dt,
                      duflxc_dt, s);
   mark(h, 0, 3, s);
-  h->launches += 3;
+  h->launches += 4;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(h, e, "LW kernel launch");
   return RRTMG_OK;
@@ -254,7 +255,7 @@ int sw_run(rrtmg_gpu_state* h, cudaStream_t s, int ncol, int nlay, int iaer, dou
   mark(h, 1, 2, s);
   launch_sw_finalize(w.su, w.sd, in.plev, in.coszen, ncol, nlay, swuflx, swdflx, swhr, swuflxc, swdflxc, swhrc, s);
   mark(h, 1, 3, s);
-  h->launches += 3;
+  h->launches += 4;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(h, e, "SW kernel launch");
   return RRTMG_OK;
@@ -279,6 +280,7 @@ void carve_adj(void* base, int ncol, int nlay, int nseed_lw, int nseed_sw, AdjLw
   a.pbnd_t = c.take<double>(16 * N);
   a.secdiff = c.take<double>(16 * N);
   a.dsec = c.take<double>(16 * L * N);
+  a.hs = c.take<double>(L * N);
   a.part = c.take<double>((size_t)kLwBands * nseed_lw * adj_lw_entries(nlay) * N);
   AdjSwWork b;
   b.idx = c.take<uint32_t>(L * N);
@@ -287,6 +289,7 @@ void carve_adj(void* base, int ncol, int nlay, int nseed_lw, int nseed_sw, AdjLw
   b.fv = c.take<double>((size_t)SF_N * L * N);
   b.ft = c.take<double>((size_t)SF_N * L * N);
   b.fq = c.take<double>((size_t)SF_N * L * N);
+  b.hs = c.take<double>(L * N);
   b.part = c.take<double>((size_t)kSwBands * nseed_sw * adj_sw_entries(nlay) * N);
   if (lw) *lw = a;
   if (sw) *sw = b;

@@ -190,6 +190,7 @@ __global__ void __launch_bounds__(128) adj_lw_prep_kernel(LwIn in, AdjLwWork w, 
     put(LF_WX3, wx3);
     put(LF_WX4, wx4);
     w.idx[o] = pack_idx(jp, jt, jt1, indself, indfor, indminor);
+    w.hs[o] = C.heatfac / (pz_prev - pz_l);
     pz_prev = pz_l;
   }
   w.laytrop[col] = laytrop;
@@ -309,6 +310,7 @@ __device__ __forceinline__ void lw_adj_band(const LwIn& in, const AdjLwWork& w, 
   double tS[MAXL], dS[MAXL], uS[MAXL];  // d(t, sd, su)/dsecdiff
   double dLb[MAXL], uLt[MAXL];          // dsd/dtlev below, dsu/dtlev above
   double Dl[MAXL + 1], Ul[MAXL + 1], lamU[MAXL + 1];
+  double ck[MAXL];                      // seed cotangents of the layer divergences
 
   // 1. layer optics with tangents (recomputed from the checkpointed fields) and
   //    the downward recursion
@@ -334,10 +336,11 @@ __device__ __forceinline__ void lw_adj_band(const LwIn& in, const AdjLwWork& w, 
       tf_d = rec_6;
     } else {
       const double e = exp(-od), om = 1.0 - e;
+      const double iod = 1.0 / od, iom = 1.0 / om;
       a = om;
       a_d = e;
-      tf = 1.0 - 2.0 * ((1.0 / od) - (e / om));
-      tf_d = 2.0 / (od * od) - 2.0 * e / (om * om);
+      tf = 1.0 - 2.0 * (iod - e * iom);
+      tf_d = 2.0 * (iod * iod) - 2.0 * e * (iom * iom);
     }
     const double plf = fracs.v;
     const size_t ol = ((size_t)(B - 1) * nlay + k) * N + c;
@@ -376,14 +379,13 @@ __device__ __forceinline__ void lw_adj_band(const LwIn& in, const AdjLwWork& w, 
   // 3. reverse sweeps, one cotangent seed at a time
   const int wib = threadIdx.x >> 5;
   const int wcol0 = blk * CPB + (wib * 32) / W;
-  const double heatfac = c_lw.heatfac;
   for (int s = 0; s < nseed; ++s) {
-    auto cdiv = [&](int kk) -> double {  // cotangent of div_kk (kk = 1..nlay), flux units
-      if (kk < 1 || kk > nlay) return 0.0;
-      const double hs = heatfac / (__ldg(in.plev + (size_t)(kk - 1) * N + c) - __ldg(in.plev + (size_t)kk * N + c));
-      if (cot) return __ldg(cot + (size_t)(kk - 1) * N + c) * hs;
-      return s == kk - 1 ? hs : 0.0;
-    };
+    // cotangents of div_1..div_nlay in flux units (ck[k-1]), seed s
+    for (int kk = 1; kk <= nlay; ++kk) {
+      const double hs = __ldg(w.hs + (size_t)(kk - 1) * N + c);
+      ck[kk - 1] = cot ? __ldg(cot + (size_t)(kk - 1) * N + c) * hs : (s == kk - 1 ? hs : 0.0);
+    }
+    auto cdiv = [&](int kk) -> double { return (kk < 1 || kk > nlay) ? 0.0 : ck[kk - 1]; };
     const double colr = cot ? __ldg(cot + (size_t)nlay * N + c) : (s == nlay ? 1.0 : 0.0);
     const double csfc = cot ? __ldg(cot + (size_t)(nlay + 1) * N + c) : (s == nlay + 1 ? 1.0 : 0.0);
     auto aU = [&](int m) { return cdiv(m + 1) - cdiv(m) + (m == nlay ? colr : 0.0) + (m == 0 ? csfc : 0.0); };
@@ -542,6 +544,7 @@ __global__ void __launch_bounds__(128) adj_sw_prep_kernel(SwIn in, AdjSwWork w, 
     put(SF_FORFAC, forfac);
     put(SF_FORFRAC, forfrac);
     w.idx[o] = pack_idx(jp, jt, jt1, indself, indfor, 1);
+    w.hs[o] = C.heatfac / (pz_prev - pz_l);
     pz_prev = pz_l;
   }
   w.laytrop[col] = laytrop;
@@ -631,7 +634,11 @@ __device__ __forceinline__ void sw_adj_band(const SwIn& in, const AdjSwWork& w, 
   double Rv[MAXL], Rt[MAXL], Rq[MAXL], Dv[MAXL], Dt[MAXL], Dq[MAXL], Tv[MAXL], Tt[MAXL], Tq[MAXL];
   double Sv[MAXL], St[MAXL], Sq[MAXL], Xv[MAXL], Xt[MAXL], Xq[MAXL];
   double tb[MAXL + 1], tn[MAXL + 1], rn[MAXL + 1], pu[MAXL + 1], pd[MAXL + 1];
+  double zf[MAXL + 1], dn[MAXL + 1];  // 1/(1 - rn pd) and fd - fu per level
+  double zu[MAXL], zd[MAXL];          // reciprocals of the upward / downward recursions per layer
   double gR[MAXL], gD[MAXL], gT[MAXL], gS[MAXL], gX[MAXL];
+  double an[MAXL + 1];                // seed cotangents of net flux per bottom-up level
+  double lb[MAXL + 1], ln[MAXL + 1], lr[MAXL + 1];  // local cotangents of tb, tn, rn per level
   for (int j = 0; j < klev; ++j) {
     const int ikl = klev - j;
     const size_t o = (size_t)(ikl - 1) * N + c;
@@ -639,22 +646,27 @@ __device__ __forceinline__ void sw_adj_band(const SwIn& in, const AdjSwWork& w, 
     SwDualView L{w.fv, w.ft, w.fq, fstride, o};
     D2 taug, taur;
     sw_gas<B, D2>(c_sw, L, ix, ikl <= lt, gg, tab, taug, taur);
-    double taua = 0., omga = 1., asya = 0.;
+    D2 ztauc, zomcc, zgcc;
     if (iaer == 10) {
       const size_t oa = c + N * ((size_t)(ikl - 1) + (size_t)nlay * (ibm - 1));
-      taua = __ldg(in.tauaer + oa);
-      omga = __ldg(in.ssaaer + oa);
-      asya = __ldg(in.asmaer + oa);
+      const double taua = __ldg(in.tauaer + oa);
+      const double omga = __ldg(in.ssaaer + oa);
+      const double asya = __ldg(in.asmaer + oa);
+      ztauc = taur + taug + taua;
+      zomcc = taur * 1.0 + taua * omga;
+      zgcc = (asya * omga * taua) / zomcc;
+      zomcc = zomcc / ztauc;
+      const D2 zf = zgcc * zgcc;
+      const D2 zwf = zomcc * zf;
+      ztauc = (1.0 - zwf) * ztauc;
+      zomcc = (zomcc - zwf) / (1.0 - zwf);
+      zgcc = (zgcc - zf) / (1.0 - zf);
+    } else {
+      // without aerosol the delta scaling is the identity (asymmetry 0)
+      ztauc = taur + taug;
+      zomcc = taur / ztauc;
+      zgcc = D2(0.0);
     }
-    D2 ztauc = taur + taug + taua;
-    D2 zomcc = taur * 1.0 + taua * omga;
-    D2 zgcc = (asya * omga * taua) / zomcc;
-    zomcc = zomcc / ztauc;
-    const D2 zf = zgcc * zgcc;
-    const D2 zwf = zomcc * zf;
-    ztauc = (1.0 - zwf) * ztauc;
-    zomcc = (zomcc - zwf) / (1.0 - zwf);
-    zgcc = (zgcc - zf) / (1.0 - zf);
     D2 rf, rfd, tr, trd;
     reftra1<D2, double>(ztauc, zomcc, zgcc, D2(prmu0), D2(bpade), (const double*)nullptr, true, rf, rfd, tr, trd);
     const D2 tx = sw_exp_tbl<D2, double>(ztauc / prmu0, D2(bpade), (const double*)nullptr, true);
@@ -668,34 +680,49 @@ __device__ __forceinline__ void sw_adj_band(const SwIn& in, const AdjSwWork& w, 
   for (int j = 0; j < klev; ++j) {
     tb[j + 1] = Xv[j] * tb[j];
     const double z = 1.0 / (1.0 - Dv[j] * rn[j]);
+    zd[j] = z;
     tn[j + 1] = tb[j] * Tv[j] + Sv[j] * ((tn[j] - tb[j]) + tb[j] * Rv[j] * rn[j]) * z;
     rn[j + 1] = Dv[j] + Sv[j] * Sv[j] * rn[j] * z;
   }
   pu[klev] = albdir; pd[klev] = albdif;
   for (int j = klev - 1; j >= 0; --j) {
     const double z = 1.0 / (1.0 - pd[j + 1] * Dv[j]);
+    zu[j] = z;
     pu[j] = Rv[j] + Sv[j] * ((Tv[j] - Xv[j]) * pd[j + 1] + Xv[j] * pu[j + 1]) * z;
     pd[j] = Dv[j] + Sv[j] * Sv[j] * pd[j + 1] * z;
+  }
+  for (int j = 0; j <= klev; ++j) {
+    const double z = 1.0 / (1.0 - rn[j] * pd[j]);
+    zf[j] = z;
+    const double fu = (tb[j] * pu[j] + (tn[j] - tb[j]) * pd[j]) * z;
+    const double fd = tb[j] + (tn[j] - tb[j] + tb[j] * pu[j] * rn[j]) * z;
+    dn[j] = fd - fu;
   }
 
   const int wib = threadIdx.x >> 5;
   const int wcol0 = blk * CPB + (wib * 32) / W;
-  const double heatfac = c_sw.heatfac;
   const double gate = lit ? 1.0 : 0.0;  // dark columns have zero SW outputs
   for (int s = 0; s < nseed; ++s) {
     // cotangent of net at bottom-up level m
-    auto cdiv = [&](int kk) -> double {  // layers 1..nlay-1 (the top layer's rate is 0)
-      if (kk < 1 || kk > nlay - 1) return 0.0;
-      const double hs = heatfac / (__ldg(in.plev + (size_t)(kk - 1) * N + c) - __ldg(in.plev + (size_t)kk * N + c));
-      if (cot) return __ldg(cot + (size_t)(nlay + 2 + kk - 1) * N + c) * hs;
-      return s == kk - 1 ? hs : 0.0;
-    };
+    // cotangent of net at every bottom-up level m (an[m]); layers 1..nlay-1 carry
+    // heating cotangents (the top layer's rate is 0)
     const double csfc = cot ? __ldg(cot + (size_t)(2 * nlay + 2) * N + c) : (s == nlay ? 1.0 : 0.0);
-    auto anet = [&](int m) { return gate * (cdiv(m) - cdiv(m + 1) + (m == 0 ? csfc : 0.0)); };
+    double cprev = 0.0;  // cdiv(m)
+    for (int m = 0; m <= nlay; ++m) {
+      double cnext = 0.0;  // cdiv(m + 1)
+      const int kk = m + 1;
+      if (kk <= nlay - 1) {
+        const double hs = __ldg(w.hs + (size_t)(kk - 1) * N + c);
+        cnext = cot ? __ldg(cot + (size_t)(nlay + 2 + kk - 1) * N + c) * hs : (s == kk - 1 ? hs : 0.0);
+      }
+      an[m] = gate * (cprev - cnext + (m == 0 ? csfc : 0.0));
+      cprev = cnext;
+    }
+    auto anet = [&](int m) { return an[m]; };
     // local cotangents of the level states at top-down level j from the fluxes there
     auto local = [&](int j, double& ltb, double& ltn, double& lrn, double& lpu, double& lpd) {
       const double a = zinc.v * anet(klev - j);
-      const double z = 1.0 / (1.0 - rn[j] * pd[j]);
+      const double z = zf[j];
       const double Af = tb[j] * pu[j] + (tn[j] - tb[j]) * pd[j];
       const double Bf = tn[j] - tb[j] + tb[j] * pu[j] * rn[j];
       // fu = Af z (cotangent -a), fd = tb + Bf z (cotangent a)
@@ -706,21 +733,21 @@ __device__ __forceinline__ void sw_adj_band(const SwIn& in, const AdjSwWork& w, 
       lrn = -a * Af * z * z * pd[j] + a * (tb[j] * pu[j] * z + Bf * z * z * pd[j]);
     };
     double lzinc = 0.0;
-    for (int j = 0; j <= klev; ++j) {
-      const double z = 1.0 / (1.0 - rn[j] * pd[j]);
-      const double fu = (tb[j] * pu[j] + (tn[j] - tb[j]) * pd[j]) * z;
-      const double fd = tb[j] + (tn[j] - tb[j] + tb[j] * pu[j] * rn[j]) * z;
-      lzinc += anet(klev - j) * (fd - fu);
-    }
+    for (int j = 0; j <= klev; ++j) lzinc += anet(klev - j) * dn[j];
     for (int j = 0; j < klev; ++j) gR[j] = gD[j] = gT[j] = gS[j] = gX[j] = 0.0;
-    // reverse of the upward sweep, carried from the top down
+    // reverse of the upward sweep, carried from the top down; the local
+    // cotangents of (tb, tn, rn) are kept for the second sweep
     double Lu = 0.0, Ld = 0.0;
+    {
+      double lpu, lpd;
+      local(klev, lb[klev], ln[klev], lr[klev], lpu, lpd);
+    }
     for (int j = 0; j < klev; ++j) {
-      double ltb, ltn, lrn, lpu, lpd;
-      local(j, ltb, ltn, lrn, lpu, lpd);
+      double lpu, lpd;
+      local(j, lb[j], ln[j], lr[j], lpu, lpd);
       Lu += lpu;
       Ld += lpd;
-      const double z = 1.0 / (1.0 - pd[j + 1] * Dv[j]);
+      const double z = zu[j];
       const double Xx = (Tv[j] - Xv[j]) * pd[j + 1] + Xv[j] * pu[j + 1];
       const double Td = Sv[j];
       gR[j] += Lu;
@@ -737,13 +764,11 @@ __device__ __forceinline__ void sw_adj_band(const SwIn& in, const AdjSwWork& w, 
     // reverse of the downward sweep, carried from the surface up
     double Lb = 0.0, Ln = 0.0, Lr = 0.0;
     for (int j = klev; j >= 1; --j) {
-      double ltb, ltn, lrn, lpu, lpd;
-      local(j, ltb, ltn, lrn, lpu, lpd);
-      Lb += ltb;
-      Ln += ltn;
-      Lr += lrn;
+      Lb += lb[j];
+      Ln += ln[j];
+      Lr += lr[j];
       const int q = j - 1;
-      const double z = 1.0 / (1.0 - Dv[q] * rn[q]);
+      const double z = zd[q];
       const double Y = (tn[q] - tb[q]) + tb[q] * Rv[q] * rn[q];
       const double Td = Sv[q];
       gX[q] += Lb * tb[q];

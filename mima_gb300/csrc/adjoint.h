@@ -29,6 +29,7 @@ struct AdjLwWork {
   double *pbnd_v, *pbnd_t;       // emissivity * plankbnd [band][col] and d/dtsfc
   double* secdiff;               // [band][col]
   double* dsec;                  // d secdiff / d q [band][lay][col]
+  double* hs;                    // heatfac / (plev(l-1) - plev(l)) [lay][col]
   double* part;                  // band partial gradients [band][seed][entry][col]
 };
 
@@ -36,6 +37,7 @@ struct AdjSwWork {
   uint32_t* idx;
   int *laytrop, *laysolfr;
   double *fv, *ft, *fq;          // setcoef fields [SF_N][lay][col]: value, d/dtlay, d/dq
+  double* hs;                    // heatfac / (plev(l-1) - plev(l)) [lay][col]
   double* part;                  // band partial gradients [band][seed][entry][col]
 };
 

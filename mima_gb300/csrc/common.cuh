@@ -139,6 +139,7 @@ struct LwWorkT {
   F *f, *planklay, *planklev, *plankbnd, *dplankbnd, *secdiff;
   int* laytrop;
   double *bu, *bd, *bdu;  // band partials [band][lev][col]
+  double* colsum;         // per-layer coldry and wk1 [2][lay][col] for the column sums
 };
 using LwWork = LwWorkT<double>;
 struct SwIn {

@@ -39,9 +39,12 @@ template <class R> __host__ __device__ inline Dual<R> operator-(const Dual<R>& a
 template <class R> __host__ __device__ inline Dual<R> operator*(const Dual<R>& a, const Dual<R>& b) {
   return {a.v * b.v, a.t * b.v + a.v * b.t, a.q * b.v + a.v * b.q};
 }
+// One reciprocal per dual division (the value is a.v * (1 / b.v), within an
+// ulp of a.v / b.v); FP64 divides are sequences on the FP64 pipe.
 template <class R> __host__ __device__ inline Dual<R> operator/(const Dual<R>& a, const Dual<R>& b) {
-  const R r = a.v / b.v;
-  return {r, (a.t - r * b.t) / b.v, (a.q - r * b.q) / b.v};
+  const R inv = (R)1 / b.v;
+  const R r = a.v * inv;
+  return {r, (a.t - r * b.t) * inv, (a.q - r * b.q) * inv};
 }
 template <class R> __host__ __device__ inline Dual<R> operator+(const Dual<R>& a, R b) { return {a.v + b, a.t, a.q}; }
 template <class R> __host__ __device__ inline Dual<R> operator+(R a, const Dual<R>& b) { return {a + b.v, b.t, b.q}; }
@@ -49,10 +52,14 @@ template <class R> __host__ __device__ inline Dual<R> operator-(const Dual<R>& a
 template <class R> __host__ __device__ inline Dual<R> operator-(R a, const Dual<R>& b) { return {a - b.v, -b.t, -b.q}; }
 template <class R> __host__ __device__ inline Dual<R> operator*(const Dual<R>& a, R b) { return {a.v * b, a.t * b, a.q * b}; }
 template <class R> __host__ __device__ inline Dual<R> operator*(R a, const Dual<R>& b) { return {a * b.v, a * b.t, a * b.q}; }
-template <class R> __host__ __device__ inline Dual<R> operator/(const Dual<R>& a, R b) { return {a.v / b, a.t / b, a.q / b}; }
+template <class R> __host__ __device__ inline Dual<R> operator/(const Dual<R>& a, R b) {
+  const R inv = (R)1 / b;
+  return {a.v * inv, a.t * inv, a.q * inv};
+}
 template <class R> __host__ __device__ inline Dual<R> operator/(R a, const Dual<R>& b) {
-  const R r = a / b.v;
-  return {r, -r * b.t / b.v, -r * b.q / b.v};
+  const R inv = (R)1 / b.v;
+  const R r = a * inv;
+  return {r, -r * b.t * inv, -r * b.q * inv};
 }
 template <class R> __host__ __device__ inline bool operator<(const Dual<R>& a, const Dual<R>& b) { return a.v < b.v; }
 template <class R> __host__ __device__ inline bool operator>(const Dual<R>& a, const Dual<R>& b) { return a.v > b.v; }
@@ -69,7 +76,10 @@ template <class R> __device__ inline Dual<R> exp(const Dual<R>& a) {
   const R e = exp(a.v);
   return {e, e * a.t, e * a.q};
 }
-template <class R> __device__ inline Dual<R> log(const Dual<R>& a) { return {log(a.v), a.t / a.v, a.q / a.v}; }
+template <class R> __device__ inline Dual<R> log(const Dual<R>& a) {
+  const R inv = (R)1 / a.v;
+  return {log(a.v), a.t * inv, a.q * inv};
+}
 template <class R> __device__ inline Dual<R> sqrt(const Dual<R>& a) {
   const R s = sqrt(a.v);
   const R h = (R)0.5 / s;

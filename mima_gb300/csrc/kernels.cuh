@@ -105,18 +105,161 @@ constexpr int kGSumFloats = (kBlock / 32) * 2 * 16 * kRow;
 #ifdef RRTMG_DEFINE_COLUMN_KERNELS
 // ---------------------------------------------------------------------------
 // LW prep: inatm (rrtmg_lw_rad.nomcica.f90:572-901) + setcoef
-// (rrtmg_lw_setcoef.f90:31-415) + secdiff (rrtmg_lw_rtrnmr.f90:271-279).
+// (rrtmg_lw_setcoef.f90:31-415) + secdiff (rrtmg_lw_rtrnmr.f90:271-279), in two
+// launches: one thread per (column, layer) for everything that depends on one
+// layer, then one thread per column for the column sums (amttl, wvttl, in
+// layer order as the reference accumulates them), laytrop, the surface and
+// bottom-level Planck terms and secdiff.  Each value is the same expression as
+// in the reference's layer loop.
 // totplnk / totplnkderiv: device tables [(ind-1) + 181*(band-1)].
 // ---------------------------------------------------------------------------
 template <class F>
-__global__ void __launch_bounds__(128) lw_prep_kernel(LwIn in, LwWorkT<F> w, const double* __restrict__ totplnk,
-                                                      const double* __restrict__ totplnkderiv, int ncol, int nlay,
-                                                      int idrv, unsigned* __restrict__ flags) {
+__global__ void __launch_bounds__(128) lw_prep_layer_kernel(LwIn in, LwWorkT<F> w, const double* __restrict__ totplnk,
+                                                            int ncol, int nlay, unsigned* __restrict__ flags) {
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= ncol) return;
+  const int l = blockIdx.y + 1;
   const LwConst& C = c_lw;
   const double amd = 28.9660, amw = 18.0160, amdw = 1.607793, amdo = 0.603428;
   const double stpfac = 296. / 1013.;
+  const size_t N = (size_t)ncol;
+  const size_t fstride = (size_t)nlay * N;
+  auto A = [&](const double* p, int ll) { return __ldg(p + (size_t)col + N * (size_t)(ll - 1)); };
+  auto P = [&](int ind, int b) { return __ldg(totplnk + (ind - 1) + 181 * (b - 1)); };
+  (void)amw;
+  unsigned flag = 0;
+  const double pz_prev = A(in.plev, l);
+  const double pavel = A(in.play, l), tavel = A(in.tlay, l);
+  const double pz_l = A(in.plev, l + 1), tz_l = A(in.tlev, l + 1);
+  const double h2o = A(in.h2o, l);
+  if (bad(pavel) || bad(tavel) || bad(pz_l) || bad(tz_l) || bad(h2o) || pavel <= 0. || tavel <= 0. ||
+      h2o < 0. || h2o >= 1. || pz_l < 0.)
+    flag = 1;
+  double wk1 = (h2o / (1. - h2o)) * amdw;
+  double wk2 = A(in.co2, l);
+  double wk3 = A(in.o3, l) * amdo;
+  double wk4 = in.n2o ? A(in.n2o, l) : 0.0;
+  double wk6 = in.ch4 ? A(in.ch4, l) : 0.0;
+  double wk7 = in.o2 ? A(in.o2, l) : 0.0;
+  double amm = (1. - wk1) * amd + wk1 * amw;
+  double coldry = (pz_prev - pz_l) * 1.e3 * C.avogad / (1.e2 * C.grav * amm * (1. + wk1));
+  double summol = 0.0;
+  summol = summol + wk2;
+  summol = summol + wk3;
+  summol = summol + wk4;
+  summol = summol + 0.0;
+  summol = summol + wk6;
+  summol = summol + wk7;
+  double wbrodl = coldry * (1. - summol);
+  wk1 = coldry * wk1;
+  wk2 = coldry * wk2;
+  wk3 = coldry * wk3;
+  wk4 = coldry * wk4;
+  double wk5 = coldry * 0.0;
+  wk6 = coldry * wk6;
+  wk7 = coldry * wk7;
+  // column sums of inatm (amttl, wvttl), formed in layer order by the column kernel
+  w.colsum[(size_t)(l - 1) * N + col] = coldry;
+  w.colsum[fstride + (size_t)(l - 1) * N + col] = wk1;
+  double wx1 = in.ccl4 ? coldry * A(in.ccl4, l) * 1.e-20 : coldry * 0.0 * 1.e-20;
+  double wx2 = in.cfc11 ? coldry * A(in.cfc11, l) * 1.e-20 : coldry * 0.0 * 1.e-20;
+  double wx3 = in.cfc12 ? coldry * A(in.cfc12, l) * 1.e-20 : coldry * 0.0 * 1.e-20;
+  double wx4 = in.cfc22 ? coldry * A(in.cfc22, l) * 1.e-20 : coldry * 0.0 * 1.e-20;
+
+  // Planck functions of the layer and its upper interface
+  const int indlay = clampi((int)(tavel - 159.), 1, 180);
+  const double tlayfrac = tavel - 159. - (double)indlay;
+  const int indlev = clampi((int)(tz_l - 159.), 1, 180);
+  const double tlevfrac = tz_l - 159. - (double)indlev;
+  for (int b = 1; b <= 16; ++b) {
+    double dbdtlev = P(indlev + 1, b) - P(indlev, b);
+    double dbdtlay = P(indlay + 1, b) - P(indlay, b);
+    w.planklay[((size_t)(b - 1) * nlay + (l - 1)) * N + col] = P(indlay, b) + tlayfrac * dbdtlay;
+    w.planklev[((size_t)(b - 1) * (nlay + 1) + l) * N + col] = P(indlev, b) + tlevfrac * dbdtlev;
+  }
+
+  const double plog = log(pavel);
+  const int jp = clampi((int)(36. - 5 * (plog + 0.04)), 1, 58);
+  const int jp1 = jp + 1;
+  const double fp = 5. * (C.preflog[jp - 1] - plog);
+  const int jt = clampi((int)(3. + (tavel - C.tref[jp - 1]) / 15.), 1, 4);
+  const double ft = ((tavel - C.tref[jp - 1]) / 15.) - (double)(jt - 3);
+  const int jt1 = clampi((int)(3. + (tavel - C.tref[jp1 - 1]) / 15.), 1, 4);
+  const double ft1 = ((tavel - C.tref[jp1 - 1]) / 15.) - (double)(jt1 - 3);
+  const double water = wk1 / coldry;
+  const double scalefac = pavel * stpfac / tavel;
+  double forfac, forfrac, selffac, selffrac = 0.0, minorfrac, factor;
+  int indfor, indself = 1, indminor;
+  if (plog > 4.56) {
+    forfac = scalefac / (1. + water);
+    factor = (332.0 - tavel) / 36.0;
+    indfor = min(2, max(1, (int)factor));
+    forfrac = factor - (double)indfor;
+    selffac = water * forfac;
+    factor = (tavel - 188.0) / 7.2;
+    indself = min(9, max(1, (int)factor - 7));
+    selffrac = factor - (double)(indself + 7);
+  } else {
+    forfac = scalefac / (1. + water);
+    factor = (tavel - 188.0) / 36.0;
+    indfor = 3;
+    forfrac = factor - 1.0;
+    selffac = water * forfac;
+  }
+  const double scaleminor = pavel / tavel;
+  const double scaleminorn2 = (pavel / tavel) * (wbrodl / (coldry + wk1));
+  factor = (tavel - 180.8) / 7.2;
+  indminor = min(18, max(1, (int)factor));
+  minorfrac = factor - (double)indminor;
+
+  double colh2o = 1.e-20 * wk1, colco2 = 1.e-20 * wk2, colo3 = 1.e-20 * wk3, coln2o = 1.e-20 * wk4;
+  double colco = 1.e-20 * wk5, colch4 = 1.e-20 * wk6, colo2 = 1.e-20 * wk7;
+  if (colco2 == 0.) colco2 = 1.e-32 * coldry;
+  if (colo3 == 0.) colo3 = 1.e-32 * coldry;
+  if (coln2o == 0.) coln2o = 1.e-32 * coldry;
+  if (colco == 0.) colco = 1.e-32 * coldry;
+  if (colch4 == 0.) colch4 = 1.e-32 * coldry;
+  const double colbrd = 1.e-20 * wbrodl;
+  const double compfp = 1. - fp;
+  const size_t o = (size_t)(l - 1) * N + col;
+  F* f = w.f;
+  f[LF_PAVEL * fstride + o] = pavel;
+  f[LF_COLDRY * fstride + o] = coldry;
+  f[LF_COLH2O * fstride + o] = colh2o;
+  f[LF_COLCO2 * fstride + o] = colco2;
+  f[LF_COLO3 * fstride + o] = colo3;
+  f[LF_COLN2O * fstride + o] = coln2o;
+  f[LF_COLCO * fstride + o] = colco;
+  f[LF_COLCH4 * fstride + o] = colch4;
+  f[LF_COLO2 * fstride + o] = colo2;
+  f[LF_COLBRD * fstride + o] = colbrd;
+  f[LF_FAC10 * fstride + o] = compfp * ft;
+  f[LF_FAC00 * fstride + o] = compfp * (1. - ft);
+  f[LF_FAC11 * fstride + o] = fp * ft1;
+  f[LF_FAC01 * fstride + o] = fp * (1. - ft1);
+  f[LF_SELFFAC * fstride + o] = colh2o * selffac;
+  f[LF_SELFFRAC * fstride + o] = selffrac;
+  f[LF_FORFAC * fstride + o] = colh2o * forfac;
+  f[LF_FORFRAC * fstride + o] = forfrac;
+  f[LF_MINORFRAC * fstride + o] = minorfrac;
+  f[LF_SCALEMINOR * fstride + o] = scaleminor;
+  f[LF_SCALEMINORN2 * fstride + o] = scaleminorn2;
+  f[LF_WX1 * fstride + o] = wx1;
+  f[LF_WX2 * fstride + o] = wx2;
+  f[LF_WX3 * fstride + o] = wx3;
+  f[LF_WX4 * fstride + o] = wx4;
+  w.idx[o] = pack_idx(jp, jt, jt1, indself, indfor, indminor);
+  if (flag) atomicOr(flags, 1u);
+}
+
+template <class F>
+__global__ void __launch_bounds__(128) lw_prep_column_kernel(LwIn in, LwWorkT<F> w, const double* __restrict__ totplnk,
+                                                             const double* __restrict__ totplnkderiv, int ncol,
+                                                             int nlay, int idrv, unsigned* __restrict__ flags) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncol) return;
+  const LwConst& C = c_lw;
+  const double amd = 28.9660, amw = 18.0160;
   const size_t N = (size_t)ncol;
   const size_t fstride = (size_t)nlay * N;
   auto A = [&](const double* p, int l) { return __ldg(p + (size_t)col + N * (size_t)(l - 1)); };
@@ -125,10 +268,9 @@ __global__ void __launch_bounds__(128) lw_prep_kernel(LwIn in, LwWorkT<F> w, con
   unsigned flag = 0;
 
   const double tbound = __ldg(in.tsfc + col);
-  double pz_prev = A(in.plev, 1);
-  const double pz0 = pz_prev;
+  const double pz0 = A(in.plev, 1);
   const double tz0 = A(in.tlev, 1);
-  if (bad(tbound) || bad(pz_prev) || bad(tz0) || tbound <= 0. || tz0 <= 0.) flag = 1;
+  if (bad(tbound) || bad(pz0) || bad(tz0) || tbound <= 0. || tz0 <= 0.) flag = 1;
   const int indbound = clampi((int)(tbound - 159.), 1, 180);
   const double tbndfrac = tbound - 159. - (double)indbound;
   const int indlev0 = clampi((int)(tz0 - 159.), 1, 180);
@@ -144,131 +286,14 @@ __global__ void __launch_bounds__(128) lw_prep_kernel(LwIn in, LwWorkT<F> w, con
       w.dplankbnd[(b - 1) * N + col] = semiss * (PD(indbound, b) + tbndfrac * dbdtlev);
     }
   }
-
   double amttl = 0.0, wvttl = 0.0;
   int laytrop = 0;
   for (int l = 1; l <= nlay; ++l) {
-    const double pavel = A(in.play, l), tavel = A(in.tlay, l);
-    const double pz_l = A(in.plev, l + 1), tz_l = A(in.tlev, l + 1);
-    const double h2o = A(in.h2o, l);
-    if (bad(pavel) || bad(tavel) || bad(pz_l) || bad(tz_l) || bad(h2o) || pavel <= 0. || tavel <= 0. ||
-        h2o < 0. || h2o >= 1. || pz_l < 0.)
-      flag = 1;
-    double wk1 = (h2o / (1. - h2o)) * amdw;
-    double wk2 = A(in.co2, l);
-    double wk3 = A(in.o3, l) * amdo;
-    double wk4 = in.n2o ? A(in.n2o, l) : 0.0;
-    double wk6 = in.ch4 ? A(in.ch4, l) : 0.0;
-    double wk7 = in.o2 ? A(in.o2, l) : 0.0;
-    double amm = (1. - wk1) * amd + wk1 * amw;
-    double coldry = (pz_prev - pz_l) * 1.e3 * C.avogad / (1.e2 * C.grav * amm * (1. + wk1));
-    double summol = 0.0;
-    summol = summol + wk2;
-    summol = summol + wk3;
-    summol = summol + wk4;
-    summol = summol + 0.0;
-    summol = summol + wk6;
-    summol = summol + wk7;
-    double wbrodl = coldry * (1. - summol);
-    wk1 = coldry * wk1;
-    wk2 = coldry * wk2;
-    wk3 = coldry * wk3;
-    wk4 = coldry * wk4;
-    double wk5 = coldry * 0.0;
-    wk6 = coldry * wk6;
-    wk7 = coldry * wk7;
+    const double coldry = w.colsum[(size_t)(l - 1) * N + col];
+    const double wk1 = w.colsum[fstride + (size_t)(l - 1) * N + col];
     amttl = amttl + coldry + wk1;
     wvttl = wvttl + wk1;
-    double wx1 = in.ccl4 ? coldry * A(in.ccl4, l) * 1.e-20 : coldry * 0.0 * 1.e-20;
-    double wx2 = in.cfc11 ? coldry * A(in.cfc11, l) * 1.e-20 : coldry * 0.0 * 1.e-20;
-    double wx3 = in.cfc12 ? coldry * A(in.cfc12, l) * 1.e-20 : coldry * 0.0 * 1.e-20;
-    double wx4 = in.cfc22 ? coldry * A(in.cfc22, l) * 1.e-20 : coldry * 0.0 * 1.e-20;
-
-    // Planck functions of the layer and its upper interface
-    const int indlay = clampi((int)(tavel - 159.), 1, 180);
-    const double tlayfrac = tavel - 159. - (double)indlay;
-    const int indlev = clampi((int)(tz_l - 159.), 1, 180);
-    const double tlevfrac = tz_l - 159. - (double)indlev;
-    for (int b = 1; b <= 16; ++b) {
-      double dbdtlev = P(indlev + 1, b) - P(indlev, b);
-      double dbdtlay = P(indlay + 1, b) - P(indlay, b);
-      w.planklay[((size_t)(b - 1) * nlay + (l - 1)) * N + col] = P(indlay, b) + tlayfrac * dbdtlay;
-      w.planklev[((size_t)(b - 1) * (nlay + 1) + l) * N + col] = P(indlev, b) + tlevfrac * dbdtlev;
-    }
-
-    const double plog = log(pavel);
-    const int jp = clampi((int)(36. - 5 * (plog + 0.04)), 1, 58);
-    const int jp1 = jp + 1;
-    const double fp = 5. * (C.preflog[jp - 1] - plog);
-    const int jt = clampi((int)(3. + (tavel - C.tref[jp - 1]) / 15.), 1, 4);
-    const double ft = ((tavel - C.tref[jp - 1]) / 15.) - (double)(jt - 3);
-    const int jt1 = clampi((int)(3. + (tavel - C.tref[jp1 - 1]) / 15.), 1, 4);
-    const double ft1 = ((tavel - C.tref[jp1 - 1]) / 15.) - (double)(jt1 - 3);
-    const double water = wk1 / coldry;
-    const double scalefac = pavel * stpfac / tavel;
-    double forfac, forfrac, selffac, selffrac = 0.0, minorfrac, factor;
-    int indfor, indself = 1, indminor;
-    if (plog > 4.56) {
-      laytrop = laytrop + 1;
-      forfac = scalefac / (1. + water);
-      factor = (332.0 - tavel) / 36.0;
-      indfor = min(2, max(1, (int)factor));
-      forfrac = factor - (double)indfor;
-      selffac = water * forfac;
-      factor = (tavel - 188.0) / 7.2;
-      indself = min(9, max(1, (int)factor - 7));
-      selffrac = factor - (double)(indself + 7);
-    } else {
-      forfac = scalefac / (1. + water);
-      factor = (tavel - 188.0) / 36.0;
-      indfor = 3;
-      forfrac = factor - 1.0;
-      selffac = water * forfac;
-    }
-    const double scaleminor = pavel / tavel;
-    const double scaleminorn2 = (pavel / tavel) * (wbrodl / (coldry + wk1));
-    factor = (tavel - 180.8) / 7.2;
-    indminor = min(18, max(1, (int)factor));
-    minorfrac = factor - (double)indminor;
-
-    double colh2o = 1.e-20 * wk1, colco2 = 1.e-20 * wk2, colo3 = 1.e-20 * wk3, coln2o = 1.e-20 * wk4;
-    double colco = 1.e-20 * wk5, colch4 = 1.e-20 * wk6, colo2 = 1.e-20 * wk7;
-    if (colco2 == 0.) colco2 = 1.e-32 * coldry;
-    if (colo3 == 0.) colo3 = 1.e-32 * coldry;
-    if (coln2o == 0.) coln2o = 1.e-32 * coldry;
-    if (colco == 0.) colco = 1.e-32 * coldry;
-    if (colch4 == 0.) colch4 = 1.e-32 * coldry;
-    const double colbrd = 1.e-20 * wbrodl;
-    const double compfp = 1. - fp;
-    const size_t o = (size_t)(l - 1) * N + col;
-    F* f = w.f;
-    f[LF_PAVEL * fstride + o] = pavel;
-    f[LF_COLDRY * fstride + o] = coldry;
-    f[LF_COLH2O * fstride + o] = colh2o;
-    f[LF_COLCO2 * fstride + o] = colco2;
-    f[LF_COLO3 * fstride + o] = colo3;
-    f[LF_COLN2O * fstride + o] = coln2o;
-    f[LF_COLCO * fstride + o] = colco;
-    f[LF_COLCH4 * fstride + o] = colch4;
-    f[LF_COLO2 * fstride + o] = colo2;
-    f[LF_COLBRD * fstride + o] = colbrd;
-    f[LF_FAC10 * fstride + o] = compfp * ft;
-    f[LF_FAC00 * fstride + o] = compfp * (1. - ft);
-    f[LF_FAC11 * fstride + o] = fp * ft1;
-    f[LF_FAC01 * fstride + o] = fp * (1. - ft1);
-    f[LF_SELFFAC * fstride + o] = colh2o * selffac;
-    f[LF_SELFFRAC * fstride + o] = selffrac;
-    f[LF_FORFAC * fstride + o] = colh2o * forfac;
-    f[LF_FORFRAC * fstride + o] = forfrac;
-    f[LF_MINORFRAC * fstride + o] = minorfrac;
-    f[LF_SCALEMINOR * fstride + o] = scaleminor;
-    f[LF_SCALEMINORN2 * fstride + o] = scaleminorn2;
-    f[LF_WX1 * fstride + o] = wx1;
-    f[LF_WX2 * fstride + o] = wx2;
-    f[LF_WX3 * fstride + o] = wx3;
-    f[LF_WX4 * fstride + o] = wx4;
-    w.idx[o] = pack_idx(jp, jt, jt1, indself, indfor, indminor);
-    pz_prev = pz_l;
+    if (log(A(in.play, l)) > 4.56) laytrop = laytrop + 1;
   }
   w.laytrop[col] = laytrop;
   const double wvsh = (amw * wvttl) / (amd * amttl);
@@ -493,41 +518,49 @@ __global__ void __launch_bounds__(128) lw_finalize_kernel(const double* __restri
                                                           int idrv, double* uflx, double* dflx, double* hr,
                                                           double* uflxc, double* dflxc, double* hrc,
                                                           double* duflx_dt, double* duflxc_dt) {
+  // one thread per (column, level); the heating of the layer below the level
+  // re-forms the band sums of the level below (same order, same rounding)
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= ncol) return;
+  const int lev = blockIdx.y;
   const LwConst& C = c_lw;
   const size_t N = (size_t)ncol;
   const double wtdiff = 0.5;
-  double fnet_prev = 0.0, pz_prev = 0.0;
-  for (int lev = 0; lev <= nlay; ++lev) {
-    double tu = 0.0, td = 0.0, tdu = 0.0;
+  auto sums = [&](int lv, double& tu, double& td) {
+    tu = 0.0;
+    td = 0.0;
     for (int b = 0; b < kLwBands; ++b) {
-      const size_t o = ((size_t)b * (nlay + 1) + lev) * N + col;
+      const size_t o = ((size_t)b * (nlay + 1) + lv) * N + col;
       tu = tu + (__ldg(bu + o) * wtdiff) * C.band[b].delwave;
       td = td + (__ldg(bd + o) * wtdiff) * C.band[b].delwave;
-      if (idrv == 1) tdu = tdu + (__ldg(bdu + o) * wtdiff) * C.band[b].delwave * C.fluxfac;
     }
     tu = tu * C.fluxfac;
     td = td * C.fluxfac;
-    const size_t oo = (size_t)lev * N + col;
-    uflx[oo] = tu;
-    dflx[oo] = td;
-    uflxc[oo] = tu;
-    dflxc[oo] = td;
-    if (idrv == 1) {
-      if (duflx_dt) duflx_dt[oo] = tdu;
-      if (duflxc_dt) duflxc_dt[oo] = tdu;
+  };
+  double tu, td;
+  sums(lev, tu, td);
+  const size_t oo = (size_t)lev * N + col;
+  uflx[oo] = tu;
+  dflx[oo] = td;
+  uflxc[oo] = tu;
+  dflxc[oo] = td;
+  if (idrv == 1) {
+    double tdu = 0.0;
+    for (int b = 0; b < kLwBands; ++b) {
+      const size_t o = ((size_t)b * (nlay + 1) + lev) * N + col;
+      tdu = tdu + (__ldg(bdu + o) * wtdiff) * C.band[b].delwave * C.fluxfac;
     }
-    const double fnet = tu - td;
-    const double pz = __ldg(plev + oo);
-    if (lev >= 1) {
-      const double h = C.heatfac * (fnet_prev - fnet) / (pz_prev - pz);
-      const size_t oh = (size_t)(lev - 1) * N + col;
-      hr[oh] = h;
-      hrc[oh] = h;
-    }
-    fnet_prev = fnet;
-    pz_prev = pz;
+    if (duflx_dt) duflx_dt[oo] = tdu;
+    if (duflxc_dt) duflxc_dt[oo] = tdu;
+  }
+  if (lev >= 1) {
+    double tu0, td0;
+    sums(lev - 1, tu0, td0);
+    const double fnet_prev = tu0 - td0, fnet = tu - td;
+    const double h = C.heatfac * (fnet_prev - fnet) / (__ldg(plev + oo - N) - __ldg(plev + oo));
+    const size_t oh = (size_t)(lev - 1) * N + col;
+    hr[oh] = h;
+    hrc[oh] = h;
   }
 }
 
@@ -549,103 +582,115 @@ __device__ __forceinline__ int sw_layreffr(int b) {
 __host__ __device__ constexpr bool sw_upper_source(int b) { return b == 16 || b == 17 || b == 27 || b == 28 || b == 29; }
 
 #ifdef RRTMG_DEFINE_COLUMN_KERNELS
+// Two launches as for LW: one thread per (column, layer), then one thread per
+// column for laytrop and the solar-source layer of every band.
 template <class F>
-__global__ void __launch_bounds__(128) sw_prep_kernel(SwIn in, SwWorkT<F> w, int ncol, int nlay,
-                                                      unsigned* __restrict__ flags) {
+__global__ void __launch_bounds__(128) sw_prep_layer_kernel(SwIn in, SwWorkT<F> w, int ncol, int nlay,
+                                                            unsigned* __restrict__ flags) {
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= ncol) return;
+  const int l = blockIdx.y + 1;
   const SwConst& C = c_sw;
   const double amd = 28.9660, amw = 18.0160, amdw = 1.607793, amdo = 0.603428;
   const double stpfac = 296. / 1013.;
   const size_t N = (size_t)ncol;
   const size_t fstride = (size_t)nlay * N;
+  auto A = [&](const double* p, int ll) { return __ldg(p + (size_t)col + N * (size_t)(ll - 1)); };
+  unsigned flag = 0;
+  const double pz_prev = A(in.plev, l);
+  const double pavel = A(in.play, l), tavel = A(in.tlay, l);
+  const double pz_l = A(in.plev, l + 1);
+  const double h2o = A(in.h2o, l);
+  if (bad(pavel) || bad(tavel) || bad(pz_l) || bad(h2o) || pavel <= 0. || tavel <= 0. || h2o < 0. || h2o >= 1. ||
+      pz_l < 0.)
+    flag = 1;
+  double wk1 = (h2o / (1. - h2o)) * amdw;
+  double wk2 = A(in.co2, l);
+  double wk3 = A(in.o3, l) * amdo;
+  double wk4 = in.n2o ? A(in.n2o, l) : 0.0;
+  double wk6 = in.ch4 ? A(in.ch4, l) : 0.0;
+  double wk7 = in.o2 ? A(in.o2, l) : 0.0;
+  double amm = (1. - wk1) * amd + wk1 * amw;
+  double coldry = (pz_prev - pz_l) * 1.e3 * C.avogad / (1.e2 * C.grav * amm * (1. + wk1));
+  wk1 = coldry * wk1;
+  wk2 = coldry * wk2;
+  wk3 = coldry * wk3;
+  wk4 = coldry * wk4;
+  wk6 = coldry * wk6;
+  wk7 = coldry * wk7;
+
+  const double plog = log(pavel);
+  const int jp = clampi((int)(36. - 5 * (plog + 0.04)), 1, 58);
+  const int jp1 = jp + 1;
+  const double fp = 5. * (C.preflog[jp - 1] - plog);
+  const int jt = clampi((int)(3. + (tavel - C.tref[jp - 1]) / 15.), 1, 4);
+  const double ft = ((tavel - C.tref[jp - 1]) / 15.) - (double)(jt - 3);
+  const int jt1 = clampi((int)(3. + (tavel - C.tref[jp1 - 1]) / 15.), 1, 4);
+  const double ft1 = ((tavel - C.tref[jp1 - 1]) / 15.) - (double)(jt1 - 3);
+  const double water = wk1 / coldry;
+  const double scalefac = pavel * stpfac / tavel;
+  double forfac, forfrac, selffac, selffrac, factor;
+  int indfor, indself;
+  const bool lower = plog > 4.56;
+  if (lower) {
+    forfac = scalefac / (1. + water);
+    factor = (332.0 - tavel) / 36.0;
+    indfor = min(2, max(1, (int)factor));
+    forfrac = factor - (double)indfor;
+    selffac = water * forfac;
+    factor = (tavel - 188.0) / 7.2;
+    indself = min(9, max(1, (int)factor - 7));
+    selffrac = factor - (double)(indself + 7);
+  } else {
+    forfac = scalefac / (1. + water);
+    factor = (tavel - 188.0) / 36.0;
+    indfor = 3;
+    forfrac = factor - 1.0;
+    selffac = 0.;
+    selffrac = 0.;
+    indself = 0;
+  }
+  double colh2o = 1.e-20 * wk1, colco2 = 1.e-20 * wk2, colo3 = 1.e-20 * wk3, coln2o = 1.e-20 * wk4;
+  double colch4 = 1.e-20 * wk6, colo2 = 1.e-20 * wk7;
+  const double colmol = 1.e-20 * coldry + colh2o;
+  if (colco2 == 0.) colco2 = 1.e-32 * coldry;
+  if (coln2o == 0.) coln2o = 1.e-32 * coldry;
+  if (colch4 == 0.) colch4 = 1.e-32 * coldry;
+  if (colo2 == 0.) colo2 = 1.e-32 * coldry;
+  const double compfp = 1. - fp;
+  const size_t o = (size_t)(l - 1) * N + col;
+  F* f = w.f;
+  f[SF_COLH2O * fstride + o] = colh2o;
+  f[SF_COLCO2 * fstride + o] = colco2;
+  f[SF_COLO3 * fstride + o] = colo3;
+  f[SF_COLCH4 * fstride + o] = colch4;
+  f[SF_COLO2 * fstride + o] = colo2;
+  f[SF_COLMOL * fstride + o] = colmol;
+  f[SF_FAC10 * fstride + o] = compfp * ft;
+  f[SF_FAC00 * fstride + o] = compfp * (1. - ft);
+  f[SF_FAC11 * fstride + o] = fp * ft1;
+  f[SF_FAC01 * fstride + o] = fp * (1. - ft1);
+  f[SF_SELFFAC * fstride + o] = selffac;
+  f[SF_SELFFRAC * fstride + o] = selffrac;
+  f[SF_FORFAC * fstride + o] = forfac;
+  f[SF_FORFRAC * fstride + o] = forfrac;
+  w.idx[o] = pack_idx(jp, jt, jt1, indself, indfor, 1);
+
+  if (flag) atomicOr(flags, 1u);
+}
+
+template <class F>
+__global__ void __launch_bounds__(128) sw_prep_column_kernel(SwIn in, SwWorkT<F> w, int ncol, int nlay,
+                                                             unsigned* __restrict__ flags) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncol) return;
+  const size_t N = (size_t)ncol;
   auto A = [&](const double* p, int l) { return __ldg(p + (size_t)col + N * (size_t)(l - 1)); };
   unsigned flag = 0;
-  double pz_prev = A(in.plev, 1);
-  int laytrop = 0;
   if (bad(__ldg(in.coszen + col))) flag = 1;
-  for (int l = 1; l <= nlay; ++l) {
-    const double pavel = A(in.play, l), tavel = A(in.tlay, l);
-    const double pz_l = A(in.plev, l + 1);
-    const double h2o = A(in.h2o, l);
-    if (bad(pavel) || bad(tavel) || bad(pz_l) || bad(h2o) || pavel <= 0. || tavel <= 0. || h2o < 0. || h2o >= 1. ||
-        pz_l < 0.)
-      flag = 1;
-    double wk1 = (h2o / (1. - h2o)) * amdw;
-    double wk2 = A(in.co2, l);
-    double wk3 = A(in.o3, l) * amdo;
-    double wk4 = in.n2o ? A(in.n2o, l) : 0.0;
-    double wk6 = in.ch4 ? A(in.ch4, l) : 0.0;
-    double wk7 = in.o2 ? A(in.o2, l) : 0.0;
-    double amm = (1. - wk1) * amd + wk1 * amw;
-    double coldry = (pz_prev - pz_l) * 1.e3 * C.avogad / (1.e2 * C.grav * amm * (1. + wk1));
-    wk1 = coldry * wk1;
-    wk2 = coldry * wk2;
-    wk3 = coldry * wk3;
-    wk4 = coldry * wk4;
-    wk6 = coldry * wk6;
-    wk7 = coldry * wk7;
-
-    const double plog = log(pavel);
-    const int jp = clampi((int)(36. - 5 * (plog + 0.04)), 1, 58);
-    const int jp1 = jp + 1;
-    const double fp = 5. * (C.preflog[jp - 1] - plog);
-    const int jt = clampi((int)(3. + (tavel - C.tref[jp - 1]) / 15.), 1, 4);
-    const double ft = ((tavel - C.tref[jp - 1]) / 15.) - (double)(jt - 3);
-    const int jt1 = clampi((int)(3. + (tavel - C.tref[jp1 - 1]) / 15.), 1, 4);
-    const double ft1 = ((tavel - C.tref[jp1 - 1]) / 15.) - (double)(jt1 - 3);
-    const double water = wk1 / coldry;
-    const double scalefac = pavel * stpfac / tavel;
-    double forfac, forfrac, selffac, selffrac, factor;
-    int indfor, indself;
-    const bool lower = plog > 4.56;
-    if (lower) {
-      laytrop = laytrop + 1;
-      forfac = scalefac / (1. + water);
-      factor = (332.0 - tavel) / 36.0;
-      indfor = min(2, max(1, (int)factor));
-      forfrac = factor - (double)indfor;
-      selffac = water * forfac;
-      factor = (tavel - 188.0) / 7.2;
-      indself = min(9, max(1, (int)factor - 7));
-      selffrac = factor - (double)(indself + 7);
-    } else {
-      forfac = scalefac / (1. + water);
-      factor = (tavel - 188.0) / 36.0;
-      indfor = 3;
-      forfrac = factor - 1.0;
-      selffac = 0.;
-      selffrac = 0.;
-      indself = 0;
-    }
-    double colh2o = 1.e-20 * wk1, colco2 = 1.e-20 * wk2, colo3 = 1.e-20 * wk3, coln2o = 1.e-20 * wk4;
-    double colch4 = 1.e-20 * wk6, colo2 = 1.e-20 * wk7;
-    const double colmol = 1.e-20 * coldry + colh2o;
-    if (colco2 == 0.) colco2 = 1.e-32 * coldry;
-    if (coln2o == 0.) coln2o = 1.e-32 * coldry;
-    if (colch4 == 0.) colch4 = 1.e-32 * coldry;
-    if (colo2 == 0.) colo2 = 1.e-32 * coldry;
-    const double compfp = 1. - fp;
-    const size_t o = (size_t)(l - 1) * N + col;
-    F* f = w.f;
-    f[SF_COLH2O * fstride + o] = colh2o;
-    f[SF_COLCO2 * fstride + o] = colco2;
-    f[SF_COLO3 * fstride + o] = colo3;
-    f[SF_COLCH4 * fstride + o] = colch4;
-    f[SF_COLO2 * fstride + o] = colo2;
-    f[SF_COLMOL * fstride + o] = colmol;
-    f[SF_FAC10 * fstride + o] = compfp * ft;
-    f[SF_FAC00 * fstride + o] = compfp * (1. - ft);
-    f[SF_FAC11 * fstride + o] = fp * ft1;
-    f[SF_FAC01 * fstride + o] = fp * (1. - ft1);
-    f[SF_SELFFAC * fstride + o] = selffac;
-    f[SF_SELFFRAC * fstride + o] = selffrac;
-    f[SF_FORFAC * fstride + o] = forfac;
-    f[SF_FORFRAC * fstride + o] = forfrac;
-    w.idx[o] = pack_idx(jp, jt, jt1, indself, indfor, 1);
-
-    pz_prev = pz_l;
-  }
+  int laytrop = 0;
+  for (int l = 1; l <= nlay; ++l)
+    if (log(A(in.play, l)) > 4.56) laytrop = laytrop + 1;
   w.laytrop[col] = laytrop;
   // Solar-source layer of every band, as the taumol16..29 loops select it:
   //   upper-loop bands (16, 17, 27, 28, 29): laysolfr = nlay, replaced by the
@@ -1035,37 +1080,41 @@ __global__ void __launch_bounds__(128) sw_finalize_kernel(const double* __restri
                                                           const double* __restrict__ coszen, int ncol, int nlay,
                                                           double* swuflx, double* swdflx, double* swhr,
                                                           double* swuflxc, double* swdflxc, double* swhrc) {
+  // one thread per (column, level), as the LW finalize
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= ncol) return;
+  const int k = blockIdx.y;
   const size_t N = (size_t)ncol;
   const bool lit = __ldg(coszen + col) >= 1.e-10;
-  double nprev = 0.0;
-  for (int k = 0; k <= nlay; ++k) {
-    double fu = 0.0, fd = 0.0;
-    if (lit) {
-      for (int b = 0; b < kSwBands; ++b) {
-        const size_t o = ((size_t)b * (nlay + 1) + k) * N + col;
-        fu = fu + __ldg(su + o);
-        fd = fd + __ldg(sd + o);
-      }
+  auto sums = [&](int lv, double& fu, double& fd) {
+    fu = 0.0;
+    fd = 0.0;
+    if (!lit) return;
+    for (int b = 0; b < kSwBands; ++b) {
+      const size_t o = ((size_t)b * (nlay + 1) + lv) * N + col;
+      fu = fu + __ldg(su + o);
+      fd = fd + __ldg(sd + o);
     }
-    const size_t oo = (size_t)k * N + col;
-    swuflx[oo] = fu;
-    swdflx[oo] = fd;
-    swuflxc[oo] = fu;
-    swdflxc[oo] = fd;
-    const double net = fd - fu;
-    if (k >= 1) {
-      const size_t oh = (size_t)(k - 1) * N + col;
-      double h = 0.0;
-      if (lit && k < nlay) {
-        const double zdpgcp = c_sw.heatfac / (__ldg(plev + (size_t)(k - 1) * N + col) - __ldg(plev + oo));
-        h = (net - nprev) * zdpgcp;
-      }
-      swhr[oh] = h;
-      swhrc[oh] = h;
+  };
+  double fu, fd;
+  sums(k, fu, fd);
+  const size_t oo = (size_t)k * N + col;
+  swuflx[oo] = fu;
+  swdflx[oo] = fd;
+  swuflxc[oo] = fu;
+  swdflxc[oo] = fd;
+  if (k >= 1) {
+    const size_t oh = (size_t)(k - 1) * N + col;
+    double h = 0.0;
+    if (lit && k < nlay) {
+      double fu0, fd0;
+      sums(k - 1, fu0, fd0);
+      const double net = fd - fu, nprev = fd0 - fu0;
+      const double zdpgcp = c_sw.heatfac / (__ldg(plev + oo - N) - __ldg(plev + oo));
+      h = (net - nprev) * zdpgcp;
     }
-    nprev = net;
+    swhr[oh] = h;
+    swhrc[oh] = h;
   }
 }
 

@@ -27,12 +27,18 @@ int sw_gpoint_blocks(const SwConst& c, int ncol) {
 
 void launch_lw_prep(const LwIn& in, const LwWork& w, const double* totplnk, const double* totplnkderiv, int ncol,
                     int nlay, int idrv, unsigned* flags, cudaStream_t s) {
-  lw_prep_kernel<double><<<(ncol + 127) / 128, 128, 0, s>>>(in, w, totplnk, totplnkderiv, ncol, nlay, idrv, flags);
+  const dim3 g((ncol + 127) / 128, nlay);
+  lw_prep_layer_kernel<double><<<g, 128, 0, s>>>(in, w, totplnk, ncol, nlay, flags);
+  lw_prep_column_kernel<double><<<(ncol + 127) / 128, 128, 0, s>>>(in, w, totplnk, totplnkderiv, ncol, nlay, idrv,
+                                                                  flags);
 }
 
 void launch_lw_prep_split(const LwIn& in, const LwWorkT<float>& w, const double* totplnk, const double* totplnkderiv,
                           int ncol, int nlay, int idrv, unsigned* flags, cudaStream_t s) {
-  lw_prep_kernel<float><<<(ncol + 127) / 128, 128, 0, s>>>(in, w, totplnk, totplnkderiv, ncol, nlay, idrv, flags);
+  const dim3 g((ncol + 127) / 128, nlay);
+  lw_prep_layer_kernel<float><<<g, 128, 0, s>>>(in, w, totplnk, ncol, nlay, flags);
+  lw_prep_column_kernel<float><<<(ncol + 127) / 128, 128, 0, s>>>(in, w, totplnk, totplnkderiv, ncol, nlay, idrv,
+                                                                 flags);
 }
 
 void launch_lw_gpoint_fp64(const LwPrep& p, const double* emis, const double* tauaer, const double* tab,
@@ -47,17 +53,19 @@ void launch_lw_gpoint_fp64(const LwPrep& p, const double* emis, const double* ta
 void launch_lw_finalize(const double* bu, const double* bd, const double* bdu, const double* plev, int ncol, int nlay,
                         int idrv, double* uflx, double* dflx, double* hr, double* uflxc, double* dflxc, double* hrc,
                         double* duflx_dt, double* duflxc_dt, cudaStream_t s) {
-  lw_finalize_kernel<<<(ncol + 127) / 128, 128, 0, s>>>(bu, bd, bdu, plev, ncol, nlay, idrv, uflx, dflx, hr, uflxc,
+  lw_finalize_kernel<<<dim3((ncol + 127) / 128, nlay + 1), 128, 0, s>>>(bu, bd, bdu, plev, ncol, nlay, idrv, uflx, dflx, hr, uflxc,
                                                         dflxc, hrc, duflx_dt, duflxc_dt);
 }
 
 void launch_sw_prep(const SwIn& in, const SwWork& w, int ncol, int nlay, unsigned* flags, cudaStream_t s) {
-  sw_prep_kernel<double><<<(ncol + 127) / 128, 128, 0, s>>>(in, w, ncol, nlay, flags);
+  sw_prep_layer_kernel<double><<<dim3((ncol + 127) / 128, nlay), 128, 0, s>>>(in, w, ncol, nlay, flags);
+  sw_prep_column_kernel<double><<<(ncol + 127) / 128, 128, 0, s>>>(in, w, ncol, nlay, flags);
 }
 
 void launch_sw_prep_split(const SwIn& in, const SwWorkT<float>& w, int ncol, int nlay, unsigned* flags,
                           cudaStream_t s) {
-  sw_prep_kernel<float><<<(ncol + 127) / 128, 128, 0, s>>>(in, w, ncol, nlay, flags);
+  sw_prep_layer_kernel<float><<<dim3((ncol + 127) / 128, nlay), 128, 0, s>>>(in, w, ncol, nlay, flags);
+  sw_prep_column_kernel<float><<<(ncol + 127) / 128, 128, 0, s>>>(in, w, ncol, nlay, flags);
 }
 
 void launch_sw_gpoint_fp64(const SwPrep& p, const SwIn& in, double adjflux, int iaer, const double* tab,
@@ -71,7 +79,7 @@ void launch_sw_gpoint_fp64(const SwPrep& p, const SwIn& in, double adjflux, int 
 void launch_sw_finalize(const double* su, const double* sd, const double* plev, const double* coszen, int ncol,
                         int nlay, double* swuflx, double* swdflx, double* swhr, double* swuflxc, double* swdflxc,
                         double* swhrc, cudaStream_t s) {
-  sw_finalize_kernel<<<(ncol + 127) / 128, 128, 0, s>>>(su, sd, plev, coszen, ncol, nlay, swuflx, swdflx, swhr,
+  sw_finalize_kernel<<<dim3((ncol + 127) / 128, nlay + 1), 128, 0, s>>>(su, sd, plev, coszen, ncol, nlay, swuflx, swdflx, swhr,
                                                         swuflxc, swdflxc, swhrc);
 }
 

@@ -186,7 +186,7 @@ def test_launch_count_is_native(gpu):
     before = gpu.launch_count()
     gpu.lw(atm)
     gpu.sw(atm)
-    assert gpu.launch_count() - before == 6
+    assert gpu.launch_count() - before == 8
 
 
 @pytest.mark.gpu

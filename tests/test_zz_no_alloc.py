@@ -61,7 +61,7 @@ def test_static_scratch_entry_point_matches_dev_entry_point(gpu):
 def test_static_scratch_entry_point_rejects_sizes_beyond_the_limit(gpu):
     import torch
     nlay = 40
-    per_col = 4 * nlay + 8 * 25 * nlay + 8 * 16 * nlay + 4 * 8 * 16 * (nlay + 1) + 3 * 8 * 16 + 4
+    per_col = 4 * nlay + 8 * 25 * nlay + 8 * 16 * nlay + 4 * 8 * 16 * (nlay + 1) + 3 * 8 * 16 + 4 + 2 * 8 * nlay
     ncol = R.STATIC_SCRATCH_BYTES // per_col + 64
     atm = A.small_atmosphere(ncol, nlay, seed=43)
     d = R.atm_device_inputs(atm)

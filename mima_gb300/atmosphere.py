@@ -179,7 +179,11 @@ CONFIGS = {
     1: dict(name="T85x40 FP64 via C-ABI + CUDA graph", grid="T85", nlay=40, ts_sigma=2.0, rh_random=False),
     2: dict(name="T170x60 FP32-split", grid="T170", nlay=60, ts_sigma=5.0, rh_random=True),
     3: dict(name="T42x40 adjoint (256 columns)", grid="T42", nlay=40, ts_sigma=2.0, rh_random=False),
-    4: dict(name="1048576x60 stress (32 T170 members)", grid="T170", nlay=60, ts_sigma=3.0, rh_random=False),
+    # 32 members x 32768 columns = 1,048,576 columns; each member has the T170
+    # configuration's column (60 layers, top 0.01 hPa) on the 256 x 128 Gaussian
+    # latitudes, with its own seed and Ts noise 3 K
+    4: dict(name="1048576x60 stress (32 members of 32768 T170-like columns)", grid="T85", nlay=60, ts_sigma=3.0,
+            rh_random=False),
 }
 
 

@@ -1,12 +1,14 @@
 // C-ABI of the GB300 RRTMG path (declared in include/rrtmg_gpu.h).
 //
-// A handle owns: the device coefficient tables (FP64 and FP32 copies), one
-// internal stream for the host-pointer entry points, a device flag word for
-// input validation, and three device workspaces grown on demand: LW scratch,
-// SW scratch (kept separate so an LW and an SW call may run concurrently on
-// different streams) and staging buffers for the host-pointer entry points.
+// A handle owns: the device coefficient tables (FP64 and FP32 copies), two
+// internal streams for the host-pointer entry points (column chunks alternate
+// between them), a device flag word for input validation, and device
+// workspaces grown on demand: LW scratch, SW scratch (kept separate so an LW
+// and an SW call may run concurrently on different streams), the adjoint's,
+// and per-stream staging and scratch for the host-pointer entry points.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -41,7 +43,11 @@ struct rrtmg_gpu_state {
   double *totplnk = nullptr, *totplnkderiv = nullptr;
   float *lw_tab32 = nullptr, *sw_tab32 = nullptr, *lw_exp32 = nullptr, *lw_tfn32 = nullptr, *sw_exp32 = nullptr;
   unsigned* flags = nullptr;
-  DevBuf lw_ws, sw_ws, io, adj_ws;
+  DevBuf lw_ws, sw_ws, adj_ws;
+  // host-pointer calls: a second stream and per-stream staging and scratch, so
+  // that column chunks alternate between the streams
+  cudaStream_t stream2 = nullptr;
+  DevBuf hio[2], hws[2];
   long long launches = 0;
   std::string err;
   // Optional per-kernel timing: events around every launch of the last LW
@@ -229,14 +235,10 @@ double adjflux_of(const rrtmg_gpu_state* h, double adjes, int dyofyr, double sco
   return adjflx * (scon / 1.36822e+03);
 }
 
-int sw_run(rrtmg_gpu_state* h, cudaStream_t s, int ncol, int nlay, int iaer, double adjes, int dyofyr, double scon,
-           const SwIn& in, double* swuflx, double* swdflx, double* swhr, double* swuflxc, double* swdflxc,
-           double* swhrc) {
-  size_t need;
-  carve_sw(nullptr, ncol, nlay, &need);
-  int rc = ensure(h, h->sw_ws, need, s);
-  if (rc) return rc;
-  SwWork w = carve_sw(h->sw_ws.p, ncol, nlay, nullptr);
+int sw_enqueue(rrtmg_gpu_state* h, cudaStream_t s, void* base, int ncol, int nlay, int iaer, double adjes,
+               int dyofyr, double scon, const SwIn& in, double* swuflx, double* swdflx, double* swhr, double* swuflxc,
+               double* swdflxc, double* swhrc) {
+  SwWork w = carve_sw(base, ncol, nlay, nullptr);
   const double adjflux = adjflux_of(h, adjes, dyofyr, scon);
   const int nb = sw_gpoint_blocks(h->host.sw, ncol);
   mark(h, 1, 0, s);
@@ -259,6 +261,106 @@ int sw_run(rrtmg_gpu_state* h, cudaStream_t s, int ncol, int nlay, int iaer, dou
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(h, e, "SW kernel launch");
   return RRTMG_OK;
+}
+
+int sw_run(rrtmg_gpu_state* h, cudaStream_t s, int ncol, int nlay, int iaer, double adjes, int dyofyr, double scon,
+           const SwIn& in, double* swuflx, double* swdflx, double* swhr, double* swuflxc, double* swdflxc,
+           double* swhrc) {
+  size_t need;
+  carve_sw(nullptr, ncol, nlay, &need);
+  int rc = ensure(h, h->sw_ws, need, s);
+  if (rc) return rc;
+  return sw_enqueue(h, s, h->sw_ws.p, ncol, nlay, iaer, adjes, dyofyr, scon, in, swuflx, swdflx, swhr, swuflxc,
+                    swdflxc, swhrc);
+}
+
+// ---------------------------------------------------------------------------
+// Host-pointer calls.  Every caller array is (ncol, rows) with the column
+// index fastest.  The columns are processed in chunks that alternate between
+// the handle's two streams: per chunk, pitched copies of the chunk's columns of
+// every input into contiguous (nc, rows) staging arrays, the kernels, and
+// pitched copies of the outputs back into the caller's arrays, so that the
+// copies of one chunk overlap the kernels of the other.
+// ---------------------------------------------------------------------------
+struct HostIn {
+  const double* p;  // may be null (optional array)
+  size_t rows;
+};
+struct HostOut {
+  double* p;  // may be null (not requested)
+  size_t rows;
+};
+constexpr int kChunkMin = 8192, kMaxChunks = 8;
+
+int read_flags(rrtmg_gpu_state* h, cudaStream_t s);
+
+// True when p is page-locked host memory (allocated or registered with CUDA).
+bool pinned(const void* p) {
+  if (!p) return true;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
+template <class Need, class Enqueue>
+int host_call(rrtmg_gpu_state* h, int ncol, const HostIn* in, int nin, const HostOut* out, int nout, Need&& ws_need,
+              Enqueue&& enqueue, const char* what) {
+  // Chunks only for page-locked arrays: pitched copies of pageable memory are
+  // staged by the driver row by row; pageable arrays move in one piece.
+  bool all_pinned = true;
+  for (int k = 0; k < nin && all_pinned; ++k) all_pinned = pinned(in[k].p);
+  for (int k = 0; k < nout && all_pinned; ++k) all_pinned = pinned(out[k].p);
+  const int nchunk = (all_pinned && ncol >= 2 * kChunkMin) ? std::min(kMaxChunks, ncol / kChunkMin) : 1;
+  int csize = (ncol + nchunk - 1) / nchunk;
+  csize = std::min(ncol, (csize + 31) / 32 * 32);
+  // staging and scratch per stream, sized for the largest chunk
+  size_t stage = 0;
+  for (int k = 0; k < nin; ++k)
+    if (in[k].p) stage += align256((size_t)csize * in[k].rows * sizeof(double));
+  for (int k = 0; k < nout; ++k)
+    if (out[k].p) stage += align256((size_t)csize * out[k].rows * sizeof(double));
+  cudaStream_t st[2] = {h->stream, h->stream2};
+  for (int i = 0; i < 2 && i < nchunk; ++i) {
+    int rc = ensure(h, h->hio[i], stage, nullptr);
+    if (!rc) rc = ensure(h, h->hws[i], ws_need(csize), nullptr);
+    if (rc) return rc;
+  }
+  const size_t pitch = (size_t)ncol * sizeof(double);
+  cudaError_t e = cudaSuccess;
+  const double* din[24];
+  double* dout[12];
+  for (int c = 0; c < nchunk && e == cudaSuccess; ++c) {
+    const int c0 = c * csize;
+    const int nc = std::min(csize, ncol - c0);
+    if (nc <= 0) break;
+    cudaStream_t s = st[c % 2];
+    Carver cv{(char*)h->hio[c % 2].p};
+    const size_t w = (size_t)nc * sizeof(double);
+    for (int k = 0; k < nin; ++k) {
+      din[k] = nullptr;
+      if (!in[k].p) continue;
+      double* d = cv.take<double>((size_t)nc * in[k].rows);
+      if (e == cudaSuccess)
+        e = nchunk == 1 ? cudaMemcpyAsync(d, in[k].p, w * in[k].rows, cudaMemcpyHostToDevice, s)
+                        : cudaMemcpy2DAsync(d, w, in[k].p + c0, pitch, w, in[k].rows, cudaMemcpyHostToDevice, s);
+      din[k] = d;
+    }
+    for (int k = 0; k < nout; ++k) dout[k] = out[k].p ? cv.take<double>((size_t)nc * out[k].rows) : nullptr;
+    if (e != cudaSuccess) break;
+    int rc = enqueue(s, h->hws[c % 2].p, nc, din, dout);
+    if (rc) return rc;
+    for (int k = 0; k < nout && e == cudaSuccess; ++k)
+      if (out[k].p)
+        e = nchunk == 1 ? cudaMemcpyAsync(out[k].p, dout[k], w * out[k].rows, cudaMemcpyDeviceToHost, s)
+                        : cudaMemcpy2DAsync(out[k].p + c0, pitch, dout[k], w, w, out[k].rows, cudaMemcpyDeviceToHost, s);
+  }
+  if (e != cudaSuccess) return cuda_fail(h, e, what);
+  e = cudaStreamSynchronize(h->stream2);
+  if (e != cudaSuccess) return cuda_fail(h, e, "synchronise");
+  return read_flags(h, h->stream);
 }
 
 // Adjoint workspace: dual prep fields and band partial gradients.
@@ -331,20 +433,6 @@ int read_flags(rrtmg_gpu_state* h, cudaStream_t s) {
   return RRTMG_OK;
 }
 
-// Staging of host arrays for the host-pointer entry points.
-struct Stage {
-  rrtmg_gpu_state* h;
-  cudaStream_t s;
-  Carver c;
-  cudaError_t err = cudaSuccess;
-  const double* in(const double* host, size_t n) {
-    if (!host) return nullptr;
-    double* d = c.take<double>(n);
-    if (d && err == cudaSuccess) err = cudaMemcpyAsync(d, host, n * sizeof(double), cudaMemcpyHostToDevice, s);
-    return d;
-  }
-  double* out(size_t n) { return c.take<double>(n); }
-};
 
 }  // namespace
 
@@ -381,6 +469,7 @@ int rrtmg_gpu_init(double cpdair, const char* table_blob, int device, rrtmg_gpu_
   }
   cudaError_t e = cudaSetDevice(device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = upload(&h->lw_tab64, h->host.lw_tab);
   if (e == cudaSuccess) e = upload(&h->sw_tab64, h->host.sw_tab);
   if (e == cudaSuccess) e = upload(&h->lw_exp64, h->host.lw_exp);
@@ -413,12 +502,14 @@ int rrtmg_gpu_finalize(rrtmg_gpu_handle h) {
   if (!h) return RRTMG_ERR_ARG;
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->stream2) cudaStreamSynchronize(h->stream2);
   void* ptrs[] = {h->lw_tab64, h->sw_tab64, h->lw_exp64, h->lw_tfn64, h->sw_exp64, h->totplnk, h->totplnkderiv,
                   h->lw_tab32, h->sw_tab32, h->lw_exp32, h->lw_tfn32, h->sw_exp32, h->flags, h->lw_ws.p,
-                  h->sw_ws.p, h->io.p, h->adj_ws.p};
+                  h->sw_ws.p, h->adj_ws.p, h->hio[0].p, h->hio[1].p, h->hws[0].p, h->hws[1].p};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->stream) cudaStreamDestroy(h->stream);
+  if (h->stream2) cudaStreamDestroy(h->stream2);
   for (auto& fam : h->ev)
     for (auto& e : fam)
       if (e) cudaEventDestroy(e);
@@ -615,41 +706,23 @@ int rrtmg_lw_c(rrtmg_gpu_handle h, int ncol, int nlay, int icld, int idrv, const
     return fail(h, RRTMG_ERR_ARG, "a required array pointer is null");
   if (idrv == 1 && !duflx_dt) return fail(h, RRTMG_ERR_ARG, "idrv = 1 needs duflx_dt");
   cudaSetDevice(h->device);
-  const size_t N = ncol, L = nlay, Lv = nlay + 1;
-  // size the staging area
-  Stage probe{h, h->stream, Carver{nullptr}};
-  auto plan = [&](Stage& st, const double** dp, double** out) {
-    dp[0] = st.in(play, L * N); dp[1] = st.in(plev, Lv * N); dp[2] = st.in(tlay, L * N); dp[3] = st.in(tlev, Lv * N);
-    dp[4] = st.in(tsfc, N); dp[5] = st.in(h2ovmr, L * N); dp[6] = st.in(o3vmr, L * N); dp[7] = st.in(co2vmr, L * N);
-    dp[8] = st.in(ch4vmr, L * N); dp[9] = st.in(n2ovmr, L * N); dp[10] = st.in(o2vmr, L * N);
-    dp[11] = st.in(cfc11vmr, L * N); dp[12] = st.in(cfc12vmr, L * N); dp[13] = st.in(cfc22vmr, L * N);
-    dp[14] = st.in(ccl4vmr, L * N); dp[15] = st.in(emis, 16 * N); dp[16] = st.in(tauaer, 16 * L * N);
-    out[0] = st.out(Lv * N); out[1] = st.out(Lv * N); out[2] = st.out(L * N); out[3] = st.out(Lv * N);
-    out[4] = st.out(Lv * N); out[5] = st.out(L * N);
-    out[6] = idrv == 1 ? st.out(Lv * N) : nullptr;
-    out[7] = idrv == 1 ? st.out(Lv * N) : nullptr;
+  const size_t L = nlay, Lv = nlay + 1;
+  const HostIn in[17] = {{play, L}, {plev, Lv}, {tlay, L}, {tlev, Lv}, {tsfc, 1}, {h2ovmr, L}, {o3vmr, L},
+                         {co2vmr, L}, {ch4vmr, L}, {n2ovmr, L}, {o2vmr, L}, {cfc11vmr, L}, {cfc12vmr, L},
+                         {cfc22vmr, L}, {ccl4vmr, L}, {emis, 16}, {tauaer, 16 * L}};
+  const HostOut out[8] = {{uflx, Lv}, {dflx, Lv}, {hr, L}, {uflxc, Lv}, {dflxc, Lv}, {hrc, L},
+                          {idrv == 1 ? duflx_dt : nullptr, Lv}, {idrv == 1 ? duflxc_dt : nullptr, Lv}};
+  auto need = [&](int nc) {
+    size_t b;
+    carve_lw(nullptr, nc, nlay, &b);
+    return b;
   };
-  const double* dp[17];
-  double* dout[8];
-  plan(probe, dp, dout);
-  rc = ensure(h, h->io, probe.c.off, h->stream);
-  if (rc) return rc;
-  Stage st{h, h->stream, Carver{(char*)h->io.p}};
-  plan(st, dp, dout);
-  if (st.err != cudaSuccess) return cuda_fail(h, st.err, "copy LW inputs");
-  LwIn in{dp[0], dp[1], dp[2], dp[3], dp[4], dp[5], dp[6], dp[7], dp[8], dp[9], dp[10], dp[11], dp[12], dp[13],
-          dp[14], dp[15], dp[16]};
-  rc = lw_run(h, h->stream, ncol, nlay, idrv, in, dout[0], dout[1], dout[2], dout[3], dout[4], dout[5], dout[6],
-              dout[7]);
-  if (rc) return rc;
-  double* hosts[8] = {uflx, dflx, hr, uflxc, dflxc, hrc, duflx_dt, duflxc_dt};
-  const size_t sizes[8] = {Lv * N, Lv * N, L * N, Lv * N, Lv * N, L * N, Lv * N, Lv * N};
-  for (int k = 0; k < 8; ++k) {
-    if (!hosts[k] || !dout[k]) continue;
-    cudaError_t e = cudaMemcpyAsync(hosts[k], dout[k], sizes[k] * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
-    if (e != cudaSuccess) return cuda_fail(h, e, "copy LW outputs");
-  }
-  return read_flags(h, h->stream);
+  auto enq = [&](cudaStream_t s, void* ws, int nc, const double* const* d, double* const* o) {
+    LwIn li{d[0], d[1], d[2], d[3], d[4], d[5], d[6], d[7], d[8], d[9], d[10], d[11], d[12], d[13], d[14], d[15],
+            d[16]};
+    return lw_enqueue(h, s, ws, nc, nlay, idrv, li, o[0], o[1], o[2], o[3], o[4], o[5], o[6], o[7]);
+  };
+  return host_call(h, ncol, in, 17, out, 8, need, enq, "copy LW arrays");
 }
 
 int rrtmg_sw_c(rrtmg_gpu_handle h, int ncol, int nlay, int icld, int iaer, const double* play, const double* plev,
@@ -675,40 +748,24 @@ int rrtmg_sw_c(rrtmg_gpu_handle h, int ncol, int nlay, int icld, int iaer, const
   if (iaer == 10 && (!tauaer || !ssaaer || !asmaer)) return fail(h, RRTMG_ERR_ARG, "iaer = 10 needs tauaer/ssaaer/asmaer");
   if (!(scon > 0.0)) return fail(h, RRTMG_ERR_ARG, "scon must be positive");
   cudaSetDevice(h->device);
-  const size_t N = ncol, L = nlay, Lv = nlay + 1;
+  const size_t L = nlay, Lv = nlay + 1;
   const bool aer = iaer == 10;
-  auto plan = [&](Stage& st, const double** dp, double** out) {
-    dp[0] = st.in(play, L * N); dp[1] = st.in(plev, Lv * N); dp[2] = st.in(tlay, L * N); dp[3] = st.in(tlev, Lv * N);
-    dp[4] = st.in(tsfc, N); dp[5] = st.in(h2ovmr, L * N); dp[6] = st.in(o3vmr, L * N); dp[7] = st.in(co2vmr, L * N);
-    dp[8] = st.in(ch4vmr, L * N); dp[9] = st.in(n2ovmr, L * N); dp[10] = st.in(o2vmr, L * N);
-    dp[11] = st.in(asdir, N); dp[12] = st.in(asdif, N); dp[13] = st.in(aldir, N); dp[14] = st.in(aldif, N);
-    dp[15] = st.in(coszen, N);
-    dp[16] = aer ? st.in(tauaer, 14 * L * N) : nullptr;
-    dp[17] = aer ? st.in(ssaaer, 14 * L * N) : nullptr;
-    dp[18] = aer ? st.in(asmaer, 14 * L * N) : nullptr;
-    for (int k = 0; k < 6; ++k) out[k] = st.out((k == 2 || k == 5) ? L * N : Lv * N);
+  const HostIn in[19] = {{play, L}, {plev, Lv}, {tlay, L}, {tlev, Lv}, {tsfc, 1}, {h2ovmr, L}, {o3vmr, L},
+                         {co2vmr, L}, {ch4vmr, L}, {n2ovmr, L}, {o2vmr, L}, {asdir, 1}, {asdif, 1}, {aldir, 1},
+                         {aldif, 1}, {coszen, 1}, {aer ? tauaer : nullptr, 14 * L}, {aer ? ssaaer : nullptr, 14 * L},
+                         {aer ? asmaer : nullptr, 14 * L}};
+  const HostOut out[6] = {{swuflx, Lv}, {swdflx, Lv}, {swhr, L}, {swuflxc, Lv}, {swdflxc, Lv}, {swhrc, L}};
+  auto need = [&](int nc) {
+    size_t b;
+    carve_sw(nullptr, nc, nlay, &b);
+    return b;
   };
-  const double* dp[19];
-  double* dout[6];
-  Stage probe{h, h->stream, Carver{nullptr}};
-  plan(probe, dp, dout);
-  rc = ensure(h, h->io, probe.c.off, h->stream);
-  if (rc) return rc;
-  Stage st{h, h->stream, Carver{(char*)h->io.p}};
-  plan(st, dp, dout);
-  if (st.err != cudaSuccess) return cuda_fail(h, st.err, "copy SW inputs");
-  SwIn in{dp[0], dp[1], dp[2], dp[3], dp[4], dp[5], dp[6], dp[7], dp[8], dp[9], dp[10], dp[11], dp[12], dp[13], dp[14],
-          dp[15], dp[16], dp[17], dp[18]};
-  rc = sw_run(h, h->stream, ncol, nlay, iaer, adjes, dyofyr, scon, in, dout[0], dout[1], dout[2], dout[3], dout[4],
-              dout[5]);
-  if (rc) return rc;
-  double* hosts[6] = {swuflx, swdflx, swhr, swuflxc, swdflxc, swhrc};
-  for (int k = 0; k < 6; ++k) {
-    const size_t n = (k == 2 || k == 5) ? L * N : Lv * N;
-    cudaError_t e = cudaMemcpyAsync(hosts[k], dout[k], n * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
-    if (e != cudaSuccess) return cuda_fail(h, e, "copy SW outputs");
-  }
-  return read_flags(h, h->stream);
+  auto enq = [&](cudaStream_t s, void* ws, int nc, const double* const* d, double* const* o) {
+    SwIn si{d[0], d[1], d[2], d[3], d[4], d[5], d[6], d[7], d[8], d[9], d[10], d[11], d[12], d[13], d[14], d[15],
+            d[16], d[17], d[18]};
+    return sw_enqueue(h, s, ws, nc, nlay, iaer, adjes, dyofyr, scon, si, o[0], o[1], o[2], o[3], o[4], o[5]);
+  };
+  return host_call(h, ncol, in, 19, out, 6, need, enq, "copy SW arrays");
 }
 
 }  // extern "C"

@@ -96,6 +96,19 @@ def _dptr(t):
     return C.cast(C.c_void_p(int(t.data_ptr())), _dp)
 
 
+def _outputs(given, shapes, ncol):
+    """Output arrays (rows, ncol): the caller's where given (checked), else new."""
+    out = {}
+    for k, rows in shapes.items():
+        a = None if given is None else given.get(k)
+        if a is None:
+            a = np.empty((rows, ncol))
+        elif a.dtype != np.float64 or a.shape != (rows, ncol) or not a.flags["C_CONTIGUOUS"]:
+            raise ValueError(f"output {k} must be a C-contiguous float64 array of shape {(rows, ncol)}")
+        out[k] = a
+    return out
+
+
 class RRTMG:
     """One GPU handle: tables loaded once (rrtmg_lw_ini/rrtmg_sw_ini)."""
 
@@ -143,16 +156,17 @@ class RRTMG:
     # ---------------- host-array drop-ins ----------------
     def rrtmg_lw(self, ncol, nlay, icld, idrv, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr,
                  ch4vmr=None, n2ovmr=None, o2vmr=None, cfc11vmr=None, cfc12vmr=None, cfc22vmr=None,
-                 ccl4vmr=None, emis=None, tauaer=None, check=True):
-        """rrtmg_lw on host arrays; returns uflx, dflx, hr, uflxc, dflxc, hrc (+ duflx_dt, duflxc_dt)."""
+                 ccl4vmr=None, emis=None, tauaer=None, check=True, out=None):
+        """rrtmg_lw on host arrays; returns uflx, dflx, hr, uflxc, dflxc, hrc (+ duflx_dt, duflxc_dt).
+        ``out`` optionally supplies the output arrays (float64, C-contiguous;
+        page-locked arrays let the library overlap copies with kernels)."""
         L, N = nlay, ncol
         ins = [_host(a) for a in (play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr,
                                   cfc11vmr, cfc12vmr, cfc22vmr, ccl4vmr, emis)]
-        out = {k: np.empty((L + 1, N)) for k in ("uflx", "dflx", "uflxc", "dflxc")}
-        out.update({k: np.empty((L, N)) for k in ("hr", "hrc")})
+        shapes = {"uflx": L + 1, "dflx": L + 1, "uflxc": L + 1, "dflxc": L + 1, "hr": L, "hrc": L}
         if idrv == 1:
-            out["duflx_dt"] = np.empty((L + 1, N))
-            out["duflxc_dt"] = np.empty((L + 1, N))
+            shapes.update(duflx_dt=L + 1, duflxc_dt=L + 1)
+        out = _outputs(out, shapes, N)
         ta = _host(tauaer)
         rc = self.lib.rrtmg_lw_c(
             self._h, C.c_int(N), C.c_int(L), C.c_int(icld), C.c_int(idrv), *[_hp(a) for a in ins],
@@ -166,13 +180,13 @@ class RRTMG:
 
     def rrtmg_sw(self, ncol, nlay, icld, iaer, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr,
                  n2ovmr, o2vmr, asdir, asdif, aldir, aldif, coszen, adjes, dyofyr, scon, tauaer=None,
-                 ssaaer=None, asmaer=None, check=True):
+                 ssaaer=None, asmaer=None, check=True, out=None):
         L, N = nlay, ncol
         ins = [_host(a) for a in (play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr,
                                   asdir, asdif, aldir, aldif, coszen)]
         aer = [_host(a) for a in (tauaer, ssaaer, asmaer)]
-        out = {k: np.empty((L + 1, N)) for k in ("swuflx", "swdflx", "swuflxc", "swdflxc")}
-        out.update({k: np.empty((L, N)) for k in ("swhr", "swhrc")})
+        out = _outputs(out, {"swuflx": L + 1, "swdflx": L + 1, "swuflxc": L + 1, "swdflxc": L + 1, "swhr": L,
+                             "swhrc": L}, N)
         rc = self.lib.rrtmg_sw_c(
             self._h, C.c_int(N), C.c_int(L), C.c_int(icld), C.c_int(iaer), *[_hp(a) for a in ins],
             C.c_double(adjes), C.c_int(dyofyr), C.c_double(scon), C.c_int(0), C.c_int(0), C.c_int(0),

@@ -16,6 +16,13 @@ Default arm: the sm_103a path through the C-ABI.
               on the timed workload
   cpu_baseline the FP64 CPU oracle (C++ restatement of the reference) on the
               host cores, bounded sample
+  kernels_ms  CUDA-event duration of each kernel of the split and FP64 steps;
+              the roofline object is for the dominant one
+  adjoint     one vector-Jacobian product against the forward it differentiates
+              (FP64, and FP32/FP64-split), full Jacobians of the 256-column
+              adjoint configuration
+--config 2: T170 x 60 (131072 columns); --config 4: the 1,048,576 x 60 stress
+ensemble (forward, forward + adjoint, memory footprint, subset errors).
 --impl reference: the CPU restatement alone, all host threads, same workload.
 
 L2 (126 MB) is flushed before every timed step by writing a 256 MB buffer on
@@ -54,6 +61,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint cost measurement")
     ap.add_argument("--members", type=int, default=32, help="stress configuration (4): ensemble members")
+    ap.add_argument("--stress-adjoint", default="split", choices=["split", "fp64"],
+                    help="stress configuration (4): precision of the adjoint")
     return ap.parse_args()
 
 
@@ -294,6 +303,11 @@ def measure_adjoint(torch, rrtmg, atmosphere, r, stream, atm, d, olw, osw, flush
                                 atm.scon)
         ms_f = time_calls(torch, stream, flush, fwd, steps, warmup)
         ms_v = time_calls(torch, stream, flush, vjp, steps, warmup)
+        # FP32/FP64-split adjoint against the split forward it pairs with
+        r.set_precision("split")
+        ms_fs = time_calls(torch, stream, flush, fwd, steps, warmup)
+        ms_vs = time_calls(torch, stream, flush, vjp, steps, warmup)
+        r.set_precision("fp64")
         a3 = atmosphere.config_atmosphere(3)
         d3 = rrtmg.atm_device_inputs(a3, dev)
         nx3, ny3 = rrtmg.adjoint_shape(a3.nlay)
@@ -307,19 +321,22 @@ def measure_adjoint(torch, rrtmg, atmosphere, r, stream, atm, d, olw, osw, flush
     return {"precision": "fp64 (analytic transcendentals)", "forward_ms": ms_f, "vjp_ms": ms_v,
             "forward_plus_vjp_over_forward": (ms_f + ms_v) / ms_f,
             "vjp_columns_per_s": atm.ncol / (ms_v * 1e-3),
+            "split": {"forward_ms": ms_fs, "vjp_ms": ms_vs, "forward_plus_vjp_over_forward": (ms_fs + ms_vs) / ms_fs,
+                      "note": "FP32 dual numbers and reverse sweeps, FP64 g-point and band sums; analytic forward"},
             "jacobian": {"workload": f"T42x40 adjoint configuration, {a3.ncol} columns", "ms": ms_j,
                          "forward_ms": ms_f3, "rows": ny3, "inputs": nx3,
                          "forward_plus_jacobian_over_forward": (ms_f3 + ms_j) / ms_f3}}
 
 
 def run_stress(args):
-    """1,048,576 x 60 stress configuration: a seeded ensemble of T170-like
-    members (131072 columns each, Ts noise 3 K), all resident in HBM; one
-    launch sequence runs the FP32-split forward of every member, a second one
-    the forward plus the FP64 adjoint (one vector-Jacobian product per member,
-    analytic transcendentals).  Reports columns/s of both, their cost ratio,
-    the peak device-memory footprint and the FP32-split error against FP64 on
-    a 4096-column subset."""
+    """1,048,576 x 60 stress configuration: a seeded ensemble of 32 members of
+    32768 T170-like columns (60 layers, top 0.01 hPa, Ts noise 3 K), all
+    resident in HBM; one launch sequence runs the FP32-split forward of every
+    member, a second one the forward plus the adjoint (one vector-Jacobian
+    product per member, analytic transcendentals; FP32/FP64-split by default).
+    Reports columns/s of both, their cost ratio, the peak device-memory
+    footprint and the FP32-split errors against FP64 (forward and adjoint) on a
+    4096-column subset."""
     import torch
     from mima_gb300 import atmosphere, rrtmg
     dev = torch.device("cuda", 0)
@@ -345,7 +362,7 @@ def run_stress(args):
         dev_step(r, stream, a, d, olw, osw)
 
     def adjoint(a, d):
-        r.set_precision("fp64")
+        r.set_precision(args.stress_adjoint)
         r.set_transcendentals("analytic")
         r.vjp_dev(stream.cuda_stream, a.ncol, a.nlay, d, cot, grad, a.adjes, a.dyofyr, a.scon)
 
@@ -386,6 +403,19 @@ def run_stress(args):
            "sw_hr_max_kday": float(np.abs(sw32["swhr"] - sw64["swhr"]).max()),
            "olr_max_wm2": float(np.abs(lw32["uflx"][-1] - lw64["uflx"][-1]).max()),
            "sfc_flux_max_wm2": float(max(np.abs(lw32[k][0] - lw64[k][0]).max() for k in ("uflx", "dflx")))}
+    # adjoint: split VJP against FP64 VJP on the same subset and cotangents
+    rng = np.random.default_rng(7)
+    csub = rng.standard_normal((ny, sub.ncol))
+    r.set_transcendentals("analytic")
+    r.set_precision("fp64")
+    g64 = r.vjp(sub, csub)
+    r.set_precision("split")
+    g32 = r.vjp(sub, csub)
+    r.set_transcendentals("table")
+    scale = np.maximum(np.abs(g64), 1e-3 * np.abs(g64).max(axis=1, keepdims=True)) + 1e-300
+    rel = np.abs(g32 - g64) / scale
+    err["vjp_split_vs_fp64_rel_max"] = float(rel.max())
+    err["vjp_split_vs_fp64_rel_p99"] = float(np.quantile(rel, 0.99))
     ncols = n * len(members)
     line = {
         "metric": METRIC, "value": ncols / (times["forward"] * 1e-3), "unit": UNIT, "n_gpus": 1,
@@ -397,7 +427,8 @@ def run_stress(args):
         "stress": {"forward_columns_per_s": ncols / (times["forward"] * 1e-3),
                    "forward_adjoint_columns_per_s": ncols / (times["forward_adjoint"] * 1e-3),
                    "forward_adjoint_over_forward": times["forward_adjoint"] / times["forward"],
-                   "adjoint": "FP64 vector-Jacobian product per member (analytic transcendentals)",
+                   "adjoint": (f"{'FP32/FP64-split' if args.stress_adjoint == 'split' else 'FP64'} "
+                               "vector-Jacobian product per member (analytic transcendentals)"),
                    "peak_device_bytes": int(peak_used), "device_bytes_before": int(total - free0),
                    "error_vs_fp64_4096_subset": err},
         "gpu_launches": 8 * len(members) * 3,

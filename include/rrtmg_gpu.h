@@ -170,8 +170,9 @@ int rrtmg_gpu_sync_status(rrtmg_gpu_handle h, void* stream);
  * with respect to
  *   inputs (nx = 3*nlay + 2): tlay of layers 1..nlay, h2ovmr (specific
  *     humidity) of layers 1..nlay, tlev of levels 0..nlay, tsfc.
- * The differentiated forward is RRTMG_TRANS_ANALYTIC in FP64 (the reference's
- * transmittance tables are piecewise constant in optical depth); no counterpart
+ * The differentiated forward is RRTMG_TRANS_ANALYTIC (the reference's
+ * transmittance tables are piecewise constant in optical depth), in FP64, or
+ * with RRTMG_PREC_SPLIT in FP32 with FP64 g-point and band sums; no counterpart
  * in the reference, which has only the LW surface-temperature derivative
  * (idrv = 1, rrtmg_lw_rtrnmr.f90:628-745).  The reverse sweeps of rtrnmr and
  * spcvrt run per g-point with the layer optics recomputed from checkpointed

@@ -410,9 +410,20 @@ int adj_run(rrtmg_gpu_state* h, cudaStream_t s, int ncol, int nlay, const LwIn& 
   AdjLwWork lw;
   AdjSwWork sw;
   carve_adj(h->adj_ws.p, ncol, nlay, nseed_lw, nseed_sw, &lw, &sw, nullptr);
-  launch_adj_lw(lin, lw, h->totplnk, h->lw_tab64, cot, nseed_lw, ncol, nlay, lw_gpoint_blocks(h->host.lw, ncol), s);
-  launch_adj_sw(sin, sw, adjflux, iaer, h->sw_tab64, cot, nseed_sw, ncol, nlay, sw_gpoint_blocks(h->host.sw, ncol),
-                s);
+  const int nbl = lw_gpoint_blocks(h->host.lw, ncol), nbs = sw_gpoint_blocks(h->host.sw, ncol);
+  if (h->precision == RRTMG_PREC_SPLIT) {
+    // FP32 checkpoints in the same carving (they take half the room)
+    const AdjLwWorkT<float> l32{lw.idx, lw.laytrop, (float*)lw.fv, (float*)lw.ft, (float*)lw.fq, (float*)lw.play_v,
+                                (float*)lw.play_t, (float*)lw.plev_v, (float*)lw.plev_t, (float*)lw.pbnd_v,
+                                (float*)lw.pbnd_t, (float*)lw.secdiff, lw.dsec, lw.hs, lw.part};
+    const AdjSwWorkT<float> s32{sw.idx, sw.laytrop, sw.laysolfr, (float*)sw.fv, (float*)sw.ft, (float*)sw.fq, sw.hs,
+                                sw.part};
+    launch_adj_lw_split(lin, l32, h->totplnk, h->lw_tab32, cot, nseed_lw, ncol, nlay, nbl, s);
+    launch_adj_sw_split(sin, s32, adjflux, iaer, h->sw_tab32, h->sw_tab64, cot, nseed_sw, ncol, nlay, nbs, s);
+  } else {
+    launch_adj_lw(lin, lw, h->totplnk, h->lw_tab64, cot, nseed_lw, ncol, nlay, nbl, s);
+    launch_adj_sw(sin, sw, adjflux, iaer, h->sw_tab64, cot, nseed_sw, ncol, nlay, nbs, s);
+  }
   launch_adj_finalize(lw, sw, lin.plev, sin.coszen, nseed_lw, nseed_sw, ncol, nlay, out, cot != nullptr, s);
   h->launches += 5;
   cudaError_t e = cudaGetLastError();

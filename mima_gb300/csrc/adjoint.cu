@@ -38,7 +38,8 @@ using D2 = Dual<double>;
 // (rrtmg_lw_rtrnmr.f90:271-279) with d secdiff / d q of every layer through
 // the column water vapour pwvcm.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) adj_lw_prep_kernel(LwIn in, AdjLwWork w, const double* __restrict__ totplnk,
+template <class F>
+__global__ void __launch_bounds__(128) adj_lw_prep_kernel(LwIn in, AdjLwWorkT<F> w, const double* __restrict__ totplnk,
                                                           int ncol, int nlay) {
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= ncol) return;
@@ -231,20 +232,20 @@ __global__ void __launch_bounds__(128) adj_lw_prep_kernel(LwIn in, AdjLwWork w, 
 // lane (cs, sl) sums entry sl of column sub-index cs over the band's NG lanes
 // in g order.  Warp-uniform calls only.
 // ---------------------------------------------------------------------------
-template <int W, int NG>
+template <int W, int NG, class TS = double>
 struct GRed {
-  double* buf;  // this warp's [W][kRow]
+  TS* buf;  // this warp's [W][kRow]
   int lane, n, first;
-  __device__ __forceinline__ void put(double v) { buf[n * kRow + lane] = v; }
+  __device__ __forceinline__ void put(TS v) { buf[n * kRow + lane] = v; }
   template <class Store>
   __device__ __forceinline__ void flush(Store&& st) {
     __syncwarp();
     const int sl = lane % W, cs = lane / W;
     if (sl < n) {
-      const double* row = buf + sl * kRow + cs * W;
+      const TS* row = buf + sl * kRow + cs * W;
       double acc = 0.0;
 #pragma unroll
-      for (int g = 0; g < NG; ++g) acc += row[g];
+      for (int g = 0; g < NG; ++g) acc += (double)row[g];
       st(first + sl, cs, acc);
     }
     __syncwarp();
@@ -259,12 +260,13 @@ struct GRed {
 constexpr int kRedDoubles = (kBlock / 32) * 16 * kRow;
 
 // Dual view of the checkpointed setcoef fields of one (layer, column).
+template <class R>
 struct LwDualView {
-  const double *fv, *ft, *fq;
+  const R *fv, *ft, *fq;
   size_t fstride, o;
-  __device__ __forceinline__ D2 operator()(int fld) const {
+  __device__ __forceinline__ Dual<R> operator()(int fld) const {
     const size_t i = (size_t)fld * fstride + o;
-    return D2(__ldg(fv + i), __ldg(ft + i), __ldg(fq + i));
+    return Dual<R>(__ldg(fv + i), __ldg(ft + i), __ldg(fq + i));
   }
 };
 
@@ -284,10 +286,11 @@ struct LwDualView {
 //   dPhi/dsu_l = lamU_l, dPhi/drad0 = lamU_0, then the chain rule through the
 //   layer tangents (tlay, q, secdiff, tlev below / above).
 // ---------------------------------------------------------------------------
-template <int B, int MAXL>
-__device__ __forceinline__ void lw_adj_band(const LwIn& in, const AdjLwWork& w, const double* __restrict__ tab,
+template <int B, class R, int MAXL>
+__device__ __forceinline__ void lw_adj_band(const LwIn& in, const AdjLwWorkT<R>& w, const R* __restrict__ tab,
                                             const double* __restrict__ cot, int nseed, int ncol, int nlay, int blk,
                                             double* sred) {
+  using DR = Dual<R>;
   constexpr int NG = lw_ng(B);
   constexpr int W = pow2ceil(NG);
   constexpr int CPB = kBlock / W;
@@ -299,70 +302,78 @@ __device__ __forceinline__ void lw_adj_band(const LwIn& in, const AdjLwWork& w, 
   const size_t N = (size_t)ncol;
   const size_t fstride = (size_t)nlay * N;
   const int lt = w.laytrop[c];
-  const double secdiff = w.secdiff[(B - 1) * N + c];
-  const double rec_6 = 0.166667;
+  const R secdiff = w.secdiff[(B - 1) * N + c];
+  const R rec_6 = (R)0.166667;
   const int E = 3 * nlay + 3;
 
   // Layer state (index l-1) and level radiances.
-  double atr[MAXL], bbu[MAXL];
-  double tT[MAXL], dT[MAXL], uT[MAXL];  // d(t, sd, su)/dtlay
-  double tQ[MAXL], dQ[MAXL], uQ[MAXL];  // d(t, sd, su)/dq
-  double tS[MAXL], dS[MAXL], uS[MAXL];  // d(t, sd, su)/dsecdiff
-  double dLb[MAXL], uLt[MAXL];          // dsd/dtlev below, dsu/dtlev above
-  double Dl[MAXL + 1], Ul[MAXL + 1], lamU[MAXL + 1];
-  double ck[MAXL];                      // seed cotangents of the layer divergences
+  R atr[MAXL], bbu[MAXL];
+  R tT[MAXL], dT[MAXL], uT[MAXL];  // d(t, sd, su)/dtlay
+  R tQ[MAXL], dQ[MAXL], uQ[MAXL];  // d(t, sd, su)/dq
+  R tS[MAXL], dS[MAXL], uS[MAXL];  // d(t, sd, su)/dsecdiff
+  R dLb[MAXL], uLt[MAXL];          // dsd/dtlev below, dsu/dtlev above
+  R Dl[MAXL + 1], Ul[MAXL + 1], nu[MAXL + 1];
+  R ck[MAXL + 1];                  // seed cotangents of the layer divergences (index k = 1..nlay; ck[0] = 0)
 
   // 1. layer optics with tangents (recomputed from the checkpointed fields) and
   //    the downward recursion
-  double radld = 0.0;
-  Dl[nlay] = 0.0;
-  D2 fr1;
+  R radld = (R)0;
+  Dl[nlay] = (R)0;
+  DR fr1;
   for (int lev = nlay; lev >= 1; --lev) {
     const int k = lev - 1;
     const size_t o = (size_t)k * N + c;
     const Idx ix = unpack_idx(__ldg(w.idx + o));
-    LwDualView L{w.fv, w.ft, w.fq, fstride, o};
-    D2 taug, fracs;
-    lw_gas<B, D2>(c_lw, c_lw, L, ix, lev <= lt, gg, tab, taug, fracs);
-    const double ta = in.tauaer ? __ldg(in.tauaer + c + N * ((size_t)k + (size_t)nlay * (B - 1))) : 0.0;
-    const double taut = taug.v + ta;
-    double od = secdiff * taut, odT = secdiff * taug.t, odQ = secdiff * taug.q, odS = taut;
-    if (od < 0.0) od = odT = odQ = odS = 0.0;
-    double a, a_d, tf, tf_d;
-    if (od <= 0.06) {
-      a = od - 0.5 * od * od;
-      a_d = 1.0 - od;
+    LwDualView<R> L{w.fv, w.ft, w.fq, fstride, o};
+    DR taug, fracs;
+    lw_gas<B, DR>(c_lw, lw_rconst<R>(), L, ix, lev <= lt, gg, tab, taug, fracs);
+    const R ta = in.tauaer ? (R)__ldg(in.tauaer + c + N * ((size_t)k + (size_t)nlay * (B - 1))) : (R)0;
+    const R taut = taug.v + ta;
+    R od = secdiff * taut, odT = secdiff * taug.t, odQ = secdiff * taug.q, odS = taut;
+    if (od < (R)0) od = odT = odQ = odS = (R)0;
+    R a, a_d, tf, tf_d;
+    if (od <= (R)0.06) {
+      a = od - (R)0.5 * od * od;
+      a_d = (R)1 - od;
       tf = rec_6 * od;
       tf_d = rec_6;
     } else {
-      const double e = exp(-od), om = 1.0 - e;
-      const double iod = 1.0 / od, iom = 1.0 / om;
+      const R e = exp(-od), om = (R)1 - e;
       a = om;
       a_d = e;
-      tf = 1.0 - 2.0 * (iod - e * iom);
-      tf_d = 2.0 * (iod * iod) - 2.0 * e * (iom * iom);
+      if (sizeof(R) == 4 && od < (R)1) {
+        // tf = 1 - 2 (1/od - 1/(e^od - 1)) by its Bernoulli series: the closed
+        // form cancels to a few digits in FP32 for small od
+        const R x2 = od * od;
+        tf = od * ((R)(1. / 6) - x2 * ((R)(1. / 360) - x2 * ((R)(1. / 15120) - x2 * (R)(1. / 604800))));
+        tf_d = (R)(1. / 6) - x2 * ((R)(1. / 120) - x2 * ((R)(1. / 3024) - x2 * (R)(1. / 86400)));
+      } else {
+        const R iod = (R)1 / od, iom = (R)1 / om;
+        tf = (R)1 - (R)2 * (iod - e * iom);
+        tf_d = (R)2 * (iod * iod) - (R)2 * e * (iom * iom);
+      }
     }
-    const double plf = fracs.v;
+    const R plf = fracs.v;
     const size_t ol = ((size_t)(B - 1) * nlay + k) * N + c;
-    const double blay = __ldg(w.play_v + ol), blay_t = __ldg(w.play_t + ol);
+    const R blay = __ldg(w.play_v + ol), blay_t = __ldg(w.play_t + ol);
     const size_t ou = ((size_t)(B - 1) * (nlay + 1) + lev) * N + c, od_ = ou - N;
-    const double pup = __ldg(w.plev_v + ou), pup_t = __ldg(w.plev_t + ou);
-    const double pdn = __ldg(w.plev_v + od_), pdn_t = __ldg(w.plev_t + od_);
-    const double dpup = pup - blay, dpdn = pdn - blay;
-    const double bd = plf * (blay + tf * dpdn), bu = plf * (blay + tf * dpup);
+    const R pup = __ldg(w.plev_v + ou), pup_t = __ldg(w.plev_t + ou);
+    const R pdn = __ldg(w.plev_v + od_), pdn_t = __ldg(w.plev_t + od_);
+    const R dpup = pup - blay, dpdn = pdn - blay;
+    const R bd = plf * (blay + tf * dpdn), bu = plf * (blay + tf * dpup);
     atr[k] = a;
     bbu[k] = bu;
-    auto tang = [&](double odx, double dplf, double dbl, double& ot, double& osd, double& osu) {
-      const double da = a_d * odx, dtf = tf_d * odx;
-      const double dbd = dplf * (blay + tf * dpdn) + plf * (dbl + dtf * dpdn - tf * dbl);
-      const double dbu = dplf * (blay + tf * dpup) + plf * (dbl + dtf * dpup - tf * dbl);
+    auto tang = [&](R odx, R dplf, R dbl, R& ot, R& osd, R& osu) {
+      const R da = a_d * odx, dtf = tf_d * odx;
+      const R dbd = dplf * (blay + tf * dpdn) + plf * (dbl + dtf * dpdn - tf * dbl);
+      const R dbu = dplf * (blay + tf * dpup) + plf * (dbl + dtf * dpup - tf * dbl);
       ot = -da;
       osd = da * bd + a * dbd;
       osu = da * bu + a * dbu;
     };
     tang(odT, fracs.t, blay_t, tT[k], dT[k], uT[k]);
-    tang(odQ, fracs.q, 0.0, tQ[k], dQ[k], uQ[k]);
-    tang(odS, 0.0, 0.0, tS[k], dS[k], uS[k]);
+    tang(odQ, fracs.q, (R)0, tQ[k], dQ[k], uQ[k]);
+    tang(odS, (R)0, (R)0, tS[k], dS[k], uS[k]);
     dLb[k] = a * plf * tf * pdn_t;
     uLt[k] = a * plf * tf * pup_t;
     radld = radld + (bd - radld) * a;
@@ -370,47 +381,55 @@ __device__ __forceinline__ void lw_adj_band(const LwIn& in, const AdjLwWork& w, 
     if (lev == 1) fr1 = fracs;
   }
   // 2. upward recursion
-  const double pb = __ldg(w.pbnd_v + (B - 1) * N + c), pb_t = __ldg(w.pbnd_t + (B - 1) * N + c);
-  const double semiss = in.emis ? __ldg(in.emis + c + N * (B - 1)) : 1.0;
-  const double reflect = 1.0 - semiss;
+  const R pb = __ldg(w.pbnd_v + (B - 1) * N + c), pb_t = __ldg(w.pbnd_t + (B - 1) * N + c);
+  const R semiss = in.emis ? (R)__ldg(in.emis + c + N * (B - 1)) : (R)1;
+  const R reflect = (R)1 - semiss;
   Ul[0] = fr1.v * pb + reflect * Dl[0];
   for (int l = 1; l <= nlay; ++l) Ul[l] = Ul[l - 1] + (bbu[l - 1] - Ul[l - 1]) * atr[l - 1];
 
-  // 3. reverse sweeps, one cotangent seed at a time
+  // 3. reverse sweeps, one cotangent seed at a time.  With c_k the cotangent of
+  //    div_k (c_0 = c_{nlay+1} = 0) the adjoints are carried as
+  //      nu_m  = lamU_m + c_m:  nu_nlay = c_olr,
+  //              nu_m = atr_{m+1} c_{m+1} + t_{m+1} nu_{m+1} (+ c_sfc at m = 0);
+  //      rho_m = lamD_m + c_{m+1}: rho_0 = -c_sfc + (1 - emis) lamU_0,
+  //              rho_m = atr_m c_m + t_m rho_{m-1};
+  //    the same recursions as for lamU, lamD without the cancellation of
+  //    c_{m+1} - t_{m+1} c_{m+1} (which costs FP32 its digits for thin layers).
   const int wib = threadIdx.x >> 5;
   const int wcol0 = blk * CPB + (wib * 32) / W;
   for (int s = 0; s < nseed; ++s) {
-    // cotangents of div_1..div_nlay in flux units (ck[k-1]), seed s
+    ck[0] = (R)0;
     for (int kk = 1; kk <= nlay; ++kk) {
       const double hs = __ldg(w.hs + (size_t)(kk - 1) * N + c);
-      ck[kk - 1] = cot ? __ldg(cot + (size_t)(kk - 1) * N + c) * hs : (s == kk - 1 ? hs : 0.0);
+      ck[kk] = (R)(cot ? __ldg(cot + (size_t)(kk - 1) * N + c) * hs : (s == kk - 1 ? hs : 0.0));
     }
-    auto cdiv = [&](int kk) -> double { return (kk < 1 || kk > nlay) ? 0.0 : ck[kk - 1]; };
-    const double colr = cot ? __ldg(cot + (size_t)nlay * N + c) : (s == nlay ? 1.0 : 0.0);
-    const double csfc = cot ? __ldg(cot + (size_t)(nlay + 1) * N + c) : (s == nlay + 1 ? 1.0 : 0.0);
-    auto aU = [&](int m) { return cdiv(m + 1) - cdiv(m) + (m == nlay ? colr : 0.0) + (m == 0 ? csfc : 0.0); };
-    auto aD = [&](int m) { return -cdiv(m + 1) + cdiv(m) - (m == 0 ? csfc : 0.0); };
-    lamU[nlay] = aU(nlay);
-    for (int m = nlay - 1; m >= 0; --m) lamU[m] = aU(m) + (1.0 - atr[m]) * lamU[m + 1];
-    GRed<W, NG> red{sred + wib * W * kRow, (int)(threadIdx.x & 31), 0, 0};
+    const R colr = (R)(cot ? __ldg(cot + (size_t)nlay * N + c) : (s == nlay ? 1.0 : 0.0));
+    const R csfc = (R)(cot ? __ldg(cot + (size_t)(nlay + 1) * N + c) : (s == nlay + 1 ? 1.0 : 0.0));
+    nu[nlay] = colr;
+    for (int m = nlay - 1; m >= 0; --m)
+      nu[m] = atr[m] * ck[m + 1] + ((R)1 - atr[m]) * nu[m + 1] + (m == 0 ? csfc : (R)0);
+    GRed<W, NG, R> red{(R*)sred + wib * W * kRow, (int)(threadIdx.x & 31), 0, 0};
     auto store = [&](int e, int cs, double v) {
       const int cc = wcol0 + cs;
       if (cc < ncol) w.part[(((size_t)(B - 1) * nseed + s) * E + e) * N + cc] = v;
     };
-    double lamD = aD(0) + reflect * lamU[0];
-    double gS = 0.0, accLev = 0.0;
+    const R lamU0 = nu[0] - ck[0];
+    R rho = -csfc + reflect * lamU0;  // rho_0
+    R gS = (R)0, accLev = (R)0;
     for (int l = 1; l <= nlay; ++l) {
       const int k = l - 1;
-      const double gt = lamU[l] * Ul[l - 1] + lamD * Dl[l];
-      const double gsd = lamD, gsu = lamU[l];
-      double gT = gt * tT[k] + gsd * dT[k] + gsu * uT[k];
-      double gQ = gt * tQ[k] + gsd * dQ[k] + gsu * uQ[k];
+      const R lamU = nu[l] - ck[l];
+      const R lamD = rho - ck[l];  // lamD_{l-1} = rho_{l-1} - c_l
+      const R gt = lamU * Ul[l - 1] + lamD * Dl[l];
+      const R gsd = lamD, gsu = lamU;
+      R gT = gt * tT[k] + gsd * dT[k] + gsu * uT[k];
+      R gQ = gt * tQ[k] + gsd * dQ[k] + gsu * uQ[k];
       if (l == 1) {
-        gT += lamU[0] * fr1.t * pb;
-        gQ += lamU[0] * fr1.q * pb;
+        gT += lamU0 * fr1.t * pb;
+        gQ += lamU0 * fr1.q * pb;
       }
       gS += gt * tS[k] + gsd * dS[k] + gsu * uS[k];
-      const double gLev = accLev + gsd * dLb[k];
+      const R gLev = accLev + gsd * dLb[k];
       accLev = gsu * uLt[k];
       red.put(gT);
       red.next(store);
@@ -418,11 +437,11 @@ __device__ __forceinline__ void lw_adj_band(const LwIn& in, const AdjLwWork& w, 
       red.next(store);
       red.put(gLev);
       red.next(store);
-      lamD = aD(l) + (1.0 - atr[k]) * lamD;
+      rho = atr[k] * ck[l] + ((R)1 - atr[k]) * rho;  // rho_l
     }
     red.put(accLev);
     red.next(store);
-    red.put(lamU[0] * fr1.v * pb_t);
+    red.put(lamU0 * fr1.v * pb_t);
     red.next(store);
     red.put(gS);
     red.next(store);
@@ -430,8 +449,15 @@ __device__ __forceinline__ void lw_adj_band(const LwIn& in, const AdjLwWork& w, 
   }
 }
 
-template <int MAXL>
-__global__ void __launch_bounds__(kBlock) lw_adj_kernel(LwIn in, AdjLwWork w, const double* __restrict__ tab,
+// Minimum resident blocks per SM asked of the register allocator for the
+// FP32/FP64-split adjoint kernels (a VJP at 32768 columns x 40 layers on
+// GB300: 42.8 ms at 1, 28.8 ms at 8 and 10, 33.2 ms at 12); the FP64 ones: 1.
+#ifndef RRTMG_SPLIT_ADJ_MINB
+#define RRTMG_SPLIT_ADJ_MINB 8
+#endif
+
+template <class R, int MAXL>
+__global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_ADJ_MINB : 1) lw_adj_kernel(LwIn in, AdjLwWorkT<R> w, const R* __restrict__ tab,
                                                         const double* __restrict__ cot, int nseed, int ncol,
                                                         int nlay) {
   __shared__ double sred[kRedDoubles];
@@ -442,7 +468,7 @@ __global__ void __launch_bounds__(kBlock) lw_adj_kernel(LwIn in, AdjLwWork w, co
     blk -= nb;
   }
 #define RRTMG_LW_ADJ_CASE(b) \
-  case b - 1: lw_adj_band<b, MAXL>(in, w, tab, cot, nseed, ncol, nlay, blk, sred); break;
+  case b - 1: lw_adj_band<b, R, MAXL>(in, w, tab, cot, nseed, ncol, nlay, blk, sred); break;
   switch (band) {
     RRTMG_LW_ADJ_CASE(1) RRTMG_LW_ADJ_CASE(2) RRTMG_LW_ADJ_CASE(3) RRTMG_LW_ADJ_CASE(4) RRTMG_LW_ADJ_CASE(5)
     RRTMG_LW_ADJ_CASE(6) RRTMG_LW_ADJ_CASE(7) RRTMG_LW_ADJ_CASE(8) RRTMG_LW_ADJ_CASE(9) RRTMG_LW_ADJ_CASE(10)
@@ -458,7 +484,8 @@ __global__ void __launch_bounds__(kBlock) lw_adj_kernel(LwIn in, AdjLwWork w, co
 // rrtmg_sw_setcoef.f90:30-286) per layer with tangents d/dtlay and d/dq of the
 // same layer, and the solar-source layer of every band (as the forward prep).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) adj_sw_prep_kernel(SwIn in, AdjSwWork w, int ncol, int nlay) {
+template <class F>
+__global__ void __launch_bounds__(128) adj_sw_prep_kernel(SwIn in, AdjSwWorkT<F> w, int ncol, int nlay) {
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= ncol) return;
   const SwConst& C = c_sw;
@@ -571,12 +598,13 @@ __global__ void __launch_bounds__(128) adj_sw_prep_kernel(SwIn in, AdjSwWork w, 
   }
 }
 
+template <class R>
 struct SwDualView {
-  const double *fv, *ft, *fq;
+  const R *fv, *ft, *fq;
   size_t fstride, o;
-  __device__ __forceinline__ D2 operator()(int fld) const {
+  __device__ __forceinline__ Dual<R> operator()(int fld) const {
     const size_t i = (size_t)fld * fstride + o;
-    return D2(__ldg(fv + i), __ldg(ft + i), __ldg(fq + i));
+    return Dual<R>(__ldg(fv + i), __ldg(ft + i), __ldg(fq + i));
   }
 };
 
@@ -597,10 +625,12 @@ struct SwDualView {
 // (tb, tn, rn) upward from the surface, collecting d Phi / d(R, Rd, T, Td, Tx)
 // of every layer, then contracts them with the layer tangents.
 // ---------------------------------------------------------------------------
-template <int B, int MAXL>
-__device__ __forceinline__ void sw_adj_band(const SwIn& in, const AdjSwWork& w, double adjflux, int iaer,
-                                            const double* __restrict__ tab, const double* __restrict__ cot,
-                                            int nseed, int ncol, int nlay, int blk, double* sred) {
+template <int B, class R, int MAXL>
+__device__ __forceinline__ void sw_adj_band(const SwIn& in, const AdjSwWorkT<R>& w, double adjflux, int iaer,
+                                            const R* __restrict__ tab, const double* __restrict__ tab64,
+                                            const double* __restrict__ cot, int nseed, int ncol, int nlay, int blk,
+                                            double* sred) {
+  using DR = Dual<R>;
   constexpr int NG = sw_ng(B);
   constexpr int W = pow2ceil(NG);
   constexpr int CPB = kBlock / W;
@@ -614,88 +644,90 @@ __device__ __forceinline__ void sw_adj_band(const SwIn& in, const AdjSwWork& w, 
   const size_t fstride = (size_t)nlay * N;
   const double coszen = __ldg(in.coszen + c);
   const bool lit = coszen >= 1.e-10;
-  const double prmu0 = lit ? coszen : 1.0;
-  const double bpade = c_sw.bpade;
+  const R prmu0 = (R)(lit ? coszen : 1.0);
+  const R bpade = (R)c_sw.bpade;
   const int lt = w.laytrop[c];
   const int klev = nlay;
   const int E = 2 * nlay;
 
-  D2 zinc(0.0);
+  DR zinc((R)0);
   const int ls = w.laysolfr[(size_t)(B - 16) * N + c];
   if (ls >= 1) {
-    SwDualView L{w.fv, w.ft, w.fq, fstride, (size_t)(ls - 1) * N + c};
-    const D2 sfz = sw_sfluxzen<B>(c_sw, L, ls <= lt, gg, tab);
-    zinc = (adjflux * sfz) * (lit ? coszen : 1.0);
+    SwDualView<R> L{w.fv, w.ft, w.fq, fstride, (size_t)(ls - 1) * N + c};
+    const DR sfz = sw_sfluxzen<B>(c_sw, L, ls <= lt, gg, tab64);
+    zinc = ((R)adjflux * sfz) * (R)(lit ? coszen : 1.0);
   }
-  const double albdir = __ldg(((ibm >= 10 && ibm <= 13) ? in.asdir : in.aldir) + c);
-  const double albdif = __ldg(((ibm >= 10 && ibm <= 13) ? in.asdif : in.aldif) + c);
+  const R albdir = (R)__ldg(((ibm >= 10 && ibm <= 13) ? in.asdir : in.aldir) + c);
+  const R albdif = (R)__ldg(((ibm >= 10 && ibm <= 13) ? in.asdif : in.aldif) + c);
 
   // layer properties (value, d/dtlay, d/dq) and level states, top-down index
-  double Rv[MAXL], Rt[MAXL], Rq[MAXL], Dv[MAXL], Dt[MAXL], Dq[MAXL], Tv[MAXL], Tt[MAXL], Tq[MAXL];
-  double Sv[MAXL], St[MAXL], Sq[MAXL], Xv[MAXL], Xt[MAXL], Xq[MAXL];
-  double tb[MAXL + 1], tn[MAXL + 1], rn[MAXL + 1], pu[MAXL + 1], pd[MAXL + 1];
-  double zf[MAXL + 1], dn[MAXL + 1];  // 1/(1 - rn pd) and fd - fu per level
-  double zu[MAXL], zd[MAXL];          // reciprocals of the upward / downward recursions per layer
-  double gR[MAXL], gD[MAXL], gT[MAXL], gS[MAXL], gX[MAXL];
-  double an[MAXL + 1];                // seed cotangents of net flux per bottom-up level
-  double lb[MAXL + 1], ln[MAXL + 1], lr[MAXL + 1];  // local cotangents of tb, tn, rn per level
+  R Rv[MAXL], Rt[MAXL], Rq[MAXL], Dv[MAXL], Dt[MAXL], Dq[MAXL], Tv[MAXL], Tt[MAXL], Tq[MAXL];
+  R Sv[MAXL], St[MAXL], Sq[MAXL], Xv[MAXL], Xt[MAXL], Xq[MAXL];
+  R tb[MAXL + 1], tn[MAXL + 1], rn[MAXL + 1], pu[MAXL + 1], pd[MAXL + 1];
+  R zf[MAXL + 1], dn[MAXL + 1];  // 1/(1 - rn pd) and fd - fu per level
+  R zu[MAXL], zd[MAXL];          // reciprocals of the upward / downward recursions per layer
+  R gR[MAXL], gD[MAXL], gT[MAXL], gS[MAXL], gX[MAXL];
+  R an[MAXL + 1];                // seed cotangents of net flux per bottom-up level
+  R lb[MAXL + 1], ln[MAXL + 1], lr[MAXL + 1];  // local cotangents of tb, tn, rn per level
   for (int j = 0; j < klev; ++j) {
     const int ikl = klev - j;
     const size_t o = (size_t)(ikl - 1) * N + c;
     const Idx ix = unpack_idx(__ldg(w.idx + o));
-    SwDualView L{w.fv, w.ft, w.fq, fstride, o};
-    D2 taug, taur;
-    sw_gas<B, D2>(c_sw, L, ix, ikl <= lt, gg, tab, taug, taur);
-    D2 ztauc, zomcc, zgcc;
+    SwDualView<R> L{w.fv, w.ft, w.fq, fstride, o};
+    DR taug, taur;
+    sw_gas<B, DR>(c_sw, L, ix, ikl <= lt, gg, tab, taug, taur);
+    DR ztauc, zomcc, zgcc;
     if (iaer == 10) {
       const size_t oa = c + N * ((size_t)(ikl - 1) + (size_t)nlay * (ibm - 1));
-      const double taua = __ldg(in.tauaer + oa);
-      const double omga = __ldg(in.ssaaer + oa);
-      const double asya = __ldg(in.asmaer + oa);
+      const R taua = (R)__ldg(in.tauaer + oa);
+      const R omga = (R)__ldg(in.ssaaer + oa);
+      const R asya = (R)__ldg(in.asmaer + oa);
       ztauc = taur + taug + taua;
-      zomcc = taur * 1.0 + taua * omga;
+      zomcc = taur * (R)1 + taua * omga;
       zgcc = (asya * omga * taua) / zomcc;
       zomcc = zomcc / ztauc;
-      const D2 zf = zgcc * zgcc;
-      const D2 zwf = zomcc * zf;
-      ztauc = (1.0 - zwf) * ztauc;
-      zomcc = (zomcc - zwf) / (1.0 - zwf);
-      zgcc = (zgcc - zf) / (1.0 - zf);
+      const DR zf = zgcc * zgcc;
+      const DR zwf = zomcc * zf;
+      ztauc = ((R)1 - zwf) * ztauc;
+      zomcc = (zomcc - zwf) / ((R)1 - zwf);
+      zgcc = (zgcc - zf) / ((R)1 - zf);
     } else {
       // without aerosol the delta scaling is the identity (asymmetry 0)
       ztauc = taur + taug;
       zomcc = taur / ztauc;
-      zgcc = D2(0.0);
+      zgcc = DR((R)0);
     }
-    D2 rf, rfd, tr, trd;
-    reftra1<D2, double>(ztauc, zomcc, zgcc, D2(prmu0), D2(bpade), (const double*)nullptr, true, rf, rfd, tr, trd);
-    const D2 tx = sw_exp_tbl<D2, double>(ztauc / prmu0, D2(bpade), (const double*)nullptr, true);
+    // the delta-Eddington solution in its cancellation-free form (the same
+    // function as reftra_sw, fewer divisions), in FP64 or FP32
+    DR rf, rfd, tr, trd;
+    reftra_split(ztauc, zomcc, zgcc, DR(prmu0), DR(bpade), (const float*)nullptr, true, rf, rfd, tr, trd, iaer != 10);
+    const DR tx = sw_exp_tbl<DR, R>(ztauc / prmu0, DR(bpade), (const R*)nullptr, true);
     Rv[j] = rf.v; Rt[j] = rf.t; Rq[j] = rf.q;
     Dv[j] = rfd.v; Dt[j] = rfd.t; Dq[j] = rfd.q;
     Tv[j] = tr.v; Tt[j] = tr.t; Tq[j] = tr.q;
     Sv[j] = trd.v; St[j] = trd.t; Sq[j] = trd.q;
     Xv[j] = tx.v; Xt[j] = tx.t; Xq[j] = tx.q;
   }
-  tb[0] = 1.0; tn[0] = 1.0; rn[0] = 0.0;
+  tb[0] = (R)1.0; tn[0] = (R)1.0; rn[0] = (R)0.0;
   for (int j = 0; j < klev; ++j) {
     tb[j + 1] = Xv[j] * tb[j];
-    const double z = 1.0 / (1.0 - Dv[j] * rn[j]);
+    const R z = (R)1.0 / ((R)1.0 - Dv[j] * rn[j]);
     zd[j] = z;
     tn[j + 1] = tb[j] * Tv[j] + Sv[j] * ((tn[j] - tb[j]) + tb[j] * Rv[j] * rn[j]) * z;
     rn[j + 1] = Dv[j] + Sv[j] * Sv[j] * rn[j] * z;
   }
   pu[klev] = albdir; pd[klev] = albdif;
   for (int j = klev - 1; j >= 0; --j) {
-    const double z = 1.0 / (1.0 - pd[j + 1] * Dv[j]);
+    const R z = (R)1.0 / ((R)1.0 - pd[j + 1] * Dv[j]);
     zu[j] = z;
     pu[j] = Rv[j] + Sv[j] * ((Tv[j] - Xv[j]) * pd[j + 1] + Xv[j] * pu[j + 1]) * z;
     pd[j] = Dv[j] + Sv[j] * Sv[j] * pd[j + 1] * z;
   }
   for (int j = 0; j <= klev; ++j) {
-    const double z = 1.0 / (1.0 - rn[j] * pd[j]);
+    const R z = (R)1.0 / ((R)1.0 - rn[j] * pd[j]);
     zf[j] = z;
-    const double fu = (tb[j] * pu[j] + (tn[j] - tb[j]) * pd[j]) * z;
-    const double fd = tb[j] + (tn[j] - tb[j] + tb[j] * pu[j] * rn[j]) * z;
+    const R fu = (tb[j] * pu[j] + (tn[j] - tb[j]) * pd[j]) * z;
+    const R fd = tb[j] + (tn[j] - tb[j] + tb[j] * pu[j] * rn[j]) * z;
     dn[j] = fd - fu;
   }
 
@@ -703,7 +735,6 @@ __device__ __forceinline__ void sw_adj_band(const SwIn& in, const AdjSwWork& w, 
   const int wcol0 = blk * CPB + (wib * 32) / W;
   const double gate = lit ? 1.0 : 0.0;  // dark columns have zero SW outputs
   for (int s = 0; s < nseed; ++s) {
-    // cotangent of net at bottom-up level m
     // cotangent of net at every bottom-up level m (an[m]); layers 1..nlay-1 carry
     // heating cotangents (the top layer's rate is 0)
     const double csfc = cot ? __ldg(cot + (size_t)(2 * nlay + 2) * N + c) : (s == nlay ? 1.0 : 0.0);
@@ -715,84 +746,84 @@ __device__ __forceinline__ void sw_adj_band(const SwIn& in, const AdjSwWork& w, 
         const double hs = __ldg(w.hs + (size_t)(kk - 1) * N + c);
         cnext = cot ? __ldg(cot + (size_t)(nlay + 2 + kk - 1) * N + c) * hs : (s == kk - 1 ? hs : 0.0);
       }
-      an[m] = gate * (cprev - cnext + (m == 0 ? csfc : 0.0));
+      an[m] = (R)(gate * (cprev - cnext + (m == 0 ? csfc : 0.0)));
       cprev = cnext;
     }
     auto anet = [&](int m) { return an[m]; };
     // local cotangents of the level states at top-down level j from the fluxes there
-    auto local = [&](int j, double& ltb, double& ltn, double& lrn, double& lpu, double& lpd) {
-      const double a = zinc.v * anet(klev - j);
-      const double z = zf[j];
-      const double Af = tb[j] * pu[j] + (tn[j] - tb[j]) * pd[j];
-      const double Bf = tn[j] - tb[j] + tb[j] * pu[j] * rn[j];
+    auto local = [&](int j, R& ltb, R& ltn, R& lrn, R& lpu, R& lpd) {
+      const R a = zinc.v * anet(klev - j);
+      const R z = zf[j];
+      const R Af = tb[j] * pu[j] + (tn[j] - tb[j]) * pd[j];
+      const R Bf = tn[j] - tb[j] + tb[j] * pu[j] * rn[j];
       // fu = Af z (cotangent -a), fd = tb + Bf z (cotangent a)
-      ltb = -a * (pu[j] - pd[j]) * z + a * (1.0 + (-1.0 + pu[j] * rn[j]) * z);
+      ltb = -a * (pu[j] - pd[j]) * z + a * ((R)1.0 + (-(R)1.0 + pu[j] * rn[j]) * z);
       ltn = -a * pd[j] * z + a * z;
       lpu = -a * tb[j] * z + a * tb[j] * rn[j] * z;
       lpd = -a * ((tn[j] - tb[j]) * z + Af * z * z * rn[j]) + a * Bf * z * z * rn[j];
       lrn = -a * Af * z * z * pd[j] + a * (tb[j] * pu[j] * z + Bf * z * z * pd[j]);
     };
-    double lzinc = 0.0;
+    R lzinc = (R)0.0;
     for (int j = 0; j <= klev; ++j) lzinc += anet(klev - j) * dn[j];
-    for (int j = 0; j < klev; ++j) gR[j] = gD[j] = gT[j] = gS[j] = gX[j] = 0.0;
+    for (int j = 0; j < klev; ++j) gR[j] = gD[j] = gT[j] = gS[j] = gX[j] = (R)0.0;
     // reverse of the upward sweep, carried from the top down; the local
     // cotangents of (tb, tn, rn) are kept for the second sweep
-    double Lu = 0.0, Ld = 0.0;
+    R Lu = (R)0.0, Ld = (R)0.0;
     {
-      double lpu, lpd;
+      R lpu, lpd;
       local(klev, lb[klev], ln[klev], lr[klev], lpu, lpd);
     }
     for (int j = 0; j < klev; ++j) {
-      double lpu, lpd;
+      R lpu, lpd;
       local(j, lb[j], ln[j], lr[j], lpu, lpd);
       Lu += lpu;
       Ld += lpd;
-      const double z = zu[j];
-      const double Xx = (Tv[j] - Xv[j]) * pd[j + 1] + Xv[j] * pu[j + 1];
-      const double Td = Sv[j];
+      const R z = zu[j];
+      const R Xx = (Tv[j] - Xv[j]) * pd[j + 1] + Xv[j] * pu[j + 1];
+      const R Td = Sv[j];
       gR[j] += Lu;
-      gS[j] += Lu * Xx * z + Ld * 2.0 * Td * pd[j + 1] * z;
+      gS[j] += Lu * Xx * z + Ld * (R)2.0 * Td * pd[j + 1] * z;
       gT[j] += Lu * Td * pd[j + 1] * z;
       gX[j] += Lu * Td * (pu[j + 1] - pd[j + 1]) * z;
-      gD[j] += Ld * (1.0 + Td * Td * pd[j + 1] * z * z * pd[j + 1]) + Lu * Td * Xx * z * z * pd[j + 1];
-      const double nLu = Lu * Td * Xv[j] * z;
-      const double nLd = Lu * (Td * (Tv[j] - Xv[j]) * z + Td * Xx * z * z * Dv[j]) +
+      gD[j] += Ld * ((R)1.0 + Td * Td * pd[j + 1] * z * z * pd[j + 1]) + Lu * Td * Xx * z * z * pd[j + 1];
+      const R nLu = Lu * Td * Xv[j] * z;
+      const R nLd = Lu * (Td * (Tv[j] - Xv[j]) * z + Td * Xx * z * z * Dv[j]) +
                          Ld * (Td * Td * z + Td * Td * pd[j + 1] * z * z * Dv[j]);
       Lu = nLu;
       Ld = nLd;
     }
     // reverse of the downward sweep, carried from the surface up
-    double Lb = 0.0, Ln = 0.0, Lr = 0.0;
+    R Lb = (R)0.0, Ln = (R)0.0, Lr = (R)0.0;
     for (int j = klev; j >= 1; --j) {
       Lb += lb[j];
       Ln += ln[j];
       Lr += lr[j];
       const int q = j - 1;
-      const double z = zd[q];
-      const double Y = (tn[q] - tb[q]) + tb[q] * Rv[q] * rn[q];
-      const double Td = Sv[q];
+      const R z = zd[q];
+      const R Y = (tn[q] - tb[q]) + tb[q] * Rv[q] * rn[q];
+      const R Td = Sv[q];
       gX[q] += Lb * tb[q];
       gT[q] += Ln * tb[q];
-      gS[q] += Ln * Y * z + Lr * 2.0 * Td * rn[q] * z;
+      gS[q] += Ln * Y * z + Lr * (R)2.0 * Td * rn[q] * z;
       gR[q] += Ln * Td * tb[q] * rn[q] * z;
-      gD[q] += Ln * Td * Y * z * z * rn[q] + Lr * (1.0 + Td * Td * rn[q] * z * z * rn[q]);
-      const double nLb = Lb * Xv[q] + Ln * (Tv[q] + Td * (-1.0 + Rv[q] * rn[q]) * z);
-      const double nLn = Ln * Td * z;
-      const double nLr = Ln * (Td * tb[q] * Rv[q] * z + Td * Y * z * z * Dv[q]) +
+      gD[q] += Ln * Td * Y * z * z * rn[q] + Lr * ((R)1.0 + Td * Td * rn[q] * z * z * rn[q]);
+      const R nLb = Lb * Xv[q] + Ln * (Tv[q] + Td * (-(R)1.0 + Rv[q] * rn[q]) * z);
+      const R nLn = Ln * Td * z;
+      const R nLr = Ln * (Td * tb[q] * Rv[q] * z + Td * Y * z * z * Dv[q]) +
                          Lr * (Td * Td * z + Td * Td * rn[q] * z * z * Dv[q]);
       Lb = nLb;
       Ln = nLn;
       Lr = nLr;
     }
-    GRed<W, NG> red{sred + wib * W * kRow, (int)(threadIdx.x & 31), 0, 0};
+    GRed<W, NG, R> red{(R*)sred + wib * W * kRow, (int)(threadIdx.x & 31), 0, 0};
     auto store = [&](int e, int cs, double v) {
       const int cc = wcol0 + cs;
       if (cc < ncol) w.part[(((size_t)(B - 16) * nseed + s) * E + e) * N + cc] = v;
     };
     for (int l = 1; l <= nlay; ++l) {
       const int j = klev - l;
-      double gt = gR[j] * Rt[j] + gD[j] * Dt[j] + gT[j] * Tt[j] + gS[j] * St[j] + gX[j] * Xt[j];
-      double gq = gR[j] * Rq[j] + gD[j] * Dq[j] + gT[j] * Tq[j] + gS[j] * Sq[j] + gX[j] * Xq[j];
+      R gt = gR[j] * Rt[j] + gD[j] * Dt[j] + gT[j] * Tt[j] + gS[j] * St[j] + gX[j] * Xt[j];
+      R gq = gR[j] * Rq[j] + gD[j] * Dq[j] + gT[j] * Tq[j] + gS[j] * Sq[j] + gX[j] * Xq[j];
       if (l == ls) {
         gt += lzinc * zinc.t;
         gq += lzinc * zinc.q;
@@ -806,9 +837,9 @@ __device__ __forceinline__ void sw_adj_band(const SwIn& in, const AdjSwWork& w, 
   }
 }
 
-template <int MAXL>
-__global__ void __launch_bounds__(kBlock) sw_adj_kernel(SwIn in, AdjSwWork w, double adjflux, int iaer,
-                                                        const double* __restrict__ tab,
+template <class R, int MAXL>
+__global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_ADJ_MINB : 1) sw_adj_kernel(SwIn in, AdjSwWorkT<R> w, double adjflux, int iaer,
+                                                        const R* __restrict__ tab, const double* __restrict__ tab64,
                                                         const double* __restrict__ cot, int nseed, int ncol,
                                                         int nlay) {
   __shared__ double sred[kRedDoubles];
@@ -819,7 +850,7 @@ __global__ void __launch_bounds__(kBlock) sw_adj_kernel(SwIn in, AdjSwWork w, do
     blk -= nb;
   }
 #define RRTMG_SW_ADJ_CASE(b) \
-  case b - 16: sw_adj_band<b, MAXL>(in, w, adjflux, iaer, tab, cot, nseed, ncol, nlay, blk, sred); break;
+  case b - 16: sw_adj_band<b, R, MAXL>(in, w, adjflux, iaer, tab, tab64, cot, nseed, ncol, nlay, blk, sred); break;
   switch (band) {
     RRTMG_SW_ADJ_CASE(16) RRTMG_SW_ADJ_CASE(17) RRTMG_SW_ADJ_CASE(18) RRTMG_SW_ADJ_CASE(19) RRTMG_SW_ADJ_CASE(20)
     RRTMG_SW_ADJ_CASE(21) RRTMG_SW_ADJ_CASE(22) RRTMG_SW_ADJ_CASE(23) RRTMG_SW_ADJ_CASE(24) RRTMG_SW_ADJ_CASE(25)
@@ -884,25 +915,47 @@ __global__ void __launch_bounds__(128) adj_finalize_kernel(AdjLwWork lw, AdjSwWo
 cudaError_t upload_constants_adjoint(const LwConst& lw, const SwConst& sw) {
   cudaError_t e = cudaMemcpyToSymbol(c_lw, &lw, sizeof(LwConst));
   if (e != cudaSuccess) return e;
+  const LwConstF f = make_lwconstf(lw);
+  e = cudaMemcpyToSymbol(c_lwf, &f, sizeof(LwConstF));
+  if (e != cudaSuccess) return e;
   return cudaMemcpyToSymbol(c_sw, &sw, sizeof(SwConst));
 }
 
 void launch_adj_lw(const LwIn& in, const AdjLwWork& w, const double* totplnk, const double* tab,
                    const double* cot, int nseed, int ncol, int nlay, int nb, cudaStream_t s) {
-  adj_lw_prep_kernel<<<(ncol + 127) / 128, 128, 0, s>>>(in, w, totplnk, ncol, nlay);
+  adj_lw_prep_kernel<double><<<(ncol + 127) / 128, 128, 0, s>>>(in, w, totplnk, ncol, nlay);
   if (maxl_for(nlay) == 64)
-    lw_adj_kernel<64><<<nb, kBlock, 0, s>>>(in, w, tab, cot, nseed, ncol, nlay);
+    lw_adj_kernel<double, 64><<<nb, kBlock, 0, s>>>(in, w, tab, cot, nseed, ncol, nlay);
   else
-    lw_adj_kernel<208><<<nb, kBlock, 0, s>>>(in, w, tab, cot, nseed, ncol, nlay);
+    lw_adj_kernel<double, 208><<<nb, kBlock, 0, s>>>(in, w, tab, cot, nseed, ncol, nlay);
+}
+
+void launch_adj_lw_split(const LwIn& in, const AdjLwWorkT<float>& w, const double* totplnk, const float* tab,
+                         const double* cot, int nseed, int ncol, int nlay, int nb, cudaStream_t s) {
+  adj_lw_prep_kernel<float><<<(ncol + 127) / 128, 128, 0, s>>>(in, w, totplnk, ncol, nlay);
+  if (maxl_for(nlay) == 64)
+    lw_adj_kernel<float, 64><<<nb, kBlock, 0, s>>>(in, w, tab, cot, nseed, ncol, nlay);
+  else
+    lw_adj_kernel<float, 208><<<nb, kBlock, 0, s>>>(in, w, tab, cot, nseed, ncol, nlay);
 }
 
 void launch_adj_sw(const SwIn& in, const AdjSwWork& w, double adjflux, int iaer, const double* tab,
                    const double* cot, int nseed, int ncol, int nlay, int nb, cudaStream_t s) {
-  adj_sw_prep_kernel<<<(ncol + 127) / 128, 128, 0, s>>>(in, w, ncol, nlay);
+  adj_sw_prep_kernel<double><<<(ncol + 127) / 128, 128, 0, s>>>(in, w, ncol, nlay);
   if (maxl_for(nlay) == 64)
-    sw_adj_kernel<64><<<nb, kBlock, 0, s>>>(in, w, adjflux, iaer, tab, cot, nseed, ncol, nlay);
+    sw_adj_kernel<double, 64><<<nb, kBlock, 0, s>>>(in, w, adjflux, iaer, tab, tab, cot, nseed, ncol, nlay);
   else
-    sw_adj_kernel<208><<<nb, kBlock, 0, s>>>(in, w, adjflux, iaer, tab, cot, nseed, ncol, nlay);
+    sw_adj_kernel<double, 208><<<nb, kBlock, 0, s>>>(in, w, adjflux, iaer, tab, tab, cot, nseed, ncol, nlay);
+}
+
+void launch_adj_sw_split(const SwIn& in, const AdjSwWorkT<float>& w, double adjflux, int iaer, const float* tab,
+                         const double* tab64, const double* cot, int nseed, int ncol, int nlay, int nb,
+                         cudaStream_t s) {
+  adj_sw_prep_kernel<float><<<(ncol + 127) / 128, 128, 0, s>>>(in, w, ncol, nlay);
+  if (maxl_for(nlay) == 64)
+    sw_adj_kernel<float, 64><<<nb, kBlock, 0, s>>>(in, w, adjflux, iaer, tab, tab64, cot, nseed, ncol, nlay);
+  else
+    sw_adj_kernel<float, 208><<<nb, kBlock, 0, s>>>(in, w, adjflux, iaer, tab, tab64, cot, nseed, ncol, nlay);
 }
 
 void launch_adj_finalize(const AdjLwWork& lw, const AdjSwWork& sw, const double* plev, const double* coszen,

@@ -9,11 +9,13 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <type_traits>
 
 namespace rrtmg {
 
 // The dual overloads below live in this namespace; keep the plain ones visible.
 using ::exp;
+using ::expm1;
 using ::fmin;
 using ::log;
 using ::pow;
@@ -23,8 +25,9 @@ template <class R>
 struct Dual {
   R v, t, q;  // value, d/dT(layer), d/dq(layer)
   __host__ __device__ Dual() : v(0), t(0), q(0) {}
-  __host__ __device__ Dual(R a) : v(a), t(0), q(0) {}
-  __host__ __device__ Dual(int a) : v((R)a), t(0), q(0) {}
+  // constant (zero tangents) from any arithmetic value
+  template <class T, typename std::enable_if<std::is_arithmetic<T>::value, int>::type = 0>
+  __host__ __device__ Dual(T a) : v((R)a), t(0), q(0) {}
   __host__ __device__ Dual(R a, R dt, R dq) : v(a), t(dt), q(dq) {}
   __host__ __device__ explicit operator int() const { return (int)v; }
   __host__ __device__ explicit operator R() const { return v; }
@@ -75,6 +78,10 @@ template <class R> __host__ __device__ inline bool operator==(const Dual<R>& a, 
 template <class R> __device__ inline Dual<R> exp(const Dual<R>& a) {
   const R e = exp(a.v);
   return {e, e * a.t, e * a.q};
+}
+template <class R> __device__ inline Dual<R> expm1(const Dual<R>& a) {
+  const R e = exp(a.v);
+  return {expm1(a.v), e * a.t, e * a.q};
 }
 template <class R> __device__ inline Dual<R> log(const Dual<R>& a) {
   const R inv = (R)1 / a.v;

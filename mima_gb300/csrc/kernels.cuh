@@ -32,6 +32,25 @@ static __constant__ LwConst c_lw;
 static __constant__ SwConst c_sw;
 static __constant__ LwConstF c_lwf;  // uploaded by the FP32-split unit only
 
+// FP32 copies of the per-layer LW constants (host side, for the upload of
+// c_lwf in every translation unit that runs FP32 gas optics).
+inline LwConstF make_lwconstf(const LwConst& lw) {
+  LwConstF f{};
+  for (int k = 0; k < 7 * 60; ++k) f.chi[k] = (float)lw.chi[k];
+  for (int j = 0; j < 61; ++j) {
+    f.r_h2oco2[j] = (float)lw.r_h2oco2[j];
+    f.r_h2oo3[j] = (float)lw.r_h2oo3[j];
+    f.r_h2on2o[j] = (float)lw.r_h2on2o[j];
+    f.r_h2och4[j] = (float)lw.r_h2och4[j];
+    f.r_n2oco2[j] = (float)lw.r_n2oco2[j];
+    f.r_o3co2[j] = (float)lw.r_o3co2[j];
+  }
+  for (int b = 0; b < kLwBands; ++b)
+    for (int k = 0; k < 4; ++k) f.refrat[b][k] = (float)lw.refrat[b][k];
+  f.oneminus = (float)lw.oneminus;
+  return f;
+}
+
 // Per-layer LW constants in the solver's arithmetic type.
 template <class R>
 __device__ __forceinline__ const auto& lw_rconst() {
@@ -815,28 +834,31 @@ __device__ __forceinline__ void reftra1(R zto1, R zw, R zg, R prmuz, R bpade, co
 
 // exp(-x) from the SW table / series together with exp(-x) - 1, the latter
 // formed without cancellation (series: -x + x^2/2; table: tbl - 1).
-__device__ __forceinline__ void sw_exp_pair(float ze1, float bpade, const float* __restrict__ exptbl, bool analytic,
-                                            float& e, float& em1) {
-  if (ze1 <= 0.06f) {
-    em1 = -ze1 + 0.5f * ze1 * ze1;
-    e = 1.f - ze1 + 0.5f * ze1 * ze1;
+// R: float, or a dual number of floats (the split adjoint).
+template <class R>
+__device__ __forceinline__ void sw_exp_pair(R ze1, R bpade, const float* __restrict__ exptbl, bool analytic, R& e,
+                                            R& em1) {
+  if (ze1 <= (R)0.06) {
+    em1 = -ze1 + (R)0.5 * ze1 * ze1;
+    e = (R)1. - ze1 + (R)0.5 * ze1 * ze1;
     return;
   }
   if (analytic) {
-    e = expf(-ze1);
-    em1 = expm1f(-ze1);
+    e = exp(-ze1);
+    em1 = expm1(-ze1);
     return;
   }
-  const float tblind = ze1 / (bpade + ze1);
-  int itind = (int)(10000.0f * tblind + 0.5f);
+  const R tblind = ze1 / (bpade + ze1);
+  int itind = (int)((R)10000.0 * tblind + (R)0.5);
   itind = itind < 0 ? 0 : (itind > kNTbl ? kNTbl : itind);
-  e = __ldg(exptbl + itind);
-  em1 = e - 1.f;
+  e = (R)__ldg(exptbl + itind);
+  em1 = e - (R)1.;
 }
 
 // FP32 delta-Eddington layer solution (same model as reftra1, kmodts = 2),
 // rearranged so that no O(1) terms cancel for optically thin or nearly
-// conservative layers, where FP32 would otherwise lose the layer absorptance:
+// conservative layers, where FP32 would otherwise lose the layer absorptance,
+// and so that no e^{+kt} is formed (scaled by e^{-kt}, see below):
 //   * the numerators zr1 e^{kt} - zr2 e^{-kt} - zr3 e^{-t/mu} (and the zt
 //     analogue) have zr1 - zr2 - zr3 = 0, so they are evaluated on the
 //     complements e - 1;
@@ -844,59 +866,70 @@ __device__ __forceinline__ void sw_exp_pair(float ze1, float bpade, const float*
 //   * (1 - beta e^{-2kt}) (k + g1) = 2k + (g1 - k)(1 - e^{-2kt});
 //   * zr4 e^{kt} + zr5 e^{-kt} = zrpp (k (e^{kt} + e^{-kt}) + g1 (e^{kt} - e^{-kt})).
 // Exponentials are the same table / series values as the reference uses.
-__device__ __forceinline__ void reftra_split(float zto1, float zw, float zg, float prmuz, float bpade,
-                                             const float* __restrict__ exptbl, bool analytic, float& pref,
-                                             float& prefd, float& ptra, float& ptrad) {
-  const float eps = 1.e-08f, zwcrit = 0.9999995f;
-  const float zg3 = 3.f * zg;
-  const float zgamma1 = (8.f - zw * (5.f + zg3)) * 0.25f;
-  const float zgamma2 = 3.f * (zw * (1.f - zg)) * 0.25f;
-  const float zgamma3 = (2.f - zg3 * prmuz) * 0.25f;
-  const float zgamma4 = 1.f - zgamma3;
-  const float r = zg / (1.f - zg);
-  const float zwo = zw / (1.f - (1.f - zw) * (r * r));
+// zg_zero: the asymmetry factor is identically 0 (no aerosol), so r = 0 and
+// zwo = zw without the two divisions.
+template <class R>
+__device__ __forceinline__ void reftra_split(R zto1, R zw, R zg, R prmuz, R bpade, const float* __restrict__ exptbl,
+                                             bool analytic, R& pref, R& prefd, R& ptra, R& ptrad,
+                                             bool zg_zero = false) {
+  const R eps = (R)1.e-08, zwcrit = (R)0.9999995;
+  const R zg3 = (R)3. * zg;
+  const R zgamma1 = ((R)8. - zw * ((R)5. + zg3)) * (R)0.25;
+  const R zgamma2 = (R)3. * (zw * ((R)1. - zg)) * (R)0.25;
+  const R zgamma3 = ((R)2. - zg3 * prmuz) * (R)0.25;
+  const R zgamma4 = (R)1. - zgamma3;
+  R zwo = zw;
+  if (!zg_zero) {
+    const R r = zg / ((R)1. - zg);
+    zwo = zw / ((R)1. - ((R)1. - zw) * (r * r));
+  }
   if (zwo >= zwcrit) {
-    const float za1 = zgamma1 * prmuz - zgamma3;
-    const float zgt = zgamma1 * zto1;
-    float ze2, m2;
-    sw_exp_pair(fminf(zto1 / prmuz, 500.f), bpade, exptbl, analytic, ze2, m2);
-    pref = (zgt + za1 * m2) / (1.f + zgt);
-    ptra = 1.f - pref;
-    prefd = zgt / (1.f + zgt);
-    ptrad = 1.f - prefd;
-    if (m2 == 0.f) {
-      pref = 0.f;
-      ptra = 1.f;
-      prefd = 0.f;
-      ptrad = 1.f;
+    const R za1 = zgamma1 * prmuz - zgamma3;
+    const R zgt = zgamma1 * zto1;
+    R ze2, m2;
+    sw_exp_pair(fmin(zto1 / prmuz, (R)500.), bpade, exptbl, analytic, ze2, m2);
+    pref = (zgt + za1 * m2) / ((R)1. + zgt);
+    ptra = (R)1. - pref;
+    prefd = zgt / ((R)1. + zgt);
+    ptrad = (R)1. - prefd;
+    if (m2 == (R)0.) {
+      pref = (R)0.;
+      ptra = (R)1.;
+      prefd = (R)0.;
+      ptrad = (R)1.;
     }
   } else {
-    const float za1 = zgamma1 * zgamma4 + zgamma2 * zgamma3;
-    const float za2 = zgamma1 * zgamma3 + zgamma2 * zgamma4;
-    const float zrk = sqrtf((2.f * (1.f - zw)) * (zgamma1 + zgamma2));
-    const float zrp = zrk * prmuz;
-    const float zrp1 = 1.f + zrp, zrm1 = 1.f - zrp, zrk2 = 2.f * zrk, zrpp = 1.f - zrp * zrp;
-    const float zr1 = zrm1 * (za2 + zrk * zgamma3);
-    const float zr2 = zrp1 * (za2 - zrk * zgamma3);
-    const float zr3 = zrk2 * (zgamma3 - za2 * prmuz);
-    const float zt1 = zrp1 * (za1 + zrk * zgamma4);
-    const float zt2 = zrm1 * (za1 - zrk * zgamma4);
-    const float zt3 = zrk2 * (zgamma4 + za1 * prmuz);
-    float zem1, m1, zem2, m2;
-    sw_exp_pair(fminf(zrk * zto1, 500.f), bpade, exptbl, analytic, zem1, m1);
-    sw_exp_pair(fminf(zto1 / prmuz, 500.f), bpade, exptbl, analytic, zem2, m2);
-    const float zep1 = 1.f / zem1, zep2 = 1.f / zem2;
-    const float p1 = -m1 * zep1, p2 = -m2 * zep2;  // e^{kt} - 1, e^{t/mu} - 1
-    const float zden = zrpp * (zrk * (zep1 + zem1) + zgamma1 * (p1 - m1));
+    const R za1 = zgamma1 * zgamma4 + zgamma2 * zgamma3;
+    const R za2 = zgamma1 * zgamma3 + zgamma2 * zgamma4;
+    const R zrk = sqrt(((R)2. * ((R)1. - zw)) * (zgamma1 + zgamma2));
+    const R zrp = zrk * prmuz;
+    const R zrp1 = (R)1. + zrp, zrm1 = (R)1. - zrp, zrk2 = (R)2. * zrk, zrpp = (R)1. - zrp * zrp;
+    const R zr1 = zrm1 * (za2 + zrk * zgamma3);
+    const R zr2 = zrp1 * (za2 - zrk * zgamma3);
+    const R zr3 = zrk2 * (zgamma3 - za2 * prmuz);
+    const R zt1 = zrp1 * (za1 + zrk * zgamma4);
+    const R zt2 = zrm1 * (za1 - zrk * zgamma4);
+    const R zt3 = zrk2 * (zgamma4 + za1 * prmuz);
+    R zem1, m1, zem2, m2;
+    sw_exp_pair(fmin(zrk * zto1, (R)500.), bpade, exptbl, analytic, zem1, m1);
+    sw_exp_pair(fmin(zto1 / prmuz, (R)500.), bpade, exptbl, analytic, zem2, m2);
+    // Numerators and denominator multiplied by E = e^{-kt} (= zem1), so that
+    // only e^{-kt}, e^{-t/mu} and their complements appear: e^{+kt} would
+    // overflow FP32 in thick layers (and its derivative already beyond kt = 44).
+    //   (e^{kt} - 1) E = -m1,  (e^{kt} + e^{-kt}) E = 1 + E^2,  (e^{kt} - e^{-kt}) E = 1 - E^2,
+    //   (e^{t/mu} - 1) e^{-t/mu} = -m2.
+    const R E = zem1;
+    const R zden = zrpp * (zrk * ((R)1. + E * E) + zgamma1 * (-m1 * ((R)2. + m1)));
     if (zden >= -eps && zden <= eps) {
       pref = eps;
       ptra = zem2;
     } else {
-      pref = zw * (zr1 * p1 - zr2 * m1 - zr3 * m2) / zden;
-      ptra = zem2 - zem2 * zw * (zt1 * p1 - zt2 * m1 - zt3 * p2) / zden;
+      const R wz = zw / zden;
+      pref = wz * (-m1 * (zr1 + zr2 * E) - zr3 * m2 * E);
+      ptra = zem2 - wz * (-m1 * zem2 * (zt1 + zt2 * E) + zt3 * m2 * E);
     }
-    const float omm = -m1 * (2.f + m1);  // 1 - e^{-2kt}
-    const float zdend = 1.f / (zrk2 + (zgamma1 - zrk) * omm);
+    const R omm = -m1 * ((R)2. + m1);  // 1 - e^{-2kt}
+    const R zdend = (R)1. / (zrk2 + (zgamma1 - zrk) * omm);
     prefd = zgamma2 * omm * zdend;
     ptrad = zrk2 * zem1 * zdend;
   }
@@ -970,7 +1003,7 @@ __device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, dou
     zgcc = (zgcc - zf) / ((R)1.0 - zf);
     R rf, rfd, tr, trd;
     if constexpr (sizeof(R) == 4)
-      reftra_split(ztauc, zomcc, zgcc, prmu0, bpade, exptbl, analytic, rf, rfd, tr, trd);
+      reftra_split(ztauc, zomcc, zgcc, prmu0, bpade, exptbl, analytic, rf, rfd, tr, trd, iaer != 10);
     else
       reftra1<R, R>(ztauc, zomcc, zgcc, prmu0, bpade, exptbl, analytic, rf, rfd, tr, trd);
     pref[jk - 1] = rf;

@@ -9,19 +9,7 @@ namespace rrtmg {
 cudaError_t upload_constants_split(const LwConst& lw, const SwConst& sw) {
   cudaError_t e = cudaMemcpyToSymbol(c_lw, &lw, sizeof(LwConst));
   if (e != cudaSuccess) return e;
-  LwConstF f{};
-  for (int k = 0; k < 7 * 60; ++k) f.chi[k] = (float)lw.chi[k];
-  for (int j = 0; j < 61; ++j) {
-    f.r_h2oco2[j] = (float)lw.r_h2oco2[j];
-    f.r_h2oo3[j] = (float)lw.r_h2oo3[j];
-    f.r_h2on2o[j] = (float)lw.r_h2on2o[j];
-    f.r_h2och4[j] = (float)lw.r_h2och4[j];
-    f.r_n2oco2[j] = (float)lw.r_n2oco2[j];
-    f.r_o3co2[j] = (float)lw.r_o3co2[j];
-  }
-  for (int b = 0; b < kLwBands; ++b)
-    for (int k = 0; k < 4; ++k) f.refrat[b][k] = (float)lw.refrat[b][k];
-  f.oneminus = (float)lw.oneminus;
+  const LwConstF f = make_lwconstf(lw);
   e = cudaMemcpyToSymbol(c_lwf, &f, sizeof(LwConstF));
   if (e != cudaSuccess) return e;
   return cudaMemcpyToSymbol(c_sw, &sw, sizeof(SwConst));

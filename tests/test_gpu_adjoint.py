@@ -240,3 +240,24 @@ def test_jacobian_against_oracle_differences(gpu, cfg3, orc):
         assert checked > 0.8 * len(xs) * atm.ncol * (2 * L + 3)
     finally:
         orc.set_table_mode(True)
+
+
+@pytest.mark.gpu
+def test_split_adjoint_against_fp64_adjoint(gpu, cfg3):
+    """FP32/FP64-split adjoint (FP32 dual numbers and reverse sweeps, FP64 sums)
+    against the FP64 adjoint, relative to each row's scale as above."""
+    gpu.set_precision("fp64")
+    j64 = gpu.jacobian(cfg3)
+    gpu.set_precision("split")
+    try:
+        j32 = gpu.jacobian(cfg3)
+    finally:
+        gpu.set_precision("fp64")
+    rowmax = np.max(np.abs(j64), axis=0, keepdims=True)
+    err = np.abs(j32 - j64) / (np.maximum(np.abs(j64), FLOOR * rowmax) + 1e-300)
+    print(f"\nsplit vs fp64 Jacobian: max {err.max():.2e}, 99.9% {np.quantile(err, 0.999):.2e}, "
+          f"99% {np.quantile(err, 0.99):.2e}")
+    assert np.isfinite(j32).all()
+    assert np.quantile(err, 0.99) <= 1e-4
+    assert np.quantile(err, 0.999) <= 1e-3
+    assert err.max() <= 1e-2

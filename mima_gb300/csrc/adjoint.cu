@@ -668,6 +668,7 @@ __device__ __forceinline__ void sw_adj_band(const SwIn& in, const AdjSwWorkT<R>&
   R zu[MAXL], zd[MAXL];          // reciprocals of the upward / downward recursions per layer
   R gR[MAXL], gD[MAXL], gT[MAXL], gS[MAXL], gX[MAXL];
   R an[MAXL + 1];                // seed cotangents of net flux per bottom-up level
+  R gtl[MAXL], gql[MAXL];         // FP32: layer gradients contracted as the sweeps go
   R lb[MAXL + 1], ln[MAXL + 1], lr[MAXL + 1];  // local cotangents of tb, tn, rn per level
   for (int j = 0; j < klev; ++j) {
     const int ikl = klev - j;
@@ -712,23 +713,27 @@ __device__ __forceinline__ void sw_adj_band(const SwIn& in, const AdjSwWorkT<R>&
   for (int j = 0; j < klev; ++j) {
     tb[j + 1] = Xv[j] * tb[j];
     const R z = (R)1.0 / ((R)1.0 - Dv[j] * rn[j]);
-    zd[j] = z;
+    if constexpr (sizeof(R) == 8) zd[j] = z;
     tn[j + 1] = tb[j] * Tv[j] + Sv[j] * ((tn[j] - tb[j]) + tb[j] * Rv[j] * rn[j]) * z;
     rn[j + 1] = Dv[j] + Sv[j] * Sv[j] * rn[j] * z;
   }
   pu[klev] = albdir; pd[klev] = albdif;
   for (int j = klev - 1; j >= 0; --j) {
     const R z = (R)1.0 / ((R)1.0 - pd[j + 1] * Dv[j]);
-    zu[j] = z;
+    if constexpr (sizeof(R) == 8) zu[j] = z;
     pu[j] = Rv[j] + Sv[j] * ((Tv[j] - Xv[j]) * pd[j + 1] + Xv[j] * pu[j + 1]) * z;
     pd[j] = Dv[j] + Sv[j] * Sv[j] * pd[j + 1] * z;
   }
-  for (int j = 0; j <= klev; ++j) {
-    const R z = (R)1.0 / ((R)1.0 - rn[j] * pd[j]);
-    zf[j] = z;
-    const R fu = (tb[j] * pu[j] + (tn[j] - tb[j]) * pd[j]) * z;
-    const R fd = tb[j] + (tn[j] - tb[j] + tb[j] * pu[j] * rn[j]) * z;
-    dn[j] = fd - fu;
+  // FP64: reciprocals and flux differences kept per level (FP64 divides are
+  // expensive); FP32 recomputes them (local-memory traffic is what costs)
+  if constexpr (sizeof(R) == 8) {
+    for (int j = 0; j <= klev; ++j) {
+      const R z = (R)1.0 / ((R)1.0 - rn[j] * pd[j]);
+      zf[j] = z;
+      const R fu = (tb[j] * pu[j] + (tn[j] - tb[j]) * pd[j]) * z;
+      const R fd = tb[j] + (tn[j] - tb[j] + tb[j] * pu[j] * rn[j]) * z;
+      dn[j] = fd - fu;
+    }
   }
 
   const int wib = threadIdx.x >> 5;
@@ -753,7 +758,11 @@ __device__ __forceinline__ void sw_adj_band(const SwIn& in, const AdjSwWorkT<R>&
     // local cotangents of the level states at top-down level j from the fluxes there
     auto local = [&](int j, R& ltb, R& ltn, R& lrn, R& lpu, R& lpd) {
       const R a = zinc.v * anet(klev - j);
-      const R z = zf[j];
+      R z;
+      if constexpr (sizeof(R) == 8)
+        z = zf[j];
+      else
+        z = (R)1.0 / ((R)1.0 - rn[j] * pd[j]);
       const R Af = tb[j] * pu[j] + (tn[j] - tb[j]) * pd[j];
       const R Bf = tn[j] - tb[j] + tb[j] * pu[j] * rn[j];
       // fu = Af z (cotangent -a), fd = tb + Bf z (cotangent a)
@@ -764,56 +773,112 @@ __device__ __forceinline__ void sw_adj_band(const SwIn& in, const AdjSwWorkT<R>&
       lrn = -a * Af * z * z * pd[j] + a * (tb[j] * pu[j] * z + Bf * z * z * pd[j]);
     };
     R lzinc = (R)0.0;
-    for (int j = 0; j <= klev; ++j) lzinc += anet(klev - j) * dn[j];
-    for (int j = 0; j < klev; ++j) gR[j] = gD[j] = gT[j] = gS[j] = gX[j] = (R)0.0;
-    // reverse of the upward sweep, carried from the top down; the local
-    // cotangents of (tb, tn, rn) are kept for the second sweep
-    R Lu = (R)0.0, Ld = (R)0.0;
-    {
-      R lpu, lpd;
-      local(klev, lb[klev], ln[klev], lr[klev], lpu, lpd);
-    }
-    for (int j = 0; j < klev; ++j) {
-      R lpu, lpd;
-      local(j, lb[j], ln[j], lr[j], lpu, lpd);
-      Lu += lpu;
-      Ld += lpd;
-      const R z = zu[j];
-      const R Xx = (Tv[j] - Xv[j]) * pd[j + 1] + Xv[j] * pu[j + 1];
-      const R Td = Sv[j];
-      gR[j] += Lu;
-      gS[j] += Lu * Xx * z + Ld * (R)2.0 * Td * pd[j + 1] * z;
-      gT[j] += Lu * Td * pd[j + 1] * z;
-      gX[j] += Lu * Td * (pu[j + 1] - pd[j + 1]) * z;
-      gD[j] += Ld * ((R)1.0 + Td * Td * pd[j + 1] * z * z * pd[j + 1]) + Lu * Td * Xx * z * z * pd[j + 1];
-      const R nLu = Lu * Td * Xv[j] * z;
-      const R nLd = Lu * (Td * (Tv[j] - Xv[j]) * z + Td * Xx * z * z * Dv[j]) +
-                         Ld * (Td * Td * z + Td * Td * pd[j + 1] * z * z * Dv[j]);
-      Lu = nLu;
-      Ld = nLd;
-    }
-    // reverse of the downward sweep, carried from the surface up
-    R Lb = (R)0.0, Ln = (R)0.0, Lr = (R)0.0;
-    for (int j = klev; j >= 1; --j) {
-      Lb += lb[j];
-      Ln += ln[j];
-      Lr += lr[j];
-      const int q = j - 1;
-      const R z = zd[q];
-      const R Y = (tn[q] - tb[q]) + tb[q] * Rv[q] * rn[q];
-      const R Td = Sv[q];
-      gX[q] += Lb * tb[q];
-      gT[q] += Ln * tb[q];
-      gS[q] += Ln * Y * z + Lr * (R)2.0 * Td * rn[q] * z;
-      gR[q] += Ln * Td * tb[q] * rn[q] * z;
-      gD[q] += Ln * Td * Y * z * z * rn[q] + Lr * ((R)1.0 + Td * Td * rn[q] * z * z * rn[q]);
-      const R nLb = Lb * Xv[q] + Ln * (Tv[q] + Td * (-(R)1.0 + Rv[q] * rn[q]) * z);
-      const R nLn = Ln * Td * z;
-      const R nLr = Ln * (Td * tb[q] * Rv[q] * z + Td * Y * z * z * Dv[q]) +
-                         Lr * (Td * Td * z + Td * Td * rn[q] * z * z * Dv[q]);
-      Lb = nLb;
-      Ln = nLn;
-      Lr = nLr;
+    if constexpr (sizeof(R) == 8) {
+      for (int j = 0; j <= klev; ++j) lzinc += anet(klev - j) * dn[j];
+      for (int j = 0; j < klev; ++j) gR[j] = gD[j] = gT[j] = gS[j] = gX[j] = (R)0.0;
+      // reverse of the upward sweep, carried from the top down; the local
+      // cotangents of (tb, tn, rn) are kept for the second sweep
+      R Lu = (R)0.0, Ld = (R)0.0;
+      {
+        R lpu, lpd;
+        local(klev, lb[klev], ln[klev], lr[klev], lpu, lpd);
+      }
+      for (int j = 0; j < klev; ++j) {
+        R lpu, lpd;
+        local(j, lb[j], ln[j], lr[j], lpu, lpd);
+        Lu += lpu;
+        Ld += lpd;
+        const R z = zu[j];
+        const R Xx = (Tv[j] - Xv[j]) * pd[j + 1] + Xv[j] * pu[j + 1];
+        const R Td = Sv[j];
+        gR[j] += Lu;
+        gS[j] += Lu * Xx * z + Ld * (R)2.0 * Td * pd[j + 1] * z;
+        gT[j] += Lu * Td * pd[j + 1] * z;
+        gX[j] += Lu * Td * (pu[j + 1] - pd[j + 1]) * z;
+        gD[j] += Ld * ((R)1.0 + Td * Td * pd[j + 1] * z * z * pd[j + 1]) + Lu * Td * Xx * z * z * pd[j + 1];
+        const R nLu = Lu * Td * Xv[j] * z;
+        const R nLd = Lu * (Td * (Tv[j] - Xv[j]) * z + Td * Xx * z * z * Dv[j]) +
+                           Ld * (Td * Td * z + Td * Td * pd[j + 1] * z * z * Dv[j]);
+        Lu = nLu;
+        Ld = nLd;
+      }
+      // reverse of the downward sweep, carried from the surface up
+      R Lb = (R)0.0, Ln = (R)0.0, Lr = (R)0.0;
+      for (int j = klev; j >= 1; --j) {
+        Lb += lb[j];
+        Ln += ln[j];
+        Lr += lr[j];
+        const int q = j - 1;
+        const R z = zd[q];
+        const R Y = (tn[q] - tb[q]) + tb[q] * Rv[q] * rn[q];
+        const R Td = Sv[q];
+        gX[q] += Lb * tb[q];
+        gT[q] += Ln * tb[q];
+        gS[q] += Ln * Y * z + Lr * (R)2.0 * Td * rn[q] * z;
+        gR[q] += Ln * Td * tb[q] * rn[q] * z;
+        gD[q] += Ln * Td * Y * z * z * rn[q] + Lr * ((R)1.0 + Td * Td * rn[q] * z * z * rn[q]);
+        const R nLb = Lb * Xv[q] + Ln * (Tv[q] + Td * (-(R)1.0 + Rv[q] * rn[q]) * z);
+        const R nLn = Ln * Td * z;
+        const R nLr = Ln * (Td * tb[q] * Rv[q] * z + Td * Y * z * z * Dv[q]) +
+                           Lr * (Td * Td * z + Td * Td * rn[q] * z * z * Dv[q]);
+        Lb = nLb;
+        Ln = nLn;
+        Lr = nLr;
+      }
+    } else {
+      for (int j = 0; j <= klev; ++j) {
+        const R z = (R)1.0 / ((R)1.0 - rn[j] * pd[j]);
+        const R fu = (tb[j] * pu[j] + (tn[j] - tb[j]) * pd[j]) * z;
+        const R fd = tb[j] + (tn[j] - tb[j] + tb[j] * pu[j] * rn[j]) * z;
+        lzinc += anet(klev - j) * (fd - fu);
+      }
+      for (int j = 0; j < klev; ++j) gtl[j] = gql[j] = (R)0.0;
+      auto contract = [&](int j, R dR, R dD, R dT, R dS, R dX) {
+        gtl[j] += dR * Rt[j] + dD * Dt[j] + dT * Tt[j] + dS * St[j] + dX * Xt[j];
+        gql[j] += dR * Rq[j] + dD * Dq[j] + dT * Tq[j] + dS * Sq[j] + dX * Xq[j];
+      };
+      // reverse of the upward sweep, carried from the top down
+      R Lu = (R)0.0, Ld = (R)0.0;
+      for (int j = 0; j < klev; ++j) {
+        R ltb, ltn, lrn, lpu, lpd;
+        local(j, ltb, ltn, lrn, lpu, lpd);
+        Lu += lpu;
+        Ld += lpd;
+        const R z = (R)1.0 / ((R)1.0 - pd[j + 1] * Dv[j]);
+        const R Xx = (Tv[j] - Xv[j]) * pd[j + 1] + Xv[j] * pu[j + 1];
+        const R Td = Sv[j];
+        contract(j, Lu, Ld * ((R)1.0 + Td * Td * pd[j + 1] * z * z * pd[j + 1]) + Lu * Td * Xx * z * z * pd[j + 1],
+                 Lu * Td * pd[j + 1] * z, Lu * Xx * z + Ld * (R)2.0 * Td * pd[j + 1] * z,
+                 Lu * Td * (pu[j + 1] - pd[j + 1]) * z);
+        const R nLu = Lu * Td * Xv[j] * z;
+        const R nLd = Lu * (Td * (Tv[j] - Xv[j]) * z + Td * Xx * z * z * Dv[j]) +
+                      Ld * (Td * Td * z + Td * Td * pd[j + 1] * z * z * Dv[j]);
+        Lu = nLu;
+        Ld = nLd;
+      }
+      // reverse of the downward sweep, carried from the surface up
+      R Lb = (R)0.0, Ln = (R)0.0, Lr = (R)0.0;
+      for (int j = klev; j >= 1; --j) {
+        R ltb, ltn, lrn, lpu, lpd;
+        local(j, ltb, ltn, lrn, lpu, lpd);
+        Lb += ltb;
+        Ln += ltn;
+        Lr += lrn;
+        const int q = j - 1;
+        const R z = (R)1.0 / ((R)1.0 - Dv[q] * rn[q]);
+        const R Y = (tn[q] - tb[q]) + tb[q] * Rv[q] * rn[q];
+        const R Td = Sv[q];
+        contract(q, Ln * Td * tb[q] * rn[q] * z,
+                 Ln * Td * Y * z * z * rn[q] + Lr * ((R)1.0 + Td * Td * rn[q] * z * z * rn[q]), Ln * tb[q],
+                 Ln * Y * z + Lr * (R)2.0 * Td * rn[q] * z, Lb * tb[q]);
+        const R nLb = Lb * Xv[q] + Ln * (Tv[q] + Td * (-(R)1.0 + Rv[q] * rn[q]) * z);
+        const R nLn = Ln * Td * z;
+        const R nLr = Ln * (Td * tb[q] * Rv[q] * z + Td * Y * z * z * Dv[q]) +
+                      Lr * (Td * Td * z + Td * Td * rn[q] * z * z * Dv[q]);
+        Lb = nLb;
+        Ln = nLn;
+        Lr = nLr;
+      }
     }
     GRed<W, NG, R> red{(R*)sred + wib * W * kRow, (int)(threadIdx.x & 31), 0, 0};
     auto store = [&](int e, int cs, double v) {
@@ -822,8 +887,14 @@ __device__ __forceinline__ void sw_adj_band(const SwIn& in, const AdjSwWorkT<R>&
     };
     for (int l = 1; l <= nlay; ++l) {
       const int j = klev - l;
-      R gt = gR[j] * Rt[j] + gD[j] * Dt[j] + gT[j] * Tt[j] + gS[j] * St[j] + gX[j] * Xt[j];
-      R gq = gR[j] * Rq[j] + gD[j] * Dq[j] + gT[j] * Tq[j] + gS[j] * Sq[j] + gX[j] * Xq[j];
+      R gt, gq;
+      if constexpr (sizeof(R) == 8) {
+        gt = gR[j] * Rt[j] + gD[j] * Dt[j] + gT[j] * Tt[j] + gS[j] * St[j] + gX[j] * Xt[j];
+        gq = gR[j] * Rq[j] + gD[j] * Dq[j] + gT[j] * Tq[j] + gS[j] * Sq[j] + gX[j] * Xq[j];
+      } else {
+        gt = gtl[j];
+        gq = gql[j];
+      }
       if (l == ls) {
         gt += lzinc * zinc.t;
         gq += lzinc * zinc.q;

@@ -60,6 +60,7 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=2048, help="columns per CPU baseline step")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint cost measurement")
+    ap.add_argument("--no-driver", action="store_true", help="skip the run_rrtmg (GCM slab) measurement")
     ap.add_argument("--members", type=int, default=32, help="stress configuration (4): ensemble members")
     ap.add_argument("--stress-adjoint", default="split", choices=["split", "fp64"],
                     help="stress configuration (4): precision of the adjoint")
@@ -328,6 +329,48 @@ def measure_adjoint(torch, rrtmg, atmosphere, r, stream, atm, d, olw, osw, flush
                          "forward_plus_jacobian_over_forward": (ms_f3 + ms_j) / ms_f3}}
 
 
+def measure_driver(torch, rrtmg, atmosphere, r, stream, dev, flush, steps, warmup, lw_sw_ms):
+    """MiMA's whole radiation step (run_rrtmg with interp_temp and the zenith
+    angle) on a T85 GCM slab of 256 x 128 points x 40 levels, FP32-split:
+    through rrtmg_run_dev on device arrays, and end to end through
+    rrtmg_run_c on page-locked host arrays."""
+    slab = atmosphere.gcm_slab(256, 128, 40, seed=12346)
+    prm = rrtmg.run_params()
+    r.set_precision("split")
+    d = {k: torch.from_numpy(np.ascontiguousarray(getattr(slab, k))).to(dev) for k in rrtmg.RUN_IN
+         if getattr(slab, k) is not None}
+    shp3, shp2 = (slab.sk, slab.sj, slab.si), (slab.sj, slab.si)
+    out = {"tdt": torch.from_numpy(slab.tdt.copy()).to(dev),
+           "coszen": torch.empty(shp2, dtype=torch.float64, device=dev),
+           "flux_sw": torch.empty(shp2, dtype=torch.float64, device=dev),
+           "flux_lw": torch.empty(shp2, dtype=torch.float64, device=dev)}
+    call = lambda: r.run_rrtmg_dev(stream.cuda_stream, prm, slab.si, slab.sj, slab.sk, 43200, 100, 365, d, out)
+    t = time_calls(torch, stream, flush, call, steps, warmup)
+    ms = float(np.mean(t))
+    status = r.sync_status(stream.cuda_stream)
+    # host arrays: inputs in, tdt in and out, coszen and surface fluxes out
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy() if a is not None else None
+    hslab = atmosphere.GcmSlab(**{k: (pin(v) if isinstance(v, np.ndarray) else v) for k, v in vars(slab).items()})
+    h2d = sum(getattr(hslab, k).nbytes for k in rrtmg.RUN_IN if getattr(hslab, k) is not None) + slab.tdt.nbytes
+    d2h = slab.tdt.nbytes + 3 * slab.lat.nbytes
+    tdt0 = pin(slab.tdt)
+    for _ in range(max(2, min(warmup, 3))):
+        r.run_rrtmg(prm, hslab, 43200, 100, tdt=tdt0, diagnostics=False)
+    ts = []
+    for _ in range(max(3, steps // 4)):
+        t0 = time.perf_counter()
+        r.run_rrtmg(prm, hslab, 43200, 100, tdt=tdt0, diagnostics=False)
+        ts.append(time.perf_counter() - t0)
+    host_ms = float(np.mean(ts)) * 1e3
+    ncol = slab.si * slab.sj
+    return {"workload": "run_rrtmg on a T85 GCM slab 256x128x40 (lonstep 1, daily-mean zenith), FP32-split",
+            "device_ms": ms, "device_columns_per_s": ncol / (ms * 1e-3),
+            "lw_sw_graph_ms": lw_sw_ms, "driver_overhead_ms": ms - lw_sw_ms,
+            "host_e2e_ms": host_ms, "host_e2e_columns_per_s": ncol / (host_ms * 1e-3),
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "status": status,
+            "api": "rrtmg_run_dev (device arrays) / rrtmg_run_c (page-locked host arrays)"}
+
+
 def run_stress(args):
     """1,048,576 x 60 stress configuration: a seeded ensemble of 32 members of
     32768 T170-like columns (60 layers, top 0.01 hPa, Ts noise 3 K), all
@@ -508,6 +551,11 @@ def run_ours(args):
         adjoint = measure_adjoint(torch, rrtmg, atmosphere, r, stream, atm, d, olw64, osw64, flush,
                                   max(3, args.steps // 4), min(args.warmup, 3))
 
+    driver = None
+    if not args.no_driver:
+        driver = measure_driver(torch, rrtmg, atmosphere, r, stream, dev, flush, max(3, args.steps // 4),
+                                min(args.warmup, 3), ms32)
+
     # end to end through the host-array entry points, pinned host memory
     e2e = None
     if not args.no_e2e:
@@ -575,6 +623,8 @@ def run_ours(args):
         line["e2e"] = e2e
     if adjoint:
         line["adjoint"] = adjoint
+    if driver:
+        line["driver"] = driver
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

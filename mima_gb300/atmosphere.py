@@ -208,3 +208,69 @@ def small_atmosphere(ncol: int, nlay: int = 40, seed: int = 7, ts_sigma: float =
     atm = make_columns(lat, nlay, p_top, rng, ts_sigma, rh=rh)
     atm.meta.update(seed=seed, small=True)
     return atm
+
+
+@dataclass
+class GcmSlab:
+    """One GCM slab as MiMA's ``run_rrtmg`` receives it
+    (``rrtm_radiation.f90:464-510``; the heights feed ``interp_temp``,
+    ``:420-460``).  Every array is C-ordered (level, latitude, longitude), i.e.
+    Fortran (si, sj, sk) with the longitude fastest; level 0 is the model top.
+    Pressures in Pa, heights in m, lat/lon in radians."""
+    si: int
+    sj: int
+    sk: int
+    lat: np.ndarray          # (sj, si)
+    lon: np.ndarray          # (sj, si)
+    p_full: np.ndarray       # (sk, sj, si)
+    p_half: np.ndarray       # (sk+1, sj, si), top interface 0 Pa as in MiMA
+    z_full: np.ndarray       # (sk, sj, si)
+    z_half: np.ndarray       # (sk+1, sj, si), 0 at the top as in MiMA (unused there)
+    t: np.ndarray            # (sk, sj, si) K
+    q: np.ndarray            # (sk, sj, si) kg/kg
+    o3: np.ndarray | None    # (sk, sj, si) O3 mass mixing ratio, or None (o3_val)
+    t_surf_rad: np.ndarray   # (sj, si) K
+    albedo: np.ndarray       # (sj, si)
+    rrtm_precip: np.ndarray | None  # (sj, si) accumulated precipitation (do_precip_albedo)
+    tdt: np.ndarray          # (sk, sj, si) K/s, the tendency before radiation
+
+
+def gcm_slab(nlon: int, nlat: int, nlev: int, seed: int, p_top: float = 10.0, ts_sigma: float = 2.0,
+             ozone: bool = True) -> GcmSlab:
+    """A seeded slab on nlon x nlat Gaussian points: surface pressure
+    1000 hPa + N(0, 10 hPa); half levels 0 Pa at the top, then log-spaced from
+    ``p_top`` (Pa) x ps/1000 hPa to ps; full levels the geometric mean of
+    their interfaces (half the first interface for the top level); the
+    temperature, humidity (RH U(0.2, 0.95)) and ozone profiles of
+    :func:`make_columns`; hydrostatic heights; albedo 0.27 +- 0.05; random
+    precipitation sums and a random prior tendency."""
+    rng = np.random.default_rng(seed)
+    lat = np.repeat(gaussian_latitudes(nlat)[:, None], nlon, axis=1)
+    lon = np.repeat((2.0 * np.pi * np.arange(nlon) / nlon)[None, :], nlat, axis=0)
+    ps = 1.0e5 + 1.0e3 * rng.standard_normal((nlat, nlon))
+    sig = np.exp(np.linspace(np.log(p_top / 1.0e5), 0.0, nlev))
+    p_half = np.empty((nlev + 1, nlat, nlon))
+    p_half[0] = 0.0
+    p_half[1:] = sig[:, None, None] * ps[None]
+    p_full = np.empty((nlev, nlat, nlon))
+    p_full[0] = 0.5 * p_half[1]
+    p_full[1:] = np.sqrt(p_half[1:-1] * p_half[2:])
+    ts = 240.0 + 60.0 * np.cos(lat) ** 2 + ts_sigma * rng.standard_normal((nlat, nlon))
+    tl = ts[None] * (p_full / ps[None]) ** (R_DRY * LAPSE / GRAV)
+    strat = tl <= T_TROP
+    t = np.maximum(tl, T_TROP)
+    z_half = np.zeros((nlev + 1, nlat, nlon))
+    z_full = np.empty((nlev, nlat, nlon))
+    for k in range(nlev - 1, -1, -1):
+        z_full[k] = z_half[k + 1] + R_DRY * t[k] / GRAV * np.log(p_half[k + 1] / p_full[k])
+        if k > 0:
+            z_half[k] = z_half[k + 1] + R_DRY * t[k] / GRAV * np.log(p_half[k + 1] / p_half[k])
+    rh = rng.uniform(0.2, 0.95, size=(nlat, nlon))
+    q = rh[None] * qsat(t, p_full / 100.0)
+    q = np.maximum(np.where(strat, 3.0e-6, q), 3.0e-6)
+    o3 = 8.0e-6 * np.exp(-0.5 * np.log10(p_full / 1000.0) ** 2) / AMDO if ozone else None
+    return GcmSlab(si=nlon, sj=nlat, sk=nlev, lat=lat, lon=lon, p_full=p_full, p_half=p_half, z_full=z_full,
+                   z_half=z_half, t=t, q=q, o3=o3, t_surf_rad=ts,
+                   albedo=0.27 + 0.05 * rng.uniform(-1.0, 1.0, size=(nlat, nlon)),
+                   rrtm_precip=rng.uniform(0.0, 2.0e-4, size=(nlat, nlon)),
+                   tdt=1.0e-5 * rng.standard_normal((nlev, nlat, nlon)))

@@ -30,6 +30,7 @@ UNITS = {
     "kernels_fp64.cu": ["--fmad=false"],
     "kernels_split.cu": [],
     "adjoint.cu": [],
+    "driver.cu": ["--fmad=false"],
     "tables_host.cu": [],
     "abi.cu": ["-Xcompiler", "-fvisibility=default"],
 }
@@ -45,7 +46,7 @@ def nvcc() -> str:
 def _stale(obj: Path, src: Path) -> bool:
     if not obj.exists():
         return True
-    deps = [src] + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + [ROOT / "include" / "rrtmg_gpu.h"]
+    deps = [src] + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + list((ROOT / "include").glob("*.h"))
     t = obj.stat().st_mtime
     return any(d.stat().st_mtime > t for d in deps)
 

@@ -18,8 +18,10 @@
 
 #include "adjoint.h"
 #include "common.cuh"
+#include "driver.h"
 #include "launch.h"
 #include "rrtmg_gpu.h"
+#include "rrtmg_run.h"
 #include "tables_host.h"
 
 using namespace rrtmg;
@@ -48,6 +50,8 @@ struct rrtmg_gpu_state {
   // that column chunks alternate between the streams
   cudaStream_t stream2 = nullptr;
   DevBuf hio[2], hws[2];
+  // run_rrtmg calls: RRTM columns, results and zonal scratch; host-array staging
+  DevBuf run_ws, run_io;
   long long launches = 0;
   std::string err;
   // Optional per-kernel timing: events around every launch of the last LW
@@ -516,7 +520,8 @@ int rrtmg_gpu_finalize(rrtmg_gpu_handle h) {
   if (h->stream2) cudaStreamSynchronize(h->stream2);
   void* ptrs[] = {h->lw_tab64, h->sw_tab64, h->lw_exp64, h->lw_tfn64, h->sw_exp64, h->totplnk, h->totplnkderiv,
                   h->lw_tab32, h->sw_tab32, h->lw_exp32, h->lw_tfn32, h->sw_exp32, h->flags, h->lw_ws.p,
-                  h->sw_ws.p, h->adj_ws.p, h->hio[0].p, h->hio[1].p, h->hws[0].p, h->hws[1].p};
+                  h->sw_ws.p, h->adj_ws.p, h->hio[0].p, h->hio[1].p, h->hws[0].p, h->hws[1].p, h->run_ws.p,
+                  h->run_io.p};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -862,3 +867,283 @@ extern "C" int rrtmg_lw_dev_static(rrtmg_gpu_handle h, void* stream, int ncol, i
   return lw_enqueue(h, (cudaStream_t)stream, base, ncol, nlay, idrv, in, uflx, dflx, hr, uflxc, dflxc, hrc,
                     duflx_dt, duflxc_dt);
 }
+
+// ---------------------------------------------------------------------------
+// run_rrtmg on the device (include/rrtmg_run.h): GCM slab -> RRTM columns ->
+// rrtmg_sw + rrtmg_lw -> GCM tendencies, all on one stream.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct RunWork {
+  RunCols c;
+  double *uflx, *dflx, *hr, *uflxc, *dflxc, *hrc;
+  double *swuflx, *swdflx, *swhr, *swuflxc, *swdflxc, *swhrc;
+  double *zq, *zp, *zt, *zsw, *zlw;
+  unsigned* flag;
+};
+
+RunWork carve_run(void* base, int sj, int sk, int ncol, bool secondary, size_t* bytes) {
+  Carver cv{(char*)base};
+  const size_t N = (size_t)ncol, L = (size_t)sk, Lv = L + 1;
+  RunWork w;
+  w.c.play = cv.take<double>(L * N);
+  w.c.plev = cv.take<double>(Lv * N);
+  w.c.tlay = cv.take<double>(L * N);
+  w.c.tlev = cv.take<double>(Lv * N);
+  w.c.tsfc = cv.take<double>(N);
+  w.c.h2o = cv.take<double>(L * N);
+  w.c.o3 = cv.take<double>(L * N);
+  w.c.co2 = cv.take<double>(L * N);
+  w.c.emis = cv.take<double>(16 * N);
+  w.c.alb = cv.take<double>(N);
+  w.c.cosz = cv.take<double>(N);
+  for (int m = 0; m < 7; ++m) w.c.gas[m] = secondary ? cv.take<double>(L * N) : nullptr;
+  double** lev[] = {&w.uflx, &w.dflx, &w.uflxc, &w.dflxc, &w.swuflx, &w.swdflx, &w.swuflxc, &w.swdflxc};
+  for (double** p : lev) *p = cv.take<double>(Lv * N);
+  double** lay[] = {&w.hr, &w.hrc, &w.swhr, &w.swhrc};
+  for (double** p : lay) *p = cv.take<double>(L * N);
+  w.zq = cv.take<double>((size_t)sj * L);
+  w.zt = cv.take<double>((size_t)sj * L);
+  w.zp = cv.take<double>(sj);
+  w.zsw = cv.take<double>(sj);
+  w.zlw = cv.take<double>(sj);
+  w.flag = cv.take<unsigned>(1);
+  if (bytes) *bytes = cv.off;
+  return w;
+}
+
+struct RunArgs {
+  int si, sj, sk, seconds, days, days_per_year;
+  RunGcm g;
+  RunOut o;
+};
+
+// Argument checks shared by the device and host entry points.
+int run_check(rrtmg_gpu_state* h, const rrtmg_run_params* p, const RunArgs& a) {
+  if (!valid_handle(h)) return RRTMG_ERR_ARG;
+  if (!p) return fail(h, RRTMG_ERR_ARG, "null rrtmg_run_params");
+  if (a.si < 1 || a.sj < 1) return fail(h, RRTMG_ERR_ARG, "si and sj must be >= 1");
+  if (p->lonstep < 1 || a.si % p->lonstep != 0) return fail(h, RRTMG_ERR_ARG, "si must be a multiple of lonstep >= 1");
+  if (a.days_per_year < 1) return fail(h, RRTMG_ERR_ARG, "days_per_year must be >= 1");
+  if (p->dt_rad_avg < 0) return fail(h, RRTMG_ERR_ARG, "dt_rad_avg must be >= 0 (resolve dt_rad_avg < 0 to dt_rad)");
+  int rc = check_dims(h, a.si / p->lonstep * a.sj, a.sk);
+  if (rc) return rc;
+  const RunGcm& g = a.g;
+  if (!g.lat || !g.lon || !g.p_full || !g.p_half || !g.z_full || !g.z_half || !g.t || !g.q || !g.t_surf ||
+      !g.albedo || !a.o.tdt || !a.o.coszen)
+    return fail(h, RRTMG_ERR_ARG, "a required array pointer is null");
+  if ((a.o.flux_sw == nullptr) != (a.o.flux_lw == nullptr))
+    return fail(h, RRTMG_ERR_ARG, "flux_sw and flux_lw: both or neither");
+  if (p->do_precip_albedo && p->num_precip > 0 && !g.precip)
+    return fail(h, RRTMG_ERR_ARG, "do_precip_albedo with num_precip > 0 needs rrtm_precip");
+  if (!(p->solr_cnst > 0.0)) return fail(h, RRTMG_ERR_ARG, "solr_cnst must be positive");
+  return RRTMG_OK;
+}
+
+// Model time of the radiation (rrtm_radiation.f90:550-558) and the
+// declination terms of compute_zenith (astro.f90:98-137).
+RunScalars run_scalars(const rrtmg_run_params& p, const RunArgs& a, int* dyofyr) {
+  const double pi = 3.14159265358979323846;
+  long long sec = a.seconds, days = a.days;
+  if (p.solday > 0) {
+    days = p.solday;
+  } else if (p.slowdown_rad != 1.0) {
+    const long long t = (long long)((double)(days * 86400 + sec) * p.slowdown_rad);
+    days = t / 86400;
+    sec = t % 86400;
+  }
+  RunScalars s{};
+  s.si = a.si;
+  s.sj = a.sj;
+  s.sk = a.sk;
+  s.lonstep = p.lonstep;
+  s.nsub = a.si / p.lonstep;
+  s.ncol = s.nsub * a.sj;
+  const int dpy = a.days_per_year;
+  s.radpersec = 2 * pi / 86400.;
+  const double radperday = 2 * pi / dpy;
+  s.radsec = (double)sec * s.radpersec;
+  s.zen_dt = p.dt_rad_avg;
+  s.dt_pi = (double)p.dt_rad_avg * s.radpersec;
+  long long d = days - (long long)(p.equinox_day * dpy);
+  d %= dpy;
+  if (d < 0) d += dpy;
+  const double radday = (double)d * radperday;
+  s.dec_sin = std::sin(p.obliq * (pi / 180.)) * std::sin(radday);
+  const double dec = std::asin(s.dec_sin);
+  s.dec_cos = std::cos(dec);
+  s.dec_tan = std::tan(dec);
+  *dyofyr = p.use_dyofyr ? (int)d : 0;  // rrtm_radiation.f90:598
+  s.zm_tracers = p.do_zm_tracers != 0;
+  s.fixed_water = p.do_fixed_water != 0;
+  s.secondary = p.include_secondary_gases != 0;
+  s.precip_albedo = p.do_precip_albedo != 0 && p.num_precip > 0;
+  s.zm_rad = p.do_zm_rad != 0;
+  s.h2o_lo = p.h2o_lower_limit;
+  s.t_lo = p.temp_lower_limit;
+  s.t_hi = p.temp_upper_limit;
+  s.co2 = p.co2ppmv * 1.e-6;
+  s.o3_val = p.o3_val;
+  s.fixed_water_val = p.fixed_water;
+  s.fixed_water_pres = p.fixed_water_pres;
+  s.fixed_water_lat = p.fixed_water_lat;
+  s.precip_albedo_val = p.precip_albedo;
+  s.precip_lat = p.precip_lat;
+  s.num_precip = p.num_precip;
+  const double gv[7] = {p.ch4_val, p.n2o_val, p.o2_val, p.cfc11_val, p.cfc12_val, p.cfc22_val, p.ccl4_val};
+  for (int m = 0; m < 7; ++m) s.gas_val[m] = gv[m];
+  return s;
+}
+
+int run_enqueue(rrtmg_gpu_state* h, cudaStream_t st, const rrtmg_run_params& p, const RunArgs& a) {
+  int dyofyr = 0;
+  const RunScalars s = run_scalars(p, a, &dyofyr);
+  size_t need;
+  carve_run(nullptr, a.sj, a.sk, s.ncol, s.secondary, &need);
+  int rc = ensure(h, h->run_ws, need, st);
+  if (rc) return rc;
+  const RunWork w = carve_run(h->run_ws.p, a.sj, a.sk, s.ncol, s.secondary, nullptr);
+  cudaError_t e = cudaMemsetAsync(w.flag, 0, sizeof(unsigned), st);
+  if (e != cudaSuccess) return cuda_fail(h, e, "run_rrtmg: clear flag");
+  launch_run_zonal(s, a.g, a.o.coszen, w.zq, w.zp, w.flag, st);
+  if (a.o.t_half) launch_run_thalf(s, a.g, a.o.t_half, st);
+  launch_run_prep(s, a.g, a.o.coszen, w.zq, w.zp, w.flag, w.c, st);
+  h->launches += a.o.t_half ? 3 : 2;
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(h, e, "run_rrtmg: input kernels");
+  const RunCols& c = w.c;
+  // rrtm_radiation.f90:683-713 (SW) and :718-749 (LW), clear sky, iaer = idrv = 0
+  const SwIn sin{c.play, c.plev, c.tlay, c.tlev, c.tsfc, c.h2o, c.o3, c.co2, c.gas[0], c.gas[1], c.gas[2],
+                 c.alb, c.alb, c.alb, c.alb, c.cosz, nullptr, nullptr, nullptr};
+  rc = sw_run(h, st, s.ncol, a.sk, 0, p.solrad, dyofyr, p.solr_cnst, sin, w.swuflx, w.swdflx, w.swhr, w.swuflxc,
+              w.swdflxc, w.swhrc);
+  if (rc) return rc;
+  const LwIn lin{c.play, c.plev, c.tlay, c.tlev, c.tsfc, c.h2o, c.o3, c.co2, c.gas[0], c.gas[1], c.gas[2],
+                 c.gas[3], c.gas[4], c.gas[5], c.gas[6], c.emis, nullptr};
+  rc = lw_run(h, st, s.ncol, a.sk, 0, lin, w.uflx, w.dflx, w.hr, w.uflxc, w.dflxc, w.hrc, nullptr, nullptr);
+  if (rc) return rc;
+  const RunRad r{w.uflx, w.dflx, w.hr, w.swuflx, w.swdflx, w.swhr};
+  if (s.zm_rad) {
+    launch_run_zonal_rad(s, r, w.zt, w.zsw, w.zlw, st);
+    h->launches += 1;
+  }
+  launch_run_post(s, r, w.zt, w.zsw, w.zlw, a.o, st);
+  h->launches += 1;
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(h, e, "run_rrtmg: output kernels");
+  return RRTMG_OK;
+}
+
+RunArgs run_args(int si, int sj, int sk, int seconds, int days, int days_per_year, const double* lat,
+                 const double* lon, const double* p_full, const double* p_half, const double* z_full,
+                 const double* z_half, const double* t, const double* q, const double* o3, const double* t_surf_rad,
+                 const double* albedo, const double* rrtm_precip, double* tdt, double* coszen, double* flux_sw,
+                 double* flux_lw, double* t_half, double* tdt_rad, double* tdt_sw, double* tdt_lw, double* olr,
+                 double* isr) {
+  RunArgs a;
+  a.si = si;
+  a.sj = sj;
+  a.sk = sk;
+  a.seconds = seconds;
+  a.days = days;
+  a.days_per_year = days_per_year;
+  a.g = RunGcm{lat, lon, p_full, p_half, z_full, z_half, t, q, o3, t_surf_rad, albedo, rrtm_precip};
+  a.o = RunOut{tdt, coszen, flux_sw, flux_lw, t_half, tdt_rad, tdt_sw, tdt_lw, olr, isr};
+  return a;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rrtmg_run_params_default(rrtmg_run_params* p) {
+  if (!p) return RRTMG_ERR_ARG;
+  std::memset(p, 0, sizeof(*p));
+  p->lonstep = 1;
+  p->dt_rad_avg = 86400;
+  p->h2o_lower_limit = 2.e-7;
+  p->temp_lower_limit = 100.;
+  p->temp_upper_limit = 370.;
+  p->co2ppmv = 300.;
+  p->fixed_water = 2.e-06;
+  p->fixed_water_pres = 100.e02;
+  p->fixed_water_lat = 90.;
+  p->precip_albedo = 0.35;
+  p->slowdown_rad = 1.0;
+  p->obliq = 23.439;
+  p->solr_cnst = 1368.22;
+  p->solrad = 1.0;
+  p->equinox_day = 0.25;
+  return RRTMG_OK;
+}
+
+int rrtmg_run_dev(rrtmg_gpu_handle h, void* stream, const rrtmg_run_params* prm, int si, int sj, int sk,
+                  int seconds, int days, int days_per_year, const double* lat, const double* lon,
+                  const double* p_full, const double* p_half, const double* z_full, const double* z_half,
+                  const double* t, const double* q, const double* o3, const double* t_surf_rad,
+                  const double* albedo, const double* rrtm_precip, double* tdt, double* coszen, double* flux_sw,
+                  double* flux_lw, double* t_half, double* tdt_rad, double* tdt_sw, double* tdt_lw, double* olr,
+                  double* isr) {
+  const RunArgs a = run_args(si, sj, sk, seconds, days, days_per_year, lat, lon, p_full, p_half, z_full, z_half, t,
+                             q, o3, t_surf_rad, albedo, rrtm_precip, tdt, coszen, flux_sw, flux_lw, t_half, tdt_rad,
+                             tdt_sw, tdt_lw, olr, isr);
+  int rc = run_check(h, prm, a);
+  if (rc) return rc;
+  cudaSetDevice(h->device);
+  return run_enqueue(h, (cudaStream_t)stream, *prm, a);
+}
+
+int rrtmg_run_c(rrtmg_gpu_handle h, const rrtmg_run_params* prm, int si, int sj, int sk, int seconds, int days,
+                int days_per_year, const double* lat, const double* lon, const double* p_full,
+                const double* p_half, const double* z_full, const double* z_half, const double* t, const double* q,
+                const double* o3, const double* t_surf_rad, const double* albedo, const double* rrtm_precip,
+                double* tdt, double* coszen, double* flux_sw, double* flux_lw, double* t_half, double* tdt_rad,
+                double* tdt_sw, double* tdt_lw, double* olr, double* isr) {
+  RunArgs a = run_args(si, sj, sk, seconds, days, days_per_year, lat, lon, p_full, p_half, z_full, z_half, t, q, o3,
+                       t_surf_rad, albedo, rrtm_precip, tdt, coszen, flux_sw, flux_lw, t_half, tdt_rad, tdt_sw,
+                       tdt_lw, olr, isr);
+  int rc = run_check(h, prm, a);
+  if (rc) return rc;
+  cudaSetDevice(h->device);
+  const size_t P = (size_t)si * sj, P3 = P * sk, P3h = P * (sk + 1);
+  // device staging: inputs, then tdt (in and out), then the outputs
+  const double** ins[] = {&a.g.lat, &a.g.lon, &a.g.p_full, &a.g.p_half, &a.g.z_full, &a.g.z_half, &a.g.t,
+                          &a.g.q, &a.g.o3, &a.g.t_surf, &a.g.albedo, &a.g.precip};
+  const size_t in_n[] = {P, P, P3, P3h, P3, P3h, P3, P3, P3, P, P, P};
+  double** outs[] = {&a.o.tdt, &a.o.coszen, &a.o.flux_sw, &a.o.flux_lw, &a.o.t_half, &a.o.tdt_rad,
+                     &a.o.tdt_sw, &a.o.tdt_lw, &a.o.olr, &a.o.isr};
+  const size_t out_n[] = {P3, P, P, P, P3h, P3, P3, P3, P, P};
+  size_t bytes = 0;
+  for (int k = 0; k < 12; ++k)
+    if (*ins[k]) bytes += align256(in_n[k] * sizeof(double));
+  for (int k = 0; k < 10; ++k)
+    if (*outs[k]) bytes += align256(out_n[k] * sizeof(double));
+  rc = ensure(h, h->run_io, bytes, nullptr);
+  if (rc) return rc;
+  cudaStream_t st = h->stream;
+  Carver cv{(char*)h->run_io.p};
+  double* host_out[10];
+  cudaError_t e = cudaSuccess;
+  for (int k = 0; k < 12 && e == cudaSuccess; ++k) {
+    if (!*ins[k]) continue;
+    double* d = cv.take<double>(in_n[k]);
+    e = cudaMemcpyAsync(d, *ins[k], in_n[k] * sizeof(double), cudaMemcpyHostToDevice, st);
+    *ins[k] = d;
+  }
+  for (int k = 0; k < 10 && e == cudaSuccess; ++k) {
+    host_out[k] = *outs[k];
+    if (!*outs[k]) continue;
+    double* d = cv.take<double>(out_n[k]);
+    if (k == 0) e = cudaMemcpyAsync(d, tdt, out_n[0] * sizeof(double), cudaMemcpyHostToDevice, st);
+    *outs[k] = d;
+  }
+  if (e != cudaSuccess) return cuda_fail(h, e, "run_rrtmg: copy inputs");
+  rc = run_enqueue(h, st, *prm, a);
+  if (rc) return rc;
+  for (int k = 0; k < 10 && e == cudaSuccess; ++k)
+    if (host_out[k]) e = cudaMemcpyAsync(host_out[k], *outs[k], out_n[k] * sizeof(double), cudaMemcpyDeviceToHost, st);
+  if (e != cudaSuccess) return cuda_fail(h, e, "run_rrtmg: copy outputs");
+  return read_flags(h, st);
+}
+
+}  // extern "C"

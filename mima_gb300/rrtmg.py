@@ -35,16 +35,49 @@ PREC = {"fp64": 0, "split": 1}
 STATIC_SCRATCH_BYTES = 64 * 1024 * 1024  # RRTMG_GPU_STATIC_SCRATCH_BYTES
 TRANS = {"table": 0, "analytic": 1}
 
-# Every symbol include/rrtmg_gpu.h declares.
+# Every symbol include/rrtmg_gpu.h and include/rrtmg_run.h declare.
 EXPORTED = ("rrtmg_gpu_init", "rrtmg_gpu_finalize", "rrtmg_gpu_set_precision", "rrtmg_gpu_error_string",
             "rrtmg_gpu_last_error", "rrtmg_gpu_launch_count", "rrtmg_lw_c", "rrtmg_sw_c", "rrtmg_lw_dev",
             "rrtmg_sw_dev", "rrtmg_gpu_reserve", "rrtmg_gpu_sync_status", "rrtmg_lw_dev_static",
             "rrtmg_gpu_set_transcendentals", "rrtmg_jacobian_dev", "rrtmg_vjp_dev", "rrtmg_gpu_set_profiling",
-            "rrtmg_gpu_profile")
+            "rrtmg_gpu_profile",
+            # include/rrtmg_run.h
+            "rrtmg_run_params_default", "rrtmg_run_dev", "rrtmg_run_c")
 KERNELS = ("lw_prep", "lw_gpoint", "lw_finalize", "sw_prep", "sw_gpoint", "sw_finalize")
 
 _lib = None
 _dp = C.POINTER(C.c_double)
+
+
+class RunParams(C.Structure):
+    """``rrtmg_run_params`` (include/rrtmg_run.h): the rrtm_radiation_nml and
+    astro_nml values MiMA's run_rrtmg reads (rrtm_radiation.f90:106-198,
+    astro.f90:22-31).  Build one with :func:`run_params`."""
+    _fields_ = [(n, C.c_int) for n in (
+        "lonstep", "do_zm_tracers", "do_zm_rad", "do_fixed_water", "include_secondary_gases", "do_precip_albedo",
+        "num_precip", "use_dyofyr", "solday", "dt_rad_avg")] + [(n, C.c_double) for n in (
+            "h2o_lower_limit", "temp_lower_limit", "temp_upper_limit", "co2ppmv", "o3_val", "fixed_water",
+            "fixed_water_pres", "fixed_water_lat", "ch4_val", "n2o_val", "o2_val", "cfc11_val", "cfc12_val",
+            "cfc22_val", "ccl4_val", "precip_albedo", "precip_lat", "slowdown_rad", "obliq", "solr_cnst", "solrad",
+            "equinox_day")]
+
+
+def run_params(**kw) -> RunParams:
+    """The reference's namelist defaults (rrtmg_run_params_default), then ``kw``."""
+    p = RunParams()
+    rc = load_library().rrtmg_run_params_default(C.byref(p))
+    if rc != RRTMG_OK:
+        raise RRTMGError(rc, "rrtmg_run_params_default")
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise AttributeError(f"rrtmg_run_params has no field {k}")
+        setattr(p, k, v)
+    return p
+
+
+# run_rrtmg arguments: inputs and outputs in the order of rrtmg_run_dev / rrtmg_run_c.
+RUN_IN = ("lat", "lon", "p_full", "p_half", "z_full", "z_half", "t", "q", "o3", "t_surf_rad", "albedo", "rrtm_precip")
+RUN_OUT = ("tdt", "coszen", "flux_sw", "flux_lw", "t_half", "tdt_rad", "tdt_sw", "tdt_lw", "olr", "isr")
 
 
 class RRTMGError(RuntimeError):
@@ -75,6 +108,7 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
     lib.rrtmg_gpu_launch_count.restype = C.c_longlong
     lib.rrtmg_gpu_reserve.argtypes = [vp, C.c_int, C.c_int]
     lib.rrtmg_gpu_sync_status.argtypes = [vp, vp]
+    lib.rrtmg_run_params_default.argtypes = [C.POINTER(RunParams)]
     _lib = lib
     return lib
 
@@ -302,6 +336,35 @@ class RRTMG:
             g("coszen"), C.c_double(adjes), C.c_int(dyofyr), C.c_double(scon), C.c_int(0), C.c_int(0),
             C.c_int(0), None, None, None, None, None, None, None, None, None, g("tauaer"), g("ssaaer"),
             g("asmaer"), None, o("swuflx"), o("swdflx"), o("swhr"), o("swuflxc"), o("swdflxc"), o("swhrc"))
+        self._check(rc)
+
+
+    def run_rrtmg(self, prm, slab, seconds, days, days_per_year=365, tdt=None, diagnostics=True):
+        """run_rrtmg on host arrays (rrtmg_run_c).  ``slab`` holds the GCM
+        arrays of :data:`RUN_IN` as C-ordered (sk[+1], sj, si) / (sj, si)
+        numpy arrays (Fortran (si, sj, sk) order); returns the outputs of
+        :data:`RUN_OUT` (tdt = the given tendency plus the radiative one)."""
+        si, sj, sk = slab.si, slab.sj, slab.sk
+        shapes = {"tdt": (sk, sj, si), "coszen": (sj, si), "flux_sw": (sj, si), "flux_lw": (sj, si),
+                  "t_half": (sk + 1, sj, si), "tdt_rad": (sk, sj, si), "tdt_sw": (sk, sj, si),
+                  "tdt_lw": (sk, sj, si), "olr": (sj, si), "isr": (sj, si)}
+        keep = RUN_OUT if diagnostics else ("tdt", "coszen", "flux_sw", "flux_lw")
+        out = {k: np.empty(shapes[k]) for k in keep}
+        out["tdt"] = np.array(slab.tdt if tdt is None else tdt, dtype=np.float64, order="C", copy=True)
+        ins = [_host(getattr(slab, k)) for k in RUN_IN]
+        rc = self.lib.rrtmg_run_c(self._h, C.byref(prm), C.c_int(si), C.c_int(sj), C.c_int(sk), C.c_int(seconds),
+                                  C.c_int(days), C.c_int(days_per_year), *[_hp(a) for a in ins],
+                                  *[_hp(out.get(k)) for k in RUN_OUT])
+        self._check(rc)
+        return out
+
+    def run_rrtmg_dev(self, stream, prm, si, sj, sk, seconds, days, days_per_year, d, out):
+        """run_rrtmg on device arrays (rrtmg_run_dev): ``d`` maps the names
+        of :data:`RUN_IN`, ``out`` those of :data:`RUN_OUT` to CUDA tensors
+        (missing optional ones are NULL)."""
+        rc = self.lib.rrtmg_run_dev(self._h, C.c_void_p(stream or 0), C.byref(prm), C.c_int(si), C.c_int(sj),
+                                    C.c_int(sk), C.c_int(seconds), C.c_int(days), C.c_int(days_per_year),
+                                    *[_dptr(d.get(k)) for k in RUN_IN], *[_dptr(out.get(k)) for k in RUN_OUT])
         self._check(rc)
 
 

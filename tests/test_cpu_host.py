@@ -16,14 +16,14 @@ ROOT = Path(__file__).resolve().parent.parent
 
 
 def header_symbols():
-    text = (ROOT / "include" / "rrtmg_gpu.h").read_text()
+    text = "".join(p.read_text() for p in sorted((ROOT / "include").glob("*.h")))
     return sorted(set(re.findall(r"^(?:int|const char\*|long long)\s+(rrtmg_\w+)\(", text, re.M)))
 
 
 def test_library_exports_every_declared_symbol():
     lib = R.load_library()
     syms = header_symbols()
-    assert len(syms) == 18
+    assert len(syms) == 21
     assert set(syms) == set(R.EXPORTED)
     for s in syms:
         assert hasattr(lib, s), s
@@ -44,6 +44,11 @@ def test_host_only_error_paths(tmp_path):
     assert lib.rrtmg_gpu_set_precision(None, 0) == R.RRTMG_ERR_ARG
     assert lib.rrtmg_gpu_finalize(None) == R.RRTMG_ERR_ARG
     assert lib.rrtmg_gpu_reserve(None, 10, 40) == R.RRTMG_ERR_ARG
+    # run_rrtmg entry points: defaults are host-only; a null handle is refused before any CUDA call
+    p = R.run_params(lonstep=2)
+    assert p.lonstep == 2 and p.dt_rad_avg == 86400 and p.solr_cnst == 1368.22
+    assert lib.rrtmg_run_params_default(None) == R.RRTMG_ERR_ARG
+    assert lib.rrtmg_run_c(None, C.byref(p), 8, 2, 10, 0, 0, 365, *([None] * 22)) == R.RRTMG_ERR_ARG
 
 
 def test_generator_configurations():

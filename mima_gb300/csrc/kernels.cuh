@@ -71,21 +71,27 @@ __device__ __forceinline__ double seg_sum(double v) {
 
 __device__ __forceinline__ bool bad(double x) { return !isfinite(x); }
 
-// FP64 g-point sums of the FP32-split solvers.  Each lane of a warp holds one
-// (column, g-point) value per level; NB value streams are staged in FP32 in
-// shared memory for up to W levels, then every lane forms one (column, level)
-// sum in FP64 -- NG conversions and NG adds (or multiply-adds with the
-// per-g weights `wt`, the SW incident fluxes) in g order -- and hands it to
-// the store.  Per lane and level that is about 2 NG / W FP64 operations,
-// against a conversion and log2(W) adds for a butterfly on every lane.
-// Rows are 33 floats wide so that the staging stores and the per-lane row
-// reads are free of bank conflicts.  All lanes of the warp must call put/next/
-// flush uniformly (the level loops are warp-uniform).
+// g-point sums of the FP32-split solvers, to FP64 accuracy without FP64
+// arithmetic per g-point.  Each lane of a warp holds one (column, g-point)
+// value per level; NB value streams are staged in FP32 in shared memory for
+// up to W levels, then every lane forms one (column, level) sum and hands it
+// to the store as a double.  The sum runs in g order as a compensated FP32
+// sum: Knuth's TwoSum splits every addition into the rounded sum and its exact
+// rounding error, and with per-g weights `wt` (the SW incident fluxes, FP32)
+// an FMA recovers the exact error of each product; the errors accumulate in a
+// second float and the result is (double)s + (double)c, within about
+// NG^2 u^2 (u = 2^-24) of the exact sum -- the accuracy of the FP64 sum it
+// replaces, at two FP64 operations per sum instead of 2 NG (GB300's FP64 rate
+// is a small fraction of its FP32 rate).  Explicitly rounded intrinsics keep
+// the compiler from contracting the error terms.  Rows are 33 floats wide so
+// that the staging stores and the per-lane row reads are free of bank
+// conflicts.  All lanes of the warp must call put/next/flush uniformly (the
+// level loops are warp-uniform).
 constexpr int kRow = 33;
 template <int W, int NG, int NB, bool WEIGHTED>
 struct GSum {
   float* buf;          // this warp's [NB][W][kRow]
-  const double* wt;    // this warp's [32] per-lane weights (WEIGHTED only)
+  const float* wt;     // this warp's [32] per-lane weights (WEIGHTED only)
   int lane, n, first, dir;
   int nb;              // streams in use (<= NB)
   __device__ __forceinline__ void put(int b, float v) { buf[(b * W + n) * kRow + lane] = v; }
@@ -98,15 +104,21 @@ struct GSum {
       for (int b = 0; b < NB; ++b) {
         if (b >= nb) break;
         const float* row = buf + (b * W + sl) * kRow + cs * W;
-        double acc = 0.0;
-#pragma unroll
+        float s = 0.f, c = 0.f;
+#pragma unroll 2
         for (int g = 0; g < NG; ++g) {
-          if constexpr (WEIGHTED)
-            acc = fma(wt[cs * W + g], (double)row[g], acc);
-          else
-            acc += (double)row[g];
+          float x = row[g];
+          if constexpr (WEIGHTED) {
+            const float wf = wt[cs * W + g];
+            const float pr = __fmul_rn(wf, x);
+            c = __fadd_rn(c, __fmaf_rn(wf, x, -pr));
+            x = pr;
+          }
+          const float t = __fadd_rn(s, x), bv = __fsub_rn(t, s);
+          c = __fadd_rn(c, __fadd_rn(__fsub_rn(s, __fsub_rn(t, bv)), __fsub_rn(x, bv)));
+          s = t;
         }
-        st(b, first + dir * sl, cs, acc);
+        st(b, first + dir * sl, cs, (double)s + (double)c);
       }
     }
     __syncwarp();
@@ -368,8 +380,8 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
   double* bdp = bd + (size_t)(B - 1) * (nlay + 1) * N + col;
   double* bup = bu + (size_t)(B - 1) * (nlay + 1) * N + col;
   double* bdup = IDRV ? bdu + (size_t)(B - 1) * (nlay + 1) * N + col : nullptr;
-  // Split path: FP64 band sums through the warp's staging buffers; the
-  // summing lane of column sub-index cs writes column wcol0 + cs.
+  // Split path: band sums through the warp's staging buffers; the summing
+  // lane of column sub-index cs writes column wcol0 + cs.
   const int wib = threadIdx.x >> 5;
   const int wcol0 = blk * CPB + (wib * 32) / W;
   GSum<W, NG, 2, false> gs{sbuf + (SPLIT ? wib * 2 * W * kRow : 0), nullptr, (int)(threadIdx.x & 31), 0, nlay - 1, -1,
@@ -940,7 +952,7 @@ __device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, dou
                                         const R* __restrict__ tab, const double* __restrict__ tab64,
                                         const R* __restrict__ exptbl, double* __restrict__ su,
                                         double* __restrict__ sd, int ncol, int nlay, bool analytic, int blk, float* sbuf,
-                                        double* swt) {
+                                        float* swt) {
   constexpr bool SPLIT = sizeof(R) == 4;
   constexpr int NG = sw_ng(B);
   constexpr int W = pow2ceil(NG);
@@ -1029,13 +1041,13 @@ __device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, dou
   // (:141-149) as soon as each level's upward reflectances are known.
   double* sup = su + (size_t)(B - 16) * (nlay + 1) * N + col;
   double* sdp = sd + (size_t)(B - 16) * (nlay + 1) * N + col;
-  // Split path: FP64 incident-flux-weighted band sums through the warp's
-  // staging buffers (levels surface first); the summing lane of column
-  // sub-index cs writes column wcol0 + cs.
+  // Split path: incident-flux-weighted band sums through the warp's staging
+  // buffers (levels surface first); the summing lane of column sub-index cs
+  // writes column wcol0 + cs.
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int wcol0 = blk * CPB + (wib * 32) / W;
   GSum<W, NG, 2, true> gs{sbuf + (SPLIT ? wib * 2 * W * kRow : 0), swt + (SPLIT ? wib * 32 : 0), lane, 0, 0, 1, 2};
-  if constexpr (SPLIT) swt[wib * 32 + lane] = active ? zincflx : 0.0;
+  if constexpr (SPLIT) swt[wib * 32 + lane] = active ? (float)zincflx : 0.f;
   auto store = [&](int b, int lev, int cs, double v) {
     const int cc = wcol0 + cs;
     if (cc < ncol) (b == 0 ? su : sd)[((size_t)(B - 16) * (nlay + 1) + lev) * N + cc] = v;
@@ -1087,7 +1099,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_SW_MINB :
                                                            const R* __restrict__ exptbl, double* su, double* sd,
                                                            int ncol, int nlay, int analytic) {
   __shared__ float sbuf[sizeof(R) == 4 ? kGSumFloats : 1];
-  __shared__ double swt[sizeof(R) == 4 ? kBlock : 1];
+  __shared__ float swt[sizeof(R) == 4 ? kBlock : 1];
   int blk = blockIdx.x, band = 0;
   for (; band < kSwBands; ++band) {
     const int nb = lw_blocks_for_band(c_sw.band[band].ngpad, ncol);

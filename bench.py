@@ -195,11 +195,21 @@ def run_reference(args):
 
 
 def graph_step(torch, r, stream, atm, d, olw, osw, precision):
-    """Capture one LW+SW step (device entry points) in a CUDA graph."""
+    """Capture one LW+SW step (device entry points) in a CUDA graph: the LW
+    call on `stream`, the SW call forked onto a second stream and joined
+    back, so that the two independent calls overlap on the GPU."""
     r.set_precision(precision)
-    call = lambda: (r.rrtmg_lw_dev(stream.cuda_stream, atm.ncol, atm.nlay, 0, 0, d, olw),
-                    r.rrtmg_sw_dev(stream.cuda_stream, atm.ncol, atm.nlay, 0, 0, d, osw, atm.adjes,
-                                   atm.dyofyr, atm.scon))
+    side = torch.cuda.Stream(device=stream.device)
+
+    def call():
+        fork = torch.cuda.Event()
+        fork.record(stream)
+        side.wait_event(fork)
+        r.rrtmg_lw_dev(stream.cuda_stream, atm.ncol, atm.nlay, 0, 0, d, olw)
+        r.rrtmg_sw_dev(side.cuda_stream, atm.ncol, atm.nlay, 0, 0, d, osw, atm.adjes, atm.dyofyr, atm.scon)
+        join = torch.cuda.Event()
+        join.record(side)
+        stream.wait_event(join)
     with torch.cuda.stream(stream):
         call()  # first call outside capture (workspace already reserved)
     stream.synchronize()

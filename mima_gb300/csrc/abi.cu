@@ -43,6 +43,7 @@ struct rrtmg_gpu_state {
   HostTables host;
   double *lw_tab64 = nullptr, *sw_tab64 = nullptr, *lw_exp64 = nullptr, *lw_tfn64 = nullptr, *sw_exp64 = nullptr;
   double *totplnk = nullptr, *totplnkderiv = nullptr;
+  float *totplnk32 = nullptr, *totplnkderiv32 = nullptr;  // FP32 copies (split prep)
   float *lw_tab32 = nullptr, *sw_tab32 = nullptr, *lw_exp32 = nullptr, *lw_tfn32 = nullptr, *sw_exp32 = nullptr;
   unsigned* flags = nullptr;
   DevBuf lw_ws, sw_ws, adj_ws;
@@ -198,7 +199,7 @@ int lw_enqueue(rrtmg_gpu_state* h, cudaStream_t s, void* base, int ncol, int nla
   const int nb = lw_gpoint_blocks(h->host.lw, ncol);
   if (h->precision == RRTMG_PREC_SPLIT) {
     const LwWorkT<float> w32 = work_as<float>(w);
-    launch_lw_prep_split(in, w32, h->totplnk, h->totplnkderiv, ncol, nlay, idrv, h->flags, s);
+    launch_lw_prep_split(in, w32, h->totplnk32, h->totplnkderiv32, ncol, nlay, idrv, h->flags, s);
     mark(h, 0, 1, s);
     launch_lw_gpoint_split(prep_of(w32), in.emis, in.tauaer, h->lw_tab32, h->lw_exp32, h->lw_tfn32, w.bu, w.bd,
                            w.bdu, ncol, nlay, idrv, nb, h->analytic, s);
@@ -209,8 +210,12 @@ int lw_enqueue(rrtmg_gpu_state* h, cudaStream_t s, void* base, int ncol, int nla
                           ncol, nlay, idrv, nb, h->analytic, s);
   }
   mark(h, 0, 2, s);
-  launch_lw_finalize(w.bu, w.bd, w.bdu, in.plev, ncol, nlay, idrv, uflx, dflx, hr, uflxc, dflxc, hrc, duflx_dt,
-                     duflxc_dt, s);
+  if (h->precision == RRTMG_PREC_SPLIT)
+    launch_lw_finalize_split(w.bu, w.bd, w.bdu, in.plev, ncol, nlay, idrv, uflx, dflx, hr, uflxc, dflxc, hrc,
+                             duflx_dt, duflxc_dt, s);
+  else
+    launch_lw_finalize(w.bu, w.bd, w.bdu, in.plev, ncol, nlay, idrv, uflx, dflx, hr, uflxc, dflxc, hrc, duflx_dt,
+                       duflxc_dt, s);
   mark(h, 0, 3, s);
   h->launches += 4;
   cudaError_t e = cudaGetLastError();
@@ -259,7 +264,11 @@ int sw_enqueue(rrtmg_gpu_state* h, cudaStream_t s, void* base, int ncol, int nla
                           h->analytic, s);
   }
   mark(h, 1, 2, s);
-  launch_sw_finalize(w.su, w.sd, in.plev, in.coszen, ncol, nlay, swuflx, swdflx, swhr, swuflxc, swdflxc, swhrc, s);
+  if (h->precision == RRTMG_PREC_SPLIT)
+    launch_sw_finalize_split(w.su, w.sd, in.plev, in.coszen, ncol, nlay, swuflx, swdflx, swhr, swuflxc, swdflxc,
+                             swhrc, s);
+  else
+    launch_sw_finalize(w.su, w.sd, in.plev, in.coszen, ncol, nlay, swuflx, swdflx, swhr, swuflxc, swdflxc, swhrc, s);
   mark(h, 1, 3, s);
   h->launches += 4;
   cudaError_t e = cudaGetLastError();
@@ -492,6 +501,8 @@ int rrtmg_gpu_init(double cpdair, const char* table_blob, int device, rrtmg_gpu_
   if (e == cudaSuccess) e = upload(&h->sw_exp64, h->host.sw_exp);
   if (e == cudaSuccess) e = upload(&h->totplnk, h->host.totplnk);
   if (e == cudaSuccess) e = upload(&h->totplnkderiv, h->host.totplnkderiv);
+  if (e == cudaSuccess) e = upload(&h->totplnk32, to_f32(h->host.totplnk));
+  if (e == cudaSuccess) e = upload(&h->totplnkderiv32, to_f32(h->host.totplnkderiv));
   if (e == cudaSuccess) e = upload(&h->lw_tab32, to_f32(h->host.lw_tab));
   if (e == cudaSuccess) e = upload(&h->sw_tab32, to_f32(h->host.sw_tab));
   if (e == cudaSuccess) e = upload(&h->lw_exp32, to_f32(h->host.lw_exp));
@@ -519,6 +530,7 @@ int rrtmg_gpu_finalize(rrtmg_gpu_handle h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->stream2) cudaStreamSynchronize(h->stream2);
   void* ptrs[] = {h->lw_tab64, h->sw_tab64, h->lw_exp64, h->lw_tfn64, h->sw_exp64, h->totplnk, h->totplnkderiv,
+                  h->totplnk32, h->totplnkderiv32,
                   h->lw_tab32, h->sw_tab32, h->lw_exp32, h->lw_tfn32, h->sw_exp32, h->flags, h->lw_ws.p,
                   h->sw_ws.p, h->adj_ws.p, h->hio[0].p, h->hio[1].p, h->hws[0].p, h->hws[1].p, h->run_ws.p,
                   h->run_io.p};

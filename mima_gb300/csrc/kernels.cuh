@@ -144,114 +144,123 @@ constexpr int kGSumFloats = (kBlock / 32) * 2 * 16 * kRow;
 // in the reference's layer loop.
 // totplnk / totplnkderiv: device tables [(ind-1) + 181*(band-1)].
 // ---------------------------------------------------------------------------
+// F is both the storage and the arithmetic type: the FP64 path computes in
+// double, the FP32-split path (whose prepared fields are FP32) in float, with
+// the same expressions in the same order; the inputs are validated in double.
 template <class F>
-__global__ void __launch_bounds__(128) lw_prep_layer_kernel(LwIn in, LwWorkT<F> w, const double* __restrict__ totplnk,
+__global__ void __launch_bounds__(128) lw_prep_layer_kernel(LwIn in, LwWorkT<F> w, const F* __restrict__ totplnk,
                                                             int ncol, int nlay, unsigned* __restrict__ flags) {
+  using T = F;
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= ncol) return;
   const int l = blockIdx.y + 1;
   const LwConst& C = c_lw;
-  const double amd = 28.9660, amw = 18.0160, amdw = 1.607793, amdo = 0.603428;
-  const double stpfac = 296. / 1013.;
+  const T amd = (T)28.9660, amw = (T)18.0160, amdw = (T)1.607793, amdo = (T)0.603428;
+  const T stpfac = (T)(296. / 1013.);
   const size_t N = (size_t)ncol;
   const size_t fstride = (size_t)nlay * N;
   auto A = [&](const double* p, int ll) { return __ldg(p + (size_t)col + N * (size_t)(ll - 1)); };
   auto P = [&](int ind, int b) { return __ldg(totplnk + (ind - 1) + 181 * (b - 1)); };
   (void)amw;
   unsigned flag = 0;
-  const double pz_prev = A(in.plev, l);
-  const double pavel = A(in.play, l), tavel = A(in.tlay, l);
-  const double pz_l = A(in.plev, l + 1), tz_l = A(in.tlev, l + 1);
-  const double h2o = A(in.h2o, l);
-  if (bad(pavel) || bad(tavel) || bad(pz_l) || bad(tz_l) || bad(h2o) || pavel <= 0. || tavel <= 0. ||
-      h2o < 0. || h2o >= 1. || pz_l < 0.)
-    flag = 1;
-  double wk1 = (h2o / (1. - h2o)) * amdw;
-  double wk2 = A(in.co2, l);
-  double wk3 = A(in.o3, l) * amdo;
-  double wk4 = in.n2o ? A(in.n2o, l) : 0.0;
-  double wk6 = in.ch4 ? A(in.ch4, l) : 0.0;
-  double wk7 = in.o2 ? A(in.o2, l) : 0.0;
-  double amm = (1. - wk1) * amd + wk1 * amw;
-  double coldry = (pz_prev - pz_l) * 1.e3 * C.avogad / (1.e2 * C.grav * amm * (1. + wk1));
-  double summol = 0.0;
+  {
+    const double pv = A(in.play, l), tv = A(in.tlay, l), pz = A(in.plev, l + 1), tz = A(in.tlev, l + 1);
+    const double q = A(in.h2o, l);
+    if (bad(pv) || bad(tv) || bad(pz) || bad(tz) || bad(q) || pv <= 0. || tv <= 0. || q < 0. || q >= 1. || pz < 0.)
+      flag = 1;
+  }
+  const T pz_prev = (T)A(in.plev, l);
+  const T pavel = (T)A(in.play, l), tavel = (T)A(in.tlay, l);
+  const T pz_l = (T)A(in.plev, l + 1), tz_l = (T)A(in.tlev, l + 1);
+  const T h2o = (T)A(in.h2o, l);
+  T wk1 = (h2o / ((T)1. - h2o)) * amdw;
+  T wk2 = (T)A(in.co2, l);
+  T wk3 = (T)A(in.o3, l) * amdo;
+  T wk4 = in.n2o ? (T)A(in.n2o, l) : (T)0.0;
+  T wk6 = in.ch4 ? (T)A(in.ch4, l) : (T)0.0;
+  T wk7 = in.o2 ? (T)A(in.o2, l) : (T)0.0;
+  T amm = ((T)1. - wk1) * amd + wk1 * amw;
+  T coldry = (pz_prev - pz_l) * (T)1.e3 * (T)C.avogad / ((T)1.e2 * (T)C.grav * amm * ((T)1. + wk1));
+  T summol = (T)0.0;
   summol = summol + wk2;
   summol = summol + wk3;
   summol = summol + wk4;
-  summol = summol + 0.0;
+  summol = summol + (T)0.0;
   summol = summol + wk6;
   summol = summol + wk7;
-  double wbrodl = coldry * (1. - summol);
+  T wbrodl = coldry * ((T)1. - summol);
   wk1 = coldry * wk1;
   wk2 = coldry * wk2;
   wk3 = coldry * wk3;
   wk4 = coldry * wk4;
-  double wk5 = coldry * 0.0;
+  T wk5 = coldry * (T)0.0;
   wk6 = coldry * wk6;
   wk7 = coldry * wk7;
   // column sums of inatm (amttl, wvttl), formed in layer order by the column kernel
   w.colsum[(size_t)(l - 1) * N + col] = coldry;
   w.colsum[fstride + (size_t)(l - 1) * N + col] = wk1;
-  double wx1 = in.ccl4 ? coldry * A(in.ccl4, l) * 1.e-20 : coldry * 0.0 * 1.e-20;
-  double wx2 = in.cfc11 ? coldry * A(in.cfc11, l) * 1.e-20 : coldry * 0.0 * 1.e-20;
-  double wx3 = in.cfc12 ? coldry * A(in.cfc12, l) * 1.e-20 : coldry * 0.0 * 1.e-20;
-  double wx4 = in.cfc22 ? coldry * A(in.cfc22, l) * 1.e-20 : coldry * 0.0 * 1.e-20;
+  const T e20 = (T)1.e-20;
+  T wx1 = in.ccl4 ? coldry * (T)A(in.ccl4, l) * e20 : coldry * (T)0.0 * e20;
+  T wx2 = in.cfc11 ? coldry * (T)A(in.cfc11, l) * e20 : coldry * (T)0.0 * e20;
+  T wx3 = in.cfc12 ? coldry * (T)A(in.cfc12, l) * e20 : coldry * (T)0.0 * e20;
+  T wx4 = in.cfc22 ? coldry * (T)A(in.cfc22, l) * e20 : coldry * (T)0.0 * e20;
 
   // Planck functions of the layer and its upper interface
-  const int indlay = clampi((int)(tavel - 159.), 1, 180);
-  const double tlayfrac = tavel - 159. - (double)indlay;
-  const int indlev = clampi((int)(tz_l - 159.), 1, 180);
-  const double tlevfrac = tz_l - 159. - (double)indlev;
+  const int indlay = clampi((int)(tavel - (T)159.), 1, 180);
+  const T tlayfrac = tavel - (T)159. - (T)indlay;
+  const int indlev = clampi((int)(tz_l - (T)159.), 1, 180);
+  const T tlevfrac = tz_l - (T)159. - (T)indlev;
   for (int b = 1; b <= 16; ++b) {
-    double dbdtlev = P(indlev + 1, b) - P(indlev, b);
-    double dbdtlay = P(indlay + 1, b) - P(indlay, b);
+    T dbdtlev = P(indlev + 1, b) - P(indlev, b);
+    T dbdtlay = P(indlay + 1, b) - P(indlay, b);
     w.planklay[((size_t)(b - 1) * nlay + (l - 1)) * N + col] = P(indlay, b) + tlayfrac * dbdtlay;
     w.planklev[((size_t)(b - 1) * (nlay + 1) + l) * N + col] = P(indlev, b) + tlevfrac * dbdtlev;
   }
 
-  const double plog = log(pavel);
-  const int jp = clampi((int)(36. - 5 * (plog + 0.04)), 1, 58);
+  const T plog = log(pavel);
+  const int jp = clampi((int)((T)36. - (T)5 * (plog + (T)0.04)), 1, 58);
   const int jp1 = jp + 1;
-  const double fp = 5. * (C.preflog[jp - 1] - plog);
-  const int jt = clampi((int)(3. + (tavel - C.tref[jp - 1]) / 15.), 1, 4);
-  const double ft = ((tavel - C.tref[jp - 1]) / 15.) - (double)(jt - 3);
-  const int jt1 = clampi((int)(3. + (tavel - C.tref[jp1 - 1]) / 15.), 1, 4);
-  const double ft1 = ((tavel - C.tref[jp1 - 1]) / 15.) - (double)(jt1 - 3);
-  const double water = wk1 / coldry;
-  const double scalefac = pavel * stpfac / tavel;
-  double forfac, forfrac, selffac, selffrac = 0.0, minorfrac, factor;
+  const T fp = (T)5. * ((T)C.preflog[jp - 1] - plog);
+  const int jt = clampi((int)((T)3. + (tavel - (T)C.tref[jp - 1]) / (T)15.), 1, 4);
+  const T ft = ((tavel - (T)C.tref[jp - 1]) / (T)15.) - (T)(jt - 3);
+  const int jt1 = clampi((int)((T)3. + (tavel - (T)C.tref[jp1 - 1]) / (T)15.), 1, 4);
+  const T ft1 = ((tavel - (T)C.tref[jp1 - 1]) / (T)15.) - (T)(jt1 - 3);
+  const T water = wk1 / coldry;
+  const T scalefac = pavel * stpfac / tavel;
+  T forfac, forfrac, selffac, selffrac = (T)0.0, minorfrac, factor;
   int indfor, indself = 1, indminor;
-  if (plog > 4.56) {
-    forfac = scalefac / (1. + water);
-    factor = (332.0 - tavel) / 36.0;
+  if (plog > (T)4.56) {
+    forfac = scalefac / ((T)1. + water);
+    factor = ((T)332.0 - tavel) / (T)36.0;
     indfor = min(2, max(1, (int)factor));
-    forfrac = factor - (double)indfor;
+    forfrac = factor - (T)indfor;
     selffac = water * forfac;
-    factor = (tavel - 188.0) / 7.2;
+    factor = (tavel - (T)188.0) / (T)7.2;
     indself = min(9, max(1, (int)factor - 7));
-    selffrac = factor - (double)(indself + 7);
+    selffrac = factor - (T)(indself + 7);
   } else {
-    forfac = scalefac / (1. + water);
-    factor = (tavel - 188.0) / 36.0;
+    forfac = scalefac / ((T)1. + water);
+    factor = (tavel - (T)188.0) / (T)36.0;
     indfor = 3;
-    forfrac = factor - 1.0;
+    forfrac = factor - (T)1.0;
     selffac = water * forfac;
   }
-  const double scaleminor = pavel / tavel;
-  const double scaleminorn2 = (pavel / tavel) * (wbrodl / (coldry + wk1));
-  factor = (tavel - 180.8) / 7.2;
+  const T scaleminor = pavel / tavel;
+  const T scaleminorn2 = (pavel / tavel) * (wbrodl / (coldry + wk1));
+  factor = (tavel - (T)180.8) / (T)7.2;
   indminor = min(18, max(1, (int)factor));
-  minorfrac = factor - (double)indminor;
+  minorfrac = factor - (T)indminor;
 
-  double colh2o = 1.e-20 * wk1, colco2 = 1.e-20 * wk2, colo3 = 1.e-20 * wk3, coln2o = 1.e-20 * wk4;
-  double colco = 1.e-20 * wk5, colch4 = 1.e-20 * wk6, colo2 = 1.e-20 * wk7;
-  if (colco2 == 0.) colco2 = 1.e-32 * coldry;
-  if (colo3 == 0.) colo3 = 1.e-32 * coldry;
-  if (coln2o == 0.) coln2o = 1.e-32 * coldry;
-  if (colco == 0.) colco = 1.e-32 * coldry;
-  if (colch4 == 0.) colch4 = 1.e-32 * coldry;
-  const double colbrd = 1.e-20 * wbrodl;
-  const double compfp = 1. - fp;
+  T colh2o = e20 * wk1, colco2 = e20 * wk2, colo3 = e20 * wk3, coln2o = e20 * wk4;
+  T colco = e20 * wk5, colch4 = e20 * wk6, colo2 = e20 * wk7;
+  const T e32 = (T)1.e-32;
+  if (colco2 == (T)0.) colco2 = e32 * coldry;
+  if (colo3 == (T)0.) colo3 = e32 * coldry;
+  if (coln2o == (T)0.) coln2o = e32 * coldry;
+  if (colco == (T)0.) colco = e32 * coldry;
+  if (colch4 == (T)0.) colch4 = e32 * coldry;
+  const T colbrd = e20 * wbrodl;
+  const T compfp = (T)1. - fp;
   const size_t o = (size_t)(l - 1) * N + col;
   F* f = w.f;
   f[LF_PAVEL * fstride + o] = pavel;
@@ -265,9 +274,9 @@ __global__ void __launch_bounds__(128) lw_prep_layer_kernel(LwIn in, LwWorkT<F> 
   f[LF_COLO2 * fstride + o] = colo2;
   f[LF_COLBRD * fstride + o] = colbrd;
   f[LF_FAC10 * fstride + o] = compfp * ft;
-  f[LF_FAC00 * fstride + o] = compfp * (1. - ft);
+  f[LF_FAC00 * fstride + o] = compfp * ((T)1. - ft);
   f[LF_FAC11 * fstride + o] = fp * ft1;
-  f[LF_FAC01 * fstride + o] = fp * (1. - ft1);
+  f[LF_FAC01 * fstride + o] = fp * ((T)1. - ft1);
   f[LF_SELFFAC * fstride + o] = colh2o * selffac;
   f[LF_SELFFRAC * fstride + o] = selffrac;
   f[LF_FORFAC * fstride + o] = colh2o * forfac;
@@ -284,31 +293,34 @@ __global__ void __launch_bounds__(128) lw_prep_layer_kernel(LwIn in, LwWorkT<F> 
 }
 
 template <class F>
-__global__ void __launch_bounds__(128) lw_prep_column_kernel(LwIn in, LwWorkT<F> w, const double* __restrict__ totplnk,
-                                                             const double* __restrict__ totplnkderiv, int ncol,
+__global__ void __launch_bounds__(128) lw_prep_column_kernel(LwIn in, LwWorkT<F> w, const F* __restrict__ totplnk,
+                                                             const F* __restrict__ totplnkderiv, int ncol,
                                                              int nlay, int idrv, unsigned* __restrict__ flags) {
+  using T = F;
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= ncol) return;
   const LwConst& C = c_lw;
-  const double amd = 28.9660, amw = 18.0160;
+  const T amd = (T)28.9660, amw = (T)18.0160;
   const size_t N = (size_t)ncol;
   const size_t fstride = (size_t)nlay * N;
   auto A = [&](const double* p, int l) { return __ldg(p + (size_t)col + N * (size_t)(l - 1)); };
   auto P = [&](int ind, int b) { return __ldg(totplnk + (ind - 1) + 181 * (b - 1)); };
   auto PD = [&](int ind, int b) { return __ldg(totplnkderiv + (ind - 1) + 181 * (b - 1)); };
   unsigned flag = 0;
-
-  const double tbound = __ldg(in.tsfc + col);
-  const double pz0 = A(in.plev, 1);
-  const double tz0 = A(in.tlev, 1);
-  if (bad(tbound) || bad(pz0) || bad(tz0) || tbound <= 0. || tz0 <= 0.) flag = 1;
-  const int indbound = clampi((int)(tbound - 159.), 1, 180);
-  const double tbndfrac = tbound - 159. - (double)indbound;
-  const int indlev0 = clampi((int)(tz0 - 159.), 1, 180);
-  const double t0frac = tz0 - 159. - (double)indlev0;
+  {
+    const double tb = __ldg(in.tsfc + col), pz = A(in.plev, 1), tz = A(in.tlev, 1);
+    if (bad(tb) || bad(pz) || bad(tz) || tb <= 0. || tz <= 0.) flag = 1;
+  }
+  const T tbound = (T)__ldg(in.tsfc + col);
+  const T pz0 = (T)A(in.plev, 1);
+  const T tz0 = (T)A(in.tlev, 1);
+  const int indbound = clampi((int)(tbound - (T)159.), 1, 180);
+  const T tbndfrac = tbound - (T)159. - (T)indbound;
+  const int indlev0 = clampi((int)(tz0 - (T)159.), 1, 180);
+  const T t0frac = tz0 - (T)159. - (T)indlev0;
   for (int b = 1; b <= 16; ++b) {
-    double semiss = in.emis ? __ldg(in.emis + col + N * (b - 1)) : 1.0;
-    double dbdtlev = P(indbound + 1, b) - P(indbound, b);
+    T semiss = in.emis ? (T)__ldg(in.emis + col + N * (b - 1)) : (T)1.0;
+    T dbdtlev = P(indbound + 1, b) - P(indbound, b);
     w.plankbnd[(b - 1) * N + col] = semiss * (P(indbound, b) + tbndfrac * dbdtlev);
     dbdtlev = P(indlev0 + 1, b) - P(indlev0, b);
     w.planklev[((size_t)(b - 1) * (nlay + 1)) * N + col] = P(indlev0, b) + t0frac * dbdtlev;
@@ -317,29 +329,33 @@ __global__ void __launch_bounds__(128) lw_prep_column_kernel(LwIn in, LwWorkT<F>
       w.dplankbnd[(b - 1) * N + col] = semiss * (PD(indbound, b) + tbndfrac * dbdtlev);
     }
   }
-  double amttl = 0.0, wvttl = 0.0;
+  T amttl = (T)0.0, wvttl = (T)0.0;
   int laytrop = 0;
   for (int l = 1; l <= nlay; ++l) {
-    const double coldry = w.colsum[(size_t)(l - 1) * N + col];
-    const double wk1 = w.colsum[fstride + (size_t)(l - 1) * N + col];
+    const T coldry = (T)w.colsum[(size_t)(l - 1) * N + col];
+    const T wk1 = (T)w.colsum[fstride + (size_t)(l - 1) * N + col];
     amttl = amttl + coldry + wk1;
     wvttl = wvttl + wk1;
-    if (log(A(in.play, l)) > 4.56) laytrop = laytrop + 1;
+    // the same test on the same value as the layer kernel's branch
+    if (log((T)A(in.play, l)) > (T)4.56) laytrop = laytrop + 1;
   }
   w.laytrop[col] = laytrop;
-  const double wvsh = (amw * wvttl) / (amd * amttl);
-  const double pwvcm = wvsh * (1.e3 * pz0) / (1.e2 * C.grav);
-  const double a0[16] = {1.66, 1.55, 1.58, 1.66, 1.54, 1.454, 1.89, 1.33, 1.668, 1.66, 1.66, 1.66, 1.66, 1.66, 1.66, 1.66};
-  const double a1[16] = {0.00, 0.25, 0.22, 0.00, 0.13, 0.446, -0.10, 0.40, -0.006, 0, 0, 0, 0, 0, 0, 0};
-  const double a2[16] = {0.00, -12.0, -11.7, 0.00, -0.72, -0.243, 0.19, -0.062, 0.414, 0, 0, 0, 0, 0, 0, 0};
+  const T wvsh = (amw * wvttl) / (amd * amttl);
+  const T pwvcm = wvsh * ((T)1.e3 * pz0) / ((T)1.e2 * (T)C.grav);
+  const T a0[16] = {(T)1.66, (T)1.55, (T)1.58, (T)1.66, (T)1.54, (T)1.454, (T)1.89, (T)1.33,
+                    (T)1.668, (T)1.66, (T)1.66, (T)1.66, (T)1.66, (T)1.66, (T)1.66, (T)1.66};
+  const T a1[16] = {(T)0.00, (T)0.25, (T)0.22, (T)0.00, (T)0.13, (T)0.446, (T)-0.10, (T)0.40,
+                    (T)-0.006, 0, 0, 0, 0, 0, 0, 0};
+  const T a2[16] = {(T)0.00, (T)-12.0, (T)-11.7, (T)0.00, (T)-0.72, (T)-0.243, (T)0.19, (T)-0.062,
+                    (T)0.414, 0, 0, 0, 0, 0, 0, 0};
   for (int b = 1; b <= 16; ++b) {
-    double s;
+    T s;
     if (b == 1 || b == 4 || b >= 10) {
-      s = 1.66;
+      s = (T)1.66;
     } else {
       s = a0[b - 1] + a1[b - 1] * exp(a2[b - 1] * pwvcm);
-      if (s > 1.80) s = 1.80;
-      if (s < 1.50) s = 1.50;
+      if (s > (T)1.80) s = (T)1.80;
+      if (s < (T)1.50) s = (T)1.50;
     }
     w.secdiff[(b - 1) * N + col] = s;
   }
@@ -615,34 +631,37 @@ __host__ __device__ constexpr bool sw_upper_source(int b) { return b == 16 || b 
 #ifdef RRTMG_DEFINE_COLUMN_KERNELS
 // Two launches as for LW: one thread per (column, layer), then one thread per
 // column for laytrop and the solar-source layer of every band.
+// F is the storage and the arithmetic type, as for the LW prep kernels.
 template <class F>
 __global__ void __launch_bounds__(128) sw_prep_layer_kernel(SwIn in, SwWorkT<F> w, int ncol, int nlay,
                                                             unsigned* __restrict__ flags) {
+  using T = F;
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= ncol) return;
   const int l = blockIdx.y + 1;
   const SwConst& C = c_sw;
-  const double amd = 28.9660, amw = 18.0160, amdw = 1.607793, amdo = 0.603428;
-  const double stpfac = 296. / 1013.;
+  const T amd = (T)28.9660, amw = (T)18.0160, amdw = (T)1.607793, amdo = (T)0.603428;
+  const T stpfac = (T)(296. / 1013.);
   const size_t N = (size_t)ncol;
   const size_t fstride = (size_t)nlay * N;
   auto A = [&](const double* p, int ll) { return __ldg(p + (size_t)col + N * (size_t)(ll - 1)); };
   unsigned flag = 0;
-  const double pz_prev = A(in.plev, l);
-  const double pavel = A(in.play, l), tavel = A(in.tlay, l);
-  const double pz_l = A(in.plev, l + 1);
-  const double h2o = A(in.h2o, l);
-  if (bad(pavel) || bad(tavel) || bad(pz_l) || bad(h2o) || pavel <= 0. || tavel <= 0. || h2o < 0. || h2o >= 1. ||
-      pz_l < 0.)
-    flag = 1;
-  double wk1 = (h2o / (1. - h2o)) * amdw;
-  double wk2 = A(in.co2, l);
-  double wk3 = A(in.o3, l) * amdo;
-  double wk4 = in.n2o ? A(in.n2o, l) : 0.0;
-  double wk6 = in.ch4 ? A(in.ch4, l) : 0.0;
-  double wk7 = in.o2 ? A(in.o2, l) : 0.0;
-  double amm = (1. - wk1) * amd + wk1 * amw;
-  double coldry = (pz_prev - pz_l) * 1.e3 * C.avogad / (1.e2 * C.grav * amm * (1. + wk1));
+  {
+    const double pv = A(in.play, l), tv = A(in.tlay, l), pz = A(in.plev, l + 1), q = A(in.h2o, l);
+    if (bad(pv) || bad(tv) || bad(pz) || bad(q) || pv <= 0. || tv <= 0. || q < 0. || q >= 1. || pz < 0.) flag = 1;
+  }
+  const T pz_prev = (T)A(in.plev, l);
+  const T pavel = (T)A(in.play, l), tavel = (T)A(in.tlay, l);
+  const T pz_l = (T)A(in.plev, l + 1);
+  const T h2o = (T)A(in.h2o, l);
+  T wk1 = (h2o / ((T)1. - h2o)) * amdw;
+  T wk2 = (T)A(in.co2, l);
+  T wk3 = (T)A(in.o3, l) * amdo;
+  T wk4 = in.n2o ? (T)A(in.n2o, l) : (T)0.0;
+  T wk6 = in.ch4 ? (T)A(in.ch4, l) : (T)0.0;
+  T wk7 = in.o2 ? (T)A(in.o2, l) : (T)0.0;
+  T amm = ((T)1. - wk1) * amd + wk1 * amw;
+  T coldry = (pz_prev - pz_l) * (T)1.e3 * (T)C.avogad / ((T)1.e2 * (T)C.grav * amm * ((T)1. + wk1));
   wk1 = coldry * wk1;
   wk2 = coldry * wk2;
   wk3 = coldry * wk3;
@@ -650,45 +669,46 @@ __global__ void __launch_bounds__(128) sw_prep_layer_kernel(SwIn in, SwWorkT<F> 
   wk6 = coldry * wk6;
   wk7 = coldry * wk7;
 
-  const double plog = log(pavel);
-  const int jp = clampi((int)(36. - 5 * (plog + 0.04)), 1, 58);
+  const T plog = log(pavel);
+  const int jp = clampi((int)((T)36. - (T)5 * (plog + (T)0.04)), 1, 58);
   const int jp1 = jp + 1;
-  const double fp = 5. * (C.preflog[jp - 1] - plog);
-  const int jt = clampi((int)(3. + (tavel - C.tref[jp - 1]) / 15.), 1, 4);
-  const double ft = ((tavel - C.tref[jp - 1]) / 15.) - (double)(jt - 3);
-  const int jt1 = clampi((int)(3. + (tavel - C.tref[jp1 - 1]) / 15.), 1, 4);
-  const double ft1 = ((tavel - C.tref[jp1 - 1]) / 15.) - (double)(jt1 - 3);
-  const double water = wk1 / coldry;
-  const double scalefac = pavel * stpfac / tavel;
-  double forfac, forfrac, selffac, selffrac, factor;
+  const T fp = (T)5. * ((T)C.preflog[jp - 1] - plog);
+  const int jt = clampi((int)((T)3. + (tavel - (T)C.tref[jp - 1]) / (T)15.), 1, 4);
+  const T ft = ((tavel - (T)C.tref[jp - 1]) / (T)15.) - (T)(jt - 3);
+  const int jt1 = clampi((int)((T)3. + (tavel - (T)C.tref[jp1 - 1]) / (T)15.), 1, 4);
+  const T ft1 = ((tavel - (T)C.tref[jp1 - 1]) / (T)15.) - (T)(jt1 - 3);
+  const T water = wk1 / coldry;
+  const T scalefac = pavel * stpfac / tavel;
+  T forfac, forfrac, selffac, selffrac, factor;
   int indfor, indself;
-  const bool lower = plog > 4.56;
+  const bool lower = plog > (T)4.56;
   if (lower) {
-    forfac = scalefac / (1. + water);
-    factor = (332.0 - tavel) / 36.0;
+    forfac = scalefac / ((T)1. + water);
+    factor = ((T)332.0 - tavel) / (T)36.0;
     indfor = min(2, max(1, (int)factor));
-    forfrac = factor - (double)indfor;
+    forfrac = factor - (T)indfor;
     selffac = water * forfac;
-    factor = (tavel - 188.0) / 7.2;
+    factor = (tavel - (T)188.0) / (T)7.2;
     indself = min(9, max(1, (int)factor - 7));
-    selffrac = factor - (double)(indself + 7);
+    selffrac = factor - (T)(indself + 7);
   } else {
-    forfac = scalefac / (1. + water);
-    factor = (tavel - 188.0) / 36.0;
+    forfac = scalefac / ((T)1. + water);
+    factor = (tavel - (T)188.0) / (T)36.0;
     indfor = 3;
-    forfrac = factor - 1.0;
-    selffac = 0.;
-    selffrac = 0.;
+    forfrac = factor - (T)1.0;
+    selffac = (T)0.;
+    selffrac = (T)0.;
     indself = 0;
   }
-  double colh2o = 1.e-20 * wk1, colco2 = 1.e-20 * wk2, colo3 = 1.e-20 * wk3, coln2o = 1.e-20 * wk4;
-  double colch4 = 1.e-20 * wk6, colo2 = 1.e-20 * wk7;
-  const double colmol = 1.e-20 * coldry + colh2o;
-  if (colco2 == 0.) colco2 = 1.e-32 * coldry;
-  if (coln2o == 0.) coln2o = 1.e-32 * coldry;
-  if (colch4 == 0.) colch4 = 1.e-32 * coldry;
-  if (colo2 == 0.) colo2 = 1.e-32 * coldry;
-  const double compfp = 1. - fp;
+  const T e20 = (T)1.e-20, e32 = (T)1.e-32;
+  T colh2o = e20 * wk1, colco2 = e20 * wk2, colo3 = e20 * wk3, coln2o = e20 * wk4;
+  T colch4 = e20 * wk6, colo2 = e20 * wk7;
+  const T colmol = e20 * coldry + colh2o;
+  if (colco2 == (T)0.) colco2 = e32 * coldry;
+  if (coln2o == (T)0.) coln2o = e32 * coldry;
+  if (colch4 == (T)0.) colch4 = e32 * coldry;
+  if (colo2 == (T)0.) colo2 = e32 * coldry;
+  const T compfp = (T)1. - fp;
   const size_t o = (size_t)(l - 1) * N + col;
   F* f = w.f;
   f[SF_COLH2O * fstride + o] = colh2o;
@@ -698,9 +718,9 @@ __global__ void __launch_bounds__(128) sw_prep_layer_kernel(SwIn in, SwWorkT<F> 
   f[SF_COLO2 * fstride + o] = colo2;
   f[SF_COLMOL * fstride + o] = colmol;
   f[SF_FAC10 * fstride + o] = compfp * ft;
-  f[SF_FAC00 * fstride + o] = compfp * (1. - ft);
+  f[SF_FAC00 * fstride + o] = compfp * ((T)1. - ft);
   f[SF_FAC11 * fstride + o] = fp * ft1;
-  f[SF_FAC01 * fstride + o] = fp * (1. - ft1);
+  f[SF_FAC01 * fstride + o] = fp * ((T)1. - ft1);
   f[SF_SELFFAC * fstride + o] = selffac;
   f[SF_SELFFRAC * fstride + o] = selffrac;
   f[SF_FORFAC * fstride + o] = forfac;
@@ -721,7 +741,7 @@ __global__ void __launch_bounds__(128) sw_prep_column_kernel(SwIn in, SwWorkT<F>
   if (bad(__ldg(in.coszen + col))) flag = 1;
   int laytrop = 0;
   for (int l = 1; l <= nlay; ++l)
-    if (log(A(in.play, l)) > 4.56) laytrop = laytrop + 1;
+    if (log((F)A(in.play, l)) > (F)4.56) laytrop = laytrop + 1;  // the layer kernel's test, in F
   w.laytrop[col] = laytrop;
   // Solar-source layer of every band, as the taumol16..29 loops select it:
   //   upper-loop bands (16, 17, 27, 28, 29): laysolfr = nlay, replaced by the

@@ -33,7 +33,7 @@ void launch_lw_prep(const LwIn& in, const LwWork& w, const double* totplnk, cons
                                                                   flags);
 }
 
-void launch_lw_prep_split(const LwIn& in, const LwWorkT<float>& w, const double* totplnk, const double* totplnkderiv,
+void launch_lw_prep_split(const LwIn& in, const LwWorkT<float>& w, const float* totplnk, const float* totplnkderiv,
                           int ncol, int nlay, int idrv, unsigned* flags, cudaStream_t s) {
   const dim3 g((ncol + 127) / 128, nlay);
   lw_prep_layer_kernel<float><<<g, 128, 0, s>>>(in, w, totplnk, ncol, nlay, flags);

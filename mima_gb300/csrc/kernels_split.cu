@@ -1,10 +1,15 @@
 // FP32-split instantiation of the g-point solvers: gas optics, transmittance
 // lookups and per-g recursions in FP32 (multiply-add contraction allowed);
-// g-point sums, band partials and everything downstream stay FP64.
+// g-point sums to FP64 accuracy, band partials and the finalize kernels below
+// in FP64.
 #include "kernels.cuh"
 #include "launch.h"
 
 namespace rrtmg {
+
+// LW band weight of the broadband sums: wtdiff * delwave(band) * fluxfac
+// (rrtmg_lw_rtrnmr.f90:720-746), folded into one factor.
+__constant__ double c_lw_bandw[kLwBands];
 
 cudaError_t upload_constants_split(const LwConst& lw, const SwConst& sw) {
   cudaError_t e = cudaMemcpyToSymbol(c_lw, &lw, sizeof(LwConst));
@@ -12,7 +17,135 @@ cudaError_t upload_constants_split(const LwConst& lw, const SwConst& sw) {
   const LwConstF f = make_lwconstf(lw);
   e = cudaMemcpyToSymbol(c_lwf, &f, sizeof(LwConstF));
   if (e != cudaSuccess) return e;
+  double bw[kLwBands];
+  for (int b = 0; b < kLwBands; ++b) bw[b] = 0.5 * lw.band[b].delwave * lw.fluxfac;
+  e = cudaMemcpyToSymbol(c_lw_bandw, bw, sizeof(bw));
+  if (e != cudaSuccess) return e;
   return cudaMemcpyToSymbol(c_sw, &sw, sizeof(SwConst));
+}
+
+// ---------------------------------------------------------------------------
+// Finalize kernels of the split path.  The same fluxes and heating rates as
+// the FP64 finalize kernels (rrtmg_lw_rtrnmr.f90:720-776; rrtmg_sw_rad
+// .nomcica.f90:712-726 with MiMA's zero top layer), from the FP64 band
+// partials, in FP64, with fewer FP64 operations: a thread walks kLevChunk
+// consecutive levels of one column, so every level's band sums are formed
+// once and the level below is carried for the heating rate, and the LW band
+// weights multiply-add into the sums.
+// ---------------------------------------------------------------------------
+constexpr int kLevChunk = 8;
+
+__global__ void __launch_bounds__(128) lw_finalize_split_kernel(const double* __restrict__ bu,
+                                                                const double* __restrict__ bd,
+                                                                const double* __restrict__ bdu,
+                                                                const double* __restrict__ plev, int ncol, int nlay,
+                                                                int idrv, double* uflx, double* dflx, double* hr,
+                                                                double* uflxc, double* dflxc, double* hrc,
+                                                                double* duflx_dt, double* duflxc_dt) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncol) return;
+  const int lev0 = blockIdx.y * kLevChunk, lev1 = min(nlay, lev0 + kLevChunk - 1);
+  const size_t N = (size_t)ncol, bs = (size_t)(nlay + 1) * N;
+  auto sums = [&](const double* a, const double* b, int lv, double& x, double& y) {
+    x = 0.0;
+    y = 0.0;
+    const size_t o = (size_t)lv * N + col;
+#pragma unroll
+    for (int k = 0; k < kLwBands; ++k) {
+      x = fma(__ldg(a + k * bs + o), c_lw_bandw[k], x);
+      y = fma(__ldg(b + k * bs + o), c_lw_bandw[k], y);
+    }
+  };
+  auto sum1 = [&](const double* a, int lv) {
+    double x = 0.0;
+    const size_t o = (size_t)lv * N + col;
+#pragma unroll
+    for (int k = 0; k < kLwBands; ++k) x = fma(__ldg(a + k * bs + o), c_lw_bandw[k], x);
+    return x;
+  };
+  double tu0 = 0.0, td0 = 0.0;
+  if (lev0 >= 1) sums(bu, bd, lev0 - 1, tu0, td0);
+  for (int lev = lev0; lev <= lev1; ++lev) {
+    double tu, td;
+    sums(bu, bd, lev, tu, td);
+    const size_t oo = (size_t)lev * N + col;
+    uflx[oo] = tu;
+    dflx[oo] = td;
+    uflxc[oo] = tu;
+    dflxc[oo] = td;
+    if (idrv == 1) {
+      const double tdu = sum1(bdu, lev);
+      if (duflx_dt) duflx_dt[oo] = tdu;
+      if (duflxc_dt) duflxc_dt[oo] = tdu;
+    }
+    if (lev >= 1) {
+      const double h = c_lw.heatfac * ((tu0 - td0) - (tu - td)) / (__ldg(plev + oo - N) - __ldg(plev + oo));
+      hr[oo - N] = h;
+      hrc[oo - N] = h;
+    }
+    tu0 = tu;
+    td0 = td;
+  }
+}
+
+__global__ void __launch_bounds__(128) sw_finalize_split_kernel(const double* __restrict__ su,
+                                                                const double* __restrict__ sd,
+                                                                const double* __restrict__ plev,
+                                                                const double* __restrict__ coszen, int ncol, int nlay,
+                                                                double* swuflx, double* swdflx, double* swhr,
+                                                                double* swuflxc, double* swdflxc, double* swhrc) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncol) return;
+  const int lev0 = blockIdx.y * kLevChunk, lev1 = min(nlay, lev0 + kLevChunk - 1);
+  const size_t N = (size_t)ncol, bs = (size_t)(nlay + 1) * N;
+  const bool lit = __ldg(coszen + col) >= 1.e-10;
+  auto sums = [&](int lv, double& fu, double& fd) {
+    fu = 0.0;
+    fd = 0.0;
+    if (!lit) return;
+    const size_t o = (size_t)lv * N + col;
+#pragma unroll
+    for (int k = 0; k < kSwBands; ++k) {
+      fu = fu + __ldg(su + k * bs + o);
+      fd = fd + __ldg(sd + k * bs + o);
+    }
+  };
+  double fu0 = 0.0, fd0 = 0.0;
+  if (lev0 >= 1) sums(lev0 - 1, fu0, fd0);
+  for (int lev = lev0; lev <= lev1; ++lev) {
+    double fu, fd;
+    sums(lev, fu, fd);
+    const size_t oo = (size_t)lev * N + col;
+    swuflx[oo] = fu;
+    swdflx[oo] = fd;
+    swuflxc[oo] = fu;
+    swdflxc[oo] = fd;
+    if (lev >= 1) {
+      double h = 0.0;
+      if (lit && lev < nlay)
+        h = ((fd - fu) - (fd0 - fu0)) * (c_sw.heatfac / (__ldg(plev + oo - N) - __ldg(plev + oo)));
+      swhr[oo - N] = h;
+      swhrc[oo - N] = h;
+    }
+    fu0 = fu;
+    fd0 = fd;
+  }
+}
+
+void launch_lw_finalize_split(const double* bu, const double* bd, const double* bdu, const double* plev, int ncol,
+                              int nlay, int idrv, double* uflx, double* dflx, double* hr, double* uflxc,
+                              double* dflxc, double* hrc, double* duflx_dt, double* duflxc_dt, cudaStream_t s) {
+  const dim3 g((ncol + 127) / 128, (nlay + 1 + kLevChunk - 1) / kLevChunk);
+  lw_finalize_split_kernel<<<g, 128, 0, s>>>(bu, bd, bdu, plev, ncol, nlay, idrv, uflx, dflx, hr, uflxc, dflxc, hrc,
+                                             duflx_dt, duflxc_dt);
+}
+
+void launch_sw_finalize_split(const double* su, const double* sd, const double* plev, const double* coszen, int ncol,
+                              int nlay, double* swuflx, double* swdflx, double* swhr, double* swuflxc,
+                              double* swdflxc, double* swhrc, cudaStream_t s) {
+  const dim3 g((ncol + 127) / 128, (nlay + 1 + kLevChunk - 1) / kLevChunk);
+  sw_finalize_split_kernel<<<g, 128, 0, s>>>(su, sd, plev, coszen, ncol, nlay, swuflx, swdflx, swhr, swuflxc, swdflxc,
+                                             swhrc);
 }
 
 void launch_lw_gpoint_split(const LwPrepT<float>& p, const double* emis, const double* tauaer, const float* tab,

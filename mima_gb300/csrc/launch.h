@@ -26,7 +26,7 @@ void launch_lw_finalize(const double* bu, const double* bd, const double* bdu, c
                         double* duflx_dt, double* duflxc_dt, cudaStream_t s);
 void launch_sw_prep(const SwIn& in, const SwWork& w, int ncol, int nlay, unsigned* flags, cudaStream_t s);
 // Prep for the FP32-split solvers: the same FP64 arithmetic, fields stored as float.
-void launch_lw_prep_split(const LwIn& in, const LwWorkT<float>& w, const double* totplnk, const double* totplnkderiv,
+void launch_lw_prep_split(const LwIn& in, const LwWorkT<float>& w, const float* totplnk, const float* totplnkderiv,
                           int ncol, int nlay, int idrv, unsigned* flags, cudaStream_t s);
 void launch_sw_prep_split(const SwIn& in, const SwWorkT<float>& w, int ncol, int nlay, unsigned* flags,
                           cudaStream_t s);
@@ -35,6 +35,13 @@ void launch_sw_gpoint_fp64(const SwPrep& p, const SwIn& in, double adjflux, int 
 void launch_sw_finalize(const double* su, const double* sd, const double* plev, const double* coszen, int ncol,
                         int nlay, double* swuflx, double* swdflx, double* swhr, double* swuflxc, double* swdflxc,
                         double* swhrc, cudaStream_t s);
+// Split-path finalize: the same outputs with fewer FP64 operations (kernels_split.cu).
+void launch_lw_finalize_split(const double* bu, const double* bd, const double* bdu, const double* plev, int ncol,
+                              int nlay, int idrv, double* uflx, double* dflx, double* hr, double* uflxc,
+                              double* dflxc, double* hrc, double* duflx_dt, double* duflxc_dt, cudaStream_t s);
+void launch_sw_finalize_split(const double* su, const double* sd, const double* plev, const double* coszen, int ncol,
+                              int nlay, double* swuflx, double* swdflx, double* swhr, double* swuflxc,
+                              double* swdflxc, double* swhrc, cudaStream_t s);
 
 // FP32-split translation unit.
 void launch_lw_gpoint_split(const LwPrepT<float>& p, const double* emis, const double* tauaer, const float* tab,

@@ -431,7 +431,7 @@ int adj_run(rrtmg_gpu_state* h, cudaStream_t s, int ncol, int nlay, const LwIn& 
                                 (float*)lw.pbnd_t, (float*)lw.secdiff, lw.dsec, lw.hs, lw.part};
     const AdjSwWorkT<float> s32{sw.idx, sw.laytrop, sw.laysolfr, (float*)sw.fv, (float*)sw.ft, (float*)sw.fq, sw.hs,
                                 sw.part};
-    launch_adj_lw_split(lin, l32, h->totplnk, h->lw_tab32, cot, nseed_lw, ncol, nlay, nbl, s);
+    launch_adj_lw_split(lin, l32, h->totplnk32, h->lw_tab32, cot, nseed_lw, ncol, nlay, nbl, s);
     launch_adj_sw_split(sin, s32, adjflux, iaer, h->sw_tab32, h->sw_tab64, cot, nseed_sw, ncol, nlay, nbs, s);
   } else {
     launch_adj_lw(lin, lw, h->totplnk, h->lw_tab64, cot, nseed_lw, ncol, nlay, nbl, s);

@@ -38,30 +38,36 @@ using D2 = Dual<double>;
 // (rrtmg_lw_rtrnmr.f90:271-279) with d secdiff / d q of every layer through
 // the column water vapour pwvcm.
 // ---------------------------------------------------------------------------
+// F is the checkpoint type and the arithmetic type (duals Dual<F>): the FP64
+// adjoint computes in double, the split adjoint in float, with the same
+// expressions in the same order.
 template <class F>
-__global__ void __launch_bounds__(128) adj_lw_prep_kernel(LwIn in, AdjLwWorkT<F> w, const double* __restrict__ totplnk,
+__global__ void __launch_bounds__(128) adj_lw_prep_kernel(LwIn in, AdjLwWorkT<F> w, const F* __restrict__ totplnk,
                                                           int ncol, int nlay) {
+  using T = F;
+  using DT = Dual<T>;
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= ncol) return;
   const LwConst& C = c_lw;
-  const double amd = 28.9660, amw = 18.0160, amdw = 1.607793, amdo = 0.603428;
-  const double stpfac = 296. / 1013.;
+  const T amd = (T)28.9660, amw = (T)18.0160, amdw = (T)1.607793, amdo = (T)0.603428;
+  const T stpfac = (T)(296. / 1013.);
+  const T one = (T)1., e20 = (T)1.e-20, e32 = (T)1.e-32, zero = (T)0.;
   const size_t N = (size_t)ncol;
   const size_t fstride = (size_t)nlay * N;
-  auto A = [&](const double* p, int l) { return __ldg(p + (size_t)col + N * (size_t)(l - 1)); };
+  auto A = [&](const double* p, int l) { return (T)__ldg(p + (size_t)col + N * (size_t)(l - 1)); };
   auto P = [&](int ind, int b) { return __ldg(totplnk + (ind - 1) + 181 * (b - 1)); };
 
-  const double tbound = __ldg(in.tsfc + col);
-  double pz_prev = A(in.plev, 1);
-  const double pz0 = pz_prev;
-  const double tz0 = A(in.tlev, 1);
-  const int indbound = clampi((int)(tbound - 159.), 1, 180);
-  const double tbndfrac = tbound - 159. - (double)indbound;
-  const int indlev0 = clampi((int)(tz0 - 159.), 1, 180);
-  const double t0frac = tz0 - 159. - (double)indlev0;
+  const T tbound = (T)__ldg(in.tsfc + col);
+  T pz_prev = A(in.plev, 1);
+  const T pz0 = pz_prev;
+  const T tz0 = A(in.tlev, 1);
+  const int indbound = clampi((int)(tbound - (T)159.), 1, 180);
+  const T tbndfrac = tbound - (T)159. - (T)indbound;
+  const int indlev0 = clampi((int)(tz0 - (T)159.), 1, 180);
+  const T t0frac = tz0 - (T)159. - (T)indlev0;
   for (int b = 1; b <= 16; ++b) {
-    const double semiss = in.emis ? __ldg(in.emis + col + N * (b - 1)) : 1.0;
-    double slope = P(indbound + 1, b) - P(indbound, b);
+    const T semiss = in.emis ? (T)__ldg(in.emis + col + N * (b - 1)) : one;
+    T slope = P(indbound + 1, b) - P(indbound, b);
     w.pbnd_v[(b - 1) * N + col] = semiss * (P(indbound, b) + tbndfrac * slope);
     w.pbnd_t[(b - 1) * N + col] = semiss * slope;
     slope = P(indlev0 + 1, b) - P(indlev0, b);
@@ -69,103 +75,103 @@ __global__ void __launch_bounds__(128) adj_lw_prep_kernel(LwIn in, AdjLwWorkT<F>
     w.plev_t[((size_t)(b - 1) * (nlay + 1)) * N + col] = slope;
   }
 
-  double amttl = 0.0, wvttl = 0.0;
+  T amttl = zero, wvttl = zero;
   int laytrop = 0;
   for (int l = 1; l <= nlay; ++l) {
-    const double pavel = A(in.play, l);
-    const D2 tavel(A(in.tlay, l), 1.0, 0.0);
-    const double pz_l = A(in.plev, l + 1), tz_l = A(in.tlev, l + 1);
-    const D2 h2o(A(in.h2o, l), 0.0, 1.0);
-    D2 wk1 = (h2o / (1. - h2o)) * amdw;
-    const double wk2 = A(in.co2, l);
-    const double wk3 = A(in.o3, l) * amdo;
-    const double wk4 = in.n2o ? A(in.n2o, l) : 0.0;
-    const double wk6 = in.ch4 ? A(in.ch4, l) : 0.0;
-    const double wk7 = in.o2 ? A(in.o2, l) : 0.0;
-    const D2 amm = (1. - wk1) * amd + wk1 * amw;
-    const D2 coldry = (pz_prev - pz_l) * 1.e3 * C.avogad / (1.e2 * C.grav * amm * (1. + wk1));
-    const double summol = wk2 + wk3 + wk4 + 0.0 + wk6 + wk7;
-    const D2 wbrodl = coldry * (1. - summol);
+    const T pavel = A(in.play, l);
+    const DT tavel(A(in.tlay, l), one, zero);
+    const T pz_l = A(in.plev, l + 1), tz_l = A(in.tlev, l + 1);
+    const DT h2o(A(in.h2o, l), zero, one);
+    DT wk1 = (h2o / (one - h2o)) * amdw;
+    const T wk2 = A(in.co2, l);
+    const T wk3 = A(in.o3, l) * amdo;
+    const T wk4 = in.n2o ? A(in.n2o, l) : zero;
+    const T wk6 = in.ch4 ? A(in.ch4, l) : zero;
+    const T wk7 = in.o2 ? A(in.o2, l) : zero;
+    const DT amm = (one - wk1) * amd + wk1 * amw;
+    const DT coldry = (pz_prev - pz_l) * (T)1.e3 * (T)C.avogad / ((T)1.e2 * (T)C.grav * amm * (one + wk1));
+    const T summol = wk2 + wk3 + wk4 + zero + wk6 + wk7;
+    const DT wbrodl = coldry * (one - summol);
     wk1 = coldry * wk1;
-    const D2 cwk2 = coldry * wk2, cwk3 = coldry * wk3, cwk4 = coldry * wk4, cwk6 = coldry * wk6,
+    const DT cwk2 = coldry * wk2, cwk3 = coldry * wk3, cwk4 = coldry * wk4, cwk6 = coldry * wk6,
              cwk7 = coldry * wk7;
     amttl = amttl + coldry.v + wk1.v;
     wvttl = wvttl + wk1.v;
     // d(wvttl)/dq_l and d(amttl)/dq_l, for d pwvcm / dq_l below
     w.dsec[(size_t)(l - 1) * N + col] = wk1.q;
     w.dsec[fstride + (size_t)(l - 1) * N + col] = coldry.q + wk1.q;
-    const D2 wx1 = in.ccl4 ? coldry * A(in.ccl4, l) * 1.e-20 : coldry * 0.0;
-    const D2 wx2 = in.cfc11 ? coldry * A(in.cfc11, l) * 1.e-20 : coldry * 0.0;
-    const D2 wx3 = in.cfc12 ? coldry * A(in.cfc12, l) * 1.e-20 : coldry * 0.0;
-    const D2 wx4 = in.cfc22 ? coldry * A(in.cfc22, l) * 1.e-20 : coldry * 0.0;
+    const DT wx1 = in.ccl4 ? coldry * A(in.ccl4, l) * e20 : coldry * zero;
+    const DT wx2 = in.cfc11 ? coldry * A(in.cfc11, l) * e20 : coldry * zero;
+    const DT wx3 = in.cfc12 ? coldry * A(in.cfc12, l) * e20 : coldry * zero;
+    const DT wx4 = in.cfc22 ? coldry * A(in.cfc22, l) * e20 : coldry * zero;
 
-    const int indlay = clampi((int)(tavel.v - 159.), 1, 180);
-    const double tlayfrac = tavel.v - 159. - (double)indlay;
-    const int indlev = clampi((int)(tz_l - 159.), 1, 180);
-    const double tlevfrac = tz_l - 159. - (double)indlev;
+    const int indlay = clampi((int)(tavel.v - (T)159.), 1, 180);
+    const T tlayfrac = tavel.v - (T)159. - (T)indlay;
+    const int indlev = clampi((int)(tz_l - (T)159.), 1, 180);
+    const T tlevfrac = tz_l - (T)159. - (T)indlev;
     for (int b = 1; b <= 16; ++b) {
-      const double sl = P(indlay + 1, b) - P(indlay, b);
-      const double sv = P(indlev + 1, b) - P(indlev, b);
+      const T sl = P(indlay + 1, b) - P(indlay, b);
+      const T sv = P(indlev + 1, b) - P(indlev, b);
       w.play_v[((size_t)(b - 1) * nlay + (l - 1)) * N + col] = P(indlay, b) + tlayfrac * sl;
       w.play_t[((size_t)(b - 1) * nlay + (l - 1)) * N + col] = sl;
       w.plev_v[((size_t)(b - 1) * (nlay + 1) + l) * N + col] = P(indlev, b) + tlevfrac * sv;
       w.plev_t[((size_t)(b - 1) * (nlay + 1) + l) * N + col] = sv;
     }
 
-    const double plog = log(pavel);
-    const int jp = clampi((int)(36. - 5 * (plog + 0.04)), 1, 58);
+    const T plog = log(pavel);
+    const int jp = clampi((int)((T)36. - (T)5 * (plog + (T)0.04)), 1, 58);
     const int jp1 = jp + 1;
-    const double fp = 5. * (C.preflog[jp - 1] - plog);
-    const int jt = clampi((int)(3. + (tavel.v - C.tref[jp - 1]) / 15.), 1, 4);
-    const D2 ft = ((tavel - C.tref[jp - 1]) / 15.) - (double)(jt - 3);
-    const int jt1 = clampi((int)(3. + (tavel.v - C.tref[jp1 - 1]) / 15.), 1, 4);
-    const D2 ft1 = ((tavel - C.tref[jp1 - 1]) / 15.) - (double)(jt1 - 3);
-    const D2 water = wk1 / coldry;
-    const D2 scalefac = (pavel * stpfac) / tavel;
-    D2 forfac, forfrac, selffac, selffrac(0.0), minorfrac, factor;
+    const T fp = (T)5. * ((T)C.preflog[jp - 1] - plog);
+    const int jt = clampi((int)((T)3. + (tavel.v - (T)C.tref[jp - 1]) / (T)15.), 1, 4);
+    const DT ft = ((tavel - (T)C.tref[jp - 1]) / (T)15.) - (T)(jt - 3);
+    const int jt1 = clampi((int)((T)3. + (tavel.v - (T)C.tref[jp1 - 1]) / (T)15.), 1, 4);
+    const DT ft1 = ((tavel - (T)C.tref[jp1 - 1]) / (T)15.) - (T)(jt1 - 3);
+    const DT water = wk1 / coldry;
+    const DT scalefac = (pavel * stpfac) / tavel;
+    DT forfac, forfrac, selffac, selffrac(zero), minorfrac, factor;
     int indfor, indself = 1, indminor;
-    if (plog > 4.56) {
+    if (plog > (T)4.56) {
       laytrop = laytrop + 1;
-      forfac = scalefac / (1. + water);
-      factor = (332.0 - tavel) / 36.0;
+      forfac = scalefac / (one + water);
+      factor = ((T)332.0 - tavel) / (T)36.0;
       indfor = min(2, max(1, (int)factor.v));
-      forfrac = factor - (double)indfor;
+      forfrac = factor - (T)indfor;
       selffac = water * forfac;
-      factor = (tavel - 188.0) / 7.2;
+      factor = (tavel - (T)188.0) / (T)7.2;
       indself = min(9, max(1, (int)factor.v - 7));
-      selffrac = factor - (double)(indself + 7);
+      selffrac = factor - (T)(indself + 7);
     } else {
-      forfac = scalefac / (1. + water);
-      factor = (tavel - 188.0) / 36.0;
+      forfac = scalefac / (one + water);
+      factor = (tavel - (T)188.0) / (T)36.0;
       indfor = 3;
-      forfrac = factor - 1.0;
+      forfrac = factor - one;
       selffac = water * forfac;
     }
-    const D2 scaleminor = pavel / tavel;
-    const D2 scaleminorn2 = (pavel / tavel) * (wbrodl / (coldry + wk1));
-    factor = (tavel - 180.8) / 7.2;
+    const DT scaleminor = pavel / tavel;
+    const DT scaleminorn2 = (pavel / tavel) * (wbrodl / (coldry + wk1));
+    factor = (tavel - (T)180.8) / (T)7.2;
     indminor = min(18, max(1, (int)factor.v));
-    minorfrac = factor - (double)indminor;
+    minorfrac = factor - (T)indminor;
 
-    const D2 colh2o = 1.e-20 * wk1;
-    D2 colco2 = 1.e-20 * cwk2, colo3 = 1.e-20 * cwk3, coln2o = 1.e-20 * cwk4;
-    D2 colco = coldry * 0.0, colch4 = 1.e-20 * cwk6;
-    const D2 colo2 = 1.e-20 * cwk7;
-    if (colco2.v == 0.) colco2 = 1.e-32 * coldry;
-    if (colo3.v == 0.) colo3 = 1.e-32 * coldry;
-    if (coln2o.v == 0.) coln2o = 1.e-32 * coldry;
-    if (colco.v == 0.) colco = 1.e-32 * coldry;
-    if (colch4.v == 0.) colch4 = 1.e-32 * coldry;
-    const D2 colbrd = 1.e-20 * wbrodl;
-    const double compfp = 1. - fp;
+    const DT colh2o = e20 * wk1;
+    DT colco2 = e20 * cwk2, colo3 = e20 * cwk3, coln2o = e20 * cwk4;
+    DT colco = coldry * zero, colch4 = e20 * cwk6;
+    const DT colo2 = e20 * cwk7;
+    if (colco2.v == zero) colco2 = e32 * coldry;
+    if (colo3.v == zero) colo3 = e32 * coldry;
+    if (coln2o.v == zero) coln2o = e32 * coldry;
+    if (colco.v == zero) colco = e32 * coldry;
+    if (colch4.v == zero) colch4 = e32 * coldry;
+    const DT colbrd = e20 * wbrodl;
+    const T compfp = one - fp;
     const size_t o = (size_t)(l - 1) * N + col;
-    auto put = [&](int fld, const D2& x) {
+    auto put = [&](int fld, const DT& x) {
       const size_t i = (size_t)fld * fstride + o;
       w.fv[i] = x.v;
       w.ft[i] = x.t;
       w.fq[i] = x.q;
     };
-    put(LF_PAVEL, D2(pavel));
+    put(LF_PAVEL, DT(pavel));
     put(LF_COLDRY, coldry);
     put(LF_COLH2O, colh2o);
     put(LF_COLCO2, colco2);
@@ -176,9 +182,9 @@ __global__ void __launch_bounds__(128) adj_lw_prep_kernel(LwIn in, AdjLwWorkT<F>
     put(LF_COLO2, colo2);
     put(LF_COLBRD, colbrd);
     put(LF_FAC10, compfp * ft);
-    put(LF_FAC00, compfp * (1. - ft));
+    put(LF_FAC00, compfp * (one - ft));
     put(LF_FAC11, fp * ft1);
-    put(LF_FAC01, fp * (1. - ft1));
+    put(LF_FAC01, fp * (one - ft1));
     put(LF_SELFFAC, colh2o * selffac);
     put(LF_SELFFRAC, selffrac);
     put(LF_FORFAC, colh2o * forfac);
@@ -191,29 +197,32 @@ __global__ void __launch_bounds__(128) adj_lw_prep_kernel(LwIn in, AdjLwWorkT<F>
     put(LF_WX3, wx3);
     put(LF_WX4, wx4);
     w.idx[o] = pack_idx(jp, jt, jt1, indself, indfor, indminor);
-    w.hs[o] = C.heatfac / (pz_prev - pz_l);
+    w.hs[o] = (double)((T)C.heatfac / (pz_prev - pz_l));
     pz_prev = pz_l;
   }
   w.laytrop[col] = laytrop;
   // secdiff(pwvcm) and d secdiff / d q_l = secdiff'(pwvcm) pwvcm (dwv_l / wvttl - dam_l / amttl)
-  const double wvsh = (amw * wvttl) / (amd * amttl);
-  const double pwvcm = wvsh * (1.e3 * pz0) / (1.e2 * C.grav);
-  const double a0[16] = {1.66, 1.55, 1.58, 1.66, 1.54, 1.454, 1.89, 1.33, 1.668, 1.66, 1.66, 1.66, 1.66, 1.66, 1.66, 1.66};
-  const double a1[16] = {0.00, 0.25, 0.22, 0.00, 0.13, 0.446, -0.10, 0.40, -0.006, 0, 0, 0, 0, 0, 0, 0};
-  const double a2[16] = {0.00, -12.0, -11.7, 0.00, -0.72, -0.243, 0.19, -0.062, 0.414, 0, 0, 0, 0, 0, 0, 0};
-  double dsdp[16];
+  const T wvsh = (amw * wvttl) / (amd * amttl);
+  const T pwvcm = wvsh * ((T)1.e3 * pz0) / ((T)1.e2 * (T)C.grav);
+  const T a0[16] = {(T)1.66, (T)1.55, (T)1.58, (T)1.66, (T)1.54, (T)1.454, (T)1.89, (T)1.33,
+                    (T)1.668, (T)1.66, (T)1.66, (T)1.66, (T)1.66, (T)1.66, (T)1.66, (T)1.66};
+  const T a1[16] = {(T)0.00, (T)0.25, (T)0.22, (T)0.00, (T)0.13, (T)0.446, (T)-0.10, (T)0.40,
+                    (T)-0.006, 0, 0, 0, 0, 0, 0, 0};
+  const T a2[16] = {(T)0.00, (T)-12.0, (T)-11.7, (T)0.00, (T)-0.72, (T)-0.243, (T)0.19, (T)-0.062,
+                    (T)0.414, 0, 0, 0, 0, 0, 0, 0};
+  T dsdp[16];
   for (int b = 1; b <= 16; ++b) {
-    double s, d = 0.0;
+    T sv, d = zero;
     if (b == 1 || b == 4 || b >= 10) {
-      s = 1.66;
+      sv = (T)1.66;
     } else {
-      const double e = exp(a2[b - 1] * pwvcm);
-      s = a0[b - 1] + a1[b - 1] * e;
+      const T e = exp(a2[b - 1] * pwvcm);
+      sv = a0[b - 1] + a1[b - 1] * e;
       d = a1[b - 1] * a2[b - 1] * e;
-      if (s > 1.80) { s = 1.80; d = 0.0; }
-      if (s < 1.50) { s = 1.50; d = 0.0; }
+      if (sv > (T)1.80) { sv = (T)1.80; d = zero; }
+      if (sv < (T)1.50) { sv = (T)1.50; d = zero; }
     }
-    w.secdiff[(b - 1) * N + col] = s;
+    w.secdiff[(b - 1) * N + col] = sv;
     dsdp[b - 1] = d;
   }
   // dsec currently holds dwv_l (rows 0..nlay-1) and dam_l (rows nlay..2nlay-1)
@@ -221,16 +230,18 @@ __global__ void __launch_bounds__(128) adj_lw_prep_kernel(LwIn in, AdjLwWorkT<F>
   // down so that the two source planes are read before band 1 and 2 reuse them.
   for (int l = 1; l <= nlay; ++l) {
     const size_t o = (size_t)(l - 1) * N + col;
-    const double dp = pwvcm * (w.dsec[o] / wvttl - w.dsec[fstride + o] / amttl);
+    const T dp = pwvcm * ((T)w.dsec[o] / wvttl - (T)w.dsec[fstride + o] / amttl);
     for (int b = 16; b >= 1; --b) w.dsec[(size_t)(b - 1) * fstride + o] = dsdp[b - 1] * dp;
   }
 }
 
 // ---------------------------------------------------------------------------
-// FP64 sums over the g-points of a band of per-lane FP64 gradient entries:
-// entries are staged in shared memory W at a time (rows padded to kRow), then
-// lane (cs, sl) sums entry sl of column sub-index cs over the band's NG lanes
-// in g order.  Warp-uniform calls only.
+// Sums over the g-points of a band of per-lane gradient entries: entries are
+// staged in shared memory W at a time (rows padded to kRow), then lane
+// (cs, sl) sums entry sl of column sub-index cs over the band's NG lanes in g
+// order.  FP64 entries are summed in FP64; FP32 entries (split adjoint) with
+// the compensated TwoSum accumulation of the forward solvers' GSum, to FP64
+// accuracy on the FP32 pipe.  Warp-uniform calls only.
 // ---------------------------------------------------------------------------
 template <int W, int NG, class TS = double>
 struct GRed {
@@ -243,10 +254,21 @@ struct GRed {
     const int sl = lane % W, cs = lane / W;
     if (sl < n) {
       const TS* row = buf + sl * kRow + cs * W;
-      double acc = 0.0;
+      if constexpr (sizeof(TS) == 4) {
+        float s = 0.f, c = 0.f;
+#pragma unroll 2
+        for (int g = 0; g < NG; ++g) {
+          const float x = row[g], t = __fadd_rn(s, x), bv = __fsub_rn(t, s);
+          c = __fadd_rn(c, __fadd_rn(__fsub_rn(s, __fsub_rn(t, bv)), __fsub_rn(x, bv)));
+          s = t;
+        }
+        st(first + sl, cs, (double)s + (double)c);
+      } else {
+        double acc = 0.0;
 #pragma unroll
-      for (int g = 0; g < NG; ++g) acc += (double)row[g];
-      st(first + sl, cs, acc);
+        for (int g = 0; g < NG; ++g) acc += (double)row[g];
+        st(first + sl, cs, acc);
+      }
     }
     __syncwarp();
     first += n;
@@ -486,71 +508,75 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_ADJ_MINB 
 // ---------------------------------------------------------------------------
 template <class F>
 __global__ void __launch_bounds__(128) adj_sw_prep_kernel(SwIn in, AdjSwWorkT<F> w, int ncol, int nlay) {
+  // F is the checkpoint and the arithmetic type, as in adj_lw_prep_kernel
+  using T = F;
+  using DT = Dual<T>;
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= ncol) return;
   const SwConst& C = c_sw;
-  const double amd = 28.9660, amw = 18.0160, amdw = 1.607793, amdo = 0.603428;
-  const double stpfac = 296. / 1013.;
+  const T amd = (T)28.9660, amw = (T)18.0160, amdw = (T)1.607793, amdo = (T)0.603428;
+  const T stpfac = (T)(296. / 1013.);
+  const T one = (T)1., e20 = (T)1.e-20, e32 = (T)1.e-32, zero = (T)0.;
   const size_t N = (size_t)ncol;
   const size_t fstride = (size_t)nlay * N;
-  auto A = [&](const double* p, int l) { return __ldg(p + (size_t)col + N * (size_t)(l - 1)); };
-  double pz_prev = A(in.plev, 1);
+  auto A = [&](const double* p, int l) { return (T)__ldg(p + (size_t)col + N * (size_t)(l - 1)); };
+  T pz_prev = A(in.plev, 1);
   int laytrop = 0;
   for (int l = 1; l <= nlay; ++l) {
-    const double pavel = A(in.play, l);
-    const D2 tavel(A(in.tlay, l), 1.0, 0.0);
-    const double pz_l = A(in.plev, l + 1);
-    const D2 h2o(A(in.h2o, l), 0.0, 1.0);
-    D2 wk1 = (h2o / (1. - h2o)) * amdw;
-    const double wk2 = A(in.co2, l);
-    const double wk3 = A(in.o3, l) * amdo;
-    const double wk4 = in.n2o ? A(in.n2o, l) : 0.0;
-    const double wk6 = in.ch4 ? A(in.ch4, l) : 0.0;
-    const double wk7 = in.o2 ? A(in.o2, l) : 0.0;
-    const D2 amm = (1. - wk1) * amd + wk1 * amw;
-    const D2 coldry = (pz_prev - pz_l) * 1.e3 * C.avogad / (1.e2 * C.grav * amm * (1. + wk1));
+    const T pavel = A(in.play, l);
+    const DT tavel(A(in.tlay, l), one, zero);
+    const T pz_l = A(in.plev, l + 1);
+    const DT h2o(A(in.h2o, l), zero, one);
+    DT wk1 = (h2o / (one - h2o)) * amdw;
+    const T wk2 = A(in.co2, l);
+    const T wk3 = A(in.o3, l) * amdo;
+    const T wk4 = in.n2o ? A(in.n2o, l) : zero;
+    const T wk6 = in.ch4 ? A(in.ch4, l) : zero;
+    const T wk7 = in.o2 ? A(in.o2, l) : zero;
+    const DT amm = (one - wk1) * amd + wk1 * amw;
+    const DT coldry = (pz_prev - pz_l) * (T)1.e3 * (T)C.avogad / ((T)1.e2 * (T)C.grav * amm * (one + wk1));
     wk1 = coldry * wk1;
-    const D2 cwk2 = coldry * wk2, cwk3 = coldry * wk3, cwk4 = coldry * wk4, cwk6 = coldry * wk6,
+    const DT cwk2 = coldry * wk2, cwk3 = coldry * wk3, cwk4 = coldry * wk4, cwk6 = coldry * wk6,
              cwk7 = coldry * wk7;
-    const double plog = log(pavel);
-    const int jp = clampi((int)(36. - 5 * (plog + 0.04)), 1, 58);
+    const T plog = log(pavel);
+    const int jp = clampi((int)((T)36. - (T)5 * (plog + (T)0.04)), 1, 58);
     const int jp1 = jp + 1;
-    const double fp = 5. * (C.preflog[jp - 1] - plog);
-    const int jt = clampi((int)(3. + (tavel.v - C.tref[jp - 1]) / 15.), 1, 4);
-    const D2 ft = ((tavel - C.tref[jp - 1]) / 15.) - (double)(jt - 3);
-    const int jt1 = clampi((int)(3. + (tavel.v - C.tref[jp1 - 1]) / 15.), 1, 4);
-    const D2 ft1 = ((tavel - C.tref[jp1 - 1]) / 15.) - (double)(jt1 - 3);
-    const D2 water = wk1 / coldry;
-    const D2 scalefac = (pavel * stpfac) / tavel;
-    D2 forfac, forfrac, selffac(0.0), selffrac(0.0), factor;
+    const T fp = (T)5. * ((T)C.preflog[jp - 1] - plog);
+    const int jt = clampi((int)((T)3. + (tavel.v - (T)C.tref[jp - 1]) / (T)15.), 1, 4);
+    const DT ft = ((tavel - (T)C.tref[jp - 1]) / (T)15.) - (T)(jt - 3);
+    const int jt1 = clampi((int)((T)3. + (tavel.v - (T)C.tref[jp1 - 1]) / (T)15.), 1, 4);
+    const DT ft1 = ((tavel - (T)C.tref[jp1 - 1]) / (T)15.) - (T)(jt1 - 3);
+    const DT water = wk1 / coldry;
+    const DT scalefac = (pavel * stpfac) / tavel;
+    DT forfac, forfrac, selffac(zero), selffrac(zero), factor;
     int indfor, indself = 0;
-    if (plog > 4.56) {
+    if (plog > (T)4.56) {
       laytrop = laytrop + 1;
-      forfac = scalefac / (1. + water);
-      factor = (332.0 - tavel) / 36.0;
+      forfac = scalefac / (one + water);
+      factor = ((T)332.0 - tavel) / (T)36.0;
       indfor = min(2, max(1, (int)factor.v));
-      forfrac = factor - (double)indfor;
+      forfrac = factor - (T)indfor;
       selffac = water * forfac;
-      factor = (tavel - 188.0) / 7.2;
+      factor = (tavel - (T)188.0) / (T)7.2;
       indself = min(9, max(1, (int)factor.v - 7));
-      selffrac = factor - (double)(indself + 7);
+      selffrac = factor - (T)(indself + 7);
     } else {
-      forfac = scalefac / (1. + water);
-      factor = (tavel - 188.0) / 36.0;
+      forfac = scalefac / (one + water);
+      factor = (tavel - (T)188.0) / (T)36.0;
       indfor = 3;
-      forfrac = factor - 1.0;
+      forfrac = factor - one;
     }
-    const D2 colh2o = 1.e-20 * wk1;
-    D2 colco2 = 1.e-20 * cwk2, colch4 = 1.e-20 * cwk6, colo2 = 1.e-20 * cwk7, coln2o = 1.e-20 * cwk4;
-    const D2 colo3 = 1.e-20 * cwk3;
-    const D2 colmol = 1.e-20 * coldry + colh2o;
-    if (colco2.v == 0.) colco2 = 1.e-32 * coldry;
-    if (coln2o.v == 0.) coln2o = 1.e-32 * coldry;
-    if (colch4.v == 0.) colch4 = 1.e-32 * coldry;
-    if (colo2.v == 0.) colo2 = 1.e-32 * coldry;
-    const double compfp = 1. - fp;
+    const DT colh2o = e20 * wk1;
+    DT colco2 = e20 * cwk2, colch4 = e20 * cwk6, colo2 = e20 * cwk7, coln2o = e20 * cwk4;
+    const DT colo3 = e20 * cwk3;
+    const DT colmol = e20 * coldry + colh2o;
+    if (colco2.v == zero) colco2 = e32 * coldry;
+    if (coln2o.v == zero) coln2o = e32 * coldry;
+    if (colch4.v == zero) colch4 = e32 * coldry;
+    if (colo2.v == zero) colo2 = e32 * coldry;
+    const T compfp = one - fp;
     const size_t o = (size_t)(l - 1) * N + col;
-    auto put = [&](int fld, const D2& x) {
+    auto put = [&](int fld, const DT& x) {
       const size_t i = (size_t)fld * fstride + o;
       w.fv[i] = x.v;
       w.ft[i] = x.t;
@@ -563,15 +589,15 @@ __global__ void __launch_bounds__(128) adj_sw_prep_kernel(SwIn in, AdjSwWorkT<F>
     put(SF_COLO2, colo2);
     put(SF_COLMOL, colmol);
     put(SF_FAC10, compfp * ft);
-    put(SF_FAC00, compfp * (1. - ft));
+    put(SF_FAC00, compfp * (one - ft));
     put(SF_FAC11, fp * ft1);
-    put(SF_FAC01, fp * (1. - ft1));
+    put(SF_FAC01, fp * (one - ft1));
     put(SF_SELFFAC, selffac);
     put(SF_SELFFRAC, selffrac);
     put(SF_FORFAC, forfac);
     put(SF_FORFRAC, forfrac);
     w.idx[o] = pack_idx(jp, jt, jt1, indself, indfor, 1);
-    w.hs[o] = C.heatfac / (pz_prev - pz_l);
+    w.hs[o] = (double)((T)C.heatfac / (pz_prev - pz_l));
     pz_prev = pz_l;
   }
   w.laytrop[col] = laytrop;
@@ -937,23 +963,28 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_ADJ_MINB 
 // layer's q through d secdiff / d q.  SW partials are already in W/m2.
 // Jacobian: one thread per (column, output row); VJP: one per column.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) adj_finalize_kernel(AdjLwWork lw, AdjSwWork sw, const double* __restrict__ coszen,
-                                                           int nseed_lw, int nseed_sw, int ncol, int nlay,
-                                                           double* __restrict__ out, int vjp) {
+// Thread per (column, output row, chunk of kAdjXChunk inputs).
+constexpr int kAdjXChunk = 8;
+__global__ void __launch_bounds__(128) adj_finalize_kernel(AdjLwWork lw, AdjSwWork sw, int nseed_lw, int nseed_sw,
+                                                           int ncol, int nlay, double* __restrict__ out, int vjp) {
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= ncol) return;
-  const int r = blockIdx.y;  // output row (Jacobian) or 0 (VJP)
   const size_t N = (size_t)ncol;
   const int L = nlay, ny = 2 * L + 3, nx = 3 * L + 2;
+  const int nxc = (nx + kAdjXChunk - 1) / kAdjXChunk;
+  const int r = blockIdx.y / nxc;  // output row (Jacobian) or 0 (VJP)
+  const int x0 = (blockIdx.y % nxc) * kAdjXChunk, x1 = min(nx, x0 + kAdjXChunk);
   const int Elw = 3 * L + 3, Esw = 2 * L;
   const double wtdiff = 0.5;
   auto lwp = [&](int b, int s, int e) { return __ldg(lw.part + (((size_t)b * nseed_lw + s) * Elw + e) * N + col); };
   auto swp = [&](int b, int s, int e) { return __ldg(sw.part + (((size_t)b * nseed_sw + s) * Esw + e) * N + col); };
-  auto wb = [&](int b) { return wtdiff * c_lw.band[b].delwave * c_lw.fluxfac; };
+  double wb[kLwBands];
+#pragma unroll
+  for (int b = 0; b < kLwBands; ++b) wb[b] = wtdiff * c_lw.band[b].delwave * c_lw.fluxfac;
   const bool do_lw = vjp || r < L + 2;
   const bool do_sw = vjp || r >= L + 2;
   const int slw = vjp ? 0 : r, ssw = vjp ? 0 : r - (L + 2);
-  for (int x = 0; x < nx; ++x) {
+  for (int x = x0; x < x1; ++x) {
     double v = 0.0;
     if (do_lw) {
       int e;
@@ -962,10 +993,11 @@ __global__ void __launch_bounds__(128) adj_finalize_kernel(AdjLwWork lw, AdjSwWo
       else if (x < 3 * L) e = 3 * (x - 2 * L) + 2;   // tlev 0..nlay-1
       else if (x == 3 * L) e = 3 * L;                // tlev nlay
       else e = 3 * L + 1;                            // tsfc
+#pragma unroll
       for (int b = 0; b < kLwBands; ++b) {
         double t = lwp(b, slw, e);
         if (x >= L && x < 2 * L) t += lwp(b, slw, 3 * L + 2) * __ldg(lw.dsec + ((size_t)b * L + (x - L)) * N + col);
-        v += wb(b) * t;
+        v += wb[b] * t;
       }
     }
     if (do_sw && x < 2 * L) {
@@ -977,7 +1009,6 @@ __global__ void __launch_bounds__(128) adj_finalize_kernel(AdjLwWork lw, AdjSwWo
     else
       out[((size_t)x * ny + r) * N + col] = v;
   }
-  (void)coszen;
 }
 
 // ---------------------------------------------------------------------------
@@ -1001,7 +1032,7 @@ void launch_adj_lw(const LwIn& in, const AdjLwWork& w, const double* totplnk, co
     lw_adj_kernel<double, 208><<<nb, kBlock, 0, s>>>(in, w, tab, cot, nseed, ncol, nlay);
 }
 
-void launch_adj_lw_split(const LwIn& in, const AdjLwWorkT<float>& w, const double* totplnk, const float* tab,
+void launch_adj_lw_split(const LwIn& in, const AdjLwWorkT<float>& w, const float* totplnk, const float* tab,
                          const double* cot, int nseed, int ncol, int nlay, int nb, cudaStream_t s) {
   adj_lw_prep_kernel<float><<<(ncol + 127) / 128, 128, 0, s>>>(in, w, totplnk, ncol, nlay);
   if (maxl_for(nlay) == 64)
@@ -1032,8 +1063,10 @@ void launch_adj_sw_split(const SwIn& in, const AdjSwWorkT<float>& w, double adjf
 void launch_adj_finalize(const AdjLwWork& lw, const AdjSwWork& sw, const double* plev, const double* coszen,
                          int nseed_lw, int nseed_sw, int ncol, int nlay, double* out, bool vjp, cudaStream_t s) {
   (void)plev;
-  dim3 grid((ncol + 127) / 128, vjp ? 1 : adj_ny(nlay));
-  adj_finalize_kernel<<<grid, 128, 0, s>>>(lw, sw, coszen, nseed_lw, nseed_sw, ncol, nlay, out, vjp ? 1 : 0);
+  (void)coszen;
+  const int nxc = (adj_nx(nlay) + kAdjXChunk - 1) / kAdjXChunk;
+  dim3 grid((ncol + 127) / 128, (vjp ? 1 : adj_ny(nlay)) * nxc);
+  adj_finalize_kernel<<<grid, 128, 0, s>>>(lw, sw, nseed_lw, nseed_sw, ncol, nlay, out, vjp ? 1 : 0);
 }
 
 }  // namespace rrtmg

@@ -57,7 +57,7 @@ void launch_adj_lw(const LwIn& in, const AdjLwWork& w, const double* totplnk, co
 void launch_adj_sw(const SwIn& in, const AdjSwWork& w, double adjflux, int iaer, const double* tab,
                    const double* cot, int nseed, int ncol, int nlay, int nb, cudaStream_t s);
 // FP32/FP64-split adjoint: FP32 dual numbers and reverse sweeps, FP64 sums.
-void launch_adj_lw_split(const LwIn& in, const AdjLwWorkT<float>& w, const double* totplnk, const float* tab,
+void launch_adj_lw_split(const LwIn& in, const AdjLwWorkT<float>& w, const float* totplnk, const float* tab,
                          const double* cot, int nseed, int ncol, int nlay, int nb, cudaStream_t s);
 void launch_adj_sw_split(const SwIn& in, const AdjSwWorkT<float>& w, double adjflux, int iaer, const float* tab,
                          const double* tab64, const double* cot, int nseed, int ncol, int nlay, int nb,

@@ -417,9 +417,12 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
   // No downward radiance enters at the top (drad(nlayers) stays 0,
   // rrtmg_lw_rtrnmr.f90:290-300).
   if (g == 0 && valid) bdp[(size_t)nlay * N] = 0.0;
+  // the packed table indices of the next layer are loaded one layer ahead
+  uint32_t idx_next = __ldg(p.idx + (size_t)(nlay - 1) * N + c);
   for (int lev = nlay; lev >= 1; --lev) {
     const size_t o = (size_t)(lev - 1) * N + c;
-    const Idx ix = unpack_idx(__ldg(p.idx + o));
+    const Idx ix = unpack_idx(idx_next);
+    if (lev > 1) idx_next = __ldg(p.idx + o - N);
     LwLayerView<R> L{p.f, fstride, o};
     R taug, fracs;
     lw_gas<B, R>(c_lw, lw_rconst<R>(), L, ix, lev <= lt, gg, tab, taug, fracs);
@@ -1010,10 +1013,13 @@ __device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, dou
   R pref[MAXL + 1], prefd[MAXL + 1], ptra[MAXL + 1], ptrad[MAXL + 1], pdbt[MAXL + 1];
   R ptdbt[MAXL + 2], ztdn[MAXL + 2], prdnd[MAXL + 2];
   ptdbt[1 - 1] = (R)1.0;
+  // the packed table indices of the next layer are loaded one layer ahead
+  uint32_t idx_next = __ldg(p.idx + (size_t)(klev - 1) * N + c);
   for (int jk = 1; jk <= klev; ++jk) {
     const int ikl = klev + 1 - jk;
     const size_t o = (size_t)(ikl - 1) * N + c;
-    const Idx ix = unpack_idx(__ldg(p.idx + o));
+    const Idx ix = unpack_idx(idx_next);
+    if (ikl > 1) idx_next = __ldg(p.idx + o - N);
     SwLayerView<R> L{p.f, fstride, o};
     R taug, taur;
     sw_gas<B, R>(c_sw, L, ix, ikl <= lt, gg, tab, taug, taur);

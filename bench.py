@@ -195,21 +195,13 @@ def run_reference(args):
 
 
 def graph_step(torch, r, stream, atm, d, olw, osw, precision):
-    """Capture one LW+SW step (device entry points) in a CUDA graph: the LW
-    call on `stream`, the SW call forked onto a second stream and joined
-    back, so that the two independent calls overlap on the GPU."""
+    """Capture one LW+SW step in a CUDA graph through the fused entry point
+    rrtmg_step_dev, which runs the SW call on a second stream of the handle
+    so that the two independent calls overlap on the GPU."""
     r.set_precision(precision)
-    side = torch.cuda.Stream(device=stream.device)
 
     def call():
-        fork = torch.cuda.Event()
-        fork.record(stream)
-        side.wait_event(fork)
-        r.rrtmg_lw_dev(stream.cuda_stream, atm.ncol, atm.nlay, 0, 0, d, olw)
-        r.rrtmg_sw_dev(side.cuda_stream, atm.ncol, atm.nlay, 0, 0, d, osw, atm.adjes, atm.dyofyr, atm.scon)
-        join = torch.cuda.Event()
-        join.record(side)
-        stream.wait_event(join)
+        r.rrtmg_step_dev(stream.cuda_stream, atm.ncol, atm.nlay, d, olw, osw, atm.adjes, atm.dyofyr, atm.scon)
     with torch.cuda.stream(stream):
         call()  # first call outside capture (workspace already reserved)
     stream.synchronize()

@@ -142,6 +142,31 @@ int rrtmg_sw_dev(rrtmg_gpu_handle h, void* stream, int ncol, int nlay, int icld,
                  double* swuflx, double* swdflx, double* swhr, double* swuflxc, double* swdflxc,
                  double* swhrc);
 
+/* Fused LW + SW step on device arrays (no single counterpart in the
+ * reference, whose run_rrtmg calls rrtmg_sw and then rrtmg_lw,
+ * rrtm_radiation.f90:686-748): the arguments of rrtmg_lw_dev and
+ * rrtmg_sw_dev merged, clear sky (icld = 0, the cloud arguments omitted), LW
+ * aerosols tauaer_lw (ncol,nlay,16) optional, SW aerosols when iaer = 10.  The
+ * results equal those of the two separate calls bit for bit.  The SW call
+ * runs on a second stream of the handle, forked from `stream` and joined back
+ * into it by events, so that the two calls overlap on the GPU; everything is
+ * complete when `stream` reaches the end of the call's work, and the call can
+ * be captured in a CUDA graph (as two parallel branches).  Calls on one
+ * handle share its workspaces: order them on one stream. */
+int rrtmg_step_dev(rrtmg_gpu_handle h, void* stream, int ncol, int nlay, int idrv, int iaer,
+                   const double* play, const double* plev, const double* tlay, const double* tlev,
+                   const double* tsfc, const double* h2ovmr, const double* o3vmr, const double* co2vmr,
+                   const double* ch4vmr, const double* n2ovmr, const double* o2vmr,
+                   const double* cfc11vmr, const double* cfc12vmr, const double* cfc22vmr,
+                   const double* ccl4vmr, const double* emis, const double* tauaer_lw,
+                   const double* asdir, const double* asdif, const double* aldir, const double* aldif,
+                   const double* coszen, double adjes, int dyofyr, double scon,
+                   const double* tauaer_sw, const double* ssaaer, const double* asmaer,
+                   double* uflx, double* dflx, double* hr, double* uflxc, double* dflxc, double* hrc,
+                   double* duflx_dt, double* duflxc_dt,
+                   double* swuflx, double* swdflx, double* swhr, double* swuflxc, double* swdflxc,
+                   double* swhrc);
+
 /* No counterpart in the reference.  Kernel timing: while enabled, the LW and
  * SW calls record CUDA events around each of their three kernels (prep,
  * g-point solver, finalize) on the call's stream (not while the stream is

@@ -53,6 +53,10 @@ struct rrtmg_gpu_state {
   DevBuf hio[2], hws[2];
   // run_rrtmg calls: RRTM columns, results and zonal scratch; host-array staging
   DevBuf run_ws, run_io;
+  // fused LW+SW calls: the SW call runs on `side`, forked from and joined back
+  // into the caller's stream with these events
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   long long launches = 0;
   std::string err;
   // Optional per-kernel timing: events around every launch of the last LW
@@ -287,6 +291,25 @@ int sw_run(rrtmg_gpu_state* h, cudaStream_t s, int ncol, int nlay, int iaer, dou
                     swdflxc, swhrc);
 }
 
+// Runs sw(side) on the handle's side stream and lw(st) on st, the side stream
+// forked from st and joined back into it by events (a pattern that stream
+// capture records as two parallel graph branches).  The join is enqueued even
+// when a launch failed, so that a capture stays well formed.
+template <class LwF, class SwF>
+int fork_lw_sw(rrtmg_gpu_state* h, cudaStream_t st, LwF&& lw, SwF&& sw) {
+  cudaError_t e = cudaEventRecord(h->fork_ev, st);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(h->side, h->fork_ev, 0);
+  if (e != cudaSuccess) return cuda_fail(h, e, "fork onto the side stream");
+  const int rs = sw(h->side);
+  const int rl = lw(st);
+  e = cudaEventRecord(h->join_ev, h->side);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(st, h->join_ev, 0);
+  if (rs) return rs;
+  if (rl) return rl;
+  if (e != cudaSuccess) return cuda_fail(h, e, "join the side stream");
+  return RRTMG_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Host-pointer calls.  Every caller array is (ncol, rows) with the column
 // index fastest.  The columns are processed in chunks that alternate between
@@ -494,6 +517,9 @@ int rrtmg_gpu_init(double cpdair, const char* table_blob, int device, rrtmg_gpu_
   cudaError_t e = cudaSetDevice(device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->join_ev, cudaEventDisableTiming);
   if (e == cudaSuccess) e = upload(&h->lw_tab64, h->host.lw_tab);
   if (e == cudaSuccess) e = upload(&h->sw_tab64, h->host.sw_tab);
   if (e == cudaSuccess) e = upload(&h->lw_exp64, h->host.lw_exp);
@@ -529,6 +555,7 @@ int rrtmg_gpu_finalize(rrtmg_gpu_handle h) {
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->stream2) cudaStreamSynchronize(h->stream2);
+  if (h->side) cudaStreamSynchronize(h->side);
   void* ptrs[] = {h->lw_tab64, h->sw_tab64, h->lw_exp64, h->lw_tfn64, h->sw_exp64, h->totplnk, h->totplnkderiv,
                   h->totplnk32, h->totplnkderiv32,
                   h->lw_tab32, h->sw_tab32, h->lw_exp32, h->lw_tfn32, h->sw_exp32, h->flags, h->lw_ws.p,
@@ -538,6 +565,9 @@ int rrtmg_gpu_finalize(rrtmg_gpu_handle h) {
     if (p) cudaFree(p);
   if (h->stream) cudaStreamDestroy(h->stream);
   if (h->stream2) cudaStreamDestroy(h->stream2);
+  if (h->side) cudaStreamDestroy(h->side);
+  if (h->fork_ev) cudaEventDestroy(h->fork_ev);
+  if (h->join_ev) cudaEventDestroy(h->join_ev);
   for (auto& fam : h->ev)
     for (auto& e : fam)
       if (e) cudaEventDestroy(e);
@@ -658,6 +688,46 @@ int rrtmg_sw_dev(rrtmg_gpu_handle h, void* stream, int ncol, int nlay, int icld,
           coszen, tauaer, ssaaer, asmaer};
   return sw_run(h, (cudaStream_t)stream, ncol, nlay, iaer, adjes, dyofyr, scon, in, swuflx, swdflx, swhr, swuflxc,
                 swdflxc, swhrc);
+}
+
+int rrtmg_step_dev(rrtmg_gpu_handle h, void* stream, int ncol, int nlay, int idrv, int iaer, const double* play,
+                   const double* plev, const double* tlay, const double* tlev, const double* tsfc,
+                   const double* h2ovmr, const double* o3vmr, const double* co2vmr, const double* ch4vmr,
+                   const double* n2ovmr, const double* o2vmr, const double* cfc11vmr, const double* cfc12vmr,
+                   const double* cfc22vmr, const double* ccl4vmr, const double* emis, const double* tauaer_lw,
+                   const double* asdir, const double* asdif, const double* aldir, const double* aldif,
+                   const double* coszen, double adjes, int dyofyr, double scon, const double* tauaer_sw,
+                   const double* ssaaer, const double* asmaer, double* uflx, double* dflx, double* hr,
+                   double* uflxc, double* dflxc, double* hrc, double* duflx_dt, double* duflxc_dt,
+                   double* swuflx, double* swdflx, double* swhr, double* swuflxc, double* swdflxc,
+                   double* swhrc) {
+  if (!valid_handle(h)) return RRTMG_ERR_ARG;
+  int rc = check_dims(h, ncol, nlay);
+  if (rc) return rc;
+  if (idrv != 0 && idrv != 1) return fail(h, RRTMG_ERR_UNSUPPORTED, "idrv must be 0 or 1");
+  if (iaer != 0 && iaer != 10) return fail(h, RRTMG_ERR_UNSUPPORTED, "iaer must be 0 or 10");
+  if (!play || !plev || !tlay || !tlev || !tsfc || !h2ovmr || !o3vmr || !co2vmr || !asdir || !asdif || !aldir ||
+      !aldif || !coszen || !uflx || !dflx || !hr || !uflxc || !dflxc || !hrc || !swuflx || !swdflx || !swhr ||
+      !swuflxc || !swdflxc || !swhrc)
+    return fail(h, RRTMG_ERR_ARG, "a required array pointer is null");
+  if (idrv == 1 && !duflx_dt) return fail(h, RRTMG_ERR_ARG, "idrv = 1 needs duflx_dt");
+  if (iaer == 10 && (!tauaer_sw || !ssaaer || !asmaer))
+    return fail(h, RRTMG_ERR_ARG, "iaer = 10 needs tauaer/ssaaer/asmaer");
+  if (!(scon > 0.0)) return fail(h, RRTMG_ERR_ARG, "scon must be positive");
+  cudaSetDevice(h->device);
+  const LwIn lin{play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr, cfc11vmr, cfc12vmr,
+                 cfc22vmr, ccl4vmr, emis, tauaer_lw};
+  const SwIn sin{play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr, asdir, asdif, aldir,
+                 aldif, coszen, tauaer_sw, ssaaer, asmaer};
+  return fork_lw_sw(
+      h, (cudaStream_t)stream,
+      [&](cudaStream_t s) {
+        return lw_run(h, s, ncol, nlay, idrv, lin, uflx, dflx, hr, uflxc, dflxc, hrc, duflx_dt, duflxc_dt);
+      },
+      [&](cudaStream_t s) {
+        return sw_run(h, s, ncol, nlay, iaer, adjes, dyofyr, scon, sin, swuflx, swdflx, swhr, swuflxc, swdflxc,
+                      swhrc);
+      });
 }
 
 static int adjoint_entry(rrtmg_gpu_handle h, void* stream, int ncol, int nlay, const double* play,
@@ -1024,15 +1094,21 @@ int run_enqueue(rrtmg_gpu_state* h, cudaStream_t st, const rrtmg_run_params& p, 
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(h, e, "run_rrtmg: input kernels");
   const RunCols& c = w.c;
-  // rrtm_radiation.f90:683-713 (SW) and :718-749 (LW), clear sky, iaer = idrv = 0
+  // rrtm_radiation.f90:683-713 (SW) and :718-749 (LW), clear sky, iaer = idrv = 0;
+  // the two calls are independent and run concurrently
   const SwIn sin{c.play, c.plev, c.tlay, c.tlev, c.tsfc, c.h2o, c.o3, c.co2, c.gas[0], c.gas[1], c.gas[2],
                  c.alb, c.alb, c.alb, c.alb, c.cosz, nullptr, nullptr, nullptr};
-  rc = sw_run(h, st, s.ncol, a.sk, 0, p.solrad, dyofyr, p.solr_cnst, sin, w.swuflx, w.swdflx, w.swhr, w.swuflxc,
-              w.swdflxc, w.swhrc);
-  if (rc) return rc;
   const LwIn lin{c.play, c.plev, c.tlay, c.tlev, c.tsfc, c.h2o, c.o3, c.co2, c.gas[0], c.gas[1], c.gas[2],
                  c.gas[3], c.gas[4], c.gas[5], c.gas[6], c.emis, nullptr};
-  rc = lw_run(h, st, s.ncol, a.sk, 0, lin, w.uflx, w.dflx, w.hr, w.uflxc, w.dflxc, w.hrc, nullptr, nullptr);
+  rc = fork_lw_sw(
+      h, st,
+      [&](cudaStream_t ls) {
+        return lw_run(h, ls, s.ncol, a.sk, 0, lin, w.uflx, w.dflx, w.hr, w.uflxc, w.dflxc, w.hrc, nullptr, nullptr);
+      },
+      [&](cudaStream_t ss) {
+        return sw_run(h, ss, s.ncol, a.sk, 0, p.solrad, dyofyr, p.solr_cnst, sin, w.swuflx, w.swdflx, w.swhr,
+                      w.swuflxc, w.swdflxc, w.swhrc);
+      });
   if (rc) return rc;
   const RunRad r{w.uflx, w.dflx, w.hr, w.swuflx, w.swdflx, w.swhr};
   if (s.zm_rad) {

@@ -40,7 +40,7 @@ EXPORTED = ("rrtmg_gpu_init", "rrtmg_gpu_finalize", "rrtmg_gpu_set_precision", "
             "rrtmg_gpu_last_error", "rrtmg_gpu_launch_count", "rrtmg_lw_c", "rrtmg_sw_c", "rrtmg_lw_dev",
             "rrtmg_sw_dev", "rrtmg_gpu_reserve", "rrtmg_gpu_sync_status", "rrtmg_lw_dev_static",
             "rrtmg_gpu_set_transcendentals", "rrtmg_jacobian_dev", "rrtmg_vjp_dev", "rrtmg_gpu_set_profiling",
-            "rrtmg_gpu_profile",
+            "rrtmg_gpu_profile", "rrtmg_step_dev",
             # include/rrtmg_run.h
             "rrtmg_run_params_default", "rrtmg_run_dev", "rrtmg_run_c")
 KERNELS = ("lw_prep", "lw_gpoint", "lw_finalize", "sw_prep", "sw_gpoint", "sw_finalize")
@@ -338,6 +338,23 @@ class RRTMG:
             g("asmaer"), None, o("swuflx"), o("swdflx"), o("swhr"), o("swuflxc"), o("swdflxc"), o("swhrc"))
         self._check(rc)
 
+
+    def rrtmg_step_dev(self, stream, ncol, nlay, d, olw, osw, adjes, dyofyr, scon, idrv=0, iaer=0, tauaer_lw=None):
+        """Fused LW + SW step on device arrays (rrtmg_step_dev): ``d`` holds
+        the inputs by rrtmg_lw / rrtmg_sw argument name (plus ``tauaer``,
+        ``ssaaer``, ``asmaer`` for iaer = 10), ``olw`` / ``osw`` the outputs."""
+        g = lambda k: _dptr(d.get(k))
+        o = lambda k: _dptr(olw.get(k))
+        q = lambda k: _dptr(osw.get(k))
+        rc = self.lib.rrtmg_step_dev(
+            self._h, C.c_void_p(stream or 0), C.c_int(ncol), C.c_int(nlay), C.c_int(idrv), C.c_int(iaer),
+            g("play"), g("plev"), g("tlay"), g("tlev"), g("tsfc"), g("h2ovmr"), g("o3vmr"), g("co2vmr"),
+            g("ch4vmr"), g("n2ovmr"), g("o2vmr"), g("cfc11vmr"), g("cfc12vmr"), g("cfc22vmr"), g("ccl4vmr"),
+            g("emis"), _dptr(tauaer_lw), g("asdir"), g("asdif"), g("aldir"), g("aldif"), g("coszen"),
+            C.c_double(adjes), C.c_int(dyofyr), C.c_double(scon), g("tauaer"), g("ssaaer"), g("asmaer"),
+            o("uflx"), o("dflx"), o("hr"), o("uflxc"), o("dflxc"), o("hrc"), o("duflx_dt"), o("duflxc_dt"),
+            q("swuflx"), q("swdflx"), q("swhr"), q("swuflxc"), q("swdflxc"), q("swhrc"))
+        self._check(rc)
 
     def run_rrtmg(self, prm, slab, seconds, days, days_per_year=365, tdt=None, diagnostics=True):
         """run_rrtmg on host arrays (rrtmg_run_c).  ``slab`` holds the GCM

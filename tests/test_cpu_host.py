@@ -23,7 +23,7 @@ def header_symbols():
 def test_library_exports_every_declared_symbol():
     lib = R.load_library()
     syms = header_symbols()
-    assert len(syms) == 21
+    assert len(syms) == 22
     assert set(syms) == set(R.EXPORTED)
     for s in syms:
         assert hasattr(lib, s), s

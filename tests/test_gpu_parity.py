@@ -164,6 +164,55 @@ def test_device_api_matches_host_api_and_graph_capture(gpu):
     assert gpu.sync_status(s.cuda_stream) == 0
 
 
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_fused_step_equals_separate_calls_and_captures(gpu, precision):
+    """rrtmg_step_dev (SW forked onto the handle's second stream) gives the
+    results of rrtmg_lw_dev + rrtmg_sw_dev bit for bit, directly and replayed
+    from a CUDA graph, with idrv = 1 and aerosols on both sides."""
+    import torch
+    rng = np.random.default_rng(31)
+    atm = A.small_atmosphere(700, 40, seed=31)
+    gpu.set_precision(precision)
+    try:
+        d = R.atm_device_inputs(atm)
+        t = lambda a: torch.from_numpy(a).cuda()
+        aer_lw = t(rng.uniform(0.0, 0.05, size=(16, atm.nlay, atm.ncol)))
+        d["tauaer"] = t(rng.uniform(0.0, 0.1, size=(14, atm.nlay, atm.ncol)))
+        d["ssaaer"] = t(rng.uniform(0.8, 1.0, size=(14, atm.nlay, atm.ncol)))
+        d["asmaer"] = t(rng.uniform(0.0, 0.8, size=(14, atm.nlay, atm.ncol)))
+        s = torch.cuda.Stream()
+        gpu.reserve(atm.ncol, atm.nlay)
+        rlw, rsw = R.device_outputs(atm.ncol, atm.nlay, idrv=1)
+        olw, osw = R.device_outputs(atm.ncol, atm.nlay, idrv=1)
+        with torch.cuda.stream(s):
+            gpu.rrtmg_lw_dev(s.cuda_stream, atm.ncol, atm.nlay, 0, 1, d, rlw, tauaer=aer_lw)
+            gpu.rrtmg_sw_dev(s.cuda_stream, atm.ncol, atm.nlay, 0, 10, d, rsw, atm.adjes, atm.dyofyr, atm.scon)
+            gpu.rrtmg_step_dev(s.cuda_stream, atm.ncol, atm.nlay, d, olw, osw, atm.adjes, atm.dyofyr, atm.scon,
+                               idrv=1, iaer=10, tauaer_lw=aer_lw)
+        s.synchronize()
+        for k in olw:
+            assert torch.equal(olw[k], rlw[k]), k
+        for k in osw:
+            assert torch.equal(osw[k], rsw[k]), k
+        for x in list(olw.values()) + list(osw.values()):
+            x.zero_()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=s):
+            gpu.rrtmg_step_dev(s.cuda_stream, atm.ncol, atm.nlay, d, olw, osw, atm.adjes, atm.dyofyr, atm.scon,
+                               idrv=1, iaer=10, tauaer_lw=aer_lw)
+        before = gpu.launch_count()
+        g.replay()
+        torch.cuda.synchronize()
+        assert gpu.launch_count() == before  # a replay issues no new library calls
+        for k in olw:
+            assert torch.equal(olw[k], rlw[k]), k
+        for k in osw:
+            assert torch.equal(osw[k], rsw[k]), k
+        assert gpu.sync_status(s.cuda_stream) == 0
+    finally:
+        gpu.set_precision("fp64")
+
+
 def test_invalid_input_and_unsupported_configurations(gpu):
     atm = A.small_atmosphere(8, 40, seed=1)
     atm.tlay[5, 3] = np.nan

@@ -134,6 +134,22 @@ def dominant_traffic(kernel, ncol):
     return None if t is None else float(t["dram_bytes_per_column"]) * ncol
 
 
+def executed_flops(kernel, ncol):
+    """Executed FP32 operations per launch of the kernel from the committed
+    ncu capture (profiles/dram_traffic.json), scaled to ncol columns."""
+    p = ROOT / "profiles" / "dram_traffic.json"
+    if not p.exists():
+        return None
+    t = json.loads(p.read_text()).get(kernel) or {}
+    f = t.get("executed_fp32_flops_per_column")
+    return None if f is None else float(f) * ncol
+
+
+# FP32 (non-tensor) peak of the GB300 at its 2070 MHz maximum SM clock:
+# 152 SMs x 128 FP32 lanes x 2 operations per FMA.
+FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12
+
+
 def measured_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -599,6 +615,14 @@ def run_ours(args):
     dom_bytes = kernel_bytes(dom, atm.ncol, atm.nlay)
     achieved = dom_bytes / (kms32[dom] * 1e-3) / 1e9
     traffic = dominant_traffic(dom, atm.ncol)
+    flops = executed_flops(dom, atm.ncol)
+    compute = None
+    if flops:
+        tf = flops / (kms32[dom] * 1e-3) / 1e12
+        compute = {"bound": "fp32 pipe", "achieved": tf, "peak": FP32_PEAK_TFLOPS, "unit": "TFLOP/s",
+                   "frac": tf / FP32_PEAK_TFLOPS, "executed_flops_per_launch": flops,
+                   "note": "executed FP32 operations (ncu, FMA = 2) / CUDA-event kernel time; nominal peak "
+                           "152 SMs x 128 lanes x 2 x 2.07 GHz"}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True, "scaling": "weak",
@@ -616,7 +640,8 @@ def run_ours(args):
                      "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "kernel": f"{dom} (FP32-split)",
                      "algorithmic_bytes_per_launch": dom_bytes, "kernel_ms": kms32[dom],
                      "note": (f"peak {src}; the g-point solvers are latency/FP-pipe bound, not HBM bound: "
-                              f"step algorithmic bytes {nbytes}")},
+                              f"step algorithmic bytes {nbytes}"),
+                     "compute": compute},
         "kernels_ms": {"split": kms32, "fp64": kms64},
         "cpu_baseline": {"value": cpu_value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{nsample} of {atm.ncol} columns, LW+SW FP64 C++ restatement"},

@@ -200,7 +200,7 @@ int lw_enqueue(rrtmg_gpu_state* h, cudaStream_t s, void* base, int ncol, int nla
                double* duflxc_dt) {
   LwWork w = carve_lw(base, ncol, nlay, nullptr);
   mark(h, 0, 0, s);
-  const int nb = lw_gpoint_blocks(h->host.lw, ncol);
+  const int nb = lw_gpoint_blocks(h->host.lw, ncol, h->precision == RRTMG_PREC_SPLIT);
   if (h->precision == RRTMG_PREC_SPLIT) {
     const LwWorkT<float> w32 = work_as<float>(w);
     launch_lw_prep_split(in, w32, h->totplnk32, h->totplnkderiv32, ncol, nlay, idrv, h->flags, s);
@@ -253,7 +253,7 @@ int sw_enqueue(rrtmg_gpu_state* h, cudaStream_t s, void* base, int ncol, int nla
                double* swdflxc, double* swhrc) {
   SwWork w = carve_sw(base, ncol, nlay, nullptr);
   const double adjflux = adjflux_of(h, adjes, dyofyr, scon);
-  const int nb = sw_gpoint_blocks(h->host.sw, ncol);
+  const int nb = sw_gpoint_blocks(h->host.sw, ncol, h->precision == RRTMG_PREC_SPLIT);
   mark(h, 1, 0, s);
   if (h->precision == RRTMG_PREC_SPLIT) {
     const SwWorkT<float> w32 = work_as<float>(w);

@@ -1,25 +1,27 @@
 // RRTMG clear-sky LW/SW column-radiation kernels for sm_103a.
 //
 // Work decomposition (per radiation call, LW and SW alike):
-//   1. prep    one thread per column: inatm + setcoef (FP64).  Writes the
-//              per-layer gas state SoA, Planck terms (LW) and solar-source
-//              layers (SW).
+//   1. prep    one thread per (column, layer): inatm + setcoef of the layer,
+//              then one thread per column for the column sums, laytrop,
+//              secdiff and the surface Planck terms (LW) or the solar-source
+//              layers (SW).  FP64 on the FP64 path, FP32 on the split path.
 //   2. gpoint  one thread per (column, g-point).  A warp holds the g-points
-//              of a single band for 32/ngpad columns (ngpad = next power of
-//              two >= the band's g count), so every warp runs one band's
-//              straight-line gas-optics code and its table loads for one
-//              column are contiguous.  Each thread evaluates taumol for its
-//              g-point layer by layer and runs that g-point's vertical
+//              of a single band for several columns (lanes per column: the
+//              next power of two >= the band's g count on the FP64 path, the
+//              g count itself on the split path), so every warp runs one
+//              band's straight-line gas-optics code and its table loads for
+//              one column are contiguous.  Each thread evaluates taumol for
+//              its g-point layer by layer and runs that g-point's vertical
 //              recursions in registers/local memory; at every level the
-//              g-point contributions of a column are summed with warp
-//              shuffles (FP64) and one lane stores the band partial.
-//   3. finalize one thread per column: band partials summed in band order
-//              (FP64), flux outputs, heating-rate differencing (FP64).
-// The column kernels (prep, finalize) are FP64 in both paths and are defined
-// only in the translation unit that defines RRTMG_DEFINE_COLUMN_KERNELS.
-// Real = double gives the FP64 path; Real = float gives the FP32-split path
-// (gas optics, transmittances, recursions in FP32; g-point sums, band sums and
-// heating-rate differences in FP64).
+//              g-point contributions of a column are summed (FP64 warp
+//              shuffles on the FP64 path, shared-memory staging with
+//              compensated FP32 sums on the split path) into FP64 band
+//              partials.
+//   3. finalize the band partials summed in band order (FP64), flux outputs,
+//              heating-rate differencing (FP64).
+// The column kernels (prep, FP64 finalize) are defined only in the
+// translation unit that defines RRTMG_DEFINE_COLUMN_KERNELS.  Real = double
+// gives the FP64 path; Real = float the FP32-split path.
 #pragma once
 #include <math.h>
 
@@ -99,7 +101,7 @@ struct GSum {
   __device__ __forceinline__ void flush(Store&& st) {
     __syncwarp();
     const int sl = lane % W, cs = lane / W;
-    if (sl < n) {
+    if (sl < n && cs < 32 / W) {
 #pragma unroll
       for (int b = 0; b < NB; ++b) {
         if (b >= nb) break;
@@ -130,6 +132,16 @@ struct GSum {
     if (++n == W) flush(st);
   }
 };
+// Lanes per column of a band with ng g-points: the next power of two on the
+// FP64 path (whose warp-shuffle sums need power-of-two groups) and in the
+// adjoint; on the split path ng itself where that fits more columns into a
+// warp (ng = 6: 5 columns instead of 4; ng = 10: 3 instead of 2; the tail
+// lanes of the warp idle), else the power of two.  Measured at 32768 columns:
+// SW solver 4.55 -> 4.1 ms, LW 3.36 -> 3.35 ms (ng for every band: LW 3.44 ms).
+__host__ __device__ constexpr int split_lanes(int ng, bool split) {
+  return (split && 32 / ng > 32 / pow2ceil(ng)) ? ng : pow2ceil(ng);
+}
+
 // Shared-memory floats of the staging buffers of one 128-thread block.
 constexpr int kGSumFloats = (kBlock / 32) * 2 * 16 * kRow;
 
@@ -377,13 +389,15 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
   const bool IDRV = idrv == 1;
   constexpr bool SPLIT = sizeof(R) == 4;
   constexpr int NG = lw_ng(B);
-  constexpr int W = pow2ceil(NG);
-  constexpr int CPB = kBlock / W;
-  const int lane_col = threadIdx.x / W, g = threadIdx.x % W;
+  constexpr int W = split_lanes(NG, SPLIT);
+  constexpr int CPW = 32 / W;
+  constexpr int CPB = (kBlock / 32) * CPW;
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int lane_col = wib * CPW + lane / W, g = lane % W;
   const int col = blk * CPB + lane_col;
-  const bool valid = col < ncol;
+  const bool valid = lane < CPW * W && col < ncol;
   const bool active = valid && g < NG;
-  const int c = valid ? col : ncol - 1;
+  const int c = valid ? col : (col < ncol ? col : ncol - 1);
   const int gg = g < NG ? g : NG - 1;
   const size_t N = (size_t)ncol;
   const int lt = p.laytrop[c];
@@ -398,9 +412,8 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
   double* bdup = IDRV ? bdu + (size_t)(B - 1) * (nlay + 1) * N + col : nullptr;
   // Split path: band sums through the warp's staging buffers; the summing
   // lane of column sub-index cs writes column wcol0 + cs.
-  const int wib = threadIdx.x >> 5;
-  const int wcol0 = blk * CPB + (wib * 32) / W;
-  GSum<W, NG, 2, false> gs{sbuf + (SPLIT ? wib * 2 * W * kRow : 0), nullptr, (int)(threadIdx.x & 31), 0, nlay - 1, -1,
+  const int wcol0 = blk * CPB + wib * CPW;
+  GSum<W, NG, 2, false> gs{sbuf + (SPLIT ? wib * 2 * W * kRow : 0), nullptr, lane, 0, nlay - 1, -1,
                            1};
   auto store_dn = [&](int b, int lev, int cs, double v) {
     const int cc = wcol0 + cs;
@@ -514,8 +527,9 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
   }
 }
 
-__host__ __device__ inline int lw_blocks_for_band(int ngpad, int ncol) {
-  const int cpb = kBlock / ngpad;
+// Blocks of a band for `lanes` lanes per column: 32 / lanes columns per warp.
+__host__ __device__ inline int lw_blocks_for_band(int lanes, int ncol) {
+  const int cpb = (kBlock / 32) * (32 / lanes);
   return (ncol + cpb - 1) / cpb;
 }
 
@@ -542,7 +556,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_LW_MINB :
   __shared__ float sbuf[sizeof(R) == 4 ? kGSumFloats : 1];
   int blk = blockIdx.x, band = 0;
   for (; band < kLwBands; ++band) {
-    const int nb = lw_blocks_for_band(c_lw.band[band].ngpad, ncol);
+    const int nb = lw_blocks_for_band(split_lanes(c_lw.band[band].ng, sizeof(R) == 4), ncol);
     if (blk < nb) break;
     blk -= nb;
   }
@@ -978,13 +992,15 @@ __device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, dou
                                         float* swt) {
   constexpr bool SPLIT = sizeof(R) == 4;
   constexpr int NG = sw_ng(B);
-  constexpr int W = pow2ceil(NG);
-  constexpr int CPB = kBlock / W;
+  constexpr int W = split_lanes(NG, SPLIT);
+  constexpr int CPW = 32 / W;
+  constexpr int CPB = (kBlock / 32) * CPW;
   constexpr int ibm = B - 15;  // 1..14
-  const int lane_col = threadIdx.x / W, g = threadIdx.x % W;
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int lane_col = wib * CPW + lane / W, g = lane % W;
   const int col = blk * CPB + lane_col;
-  const bool valid = col < ncol;
-  const int c = valid ? col : ncol - 1;
+  const bool valid = lane < CPW * W && col < ncol;
+  const int c = valid ? col : (col < ncol ? col : ncol - 1);
   const int gg = g < NG ? g : NG - 1;
   const size_t N = (size_t)ncol;
   const size_t fstride = (size_t)nlay * N;
@@ -1070,8 +1086,7 @@ __device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, dou
   // Split path: incident-flux-weighted band sums through the warp's staging
   // buffers (levels surface first); the summing lane of column sub-index cs
   // writes column wcol0 + cs.
-  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int wcol0 = blk * CPB + (wib * 32) / W;
+  const int wcol0 = blk * CPB + wib * CPW;
   GSum<W, NG, 2, true> gs{sbuf + (SPLIT ? wib * 2 * W * kRow : 0), swt + (SPLIT ? wib * 32 : 0), lane, 0, 0, 1, 2};
   if constexpr (SPLIT) swt[wib * 32 + lane] = active ? (float)zincflx : 0.f;
   auto store = [&](int b, int lev, int cs, double v) {
@@ -1128,7 +1143,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_SW_MINB :
   __shared__ float swt[sizeof(R) == 4 ? kBlock : 1];
   int blk = blockIdx.x, band = 0;
   for (; band < kSwBands; ++band) {
-    const int nb = lw_blocks_for_band(c_sw.band[band].ngpad, ncol);
+    const int nb = lw_blocks_for_band(split_lanes(c_sw.band[band].ng, sizeof(R) == 4), ncol);
     if (blk < nb) break;
     blk -= nb;
   }

@@ -14,14 +14,14 @@ cudaError_t upload_constants_fp64(const LwConst& lw, const SwConst& sw) {
   return cudaMemcpyToSymbol(c_sw, &sw, sizeof(SwConst));
 }
 
-int lw_gpoint_blocks(const LwConst& c, int ncol) {
+int lw_gpoint_blocks(const LwConst& c, int ncol, bool split) {
   int n = 0;
-  for (int b = 0; b < kLwBands; ++b) n += lw_blocks_for_band(c.band[b].ngpad, ncol);
+  for (int b = 0; b < kLwBands; ++b) n += lw_blocks_for_band(split_lanes(c.band[b].ng, split), ncol);
   return n;
 }
-int sw_gpoint_blocks(const SwConst& c, int ncol) {
+int sw_gpoint_blocks(const SwConst& c, int ncol, bool split) {
   int n = 0;
-  for (int b = 0; b < kSwBands; ++b) n += lw_blocks_for_band(c.band[b].ngpad, ncol);
+  for (int b = 0; b < kSwBands; ++b) n += lw_blocks_for_band(split_lanes(c.band[b].ng, split), ncol);
   return n;
 }
 

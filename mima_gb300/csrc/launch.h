@@ -51,8 +51,9 @@ void launch_sw_gpoint_split(const SwPrepT<float>& p, const SwIn& in, double adjf
                             const double* tab64, const float* exptbl, double* su, double* sd, int ncol, int nlay,
                             int nb, int analytic, cudaStream_t s);
 
-// Number of blocks of the g-point grids (sum over bands of columns / (128 / ngpad)).
-int lw_gpoint_blocks(const LwConst& c, int ncol);
-int sw_gpoint_blocks(const SwConst& c, int ncol);
+// Number of blocks of the g-point grids: the sum over bands of the band's
+// blocks (4 warps of 32 / lanes columns; lanes = split_lanes(ng, split)).
+int lw_gpoint_blocks(const LwConst& c, int ncol, bool split = false);
+int sw_gpoint_blocks(const SwConst& c, int ncol, bool split = false);
 
 }  // namespace rrtmg

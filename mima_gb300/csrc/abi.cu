@@ -446,7 +446,8 @@ int adj_run(rrtmg_gpu_state* h, cudaStream_t s, int ncol, int nlay, const LwIn& 
   AdjLwWork lw;
   AdjSwWork sw;
   carve_adj(h->adj_ws.p, ncol, nlay, nseed_lw, nseed_sw, &lw, &sw, nullptr);
-  const int nbl = lw_gpoint_blocks(h->host.lw, ncol), nbs = sw_gpoint_blocks(h->host.sw, ncol);
+  const bool split = h->precision == RRTMG_PREC_SPLIT;
+  const int nbl = lw_gpoint_blocks(h->host.lw, ncol, split), nbs = sw_gpoint_blocks(h->host.sw, ncol, split);
   if (h->precision == RRTMG_PREC_SPLIT) {
     // FP32 checkpoints in the same carving (they take half the room)
     const AdjLwWorkT<float> l32{lw.idx, lw.laytrop, (float*)lw.fv, (float*)lw.ft, (float*)lw.fq, (float*)lw.play_v,

@@ -252,7 +252,7 @@ struct GRed {
   __device__ __forceinline__ void flush(Store&& st) {
     __syncwarp();
     const int sl = lane % W, cs = lane / W;
-    if (sl < n) {
+    if (sl < n && cs < 32 / W) {
       const TS* row = buf + sl * kRow + cs * W;
       if constexpr (sizeof(TS) == 4) {
         float s = 0.f, c = 0.f;
@@ -314,12 +314,15 @@ __device__ __forceinline__ void lw_adj_band(const LwIn& in, const AdjLwWorkT<R>&
                                             double* sred) {
   using DR = Dual<R>;
   constexpr int NG = lw_ng(B);
-  constexpr int W = pow2ceil(NG);
-  constexpr int CPB = kBlock / W;
-  const int lane_col = threadIdx.x / W, g = threadIdx.x % W;
+  // lanes per column as in the forward solvers (packed on the split path)
+  constexpr int W = split_lanes(NG, sizeof(R) == 4);
+  constexpr int CPW = 32 / W;
+  constexpr int CPB = (kBlock / 32) * CPW;
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int lane_col = wib * CPW + lane / W, g = lane % W;
   const int col = blk * CPB + lane_col;
-  const bool valid = col < ncol;
-  const int c = valid ? col : ncol - 1;
+  const bool valid = lane < CPW * W && col < ncol;
+  const int c = valid ? col : (col < ncol ? col : ncol - 1);
   const int gg = g < NG ? g : NG - 1;
   const size_t N = (size_t)ncol;
   const size_t fstride = (size_t)nlay * N;
@@ -417,8 +420,7 @@ __device__ __forceinline__ void lw_adj_band(const LwIn& in, const AdjLwWorkT<R>&
   //              rho_m = atr_m c_m + t_m rho_{m-1};
   //    the same recursions as for lamU, lamD without the cancellation of
   //    c_{m+1} - t_{m+1} c_{m+1} (which costs FP32 its digits for thin layers).
-  const int wib = threadIdx.x >> 5;
-  const int wcol0 = blk * CPB + (wib * 32) / W;
+  const int wcol0 = blk * CPB + wib * CPW;
   for (int s = 0; s < nseed; ++s) {
     ck[0] = (R)0;
     for (int kk = 1; kk <= nlay; ++kk) {
@@ -485,7 +487,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_ADJ_MINB 
   __shared__ double sred[kRedDoubles];
   int blk = blockIdx.x, band = 0;
   for (; band < kLwBands; ++band) {
-    const int nb = lw_blocks_for_band(c_lw.band[band].ngpad, ncol);
+    const int nb = lw_blocks_for_band(split_lanes(c_lw.band[band].ng, sizeof(R) == 4), ncol);
     if (blk < nb) break;
     blk -= nb;
   }
@@ -658,13 +660,15 @@ __device__ __forceinline__ void sw_adj_band(const SwIn& in, const AdjSwWorkT<R>&
                                             double* sred) {
   using DR = Dual<R>;
   constexpr int NG = sw_ng(B);
-  constexpr int W = pow2ceil(NG);
-  constexpr int CPB = kBlock / W;
+  constexpr int W = split_lanes(NG, sizeof(R) == 4);
+  constexpr int CPW = 32 / W;
+  constexpr int CPB = (kBlock / 32) * CPW;
   constexpr int ibm = B - 15;
-  const int lane_col = threadIdx.x / W, g = threadIdx.x % W;
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int lane_col = wib * CPW + lane / W, g = lane % W;
   const int col = blk * CPB + lane_col;
-  const bool valid = col < ncol;
-  const int c = valid ? col : ncol - 1;
+  const bool valid = lane < CPW * W && col < ncol;
+  const int c = valid ? col : (col < ncol ? col : ncol - 1);
   const int gg = g < NG ? g : NG - 1;
   const size_t N = (size_t)ncol;
   const size_t fstride = (size_t)nlay * N;
@@ -762,8 +766,7 @@ __device__ __forceinline__ void sw_adj_band(const SwIn& in, const AdjSwWorkT<R>&
     }
   }
 
-  const int wib = threadIdx.x >> 5;
-  const int wcol0 = blk * CPB + (wib * 32) / W;
+  const int wcol0 = blk * CPB + wib * CPW;
   const double gate = lit ? 1.0 : 0.0;  // dark columns have zero SW outputs
   for (int s = 0; s < nseed; ++s) {
     // cotangent of net at every bottom-up level m (an[m]); layers 1..nlay-1 carry
@@ -942,7 +945,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_ADJ_MINB 
   __shared__ double sred[kRedDoubles];
   int blk = blockIdx.x, band = 0;
   for (; band < kSwBands; ++band) {
-    const int nb = lw_blocks_for_band(c_sw.band[band].ngpad, ncol);
+    const int nb = lw_blocks_for_band(split_lanes(c_sw.band[band].ng, sizeof(R) == 4), ncol);
     if (blk < nb) break;
     blk -= nb;
   }

@@ -475,9 +475,10 @@ __device__ __forceinline__ void lw_adj_band(const LwIn& in, const AdjLwWorkT<R>&
 
 // Minimum resident blocks per SM asked of the register allocator for the
 // FP32/FP64-split adjoint kernels (a VJP at 32768 columns x 40 layers on
-// GB300: 42.8 ms at 1, 28.8 ms at 8 and 10, 33.2 ms at 12); the FP64 ones: 1.
+// GB300 with packed lanes: 28.1 ms at 6, 24.0 ms at 8, 23.1 ms at 10,
+// 25.7 ms at 12); the FP64 ones: 1.
 #ifndef RRTMG_SPLIT_ADJ_MINB
-#define RRTMG_SPLIT_ADJ_MINB 8
+#define RRTMG_SPLIT_ADJ_MINB 10
 #endif
 
 template <class R, int MAXL>

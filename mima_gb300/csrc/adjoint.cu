@@ -485,7 +485,9 @@ template <class R, int MAXL>
 __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_ADJ_MINB : 1) lw_adj_kernel(LwIn in, AdjLwWorkT<R> w, const R* __restrict__ tab,
                                                         const double* __restrict__ cot, int nseed, int ncol,
                                                         int nlay) {
-  __shared__ double sred[kRedDoubles];
+  // FP32 entries take half the staging room: a smaller shared-memory carve-out
+  // leaves the split kernels more L1 for their per-thread arrays
+  __shared__ double sred[sizeof(R) == 4 ? kRedDoubles / 2 : kRedDoubles];
   int blk = blockIdx.x, band = 0;
   for (; band < kLwBands; ++band) {
     const int nb = lw_blocks_for_band(split_lanes(c_lw.band[band].ng, sizeof(R) == 4), ncol);
@@ -943,7 +945,9 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_ADJ_MINB 
                                                         const R* __restrict__ tab, const double* __restrict__ tab64,
                                                         const double* __restrict__ cot, int nseed, int ncol,
                                                         int nlay) {
-  __shared__ double sred[kRedDoubles];
+  // FP32 entries take half the staging room: a smaller shared-memory carve-out
+  // leaves the split kernels more L1 for their per-thread arrays
+  __shared__ double sred[sizeof(R) == 4 ? kRedDoubles / 2 : kRedDoubles];
   int blk = blockIdx.x, band = 0;
   for (; band < kSwBands; ++band) {
     const int nb = lw_blocks_for_band(split_lanes(c_sw.band[band].ng, sizeof(R) == 4), ncol);

@@ -87,16 +87,25 @@ __device__ __forceinline__ bool bad(double x) { return !isfinite(x); }
 // is a small fraction of its FP32 rate).  Explicitly rounded intrinsics keep
 // the compiler from contracting the error terms.  Rows are 33 floats wide so
 // that the staging stores and the per-lane row reads are free of bank
-// conflicts.  All lanes of the warp must call put/next/flush uniformly (the
-// level loops are warp-uniform).
+// conflicts.  A warp stages at most kStageRows rows: W levels of one stream
+// or half as many of two, so that the buffers of a block take 8.4 KB of shared
+// memory and a smaller shared-memory carve-out leaves L1 room for the solvers'
+// per-thread arrays.  All lanes of the warp must call put/next/flush
+// uniformly (the level loops are warp-uniform).
 constexpr int kRow = 33;
+constexpr int kStageRows = 16;
 template <int W, int NG, int NB, bool WEIGHTED>
 struct GSum {
-  float* buf;          // this warp's [NB][W][kRow]
+  float* buf;          // this warp's [kStageRows][kRow]
   const float* wt;     // this warp's [32] per-lane weights (WEIGHTED only)
   int lane, n, first, dir;
   int nb;              // streams in use (<= NB)
-  __device__ __forceinline__ void put(int b, float v) { buf[(b * W + n) * kRow + lane] = v; }
+  // levels staged per flush
+  __device__ __forceinline__ int cap() const { return W < kStageRows / nb ? W : kStageRows / nb; }
+  // streams beyond nb are not staged (the LW solver offers its idrv stream always)
+  __device__ __forceinline__ void put(int b, float v) {
+    if (b < nb) buf[(b * cap() + n) * kRow + lane] = v;
+  }
   template <class Store>
   __device__ __forceinline__ void flush(Store&& st) {
     __syncwarp();
@@ -105,7 +114,7 @@ struct GSum {
 #pragma unroll
       for (int b = 0; b < NB; ++b) {
         if (b >= nb) break;
-        const float* row = buf + (b * W + sl) * kRow + cs * W;
+        const float* row = buf + (b * cap() + sl) * kRow + cs * W;
         float s = 0.f, c = 0.f;
 #pragma unroll 2
         for (int g = 0; g < NG; ++g) {
@@ -129,7 +138,7 @@ struct GSum {
   }
   template <class Store>
   __device__ __forceinline__ void next(Store&& st) {
-    if (++n == W) flush(st);
+    if (++n == cap()) flush(st);
   }
 };
 // Lanes per column of a band with ng g-points: the next power of two on the
@@ -143,7 +152,7 @@ __host__ __device__ constexpr int split_lanes(int ng, bool split) {
 }
 
 // Shared-memory floats of the staging buffers of one 128-thread block.
-constexpr int kGSumFloats = (kBlock / 32) * 2 * 16 * kRow;
+constexpr int kGSumFloats = (kBlock / 32) * kStageRows * kRow;
 
 #ifdef RRTMG_DEFINE_COLUMN_KERNELS
 // ---------------------------------------------------------------------------
@@ -413,7 +422,7 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
   // Split path: band sums through the warp's staging buffers; the summing
   // lane of column sub-index cs writes column wcol0 + cs.
   const int wcol0 = blk * CPB + wib * CPW;
-  GSum<W, NG, 2, false> gs{sbuf + (SPLIT ? wib * 2 * W * kRow : 0), nullptr, lane, 0, nlay - 1, -1,
+  GSum<W, NG, 2, false> gs{sbuf + (SPLIT ? wib * kStageRows * kRow : 0), nullptr, lane, 0, nlay - 1, -1,
                            1};
   auto store_dn = [&](int b, int lev, int cs, double v) {
     const int cc = wcol0 + cs;
@@ -1087,7 +1096,7 @@ __device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, dou
   // buffers (levels surface first); the summing lane of column sub-index cs
   // writes column wcol0 + cs.
   const int wcol0 = blk * CPB + wib * CPW;
-  GSum<W, NG, 2, true> gs{sbuf + (SPLIT ? wib * 2 * W * kRow : 0), swt + (SPLIT ? wib * 32 : 0), lane, 0, 0, 1, 2};
+  GSum<W, NG, 2, true> gs{sbuf + (SPLIT ? wib * kStageRows * kRow : 0), swt + (SPLIT ? wib * 32 : 0), lane, 0, 0, 1, 2};
   if constexpr (SPLIT) swt[wib * 32 + lane] = active ? (float)zincflx : 0.f;
   auto store = [&](int b, int lev, int cs, double v) {
     const int cc = wcol0 + cs;

@@ -93,7 +93,10 @@ __device__ __forceinline__ bool bad(double x) { return !isfinite(x); }
 // per-thread arrays.  All lanes of the warp must call put/next/flush
 // uniformly (the level loops are warp-uniform).
 constexpr int kRow = 33;
-constexpr int kStageRows = 16;
+#ifndef RRTMG_STAGE_ROWS
+#define RRTMG_STAGE_ROWS 16
+#endif
+constexpr int kStageRows = RRTMG_STAGE_ROWS;
 template <int W, int NG, int NB, bool WEIGHTED>
 struct GSum {
   float* buf;          // this warp's [kStageRows][kRow]

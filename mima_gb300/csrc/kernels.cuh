@@ -558,7 +558,10 @@ __host__ __device__ inline int lw_blocks_for_band(int lanes, int ncol) {
 #define RRTMG_SPLIT_SW_MINB 12
 #endif
 
-template <class R, int MAXL>
+// FL < 0: analytic and idrv as passed; FL >= 0: compile-time flags (bit 0
+// analytic, bit 1 idrv = 1), so that the code of the unused branches folds
+// away (the split path instantiates all four).
+template <class R, int MAXL, int FL = -1>
 __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_LW_MINB : 1) lw_gpoint_kernel(LwPrepT<R> p, const double* __restrict__ emis,
                                                            const double* __restrict__ tauaer,
                                                            const R* __restrict__ tab, const R* __restrict__ exptbl,
@@ -572,8 +575,10 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_LW_MINB :
     if (blk < nb) break;
     blk -= nb;
   }
+  const bool an = FL < 0 ? analytic != 0 : (FL & 1) != 0;
+  const int idv = FL < 0 ? idrv : ((FL & 2) ? 1 : 0);
 #define RRTMG_LW_CASE(b) \
-  case b - 1: lw_band<b, R, MAXL>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv, analytic != 0, blk, sbuf); break;
+  case b - 1: lw_band<b, R, MAXL>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idv, an, blk, sbuf); break;
   switch (band) {
     RRTMG_LW_CASE(1) RRTMG_LW_CASE(2) RRTMG_LW_CASE(3) RRTMG_LW_CASE(4) RRTMG_LW_CASE(5) RRTMG_LW_CASE(6)
     RRTMG_LW_CASE(7) RRTMG_LW_CASE(8) RRTMG_LW_CASE(9) RRTMG_LW_CASE(10) RRTMG_LW_CASE(11) RRTMG_LW_CASE(12)
@@ -1146,7 +1151,9 @@ __device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, dou
   }
 }
 
-template <class R, int MAXL>
+// FL < 0: analytic and iaer as passed; FL >= 0: compile-time flags (bit 0
+// analytic, bit 1 iaer = 10), as for the LW kernel.
+template <class R, int MAXL, int FL = -1>
 __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_SW_MINB : 1) sw_gpoint_kernel(SwPrepT<R> p, SwIn in, double adjflux, int iaer,
                                                            const R* __restrict__ tab, const double* __restrict__ tab64,
                                                            const R* __restrict__ exptbl, double* su, double* sd,
@@ -1159,8 +1166,10 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_SW_MINB :
     if (blk < nb) break;
     blk -= nb;
   }
+  const bool an = FL < 0 ? analytic != 0 : (FL & 1) != 0;
+  const int ia = FL < 0 ? iaer : ((FL & 2) ? 10 : 0);
 #define RRTMG_SW_CASE(b) \
-  case b - 16: sw_band<b, R, MAXL>(p, in, adjflux, iaer, tab, tab64, exptbl, su, sd, ncol, nlay, analytic != 0, blk, sbuf, swt); break;
+  case b - 16: sw_band<b, R, MAXL>(p, in, adjflux, ia, tab, tab64, exptbl, su, sd, ncol, nlay, an, blk, sbuf, swt); break;
   switch (band) {
     RRTMG_SW_CASE(16) RRTMG_SW_CASE(17) RRTMG_SW_CASE(18) RRTMG_SW_CASE(19) RRTMG_SW_CASE(20) RRTMG_SW_CASE(21)
     RRTMG_SW_CASE(22) RRTMG_SW_CASE(23) RRTMG_SW_CASE(24) RRTMG_SW_CASE(25) RRTMG_SW_CASE(26) RRTMG_SW_CASE(27)

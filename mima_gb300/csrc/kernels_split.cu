@@ -148,22 +148,47 @@ void launch_sw_finalize_split(const double* su, const double* sd, const double* 
                                              swhrc);
 }
 
+// The split solvers are instantiated per (analytic, idrv / aerosol) flag pair.
+template <int MAXL>
+static void lw_split_flags(int fl, int nb, cudaStream_t s, const LwPrepT<float>& p, const double* emis,
+                           const double* tauaer, const float* tab, const float* exptbl, const float* tfntbl, double* bu,
+                           double* bd, double* bdu, int ncol, int nlay, int idrv, int analytic) {
+  auto k = fl == 0 ? lw_gpoint_kernel<float, MAXL, 0>
+         : fl == 1 ? lw_gpoint_kernel<float, MAXL, 1>
+         : fl == 2 ? lw_gpoint_kernel<float, MAXL, 2>
+                   : lw_gpoint_kernel<float, MAXL, 3>;
+  k<<<nb, kBlock, 0, s>>>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv, analytic);
+}
+
 void launch_lw_gpoint_split(const LwPrepT<float>& p, const double* emis, const double* tauaer, const float* tab,
                             const float* exptbl, const float* tfntbl, double* bu, double* bd, double* bdu, int ncol,
                             int nlay, int idrv, int nb, int analytic, cudaStream_t s) {
+  const int fl = (analytic ? 1 : 0) | (idrv == 1 ? 2 : 0);
   if (maxl_for(nlay) == 64)
-    lw_gpoint_kernel<float, 64><<<nb, kBlock, 0, s>>>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv, analytic);
+    lw_split_flags<64>(fl, nb, s, p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv, analytic);
   else
-    lw_gpoint_kernel<float, 208><<<nb, kBlock, 0, s>>>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv, analytic);
+    lw_split_flags<208>(fl, nb, s, p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv, analytic);
+}
+
+template <int MAXL>
+static void sw_split_flags(int fl, int nb, cudaStream_t s, const SwPrepT<float>& p, const SwIn& in, double adjflux,
+                           int iaer, const float* tab, const double* tab64, const float* exptbl, double* su,
+                           double* sd, int ncol, int nlay, int analytic) {
+  auto k = fl == 0 ? sw_gpoint_kernel<float, MAXL, 0>
+         : fl == 1 ? sw_gpoint_kernel<float, MAXL, 1>
+         : fl == 2 ? sw_gpoint_kernel<float, MAXL, 2>
+                   : sw_gpoint_kernel<float, MAXL, 3>;
+  k<<<nb, kBlock, 0, s>>>(p, in, adjflux, iaer, tab, tab64, exptbl, su, sd, ncol, nlay, analytic);
 }
 
 void launch_sw_gpoint_split(const SwPrepT<float>& p, const SwIn& in, double adjflux, int iaer, const float* tab,
                             const double* tab64, const float* exptbl, double* su, double* sd, int ncol, int nlay,
                             int nb, int analytic, cudaStream_t s) {
+  const int fl = (analytic ? 1 : 0) | (iaer == 10 ? 2 : 0);
   if (maxl_for(nlay) == 64)
-    sw_gpoint_kernel<float, 64><<<nb, kBlock, 0, s>>>(p, in, adjflux, iaer, tab, tab64, exptbl, su, sd, ncol, nlay, analytic);
+    sw_split_flags<64>(fl, nb, s, p, in, adjflux, iaer, tab, tab64, exptbl, su, sd, ncol, nlay, analytic);
   else
-    sw_gpoint_kernel<float, 208><<<nb, kBlock, 0, s>>>(p, in, adjflux, iaer, tab, tab64, exptbl, su, sd, ncol, nlay, analytic);
+    sw_split_flags<208>(fl, nb, s, p, in, adjflux, iaer, tab, tab64, exptbl, su, sd, ncol, nlay, analytic);
 }
 
 }  // namespace rrtmg

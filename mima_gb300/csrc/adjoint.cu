@@ -940,7 +940,9 @@ __device__ __forceinline__ void sw_adj_band(const SwIn& in, const AdjSwWorkT<R>&
   }
 }
 
-template <class R, int MAXL>
+// AER < 0: iaer as passed; 0 / 1: compile-time aerosol flag (the split adjoint
+// instantiates both, so that the aerosol code folds away without aerosols).
+template <class R, int MAXL, int AER = -1>
 __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_ADJ_MINB : 1) sw_adj_kernel(SwIn in, AdjSwWorkT<R> w, double adjflux, int iaer,
                                                         const R* __restrict__ tab, const double* __restrict__ tab64,
                                                         const double* __restrict__ cot, int nseed, int ncol,
@@ -954,8 +956,9 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_ADJ_MINB 
     if (blk < nb) break;
     blk -= nb;
   }
+  const int ia = AER < 0 ? iaer : (AER ? 10 : 0);
 #define RRTMG_SW_ADJ_CASE(b) \
-  case b - 16: sw_adj_band<b, R, MAXL>(in, w, adjflux, iaer, tab, tab64, cot, nseed, ncol, nlay, blk, sred); break;
+  case b - 16: sw_adj_band<b, R, MAXL>(in, w, adjflux, ia, tab, tab64, cot, nseed, ncol, nlay, blk, sred); break;
   switch (band) {
     RRTMG_SW_ADJ_CASE(16) RRTMG_SW_ADJ_CASE(17) RRTMG_SW_ADJ_CASE(18) RRTMG_SW_ADJ_CASE(19) RRTMG_SW_ADJ_CASE(20)
     RRTMG_SW_ADJ_CASE(21) RRTMG_SW_ADJ_CASE(22) RRTMG_SW_ADJ_CASE(23) RRTMG_SW_ADJ_CASE(24) RRTMG_SW_ADJ_CASE(25)
@@ -1063,9 +1066,11 @@ void launch_adj_sw_split(const SwIn& in, const AdjSwWorkT<float>& w, double adjf
                          cudaStream_t s) {
   adj_sw_prep_kernel<float><<<(ncol + 127) / 128, 128, 0, s>>>(in, w, ncol, nlay);
   if (maxl_for(nlay) == 64)
-    sw_adj_kernel<float, 64><<<nb, kBlock, 0, s>>>(in, w, adjflux, iaer, tab, tab64, cot, nseed, ncol, nlay);
+    (iaer == 10 ? sw_adj_kernel<float, 64, 1> : sw_adj_kernel<float, 64, 0>)<<<nb, kBlock, 0, s>>>(
+        in, w, adjflux, iaer, tab, tab64, cot, nseed, ncol, nlay);
   else
-    sw_adj_kernel<float, 208><<<nb, kBlock, 0, s>>>(in, w, adjflux, iaer, tab, tab64, cot, nseed, ncol, nlay);
+    (iaer == 10 ? sw_adj_kernel<float, 208, 1> : sw_adj_kernel<float, 208, 0>)<<<nb, kBlock, 0, s>>>(
+        in, w, adjflux, iaer, tab, tab64, cot, nseed, ncol, nlay);
 }
 
 void launch_adj_finalize(const AdjLwWork& lw, const AdjSwWork& sw, const double* plev, const double* coszen,

@@ -547,15 +547,16 @@ __host__ __device__ inline int lw_blocks_for_band(int lanes, int ncol) {
 
 // Minimum resident blocks per SM asked of the register allocator for the
 // FP32-split solvers.  They are latency-bound (table gathers, local-memory
-// column arrays), so occupancy pays even at the price of a few spills: on
-// GB300 at 32768 columns x 40 layers, 12/12 (40-42 registers) ran the LW+SW
-// split step in 11.1 ms against 19.0 ms at 1/1 (105 registers).  FP64
-// solvers: 1.
+// column arrays), so occupancy pays even at the price of spills: on GB300 at
+// 32768 columns x 40 layers, 12/12 (40 registers) first ran the LW+SW split
+// step in 11.1 ms against 19.0 ms at 1/1 (105 registers).  Re-measured with
+// the flag-specialised solvers: LW 3.11 ms at 12, 3.27 at 10; SW 3.65 ms at
+// 12, 3.58 at 14 (32 registers).  FP64 solvers: 1.
 #ifndef RRTMG_SPLIT_LW_MINB
 #define RRTMG_SPLIT_LW_MINB 12
 #endif
 #ifndef RRTMG_SPLIT_SW_MINB
-#define RRTMG_SPLIT_SW_MINB 12
+#define RRTMG_SPLIT_SW_MINB 14
 #endif
 
 // FL < 0: analytic and idrv as passed; FL >= 0: compile-time flags (bit 0

@@ -263,6 +263,7 @@ def test_split_adjoint_against_fp64_adjoint(gpu, cfg3):
     assert err.max() <= 1e-2
 
 
+@pytest.mark.gpu
 def test_split_vjp_against_split_jacobian_and_fp64_vjp(gpu, cfg3):
     """The split VJP (its own lean reverse: layer cotangents contracted with
     tangents recomputed at the end) equals cot^T J of the split Jacobian to

@@ -480,9 +480,15 @@ __device__ __forceinline__ void lw_adj_band(const LwIn& in, const AdjLwWorkT<R>&
 #ifndef RRTMG_SPLIT_ADJ_MINB
 #define RRTMG_SPLIT_ADJ_MINB 10
 #endif
+#ifndef RRTMG_SPLIT_ADJ_LW_MINB
+#define RRTMG_SPLIT_ADJ_LW_MINB RRTMG_SPLIT_ADJ_MINB
+#endif
+#ifndef RRTMG_SPLIT_ADJ_SW_MINB
+#define RRTMG_SPLIT_ADJ_SW_MINB RRTMG_SPLIT_ADJ_MINB
+#endif
 
 template <class R, int MAXL>
-__global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_ADJ_MINB : 1) lw_adj_kernel(LwIn in, AdjLwWorkT<R> w, const R* __restrict__ tab,
+__global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_ADJ_LW_MINB : 1) lw_adj_kernel(LwIn in, AdjLwWorkT<R> w, const R* __restrict__ tab,
                                                         const double* __restrict__ cot, int nseed, int ncol,
                                                         int nlay) {
   // FP32 entries take half the staging room: a smaller shared-memory carve-out
@@ -943,7 +949,7 @@ __device__ __forceinline__ void sw_adj_band(const SwIn& in, const AdjSwWorkT<R>&
 // AER < 0: iaer as passed; 0 / 1: compile-time aerosol flag (the split adjoint
 // instantiates both, so that the aerosol code folds away without aerosols).
 template <class R, int MAXL, int AER = -1>
-__global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_ADJ_MINB : 1) sw_adj_kernel(SwIn in, AdjSwWorkT<R> w, double adjflux, int iaer,
+__global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_ADJ_SW_MINB : 1) sw_adj_kernel(SwIn in, AdjSwWorkT<R> w, double adjflux, int iaer,
                                                         const R* __restrict__ tab, const double* __restrict__ tab64,
                                                         const double* __restrict__ cot, int nseed, int ncol,
                                                         int nlay) {

@@ -341,7 +341,7 @@ def measure_adjoint(torch, rrtmg, atmosphere, r, stream, atm, d, olw, osw, flush
             "forward_plus_vjp_over_forward": (ms_f + ms_v) / ms_f,
             "vjp_columns_per_s": atm.ncol / (ms_v * 1e-3),
             "split": {"forward_ms": ms_fs, "vjp_ms": ms_vs, "forward_plus_vjp_over_forward": (ms_fs + ms_vs) / ms_fs,
-                      "note": "FP32 dual numbers and reverse sweeps, FP64 g-point and band sums; analytic forward"},
+                      "note": "FP32 dual numbers and reverse sweeps, FP64-accurate g-point sums, FP64 band sums; analytic forward"},
             "jacobian": {"workload": f"T42x40 adjoint configuration, {a3.ncol} columns", "ms": ms_j,
                          "forward_ms": ms_f3, "rows": ny3, "inputs": nx3,
                          "forward_plus_jacobian_over_forward": (ms_f3 + ms_j) / ms_f3}}

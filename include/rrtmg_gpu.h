@@ -52,8 +52,9 @@ enum rrtmg_gpu_status {
 
 enum rrtmg_gpu_precision {
   RRTMG_PREC_FP64 = 0,  /* FP64 everywhere; bit-level parity target vs the FP64 reference path */
-  RRTMG_PREC_SPLIT = 1  /* FP32 gas optics, transmittances and per-g recursions; FP64 g-point
-                           accumulation and heating-rate differencing */
+  RRTMG_PREC_SPLIT = 1  /* FP32 setcoef, gas optics, transmittances and per-g recursions;
+                           g-point sums to FP64 accuracy (compensated FP32), FP64 band sums
+                           and heating-rate differencing */
 };
 
 /* Maximum number of layers (parrrtm.f90 / parrrsw.f90 mxlay). */
@@ -197,7 +198,8 @@ int rrtmg_gpu_sync_status(rrtmg_gpu_handle h, void* stream);
  *     humidity) of layers 1..nlay, tlev of levels 0..nlay, tsfc.
  * The differentiated forward is RRTMG_TRANS_ANALYTIC (the reference's
  * transmittance tables are piecewise constant in optical depth), in FP64, or
- * with RRTMG_PREC_SPLIT in FP32 with FP64 g-point and band sums; no counterpart
+ * with RRTMG_PREC_SPLIT in FP32 with FP64-accurate g-point sums and FP64 band
+ * sums; no counterpart
  * in the reference, which has only the LW surface-temperature derivative
  * (idrv = 1, rrtmg_lw_rtrnmr.f90:628-745).  The reverse sweeps of rtrnmr and
  * spcvrt run per g-point with the layer optics recomputed from checkpointed

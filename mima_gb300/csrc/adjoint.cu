@@ -17,9 +17,10 @@
 //      first-order sweeps; spcvrt: the reverse of the upward reflectance and
 //      of the downward transmission sweeps) and the layer gradients are
 //      contracted with the local tangents;
-//   4. gradients are summed over the band's g-points in FP64 (shared-memory
-//      staging, one (column, entry) sum per lane) into per-band partials,
-//      which a finalize kernel weights and sums over bands.
+//   4. gradients are summed over the band's g-points (shared-memory staging,
+//      one (column, entry) sum per lane; FP64 sums, or compensated FP32 sums
+//      in the split adjoint) into FP64 per-band partials, which a finalize
+//      kernel weights and sums over bands.
 #include <cuda_runtime.h>
 
 #include "adjoint.h"

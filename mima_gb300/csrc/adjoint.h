@@ -56,7 +56,8 @@ void launch_adj_lw(const LwIn& in, const AdjLwWork& w, const double* totplnk, co
                    const double* cot, int nseed, int ncol, int nlay, int nb, cudaStream_t s);
 void launch_adj_sw(const SwIn& in, const AdjSwWork& w, double adjflux, int iaer, const double* tab,
                    const double* cot, int nseed, int ncol, int nlay, int nb, cudaStream_t s);
-// FP32/FP64-split adjoint: FP32 dual numbers and reverse sweeps, FP64 sums.
+// FP32/FP64-split adjoint: FP32 dual numbers and reverse sweeps, g-point sums
+// to FP64 accuracy, FP64 band sums.
 void launch_adj_lw_split(const LwIn& in, const AdjLwWorkT<float>& w, const float* totplnk, const float* tab,
                          const double* cot, int nseed, int ncol, int nlay, int nb, cudaStream_t s);
 void launch_adj_sw_split(const SwIn& in, const AdjSwWorkT<float>& w, double adjflux, int iaer, const float* tab,

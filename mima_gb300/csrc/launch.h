@@ -15,7 +15,7 @@ inline int maxl_for(int nlay) { return nlay <= 64 ? 64 : 208; }
 cudaError_t upload_constants_fp64(const LwConst& lw, const SwConst& sw);
 cudaError_t upload_constants_split(const LwConst& lw, const SwConst& sw);
 
-// FP64 translation unit: prep, FP64 g-point solvers, finalize.
+// FP64 translation unit: prep (FP64 and FP32), FP64 g-point solvers, FP64 finalize.
 void launch_lw_prep(const LwIn& in, const LwWork& w, const double* totplnk, const double* totplnkderiv, int ncol,
                     int nlay, int idrv, unsigned* flags, cudaStream_t s);
 void launch_lw_gpoint_fp64(const LwPrep& p, const double* emis, const double* tauaer, const double* tab,

@@ -145,6 +145,26 @@ def executed_flops(kernel, ncol):
     return None if f is None else float(f) * ncol
 
 
+# Algorithmic FLOPs per column of the reference's clear-sky arithmetic (one
+# two-stream pass, analytic exp, every operation 1), counted by the oracle's
+# FLOP-count build at 20/40/60/80 layers and checked by tests/test_opcount.py.
+ALG_FLOPS_LAYERS = (20, 40, 60, 80)
+ALG_FLOPS_PER_COLUMN = {"lw_gpoint": (143454, 285492, 418424, 556934),
+                        "sw_gpoint": (405562, 811754, 1209065, 1612670)}
+ALG_FLOPS_FIT = {"lw_gpoint": (6866.845, 7733.75), "sw_gpoint": (20093.184, 5103.625)}
+
+
+def algorithmic_flops(kernel, nlay):
+    """Counted algorithmic FLOPs per column of the LW or SW path at nlay layers:
+    interpolated between the counted layer counts, the least-squares line
+    (slope, intercept) outside them."""
+    Ls, ys = ALG_FLOPS_LAYERS, ALG_FLOPS_PER_COLUMN[kernel]
+    if Ls[0] <= nlay <= Ls[-1]:
+        return float(np.interp(nlay, Ls, ys))
+    a, b = ALG_FLOPS_FIT[kernel]
+    return a * nlay + b
+
+
 # FP32 (non-tensor) peak of the GB300 at its 2070 MHz maximum SM clock:
 # 152 SMs x 128 FP32 lanes x 2 operations per FMA.
 FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12
@@ -623,6 +643,10 @@ def run_ours(args):
                    "frac": tf / FP32_PEAK_TFLOPS, "executed_flops_per_launch": flops,
                    "note": "executed FP32 operations (ncu, FMA = 2) / CUDA-event kernel time; nominal peak "
                            "152 SMs x 128 lanes x 2 x 2.07 GHz"}
+        alg = algorithmic_flops(dom, atm.nlay) * atm.ncol
+        atf = alg / (kms32[dom] * 1e-3) / 1e12
+        compute.update({"algorithmic_flops_per_launch": alg, "algorithmic_achieved": atf,
+                        "algorithmic_frac": atf / FP32_PEAK_TFLOPS})
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True, "scaling": "weak",

@@ -25,7 +25,8 @@ void launch_lw_finalize(const double* bu, const double* bd, const double* bdu, c
                         int idrv, double* uflx, double* dflx, double* hr, double* uflxc, double* dflxc, double* hrc,
                         double* duflx_dt, double* duflxc_dt, cudaStream_t s);
 void launch_sw_prep(const SwIn& in, const SwWork& w, int ncol, int nlay, unsigned* flags, cudaStream_t s);
-// Prep for the FP32-split solvers: the same FP64 arithmetic, fields stored as float.
+// Prep for the FP32-split solvers: the same steps in FP32 arithmetic (FP32 Planck
+// tables), fields stored as float.
 void launch_lw_prep_split(const LwIn& in, const LwWorkT<float>& w, const float* totplnk, const float* totplnkderiv,
                           int ncol, int nlay, int idrv, unsigned* flags, cudaStream_t s);
 void launch_sw_prep_split(const SwIn& in, const SwWorkT<float>& w, int ncol, int nlay, unsigned* flags,

@@ -12,6 +12,14 @@
 // Build with -ffp-contract=off.
 #include "oracle_sw.hpp"
 
+// Markers of the FLOP-count build (opcount.hpp): the work between them is the
+// reference's second ("total") two-stream pass, which in clear sky repeats the
+// clear pass, and is left out of the algorithmic count.  No-ops otherwise.
+#ifndef OPC_PAUSE
+#define OPC_PAUSE() ((void)0)
+#define OPC_RESUME() ((void)0)
+#endif
+
 #include <cmath>
 
 namespace orc {
@@ -838,33 +846,45 @@ void sw_spcvrt(SwColumn& c, double prmu0, const double* albdir, const double* al
         zomcc[jk] = (zomcc[jk] - zwf) / (1.0 - zwf);
         zgcc[jk] = (zgcc[jk] - zf) / (1.0 - zf);
         // icpr >= 1 with ptauc = 0, pomgc = 1, pasyc = 0
+        OPC_PAUSE();
         const double ptauc = 0.0, pomgc = 1.0, pasyc = 0.0;
         ztauo[jk] = ztauc[jk] + ptauc;
         zomco[jk] = ztauc[jk] * zomcc[jk] + ptauc * pomgc;
         zgco[jk] = (ptauc * pomgc * pasyc + ztauc[jk] * zomcc[jk] * zgcc[jk]) / zomco[jk];
         zomco[jk] = zomco[jk] / ztauo[jk];
+        OPC_RESUME();
       }
       reftra(klev, lrtchkclr, zgcc, prmu0, ztauc, zomcc, zrefc, zrefdc, ztrac, ztradc);
+      OPC_PAUSE();
       reftra(klev, lrtchkcld, zgco, prmu0, ztauo, zomco, zrefo, zrefdo, ztrao, ztrado);
+      OPC_RESUME();
       for (int jk = 1; jk <= klev; ++jk) {
+        OPC_PAUSE();
         const double zclear = 1.0 - 0.0, zcloud = 0.0;
         zref[jk] = zclear * zrefc[jk] + zcloud * zrefo[jk];
         zrefd[jk] = zclear * zrefdc[jk] + zcloud * zrefdo[jk];
         ztra[jk] = zclear * ztrac[jk] + zcloud * ztrao[jk];
         ztrad[jk] = zclear * ztradc[jk] + zcloud * ztrado[jk];
+        OPC_RESUME();
         double zdbtmc = sw_exp(ztauc[jk] / prmu0);
         zdbtc[jk] = zdbtmc;
         ztdbtc[jk + 1] = zdbtc[jk] * ztdbtc[jk];
+        OPC_PAUSE();
         double zdbtmo = sw_exp(ztauo[jk] / prmu0);
         zdbt[jk] = zclear * zdbtmc + zcloud * zdbtmo;
         ztdbt[jk + 1] = zdbt[jk] * ztdbt[jk];
+        OPC_RESUME();
       }
       vrtqdr(klev, zrefc, zrefdc, ztrac, ztradc, zdbtc, ztdbtc, zcd, zcu);
+      OPC_PAUSE();
       vrtqdr(klev, zref, zrefd, ztra, ztrad, zdbt, ztdbt, zfd, zfu);
+      OPC_RESUME();
       for (int jk = 1; jk <= klev + 1; ++jk) {
         int ikl = klev + 2 - jk;
+        OPC_PAUSE();
         out.fu[ikl] = out.fu[ikl] + zincflx * zfu[jk];
         out.fd[ikl] = out.fd[ikl] + zincflx * zfd[jk];
+        OPC_RESUME();
         out.cu[ikl] = out.cu[ikl] + zincflx * zcu[jk];
         out.cd[ikl] = out.cd[ikl] + zincflx * zcd[jk];
       }

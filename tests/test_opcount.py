@@ -1,0 +1,52 @@
+"""The oracle's FLOP-count build (oracle/opcount.hpp, oracle/opcount.py): it
+computes what the normal build computes, bit for bit, and its counts of the
+algorithmic work per column are linear in the layer count.  No GPU."""
+import numpy as np
+import pytest
+
+from mima_gb300 import atmosphere as A
+from oracle import opcount as P
+
+
+@pytest.fixture(scope="module")
+def counting(blob):
+    return P.load(blob)
+
+
+def test_counting_build_reproduces_the_oracle(orc, counting):
+    atm = A.small_atmosphere(5, 40, seed=21)
+    orc.set_table_mode(False)  # the count is taken in the analytic form
+    try:
+        rlw, rsw = orc.rrtmg_lw(atm), orc.rrtmg_sw(atm)
+    finally:
+        orc.set_table_mode(True)
+    lw, sw, cl, cs = P.count(atm)
+    for k in rlw:
+        np.testing.assert_array_equal(lw[k], rlw[k], err_msg=k)
+    for k in rsw:
+        np.testing.assert_array_equal(sw[k], rsw[k], err_msg=k)
+    assert P.flops(cl) > 0 and P.flops(cs) > 0
+
+
+def test_flops_per_column_linear_in_layers(blob, counting):
+    rows, flw, fsw = P.table(blob, layers=(20, 40, 60), ncol=4)
+    for L, lw, sw, _, _ in rows:
+        assert abs(lw - np.polyval(flw, L)) <= 0.02 * lw
+        assert abs(sw - np.polyval(fsw, L)) <= 0.02 * sw
+        # the structural estimates (LW 140 g x L x ~55, SW 112 g x L x ~150 FLOPs)
+        assert 0.5 <= lw / (140 * L * 55) <= 2.0
+        assert 0.5 <= sw / (112 * L * 150) <= 2.0
+    # the committed per-column figures at 40 layers (0.285 / 0.812 MFLOP), within 3 %
+    L40 = {r[0]: r for r in rows}[40]
+    assert abs(L40[1] / 0.285e6 - 1) <= 0.03 and abs(L40[2] / 0.812e6 - 1) <= 0.03
+
+
+def test_bench_constants_are_the_counted_table(blob, counting):
+    import bench
+    rows, flw, fsw = P.table(blob, layers=bench.ALG_FLOPS_LAYERS)
+    assert tuple(round(r[1]) for r in rows) == bench.ALG_FLOPS_PER_COLUMN["lw_gpoint"]
+    assert tuple(round(r[2]) for r in rows) == bench.ALG_FLOPS_PER_COLUMN["sw_gpoint"]
+    np.testing.assert_allclose(bench.ALG_FLOPS_FIT["lw_gpoint"], flw, rtol=1e-6)
+    np.testing.assert_allclose(bench.ALG_FLOPS_FIT["sw_gpoint"], fsw, rtol=1e-6)
+    assert bench.algorithmic_flops("sw_gpoint", 40) == bench.ALG_FLOPS_PER_COLUMN["sw_gpoint"][1]
+    assert bench.algorithmic_flops("lw_gpoint", 100) == pytest.approx(flw[0] * 100 + flw[1])

@@ -29,6 +29,12 @@ def test_library_exports_every_declared_symbol():
         assert hasattr(lib, s), s
 
 
+def test_integration_guide_names_every_entry_point():
+    text = (ROOT / "INTEGRATION.md").read_text()
+    missing = [s for s in header_symbols() if f"`{s}" not in text and f"{s}(" not in text]
+    assert not missing, missing
+
+
 def test_host_only_error_paths(tmp_path):
     lib = R.load_library()
     assert lib.rrtmg_gpu_error_string(0) == b"success"

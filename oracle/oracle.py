@@ -86,6 +86,21 @@ def rrtmg_lw(atm, idrv: int = 0, tauaer=None, nthreads: int = 0):
     return out
 
 
+def rrtmg_lw_bands(atm, idrv: int = 0):
+    """Per-band clear-sky LW fluxes: dict of (16, nlev, ncol) arrays "uflx",
+    "dflx" and (idrv = 1) "duflx_dt", one column at a time, W/m2."""
+    n, L = atm.ncol, atm.nlay
+    out = {k: np.zeros((16, L + 1, n)) for k in ("uflx", "dflx", "duflx_dt")}
+    args = [_f(atm.play), _f(atm.plev), _f(atm.tlay), _f(atm.tlev), _f(atm.tsfc), _f(atm.h2o),
+            _f(atm.o3), _f(atm.co2), _f(atm.ch4), _f(atm.n2o), _f(atm.o2), _f(atm.cfc11),
+            _f(atm.cfc12), _f(atm.cfc22), _f(atm.ccl4), _f(atm.emis)]
+    rc = _lib.orc_rrtmg_lw_bands(C.c_int(n), C.c_int(L), C.c_int(idrv), *[_p(a) for a in args],
+                                 _p(out["uflx"]), _p(out["dflx"]), _p(out["duflx_dt"]))
+    if rc != 0:
+        raise RuntimeError(f"orc_rrtmg_lw_bands failed ({rc})")
+    return out
+
+
 def rrtmg_sw(atm, iaer: int = 0, tauaer=None, ssaaer=None, asmaer=None, nthreads: int = 0):
     n, L = atm.ncol, atm.nlay
     out = {k: np.zeros((L + 1, n)) for k in ("swuflx", "swdflx", "swuflxc", "swdflxc")}

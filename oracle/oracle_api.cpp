@@ -120,6 +120,38 @@ int orc_rrtmg_sw(int ncol, int nlay, int icld, int iaer, const double* play, con
   return 0;
 }
 
+// Clear-sky rrtmg_lw per band: bandu/bandd/dbandu_dt (ncol, nlay+1, 16) are the
+// 16 bands' upward and downward fluxes and d(upward)/d(tsfc) (written when
+// idrv = 1), in W/m2, the per-band blocks the standalone RRTMG_LW prints.
+int orc_rrtmg_lw_bands(int ncol, int nlay, int idrv, const double* play, const double* plev, const double* tlay,
+                       const double* tlev, const double* tsfc, const double* h2ovmr, const double* o3vmr,
+                       const double* co2vmr, const double* ch4vmr, const double* n2ovmr, const double* o2vmr,
+                       const double* cfc11vmr, const double* cfc12vmr, const double* cfc22vmr,
+                       const double* ccl4vmr, const double* emis, double* bandu, double* bandd,
+                       double* dbandu_dt) {
+  if (!g_ready) return 2;
+  LwInput in{ncol, nlay, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr,
+             cfc11vmr, cfc12vmr, cfc22vmr, ccl4vmr, emis, nullptr};
+  const size_t nlev = (size_t)nlay + 1;
+  for (int iplon = 0; iplon < ncol; ++iplon) {
+    LwColumn c;
+    LwOut o;
+    o.want_bands = true;
+    o.bandu.assign(16 * nlev, 0.0);
+    o.bandd.assign(16 * nlev, 0.0);
+    o.dbandu_dt.assign(16 * nlev, 0.0);
+    lw_column(in, iplon, idrv, c, o);
+    for (size_t b = 0; b < 16; ++b)
+      for (size_t k = 0; k < nlev; ++k) {
+        size_t ix = (size_t)iplon + (size_t)ncol * (k + nlev * b);
+        bandu[ix] = o.bandu[b * nlev + k];
+        bandd[ix] = o.bandd[b * nlev + k];
+        if (idrv == 1 && dbandu_dt) dbandu_dt[ix] = o.dbandu_dt[b * nlev + k];
+      }
+  }
+  return 0;
+}
+
 // Gas optics only (stage parity): taug/fracs (ncol, nlay, 140), laytrop (ncol).
 int orc_lw_optics(int ncol, int nlay, const double* play, const double* plev, const double* tlay,
                   const double* tlev, const double* tsfc, const double* h2ovmr, const double* o3vmr,

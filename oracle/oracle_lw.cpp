@@ -1143,12 +1143,17 @@ void lw_rtrnmr(LwColumn& c, int idrv, LwOut& out) {
       drad[lev] = 0.0;
       totu[lev] = totu[lev] + uflux * T.delwave[iband];
       totd[lev] = totd[lev] + dflux * T.delwave[iband];
+      if (out.want_bands) {  // the band's own fluxes (W/m2), as the standalone RRTMG_LW prints them
+        out.bandu[(size_t)(iband - 1) * (nl + 1) + lev] = uflux * T.delwave[iband] * T.fluxfac;
+        out.bandd[(size_t)(iband - 1) * (nl + 1) + lev] = dflux * T.delwave[iband] * T.fluxfac;
+      }
     }
     if (idrv == 1) {
       for (int lev = nl; lev >= 0; --lev) {
         double duflux_dt = d_urad[lev] * wtdiff;
         d_urad[lev] = 0.0;
         dtotu_dt[lev] = dtotu_dt[lev] + duflux_dt * T.delwave[iband] * T.fluxfac;
+        if (out.want_bands) out.dbandu_dt[(size_t)(iband - 1) * (nl + 1) + lev] = duflux_dt * T.delwave[iband] * T.fluxfac;
       }
     }
   }

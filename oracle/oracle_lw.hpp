@@ -67,6 +67,10 @@ struct LwColumn {
 
 struct LwOut {
   std::vector<double> totu, totd, htr, dtotu_dt;  // levels 0..nlay (htr: layers 0..nlay-1, top 0)
+  // Per-band fluxes, filled only when want_bands is set (sized 16 * (nlay + 1)
+  // by the caller, band-major): upward, downward, d(upward)/d(tsfc) (idrv = 1).
+  bool want_bands = false;
+  std::vector<double> bandu, bandd, dbandu_dt;
 };
 
 void lw_init(const Blob& blob, double cpdair);

@@ -5,6 +5,9 @@ levels where the flux vanishes, e.g. LW downward flux at the top), heating
 rates within 1e-8 K/day absolute.  FP32-split path: heating rates within
 0.05 K/day, OLR and surface fluxes within 0.1 W/m2 of the FP64 oracle.
 """
+import json
+from pathlib import Path
+
 import numpy as np
 import pytest
 
@@ -61,6 +64,30 @@ def test_lw_idrv_surface_derivative(gpu, orc):
     atm = A.small_atmosphere(256, 40, seed=5)
     gpu.set_precision("fp64")
     check_lw(gpu.lw(atm, idrv=1), orc.rrtmg_lw(atm, idrv=1), idrv=1)
+
+
+def test_lw_surface_flux_known_answers(gpu):
+    """The surface upward LW flux of the reference's standalone RRTMG_LW runs
+    (tests/golden/rrtm_lw_std_atm_surface.json; emissivity 1, so only the
+    Planck tables, the band constants and, for the idrv = 1 run, the Planck
+    derivative enter), one column per run, through the FP64 and the split path:
+    within 1e-5 (FP64) and 5e-5 (split) of the printed values."""
+    runs = json.loads((Path(__file__).resolve().parent / "golden" / "rrtm_lw_std_atm_surface.json")
+                      .read_text())["runs"]
+    names = sorted(runs)
+    atm = A.small_atmosphere(len(names), 40, seed=3)
+    atm.tsfc = np.array([runs[n]["tbound"] for n in names])
+    atm.emis = np.ones_like(atm.emis)
+    dt = np.array([runs[n].get("dtbound", 0.0) for n in names])
+    ref = np.array([runs[n]["surface_up"][0][2] for n in names])
+    for prec, tol in (("fp64", 1e-5), ("split", 5e-5)):
+        gpu.set_precision(prec)
+        try:
+            out = gpu.lw(atm, idrv=1)
+        finally:
+            gpu.set_precision("fp64")
+        up = out["uflx"][0] + dt * out["duflx_dt"][0]
+        assert np.all(np.abs(up - ref) <= tol * ref), (prec, up - ref)
 
 
 def test_trace_gases_emissivity_and_aerosol(gpu, orc):

@@ -219,10 +219,11 @@ def run_reference(args):
         "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * float(np.median(times)),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded T85 atmospheres; synthetic LW k-distribution, AER SW tables)",
-        "config": {"workload": f"T85x40 LW+SW clear sky, {nsample}-column sample of {atm.ncol} per step"},
+        "data": "synthetic (seeded atmospheres of the configured grid; synthetic LW k-distribution, AER SW tables)",
+        "config": {"workload": workload_name(args.config, atm), "per_gpu_columns": atm.ncol,
+                   "sample": f"{nsample} of the {atm.ncol} columns per step"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{nsample} of {atm.ncol} T85 columns, LW+SW, FP64 lookup-table path"},
+                         "sample": f"{nsample} of {atm.ncol} columns, LW+SW, FP64 lookup-table path"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "reference Fortran not buildable here (no Fortran compiler); C++ FP64 restatement timed",
     }

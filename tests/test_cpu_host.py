@@ -125,3 +125,23 @@ def test_sharded_columns_gloo_world2():
     orc.load(tables.ensure_blob())
     full = orc.rrtmg_lw(A.small_atmosphere(64, 40, seed=12))["uflx"]
     assert np.array_equal(got, full)
+
+
+def test_bench_reference_arm_line():
+    """bench.py --impl reference (the CPU restatement, no GPU) prints one JSON
+    line with the contract's keys, on the same workload name as the GPU arm."""
+    import json
+    import subprocess
+    import sys
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "1", "--cpu-sample", "64", "--config", "0"],
+                       capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    import bench
+    assert d["impl"] == "reference" and d["metric"] == bench.METRIC and d["unit"] == bench.UNIT
+    assert d["value"] > 0 and d["e2e"]["value"] == d["value"] and d["cpu_baseline"]["kind"] == "port"
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+    assert d["config"]["workload"] == bench.workload_name(0, A.config_atmosphere(0))

@@ -280,3 +280,28 @@ def test_fp64_path_reproduces_golden_fixtures(gpu):
         for k in ("swuflx", "swdflx"):
             assert rel_err(sw[k], ref[f"{name}_{k}"], 1e-6) <= FLUX_TOL, (name, k)
         assert rel_err(sw["swhr"], ref[f"{name}_swhr"], 1e-3) <= HR_TOL, name
+
+
+@pytest.mark.parametrize("nlay", [100, 203])
+def test_deep_columns(gpu, orc, nlay):
+    """Columns deeper than 64 layers (the solvers' 208-level variants), up to
+    the reference's maximum of 203 layers (mxlay, parrrtm.f90 / parrrsw.f90):
+    the FP64 path against the oracle at the FP64 tolerances, with idrv = 1;
+    the split path within 0.1 W/m2 of the oracle at every level.  (The split
+    heating-rate bar is stated for 40 layers; at 203 layers to 0.01 hPa a layer
+    is down to 6e-4 hPa thick, and the same flux error is a larger rate.)"""
+    atm = A.small_atmosphere(96, nlay, seed=300 + nlay)
+    rlw, rsw = orc.rrtmg_lw(atm, idrv=1), orc.rrtmg_sw(atm)
+    gpu.set_precision("fp64")
+    check_lw(gpu.lw(atm, idrv=1), rlw, idrv=1)
+    check_sw(gpu.sw(atm), rsw)
+    gpu.set_precision("split")
+    try:
+        lw, sw = gpu.lw(atm, idrv=1), gpu.sw(atm)
+    finally:
+        gpu.set_precision("fp64")
+    for k in ("uflx", "dflx"):
+        assert np.abs(lw[k] - rlw[k]).max() <= 0.1, k
+    for k in ("swuflx", "swdflx"):
+        assert np.abs(sw[k] - rsw[k]).max() <= 0.1, k
+    assert np.isfinite(lw["hr"]).all() and np.isfinite(sw["swhr"]).all()

@@ -17,7 +17,11 @@ part of the MiMA distribution, so this module generates *synthetic* LW
 k-distributions: seeded, log-spread, increasing with g, with exactly the shapes
 the ``rrlw_kgNN`` modules declare, so they pass through the same 256 -> 140
 g-point reduction as real data would.  Every LW result built on them is a
-synthetic-k-distribution result.
+synthetic-k-distribution result.  Where a ``rrtmg_lw_k_g.f90`` is at hand (the
+AER RRTMG_LW distribution's data file), ``build_blob(..., lw_kg=path)`` (or
+``--lw-kg`` on the command line) parses the real LW k-distribution from it
+instead, with the parser of the SW data, and the kernels then compute the
+reference's physical LW fluxes.
 
 Nothing here is used at run time by the kernels: the output is one binary
 "table blob" (format below) that the C-ABI's ``rrtmg_gpu_init`` reads, reduces
@@ -229,11 +233,23 @@ def _data_from(path: Path, decls, routines=None, by_routine=False):
 
 def _sw_kg_data(path: Path, decls_by_band):
     """One pass over ``rrtmg_sw_k_g.f90``; routine ``sw_kgbNN`` fills band NN."""
+    return _kg_data(path, "sw_kgb", decls_by_band)
+
+
+def _kg_data(path: Path, prefix: str, decls_by_band):
+    """One pass over a k-distribution data file (``rrtmg_sw_k_g.f90``,
+    ``rrtmg_lw_k_g.f90``): the data assignments of routine ``<prefix>NN`` fill
+    band NN's arrays declared in ``decls_by_band[NN]``."""
     result = {b: {} for b in decls_by_band}
     for routine, st in _statements(path):
-        if not routine or not routine.startswith("sw_kgb"):
+        if not routine or not routine.startswith(prefix):
             continue
-        b = int(routine[6:])
+        try:
+            b = int(routine[len(prefix):])
+        except ValueError:
+            continue
+        if b not in decls_by_band:
+            continue
         m = re.match(r"^(\w+)\s*(\(([^=]*)\))?\s*=\s*(.+)$", st)
         if not m:
             continue
@@ -407,6 +423,27 @@ def synthetic_lw_tables(shapes: dict, seed: int = DEFAULT_LW_SEED) -> dict:
     return out
 
 
+def lw_kg_tables(path, shapes: dict) -> dict:
+    """The real LW k-distribution from a ``rrtmg_lw_k_g.f90`` (the reference's
+    data statements, routines ``lw_kgb01..16``; rrtmg_lw_init.f90 calls them
+    before the g-point reduction) for every 16-g table ``shapes`` declares
+    (the ``rrlw_kgNN`` modules): {blob_name: (array, lbounds)}, the form of
+    :func:`synthetic_lw_tables`.  A table that the file leaves unassigned or
+    only partly assigned is an error."""
+    per_band = _kg_data(Path(path), "lw_kgb", shapes)
+    out = {}
+    for b in range(1, 17):
+        for name, (lb, shape) in sorted(shapes[b].items()):
+            a = per_band[b].get(name)
+            if a is None:
+                raise ValueError(f"{path}: LW band {b} table {name} is not assigned")
+            a = np.asarray(a, dtype=np.float64)
+            if a.shape != tuple(shape) or np.isnan(a).any():
+                raise ValueError(f"{path}: LW band {b} table {name} incompletely assigned")
+            out[f"lw{b:02d}.{name}"] = (np.ascontiguousarray(a), lb)
+    return out
+
+
 def _log_table(rng, shape, lo, hi, tslope=0.0):
     """log10-spread table increasing along the trailing g axis.
 
@@ -504,11 +541,17 @@ def read_blob(path) -> dict:
     return out
 
 
-def build_blob(reference_root, out_path=DEFAULT_BLOB, lw_seed: int = DEFAULT_LW_SEED) -> Path:
-    """Parse the reference tables, add synthetic LW k-data, write the blob."""
+def build_blob(reference_root, out_path=DEFAULT_BLOB, lw_seed: int = DEFAULT_LW_SEED, lw_kg=None) -> Path:
+    """Parse the reference tables and write the blob.  The LW k-distribution
+    is the real one of ``lw_kg`` (a ``rrtmg_lw_k_g.f90``) when given, else
+    the seeded synthetic one (the MiMA tree does not ship the LW data)."""
     tables, shapes = reference_tables(reference_root)
-    tables.update(synthetic_lw_tables(shapes, lw_seed))
-    tables["meta.lw_synthetic_seed"] = (np.asarray([lw_seed], dtype=np.int32), (1,))
+    if lw_kg is not None:
+        tables.update(lw_kg_tables(lw_kg, shapes))
+        tables["meta.lw_real_kdist"] = (np.asarray([1], dtype=np.int32), (1,))
+    else:
+        tables.update(synthetic_lw_tables(shapes, lw_seed))
+        tables["meta.lw_synthetic_seed"] = (np.asarray([lw_seed], dtype=np.int32), (1,))
     write_blob(out_path, tables)
     return Path(out_path)
 
@@ -532,5 +575,7 @@ if __name__ == "__main__":
     ap.add_argument("mima_root")
     ap.add_argument("-o", "--out", default=str(DEFAULT_BLOB))
     ap.add_argument("--lw-seed", type=int, default=DEFAULT_LW_SEED)
+    ap.add_argument("--lw-kg", default=None,
+                    help="rrtmg_lw_k_g.f90 holding the real LW k-distribution (default: synthetic)")
     a = ap.parse_args()
-    print(build_blob(a.mima_root, a.out, a.lw_seed))
+    print(build_blob(a.mima_root, a.out, a.lw_seed, a.lw_kg))

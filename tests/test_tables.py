@@ -125,3 +125,84 @@ def test_kurucz_solar_source_totals(orc):
         assert np.allclose(sf.sum(axis=0), col, rtol=2e-3), b
         total += col * (50.15 / 48.37 if b == 27 else 1.0)
     assert abs(total - 1368.22) < 1.5, total
+
+
+# ---- real LW k-distribution ingestion (rrtmg_lw_k_g.f90) -------------------
+
+def _lw_band_tables(blob):
+    """The blob's 16-g LW tables {band: {name: (array, lbounds)}}."""
+    import re
+    out = {}
+    for k, v in tables.read_blob(blob).items():
+        m = re.match(r"^lw(\d\d)\.(\w+)$", k)
+        if m:
+            out.setdefault(int(m.group(1)), {})[m.group(2)] = v
+    return out
+
+
+def _write_lw_kg(path, bands, drop=None):
+    """A data file in the layout of the reference's k-distribution files
+    (routines lw_kgbNN; ``name(:, j, k) = (/ & ... /)`` column sections, five
+    values per continuation line, ``_rb`` kinds), full precision.  ``drop`` =
+    (band, name, section index) leaves one section out."""
+    lines = []
+    for b in sorted(bands):
+        lines += [f"      subroutine lw_kgb{b:02d}", f"      use rrlw_kg{b:02d}"]
+        for name in sorted(bands[b]):
+            a, lb = bands[b][name]
+            cols = [((), a)] if a.ndim == 1 else [(ix, a[(slice(None),) + ix]) for ix in np.ndindex(*a.shape[1:])]
+            for n, (ix, col) in enumerate(cols):
+                if drop == (b, name, n):
+                    continue
+                sec = ", ".join([":"] + [str(i + lo) for i, lo in zip(ix, lb[1:])])
+                lines.append(f"      {name}({sec}) = (/ &")
+                vals = [f"{v:.17e}_rb" for v in col]
+                for i in range(0, len(vals), 5):
+                    lines.append("        & " + ",".join(vals[i:i + 5]) + (" /)" if i + 5 >= len(vals) else ", &"))
+        lines.append(f"      end subroutine lw_kgb{b:02d}")
+    path.write_text("\n".join(lines) + "\n")
+
+
+def test_lw_kg_file_round_trip(blob, tmp_path):
+    bands = _lw_band_tables(blob)
+    assert sorted(bands) == list(range(1, 17))
+    shapes = {b: {n: (lb, a.shape) for n, (a, lb) in t.items()} for b, t in bands.items()}
+    p = tmp_path / "rrtmg_lw_k_g.f90"
+    _write_lw_kg(p, bands)
+    got = tables.lw_kg_tables(p, shapes)
+    assert len(got) == sum(len(t) for t in bands.values())
+    for b, t in bands.items():
+        for n, (a, lb) in t.items():
+            g, glb = got[f"lw{b:02d}.{n}"]
+            assert glb == lb and np.array_equal(g, a), (b, n)
+
+
+def test_lw_kg_file_incomplete_is_an_error(blob, tmp_path):
+    bands = _lw_band_tables(blob)
+    shapes = {b: {n: (lb, a.shape) for n, (a, lb) in t.items()} for b, t in bands.items()}
+    p = tmp_path / "partial.f90"
+    _write_lw_kg(p, bands, drop=(5, "kao", 7))
+    with pytest.raises(ValueError, match="band 5 table kao incompletely assigned"):
+        tables.lw_kg_tables(p, shapes)
+    missing = {b: dict(t) for b, t in bands.items()}
+    del missing[9]["selfrefo"]
+    _write_lw_kg(p, missing)
+    with pytest.raises(ValueError, match="band 9 table selfrefo is not assigned"):
+        tables.lw_kg_tables(p, shapes)
+
+
+def test_blob_from_lw_kg_file(blob, tmp_path):
+    """build_blob(lw_kg=...) puts the file's LW tables in the blob in place of
+    the synthetic ones; everything else is unchanged."""
+    import __graft_entry__ as ge
+    root = ge._reference_root()
+    if root is None:
+        pytest.skip("no MiMA source tree")
+    p = tmp_path / "rrtmg_lw_k_g.f90"
+    _write_lw_kg(p, _lw_band_tables(blob))
+    out = tables.build_blob(root, tmp_path / "real.bin", lw_kg=p)
+    a, b = tables.read_blob(blob), tables.read_blob(out)
+    assert "meta.lw_real_kdist" in b and "meta.lw_synthetic_seed" not in b
+    assert set(a) - {"meta.lw_synthetic_seed"} == set(b) - {"meta.lw_real_kdist"}
+    for k in set(a) & set(b):
+        assert np.array_equal(a[k][0], b[k][0]) and a[k][1] == b[k][1], k

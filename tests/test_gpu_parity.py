@@ -68,11 +68,11 @@ def test_lw_idrv_surface_derivative(gpu, orc):
 
 def test_lw_surface_flux_known_answers(gpu):
     """The surface upward LW flux of the reference's standalone RRTMG_LW runs
-    (tests/golden/rrtm_lw_std_atm_surface.json; emissivity 1, so only the
+    (tests/golden/rrtm_lw_std_atm.json; emissivity 1, so only the
     Planck tables, the band constants and, for the idrv = 1 run, the Planck
     derivative enter), one column per run, through the FP64 and the split path:
     within 1e-5 (FP64) and 5e-5 (split) of the printed values."""
-    runs = json.loads((Path(__file__).resolve().parent / "golden" / "rrtm_lw_std_atm_surface.json")
+    runs = json.loads((Path(__file__).resolve().parent / "golden" / "rrtm_lw_std_atm.json")
                       .read_text())["runs"]
     names = sorted(runs)
     atm = A.small_atmosphere(len(names), 40, seed=3)

@@ -90,6 +90,33 @@ def test_lw_surface_flux_known_answers(gpu):
         assert np.all(np.abs(up - ref) <= tol * ref), (prec, up - ref)
 
 
+def test_standard_atmospheres(gpu, orc):
+    """The reference's clear-sky standard atmospheres (the TAPE5 profiles of
+    doc_rrtm/runs_std_atm: midlatitude summer and winter, subarctic winter,
+    tropical; 51-60 layers to 0.07 hPa) as columns: the FP64 path against the
+    oracle at the FP64 tolerances, with idrv = 1; the split path within the
+    split bars (0.05 K/day heating, 0.1 W/m2 OLR and surface fluxes)."""
+    from test_oracle_std_atm import PROFILES, RUNS, std_atm_column
+    for name in PROFILES:
+        atm = std_atm_column(RUNS[name])
+        rlw, rsw = orc.rrtmg_lw(atm, idrv=1), orc.rrtmg_sw(atm)
+        gpu.set_precision("fp64")
+        check_lw(gpu.lw(atm, idrv=1), rlw, idrv=1)
+        check_sw(gpu.sw(atm), rsw)
+        gpu.set_precision("split")
+        try:
+            lw, sw = gpu.lw(atm), gpu.sw(atm)
+        finally:
+            gpu.set_precision("fp64")
+        assert np.abs(lw["hr"] - rlw["hr"]).max() <= 0.05, name
+        assert np.abs(sw["swhr"] - rsw["swhr"]).max() <= 0.05, name
+        assert abs(lw["uflx"][-1, 0] - rlw["uflx"][-1, 0]) <= 0.1, name
+        for k in ("uflx", "dflx"):
+            assert abs(lw[k][0, 0] - rlw[k][0, 0]) <= 0.1, (name, k)
+        for k in ("swuflx", "swdflx"):
+            assert abs(sw[k][0, 0] - rsw[k][0, 0]) <= 0.1, (name, k)
+
+
 def test_trace_gases_emissivity_and_aerosol(gpu, orc):
     """All optional gases non-zero, spectral emissivity < 1, LW and SW aerosols."""
     rng = np.random.default_rng(9)

@@ -88,9 +88,10 @@ int rrtmg_run_params_default(rrtmg_run_params* p);
  *     both or neither.
  *   optional outputs (NULL = not wanted): t_half (si,sj,sk+1), tdt_rad,
  *     tdt_sw, tdt_lw (si,sj,sk) K/s, olr, isr (si,sj) W/m2.
- * The call allocates only on the first use of a slab size (or after
- * rrtmg_gpu_reserve for ncol = si/lonstep*sj, nlay = sk); input validation
- * is reported by rrtmg_gpu_sync_status. */
+ * The call allocates device workspace on the first use of a slab size only
+ * (rrtmg_gpu_reserve does not cover it): make one call of that size before
+ * capturing the call in a CUDA graph.  Input validation is reported by
+ * rrtmg_gpu_sync_status. */
 int rrtmg_run_dev(rrtmg_gpu_handle h, void* stream, const rrtmg_run_params* prm, int si, int sj, int sk,
                   int seconds, int days, int days_per_year, const double* lat, const double* lon,
                   const double* p_full, const double* p_half, const double* z_full, const double* z_half,

@@ -96,7 +96,9 @@ int ensure(rrtmg_gpu_state* h, DevBuf& b, size_t need, cudaStream_t s) {
   if (b.bytes >= need) return RRTMG_OK;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   if (s != nullptr && cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone)
-    return fail(h, RRTMG_ERR_NOMEM, "workspace too small during stream capture; call rrtmg_gpu_reserve first");
+    return fail(h, RRTMG_ERR_NOMEM,
+                "workspace too small during stream capture: make one call of this size before capturing "
+                "(rrtmg_gpu_reserve covers the LW and SW calls)");
   if (b.p) cudaFree(b.p);
   b.p = nullptr;
   b.bytes = 0;
@@ -333,6 +335,8 @@ struct HostOut {
 // LW + SW host calls at 32768 columns (page-locked arrays) took 9.43 ms in one
 // chunk, 8.78 in 2 or 3, 9.17 in 4, 9.89 in 8.
 constexpr int kChunkMin = RRTMG_HOST_CHUNK, kMaxChunks = 16;
+// Most input and output arrays of one host-array call (rrtmg_sw_c: 19 / 6).
+constexpr int kMaxHostIn = 24, kMaxHostOut = 12;
 
 int read_flags(rrtmg_gpu_state* h, cudaStream_t s);
 
@@ -350,6 +354,13 @@ bool pinned(const void* p) {
 template <class Need, class Enqueue>
 int host_call(rrtmg_gpu_state* h, int ncol, const HostIn* in, int nin, const HostOut* out, int nout, Need&& ws_need,
               Enqueue&& enqueue, const char* what) {
+  if (nin > kMaxHostIn || nout > kMaxHostOut) return fail(h, RRTMG_ERR_ARG, "too many arrays for one host call");
+  // On a failure after copies were enqueued, wait for them: they read and
+  // write the caller's arrays, which the caller may free once the call returns.
+  auto drain = [h]() {
+    cudaStreamSynchronize(h->stream);
+    cudaStreamSynchronize(h->stream2);
+  };
   // Chunks only for page-locked arrays: pitched copies of pageable memory are
   // staged by the driver row by row; pageable arrays move in one piece.
   bool all_pinned = true;
@@ -372,8 +383,8 @@ int host_call(rrtmg_gpu_state* h, int ncol, const HostIn* in, int nin, const Hos
   }
   const size_t pitch = (size_t)ncol * sizeof(double);
   cudaError_t e = cudaSuccess;
-  const double* din[24];
-  double* dout[12];
+  const double* din[kMaxHostIn];
+  double* dout[kMaxHostOut];
   for (int c = 0; c < nchunk && e == cudaSuccess; ++c) {
     const int c0 = c * csize;
     const int nc = std::min(csize, ncol - c0);
@@ -393,13 +404,19 @@ int host_call(rrtmg_gpu_state* h, int ncol, const HostIn* in, int nin, const Hos
     for (int k = 0; k < nout; ++k) dout[k] = out[k].p ? cv.take<double>((size_t)nc * out[k].rows) : nullptr;
     if (e != cudaSuccess) break;
     int rc = enqueue(s, h->hws[c % 2].p, nc, din, dout);
-    if (rc) return rc;
+    if (rc) {
+      drain();
+      return rc;
+    }
     for (int k = 0; k < nout && e == cudaSuccess; ++k)
       if (out[k].p)
         e = nchunk == 1 ? cudaMemcpyAsync(out[k].p, dout[k], w * out[k].rows, cudaMemcpyDeviceToHost, s)
                         : cudaMemcpy2DAsync(out[k].p + c0, pitch, dout[k], w, w, out[k].rows, cudaMemcpyDeviceToHost, s);
   }
-  if (e != cudaSuccess) return cuda_fail(h, e, what);
+  if (e != cudaSuccess) {
+    drain();
+    return cuda_fail(h, e, what);
+  }
   e = cudaStreamSynchronize(h->stream2);
   if (e != cudaSuccess) return cuda_fail(h, e, "synchronise");
   return read_flags(h, h->stream);

@@ -1249,12 +1249,24 @@ int rrtmg_run_c(rrtmg_gpu_handle h, const rrtmg_run_params* prm, int si, int sj,
     if (k == 0) e = cudaMemcpyAsync(d, tdt, out_n[0] * sizeof(double), cudaMemcpyHostToDevice, st);
     *outs[k] = d;
   }
-  if (e != cudaSuccess) return cuda_fail(h, e, "run_rrtmg: copy inputs");
+  // On a failure after copies were enqueued, wait for them before returning:
+  // they read and write the caller's arrays.  The SW work of run_enqueue is
+  // joined back into st, so st covers it.
+  if (e != cudaSuccess) {
+    cudaStreamSynchronize(st);
+    return cuda_fail(h, e, "run_rrtmg: copy inputs");
+  }
   rc = run_enqueue(h, st, *prm, a);
-  if (rc) return rc;
+  if (rc) {
+    cudaStreamSynchronize(st);
+    return rc;
+  }
   for (int k = 0; k < 10 && e == cudaSuccess; ++k)
     if (host_out[k]) e = cudaMemcpyAsync(host_out[k], *outs[k], out_n[k] * sizeof(double), cudaMemcpyDeviceToHost, st);
-  if (e != cudaSuccess) return cuda_fail(h, e, "run_rrtmg: copy outputs");
+  if (e != cudaSuccess) {
+    cudaStreamSynchronize(st);
+    return cuda_fail(h, e, "run_rrtmg: copy outputs");
+  }
   return read_flags(h, st);
 }
 

@@ -74,7 +74,18 @@ std::string read_blob(const char* path, ArrMap& out) {
     std::memcpy(dims, r + 72, 16);
     std::memcpy(&off, r + 88, 8);
     std::memcpy(&nb, r + 96, 8);
-    if (off + nb > buf.size() || ndim > 4) return std::string("table blob entry out of range: ") + name;
+    // every entry: a known type, at most 4 dimensions, its bytes inside the
+    // file, a whole number of elements, and as many elements as its dimensions
+    const uint64_t esz = dtype == 1 ? 4 : 8;
+    if ((dtype != 0 && dtype != 1) || ndim > 4 || off > buf.size() || nb > buf.size() - off || nb % esz != 0)
+      return std::string("table blob entry out of range: ") + name;
+    uint64_t n = 1;
+    bool fits = true;
+    for (uint32_t k = 0; k < ndim && fits; ++k) {
+      fits = dims[k] <= 0x7fffffffu && (dims[k] == 0 || n <= (nb / esz) / dims[k]);
+      n *= dims[k];
+    }
+    if (!fits || n != nb / esz) return std::string("table blob entry size does not match its dimensions: ") + name;
     Arr a;
     for (uint32_t k = 0; k < ndim; ++k) a.dims.push_back((int)dims[k]);
     if (dtype == 1) {

@@ -145,3 +145,36 @@ def test_bench_reference_arm_line():
     assert d["value"] > 0 and d["e2e"]["value"] == d["value"] and d["cpu_baseline"]["kind"] == "port"
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
     assert d["config"]["workload"] == bench.workload_name(0, A.config_atmosphere(0))
+
+
+def test_blob_reader_rejects_inconsistent_entries(tmp_path, blob):
+    """rrtmg_gpu_init refuses (RRTMG_ERR_TABLES, before any CUDA call) a blob
+    whose checksum is right but one of whose entries is inconsistent: bytes
+    outside the file (including an offset that wraps around), a byte count that
+    is not a whole number of elements, dimensions that do not match the byte
+    count, an unknown type, more than 4 dimensions."""
+    import struct
+    from mima_gb300 import tables
+    body = Path(blob).read_bytes()[:-8]
+    name, dtype, ndim = struct.unpack_from("<48sII", body, 16)
+    dims = struct.unpack_from("<4I", body, 16 + 72)
+    off, nb = struct.unpack_from("<QQ", body, 16 + 88)
+    esz = 4 if dtype == 1 else 8
+    assert ndim >= 1 and nb == esz * int(np.prod(dims[:ndim]))
+    cases = {"off": ("<Q", 88, 2**64 - 8), "nb": ("<Q", 96, nb - 1), "dims": ("<I", 72, dims[0] + 1),
+             "dtype": ("<I", 48, 7), "ndim": ("<I", 52, 5), "nb_past_end": ("<Q", 96, len(body) + 64)}
+    lib = R.load_library()
+    for case, (fmt, at, value) in cases.items():
+        raw = bytearray(body)
+        struct.pack_into(fmt, raw, 16 + at, value)
+        p = tmp_path / f"{case}.bin"
+        p.write_bytes(bytes(raw) + struct.pack("<Q", tables.blob_checksum(bytes(raw))))
+        h = C.c_void_p()
+        assert lib.rrtmg_gpu_init(C.c_double(1004.64), str(p).encode(), 0, C.byref(h)) == R.RRTMG_ERR_TABLES, case
+        assert not h.value
+    # the unpatched blob passes the reader (then needs a GPU: RRTMG_ERR_CUDA without one)
+    h = C.c_void_p()
+    rc = lib.rrtmg_gpu_init(C.c_double(1004.64), str(blob).encode(), 0, C.byref(h))
+    assert rc != R.RRTMG_ERR_TABLES
+    if h.value:
+        lib.rrtmg_gpu_finalize(h)

@@ -124,10 +124,51 @@ def _hp(a):
     return None if a is None else a.ctypes.data_as(_dp)
 
 
-def _dptr(t):
+def _dptr(t, n=None, name="array", device=None):
+    """Device pointer of a CUDA float64 tensor, checked first: a tensor of
+    another type, layout, device or a smaller size would make the kernels read
+    or write outside it.  ``n``: elements the call reads or writes."""
     if t is None:
         return None
+    if not (getattr(t, "is_cuda", False) and str(t.dtype) == "torch.float64" and t.is_contiguous()):
+        raise ValueError(f"{name} must be a contiguous float64 CUDA tensor")
+    if device is not None and t.device.index is not None and t.device.index != device:
+        raise ValueError(f"{name} is on cuda:{t.device.index}, the handle on cuda:{device}")
+    if n is not None and t.numel() < n:
+        raise ValueError(f"{name} has {t.numel()} elements; the call needs {n}")
     return C.cast(C.c_void_p(int(t.data_ptr())), _dp)
+
+
+_LOOKUP = object()  # the argument's tensor is looked up by name
+
+_PER_LAYER = ("play", "tlay", "h2ovmr", "o3vmr", "co2vmr", "ch4vmr", "n2ovmr", "o2vmr", "cfc11vmr", "cfc12vmr",
+              "cfc22vmr", "ccl4vmr", "hr", "hrc", "swhr", "swhrc")
+_PER_LEVEL = ("plev", "tlev", "uflx", "dflx", "uflxc", "dflxc", "duflx_dt", "duflxc_dt", "swuflx", "swdflx",
+              "swuflxc", "swdflxc")
+_PER_COLUMN = ("tsfc", "asdir", "asdif", "aldir", "aldif", "coszen")
+
+
+def array_sizes(ncol, nlay):
+    """Elements of every rrtmg_lw / rrtmg_sw array by argument name, (rows,
+    ncol) column-fastest; ``tauaer`` is the SW one (14 bands), ``tauaer_lw``
+    the LW one (16 bands)."""
+    n = {k: nlay * ncol for k in _PER_LAYER}
+    n.update({k: (nlay + 1) * ncol for k in _PER_LEVEL})
+    n.update({k: ncol for k in _PER_COLUMN})
+    n.update(emis=16 * ncol, tauaer_lw=16 * nlay * ncol, tauaer=14 * nlay * ncol, ssaaer=14 * nlay * ncol,
+             asmaer=14 * nlay * ncol)
+    return n
+
+
+def run_array_sizes(si, sj, sk):
+    """Elements of every run_rrtmg array by name (the GCM slab's shapes)."""
+    P = si * sj
+    full, half = P * sk, P * (sk + 1)
+    n = dict(lat=P, lon=P, p_full=full, p_half=half, z_full=full, z_half=half, t=full, q=full, o3=full,
+             t_surf_rad=P, albedo=P, rrtm_precip=P)
+    n.update(tdt=full, coszen=P, flux_sw=P, flux_lw=P, t_half=half, tdt_rad=full, tdt_sw=full, tdt_lw=full,
+             olr=P, isr=P)
+    return n
 
 
 def _outputs(given, shapes, ncol):
@@ -245,16 +286,29 @@ class RRTMG:
                              tauaer, ssaaer, asmaer, check=check)
 
     # ---------------- device-array entry points ----------------
+    def _ptrs(self, ncol, nlay, *dicts):
+        """Checked device pointers: ``p(name)`` of the array of that name in
+        ``dicts`` (the first that has it), ``p(name, tensor)`` of a tensor
+        passed as its own argument (None stays NULL)."""
+        n = array_sizes(ncol, nlay)
+
+        def p(k, t=_LOOKUP):
+            if t is _LOOKUP:
+                t = next((dct[k] for dct in dicts if dct is not None and dct.get(k) is not None), None)
+            return _dptr(t, n[k], k, self.device)
+        return p
+
     def rrtmg_lw_dev(self, stream, ncol, nlay, icld, idrv, d, out, tauaer=None):
         """``d``/``out``: dicts of CUDA tensors with the argument names of rrtmg_lw."""
-        g = lambda k: _dptr(d.get(k))
-        o = lambda k: _dptr(out.get(k))
+        g = self._ptrs(ncol, nlay, d)
+        o = self._ptrs(ncol, nlay, out)
         rc = self.lib.rrtmg_lw_dev(
             self._h, C.c_void_p(stream or 0), C.c_int(ncol), C.c_int(nlay), C.c_int(icld), C.c_int(idrv),
             g("play"), g("plev"), g("tlay"), g("tlev"), g("tsfc"), g("h2ovmr"), g("o3vmr"), g("co2vmr"),
             g("ch4vmr"), g("n2ovmr"), g("o2vmr"), g("cfc11vmr"), g("cfc12vmr"), g("cfc22vmr"), g("ccl4vmr"),
-            g("emis"), C.c_int(0), C.c_int(0), C.c_int(0), None, None, None, None, None, None, _dptr(tauaer),
-            o("uflx"), o("dflx"), o("hr"), o("uflxc"), o("dflxc"), o("hrc"), o("duflx_dt"), o("duflxc_dt"))
+            g("emis"), C.c_int(0), C.c_int(0), C.c_int(0), None, None, None, None, None, None,
+            g("tauaer_lw", tauaer), o("uflx"), o("dflx"), o("hr"), o("uflxc"), o("dflxc"), o("hrc"), o("duflx_dt"),
+            o("duflxc_dt"))
         self._check(rc)
 
     def set_profiling(self, on: bool):
@@ -272,13 +326,18 @@ class RRTMG:
 
     def _adjoint(self, fn, stream, ncol, nlay, d, extra, adjes, dyofyr, scon, iaer=0, tauaer_lw=None,
                  tauaer_sw=None, ssaaer=None, asmaer=None):
-        g = lambda k: _dptr(d.get(k))
+        g = self._ptrs(ncol, nlay, d)
+        nx, ny = adjoint_shape(nlay)
+        # extra: (jac,) of nx * ny * ncol, or (cot, grad) of ny * ncol and nx * ncol
+        sizes = [nx * ny * ncol] if len(extra) == 1 else [ny * ncol, nx * ncol]
+        names = ["jac"] if len(extra) == 1 else ["cot", "grad"]
         rc = fn(self._h, C.c_void_p(stream or 0), C.c_int(ncol), C.c_int(nlay),
                 g("play"), g("plev"), g("tlay"), g("tlev"), g("tsfc"), g("h2ovmr"), g("o3vmr"), g("co2vmr"),
                 g("ch4vmr"), g("n2ovmr"), g("o2vmr"), g("cfc11vmr"), g("cfc12vmr"), g("cfc22vmr"), g("ccl4vmr"),
-                g("emis"), _dptr(tauaer_lw), g("asdir"), g("asdif"), g("aldir"), g("aldif"), g("coszen"),
-                C.c_double(adjes), C.c_int(dyofyr), C.c_double(scon), C.c_int(iaer), _dptr(tauaer_sw),
-                _dptr(ssaaer), _dptr(asmaer), *[_dptr(t) for t in extra])
+                g("emis"), g("tauaer_lw", tauaer_lw), g("asdir"), g("asdif"), g("aldir"), g("aldif"), g("coszen"),
+                C.c_double(adjes), C.c_int(dyofyr), C.c_double(scon), C.c_int(iaer), g("tauaer", tauaer_sw),
+                g("ssaaer", ssaaer), g("asmaer", asmaer),
+                *[_dptr(t, n, k, self.device) for t, n, k in zip(extra, sizes, names)])
         self._check(rc)
 
     def jacobian(self, atm):
@@ -316,19 +375,20 @@ class RRTMG:
     def rrtmg_lw_dev_static(self, stream, ncol, nlay, icld, idrv, d, out, tauaer=None):
         """As :meth:`rrtmg_lw_dev`, through the allocation-free entry point
         (scratch in the library's static device array)."""
-        g = lambda k: _dptr(d.get(k))
-        o = lambda k: _dptr(out.get(k))
+        g = self._ptrs(ncol, nlay, d)
+        o = self._ptrs(ncol, nlay, out)
         rc = self.lib.rrtmg_lw_dev_static(
             self._h, C.c_void_p(stream or 0), C.c_int(ncol), C.c_int(nlay), C.c_int(icld), C.c_int(idrv),
             g("play"), g("plev"), g("tlay"), g("tlev"), g("tsfc"), g("h2ovmr"), g("o3vmr"), g("co2vmr"),
             g("ch4vmr"), g("n2ovmr"), g("o2vmr"), g("cfc11vmr"), g("cfc12vmr"), g("cfc22vmr"), g("ccl4vmr"),
-            g("emis"), C.c_int(0), C.c_int(0), C.c_int(0), None, None, None, None, None, None, _dptr(tauaer),
-            o("uflx"), o("dflx"), o("hr"), o("uflxc"), o("dflxc"), o("hrc"), o("duflx_dt"), o("duflxc_dt"))
+            g("emis"), C.c_int(0), C.c_int(0), C.c_int(0), None, None, None, None, None, None,
+            g("tauaer_lw", tauaer), o("uflx"), o("dflx"), o("hr"), o("uflxc"), o("dflxc"), o("hrc"), o("duflx_dt"),
+            o("duflxc_dt"))
         self._check(rc)
 
     def rrtmg_sw_dev(self, stream, ncol, nlay, icld, iaer, d, out, adjes, dyofyr, scon):
-        g = lambda k: _dptr(d.get(k))
-        o = lambda k: _dptr(out.get(k))
+        g = self._ptrs(ncol, nlay, d)
+        o = self._ptrs(ncol, nlay, out)
         rc = self.lib.rrtmg_sw_dev(
             self._h, C.c_void_p(stream or 0), C.c_int(ncol), C.c_int(nlay), C.c_int(icld), C.c_int(iaer),
             g("play"), g("plev"), g("tlay"), g("tlev"), g("tsfc"), g("h2ovmr"), g("o3vmr"), g("co2vmr"),
@@ -343,14 +403,14 @@ class RRTMG:
         """Fused LW + SW step on device arrays (rrtmg_step_dev): ``d`` holds
         the inputs by rrtmg_lw / rrtmg_sw argument name (plus ``tauaer``,
         ``ssaaer``, ``asmaer`` for iaer = 10), ``olw`` / ``osw`` the outputs."""
-        g = lambda k: _dptr(d.get(k))
-        o = lambda k: _dptr(olw.get(k))
-        q = lambda k: _dptr(osw.get(k))
+        g = self._ptrs(ncol, nlay, d)
+        o = self._ptrs(ncol, nlay, olw)
+        q = self._ptrs(ncol, nlay, osw)
         rc = self.lib.rrtmg_step_dev(
             self._h, C.c_void_p(stream or 0), C.c_int(ncol), C.c_int(nlay), C.c_int(idrv), C.c_int(iaer),
             g("play"), g("plev"), g("tlay"), g("tlev"), g("tsfc"), g("h2ovmr"), g("o3vmr"), g("co2vmr"),
             g("ch4vmr"), g("n2ovmr"), g("o2vmr"), g("cfc11vmr"), g("cfc12vmr"), g("cfc22vmr"), g("ccl4vmr"),
-            g("emis"), _dptr(tauaer_lw), g("asdir"), g("asdif"), g("aldir"), g("aldif"), g("coszen"),
+            g("emis"), g("tauaer_lw", tauaer_lw), g("asdir"), g("asdif"), g("aldir"), g("aldif"), g("coszen"),
             C.c_double(adjes), C.c_int(dyofyr), C.c_double(scon), g("tauaer"), g("ssaaer"), g("asmaer"),
             o("uflx"), o("dflx"), o("hr"), o("uflxc"), o("dflxc"), o("hrc"), o("duflx_dt"), o("duflxc_dt"),
             q("swuflx"), q("swdflx"), q("swhr"), q("swuflxc"), q("swdflxc"), q("swhrc"))
@@ -379,9 +439,11 @@ class RRTMG:
         """run_rrtmg on device arrays (rrtmg_run_dev): ``d`` maps the names
         of :data:`RUN_IN`, ``out`` those of :data:`RUN_OUT` to CUDA tensors
         (missing optional ones are NULL)."""
+        n = run_array_sizes(si, sj, sk)
         rc = self.lib.rrtmg_run_dev(self._h, C.c_void_p(stream or 0), C.byref(prm), C.c_int(si), C.c_int(sj),
                                     C.c_int(sk), C.c_int(seconds), C.c_int(days), C.c_int(days_per_year),
-                                    *[_dptr(d.get(k)) for k in RUN_IN], *[_dptr(out.get(k)) for k in RUN_OUT])
+                                    *[_dptr(d.get(k), n[k], k, self.device) for k in RUN_IN],
+                                    *[_dptr(out.get(k), n[k], k, self.device) for k in RUN_OUT])
         self._check(rc)
 
 

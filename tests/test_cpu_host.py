@@ -178,3 +178,129 @@ def test_blob_reader_rejects_inconsistent_entries(tmp_path, blob):
     assert rc != R.RRTMG_ERR_TABLES
     if h.value:
         lib.rrtmg_gpu_finalize(h)
+
+
+# ---- the Python mirror's device-array wrappers against the C header ---------
+
+class _FakeTensor:
+    """Stands in for a CUDA float64 tensor: the attributes the wrappers read."""
+
+    def __init__(self, numel, ptr, dtype="torch.float64", cuda=True, contiguous=True, index=0):
+        import types
+        self._n, self._p, self._c = numel, ptr, contiguous
+        self.dtype, self.is_cuda, self.device = dtype, cuda, types.SimpleNamespace(index=index)
+
+    def numel(self):
+        return self._n
+
+    def data_ptr(self):
+        return self._p
+
+    def is_contiguous(self):
+        return self._c
+
+
+class _RecordingLib:
+    def __init__(self):
+        self.calls = {}
+
+    def __getattr__(self, name):
+        def fn(*args):
+            self.calls[name] = args
+            return 0
+        return fn
+
+
+def _header_params(fn):
+    text = "".join(p.read_text() for p in sorted((ROOT / "include").glob("*.h")))
+    m = re.search(r"^int\s+" + fn + r"\((.*?)\);", text, re.S | re.M)
+    return [re.findall(r"(\w+)\s*$", a.strip())[0] for a in m.group(1).split(",")]
+
+
+def _mirror():
+    r = object.__new__(R.RRTMG)
+    r._h, r.device, r.lib = C.c_void_p(1), 0, _RecordingLib()
+    r._check = lambda rc: None
+    return r
+
+
+def _ptr(a):
+    return None if a is None else C.cast(a, C.c_void_p).value
+
+
+def _check_positions(call, params, expect):
+    """Every pointer parameter carries the fake tensor of its name, or NULL."""
+    assert len(call) == len(params)
+    for name, arg in zip(params, call):
+        if name in expect:
+            assert _ptr(arg) == expect[name], name
+
+
+def test_device_wrappers_follow_the_header():
+    ncol, nlay = 5, 7
+    sizes = R.array_sizes(ncol, nlay)
+    fake = {k: _FakeTensor(n, 0x10000 * (i + 1)) for i, (k, n) in enumerate(sorted(sizes.items()))}
+    ptr = {k: t.data_ptr() for k, t in fake.items()}
+    cloud_lw = ["cldfr", "taucld", "cicewp", "cliqwp", "reice", "reliq"]
+    r = _mirror()
+    # rrtmg_lw_dev: the LW aerosol argument is the tauaer keyword
+    r.rrtmg_lw_dev(0, ncol, nlay, 0, 1, fake, fake, tauaer=fake["tauaer_lw"])
+    exp = {k: ptr[k] for k in _header_params("rrtmg_lw_dev") if k in ptr and k != "tauaer"}
+    exp.update({"tauaer": ptr["tauaer_lw"], **{k: None for k in cloud_lw}})
+    _check_positions(r.lib.calls["rrtmg_lw_dev"], _header_params("rrtmg_lw_dev"), exp)
+    r.rrtmg_lw_dev_static(0, ncol, nlay, 0, 1, fake, fake, tauaer=None)
+    exp["tauaer"] = None
+    _check_positions(r.lib.calls["rrtmg_lw_dev_static"], _header_params("rrtmg_lw_dev_static"), exp)
+    # rrtmg_sw_dev: tauaer/ssaaer/asmaer are the SW arrays of the input dict
+    r.rrtmg_sw_dev(0, ncol, nlay, 0, 10, fake, fake, 1.0, 0, 1360.0)
+    p = _header_params("rrtmg_sw_dev")
+    exp = {k: ptr[k] for k in p if k in ptr}
+    exp.update({k: None for k in cloud_lw + ["ssacld", "asmcld", "fsfcld", "ecaer"]})
+    _check_positions(r.lib.calls["rrtmg_sw_dev"], p, exp)
+    # rrtmg_step_dev
+    r.rrtmg_step_dev(0, ncol, nlay, fake, fake, fake, 1.0, 0, 1360.0, idrv=1, iaer=10,
+                     tauaer_lw=fake["tauaer_lw"])
+    p = _header_params("rrtmg_step_dev")
+    exp = {k: ptr[k] for k in p if k in ptr}
+    exp.update(tauaer_lw=ptr["tauaer_lw"], tauaer_sw=ptr["tauaer"])
+    _check_positions(r.lib.calls["rrtmg_step_dev"], p, exp)
+    # adjoint: aerosols only as keywords; an input dict's SW aerosols are not picked up
+    nx, ny = R.adjoint_shape(nlay)
+    jac, cot, grad = _FakeTensor(nx * ny * ncol, 0xA0000), _FakeTensor(ny * ncol, 0xB0000), _FakeTensor(nx * ncol, 0xC0000)
+    r.jacobian_dev(0, ncol, nlay, fake, jac, 1.0, 0, 1360.0)
+    p = _header_params("rrtmg_jacobian_dev")
+    exp = {k: ptr[k] for k in p if k in ptr and k not in ("tauaer_lw", "tauaer_sw", "ssaaer", "asmaer")}
+    exp.update(tauaer_lw=None, tauaer_sw=None, ssaaer=None, asmaer=None, jac=0xA0000)
+    _check_positions(r.lib.calls["rrtmg_jacobian_dev"], p, exp)
+    r.vjp_dev(0, ncol, nlay, fake, cot, grad, 1.0, 0, 1360.0, iaer=10, tauaer_sw=fake["tauaer"],
+              ssaaer=fake["ssaaer"], asmaer=fake["asmaer"])
+    p = _header_params("rrtmg_vjp_dev")
+    exp.pop("jac")
+    exp.update(tauaer_sw=ptr["tauaer"], ssaaer=ptr["ssaaer"], asmaer=ptr["asmaer"], cot=0xB0000, grad=0xC0000)
+    _check_positions(r.lib.calls["rrtmg_vjp_dev"], p, exp)
+    # run_rrtmg_dev
+    si, sj, sk = 8, 3, nlay
+    rs = R.run_array_sizes(si, sj, sk)
+    rfake = {k: _FakeTensor(n, 0x100000 * (i + 1)) for i, (k, n) in enumerate(sorted(rs.items()))}
+    r.run_rrtmg_dev(0, R.run_params(), si, sj, sk, 0, 0, 365, rfake, rfake)
+    p = _header_params("rrtmg_run_dev")
+    _check_positions(r.lib.calls["rrtmg_run_dev"], p, {k: t.data_ptr() for k, t in rfake.items()})
+
+
+def test_device_wrappers_refuse_wrong_tensors():
+    ncol, nlay = 5, 7
+    sizes = R.array_sizes(ncol, nlay)
+    good = {k: _FakeTensor(n, 0x10000 * (i + 1)) for i, (k, n) in enumerate(sorted(sizes.items()))}
+    r = _mirror()
+    bad = {"short": _FakeTensor(sizes["play"] - 1, 0x1), "float32": _FakeTensor(sizes["play"], 0x1, dtype="torch.float32"),
+           "host": _FakeTensor(sizes["play"], 0x1, cuda=False), "strided": _FakeTensor(sizes["play"], 0x1, contiguous=False),
+           "other_gpu": _FakeTensor(sizes["play"], 0x1, index=1)}
+    for case, t in bad.items():
+        with pytest.raises(ValueError):
+            r.rrtmg_lw_dev(0, ncol, nlay, 0, 0, {**good, "play": t}, good)
+        assert "rrtmg_lw_dev" not in r.lib.calls, case
+    with pytest.raises(ValueError, match="uflx has"):
+        r.rrtmg_lw_dev(0, ncol, nlay, 0, 0, good, {**good, "uflx": _FakeTensor(sizes["uflx"] - 1, 0x2)})
+    nx, ny = R.adjoint_shape(nlay)
+    with pytest.raises(ValueError, match="grad has"):
+        r.vjp_dev(0, ncol, nlay, good, _FakeTensor(ny * ncol, 0x3), _FakeTensor(nx * ncol - 1, 0x4), 1.0, 0, 1360.0)

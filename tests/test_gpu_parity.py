@@ -309,6 +309,28 @@ def test_fp64_path_reproduces_golden_fixtures(gpu):
         assert rel_err(sw["swhr"], ref[f"{name}_swhr"], 1e-3) <= HR_TOL, name
 
 
+def test_sw_conserves_energy_without_absorbers(gpu, orc):
+    """Pure Rayleigh scattering over a white surface (no absorbers): the net SW
+    flux is zero at every level, to 1e-3 W/m2 (FP64; the reference's
+    single-scattering-albedo cap of 1 - 1e-6) and to 0.1 W/m2 (split, whose
+    delta-Eddington terms for nearly conservative layers are reformulated for
+    FP32); the FP64 path equals the oracle."""
+    from test_oracle import scattering_only
+    atm = scattering_only(ncol=64)
+    gpu.set_precision("fp64")
+    sw = gpu.sw(atm)
+    check_sw(sw, orc.rrtmg_sw(atm))
+    for prec, tol, htol in (("fp64", 1e-3, 1e-5), ("split", 0.1, 0.05)):
+        gpu.set_precision(prec)
+        try:
+            sw = gpu.sw(atm)
+        finally:
+            gpu.set_precision("fp64")
+        net = sw["swdflx"] - sw["swuflx"]
+        assert np.abs(net).max() <= tol, (prec, np.abs(net).max())
+        assert np.abs(sw["swhr"]).max() <= htol, prec
+
+
 @pytest.mark.parametrize("nlay", [100, 203])
 def test_deep_columns(gpu, orc, nlay):
     """Columns deeper than 64 layers (the solvers' 208-level variants), up to

@@ -40,6 +40,44 @@ def test_toa_insolation(orc):
     assert np.allclose(sw2["swdflx"], sw["swdflx"] * (1368.22 * 1.1 / 1360.0), rtol=1e-12)
 
 
+def scattering_only(ncol=8, nlay=40, seed=5, albedo=1.0):
+    """Columns without absorbers (no H2O, O3, CO2, CH4, N2O, O2): in the SW
+    only Rayleigh scattering remains."""
+    atm = A.small_atmosphere(ncol, nlay, seed=seed)
+    for k in ("h2o", "o3", "co2", "ch4", "n2o", "o2"):
+        setattr(atm, k, np.zeros_like(atm.play))
+    atm.coszen = np.linspace(0.1, 1.0, ncol)
+    for k in ("asdir", "asdif", "aldir", "aldif"):
+        setattr(atm, k, np.full(ncol, albedo))
+    return atm
+
+
+@pytest.mark.parametrize("albedo", [1.0, 0.3, 0.0])
+def test_sw_conserves_energy_without_absorbers(orc, albedo):
+    """Pure scattering absorbs nothing: the net SW flux is the same at every
+    level (no heating), and with a white surface it is zero -- everything
+    that comes in goes back out at the top.  The reference caps the single
+    scattering albedo at oneminus = 1 - 1e-6 (rrtmg_sw_rad.nomcica.f90:447), so
+    a layer keeps up to 1e-6 of what it extinguishes: 1e-3 W/m2 of 1300 in all
+    here.  Checks reftra's conservative branch and the adding method without
+    any k-table."""
+    atm = scattering_only(albedo=albedo)
+    for tables_mode in (True, False):
+        orc.set_table_mode(tables_mode)
+        try:
+            sw = orc.rrtmg_sw(atm)
+        finally:
+            orc.set_table_mode(True)
+        L = atm.nlay
+        net = sw["swdflx"] - sw["swuflx"]
+        assert np.abs(net - net[L]).max() <= 1e-3
+        assert np.abs(sw["swhr"]).max() <= 1e-5
+        if albedo == 1.0:
+            assert np.abs(net[L]).max() <= 1e-3
+        else:  # the surface absorbs (1 - albedo) of what reaches it, and something does
+            assert (net[0] > 0.0).all()
+
+
 def test_heating_rates_follow_from_fluxes(orc):
     atm = A.small_atmosphere(32, 60, seed=3)
     lw = orc.rrtmg_lw(atm)

@@ -11,6 +11,7 @@
 // two-stream pass).
 #pragma once
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>

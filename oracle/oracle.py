@@ -101,6 +101,31 @@ def rrtmg_lw_bands(atm, idrv: int = 0):
     return out
 
 
+LW_PHASES = ("inatm", "setcoef", "taumol", "rtrnmr")
+SW_PHASES = ("inatm_sw", "setcoef_sw", "taumol_sw", "spcvrt_sw")
+
+
+def phase_times(atm):
+    """Where the time goes on the CPU: seconds per column of each phase of the
+    clear-sky LW and SW path (one thread; SW over the sunlit columns), as two
+    dicts keyed by LW_PHASES / SW_PHASES.  spcvrt_sw holds the reference's two
+    two-stream passes (the clear and the "total" one) and the heating rates."""
+    ns = (C.c_longlong * 4)()
+    lw = [_f(a) for a in (atm.play, atm.plev, atm.tlay, atm.tlev, atm.tsfc, atm.h2o, atm.o3, atm.co2, atm.ch4,
+                          atm.n2o, atm.o2, atm.cfc11, atm.cfc12, atm.cfc22, atm.ccl4, atm.emis)]
+    if _lib.orc_lw_phase_times(C.c_int(atm.ncol), C.c_int(atm.nlay), *[_p(a) for a in lw], ns) != 0:
+        raise RuntimeError("orc_lw_phase_times failed")
+    out_lw = {k: v * 1e-9 / atm.ncol for k, v in zip(LW_PHASES, ns)}
+    sw = [_f(a) for a in (atm.play, atm.plev, atm.tlay, atm.tlev, atm.tsfc, atm.h2o, atm.o3, atm.co2, atm.ch4,
+                          atm.n2o, atm.o2, atm.asdir, atm.asdif, atm.aldir, atm.aldif, atm.coszen)]
+    if _lib.orc_sw_phase_times(C.c_int(atm.ncol), C.c_int(atm.nlay), *[_p(a) for a in sw],
+                               C.c_double(atm.adjes), C.c_int(atm.dyofyr), C.c_double(atm.scon), ns) != 0:
+        raise RuntimeError("orc_sw_phase_times failed")
+    lit = max(1, int((np.asarray(atm.coszen) >= 1e-10).sum()))
+    out_sw = {k: v * 1e-9 / lit for k, v in zip(SW_PHASES, ns)}
+    return out_lw, out_sw
+
+
 def rrtmg_sw(atm, iaer: int = 0, tauaer=None, ssaaer=None, asmaer=None, nthreads: int = 0):
     n, L = atm.ncol, atm.nlay
     out = {k: np.zeros((L + 1, n)) for k in ("swuflx", "swdflx", "swuflxc", "swdflxc")}

@@ -4,6 +4,7 @@
 // rrtmg_sw (rrtmg_sw_rad.nomcica.f90:78-88) for the clear-sky subset; arrays
 // are column-major with the column index fastest.  Columns run in parallel
 // with OpenMP (the reference loops over them serially, :453 / :500).
+#include <chrono>
 #include <cstdio>
 #include <exception>
 
@@ -148,6 +149,89 @@ int orc_rrtmg_lw_bands(int ncol, int nlay, int idrv, const double* play, const d
         bandd[ix] = o.bandd[b * nlev + k];
         if (idrv == 1 && dbandu_dt) dbandu_dt[ix] = o.dbandu_dt[b * nlev + k];
       }
+  }
+  return 0;
+}
+
+// Where the time goes: the clear-sky path's phases timed separately, one
+// thread, summed over the columns, in nanoseconds (integer clock ticks, so
+// that the FLOP-count build compiles the same code).  LW: ns[0..3] = inatm,
+// setcoef, taumol (with the aerosol add), rtrnmr.  SW: ns[0..3] = inatm_sw,
+// setcoef_sw, taumol_sw, spcvrt_sw without its taumol call plus the heating
+// rates; dark columns are skipped, as in rrtmg_sw.
+static long long ticks(std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
+  return (long long)std::chrono::duration_cast<std::chrono::nanoseconds>(b - a).count();
+}
+
+int orc_lw_phase_times(int ncol, int nlay, const double* play, const double* plev, const double* tlay,
+                       const double* tlev, const double* tsfc, const double* h2ovmr, const double* o3vmr,
+                       const double* co2vmr, const double* ch4vmr, const double* n2ovmr, const double* o2vmr,
+                       const double* cfc11vmr, const double* cfc12vmr, const double* cfc22vmr,
+                       const double* ccl4vmr, const double* emis, long long* ns) {
+  if (!g_ready) return 2;
+  LwInput in{ncol, nlay, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr,
+             cfc11vmr, cfc12vmr, cfc22vmr, ccl4vmr, emis, nullptr};
+  for (int k = 0; k < 4; ++k) ns[k] = 0;
+  LwColumn c;
+  LwOut o;
+  using clk = std::chrono::steady_clock;
+  for (int iplon = 0; iplon < ncol; ++iplon) {
+    const auto t0 = clk::now();
+    lw_inatm(in, iplon, c);
+    const auto t1 = clk::now();
+    lw_setcoef(c, 0);
+    const auto t2 = clk::now();
+    lw_taumol(c);
+    int ig = 1;
+    for (int b = 1; b <= 16; ++b)
+      for (; ig <= g_lw.ngs[b]; ++ig)
+        for (int k = 1; k <= c.nlayers; ++k) c.taut[ig][k] = c.taug[ig][k] + c.taua[b][k];
+    const auto t3 = clk::now();
+    lw_rtrnmr(c, 0, o);
+    const auto t4 = clk::now();
+    ns[0] += ticks(t0, t1);
+    ns[1] += ticks(t1, t2);
+    ns[2] += ticks(t2, t3);
+    ns[3] += ticks(t3, t4);
+  }
+  return 0;
+}
+
+int orc_sw_phase_times(int ncol, int nlay, const double* play, const double* plev, const double* tlay,
+                       const double* tlev, const double* tsfc, const double* h2ovmr, const double* o3vmr,
+                       const double* co2vmr, const double* ch4vmr, const double* n2ovmr, const double* o2vmr,
+                       const double* asdir, const double* asdif, const double* aldir, const double* aldif,
+                       const double* coszen, double adjes, int dyofyr, double scon, long long* ns) {
+  if (!g_ready) return 2;
+  SwInput in{ncol, nlay, 0, dyofyr, adjes, scon, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr,
+             ch4vmr, n2ovmr, o2vmr, asdir, asdif, aldir, aldif, coszen, nullptr, nullptr, nullptr};
+  for (int k = 0; k < 4; ++k) ns[k] = 0;
+  SwColumn c;
+  SwOut o;
+  using clk = std::chrono::steady_clock;
+  for (int iplon = 0; iplon < ncol; ++iplon) {
+    if (in.coszen[iplon] < 1.e-10) continue;
+    const auto t0 = clk::now();
+    sw_inatm(in, iplon, c);
+    const auto t1 = clk::now();
+    sw_setcoef(c);
+    const auto t2 = clk::now();
+    sw_taumol(c);
+    const auto t3 = clk::now();
+    double albdir[15], albdif[15];
+    for (int ib = 1; ib <= 14; ++ib) {
+      const bool vis = ib >= 10 && ib <= 13;
+      albdir[ib] = vis ? in.asdir[iplon] : in.aldir[iplon];
+      albdif[ib] = vis ? in.asdif[iplon] : in.aldif[iplon];
+    }
+    sw_spcvrt(c, in.coszen[iplon], albdir, albdif, o, false);
+    o.hr.assign(nlay + 1, 0.);
+    for (int i = 1; i < nlay; ++i) o.hr[i] = (o.fd[i + 1] - o.fu[i + 1] - (o.fd[i] - o.fu[i])) * (g_sw.heatfac / c.pdp[i]);
+    const auto t4 = clk::now();
+    ns[0] += ticks(t0, t1);
+    ns[1] += ticks(t1, t2);
+    ns[2] += ticks(t2, t3);
+    ns[3] += ticks(t3, t4);
   }
   return 0;
 }

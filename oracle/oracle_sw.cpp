@@ -795,14 +795,14 @@ static void vrtqdr(int klev, const std::vector<double>& pref, const std::vector<
 // ---------------------------------------------------------------------------
 // spcvrt_sw, icpr = 1, idelm = 1, clear sky (pclfr = 0, cloud optics 0/1/0)
 // ---------------------------------------------------------------------------
-void sw_spcvrt(SwColumn& c, double prmu0, const double* albdir, const double* albdif, SwOut& out) {
+void sw_spcvrt(SwColumn& c, double prmu0, const double* albdir, const double* albdif, SwOut& out, bool run_taumol) {
   const SwTables& T = g_sw;
   const int klev = c.nlayers;
   out.fu.assign(klev + 2, 0.);
   out.fd.assign(klev + 2, 0.);
   out.cu.assign(klev + 2, 0.);
   out.cd.assign(klev + 2, 0.);
-  sw_taumol(c);
+  if (run_taumol) sw_taumol(c);
   const int K = klev + 2;
   std::vector<double> ztauc(K), zomcc(K), zgcc(K), ztauo(K), zomco(K), zgco(K);
   std::vector<double> zrefc(K), zrefdc(K), ztrac(K), ztradc(K), zrefo(K), zrefdo(K), ztrao(K), ztrado(K);

@@ -68,7 +68,10 @@ void sw_init(const Blob& blob, double cpdair);
 void sw_inatm(const SwInput& in, int iplon, SwColumn& c);
 void sw_setcoef(SwColumn& c);
 void sw_taumol(SwColumn& c);
-void sw_spcvrt(SwColumn& c, double prmu0, const double* albdir, const double* albdif, SwOut& out);
+// run_taumol = false: the caller has already run sw_taumol on c (the phase
+// timing of the oracle); the results are the same.
+void sw_spcvrt(SwColumn& c, double prmu0, const double* albdir, const double* albdif, SwOut& out,
+               bool run_taumol = true);
 bool sw_column(const SwInput& in, int iplon, SwColumn& c, SwOut& out);
 
 }  // namespace orc

@@ -170,3 +170,22 @@ def test_oracle_reproduces_golden_fixtures(orc):
         if k == "blob_checksum":
             continue
         np.testing.assert_allclose(now[k], ref[k], rtol=1e-11, atol=1e-12, err_msg=k)
+
+
+def test_phase_times_cover_the_call(orc):
+    """Where the time goes (orc_*_phase_times): every phase takes time, and the
+    phases together account for a plain single-threaded call of the same
+    columns (loose bounds: timings on a shared host)."""
+    import time
+    atm = A.small_atmosphere(64, 40, seed=8)
+    lw, sw = orc.phase_times(atm)
+    assert set(lw) == set(orc.LW_PHASES) and set(sw) == set(orc.SW_PHASES)
+    assert all(v > 0 for v in list(lw.values()) + list(sw.values()))
+    t0 = time.perf_counter()
+    orc.rrtmg_lw(atm, nthreads=1)
+    t1 = time.perf_counter()
+    orc.rrtmg_sw(atm, nthreads=1)
+    t2 = time.perf_counter()
+    lit = int((atm.coszen >= 1e-10).sum())
+    assert 0.2 <= sum(lw.values()) * atm.ncol / (t1 - t0) <= 5.0
+    assert 0.2 <= sum(sw.values()) * lit / (t2 - t1) <= 5.0

@@ -10,6 +10,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -91,6 +92,14 @@ std::vector<float> to_f32(const std::vector<double>& v) {
 
 size_t align256(size_t n) { return (n + 255) & ~(size_t)255; }
 
+// Failure injection for tests, on the host (no GPU fault): with
+// RRTMG_GPU_FAIL_ALLOC=1 in the environment every workspace allocation fails
+// as cudaMalloc reports an exhausted device.
+bool alloc_failure_injected() {
+  const char* v = std::getenv("RRTMG_GPU_FAIL_ALLOC");
+  return v != nullptr && v[0] == '1';
+}
+
 // Grow a workspace; refuses while the stream is being captured.
 int ensure(rrtmg_gpu_state* h, DevBuf& b, size_t need, cudaStream_t s) {
   if (b.bytes >= need) return RRTMG_OK;
@@ -102,7 +111,7 @@ int ensure(rrtmg_gpu_state* h, DevBuf& b, size_t need, cudaStream_t s) {
   if (b.p) cudaFree(b.p);
   b.p = nullptr;
   b.bytes = 0;
-  cudaError_t e = cudaMalloc(&b.p, need);
+  cudaError_t e = alloc_failure_injected() ? cudaErrorMemoryAllocation : cudaMalloc(&b.p, need);
   if (e != cudaSuccess) {
     b.p = nullptr;
     return fail(h, RRTMG_ERR_NOMEM, std::string("device workspace allocation failed: ") + cudaGetErrorString(e));

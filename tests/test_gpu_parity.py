@@ -292,6 +292,35 @@ def test_launch_count_is_native(gpu):
     assert gpu.launch_count() - before == 8
 
 
+def test_allocation_failure_is_reported_and_recoverable(blob, monkeypatch):
+    """An injected workspace allocation failure (RRTMG_GPU_FAIL_ALLOC=1, made on
+    the host) is reported as RRTMG_ERR_NOMEM by the host and device calls; the
+    handle stays usable, and once allocations succeed again the results are
+    those of an undisturbed handle."""
+    import torch
+    atm = A.small_atmosphere(96, 40, seed=61)
+    ref = R.RRTMG(blob)
+    r = R.RRTMG(blob)  # a fresh handle: no workspace yet
+    try:
+        monkeypatch.setenv("RRTMG_GPU_FAIL_ALLOC", "1")
+        for call in (lambda: r.lw(atm), lambda: r.sw(atm)):
+            with pytest.raises(R.RRTMGError) as ei:
+                call()
+            assert "allocation" in str(ei.value)
+        d = R.atm_device_inputs(atm)
+        olw, _ = R.device_outputs(atm.ncol, atm.nlay)
+        with pytest.raises(R.RRTMGError):
+            r.rrtmg_lw_dev(torch.cuda.current_stream().cuda_stream, atm.ncol, atm.nlay, 0, 0, d, olw)
+        monkeypatch.delenv("RRTMG_GPU_FAIL_ALLOC")
+        got, want = r.lw(atm), ref.lw(atm)
+        for k in want:
+            assert np.array_equal(got[k], want[k]), k
+        assert np.array_equal(r.sw(atm)["swdflx"], ref.sw(atm)["swdflx"])
+    finally:
+        r.close()
+        ref.close()
+
+
 @pytest.mark.gpu
 def test_fp64_path_reproduces_golden_fixtures(gpu):
     """The committed oracle regression fixtures (tests/golden) at the FP64 tolerance."""

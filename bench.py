@@ -206,6 +206,19 @@ def cpu_baseline(atm_full, sample, steps=1):
     return sub.ncol / float(np.median(times)), threads, sub.ncol, times
 
 
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu), else the machine type."""
+    import platform
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name:"):
+                return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return platform.machine() or "unknown"
+
+
 def run_reference(args):
     from mima_gb300 import atmosphere
     rank = int(os.environ.get("RANK", "0"))
@@ -222,7 +235,7 @@ def run_reference(args):
         "data": "synthetic (seeded atmospheres of the configured grid; synthetic LW k-distribution, AER SW tables)",
         "config": {"workload": workload_name(args.config, atm), "per_gpu_columns": atm.ncol,
                    "sample": f"{nsample} of the {atm.ncol} columns per step"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "model": cpu_model(), "kind": "port",
                          "sample": f"{nsample} of {atm.ncol} columns, LW+SW, FP64 lookup-table path"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "reference Fortran not buildable here (no Fortran compiler); C++ FP64 restatement timed",
@@ -668,7 +681,7 @@ def run_ours(args):
                               f"step algorithmic bytes {nbytes}"),
                      "compute": compute},
         "kernels_ms": {"split": kms32, "fp64": kms64},
-        "cpu_baseline": {"value": cpu_value, "unit": UNIT, "cores": threads, "kind": "port",
+        "cpu_baseline": {"value": cpu_value, "unit": UNIT, "cores": threads, "model": cpu_model(), "kind": "port",
                          "sample": f"{nsample} of {atm.ncol} columns, LW+SW FP64 C++ restatement"},
     }
     if e2e:

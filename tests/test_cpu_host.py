@@ -144,6 +144,7 @@ def test_bench_reference_arm_line():
     assert d["impl"] == "reference" and d["metric"] == bench.METRIC and d["unit"] == bench.UNIT
     assert d["value"] > 0 and d["e2e"]["value"] == d["value"] and d["cpu_baseline"]["kind"] == "port"
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+    assert d["cpu_baseline"]["cores"] >= 1 and d["cpu_baseline"]["model"]
     assert d["config"]["workload"] == bench.workload_name(0, A.config_atmosphere(0))
 
 

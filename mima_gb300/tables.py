@@ -20,8 +20,10 @@ g-point reduction as real data would.  Every LW result built on them is a
 synthetic-k-distribution result.  Where a ``rrtmg_lw_k_g.f90`` is at hand (the
 AER RRTMG_LW distribution's data file), ``build_blob(..., lw_kg=path)`` (or
 ``--lw-kg`` on the command line) parses the real LW k-distribution from it
-instead, with the parser of the SW data, and the kernels then compute the
-reference's physical LW fluxes.
+instead, with the parser of the SW data; ``lw_nc=`` / ``--lw-nc`` reads it from
+the netCDF form ``rrtmg_lw.nc`` the way the reference's
+``rrtmg_lw_read_nc.f90`` does.  The kernels then compute the reference's
+physical LW fluxes.
 
 Nothing here is used at run time by the kernels: the output is one binary
 "table blob" (format below) that the C-ABI's ``rrtmg_gpu_init`` reads, reduces
@@ -444,6 +446,92 @@ def lw_kg_tables(path, shapes: dict) -> dict:
     return out
 
 
+def lw_nc_reads(reader_src, params) -> list:
+    """The reads that the reference's netCDF reader of the LW data
+    (``rrtmg_lw_read_nc.f90``, routines ``lw_kgb01..16``) performs, in order:
+    [(band, target table, target section or None, netCDF variable, Fortran
+    start, Fortran count)], the
+    start and count vectors evaluated from the routine's parameters
+    (bandNumber, numGPoints, gPointSetNumber), ``rrlw_ncpar``'s dimension
+    constants and the absorber index ``getAbsorberIndex`` set (1-based position
+    in ``AbsorberNames``).  ``params``: integer constants of parrrtm /
+    rrlw_ncpar; the absorber names are read from ``rrlw_ncpar.f90``'s
+    directory."""
+    src = Path(reader_src)
+    names_src = (src.parent.parent / "modules" / "rrlw_ncpar.f90").read_text()
+    m = re.search(r"AbsorberNames\s*=\s*\(/(.*?)/\)", names_src.replace("&", " "), re.S)
+    absorbers = [a.strip().upper() for a in re.findall(r"'([^']*)'", m.group(1))]
+    reads, local, var = [], {}, None
+    for routine, st in _statements(src):
+        if not routine or not routine.startswith("lw_kgb"):
+            local, var = {}, None
+            continue
+        band = int(routine[6:])
+        pm = re.match(r"(?i)^integer.*parameter\s*::(.*)$", st)
+        if pm:
+            for part in _split_top(pm.group(1)):
+                k, v = part.split("=", 1)
+                v = v.strip().lower()
+                local[k.strip().lower()] = int(v) if v.lstrip("-").isdigit() else params[v]
+            continue
+        am = re.match(r"(?i)^call\s+getabsorberindex\s*\(\s*'(\w+)'\s*,\s*(\w+)\s*\)", st)
+        if am:
+            local[am.group(2).lower()] = absorbers.index(am.group(1).upper()) + 1
+            continue
+        vm = re.search(r'(?i)nf90_inq_varid\s*\(\s*ncid\s*,\s*"(\w+)"', st)
+        if vm:
+            var = vm.group(1)
+            continue
+        gm = re.search(r"(?i)nf90_get_var\s*\(\s*ncid\s*,\s*varid\s*,\s*(\w+)\s*(\(([^)]*)\))?\s*,"
+                       r"\s*start\s*=\s*\(/(.*?)/\)\s*,\s*count\s*=\s*\(/(.*?)/\)\s*\)", st)
+        if gm:
+            ev = lambda t: int(t) if t.strip().isdigit() else {**params, **local}[t.strip().lower()]
+            start = [ev(t) for t in gm.group(4).split(",")]
+            count = [ev(t) for t in gm.group(5).split(",")]
+            reads.append((band, gm.group(1).lower(), gm.group(3), var, start, count))
+    return reads
+
+
+def lw_nc_tables(nc_path, reader_src, params, shapes: dict) -> dict:
+    """The real LW k-distribution from the netCDF form of the data
+    (``rrtmg_lw.nc``), read as the reference's reader reads it
+    (:func:`lw_nc_reads`): every hyperslab in Fortran element order into its
+    16-g table.  netCDF-3 files only (scipy); a table that ``shapes`` declares
+    but no read fills is an error."""
+    from scipy.io import netcdf_file
+    with open(nc_path, "rb") as fh:
+        magic = fh.read(4)
+    if magic.startswith(b"\x89HDF"):
+        raise ValueError(f"{nc_path}: a netCDF-4 (HDF5) file; convert it to netCDF-3 (nccopy -k classic)")
+    out = {}
+    filled = {}
+    with netcdf_file(str(nc_path), "r", mmap=False) as f:
+        for band, name, section, var, start, count in lw_nc_reads(reader_src, params):
+            if name not in shapes.get(band, {}):
+                continue
+            if var not in f.variables:
+                raise ValueError(f"{nc_path}: no variable {var}")
+            a = np.asarray(f.variables[var].data, dtype=np.float64).transpose()  # Fortran axis order
+            if a.ndim != len(start) or any(s < 1 or s - 1 + c > n for s, c, n in zip(start, count, a.shape)):
+                raise ValueError(f"{nc_path}: {var} {a.shape} does not hold the hyperslab {start} + {count}")
+            hs = a[tuple(slice(s - 1, s - 1 + c) for s, c in zip(start, count))]
+            # nf90_get_var fills the target (or its section) in Fortran element order
+            try:
+                _assign(filled.setdefault(band, {}), shapes[band][name], name, section,
+                        list(hs.flatten(order="F")))
+            except AssertionError:
+                raise ValueError(f"{nc_path}: {var} for LW band {band} table {name}: {hs.size} values do not "
+                                 f"fill {section or 'the table'}") from None
+    out = {}
+    for b in range(1, 17):
+        for name, (lb, shape) in sorted(shapes[b].items()):
+            arr = filled.get(b, {}).get(name)
+            if arr is None or np.isnan(arr).any():
+                raise ValueError(f"{nc_path}: LW band {b} table {name} is not read in full from the file")
+            out[f"lw{b:02d}.{name}"] = (np.ascontiguousarray(arr), lb)
+    return out
+
+
 def _log_table(rng, shape, lo, hi, tslope=0.0):
     """log10-spread table increasing along the trailing g axis.
 
@@ -541,13 +629,30 @@ def read_blob(path) -> dict:
     return out
 
 
-def build_blob(reference_root, out_path=DEFAULT_BLOB, lw_seed: int = DEFAULT_LW_SEED, lw_kg=None) -> Path:
+def lw_nc_params(reference_root) -> dict:
+    """Integer constants the netCDF reader's start / count vectors use
+    (parrrtm, rrlw_ncpar, rrlw_kgNN)."""
+    P = _paths(reference_root)
+    return _int_params([P["lw_mod"] / "parrrtm.f90", P["lw_mod"] / "rrlw_ncpar.f90"] +
+                       sorted(P["lw_mod"].glob("rrlw_kg*.f90")))
+
+
+def build_blob(reference_root, out_path=DEFAULT_BLOB, lw_seed: int = DEFAULT_LW_SEED, lw_kg=None,
+               lw_nc=None) -> Path:
     """Parse the reference tables and write the blob.  The LW k-distribution
-    is the real one of ``lw_kg`` (a ``rrtmg_lw_k_g.f90``) when given, else
-    the seeded synthetic one (the MiMA tree does not ship the LW data)."""
+    is the real one of ``lw_kg`` (a ``rrtmg_lw_k_g.f90``) or ``lw_nc`` (a
+    netCDF-3 ``rrtmg_lw.nc``, read as ``rrtmg_lw_read_nc.f90`` reads it) when
+    given, else the seeded synthetic one (the MiMA tree does not ship the LW
+    data)."""
     tables, shapes = reference_tables(reference_root)
-    if lw_kg is not None:
-        tables.update(lw_kg_tables(lw_kg, shapes))
+    if lw_kg is not None and lw_nc is not None:
+        raise ValueError("give the LW data as rrtmg_lw_k_g.f90 or as rrtmg_lw.nc, not both")
+    if lw_kg is not None or lw_nc is not None:
+        if lw_kg is not None:
+            tables.update(lw_kg_tables(lw_kg, shapes))
+        else:
+            reader = _paths(reference_root)["lw_src"] / "rrtmg_lw_read_nc.f90"
+            tables.update(lw_nc_tables(lw_nc, reader, lw_nc_params(reference_root), shapes))
         tables["meta.lw_real_kdist"] = (np.asarray([1], dtype=np.int32), (1,))
     else:
         tables.update(synthetic_lw_tables(shapes, lw_seed))
@@ -577,5 +682,7 @@ if __name__ == "__main__":
     ap.add_argument("--lw-seed", type=int, default=DEFAULT_LW_SEED)
     ap.add_argument("--lw-kg", default=None,
                     help="rrtmg_lw_k_g.f90 holding the real LW k-distribution (default: synthetic)")
+    ap.add_argument("--lw-nc", default=None,
+                    help="rrtmg_lw.nc (netCDF-3) holding the real LW k-distribution (default: synthetic)")
     a = ap.parse_args()
-    print(build_blob(a.mima_root, a.out, a.lw_seed, a.lw_kg))
+    print(build_blob(a.mima_root, a.out, a.lw_seed, a.lw_kg, a.lw_nc))

@@ -206,3 +206,108 @@ def test_blob_from_lw_kg_file(blob, tmp_path):
     assert set(a) - {"meta.lw_synthetic_seed"} == set(b) - {"meta.lw_real_kdist"}
     for k in set(a) & set(b):
         assert np.array_equal(a[k][0], b[k][0]) and a[k][1] == b[k][1], k
+
+
+# ---- the netCDF form (rrtmg_lw.nc, read as rrtmg_lw_read_nc.f90 reads it) --
+
+def _reference_root_or_skip():
+    import __graft_entry__ as ge
+    root = ge._reference_root()
+    if root is None:
+        pytest.skip("no MiMA source tree")
+    return root
+
+
+def _nc_reads(root):
+    reader = tables._paths(root)["lw_src"] / "rrtmg_lw_read_nc.f90"
+    return reader, tables.lw_nc_reads(reader, tables.lw_nc_params(root))
+
+
+def _section(a, lb, sec):
+    if sec is None:
+        return a
+    idx = []
+    for p, lo in zip(sec.split(","), lb):
+        p = p.strip()
+        if p == ":":
+            idx.append(slice(None))
+        elif ":" in p:
+            x, y = (int(v) for v in p.split(":"))
+            idx.append(slice(x - lo, y - lo + 1))
+        else:
+            idx.append(int(p) - lo)
+    return a[tuple(idx)]
+
+
+def _write_lw_nc(path, bands, reads, skip_var=None):
+    """A netCDF-3 file holding ``bands``' tables where the reads find them:
+    each variable as large as its reads reach, dimensions in the file's
+    (reversed Fortran) order."""
+    from scipy.io import netcdf_file
+    ext = {}
+    for _, _, _, var, start, count in reads:
+        e = ext.setdefault(var, [1] * len(start))
+        for i, (s0, c) in enumerate(zip(start, count)):
+            e[i] = max(e[i], s0 - 1 + c)
+    arrays = {v: np.zeros(e) for v, e in ext.items()}
+    for b, name, sec, var, start, count in reads:
+        a, lb = bands[b][name]
+        vals = np.asarray(_section(a, lb, sec)).flatten(order="F")
+        arrays[var][tuple(slice(s0 - 1, s0 - 1 + c) for s0, c in zip(start, count))] = vals.reshape(count, order="F")
+    with netcdf_file(str(path), "w") as f:
+        for v, a in arrays.items():
+            if v == skip_var:
+                continue
+            dims = []
+            for i, n in enumerate(reversed(a.shape)):
+                dims.append(f"{v}_{i}")
+                f.createDimension(dims[-1], n)
+            f.createVariable(v, "d", tuple(dims))[:] = a.transpose()
+
+
+def test_lw_nc_reader_parse_covers_every_table(blob):
+    root = _reference_root_or_skip()
+    _, reads = _nc_reads(root)
+    bands = _lw_band_tables(blob)
+    assert len(reads) == 115
+    assert {(b, n) for b, n, *_ in reads} == {(b, n) for b, t in bands.items() for n in t}
+    for b, name, sec, var, start, count in reads:
+        a, lb = bands[b][name]
+        assert int(np.prod(count)) == np.asarray(_section(a, lb, sec)).size, (b, name)
+        assert start[-2] == b and start[-1] == 1  # band, g-point set 1
+
+
+def test_lw_nc_round_trip(blob, tmp_path):
+    root = _reference_root_or_skip()
+    reader, reads = _nc_reads(root)
+    bands = _lw_band_tables(blob)
+    shapes = {b: {n: (lb, a.shape) for n, (a, lb) in t.items()} for b, t in bands.items()}
+    p = tmp_path / "rrtmg_lw.nc"
+    _write_lw_nc(p, bands, reads)
+    got = tables.lw_nc_tables(p, reader, tables.lw_nc_params(root), shapes)
+    for b, t in bands.items():
+        for n, (a, lb) in t.items():
+            g, glb = got[f"lw{b:02d}.{n}"]
+            assert glb == lb and np.array_equal(g, a), (b, n)
+    out = tables.build_blob(root, tmp_path / "nc.bin", lw_nc=p)
+    x, y = tables.read_blob(blob), tables.read_blob(out)
+    assert "meta.lw_real_kdist" in y and set(x) - {"meta.lw_synthetic_seed"} == set(y) - {"meta.lw_real_kdist"}
+    for k in set(x) & set(y):
+        assert np.array_equal(x[k][0], y[k][0]), k
+
+
+def test_lw_nc_refuses_what_it_can_not_read(blob, tmp_path):
+    root = _reference_root_or_skip()
+    reader, reads = _nc_reads(root)
+    bands = _lw_band_tables(blob)
+    shapes = {b: {n: (lb, a.shape) for n, (a, lb) in t.items()} for b, t in bands.items()}
+    p = tmp_path / "partial.nc"
+    _write_lw_nc(p, bands, reads, skip_var="H20SelfAbsorptionCoefficients")
+    with pytest.raises(ValueError, match="no variable H20SelfAbsorptionCoefficients"):
+        tables.lw_nc_tables(p, reader, tables.lw_nc_params(root), shapes)
+    h5 = tmp_path / "hdf5.nc"
+    h5.write_bytes(b"\x89HDF\r\n\x1a\n" + b"\0" * 64)
+    with pytest.raises(ValueError, match="netCDF-4"):
+        tables.lw_nc_tables(h5, reader, tables.lw_nc_params(root), shapes)
+    with pytest.raises(ValueError, match="not both"):
+        tables.build_blob(root, tmp_path / "x.bin", lw_kg=p, lw_nc=p)

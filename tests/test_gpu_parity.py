@@ -387,3 +387,26 @@ def test_deep_columns(gpu, orc, nlay):
     for k in ("swuflx", "swdflx"):
         assert np.abs(sw[k] - rsw[k]).max() <= 0.1, k
     assert np.isfinite(lw["hr"]).all() and np.isfinite(sw["swhr"]).all()
+
+
+def test_edge_columns(gpu, orc):
+    """The fewest layers (2, 3) and columns wholly below or wholly above the
+    troposphere boundary (laytrop = nlay: the solar-source search reads past the
+    last layer, as the reference's jp(lay+1); laytrop = 0: the lower-atmosphere
+    loops are empty): FP64 against the oracle at the FP64 tolerances, split
+    within 0.1 W/m2 at every level."""
+    from test_oracle import edge_columns
+    for name, atm in edge_columns().items():
+        rlw, rsw = orc.rrtmg_lw(atm, idrv=1), orc.rrtmg_sw(atm)
+        gpu.set_precision("fp64")
+        check_lw(gpu.lw(atm, idrv=1), rlw, idrv=1)
+        check_sw(gpu.sw(atm), rsw)
+        gpu.set_precision("split")
+        try:
+            lw, sw = gpu.lw(atm), gpu.sw(atm)
+        finally:
+            gpu.set_precision("fp64")
+        for k in ("uflx", "dflx"):
+            assert np.abs(lw[k] - rlw[k]).max() <= 0.1, (name, k)
+        for k in ("swuflx", "swdflx"):
+            assert np.abs(sw[k] - rsw[k]).max() <= 0.1, (name, k)

@@ -189,3 +189,34 @@ def test_phase_times_cover_the_call(orc):
     lit = int((atm.coszen >= 1e-10).sum())
     assert 0.2 <= sum(lw.values()) * atm.ncol / (t1 - t0) <= 5.0
     assert 0.2 <= sum(sw.values()) * lit / (t2 - t1) <= 5.0
+
+
+def edge_columns():
+    """Columns at the edges of the layer structure: the fewest layers (2, 3);
+    a column wholly below the troposphere boundary ln p = 4.56 (200-1000 hPa:
+    laytrop = nlay, so the lower-atmosphere loops reach the last layer and the
+    upper ones are empty); one wholly above it (0.1-90 hPa: laytrop = 0)."""
+    def remap(atm, top, bot, log=False):
+        pt, pb = atm.plev[-1, 0], atm.plev[0, 0]
+        if log:
+            k = (np.log(bot) - np.log(top)) / (np.log(pb) - np.log(pt))
+            f = lambda p: np.exp(np.log(top) + (np.log(p) - np.log(pt)) * k)
+        else:
+            f = lambda p: top + (p - pt) * (bot - top) / (pb - pt)
+        atm.plev, atm.play = f(atm.plev), f(atm.play)
+        return atm
+    return {"nlay2": A.small_atmosphere(33, 2, seed=71), "nlay3": A.small_atmosphere(33, 3, seed=72),
+            "below_tropopause": remap(A.small_atmosphere(33, 20, seed=73), 200.0, 1000.0),
+            "above_tropopause": remap(A.small_atmosphere(33, 20, seed=74), 0.1, 90.0, log=True)}
+
+
+def test_edge_columns(orc):
+    cols = edge_columns()
+    lt = {k: (np.log(a.play) > 4.56).sum(axis=0) for k, a in cols.items()}
+    assert (lt["below_tropopause"] == 20).all() and (lt["above_tropopause"] == 0).all()
+    for k, atm in cols.items():
+        lw, sw = orc.rrtmg_lw(atm), orc.rrtmg_sw(atm)
+        for d in (lw, sw):
+            for name, v in d.items():
+                assert np.isfinite(v).all(), (k, name)
+        assert (lw["uflx"] > 0).all() and (sw["swdflx"][-1] > 0).all(), k

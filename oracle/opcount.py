@@ -71,6 +71,30 @@ def flops(c) -> float:
     return float(sum(c[k] for k in FLOP_KINDS))
 
 
+LW_PHASES = ("inatm", "setcoef", "taumol", "rtrnmr")
+SW_PHASES = ("inatm_sw", "setcoef_sw", "taumol_sw", "spcvrt_sw")
+
+
+def phase_flops(atm):
+    """FLOPs per column of each phase of the clear-sky LW and SW path (SW over
+    the sunlit columns), as two dicts keyed by LW_PHASES / SW_PHASES."""
+    nk = len(KINDS)
+    buf = (C.c_ulonglong * (4 * nk))()
+    f = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    p = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    lw = [f(a) for a in (atm.play, atm.plev, atm.tlay, atm.tlev, atm.tsfc, atm.h2o, atm.o3, atm.co2, atm.ch4,
+                         atm.n2o, atm.o2, atm.cfc11, atm.cfc12, atm.cfc22, atm.ccl4, atm.emis)]
+    _lib.orc_lw_phase_counts(C.c_int(atm.ncol), C.c_int(atm.nlay), *[p(a) for a in lw], buf)
+    per = lambda n: [flops(dict(zip(KINDS, (buf[ph * nk + k] / n for k in range(nk))))) for ph in range(4)]
+    out_lw = dict(zip(LW_PHASES, per(atm.ncol)))
+    sw = [f(a) for a in (atm.play, atm.plev, atm.tlay, atm.tlev, atm.tsfc, atm.h2o, atm.o3, atm.co2, atm.ch4,
+                         atm.n2o, atm.o2, atm.asdir, atm.asdif, atm.aldir, atm.aldif, atm.coszen)]
+    _lib.orc_sw_phase_counts(C.c_int(atm.ncol), C.c_int(atm.nlay), *[p(a) for a in sw], C.c_double(atm.adjes),
+                             C.c_int(atm.dyofyr), C.c_double(atm.scon), buf)
+    lit = max(1, int((np.asarray(atm.coszen) >= 1e-10).sum()))
+    return out_lw, dict(zip(SW_PHASES, per(lit)))
+
+
 def table(blob_path, layers=(20, 40, 60, 80), ncol: int = 8, seed: int = 11):
     """FLOPs per column of LW and SW for each layer count, and the least-squares
     line a + b L through them."""

@@ -50,3 +50,18 @@ def test_bench_constants_are_the_counted_table(blob, counting):
     np.testing.assert_allclose(bench.ALG_FLOPS_FIT["sw_gpoint"], fsw, rtol=1e-6)
     assert bench.algorithmic_flops("sw_gpoint", 40) == bench.ALG_FLOPS_PER_COLUMN["sw_gpoint"][1]
     assert bench.algorithmic_flops("lw_gpoint", 100) == pytest.approx(flw[0] * 100 + flw[1])
+
+
+def test_phase_flops_add_up_to_the_path(blob, counting):
+    """The per-phase counts (orc_*_phase_counts) add up to the whole path's:
+    exactly for LW; for SW but for the clear-sky heating rates, which the
+    whole call also computes (a few operations per layer)."""
+    atm = A.small_atmosphere(6, 40, seed=11, rh_random=False)
+    lw, sw = P.phase_flops(atm)
+    _, _, cl, cs = P.count(atm)
+    assert all(v > 0 for v in list(lw.values()) + list(sw.values()))
+    assert sum(lw.values()) == pytest.approx(P.flops(cl), rel=1e-12)
+    assert 0 <= P.flops(cs) - sum(sw.values()) <= 10 * atm.nlay
+    # the g-point work dominates both paths
+    assert (lw["taumol"] + lw["rtrnmr"]) / sum(lw.values()) > 0.9
+    assert (sw["taumol_sw"] + sw["spcvrt_sw"]) / sum(sw.values()) > 0.9

@@ -410,3 +410,41 @@ def test_edge_columns(gpu, orc):
             assert np.abs(lw[k] - rlw[k]).max() <= 0.1, (name, k)
         for k in ("swuflx", "swdflx"):
             assert np.abs(sw[k] - rsw[k]).max() <= 0.1, (name, k)
+
+
+def test_random_columns(gpu, orc):
+    """Seeded random cases across the inputs: layer counts on both sides of the
+    solvers' 64 / 208-level switch, ragged column counts, surface-temperature
+    spread, gas amounts (CO2 100-2000 ppmv, O3 and H2O scaled, the secondary
+    gases on or off), spectral emissivity, albedos, dark and sunlit columns,
+    idrv, LW and SW aerosols -- the FP64 path against the oracle at the FP64
+    tolerances."""
+    rng = np.random.default_rng(2024)
+    gpu.set_precision("fp64")
+    for case in range(12):
+        nlay = int(rng.choice([2, 5, 17, 40, 64, 65, 90]))
+        ncol = int(rng.integers(1, 200))
+        atm = A.small_atmosphere(ncol, nlay, seed=int(rng.integers(1 << 30)), ts_sigma=float(rng.uniform(0.0, 15.0)),
+                                 rh_random=bool(rng.integers(2)))
+        shp = atm.play.shape
+        atm.co2 = rng.uniform(100e-6, 2000e-6, size=shp)
+        atm.o3 = atm.o3 * rng.uniform(0.0, 3.0)
+        atm.h2o = np.clip(atm.h2o * rng.uniform(0.05, 1.5), 1e-7, 0.05)
+        if rng.integers(2):
+            atm.ch4, atm.n2o, atm.o2 = np.full(shp, 1.8e-6), np.full(shp, 3.2e-7), np.full(shp, 0.209)
+            atm.cfc11, atm.cfc12 = np.full(shp, 2.5e-10), np.full(shp, 5.0e-10)
+            atm.cfc22, atm.ccl4 = np.full(shp, 1.5e-10), np.full(shp, 1.0e-10)
+        atm.emis = rng.uniform(0.8, 1.0, size=(16, ncol))
+        atm.coszen = rng.uniform(0.0, 1.0, ncol) * (rng.uniform(size=ncol) > 0.3)
+        for k in ("asdir", "asdif", "aldir", "aldif"):
+            setattr(atm, k, rng.uniform(0.0, 0.9, ncol))
+        idrv = int(rng.integers(2))
+        lw_aer = rng.uniform(0.0, 0.05, size=(16, nlay, ncol)) if rng.integers(2) else None
+        check_lw(gpu.lw(atm, idrv=idrv, tauaer=lw_aer), orc.rrtmg_lw(atm, idrv=idrv, tauaer=lw_aer), idrv=idrv)
+        if rng.integers(2):
+            aer = dict(iaer=10, tauaer=rng.uniform(0.0, 0.1, size=(14, nlay, ncol)),
+                       ssaaer=rng.uniform(0.8, 1.0, size=(14, nlay, ncol)),
+                       asmaer=rng.uniform(0.0, 0.8, size=(14, nlay, ncol)))
+        else:
+            aer = {}
+        check_sw(gpu.sw(atm, **aer), orc.rrtmg_sw(atm, **aer))

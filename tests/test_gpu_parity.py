@@ -418,7 +418,7 @@ def test_random_columns(gpu, orc):
     spread, gas amounts (CO2 100-2000 ppmv, O3 and H2O scaled, the secondary
     gases on or off), spectral emissivity, albedos, dark and sunlit columns,
     idrv, LW and SW aerosols -- the FP64 path against the oracle at the FP64
-    tolerances."""
+    tolerances, the split path within 0.1 W/m2 of it at every level."""
     rng = np.random.default_rng(2024)
     gpu.set_precision("fp64")
     for case in range(12):
@@ -447,4 +447,14 @@ def test_random_columns(gpu, orc):
                        asmaer=rng.uniform(0.0, 0.8, size=(14, nlay, ncol)))
         else:
             aer = {}
-        check_sw(gpu.sw(atm, **aer), orc.rrtmg_sw(atm, **aer))
+        rlw, rsw = orc.rrtmg_lw(atm, idrv=idrv, tauaer=lw_aer), orc.rrtmg_sw(atm, **aer)
+        check_sw(gpu.sw(atm, **aer), rsw)
+        gpu.set_precision("split")
+        try:
+            slw, ssw = gpu.lw(atm, idrv=idrv, tauaer=lw_aer), gpu.sw(atm, **aer)
+        finally:
+            gpu.set_precision("fp64")
+        for k in ("uflx", "dflx"):
+            assert np.abs(slw[k] - rlw[k]).max() <= 0.1, (case, k)
+        for k in ("swuflx", "swdflx"):
+            assert np.abs(ssw[k] - rsw[k]).max() <= 0.1, (case, k)

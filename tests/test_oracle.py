@@ -220,3 +220,29 @@ def test_edge_columns(orc):
             for name, v in d.items():
                 assert np.isfinite(v).all(), (k, name)
         assert (lw["uflx"] > 0).all() and (sw["swdflx"][-1] > 0).all(), k
+
+
+def test_gas_optics_stage(orc, blob):
+    """The gas-optics stage on its own (orc_lw_optics / orc_sw_optics): in
+    every layer the Planck fractions of a band sum to 1 over its g-points (the
+    eta-interpolation weights sum to 1), except in LW bands 12 and 15 above
+    the troposphere boundary, which have no upper-atmosphere absorber (optical
+    depth and fractions 0, rrtmg_lw_taumol.f90 taugb12 / taugb15); the SW
+    solar source of every column sums to the Kurucz total, 1368.22 W/m2; the
+    Rayleigh optical depths are positive."""
+    from mima_gb300 import tables
+    atm = A.small_atmosphere(16, 40, seed=3, ts_sigma=8.0)
+    taug, fracs, laytrop = orc.lw_optics(atm)
+    ngc = tables.read_blob(blob)["lw.ngc"][0].ravel()
+    edges = np.concatenate([[0], np.cumsum(ngc)])
+    upper = np.arange(atm.nlay)[:, None] >= laytrop[None, :]
+    for b in range(16):
+        s = fracs[edges[b]:edges[b + 1]].sum(axis=0)
+        if b + 1 in (12, 15):
+            np.testing.assert_allclose(s[~upper], 1.0, atol=1e-12)
+            assert (s[upper] == 0.0).all() and (taug[edges[b]:edges[b + 1]][:, upper] == 0.0).all()
+        else:
+            np.testing.assert_allclose(s, 1.0, atol=1e-12, err_msg=f"band {b + 1}")
+    gtaug, taur, sfz = orc.sw_optics(atm)
+    np.testing.assert_allclose(sfz.sum(axis=0), 1368.22, rtol=1e-5)
+    assert (taur > 0).all() and (gtaug >= 0).all()

@@ -458,3 +458,23 @@ def test_random_columns(gpu, orc):
             assert np.abs(slw[k] - rlw[k]).max() <= 0.1, (case, k)
         for k in ("swuflx", "swdflx"):
             assert np.abs(ssw[k] - rsw[k]).max() <= 0.1, (case, k)
+
+
+def test_grazing_sun(gpu, orc):
+    """Sun just above the horizon (coszen 2e-10 ... 0.05, above MiMA's 1e-10
+    skip): direct-beam transmittances underflow and the exp-table index
+    saturates.  FP64 against the oracle at the FP64 tolerances; split within
+    0.1 W/m2 and 0.05 K/day."""
+    atm = A.small_atmosphere(6, 40, seed=81)
+    atm.coszen = np.array([2e-10, 1e-8, 1e-5, 1e-3, 0.01, 0.05])
+    ref = orc.rrtmg_sw(atm)
+    gpu.set_precision("fp64")
+    check_sw(gpu.sw(atm), ref)
+    gpu.set_precision("split")
+    try:
+        sw = gpu.sw(atm)
+    finally:
+        gpu.set_precision("fp64")
+    for k in ("swuflx", "swdflx"):
+        assert np.abs(sw[k] - ref[k]).max() <= 0.1, k
+    assert np.abs(sw["swhr"] - ref["swhr"]).max() <= 0.05

@@ -305,3 +305,31 @@ def test_device_wrappers_refuse_wrong_tensors():
     nx, ny = R.adjoint_shape(nlay)
     with pytest.raises(ValueError, match="grad has"):
         r.vjp_dev(0, ncol, nlay, good, _FakeTensor(ny * ncol, 0x3), _FakeTensor(nx * ncol - 1, 0x4), 1.0, 0, 1360.0)
+
+
+def test_run_params_layout_agrees_everywhere():
+    """rrtmg_run_params has one member order in the C header, the ctypes
+    mirror and the Fortran bind(C) type of the integration guide, and the
+    library's defaults fill the ctypes structure (a host-only call)."""
+    hdr = (ROOT / "include" / "rrtmg_run.h").read_text()
+    body = re.search(r"typedef struct\s*\w*\s*\{(.*?)\}\s*rrtmg_run_params;", hdr, re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    c_fields = []
+    for decl in body.split(";"):
+        m = re.match(r"\s*(int|double)\s+(.*)$", decl.strip(), re.S)
+        if m:
+            c_fields += [(m.group(1), n.strip()) for n in m.group(2).split(",")]
+    py_fields = [("int" if t is C.c_int else "double", n) for n, t in R.RunParams._fields_]
+    assert c_fields == py_fields
+    guide = (ROOT / "INTEGRATION.md").read_text()
+    ftype = re.search(r"type, bind\(C\) :: rrtmg_run_params(.*?)end type", guide, re.S).group(1)
+    f_fields = []
+    for kind, names in re.findall(r"(integer\(c_int\)|real\(c_double\)) ::(.*?)(?=integer\(c_int\)|real\(c_double\)|$)",
+                                  ftype.replace("&", " ").replace("!", "\n!"), re.S):
+        names = re.sub(r"!.*", "", names)
+        f_fields += [("int" if kind.startswith("integer") else "double", n.strip())
+                     for n in names.split(",") if n.strip()]
+    assert f_fields == c_fields
+    assert C.sizeof(R.RunParams) == 10 * 4 + 22 * 8
+    p = R.run_params()
+    assert (p.lonstep, p.dt_rad_avg, p.co2ppmv, p.obliq, p.solr_cnst) == (1, 86400, 300.0, 23.439, 1368.22)

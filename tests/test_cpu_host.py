@@ -333,3 +333,22 @@ def test_run_params_layout_agrees_everywhere():
     assert C.sizeof(R.RunParams) == 10 * 4 + 22 * 8
     p = R.run_params()
     assert (p.lonstep, p.dt_rad_avg, p.co2ppmv, p.obliq, p.solr_cnst) == (1, 86400, 300.0, 23.439, 1368.22)
+
+
+def test_fortran_interfaces_follow_the_header():
+    """Every bind(C) interface of the integration guide lists the C entry
+    point's arguments in the header's order (by name where the Fortran uses
+    the header's names; by count for rrtmg_gpu_init and
+    rrtmg_run_params_default)."""
+    guide = (ROOT / "INTEGRATION.md").read_text()
+    found = {}
+    for m in re.finditer(r"function\s+(rrtmg_\w+)\s*\((.*?)\)\s*(?:&\s*)?bind\(C,\s*name=\"(\w+)\"\)", guide, re.S):
+        args = [a.strip() for a in m.group(2).replace("&", " ").split(",")]
+        assert m.group(1) == m.group(3)
+        found[m.group(1)] = args
+    assert {"rrtmg_gpu_init", "rrtmg_lw_c", "rrtmg_sw_c", "rrtmg_run_c", "rrtmg_run_params_default"} <= set(found)
+    for fn, args in found.items():
+        params = _header_params(fn)
+        assert len(args) == len(params), fn
+        if fn not in ("rrtmg_gpu_init", "rrtmg_run_params_default"):
+            assert args == params, (fn, [(a, b) for a, b in zip(args, params) if a != b])

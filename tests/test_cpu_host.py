@@ -352,3 +352,30 @@ def test_fortran_interfaces_follow_the_header():
         assert len(args) == len(params), fn
         if fn not in ("rrtmg_gpu_init", "rrtmg_run_params_default"):
             assert args == params, (fn, [(a, b) for a, b in zip(args, params) if a != b])
+
+
+def test_fortran_dropin_calls_pass_each_argument_in_place():
+    """The drop-in rrtmg_lw / rrtmg_sw of the integration guide pass every
+    argument to rrtmg_lw_c / rrtmg_sw_c in its header position: each actual
+    argument, stripped of its kind conversion, names the dummy it lands on
+    (the handle and the optional-derivative pointers by their roles)."""
+    guide = (ROOT / "INTEGRATION.md").read_text()
+    roles = {"rrtmg_gpu": "h", "pd": "duflx_dt", "pdc": "duflxc_dt"}
+    for fn in ("rrtmg_lw_c", "rrtmg_sw_c"):
+        m = re.search(r"call rrtmg_gpu_check\(" + fn + r"\((.*?)\), \"rrtmg_", guide, re.S)
+        assert m, fn
+        text = m.group(1).replace("&", " ")
+        args, depth, cur = [], 0, ""
+        for ch in text:
+            depth += (ch == "(") - (ch == ")")
+            if ch == "," and depth == 0:
+                args.append(cur.strip())
+                cur = ""
+            else:
+                cur += ch
+        args.append(cur.strip())
+        names = []
+        for a in args:
+            k = re.match(r"(?:int|real)\((\w+),\s*c_\w+\)$", a)
+            names.append(roles.get(a, k.group(1) if k else a))
+        assert names == _header_params(fn), (fn, [(x, y) for x, y in zip(names, _header_params(fn)) if x != y])

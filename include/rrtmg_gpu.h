@@ -71,15 +71,21 @@ enum { RRTMG_TRANS_TABLE = 0, RRTMG_TRANS_ANALYTIC = 1 };
  * table_blob, performs the 256->140 / 224->112 g-point reduction, builds the
  * transmittance tables and uploads everything to `device`. */
 int rrtmg_gpu_init(double cpdair, const char* table_blob, int device, rrtmg_gpu_handle* out);
+/* No counterpart in the reference (whose tables live until the program ends):
+ * waits for the handle's streams and frees its device state. */
 int rrtmg_gpu_finalize(rrtmg_gpu_handle h);
 
-/* Selects RRTMG_PREC_FP64 (default) or RRTMG_PREC_SPLIT for later calls. */
+/* No counterpart in the reference (FP64 throughout, -r8).  Selects
+ * RRTMG_PREC_FP64 (default) or RRTMG_PREC_SPLIT for later calls. */
 int rrtmg_gpu_set_precision(rrtmg_gpu_handle h, int precision);
 
+/* No counterpart in the reference, which returns no status (errors stop the
+ * program): the meaning of a status code. */
 const char* rrtmg_gpu_error_string(int status);
 /* Detail of the last failure on this handle ("" if none). */
 const char* rrtmg_gpu_last_error(rrtmg_gpu_handle h);
-/* Number of kernel launches issued by this handle since init. */
+/* No counterpart in the reference.  Number of kernel launches issued by this
+ * handle since init. */
 long long rrtmg_gpu_launch_count(rrtmg_gpu_handle h);
 
 /* rrtmg_lw (rrtmg_lw_rad.nomcica.f90:80-89), host arrays.  tauaer (ncol,nlay,16)
@@ -181,11 +187,13 @@ int rrtmg_gpu_profile(rrtmg_gpu_handle h, float* ms);
  * RRTMG_TRANS_TABLE or RRTMG_TRANS_ANALYTIC for later calls on the handle. */
 int rrtmg_gpu_set_transcendentals(rrtmg_gpu_handle h, int mode);
 
-/* Reserves device workspace for calls of up to ncol columns and nlay layers,
- * so that later device calls allocate nothing (e.g. before graph capture). */
+/* No counterpart in the reference.  Reserves device workspace for LW, SW and
+ * fused calls of up to ncol columns and nlay layers, so that later such device
+ * calls allocate nothing (e.g. before graph capture). */
 int rrtmg_gpu_reserve(rrtmg_gpu_handle h, int ncol, int nlay);
 
-/* Waits for `stream` and reports RRTMG_ERR_INPUT if an enqueued call flagged
+/* No counterpart in the reference (which does not validate its inputs).
+ * Waits for `stream` and reports RRTMG_ERR_INPUT if an enqueued call flagged
  * invalid input (the flag is then cleared). */
 int rrtmg_gpu_sync_status(rrtmg_gpu_handle h, void* stream);
 

@@ -379,3 +379,19 @@ def test_fortran_dropin_calls_pass_each_argument_in_place():
             k = re.match(r"(?:int|real)\((\w+),\s*c_\w+\)$", a)
             names.append(roles.get(a, k.group(1) if k else a))
         assert names == _header_params(fn), (fn, [(x, y) for x, y in zip(names, _header_params(fn)) if x != y])
+
+
+def test_profile_summaries_state_their_commands():
+    """Every committed ncu summary gives the command that made it (a command
+    that runs committed files only), and every ncu command in it leaves the
+    GPU clocks alone."""
+    summaries = sorted((ROOT / "profiles").glob("*.md"))
+    assert summaries
+    for p in summaries:
+        text = p.read_text()
+        ncu = [ln for ln in text.splitlines() if ln.lstrip().startswith("ncu ")]
+        captures = [ln for ln in ncu if not ln.lstrip().startswith("ncu -i ")]  # -i reads a saved report
+        assert captures, p.name
+        assert all("--clock-control none" in ln for ln in captures), p.name
+        assert "python" in text and "..." not in "\n".join(ln for ln in text.splitlines() if "python " in ln), p.name
+        assert "_work" not in text, p.name

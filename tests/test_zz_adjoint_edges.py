@@ -4,7 +4,7 @@ against central differences of the analytic FP64 forward with the tolerances
 of tests/test_gpu_adjoint.py; the VJP against cot^T J; the split VJP against
 the FP64 VJP within bounds that catch a broken variant (the split adjoint's
 FP32 error grows with depth; 40-layer columns meet 1e-4 at the 99th
-percentile).  Collected after the other GPU test files."""
+percentile).  Collected after the adjoint, driver and parity test files."""
 import numpy as np
 import pytest
 

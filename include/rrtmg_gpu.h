@@ -257,7 +257,10 @@ int rrtmg_vjp_dev(rrtmg_gpu_handle h, void* stream, int ncol, int nlay,
  * that device current; make that first call before any stream capture.  All
  * calls on a device share the one array and it keeps the last call's
  * contents, so calls that overlap on the GPU (different streams, or different
- * handles on one device) race: order them on one stream or with events. */
+ * handles on one device) race: order them on one stream or with events.
+ * The array's device address is kept for the life of the process, so do not
+ * reset the device (cudaDeviceReset) while the library is loaded: a later
+ * call would write through the old context's address. */
 int rrtmg_lw_dev_static(rrtmg_gpu_handle h, void* stream, int ncol, int nlay, int icld, int idrv,
                         const double* play, const double* plev, const double* tlay, const double* tlev,
                         const double* tsfc, const double* h2ovmr, const double* o3vmr, const double* co2vmr,

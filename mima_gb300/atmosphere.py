@@ -96,7 +96,13 @@ def gaussian_latitudes(nlat: int) -> np.ndarray:
 
 
 def annual_mean_coszen(lat: np.ndarray, obliquity_deg: float = 23.439) -> np.ndarray:
-    """Annual mean of the daily-mean cos(zenith) of astro.f90's daily formula."""
+    """Annual mean of the daily-mean cos(zenith) of astro.f90's daily formula
+    (evaluated once per distinct latitude: the grids repeat each latitude for
+    every longitude)."""
+    lat = np.asarray(lat, dtype=np.float64)
+    uniq, inv = np.unique(lat, return_inverse=True)
+    if uniq.size < lat.size:
+        return annual_mean_coszen(uniq, obliquity_deg)[inv.reshape(lat.shape)]
     eps = np.deg2rad(obliquity_deg)
     days = np.arange(365)
     dec = np.arcsin(np.sin(eps) * np.sin(2.0 * np.pi * days / 365.0))

@@ -25,6 +25,7 @@ Usage: python tests/golden/make_rrtm_std_atm.py [MiMA source tree]
 from __future__ import annotations
 
 import json
+import os
 import re
 import sys
 from pathlib import Path
@@ -145,4 +146,7 @@ def main(root: Path) -> None:
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference"))
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MIMA_ROOT")
+    if not root:
+        sys.exit("usage: make_rrtm_std_atm.py MIMA_ROOT  (a MiMA checkout; or set MIMA_ROOT)")
+    main(Path(root))

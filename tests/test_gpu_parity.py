@@ -412,52 +412,88 @@ def test_edge_columns(gpu, orc):
             assert np.abs(sw[k] - rsw[k]).max() <= 0.1, (name, k)
 
 
+def _random_case(rng):
+    """One seeded random case of test_random_columns (the draw order is part of
+    the case definition)."""
+    nlay = int(rng.choice([2, 5, 17, 40, 64, 65, 90]))
+    ncol = int(rng.integers(1, 200))
+    atm = A.small_atmosphere(ncol, nlay, seed=int(rng.integers(1 << 30)), ts_sigma=float(rng.uniform(0.0, 15.0)),
+                             rh_random=bool(rng.integers(2)))
+    shp = atm.play.shape
+    atm.co2 = rng.uniform(100e-6, 2000e-6, size=shp)
+    atm.o3 = atm.o3 * rng.uniform(0.0, 3.0)
+    atm.h2o = np.clip(atm.h2o * rng.uniform(0.05, 1.5), 1e-7, 0.05)
+    if rng.integers(2):
+        atm.ch4, atm.n2o, atm.o2 = np.full(shp, 1.8e-6), np.full(shp, 3.2e-7), np.full(shp, 0.209)
+        atm.cfc11, atm.cfc12 = np.full(shp, 2.5e-10), np.full(shp, 5.0e-10)
+        atm.cfc22, atm.ccl4 = np.full(shp, 1.5e-10), np.full(shp, 1.0e-10)
+    atm.emis = rng.uniform(0.8, 1.0, size=(16, ncol))
+    atm.coszen = rng.uniform(0.0, 1.0, ncol) * (rng.uniform(size=ncol) > 0.3)
+    for k in ("asdir", "asdif", "aldir", "aldif"):
+        setattr(atm, k, rng.uniform(0.0, 0.9, ncol))
+    idrv = int(rng.integers(2))
+    lw_aer = rng.uniform(0.0, 0.05, size=(16, nlay, ncol)) if rng.integers(2) else None
+    if rng.integers(2):
+        aer = dict(iaer=10, tauaer=rng.uniform(0.0, 0.1, size=(14, nlay, ncol)),
+                   ssaaer=rng.uniform(0.8, 1.0, size=(14, nlay, ncol)),
+                   asmaer=rng.uniform(0.0, 0.8, size=(14, nlay, ncol)))
+    else:
+        aer = {}
+    return atm, idrv, lw_aer, aer
+
+
 def test_random_columns(gpu, orc):
     """Seeded random cases across the inputs: layer counts on both sides of the
     solvers' 64 / 208-level switch, ragged column counts, surface-temperature
     spread, gas amounts (CO2 100-2000 ppmv, O3 and H2O scaled, the secondary
-    gases on or off), spectral emissivity, albedos, dark and sunlit columns,
-    idrv, LW and SW aerosols -- the FP64 path against the oracle at the FP64
-    tolerances, the split path within 0.1 W/m2 of it at every level."""
+    gases on or off), spectral emissivity, albedos up to 0.9, dark and sunlit
+    columns, idrv, LW and SW aerosols.
+
+    FP64 path: against the oracle at the FP64 tolerances.  Split path: the bars
+    of tests/split_bars.py (0.1 W/m2 at every level; 0.05 K/day heating up to
+    60 layers, where the bar is stated), in both transcendental modes.  With the
+    analytic exponentials every column must meet them.  With the reference's
+    tables a column may miss them only where the reference itself is
+    ill-conditioned (the delta-Eddington resonance k mu0 = 1 amplifying one
+    table step): then the oracle on inputs within FP32 rounding of the given
+    ones must reproduce the split result within the bars.  Case 3 holds such a
+    column (band 25, k mu0 = 0.9993: a 1e-6 relative change of the aerosol
+    depth moves the oracle's surface flux by 2.15 W/m2)."""
+    import split_bars as SB
     rng = np.random.default_rng(2024)
     gpu.set_precision("fp64")
+    excused = {}
     for case in range(12):
-        nlay = int(rng.choice([2, 5, 17, 40, 64, 65, 90]))
-        ncol = int(rng.integers(1, 200))
-        atm = A.small_atmosphere(ncol, nlay, seed=int(rng.integers(1 << 30)), ts_sigma=float(rng.uniform(0.0, 15.0)),
-                                 rh_random=bool(rng.integers(2)))
-        shp = atm.play.shape
-        atm.co2 = rng.uniform(100e-6, 2000e-6, size=shp)
-        atm.o3 = atm.o3 * rng.uniform(0.0, 3.0)
-        atm.h2o = np.clip(atm.h2o * rng.uniform(0.05, 1.5), 1e-7, 0.05)
-        if rng.integers(2):
-            atm.ch4, atm.n2o, atm.o2 = np.full(shp, 1.8e-6), np.full(shp, 3.2e-7), np.full(shp, 0.209)
-            atm.cfc11, atm.cfc12 = np.full(shp, 2.5e-10), np.full(shp, 5.0e-10)
-            atm.cfc22, atm.ccl4 = np.full(shp, 1.5e-10), np.full(shp, 1.0e-10)
-        atm.emis = rng.uniform(0.8, 1.0, size=(16, ncol))
-        atm.coszen = rng.uniform(0.0, 1.0, ncol) * (rng.uniform(size=ncol) > 0.3)
-        for k in ("asdir", "asdif", "aldir", "aldif"):
-            setattr(atm, k, rng.uniform(0.0, 0.9, ncol))
-        idrv = int(rng.integers(2))
-        lw_aer = rng.uniform(0.0, 0.05, size=(16, nlay, ncol)) if rng.integers(2) else None
-        check_lw(gpu.lw(atm, idrv=idrv, tauaer=lw_aer), orc.rrtmg_lw(atm, idrv=idrv, tauaer=lw_aer), idrv=idrv)
-        if rng.integers(2):
-            aer = dict(iaer=10, tauaer=rng.uniform(0.0, 0.1, size=(14, nlay, ncol)),
-                       ssaaer=rng.uniform(0.8, 1.0, size=(14, nlay, ncol)),
-                       asmaer=rng.uniform(0.0, 0.8, size=(14, nlay, ncol)))
-        else:
-            aer = {}
+        atm, idrv, lw_aer, aer = _random_case(rng)
+        heating = atm.nlay <= 60
         rlw, rsw = orc.rrtmg_lw(atm, idrv=idrv, tauaer=lw_aer), orc.rrtmg_sw(atm, **aer)
+        check_lw(gpu.lw(atm, idrv=idrv, tauaer=lw_aer), rlw, idrv=idrv)
         check_sw(gpu.sw(atm, **aer), rsw)
         gpu.set_precision("split")
         try:
             slw, ssw = gpu.lw(atm, idrv=idrv, tauaer=lw_aer), gpu.sw(atm, **aer)
+            gpu.set_transcendentals("analytic")
+            alw, asw = gpu.lw(atm, idrv=idrv, tauaer=lw_aer), gpu.sw(atm, **aer)
         finally:
+            gpu.set_transcendentals("table")
             gpu.set_precision("fp64")
-        for k in ("uflx", "dflx"):
-            assert np.abs(slw[k] - rlw[k]).max() <= 0.1, (case, k)
+        excused[case] = (SB.check_lw(orc, atm, slw, rlw, idrv=idrv, tauaer=lw_aer, heating=heating)
+                         + SB.check_sw(orc, atm, ssw, rsw, aer=aer, heating=heating))
+        orc.set_table_mode(False)
+        try:
+            blw, bsw = orc.rrtmg_lw(atm, idrv=idrv, tauaer=lw_aer), orc.rrtmg_sw(atm, **aer)
+        finally:
+            orc.set_table_mode(True)
         for k in ("swuflx", "swdflx"):
-            assert np.abs(ssw[k] - rsw[k]).max() <= 0.1, (case, k)
+            assert np.abs(asw[k] - bsw[k]).max() <= SB.FLUX_BAR, (case, "analytic", k)
+        for k in ("uflx", "dflx"):
+            assert np.abs(alw[k] - blw[k]).max() <= SB.FLUX_BAR, (case, "analytic", k)
+        if heating:
+            assert np.abs(asw["swhr"] - bsw["swhr"]).max() <= SB.HR_BAR, (case, "analytic")
+            assert np.abs(alw["hr"] - blw["hr"]).max() <= SB.HR_BAR, (case, "analytic")
+    # the resonance column of case 3 needed the allowance; few others may
+    assert 20 in [c for c, _, _ in excused[3]], excused
+    assert sum(len(v) for v in excused.values()) <= 4, excused
 
 
 def test_grazing_sun(gpu, orc):

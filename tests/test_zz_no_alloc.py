@@ -58,6 +58,39 @@ def test_static_scratch_entry_point_matches_dev_entry_point(gpu):
 
 
 @pytest.mark.gpu
+def test_static_scratch_entry_point_split_precision(gpu):
+    """The FP32-split path reads the same static array as FP32 fields.  After a
+    larger FP64 call has left its data in the array, split calls through
+    rrtmg_lw_dev_static give rrtmg_lw_dev's split results bit for bit (two
+    calls in a row, different sizes, idrv 1 then 0)."""
+    import torch
+    s = torch.cuda.Stream()
+    big = A.small_atmosphere(1500, 40, seed=44)
+    d = R.atm_device_inputs(big)
+    out, _ = R.device_outputs(big.ncol, big.nlay, idrv=1)
+    gpu.set_precision("fp64")
+    with torch.cuda.stream(s):
+        gpu.rrtmg_lw_dev_static(s.cuda_stream, big.ncol, big.nlay, 0, 1, d, out)
+    s.synchronize()
+    gpu.set_precision("split")
+    try:
+        for atm, idrv in ((A.small_atmosphere(700, 40, seed=45), 1), (A.small_atmosphere(333, 60, seed=46), 0)):
+            d = R.atm_device_inputs(atm)
+            ref, _ = R.device_outputs(atm.ncol, atm.nlay, idrv=idrv)
+            got, _ = R.device_outputs(atm.ncol, atm.nlay, idrv=idrv)
+            for t in got.values():
+                t.fill_(float("nan"))
+            with torch.cuda.stream(s):
+                gpu.rrtmg_lw_dev(s.cuda_stream, atm.ncol, atm.nlay, 0, idrv, d, ref)
+                gpu.rrtmg_lw_dev_static(s.cuda_stream, atm.ncol, atm.nlay, 0, idrv, d, got)
+            assert gpu.sync_status(s.cuda_stream) == R.RRTMG_OK
+            for k in ref:
+                assert torch.equal(got[k], ref[k]), k
+    finally:
+        gpu.set_precision("fp64")
+
+
+@pytest.mark.gpu
 def test_static_scratch_entry_point_rejects_sizes_beyond_the_limit(gpu):
     import torch
     nlay = 40

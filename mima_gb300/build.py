@@ -3,7 +3,11 @@
 Every translation unit is compiled by nvcc in parallel with one
 ``-gencode arch=compute_103a,code=sm_103a``; the FP64 kernels are compiled with
 ``--fmad=false`` (separately rounded multiplies and adds, for bit-level
-reproducibility of the FP64 path), the FP32-split kernels with contraction.
+reproducibility of the FP64 path), the FP32-split kernels with contraction and
+with the hardware-approximate FP32 division and square root (within 2 ulp;
+the SW solver does about nine FP32 divisions per layer and g-point, and the
+IEEE-rounded sequences cost it 19 % of its time at T85 x 40 with no change in
+its error against the oracle).
 The library has a plain C ABI (include/rrtmg_gpu.h) and links the CUDA
 runtime statically, so it needs no torch at load time.
 """
@@ -20,6 +24,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 LIBDIR = PKG / "lib"
 LIB = LIBDIR / "librrtmg_gpu.so"
+PEAK_LIB = LIBDIR / "libfp32peak.so"   # FP32 FMA-rate microkernel for the benchmark's roofline
 OBJDIR = LIBDIR / "obj"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -28,7 +33,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 
 UNITS = {
     "kernels_fp64.cu": ["--fmad=false"],
-    "kernels_split.cu": [],
+    "kernels_split.cu": ["--prec-div=false", "--prec-sqrt=false"],
     "adjoint.cu": [],
     "driver.cu": ["--fmad=false"],
     "tables_host.cu": [],
@@ -56,6 +61,11 @@ def build(force: bool = False, verbose: bool = False, extra=None) -> Path:
     cc = nvcc()
     procs = []
     objs = []
+    peak_src = CSRC / "fp32_peak.cu"
+    if force or not PEAK_LIB.exists() or peak_src.stat().st_mtime > PEAK_LIB.stat().st_mtime:
+        cmd = [cc, *ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", str(peak_src), "-o", str(PEAK_LIB)]
+        procs.append(("fp32_peak.cu", subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT,
+                                                      text=True)))
     for unit, flags in UNITS.items():
         src = CSRC / unit
         obj = OBJDIR / (unit + ".o")
@@ -74,7 +84,7 @@ def build(force: bool = False, verbose: bool = False, extra=None) -> Path:
             print(out)
     if errors:
         raise RuntimeError("nvcc failed:\n" + "\n".join(errors))
-    if force or procs or not LIB.exists():
+    if force or any(u != "fp32_peak.cu" for u, _ in procs) or not LIB.exists():
         tmp = LIB.with_suffix(".so.tmp")
         cmd = [cc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs)]
         r = subprocess.run(cmd, capture_output=True, text=True)

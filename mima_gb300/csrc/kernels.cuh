@@ -397,7 +397,8 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
                                         const double* __restrict__ tauaer, const R* __restrict__ tab,
                                         const R* __restrict__ exptbl, const R* __restrict__ tfntbl,
                                         double* __restrict__ bu, double* __restrict__ bd, double* __restrict__ bdu,
-                                        int ncol, int nlay, int idrv, bool analytic, int blk, float* sbuf) {
+                                        int ncol, int nlay, int idrv, bool analytic, int blk, float* sbuf,
+                                        float* lvl = nullptr) {
   const bool IDRV = idrv == 1;
   constexpr bool SPLIT = sizeof(R) == 4;
   constexpr int NG = lw_ng(B);
@@ -417,7 +418,20 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
   const R bpade = (R)c_lw.bpade;
   const R rec_6 = (R)0.166667;
   const size_t fstride = (size_t)nlay * N;
-  R atrans[MAXL], bbugas[MAXL];
+#ifdef RRTMG_LW_SMEM
+  constexpr bool SMEM = SPLIT;
+#else
+  constexpr bool SMEM = false;
+#endif
+  R atrans_l[SMEM ? 1 : MAXL], bbugas_l[SMEM ? 1 : MAXL];
+  auto atrans = [&](int l) -> R& {
+    if constexpr (SMEM) return *reinterpret_cast<R*>(lvl + (size_t)l * kBlock + threadIdx.x);
+    else return atrans_l[l];
+  };
+  auto bbugas = [&](int l) -> R& {
+    if constexpr (SMEM) return *reinterpret_cast<R*>(lvl + (size_t)(nlay + l) * kBlock + threadIdx.x);
+    else return bbugas_l[l];
+  };
   R radld = (R)0., fracs1 = (R)0.;
   double* bdp = bd + (size_t)(B - 1) * (nlay + 1) * N + col;
   double* bup = bu + (size_t)(B - 1) * (nlay + 1) * N + col;
@@ -482,8 +496,8 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
       bbd = plfrac * (blay + tausfac * dplankdn);
       bbu = plfrac * (blay + tausfac * dplankup);
     }
-    atrans[lev - 1] = atr;
-    bbugas[lev - 1] = bbu;
+    atrans(lev - 1) = atr;
+    bbugas(lev - 1) = bbu;
     radld = radld + (bbd - radld) * atr;
     if constexpr (SPLIT) {
       gs.put(0, radld);
@@ -519,8 +533,9 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
     }
   }
   for (int lev = 1; lev <= nlay; ++lev) {
-    radlu = radlu + (bbugas[lev - 1] - radlu) * atrans[lev - 1];
-    if (IDRV) dlu = dlu * ((R)1.0 - atrans[lev - 1]);
+    const R at = atrans(lev - 1);
+    radlu = radlu + (bbugas(lev - 1) - radlu) * at;
+    if (IDRV) dlu = dlu * ((R)1.0 - at);
     if constexpr (SPLIT) {
       gs.put(0, radlu);
       gs.put(1, dlu);
@@ -570,6 +585,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_LW_MINB :
                                                            double* bdu, int ncol, int nlay, int idrv,
                                                            int analytic) {
   __shared__ float sbuf[sizeof(R) == 4 ? kGSumFloats : 1];
+  extern __shared__ float lw_lvl[];
   int blk = blockIdx.x, band = 0;
   for (; band < kLwBands; ++band) {
     const int nb = lw_blocks_for_band(split_lanes(c_lw.band[band].ng, sizeof(R) == 4), ncol);
@@ -579,7 +595,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_LW_MINB :
   const bool an = FL < 0 ? analytic != 0 : (FL & 1) != 0;
   const int idv = FL < 0 ? idrv : ((FL & 2) ? 1 : 0);
 #define RRTMG_LW_CASE(b) \
-  case b - 1: lw_band<b, R, MAXL>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idv, an, blk, sbuf); break;
+  case b - 1: lw_band<b, R, MAXL>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idv, an, blk, sbuf, lw_lvl); break;
   switch (band) {
     RRTMG_LW_CASE(1) RRTMG_LW_CASE(2) RRTMG_LW_CASE(3) RRTMG_LW_CASE(4) RRTMG_LW_CASE(5) RRTMG_LW_CASE(6)
     RRTMG_LW_CASE(7) RRTMG_LW_CASE(8) RRTMG_LW_CASE(9) RRTMG_LW_CASE(10) RRTMG_LW_CASE(11) RRTMG_LW_CASE(12)
@@ -934,11 +950,14 @@ __device__ __forceinline__ void sw_exp_pair(R ze1, R bpade, const float* __restr
 //   * zr4 e^{kt} + zr5 e^{-kt} = zrpp (k (e^{kt} + e^{-kt}) + g1 (e^{kt} - e^{-kt})).
 // Exponentials are the same table / series values as the reference uses.
 // zg_zero: the asymmetry factor is identically 0 (no aerosol), so r = 0 and
-// zwo = zw without the two divisions.
+// zwo = zw without the two divisions.  pdbt (optional): e^{-t/mu}, the value
+// the direct-beam lookup of spcvrt_sw (rrtmg_sw_spcvrt.f90:496-507) takes for
+// the same argument (its missing 500 cap changes nothing in FP32, where both
+// table ends are 0).
 template <class R>
 __device__ __forceinline__ void reftra_split(R zto1, R zw, R zg, R prmuz, R bpade, const float* __restrict__ exptbl,
                                              bool analytic, R& pref, R& prefd, R& ptra, R& ptrad,
-                                             bool zg_zero = false) {
+                                             bool zg_zero = false, R* pdbt = nullptr) {
   const R eps = (R)1.e-08, zwcrit = (R)0.9999995;
   const R zg3 = (R)3. * zg;
   const R zgamma1 = ((R)8. - zw * ((R)5. + zg3)) * (R)0.25;
@@ -955,6 +974,7 @@ __device__ __forceinline__ void reftra_split(R zto1, R zw, R zg, R prmuz, R bpad
     const R zgt = zgamma1 * zto1;
     R ze2, m2;
     sw_exp_pair(fmin(zto1 / prmuz, (R)500.), bpade, exptbl, analytic, ze2, m2);
+    if (pdbt) *pdbt = ze2;
     pref = (zgt + za1 * m2) / ((R)1. + zgt);
     ptra = (R)1. - pref;
     prefd = zgt / ((R)1. + zgt);
@@ -980,6 +1000,7 @@ __device__ __forceinline__ void reftra_split(R zto1, R zw, R zg, R prmuz, R bpad
     R zem1, m1, zem2, m2;
     sw_exp_pair(fmin(zrk * zto1, (R)500.), bpade, exptbl, analytic, zem1, m1);
     sw_exp_pair(fmin(zto1 / prmuz, (R)500.), bpade, exptbl, analytic, zem2, m2);
+    if (pdbt) *pdbt = zem2;
     // Numerators and denominator multiplied by E = e^{-kt} (= zem1), so that
     // only e^{-kt}, e^{-t/mu} and their complements appear: e^{+kt} would
     // overflow FP32 in thick layers (and its derivative already beyond kt = 44).
@@ -1073,16 +1094,17 @@ __device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, dou
     ztauc = ((R)1.0 - zwf) * ztauc;
     zomcc = (zomcc - zwf) / ((R)1.0 - zwf);
     zgcc = (zgcc - zf) / ((R)1.0 - zf);
-    R rf, rfd, tr, trd;
-    if constexpr (sizeof(R) == 4)
-      reftra_split(ztauc, zomcc, zgcc, prmu0, bpade, exptbl, analytic, rf, rfd, tr, trd, iaer != 10);
-    else
+    R rf, rfd, tr, trd, zdbtmc;
+    if constexpr (sizeof(R) == 4) {
+      reftra_split(ztauc, zomcc, zgcc, prmu0, bpade, exptbl, analytic, rf, rfd, tr, trd, iaer != 10, &zdbtmc);
+    } else {
       reftra1<R, R>(ztauc, zomcc, zgcc, prmu0, bpade, exptbl, analytic, rf, rfd, tr, trd);
+      zdbtmc = sw_exp_tbl<R, R>(ztauc / prmu0, bpade, exptbl, analytic);
+    }
     pref[jk - 1] = rf;
     prefd[jk - 1] = rfd;
     ptra[jk - 1] = tr;
     ptrad[jk - 1] = trd;
-    const R zdbtmc = sw_exp_tbl<R, R>(ztauc / prmu0, bpade, exptbl, analytic);
     pdbt[jk - 1] = zdbtmc;
     ptdbt[jk] = zdbtmc * ptdbt[jk - 1];
     // Downward adding sweep of vrtqdr_sw (:127-139), fused with the layer loop.

@@ -35,6 +35,18 @@ def _oracle(orc, atm, mode="table", idrv=0, lw_aer=None, aer=None):
         orc.set_table_mode(True)
 
 
+def aerosol_profile(atm, rng, nbands, tau_col_max):
+    """Aerosol optical depths (band, layer, column): a column total drawn per
+    band and column in [0, tau_col_max), spread over the layers in proportion
+    to their mass times (p / ps)^3.75 -- an aerosol scale height of about 2 km
+    under an atmospheric one of 7.5 km, so the depth sits in the lower
+    troposphere as real aerosol does."""
+    dp = atm.plev[:-1] - atm.plev[1:]
+    w = dp * (atm.play / atm.plev[0]) ** 3.75
+    w = w / w.sum(axis=0)
+    return rng.uniform(0.0, tau_col_max, size=(nbands, 1, atm.ncol)) * w[None]
+
+
 def _assert_stats(st, label):
     print(label, {k: (f"{m:.3g}", f"{r:.3g}") for k, (m, r) in st.items()})
     assert st["lw_hr"][0] <= SB.HR_BAR and st["sw_hr"][0] <= SB.HR_BAR, (label, st)
@@ -45,12 +57,14 @@ def _assert_stats(st, label):
 @pytest.mark.parametrize("nlay", [40, 60])
 @pytest.mark.parametrize("mode", ["table", "analytic"])
 def test_split_input_matrix(gpu, orc, nlay, mode):
-    """SW aerosols (iaer = 10: depth up to 0.1 per layer, single-scattering
-    albedo 0.8-1, asymmetry 0-0.8), every secondary gas, albedos up to 0.9,
-    CO2 100-2000 ppmv, suns from grazing (coszen 1e-4) to overhead, LW
-    aerosols and idrv = 1: split against the oracle, every column within the
-    bars (table mode: or reproduced by the oracle within FP32 rounding of its
-    inputs)."""
+    """SW aerosols (iaer = 10: column depth up to 1 per band in the lower
+    troposphere, single-scattering albedo 0.8-1, asymmetry 0-0.8), every
+    secondary gas, albedos up to 0.9, CO2 100-2000 ppmv, suns from grazing
+    (coszen 1e-4) to overhead, LW aerosols (column depth up to 0.3) and
+    idrv = 1: split against the oracle, every column within the bars (table
+    mode: or reproduced by the oracle within FP32 rounding of its inputs; in
+    the layers thinner than 0.01 hPa of the 60-layer columns, the heating bar
+    in its net-flux-divergence form)."""
     rng = np.random.default_rng(700 + nlay)
     n = 768
     atm = A.small_atmosphere(n, nlay, seed=710 + nlay, ts_sigma=5.0, rh_random=True)
@@ -63,8 +77,8 @@ def test_split_input_matrix(gpu, orc, nlay, mode):
     for k in ("asdir", "asdif", "aldir", "aldif"):
         setattr(atm, k, rng.uniform(0.0, 0.9, n))
     atm.coszen = np.concatenate([10.0 ** rng.uniform(-4, -1, n // 4), rng.uniform(0.1, 1.0, n - n // 4)])
-    lw_aer = rng.uniform(0.0, 0.05, size=(16, nlay, n))
-    aer = dict(iaer=10, tauaer=rng.uniform(0.0, 0.1, size=(14, nlay, n)),
+    lw_aer = aerosol_profile(atm, rng, 16, 0.3)
+    aer = dict(iaer=10, tauaer=aerosol_profile(atm, rng, 14, 1.0),
                ssaaer=rng.uniform(0.8, 1.0, size=(14, nlay, n)), asmaer=rng.uniform(0.0, 0.8, size=(14, nlay, n)))
     rlw, rsw = _oracle(orc, atm, mode, 1, lw_aer, aer)
     lw, sw = _split(gpu, atm, mode, 1, lw_aer, aer)
@@ -76,9 +90,13 @@ def test_split_input_matrix(gpu, orc, nlay, mode):
             assert np.abs(lw[k] - rlw[k]).max() <= SB.FLUX_BAR, k
         for k in ("swuflx", "swdflx"):
             assert np.abs(sw[k] - rsw[k]).max() <= SB.FLUX_BAR, k
-        assert np.abs(lw["hr"] - rlw["hr"]).max() <= SB.HR_BAR
-        assert np.abs(sw["swhr"] - rsw["swhr"]).max() <= SB.HR_BAR
-        _assert_stats(SB.error_stats(lw, rlw, sw, rsw), f"matrix L={nlay} analytic")
+        bar = SB.hr_bar(atm)
+        assert np.all(np.abs(lw["hr"] - rlw["hr"]) <= bar)
+        assert np.all(np.abs(sw["swhr"] - rsw["swhr"]) <= bar)
+        st = SB.error_stats(lw, rlw, sw, rsw)
+        print(f"matrix L={nlay} analytic", st)
+        for k in ("olr", "lw_sfc_net", "sw_sfc_net"):
+            assert st[k][0] <= SB.FLUX_BAR, (k, st)
     assert np.abs(lw["duflx_dt"] - rlw["duflx_dt"]).max() <= 1e-3
 
 

@@ -52,12 +52,15 @@ struct rrtmg_gpu_state {
   // that column chunks alternate between the streams
   cudaStream_t stream2 = nullptr;
   DevBuf hio[2], hws[2];
-  // run_rrtmg calls: RRTM columns, results and zonal scratch; host-array staging
-  DevBuf run_ws, run_io;
+  // run_rrtmg calls: RRTM columns, results, zonal scratch and the LW and SW
+  // scratch (device entry point); host-array calls: per latitude-chunk stream
+  // staging and workspace
+  DevBuf run_ws, run_cio[2], run_cws[2];
   // fused LW+SW calls: the SW call runs on `side`, forked from and joined back
-  // into the caller's stream with these events
-  cudaStream_t side = nullptr;
-  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  // into the caller's stream with these events; host-array run_rrtmg chunks on
+  // stream2 fork onto side2
+  cudaStream_t side = nullptr, side2 = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr, fork_ev2 = nullptr, join_ev2 = nullptr;
   long long launches = 0;
   std::string err;
   // Optional per-kernel timing: events around every launch of the last LW
@@ -306,15 +309,21 @@ int sw_run(rrtmg_gpu_state* h, cudaStream_t s, int ncol, int nlay, int iaer, dou
 // forked from st and joined back into it by events (a pattern that stream
 // capture records as two parallel graph branches).  The join is enqueued even
 // when a launch failed, so that a capture stays well formed.
+struct Fork {
+  cudaStream_t side;
+  cudaEvent_t fork, join;
+};
+Fork default_fork(rrtmg_gpu_state* h) { return Fork{h->side, h->fork_ev, h->join_ev}; }
+
 template <class LwF, class SwF>
-int fork_lw_sw(rrtmg_gpu_state* h, cudaStream_t st, LwF&& lw, SwF&& sw) {
-  cudaError_t e = cudaEventRecord(h->fork_ev, st);
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(h->side, h->fork_ev, 0);
+int fork_lw_sw(rrtmg_gpu_state* h, cudaStream_t st, const Fork& fk, LwF&& lw, SwF&& sw) {
+  cudaError_t e = cudaEventRecord(fk.fork, st);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(fk.side, fk.fork, 0);
   if (e != cudaSuccess) return cuda_fail(h, e, "fork onto the side stream");
-  const int rs = sw(h->side);
+  const int rs = sw(fk.side);
   const int rl = lw(st);
-  e = cudaEventRecord(h->join_ev, h->side);
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(st, h->join_ev, 0);
+  e = cudaEventRecord(fk.join, fk.side);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(st, fk.join, 0);
   if (rs) return rs;
   if (rl) return rl;
   if (e != cudaSuccess) return cuda_fail(h, e, "join the side stream");
@@ -551,8 +560,11 @@ int rrtmg_gpu_init(double cpdair, const char* table_blob, int device, rrtmg_gpu_
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->side2, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->join_ev, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->fork_ev2, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->join_ev2, cudaEventDisableTiming);
   if (e == cudaSuccess) e = upload(&h->lw_tab64, h->host.lw_tab);
   if (e == cudaSuccess) e = upload(&h->sw_tab64, h->host.sw_tab);
   if (e == cudaSuccess) e = upload(&h->lw_exp64, h->host.lw_exp);
@@ -589,18 +601,20 @@ int rrtmg_gpu_finalize(rrtmg_gpu_handle h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->stream2) cudaStreamSynchronize(h->stream2);
   if (h->side) cudaStreamSynchronize(h->side);
+  if (h->side2) cudaStreamSynchronize(h->side2);
   void* ptrs[] = {h->lw_tab64, h->sw_tab64, h->lw_exp64, h->lw_tfn64, h->sw_exp64, h->totplnk, h->totplnkderiv,
                   h->totplnk32, h->totplnkderiv32,
                   h->lw_tab32, h->sw_tab32, h->lw_exp32, h->lw_tfn32, h->sw_exp32, h->flags, h->lw_ws.p,
                   h->sw_ws.p, h->adj_ws.p, h->hio[0].p, h->hio[1].p, h->hws[0].p, h->hws[1].p, h->run_ws.p,
-                  h->run_io.p};
+                  h->run_cio[0].p, h->run_cio[1].p, h->run_cws[0].p, h->run_cws[1].p};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->stream) cudaStreamDestroy(h->stream);
   if (h->stream2) cudaStreamDestroy(h->stream2);
   if (h->side) cudaStreamDestroy(h->side);
-  if (h->fork_ev) cudaEventDestroy(h->fork_ev);
-  if (h->join_ev) cudaEventDestroy(h->join_ev);
+  if (h->side2) cudaStreamDestroy(h->side2);
+  for (cudaEvent_t ev : {h->fork_ev, h->join_ev, h->fork_ev2, h->join_ev2})
+    if (ev) cudaEventDestroy(ev);
   for (auto& fam : h->ev)
     for (auto& e : fam)
       if (e) cudaEventDestroy(e);
@@ -753,7 +767,7 @@ int rrtmg_step_dev(rrtmg_gpu_handle h, void* stream, int ncol, int nlay, int idr
   const SwIn sin{play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr, asdir, asdif, aldir,
                  aldif, coszen, tauaer_sw, ssaaer, asmaer};
   return fork_lw_sw(
-      h, (cudaStream_t)stream,
+      h, (cudaStream_t)stream, default_fork(h),
       [&](cudaStream_t s) {
         return lw_run(h, s, ncol, nlay, idrv, lin, uflx, dflx, hr, uflxc, dflxc, hrc, duflx_dt, duflxc_dt);
       },
@@ -1110,15 +1124,26 @@ RunScalars run_scalars(const rrtmg_run_params& p, const RunArgs& a, int* dyofyr)
   return s;
 }
 
-int run_enqueue(rrtmg_gpu_state* h, cudaStream_t st, const rrtmg_run_params& p, const RunArgs& a) {
+// Enqueues run_rrtmg on stream st.  Scratch (RRTM columns, results, zonal sums,
+// the LW and SW scratch) is carved from ws; the SW call is forked onto fk.side.
+// top: -1 to find on the device whether some top interface is at 0 Pa (the
+// whole slab is in the call), else the host's answer for the whole slab (the
+// call is a latitude chunk of it).
+int run_enqueue(rrtmg_gpu_state* h, cudaStream_t st, const rrtmg_run_params& p, const RunArgs& a, DevBuf& ws,
+                const Fork& fk, int top) {
   int dyofyr = 0;
   const RunScalars s = run_scalars(p, a, &dyofyr);
-  size_t need;
-  carve_run(nullptr, a.sj, a.sk, s.ncol, s.secondary, &need);
-  int rc = ensure(h, h->run_ws, need, st);
+  size_t nrun, nlw, nsw;
+  carve_run(nullptr, a.sj, a.sk, s.ncol, s.secondary, &nrun);
+  carve_lw(nullptr, s.ncol, a.sk, &nlw);
+  carve_sw(nullptr, s.ncol, a.sk, &nsw);
+  int rc = ensure(h, ws, nrun + nlw + nsw, st);
   if (rc) return rc;
-  const RunWork w = carve_run(h->run_ws.p, a.sj, a.sk, s.ncol, s.secondary, nullptr);
-  cudaError_t e = cudaMemsetAsync(w.flag, 0, sizeof(unsigned), st);
+  const RunWork w = carve_run(ws.p, a.sj, a.sk, s.ncol, s.secondary, nullptr);
+  void* lw_base = (char*)ws.p + nrun;
+  void* sw_base = (char*)lw_base + nlw;
+  // the flag is read as zero / nonzero
+  cudaError_t e = cudaMemsetAsync(w.flag, top > 0 ? 1 : 0, sizeof(unsigned), st);
   if (e != cudaSuccess) return cuda_fail(h, e, "run_rrtmg: clear flag");
   launch_run_zonal(s, a.g, a.o.coszen, w.zq, w.zp, w.flag, st);
   if (a.o.t_half) launch_run_thalf(s, a.g, a.o.t_half, st);
@@ -1134,13 +1159,14 @@ int run_enqueue(rrtmg_gpu_state* h, cudaStream_t st, const rrtmg_run_params& p, 
   const LwIn lin{c.play, c.plev, c.tlay, c.tlev, c.tsfc, c.h2o, c.o3, c.co2, c.gas[0], c.gas[1], c.gas[2],
                  c.gas[3], c.gas[4], c.gas[5], c.gas[6], c.emis, nullptr};
   rc = fork_lw_sw(
-      h, st,
+      h, st, fk,
       [&](cudaStream_t ls) {
-        return lw_run(h, ls, s.ncol, a.sk, 0, lin, w.uflx, w.dflx, w.hr, w.uflxc, w.dflxc, w.hrc, nullptr, nullptr);
+        return lw_enqueue(h, ls, lw_base, s.ncol, a.sk, 0, lin, w.uflx, w.dflx, w.hr, w.uflxc, w.dflxc, w.hrc,
+                          nullptr, nullptr);
       },
       [&](cudaStream_t ss) {
-        return sw_run(h, ss, s.ncol, a.sk, 0, p.solrad, dyofyr, p.solr_cnst, sin, w.swuflx, w.swdflx, w.swhr,
-                      w.swuflxc, w.swdflxc, w.swhrc);
+        return sw_enqueue(h, ss, sw_base, s.ncol, a.sk, 0, p.solrad, dyofyr, p.solr_cnst, sin, w.swuflx, w.swdflx,
+                          w.swhr, w.swuflxc, w.swdflxc, w.swhrc);
       });
   if (rc) return rc;
   const RunRad r{w.uflx, w.dflx, w.hr, w.swuflx, w.swdflx, w.swhr};
@@ -1211,7 +1237,7 @@ int rrtmg_run_dev(rrtmg_gpu_handle h, void* stream, const rrtmg_run_params* prm,
   int rc = run_check(h, prm, a);
   if (rc) return rc;
   cudaSetDevice(h->device);
-  return run_enqueue(h, (cudaStream_t)stream, *prm, a);
+  return run_enqueue(h, (cudaStream_t)stream, *prm, a, h->run_ws, default_fork(h), -1);
 }
 
 int rrtmg_run_c(rrtmg_gpu_handle h, const rrtmg_run_params* prm, int si, int sj, int sk, int seconds, int days,
@@ -1226,57 +1252,106 @@ int rrtmg_run_c(rrtmg_gpu_handle h, const rrtmg_run_params* prm, int si, int sj,
   int rc = run_check(h, prm, a);
   if (rc) return rc;
   cudaSetDevice(h->device);
-  const size_t P = (size_t)si * sj, P3 = P * sk, P3h = P * (sk + 1);
-  // device staging: inputs, then tdt (in and out), then the outputs
+  // Arrays are (level, latitude, longitude), longitude fastest: a block of
+  // latitude rows is `planes` strided runs of si * rows values.  On
+  // page-locked arrays the slab is processed in latitude chunks that alternate
+  // between the handle's two streams (each with its own staging, workspace
+  // and SW side stream), so that the copies of one chunk overlap the kernels
+  // of the other; every step of run_rrtmg works within a latitude row except
+  // the top-interface test, which the host makes for the whole slab.
+  const size_t plane = (size_t)si * sj;
   const double** ins[] = {&a.g.lat, &a.g.lon, &a.g.p_full, &a.g.p_half, &a.g.z_full, &a.g.z_half, &a.g.t,
                           &a.g.q, &a.g.o3, &a.g.t_surf, &a.g.albedo, &a.g.precip};
-  const size_t in_n[] = {P, P, P3, P3h, P3, P3h, P3, P3, P3, P, P, P};
+  const int in_planes[] = {1, 1, sk, sk + 1, sk, sk + 1, sk, sk, sk, 1, 1, 1};
   double** outs[] = {&a.o.tdt, &a.o.coszen, &a.o.flux_sw, &a.o.flux_lw, &a.o.t_half, &a.o.tdt_rad,
                      &a.o.tdt_sw, &a.o.tdt_lw, &a.o.olr, &a.o.isr};
-  const size_t out_n[] = {P3, P, P, P, P3h, P3, P3, P3, P, P};
-  size_t bytes = 0;
+  const int out_planes[] = {sk, 1, 1, 1, sk + 1, sk, sk, sk, 1, 1};
+  // whether some top interface of the RRTM columns is at 0 Pa
+  // (rrtm_radiation.f90:655-656), over the whole slab, as the zonal kernel
+  // finds it: p_half(i, j, 1) * 0.01 <= 0 at the columns kept by lonstep
+  int top = 0;
+  for (int j = 0; j < sj && !top; ++j)
+    for (int i = 0; i < si; i += prm->lonstep)
+      if (a.g.p_half[(size_t)si * j + i] * 0.01 <= 0.0) {
+        top = 1;
+        break;
+      }
+  bool all_pinned = true;
+  for (int k = 0; k < 12 && all_pinned; ++k) all_pinned = pinned(*ins[k]);
+  for (int k = 0; k < 10 && all_pinned; ++k) all_pinned = pinned(*outs[k]);
+  const int ncol = si / prm->lonstep * sj;
+  int nchunk = (all_pinned && ncol >= 2 * kChunkMin) ? std::min(kMaxChunks, ncol / kChunkMin) : 1;
+  nchunk = std::min(nchunk, sj);
+  const int rows = (sj + nchunk - 1) / nchunk;
+  size_t stage = 0;
   for (int k = 0; k < 12; ++k)
-    if (*ins[k]) bytes += align256(in_n[k] * sizeof(double));
+    if (*ins[k]) stage += align256((size_t)si * rows * in_planes[k] * sizeof(double));
   for (int k = 0; k < 10; ++k)
-    if (*outs[k]) bytes += align256(out_n[k] * sizeof(double));
-  rc = ensure(h, h->run_io, bytes, nullptr);
-  if (rc) return rc;
-  cudaStream_t st = h->stream;
-  Carver cv{(char*)h->run_io.p};
-  double* host_out[10];
+    if (*outs[k]) stage += align256((size_t)si * rows * out_planes[k] * sizeof(double));
+  for (int i = 0; i < 2 && i < nchunk; ++i) {
+    rc = ensure(h, h->run_cio[i], stage, nullptr);
+    if (rc) return rc;
+  }
+  cudaStream_t sts[2] = {h->stream, h->stream2};
+  const Fork fks[2] = {default_fork(h), Fork{h->side2, h->fork_ev2, h->join_ev2}};
+  auto drain = [h]() {
+    cudaStreamSynchronize(h->stream);
+    cudaStreamSynchronize(h->stream2);
+  };
   cudaError_t e = cudaSuccess;
-  for (int k = 0; k < 12 && e == cudaSuccess; ++k) {
-    if (!*ins[k]) continue;
-    double* d = cv.take<double>(in_n[k]);
-    e = cudaMemcpyAsync(d, *ins[k], in_n[k] * sizeof(double), cudaMemcpyHostToDevice, st);
-    *ins[k] = d;
+  for (int c = 0; c < nchunk; ++c) {
+    const int j0 = c * rows, nr = std::min(rows, sj - j0);
+    if (nr <= 0) break;
+    cudaStream_t st = sts[c % 2];
+    Carver cv{(char*)h->run_cio[c % 2].p};
+    const size_t off = (size_t)si * j0, w = (size_t)si * nr * sizeof(double);
+    RunArgs ac = a;
+    ac.sj = nr;
+    // copy of `planes` runs of w bytes between the slab and the chunk
+    auto copy = [&](void* dst, size_t dpitch, const void* src, size_t spitch, int planes, cudaMemcpyKind kind) {
+      return planes == 1 ? cudaMemcpyAsync(dst, src, w, kind, st)
+                         : cudaMemcpy2DAsync(dst, dpitch, src, spitch, w, planes, kind, st);
+    };
+    const double** cin[] = {&ac.g.lat, &ac.g.lon, &ac.g.p_full, &ac.g.p_half, &ac.g.z_full, &ac.g.z_half,
+                            &ac.g.t, &ac.g.q, &ac.g.o3, &ac.g.t_surf, &ac.g.albedo, &ac.g.precip};
+    for (int k = 0; k < 12 && e == cudaSuccess; ++k) {
+      if (!*ins[k]) continue;
+      double* d = cv.take<double>((size_t)si * nr * in_planes[k]);
+      e = copy(d, w, *ins[k] + off, plane * sizeof(double), in_planes[k], cudaMemcpyHostToDevice);
+      *cin[k] = d;
+    }
+    double** cout[] = {&ac.o.tdt, &ac.o.coszen, &ac.o.flux_sw, &ac.o.flux_lw, &ac.o.t_half, &ac.o.tdt_rad,
+                       &ac.o.tdt_sw, &ac.o.tdt_lw, &ac.o.olr, &ac.o.isr};
+    for (int k = 0; k < 10 && e == cudaSuccess; ++k) {
+      if (!*outs[k]) continue;
+      double* d = cv.take<double>((size_t)si * nr * out_planes[k]);
+      // tdt is read (the tendency before radiation) and written
+      if (k == 0) e = copy(d, w, *outs[0] + off, plane * sizeof(double), out_planes[0], cudaMemcpyHostToDevice);
+      *cout[k] = d;
+    }
+    // On a failure after copies were enqueued, wait for them before returning:
+    // they read and write the caller's arrays.  The SW work of run_enqueue is
+    // joined back into st, so the two streams cover it.
+    if (e != cudaSuccess) {
+      drain();
+      return cuda_fail(h, e, "run_rrtmg: copy inputs");
+    }
+    rc = run_enqueue(h, st, *prm, ac, h->run_cws[c % 2], fks[c % 2], top);
+    if (rc) {
+      drain();
+      return rc;
+    }
+    for (int k = 0; k < 10 && e == cudaSuccess; ++k)
+      if (*outs[k])
+        e = copy(*outs[k] + off, plane * sizeof(double), *cout[k], w, out_planes[k], cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+      drain();
+      return cuda_fail(h, e, "run_rrtmg: copy outputs");
+    }
   }
-  for (int k = 0; k < 10 && e == cudaSuccess; ++k) {
-    host_out[k] = *outs[k];
-    if (!*outs[k]) continue;
-    double* d = cv.take<double>(out_n[k]);
-    if (k == 0) e = cudaMemcpyAsync(d, tdt, out_n[0] * sizeof(double), cudaMemcpyHostToDevice, st);
-    *outs[k] = d;
-  }
-  // On a failure after copies were enqueued, wait for them before returning:
-  // they read and write the caller's arrays.  The SW work of run_enqueue is
-  // joined back into st, so st covers it.
-  if (e != cudaSuccess) {
-    cudaStreamSynchronize(st);
-    return cuda_fail(h, e, "run_rrtmg: copy inputs");
-  }
-  rc = run_enqueue(h, st, *prm, a);
-  if (rc) {
-    cudaStreamSynchronize(st);
-    return rc;
-  }
-  for (int k = 0; k < 10 && e == cudaSuccess; ++k)
-    if (host_out[k]) e = cudaMemcpyAsync(host_out[k], *outs[k], out_n[k] * sizeof(double), cudaMemcpyDeviceToHost, st);
-  if (e != cudaSuccess) {
-    cudaStreamSynchronize(st);
-    return cuda_fail(h, e, "run_rrtmg: copy outputs");
-  }
-  return read_flags(h, st);
+  e = cudaStreamSynchronize(h->stream2);
+  if (e != cudaSuccess) return cuda_fail(h, e, "synchronise");
+  return read_flags(h, h->stream);
 }
 
 }  // extern "C"

@@ -53,6 +53,47 @@ enum SwField {
   SF_FAC11, SF_SELFFAC, SF_SELFFRAC, SF_FORFAC, SF_FORFRAC, SF_N
 };
 
+// Table gather (k-distribution and transmittance tables, read-only, reused by
+// every cell of a band): through the read-only path; with
+// RRTMG_TAB_EVICT_LAST, with the L1 "evict last" priority, so that the
+// solvers' per-thread layer arrays streaming through L1 evict the tables last.
+template <class T>
+__device__ __forceinline__ T tld(const T* p) {
+#ifdef RRTMG_TAB_EVICT_LAST
+  if constexpr (sizeof(T) == 4) {
+    float v;
+    asm("ld.global.nc.L1::evict_last.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+  } else {
+    double v;
+    asm("ld.global.nc.L1::evict_last.f64 %0, [%1];" : "=d"(v) : "l"(p));
+    return v;
+  }
+#else
+  return __ldg(p);
+#endif
+}
+
+// Per-layer prep field of one (layer, column), read once per layer by the
+// lanes of the column: through the read-only path; with
+// RRTMG_FIELD_EVICT_FIRST, with the L1 "evict first" priority.
+template <class T>
+__device__ __forceinline__ T fld_ld(const T* p) {
+#ifdef RRTMG_FIELD_EVICT_FIRST
+  if constexpr (sizeof(T) == 4) {
+    float v;
+    asm("ld.global.nc.L1::evict_first.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+  } else {
+    double v;
+    asm("ld.global.nc.L1::evict_first.f64 %0, [%1];" : "=d"(v) : "l"(p));
+    return v;
+  }
+#else
+  return __ldg(p);
+#endif
+}
+
 // Packed integer interpolation indices of one layer.
 __host__ __device__ inline uint32_t pack_idx(int jp, int jt, int jt1, int inds, int indf, int indm) {
   return (uint32_t)jp | ((uint32_t)jt << 6) | ((uint32_t)jt1 << 9) | ((uint32_t)inds << 12) |

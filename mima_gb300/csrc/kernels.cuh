@@ -397,8 +397,7 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
                                         const double* __restrict__ tauaer, const R* __restrict__ tab,
                                         const R* __restrict__ exptbl, const R* __restrict__ tfntbl,
                                         double* __restrict__ bu, double* __restrict__ bd, double* __restrict__ bdu,
-                                        int ncol, int nlay, int idrv, bool analytic, int blk, float* sbuf,
-                                        float* lvl = nullptr) {
+                                        int ncol, int nlay, int idrv, bool analytic, int blk, float* sbuf) {
   const bool IDRV = idrv == 1;
   constexpr bool SPLIT = sizeof(R) == 4;
   constexpr int NG = lw_ng(B);
@@ -418,20 +417,7 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
   const R bpade = (R)c_lw.bpade;
   const R rec_6 = (R)0.166667;
   const size_t fstride = (size_t)nlay * N;
-#ifdef RRTMG_LW_SMEM
-  constexpr bool SMEM = SPLIT;
-#else
-  constexpr bool SMEM = false;
-#endif
-  R atrans_l[SMEM ? 1 : MAXL], bbugas_l[SMEM ? 1 : MAXL];
-  auto atrans = [&](int l) -> R& {
-    if constexpr (SMEM) return *reinterpret_cast<R*>(lvl + (size_t)l * kBlock + threadIdx.x);
-    else return atrans_l[l];
-  };
-  auto bbugas = [&](int l) -> R& {
-    if constexpr (SMEM) return *reinterpret_cast<R*>(lvl + (size_t)(nlay + l) * kBlock + threadIdx.x);
-    else return bbugas_l[l];
-  };
+  R atrans[MAXL], bbugas[MAXL];
   R radld = (R)0., fracs1 = (R)0.;
   double* bdp = bd + (size_t)(B - 1) * (nlay + 1) * N + col;
   double* bup = bu + (size_t)(B - 1) * (nlay + 1) * N + col;
@@ -490,14 +476,14 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
       const R tblind = odepth / (bpade + odepth);
       int itr = (int)((R)10000.0 * tblind + (R)0.5);
       itr = itr < 0 ? 0 : (itr > kNTbl ? kNTbl : itr);  // in range for any odepth >= 0; guards NaN input
-      const R transc = __ldg(exptbl + itr);
+      const R transc = tld(exptbl + itr);
       atr = (R)1. - transc;
-      const R tausfac = __ldg(tfntbl + itr);
+      const R tausfac = tld(tfntbl + itr);
       bbd = plfrac * (blay + tausfac * dplankdn);
       bbu = plfrac * (blay + tausfac * dplankup);
     }
-    atrans(lev - 1) = atr;
-    bbugas(lev - 1) = bbu;
+    atrans[lev - 1] = atr;
+    bbugas[lev - 1] = bbu;
     radld = radld + (bbd - radld) * atr;
     if constexpr (SPLIT) {
       gs.put(0, radld);
@@ -533,9 +519,8 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
     }
   }
   for (int lev = 1; lev <= nlay; ++lev) {
-    const R at = atrans(lev - 1);
-    radlu = radlu + (bbugas(lev - 1) - radlu) * at;
-    if (IDRV) dlu = dlu * ((R)1.0 - at);
+    radlu = radlu + (bbugas[lev - 1] - radlu) * atrans[lev - 1];
+    if (IDRV) dlu = dlu * ((R)1.0 - atrans[lev - 1]);
     if constexpr (SPLIT) {
       gs.put(0, radlu);
       gs.put(1, dlu);
@@ -585,7 +570,6 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_LW_MINB :
                                                            double* bdu, int ncol, int nlay, int idrv,
                                                            int analytic) {
   __shared__ float sbuf[sizeof(R) == 4 ? kGSumFloats : 1];
-  extern __shared__ float lw_lvl[];
   int blk = blockIdx.x, band = 0;
   for (; band < kLwBands; ++band) {
     const int nb = lw_blocks_for_band(split_lanes(c_lw.band[band].ng, sizeof(R) == 4), ncol);
@@ -595,7 +579,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_LW_MINB :
   const bool an = FL < 0 ? analytic != 0 : (FL & 1) != 0;
   const int idv = FL < 0 ? idrv : ((FL & 2) ? 1 : 0);
 #define RRTMG_LW_CASE(b) \
-  case b - 1: lw_band<b, R, MAXL>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idv, an, blk, sbuf, lw_lvl); break;
+  case b - 1: lw_band<b, R, MAXL>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idv, an, blk, sbuf); break;
   switch (band) {
     RRTMG_LW_CASE(1) RRTMG_LW_CASE(2) RRTMG_LW_CASE(3) RRTMG_LW_CASE(4) RRTMG_LW_CASE(5) RRTMG_LW_CASE(6)
     RRTMG_LW_CASE(7) RRTMG_LW_CASE(8) RRTMG_LW_CASE(9) RRTMG_LW_CASE(10) RRTMG_LW_CASE(11) RRTMG_LW_CASE(12)
@@ -842,7 +826,7 @@ __device__ __forceinline__ R sw_exp_tbl(R ze1, R bpade, const TT* __restrict__ e
   const R tblind = ze1 / (bpade + ze1);
   int itind = (int)((R)10000.0 * tblind + (R)0.5);
   itind = itind < 0 ? 0 : (itind > kNTbl ? kNTbl : itind);  // guards NaN / negative optical depths
-  return (R)__ldg(exptbl + itind);
+  return (R)tld(exptbl + itind);
 }
 
 // delta-Eddington layer reflectance/transmittance, kmodts = 2 (rrtmg_sw_reftra.f90:143-300)
@@ -934,7 +918,7 @@ __device__ __forceinline__ void sw_exp_pair(R ze1, R bpade, const float* __restr
   const R tblind = ze1 / (bpade + ze1);
   int itind = (int)((R)10000.0 * tblind + (R)0.5);
   itind = itind < 0 ? 0 : (itind > kNTbl ? kNTbl : itind);
-  e = (R)__ldg(exptbl + itind);
+  e = (R)tld(exptbl + itind);
   em1 = e - (R)1.;
 }
 

@@ -157,12 +157,7 @@ static void lw_split_flags(int fl, int nb, cudaStream_t s, const LwPrepT<float>&
          : fl == 1 ? lw_gpoint_kernel<float, MAXL, 1>
          : fl == 2 ? lw_gpoint_kernel<float, MAXL, 2>
                    : lw_gpoint_kernel<float, MAXL, 3>;
-#ifdef RRTMG_LW_SMEM
-  const size_t smem = (size_t)2 * nlay * kBlock * sizeof(float);
-#else
-  const size_t smem = 0;
-#endif
-  k<<<nb, kBlock, smem, s>>>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv, analytic);
+  k<<<nb, kBlock, 0, s>>>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv, analytic);
 }
 
 void launch_lw_gpoint_split(const LwPrepT<float>& p, const double* emis, const double* tauaer, const float* tab,

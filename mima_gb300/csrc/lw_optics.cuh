@@ -32,7 +32,7 @@ struct LwLayerView {
   const R* __restrict__ f;  // per-layer fields stored in the solver's type
   size_t fstride;           // nlay * ncol
   size_t o;                 // (lay-1) * ncol + col
-  __device__ __forceinline__ R operator()(int fld) const { return __ldg(f + (size_t)fld * fstride + o); }
+  __device__ __forceinline__ R operator()(int fld) const { return fld_ld(f + (size_t)fld * fstride + o); }
 };
 
 template <class R>
@@ -94,7 +94,7 @@ __device__ __forceinline__ W3<R> w3(R specparm, R fs, R facA, R facB) {
 template <class R, int NG, class TT>
 __device__ __forceinline__ R major9(const TT* __restrict__ ka, R specparm, R speccomb, int ind, int g,
                                     const W3<R>& w) {
-  auto K = [&](int i) { return __ldg(ka + (size_t)(i - 1) * NG + g); };
+  auto K = [&](int i) { return tld(ka + (size_t)(i - 1) * NG + g); };
   if (specparm < (R)0.125)
     return speccomb * (w.a0 * K(ind) + w.a1 * K(ind + 1) + w.a2 * K(ind + 2) + w.b0 * K(ind + 9) +
                        w.b1 * K(ind + 10) + w.b2 * K(ind + 11));
@@ -106,7 +106,7 @@ __device__ __forceinline__ R major9(const TT* __restrict__ ka, R specparm, R spe
 
 template <class R, int NG, class TT>
 __device__ __forceinline__ R interp4(const TT* __restrict__ k, R f00, R f10, R f01, R f11, int i0, int i1, int g) {
-  auto K = [&](int i) { return __ldg(k + (size_t)(i - 1) * NG + g); };
+  auto K = [&](int i) { return tld(k + (size_t)(i - 1) * NG + g); };
   return f00 * K(i0) + f10 * K(i0 + 1) + f01 * K(i1) + f11 * K(i1 + 1);
 }
 
@@ -114,7 +114,7 @@ __device__ __forceinline__ R interp4(const TT* __restrict__ k, R f00, R f10, R f
 template <class R, int NG, class TT>
 __device__ __forceinline__ R major5(const TT* __restrict__ kb, R sc, R fs, int i0, R sc1, R fs1, int i1, R f00,
                                     R f10, R f01, R f11, int g) {
-  auto K = [&](int i) { return __ldg(kb + (size_t)(i - 1) * NG + g); };
+  auto K = [&](int i) { return tld(kb + (size_t)(i - 1) * NG + g); };
   R fac000 = ((R)1. - fs) * f00, fac010 = ((R)1. - fs) * f10, fac100 = fs * f00, fac110 = fs * f10;
   R fac001 = ((R)1. - fs1) * f01, fac011 = ((R)1. - fs1) * f11, fac101 = fs1 * f01, fac111 = fs1 * f11;
   return sc * (fac000 * K(i0) + fac100 * K(i0 + 1) + fac010 * K(i0 + 5) + fac110 * K(i0 + 6)) +
@@ -124,13 +124,13 @@ __device__ __forceinline__ R major5(const TT* __restrict__ kb, R sc, R fs, int i
 // k(row, g) + frac * (k(row+1, g) - k(row, g))
 template <class R, int NG, class TT>
 __device__ __forceinline__ R lin(const TT* __restrict__ k, int row1, R frac, int g) {
-  R a = (R)__ldg(k + (size_t)(row1 - 1) * NG + g), b = (R)__ldg(k + (size_t)row1 * NG + g);
+  R a = (R)tld(k + (size_t)(row1 - 1) * NG + g), b = (R)tld(k + (size_t)row1 * NG + g);
   return a + frac * (b - a);
 }
 // Minor table k(j, indm, g) with nj rows in eta: eta- then T-interpolated.
 template <class R, int NG, class TT>
 __device__ __forceinline__ R minor_eta(const TT* __restrict__ k, int nj, int jm, R fm, int indm, R minorfrac, int g) {
-  auto K = [&](int j, int m) { return __ldg(k + ((size_t)(m - 1) * nj + (j - 1)) * NG + g); };
+  auto K = [&](int j, int m) { return tld(k + ((size_t)(m - 1) * nj + (j - 1)) * NG + g); };
   R m1 = K(jm, indm) + fm * (K(jm + 1, indm) - K(jm, indm));
   R m2 = K(jm, indm + 1) + fm * (K(jm + 1, indm + 1) - K(jm, indm + 1));
   return m1 + minorfrac * (m2 - m1);
@@ -190,7 +190,7 @@ __device__ __forceinline__ void lw_gas(const LwConst& C, const RC& CR, const V& 
   auto i_up1 = [&](int js) { return ((jp - 12) * 5 + (ix.jt1 - 1)) * bd.nspb + js; };
   auto tself = [&]() { return L(LF_SELFFAC) * lin<R, NG>(self, ix.inds, L(LF_SELFFRAC), g); };
   auto tfor = [&]() { return L(LF_FORFAC) * lin<R, NG>(forr, ix.indf, L(LF_FORFRAC), g); };
-  auto fr1 = [&](const TT* fr) { return (R)__ldg(fr + g); };
+  auto fr1 = [&](const TT* fr) { return (R)tld(fr + g); };
   auto fr_eta = [&](const TT* fr, const EtaV<R>& e) { return lin<R, NG>(fr, e.js, e.fs, g); };
   auto i4 = [&](const TT* k, int i0, int i1) {
     return interp4<R, NG>(k, L(LF_FAC00), L(LF_FAC10), L(LF_FAC01), L(LF_FAC11), i0, i1, g);
@@ -286,7 +286,7 @@ __device__ __forceinline__ void lw_gas(const LwConst& C, const RC& CR, const V& 
       R tau_major = major9<R, NG>(ka, e.specparm, e.speccomb, ind0, g, w0);
       R tau_major1 = major9<R, NG>(ka, e1.specparm, e1.speccomb, ind1, g, w1);
       if constexpr (B == 5) {
-        taug = tau_major + tau_major1 + tauself + taufor + extra + L(LF_WX1) * __ldg(tab + bd.off[LW_X1] + g);
+        taug = tau_major + tau_major1 + tauself + taufor + extra + L(LF_WX1) * tld(tab + bd.off[LW_X1] + g);
       } else if constexpr (B == 13) {
         taug = tau_major + tau_major1 + tauself + taufor + extra + extra2;
       } else {
@@ -311,7 +311,7 @@ __device__ __forceinline__ void lw_gas(const LwConst& C, const RC& CR, const V& 
           R absn2o = minor_eta<R, NG>(tab + bd.off[LW_MB1], 5, em.js, em.fs, ix.indm, L(LF_MINORFRAC), g);
           taug = maj + taufor + adjcoln2o * absn2o;
         } else {
-          taug = maj + L(LF_WX1) * __ldg(tab + bd.off[LW_X1] + g);
+          taug = maj + L(LF_WX1) * tld(tab + bd.off[LW_X1] + g);
         }
         fracs = fr_eta(frb, ep);
       } else if constexpr (B == 7) {
@@ -380,27 +380,27 @@ __device__ __forceinline__ void lw_gas(const LwConst& C, const RC& CR, const V& 
       R tauself = tself(), taufor = tfor();
       R absco2 = (lin<R, NG>(tab + bd.off[LW_MA1], ix.indm, L(LF_MINORFRAC), g));
       taug = L(LF_COLH2O) * i4(ka, i_lo(1), i_lo1(1)) + tauself + taufor + adjcolco2 * absco2 +
-             L(LF_WX2) * __ldg(tab + bd.off[LW_X1] + g) + L(LF_WX3) * __ldg(tab + bd.off[LW_X2] + g);
+             L(LF_WX2) * tld(tab + bd.off[LW_X1] + g) + L(LF_WX3) * tld(tab + bd.off[LW_X2] + g);
     } else {
-      taug = (R)0.0 + L(LF_WX2) * __ldg(tab + bd.off[LW_X1] + g) + L(LF_WX3) * __ldg(tab + bd.off[LW_X2] + g);
+      taug = (R)0.0 + L(LF_WX2) * tld(tab + bd.off[LW_X1] + g) + L(LF_WX3) * tld(tab + bd.off[LW_X2] + g);
     }
     fracs = fr1(fra);
   } else if constexpr (B == 8) {
     R adjcolco2 = adj_col<R>(L(LF_COLCO2), L(LF_COLDRY), chi(2, jp + 1), (R)3.0, (R)2.0, 0.65);
-    R x12 = L(LF_WX3) * __ldg(tab + bd.off[LW_X1] + g);
+    R x12 = L(LF_WX3) * tld(tab + bd.off[LW_X1] + g);
     if (lower) {
       R tauself = tself(), taufor = tfor();
       R absco2 = (lin<R, NG>(tab + bd.off[LW_MA1], ix.indm, L(LF_MINORFRAC), g));
       R abso3 = (lin<R, NG>(tab + bd.off[LW_MA2], ix.indm, L(LF_MINORFRAC), g));
       R absn2o = (lin<R, NG>(tab + bd.off[LW_MA3], ix.indm, L(LF_MINORFRAC), g));
       taug = L(LF_COLH2O) * i4(ka, i_lo(1), i_lo1(1)) + tauself + taufor + adjcolco2 * absco2 +
-             L(LF_COLO3) * abso3 + L(LF_COLN2O) * absn2o + x12 + L(LF_WX4) * __ldg(tab + bd.off[LW_X2] + g);
+             L(LF_COLO3) * abso3 + L(LF_COLN2O) * absn2o + x12 + L(LF_WX4) * tld(tab + bd.off[LW_X2] + g);
       fracs = fr1(fra);
     } else {
       R absco2 = (lin<R, NG>(tab + bd.off[LW_MB1], ix.indm, L(LF_MINORFRAC), g));
       R absn2o = (lin<R, NG>(tab + bd.off[LW_MB2], ix.indm, L(LF_MINORFRAC), g));
       taug = L(LF_COLO3) * i4(kb, i_up(1), i_up1(1)) + adjcolco2 * absco2 + L(LF_COLN2O) * absn2o + x12 +
-             L(LF_WX4) * __ldg(tab + bd.off[LW_X2] + g);
+             L(LF_WX4) * tld(tab + bd.off[LW_X2] + g);
       fracs = fr1(frb);
     }
   } else if constexpr (B == 10) {

@@ -25,7 +25,7 @@ template <class R, class F = R>
 struct SwLayerView {
   const F* __restrict__ f;
   size_t fstride, o;
-  __device__ __forceinline__ R operator()(int fld) const { return (R)__ldg(f + (size_t)fld * fstride + o); }
+  __device__ __forceinline__ R operator()(int fld) const { return (R)fld_ld(f + (size_t)fld * fstride + o); }
 };
 
 // Eta of the band's key-species pair at one layer; mult 8 (lower) or 4 (upper).
@@ -43,7 +43,7 @@ __device__ __forceinline__ EtaV<R> sw_band_eta(const V& L, R mult, R one_m) {
 template <class R, int NG, class TT>
 __device__ __forceinline__ R sw_major8(const TT* __restrict__ k, const EtaV<R>& e, R f00, R f10, R f01, R f11,
                                        int i0, int i1, int s, int g) {
-  auto K = [&](int i) { return __ldg(k + (size_t)(i - 1) * NG + g); };
+  auto K = [&](int i) { return tld(k + (size_t)(i - 1) * NG + g); };
   R fs = e.fs;
   R fac000 = ((R)1. - fs) * f00, fac010 = ((R)1. - fs) * f10, fac100 = fs * f00, fac110 = fs * f10;
   R fac001 = ((R)1. - fs) * f01, fac011 = ((R)1. - fs) * f11, fac101 = fs * f01, fac111 = fs * f11;
@@ -75,11 +75,11 @@ __device__ __forceinline__ void sw_gas(const SwConst& C, const V& L, const Idx& 
   auto m8 = [&](const TT* k, const EtaV<R>& e, int i0, int i1, int s) {
     return sw_major8<R, NG>(k, e, L(SF_FAC00), L(SF_FAC10), L(SF_FAC01), L(SF_FAC11), i0, i1, s, g);
   };
-  auto E = [&](int role) { return (R)__ldg(tab + bd.off[role] + g); };
+  auto E = [&](int role) { return (R)tld(tab + bd.off[role] + g); };
   const R colmol = L(SF_COLMOL);
 
   if constexpr (B == 16 || B == 18 || B == 19 || B == 21 || B == 22 || B == 17) {
-    const R rs = __ldg(rayl);
+    const R rs = tld(rayl);
     if (lower) {
       EtaV<R> e = sw_band_eta<B, R>(L, (R)8., one_m);
       R t = m8(ka, e, i_lo(e.js), i_lo1(e.js), 9) + L(SF_COLH2O) * (selft() + fort());
@@ -99,7 +99,7 @@ __device__ __forceinline__ void sw_gas(const SwConst& C, const V& L, const Idx& 
     }
     taur = colmol * rs;
   } else if constexpr (B == 20) {
-    const R rs = __ldg(rayl);
+    const R rs = tld(rayl);
     if (lower)
       taug = L(SF_COLH2O) * (i4(ka, i_lo(1), i_lo1(1)) + selft() + fort()) + L(SF_COLCH4) * E(SW_E1);
     else
@@ -108,7 +108,7 @@ __device__ __forceinline__ void sw_gas(const SwConst& C, const V& L, const Idx& 
   } else if constexpr (B == 23) {
     if (lower) taug = L(SF_COLH2O) * ((R)1.029 * i4(ka, i_lo(1), i_lo1(1)) + selft() + fort());
     else taug = (R)0.;
-    taur = colmol * __ldg(rayl + g);
+    taur = colmol * tld(rayl + g);
   } else if constexpr (B == 24) {
     if (lower) {
       EtaV<R> e = sw_band_eta<B, R>(L, (R)8., one_m);
@@ -121,25 +121,25 @@ __device__ __forceinline__ void sw_gas(const SwConst& C, const V& L, const Idx& 
   } else if constexpr (B == 25) {
     if (lower) taug = L(SF_COLH2O) * i4(ka, i_lo(1), i_lo1(1)) + L(SF_COLO3) * E(SW_E2);
     else taug = L(SF_COLO3) * E(SW_E3);
-    taur = colmol * __ldg(rayl + g);
+    taur = colmol * tld(rayl + g);
   } else if constexpr (B == 26) {
     taug = (R)0.;
-    taur = colmol * __ldg(rayl + g);
+    taur = colmol * tld(rayl + g);
   } else if constexpr (B == 27) {
     if (lower) taug = L(SF_COLO3) * i4(ka, i_lo(1), i_lo1(1));
     else taug = L(SF_COLO3) * i4(kb, i_up(1), i_up1(1));
-    taur = colmol * __ldg(rayl + g);
+    taur = colmol * tld(rayl + g);
   } else if constexpr (B == 28) {
     EtaV<R> e = sw_band_eta<B, R>(L, lower ? (R)8. : (R)4., one_m);
     if (lower) taug = m8(ka, e, i_lo(e.js), i_lo1(e.js), 9);
     else taug = m8(kb, e, i_up(e.js), i_up1(e.js), 5);
-    taur = colmol * __ldg(rayl);
+    taur = colmol * tld(rayl);
   } else {  // 29
     if (lower)
       taug = L(SF_COLH2O) * (i4(ka, i_lo(1), i_lo1(1)) + selft() + fort()) + L(SF_COLCO2) * E(SW_E2);
     else
       taug = L(SF_COLCO2) * i4(kb, i_up(1), i_up1(1)) + L(SF_COLH2O) * E(SW_E1);
-    taur = colmol * __ldg(rayl);
+    taur = colmol * tld(rayl);
   }
 }
 
@@ -161,9 +161,9 @@ __device__ __forceinline__ auto sw_sfluxzen(const SwConst& C, const V& L, bool l
     EtaV<R> e = sw_band_eta<B, R>(L, (R)8., (R)C.oneminus);
     return lin<R, NG>(sf, e.js, e.fs, g);
   } else if constexpr (B == 27) {
-    return (R)((50.15 / 48.37) * __ldg(sf + g));
+    return (R)((50.15 / 48.37) * tld(sf + g));
   } else {
-    return (R)__ldg(sf + g);
+    return (R)tld(sf + g);
   }
 }
 

@@ -416,18 +416,25 @@ class RRTMG:
             q("swuflx"), q("swdflx"), q("swhr"), q("swuflxc"), q("swdflxc"), q("swhrc"))
         self._check(rc)
 
-    def run_rrtmg(self, prm, slab, seconds, days, days_per_year=365, tdt=None, diagnostics=True):
+    def run_rrtmg(self, prm, slab, seconds, days, days_per_year=365, tdt=None, diagnostics=True, out=None):
         """run_rrtmg on host arrays (rrtmg_run_c).  ``slab`` holds the GCM
         arrays of :data:`RUN_IN` as C-ordered (sk[+1], sj, si) / (sj, si)
         numpy arrays (Fortran (si, sj, sk) order); returns the outputs of
-        :data:`RUN_OUT` (tdt = the given tendency plus the radiative one)."""
+        :data:`RUN_OUT` (tdt = the given tendency plus the radiative one).
+        ``out``: optional caller arrays for the outputs (e.g. page-locked ones;
+        ``out["tdt"]`` holds the tendency before radiation and is updated)."""
         si, sj, sk = slab.si, slab.sj, slab.sk
         shapes = {"tdt": (sk, sj, si), "coszen": (sj, si), "flux_sw": (sj, si), "flux_lw": (sj, si),
                   "t_half": (sk + 1, sj, si), "tdt_rad": (sk, sj, si), "tdt_sw": (sk, sj, si),
                   "tdt_lw": (sk, sj, si), "olr": (sj, si), "isr": (sj, si)}
-        keep = RUN_OUT if diagnostics else ("tdt", "coszen", "flux_sw", "flux_lw")
-        out = {k: np.empty(shapes[k]) for k in keep}
-        out["tdt"] = np.array(slab.tdt if tdt is None else tdt, dtype=np.float64, order="C", copy=True)
+        if out is not None:
+            for k, a in out.items():
+                if a.shape != shapes[k] or a.dtype != np.float64 or not a.flags.c_contiguous:
+                    raise ValueError(f"out[{k!r}] must be a C-contiguous float64 array of shape {shapes[k]}")
+        else:
+            keep = RUN_OUT if diagnostics else ("tdt", "coszen", "flux_sw", "flux_lw")
+            out = {k: np.empty(shapes[k]) for k in keep}
+            out["tdt"] = np.array(slab.tdt if tdt is None else tdt, dtype=np.float64, order="C", copy=True)
         ins = [_host(getattr(slab, k)) for k in RUN_IN]
         rc = self.lib.rrtmg_run_c(self._h, C.byref(prm), C.c_int(si), C.c_int(sj), C.c_int(sk), C.c_int(seconds),
                                   C.c_int(days), C.c_int(days_per_year), *[_hp(a) for a in ins],

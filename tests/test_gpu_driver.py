@@ -115,3 +115,44 @@ def test_driver_argument_errors(gpu):
     with pytest.raises(R.RRTMGError) as e:
         gpu.run_rrtmg(R.run_params(), bad, 0, 0)
     assert e.value.code == R.RRTMG_ERR_INPUT
+
+
+@pytest.mark.parametrize("si,sj,case", [(256, 128, "lonstep4_zm_rad"), (512, 128, "tracers_water_precip"),
+                                         (256, 128, "secondary_instantaneous")])
+def test_driver_host_chunks_match_device_entry(gpu, si, sj, case):
+    """rrtmg_run_c on page-locked arrays of 32768 and 65536 columns runs the
+    slab in 2 and 4 latitude chunks alternating between two streams; its
+    results equal rrtmg_run_dev's on the whole slab bit for bit.  One slab has
+    its top interfaces above 0 Pa, so the slab-wide top-interface test the
+    host makes for the chunks is checked both ways."""
+    torch = pytest.importorskip("torch")
+    slab = A.gcm_slab(si, sj, 40, seed=si + sj, ozone=True)
+    if case == "secondary_instantaneous":
+        slab.p_half[0] = 1.0  # every top interface at 1 Pa
+    prm = R.run_params(**dict(CASES[case], lonstep=1))
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    for k in R.RUN_IN:
+        if getattr(slab, k) is not None:
+            setattr(slab, k, pin(getattr(slab, k)))
+    out = {}
+    for k in R.RUN_OUT:
+        shape = slab.p_half.shape if k == "t_half" else slab.tdt.shape if k.startswith("tdt") else slab.t_surf_rad.shape
+        out[k] = pin(np.zeros(shape))
+    out["tdt"][...] = slab.tdt
+    gpu.set_precision("split")
+    try:
+        host = gpu.run_rrtmg(prm, slab, SECONDS, DAYS, out=out)
+        dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+        d = {k: dev(getattr(slab, k)) for k in R.RUN_IN if getattr(slab, k) is not None}
+        dout = {k: torch.empty(host[k].shape, dtype=torch.float64, device="cuda") for k in R.RUN_OUT}
+        dout["tdt"] = dev(slab.tdt.copy())
+        s = torch.cuda.Stream()
+        with torch.cuda.stream(s):
+            gpu.run_rrtmg_dev(s.cuda_stream, prm, slab.si, slab.sj, slab.sk, SECONDS, DAYS, 365, d, dout)
+        s.synchronize()
+    finally:
+        gpu.set_precision("fp64")
+    assert gpu.sync_status(s.cuda_stream) == R.RRTMG_OK
+    for k in R.RUN_OUT:
+        np.testing.assert_array_equal(dout[k].cpu().numpy(), host[k], err_msg=k)
+    assert host["olr"].min() > 100.0

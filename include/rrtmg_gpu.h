@@ -23,11 +23,16 @@
  *     the LW rate of the top layer is computed (rrtmg_lw_rtrnmr.f90:774-775
  *     zeroes htr(nlayers), which lies above the last output layer).
  *   - Optional gas arrays (ch4, n2o, o2, cfc*) and tauaer may be NULL (= 0).
- *   - Cloud arguments are accepted for signature compatibility and must
- *     describe clear sky: icld must be 0.  The reference coerces icld and
- *     iaer silently (:437, :471-479); this library returns
- *     RRTMG_ERR_UNSUPPORTED for any configuration it does not compute and never
- *     falls back to a CPU path.
+ *   - Clouds: rrtmg_lw_c / rrtmg_lw_dev compute icld = 1 (random overlap,
+ *     rrtmg_lw_rtrn.f90) with the cloud optical depths given (inflglw = 0,
+ *     rrtmg_lw_cldprop.f90:165-171): cldfr (ncol,nlay), taucld (16,ncol,nlay),
+ *     cicewp / cliqwp (ncol,nlay) or NULL (they only decide, with the band sum
+ *     of taucld, whether a layer's depths are kept); reice, reliq and the ice /
+ *     liquid flags are unused.  Every other entry point is clear sky
+ *     (icld = 0).  The reference coerces icld and iaer silently (:437,
+ *     :471-479); this library returns RRTMG_ERR_UNSUPPORTED for any
+ *     configuration it does not compute (icld = 2 / 3, inflglw = 1 / 2, SW
+ *     clouds) and never falls back to a CPU path.
  *   - Every entry point returns a status (0 = success).  A handle is not
  *     thread-safe; use one handle per host thread.
  */
@@ -43,7 +48,7 @@ typedef struct rrtmg_gpu_state* rrtmg_gpu_handle;
 enum rrtmg_gpu_status {
   RRTMG_OK = 0,
   RRTMG_ERR_ARG = 1,          /* bad dimension, null required pointer, bad handle */
-  RRTMG_ERR_UNSUPPORTED = 2,  /* icld != 0, iaer not in {0,10}, idrv not in {0,1} */
+  RRTMG_ERR_UNSUPPORTED = 2,  /* clouds other than LW icld = 1 / inflglw = 0, iaer not in {0,10}, idrv not in {0,1} */
   RRTMG_ERR_CUDA = 3,         /* CUDA runtime error (see rrtmg_gpu_last_error) */
   RRTMG_ERR_TABLES = 4,       /* table blob missing, malformed or checksum mismatch */
   RRTMG_ERR_INPUT = 5,        /* device-side validation flagged a non-finite or out-of-range input */
@@ -90,7 +95,9 @@ long long rrtmg_gpu_launch_count(rrtmg_gpu_handle h);
 
 /* rrtmg_lw (rrtmg_lw_rad.nomcica.f90:80-89), host arrays.  tauaer (ncol,nlay,16)
  * is always added to the gas optical depth (the reference forces iaer = 10,
- * :442).  duflx_dt/duflxc_dt (ncol,nlay+1) are written when idrv = 1. */
+ * :442).  duflx_dt/duflxc_dt (ncol,nlay+1) are written when idrv = 1.  With
+ * icld = 1 the clear-sky outputs (uflxc, dflxc, hrc, duflxc_dt) are rtrn's
+ * clear-sky stream, else they equal the total ones. */
 int rrtmg_lw_c(rrtmg_gpu_handle h, int ncol, int nlay, int icld, int idrv,
                const double* play, const double* plev, const double* tlay, const double* tlev,
                const double* tsfc, const double* h2ovmr, const double* o3vmr, const double* co2vmr,

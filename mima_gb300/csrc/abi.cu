@@ -43,6 +43,8 @@ struct rrtmg_gpu_state {
   cudaStream_t stream = nullptr;
   HostTables host;
   double *lw_tab64 = nullptr, *sw_tab64 = nullptr, *lw_exp64 = nullptr, *lw_tfn64 = nullptr, *sw_exp64 = nullptr;
+  double* lw_tau64 = nullptr;
+  float* lw_tau32 = nullptr;
   double *totplnk = nullptr, *totplnkderiv = nullptr;
   float *totplnk32 = nullptr, *totplnkderiv32 = nullptr;  // FP32 copies (split prep)
   float *lw_tab32 = nullptr, *sw_tab32 = nullptr, *lw_exp32 = nullptr, *lw_tfn32 = nullptr, *sw_exp32 = nullptr;
@@ -134,10 +136,12 @@ struct Carver {
   }
 };
 
-LwWork carve_lw(void* base, int ncol, int nlay, size_t* bytes) {
+// cloudy: also the per-layer cloud fields and the clear-sky band partials
+// (icld = 1); clear-sky calls carve neither.
+LwWork carve_lw(void* base, int ncol, int nlay, size_t* bytes, bool cloudy = false) {
   Carver c{(char*)base};
   const size_t N = (size_t)ncol, L = (size_t)nlay;
-  LwWork w;
+  LwWork w{};
   w.idx = c.take<uint32_t>(L * N);
   w.f = c.take<double>((size_t)LF_N * L * N);
   w.planklay = c.take<double>(16 * L * N);
@@ -150,6 +154,12 @@ LwWork carve_lw(void* base, int ncol, int nlay, size_t* bytes) {
   w.bd = c.take<double>(16 * (L + 1) * N);
   w.bdu = c.take<double>(16 * (L + 1) * N);
   w.colsum = c.take<double>(2 * L * N);
+  if (cloudy) {
+    w.cld = c.take<double>(2 * L * N);
+    w.buc = c.take<double>(16 * (L + 1) * N);
+    w.bdc = c.take<double>(16 * (L + 1) * N);
+    w.bduc = c.take<double>(16 * (L + 1) * N);
+  }
   if (bytes) *bytes = c.off;
   return w;
 }
@@ -182,7 +192,7 @@ int check_dims(rrtmg_gpu_state* h, int ncol, int nlay) {
 template <class F>
 LwWorkT<F> work_as(const LwWork& w) {
   return LwWorkT<F>{w.idx, (F*)w.f, (F*)w.planklay, (F*)w.planklev, (F*)w.plankbnd, (F*)w.dplankbnd, (F*)w.secdiff,
-                    w.laytrop, w.bu, w.bd, w.bdu, w.colsum};
+                    w.laytrop, w.bu, w.bd, w.bdu, w.colsum, (F*)w.cld, w.buc, w.bdc, w.bduc};
 }
 template <class F>
 SwWorkT<F> work_as(const SwWork& w) {
@@ -212,30 +222,44 @@ void mark(rrtmg_gpu_state* h, int fam, int k, cudaStream_t s) {
 int lw_enqueue(rrtmg_gpu_state* h, cudaStream_t s, void* base, int ncol, int nlay, int idrv, const LwIn& in,
                double* uflx, double* dflx, double* hr, double* uflxc, double* dflxc, double* hrc, double* duflx_dt,
                double* duflxc_dt) {
-  LwWork w = carve_lw(base, ncol, nlay, nullptr);
+  // clouds (icld = 1): the call carries cloud arrays
+  const bool cloudy = in.cldfr != nullptr;
+  LwWork w = carve_lw(base, ncol, nlay, nullptr, cloudy);
   mark(h, 0, 0, s);
   const int nb = lw_gpoint_blocks(h->host.lw, ncol, h->precision == RRTMG_PREC_SPLIT);
   if (h->precision == RRTMG_PREC_SPLIT) {
     const LwWorkT<float> w32 = work_as<float>(w);
     launch_lw_prep_split(in, w32, h->totplnk32, h->totplnkderiv32, ncol, nlay, idrv, h->flags, s);
+    if (cloudy) launch_lw_cloud_split(in, w32.cld, ncol, nlay, s);
     mark(h, 0, 1, s);
-    launch_lw_gpoint_split(prep_of(w32), in.emis, in.tauaer, h->lw_tab32, h->lw_exp32, h->lw_tfn32, w.bu, w.bd,
-                           w.bdu, ncol, nlay, idrv, nb, h->analytic, s);
+    if (cloudy)
+      launch_lw_gpoint_cld_split(prep_of(w32), w32.cld, in.taucld, in.emis, in.tauaer, h->lw_tab32, h->lw_exp32,
+                                 h->lw_tfn32, h->lw_tau32, w.bu, w.bd, w.bdu, w.buc, w.bdc, w.bduc, ncol, nlay, idrv,
+                                 nb, h->analytic, s);
+    else
+      launch_lw_gpoint_split(prep_of(w32), in.emis, in.tauaer, h->lw_tab32, h->lw_exp32, h->lw_tfn32, w.bu, w.bd,
+                             w.bdu, ncol, nlay, idrv, nb, h->analytic, s);
   } else {
     launch_lw_prep(in, w, h->totplnk, h->totplnkderiv, ncol, nlay, idrv, h->flags, s);
+    if (cloudy) launch_lw_cloud(in, w.cld, ncol, nlay, s);
     mark(h, 0, 1, s);
-    launch_lw_gpoint_fp64(prep_of(w), in.emis, in.tauaer, h->lw_tab64, h->lw_exp64, h->lw_tfn64, w.bu, w.bd, w.bdu,
-                          ncol, nlay, idrv, nb, h->analytic, s);
+    if (cloudy)
+      launch_lw_gpoint_cld_fp64(prep_of(w), w.cld, in.taucld, in.emis, in.tauaer, h->lw_tab64, h->lw_exp64,
+                                h->lw_tfn64, h->lw_tau64, w.bu, w.bd, w.bdu, w.buc, w.bdc, w.bduc, ncol, nlay, idrv,
+                                nb, h->analytic, s);
+    else
+      launch_lw_gpoint_fp64(prep_of(w), in.emis, in.tauaer, h->lw_tab64, h->lw_exp64, h->lw_tfn64, w.bu, w.bd, w.bdu,
+                            ncol, nlay, idrv, nb, h->analytic, s);
   }
   mark(h, 0, 2, s);
   if (h->precision == RRTMG_PREC_SPLIT)
     launch_lw_finalize_split(w.bu, w.bd, w.bdu, in.plev, ncol, nlay, idrv, uflx, dflx, hr, uflxc, dflxc, hrc,
-                             duflx_dt, duflxc_dt, s);
+                             duflx_dt, duflxc_dt, s, w.buc, w.bdc, w.bduc);
   else
     launch_lw_finalize(w.bu, w.bd, w.bdu, in.plev, ncol, nlay, idrv, uflx, dflx, hr, uflxc, dflxc, hrc, duflx_dt,
-                       duflxc_dt, s);
+                       duflxc_dt, s, w.buc, w.bdc, w.bduc);
   mark(h, 0, 3, s);
-  h->launches += 4;
+  h->launches += cloudy ? 5 : 4;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(h, e, "LW kernel launch");
   return RRTMG_OK;
@@ -244,10 +268,25 @@ int lw_enqueue(rrtmg_gpu_state* h, cudaStream_t s, void* base, int ncol, int nla
 int lw_run(rrtmg_gpu_state* h, cudaStream_t s, int ncol, int nlay, int idrv, const LwIn& in, double* uflx,
            double* dflx, double* hr, double* uflxc, double* dflxc, double* hrc, double* duflx_dt, double* duflxc_dt) {
   size_t need;
-  carve_lw(nullptr, ncol, nlay, &need);
+  carve_lw(nullptr, ncol, nlay, &need, in.cldfr != nullptr);
   int rc = ensure(h, h->lw_ws, need, s);
   if (rc) return rc;
   return lw_enqueue(h, s, h->lw_ws.p, ncol, nlay, idrv, in, uflx, dflx, hr, uflxc, dflxc, hrc, duflx_dt, duflxc_dt);
+}
+
+// Cloud arguments of the LW calls: icld = 0 (clear sky), or icld = 1 (random
+// overlap, rrtmg_lw_rtrn.f90) with the cloud optical depths given
+// (inflglw = 0, rrtmg_lw_cldprop.f90:165-171); icld = 2 / 3 (maximum-random,
+// maximum overlap) and the cloud-physics options inflglw = 1 / 2 are not
+// computed.
+int lw_cloud_args(rrtmg_gpu_state* h, int icld, int inflglw, const double* cldfr, const double* taucld) {
+  if (icld == 0) return RRTMG_OK;
+  if (icld != 1)
+    return fail(h, RRTMG_ERR_UNSUPPORTED, "LW clouds: only random overlap (icld = 1) is computed");
+  if (inflglw != 0)
+    return fail(h, RRTMG_ERR_UNSUPPORTED, "LW clouds: only given cloud optical depths (inflglw = 0) are computed");
+  if (!cldfr || !taucld) return fail(h, RRTMG_ERR_ARG, "icld = 1 needs cldfr and taucld");
+  return RRTMG_OK;
 }
 
 // Incident-flux scaling (inatm_sw, rrtmg_sw_rad.nomcica.f90:953-972): the
@@ -341,6 +380,7 @@ int fork_lw_sw(rrtmg_gpu_state* h, cudaStream_t st, const Fork& fk, LwF&& lw, Sw
 struct HostIn {
   const double* p;  // may be null (optional array)
   size_t rows;
+  size_t per = 1;   // values per column in a row (taucld: 16, band fastest)
 };
 struct HostOut {
   double* p;  // may be null (not requested)
@@ -390,7 +430,7 @@ int host_call(rrtmg_gpu_state* h, int ncol, const HostIn* in, int nin, const Hos
   // staging and scratch per stream, sized for the largest chunk
   size_t stage = 0;
   for (int k = 0; k < nin; ++k)
-    if (in[k].p) stage += align256((size_t)csize * in[k].rows * sizeof(double));
+    if (in[k].p) stage += align256((size_t)csize * in[k].per * in[k].rows * sizeof(double));
   for (int k = 0; k < nout; ++k)
     if (out[k].p) stage += align256((size_t)csize * out[k].rows * sizeof(double));
   cudaStream_t st[2] = {h->stream, h->stream2};
@@ -413,10 +453,12 @@ int host_call(rrtmg_gpu_state* h, int ncol, const HostIn* in, int nin, const Hos
     for (int k = 0; k < nin; ++k) {
       din[k] = nullptr;
       if (!in[k].p) continue;
-      double* d = cv.take<double>((size_t)nc * in[k].rows);
+      const size_t pk = in[k].per;
+      double* d = cv.take<double>((size_t)nc * pk * in[k].rows);
       if (e == cudaSuccess)
-        e = nchunk == 1 ? cudaMemcpyAsync(d, in[k].p, w * in[k].rows, cudaMemcpyHostToDevice, s)
-                        : cudaMemcpy2DAsync(d, w, in[k].p + c0, pitch, w, in[k].rows, cudaMemcpyHostToDevice, s);
+        e = nchunk == 1 ? cudaMemcpyAsync(d, in[k].p, w * pk * in[k].rows, cudaMemcpyHostToDevice, s)
+                        : cudaMemcpy2DAsync(d, w * pk, in[k].p + c0 * pk, pitch * pk, w * pk, in[k].rows,
+                                            cudaMemcpyHostToDevice, s);
       din[k] = d;
     }
     for (int k = 0; k < nout; ++k) dout[k] = out[k].p ? cv.take<double>((size_t)nc * out[k].rows) : nullptr;
@@ -569,6 +611,8 @@ int rrtmg_gpu_init(double cpdair, const char* table_blob, int device, rrtmg_gpu_
   if (e == cudaSuccess) e = upload(&h->sw_tab64, h->host.sw_tab);
   if (e == cudaSuccess) e = upload(&h->lw_exp64, h->host.lw_exp);
   if (e == cudaSuccess) e = upload(&h->lw_tfn64, h->host.lw_tfn);
+  if (e == cudaSuccess) e = upload(&h->lw_tau64, h->host.lw_tau);
+  if (e == cudaSuccess) e = upload(&h->lw_tau32, to_f32(h->host.lw_tau));
   if (e == cudaSuccess) e = upload(&h->sw_exp64, h->host.sw_exp);
   if (e == cudaSuccess) e = upload(&h->totplnk, h->host.totplnk);
   if (e == cudaSuccess) e = upload(&h->totplnkderiv, h->host.totplnkderiv);
@@ -603,6 +647,7 @@ int rrtmg_gpu_finalize(rrtmg_gpu_handle h) {
   if (h->side) cudaStreamSynchronize(h->side);
   if (h->side2) cudaStreamSynchronize(h->side2);
   void* ptrs[] = {h->lw_tab64, h->sw_tab64, h->lw_exp64, h->lw_tfn64, h->sw_exp64, h->totplnk, h->totplnkderiv,
+                  h->lw_tau64, h->lw_tau32,
                   h->totplnk32, h->totplnkderiv32,
                   h->lw_tab32, h->sw_tab32, h->lw_exp32, h->lw_tfn32, h->sw_exp32, h->flags, h->lw_ws.p,
                   h->sw_ws.p, h->adj_ws.p, h->hio[0].p, h->hio[1].p, h->hws[0].p, h->hws[1].p, h->run_ws.p,
@@ -690,12 +735,12 @@ int rrtmg_lw_dev(rrtmg_gpu_handle h, void* stream, int ncol, int nlay, int icld,
                  const double* cldfr, const double* taucld, const double* cicewp, const double* cliqwp,
                  const double* reice, const double* reliq, const double* tauaer, double* uflx, double* dflx,
                  double* hr, double* uflxc, double* dflxc, double* hrc, double* duflx_dt, double* duflxc_dt) {
-  (void)inflglw; (void)iceflglw; (void)liqflglw; (void)cldfr; (void)taucld; (void)cicewp; (void)cliqwp;
-  (void)reice; (void)reliq;
+  (void)iceflglw; (void)liqflglw; (void)reice; (void)reliq;
   if (!valid_handle(h)) return RRTMG_ERR_ARG;
   int rc = check_dims(h, ncol, nlay);
   if (rc) return rc;
-  if (icld != 0) return fail(h, RRTMG_ERR_UNSUPPORTED, "only clear sky (icld = 0) is computed");
+  rc = lw_cloud_args(h, icld, inflglw, cldfr, taucld);
+  if (rc) return rc;
   if (idrv != 0 && idrv != 1) return fail(h, RRTMG_ERR_UNSUPPORTED, "idrv must be 0 or 1");
   if (!play || !plev || !tlay || !tlev || !tsfc || !h2ovmr || !o3vmr || !co2vmr || !uflx || !dflx || !hr ||
       !uflxc || !dflxc || !hrc)
@@ -704,6 +749,12 @@ int rrtmg_lw_dev(rrtmg_gpu_handle h, void* stream, int ncol, int nlay, int icld,
   cudaSetDevice(h->device);
   LwIn in{play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr, cfc11vmr, cfc12vmr,
           cfc22vmr, ccl4vmr, emis, tauaer};
+  if (icld == 1) {
+    in.cldfr = cldfr;
+    in.taucld = taucld;
+    in.cicewp = cicewp;
+    in.cliqwp = cliqwp;
+  }
   return lw_run(h, (cudaStream_t)stream, ncol, nlay, idrv, in, uflx, dflx, hr, uflxc, dflxc, hrc, duflx_dt,
                 duflxc_dt);
 }
@@ -841,33 +892,38 @@ int rrtmg_lw_c(rrtmg_gpu_handle h, int ncol, int nlay, int icld, int idrv, const
                const double* cicewp, const double* cliqwp, const double* reice, const double* reliq,
                const double* tauaer, double* uflx, double* dflx, double* hr, double* uflxc, double* dflxc,
                double* hrc, double* duflx_dt, double* duflxc_dt) {
+  (void)iceflglw; (void)liqflglw; (void)reice; (void)reliq;
   if (!valid_handle(h)) return RRTMG_ERR_ARG;
   int rc = check_dims(h, ncol, nlay);
   if (rc) return rc;
-  if (icld != 0) return fail(h, RRTMG_ERR_UNSUPPORTED, "only clear sky (icld = 0) is computed");
+  rc = lw_cloud_args(h, icld, inflglw, cldfr, taucld);
+  if (rc) return rc;
   if (idrv != 0 && idrv != 1) return fail(h, RRTMG_ERR_UNSUPPORTED, "idrv must be 0 or 1");
   if (!play || !plev || !tlay || !tlev || !tsfc || !h2ovmr || !o3vmr || !co2vmr || !uflx || !dflx || !hr ||
       !uflxc || !dflxc || !hrc)
     return fail(h, RRTMG_ERR_ARG, "a required array pointer is null");
   if (idrv == 1 && !duflx_dt) return fail(h, RRTMG_ERR_ARG, "idrv = 1 needs duflx_dt");
   cudaSetDevice(h->device);
+  const bool cloudy = icld == 1;
   const size_t L = nlay, Lv = nlay + 1;
-  const HostIn in[17] = {{play, L}, {plev, Lv}, {tlay, L}, {tlev, Lv}, {tsfc, 1}, {h2ovmr, L}, {o3vmr, L},
+  const HostIn in[21] = {{play, L}, {plev, Lv}, {tlay, L}, {tlev, Lv}, {tsfc, 1}, {h2ovmr, L}, {o3vmr, L},
                          {co2vmr, L}, {ch4vmr, L}, {n2ovmr, L}, {o2vmr, L}, {cfc11vmr, L}, {cfc12vmr, L},
-                         {cfc22vmr, L}, {ccl4vmr, L}, {emis, 16}, {tauaer, 16 * L}};
+                         {cfc22vmr, L}, {ccl4vmr, L}, {emis, 16}, {tauaer, 16 * L},
+                         {cloudy ? cldfr : nullptr, L}, {cloudy ? taucld : nullptr, L, 16},
+                         {cloudy ? cicewp : nullptr, L}, {cloudy ? cliqwp : nullptr, L}};
   const HostOut out[8] = {{uflx, Lv}, {dflx, Lv}, {hr, L}, {uflxc, Lv}, {dflxc, Lv}, {hrc, L},
                           {idrv == 1 ? duflx_dt : nullptr, Lv}, {idrv == 1 ? duflxc_dt : nullptr, Lv}};
   auto need = [&](int nc) {
     size_t b;
-    carve_lw(nullptr, nc, nlay, &b);
+    carve_lw(nullptr, nc, nlay, &b, cloudy);
     return b;
   };
   auto enq = [&](cudaStream_t s, void* ws, int nc, const double* const* d, double* const* o) {
     LwIn li{d[0], d[1], d[2], d[3], d[4], d[5], d[6], d[7], d[8], d[9], d[10], d[11], d[12], d[13], d[14], d[15],
-            d[16]};
+            d[16], d[17], d[18], d[19], d[20]};
     return lw_enqueue(h, s, ws, nc, nlay, idrv, li, o[0], o[1], o[2], o[3], o[4], o[5], o[6], o[7]);
   };
-  return host_call(h, ncol, in, 17, out, 8, need, enq, "copy LW arrays");
+  return host_call(h, ncol, in, 21, out, 8, need, enq, "copy LW arrays");
 }
 
 int rrtmg_sw_c(rrtmg_gpu_handle h, int ncol, int nlay, int icld, int iaer, const double* play, const double* plev,

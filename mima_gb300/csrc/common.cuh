@@ -53,45 +53,18 @@ enum SwField {
   SF_FAC11, SF_SELFFAC, SF_SELFFRAC, SF_FORFAC, SF_FORFRAC, SF_N
 };
 
-// Table gather (k-distribution and transmittance tables, read-only, reused by
-// every cell of a band): through the read-only path; with
-// RRTMG_TAB_EVICT_LAST, with the L1 "evict last" priority, so that the
-// solvers' per-thread layer arrays streaming through L1 evict the tables last.
+// Table gather (k-distribution and transmittance tables: read-only and reused
+// by every cell of a band) and per-layer prep-field load: the read-only path.
+// L1 eviction-priority variants of both (tables evict-last, fields
+// evict-first) and a TMA prefetch of each block's band tables into L2 were
+// measured on GB300 and changed neither solver's time.
 template <class T>
 __device__ __forceinline__ T tld(const T* p) {
-#ifdef RRTMG_TAB_EVICT_LAST
-  if constexpr (sizeof(T) == 4) {
-    float v;
-    asm("ld.global.nc.L1::evict_last.f32 %0, [%1];" : "=f"(v) : "l"(p));
-    return v;
-  } else {
-    double v;
-    asm("ld.global.nc.L1::evict_last.f64 %0, [%1];" : "=d"(v) : "l"(p));
-    return v;
-  }
-#else
   return __ldg(p);
-#endif
 }
-
-// Per-layer prep field of one (layer, column), read once per layer by the
-// lanes of the column: through the read-only path; with
-// RRTMG_FIELD_EVICT_FIRST, with the L1 "evict first" priority.
 template <class T>
 __device__ __forceinline__ T fld_ld(const T* p) {
-#ifdef RRTMG_FIELD_EVICT_FIRST
-  if constexpr (sizeof(T) == 4) {
-    float v;
-    asm("ld.global.nc.L1::evict_first.f32 %0, [%1];" : "=f"(v) : "l"(p));
-    return v;
-  } else {
-    double v;
-    asm("ld.global.nc.L1::evict_first.f64 %0, [%1];" : "=d"(v) : "l"(p));
-    return v;
-  }
-#else
   return __ldg(p);
-#endif
 }
 
 // Packed integer interpolation indices of one layer.
@@ -173,6 +146,9 @@ using SwPrep = SwPrepT<double>;
 struct LwIn {
   const double *play, *plev, *tlay, *tlev, *tsfc, *h2o, *o3, *co2, *ch4, *n2o, *o2, *cfc11, *cfc12, *cfc22, *ccl4,
       *emis, *tauaer;
+  // clouds (icld = 1, inflglw = 0), null in clear sky: cldfr (ncol, nlay),
+  // taucld (16, ncol, nlay), cicewp / cliqwp (ncol, nlay) or null
+  const double *cldfr, *taucld, *cicewp, *cliqwp;
 };
 template <class F>
 struct LwWorkT {
@@ -181,6 +157,11 @@ struct LwWorkT {
   int* laytrop;
   double *bu, *bd, *bdu;  // band partials [band][lev][col]
   double* colsum;         // per-layer coldry and wk1 [2][lay][col] for the column sums
+  // clouds only (null in clear sky): per layer [cloud fraction of a cloudy
+  // layer, else 0][cldprop's 0/1 optical-depth mask] and the clear-sky band
+  // partials
+  F* cld;
+  double *buc, *bdc, *bduc;
 };
 using LwWork = LwWorkT<double>;
 struct SwIn {

@@ -539,6 +539,250 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
   }
 }
 
+// ---------------------------------------------------------------------------
+// LW g-point solver with clouds, random overlap (icld = 1, cloud optical
+// depths given): rrtmg_lw_rtrn.f90:302-520 for one g-point.  A layer is
+// cloudy when its cloud fraction is >= 1e-6 (cld[0] holds it, 0 otherwise);
+// its cloud optical depth is secdiff * taucld where cldprop keeps taucld
+// (cld[1] = 1, rrtmg_lw_cldprop.f90:167-174), else 0.  The clear-sky stream
+// follows the total stream until the first cloudy layer from the top and is
+// computed on its own above the surface once the column holds a cloud.
+// Total and clear-sky level radiances are summed over the band's g-points
+// into their own band partials.
+// ---------------------------------------------------------------------------
+template <int B, class R, int MAXL>
+__device__ __forceinline__ void lw_band_cld(const LwPrepT<R>& p, const R* __restrict__ cld,
+                                            const double* __restrict__ taucld, const double* __restrict__ emis,
+                                            const double* __restrict__ tauaer, const R* __restrict__ tab,
+                                            const R* __restrict__ exptbl, const R* __restrict__ tfntbl,
+                                            const R* __restrict__ tautbl, double* __restrict__ bu,
+                                            double* __restrict__ bd, double* __restrict__ bdu,
+                                            double* __restrict__ buc, double* __restrict__ bdc,
+                                            double* __restrict__ bduc, int ncol, int nlay, int idrv, bool analytic,
+                                            int blk, float* sbuf) {
+  const bool IDRV = idrv == 1;
+  constexpr bool SPLIT = sizeof(R) == 4;
+  constexpr int NG = lw_ng(B);
+  constexpr int W = split_lanes(NG, SPLIT);
+  constexpr int CPW = 32 / W;
+  constexpr int CPB = (kBlock / 32) * CPW;
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int lane_col = wib * CPW + lane / W, g = lane % W;
+  const int col = blk * CPB + lane_col;
+  const bool valid = lane < CPW * W && col < ncol;
+  const bool active = valid && g < NG;
+  const int c = valid ? col : (col < ncol ? col : ncol - 1);
+  const int gg = g < NG ? g : NG - 1;
+  const size_t N = (size_t)ncol;
+  const int lt = p.laytrop[c];
+  const R secdiff = p.secdiff[(B - 1) * N + c];
+  const R bpade = (R)c_lw.bpade;
+  const R rec_6 = (R)0.166667;
+  const size_t fstride = (size_t)nlay * N;
+  R atrans[MAXL], bbugas[MAXL], atot[MAXL], bbutot[MAXL], efcl[MAXL];
+  // transmittance, tau transition function and the optical depth of a table
+  // entry (exp_tbl, tfn_tbl, tau_tbl), or with the analytic functions, of od
+  auto tbl = [&](R od, R& trans, R& tfn, R& odq) {
+    if (analytic) {
+      trans = exp(-od);
+      tfn = (R)1. - (R)2. * (((R)1. / od) - (trans / ((R)1. - trans)));
+      odq = od;
+    } else {
+      const R tblind = od / (bpade + od);
+      int it = (int)((R)10000.0 * tblind + (R)0.5);
+      it = it < 0 ? 0 : (it > kNTbl ? kNTbl : it);
+      trans = tld(exptbl + it);
+      tfn = tld(tfntbl + it);
+      odq = tld(tautbl + it);
+    }
+  };
+  const size_t bo = (size_t)(B - 1) * (nlay + 1) * N;
+  // streams: downward 0 total, 1 clear; upward 0 total, 1 clear, 2 / 3 their
+  // surface-temperature derivatives (idrv = 1)
+  double* dst_dn[2] = {bd + bo, bdc + bo};
+  double* dst_up[4] = {bu + bo, buc + bo, IDRV ? bdu + bo : nullptr, IDRV ? bduc + bo : nullptr};
+  const int wcol0 = blk * CPB + wib * CPW;
+  GSum<W, NG, 4, false> gs{sbuf + (SPLIT ? wib * kStageRows * kRow : 0), nullptr, lane, 0, nlay - 1, -1, 2};
+  auto store_dn = [&](int b, int lev, int cs, double v) {
+    const int cc = wcol0 + cs;
+    if (cc < ncol) dst_dn[b][(size_t)lev * N + cc] = v;
+  };
+  auto store_up = [&](int b, int lev, int cs, double v) {
+    const int cc = wcol0 + cs;
+    if (cc < ncol && dst_up[b]) dst_up[b][(size_t)lev * N + cc] = v;
+  };
+  // FP64 path: the band's level sums by warp shuffles
+  auto sum_dn = [&](int b, int lev, R v) {
+    const double s = seg_sum<W>(active ? (double)v : 0.0);
+    if (g == 0 && valid) dst_dn[b][(size_t)lev * N + col] = s;
+  };
+  auto sum_up = [&](int b, int lev, R v) {
+    const double s = seg_sum<W>(active ? (double)v : 0.0);
+    if (g == 0 && valid && dst_up[b]) dst_up[b][(size_t)lev * N + col] = s;
+  };
+  // no downward radiance enters at the top
+  if (g == 0 && valid) {
+    dst_dn[0][(size_t)nlay * N + col] = 0.0;
+    dst_dn[1][(size_t)nlay * N + col] = 0.0;
+  }
+  R radld = (R)0., radclrd = (R)0., fracs1 = (R)0.;
+  bool iclddn = false;
+  uint32_t idx_next = __ldg(p.idx + (size_t)(nlay - 1) * N + c);
+  for (int lev = nlay; lev >= 1; --lev) {
+    const size_t o = (size_t)(lev - 1) * N + c;
+    const Idx ix = unpack_idx(idx_next);
+    if (lev > 1) idx_next = __ldg(p.idx + o - N);
+    LwLayerView<R> L{p.f, fstride, o};
+    R taug, fracs;
+    lw_gas<B, R>(c_lw, lw_rconst<R>(), L, ix, lev <= lt, gg, tab, taug, fracs);
+    R taut = taug;
+    if (tauaer) taut = taug + (R)__ldg(tauaer + c + N * ((size_t)(lev - 1) + (size_t)nlay * (B - 1)));
+    const R plfrac = fracs;
+    const R blay = __ldg(p.planklay + ((size_t)(B - 1) * nlay + (lev - 1)) * N + c);
+    const R dplankup = __ldg(p.planklev + ((size_t)(B - 1) * (nlay + 1) + lev) * N + c) - blay;
+    const R dplankdn = __ldg(p.planklev + ((size_t)(B - 1) * (nlay + 1) + lev - 1) * N + c) - blay;
+    R odepth = secdiff * taut;
+    if (odepth < (R)0.0) odepth = (R)0.0;
+    const R cf = __ldg(cld + o);
+    R atr, bbd, bbu, at = (R)0., bbut = (R)0., ef = (R)0.;
+    if (cf > (R)0.) {  // cloudy layer (rtrn :350-416)
+      iclddn = true;
+      const R odcld = secdiff * (__ldg(cld + fstride + o) * (R)__ldg(taucld + (B - 1) + 16 * o));
+      const R transcld = exp(-odcld);
+      ef = ((R)1. - transcld) * cf;
+      R odtot = odepth + odcld;
+      R gassrc, bbdtot;
+      if (odtot < (R)0.06) {
+        atr = odepth - (R)0.5 * odepth * odepth;
+        const R odepth_rec = rec_6 * odepth;
+        gassrc = plfrac * (blay + dplankdn * odepth_rec) * atr;
+        at = odtot - (R)0.5 * odtot * odtot;
+        const R odtot_rec = rec_6 * odtot;
+        bbdtot = plfrac * (blay + dplankdn * odtot_rec);
+        bbd = plfrac * (blay + dplankdn * odepth_rec);
+        bbu = plfrac * (blay + dplankup * odepth_rec);
+        bbut = plfrac * (blay + dplankup * odtot_rec);
+      } else if (odepth <= (R)0.06) {
+        atr = odepth - (R)0.5 * odepth * odepth;
+        const R odepth_rec = rec_6 * odepth;
+        gassrc = plfrac * (blay + dplankdn * odepth_rec) * atr;
+        R ttot, tfactot, odq;
+        tbl(odtot, ttot, tfactot, odq);
+        bbdtot = plfrac * (blay + tfactot * dplankdn);
+        bbd = plfrac * (blay + dplankdn * odepth_rec);
+        at = (R)1. - ttot;
+        bbu = plfrac * (blay + dplankup * odepth_rec);
+        bbut = plfrac * (blay + tfactot * dplankup);
+      } else {
+        R tgas, tfacgas, odq;
+        tbl(odepth, tgas, tfacgas, odq);
+        odepth = odq;  // tau_tbl(itgas)
+        atr = (R)1. - tgas;
+        gassrc = atr * plfrac * (blay + tfacgas * dplankdn);
+        odtot = odepth + odcld;
+        R ttot, tfactot, odq2;
+        tbl(odtot, ttot, tfactot, odq2);
+        bbdtot = plfrac * (blay + tfactot * dplankdn);
+        bbd = plfrac * (blay + tfacgas * dplankdn);
+        at = (R)1. - ttot;
+        bbu = plfrac * (blay + tfacgas * dplankup);
+        bbut = plfrac * (blay + tfactot * dplankup);
+      }
+      radld = radld - radld * (atr + ef * ((R)1. - atr)) + gassrc + cf * (bbdtot * at - gassrc);
+    } else {  // clear layer (rtrn :418-436)
+      if (odepth <= (R)0.06) {
+        atr = odepth - (R)0.5 * odepth * odepth;
+        odepth = rec_6 * odepth;
+        bbd = plfrac * (blay + dplankdn * odepth);
+        bbu = plfrac * (blay + dplankup * odepth);
+      } else {
+        R transc, tausfac, odq;
+        tbl(odepth, transc, tausfac, odq);
+        atr = (R)1. - transc;
+        bbd = plfrac * (blay + tausfac * dplankdn);
+        bbu = plfrac * (blay + tausfac * dplankup);
+      }
+      radld = radld + (bbd - radld) * atr;
+    }
+    atrans[lev - 1] = atr;
+    bbugas[lev - 1] = bbu;
+    atot[lev - 1] = at;
+    bbutot[lev - 1] = bbut;
+    efcl[lev - 1] = ef;
+    // clear-sky stream (:441-448)
+    if (iclddn)
+      radclrd = radclrd + (bbd - radclrd) * atr;
+    else
+      radclrd = radld;
+    if constexpr (SPLIT) {
+      gs.put(0, radld);
+      gs.put(1, radclrd);
+      gs.next(store_dn);
+    } else {
+      sum_dn(0, lev - 1, radld);
+      sum_dn(1, lev - 1, radclrd);
+    }
+    if (lev == 1) fracs1 = fracs;
+  }
+  if constexpr (SPLIT) {
+    if (gs.n) gs.flush(store_dn);
+    gs.first = 0;
+    gs.dir = 1;
+    gs.nb = IDRV ? 4 : 2;
+  }
+  const R semiss = emis ? (R)__ldg(emis + c + N * (B - 1)) : (R)1.0;
+  const R rad0 = fracs1 * __ldg(p.plankbnd + (B - 1) * N + c);
+  const R reflect = (R)1. - semiss;
+  R radlu = rad0 + reflect * radld;
+  R radclru = rad0 + reflect * radclrd;
+  R dlu = (R)0., dluc = (R)0.;
+  if (IDRV) {
+    dlu = fracs1 * __ldg(p.dplankbnd + (B - 1) * N + c);
+    dluc = dlu;
+  }
+  auto emit = [&](int lev) {
+    if constexpr (SPLIT) {
+      gs.put(0, radlu);
+      gs.put(1, radclru);
+      gs.put(2, dlu);
+      gs.put(3, dluc);
+      gs.next(store_up);
+    } else {
+      sum_up(0, lev, radlu);
+      sum_up(1, lev, radclru);
+      if (IDRV) {
+        sum_up(2, lev, dlu);
+        sum_up(3, lev, dluc);
+      }
+    }
+  };
+  emit(0);
+  for (int lev = 1; lev <= nlay; ++lev) {  // rtrn :478-520
+    const R atr = atrans[lev - 1];
+    const R cf = __ldg(cld + (size_t)(lev - 1) * N + c);
+    if (cf > (R)0.) {
+      const R gassrc = bbugas[lev - 1] * atr;
+      const R at = atot[lev - 1];
+      radlu = radlu - radlu * (atr + efcl[lev - 1] * ((R)1. - atr)) + gassrc + cf * (bbutot[lev - 1] * at - gassrc);
+      if (IDRV) dlu = dlu * cf * ((R)1.0 - at) + dlu * ((R)1.0 - cf) * ((R)1.0 - atr);
+    } else {
+      radlu = radlu + (bbugas[lev - 1] - radlu) * atr;
+      if (IDRV) dlu = dlu * ((R)1.0 - atr);
+    }
+    if (iclddn) {
+      radclru = radclru + (bbugas[lev - 1] - radclru) * atr;
+      if (IDRV) dluc = dluc * ((R)1.0 - atr);
+    } else {
+      radclru = radlu;
+      dluc = dlu;
+    }
+    emit(lev);
+  }
+  if constexpr (SPLIT) {
+    if (gs.n) gs.flush(store_up);
+  }
+}
+
 // Blocks of a band for `lanes` lanes per column: 32 / lanes columns per warp.
 __host__ __device__ inline int lw_blocks_for_band(int lanes, int ncol) {
   const int cpb = (kBlock / 32) * (32 / lanes);
@@ -589,17 +833,79 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_LW_MINB :
 #undef RRTMG_LW_CASE
 }
 
+// Cloudy LW g-point kernel (icld = 1): as lw_gpoint_kernel, with
+// lw_band_cld.  FL < 0: analytic and idrv as passed (FP64 path); FL >= 0:
+// compile-time flags (bit 0 analytic, bit 1 idrv; split path).
+template <class R, int MAXL, int FL>
+__global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_LW_MINB : 1)
+    lw_gpoint_cld_kernel(LwPrepT<R> p, const R* __restrict__ cld, const double* __restrict__ taucld,
+                         const double* __restrict__ emis, const double* __restrict__ tauaer,
+                         const R* __restrict__ tab, const R* __restrict__ exptbl, const R* __restrict__ tfntbl,
+                         const R* __restrict__ tautbl, double* bu, double* bd, double* bdu, double* buc, double* bdc,
+                         double* bduc, int ncol, int nlay, int idrv, int analytic) {
+  __shared__ float sbuf[sizeof(R) == 4 ? kGSumFloats : 1];
+  int blk = blockIdx.x, band = 0;
+  for (; band < kLwBands; ++band) {
+    const int nb = lw_blocks_for_band(split_lanes(c_lw.band[band].ng, sizeof(R) == 4), ncol);
+    if (blk < nb) break;
+    blk -= nb;
+  }
+  const bool an = FL < 0 ? analytic != 0 : (FL & 1) != 0;
+  const int idv = FL < 0 ? idrv : ((FL & 2) ? 1 : 0);
+#define RRTMG_LW_CASE(b)                                                                                            \
+  case b - 1:                                                                                                      \
+    lw_band_cld<b, R, MAXL>(p, cld, taucld, emis, tauaer, tab, exptbl, tfntbl, tautbl, bu, bd, bdu, buc, bdc, bduc, \
+                            ncol, nlay, idv, an, blk, sbuf);                                                       \
+    break;
+  switch (band) {
+    RRTMG_LW_CASE(1) RRTMG_LW_CASE(2) RRTMG_LW_CASE(3) RRTMG_LW_CASE(4) RRTMG_LW_CASE(5) RRTMG_LW_CASE(6)
+    RRTMG_LW_CASE(7) RRTMG_LW_CASE(8) RRTMG_LW_CASE(9) RRTMG_LW_CASE(10) RRTMG_LW_CASE(11) RRTMG_LW_CASE(12)
+    RRTMG_LW_CASE(13) RRTMG_LW_CASE(14) RRTMG_LW_CASE(15) RRTMG_LW_CASE(16)
+    default: break;
+  }
+#undef RRTMG_LW_CASE
+}
+
 #ifdef RRTMG_DEFINE_COLUMN_KERNELS
+// ---------------------------------------------------------------------------
+// Clouds of the LW call (icld = 1, cloud optical depths given), one thread per
+// (column, layer): inatm's cldfrac / tauc (rrtmg_lw_rad.nomcica.f90:866-888),
+// rtrn's cloudy-layer test cldfrac >= 1e-6 (rrtmg_lw_rtrn.f90:302-315) and
+// cldprop's rule for keeping the optical depths, cldfrac >= cldmin and
+// (ciwp + clwp >= cldmin or the band-summed depth >= cldmin), cldmin = 1e-20
+// (rrtmg_lw_cldprop.f90:155-174).  cld[0][lay][col]: the cloud fraction of a
+// cloudy layer, else 0; cld[1][lay][col]: 1 where the depths are kept, else 0.
+// ---------------------------------------------------------------------------
+template <class F>
+__global__ void __launch_bounds__(128) lw_cloud_kernel(LwIn in, F* __restrict__ cld, int ncol, int nlay) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncol) return;
+  const size_t o = (size_t)blockIdx.y * ncol + col;
+  const double cf = __ldg(in.cldfr + o);
+  double tauctot = 0.0;
+  for (int ib = 0; ib < kLwBands; ++ib) tauctot = tauctot + __ldg(in.taucld + ib + 16 * o);
+  const double cwp = (in.cicewp ? __ldg(in.cicewp + o) : 0.0) + (in.cliqwp ? __ldg(in.cliqwp + o) : 0.0);
+  const double cldmin = 1.e-20;
+  const bool kept = cf >= cldmin && (cwp >= cldmin || tauctot >= cldmin);
+  cld[o] = cf >= 1.e-6 ? (F)cf : (F)0;
+  cld[(size_t)nlay * ncol + o] = kept ? (F)1 : (F)0;
+}
+
 // ---------------------------------------------------------------------------
 // LW finalize: band sums (rrtmg_lw_rtrnmr.f90:720-746), fluxes and heating
 // (:752-776); clear-sky outputs equal the total ones in clear sky.
 // ---------------------------------------------------------------------------
+// buc, bdc, bduc: the clear-sky band partials of a cloudy call (rtrn's clear
+// stream), else null (clear sky: the clear-sky outputs are the total ones).
 __global__ void __launch_bounds__(128) lw_finalize_kernel(const double* __restrict__ bu, const double* __restrict__ bd,
                                                           const double* __restrict__ bdu,
                                                           const double* __restrict__ plev, int ncol, int nlay,
                                                           int idrv, double* uflx, double* dflx, double* hr,
                                                           double* uflxc, double* dflxc, double* hrc,
-                                                          double* duflx_dt, double* duflxc_dt) {
+                                                          double* duflx_dt, double* duflxc_dt,
+                                                          const double* __restrict__ buc = nullptr,
+                                                          const double* __restrict__ bdc = nullptr,
+                                                          const double* __restrict__ bduc = nullptr) {
   // one thread per (column, level); the heating of the layer below the level
   // re-forms the band sums of the level below (same order, same rounding)
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
@@ -608,41 +914,54 @@ __global__ void __launch_bounds__(128) lw_finalize_kernel(const double* __restri
   const LwConst& C = c_lw;
   const size_t N = (size_t)ncol;
   const double wtdiff = 0.5;
-  auto sums = [&](int lv, double& tu, double& td) {
+  auto sums = [&](const double* u, const double* d, int lv, double& tu, double& td) {
     tu = 0.0;
     td = 0.0;
     for (int b = 0; b < kLwBands; ++b) {
       const size_t o = ((size_t)b * (nlay + 1) + lv) * N + col;
-      tu = tu + (__ldg(bu + o) * wtdiff) * C.band[b].delwave;
-      td = td + (__ldg(bd + o) * wtdiff) * C.band[b].delwave;
+      tu = tu + (__ldg(u + o) * wtdiff) * C.band[b].delwave;
+      td = td + (__ldg(d + o) * wtdiff) * C.band[b].delwave;
     }
     tu = tu * C.fluxfac;
     td = td * C.fluxfac;
   };
-  double tu, td;
-  sums(lev, tu, td);
-  const size_t oo = (size_t)lev * N + col;
-  uflx[oo] = tu;
-  dflx[oo] = td;
-  uflxc[oo] = tu;
-  dflxc[oo] = td;
-  if (idrv == 1) {
+  auto dsum = [&](const double* du) {
     double tdu = 0.0;
     for (int b = 0; b < kLwBands; ++b) {
       const size_t o = ((size_t)b * (nlay + 1) + lev) * N + col;
-      tdu = tdu + (__ldg(bdu + o) * wtdiff) * C.band[b].delwave * C.fluxfac;
+      tdu = tdu + (__ldg(du + o) * wtdiff) * C.band[b].delwave * C.fluxfac;
     }
+    return tdu;
+  };
+  const bool clear_own = buc != nullptr;
+  double tu, td, tuc, tdc;
+  sums(bu, bd, lev, tu, td);
+  if (clear_own) sums(buc, bdc, lev, tuc, tdc);
+  else tuc = tu, tdc = td;
+  const size_t oo = (size_t)lev * N + col;
+  uflx[oo] = tu;
+  dflx[oo] = td;
+  uflxc[oo] = tuc;
+  dflxc[oo] = tdc;
+  if (idrv == 1) {
+    const double tdu = dsum(bdu);
     if (duflx_dt) duflx_dt[oo] = tdu;
-    if (duflxc_dt) duflxc_dt[oo] = tdu;
+    if (duflxc_dt) duflxc_dt[oo] = clear_own ? dsum(bduc) : tdu;
   }
   if (lev >= 1) {
+    const double dp = __ldg(plev + oo - N) - __ldg(plev + oo);
     double tu0, td0;
-    sums(lev - 1, tu0, td0);
-    const double fnet_prev = tu0 - td0, fnet = tu - td;
-    const double h = C.heatfac * (fnet_prev - fnet) / (__ldg(plev + oo - N) - __ldg(plev + oo));
+    sums(bu, bd, lev - 1, tu0, td0);
+    const double h = C.heatfac * ((tu0 - td0) - (tu - td)) / dp;
     const size_t oh = (size_t)(lev - 1) * N + col;
     hr[oh] = h;
-    hrc[oh] = h;
+    if (clear_own) {
+      double tuc0, tdc0;
+      sums(buc, bdc, lev - 1, tuc0, tdc0);
+      hrc[oh] = C.heatfac * ((tuc0 - tdc0) - (tuc - tdc)) / dp;
+    } else {
+      hrc[oh] = h;
+    }
   }
 }
 

@@ -50,11 +50,32 @@ void launch_lw_gpoint_fp64(const LwPrep& p, const double* emis, const double* ta
     lw_gpoint_kernel<double, 208><<<nb, kBlock, 0, s>>>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv, analytic);
 }
 
+void launch_lw_gpoint_cld_fp64(const LwPrep& p, const double* cld, const double* taucld, const double* emis,
+                               const double* tauaer, const double* tab, const double* exptbl, const double* tfntbl,
+                               const double* tautbl, double* bu, double* bd, double* bdu, double* buc, double* bdc,
+                               double* bduc, int ncol, int nlay, int idrv, int nb, int analytic, cudaStream_t s) {
+  if (maxl_for(nlay) == 64)
+    lw_gpoint_cld_kernel<double, 64, -1><<<nb, kBlock, 0, s>>>(p, cld, taucld, emis, tauaer, tab, exptbl, tfntbl, tautbl,
+                                                              bu, bd, bdu, buc, bdc, bduc, ncol, nlay, idrv, analytic);
+  else
+    lw_gpoint_cld_kernel<double, 208, -1><<<nb, kBlock, 0, s>>>(p, cld, taucld, emis, tauaer, tab, exptbl, tfntbl,
+                                                               tautbl, bu, bd, bdu, buc, bdc, bduc, ncol, nlay, idrv,
+                                                               analytic);
+}
+
+void launch_lw_cloud(const LwIn& in, double* cld, int ncol, int nlay, cudaStream_t s) {
+  lw_cloud_kernel<double><<<dim3((ncol + 127) / 128, nlay), 128, 0, s>>>(in, cld, ncol, nlay);
+}
+void launch_lw_cloud_split(const LwIn& in, float* cld, int ncol, int nlay, cudaStream_t s) {
+  lw_cloud_kernel<float><<<dim3((ncol + 127) / 128, nlay), 128, 0, s>>>(in, cld, ncol, nlay);
+}
+
 void launch_lw_finalize(const double* bu, const double* bd, const double* bdu, const double* plev, int ncol, int nlay,
                         int idrv, double* uflx, double* dflx, double* hr, double* uflxc, double* dflxc, double* hrc,
-                        double* duflx_dt, double* duflxc_dt, cudaStream_t s) {
+                        double* duflx_dt, double* duflxc_dt, cudaStream_t s, const double* buc, const double* bdc,
+                        const double* bduc) {
   lw_finalize_kernel<<<dim3((ncol + 127) / 128, nlay + 1), 128, 0, s>>>(bu, bd, bdu, plev, ncol, nlay, idrv, uflx, dflx, hr, uflxc,
-                                                        dflxc, hrc, duflx_dt, duflxc_dt);
+                                                        dflxc, hrc, duflx_dt, duflxc_dt, buc, bdc, bduc);
 }
 
 void launch_sw_prep(const SwIn& in, const SwWork& w, int ncol, int nlay, unsigned* flags, cudaStream_t s) {

@@ -35,13 +35,17 @@ cudaError_t upload_constants_split(const LwConst& lw, const SwConst& sw) {
 // ---------------------------------------------------------------------------
 constexpr int kLevChunk = 8;
 
+// buc, bdc, bduc: the clear-sky band partials of a cloudy call, else null.
 __global__ void __launch_bounds__(128) lw_finalize_split_kernel(const double* __restrict__ bu,
                                                                 const double* __restrict__ bd,
                                                                 const double* __restrict__ bdu,
                                                                 const double* __restrict__ plev, int ncol, int nlay,
                                                                 int idrv, double* uflx, double* dflx, double* hr,
                                                                 double* uflxc, double* dflxc, double* hrc,
-                                                                double* duflx_dt, double* duflxc_dt) {
+                                                                double* duflx_dt, double* duflxc_dt,
+                                                                const double* __restrict__ buc,
+                                                                const double* __restrict__ bdc,
+                                                                const double* __restrict__ bduc) {
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= ncol) return;
   const int lev0 = blockIdx.y * kLevChunk, lev1 = min(nlay, lev0 + kLevChunk - 1);
@@ -63,28 +67,37 @@ __global__ void __launch_bounds__(128) lw_finalize_split_kernel(const double* __
     for (int k = 0; k < kLwBands; ++k) x = fma(__ldg(a + k * bs + o), c_lw_bandw[k], x);
     return x;
   };
-  double tu0 = 0.0, td0 = 0.0;
-  if (lev0 >= 1) sums(bu, bd, lev0 - 1, tu0, td0);
+  const bool clear_own = buc != nullptr;
+  double tu0 = 0.0, td0 = 0.0, tuc0 = 0.0, tdc0 = 0.0;
+  if (lev0 >= 1) {
+    sums(bu, bd, lev0 - 1, tu0, td0);
+    if (clear_own) sums(buc, bdc, lev0 - 1, tuc0, tdc0);
+  }
   for (int lev = lev0; lev <= lev1; ++lev) {
-    double tu, td;
+    double tu, td, tuc, tdc;
     sums(bu, bd, lev, tu, td);
+    if (clear_own) sums(buc, bdc, lev, tuc, tdc);
+    else tuc = tu, tdc = td;
     const size_t oo = (size_t)lev * N + col;
     uflx[oo] = tu;
     dflx[oo] = td;
-    uflxc[oo] = tu;
-    dflxc[oo] = td;
+    uflxc[oo] = tuc;
+    dflxc[oo] = tdc;
     if (idrv == 1) {
       const double tdu = sum1(bdu, lev);
       if (duflx_dt) duflx_dt[oo] = tdu;
-      if (duflxc_dt) duflxc_dt[oo] = tdu;
+      if (duflxc_dt) duflxc_dt[oo] = clear_own ? sum1(bduc, lev) : tdu;
     }
     if (lev >= 1) {
-      const double h = c_lw.heatfac * ((tu0 - td0) - (tu - td)) / (__ldg(plev + oo - N) - __ldg(plev + oo));
+      const double dp = __ldg(plev + oo - N) - __ldg(plev + oo);
+      const double h = c_lw.heatfac * ((tu0 - td0) - (tu - td)) / dp;
       hr[oo - N] = h;
-      hrc[oo - N] = h;
+      hrc[oo - N] = clear_own ? c_lw.heatfac * ((tuc0 - tdc0) - (tuc - tdc)) / dp : h;
     }
     tu0 = tu;
     td0 = td;
+    tuc0 = tuc;
+    tdc0 = tdc;
   }
 }
 
@@ -134,10 +147,11 @@ __global__ void __launch_bounds__(128) sw_finalize_split_kernel(const double* __
 
 void launch_lw_finalize_split(const double* bu, const double* bd, const double* bdu, const double* plev, int ncol,
                               int nlay, int idrv, double* uflx, double* dflx, double* hr, double* uflxc,
-                              double* dflxc, double* hrc, double* duflx_dt, double* duflxc_dt, cudaStream_t s) {
+                              double* dflxc, double* hrc, double* duflx_dt, double* duflxc_dt, cudaStream_t s,
+                              const double* buc, const double* bdc, const double* bduc) {
   const dim3 g((ncol + 127) / 128, (nlay + 1 + kLevChunk - 1) / kLevChunk);
   lw_finalize_split_kernel<<<g, 128, 0, s>>>(bu, bd, bdu, plev, ncol, nlay, idrv, uflx, dflx, hr, uflxc, dflxc, hrc,
-                                             duflx_dt, duflxc_dt);
+                                             duflx_dt, duflxc_dt, buc, bdc, bduc);
 }
 
 void launch_sw_finalize_split(const double* su, const double* sd, const double* plev, const double* coszen, int ncol,
@@ -168,6 +182,33 @@ void launch_lw_gpoint_split(const LwPrepT<float>& p, const double* emis, const d
     lw_split_flags<64>(fl, nb, s, p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv, analytic);
   else
     lw_split_flags<208>(fl, nb, s, p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv, analytic);
+}
+
+// Cloudy LW (icld = 1): instantiated per (analytic, idrv) flag pair.
+template <int MAXL>
+static void lw_split_cld_flags(int fl, int nb, cudaStream_t s, const LwPrepT<float>& p, const float* cld,
+                               const double* taucld, const double* emis, const double* tauaer, const float* tab,
+                               const float* exptbl, const float* tfntbl, const float* tautbl, double* bu, double* bd,
+                               double* bdu, double* buc, double* bdc, double* bduc, int ncol, int nlay) {
+  auto k = fl == 0 ? lw_gpoint_cld_kernel<float, MAXL, 0>
+         : fl == 1 ? lw_gpoint_cld_kernel<float, MAXL, 1>
+         : fl == 2 ? lw_gpoint_cld_kernel<float, MAXL, 2>
+                   : lw_gpoint_cld_kernel<float, MAXL, 3>;
+  k<<<nb, kBlock, 0, s>>>(p, cld, taucld, emis, tauaer, tab, exptbl, tfntbl, tautbl, bu, bd, bdu, buc, bdc, bduc, ncol,
+                          nlay, 0, 0);
+}
+
+void launch_lw_gpoint_cld_split(const LwPrepT<float>& p, const float* cld, const double* taucld, const double* emis,
+                                const double* tauaer, const float* tab, const float* exptbl, const float* tfntbl,
+                                const float* tautbl, double* bu, double* bd, double* bdu, double* buc, double* bdc,
+                                double* bduc, int ncol, int nlay, int idrv, int nb, int analytic, cudaStream_t s) {
+  const int fl = (analytic ? 1 : 0) | (idrv == 1 ? 2 : 0);
+  if (maxl_for(nlay) == 64)
+    lw_split_cld_flags<64>(fl, nb, s, p, cld, taucld, emis, tauaer, tab, exptbl, tfntbl, tautbl, bu, bd, bdu, buc,
+                           bdc, bduc, ncol, nlay);
+  else
+    lw_split_cld_flags<208>(fl, nb, s, p, cld, taucld, emis, tauaer, tab, exptbl, tfntbl, tautbl, bu, bd, bdu, buc,
+                            bdc, bduc, ncol, nlay);
 }
 
 template <int MAXL>

@@ -21,9 +21,22 @@ void launch_lw_prep(const LwIn& in, const LwWork& w, const double* totplnk, cons
 void launch_lw_gpoint_fp64(const LwPrep& p, const double* emis, const double* tauaer, const double* tab,
                            const double* exptbl, const double* tfntbl, double* bu, double* bd, double* bdu, int ncol,
                            int nlay, int idrv, int nb, int analytic, cudaStream_t s);
+// buc, bdc, bduc: clear-sky band partials of a cloudy call, or null (clear sky).
 void launch_lw_finalize(const double* bu, const double* bd, const double* bdu, const double* plev, int ncol, int nlay,
                         int idrv, double* uflx, double* dflx, double* hr, double* uflxc, double* dflxc, double* hrc,
-                        double* duflx_dt, double* duflxc_dt, cudaStream_t s);
+                        double* duflx_dt, double* duflxc_dt, cudaStream_t s, const double* buc = nullptr,
+                        const double* bdc = nullptr, const double* bduc = nullptr);
+// Clouds (icld = 1): per-layer cloud fields, FP64 and FP32 storage.
+void launch_lw_cloud(const LwIn& in, double* cld, int ncol, int nlay, cudaStream_t s);
+void launch_lw_cloud_split(const LwIn& in, float* cld, int ncol, int nlay, cudaStream_t s);
+void launch_lw_gpoint_cld_fp64(const LwPrep& p, const double* cld, const double* taucld, const double* emis,
+                               const double* tauaer, const double* tab, const double* exptbl, const double* tfntbl,
+                               const double* tautbl, double* bu, double* bd, double* bdu, double* buc, double* bdc,
+                               double* bduc, int ncol, int nlay, int idrv, int nb, int analytic, cudaStream_t s);
+void launch_lw_gpoint_cld_split(const LwPrepT<float>& p, const float* cld, const double* taucld, const double* emis,
+                                const double* tauaer, const float* tab, const float* exptbl, const float* tfntbl,
+                                const float* tautbl, double* bu, double* bd, double* bdu, double* buc, double* bdc,
+                                double* bduc, int ncol, int nlay, int idrv, int nb, int analytic, cudaStream_t s);
 void launch_sw_prep(const SwIn& in, const SwWork& w, int ncol, int nlay, unsigned* flags, cudaStream_t s);
 // Prep for the FP32-split solvers: the same steps in FP32 arithmetic (FP32 Planck
 // tables), fields stored as float.
@@ -39,7 +52,8 @@ void launch_sw_finalize(const double* su, const double* sd, const double* plev, 
 // Split-path finalize: the same outputs with fewer FP64 operations (kernels_split.cu).
 void launch_lw_finalize_split(const double* bu, const double* bd, const double* bdu, const double* plev, int ncol,
                               int nlay, int idrv, double* uflx, double* dflx, double* hr, double* uflxc,
-                              double* dflxc, double* hrc, double* duflx_dt, double* duflxc_dt, cudaStream_t s);
+                              double* dflxc, double* hrc, double* duflx_dt, double* duflxc_dt, cudaStream_t s,
+                              const double* buc = nullptr, const double* bdc = nullptr, const double* bduc = nullptr);
 void launch_sw_finalize_split(const double* su, const double* sd, const double* plev, const double* coszen, int ncol,
                               int nlay, double* swuflx, double* swdflx, double* swhr, double* swuflxc,
                               double* swdflxc, double* swhrc, cudaStream_t s);

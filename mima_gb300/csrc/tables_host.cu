@@ -350,6 +350,13 @@ std::string build_host_tables(const char* blob_path, double cpdair, HostTables& 
     T.lw.fluxfac = (2.0 * std::asin(1.0)) * 2.e4;
     T.lw.bpade = 1.0 / 0.278;
     lookup_tables(T.lw_exp, &T.lw_tfn, T.lw.bpade);
+    // tau_tbl: the optical depth each entry stands for (0 and 1e10 at the ends)
+    T.lw_tau.assign(kNTbl + 1, 0.0);
+    T.lw_tau[kNTbl] = 1.e10;
+    for (int itr = 1; itr < kNTbl; ++itr) {
+      const double tfn = (double)itr / (double)kNTbl;
+      T.lw_tau[itr] = T.lw.bpade * tfn / (1.0 - tfn);
+    }
   }
 
   // ---------------- SW ----------------

@@ -11,6 +11,7 @@ namespace rrtmg {
 struct HostTables {
   std::vector<double> lw_tab, sw_tab;           // reduced band tables, g fastest
   std::vector<double> lw_exp, lw_tfn, sw_exp;   // 0..10000 lookup tables
+  std::vector<double> lw_tau;                   // optical depth of each LW table entry (rrtmg_lw_init.f90:115-122)
   std::vector<double> totplnk, totplnkderiv;    // (181, 16) Fortran order
   LwConst lw;
   SwConst sw;

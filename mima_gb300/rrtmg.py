@@ -157,6 +157,8 @@ def array_sizes(ncol, nlay):
     n.update({k: ncol for k in _PER_COLUMN})
     n.update(emis=16 * ncol, tauaer_lw=16 * nlay * ncol, tauaer=14 * nlay * ncol, ssaaer=14 * nlay * ncol,
              asmaer=14 * nlay * ncol)
+    # LW clouds: cldfr, cicewp, cliqwp (nlay, ncol); taucld Fortran (16, ncol, nlay)
+    n.update(cldfr=nlay * ncol, cicewp=nlay * ncol, cliqwp=nlay * ncol, taucld=16 * nlay * ncol)
     return n
 
 
@@ -231,10 +233,13 @@ class RRTMG:
     # ---------------- host-array drop-ins ----------------
     def rrtmg_lw(self, ncol, nlay, icld, idrv, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr,
                  ch4vmr=None, n2ovmr=None, o2vmr=None, cfc11vmr=None, cfc12vmr=None, cfc22vmr=None,
-                 ccl4vmr=None, emis=None, tauaer=None, check=True, out=None):
+                 ccl4vmr=None, emis=None, tauaer=None, check=True, out=None, inflglw=0, cldfr=None, taucld=None,
+                 cicewp=None, cliqwp=None):
         """rrtmg_lw on host arrays; returns uflx, dflx, hr, uflxc, dflxc, hrc (+ duflx_dt, duflxc_dt).
         ``out`` optionally supplies the output arrays (float64, C-contiguous;
-        page-locked arrays let the library overlap copies with kernels)."""
+        page-locked arrays let the library overlap copies with kernels).
+        Clouds (icld = 1, inflglw = 0): cldfr, cicewp, cliqwp (nlay, ncol),
+        taucld (nlay, ncol, 16) = Fortran (16, ncol, nlay)."""
         L, N = nlay, ncol
         ins = [_host(a) for a in (play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr,
                                   cfc11vmr, cfc12vmr, cfc22vmr, ccl4vmr, emis)]
@@ -243,9 +248,10 @@ class RRTMG:
             shapes.update(duflx_dt=L + 1, duflxc_dt=L + 1)
         out = _outputs(out, shapes, N)
         ta = _host(tauaer)
+        cl = [_host(a) for a in (cldfr, taucld, cicewp, cliqwp)]
         rc = self.lib.rrtmg_lw_c(
             self._h, C.c_int(N), C.c_int(L), C.c_int(icld), C.c_int(idrv), *[_hp(a) for a in ins],
-            C.c_int(0), C.c_int(0), C.c_int(0), None, None, None, None, None, None, _hp(ta),
+            C.c_int(inflglw), C.c_int(0), C.c_int(0), *[_hp(a) for a in cl], None, None, _hp(ta),
             _hp(out["uflx"]), _hp(out["dflx"]), _hp(out["hr"]), _hp(out["uflxc"]), _hp(out["dflxc"]),
             _hp(out["hrc"]), _hp(out.get("duflx_dt")), _hp(out.get("duflxc_dt")))
         out["status"] = rc
@@ -274,10 +280,14 @@ class RRTMG:
         return out
 
     # Convenience: whole Atmosphere objects (mima_gb300.atmosphere)
-    def lw(self, atm, idrv=0, tauaer=None, check=True):
-        return self.rrtmg_lw(atm.ncol, atm.nlay, 0, idrv, atm.play, atm.plev, atm.tlay, atm.tlev, atm.tsfc,
-                             atm.h2o, atm.o3, atm.co2, atm.ch4, atm.n2o, atm.o2, atm.cfc11, atm.cfc12, atm.cfc22,
-                             atm.ccl4, atm.emis, tauaer, check=check)
+    def lw(self, atm, idrv=0, tauaer=None, check=True, cloud=None):
+        """``cloud``: dict(cldfr, taucld[, cicewp, cliqwp]) for icld = 1 (random
+        overlap, given cloud optical depths), as rrtmg_lw's arguments."""
+        cl = cloud or {}
+        return self.rrtmg_lw(atm.ncol, atm.nlay, 1 if cloud else 0, idrv, atm.play, atm.plev, atm.tlay, atm.tlev,
+                             atm.tsfc, atm.h2o, atm.o3, atm.co2, atm.ch4, atm.n2o, atm.o2, atm.cfc11, atm.cfc12,
+                             atm.cfc22, atm.ccl4, atm.emis, tauaer, check=check, cldfr=cl.get("cldfr"),
+                             taucld=cl.get("taucld"), cicewp=cl.get("cicewp"), cliqwp=cl.get("cliqwp"))
 
     def sw(self, atm, iaer=0, tauaer=None, ssaaer=None, asmaer=None, check=True):
         return self.rrtmg_sw(atm.ncol, atm.nlay, 0, iaer, atm.play, atm.plev, atm.tlay, atm.tlev, atm.tsfc,
@@ -306,9 +316,9 @@ class RRTMG:
             self._h, C.c_void_p(stream or 0), C.c_int(ncol), C.c_int(nlay), C.c_int(icld), C.c_int(idrv),
             g("play"), g("plev"), g("tlay"), g("tlev"), g("tsfc"), g("h2ovmr"), g("o3vmr"), g("co2vmr"),
             g("ch4vmr"), g("n2ovmr"), g("o2vmr"), g("cfc11vmr"), g("cfc12vmr"), g("cfc22vmr"), g("ccl4vmr"),
-            g("emis"), C.c_int(0), C.c_int(0), C.c_int(0), None, None, None, None, None, None,
-            g("tauaer_lw", tauaer), o("uflx"), o("dflx"), o("hr"), o("uflxc"), o("dflxc"), o("hrc"), o("duflx_dt"),
-            o("duflxc_dt"))
+            g("emis"), C.c_int(0), C.c_int(0), C.c_int(0), g("cldfr"), g("taucld"), g("cicewp"), g("cliqwp"),
+            None, None, g("tauaer_lw", tauaer), o("uflx"), o("dflx"), o("hr"), o("uflxc"), o("dflxc"), o("hrc"),
+            o("duflx_dt"), o("duflxc_dt"))
         self._check(rc)
 
     def set_profiling(self, on: bool):

@@ -68,8 +68,11 @@ def _f(a):
     return np.ascontiguousarray(a, dtype=np.float64)
 
 
-def rrtmg_lw(atm, idrv: int = 0, tauaer=None, nthreads: int = 0):
-    """Clear-sky rrtmg_lw on ``atm``; returns dict of (nlev, ncol) arrays."""
+def rrtmg_lw(atm, idrv: int = 0, tauaer=None, nthreads: int = 0, cloud=None):
+    """rrtmg_lw on ``atm``; returns dict of (nlev, ncol) arrays.  Clear sky, or
+    with ``cloud`` = dict(cldfr=(nlay, ncol), taucld=(nlay, ncol, 16) [Fortran
+    (16, ncol, nlay)], optional cicewp / cliqwp (nlay, ncol)): icld = 1
+    (random overlap), cloud optical depths given (inflglw = 0)."""
     n, L = atm.ncol, atm.nlay
     out = {k: np.zeros((L + 1, n)) for k in ("uflx", "dflx", "uflxc", "dflxc", "duflx_dt", "duflxc_dt")}
     out.update({k: np.zeros((L, n)) for k in ("hr", "hrc")})
@@ -77,10 +80,13 @@ def rrtmg_lw(atm, idrv: int = 0, tauaer=None, nthreads: int = 0):
             _f(atm.o3), _f(atm.co2), _f(atm.ch4), _f(atm.n2o), _f(atm.o2), _f(atm.cfc11),
             _f(atm.cfc12), _f(atm.cfc22), _f(atm.ccl4), _f(atm.emis),
             None if tauaer is None else _f(tauaer)]
-    rc = _lib.orc_rrtmg_lw(C.c_int(n), C.c_int(L), C.c_int(0), C.c_int(idrv), *[_p(a) for a in args],
+    cl = cloud or {}
+    carg = [None if cl.get(k) is None else _f(cl[k]) for k in ("cldfr", "taucld", "cicewp", "cliqwp")]
+    rc = _lib.orc_rrtmg_lw(C.c_int(n), C.c_int(L), C.c_int(1 if cloud else 0), C.c_int(idrv),
+                           *[_p(a) for a in args],
                            _p(out["uflx"]), _p(out["dflx"]), _p(out["hr"]), _p(out["uflxc"]),
                            _p(out["dflxc"]), _p(out["hrc"]), _p(out["duflx_dt"]), _p(out["duflxc_dt"]),
-                           C.c_int(nthreads))
+                           C.c_int(nthreads), *[_p(a) for a in carg])
     if rc != 0:
         raise RuntimeError(f"orc_rrtmg_lw failed ({rc})")
     return out

@@ -52,11 +52,17 @@ int orc_rrtmg_lw(int ncol, int nlay, int icld, int idrv, const double* play, con
                  const double* o2vmr, const double* cfc11vmr, const double* cfc12vmr, const double* cfc22vmr,
                  const double* ccl4vmr, const double* emis, const double* tauaer, double* uflx, double* dflx,
                  double* hr, double* uflxc, double* dflxc, double* hrc, double* duflx_dt, double* duflxc_dt,
-                 int nthreads) {
+                 int nthreads, const double* cldfr, const double* taucld, const double* cicewp,
+                 const double* cliqwp) {
   if (!g_ready) return 2;
-  if (icld != 0) return 3;
+  if (icld != 0 && !(icld == 1 && cldfr && taucld)) return 3;
   LwInput in{ncol, nlay, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr,
              cfc11vmr, cfc12vmr, cfc22vmr, ccl4vmr, emis, tauaer};
+  in.icld = icld;
+  in.cldfr = cldfr;
+  in.taucld = taucld;
+  in.cicewp = cicewp;
+  in.cliqwp = cliqwp;
 #pragma omp parallel num_threads(nthreads > 0 ? nthreads : orc_max_threads())
   {
     LwColumn c;
@@ -68,17 +74,17 @@ int orc_rrtmg_lw(int ncol, int nlay, int icld, int idrv, const double* play, con
         size_t ix = (size_t)iplon + (size_t)ncol * (size_t)k;
         uflx[ix] = o.totu[k];
         dflx[ix] = o.totd[k];
-        uflxc[ix] = o.totu[k];
-        dflxc[ix] = o.totd[k];
+        uflxc[ix] = o.totuc[k];
+        dflxc[ix] = o.totdc[k];
         if (idrv == 1 && duflx_dt) {
           duflx_dt[ix] = o.dtotu_dt[k];
-          if (duflxc_dt) duflxc_dt[ix] = o.dtotu_dt[k];
+          if (duflxc_dt) duflxc_dt[ix] = o.dtotuc_dt[k];
         }
       }
       for (int k = 0; k < nlay; ++k) {
         size_t ix = (size_t)iplon + (size_t)ncol * (size_t)k;
         hr[ix] = o.htr[k];
-        hrc[ix] = o.htr[k];
+        hrc[ix] = o.htrc[k];
       }
     }
   }

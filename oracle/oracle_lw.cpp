@@ -1,5 +1,7 @@
 // CPU oracle, longwave -- TEST INFRASTRUCTURE ONLY (the checker, never the
-// product).  FP64 restatement of the reference's clear-sky RRTMG_LW path:
+// product).  FP64 restatement of the reference's RRTMG_LW path (clear sky,
+// and clouds with random overlap and given cloud optical depths: icld = 1,
+// inflglw = 0 -- cldprop rrtmg_lw_cldprop.f90:155-174, rtrn rrtmg_lw_rtrn.f90):
 //   inatm    rrtmg_lw_rad.nomcica.f90:572-901
 //   setcoef  rrtmg_lw_setcoef.f90:31-415
 //   taumol   rrtmg_lw_taumol.f90:31-3149 (taugb1..16)
@@ -142,6 +144,22 @@ void lw_inatm(const LwInput& in, int iplon, LwColumn& c) {
   for (int l = 1; l <= nlay; ++l)
     for (int ib = 1; ib <= 16; ++ib)
       c.taua[ib][l] = in.tauaer ? in.tauaer[(size_t)iplon + (size_t)ncol * ((size_t)(l - 1) + (size_t)nlay * (size_t)(ib - 1))] : 0.0;
+  // Clouds (:866-888): cldfrac(l) = cldfr(iplon,l), tauc(n,l) = taucld(n,iplon,l);
+  // then cldprop with inflag = 0 (rrtmg_lw_cldprop.f90:155-174): a layer's
+  // cloud optical depths are taken when cldfrac >= cldmin and the condensed
+  // water path or the band-summed optical depth is >= cldmin (1e-20), else 0.
+  if (in.icld >= 1) {
+    const double cldmin = 1.e-20;
+    for (int l = 1; l <= nlay; ++l) {
+      const size_t o = (size_t)iplon + (size_t)ncol * (size_t)(l - 1);
+      c.cldfrac[l] = in.cldfr[o];
+      double tauctot = 0.0;
+      for (int ib = 1; ib <= 16; ++ib) tauctot = tauctot + in.taucld[(size_t)(ib - 1) + 16 * o];
+      const double cwp = (in.cicewp ? in.cicewp[o] : 0.0) + (in.cliqwp ? in.cliqwp[o] : 0.0);
+      const bool cloudy = c.cldfrac[l] >= cldmin && (cwp >= cldmin || tauctot >= cldmin);
+      for (int ib = 1; ib <= 16; ++ib) c.taucloud[ib][l] = cloudy ? in.taucld[(size_t)(ib - 1) + 16 * o] : 0.0;
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1175,6 +1193,253 @@ void lw_rtrnmr(LwColumn& c, int idrv, LwOut& out) {
   out.dtotu_dt = dtotu_dt;
 }
 
+// ---------------------------------------------------------------------------
+// rtrn: random cloud overlap (icld = 1), rrtmg_lw_rtrn.f90:32-590.  A layer
+// is cloudy when cldfrac >= 1e-6 (:302-315); its cloud optical depth
+// secdiff * taucloud gives the effective cloud fraction (1 - e^{-odcld})
+// cldfrac.  The clear-sky stream follows the total stream until the first
+// cloudy layer from the top (iclddn, :441-448) and is computed on its own
+// everywhere above the surface once a column holds a cloud (:500-512).
+// ---------------------------------------------------------------------------
+void lw_rtrn(LwColumn& c, int idrv, LwOut& out) {
+  const LwTables& T = g_lw;
+  const int nl = c.nlayers;
+  const double wtdiff = 0.5, rec_6 = 0.166667;
+  static const double a0[17] = {0, 1.66, 1.55, 1.58, 1.66, 1.54, 1.454, 1.89, 1.33, 1.668, 1.66, 1.66, 1.66, 1.66, 1.66, 1.66, 1.66};
+  static const double a1[17] = {0, 0.00, 0.25, 0.22, 0.00, 0.13, 0.446, -0.10, 0.40, -0.006, 0.00, 0.00, 0.00, 0.00, 0.00, 0.00, 0.00};
+  static const double a2[17] = {0, 0.00, -12.0, -11.7, 0.00, -0.72, -0.243, 0.19, -0.062, 0.414, 0.00, 0.00, 0.00, 0.00, 0.00, 0.00, 0.00};
+  double secdiff[17];
+  for (int ibnd = 1; ibnd <= 16; ++ibnd) {
+    if (ibnd == 1 || ibnd == 4 || ibnd >= 10) {
+      secdiff[ibnd] = 1.66;
+    } else {
+      secdiff[ibnd] = a0[ibnd] + a1[ibnd] * std::exp(a2[ibnd] * c.pwvcm);
+      if (secdiff[ibnd] > 1.80) secdiff[ibnd] = 1.80;
+      if (secdiff[ibnd] < 1.50) secdiff[ibnd] = 1.50;
+    }
+  }
+  // cloud optical depth and effective cloud fraction per layer and band (:302-315)
+  std::vector<int> icldlyr(nl + 1, 0);
+  std::vector<double> odcld[17], efclfrac[17];
+  for (int ib = 1; ib <= 16; ++ib) {
+    odcld[ib].assign(nl + 1, 0.0);
+    efclfrac[ib].assign(nl + 1, 0.0);
+  }
+  for (int lay = 1; lay <= nl; ++lay)
+    for (int ib = 1; ib <= 16; ++ib) {
+      if (c.cldfrac[lay] >= 1.e-6) {
+        odcld[ib][lay] = secdiff[ib] * c.taucloud[ib][lay];
+        const double transcld = std::exp(-odcld[ib][lay]);
+        const double abscld = 1. - transcld;
+        efclfrac[ib][lay] = abscld * c.cldfrac[lay];
+        icldlyr[lay] = 1;
+      } else {
+        icldlyr[lay] = 0;
+      }
+    }
+  // the transmittance function and the optical depth of a table entry, or
+  // (analytic mode) of the optical depth itself
+  auto tbl = [&](double od, double& trans, double& tfn, double& odq) {
+    if (g_table_mode) {
+      const double tblind = od / (T.bpade + od);
+      const int it = (int)(10000.0 * tblind + 0.5);
+      trans = T.exp_tbl[it];
+      tfn = T.tfn_tbl[it];
+      odq = T.tau_tbl[it];
+    } else {
+      trans = std::exp(-od);
+      tfn = 1. - 2. * ((1. / od) - (trans / (1. - trans)));
+      odq = od;
+    }
+  };
+  std::vector<double> urad(nl + 1, 0.0), drad(nl + 1, 0.0), totu(nl + 1, 0.0), totd(nl + 1, 0.0);
+  std::vector<double> clru(nl + 1, 0.0), clrd(nl + 1, 0.0), totuc(nl + 1, 0.0), totdc(nl + 1, 0.0);
+  std::vector<double> d_urad(nl + 1, 0.0), d_clru(nl + 1, 0.0), dtotu_dt(nl + 1, 0.0), dtotuc_dt(nl + 1, 0.0);
+  std::vector<double> atrans(nl + 1), bbugas(nl + 1), atot(nl + 1), bbutot(nl + 1);
+  int igc = 1;
+  for (int iband = 1; iband <= 16; ++iband) {
+    const int ib = iband;  // ncbands = 16: ipat(iband, 2) = iband
+    for (; igc <= T.ngs[iband]; ++igc) {
+      double radld = 0., radclrd = 0.;
+      int iclddn = 0;
+      for (int lev = nl; lev >= 1; --lev) {
+        const double plfrac = c.fracs[igc][lev];
+        const double blay = c.planklay[iband][lev];
+        const double dplankup = c.planklev[iband][lev] - blay;
+        const double dplankdn = c.planklev[iband][lev - 1] - blay;
+        double odepth = secdiff[iband] * c.taut[igc][lev];
+        if (odepth < 0.0) odepth = 0.0;
+        double bbd;
+        if (icldlyr[lev] == 1) {  // :350-416
+          iclddn = 1;
+          double odtot = odepth + odcld[ib][lev];
+          double gassrc, bbdtot;
+          if (odtot < 0.06) {
+            atrans[lev] = odepth - 0.5 * odepth * odepth;
+            const double odepth_rec = rec_6 * odepth;
+            gassrc = plfrac * (blay + dplankdn * odepth_rec) * atrans[lev];
+            atot[lev] = odtot - 0.5 * odtot * odtot;
+            const double odtot_rec = rec_6 * odtot;
+            bbdtot = plfrac * (blay + dplankdn * odtot_rec);
+            bbd = plfrac * (blay + dplankdn * odepth_rec);
+            bbugas[lev] = plfrac * (blay + dplankup * odepth_rec);
+            bbutot[lev] = plfrac * (blay + dplankup * odtot_rec);
+          } else if (odepth <= 0.06) {
+            atrans[lev] = odepth - 0.5 * odepth * odepth;
+            const double odepth_rec = rec_6 * odepth;
+            gassrc = plfrac * (blay + dplankdn * odepth_rec) * atrans[lev];
+            odtot = odepth + odcld[ib][lev];
+            double ttot, tfactot, odq;
+            tbl(odtot, ttot, tfactot, odq);
+            bbdtot = plfrac * (blay + tfactot * dplankdn);
+            bbd = plfrac * (blay + dplankdn * odepth_rec);
+            atot[lev] = 1. - ttot;
+            bbugas[lev] = plfrac * (blay + dplankup * odepth_rec);
+            bbutot[lev] = plfrac * (blay + tfactot * dplankup);
+          } else {
+            double tgas, tfacgas, odq;
+            tbl(odepth, tgas, tfacgas, odq);
+            odepth = odq;  // odepth = tau_tbl(itgas)
+            atrans[lev] = 1. - tgas;
+            gassrc = atrans[lev] * plfrac * (blay + tfacgas * dplankdn);
+            odtot = odepth + odcld[ib][lev];
+            double ttot, tfactot, odq2;
+            tbl(odtot, ttot, tfactot, odq2);
+            bbdtot = plfrac * (blay + tfactot * dplankdn);
+            bbd = plfrac * (blay + tfacgas * dplankdn);
+            atot[lev] = 1. - ttot;
+            bbugas[lev] = plfrac * (blay + tfacgas * dplankup);
+            bbutot[lev] = plfrac * (blay + tfactot * dplankup);
+          }
+          radld = radld - radld * (atrans[lev] + efclfrac[ib][lev] * (1. - atrans[lev])) + gassrc +
+                  c.cldfrac[lev] * (bbdtot * atot[lev] - gassrc);
+          drad[lev - 1] = drad[lev - 1] + radld;
+        } else {  // clear layer (:418-436), as rtrnmr
+          if (odepth <= 0.06) {
+            atrans[lev] = odepth - 0.5 * odepth * odepth;
+            odepth = rec_6 * odepth;
+            bbd = plfrac * (blay + dplankdn * odepth);
+            bbugas[lev] = plfrac * (blay + dplankup * odepth);
+          } else {
+            double transc, tausfac, odq;
+            tbl(odepth, transc, tausfac, odq);
+            atrans[lev] = 1. - transc;
+            bbd = plfrac * (blay + tausfac * dplankdn);
+            bbugas[lev] = plfrac * (blay + tausfac * dplankup);
+          }
+          radld = radld + (bbd - radld) * atrans[lev];
+          drad[lev - 1] = drad[lev - 1] + radld;
+        }
+        if (iclddn == 1) {  // :441-448
+          radclrd = radclrd + (bbd - radclrd) * atrans[lev];
+          clrd[lev - 1] = clrd[lev - 1] + radclrd;
+        } else {
+          radclrd = radld;
+          clrd[lev - 1] = drad[lev - 1];
+        }
+      }
+      const double rad0 = c.fracs[igc][1] * c.plankbnd[iband];
+      const double reflect = 1. - c.semiss[iband];
+      double radlu = rad0 + reflect * radld;
+      double radclru = rad0 + reflect * radclrd;
+      urad[0] = urad[0] + radlu;
+      clru[0] = clru[0] + radclru;
+      double d_radlu_dt = 0.0, d_radclru_dt = 0.0;
+      if (idrv == 1) {
+        const double d_rad0_dt = c.fracs[igc][1] * c.dplankbnd_dt[iband];
+        d_radlu_dt = d_rad0_dt;
+        d_urad[0] = d_urad[0] + d_radlu_dt;
+        d_radclru_dt = d_rad0_dt;
+        d_clru[0] = d_clru[0] + d_radclru_dt;
+      }
+      for (int lev = 1; lev <= nl; ++lev) {  // :478-520
+        if (icldlyr[lev] == 1) {
+          const double gassrc = bbugas[lev] * atrans[lev];
+          radlu = radlu - radlu * (atrans[lev] + efclfrac[ib][lev] * (1. - atrans[lev])) + gassrc +
+                  c.cldfrac[lev] * (bbutot[lev] * atot[lev] - gassrc);
+          urad[lev] = urad[lev] + radlu;
+          if (idrv == 1) {
+            d_radlu_dt = d_radlu_dt * c.cldfrac[lev] * (1.0 - atot[lev]) +
+                         d_radlu_dt * (1.0 - c.cldfrac[lev]) * (1.0 - atrans[lev]);
+            d_urad[lev] = d_urad[lev] + d_radlu_dt;
+          }
+        } else {
+          radlu = radlu + (bbugas[lev] - radlu) * atrans[lev];
+          urad[lev] = urad[lev] + radlu;
+          if (idrv == 1) {
+            d_radlu_dt = d_radlu_dt * (1.0 - atrans[lev]);
+            d_urad[lev] = d_urad[lev] + d_radlu_dt;
+          }
+        }
+        if (iclddn == 1) {
+          radclru = radclru + (bbugas[lev] - radclru) * atrans[lev];
+          clru[lev] = clru[lev] + radclru;
+        } else {
+          radclru = radlu;
+          clru[lev] = urad[lev];
+        }
+        if (idrv == 1) {
+          if (iclddn == 1) {
+            d_radclru_dt = d_radclru_dt * (1.0 - atrans[lev]);
+            d_clru[lev] = d_clru[lev] + d_radclru_dt;
+          } else {
+            d_radclru_dt = d_radlu_dt;
+            d_clru[lev] = d_urad[lev];
+          }
+        }
+      }
+    }
+    for (int lev = nl; lev >= 0; --lev) {  // :526-543
+      const double uflux = urad[lev] * wtdiff, dflux = drad[lev] * wtdiff;
+      urad[lev] = 0.0;
+      drad[lev] = 0.0;
+      totu[lev] = totu[lev] + uflux * T.delwave[iband];
+      totd[lev] = totd[lev] + dflux * T.delwave[iband];
+      const double uclfl = clru[lev] * wtdiff, dclfl = clrd[lev] * wtdiff;
+      clru[lev] = 0.0;
+      clrd[lev] = 0.0;
+      totuc[lev] = totuc[lev] + uclfl * T.delwave[iband];
+      totdc[lev] = totdc[lev] + dclfl * T.delwave[iband];
+    }
+    if (idrv == 1) {
+      for (int lev = nl; lev >= 0; --lev) {
+        const double duflux_dt = d_urad[lev] * wtdiff;
+        d_urad[lev] = 0.0;
+        dtotu_dt[lev] = dtotu_dt[lev] + duflux_dt * T.delwave[iband] * T.fluxfac;
+        const double duclfl_dt = d_clru[lev] * wtdiff;
+        d_clru[lev] = 0.0;
+        dtotuc_dt[lev] = dtotuc_dt[lev] + duclfl_dt * T.delwave[iband] * T.fluxfac;
+      }
+    }
+  }
+  std::vector<double> fnet(nl + 1), fnetc(nl + 1);
+  totu[0] = totu[0] * T.fluxfac;
+  totd[0] = totd[0] * T.fluxfac;
+  fnet[0] = totu[0] - totd[0];
+  totuc[0] = totuc[0] * T.fluxfac;
+  totdc[0] = totdc[0] * T.fluxfac;
+  fnetc[0] = totuc[0] - totdc[0];
+  out.htr.assign(nl + 1, 0.0);
+  out.htrc.assign(nl + 1, 0.0);
+  for (int lev = 1; lev <= nl; ++lev) {
+    totu[lev] = totu[lev] * T.fluxfac;
+    totd[lev] = totd[lev] * T.fluxfac;
+    fnet[lev] = totu[lev] - totd[lev];
+    totuc[lev] = totuc[lev] * T.fluxfac;
+    totdc[lev] = totdc[lev] * T.fluxfac;
+    fnetc[lev] = totuc[lev] - totdc[lev];
+    const int l = lev - 1;
+    out.htr[l] = T.heatfac * (fnet[l] - fnet[lev]) / (c.pz[l] - c.pz[lev]);
+    out.htrc[l] = T.heatfac * (fnetc[l] - fnetc[lev]) / (c.pz[l] - c.pz[lev]);
+  }
+  out.totu = totu;
+  out.totd = totd;
+  out.dtotu_dt = dtotu_dt;
+  out.totuc = totuc;
+  out.totdc = totdc;
+  out.dtotuc_dt = dtotuc_dt;
+}
+
 void lw_column(const LwInput& in, int iplon, int idrv, LwColumn& c, LwOut& out) {
   lw_inatm(in, iplon, c);
   lw_setcoef(c, idrv);
@@ -1184,7 +1449,16 @@ void lw_column(const LwInput& in, int iplon, int idrv, LwColumn& c, LwOut& out) 
   for (int b = 1; b <= 16; ++b)
     for (; ig <= g_lw.ngs[b]; ++ig)
       for (int k = 1; k <= c.nlayers; ++k) c.taut[ig][k] = c.taug[ig][k] + c.taua[b][k];
-  lw_rtrnmr(c, idrv, out);
+  // icld = 1: rtrn (random overlap); clear sky: rtrnmr (:527-541)
+  if (in.icld == 1) {
+    lw_rtrn(c, idrv, out);
+  } else {
+    lw_rtrnmr(c, idrv, out);
+    out.totuc = out.totu;
+    out.totdc = out.totd;
+    out.htrc = out.htr;
+    out.dtotuc_dt = out.dtotu_dt;
+  }
 }
 
 }  // namespace orc

@@ -26,6 +26,10 @@ struct LwInput {
   int ncol, nlay;
   const double *play, *plev, *tlay, *tlev, *tsfc, *h2ovmr, *o3vmr, *co2vmr, *ch4vmr, *n2ovmr,
       *o2vmr, *cfc11vmr, *cfc12vmr, *cfc22vmr, *ccl4vmr, *emis, *tauaer;
+  // Clouds (icld = 1, inflglw = 0): cldfr (ncol, nlay), taucld (16, ncol, nlay),
+  // cicewp / cliqwp (ncol, nlay) or null.
+  int icld = 0;
+  const double *cldfr = nullptr, *taucld = nullptr, *cicewp = nullptr, *cliqwp = nullptr;
 };
 
 struct LwColumn {
@@ -42,6 +46,7 @@ struct LwColumn {
   std::vector<double> rat_h2oco2, rat_h2oco2_1, rat_h2oo3, rat_h2oo3_1, rat_h2on2o, rat_h2on2o_1,
       rat_h2och4, rat_h2och4_1, rat_n2oco2, rat_n2oco2_1, rat_o3co2, rat_o3co2_1;
   std::vector<double> taug[141], fracs[141], taut[141];
+  std::vector<double> cldfrac, taucloud[17];  // icld = 1: layer cloud fraction, cldprop's cloud optical depth
 
   void resize(int nl) {
     auto r = [&](std::vector<double>& v) { v.assign(nl + 2, 0.0); };
@@ -61,12 +66,15 @@ struct LwColumn {
     for (auto& v : taug) r(v);
     for (auto& v : fracs) r(v);
     for (auto& v : taut) r(v);
+    r(cldfrac);
+    for (auto& v : taucloud) r(v);
     for (int b = 0; b < 17; ++b) semiss[b] = plankbnd[b] = dplankbnd_dt[b] = 0.0;
   }
 };
 
 struct LwOut {
   std::vector<double> totu, totd, htr, dtotu_dt;  // levels 0..nlay (htr: layers 0..nlay-1, top 0)
+  std::vector<double> totuc, totdc, htrc, dtotuc_dt;  // clear-sky stream (rtrn, icld = 1)
   // Per-band fluxes, filled only when want_bands is set (sized 16 * (nlay + 1)
   // by the caller, band-major): upward, downward, d(upward)/d(tsfc) (idrv = 1).
   bool want_bands = false;
@@ -78,6 +86,7 @@ void lw_inatm(const LwInput& in, int iplon, LwColumn& c);
 void lw_setcoef(LwColumn& c, int idrv);
 void lw_taumol(LwColumn& c);
 void lw_rtrnmr(LwColumn& c, int idrv, LwOut& out);
+void lw_rtrn(LwColumn& c, int idrv, LwOut& out);
 void lw_column(const LwInput& in, int iplon, int idrv, LwColumn& c, LwOut& out);
 
 }  // namespace orc

@@ -247,10 +247,12 @@ def test_device_wrappers_follow_the_header():
     # rrtmg_lw_dev: the LW aerosol argument is the tauaer keyword
     r.rrtmg_lw_dev(0, ncol, nlay, 0, 1, fake, fake, tauaer=fake["tauaer_lw"])
     exp = {k: ptr[k] for k in _header_params("rrtmg_lw_dev") if k in ptr and k != "tauaer"}
-    exp.update({"tauaer": ptr["tauaer_lw"], **{k: None for k in cloud_lw}})
+    # the cloud arrays of icld = 1 (given optical depths) pass through; the
+    # cloud-physics radii do not (inflglw = 0 only)
+    exp.update({"tauaer": ptr["tauaer_lw"], "reice": None, "reliq": None})
     _check_positions(r.lib.calls["rrtmg_lw_dev"], _header_params("rrtmg_lw_dev"), exp)
     r.rrtmg_lw_dev_static(0, ncol, nlay, 0, 1, fake, fake, tauaer=None)
-    exp["tauaer"] = None
+    exp.update({"tauaer": None, **{k: None for k in cloud_lw}})
     _check_positions(r.lib.calls["rrtmg_lw_dev_static"], _header_params("rrtmg_lw_dev_static"), exp)
     # rrtmg_sw_dev: tauaer/ssaaer/asmaer are the SW arrays of the input dict
     r.rrtmg_sw_dev(0, ncol, nlay, 0, 10, fake, fake, 1.0, 0, 1360.0)

@@ -1,0 +1,156 @@
+"""LW clouds on the GPU (icld = 1: random overlap, cloud optical depths given,
+inflglw = 0) against the oracle's restatement of the reference's cldprop and
+rtrn (rrtmg_lw_cldprop.f90:155-174, rrtmg_lw_rtrn.f90).
+
+Tolerances: the FP64 path as every FP64 parity test (fluxes 1e-10 relative,
+heating 1e-8 K/day + 1e-9 relative), total and clear-sky outputs and the
+surface-temperature derivatives; the split path within the split bars
+(tests/split_bars.py: 0.1 W/m2 at every level, 0.05 K/day heating, its
+net-flux-divergence form in layers thinner than 0.01 hPa).
+"""
+import numpy as np
+import pytest
+
+import split_bars as SB
+from conftest import rel_err
+from mima_gb300 import atmosphere as A
+from mima_gb300 import rrtmg as R
+from test_gpu_parity import check_lw, hr_ok
+
+pytestmark = pytest.mark.gpu
+
+
+def cloud_fields(atm, rng):
+    """Seeded clouds below 100 hPa: about 40 % of the layers cloudy with a
+    cover up to 1, 5 % overcast, per-band optical depths up to 75 (a layer's
+    spectral shape times a heavy-tailed layer depth); among them layers whose
+    cover is below rtrn's 1e-6 (clear for the solver) and layers with cover but
+    no optical depth or water path (cldprop keeps no depth)."""
+    L, n = atm.nlay, atm.ncol
+    cf = rng.uniform(0.0, 1.0, (L, n)) * (rng.uniform(size=(L, n)) < 0.4)
+    cf[rng.uniform(size=(L, n)) < 0.05] = 1.0
+    cf[rng.uniform(size=(L, n)) < 0.02] = 5e-7
+    cf = np.where(atm.play > 100.0, cf, 0.0)
+    tau = (rng.uniform(0.0, 1.0, (L, n, 1)) ** 3 * 50.0) * rng.uniform(0.5, 1.5, (L, n, 16))
+    tau[rng.uniform(size=(L, n)) < 0.03] = 0.0
+    return dict(cldfr=cf, taucld=tau)
+
+
+def _case(nlay, seed, n=384):
+    rng = np.random.default_rng(seed)
+    atm = A.small_atmosphere(n, nlay, seed=seed, ts_sigma=5.0, rh_random=True)
+    atm.emis = rng.uniform(0.8, 1.0, size=(16, n))
+    return atm, cloud_fields(atm, rng)
+
+
+def _check_clear_outputs(out, ref, idrv):
+    for k in ("uflxc", "dflxc"):
+        assert rel_err(out[k], ref[k], 1e-3) < 1e-10, k
+    assert hr_ok(out["hrc"], ref["hrc"]), "hrc"
+    if idrv == 1:
+        assert rel_err(out["duflxc_dt"], ref["duflxc_dt"], 1e-6) < 1e-10
+
+
+@pytest.mark.parametrize("nlay", [40, 60])
+@pytest.mark.parametrize("mode", ["table", "analytic"])
+@pytest.mark.parametrize("idrv", [0, 1])
+def test_lw_clouds_fp64_matches_oracle(gpu, orc, nlay, mode, idrv):
+    atm, cl = _case(nlay, 900 + nlay + idrv)
+    orc.set_table_mode(mode == "table")
+    try:
+        ref = orc.rrtmg_lw(atm, idrv=idrv, cloud=cl)
+    finally:
+        orc.set_table_mode(True)
+    gpu.set_precision("fp64")
+    gpu.set_transcendentals(mode)
+    try:
+        out = gpu.lw(atm, idrv=idrv, cloud=cl)
+    finally:
+        gpu.set_transcendentals("table")
+    check_lw(out, ref, idrv=idrv)
+    _check_clear_outputs(out, ref, idrv)
+    # the clouds matter: OLR and the surface downward flux move
+    clear = orc.rrtmg_lw(atm)
+    assert np.abs(ref["uflx"][-1] - clear["uflx"][-1]).max() > 10.0
+
+
+@pytest.mark.parametrize("nlay", [40, 60])
+def test_lw_clouds_split_within_bars(gpu, orc, nlay):
+    atm, cl = _case(nlay, 950 + nlay, n=768)
+    ref = orc.rrtmg_lw(atm, idrv=1, cloud=cl)
+    gpu.set_precision("split")
+    try:
+        out = gpu.lw(atm, idrv=1, cloud=cl)
+    finally:
+        gpu.set_precision("fp64")
+    bar = SB.hr_bar(atm)
+    for k in ("uflx", "dflx", "uflxc", "dflxc"):
+        assert np.abs(out[k] - ref[k]).max() <= SB.FLUX_BAR, (k, np.abs(out[k] - ref[k]).max())
+    for k in ("hr", "hrc"):
+        assert np.all(np.abs(out[k] - ref[k]) <= bar), (k, np.abs(out[k] - ref[k]).max())
+    assert np.abs(out["duflx_dt"] - ref["duflx_dt"]).max() <= 1e-3
+
+
+def test_lw_clouds_without_clouds_equal_clear_sky(gpu):
+    """icld = 1 with no cloud (cover 0, or below rtrn's 1e-6) takes rtrn's clear
+    branch everywhere: the FP64 results are the clear-sky call's bit for bit,
+    the split ones within FP32 rounding."""
+    atm = A.small_atmosphere(200, 40, seed=17)
+    L, n = atm.nlay, atm.ncol
+    cl = dict(cldfr=np.full((L, n), 5e-7), taucld=np.full((L, n, 16), 3.0))
+    for prec in ("fp64", "split"):
+        gpu.set_precision(prec)
+        try:
+            a, b = gpu.lw(atm, idrv=1), gpu.lw(atm, idrv=1, cloud=cl)
+        finally:
+            gpu.set_precision("fp64")
+        for k in a:
+            if k == "status":
+                continue
+            if prec == "fp64":
+                assert np.array_equal(a[k], b[k]), k
+            else:
+                assert np.abs(a[k] - b[k]).max() <= 1e-3, k
+
+
+def test_lw_clouds_host_entry_matches_device_entry(gpu):
+    """rrtmg_lw_c (page-locked arrays, 40000 columns: two column chunks on two
+    streams, taucld copied 16 values per column) against rrtmg_lw_dev on the
+    same arrays, bit for bit."""
+    torch = pytest.importorskip("torch")
+    atm, cl = _case(40, 77, n=40000)
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    L, n = atm.nlay, atm.ncol
+    outs = {k: pin(np.zeros((L + 1 if k not in ("hr", "hrc") else L, n))) for k in
+            ("uflx", "dflx", "hr", "uflxc", "dflxc", "hrc", "duflx_dt", "duflxc_dt")}
+    gpu.set_precision("split")
+    try:
+        host = gpu.rrtmg_lw(n, L, 1, 1, *[pin(a) for a in (atm.play, atm.plev, atm.tlay, atm.tlev, atm.tsfc, atm.h2o,
+                                                            atm.o3, atm.co2, atm.ch4, atm.n2o, atm.o2, atm.cfc11,
+                                                            atm.cfc12, atm.cfc22, atm.ccl4, atm.emis)],
+                            out=outs, cldfr=pin(cl["cldfr"]), taucld=pin(cl["taucld"]))
+        d = R.atm_device_inputs(atm)
+        d["cldfr"] = torch.from_numpy(cl["cldfr"]).cuda()
+        d["taucld"] = torch.from_numpy(np.ascontiguousarray(cl["taucld"])).cuda()
+        o, _ = R.device_outputs(n, L, idrv=1)
+        s = torch.cuda.Stream()
+        with torch.cuda.stream(s):
+            gpu.rrtmg_lw_dev(s.cuda_stream, n, L, 1, 1, d, o)
+        s.synchronize()
+    finally:
+        gpu.set_precision("fp64")
+    for k in o:
+        assert np.array_equal(o[k].cpu().numpy(), host[k]), k
+
+
+def test_lw_cloud_options_not_computed_are_refused(gpu):
+    atm, cl = _case(40, 5, n=16)
+    args = (atm.ncol, atm.nlay)
+    base = (atm.play, atm.plev, atm.tlay, atm.tlev, atm.tsfc, atm.h2o, atm.o3, atm.co2)
+    o = gpu.rrtmg_lw(*args, 2, 0, *base, check=False, cldfr=cl["cldfr"], taucld=cl["taucld"])
+    assert o["status"] == R.RRTMG_ERR_UNSUPPORTED  # maximum-random overlap
+    o = gpu.rrtmg_lw(*args, 1, 0, *base, check=False, inflglw=2, cldfr=cl["cldfr"], taucld=cl["taucld"])
+    assert o["status"] == R.RRTMG_ERR_UNSUPPORTED  # cloud physics (cldprop inflag = 2)
+    o = gpu.rrtmg_lw(*args, 1, 0, *base, check=False, cldfr=cl["cldfr"])
+    assert o["status"] == R.RRTMG_ERR_ARG  # no cloud optical depths
+    assert gpu.lw(atm, cloud=cl)["status"] == R.RRTMG_OK

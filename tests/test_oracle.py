@@ -246,3 +246,47 @@ def test_gas_optics_stage(orc, blob):
     gtaug, taur, sfz = orc.sw_optics(atm)
     np.testing.assert_allclose(sfz.sum(axis=0), 1368.22, rtol=1e-5)
     assert (taur > 0).all() and (gtaug >= 0).all()
+
+
+def test_lw_clouds_random_overlap(orc):
+    """The oracle's LW clouds (icld = 1, rtrn with cldprop inflag = 0):
+    * icld = 1 with no cloud reproduces clear sky bit for bit;
+    * the clear-sky outputs of a cloudy call are the clear-sky call's;
+    * an opaque overcast layer (cover 1, depth 1e3 in every band) emits as a
+      blackbody at its own temperature, so the OLR of an isothermal column above
+      it is sigma T^4 of that temperature;
+    * random overlap is linear in the cover of a single cloudy layer: the
+      fluxes at half cover are the mean of clear and overcast;
+    * cldprop keeps no optical depth for a layer with cover but neither depth
+      nor water path, and rtrn treats a cover below 1e-6 as clear."""
+    atm = A.small_atmosphere(24, 40, seed=5)
+    L, n = atm.nlay, atm.ncol
+    clear = orc.rrtmg_lw(atm, idrv=1)
+    none = orc.rrtmg_lw(atm, idrv=1, cloud=dict(cldfr=np.zeros((L, n)), taucld=np.zeros((L, n, 16))))
+    for k in clear:
+        assert np.array_equal(none[k], clear[k]), k
+    k = 12
+    cf = np.zeros((L, n))
+    cf[k] = 1.0
+    tau = np.zeros((L, n, 16))
+    tau[k] = 1.0e3
+    over = orc.rrtmg_lw(atm, idrv=1, cloud=dict(cldfr=cf, taucld=tau))
+    for name in ("uflx", "dflx", "hr", "duflx_dt"):
+        c = "hrc" if name == "hr" else name[:-3] + "c_dt" if name == "duflx_dt" else name + "c"
+        assert np.allclose(over[c], clear[name], rtol=1e-12, atol=1e-12), name
+    half = orc.rrtmg_lw(atm, cloud=dict(cldfr=cf * 0.5, taucld=tau))
+    assert np.allclose(half["uflx"], 0.5 * (clear["uflx"] + over["uflx"]), rtol=2e-3)
+    # isothermal stratosphere above an opaque cloud: OLR = sigma T^4
+    iso = A.small_atmosphere(8, 40, seed=6)
+    T = 230.0
+    iso.tlay[k:] = T
+    iso.tlev[k:] = T
+    cfi, taui = np.zeros((L, iso.ncol)), np.zeros((L, iso.ncol, 16))
+    cfi[k], taui[k] = 1.0, 1.0e3
+    lw = orc.rrtmg_lw(iso, cloud=dict(cldfr=cfi, taucld=taui))
+    assert np.allclose(lw["uflx"][-1], SIGMA * T ** 4, rtol=0.02), (lw["uflx"][-1], SIGMA * T ** 4)
+    # no depth and no water path: no cloud optical depth; cover < 1e-6: clear layer
+    zero = orc.rrtmg_lw(atm, cloud=dict(cldfr=cf, taucld=np.zeros_like(tau)))
+    assert np.allclose(zero["uflx"], clear["uflx"], rtol=1e-12, atol=1e-9)
+    tiny = orc.rrtmg_lw(atm, cloud=dict(cldfr=cf * 5e-7, taucld=tau))
+    assert np.array_equal(tiny["uflx"], clear["uflx"])

@@ -28,11 +28,18 @@
  *     rrtmg_lw_cldprop.f90:165-171): cldfr (ncol,nlay), taucld (16,ncol,nlay),
  *     cicewp / cliqwp (ncol,nlay) or NULL (they only decide, with the band sum
  *     of taucld, whether a layer's depths are kept); reice, reliq and the ice /
- *     liquid flags are unused.  Every other entry point is clear sky
+ *     liquid flags are unused.  rrtmg_sw_c / rrtmg_sw_dev compute icld = 1,
+ *     2, 3 (identical without McICA) with the cloud optics given
+ *     (inflgsw = 0, rrtmg_sw_cldprop.f90:142-156): cldfr (ncol,nlay); taucld,
+ *     ssacld, asmcld, fsfcld (14,ncol,nlay); cicewp / cliqwp or NULL.  As the
+ *     reference's non-McICA SW (rrtmg_sw_rad.nomcica.f90:533-538), every layer
+ *     of a sunlit column must be clear or overcast (cldfr <= 1e-6 or
+ *     >= 1 - 1e-6): a partly cloudy one is reported as RRTMG_ERR_INPUT, where
+ *     the reference stops the program.  Every other entry point is clear sky
  *     (icld = 0).  The reference coerces icld and iaer silently (:437,
  *     :471-479); this library returns RRTMG_ERR_UNSUPPORTED for any
- *     configuration it does not compute (icld = 2 / 3, inflglw = 1 / 2, SW
- *     clouds) and never falls back to a CPU path.
+ *     configuration it does not compute (LW icld = 2 / 3, inflglw or inflgsw
+ *     = 1 / 2, icld outside 0..3) and never falls back to a CPU path.
  *   - Every entry point returns a status (0 = success).  A handle is not
  *     thread-safe; use one handle per host thread.
  */
@@ -48,10 +55,12 @@ typedef struct rrtmg_gpu_state* rrtmg_gpu_handle;
 enum rrtmg_gpu_status {
   RRTMG_OK = 0,
   RRTMG_ERR_ARG = 1,          /* bad dimension, null required pointer, bad handle */
-  RRTMG_ERR_UNSUPPORTED = 2,  /* clouds other than LW icld = 1 / inflglw = 0, iaer not in {0,10}, idrv not in {0,1} */
+  RRTMG_ERR_UNSUPPORTED = 2,  /* LW icld not in {0,1}, SW icld not in 0..3, cloud physics (inflglw/inflgsw != 0),
+                                 iaer not in {0,10}, idrv not in {0,1} */
   RRTMG_ERR_CUDA = 3,         /* CUDA runtime error (see rrtmg_gpu_last_error) */
   RRTMG_ERR_TABLES = 4,       /* table blob missing, malformed or checksum mismatch */
-  RRTMG_ERR_INPUT = 5,        /* device-side validation flagged a non-finite or out-of-range input */
+  RRTMG_ERR_INPUT = 5,        /* device-side validation flagged a non-finite or out-of-range input, or a
+                                 partly cloudy sunlit layer in a SW call with clouds */
   RRTMG_ERR_NOMEM = 6         /* device workspace allocation failed */
 };
 
@@ -111,7 +120,9 @@ int rrtmg_lw_c(rrtmg_gpu_handle h, int ncol, int nlay, int icld, int idrv,
 
 /* rrtmg_sw (rrtmg_sw_rad.nomcica.f90:78-88), host arrays.  Columns with
  * coszen < 1e-10 get zero fluxes and heating (MiMA's skip, :502-510).
- * iaer = 10 uses tauaer/ssaaer/asmaer (ncol,nlay,14); ecaer is ignored. */
+ * iaer = 10 uses tauaer/ssaaer/asmaer (ncol,nlay,14); ecaer is ignored.  With
+ * clouds (icld >= 1) the clear-sky outputs (swuflxc, swdflxc, swhrc) are the
+ * clear pass of spcvrt_sw, else they equal the total ones. */
 int rrtmg_sw_c(rrtmg_gpu_handle h, int ncol, int nlay, int icld, int iaer,
                const double* play, const double* plev, const double* tlay, const double* tlev,
                const double* tsfc, const double* h2ovmr, const double* o3vmr, const double* co2vmr,

@@ -164,16 +164,21 @@ LwWork carve_lw(void* base, int ncol, int nlay, size_t* bytes, bool cloudy = fal
   return w;
 }
 
-SwWork carve_sw(void* base, int ncol, int nlay, size_t* bytes) {
+SwWork carve_sw(void* base, int ncol, int nlay, size_t* bytes, bool cloudy = false) {
   Carver c{(char*)base};
   const size_t N = (size_t)ncol, L = (size_t)nlay;
-  SwWork w;
+  SwWork w{};
   w.idx = c.take<uint32_t>(L * N);
   w.f = c.take<double>((size_t)SF_N * L * N);
   w.laytrop = c.take<int>(N);
   w.laysolfr = c.take<int>(14 * N);
   w.su = c.take<double>(14 * (L + 1) * N);
   w.sd = c.take<double>(14 * (L + 1) * N);
+  if (cloudy) {
+    w.cld = c.take<double>(2 * L * N);
+    w.suc = c.take<double>(14 * (L + 1) * N);
+    w.sdc = c.take<double>(14 * (L + 1) * N);
+  }
   if (bytes) *bytes = c.off;
   return w;
 }
@@ -196,7 +201,7 @@ LwWorkT<F> work_as(const LwWork& w) {
 }
 template <class F>
 SwWorkT<F> work_as(const SwWork& w) {
-  return SwWorkT<F>{w.idx, (F*)w.f, w.laytrop, w.laysolfr, w.su, w.sd};
+  return SwWorkT<F>{w.idx, (F*)w.f, w.laytrop, w.laysolfr, w.su, w.sd, (F*)w.cld, w.suc, w.sdc};
 }
 template <class F>
 LwPrepT<F> prep_of(const LwWorkT<F>& w) {
@@ -289,6 +294,24 @@ int lw_cloud_args(rrtmg_gpu_state* h, int icld, int inflglw, const double* cldfr
   return RRTMG_OK;
 }
 
+// Cloud arguments of the SW calls: icld = 0 (clear sky), or icld = 1 with the
+// cloud optics given (inflgsw = 0, rrtmg_sw_cldprop.f90:142-156).  Without
+// McICA the reference computes clear and overcast layers only (a partly
+// cloudy layer stops it, rrtmg_sw_rad.nomcica.f90:533-538): icld = 1, 2 and 3
+// are the same there, so all three are taken; such a layer is reported by the
+// kernels as invalid input.  The cloud-physics options inflgsw = 1 / 2 are not
+// computed.
+int sw_cloud_args(rrtmg_gpu_state* h, int icld, int inflgsw, const double* cldfr, const double* taucld,
+                  const double* ssacld, const double* asmcld, const double* fsfcld) {
+  if (icld == 0) return RRTMG_OK;
+  if (icld < 0 || icld > 3) return fail(h, RRTMG_ERR_UNSUPPORTED, "icld must be in [0, 3]");
+  if (inflgsw != 0)
+    return fail(h, RRTMG_ERR_UNSUPPORTED, "SW clouds: only given cloud optics (inflgsw = 0) are computed");
+  if (!cldfr || !taucld || !ssacld || !asmcld || !fsfcld)
+    return fail(h, RRTMG_ERR_ARG, "SW clouds need cldfr, taucld, ssacld, asmcld and fsfcld");
+  return RRTMG_OK;
+}
+
 // Incident-flux scaling (inatm_sw, rrtmg_sw_rad.nomcica.f90:953-972): the
 // GCM's Earth-Sun factor, or Iqbal's day-of-year formula, times scon/1368.22.
 double adjflux_of(const rrtmg_gpu_state* h, double adjes, int dyofyr, double scon) {
@@ -304,30 +327,44 @@ double adjflux_of(const rrtmg_gpu_state* h, double adjes, int dyofyr, double sco
 int sw_enqueue(rrtmg_gpu_state* h, cudaStream_t s, void* base, int ncol, int nlay, int iaer, double adjes,
                int dyofyr, double scon, const SwIn& in, double* swuflx, double* swdflx, double* swhr, double* swuflxc,
                double* swdflxc, double* swhrc) {
-  SwWork w = carve_sw(base, ncol, nlay, nullptr);
+  // clouds (icld = 1): a clear-sky pass into the clear partials (suc, sdc) and
+  // a total-sky pass into su, sd, as the reference's two two-stream passes
+  const bool cloudy = in.cldfr != nullptr;
+  SwWork w = carve_sw(base, ncol, nlay, nullptr, cloudy);
   const double adjflux = adjflux_of(h, adjes, dyofyr, scon);
   const int nb = sw_gpoint_blocks(h->host.sw, ncol, h->precision == RRTMG_PREC_SPLIT);
+  double* cu = cloudy ? w.suc : w.su;
+  double* cd = cloudy ? w.sdc : w.sd;
   mark(h, 1, 0, s);
   if (h->precision == RRTMG_PREC_SPLIT) {
     const SwWorkT<float> w32 = work_as<float>(w);
     launch_sw_prep_split(in, w32, ncol, nlay, h->flags, s);
+    if (cloudy) launch_sw_cloud_split(in, w32.cld, ncol, nlay, h->flags, s);
     mark(h, 1, 1, s);
-    launch_sw_gpoint_split(prep_of(w32), in, adjflux, iaer, h->sw_tab32, h->sw_tab64, h->sw_exp32, w.su, w.sd, ncol,
+    launch_sw_gpoint_split(prep_of(w32), in, adjflux, iaer, h->sw_tab32, h->sw_tab64, h->sw_exp32, cu, cd, ncol,
                            nlay, nb, h->analytic, s);
+    if (cloudy)
+      launch_sw_gpoint_split(prep_of(w32), in, adjflux, iaer, h->sw_tab32, h->sw_tab64, h->sw_exp32, w.su, w.sd,
+                             ncol, nlay, nb, h->analytic, s, w32.cld);
   } else {
     launch_sw_prep(in, w, ncol, nlay, h->flags, s);
+    if (cloudy) launch_sw_cloud(in, w.cld, ncol, nlay, h->flags, s);
     mark(h, 1, 1, s);
-    launch_sw_gpoint_fp64(prep_of(w), in, adjflux, iaer, h->sw_tab64, h->sw_exp64, w.su, w.sd, ncol, nlay, nb,
+    launch_sw_gpoint_fp64(prep_of(w), in, adjflux, iaer, h->sw_tab64, h->sw_exp64, cu, cd, ncol, nlay, nb,
                           h->analytic, s);
+    if (cloudy)
+      launch_sw_gpoint_fp64(prep_of(w), in, adjflux, iaer, h->sw_tab64, h->sw_exp64, w.su, w.sd, ncol, nlay, nb,
+                            h->analytic, s, w.cld);
   }
   mark(h, 1, 2, s);
   if (h->precision == RRTMG_PREC_SPLIT)
     launch_sw_finalize_split(w.su, w.sd, in.plev, in.coszen, ncol, nlay, swuflx, swdflx, swhr, swuflxc, swdflxc,
-                             swhrc, s);
+                             swhrc, s, w.suc, w.sdc);
   else
-    launch_sw_finalize(w.su, w.sd, in.plev, in.coszen, ncol, nlay, swuflx, swdflx, swhr, swuflxc, swdflxc, swhrc, s);
+    launch_sw_finalize(w.su, w.sd, in.plev, in.coszen, ncol, nlay, swuflx, swdflx, swhr, swuflxc, swdflxc, swhrc, s,
+                       w.suc, w.sdc);
   mark(h, 1, 3, s);
-  h->launches += 4;
+  h->launches += cloudy ? 6 : 4;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(h, e, "SW kernel launch");
   return RRTMG_OK;
@@ -337,7 +374,7 @@ int sw_run(rrtmg_gpu_state* h, cudaStream_t s, int ncol, int nlay, int iaer, dou
            const SwIn& in, double* swuflx, double* swdflx, double* swhr, double* swuflxc, double* swdflxc,
            double* swhrc) {
   size_t need;
-  carve_sw(nullptr, ncol, nlay, &need);
+  carve_sw(nullptr, ncol, nlay, &need, in.cldfr != nullptr);
   int rc = ensure(h, h->sw_ws, need, s);
   if (rc) return rc;
   return sw_enqueue(h, s, h->sw_ws.p, ncol, nlay, iaer, adjes, dyofyr, scon, in, swuflx, swdflx, swhr, swuflxc,
@@ -393,8 +430,8 @@ struct HostOut {
 // LW + SW host calls at 32768 columns (page-locked arrays) took 9.43 ms in one
 // chunk, 8.78 in 2 or 3, 9.17 in 4, 9.89 in 8.
 constexpr int kChunkMin = RRTMG_HOST_CHUNK, kMaxChunks = 16;
-// Most input and output arrays of one host-array call (rrtmg_sw_c: 19 / 6).
-constexpr int kMaxHostIn = 24, kMaxHostOut = 12;
+// Most input and output arrays of one host-array call (rrtmg_sw_c: 26 / 6).
+constexpr int kMaxHostIn = 28, kMaxHostOut = 12;
 
 int read_flags(rrtmg_gpu_state* h, cudaStream_t s);
 
@@ -559,7 +596,9 @@ int read_flags(rrtmg_gpu_state* h, cudaStream_t s) {
   if (f) {
     cudaMemsetAsync(h->flags, 0, sizeof(unsigned), s);
     cudaStreamSynchronize(s);
-    return fail(h, RRTMG_ERR_INPUT, "non-finite or out-of-range input (pressure <= 0, T <= 0, q outside [0,1), NaN/Inf)");
+    if (f & 1u)
+      return fail(h, RRTMG_ERR_INPUT, "non-finite or out-of-range input (pressure <= 0, T <= 0, q outside [0,1), NaN/Inf)");
+    return fail(h, RRTMG_ERR_INPUT, "SW clouds: a partly cloudy layer (1e-6 < cldfr < 1 - 1e-6) needs McICA");
   }
   return RRTMG_OK;
 }
@@ -573,7 +612,9 @@ const char* rrtmg_gpu_error_string(int status) {
   switch (status) {
     case RRTMG_OK: return "success";
     case RRTMG_ERR_ARG: return "invalid argument";
-    case RRTMG_ERR_UNSUPPORTED: return "unsupported configuration (only clear sky, iaer 0/10, idrv 0/1)";
+    case RRTMG_ERR_UNSUPPORTED:
+      return "unsupported configuration (LW icld 0/1, SW clear or overcast layers, given cloud optics, iaer 0/10, "
+             "idrv 0/1)";
     case RRTMG_ERR_CUDA: return "CUDA error";
     case RRTMG_ERR_TABLES: return "coefficient table blob missing or invalid";
     case RRTMG_ERR_INPUT: return "invalid input values";
@@ -769,12 +810,12 @@ int rrtmg_sw_dev(rrtmg_gpu_handle h, void* stream, int ncol, int nlay, int icld,
                  const double* reice, const double* reliq, const double* tauaer, const double* ssaaer,
                  const double* asmaer, const double* ecaer, double* swuflx, double* swdflx, double* swhr,
                  double* swuflxc, double* swdflxc, double* swhrc) {
-  (void)inflgsw; (void)iceflgsw; (void)liqflgsw; (void)cldfr; (void)taucld; (void)ssacld; (void)asmcld;
-  (void)fsfcld; (void)cicewp; (void)cliqwp; (void)reice; (void)reliq; (void)ecaer;
+  (void)iceflgsw; (void)liqflgsw; (void)reice; (void)reliq; (void)ecaer;
   if (!valid_handle(h)) return RRTMG_ERR_ARG;
   int rc = check_dims(h, ncol, nlay);
   if (rc) return rc;
-  if (icld != 0) return fail(h, RRTMG_ERR_UNSUPPORTED, "only clear sky (icld = 0) is computed");
+  rc = sw_cloud_args(h, icld, inflgsw, cldfr, taucld, ssacld, asmcld, fsfcld);
+  if (rc) return rc;
   if (iaer != 0 && iaer != 10) return fail(h, RRTMG_ERR_UNSUPPORTED, "iaer must be 0 or 10");
   if (!play || !plev || !tlay || !tlev || !tsfc || !h2ovmr || !o3vmr || !co2vmr || !asdir || !asdif || !aldir ||
       !aldif || !coszen || !swuflx || !swdflx || !swhr || !swuflxc || !swdflxc || !swhrc)
@@ -784,6 +825,15 @@ int rrtmg_sw_dev(rrtmg_gpu_handle h, void* stream, int ncol, int nlay, int icld,
   cudaSetDevice(h->device);
   SwIn in{play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr, asdir, asdif, aldir, aldif,
           coszen, tauaer, ssaaer, asmaer};
+  if (icld != 0) {
+    in.cldfr = cldfr;
+    in.taucld = taucld;
+    in.ssacld = ssacld;
+    in.asmcld = asmcld;
+    in.fsfcld = fsfcld;
+    in.cicewp = cicewp;
+    in.cliqwp = cliqwp;
+  }
   return sw_run(h, (cudaStream_t)stream, ncol, nlay, iaer, adjes, dyofyr, scon, in, swuflx, swdflx, swhr, swuflxc,
                 swdflxc, swhrc);
 }
@@ -936,12 +986,12 @@ int rrtmg_sw_c(rrtmg_gpu_handle h, int ncol, int nlay, int icld, int iaer, const
                const double* reliq, const double* tauaer, const double* ssaaer, const double* asmaer,
                const double* ecaer, double* swuflx, double* swdflx, double* swhr, double* swuflxc, double* swdflxc,
                double* swhrc) {
-  (void)inflgsw; (void)iceflgsw; (void)liqflgsw; (void)cldfr; (void)taucld; (void)ssacld; (void)asmcld;
-  (void)fsfcld; (void)cicewp; (void)cliqwp; (void)reice; (void)reliq; (void)ecaer;
+  (void)iceflgsw; (void)liqflgsw; (void)reice; (void)reliq; (void)ecaer;
   if (!valid_handle(h)) return RRTMG_ERR_ARG;
   int rc = check_dims(h, ncol, nlay);
   if (rc) return rc;
-  if (icld != 0) return fail(h, RRTMG_ERR_UNSUPPORTED, "only clear sky (icld = 0) is computed");
+  rc = sw_cloud_args(h, icld, inflgsw, cldfr, taucld, ssacld, asmcld, fsfcld);
+  if (rc) return rc;
   if (iaer != 0 && iaer != 10) return fail(h, RRTMG_ERR_UNSUPPORTED, "iaer must be 0 or 10");
   if (!play || !plev || !tlay || !tlev || !tsfc || !h2ovmr || !o3vmr || !co2vmr || !asdir || !asdif || !aldir ||
       !aldif || !coszen || !swuflx || !swdflx || !swhr || !swuflxc || !swdflxc || !swhrc)
@@ -950,23 +1000,25 @@ int rrtmg_sw_c(rrtmg_gpu_handle h, int ncol, int nlay, int icld, int iaer, const
   if (!(scon > 0.0)) return fail(h, RRTMG_ERR_ARG, "scon must be positive");
   cudaSetDevice(h->device);
   const size_t L = nlay, Lv = nlay + 1;
-  const bool aer = iaer == 10;
-  const HostIn in[19] = {{play, L}, {plev, Lv}, {tlay, L}, {tlev, Lv}, {tsfc, 1}, {h2ovmr, L}, {o3vmr, L},
+  const bool aer = iaer == 10, cloudy = icld != 0;
+  auto cl = [&](const double* a) { return cloudy ? a : nullptr; };
+  const HostIn in[26] = {{play, L}, {plev, Lv}, {tlay, L}, {tlev, Lv}, {tsfc, 1}, {h2ovmr, L}, {o3vmr, L},
                          {co2vmr, L}, {ch4vmr, L}, {n2ovmr, L}, {o2vmr, L}, {asdir, 1}, {asdif, 1}, {aldir, 1},
                          {aldif, 1}, {coszen, 1}, {aer ? tauaer : nullptr, 14 * L}, {aer ? ssaaer : nullptr, 14 * L},
-                         {aer ? asmaer : nullptr, 14 * L}};
+                         {aer ? asmaer : nullptr, 14 * L}, {cl(cldfr), L}, {cl(taucld), L, 14}, {cl(ssacld), L, 14},
+                         {cl(asmcld), L, 14}, {cl(fsfcld), L, 14}, {cl(cicewp), L}, {cl(cliqwp), L}};
   const HostOut out[6] = {{swuflx, Lv}, {swdflx, Lv}, {swhr, L}, {swuflxc, Lv}, {swdflxc, Lv}, {swhrc, L}};
   auto need = [&](int nc) {
     size_t b;
-    carve_sw(nullptr, nc, nlay, &b);
+    carve_sw(nullptr, nc, nlay, &b, cloudy);
     return b;
   };
   auto enq = [&](cudaStream_t s, void* ws, int nc, const double* const* d, double* const* o) {
-    SwIn si{d[0], d[1], d[2], d[3], d[4], d[5], d[6], d[7], d[8], d[9], d[10], d[11], d[12], d[13], d[14], d[15],
-            d[16], d[17], d[18]};
+    SwIn si{d[0],  d[1],  d[2],  d[3],  d[4],  d[5],  d[6],  d[7],  d[8],  d[9],  d[10], d[11], d[12],
+            d[13], d[14], d[15], d[16], d[17], d[18], d[19], d[20], d[21], d[22], d[23], d[24], d[25]};
     return sw_enqueue(h, s, ws, nc, nlay, iaer, adjes, dyofyr, scon, si, o[0], o[1], o[2], o[3], o[4], o[5]);
   };
-  return host_call(h, ncol, in, 19, out, 6, need, enq, "copy SW arrays");
+  return host_call(h, ncol, in, 26, out, 6, need, enq, "copy SW arrays");
 }
 
 }  // extern "C"

@@ -167,6 +167,9 @@ using LwWork = LwWorkT<double>;
 struct SwIn {
   const double *play, *plev, *tlay, *tlev, *tsfc, *h2o, *o3, *co2, *ch4, *n2o, *o2, *asdir, *asdif, *aldir, *aldif,
       *coszen, *tauaer, *ssaaer, *asmaer;
+  // clouds (icld = 1, inflgsw = 0), null in clear sky: cldfr (ncol, nlay);
+  // taucld, ssacld, asmcld, fsfcld (14, ncol, nlay); cicewp / cliqwp or null
+  const double *cldfr, *taucld, *ssacld, *asmcld, *fsfcld, *cicewp, *cliqwp;
 };
 template <class F>
 struct SwWorkT {
@@ -174,6 +177,10 @@ struct SwWorkT {
   F* f;
   int *laytrop, *laysolfr;
   double *su, *sd;  // band partials [band][lev][col]
+  // clouds only (null in clear sky): per layer [cover][cldprop's 0/1 mask]
+  // and the clear-sky band partials
+  F* cld;
+  double *suc, *sdc;
 };
 using SwWork = SwWorkT<double>;
 

@@ -1326,12 +1326,15 @@ __device__ __forceinline__ void reftra_split(R zto1, R zw, R zg, R prmuz, R bpad
   }
 }
 
-template <int B, class R, int MAXL>
+// TOT: the total-sky pass of a cloudy call (icld = 1): every layer's clear
+// optics combined with its cloud optics by the cover (spcvrt_sw :459-525);
+// cld: [cover][cldprop mask] per layer.  Otherwise the clear-sky pass.
+template <int B, class R, int MAXL, bool TOT = false>
 __device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, double adjflux, int iaer,
                                         const R* __restrict__ tab, const double* __restrict__ tab64,
                                         const R* __restrict__ exptbl, double* __restrict__ su,
                                         double* __restrict__ sd, int ncol, int nlay, bool analytic, int blk, float* sbuf,
-                                        float* swt) {
+                                        float* swt, const R* __restrict__ cld = nullptr) {
   constexpr bool SPLIT = sizeof(R) == 4;
   constexpr int NG = sw_ng(B);
   constexpr int W = split_lanes(NG, SPLIT);
@@ -1403,6 +1406,42 @@ __device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, dou
     } else {
       reftra1<R, R>(ztauc, zomcc, zgcc, prmu0, bpade, exptbl, analytic, rf, rfd, tr, trd);
       zdbtmc = sw_exp_tbl<R, R>(ztauc / prmu0, bpade, exptbl, analytic);
+    }
+    if constexpr (TOT) {
+      // cldprop_sw, inflag = 0 (rrtmg_sw_cldprop.f90:142-156): delta-M scaled
+      // cloud optics where the mask keeps them, else tau 0, ssa 1, g 0
+      const R pclfr = __ldg(cld + o);
+      R ptauc = (R)0., pomgc = (R)1., pasyc = (R)0.;
+      if (__ldg(cld + fstride + o) > (R)0.) {
+        const size_t q = (size_t)(ibm - 1) + 14 * o;
+        const R taucldorig = (R)__ldg(in.taucld + q), ffp = (R)__ldg(in.fsfcld + q);
+        const R ssac = (R)__ldg(in.ssacld + q), asmc = (R)__ldg(in.asmcld + q);
+        const R ffp1 = (R)1.0 - ffp;
+        const R ffpssa = (R)1.0 - ffp * ssac;
+        pomgc = ffp1 * ssac / ffpssa;
+        ptauc = ffpssa * taucldorig;
+        pasyc = (asmc - ffp) / (ffp1);
+      }
+      // total-sky optics (spcvrt_sw :459-464), reftra only for cloudy layers
+      // (pclfr > repclc = 1e-12, :388; reftra gives 0, 1, 0, 1 otherwise)
+      const R ztauo = ztauc + ptauc;
+      R zomco = ztauc * zomcc + ptauc * pomgc;
+      const R zgco = (ptauc * pomgc * pasyc + ztauc * zomcc * zgcc) / zomco;
+      zomco = zomco / ztauo;
+      R rfo = (R)0., rfdo = (R)0., tro = (R)1., trdo = (R)1.;
+      if (pclfr > (R)1.e-12) {
+        if constexpr (sizeof(R) == 4)
+          reftra_split(ztauo, zomco, zgco, prmu0, bpade, exptbl, analytic, rfo, rfdo, tro, trdo, false);
+        else
+          reftra1<R, R>(ztauo, zomco, zgco, prmu0, bpade, exptbl, analytic, rfo, rfdo, tro, trdo);
+      }
+      const R zdbtmo = sw_exp_tbl<R, R>(ztauo / prmu0, bpade, exptbl, analytic);
+      const R zclear = (R)1.0 - pclfr, zcloud = pclfr;
+      rf = zclear * rf + zcloud * rfo;
+      rfd = zclear * rfd + zcloud * rfdo;
+      tr = zclear * tr + zcloud * tro;
+      trd = zclear * trd + zcloud * trdo;
+      zdbtmc = zclear * zdbtmc + zcloud * zdbtmo;
     }
     pref[jk - 1] = rf;
     prefd[jk - 1] = rfd;
@@ -1478,12 +1517,13 @@ __device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, dou
 }
 
 // FL < 0: analytic and iaer as passed; FL >= 0: compile-time flags (bit 0
-// analytic, bit 1 iaer = 10), as for the LW kernel.
-template <class R, int MAXL, int FL = -1>
+// analytic, bit 1 iaer = 10), as for the LW kernel.  TOT: the total-sky pass
+// of a cloudy call (cld: per-layer cover and cldprop mask), else clear sky.
+template <class R, int MAXL, int FL = -1, bool TOT = false>
 __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_SW_MINB : 1) sw_gpoint_kernel(SwPrepT<R> p, SwIn in, double adjflux, int iaer,
                                                            const R* __restrict__ tab, const double* __restrict__ tab64,
                                                            const R* __restrict__ exptbl, double* su, double* sd,
-                                                           int ncol, int nlay, int analytic) {
+                                                           int ncol, int nlay, int analytic, const R* __restrict__ cld) {
   __shared__ float sbuf[sizeof(R) == 4 ? kGSumFloats : 1];
   __shared__ float swt[sizeof(R) == 4 ? kBlock : 1];
   int blk = blockIdx.x, band = 0;
@@ -1495,7 +1535,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_SW_MINB :
   const bool an = FL < 0 ? analytic != 0 : (FL & 1) != 0;
   const int ia = FL < 0 ? iaer : ((FL & 2) ? 10 : 0);
 #define RRTMG_SW_CASE(b) \
-  case b - 16: sw_band<b, R, MAXL>(p, in, adjflux, ia, tab, tab64, exptbl, su, sd, ncol, nlay, an, blk, sbuf, swt); break;
+  case b - 16: sw_band<b, R, MAXL, TOT>(p, in, adjflux, ia, tab, tab64, exptbl, su, sd, ncol, nlay, an, blk, sbuf, swt, cld); break;
   switch (band) {
     RRTMG_SW_CASE(16) RRTMG_SW_CASE(17) RRTMG_SW_CASE(18) RRTMG_SW_CASE(19) RRTMG_SW_CASE(20) RRTMG_SW_CASE(21)
     RRTMG_SW_CASE(22) RRTMG_SW_CASE(23) RRTMG_SW_CASE(24) RRTMG_SW_CASE(25) RRTMG_SW_CASE(26) RRTMG_SW_CASE(27)
@@ -1506,48 +1546,89 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_SW_MINB :
 }
 
 #ifdef RRTMG_DEFINE_COLUMN_KERNELS
+// ---------------------------------------------------------------------------
+// Clouds of the SW call (icld = 1, cloud optics given), one thread per
+// (column, layer): inatm_sw's cldfrac (rrtmg_sw_rad.nomcica.f90:1065-1083);
+// the non-McICA SW computes clear or overcast layers only and stops on a
+// cover in (zepsec, 1 - zepsec), zepsec = 1e-6 (:533-538): such a layer of a
+// sunlit column sets flag bit 1 (reported as invalid input); cldprop_sw keeps a layer's optics
+// when cover >= cldmin and (ciwp + clwp >= cldmin or the band-summed depth >=
+// cldmin), cldmin = 1e-20 (rrtmg_sw_cldprop.f90:120-141).  cld[0][lay][col]:
+// the cover; cld[1][lay][col]: 1 where the optics are kept, else 0.
+// ---------------------------------------------------------------------------
+template <class F>
+__global__ void __launch_bounds__(128) sw_cloud_kernel(SwIn in, F* __restrict__ cld, int ncol, int nlay,
+                                                       unsigned* __restrict__ flags) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncol) return;
+  const size_t o = (size_t)blockIdx.y * ncol + col;
+  const double cf = __ldg(in.cldfr + o);
+  double tauctot = 0.0;
+  for (int ib = 0; ib < kSwBands; ++ib) tauctot = tauctot + __ldg(in.taucld + ib + 14 * o);
+  const double cwp = (in.cicewp ? __ldg(in.cicewp + o) : 0.0) + (in.cliqwp ? __ldg(in.cliqwp + o) : 0.0);
+  const double cldmin = 1.e-20, zepsec = 1.e-06;
+  // the check runs in sunlit columns only: the reference skips the others (:500-509)
+  if (cf > zepsec && cf < 1.0 - zepsec && __ldg(in.coszen + col) >= 1.e-10) atomicOr(flags, 2u);
+  const bool kept = cf >= cldmin && (cwp >= cldmin || tauctot >= cldmin);
+  cld[o] = (F)cf;
+  cld[(size_t)nlay * ncol + o] = kept ? (F)1 : (F)0;
+}
+
 // SW finalize: band sums, outputs, heating (rrtmg_sw_rad.nomcica.f90:688-726);
 // dark columns (coszen < 1e-10) get zeros (:502-510).
+// suc, sdc: the clear-sky band partials of a cloudy call (its clear pass),
+// else null (clear sky: the clear-sky outputs are the total ones).
 __global__ void __launch_bounds__(128) sw_finalize_kernel(const double* __restrict__ su, const double* __restrict__ sd,
                                                           const double* __restrict__ plev,
                                                           const double* __restrict__ coszen, int ncol, int nlay,
                                                           double* swuflx, double* swdflx, double* swhr,
-                                                          double* swuflxc, double* swdflxc, double* swhrc) {
+                                                          double* swuflxc, double* swdflxc, double* swhrc,
+                                                          const double* __restrict__ suc = nullptr,
+                                                          const double* __restrict__ sdc = nullptr) {
   // one thread per (column, level), as the LW finalize
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= ncol) return;
   const int k = blockIdx.y;
   const size_t N = (size_t)ncol;
   const bool lit = __ldg(coszen + col) >= 1.e-10;
-  auto sums = [&](int lv, double& fu, double& fd) {
+  auto sums = [&](const double* u, const double* d, int lv, double& fu, double& fd) {
     fu = 0.0;
     fd = 0.0;
     if (!lit) return;
     for (int b = 0; b < kSwBands; ++b) {
       const size_t o = ((size_t)b * (nlay + 1) + lv) * N + col;
-      fu = fu + __ldg(su + o);
-      fd = fd + __ldg(sd + o);
+      fu = fu + __ldg(u + o);
+      fd = fd + __ldg(d + o);
     }
   };
-  double fu, fd;
-  sums(k, fu, fd);
+  const bool clear_own = suc != nullptr;
+  double fu, fd, fuc, fdc;
+  sums(su, sd, k, fu, fd);
+  if (clear_own) sums(suc, sdc, k, fuc, fdc);
+  else fuc = fu, fdc = fd;
   const size_t oo = (size_t)k * N + col;
   swuflx[oo] = fu;
   swdflx[oo] = fd;
-  swuflxc[oo] = fu;
-  swdflxc[oo] = fd;
+  swuflxc[oo] = fuc;
+  swdflxc[oo] = fdc;
   if (k >= 1) {
     const size_t oh = (size_t)(k - 1) * N + col;
-    double h = 0.0;
+    double h = 0.0, hc = 0.0;
     if (lit && k < nlay) {
-      double fu0, fd0;
-      sums(k - 1, fu0, fd0);
-      const double net = fd - fu, nprev = fd0 - fu0;
       const double zdpgcp = c_sw.heatfac / (__ldg(plev + oo - N) - __ldg(plev + oo));
-      h = (net - nprev) * zdpgcp;
+      double fu0, fd0;
+      sums(su, sd, k - 1, fu0, fd0);
+      h = ((fd - fu) - (fd0 - fu0)) * zdpgcp;
+      if (clear_own) {
+        double fuc0, fdc0;
+        sums(suc, sdc, k - 1, fuc0, fdc0);
+        hc = ((fdc - fuc) - (fdc0 - fuc0)) * zdpgcp;
+      } else {
+        hc = h;
+      }
     }
     swhr[oh] = h;
-    swhrc[oh] = h;
+    swhrc[oh] = hc;
   }
 }
 

@@ -90,18 +90,35 @@ void launch_sw_prep_split(const SwIn& in, const SwWorkT<float>& w, int ncol, int
 }
 
 void launch_sw_gpoint_fp64(const SwPrep& p, const SwIn& in, double adjflux, int iaer, const double* tab,
-                           const double* exptbl, double* su, double* sd, int ncol, int nlay, int nb, int analytic, cudaStream_t s) {
+                           const double* exptbl, double* su, double* sd, int ncol, int nlay, int nb, int analytic,
+                           cudaStream_t s, const double* cld) {
+  if (cld) {
+    if (maxl_for(nlay) == 64)
+      sw_gpoint_kernel<double, 64, -1, true><<<nb, kBlock, 0, s>>>(p, in, adjflux, iaer, tab, tab, exptbl, su, sd, ncol,
+                                                                  nlay, analytic, cld);
+    else
+      sw_gpoint_kernel<double, 208, -1, true><<<nb, kBlock, 0, s>>>(p, in, adjflux, iaer, tab, tab, exptbl, su, sd, ncol,
+                                                                   nlay, analytic, cld);
+    return;
+  }
   if (maxl_for(nlay) == 64)
-    sw_gpoint_kernel<double, 64><<<nb, kBlock, 0, s>>>(p, in, adjflux, iaer, tab, tab, exptbl, su, sd, ncol, nlay, analytic);
+    sw_gpoint_kernel<double, 64><<<nb, kBlock, 0, s>>>(p, in, adjflux, iaer, tab, tab, exptbl, su, sd, ncol, nlay, analytic, nullptr);
   else
-    sw_gpoint_kernel<double, 208><<<nb, kBlock, 0, s>>>(p, in, adjflux, iaer, tab, tab, exptbl, su, sd, ncol, nlay, analytic);
+    sw_gpoint_kernel<double, 208><<<nb, kBlock, 0, s>>>(p, in, adjflux, iaer, tab, tab, exptbl, su, sd, ncol, nlay, analytic, nullptr);
+}
+
+void launch_sw_cloud(const SwIn& in, double* cld, int ncol, int nlay, unsigned* flags, cudaStream_t s) {
+  sw_cloud_kernel<double><<<dim3((ncol + 127) / 128, nlay), 128, 0, s>>>(in, cld, ncol, nlay, flags);
+}
+void launch_sw_cloud_split(const SwIn& in, float* cld, int ncol, int nlay, unsigned* flags, cudaStream_t s) {
+  sw_cloud_kernel<float><<<dim3((ncol + 127) / 128, nlay), 128, 0, s>>>(in, cld, ncol, nlay, flags);
 }
 
 void launch_sw_finalize(const double* su, const double* sd, const double* plev, const double* coszen, int ncol,
                         int nlay, double* swuflx, double* swdflx, double* swhr, double* swuflxc, double* swdflxc,
-                        double* swhrc, cudaStream_t s) {
+                        double* swhrc, cudaStream_t s, const double* suc, const double* sdc) {
   sw_finalize_kernel<<<dim3((ncol + 127) / 128, nlay + 1), 128, 0, s>>>(su, sd, plev, coszen, ncol, nlay, swuflx, swdflx, swhr,
-                                                        swuflxc, swdflxc, swhrc);
+                                                        swuflxc, swdflxc, swhrc, suc, sdc);
 }
 
 }  // namespace rrtmg

@@ -101,47 +101,61 @@ __global__ void __launch_bounds__(128) lw_finalize_split_kernel(const double* __
   }
 }
 
+// suc, sdc: the clear-sky band partials of a cloudy call, else null.
 __global__ void __launch_bounds__(128) sw_finalize_split_kernel(const double* __restrict__ su,
                                                                 const double* __restrict__ sd,
                                                                 const double* __restrict__ plev,
                                                                 const double* __restrict__ coszen, int ncol, int nlay,
                                                                 double* swuflx, double* swdflx, double* swhr,
-                                                                double* swuflxc, double* swdflxc, double* swhrc) {
+                                                                double* swuflxc, double* swdflxc, double* swhrc,
+                                                                const double* __restrict__ suc,
+                                                                const double* __restrict__ sdc) {
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= ncol) return;
   const int lev0 = blockIdx.y * kLevChunk, lev1 = min(nlay, lev0 + kLevChunk - 1);
   const size_t N = (size_t)ncol, bs = (size_t)(nlay + 1) * N;
   const bool lit = __ldg(coszen + col) >= 1.e-10;
-  auto sums = [&](int lv, double& fu, double& fd) {
+  auto sums = [&](const double* u, const double* d, int lv, double& fu, double& fd) {
     fu = 0.0;
     fd = 0.0;
     if (!lit) return;
     const size_t o = (size_t)lv * N + col;
 #pragma unroll
     for (int k = 0; k < kSwBands; ++k) {
-      fu = fu + __ldg(su + k * bs + o);
-      fd = fd + __ldg(sd + k * bs + o);
+      fu = fu + __ldg(u + k * bs + o);
+      fd = fd + __ldg(d + k * bs + o);
     }
   };
-  double fu0 = 0.0, fd0 = 0.0;
-  if (lev0 >= 1) sums(lev0 - 1, fu0, fd0);
+  const bool clear_own = suc != nullptr;
+  double fu0 = 0.0, fd0 = 0.0, fuc0 = 0.0, fdc0 = 0.0;
+  if (lev0 >= 1) {
+    sums(su, sd, lev0 - 1, fu0, fd0);
+    if (clear_own) sums(suc, sdc, lev0 - 1, fuc0, fdc0);
+  }
   for (int lev = lev0; lev <= lev1; ++lev) {
-    double fu, fd;
-    sums(lev, fu, fd);
+    double fu, fd, fuc, fdc;
+    sums(su, sd, lev, fu, fd);
+    if (clear_own) sums(suc, sdc, lev, fuc, fdc);
+    else fuc = fu, fdc = fd;
     const size_t oo = (size_t)lev * N + col;
     swuflx[oo] = fu;
     swdflx[oo] = fd;
-    swuflxc[oo] = fu;
-    swdflxc[oo] = fd;
+    swuflxc[oo] = fuc;
+    swdflxc[oo] = fdc;
     if (lev >= 1) {
-      double h = 0.0;
-      if (lit && lev < nlay)
-        h = ((fd - fu) - (fd0 - fu0)) * (c_sw.heatfac / (__ldg(plev + oo - N) - __ldg(plev + oo)));
+      double h = 0.0, hc = 0.0;
+      if (lit && lev < nlay) {
+        const double zdpgcp = c_sw.heatfac / (__ldg(plev + oo - N) - __ldg(plev + oo));
+        h = ((fd - fu) - (fd0 - fu0)) * zdpgcp;
+        hc = clear_own ? ((fdc - fuc) - (fdc0 - fuc0)) * zdpgcp : h;
+      }
       swhr[oo - N] = h;
-      swhrc[oo - N] = h;
+      swhrc[oo - N] = hc;
     }
     fu0 = fu;
     fd0 = fd;
+    fuc0 = fuc;
+    fdc0 = fdc;
   }
 }
 
@@ -156,10 +170,10 @@ void launch_lw_finalize_split(const double* bu, const double* bd, const double* 
 
 void launch_sw_finalize_split(const double* su, const double* sd, const double* plev, const double* coszen, int ncol,
                               int nlay, double* swuflx, double* swdflx, double* swhr, double* swuflxc,
-                              double* swdflxc, double* swhrc, cudaStream_t s) {
+                              double* swdflxc, double* swhrc, cudaStream_t s, const double* suc, const double* sdc) {
   const dim3 g((ncol + 127) / 128, (nlay + 1 + kLevChunk - 1) / kLevChunk);
   sw_finalize_split_kernel<<<g, 128, 0, s>>>(su, sd, plev, coszen, ncol, nlay, swuflx, swdflx, swhr, swuflxc, swdflxc,
-                                             swhrc);
+                                             swhrc, suc, sdc);
 }
 
 // The split solvers are instantiated per (analytic, idrv / aerosol) flag pair.
@@ -211,25 +225,29 @@ void launch_lw_gpoint_cld_split(const LwPrepT<float>& p, const float* cld, const
                             bdc, bduc, ncol, nlay);
 }
 
-template <int MAXL>
+template <int MAXL, bool TOT>
 static void sw_split_flags(int fl, int nb, cudaStream_t s, const SwPrepT<float>& p, const SwIn& in, double adjflux,
                            int iaer, const float* tab, const double* tab64, const float* exptbl, double* su,
-                           double* sd, int ncol, int nlay, int analytic) {
-  auto k = fl == 0 ? sw_gpoint_kernel<float, MAXL, 0>
-         : fl == 1 ? sw_gpoint_kernel<float, MAXL, 1>
-         : fl == 2 ? sw_gpoint_kernel<float, MAXL, 2>
-                   : sw_gpoint_kernel<float, MAXL, 3>;
-  k<<<nb, kBlock, 0, s>>>(p, in, adjflux, iaer, tab, tab64, exptbl, su, sd, ncol, nlay, analytic);
+                           double* sd, int ncol, int nlay, int analytic, const float* cld) {
+  auto k = fl == 0 ? sw_gpoint_kernel<float, MAXL, 0, TOT>
+         : fl == 1 ? sw_gpoint_kernel<float, MAXL, 1, TOT>
+         : fl == 2 ? sw_gpoint_kernel<float, MAXL, 2, TOT>
+                   : sw_gpoint_kernel<float, MAXL, 3, TOT>;
+  k<<<nb, kBlock, 0, s>>>(p, in, adjflux, iaer, tab, tab64, exptbl, su, sd, ncol, nlay, analytic, cld);
 }
 
 void launch_sw_gpoint_split(const SwPrepT<float>& p, const SwIn& in, double adjflux, int iaer, const float* tab,
                             const double* tab64, const float* exptbl, double* su, double* sd, int ncol, int nlay,
-                            int nb, int analytic, cudaStream_t s) {
+                            int nb, int analytic, cudaStream_t s, const float* cld) {
   const int fl = (analytic ? 1 : 0) | (iaer == 10 ? 2 : 0);
-  if (maxl_for(nlay) == 64)
-    sw_split_flags<64>(fl, nb, s, p, in, adjflux, iaer, tab, tab64, exptbl, su, sd, ncol, nlay, analytic);
-  else
-    sw_split_flags<208>(fl, nb, s, p, in, adjflux, iaer, tab, tab64, exptbl, su, sd, ncol, nlay, analytic);
+  const bool big = maxl_for(nlay) != 64;
+  if (cld) {
+    if (!big) sw_split_flags<64, true>(fl, nb, s, p, in, adjflux, iaer, tab, tab64, exptbl, su, sd, ncol, nlay, analytic, cld);
+    else sw_split_flags<208, true>(fl, nb, s, p, in, adjflux, iaer, tab, tab64, exptbl, su, sd, ncol, nlay, analytic, cld);
+  } else {
+    if (!big) sw_split_flags<64, false>(fl, nb, s, p, in, adjflux, iaer, tab, tab64, exptbl, su, sd, ncol, nlay, analytic, nullptr);
+    else sw_split_flags<208, false>(fl, nb, s, p, in, adjflux, iaer, tab, tab64, exptbl, su, sd, ncol, nlay, analytic, nullptr);
+  }
 }
 
 }  // namespace rrtmg

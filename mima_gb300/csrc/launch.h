@@ -44,11 +44,17 @@ void launch_lw_prep_split(const LwIn& in, const LwWorkT<float>& w, const float* 
                           int ncol, int nlay, int idrv, unsigned* flags, cudaStream_t s);
 void launch_sw_prep_split(const SwIn& in, const SwWorkT<float>& w, int ncol, int nlay, unsigned* flags,
                           cudaStream_t s);
+// cld: per-layer cover and cldprop mask of a cloudy call's total-sky pass, or
+// null (a clear-sky pass).
 void launch_sw_gpoint_fp64(const SwPrep& p, const SwIn& in, double adjflux, int iaer, const double* tab,
-                           const double* exptbl, double* su, double* sd, int ncol, int nlay, int nb, int analytic, cudaStream_t s);
+                           const double* exptbl, double* su, double* sd, int ncol, int nlay, int nb, int analytic,
+                           cudaStream_t s, const double* cld = nullptr);
+// SW clouds (icld = 1): per-layer cover and cldprop mask; flags a partly cloudy layer.
+void launch_sw_cloud(const SwIn& in, double* cld, int ncol, int nlay, unsigned* flags, cudaStream_t s);
+void launch_sw_cloud_split(const SwIn& in, float* cld, int ncol, int nlay, unsigned* flags, cudaStream_t s);
 void launch_sw_finalize(const double* su, const double* sd, const double* plev, const double* coszen, int ncol,
                         int nlay, double* swuflx, double* swdflx, double* swhr, double* swuflxc, double* swdflxc,
-                        double* swhrc, cudaStream_t s);
+                        double* swhrc, cudaStream_t s, const double* suc = nullptr, const double* sdc = nullptr);
 // Split-path finalize: the same outputs with fewer FP64 operations (kernels_split.cu).
 void launch_lw_finalize_split(const double* bu, const double* bd, const double* bdu, const double* plev, int ncol,
                               int nlay, int idrv, double* uflx, double* dflx, double* hr, double* uflxc,
@@ -56,7 +62,8 @@ void launch_lw_finalize_split(const double* bu, const double* bd, const double* 
                               const double* buc = nullptr, const double* bdc = nullptr, const double* bduc = nullptr);
 void launch_sw_finalize_split(const double* su, const double* sd, const double* plev, const double* coszen, int ncol,
                               int nlay, double* swuflx, double* swdflx, double* swhr, double* swuflxc,
-                              double* swdflxc, double* swhrc, cudaStream_t s);
+                              double* swdflxc, double* swhrc, cudaStream_t s, const double* suc = nullptr,
+                              const double* sdc = nullptr);
 
 // FP32-split translation unit.
 void launch_lw_gpoint_split(const LwPrepT<float>& p, const double* emis, const double* tauaer, const float* tab,
@@ -64,7 +71,7 @@ void launch_lw_gpoint_split(const LwPrepT<float>& p, const double* emis, const d
                             int nlay, int idrv, int nb, int analytic, cudaStream_t s);
 void launch_sw_gpoint_split(const SwPrepT<float>& p, const SwIn& in, double adjflux, int iaer, const float* tab,
                             const double* tab64, const float* exptbl, double* su, double* sd, int ncol, int nlay,
-                            int nb, int analytic, cudaStream_t s);
+                            int nb, int analytic, cudaStream_t s, const float* cld = nullptr);
 
 // Number of blocks of the g-point grids: the sum over bands of the band's
 // blocks (4 warps of 32 / lanes columns; lanes = split_lanes(ng, split)).

@@ -157,8 +157,10 @@ def array_sizes(ncol, nlay):
     n.update({k: ncol for k in _PER_COLUMN})
     n.update(emis=16 * ncol, tauaer_lw=16 * nlay * ncol, tauaer=14 * nlay * ncol, ssaaer=14 * nlay * ncol,
              asmaer=14 * nlay * ncol)
-    # LW clouds: cldfr, cicewp, cliqwp (nlay, ncol); taucld Fortran (16, ncol, nlay)
+    # clouds: cldfr, cicewp, cliqwp (nlay, ncol); LW taucld Fortran (16, ncol,
+    # nlay); SW taucld ("taucld_sw"), ssacld, asmcld, fsfcld Fortran (14, ncol, nlay)
     n.update(cldfr=nlay * ncol, cicewp=nlay * ncol, cliqwp=nlay * ncol, taucld=16 * nlay * ncol)
+    n.update({k: 14 * nlay * ncol for k in ("taucld_sw", "ssacld", "asmcld", "fsfcld")})
     return n
 
 
@@ -261,17 +263,23 @@ class RRTMG:
 
     def rrtmg_sw(self, ncol, nlay, icld, iaer, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr,
                  n2ovmr, o2vmr, asdir, asdif, aldir, aldif, coszen, adjes, dyofyr, scon, tauaer=None,
-                 ssaaer=None, asmaer=None, check=True, out=None):
+                 ssaaer=None, asmaer=None, check=True, out=None, inflgsw=0, cldfr=None, taucld=None, ssacld=None,
+                 asmcld=None, fsfcld=None, cicewp=None, cliqwp=None):
+        """rrtmg_sw on host arrays; returns swuflx, swdflx, swhr, swuflxc,
+        swdflxc, swhrc.  Clouds (icld >= 1, inflgsw = 0; every sunlit layer
+        clear or overcast): cldfr, cicewp, cliqwp (nlay, ncol); taucld, ssacld,
+        asmcld, fsfcld (nlay, ncol, 14) = Fortran (14, ncol, nlay)."""
         L, N = nlay, ncol
         ins = [_host(a) for a in (play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr,
                                   asdir, asdif, aldir, aldif, coszen)]
         aer = [_host(a) for a in (tauaer, ssaaer, asmaer)]
+        cl = [_host(a) for a in (cldfr, taucld, ssacld, asmcld, fsfcld, cicewp, cliqwp)]
         out = _outputs(out, {"swuflx": L + 1, "swdflx": L + 1, "swuflxc": L + 1, "swdflxc": L + 1, "swhr": L,
                              "swhrc": L}, N)
         rc = self.lib.rrtmg_sw_c(
             self._h, C.c_int(N), C.c_int(L), C.c_int(icld), C.c_int(iaer), *[_hp(a) for a in ins],
-            C.c_double(adjes), C.c_int(dyofyr), C.c_double(scon), C.c_int(0), C.c_int(0), C.c_int(0),
-            None, None, None, None, None, None, None, None, None, *[_hp(a) for a in aer], None,
+            C.c_double(adjes), C.c_int(dyofyr), C.c_double(scon), C.c_int(inflgsw), C.c_int(0), C.c_int(0),
+            *[_hp(a) for a in cl], None, None, *[_hp(a) for a in aer], None,
             _hp(out["swuflx"]), _hp(out["swdflx"]), _hp(out["swhr"]), _hp(out["swuflxc"]),
             _hp(out["swdflxc"]), _hp(out["swhrc"]))
         out["status"] = rc
@@ -289,11 +297,16 @@ class RRTMG:
                              atm.cfc22, atm.ccl4, atm.emis, tauaer, check=check, cldfr=cl.get("cldfr"),
                              taucld=cl.get("taucld"), cicewp=cl.get("cicewp"), cliqwp=cl.get("cliqwp"))
 
-    def sw(self, atm, iaer=0, tauaer=None, ssaaer=None, asmaer=None, check=True):
-        return self.rrtmg_sw(atm.ncol, atm.nlay, 0, iaer, atm.play, atm.plev, atm.tlay, atm.tlev, atm.tsfc,
-                             atm.h2o, atm.o3, atm.co2, atm.ch4, atm.n2o, atm.o2, atm.asdir, atm.asdif,
+    def sw(self, atm, iaer=0, tauaer=None, ssaaer=None, asmaer=None, check=True, cloud=None):
+        """``cloud``: dict(cldfr, taucld, ssacld, asmcld, fsfcld[, cicewp,
+        cliqwp]) for icld = 1 (given cloud optics), as rrtmg_sw's arguments."""
+        cl = cloud or {}
+        return self.rrtmg_sw(atm.ncol, atm.nlay, 1 if cloud else 0, iaer, atm.play, atm.plev, atm.tlay, atm.tlev,
+                             atm.tsfc, atm.h2o, atm.o3, atm.co2, atm.ch4, atm.n2o, atm.o2, atm.asdir, atm.asdif,
                              atm.aldir, atm.aldif, atm.coszen, atm.adjes, atm.dyofyr, atm.scon,
-                             tauaer, ssaaer, asmaer, check=check)
+                             tauaer, ssaaer, asmaer, check=check,
+                             **{k: cl.get(k) for k in ("cldfr", "taucld", "ssacld", "asmcld", "fsfcld", "cicewp",
+                                                       "cliqwp")})
 
     # ---------------- device-array entry points ----------------
     def _ptrs(self, ncol, nlay, *dicts):
@@ -396,15 +409,22 @@ class RRTMG:
             o("duflxc_dt"))
         self._check(rc)
 
-    def rrtmg_sw_dev(self, stream, ncol, nlay, icld, iaer, d, out, adjes, dyofyr, scon):
+    def rrtmg_sw_dev(self, stream, ncol, nlay, icld, iaer, d, out, adjes, dyofyr, scon, cloud=None):
+        """``d``/``out``: dicts of CUDA tensors with the argument names of
+        rrtmg_sw; ``cloud`` (icld >= 1): dict of CUDA tensors cldfr, taucld,
+        ssacld, asmcld, fsfcld[, cicewp, cliqwp] (shapes as rrtmg_sw's)."""
         g = self._ptrs(ncol, nlay, d)
         o = self._ptrs(ncol, nlay, out)
+        cl = cloud or {}
+        c = [g(k, cl.get(k)) for k in ("cldfr",)] + [g(k + "_sw" if k == "taucld" else k, cl.get(k))
+                                                     for k in ("taucld", "ssacld", "asmcld", "fsfcld")]
+        c += [g(k, cl.get(k)) for k in ("cicewp", "cliqwp")]
         rc = self.lib.rrtmg_sw_dev(
             self._h, C.c_void_p(stream or 0), C.c_int(ncol), C.c_int(nlay), C.c_int(icld), C.c_int(iaer),
             g("play"), g("plev"), g("tlay"), g("tlev"), g("tsfc"), g("h2ovmr"), g("o3vmr"), g("co2vmr"),
             g("ch4vmr"), g("n2ovmr"), g("o2vmr"), g("asdir"), g("asdif"), g("aldir"), g("aldif"),
             g("coszen"), C.c_double(adjes), C.c_int(dyofyr), C.c_double(scon), C.c_int(0), C.c_int(0),
-            C.c_int(0), None, None, None, None, None, None, None, None, None, g("tauaer"), g("ssaaer"),
+            C.c_int(0), *c, None, None, g("tauaer"), g("ssaaer"),
             g("asmaer"), None, o("swuflx"), o("swdflx"), o("swhr"), o("swuflxc"), o("swdflxc"), o("swhrc"))
         self._check(rc)
 

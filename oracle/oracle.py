@@ -132,7 +132,15 @@ def phase_times(atm):
     return out_lw, out_sw
 
 
-def rrtmg_sw(atm, iaer: int = 0, tauaer=None, ssaaer=None, asmaer=None, nthreads: int = 0):
+class PartialCloud(RuntimeError):
+    """A partly cloudy layer in a SW call with clouds: the reference's
+    non-McICA SW stops (rrtmg_sw_rad.nomcica.f90:533-538)."""
+
+
+def rrtmg_sw(atm, iaer: int = 0, tauaer=None, ssaaer=None, asmaer=None, nthreads: int = 0, cloud=None):
+    """rrtmg_sw on ``atm``.  ``cloud`` = dict(cldfr (nlay, ncol), taucld, ssacld,
+    asmcld, fsfcld (nlay, ncol, 14) [Fortran (14, ncol, nlay)], optional cicewp
+    / cliqwp (nlay, ncol)): icld = 1, cloud optics given (inflgsw = 0)."""
     n, L = atm.ncol, atm.nlay
     out = {k: np.zeros((L + 1, n)) for k in ("swuflx", "swdflx", "swuflxc", "swdflxc")}
     out.update({k: np.zeros((L, n)) for k in ("swhr", "swhrc")})
@@ -140,11 +148,17 @@ def rrtmg_sw(atm, iaer: int = 0, tauaer=None, ssaaer=None, asmaer=None, nthreads
             _f(atm.o3), _f(atm.co2), _f(atm.ch4), _f(atm.n2o), _f(atm.o2), _f(atm.asdir),
             _f(atm.asdif), _f(atm.aldir), _f(atm.aldif), _f(atm.coszen)]
     aer = [None if a is None else _f(a) for a in (tauaer, ssaaer, asmaer)]
-    rc = _lib.orc_rrtmg_sw(C.c_int(n), C.c_int(L), C.c_int(0), C.c_int(iaer), *[_p(a) for a in args],
+    cl = cloud or {}
+    carg = [None if cl.get(k) is None else _f(cl[k])
+            for k in ("cldfr", "taucld", "ssacld", "asmcld", "fsfcld", "cicewp", "cliqwp")]
+    rc = _lib.orc_rrtmg_sw(C.c_int(n), C.c_int(L), C.c_int(1 if cloud else 0), C.c_int(iaer),
+                           *[_p(a) for a in args],
                            C.c_double(atm.adjes), C.c_int(atm.dyofyr), C.c_double(atm.scon),
                            *[_p(a) for a in aer],
                            _p(out["swuflx"]), _p(out["swdflx"]), _p(out["swhr"]), _p(out["swuflxc"]),
-                           _p(out["swdflxc"]), _p(out["swhrc"]), C.c_int(nthreads))
+                           _p(out["swdflxc"]), _p(out["swhrc"]), C.c_int(nthreads), *[_p(a) for a in carg])
+    if rc == 4:
+        raise PartialCloud("a layer is partly cloudy (0 < cldfr < 1): not computed without McICA")
     if rc != 0:
         raise RuntimeError(f"orc_rrtmg_sw failed ({rc})")
     return out

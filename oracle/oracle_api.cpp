@@ -97,19 +97,35 @@ int orc_rrtmg_sw(int ncol, int nlay, int icld, int iaer, const double* play, con
                  const double* o2vmr, const double* asdir, const double* asdif, const double* aldir,
                  const double* aldif, const double* coszen, double adjes, int dyofyr, double scon,
                  const double* tauaer, const double* ssaaer, const double* asmaer, double* swuflx,
-                 double* swdflx, double* swhr, double* swuflxc, double* swdflxc, double* swhrc, int nthreads) {
+                 double* swdflx, double* swhr, double* swuflxc, double* swdflxc, double* swhrc, int nthreads,
+                 const double* cldfr, const double* taucld, const double* ssacld, const double* asmcld,
+                 const double* fsfcld, const double* cicewp, const double* cliqwp) {
   if (!g_ready) return 2;
-  if (icld != 0) return 3;
+  if (icld != 0 && !(icld == 1 && cldfr && taucld && ssacld && asmcld && fsfcld)) return 3;
   if (iaer != 0 && iaer != 10) return 3;
   SwInput in{ncol, nlay, iaer, dyofyr, adjes, scon, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr,
              ch4vmr, n2ovmr, o2vmr, asdir, asdif, aldir, aldif, coszen, tauaer, ssaaer, asmaer};
+  in.icld = icld;
+  in.cldfr = cldfr;
+  in.taucld = taucld;
+  in.ssacld = ssacld;
+  in.asmcld = asmcld;
+  in.fsfcld = fsfcld;
+  in.cicewp = cicewp;
+  in.cliqwp = cliqwp;
+  int partial = 0;
 #pragma omp parallel num_threads(nthreads > 0 ? nthreads : orc_max_threads())
   {
     SwColumn c;
     SwOut o;
 #pragma omp for schedule(dynamic, 16)
     for (int iplon = 0; iplon < ncol; ++iplon) {
-      sw_column(in, iplon, c, o);
+      bool part = false;
+      sw_column(in, iplon, c, o, &part);
+      if (part) {
+#pragma omp atomic write
+        partial = 1;
+      }
       for (int k = 1; k <= nlay + 1; ++k) {
         size_t ix = (size_t)iplon + (size_t)ncol * (size_t)(k - 1);
         swuflx[ix] = o.fu[k];
@@ -124,7 +140,7 @@ int orc_rrtmg_sw(int ncol, int nlay, int icld, int iaer, const double* play, con
       }
     }
   }
-  return 0;
+  return partial ? 4 : 0;  // 4: a partly cloudy layer (the reference stops)
 }
 
 // Clear-sky rrtmg_lw per band: bandu/bandd/dbandu_dt (ncol, nlay+1, 16) are the

@@ -1,5 +1,8 @@
 // CPU oracle, shortwave -- TEST INFRASTRUCTURE ONLY (the checker, never the
-// product).  FP64 restatement of the reference's clear-sky RRTMG_SW path:
+// product).  FP64 restatement of the reference's RRTMG_SW path (clear sky, and
+// clear or overcast layers with given cloud optics: icld = 1, inflgsw = 0 --
+// cldprop_sw rrtmg_sw_cldprop.f90:118-156, the clear / cloudy combination of
+// spcvrt_sw):
 //   inatm_sw    rrtmg_sw_rad.nomcica.f90:761-1101
 //   driver      rrtmg_sw_rad.nomcica.f90:78-731 (coszen skip :502-510,
 //               albedo bands :566-578, heating :712-726)
@@ -834,7 +837,7 @@ void sw_spcvrt(SwColumn& c, double prmu0, const double* albdir, const double* al
       for (int jk = 1; jk <= klev; ++jk) {
         int ikl = klev + 1 - jk;
         lrtchkclr[jk] = 1;
-        lrtchkcld[jk] = 0;  // pclfr = 0 > repclc is false
+        lrtchkcld[jk] = c.pclfr[ikl] > 1.e-12;  // pclfr > repclc (:263, :388)
         double taua = c.taua[ibm][ikl], omga = c.ssaa[ibm][ikl], asya = c.asma[ibm][ikl];
         ztauc[jk] = c.taur[iw][ikl] + c.taug[iw][ikl] + taua;
         zomcc[jk] = c.taur[iw][ikl] * 1.0 + taua * omga;
@@ -845,9 +848,9 @@ void sw_spcvrt(SwColumn& c, double prmu0, const double* albdir, const double* al
         ztauc[jk] = (1.0 - zwf) * ztauc[jk];
         zomcc[jk] = (zomcc[jk] - zwf) / (1.0 - zwf);
         zgcc[jk] = (zgcc[jk] - zf) / (1.0 - zf);
-        // icpr >= 1 with ptauc = 0, pomgc = 1, pasyc = 0
+        // icpr >= 1 (:459-464); clear sky: ptauc = 0, pomgc = 1, pasyc = 0
         OPC_PAUSE();
-        const double ptauc = 0.0, pomgc = 1.0, pasyc = 0.0;
+        const double ptauc = c.ptauc[ibm][ikl], pomgc = c.pomgc[ibm][ikl], pasyc = c.pasyc[ibm][ikl];
         ztauo[jk] = ztauc[jk] + ptauc;
         zomco[jk] = ztauc[jk] * zomcc[jk] + ptauc * pomgc;
         zgco[jk] = (ptauc * pomgc * pasyc + ztauc[jk] * zomcc[jk] * zgcc[jk]) / zomco[jk];
@@ -860,7 +863,8 @@ void sw_spcvrt(SwColumn& c, double prmu0, const double* albdir, const double* al
       OPC_RESUME();
       for (int jk = 1; jk <= klev; ++jk) {
         OPC_PAUSE();
-        const double zclear = 1.0 - 0.0, zcloud = 0.0;
+        const int ikl = klev + 1 - jk;
+        const double zclear = 1.0 - c.pclfr[ikl], zcloud = c.pclfr[ikl];
         zref[jk] = zclear * zrefc[jk] + zcloud * zrefo[jk];
         zrefd[jk] = zclear * zrefdc[jk] + zcloud * zrefdo[jk];
         ztra[jk] = zclear * ztrac[jk] + zcloud * ztrao[jk];
@@ -892,9 +896,43 @@ void sw_spcvrt(SwColumn& c, double prmu0, const double* albdir, const double* al
   }
 }
 
-bool sw_column(const SwInput& in, int iplon, SwColumn& c, SwOut& out) {
+// cldprop_sw with inflag = 0 (rrtmg_sw_cldprop.f90:118-156): the optics of a
+// layer whose cover is >= cldmin and whose water path or band-summed depth is
+// >= cldmin (1e-20) are delta-M scaled with the forward-scattering fraction;
+// other layers keep taucloud = 0, ssacloud = 1, asmcloud = 0.
+static void sw_cldprop(const SwInput& in, int iplon, SwColumn& c) {
+  const int nl = in.nlay, ncol = in.ncol;
+  const double cldmin = 1.e-20;
+  for (int lay = 1; lay <= nl; ++lay) {
+    const size_t o = (size_t)iplon + (size_t)ncol * (size_t)(lay - 1);
+    c.pclfr[lay] = in.cldfr[o];
+    double tauctot = 0.0;
+    for (int n = 0; n < 14; ++n) tauctot = tauctot + in.taucld[(size_t)n + 14 * o];
+    const double cwp = (in.cicewp ? in.cicewp[o] : 0.0) + (in.cliqwp ? in.cliqwp[o] : 0.0);
+    for (int ibm = 1; ibm <= 14; ++ibm) {
+      c.ptauc[ibm][lay] = 0.0;
+      c.pomgc[ibm][lay] = 1.0;
+      c.pasyc[ibm][lay] = 0.0;
+    }
+    if (c.pclfr[lay] >= cldmin && (cwp >= cldmin || tauctot >= cldmin)) {
+      for (int ibm = 1; ibm <= 14; ++ibm) {
+        const size_t q = (size_t)(ibm - 1) + 14 * o;
+        const double taucldorig_a = in.taucld[q];
+        const double ffp = in.fsfcld[q];
+        const double ffp1 = 1.0 - ffp;
+        const double ffpssa = 1.0 - ffp * in.ssacld[q];
+        c.pomgc[ibm][lay] = ffp1 * in.ssacld[q] / ffpssa;
+        c.ptauc[ibm][lay] = ffpssa * taucldorig_a;
+        c.pasyc[ibm][lay] = (in.asmcld[q] - ffp) / (ffp1);
+      }
+    }
+  }
+}
+
+bool sw_column(const SwInput& in, int iplon, SwColumn& c, SwOut& out, bool* partial) {
   const double zepzen = 1.e-10;
   int nl = in.nlay;
+  if (partial) *partial = false;
   if (in.coszen[iplon] < zepzen) {
     out.fu.assign(nl + 2, 0.);
     out.fd.assign(nl + 2, 0.);
@@ -905,6 +943,15 @@ bool sw_column(const SwInput& in, int iplon, SwColumn& c, SwOut& out) {
     return false;
   }
   sw_inatm(in, iplon, c);
+  if (in.icld >= 1) {
+    // without McICA the SW computes clear or overcast layers only (:533-538)
+    const double zepsec = 1.e-06, oneminus = 1.0 - zepsec;
+    for (int i = 1; i <= nl; ++i) {
+      const double f = in.cldfr[(size_t)iplon + (size_t)in.ncol * (size_t)(i - 1)];
+      if (f > zepsec && f < oneminus && partial) *partial = true;
+    }
+    sw_cldprop(in, iplon, c);
+  }
   sw_setcoef(c);
   double cossza = in.coszen[iplon];
   if (cossza < zepzen) cossza = zepzen;

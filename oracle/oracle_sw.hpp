@@ -27,6 +27,11 @@ struct SwInput {
   const double *play, *plev, *tlay, *tlev, *tsfc, *h2ovmr, *o3vmr, *co2vmr, *ch4vmr, *n2ovmr, *o2vmr;
   const double *asdir, *asdif, *aldir, *aldif, *coszen;
   const double *tauaer, *ssaaer, *asmaer;
+  // Clouds (icld = 1, inflgsw = 0): cldfr (ncol, nlay); taucld, ssacld, asmcld,
+  // fsfcld (14, ncol, nlay); cicewp / cliqwp (ncol, nlay) or null.
+  int icld = 0;
+  const double *cldfr = nullptr, *taucld = nullptr, *ssacld = nullptr, *asmcld = nullptr, *fsfcld = nullptr,
+               *cicewp = nullptr, *cliqwp = nullptr;
 };
 
 struct SwColumn {
@@ -39,6 +44,8 @@ struct SwColumn {
   std::vector<double> colh2o, colco2, colo3, coln2o, colch4, colo2, colmol;
   std::vector<double> fac00, fac01, fac10, fac11, selffac, selffrac, forfac, forfrac;
   std::vector<double> taug[113], taur[113];
+  // clouds: cover and cldprop_sw's delta-scaled cloud optics per band (ibm 1..14)
+  std::vector<double> pclfr, ptauc[15], pomgc[15], pasyc[15];
   double sfluxzen[113];
 
   void resize(int nl) {
@@ -54,6 +61,12 @@ struct SwColumn {
     r(fac00); r(fac01); r(fac10); r(fac11); r(selffac); r(selffrac); r(forfac); r(forfrac);
     for (auto& v : taug) r(v);
     for (auto& v : taur) r(v);
+    r(pclfr);
+    for (int b = 0; b < 15; ++b) {
+      r(ptauc[b]);
+      pomgc[b].assign(nl + 2, 1.0);
+      r(pasyc[b]);
+    }
     for (int g = 0; g < 113; ++g) sfluxzen[g] = 0.0;
     for (int b = 0; b < 30; ++b) adjflux[b] = 0.0;
   }
@@ -72,6 +85,9 @@ void sw_taumol(SwColumn& c);
 // timing of the oracle); the results are the same.
 void sw_spcvrt(SwColumn& c, double prmu0, const double* albdir, const double* albdif, SwOut& out,
                bool run_taumol = true);
-bool sw_column(const SwInput& in, int iplon, SwColumn& c, SwOut& out);
+// Returns false for a dark column (no SW); sets *partial when the column holds
+// a partly cloudy layer, which the reference's non-McICA SW refuses
+// (rrtmg_sw_rad.nomcica.f90:533-538).
+bool sw_column(const SwInput& in, int iplon, SwColumn& c, SwOut& out, bool* partial = nullptr);
 
 }  // namespace orc

@@ -48,15 +48,35 @@ def _col(a, c):
     return a[..., [c]] if isinstance(a, np.ndarray) else a
 
 
-def _perturbed(atm, aer, c, s, what):
+def _cloud_col(cloud, c, s, scale):
+    """Column c of the cloud fields ((nlay, ncol) or (nlay, ncol, nband)), the
+    cloud optical depths scaled by 1 + s when `scale`."""
+    if cloud is None:
+        return None
+    out = {k: (v[:, [c]] if v.ndim == 2 else v[:, [c], :]) for k, v in cloud.items() if v is not None}
+    if scale:
+        out["taucld"] = out["taucld"] * (1.0 + s)
+    return out
+
+
+def _perturbed(atm, aer, c, s, what, cloud=None):
+    """Column c with the inputs named by `what` scaled by 1 + s: "gas" the gas
+    amounts, "aer" the aerosol optical depths, "both" the two, "cld" the cloud
+    optical depths, "gas+cld" gases and clouds.  Returns the column, its
+    aerosol arguments and its cloud fields (None without clouds)."""
     sub = atm.subset(np.array([c]))
     a = {k: _col(v, c) for k, v in aer.items()}
-    if what in ("gas", "both"):
+    if what in ("gas", "both", "gas+cld"):
         for g in GASES:
             setattr(sub, g, getattr(sub, g) * (1.0 + s))
     if what in ("aer", "both") and "tauaer" in a:
         a["tauaer"] = a["tauaer"] * (1.0 + s)
-    return sub, a
+    return sub, a, _cloud_col(cloud, c, s, what in ("cld", "gas+cld"))
+
+
+def _whats(aer, cloud):
+    w = ("aer", "gas", "both") if "tauaer" in aer else ("gas",)
+    return w + (("cld", "gas+cld") if cloud is not None else ())
 
 
 def _misses(out, ref, flux_keys, hr_key, bar, hr_limit=None):
@@ -74,9 +94,10 @@ def _misses(out, ref, flux_keys, hr_key, bar, hr_limit=None):
     return m
 
 
-def check_sw(orc, atm, out, ref, aer=None, heating=True, max_excused_frac=0.02, hr_limit=None):
+def check_sw(orc, atm, out, ref, aer=None, heating=True, max_excused_frac=0.02, hr_limit=None, cloud=None):
     """Assert the split SW outputs `out` meet the bars against the oracle's
-    `ref`, every missing column justified by the backward-error criterion.
+    `ref`, every missing column justified by the backward-error criterion
+    (with `cloud`, the cloud optical depths are among the perturbed inputs).
     Returns the excused columns [(column, scale, what)]."""
     aer = aer or {}
     hk = "swhr" if heating else None
@@ -85,11 +106,11 @@ def check_sw(orc, atm, out, ref, aer=None, heating=True, max_excused_frac=0.02, 
     excused = []
     for c in miss:
         o = {k: out[k][:, [c]] for k in ("swuflx", "swdflx", "swhr")}
-        for what in (("aer", "gas", "both") if "tauaer" in aer else ("gas",)):
+        for what in _whats(aer, cloud):
             hit = None
             for s in PERTURB:
-                sub, a = _perturbed(atm, aer, c, s, what)
-                r = orc.rrtmg_sw(sub, **a)
+                sub, a, cl = _perturbed(atm, aer, c, s, what, cloud)
+                r = orc.rrtmg_sw(sub, cloud=cl, **a)
                 if not _misses(o, r, ("swuflx", "swdflx"), hk, bar[:, [c]], hr_limit)[0]:
                     hit = s
                     break
@@ -115,7 +136,7 @@ def check_lw(orc, atm, out, ref, idrv=0, tauaer=None, heating=True, max_excused_
         ta = None if tauaer is None else tauaer[..., [c]]
         hit = None
         for s in PERTURB:
-            sub, _ = _perturbed(atm, {}, c, s, "gas")
+            sub, _, _ = _perturbed(atm, {}, c, s, "gas")
             r = orc.rrtmg_lw(sub, idrv=idrv, tauaer=ta)
             if not _misses(o, r, ("uflx", "dflx"), hk, bar[:, [c]], hr_limit)[0]:
                 hit = s

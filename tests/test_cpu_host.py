@@ -260,6 +260,15 @@ def test_device_wrappers_follow_the_header():
     exp = {k: ptr[k] for k in p if k in ptr}
     exp.update({k: None for k in cloud_lw + ["ssacld", "asmcld", "fsfcld", "ecaer"]})
     _check_positions(r.lib.calls["rrtmg_sw_dev"], p, exp)
+    # SW clouds come from the cloud keyword (14-band arrays), never the input dict
+    cl = {"cldfr": fake["cldfr"], "taucld": fake["taucld_sw"], "ssacld": fake["ssacld"], "asmcld": fake["asmcld"],
+          "fsfcld": fake["fsfcld"], "cicewp": fake["cicewp"]}
+    r.rrtmg_sw_dev(0, ncol, nlay, 1, 0, fake, fake, 1.0, 0, 1360.0, cloud=cl)
+    exp.update({k: C.cast(t.data_ptr(), C.c_void_p).value for k, t in cl.items()})
+    exp.update(cliqwp=None)
+    _check_positions(r.lib.calls["rrtmg_sw_dev"], p, exp)
+    with pytest.raises(ValueError):  # a per-layer array is too small for the 14-band taucld
+        r.rrtmg_sw_dev(0, ncol, nlay, 1, 0, fake, fake, 1.0, 0, 1360.0, cloud={**cl, "taucld": fake["cldfr"]})
     # rrtmg_step_dev
     r.rrtmg_step_dev(0, ncol, nlay, fake, fake, fake, 1.0, 0, 1360.0, idrv=1, iaer=10,
                      tauaer_lw=fake["tauaer_lw"])

@@ -290,3 +290,86 @@ def test_lw_clouds_random_overlap(orc):
     assert np.allclose(zero["uflx"], clear["uflx"], rtol=1e-12, atol=1e-9)
     tiny = orc.rrtmg_lw(atm, cloud=dict(cldfr=cf * 5e-7, taucld=tau))
     assert np.array_equal(tiny["uflx"], clear["uflx"])
+
+
+def sw_cloud_fields(atm, rng, partial_night=True):
+    """Seeded SW clouds below 100 hPa: every layer clear or overcast (cover 0 or
+    1; a few at 5e-7 and 1 - 5e-7, inside the reference's 1e-6 margins),
+    per-band optical depths up to 75, single-scattering albedo 0.8-1,
+    asymmetry 0.7-0.9 with the delta-M forward fraction g^2; some overcast
+    layers without depth or water path.  With ``partial_night``, unlit columns
+    carry partly cloudy layers (the reference checks sunlit columns only)."""
+    L, n = atm.nlay, atm.ncol
+    u = rng.uniform(size=(L, n))
+    cf = np.where(u < 0.3, 1.0, 0.0)
+    cf[u > 0.98] = 5e-7
+    cf[(u > 0.96) & (u <= 0.98)] = 1.0 - 5e-7
+    cf = np.where(atm.play > 100.0, cf, 0.0)
+    if partial_night:
+        night = np.asarray(atm.coszen) < 1e-10
+        cf[:, night] = rng.uniform(0.2, 0.8, (L, int(night.sum())))
+    tau = (rng.uniform(0.0, 1.0, (L, n, 1)) ** 3 * 50.0) * rng.uniform(0.5, 1.5, (L, n, 14))
+    tau[rng.uniform(size=(L, n)) < 0.03] = 0.0
+    ssa = rng.uniform(0.8, 1.0, (L, n, 14))
+    ssa[rng.uniform(size=(L, n, 14)) < 0.05] = 1.0
+    asm = rng.uniform(0.7, 0.9, (L, n, 14))
+    return dict(cldfr=cf, taucld=tau, ssacld=ssa, asmcld=asm, fsfcld=asm * asm)
+
+
+def test_sw_clouds_overcast(orc):
+    """The oracle's SW clouds (icld = 1, cldprop_sw inflag = 0, spcvrt's
+    clear/total passes):
+    * icld = 1 with no cloud reproduces clear sky bit for bit, and the
+      clear-sky outputs of a cloudy call are the clear-sky call's;
+    * a thick overcast layer raises the reflected flux at the top and cuts
+      the surface downward flux;
+    * a scattering-only cloud (albedo 1) over a transparent column with black
+      ground sends all the sunlight either back up or down to the ground;
+    * an overcast layer without depth or water path keeps no cloud optics;
+    * a partly cloudy sunlit layer is refused as the reference stops, a partly
+      cloudy unlit one is not looked at."""
+    from oracle import oracle as O
+    atm = A.small_atmosphere(24, 40, seed=5)
+    L, n = atm.nlay, atm.ncol
+    z14 = np.zeros((L, n, 14))
+    clear = orc.rrtmg_sw(atm)
+    none = orc.rrtmg_sw(atm, cloud=dict(cldfr=np.zeros((L, n)), taucld=z14, ssacld=z14 + 1, asmcld=z14,
+                                        fsfcld=z14))
+    for k in clear:
+        assert np.array_equal(none[k], clear[k]), k
+    k = 10
+    cf = np.zeros((L, n))
+    cf[k] = 1.0
+    tau, ssa, asm = z14.copy(), z14 + 0.999, z14 + 0.85
+    tau[k] = 40.0
+    cl = dict(cldfr=cf, taucld=tau, ssacld=ssa, asmcld=asm, fsfcld=asm * asm)
+    over = orc.rrtmg_sw(atm, cloud=cl)
+    for name in ("swuflx", "swdflx", "swhr"):
+        assert np.array_equal(over[name + "c" if name != "swhr" else "swhrc"], clear[name]), name
+    assert np.all(over["swuflx"][-1] > 2.0 * clear["swuflx"][-1])
+    assert np.all(over["swdflx"][0] < 0.6 * clear["swdflx"][0])
+    # cover without depth or water path: no cloud optics (rounding only)
+    noop = orc.rrtmg_sw(atm, cloud=dict(cl, taucld=z14))
+    assert np.allclose(noop["swuflx"], clear["swuflx"], rtol=1e-12, atol=1e-9)
+    # scattering-only cloud, no absorbers, black ground: up at the top + down at the ground = incident
+    dry = A.small_atmosphere(6, 40, seed=3)
+    for g in ("h2o", "o3", "co2", "ch4", "n2o", "o2"):
+        setattr(dry, g, np.zeros_like(getattr(dry, g)))
+    for a in ("asdir", "asdif", "aldir", "aldif"):
+        setattr(dry, a, np.zeros_like(getattr(dry, a)))
+    cfd = np.zeros((L, dry.ncol))
+    cfd[k] = 1.0
+    taud = np.zeros((L, dry.ncol, 14))
+    taud[k] = 25.0
+    sca = dict(cldfr=cfd, taucld=taud, ssacld=taud * 0 + 1.0, asmcld=taud * 0 + 0.85, fsfcld=taud * 0 + 0.85 ** 2)
+    s = orc.rrtmg_sw(dry, cloud=sca)
+    assert np.allclose(s["swuflx"][-1] + s["swdflx"][0], s["swdflx"][-1], rtol=1e-6)
+    assert np.all(s["swuflx"][-1] > 0.3 * s["swdflx"][-1])
+    # partial cover: refused in a sunlit column, ignored in an unlit one
+    part = dict(cl, cldfr=cf * 0.5)
+    with pytest.raises(O.PartialCloud):
+        orc.rrtmg_sw(atm, cloud=part)
+    night = A.small_atmosphere(24, 40, seed=5)
+    night.coszen = np.zeros_like(night.coszen)
+    dark = orc.rrtmg_sw(night, cloud=part)
+    assert not any(np.any(v) for v in dark.values())

@@ -24,8 +24,10 @@
  *     zeroes htr(nlayers), which lies above the last output layer).
  *   - Optional gas arrays (ch4, n2o, o2, cfc*) and tauaer may be NULL (= 0).
  *   - Clouds: rrtmg_lw_c / rrtmg_lw_dev compute icld = 1 (random overlap,
- *     rrtmg_lw_rtrn.f90) with the cloud optical depths given (inflglw = 0,
- *     rrtmg_lw_cldprop.f90:165-171): cldfr (ncol,nlay), taucld (16,ncol,nlay),
+ *     rrtmg_lw_rtrn.f90) and icld = 2 / 3 (maximum/random overlap,
+ *     rrtmg_lw_rtrnmr.f90, where the non-McICA driver sends both,
+ *     rrtmg_lw_rad.nomcica.f90:527-541) with the cloud optical depths given
+ *     (inflglw = 0, rrtmg_lw_cldprop.f90:165-171): cldfr (ncol,nlay), taucld (16,ncol,nlay),
  *     cicewp / cliqwp (ncol,nlay) or NULL (they only decide, with the band sum
  *     of taucld, whether a layer's depths are kept); reice, reliq and the ice /
  *     liquid flags are unused.  rrtmg_sw_c / rrtmg_sw_dev compute icld = 1,
@@ -38,8 +40,8 @@
  *     the reference stops the program.  Every other entry point is clear sky
  *     (icld = 0).  The reference coerces icld and iaer silently (:437,
  *     :471-479); this library returns RRTMG_ERR_UNSUPPORTED for any
- *     configuration it does not compute (LW icld = 2 / 3, inflglw or inflgsw
- *     = 1 / 2, icld outside 0..3) and never falls back to a CPU path.
+ *     configuration it does not compute (inflglw or inflgsw = 1 / 2, icld
+ *     outside 0..3) and never falls back to a CPU path.
  *   - Every entry point returns a status (0 = success).  A handle is not
  *     thread-safe; use one handle per host thread.
  */
@@ -55,8 +57,8 @@ typedef struct rrtmg_gpu_state* rrtmg_gpu_handle;
 enum rrtmg_gpu_status {
   RRTMG_OK = 0,
   RRTMG_ERR_ARG = 1,          /* bad dimension, null required pointer, bad handle */
-  RRTMG_ERR_UNSUPPORTED = 2,  /* LW icld not in {0,1}, SW icld not in 0..3, cloud physics (inflglw/inflgsw != 0),
-                                 iaer not in {0,10}, idrv not in {0,1} */
+  RRTMG_ERR_UNSUPPORTED = 2,  /* icld not in 0..3, cloud physics (inflglw/inflgsw != 0), iaer not in {0,10},
+                                 idrv not in {0,1} */
   RRTMG_ERR_CUDA = 3,         /* CUDA runtime error (see rrtmg_gpu_last_error) */
   RRTMG_ERR_TABLES = 4,       /* table blob missing, malformed or checksum mismatch */
   RRTMG_ERR_INPUT = 5,        /* device-side validation flagged a non-finite or out-of-range input, or a
@@ -105,8 +107,8 @@ long long rrtmg_gpu_launch_count(rrtmg_gpu_handle h);
 /* rrtmg_lw (rrtmg_lw_rad.nomcica.f90:80-89), host arrays.  tauaer (ncol,nlay,16)
  * is always added to the gas optical depth (the reference forces iaer = 10,
  * :442).  duflx_dt/duflxc_dt (ncol,nlay+1) are written when idrv = 1.  With
- * icld = 1 the clear-sky outputs (uflxc, dflxc, hrc, duflxc_dt) are rtrn's
- * clear-sky stream, else they equal the total ones. */
+ * clouds (icld >= 1) the clear-sky outputs (uflxc, dflxc, hrc, duflxc_dt) are
+ * the solver's clear-sky stream, else they equal the total ones. */
 int rrtmg_lw_c(rrtmg_gpu_handle h, int ncol, int nlay, int icld, int idrv,
                const double* play, const double* plev, const double* tlay, const double* tlev,
                const double* tsfc, const double* h2ovmr, const double* o3vmr, const double* co2vmr,

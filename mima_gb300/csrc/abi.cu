@@ -137,8 +137,9 @@ struct Carver {
 };
 
 // cloudy: also the per-layer cloud fields and the clear-sky band partials
-// (icld = 1); clear-sky calls carve neither.
-LwWork carve_lw(void* base, int ncol, int nlay, size_t* bytes, bool cloudy = false) {
+// (icld >= 1), and with maximum/random overlap (icld = 2, 3) the overlap
+// factors; clear-sky calls carve none of them.
+LwWork carve_lw(void* base, int ncol, int nlay, size_t* bytes, bool cloudy = false, bool maxrand = false) {
   Carver c{(char*)base};
   const size_t N = (size_t)ncol, L = (size_t)nlay;
   LwWork w{};
@@ -159,6 +160,7 @@ LwWork carve_lw(void* base, int ncol, int nlay, size_t* bytes, bool cloudy = fal
     w.buc = c.take<double>(16 * (L + 1) * N);
     w.bdc = c.take<double>(16 * (L + 1) * N);
     w.bduc = c.take<double>(16 * (L + 1) * N);
+    if (maxrand) w.ovl = c.take<double>(12 * L * N);
   }
   if (bytes) *bytes = c.off;
   return w;
@@ -197,7 +199,7 @@ int check_dims(rrtmg_gpu_state* h, int ncol, int nlay) {
 template <class F>
 LwWorkT<F> work_as(const LwWork& w) {
   return LwWorkT<F>{w.idx, (F*)w.f, (F*)w.planklay, (F*)w.planklev, (F*)w.plankbnd, (F*)w.dplankbnd, (F*)w.secdiff,
-                    w.laytrop, w.bu, w.bd, w.bdu, w.colsum, (F*)w.cld, w.buc, w.bdc, w.bduc};
+                    w.laytrop, w.bu, w.bd, w.bdu, w.colsum, (F*)w.cld, w.buc, w.bdc, w.bduc, (F*)w.ovl};
 }
 template <class F>
 SwWorkT<F> work_as(const SwWork& w) {
@@ -227,31 +229,34 @@ void mark(rrtmg_gpu_state* h, int fam, int k, cudaStream_t s) {
 int lw_enqueue(rrtmg_gpu_state* h, cudaStream_t s, void* base, int ncol, int nlay, int idrv, const LwIn& in,
                double* uflx, double* dflx, double* hr, double* uflxc, double* dflxc, double* hrc, double* duflx_dt,
                double* duflxc_dt) {
-  // clouds (icld = 1): the call carries cloud arrays
-  const bool cloudy = in.cldfr != nullptr;
-  LwWork w = carve_lw(base, ncol, nlay, nullptr, cloudy);
+  // clouds (icld >= 1): the call carries cloud arrays; icld = 2, 3:
+  // maximum/random overlap with its overlap factors
+  const bool cloudy = in.cldfr != nullptr, maxrand = cloudy && in.icld >= 2;
+  LwWork w = carve_lw(base, ncol, nlay, nullptr, cloudy, maxrand);
   mark(h, 0, 0, s);
   const int nb = lw_gpoint_blocks(h->host.lw, ncol, h->precision == RRTMG_PREC_SPLIT);
   if (h->precision == RRTMG_PREC_SPLIT) {
     const LwWorkT<float> w32 = work_as<float>(w);
     launch_lw_prep_split(in, w32, h->totplnk32, h->totplnkderiv32, ncol, nlay, idrv, h->flags, s);
     if (cloudy) launch_lw_cloud_split(in, w32.cld, ncol, nlay, s);
+    if (maxrand) launch_lw_overlap_split(in.cldfr, w32.ovl, ncol, nlay, s);
     mark(h, 0, 1, s);
     if (cloudy)
       launch_lw_gpoint_cld_split(prep_of(w32), w32.cld, in.taucld, in.emis, in.tauaer, h->lw_tab32, h->lw_exp32,
                                  h->lw_tfn32, h->lw_tau32, w.bu, w.bd, w.bdu, w.buc, w.bdc, w.bduc, ncol, nlay, idrv,
-                                 nb, h->analytic, s);
+                                 nb, h->analytic, s, w32.ovl);
     else
       launch_lw_gpoint_split(prep_of(w32), in.emis, in.tauaer, h->lw_tab32, h->lw_exp32, h->lw_tfn32, w.bu, w.bd,
                              w.bdu, ncol, nlay, idrv, nb, h->analytic, s);
   } else {
     launch_lw_prep(in, w, h->totplnk, h->totplnkderiv, ncol, nlay, idrv, h->flags, s);
     if (cloudy) launch_lw_cloud(in, w.cld, ncol, nlay, s);
+    if (maxrand) launch_lw_overlap(in.cldfr, w.ovl, ncol, nlay, s);
     mark(h, 0, 1, s);
     if (cloudy)
       launch_lw_gpoint_cld_fp64(prep_of(w), w.cld, in.taucld, in.emis, in.tauaer, h->lw_tab64, h->lw_exp64,
                                 h->lw_tfn64, h->lw_tau64, w.bu, w.bd, w.bdu, w.buc, w.bdc, w.bduc, ncol, nlay, idrv,
-                                nb, h->analytic, s);
+                                nb, h->analytic, s, w.ovl);
     else
       launch_lw_gpoint_fp64(prep_of(w), in.emis, in.tauaer, h->lw_tab64, h->lw_exp64, h->lw_tfn64, w.bu, w.bd, w.bdu,
                             ncol, nlay, idrv, nb, h->analytic, s);
@@ -264,7 +269,7 @@ int lw_enqueue(rrtmg_gpu_state* h, cudaStream_t s, void* base, int ncol, int nla
     launch_lw_finalize(w.bu, w.bd, w.bdu, in.plev, ncol, nlay, idrv, uflx, dflx, hr, uflxc, dflxc, hrc, duflx_dt,
                        duflxc_dt, s, w.buc, w.bdc, w.bduc);
   mark(h, 0, 3, s);
-  h->launches += cloudy ? 5 : 4;
+  h->launches += 4 + (cloudy ? 1 : 0) + (maxrand ? 1 : 0);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(h, e, "LW kernel launch");
   return RRTMG_OK;
@@ -273,24 +278,24 @@ int lw_enqueue(rrtmg_gpu_state* h, cudaStream_t s, void* base, int ncol, int nla
 int lw_run(rrtmg_gpu_state* h, cudaStream_t s, int ncol, int nlay, int idrv, const LwIn& in, double* uflx,
            double* dflx, double* hr, double* uflxc, double* dflxc, double* hrc, double* duflx_dt, double* duflxc_dt) {
   size_t need;
-  carve_lw(nullptr, ncol, nlay, &need, in.cldfr != nullptr);
+  carve_lw(nullptr, ncol, nlay, &need, in.cldfr != nullptr, in.cldfr != nullptr && in.icld >= 2);
   int rc = ensure(h, h->lw_ws, need, s);
   if (rc) return rc;
   return lw_enqueue(h, s, h->lw_ws.p, ncol, nlay, idrv, in, uflx, dflx, hr, uflxc, dflxc, hrc, duflx_dt, duflxc_dt);
 }
 
-// Cloud arguments of the LW calls: icld = 0 (clear sky), or icld = 1 (random
-// overlap, rrtmg_lw_rtrn.f90) with the cloud optical depths given
-// (inflglw = 0, rrtmg_lw_cldprop.f90:165-171); icld = 2 / 3 (maximum-random,
-// maximum overlap) and the cloud-physics options inflglw = 1 / 2 are not
-// computed.
+// Cloud arguments of the LW calls: icld = 0 (clear sky), or clouds with the
+// cloud optical depths given (inflglw = 0, rrtmg_lw_cldprop.f90:165-171):
+// icld = 1 random overlap (rrtmg_lw_rtrn.f90), icld = 2 / 3 maximum/random
+// overlap (rrtmg_lw_rtrnmr.f90; the non-McICA driver routes both there,
+// rrtmg_lw_rad.nomcica.f90:527-541).  The cloud-physics options
+// inflglw = 1 / 2 are not computed.
 int lw_cloud_args(rrtmg_gpu_state* h, int icld, int inflglw, const double* cldfr, const double* taucld) {
   if (icld == 0) return RRTMG_OK;
-  if (icld != 1)
-    return fail(h, RRTMG_ERR_UNSUPPORTED, "LW clouds: only random overlap (icld = 1) is computed");
+  if (icld < 0 || icld > 3) return fail(h, RRTMG_ERR_UNSUPPORTED, "icld must be in [0, 3]");
   if (inflglw != 0)
     return fail(h, RRTMG_ERR_UNSUPPORTED, "LW clouds: only given cloud optical depths (inflglw = 0) are computed");
-  if (!cldfr || !taucld) return fail(h, RRTMG_ERR_ARG, "icld = 1 needs cldfr and taucld");
+  if (!cldfr || !taucld) return fail(h, RRTMG_ERR_ARG, "LW clouds need cldfr and taucld");
   return RRTMG_OK;
 }
 
@@ -613,7 +618,7 @@ const char* rrtmg_gpu_error_string(int status) {
     case RRTMG_OK: return "success";
     case RRTMG_ERR_ARG: return "invalid argument";
     case RRTMG_ERR_UNSUPPORTED:
-      return "unsupported configuration (LW icld 0/1, SW clear or overcast layers, given cloud optics, iaer 0/10, "
+      return "unsupported configuration (icld 0-3 with given cloud optics, SW clear or overcast layers, iaer 0/10, "
              "idrv 0/1)";
     case RRTMG_ERR_CUDA: return "CUDA error";
     case RRTMG_ERR_TABLES: return "coefficient table blob missing or invalid";
@@ -790,11 +795,12 @@ int rrtmg_lw_dev(rrtmg_gpu_handle h, void* stream, int ncol, int nlay, int icld,
   cudaSetDevice(h->device);
   LwIn in{play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr, cfc11vmr, cfc12vmr,
           cfc22vmr, ccl4vmr, emis, tauaer};
-  if (icld == 1) {
+  if (icld != 0) {
     in.cldfr = cldfr;
     in.taucld = taucld;
     in.cicewp = cicewp;
     in.cliqwp = cliqwp;
+    in.icld = icld;
   }
   return lw_run(h, (cudaStream_t)stream, ncol, nlay, idrv, in, uflx, dflx, hr, uflxc, dflxc, hrc, duflx_dt,
                 duflxc_dt);
@@ -954,7 +960,7 @@ int rrtmg_lw_c(rrtmg_gpu_handle h, int ncol, int nlay, int icld, int idrv, const
     return fail(h, RRTMG_ERR_ARG, "a required array pointer is null");
   if (idrv == 1 && !duflx_dt) return fail(h, RRTMG_ERR_ARG, "idrv = 1 needs duflx_dt");
   cudaSetDevice(h->device);
-  const bool cloudy = icld == 1;
+  const bool cloudy = icld != 0;
   const size_t L = nlay, Lv = nlay + 1;
   const HostIn in[21] = {{play, L}, {plev, Lv}, {tlay, L}, {tlev, Lv}, {tsfc, 1}, {h2ovmr, L}, {o3vmr, L},
                          {co2vmr, L}, {ch4vmr, L}, {n2ovmr, L}, {o2vmr, L}, {cfc11vmr, L}, {cfc12vmr, L},
@@ -965,12 +971,12 @@ int rrtmg_lw_c(rrtmg_gpu_handle h, int ncol, int nlay, int icld, int idrv, const
                           {idrv == 1 ? duflx_dt : nullptr, Lv}, {idrv == 1 ? duflxc_dt : nullptr, Lv}};
   auto need = [&](int nc) {
     size_t b;
-    carve_lw(nullptr, nc, nlay, &b, cloudy);
+    carve_lw(nullptr, nc, nlay, &b, cloudy, icld >= 2);
     return b;
   };
   auto enq = [&](cudaStream_t s, void* ws, int nc, const double* const* d, double* const* o) {
-    LwIn li{d[0], d[1], d[2], d[3], d[4], d[5], d[6], d[7], d[8], d[9], d[10], d[11], d[12], d[13], d[14], d[15],
-            d[16], d[17], d[18], d[19], d[20]};
+    LwIn li{d[0],  d[1],  d[2],  d[3],  d[4],  d[5],  d[6],  d[7],  d[8],  d[9], d[10],
+            d[11], d[12], d[13], d[14], d[15], d[16], d[17], d[18], d[19], d[20], icld};
     return lw_enqueue(h, s, ws, nc, nlay, idrv, li, o[0], o[1], o[2], o[3], o[4], o[5], o[6], o[7]);
   };
   return host_call(h, ncol, in, 21, out, 8, need, enq, "copy LW arrays");

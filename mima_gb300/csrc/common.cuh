@@ -146,9 +146,11 @@ using SwPrep = SwPrepT<double>;
 struct LwIn {
   const double *play, *plev, *tlay, *tlev, *tsfc, *h2o, *o3, *co2, *ch4, *n2o, *o2, *cfc11, *cfc12, *cfc22, *ccl4,
       *emis, *tauaer;
-  // clouds (icld = 1, inflglw = 0), null in clear sky: cldfr (ncol, nlay),
-  // taucld (16, ncol, nlay), cicewp / cliqwp (ncol, nlay) or null
+  // clouds (icld = 1, 2, 3, inflglw = 0), null in clear sky: cldfr (ncol,
+  // nlay), taucld (16, ncol, nlay), cicewp / cliqwp (ncol, nlay) or null
   const double *cldfr, *taucld, *cicewp, *cliqwp;
+  // cloud overlap with clouds: 1 random (rtrn), 2 or 3 maximum/random (rtrnmr)
+  int icld;
 };
 template <class F>
 struct LwWorkT {
@@ -162,6 +164,9 @@ struct LwWorkT {
   // partials
   F* cld;
   double *buc, *bdc, *bduc;
+  // maximum/random overlap only: rtrnmr's overlap factors per layer,
+  // [12][lay][col] (lw_overlap_kernel)
+  F* ovl;
 };
 using LwWork = LwWorkT<double>;
 struct SwIn {

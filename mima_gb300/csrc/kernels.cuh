@@ -549,6 +549,10 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
 // computed on its own above the surface once the column holds a cloud.
 // Total and clear-sky level radiances are summed over the band's g-points
 // into their own band partials.
+// With ovl (icld = 2, 3): maximum/random overlap, rrtmg_lw_rtrnmr.f90:
+// 500-705.  Through a block of adjacent cloudy layers the radiance is carried
+// as a cloudy and a clear part; at each cloudy layer's far boundary the
+// overlap factors of lw_overlap_kernel move radiance between the two.
 // ---------------------------------------------------------------------------
 template <int B, class R, int MAXL>
 __device__ __forceinline__ void lw_band_cld(const LwPrepT<R>& p, const R* __restrict__ cld,
@@ -559,7 +563,7 @@ __device__ __forceinline__ void lw_band_cld(const LwPrepT<R>& p, const R* __rest
                                             double* __restrict__ bd, double* __restrict__ bdu,
                                             double* __restrict__ buc, double* __restrict__ bdc,
                                             double* __restrict__ bduc, int ncol, int nlay, int idrv, bool analytic,
-                                            int blk, float* sbuf) {
+                                            int blk, float* sbuf, const R* __restrict__ ovl) {
   const bool IDRV = idrv == 1;
   constexpr bool SPLIT = sizeof(R) == 4;
   constexpr int NG = lw_ng(B);
@@ -627,6 +631,11 @@ __device__ __forceinline__ void lw_band_cld(const LwPrepT<R>& p, const R* __rest
   }
   R radld = (R)0., radclrd = (R)0., fracs1 = (R)0.;
   bool iclddn = false;
+  // maximum/random overlap: the cloudy and clear parts and the radiance
+  // moved between them; whether the layer above was cloudy (istcldd = 0)
+  R cldrad = (R)0., clrrad = (R)0., rad = (R)0.;
+  bool above_cloudy = false;
+  const size_t ostride = (size_t)nlay * N;  // one overlap factor's stride
   uint32_t idx_next = __ldg(p.idx + (size_t)(nlay - 1) * N + c);
   for (int lev = nlay; lev >= 1; --lev) {
     const size_t o = (size_t)(lev - 1) * N + c;
@@ -648,8 +657,7 @@ __device__ __forceinline__ void lw_band_cld(const LwPrepT<R>& p, const R* __rest
     if (cf > (R)0.) {  // cloudy layer (rtrn :350-416)
       iclddn = true;
       const R odcld = secdiff * (__ldg(cld + fstride + o) * (R)__ldg(taucld + (B - 1) + 16 * o));
-      const R transcld = exp(-odcld);
-      ef = ((R)1. - transcld) * cf;
+      if (!ovl) ef = ((R)1. - exp(-odcld)) * cf;
       R odtot = odepth + odcld;
       R gassrc, bbdtot;
       if (odtot < (R)0.06) {
@@ -688,7 +696,28 @@ __device__ __forceinline__ void lw_band_cld(const LwPrepT<R>& p, const R* __rest
         bbu = plfrac * (blay + tfacgas * dplankup);
         bbut = plfrac * (blay + tfactot * dplankup);
       }
-      radld = radld - radld * (atr + ef * ((R)1. - atr)) + gassrc + cf * (bbdtot * at - gassrc);
+      if (ovl) {  // rtrnmr :561-588
+        if (!above_cloudy) {
+          cldrad = cf * radld;
+          clrrad = radld - cldrad;
+          rad = (R)0.;
+        }
+        const R ttot = (R)1. - at;
+        const R cldsrc = bbdtot * at;
+        cldrad = cldrad * ttot + cf * cldsrc;
+        clrrad = clrrad * ((R)1. - atr) + ((R)1. - cf) * gassrc;
+        radld = cldrad + clrrad;
+        const R* od = ovl + 6 * ostride + o;  // facclr1d, faccld1d, faccmb1d, faccmb2d, facclr2d, faccld2d
+        const R radmod = rad * (__ldg(od) * ((R)1. - atr) + __ldg(od + ostride) * ttot) -
+                         __ldg(od + 2 * ostride) * gassrc + __ldg(od + 3 * ostride) * cldsrc;
+        const R oldcld = cldrad - radmod;
+        const R oldclr = clrrad + radmod;
+        rad = -radmod + __ldg(od + 4 * ostride) * oldclr - __ldg(od + 5 * ostride) * oldcld;
+        cldrad = cldrad + rad;
+        clrrad = clrrad - rad;
+      } else {
+        radld = radld - radld * (atr + ef * ((R)1. - atr)) + gassrc + cf * (bbdtot * at - gassrc);
+      }
     } else {  // clear layer (rtrn :418-436)
       if (odepth <= (R)0.06) {
         atr = odepth - (R)0.5 * odepth * odepth;
@@ -704,6 +733,7 @@ __device__ __forceinline__ void lw_band_cld(const LwPrepT<R>& p, const R* __rest
       }
       radld = radld + (bbd - radld) * atr;
     }
+    above_cloudy = cf > (R)0.;
     atrans[lev - 1] = atr;
     bbugas[lev - 1] = bbu;
     atot[lev - 1] = at;
@@ -757,18 +787,43 @@ __device__ __forceinline__ void lw_band_cld(const LwPrepT<R>& p, const R* __rest
     }
   };
   emit(0);
-  for (int lev = 1; lev <= nlay; ++lev) {  // rtrn :478-520
+  bool below_cloudy = false;  // maximum/random overlap: istcld = 0
+  rad = (R)0.;
+  for (int lev = 1; lev <= nlay; ++lev) {  // rtrn :478-520, rtrnmr :649-705
     const R atr = atrans[lev - 1];
-    const R cf = __ldg(cld + (size_t)(lev - 1) * N + c);
+    const size_t o = (size_t)(lev - 1) * N + c;
+    const R cf = __ldg(cld + o);
     if (cf > (R)0.) {
       const R gassrc = bbugas[lev - 1] * atr;
       const R at = atot[lev - 1];
-      radlu = radlu - radlu * (atr + efcl[lev - 1] * ((R)1. - atr)) + gassrc + cf * (bbutot[lev - 1] * at - gassrc);
+      if (ovl) {
+        if (!below_cloudy) {
+          cldrad = cf * radlu;
+          clrrad = radlu - cldrad;
+          rad = (R)0.;
+        }
+        const R ttot = (R)1. - at;
+        const R cldsrc = bbutot[lev - 1] * at;
+        cldrad = cldrad * ttot + cf * cldsrc;
+        clrrad = clrrad * ((R)1.0 - atr) + ((R)1. - cf) * gassrc;
+        radlu = cldrad + clrrad;
+        const R* ou = ovl + o;  // facclr1, faccld1, faccmb1, faccmb2, facclr2, faccld2 (index lev + 1)
+        const R radmod = rad * (__ldg(ou) * ((R)1.0 - atr) + __ldg(ou + ostride) * ttot) -
+                         __ldg(ou + 2 * ostride) * gassrc + __ldg(ou + 3 * ostride) * cldsrc;
+        const R oldcld = cldrad - radmod;
+        const R oldclr = clrrad + radmod;
+        rad = -radmod + __ldg(ou + 4 * ostride) * oldclr - __ldg(ou + 5 * ostride) * oldcld;
+        cldrad = cldrad + rad;
+        clrrad = clrrad - rad;
+      } else {
+        radlu = radlu - radlu * (atr + efcl[lev - 1] * ((R)1. - atr)) + gassrc + cf * (bbutot[lev - 1] * at - gassrc);
+      }
       if (IDRV) dlu = dlu * cf * ((R)1.0 - at) + dlu * ((R)1.0 - cf) * ((R)1.0 - atr);
     } else {
       radlu = radlu + (bbugas[lev - 1] - radlu) * atr;
       if (IDRV) dlu = dlu * ((R)1.0 - atr);
     }
+    below_cloudy = cf > (R)0.;
     if (iclddn) {
       radclru = radclru + (bbugas[lev - 1] - radclru) * atr;
       if (IDRV) dluc = dluc * ((R)1.0 - atr);
@@ -833,16 +888,17 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_LW_MINB :
 #undef RRTMG_LW_CASE
 }
 
-// Cloudy LW g-point kernel (icld = 1): as lw_gpoint_kernel, with
-// lw_band_cld.  FL < 0: analytic and idrv as passed (FP64 path); FL >= 0:
-// compile-time flags (bit 0 analytic, bit 1 idrv; split path).
+// Cloudy LW g-point kernel (icld = 1, 2, 3): as lw_gpoint_kernel, with
+// lw_band_cld (ovl null: random overlap, else maximum/random).  FL < 0:
+// analytic and idrv as passed (FP64 path); FL >= 0: compile-time flags (bit
+// 0 analytic, bit 1 idrv; split path).
 template <class R, int MAXL, int FL>
 __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_LW_MINB : 1)
     lw_gpoint_cld_kernel(LwPrepT<R> p, const R* __restrict__ cld, const double* __restrict__ taucld,
                          const double* __restrict__ emis, const double* __restrict__ tauaer,
                          const R* __restrict__ tab, const R* __restrict__ exptbl, const R* __restrict__ tfntbl,
                          const R* __restrict__ tautbl, double* bu, double* bd, double* bdu, double* buc, double* bdc,
-                         double* bduc, int ncol, int nlay, int idrv, int analytic) {
+                         double* bduc, int ncol, int nlay, int idrv, int analytic, const R* __restrict__ ovl) {
   __shared__ float sbuf[sizeof(R) == 4 ? kGSumFloats : 1];
   int blk = blockIdx.x, band = 0;
   for (; band < kLwBands; ++band) {
@@ -855,7 +911,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_LW_MINB :
 #define RRTMG_LW_CASE(b)                                                                                            \
   case b - 1:                                                                                                      \
     lw_band_cld<b, R, MAXL>(p, cld, taucld, emis, tauaer, tab, exptbl, tfntbl, tautbl, bu, bd, bdu, buc, bdc, bduc, \
-                            ncol, nlay, idv, an, blk, sbuf);                                                       \
+                            ncol, nlay, idv, an, blk, sbuf, ovl);                                                  \
     break;
   switch (band) {
     RRTMG_LW_CASE(1) RRTMG_LW_CASE(2) RRTMG_LW_CASE(3) RRTMG_LW_CASE(4) RRTMG_LW_CASE(5) RRTMG_LW_CASE(6)
@@ -889,6 +945,137 @@ __global__ void __launch_bounds__(128) lw_cloud_kernel(LwIn in, F* __restrict__ 
   const bool kept = cf >= cldmin && (cwp >= cldmin || tauctot >= cldmin);
   cld[o] = cf >= 1.e-6 ? (F)cf : (F)0;
   cld[(size_t)nlay * ncol + o] = kept ? (F)1 : (F)0;
+}
+
+// ---------------------------------------------------------------------------
+// Overlap factors of maximum/random cloud overlap (icld = 2, 3), one thread
+// per column: rrtmg_lw_rtrnmr.f90:326-475, an upward and a downward scan over
+// the layers that carry the rat1 / rat2 state from one cloudy layer to the
+// next (and from the upward scan into the downward one).  A cloudy layer has
+// cldfrac >= 1e-6; the factors use the raw cloud fractions of the layer and
+// its neighbours, cldfrac(0) and cldfrac(nlay + 1) taken as 0 (the reference
+// multiplies its out-of-range cldfrac(0) by a zero factor).  A factor the
+// reference zeroes at a layer below / above a clear one is the 0 that the
+// scan carries out of the clear layer.  ovl[j][lay][col], j = 0..5: facclr1,
+// faccld1, faccmb1, faccmb2, facclr2, faccld2 at index lay + 1 (read by the
+// upward pass through layer lay); j = 6..11: the same *d factors at index
+// lay - 1 (downward pass); 0 for clear layers.
+// ---------------------------------------------------------------------------
+template <class F>
+__global__ void __launch_bounds__(128) lw_overlap_kernel(const double* __restrict__ cldfr, F* __restrict__ ovl,
+                                                         int ncol, int nlay) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncol) return;
+  const size_t N = (size_t)ncol, S = (size_t)nlay * N;
+  auto cfa = [&](int lev) { return lev < 1 || lev > nlay ? 0.0 : __ldg(cldfr + (size_t)(lev - 1) * N + col); };
+  auto cloudy = [&](int lev) { return lev >= 1 && lev <= nlay && cfa(lev) >= 1.e-6; };
+  double rat1 = 0.0, rat2 = 0.0;
+  double c2clr = 0.0, c2cld = 0.0;  // facclr2 / faccld2 at the current index, carried
+  for (int lev = 1; lev <= nlay; ++lev) {
+    F* o = ovl + (size_t)(lev - 1) * N + col;
+    if (!cloudy(lev)) {
+      for (int j = 0; j < 6; ++j) o[j * S] = (F)0;
+      c2clr = c2cld = 0.0;
+      continue;
+    }
+    const bool ist = !cloudy(lev - 1);
+    const double cm = cfa(lev - 1), c0 = cfa(lev), cp = cfa(lev + 1);
+    double clr1 = 0., clr2 = 0., cld1 = 0., cld2 = 0.;
+    if (lev == nlay) {
+    } else if (cp >= c0) {
+      if (ist) {
+        if (c0 < 1.) clr2 = (cp - c0) / (1. - c0);
+      } else {
+        const double fmx = c0 > cm ? c0 : cm;
+        if (cp > fmx) {
+          clr1 = rat2;
+          clr2 = (cp - fmx) / (1. - fmx);
+        } else if (cp < fmx) {
+          clr1 = (cp - c0) / (cm - c0);
+        } else {
+          clr1 = rat2;
+        }
+      }
+      rat1 = (clr1 > 0. || clr2 > 0.) ? 1. : 0.;
+      rat2 = 0.;
+    } else {
+      if (ist) {
+        cld2 = (c0 - cp) / c0;
+      } else {
+        const double fmn = c0 < cm ? c0 : cm;
+        if (cp <= fmn) {
+          cld1 = rat1;
+          cld2 = (fmn - cp) / fmn;
+        } else {
+          cld1 = (c0 - cp) / (c0 - fmn);
+        }
+      }
+      rat1 = 0.;
+      rat2 = (cld1 > 0. || cld2 > 0.) ? 1. : 0.;
+    }
+    const double cmb1 = clr1 * c2cld * cm, cmb2 = cld1 * c2clr * (1. - cm);
+    o[0] = (F)clr1;
+    o[S] = (F)cld1;
+    o[2 * S] = (F)cmb1;
+    o[3 * S] = (F)cmb2;
+    o[4 * S] = (F)clr2;
+    o[5 * S] = (F)cld2;
+    c2clr = clr2;
+    c2cld = cld2;
+  }
+  c2clr = c2cld = 0.0;
+  for (int lev = nlay; lev >= 1; --lev) {
+    F* o = ovl + 6 * S + (size_t)(lev - 1) * N + col;
+    if (!cloudy(lev)) {
+      for (int j = 0; j < 6; ++j) o[j * S] = (F)0;
+      c2clr = c2cld = 0.0;
+      continue;
+    }
+    const bool ist = !cloudy(lev + 1);
+    const double cm = cfa(lev - 1), c0 = cfa(lev), cp = cfa(lev + 1);
+    double clr1 = 0., clr2 = 0., cld1 = 0., cld2 = 0.;
+    if (lev == 1) {
+    } else if (cm >= c0) {
+      if (ist) {
+        if (c0 < 1.) clr2 = (cm - c0) / (1. - c0);
+      } else {
+        const double fmx = c0 > cp ? c0 : cp;
+        if (cm > fmx) {
+          clr1 = rat2;
+          clr2 = (cm - fmx) / (1. - fmx);
+        } else if (cm < fmx) {
+          clr1 = (cm - c0) / (cp - c0);
+        } else {
+          clr1 = rat2;
+        }
+      }
+      rat1 = (clr1 > 0. || clr2 > 0.) ? 1. : 0.;
+      rat2 = 0.;
+    } else {
+      if (ist) {
+        cld2 = (c0 - cm) / c0;
+      } else {
+        const double fmn = c0 < cp ? c0 : cp;
+        if (cm <= fmn) {
+          cld1 = rat1;
+          cld2 = (fmn - cm) / fmn;
+        } else {
+          cld1 = (c0 - cm) / (c0 - fmn);
+        }
+      }
+      rat1 = 0.;
+      rat2 = (cld1 > 0. || cld2 > 0.) ? 1. : 0.;
+    }
+    const double cmb1 = clr1 * c2cld * cp, cmb2 = cld1 * c2clr * (1. - cp);
+    o[0] = (F)clr1;
+    o[S] = (F)cld1;
+    o[2 * S] = (F)cmb1;
+    o[3 * S] = (F)cmb2;
+    o[4 * S] = (F)clr2;
+    o[5 * S] = (F)cld2;
+    c2clr = clr2;
+    c2cld = cld2;
+  }
 }
 
 // ---------------------------------------------------------------------------

@@ -53,14 +53,16 @@ void launch_lw_gpoint_fp64(const LwPrep& p, const double* emis, const double* ta
 void launch_lw_gpoint_cld_fp64(const LwPrep& p, const double* cld, const double* taucld, const double* emis,
                                const double* tauaer, const double* tab, const double* exptbl, const double* tfntbl,
                                const double* tautbl, double* bu, double* bd, double* bdu, double* buc, double* bdc,
-                               double* bduc, int ncol, int nlay, int idrv, int nb, int analytic, cudaStream_t s) {
+                               double* bduc, int ncol, int nlay, int idrv, int nb, int analytic, cudaStream_t s,
+                               const double* ovl) {
   if (maxl_for(nlay) == 64)
     lw_gpoint_cld_kernel<double, 64, -1><<<nb, kBlock, 0, s>>>(p, cld, taucld, emis, tauaer, tab, exptbl, tfntbl, tautbl,
-                                                              bu, bd, bdu, buc, bdc, bduc, ncol, nlay, idrv, analytic);
+                                                              bu, bd, bdu, buc, bdc, bduc, ncol, nlay, idrv, analytic,
+                                                              ovl);
   else
     lw_gpoint_cld_kernel<double, 208, -1><<<nb, kBlock, 0, s>>>(p, cld, taucld, emis, tauaer, tab, exptbl, tfntbl,
                                                                tautbl, bu, bd, bdu, buc, bdc, bduc, ncol, nlay, idrv,
-                                                               analytic);
+                                                               analytic, ovl);
 }
 
 void launch_lw_cloud(const LwIn& in, double* cld, int ncol, int nlay, cudaStream_t s) {
@@ -68,6 +70,12 @@ void launch_lw_cloud(const LwIn& in, double* cld, int ncol, int nlay, cudaStream
 }
 void launch_lw_cloud_split(const LwIn& in, float* cld, int ncol, int nlay, cudaStream_t s) {
   lw_cloud_kernel<float><<<dim3((ncol + 127) / 128, nlay), 128, 0, s>>>(in, cld, ncol, nlay);
+}
+void launch_lw_overlap(const double* cldfr, double* ovl, int ncol, int nlay, cudaStream_t s) {
+  lw_overlap_kernel<double><<<(ncol + 127) / 128, 128, 0, s>>>(cldfr, ovl, ncol, nlay);
+}
+void launch_lw_overlap_split(const double* cldfr, float* ovl, int ncol, int nlay, cudaStream_t s) {
+  lw_overlap_kernel<float><<<(ncol + 127) / 128, 128, 0, s>>>(cldfr, ovl, ncol, nlay);
 }
 
 void launch_lw_finalize(const double* bu, const double* bd, const double* bdu, const double* plev, int ncol, int nlay,

@@ -198,31 +198,34 @@ void launch_lw_gpoint_split(const LwPrepT<float>& p, const double* emis, const d
     lw_split_flags<208>(fl, nb, s, p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv, analytic);
 }
 
-// Cloudy LW (icld = 1): instantiated per (analytic, idrv) flag pair.
+// Cloudy LW (icld = 1, 2, 3): instantiated per (analytic, idrv) flag pair;
+// the overlap (ovl null: random) is chosen at run time.
 template <int MAXL>
 static void lw_split_cld_flags(int fl, int nb, cudaStream_t s, const LwPrepT<float>& p, const float* cld,
                                const double* taucld, const double* emis, const double* tauaer, const float* tab,
                                const float* exptbl, const float* tfntbl, const float* tautbl, double* bu, double* bd,
-                               double* bdu, double* buc, double* bdc, double* bduc, int ncol, int nlay) {
+                               double* bdu, double* buc, double* bdc, double* bduc, int ncol, int nlay,
+                               const float* ovl) {
   auto k = fl == 0 ? lw_gpoint_cld_kernel<float, MAXL, 0>
          : fl == 1 ? lw_gpoint_cld_kernel<float, MAXL, 1>
          : fl == 2 ? lw_gpoint_cld_kernel<float, MAXL, 2>
                    : lw_gpoint_cld_kernel<float, MAXL, 3>;
   k<<<nb, kBlock, 0, s>>>(p, cld, taucld, emis, tauaer, tab, exptbl, tfntbl, tautbl, bu, bd, bdu, buc, bdc, bduc, ncol,
-                          nlay, 0, 0);
+                          nlay, 0, 0, ovl);
 }
 
 void launch_lw_gpoint_cld_split(const LwPrepT<float>& p, const float* cld, const double* taucld, const double* emis,
                                 const double* tauaer, const float* tab, const float* exptbl, const float* tfntbl,
                                 const float* tautbl, double* bu, double* bd, double* bdu, double* buc, double* bdc,
-                                double* bduc, int ncol, int nlay, int idrv, int nb, int analytic, cudaStream_t s) {
+                                double* bduc, int ncol, int nlay, int idrv, int nb, int analytic, cudaStream_t s,
+                                const float* ovl) {
   const int fl = (analytic ? 1 : 0) | (idrv == 1 ? 2 : 0);
   if (maxl_for(nlay) == 64)
     lw_split_cld_flags<64>(fl, nb, s, p, cld, taucld, emis, tauaer, tab, exptbl, tfntbl, tautbl, bu, bd, bdu, buc,
-                           bdc, bduc, ncol, nlay);
+                           bdc, bduc, ncol, nlay, ovl);
   else
     lw_split_cld_flags<208>(fl, nb, s, p, cld, taucld, emis, tauaer, tab, exptbl, tfntbl, tautbl, bu, bd, bdu, buc,
-                            bdc, bduc, ncol, nlay);
+                            bdc, bduc, ncol, nlay, ovl);
 }
 
 template <int MAXL, bool TOT>

@@ -29,14 +29,20 @@ void launch_lw_finalize(const double* bu, const double* bd, const double* bdu, c
 // Clouds (icld = 1): per-layer cloud fields, FP64 and FP32 storage.
 void launch_lw_cloud(const LwIn& in, double* cld, int ncol, int nlay, cudaStream_t s);
 void launch_lw_cloud_split(const LwIn& in, float* cld, int ncol, int nlay, cudaStream_t s);
+// Maximum/random overlap (icld = 2, 3): rtrnmr's overlap factors per layer.
+void launch_lw_overlap(const double* cldfr, double* ovl, int ncol, int nlay, cudaStream_t s);
+void launch_lw_overlap_split(const double* cldfr, float* ovl, int ncol, int nlay, cudaStream_t s);
+// ovl: the overlap factors of maximum/random overlap, or null (random overlap).
 void launch_lw_gpoint_cld_fp64(const LwPrep& p, const double* cld, const double* taucld, const double* emis,
                                const double* tauaer, const double* tab, const double* exptbl, const double* tfntbl,
                                const double* tautbl, double* bu, double* bd, double* bdu, double* buc, double* bdc,
-                               double* bduc, int ncol, int nlay, int idrv, int nb, int analytic, cudaStream_t s);
+                               double* bduc, int ncol, int nlay, int idrv, int nb, int analytic, cudaStream_t s,
+                               const double* ovl = nullptr);
 void launch_lw_gpoint_cld_split(const LwPrepT<float>& p, const float* cld, const double* taucld, const double* emis,
                                 const double* tauaer, const float* tab, const float* exptbl, const float* tfntbl,
                                 const float* tautbl, double* bu, double* bd, double* bdu, double* buc, double* bdc,
-                                double* bduc, int ncol, int nlay, int idrv, int nb, int analytic, cudaStream_t s);
+                                double* bduc, int ncol, int nlay, int idrv, int nb, int analytic, cudaStream_t s,
+                                const float* ovl = nullptr);
 void launch_sw_prep(const SwIn& in, const SwWork& w, int ncol, int nlay, unsigned* flags, cudaStream_t s);
 // Prep for the FP32-split solvers: the same steps in FP32 arithmetic (FP32 Planck
 // tables), fields stored as float.

@@ -240,8 +240,9 @@ class RRTMG:
         """rrtmg_lw on host arrays; returns uflx, dflx, hr, uflxc, dflxc, hrc (+ duflx_dt, duflxc_dt).
         ``out`` optionally supplies the output arrays (float64, C-contiguous;
         page-locked arrays let the library overlap copies with kernels).
-        Clouds (icld = 1, inflglw = 0): cldfr, cicewp, cliqwp (nlay, ncol),
-        taucld (nlay, ncol, 16) = Fortran (16, ncol, nlay)."""
+        Clouds (icld = 1 random overlap, 2 / 3 maximum/random overlap;
+        inflglw = 0): cldfr, cicewp, cliqwp (nlay, ncol), taucld
+        (nlay, ncol, 16) = Fortran (16, ncol, nlay)."""
         L, N = nlay, ncol
         ins = [_host(a) for a in (play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr,
                                   cfc11vmr, cfc12vmr, cfc22vmr, ccl4vmr, emis)]
@@ -288,11 +289,12 @@ class RRTMG:
         return out
 
     # Convenience: whole Atmosphere objects (mima_gb300.atmosphere)
-    def lw(self, atm, idrv=0, tauaer=None, check=True, cloud=None):
-        """``cloud``: dict(cldfr, taucld[, cicewp, cliqwp]) for icld = 1 (random
-        overlap, given cloud optical depths), as rrtmg_lw's arguments."""
+    def lw(self, atm, idrv=0, tauaer=None, check=True, cloud=None, icld=1):
+        """``cloud``: dict(cldfr, taucld[, cicewp, cliqwp]) (given cloud optical
+        depths, as rrtmg_lw's arguments) with overlap ``icld`` (1 random, 2 / 3
+        maximum/random)."""
         cl = cloud or {}
-        return self.rrtmg_lw(atm.ncol, atm.nlay, 1 if cloud else 0, idrv, atm.play, atm.plev, atm.tlay, atm.tlev,
+        return self.rrtmg_lw(atm.ncol, atm.nlay, icld if cloud else 0, idrv, atm.play, atm.plev, atm.tlay, atm.tlev,
                              atm.tsfc, atm.h2o, atm.o3, atm.co2, atm.ch4, atm.n2o, atm.o2, atm.cfc11, atm.cfc12,
                              atm.cfc22, atm.ccl4, atm.emis, tauaer, check=check, cldfr=cl.get("cldfr"),
                              taucld=cl.get("taucld"), cicewp=cl.get("cicewp"), cliqwp=cl.get("cliqwp"))

@@ -68,11 +68,12 @@ def _f(a):
     return np.ascontiguousarray(a, dtype=np.float64)
 
 
-def rrtmg_lw(atm, idrv: int = 0, tauaer=None, nthreads: int = 0, cloud=None):
+def rrtmg_lw(atm, idrv: int = 0, tauaer=None, nthreads: int = 0, cloud=None, icld: int = 1):
     """rrtmg_lw on ``atm``; returns dict of (nlev, ncol) arrays.  Clear sky, or
     with ``cloud`` = dict(cldfr=(nlay, ncol), taucld=(nlay, ncol, 16) [Fortran
-    (16, ncol, nlay)], optional cicewp / cliqwp (nlay, ncol)): icld = 1
-    (random overlap), cloud optical depths given (inflglw = 0)."""
+    (16, ncol, nlay)], optional cicewp / cliqwp (nlay, ncol)): cloud optical
+    depths given (inflglw = 0), random overlap (``icld`` = 1, rtrn) or
+    maximum/random overlap (``icld`` = 2 or 3, rtrnmr)."""
     n, L = atm.ncol, atm.nlay
     out = {k: np.zeros((L + 1, n)) for k in ("uflx", "dflx", "uflxc", "dflxc", "duflx_dt", "duflxc_dt")}
     out.update({k: np.zeros((L, n)) for k in ("hr", "hrc")})
@@ -82,7 +83,7 @@ def rrtmg_lw(atm, idrv: int = 0, tauaer=None, nthreads: int = 0, cloud=None):
             None if tauaer is None else _f(tauaer)]
     cl = cloud or {}
     carg = [None if cl.get(k) is None else _f(cl[k]) for k in ("cldfr", "taucld", "cicewp", "cliqwp")]
-    rc = _lib.orc_rrtmg_lw(C.c_int(n), C.c_int(L), C.c_int(1 if cloud else 0), C.c_int(idrv),
+    rc = _lib.orc_rrtmg_lw(C.c_int(n), C.c_int(L), C.c_int(icld if cloud else 0), C.c_int(idrv),
                            *[_p(a) for a in args],
                            _p(out["uflx"]), _p(out["dflx"]), _p(out["hr"]), _p(out["uflxc"]),
                            _p(out["dflxc"]), _p(out["hrc"]), _p(out["duflx_dt"]), _p(out["duflxc_dt"]),

@@ -55,7 +55,7 @@ int orc_rrtmg_lw(int ncol, int nlay, int icld, int idrv, const double* play, con
                  int nthreads, const double* cldfr, const double* taucld, const double* cicewp,
                  const double* cliqwp) {
   if (!g_ready) return 2;
-  if (icld != 0 && !(icld == 1 && cldfr && taucld)) return 3;
+  if (icld != 0 && !(icld >= 1 && icld <= 3 && cldfr && taucld)) return 3;
   LwInput in{ncol, nlay, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr,
              cfc11vmr, cfc12vmr, cfc22vmr, ccl4vmr, emis, tauaer};
   in.icld = icld;

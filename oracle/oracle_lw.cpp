@@ -1,7 +1,9 @@
 // CPU oracle, longwave -- TEST INFRASTRUCTURE ONLY (the checker, never the
 // product).  FP64 restatement of the reference's RRTMG_LW path (clear sky,
-// and clouds with random overlap and given cloud optical depths: icld = 1,
-// inflglw = 0 -- cldprop rrtmg_lw_cldprop.f90:155-174, rtrn rrtmg_lw_rtrn.f90):
+// and clouds with given cloud optical depths, inflglw = 0 -- cldprop
+// rrtmg_lw_cldprop.f90:155-174 -- with random overlap, icld = 1, rtrn
+// rrtmg_lw_rtrn.f90, or maximum/random overlap, icld = 2 / 3, rtrnmr's cloudy
+// branches rrtmg_lw_rtrnmr.f90:300-705):
 //   inatm    rrtmg_lw_rad.nomcica.f90:572-901
 //   setcoef  rrtmg_lw_setcoef.f90:31-415
 //   taumol   rrtmg_lw_taumol.f90:31-3149 (taugb1..16)
@@ -12,6 +14,7 @@
 // -ffp-contract=off so no multiply-add is fused.
 #include "oracle_lw.hpp"
 
+#include <algorithm>
 #include <cmath>
 
 namespace orc {
@@ -1440,6 +1443,436 @@ void lw_rtrn(LwColumn& c, int idrv, LwOut& out) {
   out.dtotuc_dt = dtotuc_dt;
 }
 
+// ---------------------------------------------------------------------------
+// rtrnmr with clouds: maximum/random overlap (icld = 2, 3 in the non-McICA
+// driver, rrtmg_lw_rad.nomcica.f90:527-541), rrtmg_lw_rtrnmr.f90:300-705.
+// Each cloudy layer carries a cloudy and a clear radiance; the overlap
+// factors move radiance between them at the layer's lower (upward pass) or
+// upper (downward pass) boundary, from the cloud fractions of the layer and
+// its two neighbours (:326-475).  cldfrac(0) (read as 0 x value at the lowest
+// layer, :400-401) is taken as 0; cldfrac(nlayers + 1) is the driver's zero.
+// ---------------------------------------------------------------------------
+struct MrOverlap {
+  // upward factors indexed lev + 1 (1..nl+1), downward ones lev - 1 (0..nl-1)
+  std::vector<double> faccld1, faccld2, facclr1, facclr2, faccmb1, faccmb2;
+  std::vector<double> faccld1d, faccld2d, facclr1d, facclr2d, faccmb1d, faccmb2d;
+  std::vector<int> istcld, istcldd;
+};
+
+static void lw_mr_overlap(const std::vector<double>& cf, const std::vector<int>& icldlyr, int nl, MrOverlap& o) {
+  for (auto* v : {&o.faccld1, &o.faccld2, &o.facclr1, &o.facclr2, &o.faccmb1, &o.faccmb2, &o.faccld1d, &o.faccld2d,
+                  &o.facclr1d, &o.facclr2d, &o.faccmb1d, &o.faccmb2d})
+    v->assign(nl + 2, 0.0);
+  o.istcld.assign(nl + 2, 0);
+  o.istcldd.assign(nl + 2, 0);
+  double rat1 = 0.0, rat2 = 0.0;
+  // upward (:326-403)
+  o.istcld[1] = 1;
+  o.istcldd[nl] = 1;
+  for (int lev = 1; lev <= nl; ++lev) {
+    if (icldlyr[lev] != 1) {
+      o.istcld[lev + 1] = 1;
+      continue;
+    }
+    o.istcld[lev + 1] = 0;
+    if (lev == nl) {
+      o.faccld1[lev + 1] = o.faccld2[lev + 1] = o.facclr1[lev + 1] = 0.;
+      o.facclr2[lev + 1] = o.faccmb1[lev + 1] = o.faccmb2[lev + 1] = 0.;
+    } else if (cf[lev + 1] >= cf[lev]) {
+      o.faccld1[lev + 1] = 0.;
+      o.faccld2[lev + 1] = 0.;
+      if (o.istcld[lev] == 1) {
+        o.facclr1[lev + 1] = 0.;
+        o.facclr2[lev + 1] = 0.;
+        if (cf[lev] < 1.) o.facclr2[lev + 1] = (cf[lev + 1] - cf[lev]) / (1. - cf[lev]);
+        o.facclr2[lev] = 0.;
+        o.faccld2[lev] = 0.;
+      } else {
+        const double fmax = std::max(cf[lev], cf[lev - 1]);
+        if (cf[lev + 1] > fmax) {
+          o.facclr1[lev + 1] = rat2;
+          o.facclr2[lev + 1] = (cf[lev + 1] - fmax) / (1. - fmax);
+        } else if (cf[lev + 1] < fmax) {
+          o.facclr1[lev + 1] = (cf[lev + 1] - cf[lev]) / (cf[lev - 1] - cf[lev]);
+          o.facclr2[lev + 1] = 0.;
+        } else {
+          o.facclr1[lev + 1] = rat2;
+          o.facclr2[lev + 1] = 0.;
+        }
+      }
+      if (o.facclr1[lev + 1] > 0. || o.facclr2[lev + 1] > 0.) {
+        rat1 = 1.;
+        rat2 = 0.;
+      } else {
+        rat1 = 0.;
+        rat2 = 0.;
+      }
+    } else {
+      o.facclr1[lev + 1] = 0.;
+      o.facclr2[lev + 1] = 0.;
+      if (o.istcld[lev] == 1) {
+        o.faccld1[lev + 1] = 0.;
+        o.faccld2[lev + 1] = (cf[lev] - cf[lev + 1]) / cf[lev];
+        o.facclr2[lev] = 0.;
+        o.faccld2[lev] = 0.;
+      } else {
+        const double fmin = std::min(cf[lev], cf[lev - 1]);
+        if (cf[lev + 1] <= fmin) {
+          o.faccld1[lev + 1] = rat1;
+          o.faccld2[lev + 1] = (fmin - cf[lev + 1]) / fmin;
+        } else {
+          o.faccld1[lev + 1] = (cf[lev] - cf[lev + 1]) / (cf[lev] - fmin);
+          o.faccld2[lev + 1] = 0.;
+        }
+      }
+      if (o.faccld1[lev + 1] > 0. || o.faccld2[lev + 1] > 0.) {
+        rat1 = 0.;
+        rat2 = 1.;
+      } else {
+        rat1 = 0.;
+        rat2 = 0.;
+      }
+    }
+    o.faccmb1[lev + 1] = o.facclr1[lev + 1] * o.faccld2[lev] * cf[lev - 1];
+    o.faccmb2[lev + 1] = o.faccld1[lev + 1] * o.facclr2[lev] * (1. - cf[lev - 1]);
+  }
+  // downward (:405-475)
+  for (int lev = nl; lev >= 1; --lev) {
+    if (icldlyr[lev] != 1) {
+      o.istcldd[lev - 1] = 1;
+      continue;
+    }
+    o.istcldd[lev - 1] = 0;
+    if (lev == 1) {
+      o.faccld1d[lev - 1] = o.faccld2d[lev - 1] = o.facclr1d[lev - 1] = 0.;
+      o.facclr2d[lev - 1] = o.faccmb1d[lev - 1] = o.faccmb2d[lev - 1] = 0.;
+    } else if (cf[lev - 1] >= cf[lev]) {
+      o.faccld1d[lev - 1] = 0.;
+      o.faccld2d[lev - 1] = 0.;
+      if (o.istcldd[lev] == 1) {
+        o.facclr1d[lev - 1] = 0.;
+        o.facclr2d[lev - 1] = 0.;
+        if (cf[lev] < 1.) o.facclr2d[lev - 1] = (cf[lev - 1] - cf[lev]) / (1. - cf[lev]);
+        o.facclr2d[lev] = 0.;
+        o.faccld2d[lev] = 0.;
+      } else {
+        const double fmax = std::max(cf[lev], cf[lev + 1]);
+        if (cf[lev - 1] > fmax) {
+          o.facclr1d[lev - 1] = rat2;
+          o.facclr2d[lev - 1] = (cf[lev - 1] - fmax) / (1. - fmax);
+        } else if (cf[lev - 1] < fmax) {
+          o.facclr1d[lev - 1] = (cf[lev - 1] - cf[lev]) / (cf[lev + 1] - cf[lev]);
+          o.facclr2d[lev - 1] = 0.;
+        } else {
+          o.facclr1d[lev - 1] = rat2;
+          o.facclr2d[lev - 1] = 0.;
+        }
+      }
+      if (o.facclr1d[lev - 1] > 0. || o.facclr2d[lev - 1] > 0.) {
+        rat1 = 1.;
+        rat2 = 0.;
+      } else {
+        rat1 = 0.;
+        rat2 = 0.;
+      }
+    } else {
+      o.facclr1d[lev - 1] = 0.;
+      o.facclr2d[lev - 1] = 0.;
+      if (o.istcldd[lev] == 1) {
+        o.faccld1d[lev - 1] = 0.;
+        o.faccld2d[lev - 1] = (cf[lev] - cf[lev - 1]) / cf[lev];
+        o.facclr2d[lev] = 0.;
+        o.faccld2d[lev] = 0.;
+      } else {
+        const double fmin = std::min(cf[lev], cf[lev + 1]);
+        if (cf[lev - 1] <= fmin) {
+          o.faccld1d[lev - 1] = rat1;
+          o.faccld2d[lev - 1] = (fmin - cf[lev - 1]) / fmin;
+        } else {
+          o.faccld1d[lev - 1] = (cf[lev] - cf[lev - 1]) / (cf[lev] - fmin);
+          o.faccld2d[lev - 1] = 0.;
+        }
+      }
+      if (o.faccld1d[lev - 1] > 0. || o.faccld2d[lev - 1] > 0.) {
+        rat1 = 0.;
+        rat2 = 1.;
+      } else {
+        rat1 = 0.;
+        rat2 = 0.;
+      }
+    }
+    o.faccmb1d[lev - 1] = o.facclr1d[lev - 1] * o.faccld2d[lev] * cf[lev + 1];
+    o.faccmb2d[lev - 1] = o.faccld1d[lev - 1] * o.facclr2d[lev] * (1. - cf[lev + 1]);
+  }
+}
+
+void lw_rtrnmr_cld(LwColumn& c, int idrv, LwOut& out) {
+  const LwTables& T = g_lw;
+  const int nl = c.nlayers;
+  const double wtdiff = 0.5, rec_6 = 0.166667;
+  static const double a0[17] = {0, 1.66, 1.55, 1.58, 1.66, 1.54, 1.454, 1.89, 1.33, 1.668, 1.66, 1.66, 1.66, 1.66, 1.66, 1.66, 1.66};
+  static const double a1[17] = {0, 0.00, 0.25, 0.22, 0.00, 0.13, 0.446, -0.10, 0.40, -0.006, 0.00, 0.00, 0.00, 0.00, 0.00, 0.00, 0.00};
+  static const double a2[17] = {0, 0.00, -12.0, -11.7, 0.00, -0.72, -0.243, 0.19, -0.062, 0.414, 0.00, 0.00, 0.00, 0.00, 0.00, 0.00, 0.00};
+  double secdiff[17];
+  for (int ibnd = 1; ibnd <= 16; ++ibnd) {
+    if (ibnd == 1 || ibnd == 4 || ibnd >= 10) {
+      secdiff[ibnd] = 1.66;
+    } else {
+      secdiff[ibnd] = a0[ibnd] + a1[ibnd] * std::exp(a2[ibnd] * c.pwvcm);
+      if (secdiff[ibnd] > 1.80) secdiff[ibnd] = 1.80;
+      if (secdiff[ibnd] < 1.50) secdiff[ibnd] = 1.50;
+    }
+  }
+  // cloudy layers and their cloud optical depths (:315-323)
+  std::vector<int> icldlyr(nl + 2, 0);
+  std::vector<double> odcld[17];
+  for (int ib = 1; ib <= 16; ++ib) odcld[ib].assign(nl + 1, 0.0);
+  for (int lay = 1; lay <= nl; ++lay)
+    for (int ib = 1; ib <= 16; ++ib) {
+      if (c.cldfrac[lay] >= 1.e-6) {
+        odcld[ib][lay] = secdiff[ib] * c.taucloud[ib][lay];
+        icldlyr[lay] = 1;
+      } else {
+        odcld[ib][lay] = 0.0;
+        icldlyr[lay] = 0;
+      }
+    }
+  MrOverlap ov;
+  lw_mr_overlap(c.cldfrac, icldlyr, nl, ov);
+  const std::vector<double>& cf = c.cldfrac;
+  auto tbl = [&](double od, double& trans, double& tfn, double& odq) {
+    if (g_table_mode) {
+      const double tblind = od / (T.bpade + od);
+      const int it = (int)(10000.0 * tblind + 0.5);
+      trans = T.exp_tbl[it];
+      tfn = T.tfn_tbl[it];
+      odq = T.tau_tbl[it];
+    } else {
+      trans = std::exp(-od);
+      tfn = 1. - 2. * ((1. / od) - (trans / (1. - trans)));
+      odq = od;
+    }
+  };
+  std::vector<double> urad(nl + 1, 0.0), drad(nl + 1, 0.0), totu(nl + 1, 0.0), totd(nl + 1, 0.0);
+  std::vector<double> clru(nl + 1, 0.0), clrd(nl + 1, 0.0), totuc(nl + 1, 0.0), totdc(nl + 1, 0.0);
+  std::vector<double> d_urad(nl + 1, 0.0), d_clru(nl + 1, 0.0), dtotu_dt(nl + 1, 0.0), dtotuc_dt(nl + 1, 0.0);
+  std::vector<double> atrans(nl + 1), bbugas(nl + 1), atot(nl + 1), bbutot(nl + 1);
+  int igc = 1;
+  for (int iband = 1; iband <= 16; ++iband) {
+    const int ib = iband;  // ncbands = 16: ipat(iband, 2) = iband
+    for (; igc <= T.ngs[iband]; ++igc) {
+      double radld = 0., radclrd = 0.;
+      double cldradd = 0., clrradd = 0., rad = 0.;
+      int iclddn = 0;
+      for (int lev = nl; lev >= 1; --lev) {  // :500-617
+        const double plfrac = c.fracs[igc][lev];
+        const double blay = c.planklay[iband][lev];
+        const double dplankup = c.planklev[iband][lev] - blay;
+        const double dplankdn = c.planklev[iband][lev - 1] - blay;
+        double odepth = secdiff[iband] * c.taut[igc][lev];
+        if (odepth < 0.0) odepth = 0.0;
+        double bbd;
+        if (icldlyr[lev] == 1) {
+          iclddn = 1;
+          double odtot = odepth + odcld[ib][lev];
+          double gassrc, bbdtot;
+          if (odtot < 0.06) {
+            atrans[lev] = odepth - 0.5 * odepth * odepth;
+            const double odepth_rec = rec_6 * odepth;
+            gassrc = plfrac * (blay + dplankdn * odepth_rec) * atrans[lev];
+            atot[lev] = odtot - 0.5 * odtot * odtot;
+            const double odtot_rec = rec_6 * odtot;
+            bbdtot = plfrac * (blay + dplankdn * odtot_rec);
+            bbd = plfrac * (blay + dplankdn * odepth_rec);
+            bbugas[lev] = plfrac * (blay + dplankup * odepth_rec);
+            bbutot[lev] = plfrac * (blay + dplankup * odtot_rec);
+          } else if (odepth <= 0.06) {
+            atrans[lev] = odepth - 0.5 * odepth * odepth;
+            const double odepth_rec = rec_6 * odepth;
+            gassrc = plfrac * (blay + dplankdn * odepth_rec) * atrans[lev];
+            odtot = odepth + odcld[ib][lev];
+            double ttot, tfactot, odq;
+            tbl(odtot, ttot, tfactot, odq);
+            bbdtot = plfrac * (blay + tfactot * dplankdn);
+            bbd = plfrac * (blay + dplankdn * odepth_rec);
+            atot[lev] = 1. - ttot;
+            bbugas[lev] = plfrac * (blay + dplankup * odepth_rec);
+            bbutot[lev] = plfrac * (blay + tfactot * dplankup);
+          } else {
+            double tgas, tfacgas, odq;
+            tbl(odepth, tgas, tfacgas, odq);
+            odepth = odq;  // odepth = tau_tbl(itgas)
+            atrans[lev] = 1. - tgas;
+            gassrc = atrans[lev] * plfrac * (blay + tfacgas * dplankdn);
+            odtot = odepth + odcld[ib][lev];
+            double ttot, tfactot, odq2;
+            tbl(odtot, ttot, tfactot, odq2);
+            bbdtot = plfrac * (blay + tfactot * dplankdn);
+            bbd = plfrac * (blay + tfacgas * dplankdn);
+            atot[lev] = 1. - ttot;
+            bbugas[lev] = plfrac * (blay + tfacgas * dplankup);
+            bbutot[lev] = plfrac * (blay + tfactot * dplankup);
+          }
+          if (ov.istcldd[lev] == 1) {
+            cldradd = cf[lev] * radld;
+            clrradd = radld - cldradd;
+            rad = 0.;
+          }
+          const double ttot = 1. - atot[lev];
+          const double cldsrc = bbdtot * atot[lev];
+          cldradd = cldradd * ttot + cf[lev] * cldsrc;
+          clrradd = clrradd * (1. - atrans[lev]) + (1. - cf[lev]) * gassrc;
+          radld = cldradd + clrradd;
+          drad[lev - 1] = drad[lev - 1] + radld;
+          const double radmod = rad * (ov.facclr1d[lev - 1] * (1. - atrans[lev]) + ov.faccld1d[lev - 1] * ttot) -
+                                ov.faccmb1d[lev - 1] * gassrc + ov.faccmb2d[lev - 1] * cldsrc;
+          const double oldcld = cldradd - radmod;
+          const double oldclr = clrradd + radmod;
+          rad = -radmod + ov.facclr2d[lev - 1] * oldclr - ov.faccld2d[lev - 1] * oldcld;
+          cldradd = cldradd + rad;
+          clrradd = clrradd - rad;
+        } else {
+          if (odepth <= 0.06) {
+            atrans[lev] = odepth - 0.5 * odepth * odepth;
+            odepth = rec_6 * odepth;
+            bbd = plfrac * (blay + dplankdn * odepth);
+            bbugas[lev] = plfrac * (blay + dplankup * odepth);
+          } else {
+            double transc, tausfac, odq;
+            tbl(odepth, transc, tausfac, odq);
+            atrans[lev] = 1. - transc;
+            bbd = plfrac * (blay + tausfac * dplankdn);
+            bbugas[lev] = plfrac * (blay + tausfac * dplankup);
+          }
+          radld = radld + (bbd - radld) * atrans[lev];
+          drad[lev - 1] = drad[lev - 1] + radld;
+        }
+        if (iclddn == 1) {  // :606-614
+          radclrd = radclrd + (bbd - radclrd) * atrans[lev];
+          clrd[lev - 1] = clrd[lev - 1] + radclrd;
+        } else {
+          radclrd = radld;
+          clrd[lev - 1] = drad[lev - 1];
+        }
+      }
+      const double rad0 = c.fracs[igc][1] * c.plankbnd[iband];
+      const double reflect = 1. - c.semiss[iband];
+      double radlu = rad0 + reflect * radld;
+      double radclru = rad0 + reflect * radclrd;
+      urad[0] = urad[0] + radlu;
+      clru[0] = clru[0] + radclru;
+      double d_radlu_dt = 0.0, d_radclru_dt = 0.0;
+      if (idrv == 1) {
+        const double d_rad0_dt = c.fracs[igc][1] * c.dplankbnd_dt[iband];
+        d_radlu_dt = d_rad0_dt;
+        d_urad[0] = d_urad[0] + d_radlu_dt;
+        d_radclru_dt = d_rad0_dt;
+        d_clru[0] = d_clru[0] + d_radclru_dt;
+      }
+      double cldradu = 0., clrradu = 0.;
+      rad = 0.;
+      for (int lev = 1; lev <= nl; ++lev) {  // :649-705
+        if (icldlyr[lev] == 1) {
+          const double gassrc = bbugas[lev] * atrans[lev];
+          if (ov.istcld[lev] == 1) {
+            cldradu = cf[lev] * radlu;
+            clrradu = radlu - cldradu;
+            rad = 0.;
+          }
+          const double ttot = 1. - atot[lev];
+          const double cldsrc = bbutot[lev] * atot[lev];
+          cldradu = cldradu * ttot + cf[lev] * cldsrc;
+          clrradu = clrradu * (1.0 - atrans[lev]) + (1. - cf[lev]) * gassrc;
+          radlu = cldradu + clrradu;
+          urad[lev] = urad[lev] + radlu;
+          const double radmod = rad * (ov.facclr1[lev + 1] * (1.0 - atrans[lev]) + ov.faccld1[lev + 1] * ttot) -
+                                ov.faccmb1[lev + 1] * gassrc + ov.faccmb2[lev + 1] * cldsrc;
+          const double oldcld = cldradu - radmod;
+          const double oldclr = clrradu + radmod;
+          rad = -radmod + ov.facclr2[lev + 1] * oldclr - ov.faccld2[lev + 1] * oldcld;
+          cldradu = cldradu + rad;
+          clrradu = clrradu - rad;
+          if (idrv == 1) {
+            d_radlu_dt = d_radlu_dt * cf[lev] * (1.0 - atot[lev]) + d_radlu_dt * (1.0 - cf[lev]) * (1.0 - atrans[lev]);
+            d_urad[lev] = d_urad[lev] + d_radlu_dt;
+          }
+        } else {
+          radlu = radlu + (bbugas[lev] - radlu) * atrans[lev];
+          urad[lev] = urad[lev] + radlu;
+          if (idrv == 1) {
+            d_radlu_dt = d_radlu_dt * (1.0 - atrans[lev]);
+            d_urad[lev] = d_urad[lev] + d_radlu_dt;
+          }
+        }
+        if (iclddn == 1) {
+          radclru = radclru + (bbugas[lev] - radclru) * atrans[lev];
+          clru[lev] = clru[lev] + radclru;
+        } else {
+          radclru = radlu;
+          clru[lev] = urad[lev];
+        }
+        if (idrv == 1) {
+          if (iclddn == 1) {
+            d_radclru_dt = d_radclru_dt * (1.0 - atrans[lev]);
+            d_clru[lev] = d_clru[lev] + d_radclru_dt;
+          } else {
+            d_radclru_dt = d_radlu_dt;
+            d_clru[lev] = d_urad[lev];
+          }
+        }
+      }
+    }
+    for (int lev = nl; lev >= 0; --lev) {  // :711-726
+      const double uflux = urad[lev] * wtdiff, dflux = drad[lev] * wtdiff;
+      urad[lev] = 0.0;
+      drad[lev] = 0.0;
+      totu[lev] = totu[lev] + uflux * T.delwave[iband];
+      totd[lev] = totd[lev] + dflux * T.delwave[iband];
+      const double uclfl = clru[lev] * wtdiff, dclfl = clrd[lev] * wtdiff;
+      clru[lev] = 0.0;
+      clrd[lev] = 0.0;
+      totuc[lev] = totuc[lev] + uclfl * T.delwave[iband];
+      totdc[lev] = totdc[lev] + dclfl * T.delwave[iband];
+    }
+    if (idrv == 1) {
+      for (int lev = nl; lev >= 0; --lev) {
+        const double duflux_dt = d_urad[lev] * wtdiff;
+        d_urad[lev] = 0.0;
+        dtotu_dt[lev] = dtotu_dt[lev] + duflux_dt * T.delwave[iband] * T.fluxfac;
+        const double duclfl_dt = d_clru[lev] * wtdiff;
+        d_clru[lev] = 0.0;
+        dtotuc_dt[lev] = dtotuc_dt[lev] + duclfl_dt * T.delwave[iband] * T.fluxfac;
+      }
+    }
+  }
+  std::vector<double> fnet(nl + 1), fnetc(nl + 1);
+  totu[0] = totu[0] * T.fluxfac;
+  totd[0] = totd[0] * T.fluxfac;
+  fnet[0] = totu[0] - totd[0];
+  totuc[0] = totuc[0] * T.fluxfac;
+  totdc[0] = totdc[0] * T.fluxfac;
+  fnetc[0] = totuc[0] - totdc[0];
+  out.htr.assign(nl + 1, 0.0);
+  out.htrc.assign(nl + 1, 0.0);
+  for (int lev = 1; lev <= nl; ++lev) {
+    totu[lev] = totu[lev] * T.fluxfac;
+    totd[lev] = totd[lev] * T.fluxfac;
+    fnet[lev] = totu[lev] - totd[lev];
+    totuc[lev] = totuc[lev] * T.fluxfac;
+    totdc[lev] = totdc[lev] * T.fluxfac;
+    fnetc[lev] = totuc[lev] - totdc[lev];
+    const int l = lev - 1;
+    out.htr[l] = T.heatfac * (fnet[l] - fnet[lev]) / (c.pz[l] - c.pz[lev]);
+    out.htrc[l] = T.heatfac * (fnetc[l] - fnetc[lev]) / (c.pz[l] - c.pz[lev]);
+  }
+  out.totu = totu;
+  out.totd = totd;
+  out.dtotu_dt = dtotu_dt;
+  out.totuc = totuc;
+  out.totdc = totdc;
+  out.dtotuc_dt = dtotuc_dt;
+}
+
 void lw_column(const LwInput& in, int iplon, int idrv, LwColumn& c, LwOut& out) {
   lw_inatm(in, iplon, c);
   lw_setcoef(c, idrv);
@@ -1449,9 +1882,12 @@ void lw_column(const LwInput& in, int iplon, int idrv, LwColumn& c, LwOut& out) 
   for (int b = 1; b <= 16; ++b)
     for (; ig <= g_lw.ngs[b]; ++ig)
       for (int k = 1; k <= c.nlayers; ++k) c.taut[ig][k] = c.taug[ig][k] + c.taua[b][k];
-  // icld = 1: rtrn (random overlap); clear sky: rtrnmr (:527-541)
+  // icld = 1: rtrn (random overlap); icld = 2, 3: rtrnmr with clouds
+  // (maximum/random overlap); clear sky: rtrnmr (:527-541)
   if (in.icld == 1) {
     lw_rtrn(c, idrv, out);
+  } else if (in.icld >= 2) {
+    lw_rtrnmr_cld(c, idrv, out);
   } else {
     lw_rtrnmr(c, idrv, out);
     out.totuc = out.totu;

@@ -1,6 +1,7 @@
 """Clouds on the GPU against the oracle's restatement of the reference: LW
-icld = 1 (random overlap, cloud optical depths given, inflglw = 0;
-rrtmg_lw_cldprop.f90:155-174, rrtmg_lw_rtrn.f90) and SW icld = 1 (cloud
+with cloud optical depths given (inflglw = 0, rrtmg_lw_cldprop.f90:155-174),
+icld = 1 (random overlap, rrtmg_lw_rtrn.f90) and icld = 2 / 3
+(maximum/random overlap, rrtmg_lw_rtrnmr.f90); SW icld = 1 (cloud
 optics given, inflgsw = 0, clear or overcast layers;
 rrtmg_sw_cldprop.f90:120-156, rrtmg_sw_spcvrt.f90's clear and total passes).
 
@@ -57,17 +58,18 @@ def _check_clear_outputs(out, ref, idrv):
 @pytest.mark.parametrize("nlay", [40, 60])
 @pytest.mark.parametrize("mode", ["table", "analytic"])
 @pytest.mark.parametrize("idrv", [0, 1])
-def test_lw_clouds_fp64_matches_oracle(gpu, orc, nlay, mode, idrv):
-    atm, cl = _case(nlay, 900 + nlay + idrv)
+@pytest.mark.parametrize("icld", [1, 2])
+def test_lw_clouds_fp64_matches_oracle(gpu, orc, nlay, mode, idrv, icld):
+    atm, cl = _case(nlay, 900 + nlay + idrv + 10 * icld)
     orc.set_table_mode(mode == "table")
     try:
-        ref = orc.rrtmg_lw(atm, idrv=idrv, cloud=cl)
+        ref = orc.rrtmg_lw(atm, idrv=idrv, cloud=cl, icld=icld)
     finally:
         orc.set_table_mode(True)
     gpu.set_precision("fp64")
     gpu.set_transcendentals(mode)
     try:
-        out = gpu.lw(atm, idrv=idrv, cloud=cl)
+        out = gpu.lw(atm, idrv=idrv, cloud=cl, icld=icld)
     finally:
         gpu.set_transcendentals("table")
     check_lw(out, ref, idrv=idrv)
@@ -78,12 +80,13 @@ def test_lw_clouds_fp64_matches_oracle(gpu, orc, nlay, mode, idrv):
 
 
 @pytest.mark.parametrize("nlay", [40, 60])
-def test_lw_clouds_split_within_bars(gpu, orc, nlay):
-    atm, cl = _case(nlay, 950 + nlay, n=768)
-    ref = orc.rrtmg_lw(atm, idrv=1, cloud=cl)
+@pytest.mark.parametrize("icld", [1, 2])
+def test_lw_clouds_split_within_bars(gpu, orc, nlay, icld):
+    atm, cl = _case(nlay, 950 + nlay + 10 * icld, n=768)
+    ref = orc.rrtmg_lw(atm, idrv=1, cloud=cl, icld=icld)
     gpu.set_precision("split")
     try:
-        out = gpu.lw(atm, idrv=1, cloud=cl)
+        out = gpu.lw(atm, idrv=1, cloud=cl, icld=icld)
     finally:
         gpu.set_precision("fp64")
     bar = SB.hr_bar(atm)
@@ -94,8 +97,9 @@ def test_lw_clouds_split_within_bars(gpu, orc, nlay):
     assert np.abs(out["duflx_dt"] - ref["duflx_dt"]).max() <= 1e-3
 
 
-def test_lw_clouds_without_clouds_equal_clear_sky(gpu):
-    """icld = 1 with no cloud (cover 0, or below rtrn's 1e-6) takes rtrn's clear
+@pytest.mark.parametrize("icld", [1, 2])
+def test_lw_clouds_without_clouds_equal_clear_sky(gpu, icld):
+    """Clouds with no cloud (cover 0, or below the solvers' 1e-6) take the clear
     branch everywhere: the FP64 results are the clear-sky call's bit for bit,
     the split ones within FP32 rounding."""
     atm = A.small_atmosphere(200, 40, seed=17)
@@ -104,7 +108,7 @@ def test_lw_clouds_without_clouds_equal_clear_sky(gpu):
     for prec in ("fp64", "split"):
         gpu.set_precision(prec)
         try:
-            a, b = gpu.lw(atm, idrv=1), gpu.lw(atm, idrv=1, cloud=cl)
+            a, b = gpu.lw(atm, idrv=1), gpu.lw(atm, idrv=1, cloud=cl, icld=icld)
         finally:
             gpu.set_precision("fp64")
         for k in a:
@@ -116,19 +120,33 @@ def test_lw_clouds_without_clouds_equal_clear_sky(gpu):
                 assert np.abs(a[k] - b[k]).max() <= 1e-3, k
 
 
-def test_lw_clouds_host_entry_matches_device_entry(gpu):
+def test_lw_maximum_random_overlap_icld_3_is_icld_2(gpu):
+    """The non-McICA driver sends icld = 2 and 3 to the same solver."""
+    atm, cl = _case(40, 41, n=256)
+    for prec in ("fp64", "split"):
+        gpu.set_precision(prec)
+        try:
+            a, b = gpu.lw(atm, idrv=1, cloud=cl, icld=2), gpu.lw(atm, idrv=1, cloud=cl, icld=3)
+        finally:
+            gpu.set_precision("fp64")
+        for k in a:
+            assert np.array_equal(a[k], b[k]), (prec, k)
+
+
+@pytest.mark.parametrize("icld", [1, 2])
+def test_lw_clouds_host_entry_matches_device_entry(gpu, icld):
     """rrtmg_lw_c (page-locked arrays, 40000 columns: two column chunks on two
     streams, taucld copied 16 values per column) against rrtmg_lw_dev on the
     same arrays, bit for bit."""
     torch = pytest.importorskip("torch")
-    atm, cl = _case(40, 77, n=40000)
+    atm, cl = _case(40, 77 + icld, n=40000)
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
     L, n = atm.nlay, atm.ncol
     outs = {k: pin(np.zeros((L + 1 if k not in ("hr", "hrc") else L, n))) for k in
             ("uflx", "dflx", "hr", "uflxc", "dflxc", "hrc", "duflx_dt", "duflxc_dt")}
     gpu.set_precision("split")
     try:
-        host = gpu.rrtmg_lw(n, L, 1, 1, *[pin(a) for a in (atm.play, atm.plev, atm.tlay, atm.tlev, atm.tsfc, atm.h2o,
+        host = gpu.rrtmg_lw(n, L, icld, 1, *[pin(a) for a in (atm.play, atm.plev, atm.tlay, atm.tlev, atm.tsfc, atm.h2o,
                                                             atm.o3, atm.co2, atm.ch4, atm.n2o, atm.o2, atm.cfc11,
                                                             atm.cfc12, atm.cfc22, atm.ccl4, atm.emis)],
                             out=outs, cldfr=pin(cl["cldfr"]), taucld=pin(cl["taucld"]))
@@ -138,7 +156,7 @@ def test_lw_clouds_host_entry_matches_device_entry(gpu):
         o, _ = R.device_outputs(n, L, idrv=1)
         s = torch.cuda.Stream()
         with torch.cuda.stream(s):
-            gpu.rrtmg_lw_dev(s.cuda_stream, n, L, 1, 1, d, o)
+            gpu.rrtmg_lw_dev(s.cuda_stream, n, L, icld, 1, d, o)
         s.synchronize()
     finally:
         gpu.set_precision("fp64")
@@ -150,8 +168,8 @@ def test_lw_cloud_options_not_computed_are_refused(gpu):
     atm, cl = _case(40, 5, n=16)
     args = (atm.ncol, atm.nlay)
     base = (atm.play, atm.plev, atm.tlay, atm.tlev, atm.tsfc, atm.h2o, atm.o3, atm.co2)
-    o = gpu.rrtmg_lw(*args, 2, 0, *base, check=False, cldfr=cl["cldfr"], taucld=cl["taucld"])
-    assert o["status"] == R.RRTMG_ERR_UNSUPPORTED  # maximum-random overlap
+    o = gpu.rrtmg_lw(*args, 4, 0, *base, check=False, cldfr=cl["cldfr"], taucld=cl["taucld"])
+    assert o["status"] == R.RRTMG_ERR_UNSUPPORTED  # icld outside 0..3
     o = gpu.rrtmg_lw(*args, 1, 0, *base, check=False, inflglw=2, cldfr=cl["cldfr"], taucld=cl["taucld"])
     assert o["status"] == R.RRTMG_ERR_UNSUPPORTED  # cloud physics (cldprop inflag = 2)
     o = gpu.rrtmg_lw(*args, 1, 0, *base, check=False, cldfr=cl["cldfr"])

@@ -373,3 +373,41 @@ def test_sw_clouds_overcast(orc):
     night.coszen = np.zeros_like(night.coszen)
     dark = orc.rrtmg_sw(night, cloud=part)
     assert not any(np.any(v) for v in dark.values())
+
+
+def test_lw_clouds_maximum_random_overlap(orc):
+    """The oracle's maximum/random overlap (icld = 2, 3: rtrnmr's cloudy
+    branches):
+    * with no cloud it reproduces clear sky bit for bit, for icld = 2 and 3;
+    * isolated cloudy layers overlap the same way under every assumption, so
+      it agrees with random overlap up to the transmittance tables' steps;
+    * two adjacent opaque layers of equal cover c overlap maximally: the
+      fluxes are (1 - c) x clear sky + c x overcast, where random overlap
+      leaves less of the column clear;
+    * fully overcast layers are the same under both overlaps."""
+    atm = A.small_atmosphere(24, 40, seed=5)
+    L, n = atm.nlay, atm.ncol
+    clear = orc.rrtmg_lw(atm, idrv=1)
+    z = dict(cldfr=np.zeros((L, n)), taucld=np.zeros((L, n, 16)))
+    for icld in (2, 3):
+        r = orc.rrtmg_lw(atm, idrv=1, cloud=z, icld=icld)
+        for k in clear:
+            assert np.array_equal(r[k], clear[k]), (icld, k)
+    cf, tau = np.zeros((L, n)), np.zeros((L, n, 16))
+    cf[8], cf[15], cf[22] = 0.4, 0.7, 0.3
+    tau[8], tau[15], tau[22] = 2.0, 5.0, 1.0
+    iso = dict(cldfr=cf, taucld=tau)
+    a, b = orc.rrtmg_lw(atm, idrv=1, cloud=iso, icld=1), orc.rrtmg_lw(atm, idrv=1, cloud=iso, icld=2)
+    for k in ("uflx", "dflx"):
+        assert np.abs(a[k] - b[k]).max() < 2e-3, k
+    assert np.array_equal(a["duflx_dt"], b["duflx_dt"])
+    c2, t2 = np.zeros((L, n)), np.zeros((L, n, 16))
+    c2[12:14], t2[12:14] = 0.5, 1e3
+    half_mr = orc.rrtmg_lw(atm, cloud=dict(cldfr=c2, taucld=t2), icld=2)
+    half_r = orc.rrtmg_lw(atm, cloud=dict(cldfr=c2, taucld=t2), icld=1)
+    over = orc.rrtmg_lw(atm, cloud=dict(cldfr=2 * c2, taucld=t2), icld=2)
+    for k in ("uflx", "dflx"):
+        assert np.allclose(half_mr[k], 0.5 * (clear[k] + over[k]), rtol=1e-12, atol=1e-9), k
+    assert np.all(half_mr["uflx"][-1] > half_r["uflx"][-1] + 5.0)
+    over_r = orc.rrtmg_lw(atm, cloud=dict(cldfr=2 * c2, taucld=t2), icld=1)
+    assert np.allclose(over["uflx"], over_r["uflx"], rtol=1e-12, atol=1e-9)

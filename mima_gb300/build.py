@@ -56,19 +56,31 @@ def _stale(obj: Path, src: Path) -> bool:
     return any(d.stat().st_mtime > t for d in deps)
 
 
-def build(force: bool = False, verbose: bool = False, extra=None) -> Path:
+def build(force: bool = False, verbose: bool = False, extra=None, variant: str | None = None) -> Path:
+    """Builds the library.  ``variant``: a named build with the ``extra`` nvcc
+    flags (e.g. ``-DRRTMG_TABLE_PREFETCH_L2=0``, no L2 prefetch of the band
+    tables) into ``lib/variants/<variant>/``, for timing it beside the default
+    library (load it with RRTMG_GPU_LIB)."""
+    if variant:
+        vdir = LIBDIR / "variants" / variant
+        return _build_into(vdir / "obj", vdir / "librrtmg_gpu.so", force, verbose, extra)
+    return _build_into(OBJDIR, LIB, force, verbose, extra, peak=True)
+
+
+def _build_into(objdir: Path, lib: Path, force: bool, verbose: bool, extra, peak: bool = False) -> Path:
     OBJDIR.mkdir(parents=True, exist_ok=True)
+    objdir.mkdir(parents=True, exist_ok=True)
     cc = nvcc()
     procs = []
     objs = []
     peak_src = CSRC / "fp32_peak.cu"
-    if force or not PEAK_LIB.exists() or peak_src.stat().st_mtime > PEAK_LIB.stat().st_mtime:
+    if peak and (force or not PEAK_LIB.exists() or peak_src.stat().st_mtime > PEAK_LIB.stat().st_mtime):
         cmd = [cc, *ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", str(peak_src), "-o", str(PEAK_LIB)]
         procs.append(("fp32_peak.cu", subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT,
                                                       text=True)))
     for unit, flags in UNITS.items():
         src = CSRC / unit
-        obj = OBJDIR / (unit + ".o")
+        obj = objdir / (unit + ".o")
         objs.append(obj)
         if force or _stale(obj, src):
             cmd = [cc, *ARCH, *COMMON, *flags, *(extra or []), "-c", str(src), "-o", str(obj)]
@@ -84,14 +96,14 @@ def build(force: bool = False, verbose: bool = False, extra=None) -> Path:
             print(out)
     if errors:
         raise RuntimeError("nvcc failed:\n" + "\n".join(errors))
-    if force or any(u != "fp32_peak.cu" for u, _ in procs) or not LIB.exists():
-        tmp = LIB.with_suffix(".so.tmp")
+    if force or any(u != "fp32_peak.cu" for u, _ in procs) or not lib.exists():
+        tmp = lib.with_suffix(".so.tmp")
         cmd = [cc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
-        os.replace(tmp, LIB)
-    return LIB
+        os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":

@@ -39,6 +39,7 @@ struct BandDesc {
   int nspa, nspb;
   int off[16];     // element offset of each role's table, -1 if the band has none
   int nrow[16];    // extent of the first non-g index of 2-/3-d tables (row stride helper)
+  int tbeg, tend;  // element range of all the band's tables (multiples of 4: 16-byte aligned)
   double delwave;
 };
 
@@ -56,8 +57,7 @@ enum SwField {
 // Table gather (k-distribution and transmittance tables: read-only and reused
 // by every cell of a band) and per-layer prep-field load: the read-only path.
 // L1 eviction-priority variants of both (tables evict-last, fields
-// evict-first) and a TMA prefetch of each block's band tables into L2 were
-// measured on GB300 and changed neither solver's time.
+// evict-first) were measured on GB300 and changed neither solver's time.
 template <class T>
 __device__ __forceinline__ T tld(const T* p) {
   return __ldg(p);
@@ -65,6 +65,21 @@ __device__ __forceinline__ T tld(const T* p) {
 template <class T>
 __device__ __forceinline__ T fld_ld(const T* p) {
   return __ldg(p);
+}
+
+// Stages a band's k-distribution tables into L2 through the bulk-copy (TMA)
+// unit: one cp.async.bulk.prefetch.L2 of the band's table range, whose start
+// and length are multiples of 16 bytes (BandDesc::tbeg / tend).  Issued by
+// one thread of each g-point block before its first gather; a hint, it
+// neither waits nor changes any result.
+#ifndef RRTMG_TABLE_PREFETCH_L2
+#define RRTMG_TABLE_PREFETCH_L2 1
+#endif
+template <class T>
+__device__ __forceinline__ void prefetch_band_l2(const T* tab, const BandDesc& bd) {
+  const unsigned bytes = (unsigned)((bd.tend - bd.tbeg) * (int)sizeof(T));
+  if (!RRTMG_TABLE_PREFETCH_L2 || bytes == 0) return;
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(tab + bd.tbeg), "r"(bytes) : "memory");
 }
 
 // Packed integer interpolation indices of one layer.

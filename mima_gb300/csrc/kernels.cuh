@@ -875,6 +875,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_LW_MINB :
     if (blk < nb) break;
     blk -= nb;
   }
+  if (threadIdx.x == 0 && band < kLwBands) prefetch_band_l2(tab, c_lw.band[band]);
   const bool an = FL < 0 ? analytic != 0 : (FL & 1) != 0;
   const int idv = FL < 0 ? idrv : ((FL & 2) ? 1 : 0);
 #define RRTMG_LW_CASE(b) \
@@ -906,6 +907,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_LW_MINB :
     if (blk < nb) break;
     blk -= nb;
   }
+  if (threadIdx.x == 0 && band < kLwBands) prefetch_band_l2(tab, c_lw.band[band]);
   const bool an = FL < 0 ? analytic != 0 : (FL & 1) != 0;
   const int idv = FL < 0 ? idrv : ((FL & 2) ? 1 : 0);
 #define RRTMG_LW_CASE(b)                                                                                            \
@@ -1719,6 +1721,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_SW_MINB :
     if (blk < nb) break;
     blk -= nb;
   }
+  if (threadIdx.x == 0 && band < kSwBands) prefetch_band_l2(tab, c_sw.band[band]);
   const bool an = FL < 0 ? analytic != 0 : (FL & 1) != 0;
   const int ia = FL < 0 ? iaer : ((FL & 2) ? 10 : 0);
 #define RRTMG_SW_CASE(b) \

@@ -125,6 +125,12 @@ std::vector<double> reduction_weights(int nbnd, const std::vector<int>& ngc, con
   return rwgt;
 }
 
+// Pads a table to a multiple of 4 elements, so that the next band's tables
+// start 16-byte aligned in FP32 and FP64 (the bulk-copy unit's alignment).
+void pad4(std::vector<double>& v) {
+  while (v.size() % 4) v.push_back(0.0);
+}
+
 // Reduce one table along axis gaxis to ngc g-points and append it to dst in
 // device layout.  Returns the element offset.
 int reduce_append(const Arr& a, int gaxis, int ngc, const int* ngn, const double* rw, bool weighted,
@@ -290,6 +296,8 @@ std::string build_host_tables(const char* blob_path, double cpdair, HostTables& 
       bd.nspb = nspb[b - 1];
       bd.delwave = delwave[b - 1];
       for (int r = 0; r < 16; ++r) bd.off[r] = -1;
+      pad4(T.lw_tab);
+      bd.tbeg = (int)T.lw_tab.size();
       char pre[8];
       std::snprintf(pre, sizeof pre, "lw%02d.", b);
       for (const auto& kv : m) {
@@ -306,6 +314,8 @@ std::string build_host_tables(const char* blob_path, double cpdair, HostTables& 
       }
       for (int r : {LW_KA, LW_SELF, LW_FOR, LW_FRA})
         if (bd.off[r] < 0) return "LW band lacks a key table";
+      pad4(T.lw_tab);
+      bd.tend = (int)T.lw_tab.size();
       goff += bd.ng;
     }
     // Bands without an upper key table still get a valid pointer.
@@ -380,6 +390,8 @@ std::string build_host_tables(const char* blob_path, double cpdair, HostTables& 
       bd.nspb = nspb[ib];
       bd.delwave = delwave[ib];
       for (int r = 0; r < 16; ++r) bd.off[r] = -1;
+      pad4(T.sw_tab);
+      bd.tbeg = (int)T.sw_tab.size();
       char pre[8];
       std::snprintf(pre, sizeof pre, "sw%02d.", b);
       for (const auto& kv : m) {
@@ -400,6 +412,8 @@ std::string build_host_tables(const char* blob_path, double cpdair, HostTables& 
         bd.nrow[role] = kv.second.dims[0];
       }
       if (bd.off[SW_SFLUX] < 0 || bd.off[SW_RAYL] < 0) return "SW band lacks solar source or Rayleigh table";
+      pad4(T.sw_tab);
+      bd.tend = (int)T.sw_tab.size();
       goff += bd.ng;
     }
     for (int b = 0; b < 14; ++b)

@@ -48,6 +48,9 @@ struct rrtmg_gpu_state {
   double *totplnk = nullptr, *totplnkderiv = nullptr;
   float *totplnk32 = nullptr, *totplnkderiv32 = nullptr;  // FP32 copies (split prep)
   float *lw_tab32 = nullptr, *sw_tab32 = nullptr, *lw_exp32 = nullptr, *lw_tfn32 = nullptr, *sw_exp32 = nullptr;
+  // FP32 LW transmittance and tau transition function side by side (one
+  // gather per table lookup in the split LW solver)
+  float2* lw_exptfn32 = nullptr;
   unsigned* flags = nullptr;
   DevBuf lw_ws, sw_ws, adj_ws;
   // host-pointer calls: a second stream and per-stream staging and scratch, so
@@ -92,6 +95,12 @@ cudaError_t upload(T** dst, const std::vector<T>& src) {
 std::vector<float> to_f32(const std::vector<double>& v) {
   std::vector<float> f(v.size());
   for (size_t i = 0; i < v.size(); ++i) f[i] = (float)v[i];
+  return f;
+}
+
+std::vector<float2> interleave_f32(const std::vector<double>& a, const std::vector<double>& b) {
+  std::vector<float2> f(a.size());
+  for (size_t i = 0; i < a.size(); ++i) f[i] = make_float2((float)a[i], (float)b[i]);
   return f;
 }
 
@@ -246,7 +255,7 @@ int lw_enqueue(rrtmg_gpu_state* h, cudaStream_t s, void* base, int ncol, int nla
                                  h->lw_tfn32, h->lw_tau32, w.bu, w.bd, w.bdu, w.buc, w.bdc, w.bduc, ncol, nlay, idrv,
                                  nb, h->analytic, s, w32.ovl);
     else
-      launch_lw_gpoint_split(prep_of(w32), in.emis, in.tauaer, h->lw_tab32, h->lw_exp32, h->lw_tfn32, w.bu, w.bd,
+      launch_lw_gpoint_split(prep_of(w32), in.emis, in.tauaer, h->lw_tab32, h->lw_exptfn32, w.bu, w.bd,
                              w.bdu, ncol, nlay, idrv, nb, h->analytic, s);
   } else {
     launch_lw_prep(in, w, h->totplnk, h->totplnkderiv, ncol, nlay, idrv, h->flags, s);
@@ -668,6 +677,7 @@ int rrtmg_gpu_init(double cpdair, const char* table_blob, int device, rrtmg_gpu_
   if (e == cudaSuccess) e = upload(&h->sw_tab32, to_f32(h->host.sw_tab));
   if (e == cudaSuccess) e = upload(&h->lw_exp32, to_f32(h->host.lw_exp));
   if (e == cudaSuccess) e = upload(&h->lw_tfn32, to_f32(h->host.lw_tfn));
+  if (e == cudaSuccess) e = upload(&h->lw_exptfn32, interleave_f32(h->host.lw_exp, h->host.lw_tfn));
   if (e == cudaSuccess) e = upload(&h->sw_exp32, to_f32(h->host.sw_exp));
   if (e == cudaSuccess) e = cudaMalloc((void**)&h->flags, sizeof(unsigned));
   if (e == cudaSuccess) e = cudaMemset(h->flags, 0, sizeof(unsigned));
@@ -695,7 +705,8 @@ int rrtmg_gpu_finalize(rrtmg_gpu_handle h) {
   void* ptrs[] = {h->lw_tab64, h->sw_tab64, h->lw_exp64, h->lw_tfn64, h->sw_exp64, h->totplnk, h->totplnkderiv,
                   h->lw_tau64, h->lw_tau32,
                   h->totplnk32, h->totplnkderiv32,
-                  h->lw_tab32, h->sw_tab32, h->lw_exp32, h->lw_tfn32, h->sw_exp32, h->flags, h->lw_ws.p,
+                  h->lw_tab32, h->sw_tab32, h->lw_exp32, h->lw_tfn32, h->lw_exptfn32, h->sw_exp32, h->flags,
+                  h->lw_ws.p,
                   h->sw_ws.p, h->adj_ws.p, h->hio[0].p, h->hio[1].p, h->hws[0].p, h->hws[1].p, h->run_ws.p,
                   h->run_cio[0].p, h->run_cio[1].p, h->run_cws[0].p, h->run_cws[1].p};
   for (void* p : ptrs)

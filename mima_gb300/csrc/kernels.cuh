@@ -392,12 +392,15 @@ __global__ void __launch_bounds__(128) lw_prep_column_kernel(LwIn in, LwWorkT<F>
 // LW g-point solver: taumol + rtrnmr clear-sky branch
 // (rrtmg_lw_rtrnmr.f90:505-616 downward, :628-713 upward) for one g-point.
 // ---------------------------------------------------------------------------
+// Split path: the two table lookups of a layer are one gather of exptfn
+// (exp_tbl and tfn_tbl interleaved); FP64 path: exptbl and tfntbl.
 template <int B, class R, int MAXL>
 __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __restrict__ emis,
                                         const double* __restrict__ tauaer, const R* __restrict__ tab,
                                         const R* __restrict__ exptbl, const R* __restrict__ tfntbl,
                                         double* __restrict__ bu, double* __restrict__ bd, double* __restrict__ bdu,
-                                        int ncol, int nlay, int idrv, bool analytic, int blk, float* sbuf) {
+                                        int ncol, int nlay, int idrv, bool analytic, int blk, float* sbuf,
+                                        const float2* __restrict__ exptfn) {
   const bool IDRV = idrv == 1;
   constexpr bool SPLIT = sizeof(R) == 4;
   constexpr int NG = lw_ng(B);
@@ -442,8 +445,12 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
   // No downward radiance enters at the top (drad(nlayers) stays 0,
   // rrtmg_lw_rtrnmr.f90:290-300).
   if (g == 0 && valid) bdp[(size_t)nlay * N] = 0.0;
-  // the packed table indices of the next layer are loaded one layer ahead
+  // the packed table indices of the next layer are loaded one layer ahead;
+  // a level's Planck term is loaded once, as the lower level of the layer
+  // above and the upper level of the layer below
   uint32_t idx_next = __ldg(p.idx + (size_t)(nlay - 1) * N + c);
+  const R* plev_b = p.planklev + (size_t)(B - 1) * (nlay + 1) * N + c;
+  R plev_up = __ldg(plev_b + (size_t)nlay * N);
   for (int lev = nlay; lev >= 1; --lev) {
     const size_t o = (size_t)(lev - 1) * N + c;
     const Idx ix = unpack_idx(idx_next);
@@ -455,8 +462,10 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
     if (tauaer) taut = taug + (R)__ldg(tauaer + c + N * ((size_t)(lev - 1) + (size_t)nlay * (B - 1)));
     const R plfrac = fracs;
     const R blay = __ldg(p.planklay + ((size_t)(B - 1) * nlay + (lev - 1)) * N + c);
-    const R dplankup = __ldg(p.planklev + ((size_t)(B - 1) * (nlay + 1) + lev) * N + c) - blay;
-    const R dplankdn = __ldg(p.planklev + ((size_t)(B - 1) * (nlay + 1) + lev - 1) * N + c) - blay;
+    const R plev_dn = __ldg(plev_b + (size_t)(lev - 1) * N);
+    const R dplankup = plev_up - blay;
+    const R dplankdn = plev_dn - blay;
+    plev_up = plev_dn;
     R odepth = secdiff * taut;
     if (odepth < (R)0.0) odepth = (R)0.0;
     R atr, bbd, bbu;
@@ -476,9 +485,16 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
       const R tblind = odepth / (bpade + odepth);
       int itr = (int)((R)10000.0 * tblind + (R)0.5);
       itr = itr < 0 ? 0 : (itr > kNTbl ? kNTbl : itr);  // in range for any odepth >= 0; guards NaN input
-      const R transc = tld(exptbl + itr);
+      R transc, tausfac;
+      if constexpr (SPLIT) {
+        const float2 et = __ldg(exptfn + itr);
+        transc = et.x;
+        tausfac = et.y;
+      } else {
+        transc = tld(exptbl + itr);
+        tausfac = tld(tfntbl + itr);
+      }
       atr = (R)1. - transc;
-      const R tausfac = tld(tfntbl + itr);
       bbd = plfrac * (blay + tausfac * dplankdn);
       bbu = plfrac * (blay + tausfac * dplankup);
     }
@@ -867,7 +883,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_LW_MINB :
                                                            const R* __restrict__ tab, const R* __restrict__ exptbl,
                                                            const R* __restrict__ tfntbl, double* bu, double* bd,
                                                            double* bdu, int ncol, int nlay, int idrv,
-                                                           int analytic) {
+                                                           int analytic, const float2* __restrict__ exptfn = nullptr) {
   __shared__ float sbuf[sizeof(R) == 4 ? kGSumFloats : 1];
   int blk = blockIdx.x, band = 0;
   for (; band < kLwBands; ++band) {
@@ -879,7 +895,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_LW_MINB :
   const bool an = FL < 0 ? analytic != 0 : (FL & 1) != 0;
   const int idv = FL < 0 ? idrv : ((FL & 2) ? 1 : 0);
 #define RRTMG_LW_CASE(b) \
-  case b - 1: lw_band<b, R, MAXL>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idv, an, blk, sbuf); break;
+  case b - 1: lw_band<b, R, MAXL>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idv, an, blk, sbuf, exptfn); break;
   switch (band) {
     RRTMG_LW_CASE(1) RRTMG_LW_CASE(2) RRTMG_LW_CASE(3) RRTMG_LW_CASE(4) RRTMG_LW_CASE(5) RRTMG_LW_CASE(6)
     RRTMG_LW_CASE(7) RRTMG_LW_CASE(8) RRTMG_LW_CASE(9) RRTMG_LW_CASE(10) RRTMG_LW_CASE(11) RRTMG_LW_CASE(12)

@@ -179,23 +179,23 @@ void launch_sw_finalize_split(const double* su, const double* sd, const double* 
 // The split solvers are instantiated per (analytic, idrv / aerosol) flag pair.
 template <int MAXL>
 static void lw_split_flags(int fl, int nb, cudaStream_t s, const LwPrepT<float>& p, const double* emis,
-                           const double* tauaer, const float* tab, const float* exptbl, const float* tfntbl, double* bu,
-                           double* bd, double* bdu, int ncol, int nlay, int idrv, int analytic) {
+                           const double* tauaer, const float* tab, const float2* exptfn, double* bu, double* bd,
+                           double* bdu, int ncol, int nlay, int idrv, int analytic) {
   auto k = fl == 0 ? lw_gpoint_kernel<float, MAXL, 0>
          : fl == 1 ? lw_gpoint_kernel<float, MAXL, 1>
          : fl == 2 ? lw_gpoint_kernel<float, MAXL, 2>
                    : lw_gpoint_kernel<float, MAXL, 3>;
-  k<<<nb, kBlock, 0, s>>>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv, analytic);
+  k<<<nb, kBlock, 0, s>>>(p, emis, tauaer, tab, nullptr, nullptr, bu, bd, bdu, ncol, nlay, idrv, analytic, exptfn);
 }
 
 void launch_lw_gpoint_split(const LwPrepT<float>& p, const double* emis, const double* tauaer, const float* tab,
-                            const float* exptbl, const float* tfntbl, double* bu, double* bd, double* bdu, int ncol,
-                            int nlay, int idrv, int nb, int analytic, cudaStream_t s) {
+                            const float2* exptfn, double* bu, double* bd, double* bdu, int ncol, int nlay, int idrv,
+                            int nb, int analytic, cudaStream_t s) {
   const int fl = (analytic ? 1 : 0) | (idrv == 1 ? 2 : 0);
   if (maxl_for(nlay) == 64)
-    lw_split_flags<64>(fl, nb, s, p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv, analytic);
+    lw_split_flags<64>(fl, nb, s, p, emis, tauaer, tab, exptfn, bu, bd, bdu, ncol, nlay, idrv, analytic);
   else
-    lw_split_flags<208>(fl, nb, s, p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idrv, analytic);
+    lw_split_flags<208>(fl, nb, s, p, emis, tauaer, tab, exptfn, bu, bd, bdu, ncol, nlay, idrv, analytic);
 }
 
 // Cloudy LW (icld = 1, 2, 3): instantiated per (analytic, idrv) flag pair;

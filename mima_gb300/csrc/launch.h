@@ -72,8 +72,9 @@ void launch_sw_finalize_split(const double* su, const double* sd, const double* 
                               const double* sdc = nullptr);
 
 // FP32-split translation unit.
+// exptfn: the FP32 transmittance and tau transition tables interleaved.
 void launch_lw_gpoint_split(const LwPrepT<float>& p, const double* emis, const double* tauaer, const float* tab,
-                            const float* exptbl, const float* tfntbl, double* bu, double* bd, double* bdu, int ncol,
+                            const float2* exptfn, double* bu, double* bd, double* bdu, int ncol,
                             int nlay, int idrv, int nb, int analytic, cudaStream_t s);
 void launch_sw_gpoint_split(const SwPrepT<float>& p, const SwIn& in, double adjflux, int iaer, const float* tab,
                             const double* tab64, const float* exptbl, double* su, double* sd, int ncol, int nlay,

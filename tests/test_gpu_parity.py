@@ -282,9 +282,12 @@ def test_invalid_input_and_unsupported_configurations(gpu):
     out = gpu.lw(atm, check=False)
     assert out["status"] == R.RRTMG_ERR_INPUT
     atm = A.small_atmosphere(8, 40, seed=1)
+    o = gpu.rrtmg_lw(atm.ncol, atm.nlay, 4, 0, atm.play, atm.plev, atm.tlay, atm.tlev, atm.tsfc, atm.h2o,
+                     atm.o3, atm.co2, check=False)
+    assert o["status"] == R.RRTMG_ERR_UNSUPPORTED  # icld outside 0..3
     o = gpu.rrtmg_lw(atm.ncol, atm.nlay, 2, 0, atm.play, atm.plev, atm.tlay, atm.tlev, atm.tsfc, atm.h2o,
                      atm.o3, atm.co2, check=False)
-    assert o["status"] == R.RRTMG_ERR_UNSUPPORTED
+    assert o["status"] == R.RRTMG_ERR_ARG  # clouds without cloud arrays
     o = gpu.rrtmg_sw(atm.ncol, atm.nlay, 0, 6, atm.play, atm.plev, atm.tlay, atm.tlev, atm.tsfc, atm.h2o,
                      atm.o3, atm.co2, None, None, None, atm.asdir, atm.asdif, atm.aldir, atm.aldif,
                      atm.coszen, 1.0, 0, 1360.0, check=False)

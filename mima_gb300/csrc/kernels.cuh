@@ -81,10 +81,11 @@ __device__ __forceinline__ bool bad(double x) { return !isfinite(x); }
 // sum: Knuth's TwoSum splits every addition into the rounded sum and its exact
 // rounding error, and with per-g weights `wt` (the SW incident fluxes, FP32)
 // an FMA recovers the exact error of each product; the errors accumulate in a
-// second float and the result is (double)s + (double)c, within about
-// NG^2 u^2 (u = 2^-24) of the exact sum -- the accuracy of the FP64 sum it
-// replaces, at two FP64 operations per sum instead of 2 NG (GB300's FP64 rate
-// is a small fraction of its FP32 rate).  Explicitly rounded intrinsics keep
+// second float; the pair (s, c) is stored as is (a float2 band partial), its
+// value s + c within about NG^2 u^2 (u = 2^-24) of the exact sum -- the
+// accuracy of the FP64 sum it replaces, with no FP64 operation in the solver
+// (GB300's FP64 rate is a small fraction of its FP32 rate; the finalize
+// kernels add the pairs of all bands by the same compensated summation).  Explicitly rounded intrinsics keep
 // the compiler from contracting the error terms.  Rows are 33 floats wide so
 // that the staging stores and the per-lane row reads are free of bank
 // conflicts.  A warp stages at most kStageRows rows: W levels of one stream
@@ -132,7 +133,7 @@ struct GSum {
           c = __fadd_rn(c, __fadd_rn(__fsub_rn(s, __fsub_rn(t, bv)), __fsub_rn(x, bv)));
           s = t;
         }
-        st(b, first + dir * sl, cs, (double)s + (double)c);
+        st(b, first + dir * sl, cs, s, c);
       }
     }
     __syncwarp();
@@ -156,6 +157,11 @@ __host__ __device__ constexpr int split_lanes(int ng, bool split) {
 
 // Shared-memory floats of the staging buffers of one 128-thread block.
 constexpr int kGSumFloats = (kBlock / 32) * kStageRows * kRow;
+
+// The split path's band partials: a double slot of the band-partial arrays
+// holds one compensated pair (s, c) of the g-point sum (8 bytes either way).
+__device__ __forceinline__ float2* as_pair(double* p) { return reinterpret_cast<float2*>(p); }
+__device__ __forceinline__ const float2* as_pair(const double* p) { return reinterpret_cast<const float2*>(p); }
 
 #ifdef RRTMG_DEFINE_COLUMN_KERNELS
 // ---------------------------------------------------------------------------
@@ -430,17 +436,17 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
   const int wcol0 = blk * CPB + wib * CPW;
   GSum<W, NG, 2, false> gs{sbuf + (SPLIT ? wib * kStageRows * kRow : 0), nullptr, lane, 0, nlay - 1, -1,
                            1};
-  auto store_dn = [&](int b, int lev, int cs, double v) {
+  auto store_dn = [&](int b, int lev, int cs, float s, float cmp) {
     const int cc = wcol0 + cs;
-    if (cc < ncol) bd[((size_t)(B - 1) * (nlay + 1) + lev) * N + cc] = v;
+    if (cc < ncol) as_pair(bd)[((size_t)(B - 1) * (nlay + 1) + lev) * N + cc] = make_float2(s, cmp);
   };
-  auto store_up = [&](int b, int lev, int cs, double v) {
+  auto store_up = [&](int b, int lev, int cs, float s, float cmp) {
     const int cc = wcol0 + cs;
     if (cc >= ncol) return;
     if (b == 0)
-      bu[((size_t)(B - 1) * (nlay + 1) + lev) * N + cc] = v;
+      as_pair(bu)[((size_t)(B - 1) * (nlay + 1) + lev) * N + cc] = make_float2(s, cmp);
     else if (IDRV)
-      bdu[((size_t)(B - 1) * (nlay + 1) + lev) * N + cc] = v;
+      as_pair(bdu)[((size_t)(B - 1) * (nlay + 1) + lev) * N + cc] = make_float2(s, cmp);
   };
   // No downward radiance enters at the top (drad(nlayers) stays 0,
   // rrtmg_lw_rtrnmr.f90:290-300).
@@ -623,13 +629,13 @@ __device__ __forceinline__ void lw_band_cld(const LwPrepT<R>& p, const R* __rest
   double* dst_up[4] = {bu + bo, buc + bo, IDRV ? bdu + bo : nullptr, IDRV ? bduc + bo : nullptr};
   const int wcol0 = blk * CPB + wib * CPW;
   GSum<W, NG, 4, false> gs{sbuf + (SPLIT ? wib * kStageRows * kRow : 0), nullptr, lane, 0, nlay - 1, -1, 2};
-  auto store_dn = [&](int b, int lev, int cs, double v) {
+  auto store_dn = [&](int b, int lev, int cs, float s, float cmp) {
     const int cc = wcol0 + cs;
-    if (cc < ncol) dst_dn[b][(size_t)lev * N + cc] = v;
+    if (cc < ncol) as_pair(dst_dn[b])[(size_t)lev * N + cc] = make_float2(s, cmp);
   };
-  auto store_up = [&](int b, int lev, int cs, double v) {
+  auto store_up = [&](int b, int lev, int cs, float s, float cmp) {
     const int cc = wcol0 + cs;
-    if (cc < ncol && dst_up[b]) dst_up[b][(size_t)lev * N + cc] = v;
+    if (cc < ncol && dst_up[b]) as_pair(dst_up[b])[(size_t)lev * N + cc] = make_float2(s, cmp);
   };
   // FP64 path: the band's level sums by warp shuffles
   auto sum_dn = [&](int b, int lev, R v) {
@@ -1676,9 +1682,9 @@ __device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, dou
   const int wcol0 = blk * CPB + wib * CPW;
   GSum<W, NG, 2, true> gs{sbuf + (SPLIT ? wib * kStageRows * kRow : 0), swt + (SPLIT ? wib * 32 : 0), lane, 0, 0, 1, 2};
   if constexpr (SPLIT) swt[wib * 32 + lane] = active ? (float)zincflx : 0.f;
-  auto store = [&](int b, int lev, int cs, double v) {
+  auto store = [&](int b, int lev, int cs, float s, float cmp) {
     const int cc = wcol0 + cs;
-    if (cc < ncol) (b == 0 ? su : sd)[((size_t)(B - 16) * (nlay + 1) + lev) * N + cc] = v;
+    if (cc < ncol) as_pair(b == 0 ? su : sd)[((size_t)(B - 16) * (nlay + 1) + lev) * N + cc] = make_float2(s, cmp);
   };
   R prup = albdir, prupd = albdif;  // level klev+1 (surface)
   for (int jk = klev + 1; jk >= 1; --jk) {

@@ -8,8 +8,9 @@
 namespace rrtmg {
 
 // LW band weight of the broadband sums: wtdiff * delwave(band) * fluxfac
-// (rrtmg_lw_rtrnmr.f90:720-746), folded into one factor.
-__constant__ double c_lw_bandw[kLwBands];
+// (rrtmg_lw_rtrnmr.f90:720-746), folded into one factor and split into two
+// floats (w = hi + lo to 2^-48) for the compensated FP32 band sums.
+__constant__ float2 c_lw_bandw[kLwBands];
 
 cudaError_t upload_constants_split(const LwConst& lw, const SwConst& sw) {
   cudaError_t e = cudaMemcpyToSymbol(c_lw, &lw, sizeof(LwConst));
@@ -17,8 +18,12 @@ cudaError_t upload_constants_split(const LwConst& lw, const SwConst& sw) {
   const LwConstF f = make_lwconstf(lw);
   e = cudaMemcpyToSymbol(c_lwf, &f, sizeof(LwConstF));
   if (e != cudaSuccess) return e;
-  double bw[kLwBands];
-  for (int b = 0; b < kLwBands; ++b) bw[b] = 0.5 * lw.band[b].delwave * lw.fluxfac;
+  float2 bw[kLwBands];
+  for (int b = 0; b < kLwBands; ++b) {
+    const double w = 0.5 * lw.band[b].delwave * lw.fluxfac;
+    bw[b].x = (float)w;
+    bw[b].y = (float)(w - (double)bw[b].x);
+  }
   e = cudaMemcpyToSymbol(c_lw_bandw, bw, sizeof(bw));
   if (e != cudaSuccess) return e;
   return cudaMemcpyToSymbol(c_sw, &sw, sizeof(SwConst));
@@ -27,13 +32,40 @@ cudaError_t upload_constants_split(const LwConst& lw, const SwConst& sw) {
 // ---------------------------------------------------------------------------
 // Finalize kernels of the split path.  The same fluxes and heating rates as
 // the FP64 finalize kernels (rrtmg_lw_rtrnmr.f90:720-776; rrtmg_sw_rad
-// .nomcica.f90:712-726 with MiMA's zero top layer), from the FP64 band
-// partials, in FP64, with fewer FP64 operations: a thread walks kLevChunk
-// consecutive levels of one column, so every level's band sums are formed
-// once and the level below is carried for the heating rate, and the LW band
-// weights multiply-add into the sums.
+// .nomcica.f90:712-726 with MiMA's zero top layer), from the band partials
+// (compensated FP32 pairs, s + c): the bands are summed by compensated FP32
+// arithmetic (Knuth's TwoSum per addition, an FMA recovering each product's
+// rounding error, the error terms gathered in a second float), within about
+// 2^-44 of the exact sum of the partials, and only the broadband flux (the
+// pair's value) and the heating-rate difference are formed in FP64.  A thread
+// walks kLevChunk consecutive levels of one column, so every level's band sums
+// are formed once and the level below is carried for the heating rate.
 // ---------------------------------------------------------------------------
 constexpr int kLevChunk = 8;
+
+// Compensated FP32 sum; explicitly rounded operations, so that contraction
+// cannot merge the error terms.
+struct CSum {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    const float t = __fadd_rn(s, x), bv = __fsub_rn(t, s);
+    c = __fadd_rn(c, __fadd_rn(__fsub_rn(s, __fsub_rn(t, bv)), __fsub_rn(x, bv)));
+    s = t;
+  }
+  // a band partial (s + c)
+  __device__ __forceinline__ void add(float2 p) {
+    add(p.x);
+    c = __fadd_rn(c, p.y);
+  }
+  // a band partial times a weight (w.x + w.y)
+  __device__ __forceinline__ void add(float2 p, float2 w) {
+    const float pr = __fmul_rn(p.x, w.x);
+    c = __fadd_rn(c, __fmaf_rn(p.x, w.x, -pr));
+    c = __fadd_rn(c, __fmaf_rn(p.x, w.y, __fmul_rn(p.y, w.x)));
+    add(pr);
+  }
+  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
 
 // buc, bdc, bduc: the clear-sky band partials of a cloudy call, else null.
 __global__ void __launch_bounds__(128) lw_finalize_split_kernel(const double* __restrict__ bu,
@@ -51,21 +83,22 @@ __global__ void __launch_bounds__(128) lw_finalize_split_kernel(const double* __
   const int lev0 = blockIdx.y * kLevChunk, lev1 = min(nlay, lev0 + kLevChunk - 1);
   const size_t N = (size_t)ncol, bs = (size_t)(nlay + 1) * N;
   auto sums = [&](const double* a, const double* b, int lv, double& x, double& y) {
-    x = 0.0;
-    y = 0.0;
+    CSum sx, sy;
     const size_t o = (size_t)lv * N + col;
 #pragma unroll
     for (int k = 0; k < kLwBands; ++k) {
-      x = fma(__ldg(a + k * bs + o), c_lw_bandw[k], x);
-      y = fma(__ldg(b + k * bs + o), c_lw_bandw[k], y);
+      sx.add(__ldg(as_pair(a) + k * bs + o), c_lw_bandw[k]);
+      sy.add(__ldg(as_pair(b) + k * bs + o), c_lw_bandw[k]);
     }
+    x = sx.value();
+    y = sy.value();
   };
   auto sum1 = [&](const double* a, int lv) {
-    double x = 0.0;
+    CSum sx;
     const size_t o = (size_t)lv * N + col;
 #pragma unroll
-    for (int k = 0; k < kLwBands; ++k) x = fma(__ldg(a + k * bs + o), c_lw_bandw[k], x);
-    return x;
+    for (int k = 0; k < kLwBands; ++k) sx.add(__ldg(as_pair(a) + k * bs + o), c_lw_bandw[k]);
+    return sx.value();
   };
   const bool clear_own = buc != nullptr;
   double tu0 = 0.0, td0 = 0.0, tuc0 = 0.0, tdc0 = 0.0;
@@ -119,12 +152,15 @@ __global__ void __launch_bounds__(128) sw_finalize_split_kernel(const double* __
     fu = 0.0;
     fd = 0.0;
     if (!lit) return;
+    CSum su_, sd_;
     const size_t o = (size_t)lv * N + col;
 #pragma unroll
     for (int k = 0; k < kSwBands; ++k) {
-      fu = fu + __ldg(u + k * bs + o);
-      fd = fd + __ldg(d + k * bs + o);
+      su_.add(__ldg(as_pair(u) + k * bs + o));
+      sd_.add(__ldg(as_pair(d) + k * bs + o));
     }
+    fu = su_.value();
+    fd = sd_.value();
   };
   const bool clear_own = suc != nullptr;
   double fu0 = 0.0, fd0 = 0.0, fuc0 = 0.0, fdc0 = 0.0;

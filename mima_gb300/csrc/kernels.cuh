@@ -163,6 +163,18 @@ constexpr int kGSumFloats = (kBlock / 32) * kStageRows * kRow;
 __device__ __forceinline__ float2* as_pair(double* p) { return reinterpret_cast<float2*>(p); }
 __device__ __forceinline__ const float2* as_pair(const double* p) { return reinterpret_cast<const float2*>(p); }
 
+// Per-thread layer state that one sweep writes together and the other reads
+// together, kept side by side so that each layer's store and load is one wide
+// local-memory access instead of two or four.
+template <class R>
+struct __align__(2 * sizeof(R)) Pair2 {
+  R a, b;
+};
+template <class R>
+struct __align__(4 * sizeof(R)) Quad {
+  R a, b, c, d;
+};
+
 #ifdef RRTMG_DEFINE_COLUMN_KERNELS
 // ---------------------------------------------------------------------------
 // LW prep: inatm (rrtmg_lw_rad.nomcica.f90:572-901) + setcoef
@@ -426,7 +438,7 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
   const R bpade = (R)c_lw.bpade;
   const R rec_6 = (R)0.166667;
   const size_t fstride = (size_t)nlay * N;
-  R atrans[MAXL], bbugas[MAXL];
+  Pair2<R> ab[MAXL];  // {atrans, bbugas} of each layer
   R radld = (R)0., fracs1 = (R)0.;
   double* bdp = bd + (size_t)(B - 1) * (nlay + 1) * N + col;
   double* bup = bu + (size_t)(B - 1) * (nlay + 1) * N + col;
@@ -504,8 +516,7 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
       bbd = plfrac * (blay + tausfac * dplankdn);
       bbu = plfrac * (blay + tausfac * dplankup);
     }
-    atrans[lev - 1] = atr;
-    bbugas[lev - 1] = bbu;
+    ab[lev - 1] = Pair2<R>{atr, bbu};
     radld = radld + (bbd - radld) * atr;
     if constexpr (SPLIT) {
       gs.put(0, radld);
@@ -541,8 +552,9 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
     }
   }
   for (int lev = 1; lev <= nlay; ++lev) {
-    radlu = radlu + (bbugas[lev - 1] - radlu) * atrans[lev - 1];
-    if (IDRV) dlu = dlu * ((R)1.0 - atrans[lev - 1]);
+    const Pair2<R> l = ab[lev - 1];
+    radlu = radlu + (l.b - radlu) * l.a;
+    if (IDRV) dlu = dlu * ((R)1.0 - l.a);
     if constexpr (SPLIT) {
       gs.put(0, radlu);
       gs.put(1, dlu);
@@ -605,7 +617,8 @@ __device__ __forceinline__ void lw_band_cld(const LwPrepT<R>& p, const R* __rest
   const R bpade = (R)c_lw.bpade;
   const R rec_6 = (R)0.166667;
   const size_t fstride = (size_t)nlay * N;
-  R atrans[MAXL], bbugas[MAXL], atot[MAXL], bbutot[MAXL], efcl[MAXL];
+  Quad<R> lq[MAXL];  // {atrans, bbugas, atot, bbutot} of each layer
+  R efcl[MAXL];
   // transmittance, tau transition function and the optical depth of a table
   // entry (exp_tbl, tfn_tbl, tau_tbl), or with the analytic functions, of od
   auto tbl = [&](R od, R& trans, R& tfn, R& odq) {
@@ -756,10 +769,7 @@ __device__ __forceinline__ void lw_band_cld(const LwPrepT<R>& p, const R* __rest
       radld = radld + (bbd - radld) * atr;
     }
     above_cloudy = cf > (R)0.;
-    atrans[lev - 1] = atr;
-    bbugas[lev - 1] = bbu;
-    atot[lev - 1] = at;
-    bbutot[lev - 1] = bbut;
+    lq[lev - 1] = Quad<R>{atr, bbu, at, bbut};
     efcl[lev - 1] = ef;
     // clear-sky stream (:441-448)
     if (iclddn)
@@ -812,12 +822,13 @@ __device__ __forceinline__ void lw_band_cld(const LwPrepT<R>& p, const R* __rest
   bool below_cloudy = false;  // maximum/random overlap: istcld = 0
   rad = (R)0.;
   for (int lev = 1; lev <= nlay; ++lev) {  // rtrn :478-520, rtrnmr :649-705
-    const R atr = atrans[lev - 1];
+    const Quad<R> l = lq[lev - 1];
+    const R atr = l.a, bbugas = l.b, bbutot = l.d;
     const size_t o = (size_t)(lev - 1) * N + c;
     const R cf = __ldg(cld + o);
     if (cf > (R)0.) {
-      const R gassrc = bbugas[lev - 1] * atr;
-      const R at = atot[lev - 1];
+      const R gassrc = bbugas * atr;
+      const R at = l.c;
       if (ovl) {
         if (!below_cloudy) {
           cldrad = cf * radlu;
@@ -825,7 +836,7 @@ __device__ __forceinline__ void lw_band_cld(const LwPrepT<R>& p, const R* __rest
           rad = (R)0.;
         }
         const R ttot = (R)1. - at;
-        const R cldsrc = bbutot[lev - 1] * at;
+        const R cldsrc = bbutot * at;
         cldrad = cldrad * ttot + cf * cldsrc;
         clrrad = clrrad * ((R)1.0 - atr) + ((R)1. - cf) * gassrc;
         radlu = cldrad + clrrad;
@@ -838,16 +849,16 @@ __device__ __forceinline__ void lw_band_cld(const LwPrepT<R>& p, const R* __rest
         cldrad = cldrad + rad;
         clrrad = clrrad - rad;
       } else {
-        radlu = radlu - radlu * (atr + efcl[lev - 1] * ((R)1. - atr)) + gassrc + cf * (bbutot[lev - 1] * at - gassrc);
+        radlu = radlu - radlu * (atr + efcl[lev - 1] * ((R)1. - atr)) + gassrc + cf * (bbutot * at - gassrc);
       }
       if (IDRV) dlu = dlu * cf * ((R)1.0 - at) + dlu * ((R)1.0 - cf) * ((R)1.0 - atr);
     } else {
-      radlu = radlu + (bbugas[lev - 1] - radlu) * atr;
+      radlu = radlu + (bbugas - radlu) * atr;
       if (IDRV) dlu = dlu * ((R)1.0 - atr);
     }
     below_cloudy = cf > (R)0.;
     if (iclddn) {
-      radclru = radclru + (bbugas[lev - 1] - radclru) * atr;
+      radclru = radclru + (bbugas - radclru) * atr;
       if (IDRV) dluc = dluc * ((R)1.0 - atr);
     } else {
       radclru = radlu;
@@ -1581,10 +1592,12 @@ __device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, dou
   const R albdir = (R)__ldg(((ibm >= 10 && ibm <= 13) ? in.asdir : in.aldir) + c);
   const R albdif = (R)__ldg(((ibm >= 10 && ibm <= 13) ? in.asdif : in.aldif) + c);
 
-  // Layer arrays, top-down index jk = 1..klev (+ surface klev+1).
-  R pref[MAXL + 1], prefd[MAXL + 1], ptra[MAXL + 1], ptrad[MAXL + 1], pdbt[MAXL + 1];
-  R ptdbt[MAXL + 2], ztdn[MAXL + 2], prdnd[MAXL + 2];
-  ptdbt[1 - 1] = (R)1.0;
+  // Layer and level state, top-down (jk = 1..klev, + surface klev+1):
+  // lay[k] = {pref, prefd, ptra, ptrad} of layer k (0-based);
+  // lvl[j] = {ptdbt, ztdn, prdnd} of level j and pdbt of layer j.  The level
+  // above the current layer is carried in registers (tdbt1, tdn1, rdnd1).
+  Quad<R> lay[MAXL + 1], lvl[MAXL + 2];
+  R tdbt1 = (R)1.0, tdn1 = (R)1.0, rdnd1 = (R)0.0;
   // the packed table indices of the next layer are loaded one layer ahead
   uint32_t idx_next = __ldg(p.idx + (size_t)(klev - 1) * N + c);
   for (int jk = 1; jk <= klev; ++jk) {
@@ -1654,24 +1667,23 @@ __device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, dou
       trd = zclear * trd + zcloud * trdo;
       zdbtmc = zclear * zdbtmc + zcloud * zdbtmo;
     }
-    pref[jk - 1] = rf;
-    prefd[jk - 1] = rfd;
-    ptra[jk - 1] = tr;
-    ptrad[jk - 1] = trd;
-    pdbt[jk - 1] = zdbtmc;
-    ptdbt[jk] = zdbtmc * ptdbt[jk - 1];
-    // Downward adding sweep of vrtqdr_sw (:127-139), fused with the layer loop.
+    lay[jk - 1] = Quad<R>{rf, rfd, tr, trd};
+    lvl[jk - 1] = Quad<R>{tdbt1, tdn1, rdnd1, zdbtmc};
+    // Downward adding sweep of vrtqdr_sw (:127-139), fused with the layer loop
+    // (level 0: ptdbt = ztdn = 1, prdnd = 0).
+    const R tdbt = zdbtmc * tdbt1;
     if (jk == 1) {
-      ztdn[0] = (R)1.;
-      prdnd[0] = (R)0.;
-      ztdn[1] = tr;
-      prdnd[1] = rfd;
+      tdn1 = tr;
+      rdnd1 = rfd;
     } else {
-      const R zreflect = (R)1. / ((R)1. - rfd * prdnd[jk - 1]);
-      ztdn[jk] = ptdbt[jk - 1] * tr + (trd * ((ztdn[jk - 1] - ptdbt[jk - 1]) + ptdbt[jk - 1] * rf * prdnd[jk - 1])) * zreflect;
-      prdnd[jk] = rfd + trd * trd * prdnd[jk - 1] * zreflect;
+      const R zreflect = (R)1. / ((R)1. - rfd * rdnd1);
+      const R tdn = tdbt1 * tr + (trd * ((tdn1 - tdbt1) + tdbt1 * rf * rdnd1)) * zreflect;
+      rdnd1 = rfd + trd * trd * rdnd1 * zreflect;
+      tdn1 = tdn;
     }
+    tdbt1 = tdbt;
   }
+  lvl[klev] = Quad<R>{tdbt1, tdn1, rdnd1, (R)0.};
   // Upward sweep (vrtqdr_sw :104-124) from the surface, with the level fluxes
   // (:141-149) as soon as each level's upward reflectances are known.
   double* sup = su + (size_t)(B - 16) * (nlay + 1) * N + col;
@@ -1688,23 +1700,25 @@ __device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, dou
   };
   R prup = albdir, prupd = albdif;  // level klev+1 (surface)
   for (int jk = klev + 1; jk >= 1; --jk) {
+    const Quad<R> lv = lvl[jk - 1];  // level jk-1, and the direct beam of layer jk-1
     if (jk <= klev) {
-      const int k = jk - 1;
+      const Quad<R> ly = lay[jk - 1];
+      const R pref = ly.a, prefd = ly.b, ptra = ly.c, ptrad = ly.d, pdbt = lv.d;
       if (jk == klev) {
-        const R zreflect = (R)1. / ((R)1. - albdif * prefd[k]);
-        const R nup = pref[k] + (ptrad[k] * ((ptra[k] - pdbt[k]) * albdif + pdbt[k] * albdir)) * zreflect;
-        const R nupd = prefd[k] + ptrad[k] * ptrad[k] * albdif * zreflect;
+        const R zreflect = (R)1. / ((R)1. - albdif * prefd);
+        const R nup = pref + (ptrad * ((ptra - pdbt) * albdif + pdbt * albdir)) * zreflect;
+        const R nupd = prefd + ptrad * ptrad * albdif * zreflect;
         prup = nup;
         prupd = nupd;
       } else {
-        const R zreflect = (R)1. / ((R)1. - prupd * prefd[k]);
-        const R nup = pref[k] + (ptrad[k] * ((ptra[k] - pdbt[k]) * prupd + pdbt[k] * prup)) * zreflect;
-        const R nupd = prefd[k] + ptrad[k] * ptrad[k] * prupd * zreflect;
+        const R zreflect = (R)1. / ((R)1. - prupd * prefd);
+        const R nup = pref + (ptrad * ((ptra - pdbt) * prupd + pdbt * prup)) * zreflect;
+        const R nupd = prefd + ptrad * ptrad * prupd * zreflect;
         prup = nup;
         prupd = nupd;
       }
     }
-    const R tdbt = ptdbt[jk - 1], tdn = ztdn[jk - 1], rdnd = prdnd[jk - 1];
+    const R tdbt = lv.a, tdn = lv.b, rdnd = lv.c;
     const R zreflect = (R)1. / ((R)1. - rdnd * prupd);
     const R pfu = (tdbt * prup + (tdn - tdbt) * prupd) * zreflect;
     const R pfd = tdbt + (tdn - tdbt + tdbt * prup * rdnd) * zreflect;

@@ -883,12 +883,14 @@ __host__ __device__ inline int lw_blocks_for_band(int lanes, int ncol) {
 // 32768 columns x 40 layers, 12/12 (40 registers) first ran the LW+SW split
 // step in 11.1 ms against 19.0 ms at 1/1 (105 registers).  Re-measured with
 // the flag-specialised solvers: LW 3.11 ms at 12, 3.27 at 10; SW 3.65 ms at
-// 12, 3.58 at 14 (32 registers).  FP64 solvers: 1.
+// 12, 3.58 at 14 (32 registers); with the SW layer state in packed records:
+// SW 2.46 ms at 12 (40 registers), 2.51 at 14 and 16, 2.55 at 10.  FP64
+// solvers: 1.
 #ifndef RRTMG_SPLIT_LW_MINB
 #define RRTMG_SPLIT_LW_MINB 12
 #endif
 #ifndef RRTMG_SPLIT_SW_MINB
-#define RRTMG_SPLIT_SW_MINB 14
+#define RRTMG_SPLIT_SW_MINB 12
 #endif
 
 // FL < 0: analytic and idrv as passed; FL >= 0: compile-time flags (bit 0

@@ -884,10 +884,11 @@ __host__ __device__ inline int lw_blocks_for_band(int lanes, int ncol) {
 // step in 11.1 ms against 19.0 ms at 1/1 (105 registers).  Re-measured with
 // the flag-specialised solvers: LW 3.11 ms at 12, 3.27 at 10; SW 3.65 ms at
 // 12, 3.58 at 14 (32 registers); with the SW layer state in packed records:
-// SW 2.46 ms at 12 (40 registers), 2.51 at 14 and 16, 2.55 at 10.  FP64
-// solvers: 1.
+// SW 2.46 ms at 12 (40 registers), 2.51 at 14 and 16, 2.55 at 10; with the LW
+// layer state packed and the exp / tfn gather merged: LW 3.17 ms at 12 and 11,
+// 3.29 at 10, 2.99-3.04 at 13, 14 and 16.  FP64 solvers: 1.
 #ifndef RRTMG_SPLIT_LW_MINB
-#define RRTMG_SPLIT_LW_MINB 12
+#define RRTMG_SPLIT_LW_MINB 13
 #endif
 #ifndef RRTMG_SPLIT_SW_MINB
 #define RRTMG_SPLIT_SW_MINB 12

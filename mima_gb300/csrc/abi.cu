@@ -160,15 +160,15 @@ LwWork carve_lw(void* base, int ncol, int nlay, size_t* bytes, bool cloudy = fal
   w.dplankbnd = c.take<double>(16 * N);
   w.secdiff = c.take<double>(16 * N);
   w.laytrop = c.take<int>(N);
-  w.bu = c.take<double>(16 * (L + 1) * N);
-  w.bd = c.take<double>(16 * (L + 1) * N);
-  w.bdu = c.take<double>(16 * (L + 1) * N);
+  w.bu = c.take<double>(kLwSlots * (L + 1) * N);
+  w.bd = c.take<double>(kLwSlots * (L + 1) * N);
+  w.bdu = c.take<double>(kLwSlots * (L + 1) * N);
   w.colsum = c.take<double>(2 * L * N);
   if (cloudy) {
     w.cld = c.take<double>(2 * L * N);
-    w.buc = c.take<double>(16 * (L + 1) * N);
-    w.bdc = c.take<double>(16 * (L + 1) * N);
-    w.bduc = c.take<double>(16 * (L + 1) * N);
+    w.buc = c.take<double>(kLwSlots * (L + 1) * N);
+    w.bdc = c.take<double>(kLwSlots * (L + 1) * N);
+    w.bduc = c.take<double>(kLwSlots * (L + 1) * N);
     if (maxrand) w.ovl = c.take<double>(12 * L * N);
   }
   if (bytes) *bytes = c.off;
@@ -183,12 +183,12 @@ SwWork carve_sw(void* base, int ncol, int nlay, size_t* bytes, bool cloudy = fal
   w.f = c.take<double>((size_t)SF_N * L * N);
   w.laytrop = c.take<int>(N);
   w.laysolfr = c.take<int>(14 * N);
-  w.su = c.take<double>(14 * (L + 1) * N);
-  w.sd = c.take<double>(14 * (L + 1) * N);
+  w.su = c.take<double>(kSwSlots * (L + 1) * N);
+  w.sd = c.take<double>(kSwSlots * (L + 1) * N);
   if (cloudy) {
     w.cld = c.take<double>(2 * L * N);
-    w.suc = c.take<double>(14 * (L + 1) * N);
-    w.sdc = c.take<double>(14 * (L + 1) * N);
+    w.suc = c.take<double>(kSwSlots * (L + 1) * N);
+    w.sdc = c.take<double>(kSwSlots * (L + 1) * N);
   }
   if (bytes) *bytes = c.off;
   return w;
@@ -243,7 +243,7 @@ int lw_enqueue(rrtmg_gpu_state* h, cudaStream_t s, void* base, int ncol, int nla
   const bool cloudy = in.cldfr != nullptr, maxrand = cloudy && in.icld >= 2;
   LwWork w = carve_lw(base, ncol, nlay, nullptr, cloudy, maxrand);
   mark(h, 0, 0, s);
-  const int nb = lw_gpoint_blocks(h->host.lw, ncol, h->precision == RRTMG_PREC_SPLIT);
+  const int nb = h->precision == RRTMG_PREC_SPLIT ? lw_slot_blocks(ncol) : lw_gpoint_blocks(h->host.lw, ncol);
   if (h->precision == RRTMG_PREC_SPLIT) {
     const LwWorkT<float> w32 = work_as<float>(w);
     launch_lw_prep_split(in, w32, h->totplnk32, h->totplnkderiv32, ncol, nlay, idrv, h->flags, s);
@@ -346,7 +346,7 @@ int sw_enqueue(rrtmg_gpu_state* h, cudaStream_t s, void* base, int ncol, int nla
   const bool cloudy = in.cldfr != nullptr;
   SwWork w = carve_sw(base, ncol, nlay, nullptr, cloudy);
   const double adjflux = adjflux_of(h, adjes, dyofyr, scon);
-  const int nb = sw_gpoint_blocks(h->host.sw, ncol, h->precision == RRTMG_PREC_SPLIT);
+  const int nb = h->precision == RRTMG_PREC_SPLIT ? sw_slot_blocks(ncol) : sw_gpoint_blocks(h->host.sw, ncol);
   double* cu = cloudy ? w.suc : w.su;
   double* cd = cloudy ? w.sdc : w.sd;
   mark(h, 1, 0, s);

@@ -155,6 +155,24 @@ __host__ __device__ constexpr int split_lanes(int ng, bool split) {
   return (split && 32 / ng > 32 / pow2ceil(ng)) ? ng : pow2ceil(ng);
 }
 
+// Sub-bands of the split path ("slots"): the SW bands of 12 g-points, whose
+// warps would idle 4 of every 16 lanes, run as groups of 8 + 4 g-points, each
+// group with its own lanes per column and its own band partial; every other
+// band is one slot.  The finalize kernels sum the slots.  Measured at T85 x 40
+// (GB300): SW solver 2.46 -> 2.28 ms; the same split of the LW bands of 12 and
+// 14 g-points (8 + 4, 8 + 4 + 2) made the LW solver slower, 3.0 -> 3.43 ms, so
+// every LW band is one slot.
+struct SubBand {
+  int band, g0, ng;  // band (LW 1..16, SW 16..29), first g-point in the band, g-points
+};
+__host__ __device__ constexpr SubBand lw_slot(int s) { return SubBand{s + 1, 0, lw_ng(s + 1)}; }
+__host__ __device__ constexpr SubBand sw_slot(int s) {
+  constexpr SubBand t[kSwSlots] = {{16, 0, 6}, {17, 0, 8}, {17, 8, 4}, {18, 0, 8}, {19, 0, 8}, {20, 0, 10},
+                                   {21, 0, 10}, {22, 0, 2}, {23, 0, 10}, {24, 0, 8}, {25, 0, 6}, {26, 0, 6},
+                                   {27, 0, 8}, {28, 0, 6}, {29, 0, 8}, {29, 8, 4}};
+  return t[s];
+}
+
 // Shared-memory floats of the staging buffers of one 128-thread block.
 constexpr int kGSumFloats = (kBlock / 32) * kStageRows * kRow;
 
@@ -412,7 +430,10 @@ __global__ void __launch_bounds__(128) lw_prep_column_kernel(LwIn in, LwWorkT<F>
 // ---------------------------------------------------------------------------
 // Split path: the two table lookups of a layer are one gather of exptfn
 // (exp_tbl and tfn_tbl interleaved); FP64 path: exptbl and tfntbl.
-template <int B, class R, int MAXL>
+// G0, NS: the g-points [G0, G0 + NS) of the band that this call computes
+// (a sub-band of the split path, else the whole band); SLOT: its band-partial
+// index.
+template <int B, class R, int MAXL, int G0 = 0, int NS = lw_ng(B), int SLOT = B - 1>
 __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __restrict__ emis,
                                         const double* __restrict__ tauaer, const R* __restrict__ tab,
                                         const R* __restrict__ exptbl, const R* __restrict__ tfntbl,
@@ -421,7 +442,7 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
                                         const float2* __restrict__ exptfn) {
   const bool IDRV = idrv == 1;
   constexpr bool SPLIT = sizeof(R) == 4;
-  constexpr int NG = lw_ng(B);
+  constexpr int NG = NS;
   constexpr int W = split_lanes(NG, SPLIT);
   constexpr int CPW = 32 / W;
   constexpr int CPB = (kBlock / 32) * CPW;
@@ -431,7 +452,7 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
   const bool valid = lane < CPW * W && col < ncol;
   const bool active = valid && g < NG;
   const int c = valid ? col : (col < ncol ? col : ncol - 1);
-  const int gg = g < NG ? g : NG - 1;
+  const int gg = G0 + (g < NG ? g : NG - 1);
   const size_t N = (size_t)ncol;
   const int lt = p.laytrop[c];
   const R secdiff = p.secdiff[(B - 1) * N + c];
@@ -440,9 +461,9 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
   const size_t fstride = (size_t)nlay * N;
   Pair2<R> ab[MAXL];  // {atrans, bbugas} of each layer
   R radld = (R)0., fracs1 = (R)0.;
-  double* bdp = bd + (size_t)(B - 1) * (nlay + 1) * N + col;
-  double* bup = bu + (size_t)(B - 1) * (nlay + 1) * N + col;
-  double* bdup = IDRV ? bdu + (size_t)(B - 1) * (nlay + 1) * N + col : nullptr;
+  double* bdp = bd + (size_t)SLOT * (nlay + 1) * N + col;
+  double* bup = bu + (size_t)SLOT * (nlay + 1) * N + col;
+  double* bdup = IDRV ? bdu + (size_t)SLOT * (nlay + 1) * N + col : nullptr;
   // Split path: band sums through the warp's staging buffers; the summing
   // lane of column sub-index cs writes column wcol0 + cs.
   const int wcol0 = blk * CPB + wib * CPW;
@@ -450,15 +471,15 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
                            1};
   auto store_dn = [&](int b, int lev, int cs, float s, float cmp) {
     const int cc = wcol0 + cs;
-    if (cc < ncol) as_pair(bd)[((size_t)(B - 1) * (nlay + 1) + lev) * N + cc] = make_float2(s, cmp);
+    if (cc < ncol) as_pair(bd)[((size_t)SLOT * (nlay + 1) + lev) * N + cc] = make_float2(s, cmp);
   };
   auto store_up = [&](int b, int lev, int cs, float s, float cmp) {
     const int cc = wcol0 + cs;
     if (cc >= ncol) return;
     if (b == 0)
-      as_pair(bu)[((size_t)(B - 1) * (nlay + 1) + lev) * N + cc] = make_float2(s, cmp);
+      as_pair(bu)[((size_t)SLOT * (nlay + 1) + lev) * N + cc] = make_float2(s, cmp);
     else if (IDRV)
-      as_pair(bdu)[((size_t)(B - 1) * (nlay + 1) + lev) * N + cc] = make_float2(s, cmp);
+      as_pair(bdu)[((size_t)SLOT * (nlay + 1) + lev) * N + cc] = make_float2(s, cmp);
   };
   // No downward radiance enters at the top (drad(nlayers) stays 0,
   // rrtmg_lw_rtrnmr.f90:290-300).
@@ -588,7 +609,7 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
 // as a cloudy and a clear part; at each cloudy layer's far boundary the
 // overlap factors of lw_overlap_kernel move radiance between the two.
 // ---------------------------------------------------------------------------
-template <int B, class R, int MAXL>
+template <int B, class R, int MAXL, int G0 = 0, int NS = lw_ng(B), int SLOT = B - 1>
 __device__ __forceinline__ void lw_band_cld(const LwPrepT<R>& p, const R* __restrict__ cld,
                                             const double* __restrict__ taucld, const double* __restrict__ emis,
                                             const double* __restrict__ tauaer, const R* __restrict__ tab,
@@ -600,7 +621,7 @@ __device__ __forceinline__ void lw_band_cld(const LwPrepT<R>& p, const R* __rest
                                             int blk, float* sbuf, const R* __restrict__ ovl) {
   const bool IDRV = idrv == 1;
   constexpr bool SPLIT = sizeof(R) == 4;
-  constexpr int NG = lw_ng(B);
+  constexpr int NG = NS;
   constexpr int W = split_lanes(NG, SPLIT);
   constexpr int CPW = 32 / W;
   constexpr int CPB = (kBlock / 32) * CPW;
@@ -610,7 +631,7 @@ __device__ __forceinline__ void lw_band_cld(const LwPrepT<R>& p, const R* __rest
   const bool valid = lane < CPW * W && col < ncol;
   const bool active = valid && g < NG;
   const int c = valid ? col : (col < ncol ? col : ncol - 1);
-  const int gg = g < NG ? g : NG - 1;
+  const int gg = G0 + (g < NG ? g : NG - 1);
   const size_t N = (size_t)ncol;
   const int lt = p.laytrop[c];
   const R secdiff = p.secdiff[(B - 1) * N + c];
@@ -635,7 +656,7 @@ __device__ __forceinline__ void lw_band_cld(const LwPrepT<R>& p, const R* __rest
       odq = tld(tautbl + it);
     }
   };
-  const size_t bo = (size_t)(B - 1) * (nlay + 1) * N;
+  const size_t bo = (size_t)SLOT * (nlay + 1) * N;
   // streams: downward 0 total, 1 clear; upward 0 total, 1 clear, 2 / 3 their
   // surface-temperature derivatives (idrv = 1)
   double* dst_dn[2] = {bd + bo, bdc + bo};
@@ -877,6 +898,33 @@ __host__ __device__ inline int lw_blocks_for_band(int lanes, int ncol) {
   return (ncol + cpb - 1) / cpb;
 }
 
+// The g-point grids enumerate their units -- the slots on the split path, the
+// bands on the FP64 path -- then the column blocks of each: the unit of grid
+// block blk, blk becoming the block's index within the unit (a past-the-end
+// unit for blocks beyond the grid's work).
+template <bool SPLIT>
+__device__ __forceinline__ int lw_unit_of_block(int& blk, int ncol) {
+  int u = 0;
+  for (; u < (SPLIT ? kLwSlots : kLwBands); ++u) {
+    const int nb = lw_blocks_for_band(SPLIT ? split_lanes(lw_slot(u).ng, true) : split_lanes(c_lw.band[u].ng, false),
+                                      ncol);
+    if (blk < nb) break;
+    blk -= nb;
+  }
+  return u;
+}
+template <bool SPLIT>
+__device__ __forceinline__ int sw_unit_of_block(int& blk, int ncol) {
+  int u = 0;
+  for (; u < (SPLIT ? kSwSlots : kSwBands); ++u) {
+    const int nb = lw_blocks_for_band(SPLIT ? split_lanes(sw_slot(u).ng, true) : split_lanes(c_sw.band[u].ng, false),
+                                      ncol);
+    if (blk < nb) break;
+    blk -= nb;
+  }
+  return u;
+}
+
 // Minimum resident blocks per SM asked of the register allocator for the
 // FP32-split solvers.  They are latency-bound (table gathers, local-memory
 // column arrays), so occupancy pays even at the price of spills: on GB300 at
@@ -905,24 +953,37 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_LW_MINB :
                                                            double* bdu, int ncol, int nlay, int idrv,
                                                            int analytic, const float2* __restrict__ exptfn = nullptr) {
   __shared__ float sbuf[sizeof(R) == 4 ? kGSumFloats : 1];
-  int blk = blockIdx.x, band = 0;
-  for (; band < kLwBands; ++band) {
-    const int nb = lw_blocks_for_band(split_lanes(c_lw.band[band].ng, sizeof(R) == 4), ncol);
-    if (blk < nb) break;
-    blk -= nb;
-  }
+  constexpr bool SPLIT = sizeof(R) == 4;
+  int blk = blockIdx.x;
+  const int unit = lw_unit_of_block<SPLIT>(blk, ncol);  // slot (split) or band (FP64)
+  const int band = SPLIT ? (unit < kLwSlots ? lw_slot(unit).band - 1 : kLwBands) : unit;
   if (threadIdx.x == 0 && band < kLwBands) prefetch_band_l2(tab, c_lw.band[band]);
   const bool an = FL < 0 ? analytic != 0 : (FL & 1) != 0;
   const int idv = FL < 0 ? idrv : ((FL & 2) ? 1 : 0);
+  if constexpr (SPLIT) {
+#define RRTMG_LW_SLOT(s)                                                                                           \
+  case s:                                                                                                          \
+    lw_band<lw_slot(s).band, R, MAXL, lw_slot(s).g0, lw_slot(s).ng, s>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, \
+                                                                       bdu, ncol, nlay, idv, an, blk, sbuf, exptfn); \
+    break;
+    switch (unit) {
+      RRTMG_LW_SLOT(0) RRTMG_LW_SLOT(1) RRTMG_LW_SLOT(2) RRTMG_LW_SLOT(3) RRTMG_LW_SLOT(4) RRTMG_LW_SLOT(5)
+      RRTMG_LW_SLOT(6) RRTMG_LW_SLOT(7) RRTMG_LW_SLOT(8) RRTMG_LW_SLOT(9) RRTMG_LW_SLOT(10) RRTMG_LW_SLOT(11)
+      RRTMG_LW_SLOT(12) RRTMG_LW_SLOT(13) RRTMG_LW_SLOT(14) RRTMG_LW_SLOT(15)
+      default: break;
+    }
+#undef RRTMG_LW_SLOT
+  } else {
 #define RRTMG_LW_CASE(b) \
   case b - 1: lw_band<b, R, MAXL>(p, emis, tauaer, tab, exptbl, tfntbl, bu, bd, bdu, ncol, nlay, idv, an, blk, sbuf, exptfn); break;
-  switch (band) {
-    RRTMG_LW_CASE(1) RRTMG_LW_CASE(2) RRTMG_LW_CASE(3) RRTMG_LW_CASE(4) RRTMG_LW_CASE(5) RRTMG_LW_CASE(6)
-    RRTMG_LW_CASE(7) RRTMG_LW_CASE(8) RRTMG_LW_CASE(9) RRTMG_LW_CASE(10) RRTMG_LW_CASE(11) RRTMG_LW_CASE(12)
-    RRTMG_LW_CASE(13) RRTMG_LW_CASE(14) RRTMG_LW_CASE(15) RRTMG_LW_CASE(16)
-    default: break;
-  }
+    switch (unit) {
+      RRTMG_LW_CASE(1) RRTMG_LW_CASE(2) RRTMG_LW_CASE(3) RRTMG_LW_CASE(4) RRTMG_LW_CASE(5) RRTMG_LW_CASE(6)
+      RRTMG_LW_CASE(7) RRTMG_LW_CASE(8) RRTMG_LW_CASE(9) RRTMG_LW_CASE(10) RRTMG_LW_CASE(11) RRTMG_LW_CASE(12)
+      RRTMG_LW_CASE(13) RRTMG_LW_CASE(14) RRTMG_LW_CASE(15) RRTMG_LW_CASE(16)
+      default: break;
+    }
 #undef RRTMG_LW_CASE
+  }
 }
 
 // Cloudy LW g-point kernel (icld = 1, 2, 3): as lw_gpoint_kernel, with
@@ -937,27 +998,41 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_LW_MINB :
                          const R* __restrict__ tautbl, double* bu, double* bd, double* bdu, double* buc, double* bdc,
                          double* bduc, int ncol, int nlay, int idrv, int analytic, const R* __restrict__ ovl) {
   __shared__ float sbuf[sizeof(R) == 4 ? kGSumFloats : 1];
-  int blk = blockIdx.x, band = 0;
-  for (; band < kLwBands; ++band) {
-    const int nb = lw_blocks_for_band(split_lanes(c_lw.band[band].ng, sizeof(R) == 4), ncol);
-    if (blk < nb) break;
-    blk -= nb;
-  }
+  constexpr bool SPLIT = sizeof(R) == 4;
+  int blk = blockIdx.x;
+  const int unit = lw_unit_of_block<SPLIT>(blk, ncol);  // slot (split) or band (FP64)
+  const int band = SPLIT ? (unit < kLwSlots ? lw_slot(unit).band - 1 : kLwBands) : unit;
   if (threadIdx.x == 0 && band < kLwBands) prefetch_band_l2(tab, c_lw.band[band]);
   const bool an = FL < 0 ? analytic != 0 : (FL & 1) != 0;
   const int idv = FL < 0 ? idrv : ((FL & 2) ? 1 : 0);
+  if constexpr (SPLIT) {
+#define RRTMG_LW_SLOT(s)                                                                                          \
+  case s:                                                                                                         \
+    lw_band_cld<lw_slot(s).band, R, MAXL, lw_slot(s).g0, lw_slot(s).ng, s>(                                      \
+        p, cld, taucld, emis, tauaer, tab, exptbl, tfntbl, tautbl, bu, bd, bdu, buc, bdc, bduc, ncol, nlay, idv, an, \
+        blk, sbuf, ovl);                                                                                          \
+    break;
+    switch (unit) {
+      RRTMG_LW_SLOT(0) RRTMG_LW_SLOT(1) RRTMG_LW_SLOT(2) RRTMG_LW_SLOT(3) RRTMG_LW_SLOT(4) RRTMG_LW_SLOT(5)
+      RRTMG_LW_SLOT(6) RRTMG_LW_SLOT(7) RRTMG_LW_SLOT(8) RRTMG_LW_SLOT(9) RRTMG_LW_SLOT(10) RRTMG_LW_SLOT(11)
+      RRTMG_LW_SLOT(12) RRTMG_LW_SLOT(13) RRTMG_LW_SLOT(14) RRTMG_LW_SLOT(15)
+      default: break;
+    }
+#undef RRTMG_LW_SLOT
+  } else {
 #define RRTMG_LW_CASE(b)                                                                                            \
   case b - 1:                                                                                                      \
     lw_band_cld<b, R, MAXL>(p, cld, taucld, emis, tauaer, tab, exptbl, tfntbl, tautbl, bu, bd, bdu, buc, bdc, bduc, \
                             ncol, nlay, idv, an, blk, sbuf, ovl);                                                  \
     break;
-  switch (band) {
-    RRTMG_LW_CASE(1) RRTMG_LW_CASE(2) RRTMG_LW_CASE(3) RRTMG_LW_CASE(4) RRTMG_LW_CASE(5) RRTMG_LW_CASE(6)
-    RRTMG_LW_CASE(7) RRTMG_LW_CASE(8) RRTMG_LW_CASE(9) RRTMG_LW_CASE(10) RRTMG_LW_CASE(11) RRTMG_LW_CASE(12)
-    RRTMG_LW_CASE(13) RRTMG_LW_CASE(14) RRTMG_LW_CASE(15) RRTMG_LW_CASE(16)
-    default: break;
-  }
+    switch (unit) {
+      RRTMG_LW_CASE(1) RRTMG_LW_CASE(2) RRTMG_LW_CASE(3) RRTMG_LW_CASE(4) RRTMG_LW_CASE(5) RRTMG_LW_CASE(6)
+      RRTMG_LW_CASE(7) RRTMG_LW_CASE(8) RRTMG_LW_CASE(9) RRTMG_LW_CASE(10) RRTMG_LW_CASE(11) RRTMG_LW_CASE(12)
+      RRTMG_LW_CASE(13) RRTMG_LW_CASE(14) RRTMG_LW_CASE(15) RRTMG_LW_CASE(16)
+      default: break;
+    }
 #undef RRTMG_LW_CASE
+  }
 }
 
 #ifdef RRTMG_DEFINE_COLUMN_KERNELS
@@ -1554,14 +1629,14 @@ __device__ __forceinline__ void reftra_split(R zto1, R zw, R zg, R prmuz, R bpad
 // TOT: the total-sky pass of a cloudy call (icld = 1): every layer's clear
 // optics combined with its cloud optics by the cover (spcvrt_sw :459-525);
 // cld: [cover][cldprop mask] per layer.  Otherwise the clear-sky pass.
-template <int B, class R, int MAXL, bool TOT = false>
+template <int B, class R, int MAXL, bool TOT = false, int G0 = 0, int NS = sw_ng(B), int SLOT = B - 16>
 __device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, double adjflux, int iaer,
                                         const R* __restrict__ tab, const double* __restrict__ tab64,
                                         const R* __restrict__ exptbl, double* __restrict__ su,
                                         double* __restrict__ sd, int ncol, int nlay, bool analytic, int blk, float* sbuf,
                                         float* swt, const R* __restrict__ cld = nullptr) {
   constexpr bool SPLIT = sizeof(R) == 4;
-  constexpr int NG = sw_ng(B);
+  constexpr int NG = NS;
   constexpr int W = split_lanes(NG, SPLIT);
   constexpr int CPW = 32 / W;
   constexpr int CPB = (kBlock / 32) * CPW;
@@ -1571,7 +1646,7 @@ __device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, dou
   const int col = blk * CPB + lane_col;
   const bool valid = lane < CPW * W && col < ncol;
   const int c = valid ? col : (col < ncol ? col : ncol - 1);
-  const int gg = g < NG ? g : NG - 1;
+  const int gg = G0 + (g < NG ? g : NG - 1);
   const size_t N = (size_t)ncol;
   const size_t fstride = (size_t)nlay * N;
   const double coszen = __ldg(in.coszen + c);
@@ -1689,8 +1764,8 @@ __device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, dou
   lvl[klev] = Quad<R>{tdbt1, tdn1, rdnd1, (R)0.};
   // Upward sweep (vrtqdr_sw :104-124) from the surface, with the level fluxes
   // (:141-149) as soon as each level's upward reflectances are known.
-  double* sup = su + (size_t)(B - 16) * (nlay + 1) * N + col;
-  double* sdp = sd + (size_t)(B - 16) * (nlay + 1) * N + col;
+  double* sup = su + (size_t)SLOT * (nlay + 1) * N + col;
+  double* sdp = sd + (size_t)SLOT * (nlay + 1) * N + col;
   // Split path: incident-flux-weighted band sums through the warp's staging
   // buffers (levels surface first); the summing lane of column sub-index cs
   // writes column wcol0 + cs.
@@ -1699,7 +1774,7 @@ __device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, dou
   if constexpr (SPLIT) swt[wib * 32 + lane] = active ? (float)zincflx : 0.f;
   auto store = [&](int b, int lev, int cs, float s, float cmp) {
     const int cc = wcol0 + cs;
-    if (cc < ncol) as_pair(b == 0 ? su : sd)[((size_t)(B - 16) * (nlay + 1) + lev) * N + cc] = make_float2(s, cmp);
+    if (cc < ncol) as_pair(b == 0 ? su : sd)[((size_t)SLOT * (nlay + 1) + lev) * N + cc] = make_float2(s, cmp);
   };
   R prup = albdir, prupd = albdif;  // level klev+1 (surface)
   for (int jk = klev + 1; jk >= 1; --jk) {
@@ -1754,24 +1829,38 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_SW_MINB :
                                                            int ncol, int nlay, int analytic, const R* __restrict__ cld) {
   __shared__ float sbuf[sizeof(R) == 4 ? kGSumFloats : 1];
   __shared__ float swt[sizeof(R) == 4 ? kBlock : 1];
-  int blk = blockIdx.x, band = 0;
-  for (; band < kSwBands; ++band) {
-    const int nb = lw_blocks_for_band(split_lanes(c_sw.band[band].ng, sizeof(R) == 4), ncol);
-    if (blk < nb) break;
-    blk -= nb;
-  }
+  constexpr bool SPLIT = sizeof(R) == 4;
+  int blk = blockIdx.x;
+  const int unit = sw_unit_of_block<SPLIT>(blk, ncol);  // slot (split) or band (FP64)
+  const int band = SPLIT ? (unit < kSwSlots ? sw_slot(unit).band - 16 : kSwBands) : unit;
   if (threadIdx.x == 0 && band < kSwBands) prefetch_band_l2(tab, c_sw.band[band]);
   const bool an = FL < 0 ? analytic != 0 : (FL & 1) != 0;
   const int ia = FL < 0 ? iaer : ((FL & 2) ? 10 : 0);
+  if constexpr (SPLIT) {
+#define RRTMG_SW_SLOT(s)                                                                                         \
+  case s:                                                                                                        \
+    sw_band<sw_slot(s).band, R, MAXL, TOT, sw_slot(s).g0, sw_slot(s).ng, s>(p, in, adjflux, ia, tab, tab64, exptbl, \
+                                                                          su, sd, ncol, nlay, an, blk, sbuf, swt,  \
+                                                                          cld);                                    \
+    break;
+    switch (unit) {
+      RRTMG_SW_SLOT(0) RRTMG_SW_SLOT(1) RRTMG_SW_SLOT(2) RRTMG_SW_SLOT(3) RRTMG_SW_SLOT(4) RRTMG_SW_SLOT(5)
+      RRTMG_SW_SLOT(6) RRTMG_SW_SLOT(7) RRTMG_SW_SLOT(8) RRTMG_SW_SLOT(9) RRTMG_SW_SLOT(10) RRTMG_SW_SLOT(11)
+      RRTMG_SW_SLOT(12) RRTMG_SW_SLOT(13) RRTMG_SW_SLOT(14) RRTMG_SW_SLOT(15)
+      default: break;
+    }
+#undef RRTMG_SW_SLOT
+  } else {
 #define RRTMG_SW_CASE(b) \
   case b - 16: sw_band<b, R, MAXL, TOT>(p, in, adjflux, ia, tab, tab64, exptbl, su, sd, ncol, nlay, an, blk, sbuf, swt, cld); break;
-  switch (band) {
-    RRTMG_SW_CASE(16) RRTMG_SW_CASE(17) RRTMG_SW_CASE(18) RRTMG_SW_CASE(19) RRTMG_SW_CASE(20) RRTMG_SW_CASE(21)
-    RRTMG_SW_CASE(22) RRTMG_SW_CASE(23) RRTMG_SW_CASE(24) RRTMG_SW_CASE(25) RRTMG_SW_CASE(26) RRTMG_SW_CASE(27)
-    RRTMG_SW_CASE(28) RRTMG_SW_CASE(29)
-    default: break;
-  }
+    switch (unit) {
+      RRTMG_SW_CASE(16) RRTMG_SW_CASE(17) RRTMG_SW_CASE(18) RRTMG_SW_CASE(19) RRTMG_SW_CASE(20) RRTMG_SW_CASE(21)
+      RRTMG_SW_CASE(22) RRTMG_SW_CASE(23) RRTMG_SW_CASE(24) RRTMG_SW_CASE(25) RRTMG_SW_CASE(26) RRTMG_SW_CASE(27)
+      RRTMG_SW_CASE(28) RRTMG_SW_CASE(29)
+      default: break;
+    }
 #undef RRTMG_SW_CASE
+  }
 }
 
 #ifdef RRTMG_DEFINE_COLUMN_KERNELS

@@ -24,6 +24,16 @@ int sw_gpoint_blocks(const SwConst& c, int ncol, bool split) {
   for (int b = 0; b < kSwBands; ++b) n += lw_blocks_for_band(split_lanes(c.band[b].ng, split), ncol);
   return n;
 }
+int lw_slot_blocks(int ncol) {
+  int n = 0;
+  for (int s = 0; s < kLwSlots; ++s) n += lw_blocks_for_band(split_lanes(lw_slot(s).ng, true), ncol);
+  return n;
+}
+int sw_slot_blocks(int ncol) {
+  int n = 0;
+  for (int s = 0; s < kSwSlots; ++s) n += lw_blocks_for_band(split_lanes(sw_slot(s).ng, true), ncol);
+  return n;
+}
 
 void launch_lw_prep(const LwIn& in, const LwWork& w, const double* totplnk, const double* totplnkderiv, int ncol,
                     int nlay, int idrv, unsigned* flags, cudaStream_t s) {

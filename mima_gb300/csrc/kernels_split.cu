@@ -7,10 +7,11 @@
 
 namespace rrtmg {
 
-// LW band weight of the broadband sums: wtdiff * delwave(band) * fluxfac
-// (rrtmg_lw_rtrnmr.f90:720-746), folded into one factor and split into two
-// floats (w = hi + lo to 2^-48) for the compensated FP32 band sums.
-__constant__ float2 c_lw_bandw[kLwBands];
+// LW band weight of the broadband sums per slot (sub-band): wtdiff *
+// delwave(band) * fluxfac (rrtmg_lw_rtrnmr.f90:720-746), folded into one
+// factor and split into two floats (w = hi + lo to 2^-48) for the compensated
+// FP32 band sums.
+__constant__ float2 c_lw_bandw[kLwSlots];
 
 cudaError_t upload_constants_split(const LwConst& lw, const SwConst& sw) {
   cudaError_t e = cudaMemcpyToSymbol(c_lw, &lw, sizeof(LwConst));
@@ -18,11 +19,11 @@ cudaError_t upload_constants_split(const LwConst& lw, const SwConst& sw) {
   const LwConstF f = make_lwconstf(lw);
   e = cudaMemcpyToSymbol(c_lwf, &f, sizeof(LwConstF));
   if (e != cudaSuccess) return e;
-  float2 bw[kLwBands];
-  for (int b = 0; b < kLwBands; ++b) {
-    const double w = 0.5 * lw.band[b].delwave * lw.fluxfac;
-    bw[b].x = (float)w;
-    bw[b].y = (float)(w - (double)bw[b].x);
+  float2 bw[kLwSlots];
+  for (int k = 0; k < kLwSlots; ++k) {
+    const double w = 0.5 * lw.band[lw_slot(k).band - 1].delwave * lw.fluxfac;
+    bw[k].x = (float)w;
+    bw[k].y = (float)(w - (double)bw[k].x);
   }
   e = cudaMemcpyToSymbol(c_lw_bandw, bw, sizeof(bw));
   if (e != cudaSuccess) return e;
@@ -93,7 +94,7 @@ __global__ void __launch_bounds__(128) lw_finalize_split_kernel(const double* __
     CSum sx, sy;
     const size_t o = (size_t)lv * N + col;
 #pragma unroll
-    for (int k = 0; k < kLwBands; ++k) {
+    for (int k = 0; k < kLwSlots; ++k) {
       sx.add(__ldg(as_pair(a) + k * bs + o), c_lw_bandw[k]);
       sy.add(__ldg(as_pair(b) + k * bs + o), c_lw_bandw[k]);
     }
@@ -104,7 +105,7 @@ __global__ void __launch_bounds__(128) lw_finalize_split_kernel(const double* __
     CSum sx;
     const size_t o = (size_t)lv * N + col;
 #pragma unroll
-    for (int k = 0; k < kLwBands; ++k) sx.add(__ldg(as_pair(a) + k * bs + o), c_lw_bandw[k]);
+    for (int k = 0; k < kLwSlots; ++k) sx.add(__ldg(as_pair(a) + k * bs + o), c_lw_bandw[k]);
     return sx.value();
   };
   const bool clear_own = buc != nullptr;
@@ -162,7 +163,7 @@ __global__ void __launch_bounds__(128) sw_finalize_split_kernel(const double* __
     CSum su_, sd_;
     const size_t o = (size_t)lv * N + col;
 #pragma unroll
-    for (int k = 0; k < kSwBands; ++k) {
+    for (int k = 0; k < kSwSlots; ++k) {
       su_.add(__ldg(as_pair(u) + k * bs + o));
       sd_.add(__ldg(as_pair(d) + k * bs + o));
     }

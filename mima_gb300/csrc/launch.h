@@ -84,5 +84,8 @@ void launch_sw_gpoint_split(const SwPrepT<float>& p, const SwIn& in, double adjf
 // blocks (4 warps of 32 / lanes columns; lanes = split_lanes(ng, split)).
 int lw_gpoint_blocks(const LwConst& c, int ncol, bool split = false);
 int sw_gpoint_blocks(const SwConst& c, int ncol, bool split = false);
+// Blocks of the split forward grids, which enumerate the slots (sub-bands).
+int lw_slot_blocks(int ncol);
+int sw_slot_blocks(int ncol);
 
 }  // namespace rrtmg

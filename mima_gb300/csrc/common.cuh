@@ -22,7 +22,10 @@ constexpr int kLwG = 140;
 constexpr int kSwBands = 14;
 // Sub-bands (slots) of the split path's g-point grids (kernels.cuh lw_slot /
 // sw_slot): rows of the band-partial arrays.
-constexpr int kLwSlots = 16, kSwSlots = 16;
+#ifndef RRTMG_LW_SUBBANDS
+#define RRTMG_LW_SUBBANDS 1
+#endif
+constexpr int kLwSlots = RRTMG_LW_SUBBANDS ? 19 : 16, kSwSlots = 16;
 constexpr int kSwG = 112;
 constexpr int kBlock = 128;  // threads per block in the g-point kernels
 constexpr int kNTbl = 10000;

@@ -155,17 +155,27 @@ __host__ __device__ constexpr int split_lanes(int ng, bool split) {
   return (split && 32 / ng > 32 / pow2ceil(ng)) ? ng : pow2ceil(ng);
 }
 
-// Sub-bands of the split path ("slots"): the SW bands of 12 g-points, whose
+// Sub-bands of the split path ("slots"): the bands of 12 g-points, whose
 // warps would idle 4 of every 16 lanes, run as groups of 8 + 4 g-points, each
 // group with its own lanes per column and its own band partial; every other
 // band is one slot.  The finalize kernels sum the slots.  Measured at T85 x 40
-// (GB300): SW solver 2.46 -> 2.28 ms; the same split of the LW bands of 12 and
-// 14 g-points (8 + 4, 8 + 4 + 2) made the LW solver slower, 3.0 -> 3.43 ms, so
-// every LW band is one slot.
+// (GB300): SW solver 2.46 -> 2.28 ms; LW solver 2.99 -> 2.86 ms (finalize
+// 0.08 -> 0.11 ms) with its 12-g-point bands split, but 3.43 ms when its band
+// of 14 g-points was split too (8 + 4 + 2), which therefore stays whole.
+// RRTMG_LW_SUBBANDS=0 builds the LW solver with one slot per band.
 struct SubBand {
   int band, g0, ng;  // band (LW 1..16, SW 16..29), first g-point in the band, g-points
 };
+#if RRTMG_LW_SUBBANDS
+__host__ __device__ constexpr SubBand lw_slot(int s) {
+  constexpr SubBand t[kLwSlots] = {{1, 0, 10}, {2, 0, 8},  {2, 8, 4},  {3, 0, 16}, {4, 0, 14}, {5, 0, 16}, {6, 0, 8},
+                                   {7, 0, 8},  {7, 8, 4},  {8, 0, 8},  {9, 0, 8},  {9, 8, 4},  {10, 0, 6}, {11, 0, 8},
+                                   {12, 0, 8}, {13, 0, 4}, {14, 0, 2}, {15, 0, 2}, {16, 0, 2}};
+  return t[s];
+}
+#else
 __host__ __device__ constexpr SubBand lw_slot(int s) { return SubBand{s + 1, 0, lw_ng(s + 1)}; }
+#endif
 __host__ __device__ constexpr SubBand sw_slot(int s) {
   constexpr SubBand t[kSwSlots] = {{16, 0, 6}, {17, 0, 8}, {17, 8, 4}, {18, 0, 8}, {19, 0, 8}, {20, 0, 10},
                                    {21, 0, 10}, {22, 0, 2}, {23, 0, 10}, {24, 0, 8}, {25, 0, 6}, {26, 0, 6},
@@ -970,6 +980,9 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_LW_MINB :
       RRTMG_LW_SLOT(0) RRTMG_LW_SLOT(1) RRTMG_LW_SLOT(2) RRTMG_LW_SLOT(3) RRTMG_LW_SLOT(4) RRTMG_LW_SLOT(5)
       RRTMG_LW_SLOT(6) RRTMG_LW_SLOT(7) RRTMG_LW_SLOT(8) RRTMG_LW_SLOT(9) RRTMG_LW_SLOT(10) RRTMG_LW_SLOT(11)
       RRTMG_LW_SLOT(12) RRTMG_LW_SLOT(13) RRTMG_LW_SLOT(14) RRTMG_LW_SLOT(15)
+#if RRTMG_LW_SUBBANDS
+      RRTMG_LW_SLOT(16) RRTMG_LW_SLOT(17) RRTMG_LW_SLOT(18)
+#endif
       default: break;
     }
 #undef RRTMG_LW_SLOT
@@ -1016,6 +1029,9 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_LW_MINB :
       RRTMG_LW_SLOT(0) RRTMG_LW_SLOT(1) RRTMG_LW_SLOT(2) RRTMG_LW_SLOT(3) RRTMG_LW_SLOT(4) RRTMG_LW_SLOT(5)
       RRTMG_LW_SLOT(6) RRTMG_LW_SLOT(7) RRTMG_LW_SLOT(8) RRTMG_LW_SLOT(9) RRTMG_LW_SLOT(10) RRTMG_LW_SLOT(11)
       RRTMG_LW_SLOT(12) RRTMG_LW_SLOT(13) RRTMG_LW_SLOT(14) RRTMG_LW_SLOT(15)
+#if RRTMG_LW_SUBBANDS
+      RRTMG_LW_SLOT(16) RRTMG_LW_SLOT(17) RRTMG_LW_SLOT(18)
+#endif
       default: break;
     }
 #undef RRTMG_LW_SLOT

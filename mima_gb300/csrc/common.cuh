@@ -25,7 +25,7 @@ constexpr int kSwBands = 14;
 #ifndef RRTMG_LW_SUBBANDS
 #define RRTMG_LW_SUBBANDS 1
 #endif
-constexpr int kLwSlots = RRTMG_LW_SUBBANDS ? 19 : 16, kSwSlots = 16;
+constexpr int kLwSlots = RRTMG_LW_SUBBANDS ? 20 : 16, kSwSlots = 16;
 constexpr int kSwG = 112;
 constexpr int kBlock = 128;  // threads per block in the g-point kernels
 constexpr int kNTbl = 10000;

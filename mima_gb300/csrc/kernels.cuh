@@ -160,17 +160,19 @@ __host__ __device__ constexpr int split_lanes(int ng, bool split) {
 // group with its own lanes per column and its own band partial; every other
 // band is one slot.  The finalize kernels sum the slots.  Measured at T85 x 40
 // (GB300): SW solver 2.46 -> 2.28 ms; LW solver 2.99 -> 2.86 ms (finalize
-// 0.08 -> 0.11 ms) with its 12-g-point bands split, but 3.43 ms when its band
-// of 14 g-points was split too (8 + 4 + 2), which therefore stays whole.
-// RRTMG_LW_SUBBANDS=0 builds the LW solver with one slot per band.
+// 0.08 -> 0.11 ms) with its 12-g-point bands split, and 2.90 -> 2.78 ms with
+// its band of 14 g-points as 8 + 6 (a 6-lane group packs 5 columns in a
+// warp); as 8 + 4 + 2 it took 3.43 ms (a 2-lane group spreads each table
+// gather over 16 columns).  RRTMG_LW_SUBBANDS=0 builds the LW solver with one
+// slot per band.
 struct SubBand {
   int band, g0, ng;  // band (LW 1..16, SW 16..29), first g-point in the band, g-points
 };
 #if RRTMG_LW_SUBBANDS
 __host__ __device__ constexpr SubBand lw_slot(int s) {
-  constexpr SubBand t[kLwSlots] = {{1, 0, 10}, {2, 0, 8},  {2, 8, 4},  {3, 0, 16}, {4, 0, 14}, {5, 0, 16}, {6, 0, 8},
-                                   {7, 0, 8},  {7, 8, 4},  {8, 0, 8},  {9, 0, 8},  {9, 8, 4},  {10, 0, 6}, {11, 0, 8},
-                                   {12, 0, 8}, {13, 0, 4}, {14, 0, 2}, {15, 0, 2}, {16, 0, 2}};
+  constexpr SubBand t[kLwSlots] = {{1, 0, 10}, {2, 0, 8},  {2, 8, 4},  {3, 0, 16}, {4, 0, 8},  {4, 8, 6},  {5, 0, 16},
+                                   {6, 0, 8},  {7, 0, 8},  {7, 8, 4},  {8, 0, 8},  {9, 0, 8},  {9, 8, 4},  {10, 0, 6},
+                                   {11, 0, 8}, {12, 0, 8}, {13, 0, 4}, {14, 0, 2}, {15, 0, 2}, {16, 0, 2}};
   return t[s];
 }
 #else
@@ -981,7 +983,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_LW_MINB :
       RRTMG_LW_SLOT(6) RRTMG_LW_SLOT(7) RRTMG_LW_SLOT(8) RRTMG_LW_SLOT(9) RRTMG_LW_SLOT(10) RRTMG_LW_SLOT(11)
       RRTMG_LW_SLOT(12) RRTMG_LW_SLOT(13) RRTMG_LW_SLOT(14) RRTMG_LW_SLOT(15)
 #if RRTMG_LW_SUBBANDS
-      RRTMG_LW_SLOT(16) RRTMG_LW_SLOT(17) RRTMG_LW_SLOT(18)
+      RRTMG_LW_SLOT(16) RRTMG_LW_SLOT(17) RRTMG_LW_SLOT(18) RRTMG_LW_SLOT(19)
 #endif
       default: break;
     }
@@ -1030,7 +1032,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_LW_MINB :
       RRTMG_LW_SLOT(6) RRTMG_LW_SLOT(7) RRTMG_LW_SLOT(8) RRTMG_LW_SLOT(9) RRTMG_LW_SLOT(10) RRTMG_LW_SLOT(11)
       RRTMG_LW_SLOT(12) RRTMG_LW_SLOT(13) RRTMG_LW_SLOT(14) RRTMG_LW_SLOT(15)
 #if RRTMG_LW_SUBBANDS
-      RRTMG_LW_SLOT(16) RRTMG_LW_SLOT(17) RRTMG_LW_SLOT(18)
+      RRTMG_LW_SLOT(16) RRTMG_LW_SLOT(17) RRTMG_LW_SLOT(18) RRTMG_LW_SLOT(19)
 #endif
       default: break;
     }

@@ -332,12 +332,18 @@ __device__ __forceinline__ void lw_adj_band(const LwIn& in, const AdjLwWorkT<R>&
   const R rec_6 = (R)0.166667;
   const int E = 3 * nlay + 3;
 
-  // Layer state (index l-1) and level radiances.
-  R atr[MAXL], bbu[MAXL];
-  R tT[MAXL], dT[MAXL], uT[MAXL];  // d(t, sd, su)/dtlay
-  R tQ[MAXL], dQ[MAXL], uQ[MAXL];  // d(t, sd, su)/dq
-  R tS[MAXL], dS[MAXL], uS[MAXL];  // d(t, sd, su)/dsecdiff
-  R dLb[MAXL], uLt[MAXL];          // dsd/dtlev below, dsu/dtlev above
+  // Layer state (index l-1) and level radiances.  The tangents of a layer
+  // are written together and read together, so they sit side by side in
+  // records (one wide local access each):
+  //   tq[k].T = {t, sd, su}/dtlay and dsd/dtlev below,
+  //   tq[k].Q = {t, sd, su}/dq and dsu/dtlev above,
+  //   ts[k]   = {t, sd, su}/dsecdiff.
+  struct TQ {
+    Quad<R> T, Q;
+  };
+  Pair2<R> ab[MAXL];  // {atr, bbu}
+  TQ tq[MAXL];
+  Quad<R> ts[MAXL];
   R Dl[MAXL + 1], Ul[MAXL + 1], nu[MAXL + 1];
   R ck[MAXL + 1];                  // seed cotangents of the layer divergences (index k = 1..nlay; ck[0] = 0)
 
@@ -387,8 +393,7 @@ __device__ __forceinline__ void lw_adj_band(const LwIn& in, const AdjLwWorkT<R>&
     const R pdn = __ldg(w.plev_v + od_), pdn_t = __ldg(w.plev_t + od_);
     const R dpup = pup - blay, dpdn = pdn - blay;
     const R bd = plf * (blay + tf * dpdn), bu = plf * (blay + tf * dpup);
-    atr[k] = a;
-    bbu[k] = bu;
+    ab[k] = Pair2<R>{a, bu};
     auto tang = [&](R odx, R dplf, R dbl, R& ot, R& osd, R& osu) {
       const R da = a_d * odx, dtf = tf_d * odx;
       const R dbd = dplf * (blay + tf * dpdn) + plf * (dbl + dtf * dpdn - tf * dbl);
@@ -397,11 +402,16 @@ __device__ __forceinline__ void lw_adj_band(const LwIn& in, const AdjLwWorkT<R>&
       osd = da * bd + a * dbd;
       osu = da * bu + a * dbu;
     };
-    tang(odT, fracs.t, blay_t, tT[k], dT[k], uT[k]);
-    tang(odQ, fracs.q, (R)0, tQ[k], dQ[k], uQ[k]);
-    tang(odS, (R)0, (R)0, tS[k], dS[k], uS[k]);
-    dLb[k] = a * plf * tf * pdn_t;
-    uLt[k] = a * plf * tf * pup_t;
+    TQ r;
+    Quad<R> rs;
+    tang(odT, fracs.t, blay_t, r.T.a, r.T.b, r.T.c);
+    tang(odQ, fracs.q, (R)0, r.Q.a, r.Q.b, r.Q.c);
+    tang(odS, (R)0, (R)0, rs.a, rs.b, rs.c);
+    r.T.d = a * plf * tf * pdn_t;
+    r.Q.d = a * plf * tf * pup_t;
+    rs.d = (R)0;
+    tq[k] = r;
+    ts[k] = rs;
     radld = radld + (bd - radld) * a;
     Dl[k] = radld;
     if (lev == 1) fr1 = fracs;
@@ -411,7 +421,10 @@ __device__ __forceinline__ void lw_adj_band(const LwIn& in, const AdjLwWorkT<R>&
   const R semiss = in.emis ? (R)__ldg(in.emis + c + N * (B - 1)) : (R)1;
   const R reflect = (R)1 - semiss;
   Ul[0] = fr1.v * pb + reflect * Dl[0];
-  for (int l = 1; l <= nlay; ++l) Ul[l] = Ul[l - 1] + (bbu[l - 1] - Ul[l - 1]) * atr[l - 1];
+  for (int l = 1; l <= nlay; ++l) {
+    const Pair2<R> x = ab[l - 1];
+    Ul[l] = Ul[l - 1] + (x.b - Ul[l - 1]) * x.a;
+  }
 
   // 3. reverse sweeps, one cotangent seed at a time.  With c_k the cotangent of
   //    div_k (c_0 = c_{nlay+1} = 0) the adjoints are carried as
@@ -431,8 +444,10 @@ __device__ __forceinline__ void lw_adj_band(const LwIn& in, const AdjLwWorkT<R>&
     const R colr = (R)(cot ? __ldg(cot + (size_t)nlay * N + c) : (s == nlay ? 1.0 : 0.0));
     const R csfc = (R)(cot ? __ldg(cot + (size_t)(nlay + 1) * N + c) : (s == nlay + 1 ? 1.0 : 0.0));
     nu[nlay] = colr;
-    for (int m = nlay - 1; m >= 0; --m)
-      nu[m] = atr[m] * ck[m + 1] + ((R)1 - atr[m]) * nu[m + 1] + (m == 0 ? csfc : (R)0);
+    for (int m = nlay - 1; m >= 0; --m) {
+      const R am = ab[m].a;
+      nu[m] = am * ck[m + 1] + ((R)1 - am) * nu[m + 1] + (m == 0 ? csfc : (R)0);
+    }
     GRed<W, NG, R> red{(R*)sred + wib * W * kRow, (int)(threadIdx.x & 31), 0, 0};
     auto store = [&](int e, int cs, double v) {
       const int cc = wcol0 + cs;
@@ -447,22 +462,25 @@ __device__ __forceinline__ void lw_adj_band(const LwIn& in, const AdjLwWorkT<R>&
       const R lamD = rho - ck[l];  // lamD_{l-1} = rho_{l-1} - c_l
       const R gt = lamU * Ul[l - 1] + lamD * Dl[l];
       const R gsd = lamD, gsu = lamU;
-      R gT = gt * tT[k] + gsd * dT[k] + gsu * uT[k];
-      R gQ = gt * tQ[k] + gsd * dQ[k] + gsu * uQ[k];
+      const TQ r = tq[k];
+      const Quad<R> rs = ts[k];
+      R gT = gt * r.T.a + gsd * r.T.b + gsu * r.T.c;
+      R gQ = gt * r.Q.a + gsd * r.Q.b + gsu * r.Q.c;
       if (l == 1) {
         gT += lamU0 * fr1.t * pb;
         gQ += lamU0 * fr1.q * pb;
       }
-      gS += gt * tS[k] + gsd * dS[k] + gsu * uS[k];
-      const R gLev = accLev + gsd * dLb[k];
-      accLev = gsu * uLt[k];
+      gS += gt * rs.a + gsd * rs.b + gsu * rs.c;
+      const R gLev = accLev + gsd * r.T.d;
+      accLev = gsu * r.Q.d;
       red.put(gT);
       red.next(store);
       red.put(gQ);
       red.next(store);
       red.put(gLev);
       red.next(store);
-      rho = atr[k] * ck[l] + ((R)1 - atr[k]) * rho;  // rho_l
+      const R ak = ab[k].a;
+      rho = ak * ck[l] + ((R)1 - ak) * rho;  // rho_l
     }
     red.put(accLev);
     red.next(store);

@@ -264,7 +264,7 @@ int rrtmg_vjp_dev(rrtmg_gpu_handle h, void* stream, int ncol, int nlay,
 
 /* Size of the library's static LW device scratch (64 MiB), held by every GPU
  * that loads the library until process exit.  At nlay = 40 a call needs about
- * 35.3 KB per column, so up to about 1900 columns fit; at nlay = 60, about 1280. */
+ * 39.2 KB per column, so up to about 1700 columns fit; at nlay = 60, about 1150. */
 #define RRTMG_GPU_STATIC_SCRATCH_BYTES (64u * 1024u * 1024u)
 
 /* No counterpart in the reference.  Same arguments and results as

@@ -94,7 +94,10 @@ def test_static_scratch_entry_point_split_precision(gpu):
 def test_static_scratch_entry_point_rejects_sizes_beyond_the_limit(gpu):
     import torch
     nlay = 40
-    per_col = 4 * nlay + 8 * 25 * nlay + 8 * 16 * nlay + 4 * 8 * 16 * (nlay + 1) + 3 * 8 * 16 + 4 + 2 * 8 * nlay
+    # LW scratch per column: indices, 25 fields, Planck terms by layer and level, three band-partial
+    # arrays of 20 rows (the split path's slots), surface terms, laytrop, column sums
+    per_col = (4 * nlay + 8 * 25 * nlay + 8 * 16 * nlay + 8 * 16 * (nlay + 1) + 3 * 8 * 20 * (nlay + 1)
+               + 3 * 8 * 16 + 4 + 2 * 8 * nlay)
     ncol = R.STATIC_SCRATCH_BYTES // per_col + 64
     atm = A.small_atmosphere(ncol, nlay, seed=43)
     d = R.atm_device_inputs(atm)

@@ -354,6 +354,17 @@ def reference_tables(root) -> dict:
     for k, v in st.items():
         out[f"lw.{k}"] = (_as_struct(k, v), (1,))
 
+    # ---- cloud optical properties (lwcldpr, swcldpr): cldprop / cldprop_sw ---
+    for src, mod, routine, prefix, prm in ((linit, P["lw_mod"] / "rrlw_cld.f90", "lwcldpr", "lwcld", lw_params),
+                                          (sinit, P["sw_mod"] / "rrsw_cld.f90", "swcldpr", "swcld", sw_params)):
+        decl = _decls(mod, prm)
+        data = _data_from(src, decl, routines={routine})
+        for k, (lb, _shape) in decl.items():
+            a = np.asarray(data.get(k, np.nan), dtype=np.float64)
+            if np.isnan(a).any():
+                raise ValueError(f"cloud table {k} incompletely assigned")
+            out[f"{prefix}.{k}"] = (np.atleast_1d(a), lb if lb else (1,))
+
     # ---- LW table shapes (for the synthetic generator) ----------------------
     shapes = {}
     for b in range(1, 17):

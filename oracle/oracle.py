@@ -68,12 +68,19 @@ def _f(a):
     return np.ascontiguousarray(a, dtype=np.float64)
 
 
+class CloudRangeError(RuntimeError):
+    """A cloud effective radius outside the range of its parameterisation's
+    table: the reference's cldprop / cldprop_sw stop."""
+
+
 def rrtmg_lw(atm, idrv: int = 0, tauaer=None, nthreads: int = 0, cloud=None, icld: int = 1):
     """rrtmg_lw on ``atm``; returns dict of (nlev, ncol) arrays.  Clear sky, or
     with ``cloud`` = dict(cldfr=(nlay, ncol), taucld=(nlay, ncol, 16) [Fortran
-    (16, ncol, nlay)], optional cicewp / cliqwp (nlay, ncol)): cloud optical
-    depths given (inflglw = 0), random overlap (``icld`` = 1, rtrn) or
-    maximum/random overlap (``icld`` = 2 or 3, rtrnmr)."""
+    (16, ncol, nlay)], cicewp / cliqwp (nlay, ncol), and for the cloud physics
+    inflag (0: optical depths given, 1: abscld1 x water path, 2: ice and
+    liquid parameterisations), iceflag, liqflag, reice / reliq (nlay, ncol)):
+    random overlap (``icld`` = 1, rtrn) or maximum/random overlap (``icld`` =
+    2 or 3, rtrnmr)."""
     n, L = atm.ncol, atm.nlay
     out = {k: np.zeros((L + 1, n)) for k in ("uflx", "dflx", "uflxc", "dflxc", "duflx_dt", "duflxc_dt")}
     out.update({k: np.zeros((L, n)) for k in ("hr", "hrc")})
@@ -83,11 +90,15 @@ def rrtmg_lw(atm, idrv: int = 0, tauaer=None, nthreads: int = 0, cloud=None, icl
             None if tauaer is None else _f(tauaer)]
     cl = cloud or {}
     carg = [None if cl.get(k) is None else _f(cl[k]) for k in ("cldfr", "taucld", "cicewp", "cliqwp")]
+    rad = [None if cl.get(k) is None else _f(cl[k]) for k in ("reice", "reliq")]
+    flags = [C.c_int(int(cl.get(k, 0))) for k in ("inflag", "iceflag", "liqflag")]
     rc = _lib.orc_rrtmg_lw(C.c_int(n), C.c_int(L), C.c_int(icld if cloud else 0), C.c_int(idrv),
                            *[_p(a) for a in args],
                            _p(out["uflx"]), _p(out["dflx"]), _p(out["hr"]), _p(out["uflxc"]),
                            _p(out["dflxc"]), _p(out["hrc"]), _p(out["duflx_dt"]), _p(out["duflxc_dt"]),
-                           C.c_int(nthreads), *[_p(a) for a in carg])
+                           C.c_int(nthreads), *[_p(a) for a in carg], *flags, *[_p(a) for a in rad])
+    if rc == 5:
+        raise CloudRangeError("an effective radius is outside its parameterisation's range (cldprop stops)")
     if rc != 0:
         raise RuntimeError(f"orc_rrtmg_lw failed ({rc})")
     return out
@@ -141,7 +152,9 @@ class PartialCloud(RuntimeError):
 def rrtmg_sw(atm, iaer: int = 0, tauaer=None, ssaaer=None, asmaer=None, nthreads: int = 0, cloud=None):
     """rrtmg_sw on ``atm``.  ``cloud`` = dict(cldfr (nlay, ncol), taucld, ssacld,
     asmcld, fsfcld (nlay, ncol, 14) [Fortran (14, ncol, nlay)], optional cicewp
-    / cliqwp (nlay, ncol)): icld = 1, cloud optics given (inflgsw = 0)."""
+    / cliqwp (nlay, ncol)): icld = 1, cloud optics given (inflgsw = 0); or
+    with inflag = 2, iceflag (1..3), liqflag (1), cicewp / cliqwp and reice /
+    reliq (nlay, ncol): the optics from the ice and liquid parameterisations."""
     n, L = atm.ncol, atm.nlay
     out = {k: np.zeros((L + 1, n)) for k in ("swuflx", "swdflx", "swuflxc", "swdflxc")}
     out.update({k: np.zeros((L, n)) for k in ("swhr", "swhrc")})
@@ -152,12 +165,17 @@ def rrtmg_sw(atm, iaer: int = 0, tauaer=None, ssaaer=None, asmaer=None, nthreads
     cl = cloud or {}
     carg = [None if cl.get(k) is None else _f(cl[k])
             for k in ("cldfr", "taucld", "ssacld", "asmcld", "fsfcld", "cicewp", "cliqwp")]
+    rad = [None if cl.get(k) is None else _f(cl[k]) for k in ("reice", "reliq")]
+    flags = [C.c_int(int(cl.get(k, 0))) for k in ("inflag", "iceflag", "liqflag")]
     rc = _lib.orc_rrtmg_sw(C.c_int(n), C.c_int(L), C.c_int(1 if cloud else 0), C.c_int(iaer),
                            *[_p(a) for a in args],
                            C.c_double(atm.adjes), C.c_int(atm.dyofyr), C.c_double(atm.scon),
                            *[_p(a) for a in aer],
                            _p(out["swuflx"]), _p(out["swdflx"]), _p(out["swhr"]), _p(out["swuflxc"]),
-                           _p(out["swdflxc"]), _p(out["swhrc"]), C.c_int(nthreads), *[_p(a) for a in carg])
+                           _p(out["swdflxc"]), _p(out["swhrc"]), C.c_int(nthreads), *[_p(a) for a in carg],
+                           *flags, *[_p(a) for a in rad])
+    if rc == 5:
+        raise CloudRangeError("an effective size is outside its parameterisation's range (cldprop_sw stops)")
     if rc == 4:
         raise PartialCloud("a layer is partly cloudy (0 < cldfr < 1): not computed without McICA")
     if rc != 0:

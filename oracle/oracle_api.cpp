@@ -53,9 +53,14 @@ int orc_rrtmg_lw(int ncol, int nlay, int icld, int idrv, const double* play, con
                  const double* ccl4vmr, const double* emis, const double* tauaer, double* uflx, double* dflx,
                  double* hr, double* uflxc, double* dflxc, double* hrc, double* duflx_dt, double* duflxc_dt,
                  int nthreads, const double* cldfr, const double* taucld, const double* cicewp,
-                 const double* cliqwp) {
+                 const double* cliqwp, int inflag, int iceflag, int liqflag, const double* reice,
+                 const double* reliq) {
   if (!g_ready) return 2;
-  if (icld != 0 && !(icld >= 1 && icld <= 3 && cldfr && taucld)) return 3;
+  if (icld != 0 && !(icld >= 1 && icld <= 3 && cldfr)) return 3;
+  if (icld != 0 && inflag == 0 && !taucld) return 3;
+  if (icld != 0 && inflag >= 1 && !(cicewp && cliqwp)) return 3;
+  if (icld != 0 && inflag == 2 && !(iceflag >= 0 && iceflag <= 3 && liqflag >= 0 && liqflag <= 1 && reice && reliq))
+    return 3;
   LwInput in{ncol, nlay, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr,
              cfc11vmr, cfc12vmr, cfc22vmr, ccl4vmr, emis, tauaer};
   in.icld = icld;
@@ -63,13 +68,20 @@ int orc_rrtmg_lw(int ncol, int nlay, int icld, int idrv, const double* play, con
   in.taucld = taucld;
   in.cicewp = cicewp;
   in.cliqwp = cliqwp;
-#pragma omp parallel num_threads(nthreads > 0 ? nthreads : orc_max_threads())
+  in.inflag = inflag;
+  in.iceflag = iceflag;
+  in.liqflag = liqflag;
+  in.reice = reice;
+  in.reliq = reliq;
+  int stopped = 0;
+#pragma omp parallel num_threads(nthreads > 0 ? nthreads : orc_max_threads()) reduction(| : stopped)
   {
     LwColumn c;
     LwOut o;
 #pragma omp for schedule(dynamic, 16)
     for (int iplon = 0; iplon < ncol; ++iplon) {
       lw_column(in, iplon, idrv, c, o);
+      if (c.cld_error) stopped = 1;
       for (int k = 0; k <= nlay; ++k) {
         size_t ix = (size_t)iplon + (size_t)ncol * (size_t)k;
         uflx[ix] = o.totu[k];
@@ -88,7 +100,7 @@ int orc_rrtmg_lw(int ncol, int nlay, int icld, int idrv, const double* play, con
       }
     }
   }
-  return 0;
+  return stopped ? 5 : 0;  // 5: cldprop stopped (an effective radius out of range)
 }
 
 int orc_rrtmg_sw(int ncol, int nlay, int icld, int iaer, const double* play, const double* plev,
@@ -99,9 +111,15 @@ int orc_rrtmg_sw(int ncol, int nlay, int icld, int iaer, const double* play, con
                  const double* tauaer, const double* ssaaer, const double* asmaer, double* swuflx,
                  double* swdflx, double* swhr, double* swuflxc, double* swdflxc, double* swhrc, int nthreads,
                  const double* cldfr, const double* taucld, const double* ssacld, const double* asmcld,
-                 const double* fsfcld, const double* cicewp, const double* cliqwp) {
+                 const double* fsfcld, const double* cicewp, const double* cliqwp, int inflag, int iceflag,
+                 int liqflag, const double* reice, const double* reliq) {
   if (!g_ready) return 2;
-  if (icld != 0 && !(icld == 1 && cldfr && taucld && ssacld && asmcld && fsfcld)) return 3;
+  if (icld != 0 && !(icld == 1 && cldfr)) return 3;
+  if (icld != 0 && inflag == 0 && !(taucld && ssacld && asmcld && fsfcld)) return 3;
+  if (icld != 0 && inflag == 2 &&
+      !(iceflag >= 1 && iceflag <= 3 && liqflag == 1 && cicewp && cliqwp && reice && reliq))
+    return 3;
+  if (icld != 0 && inflag != 0 && inflag != 2) return 3;
   if (iaer != 0 && iaer != 10) return 3;
   SwInput in{ncol, nlay, iaer, dyofyr, adjes, scon, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr,
              ch4vmr, n2ovmr, o2vmr, asdir, asdif, aldir, aldif, coszen, tauaer, ssaaer, asmaer};
@@ -113,19 +131,22 @@ int orc_rrtmg_sw(int ncol, int nlay, int icld, int iaer, const double* play, con
   in.fsfcld = fsfcld;
   in.cicewp = cicewp;
   in.cliqwp = cliqwp;
-  int partial = 0;
-#pragma omp parallel num_threads(nthreads > 0 ? nthreads : orc_max_threads())
+  in.inflag = inflag;
+  in.iceflag = iceflag;
+  in.liqflag = liqflag;
+  in.reice = reice;
+  in.reliq = reliq;
+  int partial = 0, stopped = 0;
+#pragma omp parallel num_threads(nthreads > 0 ? nthreads : orc_max_threads()) reduction(| : partial, stopped)
   {
     SwColumn c;
     SwOut o;
 #pragma omp for schedule(dynamic, 16)
     for (int iplon = 0; iplon < ncol; ++iplon) {
-      bool part = false;
-      sw_column(in, iplon, c, o, &part);
-      if (part) {
-#pragma omp atomic write
-        partial = 1;
-      }
+      bool part = false, stop = false;
+      sw_column(in, iplon, c, o, &part, &stop);
+      if (part) partial = 1;
+      if (stop) stopped = 1;
       for (int k = 1; k <= nlay + 1; ++k) {
         size_t ix = (size_t)iplon + (size_t)ncol * (size_t)(k - 1);
         swuflx[ix] = o.fu[k];
@@ -140,7 +161,9 @@ int orc_rrtmg_sw(int ncol, int nlay, int icld, int iaer, const double* play, con
       }
     }
   }
-  return partial ? 4 : 0;  // 4: a partly cloudy layer (the reference stops)
+  // 5: cldprop_sw stopped (a size out of its range); 4: a partly cloudy
+  // layer (the reference's non-McICA SW stops)
+  return stopped ? 5 : partial ? 4 : 0;
 }
 
 // Clear-sky rrtmg_lw per band: bandu/bandd/dbandu_dt (ncol, nlay+1, 16) are the

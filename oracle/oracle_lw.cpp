@@ -64,6 +64,13 @@ void lw_init(const Blob& blob, double cpdair) {
   T.totplk16 = blob.r("lw.totplk16");
   T.totplnkderiv = blob.r("lw.totplnkderiv");
   T.totplk16deriv = blob.r("lw.totplk16deriv");
+  T.absice0 = blob.r("lwcld.absice0");
+  T.absice1 = blob.r("lwcld.absice1");
+  T.absice2 = blob.r("lwcld.absice2");
+  T.absice3 = blob.r("lwcld.absice3");
+  T.absliq1 = blob.r("lwcld.absliq1");
+  T.abscld1 = blob.r("lwcld.abscld1").v.at(0);
+  T.absliq0 = blob.r("lwcld.absliq0").v.at(0);
 
   // rrtmg_lw_init.f90:106-124
   const int ntbl = 10000;
@@ -92,6 +99,84 @@ void lw_init(const Blob& blob, double cpdair) {
   // rrtmg_lw_rad.nomcica.f90:419-421
   T.oneminus = 1.0 - 1.e-6;
   T.fluxfac = (2.0 * std::asin(1.0)) * 2.e4;
+}
+
+// ---------------------------------------------------------------------------
+// cldprop with separate ice and liquid parameterisations (inflag = 2),
+// rrtmg_lw_cldprop.f90:185-270, for one layer whose optics are formed.
+// Sets the layer's taucloud for cloud bands 1..ncbands, with ncbands the
+// running value the reference keeps across its layer loop (1 at the start; 5
+// after an iceflag = 1 ice cloud; 16 after an iceflag 2 / 3 ice cloud or a
+// liqflag = 1 liquid cloud).  icb maps the 16 (or 5) cloud bands onto the
+// coefficient bands of the parameterisation in use.  Returns false where the
+// reference stops (an effective radius outside its table's range).
+// ---------------------------------------------------------------------------
+static const int kIpat[16][3] = {{1, 1, 1},  {1, 2, 2},  {1, 3, 3},  {1, 3, 4},  {1, 3, 5},  {1, 4, 6},
+                                 {1, 4, 7},  {1, 4, 8},  {1, 5, 9},  {1, 5, 10}, {1, 5, 11}, {1, 5, 12},
+                                 {1, 5, 13}, {1, 5, 14}, {1, 5, 15}, {1, 5, 16}};  // ipat = icb (16, 0:2)
+
+int lw_cloud_band(int iband, int ncbands) { return kIpat[iband - 1][ncbands == 1 ? 0 : ncbands == 5 ? 1 : 2]; }
+
+bool lw_cldprop_phys(const LwInput& in, double ciwp, double clwp, double radice, double radliq, LwColumn& c,
+                     int lay) {
+  const LwTables& T = g_lw;
+  double abscoice[17] = {0}, abscoliq[17] = {0};
+  int iceind = 0, liqind = 0;
+  if (ciwp == 0.0) {
+    abscoice[1] = 0.0;
+    iceind = 0;
+  } else if (in.iceflag == 0) {
+    if (radice < 10.0) return false;
+    abscoice[1] = T.absice0(1) + T.absice0(2) / radice;
+    iceind = 0;
+  } else if (in.iceflag == 1) {
+    if (radice < 13.0 || radice > 130.) return false;
+    c.ncbands = 5;
+    for (int ib = 1; ib <= 5; ++ib) abscoice[ib] = T.absice1(1, ib) + T.absice1(2, ib) / radice;
+    iceind = 1;
+  } else if (in.iceflag == 2) {
+    if (radice < 5.0 || radice > 131.0) return false;
+    c.ncbands = 16;
+    const double factor = (radice - 2.) / 3.;
+    int index = (int)factor;
+    if (index == 43) index = 42;
+    const double fint = factor - (double)index;
+    for (int ib = 1; ib <= 16; ++ib)
+      abscoice[ib] = T.absice2(index, ib) + fint * (T.absice2(index + 1, ib) - (T.absice2(index, ib)));
+    iceind = 2;
+  } else {
+    if (radice < 5.0 || radice > 140.0) return false;
+    c.ncbands = 16;
+    const double factor = (radice - 2.) / 3.;
+    int index = (int)factor;
+    if (index == 46) index = 45;
+    const double fint = factor - (double)index;
+    for (int ib = 1; ib <= 16; ++ib)
+      abscoice[ib] = T.absice3(index, ib) + fint * (T.absice3(index + 1, ib) - (T.absice3(index, ib)));
+    iceind = 2;
+  }
+  if (clwp == 0.0) {
+    abscoliq[1] = 0.0;
+    liqind = 0;
+    if (iceind == 1) iceind = 2;
+  } else if (in.liqflag == 0) {
+    abscoliq[1] = T.absliq0;
+    liqind = 0;
+    if (iceind == 1) iceind = 2;
+  } else {
+    if (radliq < 2.5 || radliq > 60.) return false;
+    int index = (int)(radliq - 1.5);
+    if (index == 0) index = 1;
+    if (index == 58) index = 57;
+    const double fint = radliq - 1.5 - (double)index;
+    c.ncbands = 16;
+    for (int ib = 1; ib <= 16; ++ib)
+      abscoliq[ib] = T.absliq1(index, ib) + fint * (T.absliq1(index + 1, ib) - (T.absliq1(index, ib)));
+    liqind = 2;
+  }
+  for (int ib = 1; ib <= c.ncbands; ++ib)
+    c.taucloud[ib][lay] = ciwp * abscoice[kIpat[ib - 1][iceind]] + clwp * abscoliq[kIpat[ib - 1][liqind]];
+  return true;
 }
 
 // ---------------------------------------------------------------------------
@@ -148,19 +233,32 @@ void lw_inatm(const LwInput& in, int iplon, LwColumn& c) {
     for (int ib = 1; ib <= 16; ++ib)
       c.taua[ib][l] = in.tauaer ? in.tauaer[(size_t)iplon + (size_t)ncol * ((size_t)(l - 1) + (size_t)nlay * (size_t)(ib - 1))] : 0.0;
   // Clouds (:866-888): cldfrac(l) = cldfr(iplon,l), tauc(n,l) = taucld(n,iplon,l);
-  // then cldprop with inflag = 0 (rrtmg_lw_cldprop.f90:155-174): a layer's
-  // cloud optical depths are taken when cldfrac >= cldmin and the condensed
-  // water path or the band-summed optical depth is >= cldmin (1e-20), else 0.
+  // then cldprop (rrtmg_lw_cldprop.f90:155-270): a layer's cloud optical
+  // depths are formed when cldfrac >= cldmin and the condensed water path or
+  // the band-summed optical depth is >= cldmin (1e-20), else they are 0.
+  c.ncbands = 1;
+  c.cld_error = false;
   if (in.icld >= 1) {
     const double cldmin = 1.e-20;
     for (int l = 1; l <= nlay; ++l) {
       const size_t o = (size_t)iplon + (size_t)ncol * (size_t)(l - 1);
       c.cldfrac[l] = in.cldfr[o];
       double tauctot = 0.0;
-      for (int ib = 1; ib <= 16; ++ib) tauctot = tauctot + in.taucld[(size_t)(ib - 1) + 16 * o];
-      const double cwp = (in.cicewp ? in.cicewp[o] : 0.0) + (in.cliqwp ? in.cliqwp[o] : 0.0);
-      const bool cloudy = c.cldfrac[l] >= cldmin && (cwp >= cldmin || tauctot >= cldmin);
-      for (int ib = 1; ib <= 16; ++ib) c.taucloud[ib][l] = cloudy ? in.taucld[(size_t)(ib - 1) + 16 * o] : 0.0;
+      for (int ib = 1; ib <= 16; ++ib) tauctot = tauctot + (in.taucld ? in.taucld[(size_t)(ib - 1) + 16 * o] : 0.0);
+      const double ciwp = in.cicewp ? in.cicewp[o] : 0.0, clwp = in.cliqwp ? in.cliqwp[o] : 0.0;
+      const double cwp = ciwp + clwp;
+      for (int ib = 1; ib <= 16; ++ib) c.taucloud[ib][l] = 0.0;
+      if (!(c.cldfrac[l] >= cldmin && (cwp >= cldmin || tauctot >= cldmin))) continue;
+      if (in.inflag == 0) {
+        c.ncbands = 16;
+        for (int ib = 1; ib <= 16; ++ib) c.taucloud[ib][l] = in.taucld[(size_t)(ib - 1) + 16 * o];
+      } else if (in.inflag == 1) {
+        c.ncbands = 16;
+        for (int ib = 1; ib <= 16; ++ib) c.taucloud[ib][l] = g_lw.abscld1 * cwp;
+      } else {
+        if (!lw_cldprop_phys(in, ciwp, clwp, in.reice ? in.reice[o] : 0.0, in.reliq ? in.reliq[o] : 0.0, c, l))
+          c.cld_error = true;
+      }
     }
   }
 }
@@ -1261,7 +1359,7 @@ void lw_rtrn(LwColumn& c, int idrv, LwOut& out) {
   std::vector<double> atrans(nl + 1), bbugas(nl + 1), atot(nl + 1), bbutot(nl + 1);
   int igc = 1;
   for (int iband = 1; iband <= 16; ++iband) {
-    const int ib = iband;  // ncbands = 16: ipat(iband, 2) = iband
+    const int ib = lw_cloud_band(iband, c.ncbands);  // ipat(iband, ...) (rrtmg_lw_rtrn.f90:324-330)
     for (; igc <= T.ngs[iband]; ++igc) {
       double radld = 0., radclrd = 0.;
       int iclddn = 0;
@@ -1659,7 +1757,7 @@ void lw_rtrnmr_cld(LwColumn& c, int idrv, LwOut& out) {
   std::vector<double> atrans(nl + 1), bbugas(nl + 1), atot(nl + 1), bbutot(nl + 1);
   int igc = 1;
   for (int iband = 1; iband <= 16; ++iband) {
-    const int ib = iband;  // ncbands = 16: ipat(iband, 2) = iband
+    const int ib = lw_cloud_band(iband, c.ncbands);  // ipat(iband, ...) (rrtmg_lw_rtrn.f90:324-330)
     for (; igc <= T.ngs[iband]; ++igc) {
       double radld = 0., radclrd = 0.;
       double cldradd = 0., clrradd = 0., rad = 0.;

@@ -17,6 +17,9 @@ struct LwTables {
   int ngc[17], ngs[17], nspa[17], nspb[17];
   double tau_tbl[10001], exp_tbl[10001], tfn_tbl[10001];
   double bpade, heatfac, fluxfac, oneminus, grav, avogad;
+  // cloud optical properties (rrlw_cld: lwcldpr, rrtmg_lw_init.f90:2018-2656)
+  FArr absice0, absice1, absice2, absice3, absliq1;
+  double abscld1 = 0.0, absliq0 = 0.0;
 };
 extern LwTables g_lw;
 
@@ -30,6 +33,10 @@ struct LwInput {
   // cicewp / cliqwp (ncol, nlay) or null.
   int icld = 0;
   const double *cldfr = nullptr, *taucld = nullptr, *cicewp = nullptr, *cliqwp = nullptr;
+  // cloud physics (inflag = 1: abscld1 x water path; 2: ice and liquid
+  // parameterisations selected by iceflag / liqflag, radii reice / reliq)
+  int inflag = 0, iceflag = 0, liqflag = 0;
+  const double *reice = nullptr, *reliq = nullptr;
 };
 
 struct LwColumn {
@@ -46,7 +53,9 @@ struct LwColumn {
   std::vector<double> rat_h2oco2, rat_h2oco2_1, rat_h2oo3, rat_h2oo3_1, rat_h2on2o, rat_h2on2o_1,
       rat_h2och4, rat_h2och4_1, rat_n2oco2, rat_n2oco2_1, rat_o3co2, rat_o3co2_1;
   std::vector<double> taug[141], fracs[141], taut[141];
-  std::vector<double> cldfrac, taucloud[17];  // icld = 1: layer cloud fraction, cldprop's cloud optical depth
+  std::vector<double> cldfrac, taucloud[17];  // icld >= 1: layer cloud fraction, cldprop's cloud optical depth
+  int ncbands = 1;        // cldprop's number of cloud bands (1, 5 or 16), the last value it set
+  bool cld_error = false;  // cldprop stopped (an effective radius out of its table's range)
 
   void resize(int nl) {
     auto r = [&](std::vector<double>& v) { v.assign(nl + 2, 0.0); };

@@ -80,6 +80,14 @@ void sw_init(const Blob& blob, double cpdair) {
   T.heatfac = T.grav * 8.6400e4 / (cpdair * 1.e2);
   T.oneminus = 1.0 - 1.e-06;
   T.pi = 2. * std::asin(1.);
+  for (auto [f, name] : {std::pair<FArr*, const char*>{&T.extliq1, "extliq1"}, {&T.ssaliq1, "ssaliq1"},
+                         {&T.asyliq1, "asyliq1"}, {&T.extice2, "extice2"}, {&T.ssaice2, "ssaice2"},
+                         {&T.asyice2, "asyice2"}, {&T.extice3, "extice3"}, {&T.ssaice3, "ssaice3"},
+                         {&T.asyice3, "asyice3"}, {&T.fdlice3, "fdlice3"}, {&T.abari, "abari"},
+                         {&T.bbari, "bbari"}, {&T.cbari, "cbari"}, {&T.dbari, "dbari"}, {&T.ebari, "ebari"},
+                         {&T.fbari, "fbari"}})
+    *f = blob.r(std::string("swcld.") + name);
+  T.wavenum2 = blob.r("sw.wavenum2");
 }
 
 // exp(-x) through the SW lookup table with the reference's small-x series
@@ -896,25 +904,144 @@ void sw_spcvrt(SwColumn& c, double prmu0, const double* albdir, const double* al
   }
 }
 
-// cldprop_sw with inflag = 0 (rrtmg_sw_cldprop.f90:118-156): the optics of a
-// layer whose cover is >= cldmin and whose water path or band-summed depth is
-// >= cldmin (1e-20) are delta-M scaled with the forward-scattering fraction;
-// other layers keep taucloud = 0, ssacloud = 1, asmcloud = 0.
-static void sw_cldprop(const SwInput& in, int iplon, SwColumn& c) {
+// cldprop_sw, inflag = 2 (rrtmg_sw_cldprop.f90:158-340) for one layer whose
+// optics are formed: ice (Ebert-Curry coefficients by band limit, iceflag 1;
+// the STREAMER table, 2; Fu's table with its delta fractions, 3) and liquid
+// (Hu-Stamnes table, liqflag 1) extinction, single-scattering albedo and
+// asymmetry, each delta-M scaled, combined into the layer's delta-scaled
+// optics.  Returns false where the reference stops.
+static bool sw_cldprop_phys(const SwInput& in, double ciwp, double clwp, double radice, double radliq,
+                            double* taucloud, double* ssacloud, double* asmcloud) {
+  const SwTables& T = g_sw;
+  const double eps = 1.e-06, cldmin = 1.e-20;
+  double extcoice[30], ssacoice[30], gice[30], forwice[30], extcoliq[30], ssacoliq[30], gliq[30], forwliq[30];
+  auto ice_ok = [&](int ib) {
+    return !(extcoice[ib] < 0.0 || ssacoice[ib] > 1.0 || ssacoice[ib] < 0.0 || gice[ib] > 1.0 || gice[ib] < 0.0);
+  };
+  if (ciwp == 0.0) {
+    for (int ib = 16; ib <= 29; ++ib) extcoice[ib] = ssacoice[ib] = gice[ib] = forwice[ib] = 0.0;
+  } else if (in.iceflag == 1) {
+    if (radice < 13.0 || radice > 130.) return false;
+    for (int ib = 16; ib <= 29; ++ib) {
+      const double wn = T.wavenum2(ib - 15);
+      int icx = 5;
+      if (wn > 1.43e04) icx = 1;
+      else if (wn > 7.7e03) icx = 2;
+      else if (wn > 5.3e03) icx = 3;
+      else if (wn > 4.0e03) icx = 4;
+      extcoice[ib] = T.abari(icx) + T.bbari(icx) / radice;
+      ssacoice[ib] = 1. - T.cbari(icx) - T.dbari(icx) * radice;
+      gice[ib] = T.ebari(icx) + T.fbari(icx) * radice;
+      if (gice[ib] >= 1.0) gice[ib] = 1.0 - eps;
+      forwice[ib] = gice[ib] * gice[ib];
+      if (!ice_ok(ib)) return false;
+    }
+  } else if (in.iceflag == 2) {
+    if (radice < 5.0 || radice > 131.0) return false;
+    const double factor = (radice - 2.) / 3.;
+    int index = (int)factor;
+    if (index == 43) index = 42;
+    const double fint = factor - (double)index;
+    for (int ib = 16; ib <= 29; ++ib) {
+      extcoice[ib] = T.extice2(index, ib) + fint * (T.extice2(index + 1, ib) - T.extice2(index, ib));
+      ssacoice[ib] = T.ssaice2(index, ib) + fint * (T.ssaice2(index + 1, ib) - T.ssaice2(index, ib));
+      gice[ib] = T.asyice2(index, ib) + fint * (T.asyice2(index + 1, ib) - T.asyice2(index, ib));
+      forwice[ib] = gice[ib] * gice[ib];
+      if (!ice_ok(ib)) return false;
+    }
+  } else {
+    if (radice < 5.0 || radice > 140.0) return false;
+    const double factor = (radice - 2.) / 3.;
+    int index = (int)factor;
+    if (index == 46) index = 45;
+    const double fint = factor - (double)index;
+    for (int ib = 16; ib <= 29; ++ib) {
+      extcoice[ib] = T.extice3(index, ib) + fint * (T.extice3(index + 1, ib) - T.extice3(index, ib));
+      ssacoice[ib] = T.ssaice3(index, ib) + fint * (T.ssaice3(index + 1, ib) - T.ssaice3(index, ib));
+      gice[ib] = T.asyice3(index, ib) + fint * (T.asyice3(index + 1, ib) - T.asyice3(index, ib));
+      const double fdelta = T.fdlice3(index, ib) + fint * (T.fdlice3(index + 1, ib) - T.fdlice3(index, ib));
+      if (fdelta < 0.0 || fdelta > 1.0) return false;
+      forwice[ib] = fdelta + 0.5 / ssacoice[ib];
+      if (forwice[ib] > gice[ib]) forwice[ib] = gice[ib];
+      if (!ice_ok(ib)) return false;
+    }
+  }
+  if (clwp == 0.0) {
+    for (int ib = 16; ib <= 29; ++ib) extcoliq[ib] = ssacoliq[ib] = gliq[ib] = forwliq[ib] = 0.0;
+  } else {
+    if (radliq < 2.5 || radliq > 60.) return false;
+    int index = (int)(radliq - 1.5);
+    if (index == 0) index = 1;
+    if (index == 58) index = 57;
+    const double fint = radliq - 1.5 - (double)index;
+    for (int ib = 16; ib <= 29; ++ib) {
+      extcoliq[ib] = T.extliq1(index, ib) + fint * (T.extliq1(index + 1, ib) - T.extliq1(index, ib));
+      ssacoliq[ib] = T.ssaliq1(index, ib) + fint * (T.ssaliq1(index + 1, ib) - T.ssaliq1(index, ib));
+      if (fint < 0. && ssacoliq[ib] > 1.) ssacoliq[ib] = T.ssaliq1(index, ib);
+      gliq[ib] = T.asyliq1(index, ib) + fint * (T.asyliq1(index + 1, ib) - T.asyliq1(index, ib));
+      forwliq[ib] = gliq[ib] * gliq[ib];
+      if (extcoliq[ib] < 0.0 || ssacoliq[ib] > 1.0 || ssacoliq[ib] < 0.0 || gliq[ib] > 1.0 || gliq[ib] < 0.0)
+        return false;
+    }
+  }
+  for (int ib = 16; ib <= 29; ++ib) {
+    const double tauliqorig = clwp * extcoliq[ib];
+    const double tauiceorig = ciwp * extcoice[ib];
+    const double ssaliq = ssacoliq[ib] * (1.0 - forwliq[ib]) / (1.0 - forwliq[ib] * ssacoliq[ib]);
+    const double tauliq = (1.0 - forwliq[ib] * ssacoliq[ib]) * tauliqorig;
+    const double ssaice = ssacoice[ib] * (1.0 - forwice[ib]) / (1.0 - forwice[ib] * ssacoice[ib]);
+    const double tauice = (1.0 - forwice[ib] * ssacoice[ib]) * tauiceorig;
+    const double scatliq = ssaliq * tauliq;
+    double scatice = ssaice * tauice;
+    double tc = tauliq + tauice;
+    if (tc == 0.0) tc = cldmin;
+    if (scatice == 0.0) scatice = cldmin;
+    taucloud[ib - 16] = tc;
+    ssacloud[ib - 16] = (scatliq + scatice) / tc;
+    if (in.iceflag == 3)
+      asmcloud[ib - 16] = (1.0 / (scatliq + scatice)) *
+                          (scatliq * (gliq[ib] - forwliq[ib]) / (1.0 - forwliq[ib]) +
+                           scatice * ((gice[ib] - forwice[ib]) / (1.0 - forwice[ib])));
+    else
+      asmcloud[ib - 16] = (scatliq * (gliq[ib] - forwliq[ib]) / (1.0 - forwliq[ib]) +
+                           scatice * (gice[ib] - forwice[ib]) / (1.0 - forwice[ib])) /
+                          (scatliq + scatice);
+  }
+  return true;
+}
+
+// cldprop_sw (rrtmg_sw_cldprop.f90:118-340): the optics of a layer whose
+// cover is >= cldmin and whose water path or band-summed depth is >= cldmin
+// (1e-20) are formed -- with inflag = 0 the given optics delta-M scaled with
+// the forward-scattering fraction, with inflag = 2 by sw_cldprop_phys; other
+// layers keep taucloud = 0, ssacloud = 1, asmcloud = 0.  Returns false where
+// the reference stops.
+static bool sw_cldprop(const SwInput& in, int iplon, SwColumn& c) {
   const int nl = in.nlay, ncol = in.ncol;
   const double cldmin = 1.e-20;
   for (int lay = 1; lay <= nl; ++lay) {
     const size_t o = (size_t)iplon + (size_t)ncol * (size_t)(lay - 1);
     c.pclfr[lay] = in.cldfr[o];
     double tauctot = 0.0;
-    for (int n = 0; n < 14; ++n) tauctot = tauctot + in.taucld[(size_t)n + 14 * o];
-    const double cwp = (in.cicewp ? in.cicewp[o] : 0.0) + (in.cliqwp ? in.cliqwp[o] : 0.0);
+    for (int n = 0; n < 14; ++n) tauctot = tauctot + (in.taucld ? in.taucld[(size_t)n + 14 * o] : 0.0);
+    const double ciwp = in.cicewp ? in.cicewp[o] : 0.0, clwp = in.cliqwp ? in.cliqwp[o] : 0.0;
+    const double cwp = ciwp + clwp;
     for (int ibm = 1; ibm <= 14; ++ibm) {
       c.ptauc[ibm][lay] = 0.0;
       c.pomgc[ibm][lay] = 1.0;
       c.pasyc[ibm][lay] = 0.0;
     }
-    if (c.pclfr[lay] >= cldmin && (cwp >= cldmin || tauctot >= cldmin)) {
+    if (c.pclfr[lay] >= cldmin && (cwp >= cldmin || tauctot >= cldmin) && in.inflag == 2) {
+      double tc[14], ssa[14], asm_[14];
+      if (!sw_cldprop_phys(in, ciwp, clwp, in.reice ? in.reice[o] : 0.0, in.reliq ? in.reliq[o] : 0.0, tc, ssa,
+                           asm_))
+        return false;
+      for (int ibm = 1; ibm <= 14; ++ibm) {
+        c.ptauc[ibm][lay] = tc[ibm - 1];
+        c.pomgc[ibm][lay] = ssa[ibm - 1];
+        c.pasyc[ibm][lay] = asm_[ibm - 1];
+      }
+    } else if (c.pclfr[lay] >= cldmin && (cwp >= cldmin || tauctot >= cldmin)) {
       for (int ibm = 1; ibm <= 14; ++ibm) {
         const size_t q = (size_t)(ibm - 1) + 14 * o;
         const double taucldorig_a = in.taucld[q];
@@ -927,12 +1054,14 @@ static void sw_cldprop(const SwInput& in, int iplon, SwColumn& c) {
       }
     }
   }
+  return true;
 }
 
-bool sw_column(const SwInput& in, int iplon, SwColumn& c, SwOut& out, bool* partial) {
+bool sw_column(const SwInput& in, int iplon, SwColumn& c, SwOut& out, bool* partial, bool* stopped) {
   const double zepzen = 1.e-10;
   int nl = in.nlay;
   if (partial) *partial = false;
+  if (stopped) *stopped = false;
   if (in.coszen[iplon] < zepzen) {
     out.fu.assign(nl + 2, 0.);
     out.fd.assign(nl + 2, 0.);
@@ -950,7 +1079,7 @@ bool sw_column(const SwInput& in, int iplon, SwColumn& c, SwOut& out, bool* part
       const double f = in.cldfr[(size_t)iplon + (size_t)in.ncol * (size_t)(i - 1)];
       if (f > zepsec && f < oneminus && partial) *partial = true;
     }
-    sw_cldprop(in, iplon, c);
+    if (!sw_cldprop(in, iplon, c) && stopped) *stopped = true;
   }
   sw_setcoef(c);
   double cossza = in.coszen[iplon];

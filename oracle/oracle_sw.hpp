@@ -16,6 +16,10 @@ struct SwTables {
   int ngc[30], ngs[30], nspa[30], nspb[30];
   double exp_tbl[10001];
   double bpade, heatfac, oneminus, grav, avogad, pi;
+  // cloud optical properties (rrsw_cld: swcldpr, rrtmg_sw_init.f90:1519-3341)
+  // and the band limits (wavenum2) that select the Ebert-Curry coefficients
+  FArr extliq1, ssaliq1, asyliq1, extice2, ssaice2, asyice2, extice3, ssaice3, asyice3, fdlice3;
+  FArr abari, bbari, cbari, dbari, ebari, fbari, wavenum2;
 };
 extern SwTables g_sw;
 
@@ -32,6 +36,10 @@ struct SwInput {
   int icld = 0;
   const double *cldfr = nullptr, *taucld = nullptr, *ssacld = nullptr, *asmcld = nullptr, *fsfcld = nullptr,
                *cicewp = nullptr, *cliqwp = nullptr;
+  // cloud physics (inflag = 2: ice and liquid parameterisations selected by
+  // iceflag (1..3) and liqflag (1), effective sizes reice / reliq)
+  int inflag = 0, iceflag = 0, liqflag = 0;
+  const double *reice = nullptr, *reliq = nullptr;
 };
 
 struct SwColumn {
@@ -88,6 +96,9 @@ void sw_spcvrt(SwColumn& c, double prmu0, const double* albdir, const double* al
 // Returns false for a dark column (no SW); sets *partial when the column holds
 // a partly cloudy layer, which the reference's non-McICA SW refuses
 // (rrtmg_sw_rad.nomcica.f90:533-538).
-bool sw_column(const SwInput& in, int iplon, SwColumn& c, SwOut& out, bool* partial = nullptr);
+// *stopped: cldprop_sw stopped for this column (a size out of range or an
+// optical property out of its physical range).
+bool sw_column(const SwInput& in, int iplon, SwColumn& c, SwOut& out, bool* partial = nullptr,
+               bool* stopped = nullptr);
 
 }  // namespace orc

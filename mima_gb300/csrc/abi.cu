@@ -51,6 +51,7 @@ struct rrtmg_gpu_state {
   // FP32 LW transmittance and tau transition function side by side (one
   // gather per table lookup in the split LW solver)
   float2* lw_exptfn32 = nullptr;
+  double* cldtab = nullptr;  // cloud optical property tables (ct:: offsets)
   unsigned* flags = nullptr;
   DevBuf lw_ws, sw_ws, adj_ws;
   // host-pointer calls: a second stream and per-stream staging and scratch, so
@@ -146,9 +147,11 @@ struct Carver {
 };
 
 // cloudy: also the per-layer cloud fields and the clear-sky band partials
-// (icld >= 1), and with maximum/random overlap (icld = 2, 3) the overlap
-// factors; clear-sky calls carve none of them.
-LwWork carve_lw(void* base, int ncol, int nlay, size_t* bytes, bool cloudy = false, bool maxrand = false) {
+// (icld >= 1), with maximum/random overlap (icld = 2, 3) the overlap factors,
+// and with cloud physics (inflag 1 / 2) the formed cloud depths; clear-sky
+// calls carve none of them.
+LwWork carve_lw(void* base, int ncol, int nlay, size_t* bytes, bool cloudy = false, bool maxrand = false,
+                bool phys = false) {
   Carver c{(char*)base};
   const size_t N = (size_t)ncol, L = (size_t)nlay;
   LwWork w{};
@@ -170,12 +173,13 @@ LwWork carve_lw(void* base, int ncol, int nlay, size_t* bytes, bool cloudy = fal
     w.bdc = c.take<double>(kLwSlots * (L + 1) * N);
     w.bduc = c.take<double>(kLwSlots * (L + 1) * N);
     if (maxrand) w.ovl = c.take<double>(12 * L * N);
+    if (phys) w.odc = c.take<double>(16 * L * N);
   }
   if (bytes) *bytes = c.off;
   return w;
 }
 
-SwWork carve_sw(void* base, int ncol, int nlay, size_t* bytes, bool cloudy = false) {
+SwWork carve_sw(void* base, int ncol, int nlay, size_t* bytes, bool cloudy = false, bool phys = false) {
   Carver c{(char*)base};
   const size_t N = (size_t)ncol, L = (size_t)nlay;
   SwWork w{};
@@ -189,6 +193,7 @@ SwWork carve_sw(void* base, int ncol, int nlay, size_t* bytes, bool cloudy = fal
     w.cld = c.take<double>(2 * L * N);
     w.suc = c.take<double>(kSwSlots * (L + 1) * N);
     w.sdc = c.take<double>(kSwSlots * (L + 1) * N);
+    if (phys) w.cldopt = c.take<double>(3 * 14 * L * N);
   }
   if (bytes) *bytes = c.off;
   return w;
@@ -208,11 +213,11 @@ int check_dims(rrtmg_gpu_state* h, int ncol, int nlay) {
 template <class F>
 LwWorkT<F> work_as(const LwWork& w) {
   return LwWorkT<F>{w.idx, (F*)w.f, (F*)w.planklay, (F*)w.planklev, (F*)w.plankbnd, (F*)w.dplankbnd, (F*)w.secdiff,
-                    w.laytrop, w.bu, w.bd, w.bdu, w.colsum, (F*)w.cld, w.buc, w.bdc, w.bduc, (F*)w.ovl};
+                    w.laytrop, w.bu, w.bd, w.bdu, w.colsum, (F*)w.cld, w.buc, w.bdc, w.bduc, (F*)w.ovl, w.odc};
 }
 template <class F>
 SwWorkT<F> work_as(const SwWork& w) {
-  return SwWorkT<F>{w.idx, (F*)w.f, w.laytrop, w.laysolfr, w.su, w.sd, (F*)w.cld, w.suc, w.sdc};
+  return SwWorkT<F>{w.idx, (F*)w.f, w.laytrop, w.laysolfr, w.su, w.sd, (F*)w.cld, w.suc, w.sdc, w.cldopt};
 }
 template <class F>
 LwPrepT<F> prep_of(const LwWorkT<F>& w) {
@@ -241,31 +246,41 @@ int lw_enqueue(rrtmg_gpu_state* h, cudaStream_t s, void* base, int ncol, int nla
   // clouds (icld >= 1): the call carries cloud arrays; icld = 2, 3:
   // maximum/random overlap with its overlap factors
   const bool cloudy = in.cldfr != nullptr, maxrand = cloudy && in.icld >= 2;
-  LwWork w = carve_lw(base, ncol, nlay, nullptr, cloudy, maxrand);
+  // cloud physics (inflag 1 / 2): the depths are formed on the device, after
+  // prep (they carry secdiff), and handed to the solver in place of taucld
+  const bool phys = cloudy && in.inflag != 0;
+  LwWork w = carve_lw(base, ncol, nlay, nullptr, cloudy, maxrand, phys);
+  const double* taucld = phys ? w.odc : in.taucld;
   mark(h, 0, 0, s);
   const int nb = h->precision == RRTMG_PREC_SPLIT ? lw_slot_blocks(ncol) : lw_gpoint_blocks(h->host.lw, ncol);
   if (h->precision == RRTMG_PREC_SPLIT) {
     const LwWorkT<float> w32 = work_as<float>(w);
     launch_lw_prep_split(in, w32, h->totplnk32, h->totplnkderiv32, ncol, nlay, idrv, h->flags, s);
-    if (cloudy) launch_lw_cloud_split(in, w32.cld, ncol, nlay, s);
+    if (phys)
+      launch_lw_cldphys_split(in, w32.secdiff, h->cldtab, w32.cld, w.odc, ncol, nlay, h->flags, s);
+    else if (cloudy)
+      launch_lw_cloud_split(in, w32.cld, ncol, nlay, s);
     if (maxrand) launch_lw_overlap_split(in.cldfr, w32.ovl, ncol, nlay, s);
     mark(h, 0, 1, s);
     if (cloudy)
-      launch_lw_gpoint_cld_split(prep_of(w32), w32.cld, in.taucld, in.emis, in.tauaer, h->lw_tab32, h->lw_exp32,
+      launch_lw_gpoint_cld_split(prep_of(w32), w32.cld, taucld, in.emis, in.tauaer, h->lw_tab32, h->lw_exp32,
                                  h->lw_tfn32, h->lw_tau32, w.bu, w.bd, w.bdu, w.buc, w.bdc, w.bduc, ncol, nlay, idrv,
-                                 nb, h->analytic, s, w32.ovl);
+                                 nb, h->analytic, s, w32.ovl, phys);
     else
       launch_lw_gpoint_split(prep_of(w32), in.emis, in.tauaer, h->lw_tab32, h->lw_exptfn32, w.bu, w.bd,
                              w.bdu, ncol, nlay, idrv, nb, h->analytic, s);
   } else {
     launch_lw_prep(in, w, h->totplnk, h->totplnkderiv, ncol, nlay, idrv, h->flags, s);
-    if (cloudy) launch_lw_cloud(in, w.cld, ncol, nlay, s);
+    if (phys)
+      launch_lw_cldphys(in, w.secdiff, h->cldtab, w.cld, w.odc, ncol, nlay, h->flags, s);
+    else if (cloudy)
+      launch_lw_cloud(in, w.cld, ncol, nlay, s);
     if (maxrand) launch_lw_overlap(in.cldfr, w.ovl, ncol, nlay, s);
     mark(h, 0, 1, s);
     if (cloudy)
-      launch_lw_gpoint_cld_fp64(prep_of(w), w.cld, in.taucld, in.emis, in.tauaer, h->lw_tab64, h->lw_exp64,
+      launch_lw_gpoint_cld_fp64(prep_of(w), w.cld, taucld, in.emis, in.tauaer, h->lw_tab64, h->lw_exp64,
                                 h->lw_tfn64, h->lw_tau64, w.bu, w.bd, w.bdu, w.buc, w.bdc, w.bduc, ncol, nlay, idrv,
-                                nb, h->analytic, s, w.ovl);
+                                nb, h->analytic, s, w.ovl, phys);
     else
       launch_lw_gpoint_fp64(prep_of(w), in.emis, in.tauaer, h->lw_tab64, h->lw_exp64, h->lw_tfn64, w.bu, w.bd, w.bdu,
                             ncol, nlay, idrv, nb, h->analytic, s);
@@ -287,24 +302,34 @@ int lw_enqueue(rrtmg_gpu_state* h, cudaStream_t s, void* base, int ncol, int nla
 int lw_run(rrtmg_gpu_state* h, cudaStream_t s, int ncol, int nlay, int idrv, const LwIn& in, double* uflx,
            double* dflx, double* hr, double* uflxc, double* dflxc, double* hrc, double* duflx_dt, double* duflxc_dt) {
   size_t need;
-  carve_lw(nullptr, ncol, nlay, &need, in.cldfr != nullptr, in.cldfr != nullptr && in.icld >= 2);
+  carve_lw(nullptr, ncol, nlay, &need, in.cldfr != nullptr, in.cldfr != nullptr && in.icld >= 2,
+           in.cldfr != nullptr && in.inflag != 0);
   int rc = ensure(h, h->lw_ws, need, s);
   if (rc) return rc;
   return lw_enqueue(h, s, h->lw_ws.p, ncol, nlay, idrv, in, uflx, dflx, hr, uflxc, dflxc, hrc, duflx_dt, duflxc_dt);
 }
 
-// Cloud arguments of the LW calls: icld = 0 (clear sky), or clouds with the
-// cloud optical depths given (inflglw = 0, rrtmg_lw_cldprop.f90:165-171):
+// Cloud arguments of the LW calls: icld = 0 (clear sky), or clouds with
 // icld = 1 random overlap (rrtmg_lw_rtrn.f90), icld = 2 / 3 maximum/random
 // overlap (rrtmg_lw_rtrnmr.f90; the non-McICA driver routes both there,
-// rrtmg_lw_rad.nomcica.f90:527-541).  The cloud-physics options
-// inflglw = 1 / 2 are not computed.
-int lw_cloud_args(rrtmg_gpu_state* h, int icld, int inflglw, const double* cldfr, const double* taucld) {
+// rrtmg_lw_rad.nomcica.f90:527-541).  cldprop's options
+// (rrtmg_lw_cldprop.f90:155-270): inflglw = 0 optical depths given (taucld);
+// 1 abscld1 x water path (cicewp, cliqwp); 2 ice (iceflglw 0-3) and liquid
+// (liqflglw 0-1) parameterisations with the water paths and effective sizes
+// (reice, reliq).
+int lw_cloud_args(rrtmg_gpu_state* h, int icld, int inflglw, int iceflglw, int liqflglw, const double* cldfr,
+                  const double* taucld, const double* cicewp, const double* cliqwp, const double* reice,
+                  const double* reliq) {
   if (icld == 0) return RRTMG_OK;
   if (icld < 0 || icld > 3) return fail(h, RRTMG_ERR_UNSUPPORTED, "icld must be in [0, 3]");
-  if (inflglw != 0)
-    return fail(h, RRTMG_ERR_UNSUPPORTED, "LW clouds: only given cloud optical depths (inflglw = 0) are computed");
-  if (!cldfr || !taucld) return fail(h, RRTMG_ERR_ARG, "LW clouds need cldfr and taucld");
+  if (inflglw < 0 || inflglw > 2) return fail(h, RRTMG_ERR_UNSUPPORTED, "inflglw must be in [0, 2]");
+  if (inflglw == 2 && (iceflglw < 0 || iceflglw > 3 || liqflglw < 0 || liqflglw > 1))
+    return fail(h, RRTMG_ERR_UNSUPPORTED, "LW cloud physics: iceflglw must be in [0, 3] and liqflglw in [0, 1]");
+  if (!cldfr) return fail(h, RRTMG_ERR_ARG, "LW clouds need cldfr");
+  if (inflglw == 0 && !taucld) return fail(h, RRTMG_ERR_ARG, "LW clouds with inflglw = 0 need taucld");
+  if (inflglw >= 1 && (!cicewp || !cliqwp))
+    return fail(h, RRTMG_ERR_ARG, "LW cloud physics needs cicewp and cliqwp");
+  if (inflglw == 2 && (!reice || !reliq)) return fail(h, RRTMG_ERR_ARG, "LW cloud physics needs reice and reliq");
   return RRTMG_OK;
 }
 
@@ -313,16 +338,24 @@ int lw_cloud_args(rrtmg_gpu_state* h, int icld, int inflglw, const double* cldfr
 // McICA the reference computes clear and overcast layers only (a partly
 // cloudy layer stops it, rrtmg_sw_rad.nomcica.f90:533-538): icld = 1, 2 and 3
 // are the same there, so all three are taken; such a layer is reported by the
-// kernels as invalid input.  The cloud-physics options inflgsw = 1 / 2 are not
-// computed.
-int sw_cloud_args(rrtmg_gpu_state* h, int icld, int inflgsw, const double* cldfr, const double* taucld,
-                  const double* ssacld, const double* asmcld, const double* fsfcld) {
+// kernels as invalid input.  cldprop_sw's options (rrtmg_sw_cldprop.f90:40,
+// 118-340): inflgsw = 0 optics given; 2 ice (iceflgsw 1-3) and liquid
+// (liqflgsw 1) parameterisations with the water paths and effective sizes.
+// The reference's cldprop_sw has no branch for the others (inflgsw = 1 leaves
+// its layers without cloud optics); they are refused.
+int sw_cloud_args(rrtmg_gpu_state* h, int icld, int inflgsw, int iceflgsw, int liqflgsw, const double* cldfr,
+                  const double* taucld, const double* ssacld, const double* asmcld, const double* fsfcld,
+                  const double* cicewp, const double* cliqwp, const double* reice, const double* reliq) {
   if (icld == 0) return RRTMG_OK;
   if (icld < 0 || icld > 3) return fail(h, RRTMG_ERR_UNSUPPORTED, "icld must be in [0, 3]");
-  if (inflgsw != 0)
-    return fail(h, RRTMG_ERR_UNSUPPORTED, "SW clouds: only given cloud optics (inflgsw = 0) are computed");
-  if (!cldfr || !taucld || !ssacld || !asmcld || !fsfcld)
-    return fail(h, RRTMG_ERR_ARG, "SW clouds need cldfr, taucld, ssacld, asmcld and fsfcld");
+  if (inflgsw != 0 && inflgsw != 2) return fail(h, RRTMG_ERR_UNSUPPORTED, "inflgsw must be 0 or 2");
+  if (inflgsw == 2 && (iceflgsw < 1 || iceflgsw > 3 || liqflgsw != 1))
+    return fail(h, RRTMG_ERR_UNSUPPORTED, "SW cloud physics: iceflgsw must be in [1, 3] and liqflgsw 1");
+  if (!cldfr) return fail(h, RRTMG_ERR_ARG, "SW clouds need cldfr");
+  if (inflgsw == 0 && (!taucld || !ssacld || !asmcld || !fsfcld))
+    return fail(h, RRTMG_ERR_ARG, "SW clouds with inflgsw = 0 need taucld, ssacld, asmcld and fsfcld");
+  if (inflgsw == 2 && (!cicewp || !cliqwp || !reice || !reliq))
+    return fail(h, RRTMG_ERR_ARG, "SW cloud physics needs cicewp, cliqwp, reice and reliq");
   return RRTMG_OK;
 }
 
@@ -344,7 +377,19 @@ int sw_enqueue(rrtmg_gpu_state* h, cudaStream_t s, void* base, int ncol, int nla
   // clouds (icld = 1): a clear-sky pass into the clear partials (suc, sdc) and
   // a total-sky pass into su, sd, as the reference's two two-stream passes
   const bool cloudy = in.cldfr != nullptr;
-  SwWork w = carve_sw(base, ncol, nlay, nullptr, cloudy);
+  // cloud physics (inflag = 2): the cloud kernel forms the optics, which the
+  // total-sky pass reads in place of the given ones (no forward fraction: they
+  // are delta-scaled already)
+  const bool phys = cloudy && in.inflag == 2;
+  SwWork w = carve_sw(base, ncol, nlay, nullptr, cloudy, phys);
+  SwIn tin = in;
+  if (phys) {
+    const size_t S = (size_t)14 * nlay * ncol;
+    tin.taucld = w.cldopt;
+    tin.ssacld = w.cldopt + S;
+    tin.asmcld = w.cldopt + 2 * S;
+    tin.fsfcld = nullptr;
+  }
   const double adjflux = adjflux_of(h, adjes, dyofyr, scon);
   const int nb = h->precision == RRTMG_PREC_SPLIT ? sw_slot_blocks(ncol) : sw_gpoint_blocks(h->host.sw, ncol);
   double* cu = cloudy ? w.suc : w.su;
@@ -353,21 +398,21 @@ int sw_enqueue(rrtmg_gpu_state* h, cudaStream_t s, void* base, int ncol, int nla
   if (h->precision == RRTMG_PREC_SPLIT) {
     const SwWorkT<float> w32 = work_as<float>(w);
     launch_sw_prep_split(in, w32, ncol, nlay, h->flags, s);
-    if (cloudy) launch_sw_cloud_split(in, w32.cld, ncol, nlay, h->flags, s);
+    if (cloudy) launch_sw_cloud_split(in, w32.cld, ncol, nlay, h->flags, s, h->cldtab, w.cldopt);
     mark(h, 1, 1, s);
     launch_sw_gpoint_split(prep_of(w32), in, adjflux, iaer, h->sw_tab32, h->sw_tab64, h->sw_exp32, cu, cd, ncol,
                            nlay, nb, h->analytic, s);
     if (cloudy)
-      launch_sw_gpoint_split(prep_of(w32), in, adjflux, iaer, h->sw_tab32, h->sw_tab64, h->sw_exp32, w.su, w.sd,
+      launch_sw_gpoint_split(prep_of(w32), tin, adjflux, iaer, h->sw_tab32, h->sw_tab64, h->sw_exp32, w.su, w.sd,
                              ncol, nlay, nb, h->analytic, s, w32.cld);
   } else {
     launch_sw_prep(in, w, ncol, nlay, h->flags, s);
-    if (cloudy) launch_sw_cloud(in, w.cld, ncol, nlay, h->flags, s);
+    if (cloudy) launch_sw_cloud(in, w.cld, ncol, nlay, h->flags, s, h->cldtab, w.cldopt);
     mark(h, 1, 1, s);
     launch_sw_gpoint_fp64(prep_of(w), in, adjflux, iaer, h->sw_tab64, h->sw_exp64, cu, cd, ncol, nlay, nb,
                           h->analytic, s);
     if (cloudy)
-      launch_sw_gpoint_fp64(prep_of(w), in, adjflux, iaer, h->sw_tab64, h->sw_exp64, w.su, w.sd, ncol, nlay, nb,
+      launch_sw_gpoint_fp64(prep_of(w), tin, adjflux, iaer, h->sw_tab64, h->sw_exp64, w.su, w.sd, ncol, nlay, nb,
                             h->analytic, s, w.cld);
   }
   mark(h, 1, 2, s);
@@ -388,7 +433,7 @@ int sw_run(rrtmg_gpu_state* h, cudaStream_t s, int ncol, int nlay, int iaer, dou
            const SwIn& in, double* swuflx, double* swdflx, double* swhr, double* swuflxc, double* swdflxc,
            double* swhrc) {
   size_t need;
-  carve_sw(nullptr, ncol, nlay, &need, in.cldfr != nullptr);
+  carve_sw(nullptr, ncol, nlay, &need, in.cldfr != nullptr, in.cldfr != nullptr && in.inflag == 2);
   int rc = ensure(h, h->sw_ws, need, s);
   if (rc) return rc;
   return sw_enqueue(h, s, h->sw_ws.p, ncol, nlay, iaer, adjes, dyofyr, scon, in, swuflx, swdflx, swhr, swuflxc,
@@ -612,6 +657,10 @@ int read_flags(rrtmg_gpu_state* h, cudaStream_t s) {
     cudaStreamSynchronize(s);
     if (f & 1u)
       return fail(h, RRTMG_ERR_INPUT, "non-finite or out-of-range input (pressure <= 0, T <= 0, q outside [0,1), NaN/Inf)");
+    if (f & 4u)
+      return fail(h, RRTMG_ERR_INPUT,
+                  "clouds: an effective size outside its parameterisation's range, or a cloud optical property "
+                  "outside its physical range (cldprop / cldprop_sw stop)");
     return fail(h, RRTMG_ERR_INPUT, "SW clouds: a partly cloudy layer (1e-6 < cldfr < 1 - 1e-6) needs McICA");
   }
   return RRTMG_OK;
@@ -627,8 +676,8 @@ const char* rrtmg_gpu_error_string(int status) {
     case RRTMG_OK: return "success";
     case RRTMG_ERR_ARG: return "invalid argument";
     case RRTMG_ERR_UNSUPPORTED:
-      return "unsupported configuration (icld 0-3 with given cloud optics, SW clear or overcast layers, iaer 0/10, "
-             "idrv 0/1)";
+      return "unsupported configuration (icld 0-3; LW inflglw 0-2, iceflglw 0-3, liqflglw 0-1; SW inflgsw 0 or 2, "
+             "iceflgsw 1-3, liqflgsw 1, clear or overcast layers; iaer 0/10; idrv 0/1)";
     case RRTMG_ERR_CUDA: return "CUDA error";
     case RRTMG_ERR_TABLES: return "coefficient table blob missing or invalid";
     case RRTMG_ERR_INPUT: return "invalid input values";
@@ -679,6 +728,7 @@ int rrtmg_gpu_init(double cpdair, const char* table_blob, int device, rrtmg_gpu_
   if (e == cudaSuccess) e = upload(&h->lw_tfn32, to_f32(h->host.lw_tfn));
   if (e == cudaSuccess) e = upload(&h->lw_exptfn32, interleave_f32(h->host.lw_exp, h->host.lw_tfn));
   if (e == cudaSuccess) e = upload(&h->sw_exp32, to_f32(h->host.sw_exp));
+  if (e == cudaSuccess) e = upload(&h->cldtab, h->host.cld);
   if (e == cudaSuccess) e = cudaMalloc((void**)&h->flags, sizeof(unsigned));
   if (e == cudaSuccess) e = cudaMemset(h->flags, 0, sizeof(unsigned));
   if (e == cudaSuccess) e = upload_constants_fp64(h->host.lw, h->host.sw);
@@ -705,7 +755,7 @@ int rrtmg_gpu_finalize(rrtmg_gpu_handle h) {
   void* ptrs[] = {h->lw_tab64, h->sw_tab64, h->lw_exp64, h->lw_tfn64, h->sw_exp64, h->totplnk, h->totplnkderiv,
                   h->lw_tau64, h->lw_tau32,
                   h->totplnk32, h->totplnkderiv32,
-                  h->lw_tab32, h->sw_tab32, h->lw_exp32, h->lw_tfn32, h->lw_exptfn32, h->sw_exp32, h->flags,
+                  h->lw_tab32, h->sw_tab32, h->lw_exp32, h->lw_tfn32, h->lw_exptfn32, h->sw_exp32, h->cldtab, h->flags,
                   h->lw_ws.p,
                   h->sw_ws.p, h->adj_ws.p, h->hio[0].p, h->hio[1].p, h->hws[0].p, h->hws[1].p, h->run_ws.p,
                   h->run_cio[0].p, h->run_cio[1].p, h->run_cws[0].p, h->run_cws[1].p};
@@ -792,11 +842,10 @@ int rrtmg_lw_dev(rrtmg_gpu_handle h, void* stream, int ncol, int nlay, int icld,
                  const double* cldfr, const double* taucld, const double* cicewp, const double* cliqwp,
                  const double* reice, const double* reliq, const double* tauaer, double* uflx, double* dflx,
                  double* hr, double* uflxc, double* dflxc, double* hrc, double* duflx_dt, double* duflxc_dt) {
-  (void)iceflglw; (void)liqflglw; (void)reice; (void)reliq;
   if (!valid_handle(h)) return RRTMG_ERR_ARG;
   int rc = check_dims(h, ncol, nlay);
   if (rc) return rc;
-  rc = lw_cloud_args(h, icld, inflglw, cldfr, taucld);
+  rc = lw_cloud_args(h, icld, inflglw, iceflglw, liqflglw, cldfr, taucld, cicewp, cliqwp, reice, reliq);
   if (rc) return rc;
   if (idrv != 0 && idrv != 1) return fail(h, RRTMG_ERR_UNSUPPORTED, "idrv must be 0 or 1");
   if (!play || !plev || !tlay || !tlev || !tsfc || !h2ovmr || !o3vmr || !co2vmr || !uflx || !dflx || !hr ||
@@ -812,6 +861,11 @@ int rrtmg_lw_dev(rrtmg_gpu_handle h, void* stream, int ncol, int nlay, int icld,
     in.cicewp = cicewp;
     in.cliqwp = cliqwp;
     in.icld = icld;
+    in.inflag = inflglw;
+    in.iceflag = iceflglw;
+    in.liqflag = liqflglw;
+    in.reice = reice;
+    in.reliq = reliq;
   }
   return lw_run(h, (cudaStream_t)stream, ncol, nlay, idrv, in, uflx, dflx, hr, uflxc, dflxc, hrc, duflx_dt,
                 duflxc_dt);
@@ -827,11 +881,12 @@ int rrtmg_sw_dev(rrtmg_gpu_handle h, void* stream, int ncol, int nlay, int icld,
                  const double* reice, const double* reliq, const double* tauaer, const double* ssaaer,
                  const double* asmaer, const double* ecaer, double* swuflx, double* swdflx, double* swhr,
                  double* swuflxc, double* swdflxc, double* swhrc) {
-  (void)iceflgsw; (void)liqflgsw; (void)reice; (void)reliq; (void)ecaer;
+  (void)ecaer;
   if (!valid_handle(h)) return RRTMG_ERR_ARG;
   int rc = check_dims(h, ncol, nlay);
   if (rc) return rc;
-  rc = sw_cloud_args(h, icld, inflgsw, cldfr, taucld, ssacld, asmcld, fsfcld);
+  rc = sw_cloud_args(h, icld, inflgsw, iceflgsw, liqflgsw, cldfr, taucld, ssacld, asmcld, fsfcld, cicewp, cliqwp,
+                     reice, reliq);
   if (rc) return rc;
   if (iaer != 0 && iaer != 10) return fail(h, RRTMG_ERR_UNSUPPORTED, "iaer must be 0 or 10");
   if (!play || !plev || !tlay || !tlev || !tsfc || !h2ovmr || !o3vmr || !co2vmr || !asdir || !asdif || !aldir ||
@@ -850,6 +905,11 @@ int rrtmg_sw_dev(rrtmg_gpu_handle h, void* stream, int ncol, int nlay, int icld,
     in.fsfcld = fsfcld;
     in.cicewp = cicewp;
     in.cliqwp = cliqwp;
+    in.inflag = inflgsw;
+    in.iceflag = iceflgsw;
+    in.liqflag = liqflgsw;
+    in.reice = reice;
+    in.reliq = reliq;
   }
   return sw_run(h, (cudaStream_t)stream, ncol, nlay, iaer, adjes, dyofyr, scon, in, swuflx, swdflx, swhr, swuflxc,
                 swdflxc, swhrc);
@@ -959,11 +1019,10 @@ int rrtmg_lw_c(rrtmg_gpu_handle h, int ncol, int nlay, int icld, int idrv, const
                const double* cicewp, const double* cliqwp, const double* reice, const double* reliq,
                const double* tauaer, double* uflx, double* dflx, double* hr, double* uflxc, double* dflxc,
                double* hrc, double* duflx_dt, double* duflxc_dt) {
-  (void)iceflglw; (void)liqflglw; (void)reice; (void)reliq;
   if (!valid_handle(h)) return RRTMG_ERR_ARG;
   int rc = check_dims(h, ncol, nlay);
   if (rc) return rc;
-  rc = lw_cloud_args(h, icld, inflglw, cldfr, taucld);
+  rc = lw_cloud_args(h, icld, inflglw, iceflglw, liqflglw, cldfr, taucld, cicewp, cliqwp, reice, reliq);
   if (rc) return rc;
   if (idrv != 0 && idrv != 1) return fail(h, RRTMG_ERR_UNSUPPORTED, "idrv must be 0 or 1");
   if (!play || !plev || !tlay || !tlev || !tsfc || !h2ovmr || !o3vmr || !co2vmr || !uflx || !dflx || !hr ||
@@ -971,26 +1030,34 @@ int rrtmg_lw_c(rrtmg_gpu_handle h, int ncol, int nlay, int icld, int idrv, const
     return fail(h, RRTMG_ERR_ARG, "a required array pointer is null");
   if (idrv == 1 && !duflx_dt) return fail(h, RRTMG_ERR_ARG, "idrv = 1 needs duflx_dt");
   cudaSetDevice(h->device);
-  const bool cloudy = icld != 0;
+  const bool cloudy = icld != 0, phys2 = cloudy && inflglw == 2;
   const size_t L = nlay, Lv = nlay + 1;
-  const HostIn in[21] = {{play, L}, {plev, Lv}, {tlay, L}, {tlev, Lv}, {tsfc, 1}, {h2ovmr, L}, {o3vmr, L},
+  const HostIn in[23] = {{play, L}, {plev, Lv}, {tlay, L}, {tlev, Lv}, {tsfc, 1}, {h2ovmr, L}, {o3vmr, L},
                          {co2vmr, L}, {ch4vmr, L}, {n2ovmr, L}, {o2vmr, L}, {cfc11vmr, L}, {cfc12vmr, L},
                          {cfc22vmr, L}, {ccl4vmr, L}, {emis, 16}, {tauaer, 16 * L},
                          {cloudy ? cldfr : nullptr, L}, {cloudy ? taucld : nullptr, L, 16},
-                         {cloudy ? cicewp : nullptr, L}, {cloudy ? cliqwp : nullptr, L}};
+                         {cloudy ? cicewp : nullptr, L}, {cloudy ? cliqwp : nullptr, L},
+                         {phys2 ? reice : nullptr, L}, {phys2 ? reliq : nullptr, L}};
   const HostOut out[8] = {{uflx, Lv}, {dflx, Lv}, {hr, L}, {uflxc, Lv}, {dflxc, Lv}, {hrc, L},
                           {idrv == 1 ? duflx_dt : nullptr, Lv}, {idrv == 1 ? duflxc_dt : nullptr, Lv}};
   auto need = [&](int nc) {
     size_t b;
-    carve_lw(nullptr, nc, nlay, &b, cloudy, icld >= 2);
+    carve_lw(nullptr, nc, nlay, &b, cloudy, icld >= 2, cloudy && inflglw != 0);
     return b;
   };
   auto enq = [&](cudaStream_t s, void* ws, int nc, const double* const* d, double* const* o) {
     LwIn li{d[0],  d[1],  d[2],  d[3],  d[4],  d[5],  d[6],  d[7],  d[8],  d[9], d[10],
             d[11], d[12], d[13], d[14], d[15], d[16], d[17], d[18], d[19], d[20], icld};
+    if (cloudy) {
+      li.inflag = inflglw;
+      li.iceflag = iceflglw;
+      li.liqflag = liqflglw;
+      li.reice = d[21];
+      li.reliq = d[22];
+    }
     return lw_enqueue(h, s, ws, nc, nlay, idrv, li, o[0], o[1], o[2], o[3], o[4], o[5], o[6], o[7]);
   };
-  return host_call(h, ncol, in, 21, out, 8, need, enq, "copy LW arrays");
+  return host_call(h, ncol, in, 23, out, 8, need, enq, "copy LW arrays");
 }
 
 int rrtmg_sw_c(rrtmg_gpu_handle h, int ncol, int nlay, int icld, int iaer, const double* play, const double* plev,
@@ -1003,11 +1070,12 @@ int rrtmg_sw_c(rrtmg_gpu_handle h, int ncol, int nlay, int icld, int iaer, const
                const double* reliq, const double* tauaer, const double* ssaaer, const double* asmaer,
                const double* ecaer, double* swuflx, double* swdflx, double* swhr, double* swuflxc, double* swdflxc,
                double* swhrc) {
-  (void)iceflgsw; (void)liqflgsw; (void)reice; (void)reliq; (void)ecaer;
+  (void)ecaer;
   if (!valid_handle(h)) return RRTMG_ERR_ARG;
   int rc = check_dims(h, ncol, nlay);
   if (rc) return rc;
-  rc = sw_cloud_args(h, icld, inflgsw, cldfr, taucld, ssacld, asmcld, fsfcld);
+  rc = sw_cloud_args(h, icld, inflgsw, iceflgsw, liqflgsw, cldfr, taucld, ssacld, asmcld, fsfcld, cicewp, cliqwp,
+                     reice, reliq);
   if (rc) return rc;
   if (iaer != 0 && iaer != 10) return fail(h, RRTMG_ERR_UNSUPPORTED, "iaer must be 0 or 10");
   if (!play || !plev || !tlay || !tlev || !tsfc || !h2ovmr || !o3vmr || !co2vmr || !asdir || !asdif || !aldir ||
@@ -1017,25 +1085,34 @@ int rrtmg_sw_c(rrtmg_gpu_handle h, int ncol, int nlay, int icld, int iaer, const
   if (!(scon > 0.0)) return fail(h, RRTMG_ERR_ARG, "scon must be positive");
   cudaSetDevice(h->device);
   const size_t L = nlay, Lv = nlay + 1;
-  const bool aer = iaer == 10, cloudy = icld != 0;
+  const bool aer = iaer == 10, cloudy = icld != 0, phys = cloudy && inflgsw == 2;
   auto cl = [&](const double* a) { return cloudy ? a : nullptr; };
-  const HostIn in[26] = {{play, L}, {plev, Lv}, {tlay, L}, {tlev, Lv}, {tsfc, 1}, {h2ovmr, L}, {o3vmr, L},
+  auto ph = [&](const double* a) { return phys ? a : nullptr; };
+  const HostIn in[28] = {{play, L}, {plev, Lv}, {tlay, L}, {tlev, Lv}, {tsfc, 1}, {h2ovmr, L}, {o3vmr, L},
                          {co2vmr, L}, {ch4vmr, L}, {n2ovmr, L}, {o2vmr, L}, {asdir, 1}, {asdif, 1}, {aldir, 1},
                          {aldif, 1}, {coszen, 1}, {aer ? tauaer : nullptr, 14 * L}, {aer ? ssaaer : nullptr, 14 * L},
                          {aer ? asmaer : nullptr, 14 * L}, {cl(cldfr), L}, {cl(taucld), L, 14}, {cl(ssacld), L, 14},
-                         {cl(asmcld), L, 14}, {cl(fsfcld), L, 14}, {cl(cicewp), L}, {cl(cliqwp), L}};
+                         {cl(asmcld), L, 14}, {cl(fsfcld), L, 14}, {cl(cicewp), L}, {cl(cliqwp), L},
+                         {ph(reice), L}, {ph(reliq), L}};
   const HostOut out[6] = {{swuflx, Lv}, {swdflx, Lv}, {swhr, L}, {swuflxc, Lv}, {swdflxc, Lv}, {swhrc, L}};
   auto need = [&](int nc) {
     size_t b;
-    carve_sw(nullptr, nc, nlay, &b, cloudy);
+    carve_sw(nullptr, nc, nlay, &b, cloudy, phys);
     return b;
   };
   auto enq = [&](cudaStream_t s, void* ws, int nc, const double* const* d, double* const* o) {
     SwIn si{d[0],  d[1],  d[2],  d[3],  d[4],  d[5],  d[6],  d[7],  d[8],  d[9],  d[10], d[11], d[12],
             d[13], d[14], d[15], d[16], d[17], d[18], d[19], d[20], d[21], d[22], d[23], d[24], d[25]};
+    if (cloudy) {
+      si.inflag = inflgsw;
+      si.iceflag = iceflgsw;
+      si.liqflag = liqflgsw;
+      si.reice = d[26];
+      si.reliq = d[27];
+    }
     return sw_enqueue(h, s, ws, nc, nlay, iaer, adjes, dyofyr, scon, si, o[0], o[1], o[2], o[3], o[4], o[5]);
   };
-  return host_call(h, ncol, in, 26, out, 6, need, enq, "copy SW arrays");
+  return host_call(h, ncol, in, 28, out, 6, need, enq, "copy SW arrays");
 }
 
 }  // extern "C"

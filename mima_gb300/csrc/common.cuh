@@ -167,11 +167,17 @@ using SwPrep = SwPrepT<double>;
 struct LwIn {
   const double *play, *plev, *tlay, *tlev, *tsfc, *h2o, *o3, *co2, *ch4, *n2o, *o2, *cfc11, *cfc12, *cfc22, *ccl4,
       *emis, *tauaer;
-  // clouds (icld = 1, 2, 3, inflglw = 0), null in clear sky: cldfr (ncol,
-  // nlay), taucld (16, ncol, nlay), cicewp / cliqwp (ncol, nlay) or null
+  // clouds (icld = 1, 2, 3), null in clear sky: cldfr (ncol, nlay), taucld
+  // (16, ncol, nlay; may be null with inflag 1 / 2), cicewp / cliqwp (ncol,
+  // nlay) or null
   const double *cldfr, *taucld, *cicewp, *cliqwp;
   // cloud overlap with clouds: 1 random (rtrn), 2 or 3 maximum/random (rtrnmr)
   int icld;
+  // cldprop's choice (0: depths given; 1: abscld1 x water path; 2: ice and
+  // liquid parameterisations iceflag 0-3, liqflag 0-1 with the effective
+  // sizes reice / reliq (ncol, nlay))
+  int inflag, iceflag, liqflag;
+  const double *reice, *reliq;
 };
 template <class F>
 struct LwWorkT {
@@ -188,15 +194,53 @@ struct LwWorkT {
   // maximum/random overlap only: rtrnmr's overlap factors per layer,
   // [12][lay][col] (lw_overlap_kernel)
   F* ovl;
+  // cloud physics (inflag 1 / 2) only: the cloud optical depth of each band
+  // already along the diffusivity angle, secdiff(ib) x taucloud(ib) with ib
+  // the band's cloud band (16 bands fastest, per layer and column)
+  double* odc;
 };
 using LwWork = LwWorkT<double>;
 struct SwIn {
   const double *play, *plev, *tlay, *tlev, *tsfc, *h2o, *o3, *co2, *ch4, *n2o, *o2, *asdir, *asdif, *aldir, *aldif,
       *coszen, *tauaer, *ssaaer, *asmaer;
-  // clouds (icld = 1, inflgsw = 0), null in clear sky: cldfr (ncol, nlay);
-  // taucld, ssacld, asmcld, fsfcld (14, ncol, nlay); cicewp / cliqwp or null
+  // clouds (icld = 1), null in clear sky: cldfr (ncol, nlay); taucld,
+  // ssacld, asmcld, fsfcld (14, ncol, nlay); cicewp / cliqwp or null.  The
+  // total-sky pass reads fsfcld = null as no forward fraction.
   const double *cldfr, *taucld, *ssacld, *asmcld, *fsfcld, *cicewp, *cliqwp;
+  // cldprop_sw's choice (0: optics given; 2: ice iceflag 1-3 and liquid
+  // liqflag 1 parameterisations with the effective sizes reice / reliq)
+  int inflag, iceflag, liqflag;
+  const double *reice, *reliq;
 };
+// ---------------------------------------------------------------------------
+// Cloud optical property tables (rrlw_cld and rrsw_cld, filled by lwcldpr /
+// swcldpr, rrtmg_lw_init.f90 and rrtmg_sw_init.f90) in one FP64 array, each
+// table in Fortran order at its offset below, with the SW band limits
+// wavenum2 (rrsw_wvn) that select the Ebert-Curry coefficients.
+// ---------------------------------------------------------------------------
+namespace ct {
+constexpr int ABSICE0 = 0;                   // (2)
+constexpr int ABSICE1 = ABSICE0 + 2;         // (2, 5)
+constexpr int ABSICE2 = ABSICE1 + 10;        // (43, 16)
+constexpr int ABSICE3 = ABSICE2 + 43 * 16;   // (46, 16)
+constexpr int ABSLIQ0 = ABSICE3 + 46 * 16;   // scalar
+constexpr int ABSLIQ1 = ABSLIQ0 + 1;         // (58, 16)
+constexpr int ABSCLD1 = ABSLIQ1 + 58 * 16;   // scalar
+constexpr int EXTLIQ1 = ABSCLD1 + 1;         // (58, 16:29), then ssaliq1, asyliq1
+constexpr int SSALIQ1 = EXTLIQ1 + 58 * 14;
+constexpr int ASYLIQ1 = SSALIQ1 + 58 * 14;
+constexpr int EXTICE2 = ASYLIQ1 + 58 * 14;   // (43, 16:29), then ssaice2, asyice2
+constexpr int SSAICE2 = EXTICE2 + 43 * 14;
+constexpr int ASYICE2 = SSAICE2 + 43 * 14;
+constexpr int EXTICE3 = ASYICE2 + 43 * 14;   // (46, 16:29), then ssaice3, asyice3, fdlice3
+constexpr int SSAICE3 = EXTICE3 + 46 * 14;
+constexpr int ASYICE3 = SSAICE3 + 46 * 14;
+constexpr int FDLICE3 = ASYICE3 + 46 * 14;
+constexpr int ABARI = FDLICE3 + 46 * 14;     // (5) each: abari, bbari, cbari, dbari, ebari, fbari
+constexpr int WAVENUM2 = ABARI + 6 * 5;      // (16:29)
+constexpr int SIZE = WAVENUM2 + 14;
+}  // namespace ct
+
 template <class F>
 struct SwWorkT {
   uint32_t* idx;
@@ -207,6 +251,9 @@ struct SwWorkT {
   // and the clear-sky band partials
   F* cld;
   double *suc, *sdc;
+  // cloud physics (inflag = 2) only: cldprop_sw's delta-scaled optics,
+  // [tau, ssa, g][14 bands fastest, per layer and column]
+  double* cldopt;
 };
 using SwWork = SwWorkT<double>;
 

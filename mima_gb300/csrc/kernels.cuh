@@ -616,6 +616,8 @@ __device__ __forceinline__ void lw_band(const LwPrepT<R>& p, const double* __res
 // computed on its own above the surface once the column holds a cloud.
 // Total and clear-sky level radiances are summed over the band's g-points
 // into their own band partials.
+// scaled (cloud physics): taucld holds lw_cldphys_kernel's depths, already
+// along the diffusivity angle of their cloud band.
 // With ovl (icld = 2, 3): maximum/random overlap, rrtmg_lw_rtrnmr.f90:
 // 500-705.  Through a block of adjacent cloudy layers the radiance is carried
 // as a cloudy and a clear part; at each cloudy layer's far boundary the
@@ -630,7 +632,7 @@ __device__ __forceinline__ void lw_band_cld(const LwPrepT<R>& p, const R* __rest
                                             double* __restrict__ bd, double* __restrict__ bdu,
                                             double* __restrict__ buc, double* __restrict__ bdc,
                                             double* __restrict__ bduc, int ncol, int nlay, int idrv, bool analytic,
-                                            int blk, float* sbuf, const R* __restrict__ ovl) {
+                                            int blk, float* sbuf, const R* __restrict__ ovl, bool scaled) {
   const bool IDRV = idrv == 1;
   constexpr bool SPLIT = sizeof(R) == 4;
   constexpr int NG = NS;
@@ -647,6 +649,7 @@ __device__ __forceinline__ void lw_band_cld(const LwPrepT<R>& p, const R* __rest
   const size_t N = (size_t)ncol;
   const int lt = p.laytrop[c];
   const R secdiff = p.secdiff[(B - 1) * N + c];
+  const R seccld = scaled ? (R)1. : secdiff;
   const R bpade = (R)c_lw.bpade;
   const R rec_6 = (R)0.166667;
   const size_t fstride = (size_t)nlay * N;
@@ -724,7 +727,7 @@ __device__ __forceinline__ void lw_band_cld(const LwPrepT<R>& p, const R* __rest
     R atr, bbd, bbu, at = (R)0., bbut = (R)0., ef = (R)0.;
     if (cf > (R)0.) {  // cloudy layer (rtrn :350-416)
       iclddn = true;
-      const R odcld = secdiff * (__ldg(cld + fstride + o) * (R)__ldg(taucld + (B - 1) + 16 * o));
+      const R odcld = seccld * (__ldg(cld + fstride + o) * (R)__ldg(taucld + (B - 1) + 16 * o));
       if (!ovl) ef = ((R)1. - exp(-odcld)) * cf;
       R odtot = odepth + odcld;
       R gassrc, bbdtot;
@@ -1011,7 +1014,8 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_LW_MINB :
                          const double* __restrict__ emis, const double* __restrict__ tauaer,
                          const R* __restrict__ tab, const R* __restrict__ exptbl, const R* __restrict__ tfntbl,
                          const R* __restrict__ tautbl, double* bu, double* bd, double* bdu, double* buc, double* bdc,
-                         double* bduc, int ncol, int nlay, int idrv, int analytic, const R* __restrict__ ovl) {
+                         double* bduc, int ncol, int nlay, int idrv, int analytic, const R* __restrict__ ovl,
+                         int scaled) {
   __shared__ float sbuf[sizeof(R) == 4 ? kGSumFloats : 1];
   constexpr bool SPLIT = sizeof(R) == 4;
   int blk = blockIdx.x;
@@ -1025,7 +1029,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_LW_MINB :
   case s:                                                                                                         \
     lw_band_cld<lw_slot(s).band, R, MAXL, lw_slot(s).g0, lw_slot(s).ng, s>(                                      \
         p, cld, taucld, emis, tauaer, tab, exptbl, tfntbl, tautbl, bu, bd, bdu, buc, bdc, bduc, ncol, nlay, idv, an, \
-        blk, sbuf, ovl);                                                                                          \
+        blk, sbuf, ovl, scaled != 0);                                                                             \
     break;
     switch (unit) {
       RRTMG_LW_SLOT(0) RRTMG_LW_SLOT(1) RRTMG_LW_SLOT(2) RRTMG_LW_SLOT(3) RRTMG_LW_SLOT(4) RRTMG_LW_SLOT(5)
@@ -1041,7 +1045,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_LW_MINB :
 #define RRTMG_LW_CASE(b)                                                                                            \
   case b - 1:                                                                                                      \
     lw_band_cld<b, R, MAXL>(p, cld, taucld, emis, tauaer, tab, exptbl, tfntbl, tautbl, bu, bd, bdu, buc, bdc, bduc, \
-                            ncol, nlay, idv, an, blk, sbuf, ovl);                                                  \
+                            ncol, nlay, idv, an, blk, sbuf, ovl, scaled != 0);                                     \
     break;
     switch (unit) {
       RRTMG_LW_CASE(1) RRTMG_LW_CASE(2) RRTMG_LW_CASE(3) RRTMG_LW_CASE(4) RRTMG_LW_CASE(5) RRTMG_LW_CASE(6)
@@ -1076,6 +1080,156 @@ __global__ void __launch_bounds__(128) lw_cloud_kernel(LwIn in, F* __restrict__ 
   const bool kept = cf >= cldmin && (cwp >= cldmin || tauctot >= cldmin);
   cld[o] = cf >= 1.e-6 ? (F)cf : (F)0;
   cld[(size_t)nlay * ncol + o] = kept ? (F)1 : (F)0;
+}
+
+// ---------------------------------------------------------------------------
+// LW cloud physics (cldprop with inflag = 1 or 2, rrtmg_lw_cldprop.f90:
+// 155-270, and rtrn / rtrnmr's cloud depths along the diffusivity angle,
+// rrtmg_lw_rtrn.f90:302-330).
+//
+// cldprop keeps a count of cloud bands, ncbands, across its layer loop
+// (bottom to top): 1 at the start, 16 after a layer with given depths or
+// inflag = 1, after an iceflag 2 / 3 ice cloud or a liqflag = 1 liquid cloud,
+// 5 after an iceflag = 1 ice cloud; a layer fills cloud bands 1..ncbands as
+// the count stands after it.  The radiative transfer then takes band iband's
+// cloud depth from cloud band ipat(iband, final count) -- so an ice-only
+// iceflag = 1 layer at the top of a column leaves every layer of that column
+// with 5 cloud bands.
+// ---------------------------------------------------------------------------
+// Cloud band of band iband (1..16) with ncb cloud bands (ipat, icb).
+__device__ __forceinline__ int lw_cloud_band(int iband, int ncb) {
+  if (ncb == 1) return 1;
+  if (ncb == 5) return iband <= 2 ? iband : iband <= 5 ? 3 : iband <= 8 ? 4 : 5;
+  return iband;
+}
+// Whether a layer's optics are formed: cover >= cldmin and water path or
+// band-summed given depth >= cldmin (cldmin = 1e-20).
+__device__ __forceinline__ bool lw_cloud_kept(const LwIn& in, size_t o, double& cf, double& ciwp, double& clwp) {
+  cf = __ldg(in.cldfr + o);
+  ciwp = in.cicewp ? __ldg(in.cicewp + o) : 0.0;
+  clwp = in.cliqwp ? __ldg(in.cliqwp + o) : 0.0;
+  double tauctot = 0.0;
+  if (in.taucld)
+    for (int ib = 0; ib < kLwBands; ++ib) tauctot = tauctot + __ldg(in.taucld + ib + 16 * o);
+  const double cwp = ciwp + clwp, cldmin = 1.e-20;
+  return cf >= cldmin && (cwp >= cldmin || tauctot >= cldmin);
+}
+// One formed layer: advances ncb, gives the icb columns of the ice and liquid
+// coefficients (0: one value, 1: 5 ice bands, 2: per band); false where the
+// reference stops (a size outside its table; not-a-number sizes too).
+__device__ __forceinline__ bool lw_cloud_layer(const LwIn& in, double ciwp, double clwp, double radice,
+                                               double radliq, int& ncb, int& iceind, int& liqind) {
+  iceind = 0;
+  liqind = 0;
+  if (in.inflag == 1) {
+    ncb = 16;
+    return true;
+  }
+  bool ok = true;
+  if (ciwp != 0.0) {
+    if (in.iceflag == 0) {
+      ok = radice >= 10.0;
+    } else if (in.iceflag == 1) {
+      ok = radice >= 13.0 && radice <= 130.0;
+      ncb = 5;
+      iceind = 1;
+    } else {
+      ok = radice >= 5.0 && radice <= (in.iceflag == 2 ? 131.0 : 140.0);
+      ncb = 16;
+      iceind = 2;
+    }
+  }
+  if (clwp == 0.0 || in.liqflag == 0) {
+    if (iceind == 1) iceind = 2;
+  } else {
+    ok = ok && radliq >= 2.5 && radliq <= 60.0;
+    ncb = 16;
+    liqind = 2;
+  }
+  return ok;
+}
+// Interpolation in a (rows, bands) table at a 1-based row and fraction.
+__device__ __forceinline__ double cld_interp(const double* t, int rows, int index, double fint, int col) {
+  const double a = __ldg(t + (index - 1) + rows * col), b = __ldg(t + index + rows * col);
+  return a + fint * (b - a);
+}
+// Ice and liquid absorption coefficients (m2/g) of coefficient band k.
+__device__ __forceinline__ double lw_absice(const LwIn& in, const double* T, double ciwp, double radice, int k) {
+  if (ciwp == 0.0) return 0.0;
+  if (in.iceflag == 0) return __ldg(T + ct::ABSICE0) + __ldg(T + ct::ABSICE0 + 1) / radice;
+  if (in.iceflag == 1)
+    return __ldg(T + ct::ABSICE1 + 2 * (k - 1)) + __ldg(T + ct::ABSICE1 + 1 + 2 * (k - 1)) / radice;
+  const int rows = in.iceflag == 2 ? 43 : 46;
+  const double factor = (radice - 2.) / 3.;
+  int index = (int)factor;
+  if (index == rows) index = rows - 1;
+  return cld_interp(T + (in.iceflag == 2 ? ct::ABSICE2 : ct::ABSICE3), rows, index, factor - (double)index, k - 1);
+}
+__device__ __forceinline__ double lw_absliq(const LwIn& in, const double* T, double clwp, double radliq, int k) {
+  if (clwp == 0.0) return 0.0;
+  if (in.liqflag == 0) return __ldg(T + ct::ABSLIQ0);
+  int index = (int)(radliq - 1.5);
+  if (index == 0) index = 1;
+  if (index == 58) index = 57;
+  return cld_interp(T + ct::ABSLIQ1, 58, index, radliq - 1.5 - (double)index, k - 1);
+}
+
+// One thread per column: the cover and formed-layer mask of every layer (as
+// lw_cloud_kernel) and odc[lay][col][iband] = secdiff(ib) x taucloud(lay, ib),
+// ib = ipat(iband, ncbands), the cloud depth rtrn / rtrnmr use (0 for a
+// layer whose optics are not formed or that filled fewer cloud bands).  A
+// size outside its table sets flag bit 2 (reported as invalid input) and
+// leaves the column's depths 0.
+template <class F>
+__global__ void __launch_bounds__(128) lw_cldphys_kernel(LwIn in, const F* __restrict__ secdiff,
+                                                         const double* __restrict__ T, F* __restrict__ cld,
+                                                         double* __restrict__ odc, int ncol, int nlay,
+                                                         unsigned* __restrict__ flags) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncol) return;
+  const size_t N = (size_t)ncol, S = (size_t)nlay * N;
+  int ncb = 1;
+  bool ok = true;
+  for (int l = 0; l < nlay; ++l) {
+    const size_t o = (size_t)l * N + col;
+    double cf, ciwp, clwp;
+    const bool kept = lw_cloud_kept(in, o, cf, ciwp, clwp);
+    cld[o] = cf >= 1.e-6 ? (F)cf : (F)0;
+    cld[S + o] = kept ? (F)1 : (F)0;
+    int ii, li;
+    if (kept && !lw_cloud_layer(in, ciwp, clwp, in.reice ? __ldg(in.reice + o) : 0.0,
+                                in.reliq ? __ldg(in.reliq + o) : 0.0, ncb, ii, li))
+      ok = false;
+  }
+  if (!ok) atomicOr(flags, 4u);
+  int run = 1;
+  for (int l = 0; l < nlay; ++l) {
+    const size_t o = (size_t)l * N + col;
+    double* d = odc + 16 * o;
+    double cf, ciwp, clwp;
+    const bool kept = lw_cloud_kept(in, o, cf, ciwp, clwp);
+    if (!ok || !kept) {
+      for (int b = 0; b < kLwBands; ++b) d[b] = 0.0;
+      continue;
+    }
+    const double radice = in.reice ? __ldg(in.reice + o) : 0.0, radliq = in.reliq ? __ldg(in.reliq + o) : 0.0;
+    int iceind, liqind;
+    lw_cloud_layer(in, ciwp, clwp, radice, radliq, run, iceind, liqind);
+    for (int iband = 1; iband <= kLwBands; ++iband) {
+      const int ib = lw_cloud_band(iband, ncb);
+      double tc = 0.0;
+      if (ib <= run) {
+        if (in.inflag == 1) {
+          tc = __ldg(T + ct::ABSCLD1) * (ciwp + clwp);
+        } else {
+          const int ki = lw_cloud_band(ib, iceind == 0 ? 1 : iceind == 1 ? 5 : 16);
+          const int kl = lw_cloud_band(ib, liqind == 0 ? 1 : 16);
+          tc = ciwp * lw_absice(in, T, ciwp, radice, ki) + clwp * lw_absliq(in, T, clwp, radliq, kl);
+        }
+      }
+      d[iband - 1] = (double)secdiff[(size_t)(ib - 1) * N + col] * tc;
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1734,7 +1888,7 @@ __device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, dou
       R ptauc = (R)0., pomgc = (R)1., pasyc = (R)0.;
       if (__ldg(cld + fstride + o) > (R)0.) {
         const size_t q = (size_t)(ibm - 1) + 14 * o;
-        const R taucldorig = (R)__ldg(in.taucld + q), ffp = (R)__ldg(in.fsfcld + q);
+        const R taucldorig = (R)__ldg(in.taucld + q), ffp = in.fsfcld ? (R)__ldg(in.fsfcld + q) : (R)0.;
         const R ssac = (R)__ldg(in.ssacld + q), asmc = (R)__ldg(in.asmcld + q);
         const R ffp1 = (R)1.0 - ffp;
         const R ffpssa = (R)1.0 - ffp * ssac;
@@ -1883,6 +2037,102 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_SW_MINB :
 
 #ifdef RRTMG_DEFINE_COLUMN_KERNELS
 // ---------------------------------------------------------------------------
+// SW cloud physics of one formed layer (cldprop_sw, inflag = 2,
+// rrtmg_sw_cldprop.f90:158-340): per band the ice extinction (m2/g), single-
+// scattering albedo, asymmetry and forward fraction of Ebert and Curry's fit
+// (iceflag 1; its five spectral intervals chosen by the band's upper limit
+// wavenum2), of Key's Streamer table (2) or of Fu's table with its delta
+// fractions (3), and those of Hu and Stamnes' liquid table (liqflag 1); each
+// delta-M scaled and combined into the layer's delta-scaled depth tau,
+// albedo ssa and asymmetry g (written with 1-band stride).  A zero depth or
+// ice scattering becomes cldmin = 1e-20.  Returns false (nothing written)
+// where the reference stops: a size outside its table (not-a-number sizes
+// too), or a coefficient outside its physical range.
+// ---------------------------------------------------------------------------
+__device__ __noinline__ bool sw_cloud_optics(const SwIn& in, const double* __restrict__ T, double ciwp, double clwp,
+                                             double radice, double radliq, double* tau, double* ssa, double* g) {
+  const double eps = 1.e-06, cldmin = 1.e-20;
+  if (ciwp != 0.0) {
+    const bool ok = in.iceflag == 1   ? (radice >= 13.0 && radice <= 130.0)
+                    : in.iceflag == 2 ? (radice >= 5.0 && radice <= 131.0)
+                                      : (radice >= 5.0 && radice <= 140.0);
+    if (!ok) return false;
+  }
+  if (clwp != 0.0 && !(radliq >= 2.5 && radliq <= 60.0)) return false;
+  const int irows = in.iceflag == 2 ? 43 : 46;
+  const double ifactor = (radice - 2.) / 3.;
+  int iindex = (int)ifactor;
+  if (ciwp != 0.0 && in.iceflag >= 2 && iindex == irows) iindex = irows - 1;
+  const double ifint = ifactor - (double)iindex;
+  int lindex = (int)(radliq - 1.5);
+  if (lindex == 0) lindex = 1;
+  if (lindex == 58) lindex = 57;
+  const double lfint = radliq - 1.5 - (double)lindex;
+  double tc[kSwBands], sc[kSwBands], gc[kSwBands];
+  for (int k = 0; k < kSwBands; ++k) {  // band 16 + k
+    double ext_i = 0.0, ssa_i = 0.0, g_i = 0.0, fw_i = 0.0;
+    if (ciwp != 0.0) {
+      if (in.iceflag == 1) {
+        const double wn = __ldg(T + ct::WAVENUM2 + k);
+        const int icx = wn > 1.43e04 ? 0 : wn > 7.7e03 ? 1 : wn > 5.3e03 ? 2 : wn > 4.0e03 ? 3 : 4;
+        const double* c = T + ct::ABARI + icx;
+        ext_i = __ldg(c) + __ldg(c + 5) / radice;
+        ssa_i = 1. - __ldg(c + 10) - __ldg(c + 15) * radice;
+        g_i = __ldg(c + 20) + __ldg(c + 25) * radice;
+        if (g_i >= 1.0) g_i = 1.0 - eps;
+        fw_i = g_i * g_i;
+      } else if (in.iceflag == 2) {
+        ext_i = cld_interp(T + ct::EXTICE2, 43, iindex, ifint, k);
+        ssa_i = cld_interp(T + ct::SSAICE2, 43, iindex, ifint, k);
+        g_i = cld_interp(T + ct::ASYICE2, 43, iindex, ifint, k);
+        fw_i = g_i * g_i;
+      } else {
+        ext_i = cld_interp(T + ct::EXTICE3, 46, iindex, ifint, k);
+        ssa_i = cld_interp(T + ct::SSAICE3, 46, iindex, ifint, k);
+        g_i = cld_interp(T + ct::ASYICE3, 46, iindex, ifint, k);
+        const double fdelta = cld_interp(T + ct::FDLICE3, 46, iindex, ifint, k);
+        if (fdelta < 0.0 || fdelta > 1.0) return false;
+        fw_i = fdelta + 0.5 / ssa_i;
+        if (fw_i > g_i) fw_i = g_i;
+      }
+      if (ext_i < 0.0 || ssa_i > 1.0 || ssa_i < 0.0 || g_i > 1.0 || g_i < 0.0) return false;
+    }
+    double ext_l = 0.0, ssa_l = 0.0, g_l = 0.0, fw_l = 0.0;
+    if (clwp != 0.0) {
+      ext_l = cld_interp(T + ct::EXTLIQ1, 58, lindex, lfint, k);
+      ssa_l = cld_interp(T + ct::SSALIQ1, 58, lindex, lfint, k);
+      if (lfint < 0. && ssa_l > 1.) ssa_l = __ldg(T + ct::SSALIQ1 + (lindex - 1) + 58 * k);
+      g_l = cld_interp(T + ct::ASYLIQ1, 58, lindex, lfint, k);
+      fw_l = g_l * g_l;
+      if (ext_l < 0.0 || ssa_l > 1.0 || ssa_l < 0.0 || g_l > 1.0 || g_l < 0.0) return false;
+    }
+    const double tauliqorig = clwp * ext_l, tauiceorig = ciwp * ext_i;
+    const double ssaliq = ssa_l * (1.0 - fw_l) / (1.0 - fw_l * ssa_l);
+    const double tauliq = (1.0 - fw_l * ssa_l) * tauliqorig;
+    const double ssaice = ssa_i * (1.0 - fw_i) / (1.0 - fw_i * ssa_i);
+    const double tauice = (1.0 - fw_i * ssa_i) * tauiceorig;
+    const double scatliq = ssaliq * tauliq;
+    double scatice = ssaice * tauice;
+    double t = tauliq + tauice;
+    if (t == 0.0) t = cldmin;
+    if (scatice == 0.0) scatice = cldmin;
+    tc[k] = t;
+    sc[k] = (scatliq + scatice) / t;
+    if (in.iceflag == 3)
+      gc[k] = (1.0 / (scatliq + scatice)) *
+              (scatliq * (g_l - fw_l) / (1.0 - fw_l) + scatice * ((g_i - fw_i) / (1.0 - fw_i)));
+    else
+      gc[k] = (scatliq * (g_l - fw_l) / (1.0 - fw_l) + scatice * (g_i - fw_i) / (1.0 - fw_i)) / (scatliq + scatice);
+  }
+  for (int k = 0; k < kSwBands; ++k) {
+    tau[k] = tc[k];
+    ssa[k] = sc[k];
+    g[k] = gc[k];
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
 // Clouds of the SW call (icld = 1, cloud optics given), one thread per
 // (column, layer): inatm_sw's cldfrac (rrtmg_sw_rad.nomcica.f90:1065-1083);
 // the non-McICA SW computes clear or overcast layers only and stops on a
@@ -1892,20 +2142,40 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_SW_MINB :
 // cldmin), cldmin = 1e-20 (rrtmg_sw_cldprop.f90:120-141).  cld[0][lay][col]:
 // the cover; cld[1][lay][col]: 1 where the optics are kept, else 0.
 // ---------------------------------------------------------------------------
+// With cloud physics (inflag = 2), a sunlit layer whose optics are formed
+// gets them from sw_cloud_optics into opt; a size or optical property that
+// stops the reference sets flag bit 2.
 template <class F>
 __global__ void __launch_bounds__(128) sw_cloud_kernel(SwIn in, F* __restrict__ cld, int ncol, int nlay,
-                                                       unsigned* __restrict__ flags) {
+                                                       unsigned* __restrict__ flags, const double* __restrict__ T,
+                                                       double* __restrict__ opt) {
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= ncol) return;
   const size_t o = (size_t)blockIdx.y * ncol + col;
   const double cf = __ldg(in.cldfr + o);
   double tauctot = 0.0;
-  for (int ib = 0; ib < kSwBands; ++ib) tauctot = tauctot + __ldg(in.taucld + ib + 14 * o);
-  const double cwp = (in.cicewp ? __ldg(in.cicewp + o) : 0.0) + (in.cliqwp ? __ldg(in.cliqwp + o) : 0.0);
+  if (in.taucld)
+    for (int ib = 0; ib < kSwBands; ++ib) tauctot = tauctot + __ldg(in.taucld + ib + 14 * o);
+  const double ciwp = in.cicewp ? __ldg(in.cicewp + o) : 0.0, clwp = in.cliqwp ? __ldg(in.cliqwp + o) : 0.0;
+  const double cwp = ciwp + clwp;
   const double cldmin = 1.e-20, zepsec = 1.e-06;
-  // the check runs in sunlit columns only: the reference skips the others (:500-509)
-  if (cf > zepsec && cf < 1.0 - zepsec && __ldg(in.coszen + col) >= 1.e-10) atomicOr(flags, 2u);
-  const bool kept = cf >= cldmin && (cwp >= cldmin || tauctot >= cldmin);
+  // the checks run in sunlit columns only: the reference skips the others (:500-509)
+  const bool lit = __ldg(in.coszen + col) >= 1.e-10;
+  if (cf > zepsec && cf < 1.0 - zepsec && lit) atomicOr(flags, 2u);
+  bool kept = cf >= cldmin && (cwp >= cldmin || tauctot >= cldmin);
+  if (in.inflag == 2 && kept) {
+    // unlit columns (whose outputs are zeros) and a failed layer keep no
+    // optics, so that the total-sky pass reads only optics written here
+    const size_t S = (size_t)nlay * ncol;
+    if (!lit) {
+      kept = false;
+    } else if (!sw_cloud_optics(in, T, ciwp, clwp, in.reice ? __ldg(in.reice + o) : 0.0,
+                                in.reliq ? __ldg(in.reliq + o) : 0.0, opt + 14 * o, opt + 14 * (S + o),
+                                opt + 14 * (2 * S + o))) {
+      atomicOr(flags, 4u);
+      kept = false;
+    }
+  }
   cld[o] = (F)cf;
   cld[(size_t)nlay * ncol + o] = kept ? (F)1 : (F)0;
 }

@@ -64,15 +64,15 @@ void launch_lw_gpoint_cld_fp64(const LwPrep& p, const double* cld, const double*
                                const double* tauaer, const double* tab, const double* exptbl, const double* tfntbl,
                                const double* tautbl, double* bu, double* bd, double* bdu, double* buc, double* bdc,
                                double* bduc, int ncol, int nlay, int idrv, int nb, int analytic, cudaStream_t s,
-                               const double* ovl) {
+                               const double* ovl, bool scaled) {
   if (maxl_for(nlay) == 64)
     lw_gpoint_cld_kernel<double, 64, -1><<<nb, kBlock, 0, s>>>(p, cld, taucld, emis, tauaer, tab, exptbl, tfntbl, tautbl,
                                                               bu, bd, bdu, buc, bdc, bduc, ncol, nlay, idrv, analytic,
-                                                              ovl);
+                                                              ovl, scaled ? 1 : 0);
   else
     lw_gpoint_cld_kernel<double, 208, -1><<<nb, kBlock, 0, s>>>(p, cld, taucld, emis, tauaer, tab, exptbl, tfntbl,
                                                                tautbl, bu, bd, bdu, buc, bdc, bduc, ncol, nlay, idrv,
-                                                               analytic, ovl);
+                                                               analytic, ovl, scaled ? 1 : 0);
 }
 
 void launch_lw_cloud(const LwIn& in, double* cld, int ncol, int nlay, cudaStream_t s) {
@@ -80,6 +80,14 @@ void launch_lw_cloud(const LwIn& in, double* cld, int ncol, int nlay, cudaStream
 }
 void launch_lw_cloud_split(const LwIn& in, float* cld, int ncol, int nlay, cudaStream_t s) {
   lw_cloud_kernel<float><<<dim3((ncol + 127) / 128, nlay), 128, 0, s>>>(in, cld, ncol, nlay);
+}
+void launch_lw_cldphys(const LwIn& in, const double* secdiff, const double* cldtab, double* cld, double* odc, int ncol,
+                       int nlay, unsigned* flags, cudaStream_t s) {
+  lw_cldphys_kernel<double><<<(ncol + 127) / 128, 128, 0, s>>>(in, secdiff, cldtab, cld, odc, ncol, nlay, flags);
+}
+void launch_lw_cldphys_split(const LwIn& in, const float* secdiff, const double* cldtab, float* cld, double* odc,
+                             int ncol, int nlay, unsigned* flags, cudaStream_t s) {
+  lw_cldphys_kernel<float><<<(ncol + 127) / 128, 128, 0, s>>>(in, secdiff, cldtab, cld, odc, ncol, nlay, flags);
 }
 void launch_lw_overlap(const double* cldfr, double* ovl, int ncol, int nlay, cudaStream_t s) {
   lw_overlap_kernel<double><<<(ncol + 127) / 128, 128, 0, s>>>(cldfr, ovl, ncol, nlay);
@@ -125,11 +133,13 @@ void launch_sw_gpoint_fp64(const SwPrep& p, const SwIn& in, double adjflux, int 
     sw_gpoint_kernel<double, 208><<<nb, kBlock, 0, s>>>(p, in, adjflux, iaer, tab, tab, exptbl, su, sd, ncol, nlay, analytic, nullptr);
 }
 
-void launch_sw_cloud(const SwIn& in, double* cld, int ncol, int nlay, unsigned* flags, cudaStream_t s) {
-  sw_cloud_kernel<double><<<dim3((ncol + 127) / 128, nlay), 128, 0, s>>>(in, cld, ncol, nlay, flags);
+void launch_sw_cloud(const SwIn& in, double* cld, int ncol, int nlay, unsigned* flags, cudaStream_t s,
+                     const double* cldtab, double* opt) {
+  sw_cloud_kernel<double><<<dim3((ncol + 127) / 128, nlay), 128, 0, s>>>(in, cld, ncol, nlay, flags, cldtab, opt);
 }
-void launch_sw_cloud_split(const SwIn& in, float* cld, int ncol, int nlay, unsigned* flags, cudaStream_t s) {
-  sw_cloud_kernel<float><<<dim3((ncol + 127) / 128, nlay), 128, 0, s>>>(in, cld, ncol, nlay, flags);
+void launch_sw_cloud_split(const SwIn& in, float* cld, int ncol, int nlay, unsigned* flags, cudaStream_t s,
+                           const double* cldtab, double* opt) {
+  sw_cloud_kernel<float><<<dim3((ncol + 127) / 128, nlay), 128, 0, s>>>(in, cld, ncol, nlay, flags, cldtab, opt);
 }
 
 void launch_sw_finalize(const double* su, const double* sd, const double* plev, const double* coszen, int ncol,

@@ -249,27 +249,27 @@ static void lw_split_cld_flags(int fl, int nb, cudaStream_t s, const LwPrepT<flo
                                const double* taucld, const double* emis, const double* tauaer, const float* tab,
                                const float* exptbl, const float* tfntbl, const float* tautbl, double* bu, double* bd,
                                double* bdu, double* buc, double* bdc, double* bduc, int ncol, int nlay,
-                               const float* ovl) {
+                               const float* ovl, bool scaled) {
   auto k = fl == 0 ? lw_gpoint_cld_kernel<float, MAXL, 0>
          : fl == 1 ? lw_gpoint_cld_kernel<float, MAXL, 1>
          : fl == 2 ? lw_gpoint_cld_kernel<float, MAXL, 2>
                    : lw_gpoint_cld_kernel<float, MAXL, 3>;
   k<<<nb, kBlock, 0, s>>>(p, cld, taucld, emis, tauaer, tab, exptbl, tfntbl, tautbl, bu, bd, bdu, buc, bdc, bduc, ncol,
-                          nlay, 0, 0, ovl);
+                          nlay, 0, 0, ovl, scaled ? 1 : 0);
 }
 
 void launch_lw_gpoint_cld_split(const LwPrepT<float>& p, const float* cld, const double* taucld, const double* emis,
                                 const double* tauaer, const float* tab, const float* exptbl, const float* tfntbl,
                                 const float* tautbl, double* bu, double* bd, double* bdu, double* buc, double* bdc,
                                 double* bduc, int ncol, int nlay, int idrv, int nb, int analytic, cudaStream_t s,
-                                const float* ovl) {
+                                const float* ovl, bool scaled) {
   const int fl = (analytic ? 1 : 0) | (idrv == 1 ? 2 : 0);
   if (maxl_for(nlay) == 64)
     lw_split_cld_flags<64>(fl, nb, s, p, cld, taucld, emis, tauaer, tab, exptbl, tfntbl, tautbl, bu, bd, bdu, buc,
-                           bdc, bduc, ncol, nlay, ovl);
+                           bdc, bduc, ncol, nlay, ovl, scaled);
   else
     lw_split_cld_flags<208>(fl, nb, s, p, cld, taucld, emis, tauaer, tab, exptbl, tfntbl, tautbl, bu, bd, bdu, buc,
-                            bdc, bduc, ncol, nlay, ovl);
+                            bdc, bduc, ncol, nlay, ovl, scaled);
 }
 
 template <int MAXL, bool TOT>

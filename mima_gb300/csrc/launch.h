@@ -29,20 +29,27 @@ void launch_lw_finalize(const double* bu, const double* bd, const double* bdu, c
 // Clouds (icld = 1): per-layer cloud fields, FP64 and FP32 storage.
 void launch_lw_cloud(const LwIn& in, double* cld, int ncol, int nlay, cudaStream_t s);
 void launch_lw_cloud_split(const LwIn& in, float* cld, int ncol, int nlay, cudaStream_t s);
+// Cloud physics (inflag 1 / 2): the cloud fields of launch_lw_cloud and the
+// cloud depths along the diffusivity angle (odc); cldtab: ct:: tables.
+void launch_lw_cldphys(const LwIn& in, const double* secdiff, const double* cldtab, double* cld, double* odc, int ncol,
+                       int nlay, unsigned* flags, cudaStream_t s);
+void launch_lw_cldphys_split(const LwIn& in, const float* secdiff, const double* cldtab, float* cld, double* odc,
+                             int ncol, int nlay, unsigned* flags, cudaStream_t s);
 // Maximum/random overlap (icld = 2, 3): rtrnmr's overlap factors per layer.
 void launch_lw_overlap(const double* cldfr, double* ovl, int ncol, int nlay, cudaStream_t s);
 void launch_lw_overlap_split(const double* cldfr, float* ovl, int ncol, int nlay, cudaStream_t s);
 // ovl: the overlap factors of maximum/random overlap, or null (random overlap).
+// scaled: taucld is launch_lw_cldphys's odc (depths along the diffusivity angle).
 void launch_lw_gpoint_cld_fp64(const LwPrep& p, const double* cld, const double* taucld, const double* emis,
                                const double* tauaer, const double* tab, const double* exptbl, const double* tfntbl,
                                const double* tautbl, double* bu, double* bd, double* bdu, double* buc, double* bdc,
                                double* bduc, int ncol, int nlay, int idrv, int nb, int analytic, cudaStream_t s,
-                               const double* ovl = nullptr);
+                               const double* ovl = nullptr, bool scaled = false);
 void launch_lw_gpoint_cld_split(const LwPrepT<float>& p, const float* cld, const double* taucld, const double* emis,
                                 const double* tauaer, const float* tab, const float* exptbl, const float* tfntbl,
                                 const float* tautbl, double* bu, double* bd, double* bdu, double* buc, double* bdc,
                                 double* bduc, int ncol, int nlay, int idrv, int nb, int analytic, cudaStream_t s,
-                                const float* ovl = nullptr);
+                                const float* ovl = nullptr, bool scaled = false);
 void launch_sw_prep(const SwIn& in, const SwWork& w, int ncol, int nlay, unsigned* flags, cudaStream_t s);
 // Prep for the FP32-split solvers: the same steps in FP32 arithmetic (FP32 Planck
 // tables), fields stored as float.
@@ -55,9 +62,13 @@ void launch_sw_prep_split(const SwIn& in, const SwWorkT<float>& w, int ncol, int
 void launch_sw_gpoint_fp64(const SwPrep& p, const SwIn& in, double adjflux, int iaer, const double* tab,
                            const double* exptbl, double* su, double* sd, int ncol, int nlay, int nb, int analytic,
                            cudaStream_t s, const double* cld = nullptr);
-// SW clouds (icld = 1): per-layer cover and cldprop mask; flags a partly cloudy layer.
-void launch_sw_cloud(const SwIn& in, double* cld, int ncol, int nlay, unsigned* flags, cudaStream_t s);
-void launch_sw_cloud_split(const SwIn& in, float* cld, int ncol, int nlay, unsigned* flags, cudaStream_t s);
+// SW clouds (icld = 1): per-layer cover and cldprop mask; flags a partly cloudy
+// layer.  With cloud physics (in.inflag = 2) also the optics of formed layers
+// into opt ([tau, ssa, g][lay][col][band]) from the ct:: tables cldtab.
+void launch_sw_cloud(const SwIn& in, double* cld, int ncol, int nlay, unsigned* flags, cudaStream_t s,
+                     const double* cldtab = nullptr, double* opt = nullptr);
+void launch_sw_cloud_split(const SwIn& in, float* cld, int ncol, int nlay, unsigned* flags, cudaStream_t s,
+                           const double* cldtab = nullptr, double* opt = nullptr);
 void launch_sw_finalize(const double* su, const double* sd, const double* plev, const double* coszen, int ncol,
                         int nlay, double* swuflx, double* swdflx, double* swhr, double* swuflxc, double* swdflxc,
                         double* swhrc, cudaStream_t s, const double* suc = nullptr, const double* sdc = nullptr);

@@ -10,6 +10,7 @@
 // nong_flat * ng + g.  Also builds the transmittance / tau-transition lookup
 // tables (rrtmg_lw_init.f90:106-124, rrtmg_sw_init.f90:96-104) and the
 // constant-memory blocks.
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -430,6 +431,35 @@ std::string build_host_tables(const char* blob_path, double cpdair, HostTables& 
     T.sw.pi = 2. * std::asin(1.);
     T.sw.bpade = 1.0 / 0.278;
     lookup_tables(T.sw_exp, nullptr, T.sw.bpade);
+  }
+
+  // ---------------- cloud optical properties ----------------
+  {
+    T.cld.assign(ct::SIZE, 0.0);
+    struct Part {
+      const char* name;
+      int off;
+      size_t n;
+    };
+    const Part parts[] = {
+        {"lwcld.absice0", ct::ABSICE0, 2},        {"lwcld.absice1", ct::ABSICE1, 10},
+        {"lwcld.absice2", ct::ABSICE2, 43 * 16},  {"lwcld.absice3", ct::ABSICE3, 46 * 16},
+        {"lwcld.absliq0", ct::ABSLIQ0, 1},        {"lwcld.absliq1", ct::ABSLIQ1, 58 * 16},
+        {"lwcld.abscld1", ct::ABSCLD1, 1},        {"swcld.extliq1", ct::EXTLIQ1, 58 * 14},
+        {"swcld.ssaliq1", ct::SSALIQ1, 58 * 14},  {"swcld.asyliq1", ct::ASYLIQ1, 58 * 14},
+        {"swcld.extice2", ct::EXTICE2, 43 * 14},  {"swcld.ssaice2", ct::SSAICE2, 43 * 14},
+        {"swcld.asyice2", ct::ASYICE2, 43 * 14},  {"swcld.extice3", ct::EXTICE3, 46 * 14},
+        {"swcld.ssaice3", ct::SSAICE3, 46 * 14},  {"swcld.asyice3", ct::ASYICE3, 46 * 14},
+        {"swcld.fdlice3", ct::FDLICE3, 46 * 14},  {"swcld.abari", ct::ABARI, 5},
+        {"swcld.bbari", ct::ABARI + 5, 5},        {"swcld.cbari", ct::ABARI + 10, 5},
+        {"swcld.dbari", ct::ABARI + 15, 5},       {"swcld.ebari", ct::ABARI + 20, 5},
+        {"swcld.fbari", ct::ABARI + 25, 5},       {"sw.wavenum2", ct::WAVENUM2, 14}};
+    for (const Part& p : parts) {
+      auto v = reals(m, p.name, err);
+      if (!err.empty()) return err;
+      if (v.size() != p.n) return std::string("cloud table malformed: ") + p.name;
+      std::copy(v.begin(), v.end(), T.cld.begin() + p.off);
+    }
   }
   return "";
 }

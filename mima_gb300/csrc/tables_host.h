@@ -13,6 +13,7 @@ struct HostTables {
   std::vector<double> lw_exp, lw_tfn, sw_exp;   // 0..10000 lookup tables
   std::vector<double> lw_tau;                   // optical depth of each LW table entry (rrtmg_lw_init.f90:115-122)
   std::vector<double> totplnk, totplnkderiv;    // (181, 16) Fortran order
+  std::vector<double> cld;                      // cloud optical property tables, ct:: offsets
   LwConst lw;
   SwConst sw;
 };

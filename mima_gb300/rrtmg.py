@@ -157,9 +157,11 @@ def array_sizes(ncol, nlay):
     n.update({k: ncol for k in _PER_COLUMN})
     n.update(emis=16 * ncol, tauaer_lw=16 * nlay * ncol, tauaer=14 * nlay * ncol, ssaaer=14 * nlay * ncol,
              asmaer=14 * nlay * ncol)
-    # clouds: cldfr, cicewp, cliqwp (nlay, ncol); LW taucld Fortran (16, ncol,
-    # nlay); SW taucld ("taucld_sw"), ssacld, asmcld, fsfcld Fortran (14, ncol, nlay)
-    n.update(cldfr=nlay * ncol, cicewp=nlay * ncol, cliqwp=nlay * ncol, taucld=16 * nlay * ncol)
+    # clouds: cldfr, cicewp, cliqwp, reice, reliq (nlay, ncol); LW taucld
+    # Fortran (16, ncol, nlay); SW taucld ("taucld_sw"), ssacld, asmcld, fsfcld
+    # Fortran (14, ncol, nlay)
+    n.update(cldfr=nlay * ncol, cicewp=nlay * ncol, cliqwp=nlay * ncol, taucld=16 * nlay * ncol,
+             reice=nlay * ncol, reliq=nlay * ncol)
     n.update({k: 14 * nlay * ncol for k in ("taucld_sw", "ssacld", "asmcld", "fsfcld")})
     return n
 
@@ -230,19 +232,26 @@ class RRTMG:
 
     def _check(self, rc):
         if rc != RRTMG_OK:
-            raise RRTMGError(rc, self.lib.rrtmg_gpu_last_error(self._h).decode())
+            raise RRTMGError(rc, self.last_error())
+
+    def last_error(self) -> str:
+        """The message of the handle's last failed call."""
+        return self.lib.rrtmg_gpu_last_error(self._h).decode()
 
     # ---------------- host-array drop-ins ----------------
     def rrtmg_lw(self, ncol, nlay, icld, idrv, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr,
                  ch4vmr=None, n2ovmr=None, o2vmr=None, cfc11vmr=None, cfc12vmr=None, cfc22vmr=None,
                  ccl4vmr=None, emis=None, tauaer=None, check=True, out=None, inflglw=0, cldfr=None, taucld=None,
-                 cicewp=None, cliqwp=None):
+                 cicewp=None, cliqwp=None, iceflglw=0, liqflglw=0, reice=None, reliq=None):
         """rrtmg_lw on host arrays; returns uflx, dflx, hr, uflxc, dflxc, hrc (+ duflx_dt, duflxc_dt).
         ``out`` optionally supplies the output arrays (float64, C-contiguous;
         page-locked arrays let the library overlap copies with kernels).
-        Clouds (icld = 1 random overlap, 2 / 3 maximum/random overlap;
-        inflglw = 0): cldfr, cicewp, cliqwp (nlay, ncol), taucld
-        (nlay, ncol, 16) = Fortran (16, ncol, nlay)."""
+        Clouds (icld = 1 random overlap, 2 / 3 maximum/random overlap):
+        cldfr, cicewp, cliqwp (nlay, ncol), and with inflglw = 0 taucld
+        (nlay, ncol, 16) = Fortran (16, ncol, nlay); inflglw = 1 forms the
+        depths from the water paths, inflglw = 2 from the ice (iceflglw 0-3)
+        and liquid (liqflglw 0-1) parameterisations with the effective sizes
+        reice, reliq (nlay, ncol)."""
         L, N = nlay, ncol
         ins = [_host(a) for a in (play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr,
                                   cfc11vmr, cfc12vmr, cfc22vmr, ccl4vmr, emis)]
@@ -251,10 +260,10 @@ class RRTMG:
             shapes.update(duflx_dt=L + 1, duflxc_dt=L + 1)
         out = _outputs(out, shapes, N)
         ta = _host(tauaer)
-        cl = [_host(a) for a in (cldfr, taucld, cicewp, cliqwp)]
+        cl = [_host(a) for a in (cldfr, taucld, cicewp, cliqwp, reice, reliq)]
         rc = self.lib.rrtmg_lw_c(
             self._h, C.c_int(N), C.c_int(L), C.c_int(icld), C.c_int(idrv), *[_hp(a) for a in ins],
-            C.c_int(inflglw), C.c_int(0), C.c_int(0), *[_hp(a) for a in cl], None, None, _hp(ta),
+            C.c_int(inflglw), C.c_int(iceflglw), C.c_int(liqflglw), *[_hp(a) for a in cl], _hp(ta),
             _hp(out["uflx"]), _hp(out["dflx"]), _hp(out["hr"]), _hp(out["uflxc"]), _hp(out["dflxc"]),
             _hp(out["hrc"]), _hp(out.get("duflx_dt")), _hp(out.get("duflxc_dt")))
         out["status"] = rc
@@ -265,22 +274,26 @@ class RRTMG:
     def rrtmg_sw(self, ncol, nlay, icld, iaer, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr,
                  n2ovmr, o2vmr, asdir, asdif, aldir, aldif, coszen, adjes, dyofyr, scon, tauaer=None,
                  ssaaer=None, asmaer=None, check=True, out=None, inflgsw=0, cldfr=None, taucld=None, ssacld=None,
-                 asmcld=None, fsfcld=None, cicewp=None, cliqwp=None):
+                 asmcld=None, fsfcld=None, cicewp=None, cliqwp=None, iceflgsw=0, liqflgsw=0, reice=None,
+                 reliq=None):
         """rrtmg_sw on host arrays; returns swuflx, swdflx, swhr, swuflxc,
-        swdflxc, swhrc.  Clouds (icld >= 1, inflgsw = 0; every sunlit layer
-        clear or overcast): cldfr, cicewp, cliqwp (nlay, ncol); taucld, ssacld,
-        asmcld, fsfcld (nlay, ncol, 14) = Fortran (14, ncol, nlay)."""
+        swdflxc, swhrc.  Clouds (icld >= 1; every sunlit layer clear or
+        overcast): cldfr, cicewp, cliqwp (nlay, ncol); with inflgsw = 0 taucld,
+        ssacld, asmcld, fsfcld (nlay, ncol, 14) = Fortran (14, ncol, nlay);
+        inflgsw = 2 forms the optics from the ice (iceflgsw 1-3) and liquid
+        (liqflgsw 1) parameterisations with the effective sizes reice, reliq
+        (nlay, ncol)."""
         L, N = nlay, ncol
         ins = [_host(a) for a in (play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr,
                                   asdir, asdif, aldir, aldif, coszen)]
         aer = [_host(a) for a in (tauaer, ssaaer, asmaer)]
-        cl = [_host(a) for a in (cldfr, taucld, ssacld, asmcld, fsfcld, cicewp, cliqwp)]
+        cl = [_host(a) for a in (cldfr, taucld, ssacld, asmcld, fsfcld, cicewp, cliqwp, reice, reliq)]
         out = _outputs(out, {"swuflx": L + 1, "swdflx": L + 1, "swuflxc": L + 1, "swdflxc": L + 1, "swhr": L,
                              "swhrc": L}, N)
         rc = self.lib.rrtmg_sw_c(
             self._h, C.c_int(N), C.c_int(L), C.c_int(icld), C.c_int(iaer), *[_hp(a) for a in ins],
-            C.c_double(adjes), C.c_int(dyofyr), C.c_double(scon), C.c_int(inflgsw), C.c_int(0), C.c_int(0),
-            *[_hp(a) for a in cl], None, None, *[_hp(a) for a in aer], None,
+            C.c_double(adjes), C.c_int(dyofyr), C.c_double(scon), C.c_int(inflgsw), C.c_int(iceflgsw),
+            C.c_int(liqflgsw), *[_hp(a) for a in cl], *[_hp(a) for a in aer], None,
             _hp(out["swuflx"]), _hp(out["swdflx"]), _hp(out["swhr"]), _hp(out["swuflxc"]),
             _hp(out["swdflxc"]), _hp(out["swhrc"]))
         out["status"] = rc
@@ -291,24 +304,30 @@ class RRTMG:
     # Convenience: whole Atmosphere objects (mima_gb300.atmosphere)
     def lw(self, atm, idrv=0, tauaer=None, check=True, cloud=None, icld=1):
         """``cloud``: dict(cldfr, taucld[, cicewp, cliqwp]) (given cloud optical
-        depths, as rrtmg_lw's arguments) with overlap ``icld`` (1 random, 2 / 3
-        maximum/random)."""
+        depths, as rrtmg_lw's arguments), or with ``inflag`` 1 / 2 (and
+        ``iceflag``, ``liqflag``, ``reice``, ``reliq``) the cloud physics, with
+        overlap ``icld`` (1 random, 2 / 3 maximum/random)."""
         cl = cloud or {}
         return self.rrtmg_lw(atm.ncol, atm.nlay, icld if cloud else 0, idrv, atm.play, atm.plev, atm.tlay, atm.tlev,
                              atm.tsfc, atm.h2o, atm.o3, atm.co2, atm.ch4, atm.n2o, atm.o2, atm.cfc11, atm.cfc12,
                              atm.cfc22, atm.ccl4, atm.emis, tauaer, check=check, cldfr=cl.get("cldfr"),
-                             taucld=cl.get("taucld"), cicewp=cl.get("cicewp"), cliqwp=cl.get("cliqwp"))
+                             taucld=cl.get("taucld"), cicewp=cl.get("cicewp"), cliqwp=cl.get("cliqwp"),
+                             inflglw=int(cl.get("inflag", 0)), iceflglw=int(cl.get("iceflag", 0)),
+                             liqflglw=int(cl.get("liqflag", 0)), reice=cl.get("reice"), reliq=cl.get("reliq"))
 
     def sw(self, atm, iaer=0, tauaer=None, ssaaer=None, asmaer=None, check=True, cloud=None):
         """``cloud``: dict(cldfr, taucld, ssacld, asmcld, fsfcld[, cicewp,
-        cliqwp]) for icld = 1 (given cloud optics), as rrtmg_sw's arguments."""
+        cliqwp]) for icld = 1 (given cloud optics), as rrtmg_sw's arguments, or
+        dict(cldfr, cicewp, cliqwp, reice, reliq, inflag=2, iceflag, liqflag)
+        (cloud physics)."""
         cl = cloud or {}
         return self.rrtmg_sw(atm.ncol, atm.nlay, 1 if cloud else 0, iaer, atm.play, atm.plev, atm.tlay, atm.tlev,
                              atm.tsfc, atm.h2o, atm.o3, atm.co2, atm.ch4, atm.n2o, atm.o2, atm.asdir, atm.asdif,
                              atm.aldir, atm.aldif, atm.coszen, atm.adjes, atm.dyofyr, atm.scon,
-                             tauaer, ssaaer, asmaer, check=check,
+                             tauaer, ssaaer, asmaer, check=check, inflgsw=int(cl.get("inflag", 0)),
+                             iceflgsw=int(cl.get("iceflag", 0)), liqflgsw=int(cl.get("liqflag", 0)),
                              **{k: cl.get(k) for k in ("cldfr", "taucld", "ssacld", "asmcld", "fsfcld", "cicewp",
-                                                       "cliqwp")})
+                                                       "cliqwp", "reice", "reliq")})
 
     # ---------------- device-array entry points ----------------
     def _ptrs(self, ncol, nlay, *dicts):
@@ -323,17 +342,19 @@ class RRTMG:
             return _dptr(t, n[k], k, self.device)
         return p
 
-    def rrtmg_lw_dev(self, stream, ncol, nlay, icld, idrv, d, out, tauaer=None):
-        """``d``/``out``: dicts of CUDA tensors with the argument names of rrtmg_lw."""
+    def rrtmg_lw_dev(self, stream, ncol, nlay, icld, idrv, d, out, tauaer=None, inflglw=0, iceflglw=0,
+                     liqflglw=0):
+        """``d``/``out``: dicts of CUDA tensors with the argument names of
+        rrtmg_lw (clouds: cldfr, taucld, cicewp, cliqwp, reice, reliq)."""
         g = self._ptrs(ncol, nlay, d)
         o = self._ptrs(ncol, nlay, out)
         rc = self.lib.rrtmg_lw_dev(
             self._h, C.c_void_p(stream or 0), C.c_int(ncol), C.c_int(nlay), C.c_int(icld), C.c_int(idrv),
             g("play"), g("plev"), g("tlay"), g("tlev"), g("tsfc"), g("h2ovmr"), g("o3vmr"), g("co2vmr"),
             g("ch4vmr"), g("n2ovmr"), g("o2vmr"), g("cfc11vmr"), g("cfc12vmr"), g("cfc22vmr"), g("ccl4vmr"),
-            g("emis"), C.c_int(0), C.c_int(0), C.c_int(0), g("cldfr"), g("taucld"), g("cicewp"), g("cliqwp"),
-            None, None, g("tauaer_lw", tauaer), o("uflx"), o("dflx"), o("hr"), o("uflxc"), o("dflxc"), o("hrc"),
-            o("duflx_dt"), o("duflxc_dt"))
+            g("emis"), C.c_int(inflglw), C.c_int(iceflglw), C.c_int(liqflglw), g("cldfr"), g("taucld"),
+            g("cicewp"), g("cliqwp"), g("reice"), g("reliq"), g("tauaer_lw", tauaer), o("uflx"), o("dflx"),
+            o("hr"), o("uflxc"), o("dflxc"), o("hrc"), o("duflx_dt"), o("duflxc_dt"))
         self._check(rc)
 
     def set_profiling(self, on: bool):
@@ -414,19 +435,21 @@ class RRTMG:
     def rrtmg_sw_dev(self, stream, ncol, nlay, icld, iaer, d, out, adjes, dyofyr, scon, cloud=None):
         """``d``/``out``: dicts of CUDA tensors with the argument names of
         rrtmg_sw; ``cloud`` (icld >= 1): dict of CUDA tensors cldfr, taucld,
-        ssacld, asmcld, fsfcld[, cicewp, cliqwp] (shapes as rrtmg_sw's)."""
+        ssacld, asmcld, fsfcld[, cicewp, cliqwp] (shapes as rrtmg_sw's), or for
+        the cloud physics cldfr, cicewp, cliqwp, reice, reliq with the ints
+        inflag = 2, iceflag, liqflag."""
         g = self._ptrs(ncol, nlay, d)
         o = self._ptrs(ncol, nlay, out)
         cl = cloud or {}
         c = [g(k, cl.get(k)) for k in ("cldfr",)] + [g(k + "_sw" if k == "taucld" else k, cl.get(k))
                                                      for k in ("taucld", "ssacld", "asmcld", "fsfcld")]
-        c += [g(k, cl.get(k)) for k in ("cicewp", "cliqwp")]
+        c += [g(k, cl.get(k)) for k in ("cicewp", "cliqwp", "reice", "reliq")]
+        fl = [C.c_int(int(cl.get(k, 0))) for k in ("inflag", "iceflag", "liqflag")]
         rc = self.lib.rrtmg_sw_dev(
             self._h, C.c_void_p(stream or 0), C.c_int(ncol), C.c_int(nlay), C.c_int(icld), C.c_int(iaer),
             g("play"), g("plev"), g("tlay"), g("tlev"), g("tsfc"), g("h2ovmr"), g("o3vmr"), g("co2vmr"),
             g("ch4vmr"), g("n2ovmr"), g("o2vmr"), g("asdir"), g("asdif"), g("aldir"), g("aldif"),
-            g("coszen"), C.c_double(adjes), C.c_int(dyofyr), C.c_double(scon), C.c_int(0), C.c_int(0),
-            C.c_int(0), *c, None, None, g("tauaer"), g("ssaaer"),
+            g("coszen"), C.c_double(adjes), C.c_int(dyofyr), C.c_double(scon), *fl, *c, g("tauaer"), g("ssaaer"),
             g("asmaer"), None, o("swuflx"), o("swdflx"), o("swhr"), o("swuflxc"), o("swdflxc"), o("swhrc"))
         self._check(rc)
 

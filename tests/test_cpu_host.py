@@ -247,10 +247,12 @@ def test_device_wrappers_follow_the_header():
     # rrtmg_lw_dev: the LW aerosol argument is the tauaer keyword
     r.rrtmg_lw_dev(0, ncol, nlay, 0, 1, fake, fake, tauaer=fake["tauaer_lw"])
     exp = {k: ptr[k] for k in _header_params("rrtmg_lw_dev") if k in ptr and k != "tauaer"}
-    # the cloud arrays of icld = 1 (given optical depths) pass through; the
-    # cloud-physics radii do not (inflglw = 0 only)
-    exp.update({"tauaer": ptr["tauaer_lw"], "reice": None, "reliq": None})
+    # the cloud arrays, the cloud-physics sizes among them, pass through by name
+    exp.update({"tauaer": ptr["tauaer_lw"]})
     _check_positions(r.lib.calls["rrtmg_lw_dev"], _header_params("rrtmg_lw_dev"), exp)
+    r.rrtmg_lw_dev(0, ncol, nlay, 2, 1, fake, fake, inflglw=2, iceflglw=3, liqflglw=1)
+    call, par = r.lib.calls["rrtmg_lw_dev"], _header_params("rrtmg_lw_dev")
+    assert [call[par.index(k)].value for k in ("inflglw", "iceflglw", "liqflglw")] == [2, 3, 1]
     r.rrtmg_lw_dev_static(0, ncol, nlay, 0, 1, fake, fake, tauaer=None)
     exp.update({"tauaer": None, **{k: None for k in cloud_lw}})
     _check_positions(r.lib.calls["rrtmg_lw_dev_static"], _header_params("rrtmg_lw_dev_static"), exp)
@@ -267,6 +269,15 @@ def test_device_wrappers_follow_the_header():
     exp.update({k: C.cast(t.data_ptr(), C.c_void_p).value for k, t in cl.items()})
     exp.update(cliqwp=None)
     _check_positions(r.lib.calls["rrtmg_sw_dev"], p, exp)
+    # cloud physics: the sizes and the flags of the cloud keyword
+    phys = {"cldfr": fake["cldfr"], "cicewp": fake["cicewp"], "cliqwp": fake["cliqwp"], "reice": fake["reice"],
+            "reliq": fake["reliq"], "inflag": 2, "iceflag": 3, "liqflag": 1}
+    r.rrtmg_sw_dev(0, ncol, nlay, 1, 0, fake, fake, 1.0, 0, 1360.0, cloud=phys)
+    exp.update({k: ptr[k] for k in ("cldfr", "cicewp", "cliqwp", "reice", "reliq")})
+    exp.update(taucld=None, ssacld=None, asmcld=None, fsfcld=None)
+    call = r.lib.calls["rrtmg_sw_dev"]
+    _check_positions(call, p, exp)
+    assert [call[p.index(k)].value for k in ("inflgsw", "iceflgsw", "liqflgsw")] == [2, 3, 1]
     with pytest.raises(ValueError):  # a per-layer array is too small for the 14-band taucld
         r.rrtmg_sw_dev(0, ncol, nlay, 1, 0, fake, fake, 1.0, 0, 1360.0, cloud={**cl, "taucld": fake["cldfr"]})
     # rrtmg_step_dev

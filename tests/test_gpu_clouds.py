@@ -170,8 +170,10 @@ def test_lw_cloud_options_not_computed_are_refused(gpu):
     base = (atm.play, atm.plev, atm.tlay, atm.tlev, atm.tsfc, atm.h2o, atm.o3, atm.co2)
     o = gpu.rrtmg_lw(*args, 4, 0, *base, check=False, cldfr=cl["cldfr"], taucld=cl["taucld"])
     assert o["status"] == R.RRTMG_ERR_UNSUPPORTED  # icld outside 0..3
+    o = gpu.rrtmg_lw(*args, 1, 0, *base, check=False, inflglw=3, cldfr=cl["cldfr"], taucld=cl["taucld"])
+    assert o["status"] == R.RRTMG_ERR_UNSUPPORTED  # cldprop has no inflag = 3
     o = gpu.rrtmg_lw(*args, 1, 0, *base, check=False, inflglw=2, cldfr=cl["cldfr"], taucld=cl["taucld"])
-    assert o["status"] == R.RRTMG_ERR_UNSUPPORTED  # cloud physics (cldprop inflag = 2)
+    assert o["status"] == R.RRTMG_ERR_ARG  # cloud physics without water paths and sizes
     o = gpu.rrtmg_lw(*args, 1, 0, *base, check=False, cldfr=cl["cldfr"])
     assert o["status"] == R.RRTMG_ERR_ARG  # no cloud optical depths
     assert gpu.lw(atm, cloud=cl)["status"] == R.RRTMG_OK
@@ -339,8 +341,10 @@ def test_sw_cloud_options_not_computed_are_refused(gpu):
     base = (atm.play, atm.plev, atm.tlay, atm.tlev, atm.tsfc, atm.h2o, atm.o3, atm.co2, atm.ch4, atm.n2o,
             atm.o2, atm.asdir, atm.asdif, atm.aldir, atm.aldif, atm.coszen, atm.adjes, atm.dyofyr, atm.scon)
     args = (atm.ncol, atm.nlay)
+    o = gpu.rrtmg_sw(*args, 1, 0, *base, check=False, inflgsw=1, **cl)
+    assert o["status"] == R.RRTMG_ERR_UNSUPPORTED  # cldprop_sw has no inflag = 1 branch
     o = gpu.rrtmg_sw(*args, 1, 0, *base, check=False, inflgsw=2, **cl)
-    assert o["status"] == R.RRTMG_ERR_UNSUPPORTED  # cloud physics (cldprop_sw inflag = 2)
+    assert o["status"] == R.RRTMG_ERR_UNSUPPORTED  # cloud physics with iceflgsw = 0
     o = gpu.rrtmg_sw(*args, 4, 0, *base, check=False, **cl)
     assert o["status"] == R.RRTMG_ERR_UNSUPPORTED  # icld outside 0..3
     o = gpu.rrtmg_sw(*args, 1, 0, *base, check=False, cldfr=cl["cldfr"], taucld=cl["taucld"])

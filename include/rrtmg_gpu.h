@@ -26,22 +26,30 @@
  *   - Clouds: rrtmg_lw_c / rrtmg_lw_dev compute icld = 1 (random overlap,
  *     rrtmg_lw_rtrn.f90) and icld = 2 / 3 (maximum/random overlap,
  *     rrtmg_lw_rtrnmr.f90, where the non-McICA driver sends both,
- *     rrtmg_lw_rad.nomcica.f90:527-541) with the cloud optical depths given
- *     (inflglw = 0, rrtmg_lw_cldprop.f90:165-171): cldfr (ncol,nlay), taucld (16,ncol,nlay),
- *     cicewp / cliqwp (ncol,nlay) or NULL (they only decide, with the band sum
- *     of taucld, whether a layer's depths are kept); reice, reliq and the ice /
- *     liquid flags are unused.  rrtmg_sw_c / rrtmg_sw_dev compute icld = 1,
- *     2, 3 (identical without McICA) with the cloud optics given
- *     (inflgsw = 0, rrtmg_sw_cldprop.f90:142-156): cldfr (ncol,nlay); taucld,
- *     ssacld, asmcld, fsfcld (14,ncol,nlay); cicewp / cliqwp or NULL.  As the
- *     reference's non-McICA SW (rrtmg_sw_rad.nomcica.f90:533-538), every layer
- *     of a sunlit column must be clear or overcast (cldfr <= 1e-6 or
- *     >= 1 - 1e-6): a partly cloudy one is reported as RRTMG_ERR_INPUT, where
- *     the reference stops the program.  Every other entry point is clear sky
- *     (icld = 0).  The reference coerces icld and iaer silently (:437,
- *     :471-479); this library returns RRTMG_ERR_UNSUPPORTED for any
- *     configuration it does not compute (inflglw or inflgsw = 1 / 2, icld
- *     outside 0..3) and never falls back to a CPU path.
+ *     rrtmg_lw_rad.nomcica.f90:527-541) with cldprop's options
+ *     (rrtmg_lw_cldprop.f90:155-270): inflglw = 0 cloud optical depths
+ *     given, taucld (16,ncol,nlay); 1 abscld1 x (cicewp + cliqwp); 2 the ice
+ *     (iceflglw 0-3) and liquid (liqflglw 0-1) parameterisations with the
+ *     effective sizes reice / reliq (ncol,nlay, microns).  cldfr (ncol,nlay)
+ *     always; cicewp / cliqwp (ncol,nlay, g/m2) required for inflglw 1 / 2,
+ *     else NULL or given (they decide, with the band sum of taucld, whether a
+ *     layer's optics are formed).  rrtmg_sw_c / rrtmg_sw_dev compute icld = 1,
+ *     2, 3 (identical without McICA) with cldprop_sw's options
+ *     (rrtmg_sw_cldprop.f90:118-340): inflgsw = 0 cloud optics given, taucld,
+ *     ssacld, asmcld, fsfcld (14,ncol,nlay); 2 the ice (iceflgsw 1-3) and
+ *     liquid (liqflgsw 1) parameterisations with cicewp / cliqwp and reice /
+ *     reliq.  As the reference's non-McICA SW (rrtmg_sw_rad.nomcica.f90:
+ *     533-538), every layer of a sunlit column must be clear or overcast
+ *     (cldfr <= 1e-6 or >= 1 - 1e-6): a partly cloudy one is reported as
+ *     RRTMG_ERR_INPUT, where the reference stops the program; so is an
+ *     effective size outside its parameterisation's table (or not a number)
+ *     or a cloud optical property outside its physical range in a layer whose
+ *     optics are formed (cldprop / cldprop_sw stop).  Every other entry point
+ *     is clear sky (icld = 0).  The reference coerces icld and iaer silently
+ *     (:437, :471-479); this library returns RRTMG_ERR_UNSUPPORTED for any
+ *     configuration it does not compute (icld outside 0..3, inflglw outside
+ *     0..2, inflgsw other than 0 / 2, SW cloud physics with iceflgsw outside
+ *     1..3 or liqflgsw other than 1) and never falls back to a CPU path.
  *   - Every entry point returns a status (0 = success).  A handle is not
  *     thread-safe; use one handle per host thread.
  */
@@ -57,12 +65,13 @@ typedef struct rrtmg_gpu_state* rrtmg_gpu_handle;
 enum rrtmg_gpu_status {
   RRTMG_OK = 0,
   RRTMG_ERR_ARG = 1,          /* bad dimension, null required pointer, bad handle */
-  RRTMG_ERR_UNSUPPORTED = 2,  /* icld not in 0..3, cloud physics (inflglw/inflgsw != 0), iaer not in {0,10},
-                                 idrv not in {0,1} */
+  RRTMG_ERR_UNSUPPORTED = 2,  /* icld not in 0..3, a cloud option not computed (inflglw not in 0..2, inflgsw
+                                 not 0 / 2, SW iceflgsw / liqflgsw), iaer not in {0,10}, idrv not in {0,1} */
   RRTMG_ERR_CUDA = 3,         /* CUDA runtime error (see rrtmg_gpu_last_error) */
   RRTMG_ERR_TABLES = 4,       /* table blob missing, malformed or checksum mismatch */
-  RRTMG_ERR_INPUT = 5,        /* device-side validation flagged a non-finite or out-of-range input, or a
-                                 partly cloudy sunlit layer in a SW call with clouds */
+  RRTMG_ERR_INPUT = 5,        /* device-side validation flagged a non-finite or out-of-range input, a
+                                 partly cloudy sunlit layer in a SW call with clouds, or a cloud size or
+                                 optical property outside its parameterisation's range */
   RRTMG_ERR_NOMEM = 6         /* device workspace allocation failed */
 };
 

@@ -61,6 +61,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint cost measurement")
     ap.add_argument("--no-driver", action="store_true", help="skip the run_rrtmg (GCM slab) measurement")
+    ap.add_argument("--no-clouds", action="store_true", help="skip the cloudy-step measurement")
     ap.add_argument("--members", type=int, default=32, help="stress configuration (4): ensemble members")
     ap.add_argument("--stress-adjoint", default="split", choices=["split", "fp64"],
                     help="stress configuration (4): precision of the adjoint")
@@ -403,6 +404,57 @@ def measure_adjoint(torch, rrtmg, atmosphere, r, stream, atm, d, olw, osw, flush
                          "forward_plus_jacobian_over_forward": (ms_f3 + ms_j) / ms_f3}}
 
 
+def measure_clouds(torch, rrtmg, atmosphere, r, stream, atm, d, flush, steps, warmup, dev):
+    """The cloudy step on the same columns: seeded overcast clouds with the
+    cloud physics (LW maximum/random overlap, cldprop inflag 2 with Fu ice and
+    Hu-Stamnes liquid; SW cldprop_sw inflag 2, the same parameterisations),
+    LW then SW on one stream (no graph), FP32-split and FP64, L2 flushed
+    before each step; beside it the clear-sky step timed the same way.  The
+    split outputs' error against the FP64 ones."""
+    cl = atmosphere.cloud_physics_fields(atm, seed=2024)
+    dc = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in cl.items()}
+    flags = dict(inflag=2, iceflag=3, liqflag=1)
+    dl = dict(d, **dc)
+    outs = {pr: rrtmg.device_outputs(atm.ncol, atm.nlay, dev) for pr in ("split", "fp64")}
+
+    def cloudy(pr):
+        olw, osw = outs[pr]
+        r.rrtmg_lw_dev(stream.cuda_stream, atm.ncol, atm.nlay, 2, 0, dl, olw, inflglw=2, iceflglw=3, liqflglw=1)
+        r.rrtmg_sw_dev(stream.cuda_stream, atm.ncol, atm.nlay, 1, 0, d, osw, atm.adjes, atm.dyofyr, atm.scon,
+                       cloud=dict(dc, **flags))
+
+    res = {}
+    try:
+        for pr in ("split", "fp64"):
+            r.set_precision(pr)
+            n = steps if pr == "split" else max(2, steps // 4)
+            res[pr] = time_calls(torch, stream, flush, lambda: cloudy(pr), n, warmup)
+            if r.sync_status(stream.cuda_stream) != 0:
+                return {"status": "error", "message": r.last_error()}
+        r.set_precision("split")
+        olw, osw = outs["split"]
+        clear_ms = time_calls(torch, stream, flush, lambda: dev_step(r, stream, atm, d, olw, osw), steps, warmup)
+        cloudy("split")
+        torch.cuda.synchronize()
+    finally:
+        r.set_precision("split")
+    (l32, s32), (l64, s64) = outs["split"], outs["fp64"]
+    hr = float((l32["hr"] - l64["hr"]).abs().max())
+    shr = float((s32["swhr"] - s64["swhr"]).abs().max())
+    olr = float((l32["uflx"][-1] - l64["uflx"][-1]).abs().max())
+    sfc = max(float((l32[k][0] - l64[k][0]).abs().max()) for k in ("uflx", "dflx"))
+    sfc = max(sfc, max(float((s32[k][0] - s64[k][0]).abs().max()) for k in ("swuflx", "swdflx")))
+    return {"workload": (f"{atm.ncol} columns x {atm.nlay} layers, {100 * float(cl['cldfr'].mean()):.1f} % of the "
+                         "layers overcast; LW icld 2 inflglw 2 (iceflglw 3, liqflglw 1), SW icld 1 inflgsw 2 "
+                         "(iceflgsw 3, liqflgsw 1)"),
+            "split_ms": res["split"], "columns_per_s": atm.ncol / (res["split"] * 1e-3),
+            "fp64_ms": res["fp64"], "split_over_fp64": res["fp64"] / res["split"],
+            "clear_sky_same_calls_ms": clear_ms,
+            "error_vs_fp64": {"lw_hr_max_kday": hr, "sw_hr_max_kday": shr, "olr_max_wm2": olr,
+                              "sfc_flux_max_wm2": sfc},
+            "timing": "LW then SW device calls on one stream, CUDA events, L2 flushed before each step"}
+
+
 def measure_driver(torch, rrtmg, atmosphere, r, stream, dev, flush, steps, warmup, lw_sw_ms):
     """MiMA's whole radiation step (run_rrtmg with interp_temp and the zenith
     angle) on a T85 GCM slab of 256 x 128 points x 40 levels, FP32-split:
@@ -628,6 +680,11 @@ def run_ours(args):
         adjoint = measure_adjoint(torch, rrtmg, atmosphere, r, stream, atm, d, olw64, osw64, flush,
                                   max(3, args.steps // 4), min(args.warmup, 3))
 
+    clouds = None
+    if not args.no_clouds:
+        clouds = measure_clouds(torch, rrtmg, atmosphere, r, stream, atm, d, flush, max(3, args.steps // 4),
+                                min(args.warmup, 3), dev)
+
     driver = None
     if not args.no_driver:
         # the driver slab is the T85 x 40 grid: its LW + SW step is this run's
@@ -722,6 +779,8 @@ def run_ours(args):
         line["adjoint"] = adjoint
     if driver:
         line["driver"] = driver
+    if clouds:
+        line["clouds"] = clouds
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -216,6 +216,26 @@ def small_atmosphere(ncol: int, nlay: int = 40, seed: int = 7, ts_sigma: float =
     return atm
 
 
+
+def cloud_physics_fields(atm: Atmosphere, seed: int) -> dict:
+    """Seeded overcast clouds for the cloud-physics paths, (nlay, ncol) arrays:
+    about 35 % of the layers below 100 hPa overcast (cover 1, so that the
+    non-McICA SW takes them too); ice water path up to ~120 g/m2 above
+    600 hPa, liquid up to ~140 g/m2 below 300 hPa (both in between), one
+    cloudy layer in twenty without water; ice effective sizes 14-125 um and
+    liquid radii 3-55 um, inside every parameterisation's range."""
+    rng = np.random.default_rng(seed)
+    L, n = atm.nlay, atm.ncol
+    cf = np.where((rng.uniform(size=(L, n)) < 0.35) & (atm.play > 100.0), 1.0, 0.0)
+    ciwp = np.where(atm.play < 600.0, rng.uniform(0.0, 40.0, (L, n)) ** 1.3, 0.0)
+    clwp = np.where(atm.play > 300.0, rng.uniform(0.0, 60.0, (L, n)) ** 1.2, 0.0)
+    dry = rng.uniform(size=(L, n)) < 0.05
+    ciwp[dry] = 0.0
+    clwp[dry] = 0.0
+    return dict(cldfr=cf, cicewp=ciwp, cliqwp=clwp, reice=rng.uniform(14.0, 125.0, (L, n)),
+                reliq=rng.uniform(3.0, 55.0, (L, n)))
+
+
 @dataclass
 class GcmSlab:
     """One GCM slab as MiMA's ``run_rrtmg`` receives it

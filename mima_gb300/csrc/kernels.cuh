@@ -1728,23 +1728,39 @@ __device__ __forceinline__ void sw_exp_pair(R ze1, R bpade, const float* __restr
 // zwo = zw without the two divisions.  pdbt (optional): e^{-t/mu}, the value
 // the direct-beam lookup of spcvrt_sw (rrtmg_sw_spcvrt.f90:496-507) takes for
 // the same argument (its missing 500 cap changes nothing in FP32, where both
-// table ends are 0).
+// table ends are 0).  cw (optional, >= 0): the co-albedo 1 - zw formed
+// without cancellation by the caller.  An FP32 albedo within 1e-5 of 1 holds
+// its co-albedo to a few per cent only, and the absorptance of an optically
+// thick, nearly conservative layer (a cloud) scales with it; with cw the
+// conservative-branch test is made on the co-albedo of zwo, 1 - zwo =
+// cw (1 - r^2) / (1 - cw r^2), as the reference's FP64 test resolves it.
 template <class R>
 __device__ __forceinline__ void reftra_split(R zto1, R zw, R zg, R prmuz, R bpade, const float* __restrict__ exptbl,
                                              bool analytic, R& pref, R& prefd, R& ptra, R& ptrad,
-                                             bool zg_zero = false, R* pdbt = nullptr) {
+                                             bool zg_zero = false, R* pdbt = nullptr, R cw = (R)-1.) {
   const R eps = (R)1.e-08, zwcrit = (R)0.9999995;
   const R zg3 = (R)3. * zg;
   const R zgamma1 = ((R)8. - zw * ((R)5. + zg3)) * (R)0.25;
   const R zgamma2 = (R)3. * (zw * ((R)1. - zg)) * (R)0.25;
   const R zgamma3 = ((R)2. - zg3 * prmuz) * (R)0.25;
   const R zgamma4 = (R)1. - zgamma3;
-  R zwo = zw;
-  if (!zg_zero) {
-    const R r = zg / ((R)1. - zg);
-    zwo = zw / ((R)1. - ((R)1. - zw) * (r * r));
+  const bool own_cw = cw >= (R)0.;
+  if (!own_cw) cw = (R)1. - zw;
+  bool conservative;
+  if (own_cw) {
+    // zwo = zw / den: a negative den makes zwo negative, a zero one infinite
+    const R r2 = zg_zero ? (R)0. : (zg / ((R)1. - zg)) * (zg / ((R)1. - zg));
+    const R den = (R)1. - cw * r2;
+    conservative = den > (R)0. ? cw * ((R)1. - r2) <= (R)(1. - 0.9999995) * den : den == (R)0.;
+  } else {
+    R zwo = zw;
+    if (!zg_zero) {
+      const R r = zg / ((R)1. - zg);
+      zwo = zw / ((R)1. - cw * (r * r));
+    }
+    conservative = zwo >= zwcrit;
   }
-  if (zwo >= zwcrit) {
+  if (conservative) {
     const R za1 = zgamma1 * prmuz - zgamma3;
     const R zgt = zgamma1 * zto1;
     R ze2, m2;
@@ -1763,7 +1779,7 @@ __device__ __forceinline__ void reftra_split(R zto1, R zw, R zg, R prmuz, R bpad
   } else {
     const R za1 = zgamma1 * zgamma4 + zgamma2 * zgamma3;
     const R za2 = zgamma1 * zgamma3 + zgamma2 * zgamma4;
-    const R zrk = sqrt(((R)2. * ((R)1. - zw)) * (zgamma1 + zgamma2));
+    const R zrk = sqrt(((R)2. * cw) * (zgamma1 + zgamma2));
     const R zrp = zrk * prmuz;
     const R zrp1 = (R)1. + zrp, zrm1 = (R)1. - zrp, zrk2 = (R)2. * zrk, zrpp = (R)1. - zrp * zrp;
     const R zr1 = zrm1 * (za2 + zrk * zgamma3);
@@ -1859,10 +1875,13 @@ __device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, dou
     R taug, taur;
     sw_gas<B, R>(c_sw, L, ix, ikl <= lt, gg, tab, taug, taur);
     R taua = (R)0., omga = (R)1., asya = (R)0.;
+    R cwa = (R)0.;  // the aerosol co-albedo 1 - omga, formed in FP64 (cloudy split pass)
     if (iaer == 10) {
       const size_t oa = c + N * ((size_t)(ikl - 1) + (size_t)nlay * (ibm - 1));
       taua = (R)__ldg(in.tauaer + oa);
-      omga = (R)__ldg(in.ssaaer + oa);
+      const double ssaa = __ldg(in.ssaaer + oa);
+      omga = (R)ssaa;
+      if constexpr (TOT && sizeof(R) == 4) cwa = (R)(1.0 - ssaa);
       asya = (R)__ldg(in.asmaer + oa);
     }
     R ztauc = taur + taug + taua;
@@ -1886,6 +1905,7 @@ __device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, dou
       // cloud optics where the mask keeps them, else tau 0, ssa 1, g 0
       const R pclfr = __ldg(cld + o);
       R ptauc = (R)0., pomgc = (R)1., pasyc = (R)0.;
+      R pcw = (R)0.;  // split path: the cloud's delta-scaled co-albedo 1 - pomgc
       if (__ldg(cld + fstride + o) > (R)0.) {
         const size_t q = (size_t)(ibm - 1) + 14 * o;
         const R taucldorig = (R)__ldg(in.taucld + q), ffp = in.fsfcld ? (R)__ldg(in.fsfcld + q) : (R)0.;
@@ -1895,6 +1915,11 @@ __device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, dou
         pomgc = ffp1 * ssac / ffpssa;
         ptauc = ffpssa * taucldorig;
         pasyc = (asmc - ffp) / (ffp1);
+        if constexpr (sizeof(R) == 4) {
+          // 1 - ffp1 ssac / ffpssa = (1 - ssac) / (1 - ffp ssac), from the FP64 inputs
+          const double ssad = __ldg(in.ssacld + q), ffpd = in.fsfcld ? __ldg(in.fsfcld + q) : 0.0;
+          pcw = (R)((1.0 - ssad) / (1.0 - ffpd * ssad));
+        }
       }
       // total-sky optics (spcvrt_sw :459-464), reftra only for cloudy layers
       // (pclfr > repclc = 1e-12, :388; reftra gives 0, 1, 0, 1 otherwise)
@@ -1904,10 +1929,17 @@ __device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, dou
       zomco = zomco / ztauo;
       R rfo = (R)0., rfdo = (R)0., tro = (R)1., trdo = (R)1.;
       if (pclfr > (R)1.e-12) {
-        if constexpr (sizeof(R) == 4)
-          reftra_split(ztauo, zomco, zgco, prmu0, bpade, exptbl, analytic, rfo, rfdo, tro, trdo, false);
-        else
+        if constexpr (sizeof(R) == 4) {
+          // the total co-albedo from the clear one (gas absorption and aerosol
+          // co-albedo over the depth, through the delta-M scaling: 1 - w' =
+          // (1 - w) / (1 - f w)) and the cloud's, without cancellation
+          const R cwc = (taug + taua * cwa) / ((taur + taug + taua) * ((R)1.0 - zwf));
+          const R cwo = (ztauc * cwc + ptauc * pcw) / ztauo;
+          reftra_split(ztauo, zomco, zgco, prmu0, bpade, exptbl, analytic, rfo, rfdo, tro, trdo, false, (R*)nullptr,
+                       cwo);
+        } else {
           reftra1<R, R>(ztauo, zomco, zgco, prmu0, bpade, exptbl, analytic, rfo, rfdo, tro, trdo);
+        }
       }
       const R zdbtmo = sw_exp_tbl<R, R>(ztauo / prmu0, bpade, exptbl, analytic);
       const R zclear = (R)1.0 - pclfr, zcloud = pclfr;

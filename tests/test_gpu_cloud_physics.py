@@ -224,3 +224,27 @@ def test_cloud_physics_options_refused(gpu):
     assert gpu.lw(atm, cloud=_phys(no_sizes, 2, 2, 1), check=False)["status"] == R.RRTMG_ERR_ARG
     assert gpu.sw(atm, cloud=_phys(no_sizes, 2, 2, 1), check=False)["status"] == R.RRTMG_ERR_ARG
     assert gpu.lw(atm, cloud=_phys(no_sizes, 1, 0, 0))["status"] == R.RRTMG_OK  # inflag 1 needs no sizes
+
+
+def test_cloud_physics_split_t85_full_grid(gpu, orc):
+    """The benchmark's cloudy step (T85 x 40, every column, the seeded
+    overcast clouds of atmosphere.cloud_physics_fields with Fu ice and
+    Hu-Stamnes liquid): the split path within the split bars of the oracle.
+    Among its columns a thick ice cloud at 112 hPa under a low sun, whose
+    albedo lies within 1e-6 of 1 in several bands: its absorptance follows
+    the co-albedo, which the split total-sky pass forms without cancellation."""
+    atm = A.config_atmosphere(1)
+    cl = A.cloud_physics_fields(atm, seed=2024)
+    cloud = _phys(cl, 2, 3, 1)
+    rlw = orc.rrtmg_lw(atm, cloud=cloud, icld=2)
+    rsw = orc.rrtmg_sw(atm, cloud=cloud)
+    gpu.set_precision("split")
+    try:
+        lw, sw = gpu.lw(atm, cloud=cloud, icld=2), gpu.sw(atm, cloud=cloud)
+    finally:
+        gpu.set_precision("fp64")
+    bar = SB.hr_bar(atm)
+    for out, ref, keys, hk in ((lw, rlw, ("uflx", "dflx"), "hr"), (sw, rsw, ("swuflx", "swdflx"), "swhr")):
+        for k in keys:
+            assert np.abs(out[k] - ref[k]).max() <= SB.FLUX_BAR, (k, np.abs(out[k] - ref[k]).max())
+        assert np.all(np.abs(out[hk] - ref[hk]) <= bar), (hk, np.abs(out[hk] - ref[hk]).max())

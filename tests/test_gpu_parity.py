@@ -69,6 +69,29 @@ def test_t42_full_grid_fp64(gpu, orc):
     check_sw(gpu.sw(atm), orc.rrtmg_sw(atm))
 
 
+def test_t85_full_grid_fp64_and_split(gpu, orc):
+    """Configuration 1, the benchmark's headline workload: T85 x 40 layers,
+    32768 columns, every column.  FP64 within the FP64 parity tolerance of
+    the oracle; FP32-split within the split bars (0.1 W/m2 at every level,
+    the heating bar of tests/split_bars.py) against the same oracle outputs."""
+    import split_bars as SB
+    atm = A.config_atmosphere(1)
+    rlw, rsw = orc.rrtmg_lw(atm), orc.rrtmg_sw(atm)
+    gpu.set_precision("fp64")
+    check_lw(gpu.lw(atm), rlw)
+    check_sw(gpu.sw(atm), rsw)
+    gpu.set_precision("split")
+    try:
+        lw, sw = gpu.lw(atm), gpu.sw(atm)
+    finally:
+        gpu.set_precision("fp64")
+    bar = SB.hr_bar(atm)
+    for out, ref, keys, hk in ((lw, rlw, ("uflx", "dflx"), "hr"), (sw, rsw, ("swuflx", "swdflx"), "swhr")):
+        for k in keys:
+            assert np.abs(out[k] - ref[k]).max() <= SB.FLUX_BAR, (k, np.abs(out[k] - ref[k]).max())
+        assert np.all(np.abs(out[hk] - ref[hk]) <= bar), (hk, np.abs(out[hk] - ref[hk]).max())
+
+
 def test_lw_idrv_surface_derivative(gpu, orc):
     atm = A.small_atmosphere(256, 40, seed=5)
     gpu.set_precision("fp64")

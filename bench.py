@@ -700,7 +700,8 @@ def run_ours(args):
         for k, v in d.items():
             pin[k] = v.cpu().pin_memory()
         hp = lambda k: pin[k].numpy()
-        h2d = sum(pin[k].numel() * 8 for k in set(lw_keys) | set(sw_keys))
+        # the two calls copy their own inputs: the arrays both take move twice
+        h2d = sum(pin[k].numel() * 8 for k in lw_keys) + sum(pin[k].numel() * 8 for k in sw_keys)
         d2h = 8 * atm.ncol * (8 * (atm.nlay + 1) + 4 * atm.nlay)
         # page-locked output arrays, as for the inputs
         pout = lambda rows: torch.empty((rows, atm.ncol), dtype=torch.float64).pin_memory().numpy()

@@ -52,6 +52,7 @@ struct rrtmg_gpu_state {
   // gather per table lookup in the split LW solver)
   float2* lw_exptfn32 = nullptr;
   double* cldtab = nullptr;  // cloud optical property tables (ct:: offsets)
+  float* cldtab32 = nullptr;  // their FP32 copy (split LW cloud physics)
   unsigned* flags = nullptr;
   DevBuf lw_ws, sw_ws, adj_ws;
   // host-pointer calls: a second stream and per-stream staging and scratch, so
@@ -257,7 +258,7 @@ int lw_enqueue(rrtmg_gpu_state* h, cudaStream_t s, void* base, int ncol, int nla
     const LwWorkT<float> w32 = work_as<float>(w);
     launch_lw_prep_split(in, w32, h->totplnk32, h->totplnkderiv32, ncol, nlay, idrv, h->flags, s);
     if (phys)
-      launch_lw_cldphys_split(in, w32.secdiff, h->cldtab, w32.cld, w.odc, ncol, nlay, h->flags, s);
+      launch_lw_cldphys_split(in, w32.secdiff, h->cldtab32, w32.cld, w.odc, ncol, nlay, h->flags, s);
     else if (cloudy)
       launch_lw_cloud_split(in, w32.cld, ncol, nlay, s);
     if (maxrand) launch_lw_overlap_split(in.cldfr, w32.ovl, ncol, nlay, s);
@@ -729,6 +730,7 @@ int rrtmg_gpu_init(double cpdair, const char* table_blob, int device, rrtmg_gpu_
   if (e == cudaSuccess) e = upload(&h->lw_exptfn32, interleave_f32(h->host.lw_exp, h->host.lw_tfn));
   if (e == cudaSuccess) e = upload(&h->sw_exp32, to_f32(h->host.sw_exp));
   if (e == cudaSuccess) e = upload(&h->cldtab, h->host.cld);
+  if (e == cudaSuccess) e = upload(&h->cldtab32, to_f32(h->host.cld));
   if (e == cudaSuccess) e = cudaMalloc((void**)&h->flags, sizeof(unsigned));
   if (e == cudaSuccess) e = cudaMemset(h->flags, 0, sizeof(unsigned));
   if (e == cudaSuccess) e = upload_constants_fp64(h->host.lw, h->host.sw);
@@ -755,7 +757,7 @@ int rrtmg_gpu_finalize(rrtmg_gpu_handle h) {
   void* ptrs[] = {h->lw_tab64, h->sw_tab64, h->lw_exp64, h->lw_tfn64, h->sw_exp64, h->totplnk, h->totplnkderiv,
                   h->lw_tau64, h->lw_tau32,
                   h->totplnk32, h->totplnkderiv32,
-                  h->lw_tab32, h->sw_tab32, h->lw_exp32, h->lw_tfn32, h->lw_exptfn32, h->sw_exp32, h->cldtab, h->flags,
+                  h->lw_tab32, h->sw_tab32, h->lw_exp32, h->lw_tfn32, h->lw_exptfn32, h->sw_exp32, h->cldtab, h->cldtab32, h->flags,
                   h->lw_ws.p,
                   h->sw_ws.p, h->adj_ws.p, h->hio[0].p, h->hio[1].p, h->hws[0].p, h->hws[1].p, h->run_ws.p,
                   h->run_cio[0].p, h->run_cio[1].p, h->run_cws[0].p, h->run_cws[1].p};

@@ -1149,44 +1149,55 @@ __device__ __forceinline__ bool lw_cloud_layer(const LwIn& in, double ciwp, doub
   return ok;
 }
 // Interpolation in a (rows, bands) table at a 1-based row and fraction.
-__device__ __forceinline__ double cld_interp(const double* t, int rows, int index, double fint, int col) {
-  const double a = __ldg(t + (index - 1) + rows * col), b = __ldg(t + index + rows * col);
+template <class A>
+__device__ __forceinline__ A cld_interp(const A* t, int rows, int index, A fint, int col) {
+  const A a = __ldg(t + (index - 1) + rows * col), b = __ldg(t + index + rows * col);
   return a + fint * (b - a);
 }
-// Ice and liquid absorption coefficients (m2/g) of coefficient band k.
-__device__ __forceinline__ double lw_absice(const LwIn& in, const double* T, double ciwp, double radice, int k) {
-  if (ciwp == 0.0) return 0.0;
-  if (in.iceflag == 0) return __ldg(T + ct::ABSICE0) + __ldg(T + ct::ABSICE0 + 1) / radice;
+// Ice and liquid absorption coefficients (m2/g) of coefficient band k, in
+// the arithmetic A of the tables T (FP64; FP32 on the split path, whose
+// g-point solver takes the depths in FP32).  The table rows are chosen in
+// FP64 on both paths.
+template <class A>
+__device__ __forceinline__ A lw_absice(const LwIn& in, const A* T, double ciwp, double radice, int k) {
+  if (ciwp == 0.0) return (A)0.;
+  if (in.iceflag == 0) return __ldg(T + ct::ABSICE0) + __ldg(T + ct::ABSICE0 + 1) / (A)radice;
   if (in.iceflag == 1)
-    return __ldg(T + ct::ABSICE1 + 2 * (k - 1)) + __ldg(T + ct::ABSICE1 + 1 + 2 * (k - 1)) / radice;
+    return __ldg(T + ct::ABSICE1 + 2 * (k - 1)) + __ldg(T + ct::ABSICE1 + 1 + 2 * (k - 1)) / (A)radice;
   const int rows = in.iceflag == 2 ? 43 : 46;
   const double factor = (radice - 2.) / 3.;
   int index = (int)factor;
   if (index == rows) index = rows - 1;
-  return cld_interp(T + (in.iceflag == 2 ? ct::ABSICE2 : ct::ABSICE3), rows, index, factor - (double)index, k - 1);
+  return cld_interp<A>(T + (in.iceflag == 2 ? ct::ABSICE2 : ct::ABSICE3), rows, index, (A)(factor - (double)index),
+                       k - 1);
 }
-__device__ __forceinline__ double lw_absliq(const LwIn& in, const double* T, double clwp, double radliq, int k) {
-  if (clwp == 0.0) return 0.0;
+template <class A>
+__device__ __forceinline__ A lw_absliq(const LwIn& in, const A* T, double clwp, double radliq, int k) {
+  if (clwp == 0.0) return (A)0.;
   if (in.liqflag == 0) return __ldg(T + ct::ABSLIQ0);
   int index = (int)(radliq - 1.5);
   if (index == 0) index = 1;
   if (index == 58) index = 57;
-  return cld_interp(T + ct::ABSLIQ1, 58, index, radliq - 1.5 - (double)index, k - 1);
+  return cld_interp<A>(T + ct::ABSLIQ1, 58, index, (A)(radliq - 1.5 - (double)index), k - 1);
 }
 
-// One thread per column: the cover and formed-layer mask of every layer (as
+// One thread per (column, band), the 16 band threads of a column adjacent:
+// the cover and formed-layer mask of every layer (band 1's thread, as
 // lw_cloud_kernel) and odc[lay][col][iband] = secdiff(ib) x taucloud(lay, ib),
-// ib = ipat(iband, ncbands), the cloud depth rtrn / rtrnmr use (0 for a
-// layer whose optics are not formed or that filled fewer cloud bands).  A
-// size outside its table sets flag bit 2 (reported as invalid input) and
-// leaves the column's depths 0.
+// ib = ipat(iband, ncbands), the cloud depth rtrn / rtrnmr use (0 for a layer
+// whose optics are not formed or that filled fewer cloud bands).  Every band
+// thread scans the column's layers for the final count of cloud bands, then
+// walks them again with the running count.  A size outside its table sets
+// flag bit 2 (reported as invalid input) and leaves the column's depths 0.
 template <class F>
 __global__ void __launch_bounds__(128) lw_cldphys_kernel(LwIn in, const F* __restrict__ secdiff,
-                                                         const double* __restrict__ T, F* __restrict__ cld,
+                                                         const F* __restrict__ T, F* __restrict__ cld,
                                                          double* __restrict__ odc, int ncol, int nlay,
                                                          unsigned* __restrict__ flags) {
-  const int col = blockIdx.x * blockDim.x + threadIdx.x;
-  if (col >= ncol) return;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)ncol * kLwBands) return;
+  const int col = (int)(t / kLwBands), iband = (int)(t % kLwBands) + 1;
+  const bool lead = iband == 1;
   const size_t N = (size_t)ncol, S = (size_t)nlay * N;
   int ncb = 1;
   bool ok = true;
@@ -1194,41 +1205,39 @@ __global__ void __launch_bounds__(128) lw_cldphys_kernel(LwIn in, const F* __res
     const size_t o = (size_t)l * N + col;
     double cf, ciwp, clwp;
     const bool kept = lw_cloud_kept(in, o, cf, ciwp, clwp);
-    cld[o] = cf >= 1.e-6 ? (F)cf : (F)0;
-    cld[S + o] = kept ? (F)1 : (F)0;
+    if (lead) {
+      cld[o] = cf >= 1.e-6 ? (F)cf : (F)0;
+      cld[S + o] = kept ? (F)1 : (F)0;
+    }
     int ii, li;
     if (kept && !lw_cloud_layer(in, ciwp, clwp, in.reice ? __ldg(in.reice + o) : 0.0,
                                 in.reliq ? __ldg(in.reliq + o) : 0.0, ncb, ii, li))
       ok = false;
   }
-  if (!ok) atomicOr(flags, 4u);
+  if (!ok && lead) atomicOr(flags, 4u);
+  const int ib = lw_cloud_band(iband, ncb);
+  const F sec = secdiff[(size_t)(ib - 1) * N + col];
   int run = 1;
   for (int l = 0; l < nlay; ++l) {
     const size_t o = (size_t)l * N + col;
-    double* d = odc + 16 * o;
     double cf, ciwp, clwp;
     const bool kept = lw_cloud_kept(in, o, cf, ciwp, clwp);
-    if (!ok || !kept) {
-      for (int b = 0; b < kLwBands; ++b) d[b] = 0.0;
-      continue;
-    }
-    const double radice = in.reice ? __ldg(in.reice + o) : 0.0, radliq = in.reliq ? __ldg(in.reliq + o) : 0.0;
-    int iceind, liqind;
-    lw_cloud_layer(in, ciwp, clwp, radice, radliq, run, iceind, liqind);
-    for (int iband = 1; iband <= kLwBands; ++iband) {
-      const int ib = lw_cloud_band(iband, ncb);
-      double tc = 0.0;
+    F tc = (F)0.;
+    if (ok && kept) {
+      const double radice = in.reice ? __ldg(in.reice + o) : 0.0, radliq = in.reliq ? __ldg(in.reliq + o) : 0.0;
+      int iceind, liqind;
+      lw_cloud_layer(in, ciwp, clwp, radice, radliq, run, iceind, liqind);
       if (ib <= run) {
         if (in.inflag == 1) {
-          tc = __ldg(T + ct::ABSCLD1) * (ciwp + clwp);
+          tc = __ldg(T + ct::ABSCLD1) * (F)(ciwp + clwp);
         } else {
           const int ki = lw_cloud_band(ib, iceind == 0 ? 1 : iceind == 1 ? 5 : 16);
           const int kl = lw_cloud_band(ib, liqind == 0 ? 1 : 16);
-          tc = ciwp * lw_absice(in, T, ciwp, radice, ki) + clwp * lw_absliq(in, T, clwp, radliq, kl);
+          tc = (F)ciwp * lw_absice<F>(in, T, ciwp, radice, ki) + (F)clwp * lw_absliq<F>(in, T, clwp, radliq, kl);
         }
       }
-      d[iband - 1] = (double)secdiff[(size_t)(ib - 1) * N + col] * tc;
     }
+    odc[16 * o + (iband - 1)] = ok && kept ? (double)(sec * tc) : 0.0;
   }
 }
 
@@ -2069,98 +2078,89 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_SW_MINB :
 
 #ifdef RRTMG_DEFINE_COLUMN_KERNELS
 // ---------------------------------------------------------------------------
-// SW cloud physics of one formed layer (cldprop_sw, inflag = 2,
-// rrtmg_sw_cldprop.f90:158-340): per band the ice extinction (m2/g), single-
-// scattering albedo, asymmetry and forward fraction of Ebert and Curry's fit
-// (iceflag 1; its five spectral intervals chosen by the band's upper limit
-// wavenum2), of Key's Streamer table (2) or of Fu's table with its delta
-// fractions (3), and those of Hu and Stamnes' liquid table (liqflag 1); each
-// delta-M scaled and combined into the layer's delta-scaled depth tau,
-// albedo ssa and asymmetry g (written with 1-band stride).  A zero depth or
-// ice scattering becomes cldmin = 1e-20.  Returns false (nothing written)
-// where the reference stops: a size outside its table (not-a-number sizes
-// too), or a coefficient outside its physical range.
+// SW cloud physics of one band k (band 16 + k) of one formed layer
+// (cldprop_sw, inflag = 2, rrtmg_sw_cldprop.f90:158-340): the ice extinction
+// (m2/g), single-scattering albedo, asymmetry and forward fraction of Ebert
+// and Curry's fit (iceflag 1; its five spectral intervals chosen by the band's
+// upper limit wavenum2), of Key's Streamer table (2) or of Fu's table with its
+// delta fractions (3), and those of Hu and Stamnes' liquid table (liqflag 1);
+// each delta-M scaled and combined into the band's delta-scaled depth tau,
+// albedo ssa and asymmetry g.  A zero depth or ice scattering becomes cldmin =
+// 1e-20.  Returns false (nothing written) where the reference stops: a size
+// outside its table (not-a-number sizes too), or a coefficient outside its
+// physical range.
 // ---------------------------------------------------------------------------
-__device__ __noinline__ bool sw_cloud_optics(const SwIn& in, const double* __restrict__ T, double ciwp, double clwp,
-                                             double radice, double radliq, double* tau, double* ssa, double* g) {
+__device__ __forceinline__ bool sw_cloud_band_optics(const SwIn& in, const double* __restrict__ T, double ciwp,
+                                                     double clwp, double radice, double radliq, int k, double* tau,
+                                                     double* ssa, double* g) {
   const double eps = 1.e-06, cldmin = 1.e-20;
+  double ext_i = 0.0, ssa_i = 0.0, g_i = 0.0, fw_i = 0.0;
   if (ciwp != 0.0) {
-    const bool ok = in.iceflag == 1   ? (radice >= 13.0 && radice <= 130.0)
-                    : in.iceflag == 2 ? (radice >= 5.0 && radice <= 131.0)
-                                      : (radice >= 5.0 && radice <= 140.0);
-    if (!ok) return false;
-  }
-  if (clwp != 0.0 && !(radliq >= 2.5 && radliq <= 60.0)) return false;
-  const int irows = in.iceflag == 2 ? 43 : 46;
-  const double ifactor = (radice - 2.) / 3.;
-  int iindex = (int)ifactor;
-  if (ciwp != 0.0 && in.iceflag >= 2 && iindex == irows) iindex = irows - 1;
-  const double ifint = ifactor - (double)iindex;
-  int lindex = (int)(radliq - 1.5);
-  if (lindex == 0) lindex = 1;
-  if (lindex == 58) lindex = 57;
-  const double lfint = radliq - 1.5 - (double)lindex;
-  double tc[kSwBands], sc[kSwBands], gc[kSwBands];
-  for (int k = 0; k < kSwBands; ++k) {  // band 16 + k
-    double ext_i = 0.0, ssa_i = 0.0, g_i = 0.0, fw_i = 0.0;
-    if (ciwp != 0.0) {
-      if (in.iceflag == 1) {
-        const double wn = __ldg(T + ct::WAVENUM2 + k);
-        const int icx = wn > 1.43e04 ? 0 : wn > 7.7e03 ? 1 : wn > 5.3e03 ? 2 : wn > 4.0e03 ? 3 : 4;
-        const double* c = T + ct::ABARI + icx;
-        ext_i = __ldg(c) + __ldg(c + 5) / radice;
-        ssa_i = 1. - __ldg(c + 10) - __ldg(c + 15) * radice;
-        g_i = __ldg(c + 20) + __ldg(c + 25) * radice;
-        if (g_i >= 1.0) g_i = 1.0 - eps;
-        fw_i = g_i * g_i;
-      } else if (in.iceflag == 2) {
-        ext_i = cld_interp(T + ct::EXTICE2, 43, iindex, ifint, k);
-        ssa_i = cld_interp(T + ct::SSAICE2, 43, iindex, ifint, k);
-        g_i = cld_interp(T + ct::ASYICE2, 43, iindex, ifint, k);
+    if (in.iceflag == 1) {
+      if (!(radice >= 13.0 && radice <= 130.0)) return false;
+      const double wn = __ldg(T + ct::WAVENUM2 + k);
+      const int icx = wn > 1.43e04 ? 0 : wn > 7.7e03 ? 1 : wn > 5.3e03 ? 2 : wn > 4.0e03 ? 3 : 4;
+      const double* c = T + ct::ABARI + icx;
+      ext_i = __ldg(c) + __ldg(c + 5) / radice;
+      ssa_i = 1. - __ldg(c + 10) - __ldg(c + 15) * radice;
+      g_i = __ldg(c + 20) + __ldg(c + 25) * radice;
+      if (g_i >= 1.0) g_i = 1.0 - eps;
+      fw_i = g_i * g_i;
+    } else {
+      const int rows = in.iceflag == 2 ? 43 : 46;
+      if (!(radice >= 5.0 && radice <= (in.iceflag == 2 ? 131.0 : 140.0))) return false;
+      const double factor = (radice - 2.) / 3.;
+      int index = (int)factor;
+      if (index == rows) index = rows - 1;
+      const double fint = factor - (double)index;
+      if (in.iceflag == 2) {
+        ext_i = cld_interp(T + ct::EXTICE2, 43, index, fint, k);
+        ssa_i = cld_interp(T + ct::SSAICE2, 43, index, fint, k);
+        g_i = cld_interp(T + ct::ASYICE2, 43, index, fint, k);
         fw_i = g_i * g_i;
       } else {
-        ext_i = cld_interp(T + ct::EXTICE3, 46, iindex, ifint, k);
-        ssa_i = cld_interp(T + ct::SSAICE3, 46, iindex, ifint, k);
-        g_i = cld_interp(T + ct::ASYICE3, 46, iindex, ifint, k);
-        const double fdelta = cld_interp(T + ct::FDLICE3, 46, iindex, ifint, k);
+        ext_i = cld_interp(T + ct::EXTICE3, 46, index, fint, k);
+        ssa_i = cld_interp(T + ct::SSAICE3, 46, index, fint, k);
+        g_i = cld_interp(T + ct::ASYICE3, 46, index, fint, k);
+        const double fdelta = cld_interp(T + ct::FDLICE3, 46, index, fint, k);
         if (fdelta < 0.0 || fdelta > 1.0) return false;
         fw_i = fdelta + 0.5 / ssa_i;
         if (fw_i > g_i) fw_i = g_i;
       }
-      if (ext_i < 0.0 || ssa_i > 1.0 || ssa_i < 0.0 || g_i > 1.0 || g_i < 0.0) return false;
     }
-    double ext_l = 0.0, ssa_l = 0.0, g_l = 0.0, fw_l = 0.0;
-    if (clwp != 0.0) {
-      ext_l = cld_interp(T + ct::EXTLIQ1, 58, lindex, lfint, k);
-      ssa_l = cld_interp(T + ct::SSALIQ1, 58, lindex, lfint, k);
-      if (lfint < 0. && ssa_l > 1.) ssa_l = __ldg(T + ct::SSALIQ1 + (lindex - 1) + 58 * k);
-      g_l = cld_interp(T + ct::ASYLIQ1, 58, lindex, lfint, k);
-      fw_l = g_l * g_l;
-      if (ext_l < 0.0 || ssa_l > 1.0 || ssa_l < 0.0 || g_l > 1.0 || g_l < 0.0) return false;
-    }
-    const double tauliqorig = clwp * ext_l, tauiceorig = ciwp * ext_i;
-    const double ssaliq = ssa_l * (1.0 - fw_l) / (1.0 - fw_l * ssa_l);
-    const double tauliq = (1.0 - fw_l * ssa_l) * tauliqorig;
-    const double ssaice = ssa_i * (1.0 - fw_i) / (1.0 - fw_i * ssa_i);
-    const double tauice = (1.0 - fw_i * ssa_i) * tauiceorig;
-    const double scatliq = ssaliq * tauliq;
-    double scatice = ssaice * tauice;
-    double t = tauliq + tauice;
-    if (t == 0.0) t = cldmin;
-    if (scatice == 0.0) scatice = cldmin;
-    tc[k] = t;
-    sc[k] = (scatliq + scatice) / t;
-    if (in.iceflag == 3)
-      gc[k] = (1.0 / (scatliq + scatice)) *
-              (scatliq * (g_l - fw_l) / (1.0 - fw_l) + scatice * ((g_i - fw_i) / (1.0 - fw_i)));
-    else
-      gc[k] = (scatliq * (g_l - fw_l) / (1.0 - fw_l) + scatice * (g_i - fw_i) / (1.0 - fw_i)) / (scatliq + scatice);
+    if (ext_i < 0.0 || ssa_i > 1.0 || ssa_i < 0.0 || g_i > 1.0 || g_i < 0.0) return false;
   }
-  for (int k = 0; k < kSwBands; ++k) {
-    tau[k] = tc[k];
-    ssa[k] = sc[k];
-    g[k] = gc[k];
+  double ext_l = 0.0, ssa_l = 0.0, g_l = 0.0, fw_l = 0.0;
+  if (clwp != 0.0) {
+    if (!(radliq >= 2.5 && radliq <= 60.0)) return false;
+    int index = (int)(radliq - 1.5);
+    if (index == 0) index = 1;
+    if (index == 58) index = 57;
+    const double fint = radliq - 1.5 - (double)index;
+    ext_l = cld_interp(T + ct::EXTLIQ1, 58, index, fint, k);
+    ssa_l = cld_interp(T + ct::SSALIQ1, 58, index, fint, k);
+    if (fint < 0. && ssa_l > 1.) ssa_l = __ldg(T + ct::SSALIQ1 + (index - 1) + 58 * k);
+    g_l = cld_interp(T + ct::ASYLIQ1, 58, index, fint, k);
+    fw_l = g_l * g_l;
+    if (ext_l < 0.0 || ssa_l > 1.0 || ssa_l < 0.0 || g_l > 1.0 || g_l < 0.0) return false;
   }
+  const double tauliqorig = clwp * ext_l, tauiceorig = ciwp * ext_i;
+  const double ssaliq = ssa_l * (1.0 - fw_l) / (1.0 - fw_l * ssa_l);
+  const double tauliq = (1.0 - fw_l * ssa_l) * tauliqorig;
+  const double ssaice = ssa_i * (1.0 - fw_i) / (1.0 - fw_i * ssa_i);
+  const double tauice = (1.0 - fw_i * ssa_i) * tauiceorig;
+  const double scatliq = ssaliq * tauliq;
+  double scatice = ssaice * tauice;
+  double t = tauliq + tauice;
+  if (t == 0.0) t = cldmin;
+  if (scatice == 0.0) scatice = cldmin;
+  *tau = t;
+  *ssa = (scatliq + scatice) / t;
+  if (in.iceflag == 3)
+    *g = (1.0 / (scatliq + scatice)) *
+         (scatliq * (g_l - fw_l) / (1.0 - fw_l) + scatice * ((g_i - fw_i) / (1.0 - fw_i)));
+  else
+    *g = (scatliq * (g_l - fw_l) / (1.0 - fw_l) + scatice * (g_i - fw_i) / (1.0 - fw_i)) / (scatliq + scatice);
   return true;
 }
 
@@ -2175,41 +2175,71 @@ __device__ __noinline__ bool sw_cloud_optics(const SwIn& in, const double* __res
 // the cover; cld[1][lay][col]: 1 where the optics are kept, else 0.
 // ---------------------------------------------------------------------------
 // With cloud physics (inflag = 2), a sunlit layer whose optics are formed
-// gets them from sw_cloud_optics into opt; a size or optical property that
-// stops the reference sets flag bit 2.
+// gets them from sw_cloud_band_optics into opt ([tau, ssa, g][lay][col]
+// [band]); a size or optical property that stops the reference sets flag bit
+// 2.  Formed layers are few and scattered, so the warp computes them two at a
+// time with a lane per band, instead of a lane per layer idling the others.
 template <class F>
 __global__ void __launch_bounds__(128) sw_cloud_kernel(SwIn in, F* __restrict__ cld, int ncol, int nlay,
                                                        unsigned* __restrict__ flags, const double* __restrict__ T,
                                                        double* __restrict__ opt) {
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
-  if (col >= ncol) return;
-  const size_t o = (size_t)blockIdx.y * ncol + col;
-  const double cf = __ldg(in.cldfr + o);
-  double tauctot = 0.0;
-  if (in.taucld)
-    for (int ib = 0; ib < kSwBands; ++ib) tauctot = tauctot + __ldg(in.taucld + ib + 14 * o);
-  const double ciwp = in.cicewp ? __ldg(in.cicewp + o) : 0.0, clwp = in.cliqwp ? __ldg(in.cliqwp + o) : 0.0;
-  const double cwp = ciwp + clwp;
-  const double cldmin = 1.e-20, zepsec = 1.e-06;
-  // the checks run in sunlit columns only: the reference skips the others (:500-509)
-  const bool lit = __ldg(in.coszen + col) >= 1.e-10;
-  if (cf > zepsec && cf < 1.0 - zepsec && lit) atomicOr(flags, 2u);
-  bool kept = cf >= cldmin && (cwp >= cldmin || tauctot >= cldmin);
-  if (in.inflag == 2 && kept) {
-    // unlit columns (whose outputs are zeros) and a failed layer keep no
-    // optics, so that the total-sky pass reads only optics written here
-    const size_t S = (size_t)nlay * ncol;
-    if (!lit) {
-      kept = false;
-    } else if (!sw_cloud_optics(in, T, ciwp, clwp, in.reice ? __ldg(in.reice + o) : 0.0,
-                                in.reliq ? __ldg(in.reliq + o) : 0.0, opt + 14 * o, opt + 14 * (S + o),
-                                opt + 14 * (2 * S + o))) {
+  const bool here = col < ncol;  // every lane stays for the warp's shuffles
+  const size_t S = (size_t)nlay * ncol;
+  const size_t o = (size_t)blockIdx.y * ncol + (here ? col : 0);
+  double cf = 0.0, ciwp = 0.0, clwp = 0.0;
+  bool kept = false, lit = false;
+  if (here) {
+    cf = __ldg(in.cldfr + o);
+    double tauctot = 0.0;
+    if (in.taucld)
+      for (int ib = 0; ib < kSwBands; ++ib) tauctot = tauctot + __ldg(in.taucld + ib + 14 * o);
+    ciwp = in.cicewp ? __ldg(in.cicewp + o) : 0.0;
+    clwp = in.cliqwp ? __ldg(in.cliqwp + o) : 0.0;
+    const double cwp = ciwp + clwp;
+    const double cldmin = 1.e-20, zepsec = 1.e-06;
+    // the checks run in sunlit columns only: the reference skips the others (:500-509)
+    lit = __ldg(in.coszen + col) >= 1.e-10;
+    if (cf > zepsec && cf < 1.0 - zepsec && lit) atomicOr(flags, 2u);
+    kept = cf >= cldmin && (cwp >= cldmin || tauctot >= cldmin);
+    // unlit columns (whose outputs are zeros) keep no optics, so that the
+    // total-sky pass reads only optics written here
+    if (in.inflag == 2 && !lit) kept = false;
+  }
+  if (in.inflag == 2) {
+    const int lane = threadIdx.x & 31;
+    const double radice = here && in.reice ? __ldg(in.reice + o) : 0.0;
+    const double radliq = here && in.reliq ? __ldg(in.reliq + o) : 0.0;
+    bool failed = false;
+    // two layers per pass: lanes 0-15 take the first, 16-31 the second, a
+    // lane per band
+    const int half = lane >> 4, band = lane & 15;
+    for (unsigned todo = __ballot_sync(0xffffffffu, kept); todo;) {
+      const int src0 = __ffs(todo) - 1;
+      todo &= todo - 1;
+      const int src1 = todo ? __ffs(todo) - 1 : -1;
+      if (todo) todo &= todo - 1;
+      const int src = half ? src1 : src0;
+      const int from = src < 0 ? src0 : src;
+      const double ci = __shfl_sync(0xffffffffu, ciwp, from), cl = __shfl_sync(0xffffffffu, clwp, from);
+      const double ri = __shfl_sync(0xffffffffu, radice, from), rl = __shfl_sync(0xffffffffu, radliq, from);
+      const size_t os = __shfl_sync(0xffffffffu, (unsigned long long)o, from);
+      bool ok = true;
+      if (src >= 0 && band < kSwBands)
+        ok = sw_cloud_band_optics(in, T, ci, cl, ri, rl, band, opt + 14 * os + band, opt + 14 * (S + os) + band,
+                                  opt + 14 * (2 * S + os) + band);
+      const unsigned bad = __ballot_sync(0xffffffffu, !ok);
+      if ((lane == src0 && (bad & 0xffffu)) || (lane == src1 && (bad >> 16))) failed = true;
+    }
+    if (failed) {
       atomicOr(flags, 4u);
       kept = false;
     }
   }
-  cld[o] = (F)cf;
-  cld[(size_t)nlay * ncol + o] = kept ? (F)1 : (F)0;
+  if (here) {
+    cld[o] = (F)cf;
+    cld[S + o] = kept ? (F)1 : (F)0;
+  }
 }
 
 // SW finalize: band sums, outputs, heating (rrtmg_sw_rad.nomcica.f90:688-726);

@@ -83,11 +83,11 @@ void launch_lw_cloud_split(const LwIn& in, float* cld, int ncol, int nlay, cudaS
 }
 void launch_lw_cldphys(const LwIn& in, const double* secdiff, const double* cldtab, double* cld, double* odc, int ncol,
                        int nlay, unsigned* flags, cudaStream_t s) {
-  lw_cldphys_kernel<double><<<(ncol + 127) / 128, 128, 0, s>>>(in, secdiff, cldtab, cld, odc, ncol, nlay, flags);
+  lw_cldphys_kernel<double><<<(unsigned)(((long long)ncol * kLwBands + 127) / 128), 128, 0, s>>>(in, secdiff, cldtab, cld, odc, ncol, nlay, flags);
 }
-void launch_lw_cldphys_split(const LwIn& in, const float* secdiff, const double* cldtab, float* cld, double* odc,
+void launch_lw_cldphys_split(const LwIn& in, const float* secdiff, const float* cldtab, float* cld, double* odc,
                              int ncol, int nlay, unsigned* flags, cudaStream_t s) {
-  lw_cldphys_kernel<float><<<(ncol + 127) / 128, 128, 0, s>>>(in, secdiff, cldtab, cld, odc, ncol, nlay, flags);
+  lw_cldphys_kernel<float><<<(unsigned)(((long long)ncol * kLwBands + 127) / 128), 128, 0, s>>>(in, secdiff, cldtab, cld, odc, ncol, nlay, flags);
 }
 void launch_lw_overlap(const double* cldfr, double* ovl, int ncol, int nlay, cudaStream_t s) {
   lw_overlap_kernel<double><<<(ncol + 127) / 128, 128, 0, s>>>(cldfr, ovl, ncol, nlay);

@@ -30,10 +30,11 @@ void launch_lw_finalize(const double* bu, const double* bd, const double* bdu, c
 void launch_lw_cloud(const LwIn& in, double* cld, int ncol, int nlay, cudaStream_t s);
 void launch_lw_cloud_split(const LwIn& in, float* cld, int ncol, int nlay, cudaStream_t s);
 // Cloud physics (inflag 1 / 2): the cloud fields of launch_lw_cloud and the
-// cloud depths along the diffusivity angle (odc); cldtab: ct:: tables.
+// cloud depths along the diffusivity angle (odc); cldtab: ct:: tables (FP32
+// copy on the split path).
 void launch_lw_cldphys(const LwIn& in, const double* secdiff, const double* cldtab, double* cld, double* odc, int ncol,
                        int nlay, unsigned* flags, cudaStream_t s);
-void launch_lw_cldphys_split(const LwIn& in, const float* secdiff, const double* cldtab, float* cld, double* odc,
+void launch_lw_cldphys_split(const LwIn& in, const float* secdiff, const float* cldtab, float* cld, double* odc,
                              int ncol, int nlay, unsigned* flags, cudaStream_t s);
 // Maximum/random overlap (icld = 2, 3): rtrnmr's overlap factors per layer.
 void launch_lw_overlap(const double* cldfr, double* ovl, int ncol, int nlay, cudaStream_t s);

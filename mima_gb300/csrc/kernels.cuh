@@ -806,7 +806,7 @@ __device__ __forceinline__ void lw_band_cld(const LwPrepT<R>& p, const R* __rest
     }
     above_cloudy = cf > (R)0.;
     lq[lev - 1] = Quad<R>{atr, bbu, at, bbut};
-    efcl[lev - 1] = ef;
+    if (!ovl) efcl[lev - 1] = ef;  // read by random overlap only
     // clear-sky stream (:441-448)
     if (iclddn)
       radclrd = radclrd + (bbd - radclrd) * atr;

@@ -653,7 +653,9 @@ __device__ __forceinline__ void lw_band_cld(const LwPrepT<R>& p, const R* __rest
   const R bpade = (R)c_lw.bpade;
   const R rec_6 = (R)0.166667;
   const size_t fstride = (size_t)nlay * N;
-  Quad<R> lq[MAXL];  // {atrans, bbugas, atot, bbutot} of each layer
+  // {atrans, bbugas} of each layer and {atot, bbutot} of each cloudy one: a
+  // clear layer moves half the bytes of a cloudy one through local memory
+  Pair2<R> lq[MAXL], lqc[MAXL];
   R efcl[MAXL];
   // transmittance, tau transition function and the optical depth of a table
   // entry (exp_tbl, tfn_tbl, tau_tbl), or with the analytic functions, of od
@@ -805,7 +807,8 @@ __device__ __forceinline__ void lw_band_cld(const LwPrepT<R>& p, const R* __rest
       radld = radld + (bbd - radld) * atr;
     }
     above_cloudy = cf > (R)0.;
-    lq[lev - 1] = Quad<R>{atr, bbu, at, bbut};
+    lq[lev - 1] = Pair2<R>{atr, bbu};
+    if (cf > (R)0.) lqc[lev - 1] = Pair2<R>{at, bbut};
     if (!ovl) efcl[lev - 1] = ef;  // read by random overlap only
     // clear-sky stream (:441-448)
     if (iclddn)
@@ -858,13 +861,14 @@ __device__ __forceinline__ void lw_band_cld(const LwPrepT<R>& p, const R* __rest
   bool below_cloudy = false;  // maximum/random overlap: istcld = 0
   rad = (R)0.;
   for (int lev = 1; lev <= nlay; ++lev) {  // rtrn :478-520, rtrnmr :649-705
-    const Quad<R> l = lq[lev - 1];
-    const R atr = l.a, bbugas = l.b, bbutot = l.d;
+    const Pair2<R> l = lq[lev - 1];
+    const R atr = l.a, bbugas = l.b;
     const size_t o = (size_t)(lev - 1) * N + c;
     const R cf = __ldg(cld + o);
     if (cf > (R)0.) {
       const R gassrc = bbugas * atr;
-      const R at = l.c;
+      const Pair2<R> lc = lqc[lev - 1];
+      const R at = lc.a, bbutot = lc.b;
       if (ovl) {
         if (!below_cloudy) {
           cldrad = cf * radlu;

@@ -1914,53 +1914,58 @@ __device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, dou
       zdbtmc = sw_exp_tbl<R, R>(ztauc / prmu0, bpade, exptbl, analytic);
     }
     if constexpr (TOT) {
+      // A layer without cover keeps its clear optics: the reference's cover-weighted
+      // combination below gives them back exactly (1 x clear + 0 x total), so the
+      // total-sky optics of such a layer are skipped.
       // cldprop_sw, inflag = 0 (rrtmg_sw_cldprop.f90:142-156): delta-M scaled
       // cloud optics where the mask keeps them, else tau 0, ssa 1, g 0
       const R pclfr = __ldg(cld + o);
-      R ptauc = (R)0., pomgc = (R)1., pasyc = (R)0.;
-      R pcw = (R)0.;  // split path: the cloud's delta-scaled co-albedo 1 - pomgc
-      if (__ldg(cld + fstride + o) > (R)0.) {
-        const size_t q = (size_t)(ibm - 1) + 14 * o;
-        const R taucldorig = (R)__ldg(in.taucld + q), ffp = in.fsfcld ? (R)__ldg(in.fsfcld + q) : (R)0.;
-        const R ssac = (R)__ldg(in.ssacld + q), asmc = (R)__ldg(in.asmcld + q);
-        const R ffp1 = (R)1.0 - ffp;
-        const R ffpssa = (R)1.0 - ffp * ssac;
-        pomgc = ffp1 * ssac / ffpssa;
-        ptauc = ffpssa * taucldorig;
-        pasyc = (asmc - ffp) / (ffp1);
-        if constexpr (sizeof(R) == 4) {
-          // 1 - ffp1 ssac / ffpssa = (1 - ssac) / (1 - ffp ssac), from the FP64 inputs
-          const double ssad = __ldg(in.ssacld + q), ffpd = in.fsfcld ? __ldg(in.fsfcld + q) : 0.0;
-          pcw = (R)((1.0 - ssad) / (1.0 - ffpd * ssad));
+      if (pclfr > (R)0.) {
+        R ptauc = (R)0., pomgc = (R)1., pasyc = (R)0.;
+        R pcw = (R)0.;  // split path: the cloud's delta-scaled co-albedo 1 - pomgc
+        if (__ldg(cld + fstride + o) > (R)0.) {
+          const size_t q = (size_t)(ibm - 1) + 14 * o;
+          const R taucldorig = (R)__ldg(in.taucld + q), ffp = in.fsfcld ? (R)__ldg(in.fsfcld + q) : (R)0.;
+          const R ssac = (R)__ldg(in.ssacld + q), asmc = (R)__ldg(in.asmcld + q);
+          const R ffp1 = (R)1.0 - ffp;
+          const R ffpssa = (R)1.0 - ffp * ssac;
+          pomgc = ffp1 * ssac / ffpssa;
+          ptauc = ffpssa * taucldorig;
+          pasyc = (asmc - ffp) / (ffp1);
+          if constexpr (sizeof(R) == 4) {
+            // 1 - ffp1 ssac / ffpssa = (1 - ssac) / (1 - ffp ssac), from the FP64 inputs
+            const double ssad = __ldg(in.ssacld + q), ffpd = in.fsfcld ? __ldg(in.fsfcld + q) : 0.0;
+            pcw = (R)((1.0 - ssad) / (1.0 - ffpd * ssad));
+          }
         }
-      }
-      // total-sky optics (spcvrt_sw :459-464), reftra only for cloudy layers
-      // (pclfr > repclc = 1e-12, :388; reftra gives 0, 1, 0, 1 otherwise)
-      const R ztauo = ztauc + ptauc;
-      R zomco = ztauc * zomcc + ptauc * pomgc;
-      const R zgco = (ptauc * pomgc * pasyc + ztauc * zomcc * zgcc) / zomco;
-      zomco = zomco / ztauo;
-      R rfo = (R)0., rfdo = (R)0., tro = (R)1., trdo = (R)1.;
-      if (pclfr > (R)1.e-12) {
-        if constexpr (sizeof(R) == 4) {
-          // the total co-albedo from the clear one (gas absorption and aerosol
-          // co-albedo over the depth, through the delta-M scaling: 1 - w' =
-          // (1 - w) / (1 - f w)) and the cloud's, without cancellation
-          const R cwc = (taug + taua * cwa) / ((taur + taug + taua) * ((R)1.0 - zwf));
-          const R cwo = (ztauc * cwc + ptauc * pcw) / ztauo;
-          reftra_split(ztauo, zomco, zgco, prmu0, bpade, exptbl, analytic, rfo, rfdo, tro, trdo, false, (R*)nullptr,
-                       cwo);
-        } else {
-          reftra1<R, R>(ztauo, zomco, zgco, prmu0, bpade, exptbl, analytic, rfo, rfdo, tro, trdo);
+        // total-sky optics (spcvrt_sw :459-464), reftra only for cloudy layers
+        // (pclfr > repclc = 1e-12, :388; reftra gives 0, 1, 0, 1 otherwise)
+        const R ztauo = ztauc + ptauc;
+        R zomco = ztauc * zomcc + ptauc * pomgc;
+        const R zgco = (ptauc * pomgc * pasyc + ztauc * zomcc * zgcc) / zomco;
+        zomco = zomco / ztauo;
+        R rfo = (R)0., rfdo = (R)0., tro = (R)1., trdo = (R)1.;
+        if (pclfr > (R)1.e-12) {
+          if constexpr (sizeof(R) == 4) {
+            // the total co-albedo from the clear one (gas absorption and aerosol
+            // co-albedo over the depth, through the delta-M scaling: 1 - w' =
+            // (1 - w) / (1 - f w)) and the cloud's, without cancellation
+            const R cwc = (taug + taua * cwa) / ((taur + taug + taua) * ((R)1.0 - zwf));
+            const R cwo = (ztauc * cwc + ptauc * pcw) / ztauo;
+            reftra_split(ztauo, zomco, zgco, prmu0, bpade, exptbl, analytic, rfo, rfdo, tro, trdo, false, (R*)nullptr,
+                         cwo);
+          } else {
+            reftra1<R, R>(ztauo, zomco, zgco, prmu0, bpade, exptbl, analytic, rfo, rfdo, tro, trdo);
+          }
         }
+        const R zdbtmo = sw_exp_tbl<R, R>(ztauo / prmu0, bpade, exptbl, analytic);
+        const R zclear = (R)1.0 - pclfr, zcloud = pclfr;
+        rf = zclear * rf + zcloud * rfo;
+        rfd = zclear * rfd + zcloud * rfdo;
+        tr = zclear * tr + zcloud * tro;
+        trd = zclear * trd + zcloud * trdo;
+        zdbtmc = zclear * zdbtmc + zcloud * zdbtmo;
       }
-      const R zdbtmo = sw_exp_tbl<R, R>(ztauo / prmu0, bpade, exptbl, analytic);
-      const R zclear = (R)1.0 - pclfr, zcloud = pclfr;
-      rf = zclear * rf + zcloud * rfo;
-      rfd = zclear * rfd + zcloud * rfdo;
-      tr = zclear * tr + zcloud * tro;
-      trd = zclear * trd + zcloud * trdo;
-      zdbtmc = zclear * zdbtmc + zcloud * zdbtmo;
     }
     lay[jk - 1] = Quad<R>{rf, rfd, tr, trd};
     lvl[jk - 1] = Quad<R>{tdbt1, tdn1, rdnd1, zdbtmc};

@@ -180,7 +180,11 @@ LwWork carve_lw(void* base, int ncol, int nlay, size_t* bytes, bool cloudy = fal
   return w;
 }
 
-SwWork carve_sw(void* base, int ncol, int nlay, size_t* bytes, bool cloudy = false, bool phys = false) {
+// cloudy: the per-layer cloud fields and the clear-pass band partials, and on
+// the split path (split) the total-sky pass's cloud optics; with cloud
+// physics on the FP64 path (phys) the formed optics.
+SwWork carve_sw(void* base, int ncol, int nlay, size_t* bytes, bool cloudy = false, bool phys = false,
+                bool split = false) {
   Carver c{(char*)base};
   const size_t N = (size_t)ncol, L = (size_t)nlay;
   SwWork w{};
@@ -194,7 +198,8 @@ SwWork carve_sw(void* base, int ncol, int nlay, size_t* bytes, bool cloudy = fal
     w.cld = c.take<double>(2 * L * N);
     w.suc = c.take<double>(kSwSlots * (L + 1) * N);
     w.sdc = c.take<double>(kSwSlots * (L + 1) * N);
-    if (phys) w.cldopt = c.take<double>(3 * 14 * L * N);
+    if (phys && !split) w.cldopt = c.take<double>(3 * 14 * L * N);
+    if (split) w.cldq = c.take<float4>(14 * L * N);
   }
   if (bytes) *bytes = c.off;
   return w;
@@ -218,7 +223,7 @@ LwWorkT<F> work_as(const LwWork& w) {
 }
 template <class F>
 SwWorkT<F> work_as(const SwWork& w) {
-  return SwWorkT<F>{w.idx, (F*)w.f, w.laytrop, w.laysolfr, w.su, w.sd, (F*)w.cld, w.suc, w.sdc, w.cldopt};
+  return SwWorkT<F>{w.idx, (F*)w.f, w.laytrop, w.laysolfr, w.su, w.sd, (F*)w.cld, w.suc, w.sdc, w.cldopt, w.cldq};
 }
 template <class F>
 LwPrepT<F> prep_of(const LwWorkT<F>& w) {
@@ -382,9 +387,12 @@ int sw_enqueue(rrtmg_gpu_state* h, cudaStream_t s, void* base, int ncol, int nla
   // total-sky pass reads in place of the given ones (no forward fraction: they
   // are delta-scaled already)
   const bool phys = cloudy && in.inflag == 2;
-  SwWork w = carve_sw(base, ncol, nlay, nullptr, cloudy, phys);
+  const bool split = h->precision == RRTMG_PREC_SPLIT;
+  SwWork w = carve_sw(base, ncol, nlay, nullptr, cloudy, phys, split);
   SwIn tin = in;
-  if (phys) {
+  if (split) {
+    tin.cldq = w.cldq;
+  } else if (phys) {
     const size_t S = (size_t)14 * nlay * ncol;
     tin.taucld = w.cldopt;
     tin.ssacld = w.cldopt + S;
@@ -399,7 +407,7 @@ int sw_enqueue(rrtmg_gpu_state* h, cudaStream_t s, void* base, int ncol, int nla
   if (h->precision == RRTMG_PREC_SPLIT) {
     const SwWorkT<float> w32 = work_as<float>(w);
     launch_sw_prep_split(in, w32, ncol, nlay, h->flags, s);
-    if (cloudy) launch_sw_cloud_split(in, w32.cld, ncol, nlay, h->flags, s, h->cldtab, w.cldopt);
+    if (cloudy) launch_sw_cloud_split(in, w32.cld, ncol, nlay, h->flags, s, h->cldtab, w.cldq);
     mark(h, 1, 1, s);
     launch_sw_gpoint_split(prep_of(w32), in, adjflux, iaer, h->sw_tab32, h->sw_tab64, h->sw_exp32, cu, cd, ncol,
                            nlay, nb, h->analytic, s);
@@ -434,7 +442,8 @@ int sw_run(rrtmg_gpu_state* h, cudaStream_t s, int ncol, int nlay, int iaer, dou
            const SwIn& in, double* swuflx, double* swdflx, double* swhr, double* swuflxc, double* swdflxc,
            double* swhrc) {
   size_t need;
-  carve_sw(nullptr, ncol, nlay, &need, in.cldfr != nullptr, in.cldfr != nullptr && in.inflag == 2);
+  carve_sw(nullptr, ncol, nlay, &need, in.cldfr != nullptr, in.cldfr != nullptr && in.inflag == 2,
+           h->precision == RRTMG_PREC_SPLIT);
   int rc = ensure(h, h->sw_ws, need, s);
   if (rc) return rc;
   return sw_enqueue(h, s, h->sw_ws.p, ncol, nlay, iaer, adjes, dyofyr, scon, in, swuflx, swdflx, swhr, swuflxc,
@@ -1099,7 +1108,7 @@ int rrtmg_sw_c(rrtmg_gpu_handle h, int ncol, int nlay, int icld, int iaer, const
   const HostOut out[6] = {{swuflx, Lv}, {swdflx, Lv}, {swhr, L}, {swuflxc, Lv}, {swdflxc, Lv}, {swhrc, L}};
   auto need = [&](int nc) {
     size_t b;
-    carve_sw(nullptr, nc, nlay, &b, cloudy, phys);
+    carve_sw(nullptr, nc, nlay, &b, cloudy, phys, h->precision == RRTMG_PREC_SPLIT);
     return b;
   };
   auto enq = [&](cudaStream_t s, void* ws, int nc, const double* const* d, double* const* o) {

@@ -211,6 +211,10 @@ struct SwIn {
   // liqflag 1 parameterisations with the effective sizes reice / reliq)
   int inflag, iceflag, liqflag;
   const double *reice, *reliq;
+  // split path, total-sky pass only (a workspace array, not a caller input):
+  // per layer and band {delta-scaled cloud depth, albedo, asymmetry,
+  // co-albedo}, formed in FP64 by sw_cloud_kernel
+  const float4* cldq;
 };
 // ---------------------------------------------------------------------------
 // Cloud optical property tables (rrlw_cld and rrsw_cld, filled by lwcldpr /
@@ -251,9 +255,11 @@ struct SwWorkT {
   // and the clear-sky band partials
   F* cld;
   double *suc, *sdc;
-  // cloud physics (inflag = 2) only: cldprop_sw's delta-scaled optics,
-  // [tau, ssa, g][14 bands fastest, per layer and column]
+  // cloud physics (inflag = 2), FP64 path only: cldprop_sw's delta-scaled
+  // optics, [tau, ssa, g][14 bands fastest, per layer and column]
   double* cldopt;
+  // clouds, split path only: the cloud optics of the total-sky pass (SwIn::cldq)
+  float4* cldq;
 };
 using SwWork = SwWorkT<double>;
 

@@ -1923,7 +1923,14 @@ __device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, dou
       if (pclfr > (R)0.) {
         R ptauc = (R)0., pomgc = (R)1., pasyc = (R)0.;
         R pcw = (R)0.;  // split path: the cloud's delta-scaled co-albedo 1 - pomgc
-        if (__ldg(cld + fstride + o) > (R)0.) {
+        if (sizeof(R) == 4 && __ldg(cld + fstride + o) > (R)0.) {
+          // split path: the band's optics as sw_cloud_kernel formed them
+          const float4 qv = __ldg(in.cldq + (size_t)(ibm - 1) + 14 * o);
+          ptauc = (R)qv.x;
+          pomgc = (R)qv.y;
+          pasyc = (R)qv.z;
+          pcw = (R)qv.w;
+        } else if (__ldg(cld + fstride + o) > (R)0.) {
           const size_t q = (size_t)(ibm - 1) + 14 * o;
           const R taucldorig = (R)__ldg(in.taucld + q), ffp = in.fsfcld ? (R)__ldg(in.fsfcld + q) : (R)0.;
           const R ssac = (R)__ldg(in.ssacld + q), asmc = (R)__ldg(in.asmcld + q);
@@ -1932,11 +1939,6 @@ __device__ __forceinline__ void sw_band(const SwPrepT<R>& p, const SwIn& in, dou
           pomgc = ffp1 * ssac / ffpssa;
           ptauc = ffpssa * taucldorig;
           pasyc = (asmc - ffp) / (ffp1);
-          if constexpr (sizeof(R) == 4) {
-            // 1 - ffp1 ssac / ffpssa = (1 - ssac) / (1 - ffp ssac), from the FP64 inputs
-            const double ssad = __ldg(in.ssacld + q), ffpd = in.fsfcld ? __ldg(in.fsfcld + q) : 0.0;
-            pcw = (R)((1.0 - ssad) / (1.0 - ffpd * ssad));
-          }
         }
         // total-sky optics (spcvrt_sw :459-464), reftra only for cloudy layers
         // (pclfr > repclc = 1e-12, :388; reftra gives 0, 1, 0, 1 otherwise)
@@ -2100,8 +2102,8 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? RRTMG_SPLIT_SW_MINB :
 // physical range.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ bool sw_cloud_band_optics(const SwIn& in, const double* __restrict__ T, double ciwp,
-                                                     double clwp, double radice, double radliq, int k, double* tau,
-                                                     double* ssa, double* g) {
+                                                     double clwp, double radice, double radliq, int k, double& tau,
+                                                     double& ssa, double& g) {
   const double eps = 1.e-06, cldmin = 1.e-20;
   double ext_i = 0.0, ssa_i = 0.0, g_i = 0.0, fw_i = 0.0;
   if (ciwp != 0.0) {
@@ -2163,13 +2165,13 @@ __device__ __forceinline__ bool sw_cloud_band_optics(const SwIn& in, const doubl
   double t = tauliq + tauice;
   if (t == 0.0) t = cldmin;
   if (scatice == 0.0) scatice = cldmin;
-  *tau = t;
-  *ssa = (scatliq + scatice) / t;
+  tau = t;
+  ssa = (scatliq + scatice) / t;
   if (in.iceflag == 3)
-    *g = (1.0 / (scatliq + scatice)) *
-         (scatliq * (g_l - fw_l) / (1.0 - fw_l) + scatice * ((g_i - fw_i) / (1.0 - fw_i)));
+    g = (1.0 / (scatliq + scatice)) *
+        (scatliq * (g_l - fw_l) / (1.0 - fw_l) + scatice * ((g_i - fw_i) / (1.0 - fw_i)));
   else
-    *g = (scatliq * (g_l - fw_l) / (1.0 - fw_l) + scatice * (g_i - fw_i) / (1.0 - fw_i)) / (scatliq + scatice);
+    g = (scatliq * (g_l - fw_l) / (1.0 - fw_l) + scatice * (g_i - fw_i) / (1.0 - fw_i)) / (scatliq + scatice);
   return true;
 }
 
@@ -2186,12 +2188,18 @@ __device__ __forceinline__ bool sw_cloud_band_optics(const SwIn& in, const doubl
 // With cloud physics (inflag = 2), a sunlit layer whose optics are formed
 // gets them from sw_cloud_band_optics into opt ([tau, ssa, g][lay][col]
 // [band]); a size or optical property that stops the reference sets flag bit
-// 2.  Formed layers are few and scattered, so the warp computes them two at a
-// time with a lane per band, instead of a lane per layer idling the others.
+// 2.  On the split path (quads) every formed layer's band optics go, as the
+// total-sky pass takes them, into quads[lay][col][band] = {delta-scaled depth,
+// albedo, asymmetry, co-albedo}, formed in FP64 once per band instead of once
+// per g-point: with given optics, cldprop_sw's delta-M scaling
+// (rrtmg_sw_cldprop.f90:142-156) and 1 - w' = (1 - ssa) / (1 - f ssa); with
+// the physics, its outputs and 1 - ssa.  Formed layers are few and
+// scattered, so the warp computes them two at a time with a lane per band,
+// instead of a lane per layer idling the others.
 template <class F>
 __global__ void __launch_bounds__(128) sw_cloud_kernel(SwIn in, F* __restrict__ cld, int ncol, int nlay,
                                                        unsigned* __restrict__ flags, const double* __restrict__ T,
-                                                       double* __restrict__ opt) {
+                                                       double* __restrict__ opt, float4* __restrict__ quads) {
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   const bool here = col < ncol;  // every lane stays for the warp's shuffles
   const size_t S = (size_t)nlay * ncol;
@@ -2215,7 +2223,7 @@ __global__ void __launch_bounds__(128) sw_cloud_kernel(SwIn in, F* __restrict__ 
     // total-sky pass reads only optics written here
     if (in.inflag == 2 && !lit) kept = false;
   }
-  if (in.inflag == 2) {
+  if (in.inflag == 2 || quads) {
     const int lane = threadIdx.x & 31;
     const double radice = here && in.reice ? __ldg(in.reice + o) : 0.0;
     const double radliq = here && in.reliq ? __ldg(in.reliq + o) : 0.0;
@@ -2234,9 +2242,29 @@ __global__ void __launch_bounds__(128) sw_cloud_kernel(SwIn in, F* __restrict__ 
       const double ri = __shfl_sync(0xffffffffu, radice, from), rl = __shfl_sync(0xffffffffu, radliq, from);
       const size_t os = __shfl_sync(0xffffffffu, (unsigned long long)o, from);
       bool ok = true;
-      if (src >= 0 && band < kSwBands)
-        ok = sw_cloud_band_optics(in, T, ci, cl, ri, rl, band, opt + 14 * os + band, opt + 14 * (S + os) + band,
-                                  opt + 14 * (2 * S + os) + band);
+      if (src >= 0 && band < kSwBands) {
+        const size_t q = 14 * os + band;
+        double tau, ssa, g, cw;
+        if (in.inflag == 2) {
+          ok = sw_cloud_band_optics(in, T, ci, cl, ri, rl, band, tau, ssa, g);
+          cw = 1.0 - ssa;
+        } else {
+          const double tc = __ldg(in.taucld + q), ffp = in.fsfcld ? __ldg(in.fsfcld + q) : 0.0;
+          const double ssac = __ldg(in.ssacld + q), asmc = __ldg(in.asmcld + q);
+          const double ffp1 = 1.0 - ffp, ffpssa = 1.0 - ffp * ssac;
+          tau = ffpssa * tc;
+          ssa = ffp1 * ssac / ffpssa;
+          g = (asmc - ffp) / ffp1;
+          cw = (1.0 - ssac) / ffpssa;
+        }
+        if (ok && quads) {
+          quads[q] = make_float4((float)tau, (float)ssa, (float)g, (float)cw);
+        } else if (ok) {
+          opt[q] = tau;
+          opt[14 * S + q] = ssa;
+          opt[28 * S + q] = g;
+        }
+      }
       const unsigned bad = __ballot_sync(0xffffffffu, !ok);
       if ((lane == src0 && (bad & 0xffffu)) || (lane == src1 && (bad >> 16))) failed = true;
     }

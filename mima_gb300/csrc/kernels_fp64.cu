@@ -135,11 +135,13 @@ void launch_sw_gpoint_fp64(const SwPrep& p, const SwIn& in, double adjflux, int 
 
 void launch_sw_cloud(const SwIn& in, double* cld, int ncol, int nlay, unsigned* flags, cudaStream_t s,
                      const double* cldtab, double* opt) {
-  sw_cloud_kernel<double><<<dim3((ncol + 127) / 128, nlay), 128, 0, s>>>(in, cld, ncol, nlay, flags, cldtab, opt);
+  sw_cloud_kernel<double><<<dim3((ncol + 127) / 128, nlay), 128, 0, s>>>(in, cld, ncol, nlay, flags, cldtab, opt,
+                                                                        nullptr);
 }
 void launch_sw_cloud_split(const SwIn& in, float* cld, int ncol, int nlay, unsigned* flags, cudaStream_t s,
-                           const double* cldtab, double* opt) {
-  sw_cloud_kernel<float><<<dim3((ncol + 127) / 128, nlay), 128, 0, s>>>(in, cld, ncol, nlay, flags, cldtab, opt);
+                           const double* cldtab, float4* quads) {
+  sw_cloud_kernel<float><<<dim3((ncol + 127) / 128, nlay), 128, 0, s>>>(in, cld, ncol, nlay, flags, cldtab, nullptr,
+                                                                       quads);
 }
 
 void launch_sw_finalize(const double* su, const double* sd, const double* plev, const double* coszen, int ncol,

@@ -65,11 +65,13 @@ void launch_sw_gpoint_fp64(const SwPrep& p, const SwIn& in, double adjflux, int 
                            cudaStream_t s, const double* cld = nullptr);
 // SW clouds (icld = 1): per-layer cover and cldprop mask; flags a partly cloudy
 // layer.  With cloud physics (in.inflag = 2) also the optics of formed layers
-// into opt ([tau, ssa, g][lay][col][band]) from the ct:: tables cldtab.
+// into opt ([tau, ssa, g][lay][col][band]) from the ct:: tables cldtab; on the
+// split path the total-sky pass's cloud optics of every formed layer into
+// quads (SwIn::cldq).
 void launch_sw_cloud(const SwIn& in, double* cld, int ncol, int nlay, unsigned* flags, cudaStream_t s,
                      const double* cldtab = nullptr, double* opt = nullptr);
 void launch_sw_cloud_split(const SwIn& in, float* cld, int ncol, int nlay, unsigned* flags, cudaStream_t s,
-                           const double* cldtab = nullptr, double* opt = nullptr);
+                           const double* cldtab, float4* quads);
 void launch_sw_finalize(const double* su, const double* sd, const double* plev, const double* coszen, int ncol,
                         int nlay, double* swuflx, double* swdflx, double* swhr, double* swuflxc, double* swdflxc,
                         double* swhrc, cudaStream_t s, const double* suc = nullptr, const double* sdc = nullptr);

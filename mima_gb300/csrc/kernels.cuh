@@ -1245,6 +1245,117 @@ __global__ void __launch_bounds__(128) lw_cldphys_kernel(LwIn in, const F* __res
   }
 }
 
+// The split path's LW cloud physics: as lw_cldphys_kernel, with the layer
+// tests (cldprop's keep rule, the size ranges, the count of cloud bands a
+// layer leaves, the table rows and fractions of its sizes) taken once per
+// layer, in FP64 as the reference takes them, by the column's 16 band threads
+// together -- each a sixteenth of the layers -- and shared through shared
+// memory; the depths then follow in FP32.  Dynamic shared memory: 8 columns x
+// nlay layers of LwCldLay.
+struct LwCldLay {
+  float ciwp, clwp, rice, ifint, lfint;
+  unsigned char iidx, lidx;  // table rows (1-based)
+  // bit 0 kept, bits 1-2 the count the layer leaves (0 unchanged, 1: 5, 2: 16),
+  // bits 3-4 iceind, bit 5 liqind = 2, bit 6 ice present, bit 7 liquid present
+  unsigned char code;
+};
+static_assert(sizeof(LwCldLay) == 24, "LwCldLay: 24 bytes (39 KB of shared memory at 203 layers)");
+__global__ void __launch_bounds__(128) lw_cldphys_split_kernel(LwIn in, const float* __restrict__ secdiff,
+                                                               const float* __restrict__ T, float* __restrict__ cld,
+                                                               double* __restrict__ odc, int ncol, int nlay,
+                                                               unsigned* __restrict__ flags) {
+  extern __shared__ LwCldLay slay[];
+  __shared__ int sbad[kBlock / kLwBands];
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = t < (long long)ncol * kLwBands;
+  const int cib = threadIdx.x / kLwBands, iband = threadIdx.x % kLwBands + 1;
+  const int col = valid ? (int)(t / kLwBands) : 0;
+  const size_t N = (size_t)ncol, S = (size_t)nlay * N;
+  LwCldLay* L = slay + (size_t)cib * nlay;
+  if (iband == 1) sbad[cib] = 0;
+  __syncthreads();
+  if (valid) {
+    for (int l = iband - 1; l < nlay; l += kLwBands) {
+      const size_t o = (size_t)l * N + col;
+      double cf, ciwp, clwp;
+      const bool kept = lw_cloud_kept(in, o, cf, ciwp, clwp);
+      cld[o] = cf >= 1.e-6 ? (float)cf : 0.f;
+      cld[S + o] = kept ? 1.f : 0.f;
+      LwCldLay r{};
+      r.code = kept ? 1 : 0;
+      if (kept) {
+        const double radice = in.reice ? __ldg(in.reice + o) : 0.0, radliq = in.reliq ? __ldg(in.reliq + o) : 0.0;
+        int ncb = 0, ii, li;
+        if (!lw_cloud_layer(in, ciwp, clwp, radice, radliq, ncb, ii, li)) sbad[cib] = 1;
+        r.code |= (unsigned char)(((ncb == 5 ? 1 : ncb == 16 ? 2 : 0) << 1) | (ii << 3) | (li == 2 ? 32 : 0) |
+                                  (ciwp != 0.0 ? 64 : 0) | (clwp != 0.0 ? 128 : 0));
+        r.ciwp = (float)ciwp;
+        r.clwp = (float)clwp;
+        r.rice = (float)radice;
+        if (in.inflag == 2 && ciwp != 0.0 && in.iceflag >= 2 && radice >= 5.0 && radice <= 140.0) {
+          const int rows = in.iceflag == 2 ? 43 : 46;
+          const double factor = (radice - 2.) / 3.;
+          int index = (int)factor;
+          if (index == rows) index = rows - 1;
+          r.iidx = (unsigned char)index;
+          r.ifint = (float)(factor - (double)index);
+        }
+        if (in.inflag == 2 && clwp != 0.0 && in.liqflag == 1 && radliq >= 2.5 && radliq <= 60.0) {
+          int index = (int)(radliq - 1.5);
+          if (index == 0) index = 1;
+          if (index == 58) index = 57;
+          r.lidx = (unsigned char)index;
+          r.lfint = (float)(radliq - 1.5 - (double)index);
+        }
+      }
+      L[l] = r;
+    }
+  }
+  __syncthreads();
+  if (!valid) return;
+  const bool ok = sbad[cib] == 0;
+  if (!ok && iband == 1) atomicOr(flags, 4u);
+  int ncb = 1;
+  for (int l = 0; l < nlay; ++l) {
+    const int set = (L[l].code >> 1) & 3;
+    if (set) ncb = set == 1 ? 5 : 16;
+  }
+  const int ib = lw_cloud_band(iband, ncb);
+  const float sec = secdiff[(size_t)(ib - 1) * N + col];
+  int run = 1;
+  for (int l = 0; l < nlay; ++l) {
+    const LwCldLay r = L[l];
+    const bool kept = r.code & 1;
+    float tc = 0.f;
+    if (ok && kept) {
+      const int set = (r.code >> 1) & 3;
+      if (set) run = set == 1 ? 5 : 16;
+      if (ib <= run) {
+        if (in.inflag == 1) {
+          tc = __ldg(T + ct::ABSCLD1) * (r.ciwp + r.clwp);
+        } else {
+          const int iceind = (r.code >> 3) & 3, liqind = (r.code & 32) ? 2 : 0;
+          const int ki = lw_cloud_band(ib, iceind == 0 ? 1 : iceind == 1 ? 5 : 16);
+          const int kl = lw_cloud_band(ib, liqind == 0 ? 1 : 16);
+          float ai = 0.f, al = 0.f;
+          if (r.code & 64) {
+            if (in.iceflag == 0)
+              ai = __ldg(T + ct::ABSICE0) + __ldg(T + ct::ABSICE0 + 1) / r.rice;
+            else if (in.iceflag == 1)
+              ai = __ldg(T + ct::ABSICE1 + 2 * (ki - 1)) + __ldg(T + ct::ABSICE1 + 1 + 2 * (ki - 1)) / r.rice;
+            else
+              ai = cld_interp<float>(T + (in.iceflag == 2 ? ct::ABSICE2 : ct::ABSICE3), in.iceflag == 2 ? 43 : 46,
+                                     r.iidx, r.ifint, ki - 1);
+          }
+          if (r.code & 128) al = in.liqflag == 0 ? __ldg(T + ct::ABSLIQ0) : cld_interp<float>(T + ct::ABSLIQ1, 58, r.lidx, r.lfint, kl - 1);
+          tc = r.ciwp * ai + r.clwp * al;
+        }
+      }
+    }
+    odc[16 * ((size_t)l * N + col) + (iband - 1)] = ok && kept ? (double)(sec * tc) : 0.0;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Overlap factors of maximum/random cloud overlap (icld = 2, 3), one thread
 // per column: rrtmg_lw_rtrnmr.f90:326-475, an upward and a downward scan over

@@ -87,7 +87,10 @@ void launch_lw_cldphys(const LwIn& in, const double* secdiff, const double* cldt
 }
 void launch_lw_cldphys_split(const LwIn& in, const float* secdiff, const float* cldtab, float* cld, double* odc,
                              int ncol, int nlay, unsigned* flags, cudaStream_t s) {
-  lw_cldphys_kernel<float><<<(unsigned)(((long long)ncol * kLwBands + 127) / 128), 128, 0, s>>>(in, secdiff, cldtab, cld, odc, ncol, nlay, flags);
+  // 8 columns x nlay layer records of 24 bytes: at most 39 KB at 203 layers
+  const size_t smem = (size_t)(kBlock / kLwBands) * nlay * sizeof(LwCldLay);
+  lw_cldphys_split_kernel<<<(unsigned)(((long long)ncol * kLwBands + 127) / 128), 128, smem, s>>>(
+      in, secdiff, cldtab, cld, odc, ncol, nlay, flags);
 }
 void launch_lw_overlap(const double* cldfr, double* ovl, int ncol, int nlay, cudaStream_t s) {
   lw_overlap_kernel<double><<<(ncol + 127) / 128, 128, 0, s>>>(cldfr, ovl, ncol, nlay);

@@ -248,3 +248,31 @@ def test_cloud_physics_split_t85_full_grid(gpu, orc):
         for k in keys:
             assert np.abs(out[k] - ref[k]).max() <= SB.FLUX_BAR, (k, np.abs(out[k] - ref[k]).max())
         assert np.all(np.abs(out[hk] - ref[hk]) <= bar), (hk, np.abs(out[hk] - ref[hk]).max())
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_cloud_physics_deep_and_ragged(gpu, orc, precision):
+    """120 layers (the deep-column build of the solvers; the split LW cloud
+    physics keeps 120 layer records per column in shared memory) and 77
+    columns (warps with idle lanes in the SW cloud kernel, which computes a
+    warp's formed layers together): LW maximum/random overlap with iceflag 1
+    and liquid, SW Fu ice."""
+    atm = A.small_atmosphere(77, 120, seed=19)
+    cl = physics_fields(atm, np.random.default_rng(10), overcast=True)
+    lw_c, sw_c = _phys(cl, 2, 1, 1), _phys(cl, 2, 3, 1)
+    rlw = orc.rrtmg_lw(atm, idrv=1, cloud=lw_c, icld=2)
+    rsw = orc.rrtmg_sw(atm, cloud=sw_c)
+    gpu.set_precision(precision)
+    try:
+        lw, sw = gpu.lw(atm, idrv=1, cloud=lw_c, icld=2), gpu.sw(atm, cloud=sw_c)
+    finally:
+        gpu.set_precision("fp64")
+    if precision == "fp64":
+        check_lw(lw, rlw, idrv=1)
+        check_sw(sw, rsw)
+        return
+    bar = SB.hr_bar(atm)
+    for out, ref, keys, hk in ((lw, rlw, ("uflx", "dflx"), "hr"), (sw, rsw, ("swuflx", "swdflx"), "swhr")):
+        for k in keys:
+            assert np.abs(out[k] - ref[k]).max() <= SB.FLUX_BAR, (k, np.abs(out[k] - ref[k]).max())
+        assert np.all(np.abs(out[hk] - ref[hk]) <= bar), (hk, np.abs(out[hk] - ref[hk]).max())

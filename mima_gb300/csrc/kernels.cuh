@@ -98,11 +98,12 @@ constexpr int kRow = 33;
 #define RRTMG_STAGE_ROWS 16
 #endif
 constexpr int kStageRows = RRTMG_STAGE_ROWS;
-// The clear-sky LW solver stages 8 rows: more L1 for its per-thread arrays
-// (measured at T85 x 40: LW 2.738 -> 2.713 ms; the SW solver, 2.283 ->
-// 2.344 ms at 8 rows, keeps 16).
+// The clear-sky LW solver stages 4 rows: more L1 for its per-thread arrays
+// (measured at T85 x 40: LW 2.738 ms at 16 rows, 2.713 at 8; 2.752 at 8 and
+// 2.731 at 4 on another GB300; the SW solver, 2.283 -> 2.344 ms at 8 rows,
+// keeps 16).
 #ifndef RRTMG_LW_STAGE_ROWS
-#define RRTMG_LW_STAGE_ROWS 8
+#define RRTMG_LW_STAGE_ROWS 4
 #endif
 constexpr int kLwStageRows = RRTMG_LW_STAGE_ROWS;
 template <int W, int NG, int NB, bool WEIGHTED, int ROWS = kStageRows>

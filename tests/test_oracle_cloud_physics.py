@@ -148,3 +148,70 @@ def test_physics_size_out_of_range_stops(orc, case):
         call(atm, cloud=dict(phys, inflag=2, **flags))
     phys[water][lay, col] = 0.0
     call(atm, cloud=dict(phys, inflag=2, **flags))
+
+
+# secdiff of a column without water vapour (pwvcm = 0): a0 + a1 clipped to
+# [1.50, 1.80], 1.66 in bands 1, 4 and 10-16 (rrtmg_lw_rtrnmr.f90:271-279)
+_A0 = [1.66, 1.55, 1.58, 1.66, 1.54, 1.454, 1.89, 1.33, 1.668] + [1.66] * 7
+_A1 = [0.00, 0.25, 0.22, 0.00, 0.13, 0.446, -0.10, 0.40, -0.006] + [0.00] * 7
+
+
+def _secdiff_dry():
+    s = []
+    for b in range(1, 17):
+        if b in (1, 4) or b >= 10:
+            s.append(1.66)
+        else:
+            v = _A0[b - 1] + _A1[b - 1] * 1.0
+            s.append(1.80 if v > 1.80 else 1.50 if v < 1.50 else v)
+    return np.array(s)
+
+
+def test_lw_physics_running_band_count(orc, blob):
+    """cldprop's count of cloud bands runs across its layer loop, and rtrn
+    takes band b's cloud depth from cloud band ipat(b, count) along that
+    cloud band's diffusivity angle: two lower layers of ice and liquid
+    (iceflag 1, liqflag 1: 16 cloud bands) under an ice-only layer (5 cloud
+    bands) leave the whole column with 5, so every layer's depth in band b is
+    secdiff(ib) x taucloud(ib), ib = ipat(b, 5), with the ice coefficient band
+    icb(ib, 1) in the mixed layers and ib in the ice-only one.  Stated here
+    from the tables in a dry column (known secdiff) and handed to the given-
+    depth path, the fluxes agree."""
+    atm = A.small_atmosphere(6, 40, seed=21)
+    atm.h2o = np.zeros_like(atm.h2o)
+    L, n = atm.nlay, atm.ncol
+    k1, k2 = (int(np.argmin(np.abs(atm.play[:, 0] - p))) for p in (800.0, 600.0))
+    k3 = int(np.argmin(np.abs(atm.play[:, 0] - 300.0)))
+    assert k1 < k2 < k3
+    z = np.zeros((L, n))
+    cf, ciwp, clwp, rei, rel = z.copy(), z.copy(), z.copy(), z + 40.0, z + 10.0
+    col = lambda *v: np.array(v)[:, None]
+    cf[[k1, k2, k3]] = col(0.7, 0.6, 0.5)
+    ciwp[[k1, k2, k3]] = col(8.0, 15.0, 30.0)
+    clwp[[k1, k2]] = col(60.0, 25.0)
+    rei[[k1, k2, k3]] = col(25.0, 50.0, 90.0)
+    rel[[k1, k2]] = col(7.0, 14.0)
+    phys = dict(cldfr=cf, cicewp=ciwp, cliqwp=clwp, reice=rei, reliq=rel)
+    r = orc.rrtmg_lw(atm, idrv=1, cloud=dict(phys, inflag=2, iceflag=1, liqflag=1))
+
+    T = CO._tab(blob)
+    ice1 = T["lwcld.absice1"]  # (2, 5)
+    sec = _secdiff_dry()
+    ipat5 = CO.ICB5  # ipat(b, 5-band count) = icb(b, 1)
+    tau = np.zeros((L, n, 16))
+    for k in (k1, k2, k3):
+        liq = CO.lw_taucloud(blob, np.zeros(n), clwp[k], rei[k], rel[k], 2) / np.maximum(clwp[k], 1e-300)[:, None]
+        for b in range(1, 17):
+            ib = ipat5[b - 1]
+            kice = ipat5[ib - 1] if clwp[k, 0] != 0.0 else ib   # icb(ib, iceind)
+            absice = ice1[0, kice - 1] + ice1[1, kice - 1] / rei[k]
+            tc = ciwp[k] * absice + (clwp[k] * liq[:, ib - 1] if clwp[k, 0] != 0.0 else 0.0)
+            tau[k, :, b - 1] = sec[ib - 1] * tc / sec[b - 1]
+    g = orc.rrtmg_lw(atm, idrv=1, cloud=dict(cldfr=cf, taucld=tau, cicewp=ciwp, cliqwp=clwp))
+    for key in r:
+        np.testing.assert_allclose(r[key], g[key], rtol=1e-11, atol=1e-9, err_msg=key)
+    # the count matters: with liquid in the top layer too (16 bands) the fluxes move
+    clwp16 = clwp.copy()
+    clwp16[k3] = 1.0
+    r16 = orc.rrtmg_lw(atm, cloud=dict(phys, cliqwp=clwp16, inflag=2, iceflag=1, liqflag=1))
+    assert np.abs(r16["uflx"][-1] - r["uflx"][-1]).max() > 0.1

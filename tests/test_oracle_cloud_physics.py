@@ -215,3 +215,27 @@ def test_lw_physics_running_band_count(orc, blob):
     clwp16[k3] = 1.0
     r16 = orc.rrtmg_lw(atm, cloud=dict(phys, cliqwp=clwp16, inflag=2, iceflag=1, liqflag=1))
     assert np.abs(r16["uflx"][-1] - r["uflx"][-1]).max() > 0.1
+
+
+def test_lw_physics_single_cloud_band(orc, blob):
+    """iceflag 0 with liqflag 0 keeps one cloud band (absice0, absliq0): every
+    band takes cloud band 1's depth along secdiff(1) = 1.66, stated here in a
+    dry column and handed in as given depths."""
+    atm = A.small_atmosphere(6, 40, seed=22)
+    atm.h2o = np.zeros_like(atm.h2o)
+    L, n = atm.nlay, atm.ncol
+    rng = np.random.default_rng(23)
+    cf = np.where((rng.uniform(size=(L, n)) < 0.3) & (atm.play > 150.0), rng.uniform(0.2, 1.0, (L, n)), 0.0)
+    ciwp = np.where(atm.play < 600.0, rng.uniform(0.0, 30.0, (L, n)), 0.0)
+    clwp = np.where(atm.play > 400.0, rng.uniform(0.0, 50.0, (L, n)), 0.0)
+    rei = rng.uniform(10.0, 120.0, (L, n))
+    phys = dict(cldfr=cf, cicewp=ciwp, cliqwp=clwp, reice=rei, reliq=rei * 0 + 10.0)
+    r = orc.rrtmg_lw(atm, cloud=dict(phys, inflag=2, iceflag=0, liqflag=0), icld=2)
+    T = CO._tab(blob)
+    ice0, liq0 = T["lwcld.absice0"], T["lwcld.absliq0"][0]
+    tc = np.where(ciwp != 0.0, ciwp * (ice0[0] + ice0[1] / rei), 0.0) + clwp * liq0
+    sec = _secdiff_dry()
+    tau = (1.66 * tc)[:, :, None] / sec[None, None, :]
+    g = orc.rrtmg_lw(atm, cloud=dict(cldfr=cf, taucld=tau, cicewp=ciwp, cliqwp=clwp), icld=2)
+    for key in r:
+        np.testing.assert_allclose(r[key], g[key], rtol=1e-11, atol=1e-9, err_msg=key)

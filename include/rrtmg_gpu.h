@@ -216,9 +216,12 @@ int rrtmg_gpu_profile(rrtmg_gpu_handle h, float* ms);
  * RRTMG_TRANS_TABLE or RRTMG_TRANS_ANALYTIC for later calls on the handle. */
 int rrtmg_gpu_set_transcendentals(rrtmg_gpu_handle h, int mode);
 
-/* No counterpart in the reference.  Reserves device workspace for LW, SW and
- * fused calls of up to ncol columns and nlay layers, so that later such device
- * calls allocate nothing (e.g. before graph capture). */
+/* No counterpart in the reference.  Reserves device workspace for clear-sky
+ * LW, SW and fused calls of up to ncol columns and nlay layers, so that later
+ * such device calls allocate nothing (e.g. before graph capture).  A call with
+ * clouds needs more (cloud fields, the clear-sky partials, overlap factors,
+ * formed cloud optics): its first call of a size grows the workspace, and
+ * later calls of that size and configuration allocate nothing. */
 int rrtmg_gpu_reserve(rrtmg_gpu_handle h, int ncol, int nlay);
 
 /* No counterpart in the reference (which does not validate its inputs).

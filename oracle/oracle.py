@@ -219,3 +219,43 @@ def table(key: str, name: str) -> np.ndarray:
         buf = np.zeros(n)
         _lib.orc_table(key.encode(), name.encode(), _p(buf), C.c_int(n))
     return buf[:n].copy()
+
+
+def mt_ints(seed: int, n: int) -> np.ndarray:
+    """The first n tempered 32-bit draws of the reference's Mersenne Twister
+    (mcica_random_numbers.f90) seeded with ``seed``."""
+    out = np.zeros(n, dtype=np.uint32)
+    _lib.orc_mt_ints(C.c_int32(seed), C.c_int(n), out.ctypes.data_as(C.POINTER(C.c_uint32)))
+    return out
+
+
+def mcica_subcol(side, atm, cloud, icld: int = 2, irng: int = 1, permuteseed: int = 1):
+    """McICA's stochastic sub-columns (mcica_subcol_lw / mcica_subcol_sw): the
+    cloud fields of ``cloud`` (cldfr, cicewp, cliqwp (nlay, ncol); LW taucld
+    (nlay, ncol, 16); SW taucld, ssacld, asmcld, fsfcld (nlay, ncol, 14))
+    drawn onto one binary cloud mask per g-point (140 LW, 112 SW) and layer,
+    with overlap ``icld`` (1 random, 2 maximum/random, 3 maximum) from the
+    reference's generator ``irng`` (0 kissvec, 1 Mersenne Twister) and
+    ``permuteseed``.  Returns dict of (nlay, ncol, ng) arrays: cldfr, cicewp,
+    cliqwp and the band optics of the cloudy sub-columns."""
+    from mima_gb300 import tables
+    n, L = atm.ncol, atm.nlay
+    blob = tables.read_blob(tables.ensure_blob())
+    ngb = np.asarray(blob[f"{side}.ngb"][0], dtype=np.int64)
+    band = (ngb - ngb[0]).astype(np.int32)
+    nsub, nband = band.size, (16 if side == "lw" else 14)
+    names = ["taucld"] if side == "lw" else ["taucld", "ssacld", "asmcld", "fsfcld"]
+    clear = np.array([0.0] if side == "lw" else [0.0, 1.0, 0.0, 0.0])
+    fields = np.ascontiguousarray(np.stack([np.broadcast_to(cloud[k], (L, n, nband)) for k in names]),
+                                  dtype=np.float64)
+    out = {k: np.zeros((L, n, nsub)) for k in ("cldfr", "cicewp", "cliqwp")}
+    fo = np.zeros((len(names), L, n, nsub))
+    rc = _lib.orc_mcica_subcol(C.c_int(n), C.c_int(L), C.c_int(nsub), C.c_int(icld), C.c_int(irng),
+                               C.c_int(permuteseed), _p(_f(atm.play)), _p(_f(cloud["cldfr"])),
+                               _p(_f(cloud["cicewp"])), _p(_f(cloud["cliqwp"])), C.c_int(nband),
+                               band.ctypes.data_as(C.POINTER(C.c_int)), C.c_int(len(names)), _p(fields),
+                               _p(clear), _p(out["cldfr"]), _p(out["cicewp"]), _p(out["cliqwp"]), _p(fo))
+    if rc != 0:
+        raise RuntimeError(f"orc_mcica_subcol failed ({rc})")
+    out.update({k: fo[j] for j, k in enumerate(names)})
+    return out

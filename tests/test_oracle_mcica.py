@@ -1,0 +1,111 @@
+"""The oracle's McICA stochastic cloud generator (mcica_subcol_gen_lw.f90 /
+mcica_subcol_gen_sw.f90 with mcica_random_numbers.f90), CPU:
+* its Mersenne Twister against numpy's MT19937 with the same scalar seeding;
+* the sub-column masks: the cloudy share of every layer is its cover, binary
+  covers give binary masks, maximum overlap nests the masks by cover,
+  maximum/random overlap keeps adjacent layers of equal cover identical,
+  random overlap draws layers independently;
+* the band optics of a cloudy sub-column are those of its g-point's band,
+  clear sub-columns carry the clear values;
+* the reference's stops: kissvec's seeding needs the layers from the surface
+  up, icld must be in 0..3."""
+import numpy as np
+import pytest
+
+from mima_gb300 import atmosphere as A
+
+
+@pytest.mark.parametrize("seed", [1, 5489, 123456789])
+def test_mersenne_twister_matches_numpy(orc, seed):
+    bg = np.random.MT19937()
+    bg._legacy_seeding(seed)
+    assert np.array_equal(orc.mt_ints(seed, 2000), bg.random_raw(2000).astype(np.uint32))
+
+
+def _clouds(atm, rng, binary=False):
+    L, n = atm.nlay, atm.ncol
+    cf = rng.uniform(0.05, 1.0, (L, n)) * (rng.uniform(size=(L, n)) < 0.5)
+    if binary:
+        cf = np.where(cf > 0.0, 1.0, 0.0)
+    cf = np.where(atm.play > 150.0, cf, 0.0)
+    tau = rng.uniform(0.5, 20.0, (L, n, 16))
+    return dict(cldfr=cf, cicewp=cf * 11.0, cliqwp=cf * 23.0, taucld=tau)
+
+
+@pytest.mark.parametrize("irng", [0, 1])
+@pytest.mark.parametrize("icld", [1, 2, 3])
+def test_subcolumn_cover_is_the_layer_cover(orc, irng, icld):
+    atm = A.small_atmosphere(64, 40, seed=31)
+    cl = _clouds(atm, np.random.default_rng(32))
+    s = orc.mcica_subcol("lw", atm, cl, icld=icld, irng=irng, permuteseed=7)
+    share = s["cldfr"].mean(axis=2)           # (nlay, ncol): 140 draws each
+    err = np.abs(share - cl["cldfr"])
+    # the share of 140 g-points per (layer, column), pooled over the columns
+    assert np.abs(share.mean(axis=1) - cl["cldfr"].mean(axis=1)).max() < 0.06
+    assert err.mean() < 0.05
+    assert set(np.unique(s["cldfr"])) <= {0.0, 1.0}
+    cloudy = s["cldfr"] == 1.0
+    assert np.array_equal(s["cicewp"], np.where(cloudy, cl["cicewp"][:, :, None], 0.0))
+    assert np.array_equal(s["cliqwp"], np.where(cloudy, cl["cliqwp"][:, :, None], 0.0))
+
+
+def test_binary_covers_give_binary_masks(orc):
+    atm = A.small_atmosphere(16, 40, seed=33)
+    cl = _clouds(atm, np.random.default_rng(34), binary=True)
+    for icld in (1, 2, 3):
+        s = orc.mcica_subcol("lw", atm, cl, icld=icld, irng=0)
+        assert np.array_equal(s["cldfr"], np.repeat(cl["cldfr"][:, :, None], 140, axis=2)), icld
+
+
+def test_overlap_structure(orc):
+    atm = A.small_atmosphere(32, 40, seed=35)
+    L, n = atm.nlay, atm.ncol
+    rng = np.random.default_rng(36)
+    cf = np.zeros((L, n))
+    cf[5:9] = rng.uniform(0.2, 0.8, (4, n))
+    cf[12:14] = 0.5
+    cl = dict(cldfr=cf, cicewp=cf, cliqwp=cf, taucld=np.ones((L, n, 16)))
+    # maximum overlap: a sub-column cloudy in a layer is cloudy in every layer of larger cover
+    s3 = orc.mcica_subcol("lw", atm, cl, icld=3, irng=1)["cldfr"] == 1.0
+    for a in range(L):
+        for b in range(L):
+            wider = cf[b] >= cf[a]
+            assert np.all(~s3[a] | ~wider[:, None] | s3[b])
+    # maximum/random: adjacent layers of equal cover share their masks
+    s2 = orc.mcica_subcol("lw", atm, cl, icld=2, irng=1)["cldfr"] == 1.0
+    assert np.array_equal(s2[12], s2[13])
+    # random overlap: adjacent layers independent (joint share ~ product)
+    s1 = orc.mcica_subcol("lw", atm, cl, icld=1, irng=1)["cldfr"] == 1.0
+    joint = (s1[12] & s1[13]).mean()
+    assert abs(joint - 0.25) < 0.04
+    assert abs((s2[12] & s2[13]).mean() - 0.5) < 0.05
+
+
+def test_band_optics_follow_the_g_point(orc, blob):
+    from mima_gb300 import tables
+    atm = A.small_atmosphere(8, 40, seed=37)
+    L, n = atm.nlay, atm.ncol
+    rng = np.random.default_rng(38)
+    cf = np.where(atm.play > 150.0, 0.7, 0.0)
+    sw = dict(cldfr=cf, cicewp=cf, cliqwp=cf, taucld=rng.uniform(1, 5, (L, n, 14)),
+              ssacld=rng.uniform(0.9, 1.0, (L, n, 14)), asmcld=rng.uniform(0.7, 0.9, (L, n, 14)),
+              fsfcld=rng.uniform(0.5, 0.8, (L, n, 14)))
+    s = orc.mcica_subcol("sw", atm, sw, icld=2, irng=0)
+    ngb = np.asarray(tables.read_blob(blob)["sw.ngb"][0]) - 16
+    cloudy = s["cldfr"] == 1.0
+    assert cloudy.any() and (~cloudy).any()
+    for k, clear in (("taucld", 0.0), ("ssacld", 1.0), ("asmcld", 0.0), ("fsfcld", 0.0)):
+        want = np.where(cloudy, sw[k][:, :, ngb], clear)
+        assert np.array_equal(s[k], want), k
+
+
+def test_generator_stops(orc):
+    atm = A.small_atmosphere(4, 40, seed=39)
+    cl = _clouds(atm, np.random.default_rng(40))
+    top_down = atm.subset(np.arange(4))
+    top_down.play = top_down.play[::-1].copy()
+    with pytest.raises(RuntimeError):
+        orc.mcica_subcol("lw", top_down, {k: v[::-1].copy() for k, v in cl.items()}, icld=2, irng=0)
+    orc.mcica_subcol("lw", top_down, {k: v[::-1].copy() for k, v in cl.items()}, icld=2, irng=1)
+    with pytest.raises(RuntimeError):
+        orc.mcica_subcol("lw", atm, cl, icld=4)

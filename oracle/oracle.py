@@ -259,3 +259,31 @@ def mcica_subcol(side, atm, cloud, icld: int = 2, irng: int = 1, permuteseed: in
         raise RuntimeError(f"orc_mcica_subcol failed ({rc})")
     out.update({k: fo[j] for j, k in enumerate(names)})
     return out
+
+
+def rrtmg_lw_mcica(atm, sub, idrv: int = 0, tauaer=None, nthreads: int = 0, inflag: int = 0, iceflag: int = 0,
+                   liqflag: int = 0, reice=None, reliq=None):
+    """McICA rrtmg_lw (rrtmg_lw_rad.f90) on ``atm`` with the sub-column clouds
+    ``sub`` (as mcica_subcol("lw", ...) returns: cldfr, taucld, cicewp,
+    cliqwp (nlay, ncol, 140)), cldprmc's ``inflag`` (0 depths given, 2 the
+    parameterisations with ``reice`` / ``reliq`` (nlay, ncol)) and rtrnmc.
+    Returns the dict of rrtmg_lw."""
+    n, L = atm.ncol, atm.nlay
+    out = {k: np.zeros((L + 1, n)) for k in ("uflx", "dflx", "uflxc", "dflxc", "duflx_dt", "duflxc_dt")}
+    out.update({k: np.zeros((L, n)) for k in ("hr", "hrc")})
+    args = [_f(atm.play), _f(atm.plev), _f(atm.tlay), _f(atm.tlev), _f(atm.tsfc), _f(atm.h2o),
+            _f(atm.o3), _f(atm.co2), _f(atm.ch4), _f(atm.n2o), _f(atm.o2), _f(atm.cfc11),
+            _f(atm.cfc12), _f(atm.cfc22), _f(atm.ccl4), _f(atm.emis)]
+    cl = [_f(sub[k]) for k in ("cldfr", "taucld", "cicewp", "cliqwp")]
+    rad = [None if a is None else _f(a) for a in (reice, reliq)]
+    rc = _lib.orc_rrtmg_lw_mcica(C.c_int(n), C.c_int(L), C.c_int(1), C.c_int(idrv), *[_p(a) for a in args],
+                                 C.c_int(inflag), C.c_int(iceflag), C.c_int(liqflag), *[_p(a) for a in cl],
+                                 *[_p(a) for a in rad], _p(None if tauaer is None else _f(tauaer)),
+                                 _p(out["uflx"]), _p(out["dflx"]), _p(out["hr"]), _p(out["uflxc"]),
+                                 _p(out["dflxc"]), _p(out["hrc"]), _p(out["duflx_dt"]), _p(out["duflxc_dt"]),
+                                 C.c_int(nthreads))
+    if rc == 5:
+        raise CloudRangeError("cldprmc stops (inflag 1, or a size outside its table)")
+    if rc != 0:
+        raise RuntimeError(f"orc_rrtmg_lw_mcica failed ({rc})")
+    return out

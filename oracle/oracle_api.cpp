@@ -20,6 +20,43 @@ using namespace orc;
 static Blob g_blob;
 static int g_ready = 0;
 
+extern "C" int orc_max_threads();
+
+// Every column of an LW call, in parallel; true where cldprop / cldprmc
+// stopped in some column.
+static int lw_columns(const LwInput& in, int idrv, double* uflx, double* dflx, double* hr, double* uflxc,
+                      double* dflxc, double* hrc, double* duflx_dt, double* duflxc_dt, int nthreads) {
+  const int ncol = in.ncol, nlay = in.nlay;
+  int stopped = 0;
+#pragma omp parallel num_threads(nthreads > 0 ? nthreads : orc_max_threads()) reduction(| : stopped)
+  {
+    LwColumn c;
+    LwOut o;
+#pragma omp for schedule(dynamic, 16)
+    for (int iplon = 0; iplon < ncol; ++iplon) {
+      lw_column(in, iplon, idrv, c, o);
+      if (c.cld_error) stopped = 1;
+      for (int k = 0; k <= nlay; ++k) {
+        size_t ix = (size_t)iplon + (size_t)ncol * (size_t)k;
+        uflx[ix] = o.totu[k];
+        dflx[ix] = o.totd[k];
+        uflxc[ix] = o.totuc[k];
+        dflxc[ix] = o.totdc[k];
+        if (idrv == 1 && duflx_dt) {
+          duflx_dt[ix] = o.dtotu_dt[k];
+          if (duflxc_dt) duflxc_dt[ix] = o.dtotuc_dt[k];
+        }
+      }
+      for (int k = 0; k < nlay; ++k) {
+        size_t ix = (size_t)iplon + (size_t)ncol * (size_t)k;
+        hr[ix] = o.htr[k];
+        hrc[ix] = o.htrc[k];
+      }
+    }
+  }
+  return stopped;
+}
+
 extern "C" {
 
 int orc_init(const char* blob_path, double cpdair) {
@@ -73,34 +110,40 @@ int orc_rrtmg_lw(int ncol, int nlay, int icld, int idrv, const double* play, con
   in.liqflag = liqflag;
   in.reice = reice;
   in.reliq = reliq;
-  int stopped = 0;
-#pragma omp parallel num_threads(nthreads > 0 ? nthreads : orc_max_threads()) reduction(| : stopped)
-  {
-    LwColumn c;
-    LwOut o;
-#pragma omp for schedule(dynamic, 16)
-    for (int iplon = 0; iplon < ncol; ++iplon) {
-      lw_column(in, iplon, idrv, c, o);
-      if (c.cld_error) stopped = 1;
-      for (int k = 0; k <= nlay; ++k) {
-        size_t ix = (size_t)iplon + (size_t)ncol * (size_t)k;
-        uflx[ix] = o.totu[k];
-        dflx[ix] = o.totd[k];
-        uflxc[ix] = o.totuc[k];
-        dflxc[ix] = o.totdc[k];
-        if (idrv == 1 && duflx_dt) {
-          duflx_dt[ix] = o.dtotu_dt[k];
-          if (duflxc_dt) duflxc_dt[ix] = o.dtotuc_dt[k];
-        }
-      }
-      for (int k = 0; k < nlay; ++k) {
-        size_t ix = (size_t)iplon + (size_t)ncol * (size_t)k;
-        hr[ix] = o.htr[k];
-        hrc[ix] = o.htrc[k];
-      }
-    }
-  }
+  const int stopped = lw_columns(in, idrv, uflx, dflx, hr, uflxc, dflxc, hrc, duflx_dt, duflxc_dt, nthreads);
   return stopped ? 5 : 0;  // 5: cldprop stopped (an effective radius out of range)
+}
+
+// McICA rrtmg_lw (rrtmg_lw_rad.f90:80-276): the clear-sky inputs of
+// orc_rrtmg_lw with the sub-column clouds cldfmcl, taucmcl, ciwpmcl, clwpmcl
+// (140, ncol, nlay), reicmcl / relqmcl (ncol, nlay), cldprmc's inflag 0 / 2
+// (1 stops) and rtrnmc.  Returns 3 for a bad argument, 5 where cldprmc stops.
+int orc_rrtmg_lw_mcica(int ncol, int nlay, int icld, int idrv, const double* play, const double* plev,
+                       const double* tlay, const double* tlev, const double* tsfc, const double* h2ovmr,
+                       const double* o3vmr, const double* co2vmr, const double* ch4vmr, const double* n2ovmr,
+                       const double* o2vmr, const double* cfc11vmr, const double* cfc12vmr,
+                       const double* cfc22vmr, const double* ccl4vmr, const double* emis, int inflag, int iceflag,
+                       int liqflag, const double* cldfmcl, const double* taucmcl, const double* ciwpmcl,
+                       const double* clwpmcl, const double* reicmcl, const double* relqmcl, const double* tauaer,
+                       double* uflx, double* dflx, double* hr, double* uflxc, double* dflxc, double* hrc,
+                       double* duflx_dt, double* duflxc_dt, int nthreads) {
+  if (!g_ready) return 2;
+  if (icld != 0 && !cldfmcl) return 3;
+  LwInput in{ncol, nlay, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr,
+             cfc11vmr, cfc12vmr, cfc22vmr, ccl4vmr, emis, tauaer};
+  in.icld = icld;
+  in.inflag = inflag;
+  in.iceflag = iceflag;
+  in.liqflag = liqflag;
+  in.mcica = true;
+  in.cldfmcl = cldfmcl;
+  in.taucmcl = taucmcl;
+  in.ciwpmcl = ciwpmcl;
+  in.clwpmcl = clwpmcl;
+  in.reicmcl = reicmcl;
+  in.relqmcl = relqmcl;
+  const int stopped = lw_columns(in, idrv, uflx, dflx, hr, uflxc, dflxc, hrc, duflx_dt, duflxc_dt, nthreads);
+  return stopped ? 5 : 0;
 }
 
 int orc_rrtmg_sw(int ncol, int nlay, int icld, int iaer, const double* play, const double* plev,

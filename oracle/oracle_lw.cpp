@@ -180,6 +180,88 @@ bool lw_cldprop_phys(const LwInput& in, double ciwp, double clwp, double radice,
 }
 
 // ---------------------------------------------------------------------------
+// McICA's cloud inputs and cldprmc (rrtmg_lw_rad.f90 inatm :454-470,
+// rrtmg_lw_cldprmc.f90): each g-point's sub-column cover, depth, ice and
+// liquid water paths of a layer; with inflag = 2 the depth formed from the
+// water paths by the parameterisations at the g-point's band ngb(ig) (the
+// 5-band ice fit at icb(ngb(ig)) for iceflag = 1) where cover >= cldmin and
+// water path or depth >= cldmin; inflag = 0 keeps the given depths; inflag
+// = 1 stops (not available with McICA), as does a size outside its table.
+// ---------------------------------------------------------------------------
+static void lw_cldprmc(const LwInput& in, int iplon, LwColumn& c) {
+  const LwTables& T = g_lw;
+  const int nl = c.nlayers, L1 = nl + 1;
+  const size_t N = (size_t)in.ncol;
+  c.cldfmc.assign((size_t)140 * L1, 0.0);
+  c.taucmc.assign((size_t)140 * L1, 0.0);
+  int bandof[141];
+  for (int b = 1, ig = 1; b <= 16; ++b)
+    for (; ig <= T.ngs[b]; ++ig) bandof[ig] = b;
+  const double cldmin = 1.e-20;
+  for (int l = 1; l <= nl; ++l) {
+    const size_t ol = (size_t)iplon + N * (size_t)(l - 1);
+    const double radice = in.reicmcl ? in.reicmcl[ol] : 0.0, radliq = in.relqmcl ? in.relqmcl[ol] : 0.0;
+    for (int ig = 1; ig <= 140; ++ig) {
+      const size_t q = (size_t)(ig - 1) + 140 * ol;
+      const double cf = in.cldfmcl[q], tau = in.taucmcl ? in.taucmcl[q] : 0.0;
+      const double ciwp = in.ciwpmcl ? in.ciwpmcl[q] : 0.0, clwp = in.clwpmcl ? in.clwpmcl[q] : 0.0;
+      const size_t k = (size_t)(ig - 1) * L1 + l;
+      c.cldfmc[k] = cf;
+      c.taucmc[k] = tau;
+      if (!(cf >= cldmin && (ciwp + clwp >= cldmin || tau >= cldmin))) continue;
+      if (in.inflag == 0) continue;
+      if (in.inflag == 1) {
+        c.cld_error = true;
+        continue;
+      }
+      const int nb = bandof[ig];
+      double abscoice = 0.0, abscoliq = 0.0;
+      if (ciwp == 0.0) {
+        abscoice = 0.0;
+      } else if (in.iceflag == 0) {
+        if (radice < 10.0) c.cld_error = true;
+        abscoice = T.absice0(1) + T.absice0(2) / radice;
+      } else if (in.iceflag == 1) {
+        if (radice < 13.0 || radice > 130.) {
+          c.cld_error = true;
+          continue;
+        }
+        const int ib = kIpat[nb - 1][1];
+        abscoice = T.absice1(1, ib) + T.absice1(2, ib) / radice;
+      } else {
+        const bool two = in.iceflag == 2;
+        if (radice < 5.0 || radice > (two ? 131.0 : 140.0)) {
+          c.cld_error = true;
+          continue;
+        }
+        const double factor = (radice - 2.) / 3.;
+        int index = (int)factor;
+        if (index == (two ? 43 : 46)) index = two ? 42 : 45;
+        const double fint = factor - (double)index;
+        const FArr& t = two ? T.absice2 : T.absice3;
+        abscoice = t(index, nb) + fint * (t(index + 1, nb) - (t(index, nb)));
+      }
+      if (clwp == 0.0) {
+        abscoliq = 0.0;
+      } else if (in.liqflag == 0) {
+        abscoliq = T.absliq0;
+      } else {
+        if (radliq < 2.5 || radliq > 60.) {
+          c.cld_error = true;
+          continue;
+        }
+        int index = (int)(radliq - 1.5);
+        if (index == 0) index = 1;
+        if (index == 58) index = 57;
+        const double fint = radliq - 1.5 - (double)index;
+        abscoliq = T.absliq1(index, nb) + fint * (T.absliq1(index + 1, nb) - (T.absliq1(index, nb)));
+      }
+      c.taucmc[k] = ciwp * abscoice + clwp * abscoliq;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // inatm: rrtmg_lw_rad.nomcica.f90:572-901 (MiMA: h2ovmr carries specific
 // humidity, o3vmr carries the O3 mass mixing ratio, :775-778)
 // ---------------------------------------------------------------------------
@@ -238,7 +320,10 @@ void lw_inatm(const LwInput& in, int iplon, LwColumn& c) {
   // the band-summed optical depth is >= cldmin (1e-20), else they are 0.
   c.ncbands = 1;
   c.cld_error = false;
-  if (in.icld >= 1) {
+  c.mcica = in.mcica && in.icld >= 1;
+  if (c.mcica) {
+    lw_cldprmc(in, iplon, c);
+  } else if (in.icld >= 1) {
     const double cldmin = 1.e-20;
     for (int l = 1; l <= nlay; ++l) {
       const size_t o = (size_t)iplon + (size_t)ncol * (size_t)(l - 1);
@@ -1326,7 +1411,29 @@ void lw_rtrn(LwColumn& c, int idrv, LwOut& out) {
     odcld[ib].assign(nl + 1, 0.0);
     efclfrac[ib].assign(nl + 1, 0.0);
   }
-  for (int lay = 1; lay <= nl; ++lay)
+  // McICA (rtrnmc, rrtmg_lw_rtrnmc.f90:146-170): per g-point, a sub-column is
+  // cloudy where its cover is 1, its depth secdiff(ngb(ig)) x taucmc; a layer
+  // takes the cloudy branch for all its g-points when any of them is cloudy
+  const int L1 = nl + 1;
+  std::vector<double> odg, efg;
+  if (c.mcica) {
+    odg.assign((size_t)140 * L1, 0.0);
+    efg.assign((size_t)140 * L1, 0.0);
+    for (int lay = 1; lay <= nl; ++lay) {
+      icldlyr[lay] = 0;
+      for (int b = 1, ig = 1; b <= 16; ++b)
+        for (; ig <= T.ngs[b]; ++ig) {
+          const size_t k = (size_t)(ig - 1) * L1 + lay;
+          if (c.cldfmc[k] == 1.0) {
+            odg[k] = secdiff[b] * c.taucmc[k];
+            const double transcld = std::exp(-odg[k]);
+            efg[k] = (1.0 - transcld) * c.cldfmc[k];
+            icldlyr[lay] = 1;
+          }
+        }
+    }
+  }
+  for (int lay = 1; lay <= nl && !c.mcica; ++lay)
     for (int ib = 1; ib <= 16; ++ib) {
       if (c.cldfrac[lay] >= 1.e-6) {
         odcld[ib][lay] = secdiff[ib] * c.taucloud[ib][lay];
@@ -1361,6 +1468,10 @@ void lw_rtrn(LwColumn& c, int idrv, LwOut& out) {
   for (int iband = 1; iband <= 16; ++iband) {
     const int ib = lw_cloud_band(iband, c.ncbands);  // ipat(iband, ...) (rrtmg_lw_rtrn.f90:324-330)
     for (; igc <= T.ngs[iband]; ++igc) {
+      // the cloud depth, effective cover and cover of layer lev for this g-point
+      auto OD = [&](int lev) { return c.mcica ? odg[(size_t)(igc - 1) * L1 + lev] : odcld[ib][lev]; };
+      auto EF = [&](int lev) { return c.mcica ? efg[(size_t)(igc - 1) * L1 + lev] : efclfrac[ib][lev]; };
+      auto CF = [&](int lev) { return c.mcica ? c.cldfmc[(size_t)(igc - 1) * L1 + lev] : c.cldfrac[lev]; };
       double radld = 0., radclrd = 0.;
       int iclddn = 0;
       for (int lev = nl; lev >= 1; --lev) {
@@ -1373,7 +1484,7 @@ void lw_rtrn(LwColumn& c, int idrv, LwOut& out) {
         double bbd;
         if (icldlyr[lev] == 1) {  // :350-416
           iclddn = 1;
-          double odtot = odepth + odcld[ib][lev];
+          double odtot = odepth + OD(lev);
           double gassrc, bbdtot;
           if (odtot < 0.06) {
             atrans[lev] = odepth - 0.5 * odepth * odepth;
@@ -1389,7 +1500,7 @@ void lw_rtrn(LwColumn& c, int idrv, LwOut& out) {
             atrans[lev] = odepth - 0.5 * odepth * odepth;
             const double odepth_rec = rec_6 * odepth;
             gassrc = plfrac * (blay + dplankdn * odepth_rec) * atrans[lev];
-            odtot = odepth + odcld[ib][lev];
+            odtot = odepth + OD(lev);
             double ttot, tfactot, odq;
             tbl(odtot, ttot, tfactot, odq);
             bbdtot = plfrac * (blay + tfactot * dplankdn);
@@ -1403,7 +1514,7 @@ void lw_rtrn(LwColumn& c, int idrv, LwOut& out) {
             odepth = odq;  // odepth = tau_tbl(itgas)
             atrans[lev] = 1. - tgas;
             gassrc = atrans[lev] * plfrac * (blay + tfacgas * dplankdn);
-            odtot = odepth + odcld[ib][lev];
+            odtot = odepth + OD(lev);
             double ttot, tfactot, odq2;
             tbl(odtot, ttot, tfactot, odq2);
             bbdtot = plfrac * (blay + tfactot * dplankdn);
@@ -1412,8 +1523,8 @@ void lw_rtrn(LwColumn& c, int idrv, LwOut& out) {
             bbugas[lev] = plfrac * (blay + tfacgas * dplankup);
             bbutot[lev] = plfrac * (blay + tfactot * dplankup);
           }
-          radld = radld - radld * (atrans[lev] + efclfrac[ib][lev] * (1. - atrans[lev])) + gassrc +
-                  c.cldfrac[lev] * (bbdtot * atot[lev] - gassrc);
+          radld = radld - radld * (atrans[lev] + EF(lev) * (1. - atrans[lev])) + gassrc +
+                  CF(lev) * (bbdtot * atot[lev] - gassrc);
           drad[lev - 1] = drad[lev - 1] + radld;
         } else {  // clear layer (:418-436), as rtrnmr
           if (odepth <= 0.06) {
@@ -1456,12 +1567,12 @@ void lw_rtrn(LwColumn& c, int idrv, LwOut& out) {
       for (int lev = 1; lev <= nl; ++lev) {  // :478-520
         if (icldlyr[lev] == 1) {
           const double gassrc = bbugas[lev] * atrans[lev];
-          radlu = radlu - radlu * (atrans[lev] + efclfrac[ib][lev] * (1. - atrans[lev])) + gassrc +
-                  c.cldfrac[lev] * (bbutot[lev] * atot[lev] - gassrc);
+          radlu = radlu - radlu * (atrans[lev] + EF(lev) * (1. - atrans[lev])) + gassrc +
+                  CF(lev) * (bbutot[lev] * atot[lev] - gassrc);
           urad[lev] = urad[lev] + radlu;
           if (idrv == 1) {
-            d_radlu_dt = d_radlu_dt * c.cldfrac[lev] * (1.0 - atot[lev]) +
-                         d_radlu_dt * (1.0 - c.cldfrac[lev]) * (1.0 - atrans[lev]);
+            d_radlu_dt = d_radlu_dt * CF(lev) * (1.0 - atot[lev]) +
+                         d_radlu_dt * (1.0 - CF(lev)) * (1.0 - atrans[lev]);
             d_urad[lev] = d_urad[lev] + d_radlu_dt;
           }
         } else {
@@ -1982,7 +2093,9 @@ void lw_column(const LwInput& in, int iplon, int idrv, LwColumn& c, LwOut& out) 
       for (int k = 1; k <= c.nlayers; ++k) c.taut[ig][k] = c.taug[ig][k] + c.taua[b][k];
   // icld = 1: rtrn (random overlap); icld = 2, 3: rtrnmr with clouds
   // (maximum/random overlap); clear sky: rtrnmr (:527-541)
-  if (in.icld == 1) {
+  // McICA: rtrnmc whatever the overlap (rrtmg_lw_rad.f90:250), the overlap
+  // being in the sub-columns already
+  if (c.mcica || in.icld == 1) {
     lw_rtrn(c, idrv, out);
   } else if (in.icld >= 2) {
     lw_rtrnmr_cld(c, idrv, out);

@@ -37,6 +37,12 @@ struct LwInput {
   // parameterisations selected by iceflag / liqflag, radii reice / reliq)
   int inflag = 0, iceflag = 0, liqflag = 0;
   const double *reice = nullptr, *reliq = nullptr;
+  // McICA (rrtmg_lw_rad.f90): per-g-point sub-column clouds cldfmcl,
+  // taucmcl, ciwpmcl, clwpmcl (140, ncol, nlay), sizes reicmcl / relqmcl
+  // (ncol, nlay); with mcica set the solver is rtrnmc
+  bool mcica = false;
+  const double *cldfmcl = nullptr, *taucmcl = nullptr, *ciwpmcl = nullptr, *clwpmcl = nullptr;
+  const double *reicmcl = nullptr, *relqmcl = nullptr;
 };
 
 struct LwColumn {
@@ -56,6 +62,9 @@ struct LwColumn {
   std::vector<double> cldfrac, taucloud[17];  // icld >= 1: layer cloud fraction, cldprop's cloud optical depth
   int ncbands = 1;        // cldprop's number of cloud bands (1, 5 or 16), the last value it set
   bool cld_error = false;  // cldprop stopped (an effective radius out of its table's range)
+  // McICA: cloud cover and depth of each g-point and layer, [g - 1][layer]
+  bool mcica = false;
+  std::vector<double> cldfmc, taucmc;
 
   void resize(int nl) {
     auto r = [&](std::vector<double>& v) { v.assign(nl + 2, 0.0); };

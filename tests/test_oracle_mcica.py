@@ -8,7 +8,11 @@ mcica_subcol_gen_sw.f90 with mcica_random_numbers.f90), CPU:
 * the band optics of a cloudy sub-column are those of its g-point's band,
   clear sub-columns carry the clear values;
 * the reference's stops: kissvec's seeding needs the layers from the surface
-  up, icld must be in 0..3."""
+  up, icld must be in 0..3;
+* McICA LW (cldprmc, rtrnmc of rrtmg_lw_cldprmc.f90 / rrtmg_lw_rtrnmc.f90):
+  binary covers reproduce rtrn's random overlap bit for bit, with given
+  depths and with cldprmc's ice / liquid parameterisations; partial covers
+  move the fluxes with the overlap."""
 import numpy as np
 import pytest
 
@@ -109,3 +113,59 @@ def test_generator_stops(orc):
     orc.mcica_subcol("lw", top_down, {k: v[::-1].copy() for k, v in cl.items()}, icld=2, irng=1)
     with pytest.raises(RuntimeError):
         orc.mcica_subcol("lw", atm, cl, icld=4)
+
+
+def test_lw_mcica_binary_covers_equal_random_overlap(orc):
+    """rtrnmc on binary sub-columns (every g-point of a layer cloudy or clear)
+    is rtrn's random overlap of covers 0 / 1, bit for bit: same depths along
+    secdiff(ngb), same cloudy branch."""
+    atm = A.small_atmosphere(24, 40, seed=41)
+    cl = _clouds(atm, np.random.default_rng(42), binary=True)
+    sub = orc.mcica_subcol("lw", atm, cl, icld=2, irng=0)
+    mc = orc.rrtmg_lw_mcica(atm, sub, idrv=1)
+    ref = orc.rrtmg_lw(atm, idrv=1, cloud=dict(cldfr=cl["cldfr"], taucld=cl["taucld"]), icld=1)
+    for k in ref:
+        assert np.array_equal(mc[k], ref[k]), k
+
+
+@pytest.mark.parametrize("iceflag", [1, 2, 3])
+def test_lw_mcica_physics_binary_covers(orc, iceflag):
+    """cldprmc's per-g-point parameterisations on binary sub-columns equal
+    cldprop's per band when the column keeps 16 cloud bands (liquid, liqflag 1,
+    in every cloudy layer), bit for bit."""
+    atm = A.small_atmosphere(16, 40, seed=43)
+    rng = np.random.default_rng(44)
+    cl = _clouds(atm, rng, binary=True)
+    cl["cliqwp"] = np.where(cl["cldfr"] > 0, rng.uniform(1.0, 40.0, cl["cldfr"].shape), 0.0)
+    cl["cicewp"] = np.where((cl["cldfr"] > 0) & (atm.play < 700), rng.uniform(0.5, 30.0, cl["cldfr"].shape), 0.0)
+    rei, rel = rng.uniform(20.0, 120.0, cl["cldfr"].shape), rng.uniform(4.0, 40.0, cl["cldfr"].shape)
+    sub = orc.mcica_subcol("lw", atm, dict(cl, taucld=np.zeros_like(cl["taucld"])), icld=1, irng=1)
+    mc = orc.rrtmg_lw_mcica(atm, sub, inflag=2, iceflag=iceflag, liqflag=1, reice=rei, reliq=rel)
+    ref = orc.rrtmg_lw(atm, icld=1, cloud=dict(cldfr=cl["cldfr"], cicewp=cl["cicewp"], cliqwp=cl["cliqwp"],
+                                               reice=rei, reliq=rel, inflag=2, iceflag=iceflag, liqflag=1))
+    for k in ref:
+        assert np.array_equal(mc[k], ref[k]), k
+
+
+def test_lw_mcica_partial_covers(orc):
+    """Twelve adjacent layers at cover 0.5 with opaque cloud: random overlap
+    leaves almost no g-point clear (0.5^12), so its fluxes are the overcast
+    column's; maximum and maximum/random overlap make one block, clear in
+    half the g-points, so their OLR is the mean of clear sky and overcast
+    (within the scatter of 140 draws)."""
+    atm = A.small_atmosphere(64, 40, seed=45)
+    L, n = atm.nlay, atm.ncol
+    cf = np.zeros((L, n))
+    cf[8:20] = 0.5
+    cl = dict(cldfr=cf, cicewp=cf * 0, cliqwp=cf * 0, taucld=np.full((L, n, 16), 5.0))
+    clear = orc.rrtmg_lw(atm)["uflx"][-1]
+    over = orc.rrtmg_lw(atm, cloud=dict(cldfr=np.where(cf > 0, 1.0, 0.0), taucld=cl["taucld"]), icld=1)["uflx"][-1]
+    olr = {icld: orc.rrtmg_lw_mcica(atm, orc.mcica_subcol("lw", atm, cl, icld=icld, irng=1))["uflx"][-1]
+           for icld in (1, 2, 3)}
+    assert np.abs(olr[1] - over).max() < 0.5
+    for icld in (2, 3):
+        assert np.all(olr[icld] > over + 10.0) and np.all(olr[icld] < clear - 10.0)
+        assert abs((olr[icld] - 0.5 * (clear + over)).mean()) < 5.0
+    with pytest.raises(orc.CloudRangeError):
+        s = orc.mcica_subcol("lw", atm, dict(cl, cicewp=cf * 3.0), icld=1, irng=1)
+        orc.rrtmg_lw_mcica(atm, s, inflag=1)

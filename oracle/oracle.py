@@ -287,3 +287,35 @@ def rrtmg_lw_mcica(atm, sub, idrv: int = 0, tauaer=None, nthreads: int = 0, infl
     if rc != 0:
         raise RuntimeError(f"orc_rrtmg_lw_mcica failed ({rc})")
     return out
+
+
+def rrtmg_sw_mcica(atm, sub, iaer: int = 0, tauaer=None, ssaaer=None, asmaer=None, nthreads: int = 0,
+                   inflag: int = 0, iceflag: int = 0, liqflag: int = 0, reice=None, reliq=None):
+    """McICA rrtmg_sw (rrtmg_sw_rad.f90) on ``atm`` with the sub-column clouds
+    ``sub`` (as mcica_subcol("sw", ...) returns: cldfr, taucld, ssacld,
+    asmcld, fsfcld, cicewp, cliqwp (nlay, ncol, 112)), cldprmc_sw's ``inflag``
+    (0 optics given, 2 the parameterisations with ``reice`` / ``reliq``
+    (nlay, ncol)) and spcvmc_sw.  Every column is computed, dark ones with
+    cos(zenith) clamped to 1e-10 as the McICA driver does.  Returns the dict
+    of rrtmg_sw."""
+    n, L = atm.ncol, atm.nlay
+    out = {k: np.zeros((L + 1, n)) for k in ("swuflx", "swdflx", "swuflxc", "swdflxc")}
+    out.update({k: np.zeros((L, n)) for k in ("swhr", "swhrc")})
+    args = [_f(atm.play), _f(atm.plev), _f(atm.tlay), _f(atm.tlev), _f(atm.tsfc), _f(atm.h2o),
+            _f(atm.o3), _f(atm.co2), _f(atm.ch4), _f(atm.n2o), _f(atm.o2), _f(atm.asdir),
+            _f(atm.asdif), _f(atm.aldir), _f(atm.aldif), _f(atm.coszen)]
+    cl = [None if sub.get(k) is None else _f(sub[k])
+          for k in ("cldfr", "taucld", "ssacld", "asmcld", "fsfcld", "cicewp", "cliqwp")]
+    rad = [None if a is None else _f(a) for a in (reice, reliq)]
+    aer = [None if a is None else _f(a) for a in (tauaer, ssaaer, asmaer)]
+    rc = _lib.orc_rrtmg_sw_mcica(C.c_int(n), C.c_int(L), C.c_int(1), C.c_int(iaer), *[_p(a) for a in args],
+                                 C.c_double(atm.adjes), C.c_int(atm.dyofyr), C.c_double(atm.scon),
+                                 C.c_int(inflag), C.c_int(iceflag), C.c_int(liqflag), *[_p(a) for a in cl],
+                                 *[_p(a) for a in rad], *[_p(a) for a in aer],
+                                 _p(out["swuflx"]), _p(out["swdflx"]), _p(out["swhr"]), _p(out["swuflxc"]),
+                                 _p(out["swdflxc"]), _p(out["swhrc"]), C.c_int(nthreads))
+    if rc == 5:
+        raise CloudRangeError("cldprmc_sw stops (inflag 1, or a size outside its table)")
+    if rc != 0:
+        raise RuntimeError(f"orc_rrtmg_sw_mcica failed ({rc})")
+    return out

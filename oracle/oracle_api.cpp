@@ -57,6 +57,40 @@ static int lw_columns(const LwInput& in, int idrv, double* uflx, double* dflx, d
   return stopped;
 }
 
+// Every column of an SW call, in parallel; *partial / *stopped as sw_column
+// reports them for some column.
+static void sw_columns(const SwInput& in, double* swuflx, double* swdflx, double* swhr, double* swuflxc,
+                       double* swdflxc, double* swhrc, int nthreads, int* partial_out, int* stopped_out) {
+  const int ncol = in.ncol, nlay = in.nlay;
+  int partial = 0, stopped = 0;
+#pragma omp parallel num_threads(nthreads > 0 ? nthreads : orc_max_threads()) reduction(| : partial, stopped)
+  {
+    SwColumn c;
+    SwOut o;
+#pragma omp for schedule(dynamic, 16)
+    for (int iplon = 0; iplon < ncol; ++iplon) {
+      bool part = false, stop = false;
+      sw_column(in, iplon, c, o, &part, &stop);
+      if (part) partial = 1;
+      if (stop) stopped = 1;
+      for (int k = 1; k <= nlay + 1; ++k) {
+        size_t ix = (size_t)iplon + (size_t)ncol * (size_t)(k - 1);
+        swuflx[ix] = o.fu[k];
+        swdflx[ix] = o.fd[k];
+        swuflxc[ix] = o.cu[k];
+        swdflxc[ix] = o.cd[k];
+      }
+      for (int k = 1; k <= nlay; ++k) {
+        size_t ix = (size_t)iplon + (size_t)ncol * (size_t)(k - 1);
+        swhr[ix] = o.hr[k];
+        swhrc[ix] = o.hrc[k];
+      }
+    }
+  }
+  *partial_out = partial;
+  *stopped_out = stopped;
+}
+
 extern "C" {
 
 int orc_init(const char* blob_path, double cpdair) {
@@ -180,33 +214,55 @@ int orc_rrtmg_sw(int ncol, int nlay, int icld, int iaer, const double* play, con
   in.reice = reice;
   in.reliq = reliq;
   int partial = 0, stopped = 0;
-#pragma omp parallel num_threads(nthreads > 0 ? nthreads : orc_max_threads()) reduction(| : partial, stopped)
-  {
-    SwColumn c;
-    SwOut o;
-#pragma omp for schedule(dynamic, 16)
-    for (int iplon = 0; iplon < ncol; ++iplon) {
-      bool part = false, stop = false;
-      sw_column(in, iplon, c, o, &part, &stop);
-      if (part) partial = 1;
-      if (stop) stopped = 1;
-      for (int k = 1; k <= nlay + 1; ++k) {
-        size_t ix = (size_t)iplon + (size_t)ncol * (size_t)(k - 1);
-        swuflx[ix] = o.fu[k];
-        swdflx[ix] = o.fd[k];
-        swuflxc[ix] = o.cu[k];
-        swdflxc[ix] = o.cd[k];
-      }
-      for (int k = 1; k <= nlay; ++k) {
-        size_t ix = (size_t)iplon + (size_t)ncol * (size_t)(k - 1);
-        swhr[ix] = o.hr[k];
-        swhrc[ix] = o.hrc[k];
-      }
-    }
-  }
+  sw_columns(in, swuflx, swdflx, swhr, swuflxc, swdflxc, swhrc, nthreads, &partial, &stopped);
   // 5: cldprop_sw stopped (a size out of its range); 4: a partly cloudy
   // layer (the reference's non-McICA SW stops)
   return stopped ? 5 : partial ? 4 : 0;
+}
+
+// McICA rrtmg_sw (rrtmg_sw_rad.f90:84-90): the argument list of orc_rrtmg_sw
+// with the sub-column clouds cldfmcl, taucmcl, ssacmcl, asmcmcl, fsfcmcl,
+// ciwpmcl, clwpmcl (112, ncol, nlay) in place of the layer clouds, reicmcl /
+// relqmcl (ncol, nlay); cldprmc_sw's inflag 0 (optics given) or 2 (iceflag
+// 1..3, liqflag 1).  Returns 3 for missing or invalid inputs, 5 where
+// cldprmc_sw stops.
+int orc_rrtmg_sw_mcica(int ncol, int nlay, int icld, int iaer, const double* play, const double* plev,
+                       const double* tlay, const double* tlev, const double* tsfc, const double* h2ovmr,
+                       const double* o3vmr, const double* co2vmr, const double* ch4vmr, const double* n2ovmr,
+                       const double* o2vmr, const double* asdir, const double* asdif, const double* aldir,
+                       const double* aldif, const double* coszen, double adjes, int dyofyr, double scon,
+                       int inflag, int iceflag, int liqflag, const double* cldfmcl, const double* taucmcl,
+                       const double* ssacmcl, const double* asmcmcl, const double* fsfcmcl,
+                       const double* ciwpmcl, const double* clwpmcl, const double* reicmcl,
+                       const double* relqmcl, const double* tauaer, const double* ssaaer, const double* asmaer,
+                       double* swuflx, double* swdflx, double* swhr, double* swuflxc, double* swdflxc,
+                       double* swhrc, int nthreads) {
+  if (!g_ready) return 2;
+  if (icld != 0 && !cldfmcl) return 3;
+  if (icld != 0 && inflag == 0 && !(taucmcl && ssacmcl && asmcmcl && fsfcmcl)) return 3;
+  if (icld != 0 && inflag == 2 &&
+      !(iceflag >= 1 && iceflag <= 3 && liqflag == 1 && ciwpmcl && clwpmcl && reicmcl && relqmcl))
+    return 3;
+  if (iaer != 0 && iaer != 10) return 3;
+  SwInput in{ncol, nlay, iaer, dyofyr, adjes, scon, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr,
+             ch4vmr, n2ovmr, o2vmr, asdir, asdif, aldir, aldif, coszen, tauaer, ssaaer, asmaer};
+  in.icld = icld;
+  in.inflag = inflag;
+  in.iceflag = iceflag;
+  in.liqflag = liqflag;
+  in.reice = reicmcl;
+  in.reliq = relqmcl;
+  in.mcica = true;
+  in.cldfmcl = cldfmcl;
+  in.taucmcl = taucmcl;
+  in.ssacmcl = ssacmcl;
+  in.asmcmcl = asmcmcl;
+  in.fsfcmcl = fsfcmcl;
+  in.ciwpmcl = ciwpmcl;
+  in.clwpmcl = clwpmcl;
+  int partial = 0, stopped = 0;
+  sw_columns(in, swuflx, swdflx, swhr, swuflxc, swdflxc, swhrc, nthreads, &partial, &stopped);
+  return stopped ? 5 : 0;
 }
 
 // Clear-sky rrtmg_lw per band: bandu/bandd/dbandu_dt (ncol, nlay+1, 16) are the

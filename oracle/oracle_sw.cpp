@@ -825,6 +825,13 @@ void sw_spcvrt(SwColumn& c, double prmu0, const double* albdir, const double* al
     int ibm = jb - 15;
     for (int jg = 1; jg <= T.ngc[jb]; ++jg) {
       iw = iw + 1;
+      // spcvmc_sw (rrtmg_sw_spcvmc.f90:388, 412-413, 462-474, 504-505): the
+      // g-point's own cover and cloud optics in place of the band's
+      const size_t gk = (size_t)(iw - 1) * (size_t)K;
+      auto CF = [&](int lay) { return c.mcica ? c.cldfmc[gk + lay] : c.pclfr[lay]; };
+      auto TC = [&](int lay) { return c.mcica ? c.taucmc[gk + lay] : c.ptauc[ibm][lay]; };
+      auto OC = [&](int lay) { return c.mcica ? c.ssacmc[gk + lay] : c.pomgc[ibm][lay]; };
+      auto AC = [&](int lay) { return c.mcica ? c.asmcmc[gk + lay] : c.pasyc[ibm][lay]; };
       double zincflx = c.adjflux[jb] * c.sfluxzen[iw] * prmu0;
       ztdbtc[1] = 1.0;
       zdbtc[klev + 1] = 0.0;
@@ -845,7 +852,7 @@ void sw_spcvrt(SwColumn& c, double prmu0, const double* albdir, const double* al
       for (int jk = 1; jk <= klev; ++jk) {
         int ikl = klev + 1 - jk;
         lrtchkclr[jk] = 1;
-        lrtchkcld[jk] = c.pclfr[ikl] > 1.e-12;  // pclfr > repclc (:263, :388)
+        lrtchkcld[jk] = CF(ikl) > 1.e-12;  // pclfr > repclc (:263, :388)
         double taua = c.taua[ibm][ikl], omga = c.ssaa[ibm][ikl], asya = c.asma[ibm][ikl];
         ztauc[jk] = c.taur[iw][ikl] + c.taug[iw][ikl] + taua;
         zomcc[jk] = c.taur[iw][ikl] * 1.0 + taua * omga;
@@ -858,7 +865,7 @@ void sw_spcvrt(SwColumn& c, double prmu0, const double* albdir, const double* al
         zgcc[jk] = (zgcc[jk] - zf) / (1.0 - zf);
         // icpr >= 1 (:459-464); clear sky: ptauc = 0, pomgc = 1, pasyc = 0
         OPC_PAUSE();
-        const double ptauc = c.ptauc[ibm][ikl], pomgc = c.pomgc[ibm][ikl], pasyc = c.pasyc[ibm][ikl];
+        const double ptauc = TC(ikl), pomgc = OC(ikl), pasyc = AC(ikl);
         ztauo[jk] = ztauc[jk] + ptauc;
         zomco[jk] = ztauc[jk] * zomcc[jk] + ptauc * pomgc;
         zgco[jk] = (ptauc * pomgc * pasyc + ztauc[jk] * zomcc[jk] * zgcc[jk]) / zomco[jk];
@@ -872,7 +879,7 @@ void sw_spcvrt(SwColumn& c, double prmu0, const double* albdir, const double* al
       for (int jk = 1; jk <= klev; ++jk) {
         OPC_PAUSE();
         const int ikl = klev + 1 - jk;
-        const double zclear = 1.0 - c.pclfr[ikl], zcloud = c.pclfr[ikl];
+        const double zclear = 1.0 - CF(ikl), zcloud = CF(ikl);
         zref[jk] = zclear * zrefc[jk] + zcloud * zrefo[jk];
         zrefd[jk] = zclear * zrefdc[jk] + zcloud * zrefdo[jk];
         ztra[jk] = zclear * ztrac[jk] + zcloud * ztrao[jk];
@@ -909,20 +916,24 @@ void sw_spcvrt(SwColumn& c, double prmu0, const double* albdir, const double* al
 // the STREAMER table, 2; Fu's table with its delta fractions, 3) and liquid
 // (Hu-Stamnes table, liqflag 1) extinction, single-scattering albedo and
 // asymmetry, each delta-M scaled, combined into the layer's delta-scaled
-// optics.  Returns false where the reference stops.
+// optics.  Returns false where the reference stops.  band = 0: the 14 bands
+// (cldprop_sw); band = 16..29: that band alone, as cldprmc_sw forms one
+// g-point's optics on its band ngb(ig) (rrtmg_sw_cldprmc.f90:163-298), its
+// stops taken on that band only.
 static bool sw_cldprop_phys(const SwInput& in, double ciwp, double clwp, double radice, double radliq,
-                            double* taucloud, double* ssacloud, double* asmcloud) {
+                            double* taucloud, double* ssacloud, double* asmcloud, int band = 0) {
   const SwTables& T = g_sw;
+  const int lo = band ? band : 16, hi = band ? band : 29;
   const double eps = 1.e-06, cldmin = 1.e-20;
   double extcoice[30], ssacoice[30], gice[30], forwice[30], extcoliq[30], ssacoliq[30], gliq[30], forwliq[30];
   auto ice_ok = [&](int ib) {
     return !(extcoice[ib] < 0.0 || ssacoice[ib] > 1.0 || ssacoice[ib] < 0.0 || gice[ib] > 1.0 || gice[ib] < 0.0);
   };
   if (ciwp == 0.0) {
-    for (int ib = 16; ib <= 29; ++ib) extcoice[ib] = ssacoice[ib] = gice[ib] = forwice[ib] = 0.0;
+    for (int ib = lo; ib <= hi; ++ib) extcoice[ib] = ssacoice[ib] = gice[ib] = forwice[ib] = 0.0;
   } else if (in.iceflag == 1) {
     if (radice < 13.0 || radice > 130.) return false;
-    for (int ib = 16; ib <= 29; ++ib) {
+    for (int ib = lo; ib <= hi; ++ib) {
       const double wn = T.wavenum2(ib - 15);
       int icx = 5;
       if (wn > 1.43e04) icx = 1;
@@ -942,7 +953,7 @@ static bool sw_cldprop_phys(const SwInput& in, double ciwp, double clwp, double 
     int index = (int)factor;
     if (index == 43) index = 42;
     const double fint = factor - (double)index;
-    for (int ib = 16; ib <= 29; ++ib) {
+    for (int ib = lo; ib <= hi; ++ib) {
       extcoice[ib] = T.extice2(index, ib) + fint * (T.extice2(index + 1, ib) - T.extice2(index, ib));
       ssacoice[ib] = T.ssaice2(index, ib) + fint * (T.ssaice2(index + 1, ib) - T.ssaice2(index, ib));
       gice[ib] = T.asyice2(index, ib) + fint * (T.asyice2(index + 1, ib) - T.asyice2(index, ib));
@@ -955,7 +966,7 @@ static bool sw_cldprop_phys(const SwInput& in, double ciwp, double clwp, double 
     int index = (int)factor;
     if (index == 46) index = 45;
     const double fint = factor - (double)index;
-    for (int ib = 16; ib <= 29; ++ib) {
+    for (int ib = lo; ib <= hi; ++ib) {
       extcoice[ib] = T.extice3(index, ib) + fint * (T.extice3(index + 1, ib) - T.extice3(index, ib));
       ssacoice[ib] = T.ssaice3(index, ib) + fint * (T.ssaice3(index + 1, ib) - T.ssaice3(index, ib));
       gice[ib] = T.asyice3(index, ib) + fint * (T.asyice3(index + 1, ib) - T.asyice3(index, ib));
@@ -967,14 +978,14 @@ static bool sw_cldprop_phys(const SwInput& in, double ciwp, double clwp, double 
     }
   }
   if (clwp == 0.0) {
-    for (int ib = 16; ib <= 29; ++ib) extcoliq[ib] = ssacoliq[ib] = gliq[ib] = forwliq[ib] = 0.0;
+    for (int ib = lo; ib <= hi; ++ib) extcoliq[ib] = ssacoliq[ib] = gliq[ib] = forwliq[ib] = 0.0;
   } else {
     if (radliq < 2.5 || radliq > 60.) return false;
     int index = (int)(radliq - 1.5);
     if (index == 0) index = 1;
     if (index == 58) index = 57;
     const double fint = radliq - 1.5 - (double)index;
-    for (int ib = 16; ib <= 29; ++ib) {
+    for (int ib = lo; ib <= hi; ++ib) {
       extcoliq[ib] = T.extliq1(index, ib) + fint * (T.extliq1(index + 1, ib) - T.extliq1(index, ib));
       ssacoliq[ib] = T.ssaliq1(index, ib) + fint * (T.ssaliq1(index + 1, ib) - T.ssaliq1(index, ib));
       if (fint < 0. && ssacoliq[ib] > 1.) ssacoliq[ib] = T.ssaliq1(index, ib);
@@ -984,7 +995,7 @@ static bool sw_cldprop_phys(const SwInput& in, double ciwp, double clwp, double 
         return false;
     }
   }
-  for (int ib = 16; ib <= 29; ++ib) {
+  for (int ib = lo; ib <= hi; ++ib) {
     const double tauliqorig = clwp * extcoliq[ib];
     const double tauiceorig = ciwp * extcoice[ib];
     const double ssaliq = ssacoliq[ib] * (1.0 - forwliq[ib]) / (1.0 - forwliq[ib] * ssacoliq[ib]);
@@ -1057,12 +1068,69 @@ static bool sw_cldprop(const SwInput& in, int iplon, SwColumn& c) {
   return true;
 }
 
+// McICA's cloud inputs (inatm_sw, rrtmg_sw_rad.f90:1084-1099) and cldprmc_sw
+// (rrtmg_sw_cldprmc.f90:117-328): per g-point iw and layer, a sub-column whose
+// cover is >= cldmin and whose water path or own depth is >= cldmin (1e-20)
+// gets its optics formed -- inflag = 0 the given ones delta-M scaled with the
+// forward-scattering fraction, inflag = 2 the parameterisations on its band
+// ngb(iw); other sub-columns keep the optics given.  inflag = 1 stops (not
+// available with McICA), as does a size or optical property out of range.
+static bool sw_cldprmc(const SwInput& in, int iplon, SwColumn& c) {
+  const int nl = in.nlay, ncol = in.ncol, L2 = nl + 2;
+  const double cldmin = 1.e-20;
+  c.cldfmc.assign((size_t)112 * L2, 0.0);
+  c.taucmc.assign((size_t)112 * L2, 0.0);
+  c.ssacmc.assign((size_t)112 * L2, 1.0);
+  c.asmcmc.assign((size_t)112 * L2, 0.0);
+  for (int lay = 1; lay <= nl; ++lay) {
+    const size_t o = (size_t)iplon + (size_t)ncol * (size_t)(lay - 1);
+    int iw = 0;
+    for (int jb = 16; jb <= 29; ++jb)
+      for (int jg = 1; jg <= g_sw.ngc[jb]; ++jg) {
+        iw = iw + 1;
+        const size_t q = (size_t)(iw - 1) + 112 * o, k = (size_t)(iw - 1) * L2 + lay;
+        const double cf = in.cldfmcl[q];
+        double tau = in.taucmcl ? in.taucmcl[q] : 0.0;
+        double ssa = in.ssacmcl ? in.ssacmcl[q] : 1.0;
+        double asy = in.asmcmcl ? in.asmcmcl[q] : 0.0;
+        const double ciwp = in.ciwpmcl ? in.ciwpmcl[q] : 0.0, clwp = in.clwpmcl ? in.clwpmcl[q] : 0.0;
+        const double cwp = ciwp + clwp;
+        if (cf >= cldmin && (cwp >= cldmin || tau >= cldmin)) {
+          if (in.inflag == 0) {
+            const double ffp = in.fsfcmcl[q];
+            const double ffp1 = 1.0 - ffp;
+            const double ffpssa = 1.0 - ffp * ssa;
+            const double ssacloud_a = ffp1 * ssa / ffpssa;
+            tau = ffpssa * tau;
+            ssa = ssacloud_a;
+            asy = (asy - ffp) / (ffp1);
+          } else if (in.inflag == 1) {
+            return false;
+          } else if (in.inflag == 2) {
+            double tc[14], sc[14], ac[14];
+            if (!sw_cldprop_phys(in, ciwp, clwp, in.reice ? in.reice[o] : 0.0, in.reliq ? in.reliq[o] : 0.0, tc,
+                                 sc, ac, jb))
+              return false;
+            tau = tc[jb - 16];
+            ssa = sc[jb - 16];
+            asy = ac[jb - 16];
+          }
+        }
+        c.cldfmc[k] = cf;
+        c.taucmc[k] = tau;
+        c.ssacmc[k] = ssa;
+        c.asmcmc[k] = asy;
+      }
+  }
+  return true;
+}
+
 bool sw_column(const SwInput& in, int iplon, SwColumn& c, SwOut& out, bool* partial, bool* stopped) {
   const double zepzen = 1.e-10;
   int nl = in.nlay;
   if (partial) *partial = false;
   if (stopped) *stopped = false;
-  if (in.coszen[iplon] < zepzen) {
+  if (!in.mcica && in.coszen[iplon] < zepzen) {
     out.fu.assign(nl + 2, 0.);
     out.fd.assign(nl + 2, 0.);
     out.cu.assign(nl + 2, 0.);
@@ -1072,7 +1140,10 @@ bool sw_column(const SwInput& in, int iplon, SwColumn& c, SwOut& out, bool* part
     return false;
   }
   sw_inatm(in, iplon, c);
-  if (in.icld >= 1) {
+  c.mcica = in.mcica && in.icld >= 1;
+  if (c.mcica) {
+    if (!sw_cldprmc(in, iplon, c) && stopped) *stopped = true;
+  } else if (in.icld >= 1) {
     // without McICA the SW computes clear or overcast layers only (:533-538)
     const double zepsec = 1.e-06, oneminus = 1.0 - zepsec;
     for (int i = 1; i <= nl; ++i) {

@@ -40,6 +40,12 @@ struct SwInput {
   // iceflag (1..3) and liqflag (1), effective sizes reice / reliq)
   int inflag = 0, iceflag = 0, liqflag = 0;
   const double *reice = nullptr, *reliq = nullptr;
+  // McICA (rrtmg_sw_rad.f90:84-90): sub-column clouds, one per g-point, in
+  // place of cldfr / taucld / ... -- cldfmcl, taucmcl, ssacmcl, asmcmcl,
+  // fsfcmcl, ciwpmcl, clwpmcl (112, ncol, nlay); reice / reliq as above.
+  bool mcica = false;
+  const double *cldfmcl = nullptr, *taucmcl = nullptr, *ssacmcl = nullptr, *asmcmcl = nullptr,
+               *fsfcmcl = nullptr, *ciwpmcl = nullptr, *clwpmcl = nullptr;
 };
 
 struct SwColumn {
@@ -54,6 +60,10 @@ struct SwColumn {
   std::vector<double> taug[113], taur[113];
   // clouds: cover and cldprop_sw's delta-scaled cloud optics per band (ibm 1..14)
   std::vector<double> pclfr, ptauc[15], pomgc[15], pasyc[15];
+  // McICA: cover and cldprmc_sw's delta-scaled optics per g-point,
+  // [(iw - 1) * (nlayers + 2) + lay]
+  bool mcica = false;
+  std::vector<double> cldfmc, taucmc, ssacmc, asmcmc;
   double sfluxzen[113];
 
   void resize(int nl) {
@@ -95,7 +105,10 @@ void sw_spcvrt(SwColumn& c, double prmu0, const double* albdir, const double* al
                bool run_taumol = true);
 // Returns false for a dark column (no SW); sets *partial when the column holds
 // a partly cloudy layer, which the reference's non-McICA SW refuses
-// (rrtmg_sw_rad.nomcica.f90:533-538).
+// (rrtmg_sw_rad.nomcica.f90:533-538).  With in.mcica the McICA driver
+// (rrtmg_sw_rad.f90): cldprmc_sw and spcvmc_sw, every column computed (the
+// McICA driver has no dark-column skip: cos(zenith) is clamped to 1e-10),
+// partial covers allowed.
 // *stopped: cldprop_sw stopped for this column (a size out of range or an
 // optical property out of its physical range).
 bool sw_column(const SwInput& in, int iplon, SwColumn& c, SwOut& out, bool* partial = nullptr,

@@ -12,7 +12,11 @@ mcica_subcol_gen_sw.f90 with mcica_random_numbers.f90), CPU:
 * McICA LW (cldprmc, rtrnmc of rrtmg_lw_cldprmc.f90 / rrtmg_lw_rtrnmc.f90):
   binary covers reproduce rtrn's random overlap bit for bit, with given
   depths and with cldprmc's ice / liquid parameterisations; partial covers
-  move the fluxes with the overlap."""
+  move the fluxes with the overlap;
+* McICA SW (cldprmc_sw, spcvmc_sw of rrtmg_sw_cldprmc.f90 /
+  rrtmg_sw_spcvmc.f90): the same pins against spcvrt on clear / overcast
+  layers, and the McICA driver's dark columns (computed at cos(zenith) =
+  1e-10, not skipped)."""
 import numpy as np
 import pytest
 
@@ -169,3 +173,86 @@ def test_lw_mcica_partial_covers(orc):
     with pytest.raises(orc.CloudRangeError):
         s = orc.mcica_subcol("lw", atm, dict(cl, cicewp=cf * 3.0), icld=1, irng=1)
         orc.rrtmg_lw_mcica(atm, s, inflag=1)
+
+
+def _sw_clouds(atm, rng, binary=True):
+    L, n = atm.nlay, atm.ncol
+    cf = (rng.uniform(size=(L, n)) < 0.3) * 1.0
+    if not binary:
+        cf = cf * rng.uniform(0.1, 1.0, (L, n))
+    cf = np.where(atm.play > 150.0, cf, 0.0)
+    return dict(cldfr=cf, cicewp=cf * 0.0, cliqwp=cf * 0.0, taucld=rng.uniform(0.5, 20.0, (L, n, 14)),
+                ssacld=rng.uniform(0.9, 0.999999, (L, n, 14)), asmcld=rng.uniform(0.7, 0.9, (L, n, 14)),
+                fsfcld=rng.uniform(0.5, 0.8, (L, n, 14)))
+
+
+def _sunlit_and_dark(atm, mc, ref):
+    """McICA computes dark columns too (cos(zenith) clamped to 1e-10): their
+    fluxes are of order 1e-7 W/m2 where the non-McICA driver writes zeros."""
+    lit = atm.coszen >= 1e-10
+    for k in ref:
+        assert np.array_equal(mc[k][:, lit], ref[k][:, lit]), k
+        assert np.all(np.abs(mc[k][:, ~lit]) < 1e-5) and np.all(ref[k][:, ~lit] == 0.0), k
+
+
+def test_sw_mcica_binary_covers_equal_overcast_layers(orc):
+    """spcvmc on binary sub-columns is spcvrt on clear / overcast layers, bit
+    for bit in the sunlit columns: cldprmc_sw delta-scales each g-point's copy
+    of its band's optics as cldprop_sw scales the band's."""
+    atm = A.small_atmosphere(24, 40, seed=51)
+    atm.coszen[3] = 0.0
+    cl = _sw_clouds(atm, np.random.default_rng(52))
+    sub = orc.mcica_subcol("sw", atm, cl, icld=2, irng=0)
+    mc = orc.rrtmg_sw_mcica(atm, sub)
+    ref = orc.rrtmg_sw(atm, cloud=cl)
+    _sunlit_and_dark(atm, mc, ref)
+
+
+@pytest.mark.parametrize("iceflag", [1, 2, 3])
+def test_sw_mcica_physics_binary_covers(orc, iceflag):
+    """cldprmc_sw's parameterisations, one g-point on its band, equal
+    cldprop_sw's on all 14 bands for binary sub-columns, bit for bit."""
+    atm = A.small_atmosphere(16, 40, seed=53)
+    rng = np.random.default_rng(54)
+    cl = _sw_clouds(atm, rng)
+    cf = cl["cldfr"]
+    cl["cliqwp"] = np.where(cf > 0, rng.uniform(1.0, 40.0, cf.shape), 0.0)
+    cl["cicewp"] = np.where((cf > 0) & (atm.play < 700), rng.uniform(0.5, 30.0, cf.shape), 0.0)
+    rei, rel = rng.uniform(20.0, 120.0, cf.shape), rng.uniform(4.0, 40.0, cf.shape)
+    sub = orc.mcica_subcol("sw", atm, cl, icld=1, irng=1)
+    mc = orc.rrtmg_sw_mcica(atm, sub, inflag=2, iceflag=iceflag, liqflag=1, reice=rei, reliq=rel)
+    ref = orc.rrtmg_sw(atm, cloud=dict(cldfr=cf, cicewp=cl["cicewp"], cliqwp=cl["cliqwp"], reice=rei, reliq=rel,
+                                       inflag=2, iceflag=iceflag, liqflag=1))
+    _sunlit_and_dark(atm, mc, ref)
+
+
+def test_sw_mcica_partial_covers(orc):
+    """Twelve adjacent layers at cover 0.5: maximum and maximum/random
+    overlap make one block, clear in half the g-points, so the upward flux at
+    the top lies halfway between clear sky and overcast (within the scatter of
+    112 draws); random overlap leaves about six of the twelve layers cloudy in
+    every g-point, which reflects most but not all of what the overcast
+    column does; inflag = 1 stops, as cldprmc_sw does."""
+    atm = A.small_atmosphere(64, 40, seed=55)
+    L, n = atm.nlay, atm.ncol
+    cf = np.zeros((L, n))
+    cf[8:20] = 0.5
+    cl = dict(cldfr=cf, cicewp=cf * 0, cliqwp=cf * 0, taucld=np.full((L, n, 14), 5.0),
+              ssacld=np.full((L, n, 14), 0.999), asmcld=np.full((L, n, 14), 0.85),
+              fsfcld=np.full((L, n, 14), 0.7225))
+    lit = atm.coszen >= 1e-10
+    clear = orc.rrtmg_sw(atm)["swuflx"][-1]
+    over = orc.rrtmg_sw(atm, cloud=dict(cl, cldfr=np.where(cf > 0, 1.0, 0.0)))["swuflx"][-1]
+    up = {icld: orc.rrtmg_sw_mcica(atm, orc.mcica_subcol("sw", atm, cl, icld=icld, irng=1))["swuflx"][-1]
+          for icld in (1, 2, 3)}
+    span = (over - clear)[lit]
+    assert span.min() > 20.0
+    frac = (up[1] - clear)[lit] / span
+    assert np.all(frac > 0.8) and np.all(frac < 1.0)
+    for icld in (2, 3):
+        frac = (up[icld] - clear)[lit] / span
+        assert np.all(frac > 0.15) and np.all(frac < 0.85)
+        assert abs(frac.mean() - 0.5) < 0.08
+    with pytest.raises(orc.CloudRangeError):
+        s = orc.mcica_subcol("sw", atm, dict(cl, cicewp=cf * 3.0), icld=1, irng=1)
+        orc.rrtmg_sw_mcica(atm, s, inflag=1)

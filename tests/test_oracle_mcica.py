@@ -256,3 +256,81 @@ def test_sw_mcica_partial_covers(orc):
     with pytest.raises(orc.CloudRangeError):
         s = orc.mcica_subcol("sw", atm, dict(cl, cicewp=cf * 3.0), icld=1, irng=1)
         orc.rrtmg_sw_mcica(atm, s, inflag=1)
+
+
+def _kiss_masks_numpy(play, cldfr, nsub, icld, permuteseed):
+    """A second restatement of generate_stochastic_clouds with kissvec
+    (mcica_subcol_gen_lw.f90), vectorised over the columns in numpy uint32
+    arithmetic: the masks (nlay, ncol, nsub)."""
+    L, n = cldfr.shape
+    p = play[:4] * 1.0e2
+    s = np.trunc((p - np.trunc(p)) * 1.0e9).astype(np.int64).astype(np.uint32)
+    st = [s[0].copy(), s[1].copy(), s[2].copy(), s[3].copy()]
+    u = np.uint32
+
+    def m(k, sh):
+        return k ^ ((k << u(sh)) if sh > 0 else (k >> u(-sh)))
+
+    def draw():
+        with np.errstate(over="ignore"):
+            st[0] = u(69069) * st[0] + u(1327217885)
+            st[1] = m(m(m(st[1], 13), -17), 5)
+            st[2] = u(18000) * (st[2] & u(65535)) + (st[2] >> u(16))
+            st[3] = u(30903) * (st[3] & u(65535)) + (st[3] >> u(16))
+            k = (st[0] + st[1] + (st[2] << u(16)) + st[3]).view(np.int32)
+        return k.astype(np.float64) * 2.328306e-10 + 0.5
+
+    for _ in range(permuteseed):
+        draw()
+    cdf = np.zeros((nsub, n, L))
+    for g in range(nsub):
+        if icld == 3:
+            cdf[g] = draw()[:, None]
+        else:
+            for lay in range(L):
+                cdf[g, :, lay] = draw()
+    return _masks(cdf, cldfr, icld)
+
+
+def _mt_masks_numpy(cldfr, nsub, icld, permuteseed):
+    """The same with the Mersenne Twister (numpy's MT19937 under the scalar
+    seeding), drawn sub-column by sub-column, column by column, layer by
+    layer (one draw per column and sub-column under maximum overlap)."""
+    L, n = cldfr.shape
+    bg = np.random.MT19937()
+    bg._legacy_seeding(permuteseed)
+    per = 1 if icld == 3 else L
+    r = bg.random_raw(nsub * n * per).astype(np.float64) / 4294967295.0
+    cdf = np.broadcast_to(r.reshape(nsub, n, per), (nsub, n, L)).copy()
+    return _masks(cdf, cldfr, icld)
+
+
+def _masks(cdf, cldfr, icld):
+    L = cldfr.shape[0]
+    cf = np.where(cldfr < 1e-20, 0.0, cldfr)
+    if icld == 2:
+        for lay in range(1, L):
+            keep = cdf[:, :, lay - 1] > 1.0 - cf[lay - 1]
+            cdf[:, :, lay] = np.where(keep, cdf[:, :, lay - 1], cdf[:, :, lay] * (1.0 - cf[lay - 1]))
+    return (cdf >= 1.0 - cf.T[None]).transpose(2, 1, 0).astype(np.float64)
+
+
+@pytest.mark.parametrize("icld", [1, 2, 3])
+def test_masks_match_numpy_restatement(orc, icld):
+    """Both generators' masks, LW (140) and SW (112) sub-columns, equal a
+    numpy restatement of the generator bit for bit."""
+    atm = A.small_atmosphere(48, 40, seed=57)
+    rng = np.random.default_rng(58)
+    # kissvec seeds each column from its pressures: give every column its own
+    atm.play = atm.play + rng.uniform(0.0, 1e-3, atm.play.shape)
+    cl = _clouds(atm, rng)
+    for side, nsub in (("lw", 140), ("sw", 112)):
+        c = cl if side == "lw" else dict(cl, taucld=np.ones((atm.nlay, atm.ncol, 14)),
+                                         ssacld=np.ones((atm.nlay, atm.ncol, 14)),
+                                         asmcld=np.zeros((atm.nlay, atm.ncol, 14)),
+                                         fsfcld=np.zeros((atm.nlay, atm.ncol, 14)))
+        for irng, want in ((0, _kiss_masks_numpy(atm.play, cl["cldfr"], nsub, icld, 3)),
+                           (1, _mt_masks_numpy(cl["cldfr"], nsub, icld, 3))):
+            assert 0.02 < want.mean() < 0.98
+            s = orc.mcica_subcol(side, atm, c, icld=icld, irng=irng, permuteseed=3)
+            assert np.array_equal(s["cldfr"], want), (side, irng)

@@ -334,3 +334,32 @@ def test_masks_match_numpy_restatement(orc, icld):
             assert 0.02 < want.mean() < 0.98
             s = orc.mcica_subcol(side, atm, c, icld=icld, irng=irng, permuteseed=3)
             assert np.array_equal(s["cldfr"], want), (side, irng)
+
+
+@pytest.mark.parametrize("irng", [0, 1])
+@pytest.mark.parametrize("icld", [1, 2])
+def test_lw_mcica_mean_is_the_deterministic_overlap(orc, icld, irng):
+    """McICA samples the overlap that rtrn (random) and rtrnmr
+    (maximum/random) treat exactly, layer by layer: over 512 copies of a
+    column with three partly cloudy decks (covers 0.6, 0.3, 0.4), each
+    drawing its own sub-columns, the mean fluxes at every level and the mean
+    heating of every layer equal the deterministic ones within 4.5 standard
+    errors of the mean."""
+    n = 512
+    atm = A.small_atmosphere(1, 40, seed=61).subset(np.zeros(n, dtype=np.int64))
+    rng = np.random.default_rng(62)
+    atm.play = atm.play + rng.uniform(0.0, 1e-3, atm.play.shape)   # kissvec: a seed per column
+    L = atm.nlay
+    cf = np.zeros((L, n))
+    cf[5:9], cf[9:11], cf[20:24] = 0.6, 0.3, 0.4
+    tau = np.broadcast_to(rng.uniform(0.3, 3.0, (L, 1, 16)), (L, n, 16)).copy()
+    ref = orc.rrtmg_lw(atm, cloud=dict(cldfr=cf, taucld=tau), icld=icld)
+    sub = orc.mcica_subcol("lw", atm, dict(cldfr=cf, cicewp=cf * 0, cliqwp=cf * 0, taucld=tau), icld=icld,
+                           irng=irng)
+    mc = orc.rrtmg_lw_mcica(atm, sub)
+    for k in ("uflx", "dflx", "hr"):
+        d = mc[k] - ref[k]
+        se = d.std(axis=1) / np.sqrt(n)
+        noisy = se > 1e-9
+        assert np.all(np.abs(d.mean(axis=1)[noisy]) < 4.5 * se[noisy]), k
+        assert np.all(np.abs(d.mean(axis=1)[~noisy]) < 1e-9), k

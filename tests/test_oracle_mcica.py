@@ -195,16 +195,26 @@ def _sunlit_and_dark(atm, mc, ref):
         assert np.all(np.abs(mc[k][:, ~lit]) < 1e-5) and np.all(ref[k][:, ~lit] == 0.0), k
 
 
-def test_sw_mcica_binary_covers_equal_overcast_layers(orc):
+@pytest.mark.parametrize("iaer", [0, 10])
+def test_sw_mcica_binary_covers_equal_overcast_layers(orc, iaer):
     """spcvmc on binary sub-columns is spcvrt on clear / overcast layers, bit
-    for bit in the sunlit columns: cldprmc_sw delta-scales each g-point's copy
-    of its band's optics as cldprop_sw scales the band's."""
+    for bit in the sunlit columns, without and with aerosols (iaer = 10):
+    cldprmc_sw delta-scales each g-point's copy of its band's optics as
+    cldprop_sw scales the band's."""
     atm = A.small_atmosphere(24, 40, seed=51)
     atm.coszen[3] = 0.0
-    cl = _sw_clouds(atm, np.random.default_rng(52))
+    rng = np.random.default_rng(52)
+    cl = _sw_clouds(atm, rng)
+    L, n = atm.nlay, atm.ncol
+    prof = (atm.play / atm.play[0]) ** 3.75
+    aer = {} if iaer == 0 else dict(tauaer=rng.uniform(0.0, 0.05, (14, L, n)) * prof,
+                                    ssaaer=rng.uniform(0.8, 1.0, (14, L, n)),
+                                    asmaer=rng.uniform(0.5, 0.8, (14, L, n)))
     sub = orc.mcica_subcol("sw", atm, cl, icld=2, irng=0)
-    mc = orc.rrtmg_sw_mcica(atm, sub)
-    ref = orc.rrtmg_sw(atm, cloud=cl)
+    mc = orc.rrtmg_sw_mcica(atm, sub, iaer=iaer, **aer)
+    ref = orc.rrtmg_sw(atm, iaer=iaer, cloud=cl, **aer)
+    if iaer:
+        assert np.abs(mc["swuflxc"] - orc.rrtmg_sw(atm, cloud=cl)["swuflxc"]).max() > 0.1
     _sunlit_and_dark(atm, mc, ref)
 
 

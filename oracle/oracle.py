@@ -319,3 +319,14 @@ def rrtmg_sw_mcica(atm, sub, iaer: int = 0, tauaer=None, ssaaer=None, asmaer=Non
     if rc != 0:
         raise RuntimeError(f"orc_rrtmg_sw_mcica failed ({rc})")
     return out
+
+
+def mt_jump_ints(seed: int, jump: int, n: int):
+    """The n Mersenne Twister draws after the first ``jump`` ones, by the
+    F2-linear jump-ahead (no draw of the first ``jump`` is made); and the
+    degree of the characteristic polynomial found."""
+    out = np.zeros(n, dtype=np.uint32)
+    _lib.orc_mt_jump_ints.restype = C.c_int
+    deg = _lib.orc_mt_jump_ints(C.c_int32(seed), C.c_uint64(jump), C.c_int(n),
+                                out.ctypes.data_as(C.POINTER(C.c_uint32)))
+    return out, deg

@@ -58,6 +58,153 @@ struct Twister {
   double next_real() { return (double)next_int() / 4294967295.0; }
 };
 
+// ---------------------------------------------------------------------------
+// Jump-ahead of the Mersenne Twister (the F2-linear jump of Haramoto,
+// Matsumoto, Nishimura, Panneton and L'Ecuyer, "Efficient jump ahead for
+// F2-linear random number generators", 2008): the state J words ahead is
+// g(T) applied to the state, T the one-word transition and g(x) = x^J mod
+// phi(x), phi the characteristic polynomial of T (degree 19937).  A prototype
+// of the host side of a device generator that starts each sub-column's
+// stream at its own offset; the tests check it against the serial stream.
+// ---------------------------------------------------------------------------
+
+// The transition one word at a time: 624 words in a ring, the next word
+// x[k + 624] = x[k + 397] ^ twist(x[k], x[k + 1]) written over x[k].
+struct MtRing {
+  uint32_t x[624];
+  int k = 0;
+  uint32_t step() {
+    const uint32_t v = x[(k + 397) % 624] ^ Twister::twist(x[k], x[(k + 1) % 624]);
+    x[k] = v;
+    k = (k + 1) % 624;
+    return v;
+  }
+  static uint32_t temper(uint32_t y) {
+    y ^= y >> 11;
+    y ^= (y << 7) & 0x9d2c5680u;
+    y ^= (y << 15) & 0xefc60000u;
+    return y ^ (y >> 18);
+  }
+};
+
+// Polynomials over GF(2), bit i of word i / 64 the coefficient of x^i.
+struct Poly {
+  std::vector<uint64_t> w;
+  explicit Poly(int nbits = 0) : w((size_t)(nbits + 64) / 64, 0) {}
+  bool bit(int i) const { return (size_t)(i >> 6) < w.size() && ((w[(size_t)i >> 6] >> (i & 63)) & 1u); }
+  void flip(int i) {
+    if ((size_t)(i >> 6) >= w.size()) w.resize((size_t)(i >> 6) + 1, 0);
+    w[(size_t)i >> 6] ^= (uint64_t)1 << (i & 63);
+  }
+  int deg() const {
+    for (size_t j = w.size(); j-- > 0;)
+      if (w[j]) return (int)(j * 64) + 63 - __builtin_clzll(w[j]);
+    return -1;
+  }
+  // this ^= src * x^sh
+  void add_shifted(const Poly& src, int sh) {
+    const int ds = src.deg();
+    if (ds < 0) return;
+    const size_t need = (size_t)(ds + sh) / 64 + 1;
+    if (w.size() < need) w.resize(need, 0);
+    const int q = sh >> 6, r = sh & 63;
+    for (size_t j = 0; j < src.w.size(); ++j) {
+      const uint64_t v = src.w[j];
+      if (!v) continue;
+      w[j + q] ^= v << r;
+      if (r && j + q + 1 < w.size()) w[j + q + 1] ^= v >> (64 - r);
+    }
+  }
+};
+
+// The remainder of a modulo m.
+static void poly_mod(Poly& a, const Poly& m) {
+  const int dm = m.deg();
+  for (int d = a.deg(); d >= dm; d = a.deg()) a.add_shifted(m, d - dm);
+}
+
+// The square of a over GF(2): coefficient i moves to 2i.
+static Poly poly_square(const Poly& a) {
+  Poly r(2 * (a.deg() + 1));
+  for (int i = 0, d = a.deg(); i <= d; ++i)
+    if (a.bit(i)) r.flip(2 * i);
+  return r;
+}
+
+// phi(x): the minimal polynomial of the bit sequence of the generator's
+// words (their top bits), by Berlekamp-Massey over 2 x 19937 + 64 bits; for
+// MT19937 it is the characteristic polynomial of the transition (degree
+// 19937).  Computed once.
+static const Poly& mt_charpoly() {
+  static Poly phi = [] {
+    const int N = 2 * 19937 + 64;
+    MtRing g;
+    Twister t(5489);
+    for (int i = 0; i < 624; ++i) g.x[i] = t.st[i];
+    std::vector<uint8_t> s(N);
+    for (int i = 0; i < N; ++i) s[i] = (uint8_t)(g.step() >> 31);
+    // connection polynomial C (s_n = sum_{j=1..L} c_j s_{n-j})
+    std::vector<uint8_t> C(N + 1, 0), B(N + 1, 0), T;
+    C[0] = B[0] = 1;
+    int L = 0, m = 1;
+    for (int n = 0; n < N; ++n) {
+      uint8_t d = s[n];
+      for (int j = 1; j <= L; ++j) d ^= (uint8_t)(C[j] & s[n - j]);
+      if (!d) {
+        ++m;
+      } else if (2 * L <= n) {
+        T = C;
+        for (int j = 0; j + m <= N; ++j) C[j + m] ^= B[j];
+        L = n + 1 - L;
+        B = T;
+        m = 1;
+      } else {
+        for (int j = 0; j + m <= N; ++j) C[j + m] ^= B[j];
+        ++m;
+      }
+    }
+    // phi(x) = x^L C(1/x)
+    Poly p(L);
+    for (int j = 0; j <= L; ++j)
+      if (C[j]) p.flip(L - j);
+    return p;
+  }();
+  return phi;
+}
+
+// x^J mod phi(x), square and multiply from the top bit of J.
+static Poly mt_jump_poly(uint64_t J) {
+  const Poly& phi = mt_charpoly();
+  Poly r(1);
+  r.flip(0);
+  for (int b = 63; b >= 0; --b) {
+    r = poly_square(r);
+    poly_mod(r, phi);
+    if ((J >> b) & 1u) {
+      Poly x(r.deg() + 2);
+      x.add_shifted(r, 1);
+      r = x;
+      poly_mod(r, phi);
+    }
+  }
+  return r;
+}
+
+// g(T) applied to the ring by Horner's rule: acc = T(acc) ^ g_k * start,
+// k from deg g down to 0.  The result is aligned to k = 0.
+static void mt_apply(const Poly& g, MtRing& ring) {
+  MtRing acc;
+  for (int i = 0; i < 624; ++i) acc.x[i] = 0;
+  for (int k = g.deg(); k >= 0; --k) {
+    acc.step();
+    if (g.bit(k))
+      for (int i = 0; i < 624; ++i) acc.x[(acc.k + i) % 624] ^= ring.x[(ring.k + i) % 624];
+  }
+  MtRing out;
+  for (int i = 0; i < 624; ++i) out.x[i] = acc.x[(acc.k + i) % 624];
+  ring = out;
+}
+
 }  // namespace
 
 extern "C" {
@@ -66,6 +213,18 @@ extern "C" {
 void orc_mt_ints(int32_t seed, int n, uint32_t* out) {
   Twister t(seed);
   for (int i = 0; i < n; ++i) out[i] = t.next_int();
+}
+
+// The n tempered draws that follow the first `jump` draws of the Mersenne
+// Twister seeded with seed, reached by the jump-ahead above (no draw of the
+// first `jump` is made).  Returns the degree of phi (19937).
+int orc_mt_jump_ints(int32_t seed, uint64_t jump, int n, uint32_t* out) {
+  MtRing ring;
+  Twister t(seed);
+  for (int i = 0; i < 624; ++i) ring.x[i] = t.st[i];
+  mt_apply(mt_jump_poly(jump), ring);
+  for (int i = 0; i < n; ++i) out[i] = MtRing::temper(ring.step());
+  return mt_charpoly().deg();
 }
 
 // generate_stochastic_clouds[_sw] for ncol columns of nlay layers (arrays

@@ -373,3 +373,27 @@ def test_lw_mcica_mean_is_the_deterministic_overlap(orc, icld, irng):
         noisy = se > 1e-9
         assert np.all(np.abs(d.mean(axis=1)[noisy]) < 4.5 * se[noisy]), k
         assert np.all(np.abs(d.mean(axis=1)[~noisy]) < 1e-9), k
+
+
+def _numpy_mt_after(seed, jump, n):
+    bg = np.random.MT19937()
+    bg._legacy_seeding(seed)
+    left = jump
+    while left:
+        c = min(left, 1 << 23)
+        bg.random_raw(c)
+        left -= c
+    return bg.random_raw(n).astype(np.uint32)
+
+
+@pytest.mark.parametrize("jump", [0, 1, 623, 624, 625, 100003, 140 * 8192 * 40])
+def test_mersenne_twister_jump_ahead(orc, jump):
+    """The F2-linear jump-ahead that lets each McICA sub-column start its
+    draws at its own offset of the one Mersenne Twister stream (sub-column g
+    of a T42 x 40 call starts g x 8192 x 40 words in): Berlekamp-Massey finds
+    the degree-19937 characteristic polynomial, and the draws after a jump
+    equal the serial stream's (numpy's MT19937 drawn through the skipped
+    words)."""
+    got, deg = orc.mt_jump_ints(7, jump, 64)
+    assert deg == 19937
+    assert np.array_equal(got, _numpy_mt_after(7, jump, 64))

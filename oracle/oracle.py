@@ -330,3 +330,13 @@ def mt_jump_ints(seed: int, jump: int, n: int):
     deg = _lib.orc_mt_jump_ints(C.c_int32(seed), C.c_uint64(jump), C.c_int(n),
                                 out.ctypes.data_as(C.POINTER(C.c_uint32)))
     return out, deg
+
+
+def mt_subcol_starts(seed: int, stride: int, nsub: int, n: int):
+    """The first n draws of nsub Mersenne Twister streams starting ``stride``
+    words apart, the starts reached by one jump polynomial applied in a chain:
+    (nsub, n) uint32."""
+    out = np.zeros((nsub, n), dtype=np.uint32)
+    _lib.orc_mt_subcol_starts(C.c_int32(seed), C.c_uint64(stride), C.c_int(nsub), C.c_int(n),
+                              out.ctypes.data_as(C.POINTER(C.c_uint32)))
+    return out

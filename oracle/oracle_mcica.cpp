@@ -227,6 +227,23 @@ int orc_mt_jump_ints(int32_t seed, uint64_t jump, int n, uint32_t* out) {
   return mt_charpoly().deg();
 }
 
+// The start states of nsub sub-column streams `stride` words apart (McICA's
+// Mersenne Twister path draws sub-column g from word g * ncol * nlay of the
+// stream): one jump polynomial x^stride mod phi, applied in a chain, each
+// start reached from the one before.  out (nsub, n): the first n draws from
+// each start.
+void orc_mt_subcol_starts(int32_t seed, uint64_t stride, int nsub, int n, uint32_t* out) {
+  MtRing ring;
+  Twister t(seed);
+  for (int i = 0; i < 624; ++i) ring.x[i] = t.st[i];
+  const Poly g = mt_jump_poly(stride);
+  for (int s = 0; s < nsub; ++s) {
+    if (s) mt_apply(g, ring);
+    MtRing r = ring;
+    for (int i = 0; i < n; ++i) out[(size_t)s * n + i] = MtRing::temper(r.step());
+  }
+}
+
 // generate_stochastic_clouds[_sw] for ncol columns of nlay layers (arrays
 // (ncol, nlay), column fastest, layer 1 at the surface): nsub sub-columns
 // (the g-points), overlap icld (1 random, 2 maximum/random, 3 maximum), irng

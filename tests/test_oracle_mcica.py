@@ -397,3 +397,15 @@ def test_mersenne_twister_jump_ahead(orc, jump):
     got, deg = orc.mt_jump_ints(7, jump, 64)
     assert deg == 19937
     assert np.array_equal(got, _numpy_mt_after(7, jump, 64))
+
+
+def test_mersenne_twister_subcolumn_starts(orc):
+    """The 140 sub-column start states of a McICA call (1000 columns x 40
+    layers: 40000 words apart), reached by one jump polynomial applied in a
+    chain, give the serial stream's words at every start."""
+    stride, nsub, n = 1000 * 40, 140, 48
+    got = orc.mt_subcol_starts(3, stride, nsub, n)
+    bg = np.random.MT19937()
+    bg._legacy_seeding(3)
+    serial = bg.random_raw(stride * nsub).astype(np.uint32).reshape(nsub, stride)
+    assert np.array_equal(got, serial[:, :n])

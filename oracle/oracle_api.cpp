@@ -220,7 +220,7 @@ int orc_rrtmg_sw(int ncol, int nlay, int icld, int iaer, const double* play, con
   return stopped ? 5 : partial ? 4 : 0;
 }
 
-// McICA rrtmg_sw (rrtmg_sw_rad.f90:84-90): the argument list of orc_rrtmg_sw
+// McICA rrtmg_sw (rrtmg_sw_rad.f90:80-90): the argument list of orc_rrtmg_sw
 // with the sub-column clouds cldfmcl, taucmcl, ssacmcl, asmcmcl, fsfcmcl,
 // ciwpmcl, clwpmcl (112, ncol, nlay) in place of the layer clouds, reicmcl /
 // relqmcl (ncol, nlay); cldprmc_sw's inflag 0 (optics given) or 2 (iceflag

@@ -180,7 +180,7 @@ bool lw_cldprop_phys(const LwInput& in, double ciwp, double clwp, double radice,
 }
 
 // ---------------------------------------------------------------------------
-// McICA's cloud inputs and cldprmc (rrtmg_lw_rad.f90 inatm :454-470,
+// McICA's cloud inputs and cldprmc (rrtmg_lw_rad.f90 inatm :882-891,
 // rrtmg_lw_cldprmc.f90): each g-point's sub-column cover, depth, ice and
 // liquid water paths of a layer; with inflag = 2 the depth formed from the
 // water paths by the parameterisations at the g-point's band ngb(ig) (the
@@ -1411,7 +1411,7 @@ void lw_rtrn(LwColumn& c, int idrv, LwOut& out) {
     odcld[ib].assign(nl + 1, 0.0);
     efclfrac[ib].assign(nl + 1, 0.0);
   }
-  // McICA (rtrnmc, rrtmg_lw_rtrnmc.f90:146-170): per g-point, a sub-column is
+  // McICA (rtrnmc, rrtmg_lw_rtrnmc.f90:279-310): per g-point, a sub-column is
   // cloudy where its cover is 1, its depth secdiff(ngb(ig)) x taucmc; a layer
   // takes the cloudy branch for all its g-points when any of them is cloudy
   const int L1 = nl + 1;
@@ -2093,7 +2093,7 @@ void lw_column(const LwInput& in, int iplon, int idrv, LwColumn& c, LwOut& out) 
       for (int k = 1; k <= c.nlayers; ++k) c.taut[ig][k] = c.taug[ig][k] + c.taua[b][k];
   // icld = 1: rtrn (random overlap); icld = 2, 3: rtrnmr with clouds
   // (maximum/random overlap); clear sky: rtrnmr (:527-541)
-  // McICA: rtrnmc whatever the overlap (rrtmg_lw_rad.f90:250), the overlap
+  // McICA: rtrnmc whatever the overlap (rrtmg_lw_rad.f90:543), the overlap
   // being in the sub-columns already
   if (c.mcica || in.icld == 1) {
     lw_rtrn(c, idrv, out);

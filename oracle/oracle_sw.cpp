@@ -918,7 +918,7 @@ void sw_spcvrt(SwColumn& c, double prmu0, const double* albdir, const double* al
 // asymmetry, each delta-M scaled, combined into the layer's delta-scaled
 // optics.  Returns false where the reference stops.  band = 0: the 14 bands
 // (cldprop_sw); band = 16..29: that band alone, as cldprmc_sw forms one
-// g-point's optics on its band ngb(ig) (rrtmg_sw_cldprmc.f90:163-298), its
+// g-point's optics on its band ngb(ig) (rrtmg_sw_cldprmc.f90:150-320), its
 // stops taken on that band only.
 static bool sw_cldprop_phys(const SwInput& in, double ciwp, double clwp, double radice, double radliq,
                             double* taucloud, double* ssacloud, double* asmcloud, int band = 0) {
@@ -1069,7 +1069,7 @@ static bool sw_cldprop(const SwInput& in, int iplon, SwColumn& c) {
 }
 
 // McICA's cloud inputs (inatm_sw, rrtmg_sw_rad.f90:1084-1099) and cldprmc_sw
-// (rrtmg_sw_cldprmc.f90:117-328): per g-point iw and layer, a sub-column whose
+// (rrtmg_sw_cldprmc.f90:112-328): per g-point iw and layer, a sub-column whose
 // cover is >= cldmin and whose water path or own depth is >= cldmin (1e-20)
 // gets its optics formed -- inflag = 0 the given ones delta-M scaled with the
 // forward-scattering fraction, inflag = 2 the parameterisations on its band

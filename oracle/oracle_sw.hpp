@@ -40,7 +40,7 @@ struct SwInput {
   // iceflag (1..3) and liqflag (1), effective sizes reice / reliq)
   int inflag = 0, iceflag = 0, liqflag = 0;
   const double *reice = nullptr, *reliq = nullptr;
-  // McICA (rrtmg_sw_rad.f90:84-90): sub-column clouds, one per g-point, in
+  // McICA (rrtmg_sw_rad.f90:80-90): sub-column clouds, one per g-point, in
   // place of cldfr / taucld / ... -- cldfmcl, taucmcl, ssacmcl, asmcmcl,
   // fsfcmcl, ciwpmcl, clwpmcl (112, ncol, nlay); reice / reliq as above.
   bool mcica = false;

@@ -2,7 +2,8 @@
 
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use
 this module, as the checker.  It builds ``oracle/build/liboracle.so`` (the C++
-FP64 restatement of the reference's clear-sky RRTMG path, see the .cpp files
+FP64 restatement of the reference's RRTMG path -- clear sky, the non-McICA
+cloudy paths and McICA with its stochastic cloud generator; see the .cpp files
 for the file:line each function follows) with ``make`` when it is missing.
 """
 from __future__ import annotations

@@ -1,7 +1,8 @@
 // CPU oracle, C entry points -- TEST INFRASTRUCTURE ONLY.  Called (via
 // ctypes) by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg.
 // The argument lists follow rrtmg_lw (rrtmg_lw_rad.nomcica.f90:80-89) and
-// rrtmg_sw (rrtmg_sw_rad.nomcica.f90:78-88) for the clear-sky subset; arrays
+// rrtmg_sw (rrtmg_sw_rad.nomcica.f90:78-88), and for the McICA entry points
+// the McICA drivers' (rrtmg_lw_rad.f90:80-276, rrtmg_sw_rad.f90:80-90); arrays
 // are column-major with the column index fastest.  Columns run in parallel
 // with OpenMP (the reference loops over them serially, :453 / :500).
 #include <chrono>

@@ -67,6 +67,17 @@ def count(atm):
     return lw, sw, per(cl), per(cs)
 
 
+def count_clouds(atm, lw_cloud, sw_cloud, lw_icld: int = 2):
+    """Operation counts per column of a cloudy LW call (overlap ``lw_icld``)
+    and a cloudy SW call on ``atm``: the cloud physics, the cloudy solver
+    branches and the SW total-sky pass (work of its own in a call with
+    clouds) counted.  Returns (counts_lw, counts_sw)."""
+    _, cl = _counted(O.rrtmg_lw, atm, cloud=lw_cloud, icld=lw_icld)
+    _, cs = _counted(O.rrtmg_sw, atm, cloud=sw_cloud)
+    per = lambda c: {k: v / atm.ncol for k, v in c.items()}
+    return per(cl), per(cs)
+
+
 def flops(c) -> float:
     return float(sum(c[k] for k in FLOP_KINDS))
 

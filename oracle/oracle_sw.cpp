@@ -804,7 +804,9 @@ static void vrtqdr(int klev, const std::vector<double>& pref, const std::vector<
 }
 
 // ---------------------------------------------------------------------------
-// spcvrt_sw, icpr = 1, idelm = 1, clear sky (pclfr = 0, cloud optics 0/1/0)
+// spcvrt_sw / spcvmc_sw, icpr = 1, idelm = 1: the clear pass, and the total
+// pass combined with it by the cover, per band (non-McICA) or per g-point
+// (McICA); clear sky has cover 0 and cloud optics 0 / 1 / 0
 // ---------------------------------------------------------------------------
 void sw_spcvrt(SwColumn& c, double prmu0, const double* albdir, const double* albdif, SwOut& out, bool run_taumol) {
   const SwTables& T = g_sw;
@@ -864,46 +866,46 @@ void sw_spcvrt(SwColumn& c, double prmu0, const double* albdir, const double* al
         zomcc[jk] = (zomcc[jk] - zwf) / (1.0 - zwf);
         zgcc[jk] = (zgcc[jk] - zf) / (1.0 - zf);
         // icpr >= 1 (:459-464); clear sky: ptauc = 0, pomgc = 1, pasyc = 0
-        OPC_PAUSE();
+        if (!c.total_pass) OPC_PAUSE();
         const double ptauc = TC(ikl), pomgc = OC(ikl), pasyc = AC(ikl);
         ztauo[jk] = ztauc[jk] + ptauc;
         zomco[jk] = ztauc[jk] * zomcc[jk] + ptauc * pomgc;
         zgco[jk] = (ptauc * pomgc * pasyc + ztauc[jk] * zomcc[jk] * zgcc[jk]) / zomco[jk];
         zomco[jk] = zomco[jk] / ztauo[jk];
-        OPC_RESUME();
+        if (!c.total_pass) OPC_RESUME();
       }
       reftra(klev, lrtchkclr, zgcc, prmu0, ztauc, zomcc, zrefc, zrefdc, ztrac, ztradc);
-      OPC_PAUSE();
+      if (!c.total_pass) OPC_PAUSE();
       reftra(klev, lrtchkcld, zgco, prmu0, ztauo, zomco, zrefo, zrefdo, ztrao, ztrado);
-      OPC_RESUME();
+      if (!c.total_pass) OPC_RESUME();
       for (int jk = 1; jk <= klev; ++jk) {
-        OPC_PAUSE();
+        if (!c.total_pass) OPC_PAUSE();
         const int ikl = klev + 1 - jk;
         const double zclear = 1.0 - CF(ikl), zcloud = CF(ikl);
         zref[jk] = zclear * zrefc[jk] + zcloud * zrefo[jk];
         zrefd[jk] = zclear * zrefdc[jk] + zcloud * zrefdo[jk];
         ztra[jk] = zclear * ztrac[jk] + zcloud * ztrao[jk];
         ztrad[jk] = zclear * ztradc[jk] + zcloud * ztrado[jk];
-        OPC_RESUME();
+        if (!c.total_pass) OPC_RESUME();
         double zdbtmc = sw_exp(ztauc[jk] / prmu0);
         zdbtc[jk] = zdbtmc;
         ztdbtc[jk + 1] = zdbtc[jk] * ztdbtc[jk];
-        OPC_PAUSE();
+        if (!c.total_pass) OPC_PAUSE();
         double zdbtmo = sw_exp(ztauo[jk] / prmu0);
         zdbt[jk] = zclear * zdbtmc + zcloud * zdbtmo;
         ztdbt[jk + 1] = zdbt[jk] * ztdbt[jk];
-        OPC_RESUME();
+        if (!c.total_pass) OPC_RESUME();
       }
       vrtqdr(klev, zrefc, zrefdc, ztrac, ztradc, zdbtc, ztdbtc, zcd, zcu);
-      OPC_PAUSE();
+      if (!c.total_pass) OPC_PAUSE();
       vrtqdr(klev, zref, zrefd, ztra, ztrad, zdbt, ztdbt, zfd, zfu);
-      OPC_RESUME();
+      if (!c.total_pass) OPC_RESUME();
       for (int jk = 1; jk <= klev + 1; ++jk) {
         int ikl = klev + 2 - jk;
-        OPC_PAUSE();
+        if (!c.total_pass) OPC_PAUSE();
         out.fu[ikl] = out.fu[ikl] + zincflx * zfu[jk];
         out.fd[ikl] = out.fd[ikl] + zincflx * zfd[jk];
-        OPC_RESUME();
+        if (!c.total_pass) OPC_RESUME();
         out.cu[ikl] = out.cu[ikl] + zincflx * zcu[jk];
         out.cd[ikl] = out.cd[ikl] + zincflx * zcd[jk];
       }
@@ -1140,6 +1142,7 @@ bool sw_column(const SwInput& in, int iplon, SwColumn& c, SwOut& out, bool* part
     return false;
   }
   sw_inatm(in, iplon, c);
+  c.total_pass = in.icld >= 1;
   c.mcica = in.mcica && in.icld >= 1;
   if (c.mcica) {
     if (!sw_cldprmc(in, iplon, c) && stopped) *stopped = true;

@@ -64,6 +64,9 @@ struct SwColumn {
   // [(iw - 1) * (nlayers + 2) + lay]
   bool mcica = false;
   std::vector<double> cldfmc, taucmc, ssacmc, asmcmc;
+  // a call with clouds: its total-sky two-stream pass is work of its own
+  // (the op-counting build counts it; in clear sky it repeats the clear pass)
+  bool total_pass = false;
   double sfluxzen[113];
 
   void resize(int nl) {

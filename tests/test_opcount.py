@@ -65,3 +65,35 @@ def test_phase_flops_add_up_to_the_path(blob, counting):
     # the g-point work dominates both paths
     assert (lw["taumol"] + lw["rtrnmr"]) / sum(lw.values()) > 0.9
     assert (sw["taumol_sw"] + sw["spcvrt_sw"]) / sum(sw.values()) > 0.9
+
+
+def test_cloudy_counts(orc, counting):
+    """Cloudy calls in the counting build: the same fluxes as the normal
+    build, bit for bit; with no cover the LW cloudy call does the clear work
+    and rtrnmr's overlap bookkeeping over every layer (under 5 % more), the SW
+    one adds its total-sky pass (counted in a call with clouds); overcast
+    layers with the cloud physics add work on both sides."""
+    atm = A.small_atmosphere(6, 40, seed=23)
+    cf = np.zeros((atm.nlay, atm.ncol))
+    none = dict(cldfr=cf, cicewp=cf, cliqwp=cf, reice=cf + 30.0, reliq=cf + 10.0, inflag=2, iceflag=3, liqflag=1)
+    cf1 = cf.copy()
+    cf1[5:9] = 1.0
+    over = dict(none, cldfr=cf1, cicewp=cf1 * 20.0, cliqwp=cf1 * 30.0)
+    _, _, clr_lw, clr_sw = P.count(atm)
+    n_lw, n_sw = P.count_clouds(atm, none, none)
+    o_lw, o_sw = P.count_clouds(atm, over, over)
+    assert P.flops(clr_lw) <= P.flops(n_lw) < 1.05 * P.flops(clr_lw)
+    assert 1.2 * P.flops(clr_sw) < P.flops(n_sw) < 2.0 * P.flops(clr_sw)
+    assert P.flops(o_lw) > P.flops(n_lw) and P.flops(o_sw) > P.flops(n_sw)
+    orc.set_table_mode(False)
+    try:
+        rlw = orc.rrtmg_lw(atm, cloud=over, icld=2)
+        rsw = orc.rrtmg_sw(atm, cloud=over)
+    finally:
+        orc.set_table_mode(True)
+    lw, _ = P._counted(orc.rrtmg_lw, atm, cloud=over, icld=2)
+    sw, _ = P._counted(orc.rrtmg_sw, atm, cloud=over)
+    for k in rlw:
+        np.testing.assert_array_equal(lw[k], rlw[k], err_msg=k)
+    for k in rsw:
+        np.testing.assert_array_equal(sw[k], rsw[k], err_msg=k)

@@ -409,3 +409,18 @@ def test_mersenne_twister_subcolumn_starts(orc):
     bg._legacy_seeding(3)
     serial = bg.random_raw(stride * nsub).astype(np.uint32).reshape(nsub, stride)
     assert np.array_equal(got, serial[:, :n])
+
+
+def test_mcica_results_do_not_depend_on_threads(orc):
+    """The McICA paths keep their per-g-point cloud state in each thread's own
+    column: one thread and four give the same fluxes bit for bit."""
+    atm = A.small_atmosphere(40, 40, seed=63)
+    rng = np.random.default_rng(64)
+    lw_cl = _clouds(atm, rng)
+    sw_cl = _sw_clouds(atm, rng, binary=False)
+    lw_sub = orc.mcica_subcol("lw", atm, lw_cl, icld=2, irng=1)
+    sw_sub = orc.mcica_subcol("sw", atm, sw_cl, icld=2, irng=1)
+    for f, sub in ((orc.rrtmg_lw_mcica, lw_sub), (orc.rrtmg_sw_mcica, sw_sub)):
+        one, four = f(atm, sub, nthreads=1), f(atm, sub, nthreads=4)
+        for k in one:
+            assert np.array_equal(one[k], four[k]), k

@@ -424,3 +424,21 @@ def test_mcica_results_do_not_depend_on_threads(orc):
         one, four = f(atm, sub, nthreads=1), f(atm, sub, nthreads=4)
         for k in one:
             assert np.array_equal(one[k], four[k]), k
+
+
+@pytest.mark.parametrize("icld", [1, 2, 3])
+def test_mt_masks_from_jumped_subcolumn_streams(orc, icld):
+    """The device plan for the Mersenne Twister path, emulated: each
+    sub-column draws its block from its own start, stride ncol x nlay words
+    apart (ncol under maximum overlap), the starts reached by jump-ahead; the
+    masks equal the serial generator's bit for bit."""
+    atm = A.small_atmosphere(16, 40, seed=65)
+    cl = _clouds(atm, np.random.default_rng(66))
+    L, n, nsub = atm.nlay, atm.ncol, 140
+    per = 1 if icld == 3 else L
+    blocks = orc.mt_subcol_starts(5, n * per, nsub, n * per)
+    cdf = np.broadcast_to((blocks.astype(np.float64) / 4294967295.0).reshape(nsub, n, per), (nsub, n, L)).copy()
+    want = orc.mcica_subcol("lw", atm, cl, icld=icld, irng=1, permuteseed=5)["cldfr"]
+    got = _masks(cdf, cl["cldfr"], icld)
+    assert 0.02 < got.mean() < 0.98
+    assert np.array_equal(got, want)

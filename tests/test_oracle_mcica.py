@@ -132,11 +132,17 @@ def test_lw_mcica_binary_covers_equal_random_overlap(orc):
         assert np.array_equal(mc[k], ref[k]), k
 
 
-@pytest.mark.parametrize("iceflag", [1, 2, 3])
+@pytest.mark.parametrize("iceflag", [0, 1, 2, 3])
 def test_lw_mcica_physics_binary_covers(orc, iceflag):
     """cldprmc's per-g-point parameterisations on binary sub-columns equal
     cldprop's per band when the column keeps 16 cloud bands (liquid, liqflag 1,
-    in every cloudy layer), bit for bit."""
+    in every cloudy layer), bit for bit, gray ice (iceflag 0) included.  With
+    gray liquid (liqflag 0) the reference's two routines differ: cldprop
+    scales each of its ncbands cloud bands by that band's diffusivity
+    secdiff(ib) (rrtmg_lw_rtrn.f90), so a single gray cloud band carries band
+    1's into every band where cldprmc / rtrnmc take secdiff(ngb(g)), and
+    cldprop's ice band map changes with liquid gray (iceind 1 -> 2,
+    rrtmg_lw_cldprop.f90:244)."""
     atm = A.small_atmosphere(16, 40, seed=43)
     rng = np.random.default_rng(44)
     cl = _clouds(atm, rng, binary=True)

@@ -136,13 +136,7 @@ def test_lw_mcica_binary_covers_equal_random_overlap(orc):
 def test_lw_mcica_physics_binary_covers(orc, iceflag):
     """cldprmc's per-g-point parameterisations on binary sub-columns equal
     cldprop's per band when the column keeps 16 cloud bands (liquid, liqflag 1,
-    in every cloudy layer), bit for bit, gray ice (iceflag 0) included.  With
-    gray liquid (liqflag 0) the reference's two routines differ: cldprop
-    scales each of its ncbands cloud bands by that band's diffusivity
-    secdiff(ib) (rrtmg_lw_rtrn.f90), so a single gray cloud band carries band
-    1's into every band where cldprmc / rtrnmc take secdiff(ngb(g)), and
-    cldprop's ice band map changes with liquid gray (iceind 1 -> 2,
-    rrtmg_lw_cldprop.f90:244)."""
+    in every cloudy layer), bit for bit, gray ice (iceflag 0) included."""
     atm = A.small_atmosphere(16, 40, seed=43)
     rng = np.random.default_rng(44)
     cl = _clouds(atm, rng, binary=True)
@@ -448,3 +442,27 @@ def test_mt_masks_from_jumped_subcolumn_streams(orc, icld):
     got = _masks(cdf, cl["cldfr"], icld)
     assert 0.02 < got.mean() < 0.98
     assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("iceflag", [2, 3])
+def test_lw_mcica_gray_liquid_binary_covers(orc, iceflag):
+    """Gray liquid (liqflag 0) with a 16-band ice scheme in every cloudy
+    layer: cldprmc equals cldprop bit for bit.  (Where the two routines of the
+    reference differ: cldprop / rtrn scale each of the column's ncbands cloud
+    bands by secdiff of that cloud band's index, so with 1 or 5 cloud bands --
+    gray ice, iceflag 1 -- bands share a diffusivity where cldprmc / rtrnmc
+    take secdiff(ngb(g)); and cldprop's count of cloud bands runs across the
+    layers, so a layer filled while it was 1 keeps its depth in band 1 only.)"""
+    atm = A.small_atmosphere(16, 40, seed=43)
+    rng = np.random.default_rng(44)
+    cl = _clouds(atm, rng, binary=True)
+    cf = cl["cldfr"]
+    cl["cliqwp"] = np.where(cf > 0, rng.uniform(1.0, 40.0, cf.shape), 0.0)
+    cl["cicewp"] = np.where(cf > 0, rng.uniform(0.5, 30.0, cf.shape), 0.0)
+    rei, rel = rng.uniform(20.0, 120.0, cf.shape), rng.uniform(4.0, 40.0, cf.shape)
+    sub = orc.mcica_subcol("lw", atm, dict(cl, taucld=np.zeros_like(cl["taucld"])), icld=1, irng=1)
+    mc = orc.rrtmg_lw_mcica(atm, sub, inflag=2, iceflag=iceflag, liqflag=0, reice=rei, reliq=rel)
+    ref = orc.rrtmg_lw(atm, icld=1, cloud=dict(cldfr=cf, cicewp=cl["cicewp"], cliqwp=cl["cliqwp"], reice=rei,
+                                               reliq=rel, inflag=2, iceflag=iceflag, liqflag=0))
+    for k in ref:
+        assert np.array_equal(mc[k], ref[k]), k
